@@ -1,0 +1,162 @@
+"""ctypes front end of the FP64 CPU oracle (test infrastructure only).
+
+Only the test suite, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` may import this module; it is the checker of the CUDA path, never
+part of it.  The restatement itself lives in ``tracer_oracle.c`` with
+file:line citations of the reference routines it follows.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+HOR = {"MUSCL": 0, "MFCT": 1, "UPW1": 2}
+VER = {"QR4C": 0, "UPW1": 1}
+
+_P = C.c_void_p
+
+
+class _OrMesh(C.Structure):
+    _fields_ = [("nod2D", C.c_int), ("elem2D", C.c_int), ("edge2D", C.c_int), ("nl", C.c_int)] + \
+        [(n, _P) for n in ("elem2D_nodes", "edges", "edge_tri", "nod_in_elem2D_ptr", "nod_in_elem2D",
+                           "nlevels", "ulevels", "nlevels_nod2D", "ulevels_nod2D", "nlevels_nod2D_min",
+                           "ulevels_nod2D_max", "coord_nod2D", "elem_area", "elem_cos", "edge_dxdy",
+                           "edge_cross_dxdy", "gradient_sca", "area", "areasvol", "hnode", "hnode_new",
+                           "helem", "Z_3d_n", "zbar_3d_n", "zbar_n_bot")] + \
+        [("cyclic_length", C.c_double)]
+
+
+class _OrCfg(C.Structure):
+    _fields_ = [("hor", C.c_int), ("ver", C.c_int), ("lim_fct", C.c_int), ("ph", C.c_double),
+                ("pv", C.c_double), ("ab_order", C.c_int), ("i_vert_diff", C.c_int)]
+
+
+class _OrWork(C.Structure):
+    _fields_ = [(n, _P) for n in ("nboundary_lay", "edge_up_dn_tri", "edge_up_dn_grad", "tr_xy", "tr_z",
+                                  "fct_LO", "adv_flux_hor", "adv_flux_ver", "fct_ttf_max", "fct_ttf_min",
+                                  "fct_plus", "fct_minus", "tvert_max", "tvert_min", "del_ttf",
+                                  "del_ttf_advhoriz", "del_ttf_advvert")]
+
+
+_lib: Optional[C.CDLL] = None
+
+
+def build() -> str:
+    """Compile the oracle with its Makefile (gcc only, seconds)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        for name in ("or_muscl_adv_init", "or_init_tracers_AB", "or_tracer_gradient_elements",
+                     "or_fill_up_dn_grad", "or_adv_tra_hor_upw1", "or_adv_tra_hor_muscl", "or_adv_tra_hor_mfct",
+                     "or_adv_tra_ver_upw1", "or_adv_tra_ver_qr4c", "or_oce_tra_adv_fct",
+                     "or_oce_tra_adv_flux2dtracer", "or_do_oce_adv_tra", "or_diff_ver_part_impl_ale",
+                     "or_tracer_step", "or_set_threads", "or_get_threads"):
+            getattr(L, name)
+        L.or_tracer_step.restype = C.c_int
+        L.or_do_oce_adv_tra.restype = C.c_int
+        L.or_set_threads.argtypes = [C.c_int]
+        _lib = L
+    return _lib
+
+
+def set_threads(n: int) -> None:
+    lib().or_set_threads(int(n))
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(_P)
+
+
+def cfg_struct(hor="MUSCL", ver="QR4C", lim="FCT", ph=0.0, pv=1.0, ab_order=2, i_vert_diff=True) -> _OrCfg:
+    return _OrCfg(HOR[hor], VER[ver], 1 if lim == "FCT" else 0, float(ph), float(pv), int(ab_order),
+                  1 if i_vert_diff else 0)
+
+
+class OracleMesh:
+    """Holds contiguous copies of the mesh arrays and the C struct that points at them."""
+
+    def __init__(self, mesh):
+        self.mesh = mesh
+        i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+        f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        self._keep = {
+            "elem2D_nodes": i32(mesh.elem2D_nodes), "edges": i32(mesh.edges), "edge_tri": i32(mesh.edge_tri),
+            "nod_in_elem2D_ptr": i32(mesh.nod_in_elem2D_ptr), "nod_in_elem2D": i32(mesh.nod_in_elem2D),
+            "nlevels": i32(mesh.nlevels), "ulevels": i32(mesh.ulevels), "nlevels_nod2D": i32(mesh.nlevels_nod2D),
+            "ulevels_nod2D": i32(mesh.ulevels_nod2D), "nlevels_nod2D_min": i32(mesh.nlevels_nod2D_min),
+            "ulevels_nod2D_max": i32(mesh.ulevels_nod2D_max), "coord_nod2D": f64(mesh.coord_nod2D),
+            "elem_area": f64(mesh.elem_area), "elem_cos": f64(mesh.elem_cos), "edge_dxdy": f64(mesh.edge_dxdy),
+            "edge_cross_dxdy": f64(mesh.edge_cross_dxdy), "gradient_sca": f64(mesh.gradient_sca),
+            "area": f64(mesh.area), "areasvol": f64(mesh.areasvol), "hnode": f64(mesh.hnode),
+            "hnode_new": f64(mesh.hnode_new), "helem": f64(mesh.helem), "Z_3d_n": f64(mesh.Z_3d_n),
+            "zbar_3d_n": f64(mesh.zbar_3d_n), "zbar_n_bot": f64(mesh.zbar_n_bot),
+        }
+        s = _OrMesh()
+        s.nod2D, s.elem2D, s.edge2D, s.nl = mesh.nod2D, mesh.elem2D, mesh.edge2D, mesh.nl
+        for k, v in self._keep.items():
+            setattr(s, k, v.ctypes.data_as(_P))
+        s.cyclic_length = float(mesh.cyclic_length)
+        self.s = s
+        N2, E2, T2, nl = mesh.nod2D, mesh.edge2D, mesh.elem2D, mesh.nl
+        L1 = nl - 1
+        z = lambda *shape: np.zeros(shape, dtype=np.float64)
+        self.work = {
+            "nboundary_lay": np.zeros(N2, np.int32), "edge_up_dn_tri": np.zeros((E2, 2), np.int32),
+            "edge_up_dn_grad": z(E2, L1, 4), "tr_xy": z(T2, L1, 2), "tr_z": z(N2, nl),
+            "fct_LO": z(N2, L1), "adv_flux_hor": z(E2, L1), "adv_flux_ver": z(N2, nl),
+            "fct_ttf_max": z(N2, L1), "fct_ttf_min": z(N2, L1), "fct_plus": z(N2, L1), "fct_minus": z(N2, L1),
+            "tvert_max": z(N2, L1), "tvert_min": z(N2, L1), "del_ttf": z(N2, L1),
+            "del_ttf_advhoriz": z(N2, L1), "del_ttf_advvert": z(N2, L1),
+        }
+        w = _OrWork()
+        for k, v in self.work.items():
+            setattr(w, k, v.ctypes.data_as(_P))
+        self.w = w
+        lib().or_muscl_adv_init(C.byref(self.s), C.byref(self.w))
+
+    # ---- whole tracer step -------------------------------------------------
+    def tracer_step(self, forcing, cfg: _OrCfg, values, valuesAB, valuesold, dt=None) -> None:
+        """One per-tracer body of solve_tracers_ale, in place on ``values``/``valuesold``."""
+        for a in (values, valuesAB, valuesold):
+            assert a.flags.c_contiguous and a.dtype == np.float64
+        rc = lib().or_tracer_step(C.byref(self.s), C.byref(cfg), C.c_double(forcing.dt if dt is None else dt),
+                                  _ptr(forcing.uv), _ptr(forcing.w), _ptr(forcing.w_i), _ptr(forcing.w_e),
+                                  _ptr(forcing.Kv), _ptr(forcing.bc_surface), _ptr(values), _ptr(valuesAB),
+                                  _ptr(valuesold), C.byref(self.w))
+        if rc != 0:
+            raise RuntimeError(f"oracle tracer step failed with status {rc}")
+
+    def init_tracers_AB(self, cfg, values, valuesAB, valuesold) -> None:
+        lib().or_init_tracers_AB(C.byref(self.s), C.byref(cfg), _ptr(values), _ptr(valuesAB), _ptr(valuesold),
+                                 C.byref(self.w))
+
+    def do_oce_adv_tra(self, forcing, cfg, values, valuesAB, dt=None) -> None:
+        rc = lib().or_do_oce_adv_tra(C.byref(self.s), C.c_double(forcing.dt if dt is None else dt),
+                                     _ptr(forcing.uv), _ptr(forcing.w), _ptr(forcing.w_i), _ptr(forcing.w_e),
+                                     C.byref(cfg), _ptr(values), _ptr(valuesAB), C.byref(self.w))
+        if rc != 0:
+            raise RuntimeError(f"oracle do_oce_adv_tra failed with status {rc}")
+
+    def diff_ver_part_impl_ale(self, forcing, values, dt=None) -> None:
+        lib().or_diff_ver_part_impl_ale(C.byref(self.s), C.c_double(forcing.dt if dt is None else dt),
+                                        _ptr(forcing.Kv), _ptr(forcing.bc_surface), _ptr(values))
+
+
+def ensure_f64(forcing):
+    for k in ("uv", "w", "w_e", "w_i", "Kv", "bc_surface"):
+        setattr(forcing, k, np.ascontiguousarray(getattr(forcing, k), dtype=np.float64))
+    return forcing

@@ -1,0 +1,786 @@
+/*
+ * tracer_oracle.c -- FP64 CPU restatement of FESOM2's tracer-transport step.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker).  See tracer_oracle.h.
+ *
+ * Each routine restates the reference loop for loop, in the reference's
+ * evaluation order (left to right, no contraction: build with
+ * -ffp-contract=off), with 1-based level indices as in the Fortran.  With one
+ * thread every edge scatter runs in ascending edge order, which is the
+ * reference's serial (and OPENMP_REPRODUCIBLE) order.  With more threads the
+ * loops are split the way the reference's !$OMP directives split them and the
+ * scatters take a per-node lock (the reference's default OpenMP build).
+ *
+ * Literal constants follow the reference's GNU build, which promotes default
+ * reals to 8 bytes (-fdefault-real-8, src/CMakeLists.txt:383-388): flux_eps is
+ * the double 1e-16 and bignumber the double 1e3.
+ */
+#include "tracer_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static int g_threads = 1;
+void or_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
+int or_get_threads(void) { return g_threads; }
+
+#define R_EARTH 6367500.0        /* src/oce_modules.F90:29 */
+#define AB_EPSILON 0.1           /* src/oce_modules.F90:105 */
+
+#define OMP_FOR _Pragma("omp parallel for schedule(static) if(g_threads > 1) num_threads(g_threads)")
+
+/* ---- per-node locks for the OpenMP scatters ----------------------------- */
+#ifdef _OPENMP
+static omp_lock_t *g_locks = NULL;
+static int g_nlocks = 0;
+static void locks_ensure(int n) {
+    if (g_nlocks >= n) return;
+    if (g_locks) {
+        for (int i = 0; i < g_nlocks; i++) omp_destroy_lock(&g_locks[i]);
+        free(g_locks);
+    }
+    g_locks = (omp_lock_t *)malloc(sizeof(omp_lock_t) * (size_t)n);
+    for (int i = 0; i < n; i++) omp_init_lock(&g_locks[i]);
+    g_nlocks = n;
+}
+#define LOCK(n)   do { if (g_threads > 1) omp_set_lock(&g_locks[(n)]); } while (0)
+#define UNLOCK(n) do { if (g_threads > 1) omp_unset_lock(&g_locks[(n)]); } while (0)
+#else
+static void locks_ensure(int n) { (void)n; }
+#define LOCK(n)   do { } while (0)
+#define UNLOCK(n) do { } while (0)
+#endif
+
+/* ---- accessors: Fortran a(level, entity), level 1-based, entity 0-based --- */
+#define IX1(nz, n) ((size_t)(n) * (size_t)L1 + (size_t)((nz) - 1))
+#define IXN(nz, n) ((size_t)(n) * (size_t)NL + (size_t)((nz) - 1))
+
+static inline double dmax(double a, double b) { return a > b ? a : b; }
+static inline double dmin(double a, double b) { return a < b ? a : b; }
+
+/* ========================================================================== */
+/* muscl_adv_init / find_up_downwind_triangles  (src/oce_muscl_adv.F90:32-352) */
+/* ========================================================================== */
+void or_muscl_adv_init(const or_mesh *m, or_work *w) {
+    const int NL = m->nl;
+    /* nboundary_lay (:92-155) */
+    for (int n = 0; n < m->nod2D; n++) w->nboundary_lay[n] = NL - 1;
+    for (int e = 0; e < m->edge2D; e++) {
+        int n1 = m->edges[2 * e], n2 = m->edges[2 * e + 1];
+        int t1 = m->edge_tri[2 * e], t2 = m->edge_tri[2 * e + 1];
+        if (t1 < 0 || t2 < 0) {
+            w->nboundary_lay[n1] = 0;
+            w->nboundary_lay[n2] = 0;
+        } else {
+            int mv = (m->nlevels[t1] < m->nlevels[t2] ? m->nlevels[t1] : m->nlevels[t2]) - 1;
+            if (mv < w->nboundary_lay[n1]) w->nboundary_lay[n1] = mv;
+            if (mv < w->nboundary_lay[n2]) w->nboundary_lay[n2] = mv;
+        }
+    }
+    /* find_up_downwind_triangles (:240-333) */
+    const double cyc = m->cyclic_length;
+    const double *X = m->coord_nod2D;
+    for (int e = 0; e < m->edge2D; e++) {
+        w->edge_up_dn_tri[2 * e] = -1;
+        w->edge_up_dn_tri[2 * e + 1] = -1;
+    }
+    for (int e = 0; e < m->edge2D; e++) {
+        int ed[2] = {m->edges[2 * e], m->edges[2 * e + 1]};
+        double x[2];
+        x[0] = X[2 * ed[1]] - X[2 * ed[0]];
+        x[1] = X[2 * ed[1] + 1] - X[2 * ed[0] + 1];
+        if (x[0] > cyc / 2.0) x[0] = x[0] - cyc;
+        if (x[0] < -cyc / 2.0) x[0] = x[0] + cyc;
+        for (int side = 0; side < 2; side++) {
+            /* side 0: look upwind of node 1 (x = -x); side 1: of node 2 (x restored) */
+            x[0] = -x[0];
+            x[1] = -x[1];
+            int node = ed[side];
+            for (int k = m->nod_in_elem2D_ptr[node]; k < m->nod_in_elem2D_ptr[node + 1]; k++) {
+                int elem = m->nod_in_elem2D[k];
+                const int *en = &m->elem2D_nodes[3 * elem];
+                int i0, i1, i2;
+                if (en[0] == node) { i0 = 0; i1 = 1; i2 = 2; }
+                else if (en[1] == node) { i0 = 1; i1 = 0; i2 = 2; }
+                else { i0 = 2; i1 = 0; i2 = 1; }
+                double b[2], c[2];
+                b[0] = X[2 * en[i1]] - X[2 * en[i0]];
+                b[1] = X[2 * en[i1] + 1] - X[2 * en[i0] + 1];
+                c[0] = X[2 * en[i2]] - X[2 * en[i0]];
+                c[1] = X[2 * en[i2] + 1] - X[2 * en[i0] + 1];
+                if (b[0] > cyc / 2.0) b[0] = b[0] - cyc;
+                if (b[0] < -cyc / 2.0) b[0] = b[0] + cyc;
+                if (c[0] > cyc / 2.0) c[0] = c[0] - cyc;
+                if (c[0] < -cyc / 2.0) c[0] = c[0] + cyc;
+                double cr = 0.0; cr += c[0] * c[0]; cr += c[1] * c[1];
+                double s = 0.0; s += b[0] * c[0]; s += b[1] * c[1];
+                double bx = s / cr;
+                double by = (-(b[0] * c[1]) + b[1] * c[0]) / cr;
+                s = 0.0; s += x[0] * c[0]; s += x[1] * c[1];
+                double xx = s / cr;
+                double xy = (-(x[0] * c[1]) + x[1] * c[0]) / cr;
+                double ab = atan2(by, bx);
+                double ax = atan2(xy, xx);
+                if ((ab > 0.0) && (ax > 0.0) && (ax < ab)) { w->edge_up_dn_tri[2 * e + side] = elem; continue; }
+                if ((ab < 0.0) && (ax < 0.0) && (ax > ab)) { w->edge_up_dn_tri[2 * e + side] = elem; continue; }
+                if ((ab == ax) || (ax == 0.0)) { w->edge_up_dn_tri[2 * e + side] = elem; continue; }
+            }
+        }
+    }
+    const int L1 = NL - 1;
+    memset(w->edge_up_dn_grad, 0, sizeof(double) * 4 * (size_t)L1 * (size_t)m->edge2D);
+}
+
+/* ========================================================================== */
+/* gradients (src/oce_tracer_mod.F90:147-232) and fill_up_dn_grad             */
+/* ========================================================================== */
+void or_tracer_gradient_elements(const or_mesh *m, const double *ttf, double *tr_xy) {
+    const int L1 = m->nl - 1;
+    OMP_FOR
+    for (int elem = 0; elem < m->elem2D; elem++) {
+        const int *en = &m->elem2D_nodes[3 * elem];
+        const double *gs = &m->gradient_sca[6 * elem];
+        for (int nz = m->ulevels[elem]; nz <= m->nlevels[elem] - 1; nz++) {
+            double s = 0.0;
+            s += gs[0] * ttf[IX1(nz, en[0])];
+            s += gs[1] * ttf[IX1(nz, en[1])];
+            s += gs[2] * ttf[IX1(nz, en[2])];
+            tr_xy[2 * IX1(nz, elem)] = s;
+            s = 0.0;
+            s += gs[3] * ttf[IX1(nz, en[0])];
+            s += gs[4] * ttf[IX1(nz, en[1])];
+            s += gs[5] * ttf[IX1(nz, en[2])];
+            tr_xy[2 * IX1(nz, elem) + 1] = s;
+        }
+    }
+}
+
+void or_tracer_gradient_z(const or_mesh *m, const double *ttf, double *tr_z) {
+    const int NL = m->nl, L1 = NL - 1;
+    OMP_FOR
+    for (int n = 0; n < m->nod2D; n++) {
+        int nzmax = m->nlevels_nod2D[n], nzmin = m->ulevels_nod2D[n];
+        for (int nz = nzmin + 1; nz <= nzmax - 1; nz++) {
+            double dz = 0.5 * (m->hnode[IX1(nz - 1, n)] + m->hnode[IX1(nz, n)]);
+            tr_z[IXN(nz, n)] = (ttf[IX1(nz - 1, n)] - ttf[IX1(nz, n)]) / dz;
+        }
+        tr_z[IXN(nzmin, n)] = 0.0;
+        tr_z[IXN(nzmax, n)] = 0.0;
+    }
+}
+
+/* area-weighted mean of tr_xy over the node's elements that are wet at nz */
+static inline void node_mean_grad(const or_mesh *m, const double *tr_xy, int node, int nz, double *gx,
+                                  double *gy) {
+    const int L1 = m->nl - 1;
+    double tvol = 0.0, tx = 0.0, ty = 0.0;
+    for (int k = m->nod_in_elem2D_ptr[node]; k < m->nod_in_elem2D_ptr[node + 1]; k++) {
+        int elem = m->nod_in_elem2D[k];
+        if (m->nlevels[elem] - 1 < nz || nz < m->ulevels[elem]) continue;
+        tvol = tvol + m->elem_area[elem];
+        tx = tx + tr_xy[2 * IX1(nz, elem)] * m->elem_area[elem];
+        ty = ty + tr_xy[2 * IX1(nz, elem) + 1] * m->elem_area[elem];
+    }
+    *gx = tx / tvol;
+    *gy = ty / tvol;
+}
+
+void or_fill_up_dn_grad(const or_mesh *m, or_work *w) {
+    const int L1 = m->nl - 1;
+    double *G = w->edge_up_dn_grad;
+#define GR(k, nz, e) G[4 * IX1(nz, e) + (k) - 1]
+    OMP_FOR
+    for (int edge = 0; edge < m->edge2D; edge++) {
+        int ed[2] = {m->edges[2 * edge], m->edges[2 * edge + 1]};
+        int up = w->edge_up_dn_tri[2 * edge], dn = w->edge_up_dn_tri[2 * edge + 1];
+        double gx, gy;
+        if (up >= 0 && dn >= 0) {
+            int nzmin = m->ulevels_nod2D_max[ed[0]] > m->ulevels_nod2D_max[ed[1]] ? m->ulevels_nod2D_max[ed[0]]
+                                                                                 : m->ulevels_nod2D_max[ed[1]];
+            int nzmax = m->nlevels_nod2D_min[ed[0]] < m->nlevels_nod2D_min[ed[1]] ? m->nlevels_nod2D_min[ed[0]]
+                                                                                 : m->nlevels_nod2D_min[ed[1]];
+            for (int nz = m->ulevels_nod2D[ed[0]]; nz <= nzmin - 1; nz++) {
+                node_mean_grad(m, w->tr_xy, ed[0], nz, &gx, &gy);
+                GR(1, nz, edge) = gx; GR(3, nz, edge) = gy;
+            }
+            for (int nz = m->ulevels_nod2D[ed[1]]; nz <= nzmin - 1; nz++) {
+                node_mean_grad(m, w->tr_xy, ed[1], nz, &gx, &gy);
+                GR(2, nz, edge) = gx; GR(4, nz, edge) = gy;
+            }
+            for (int nz = nzmin; nz <= nzmax - 1; nz++) {
+                GR(1, nz, edge) = w->tr_xy[2 * IX1(nz, up)];
+                GR(2, nz, edge) = w->tr_xy[2 * IX1(nz, dn)];
+                GR(3, nz, edge) = w->tr_xy[2 * IX1(nz, up) + 1];
+                GR(4, nz, edge) = w->tr_xy[2 * IX1(nz, dn) + 1];
+            }
+            for (int nz = nzmax; nz <= m->nlevels_nod2D[ed[0]] - 1; nz++) {
+                node_mean_grad(m, w->tr_xy, ed[0], nz, &gx, &gy);
+                GR(1, nz, edge) = gx; GR(3, nz, edge) = gy;
+            }
+            for (int nz = nzmax; nz <= m->nlevels_nod2D[ed[1]] - 1; nz++) {
+                node_mean_grad(m, w->tr_xy, ed[1], nz, &gx, &gy);
+                GR(2, nz, edge) = gx; GR(4, nz, edge) = gy;
+            }
+        } else {
+            for (int nz = m->ulevels_nod2D[ed[0]]; nz <= m->nlevels_nod2D[ed[0]] - 1; nz++) {
+                node_mean_grad(m, w->tr_xy, ed[0], nz, &gx, &gy);
+                GR(1, nz, edge) = gx; GR(3, nz, edge) = gy;
+            }
+            for (int nz = m->ulevels_nod2D[ed[1]]; nz <= m->nlevels_nod2D[ed[1]] - 1; nz++) {
+                node_mean_grad(m, w->tr_xy, ed[1], nz, &gx, &gy);
+                GR(2, nz, edge) = gx; GR(4, nz, edge) = gy;
+            }
+        }
+    }
+#undef GR
+}
+
+/* ========================================================================== */
+/* init_tracers_AB (src/oce_tracer_mod.F90:13-143)                             */
+/* ========================================================================== */
+void or_init_tracers_AB(const or_mesh *m, const or_tra_cfg *c, double *values, double *valuesAB,
+                        double *valuesold, or_work *w) {
+    const int L1 = m->nl - 1;
+    const size_t N = (size_t)L1 * (size_t)m->nod2D;
+    memset(w->del_ttf, 0, sizeof(double) * N);
+    memset(w->del_ttf_advhoriz, 0, sizeof(double) * N);
+    memset(w->del_ttf_advvert, 0, sizeof(double) * N);
+    if (c->ab_order == 2) {
+        const double ca = 0.5 + AB_EPSILON, cb = 1.5 + AB_EPSILON;
+        OMP_FOR
+        for (long i = 0; i < (long)N; i++) valuesAB[i] = -(ca * valuesold[i]) + cb * values[i];
+        OMP_FOR
+        for (long i = 0; i < (long)N; i++) valuesold[i] = values[i];
+    } else {
+        OMP_FOR
+        for (long i = 0; i < (long)N; i++) {
+            double v = 5.0 * valuesold[2 * i + 1] - 16.0 * valuesold[2 * i] + 23.0 * values[i];
+            valuesAB[i] = v / 12.0;
+        }
+        OMP_FOR
+        for (long i = 0; i < (long)N; i++) {
+            valuesold[2 * i + 1] = valuesold[2 * i];
+            valuesold[2 * i] = values[i];
+        }
+    }
+    or_tracer_gradient_elements(m, values, w->tr_xy);
+    or_tracer_gradient_z(m, values, w->tr_z);
+    or_fill_up_dn_grad(m, w);
+}
+
+/* ========================================================================== */
+/* horizontal fluxes (src/oce_adv_tra_hor.F90)                                 */
+/* ========================================================================== */
+typedef struct {
+    int n1, n2, el1, el2, nl1, nu1, nl2, nu2;
+    double dX1, dY1, dX2, dY2, a;
+} edge_geo;
+
+static inline void edge_setup(const or_mesh *m, int edge, edge_geo *g) {
+    g->n1 = m->edges[2 * edge];
+    g->n2 = m->edges[2 * edge + 1];
+    g->el1 = m->edge_tri[2 * edge];
+    g->el2 = m->edge_tri[2 * edge + 1];
+    g->nl1 = m->nlevels[g->el1] - 1;
+    g->nu1 = m->ulevels[g->el1];
+    g->dX1 = m->edge_cross_dxdy[4 * edge + 0];
+    g->dY1 = m->edge_cross_dxdy[4 * edge + 1];
+    g->a = R_EARTH * m->elem_cos[g->el1];
+    g->nl2 = 0;
+    g->nu2 = 0;
+    g->dX2 = 0.0;
+    g->dY2 = 0.0;
+    if (g->el2 >= 0) {
+        g->dX2 = m->edge_cross_dxdy[4 * edge + 2];
+        g->dY2 = m->edge_cross_dxdy[4 * edge + 3];
+        g->nl2 = m->nlevels[g->el2] - 1;
+        g->nu2 = m->ulevels[g->el2];
+        g->a = 0.5 * (g->a + R_EARTH * m->elem_cos[g->el2]);
+    }
+}
+
+#define VEL(c, nz, el) vel[2 * IX1(nz, el) + (c) - 1]
+
+/* volume flux of segment 1, segment 2, both (oce_adv_tra_hor.F90:170,190,211-212) */
+static inline double vflux1(const or_mesh *m, const double *vel, const edge_geo *g, int nz) {
+    const int L1 = m->nl - 1;
+    return (-(VEL(2, nz, g->el1) * g->dX1) + VEL(1, nz, g->el1) * g->dY1) * m->helem[IX1(nz, g->el1)];
+}
+static inline double vflux2(const or_mesh *m, const double *vel, const edge_geo *g, int nz) {
+    const int L1 = m->nl - 1;
+    return (VEL(2, nz, g->el2) * g->dX2 - VEL(1, nz, g->el2) * g->dY2) * m->helem[IX1(nz, g->el2)];
+}
+static inline double vflux12(const or_mesh *m, const double *vel, const edge_geo *g, int nz) {
+    return vflux1(m, vel, g, nz) + vflux2(m, vel, g, nz);
+}
+
+void or_adv_tra_hor_upw1(const or_mesh *m, const double *vel, const double *ttf, double *flux, int init_zero) {
+    const int L1 = m->nl - 1;
+    if (init_zero) memset(flux, 0, sizeof(double) * (size_t)L1 * (size_t)m->edge2D);
+    OMP_FOR
+    for (int edge = 0; edge < m->edge2D; edge++) {
+        edge_geo g;
+        edge_setup(m, edge, &g);
+        int nl12 = g.nl1 < g.nl2 ? g.nl1 : g.nl2;
+        int nu12 = g.nu1 > g.nu2 ? g.nu1 : g.nu2;
+#define UPW(vf)                                                                                          \
+    flux[IX1(nz, edge)] = -(0.5 * (ttf[IX1(nz, g.n1)] * ((vf) + fabs(vf)) + ttf[IX1(nz, g.n2)] * ((vf) - fabs(vf)))) - \
+                          flux[IX1(nz, edge)]
+        for (int nz = g.nu1; nz <= nu12 - 1; nz++) { double vf = vflux1(m, vel, &g, nz); UPW(vf); }
+        if (g.nu2 > 0)
+            for (int nz = g.nu2; nz <= nu12 - 1; nz++) { double vf = vflux2(m, vel, &g, nz); UPW(vf); }
+        for (int nz = nu12; nz <= nl12; nz++) { double vf = vflux12(m, vel, &g, nz); UPW(vf); }
+        for (int nz = nl12 + 1; nz <= g.nl1; nz++) { double vf = vflux1(m, vel, &g, nz); UPW(vf); }
+        for (int nz = nl12 + 1; nz <= g.nl2; nz++) { double vf = vflux2(m, vel, &g, nz); UPW(vf); }
+#undef UPW
+    }
+}
+
+/* MUSCL (use_clo = 1, :261-542) and MFCT (use_clo = 0, :546-834) */
+static void hor_ho(const or_mesh *m, const double *vel, const double *ttf, double num_ord, double *flux,
+                   const double *G, const int *nboundary_lay, int use_clo, int init_zero) {
+    const int L1 = m->nl - 1;
+    if (init_zero) memset(flux, 0, sizeof(double) * (size_t)L1 * (size_t)m->edge2D);
+    OMP_FOR
+    for (int edge = 0; edge < m->edge2D; edge++) {
+        edge_geo g;
+        edge_setup(m, edge, &g);
+        int nl12 = g.nl1 < g.nl2 ? g.nl1 : g.nl2;
+        int nu12 = g.nu1 > g.nu2 ? g.nu1 : g.nu2;
+        const double ex = m->edge_dxdy[2 * edge], ey = m->edge_dxdy[2 * edge + 1];
+#define HO(vf)                                                                                                 \
+    do {                                                                                                       \
+        double t1 = ttf[IX1(nz, g.n1)], t2 = ttf[IX1(nz, g.n2)];                                               \
+        const double *gg = &G[4 * IX1(nz, edge)];                                                              \
+        double Tmean2, Tmean1;                                                                                 \
+        if (use_clo) {                                                                                         \
+            double clo1 = (nboundary_lay[g.n1] - nz) >= 0 ? 1.0 : 0.0;                                         \
+            double clo2 = (nboundary_lay[g.n2] - nz) >= 0 ? 1.0 : 0.0;                                         \
+            Tmean2 = t2 - (2.0 * (t2 - t1) + ex * g.a * gg[1] + ey * R_EARTH * gg[3]) / 6.0 * clo2;           \
+            Tmean1 = t1 + (2.0 * (t2 - t1) + ex * g.a * gg[0] + ey * R_EARTH * gg[2]) / 6.0 * clo1;           \
+        } else {                                                                                               \
+            Tmean2 = t2 - (2.0 * (t2 - t1) + ex * g.a * gg[1] + ey * R_EARTH * gg[3]) / 6.0;                  \
+            Tmean1 = t1 + (2.0 * (t2 - t1) + ex * g.a * gg[0] + ey * R_EARTH * gg[2]) / 6.0;                  \
+        }                                                                                                      \
+        double cHO = ((vf) + fabs(vf)) * Tmean1 + ((vf) - fabs(vf)) * Tmean2;                                  \
+        flux[IX1(nz, edge)] =                                                                                  \
+            -(0.5 * (1.0 - num_ord) * cHO) - (vf) * num_ord * 0.5 * (Tmean1 + Tmean2) - flux[IX1(nz, edge)];   \
+    } while (0)
+        for (int nz = g.nu1; nz <= nu12 - 1; nz++) { double vf = vflux1(m, vel, &g, nz); HO(vf); }
+        if (g.nu2 > 0)
+            for (int nz = g.nu2; nz <= nu12 - 1; nz++) { double vf = vflux2(m, vel, &g, nz); HO(vf); }
+        for (int nz = nu12; nz <= nl12; nz++) { double vf = vflux12(m, vel, &g, nz); HO(vf); }
+        for (int nz = nl12 + 1; nz <= g.nl1; nz++) { double vf = vflux1(m, vel, &g, nz); HO(vf); }
+        for (int nz = nl12 + 1; nz <= g.nl2; nz++) { double vf = vflux2(m, vel, &g, nz); HO(vf); }
+#undef HO
+    }
+}
+
+void or_adv_tra_hor_muscl(const or_mesh *m, const double *vel, const double *ttf, double num_ord, double *flux,
+                          const double *edge_up_dn_grad, const int *nboundary_lay, int init_zero) {
+    hor_ho(m, vel, ttf, num_ord, flux, edge_up_dn_grad, nboundary_lay, 1, init_zero);
+}
+void or_adv_tra_hor_mfct(const or_mesh *m, const double *vel, const double *ttf, double num_ord, double *flux,
+                         const double *edge_up_dn_grad, int init_zero) {
+    hor_ho(m, vel, ttf, num_ord, flux, edge_up_dn_grad, NULL, 0, init_zero);
+}
+
+/* ========================================================================== */
+/* vertical fluxes (src/oce_adv_tra_ver.F90:244-434)                           */
+/* ========================================================================== */
+void or_adv_tra_ver_upw1(const or_mesh *m, const double *W, const double *ttf, double *flux, int init_zero) {
+    const int NL = m->nl, L1 = NL - 1;
+    if (init_zero) memset(flux, 0, sizeof(double) * (size_t)NL * (size_t)m->nod2D);
+    OMP_FOR
+    for (int n = 0; n < m->nod2D; n++) {
+        int nzmax = m->nlevels_nod2D[n], nzmin = m->ulevels_nod2D[n];
+        int nz = nzmin;
+        flux[IXN(nz, n)] = -(W[IXN(nz, n)] * ttf[IX1(nz, n)] * m->area[IXN(nz, n)]) - flux[IXN(nz, n)];
+        nz = nzmax;
+        flux[IXN(nz, n)] = 0.0 - flux[IXN(nz, n)];
+        for (nz = nzmin + 1; nz <= nzmax - 1; nz++) {
+            double Wv = W[IXN(nz, n)];
+            flux[IXN(nz, n)] = -(0.5 * (ttf[IX1(nz, n)] * (Wv + fabs(Wv)) + ttf[IX1(nz - 1, n)] * (Wv - fabs(Wv))) *
+                                 m->area[IXN(nz, n)]) -
+                               flux[IXN(nz, n)];
+        }
+    }
+}
+
+void or_adv_tra_ver_qr4c(const or_mesh *m, const double *W, const double *ttf, double num_ord, double *flux,
+                         int init_zero) {
+    const int NL = m->nl, L1 = NL - 1;
+    if (init_zero) memset(flux, 0, sizeof(double) * (size_t)NL * (size_t)m->nod2D);
+    const double *Zn = m->Z_3d_n, *zb = m->zbar_3d_n;
+    OMP_FOR
+    for (int n = 0; n < m->nod2D; n++) {
+        int nzmax = m->nlevels_nod2D[n], nzmin = m->ulevels_nod2D[n];
+        int nz = nzmin;
+        flux[IXN(nz, n)] = -(ttf[IX1(nz, n)] * W[IXN(nz, n)] * m->area[IXN(nz, n)]) - flux[IXN(nz, n)];
+        nz = nzmin + 1;
+        flux[IXN(nz, n)] = -(0.5 * (ttf[IX1(nz - 1, n)] + ttf[IX1(nz, n)]) * W[IXN(nz, n)] * m->area[IXN(nz, n)]) -
+                           flux[IXN(nz, n)];
+        nz = nzmax - 1;
+        flux[IXN(nz, n)] = -(0.5 * (ttf[IX1(nz - 1, n)] + ttf[IX1(nz, n)]) * W[IXN(nz, n)] * m->area[IXN(nz, n)]) -
+                           flux[IXN(nz, n)];
+        nz = nzmax;
+        flux[IXN(nz, n)] = 0.0 - flux[IXN(nz, n)];
+        for (nz = nzmin + 2; nz <= nzmax - 2; nz++) {
+            double qc = (ttf[IX1(nz - 1, n)] - ttf[IX1(nz, n)]) / (Zn[IX1(nz - 1, n)] - Zn[IX1(nz, n)]);
+            double qu = (ttf[IX1(nz, n)] - ttf[IX1(nz + 1, n)]) / (Zn[IX1(nz, n)] - Zn[IX1(nz + 1, n)]);
+            double qd = (ttf[IX1(nz - 2, n)] - ttf[IX1(nz - 1, n)]) / (Zn[IX1(nz - 2, n)] - Zn[IX1(nz - 1, n)]);
+            double Tmean1 = ttf[IX1(nz, n)] + (2.0 * qc + qu) * (zb[IXN(nz, n)] - Zn[IX1(nz, n)]) / 3.0;
+            double Tmean2 = ttf[IX1(nz - 1, n)] + (2.0 * qc + qd) * (zb[IXN(nz, n)] - Zn[IX1(nz - 1, n)]) / 3.0;
+            double Wv = W[IXN(nz, n)];
+            double Tmean = (Wv + fabs(Wv)) * Tmean1 + (Wv - fabs(Wv)) * Tmean2;
+            flux[IXN(nz, n)] = (-(0.5 * (1.0 - num_ord) * Tmean) - num_ord * (0.5 * (Tmean1 + Tmean2)) * Wv) *
+                                   m->area[IXN(nz, n)] -
+                               flux[IXN(nz, n)];
+        }
+    }
+}
+
+/* ========================================================================== */
+/* FCT limiter (src/oce_adv_tra_fct.F90:72-512)                                */
+/* ========================================================================== */
+static inline void edge_scatter_range(const or_mesh *m, int edge, int *nu12, int *nl12) {
+    int el1 = m->edge_tri[2 * edge], el2 = m->edge_tri[2 * edge + 1];
+    int nl1 = m->nlevels[el1] - 1, nu1 = m->ulevels[el1];
+    int nl2 = 0, nu2 = 0;
+    if (el2 >= 0) {
+        nl2 = m->nlevels[el2] - 1;
+        nu2 = m->ulevels[el2];
+    }
+    *nl12 = nl1 > nl2 ? nl1 : nl2;
+    *nu12 = nu1;
+    if (nu2 > 0) *nu12 = nu1 < nu2 ? nu1 : nu2;
+}
+
+void or_oce_tra_adv_fct(const or_mesh *m, double dt, const double *ttf, const double *lo, double *adf_h,
+                        double *adf_v, or_work *w) {
+    const int NL = m->nl, L1 = NL - 1;
+    const double flux_eps = 1e-16, bignumber = 1e3;
+    double *fmax = w->fct_ttf_max, *fmin = w->fct_ttf_min, *fplus = w->fct_plus, *fminus = w->fct_minus;
+    double *tmax = w->tvert_max, *tmin = w->tvert_min;
+    double *AUX = w->edge_up_dn_grad; /* AUX(1:2, nz, elem) aliases edge_up_dn_grad */
+#define AUXA(k, nz, el) AUX[4 * IX1(nz, el) + (k) - 1]
+    locks_ensure(m->nod2D);
+    /* a1 */
+    OMP_FOR
+    for (int n = 0; n < m->nod2D; n++)
+        for (int nz = m->ulevels_nod2D[n]; nz <= m->nlevels_nod2D[n] - 1; nz++) {
+            fmax[IX1(nz, n)] = dmax(lo[IX1(nz, n)], ttf[IX1(nz, n)]);
+            fmin[IX1(nz, n)] = dmin(lo[IX1(nz, n)], ttf[IX1(nz, n)]);
+        }
+    /* a2 */
+    OMP_FOR
+    for (int elem = 0; elem < m->elem2D; elem++) {
+        const int *en = &m->elem2D_nodes[3 * elem];
+        int nu1 = m->ulevels[elem], nl1 = m->nlevels[elem];
+        if (nu1 > 1)
+            for (int nz = 1; nz <= nu1 - 1; nz++) { AUXA(1, nz, elem) = -bignumber; AUXA(2, nz, elem) = bignumber; }
+        for (int nz = nu1; nz <= nl1 - 1; nz++) {
+            AUXA(1, nz, elem) = dmax(dmax(fmax[IX1(nz, en[0])], fmax[IX1(nz, en[1])]), fmax[IX1(nz, en[2])]);
+            AUXA(2, nz, elem) = dmin(dmin(fmin[IX1(nz, en[0])], fmin[IX1(nz, en[1])]), fmin[IX1(nz, en[2])]);
+        }
+        if (nl1 <= NL - 1)
+            for (int nz = nl1; nz <= NL - 1; nz++) { AUXA(1, nz, elem) = -bignumber; AUXA(2, nz, elem) = bignumber; }
+    }
+    /* a3 */
+    OMP_FOR
+    for (int n = 0; n < m->nod2D; n++) {
+        int k0 = m->nod_in_elem2D_ptr[n], k1 = m->nod_in_elem2D_ptr[n + 1];
+        for (int nz = m->ulevels_nod2D[n]; nz <= m->nlevels_nod2D[n] - 1; nz++) {
+            tmax[IX1(nz, n)] = AUXA(1, nz, m->nod_in_elem2D[k0]);
+            tmin[IX1(nz, n)] = AUXA(2, nz, m->nod_in_elem2D[k0]);
+            for (int k = k0 + 1; k < k1; k++) {
+                tmax[IX1(nz, n)] = dmax(tmax[IX1(nz, n)], AUXA(1, nz, m->nod_in_elem2D[k]));
+                tmin[IX1(nz, n)] = dmin(tmin[IX1(nz, n)], AUXA(2, nz, m->nod_in_elem2D[k]));
+            }
+        }
+    }
+    /* bound increments */
+    OMP_FOR
+    for (int n = 0; n < m->nod2D; n++) {
+        int nu1 = m->ulevels_nod2D[n], nl1 = m->nlevels_nod2D[n];
+        fmax[IX1(nu1, n)] = tmax[IX1(nu1, n)] - lo[IX1(nu1, n)];
+        fmin[IX1(nu1, n)] = tmin[IX1(nu1, n)] - lo[IX1(nu1, n)];
+        for (int nz = nu1 + 1; nz <= nl1 - 2; nz++) {
+            fmax[IX1(nz, n)] = dmax(dmax(tmax[IX1(nz - 1, n)], tmax[IX1(nz, n)]), tmax[IX1(nz + 1, n)]) - lo[IX1(nz, n)];
+            fmin[IX1(nz, n)] = dmin(dmin(tmin[IX1(nz - 1, n)], tmin[IX1(nz, n)]), tmin[IX1(nz + 1, n)]) - lo[IX1(nz, n)];
+        }
+        int nz = nl1 - 1;
+        fmax[IX1(nz, n)] = tmax[IX1(nz, n)] - lo[IX1(nz, n)];
+        fmin[IX1(nz, n)] = tmin[IX1(nz, n)] - lo[IX1(nz, n)];
+    }
+    /* b1: vertical part */
+    OMP_FOR
+    for (int n = 0; n < m->nod2D; n++)
+        for (int nz = m->ulevels_nod2D[n]; nz <= m->nlevels_nod2D[n] - 1; nz++) {
+            fplus[IX1(nz, n)] = 0.0;
+            fminus[IX1(nz, n)] = 0.0;
+        }
+    OMP_FOR
+    for (int n = 0; n < m->nod2D; n++)
+        for (int nz = m->ulevels_nod2D[n]; nz <= m->nlevels_nod2D[n] - 1; nz++) {
+            fplus[IX1(nz, n)] = fplus[IX1(nz, n)] + (dmax(0.0, adf_v[IXN(nz, n)]) + dmax(0.0, -adf_v[IXN(nz + 1, n)]));
+            fminus[IX1(nz, n)] = fminus[IX1(nz, n)] + (dmin(0.0, adf_v[IXN(nz, n)]) + dmin(0.0, -adf_v[IXN(nz + 1, n)]));
+        }
+    /* b1: horizontal scatter */
+    OMP_FOR
+    for (int edge = 0; edge < m->edge2D; edge++) {
+        int n1 = m->edges[2 * edge], n2 = m->edges[2 * edge + 1], nu12, nl12;
+        edge_scatter_range(m, edge, &nu12, &nl12);
+        LOCK(n1);
+        for (int nz = nu12; nz <= nl12; nz++) {
+            fplus[IX1(nz, n1)] = fplus[IX1(nz, n1)] + dmax(0.0, adf_h[IX1(nz, edge)]);
+            fminus[IX1(nz, n1)] = fminus[IX1(nz, n1)] + dmin(0.0, adf_h[IX1(nz, edge)]);
+        }
+        UNLOCK(n1);
+        LOCK(n2);
+        for (int nz = nu12; nz <= nl12; nz++) {
+            fplus[IX1(nz, n2)] = fplus[IX1(nz, n2)] + dmax(0.0, -adf_h[IX1(nz, edge)]);
+            fminus[IX1(nz, n2)] = fminus[IX1(nz, n2)] + dmin(0.0, -adf_h[IX1(nz, edge)]);
+        }
+        UNLOCK(n2);
+    }
+    /* b2 */
+    OMP_FOR
+    for (int n = 0; n < m->nod2D; n++)
+        for (int nz = m->ulevels_nod2D[n]; nz <= m->nlevels_nod2D[n] - 1; nz++) {
+            double flux = fplus[IX1(nz, n)] * dt / m->areasvol[IXN(nz, n)] / m->hnode_new[IX1(nz, n)] + flux_eps;
+            fplus[IX1(nz, n)] = dmin(1.0, fmax[IX1(nz, n)] / flux);
+            flux = fminus[IX1(nz, n)] * dt / m->areasvol[IXN(nz, n)] / m->hnode_new[IX1(nz, n)] - flux_eps;
+            fminus[IX1(nz, n)] = dmin(1.0, fmin[IX1(nz, n)] / flux);
+        }
+    /* b3: vertical */
+    OMP_FOR
+    for (int n = 0; n < m->nod2D; n++) {
+        int nu1 = m->ulevels_nod2D[n], nl1 = m->nlevels_nod2D[n];
+        int nz = nu1;
+        double ae = 1.0, flux = adf_v[IXN(nz, n)];
+        if (flux >= 0.0) ae = dmin(ae, fplus[IX1(nz, n)]);
+        else ae = dmin(ae, fminus[IX1(nz, n)]);
+        adf_v[IXN(nz, n)] = ae * adf_v[IXN(nz, n)];
+        for (nz = nu1 + 1; nz <= nl1 - 1; nz++) {
+            ae = 1.0;
+            flux = adf_v[IXN(nz, n)];
+            if (flux >= 0.0) {
+                ae = dmin(ae, fminus[IX1(nz - 1, n)]);
+                ae = dmin(ae, fplus[IX1(nz, n)]);
+            } else {
+                ae = dmin(ae, fplus[IX1(nz - 1, n)]);
+                ae = dmin(ae, fminus[IX1(nz, n)]);
+            }
+            adf_v[IXN(nz, n)] = ae * adf_v[IXN(nz, n)];
+        }
+    }
+    /* b3: horizontal */
+    OMP_FOR
+    for (int edge = 0; edge < m->edge2D; edge++) {
+        int n1 = m->edges[2 * edge], n2 = m->edges[2 * edge + 1], nu12, nl12;
+        edge_scatter_range(m, edge, &nu12, &nl12);
+        for (int nz = nu12; nz <= nl12; nz++) {
+            double ae = 1.0, flux = adf_h[IX1(nz, edge)];
+            if (flux >= 0.0) {
+                ae = dmin(ae, fplus[IX1(nz, n1)]);
+                ae = dmin(ae, fminus[IX1(nz, n2)]);
+            } else {
+                ae = dmin(ae, fminus[IX1(nz, n1)]);
+                ae = dmin(ae, fplus[IX1(nz, n2)]);
+            }
+            adf_h[IX1(nz, edge)] = ae * adf_h[IX1(nz, edge)];
+        }
+    }
+#undef AUXA
+}
+
+/* ========================================================================== */
+/* oce_tra_adv_flux2dtracer (src/oce_adv_tra_driver.F90:494-646)               */
+/* ========================================================================== */
+void or_oce_tra_adv_flux2dtracer(const or_mesh *m, double dt, double *dttf_h, double *dttf_v,
+                                 const double *flux_h, const double *flux_v, int use_lo, const double *ttf,
+                                 const double *lo) {
+    const int NL = m->nl, L1 = NL - 1;
+    locks_ensure(m->nod2D);
+    if (use_lo) {
+        OMP_FOR
+        for (int n = 0; n < m->nod2D; n++)
+            for (int nz = m->ulevels_nod2D[n]; nz <= m->nlevels_nod2D[n] - 1; nz++)
+                dttf_v[IX1(nz, n)] = dttf_v[IX1(nz, n)] - ttf[IX1(nz, n)] * m->hnode[IX1(nz, n)] +
+                                     lo[IX1(nz, n)] * m->hnode_new[IX1(nz, n)];
+    }
+    OMP_FOR
+    for (int n = 0; n < m->nod2D; n++)
+        for (int nz = m->ulevels_nod2D[n]; nz <= m->nlevels_nod2D[n] - 1; nz++)
+            dttf_v[IX1(nz, n)] = dttf_v[IX1(nz, n)] + (flux_v[IXN(nz, n)] - flux_v[IXN(nz + 1, n)]) * dt /
+                                                          m->areasvol[IXN(nz, n)];
+    OMP_FOR
+    for (int edge = 0; edge < m->edge2D; edge++) {
+        int n1 = m->edges[2 * edge], n2 = m->edges[2 * edge + 1], nu12, nl12;
+        edge_scatter_range(m, edge, &nu12, &nl12);
+        LOCK(n1);
+        for (int nz = nu12; nz <= nl12; nz++)
+            dttf_h[IX1(nz, n1)] = dttf_h[IX1(nz, n1)] + flux_h[IX1(nz, edge)] * dt / m->areasvol[IXN(nz, n1)];
+        UNLOCK(n1);
+        LOCK(n2);
+        for (int nz = nu12; nz <= nl12; nz++)
+            dttf_h[IX1(nz, n2)] = dttf_h[IX1(nz, n2)] - flux_h[IX1(nz, edge)] * dt / m->areasvol[IXN(nz, n2)];
+        UNLOCK(n2);
+    }
+}
+
+/* ========================================================================== */
+/* do_oce_adv_tra (src/oce_adv_tra_driver.F90:46-490)                          */
+/* ========================================================================== */
+int or_do_oce_adv_tra(const or_mesh *m, double dt, const double *vel, const double *W, const double *WI,
+                      const double *WE, const or_tra_cfg *c, const double *ttf, const double *ttfAB,
+                      or_work *w) {
+    (void)WI;
+    const int NL = m->nl, L1 = NL - 1;
+    locks_ensure(m->nod2D);
+    if (c->hor < 0 || c->hor > 2 || c->ver < 0 || c->ver > 1) return 1;
+    double *fct_LO = w->fct_LO, *afh = w->adv_flux_hor, *afv = w->adv_flux_ver;
+    if (c->lim_fct) {
+        or_adv_tra_hor_upw1(m, vel, ttf, afh, 1);
+        OMP_FOR
+        for (long i = 0; i < (long)L1 * m->nod2D; i++) fct_LO[i] = 0.0;
+        OMP_FOR
+        for (int e = 0; e < m->edge2D; e++) {
+            int n1 = m->edges[2 * e], n2 = m->edges[2 * e + 1], nu12, nl12;
+            edge_scatter_range(m, e, &nu12, &nl12);
+            LOCK(n1);
+            for (int nz = nu12; nz <= nl12; nz++) fct_LO[IX1(nz, n1)] = fct_LO[IX1(nz, n1)] + afh[IX1(nz, e)];
+            UNLOCK(n1);
+            LOCK(n2);
+            for (int nz = nu12; nz <= nl12; nz++) fct_LO[IX1(nz, n2)] = fct_LO[IX1(nz, n2)] - afh[IX1(nz, e)];
+            UNLOCK(n2);
+        }
+        or_adv_tra_ver_upw1(m, WE, ttf, afv, 1);
+        OMP_FOR
+        for (int n = 0; n < m->nod2D; n++)
+            for (int nz = m->ulevels_nod2D[n]; nz <= m->nlevels_nod2D[n] - 1; nz++)
+                fct_LO[IX1(nz, n)] = (ttf[IX1(nz, n)] * m->hnode[IX1(nz, n)] +
+                                      (fct_LO[IX1(nz, n)] + (afv[IXN(nz, n)] - afv[IXN(nz + 1, n)])) * dt /
+                                          m->areasvol[IXN(nz, n)]) /
+                                     m->hnode_new[IX1(nz, n)];
+    }
+    int zero = c->lim_fct ? 0 : 1;
+    if (c->hor == OR_HOR_MUSCL)
+        or_adv_tra_hor_muscl(m, vel, ttfAB, c->ph, afh, w->edge_up_dn_grad, w->nboundary_lay, zero);
+    else if (c->hor == OR_HOR_MFCT)
+        or_adv_tra_hor_mfct(m, vel, ttfAB, c->ph, afh, w->edge_up_dn_grad, zero);
+    else
+        or_adv_tra_hor_upw1(m, vel, ttfAB, afh, zero);
+    const double *pw = c->lim_fct ? W : WE;
+    if (c->ver == OR_VER_QR4C)
+        or_adv_tra_ver_qr4c(m, pw, ttfAB, c->pv, afv, zero);
+    else
+        or_adv_tra_ver_upw1(m, pw, ttfAB, afv, zero);
+    if (c->lim_fct) {
+        or_oce_tra_adv_fct(m, dt, ttf, fct_LO, afh, afv, w);
+        or_oce_tra_adv_flux2dtracer(m, dt, w->del_ttf_advhoriz, w->del_ttf_advvert, afh, afv, 1, ttf, fct_LO);
+    } else {
+        or_oce_tra_adv_flux2dtracer(m, dt, w->del_ttf_advhoriz, w->del_ttf_advvert, afh, afv, 0, NULL, NULL);
+    }
+    return 0;
+}
+
+/* ========================================================================== */
+/* diff_ver_part_impl_ale (src/oce_ale_tracer.F90:907-1435)                    */
+/* ========================================================================== */
+void or_diff_ver_part_impl_ale(const or_mesh *m, double dt, const double *Kv, const double *bc_surf,
+                               double *values) {
+    const int NL = m->nl, L1 = NL - 1;
+    OMP_FOR
+    for (int n = 0; n < m->nod2D; n++) {
+        double a[NL + 1], b[NL + 1], c[NL + 1], tr[NL + 1], cp[NL + 1], tp[NL + 1];
+        double zbar_n[NL + 1], Z_n[NL + 1];
+        for (int k = 0; k <= NL; k++) { a[k] = b[k] = c[k] = tr[k] = tp[k] = cp[k] = 0.0; zbar_n[k] = 0.0; Z_n[k] = 0.0; }
+        const double *hn = &m->hnode_new[IX1(1, n)] - 1;   /* hn[nz], nz 1-based */
+        const double *ar = &m->area[IXN(1, n)] - 1;
+        const double *av = &m->areasvol[IXN(1, n)] - 1;
+        const double *kv = &Kv[IXN(1, n)] - 1;
+        double *T = &values[IX1(1, n)] - 1;
+        int nzmax = m->nlevels_nod2D[n], nzmin = m->ulevels_nod2D[n];
+        zbar_n[nzmax] = m->zbar_n_bot[n];
+        Z_n[nzmax - 1] = zbar_n[nzmax] + hn[nzmax - 1] / 2.0;
+        for (int nz = nzmax - 1; nz >= nzmin + 1; nz--) {
+            zbar_n[nz] = zbar_n[nz + 1] + hn[nz];
+            Z_n[nz - 1] = zbar_n[nz] + hn[nz - 1] / 2.0;
+        }
+        zbar_n[nzmin] = zbar_n[nzmin + 1] + hn[nzmin];
+        int nz = nzmin;
+        double zinv2 = 1.0 / (Z_n[nz] - Z_n[nz + 1]);
+        double zinv = 1.0 * dt;
+        a[nz] = 0.0;
+        c[nz] = -(kv[nz + 1] * zinv2 * zinv * ar[nz + 1] / av[nz]);
+        b[nz] = -c[nz] + hn[nz];
+        double zinv1 = zinv2;
+        for (nz = nzmin + 1; nz <= nzmax - 2; nz++) {
+            zinv2 = 1.0 / (Z_n[nz] - Z_n[nz + 1]);
+            a[nz] = -(kv[nz] * zinv1 * zinv * (ar[nz] / av[nz]));
+            c[nz] = -(kv[nz + 1] * zinv2 * zinv * ar[nz + 1] / av[nz]);
+            b[nz] = -a[nz] - c[nz] + hn[nz];
+            zinv1 = zinv2;
+        }
+        nz = nzmax - 1;
+        zinv = 1.0 * dt;
+        a[nz] = -(kv[nz] * zinv1 * zinv * (ar[nz] / av[nz]));
+        c[nz] = 0.0;
+        b[nz] = -a[nz] + hn[nz];
+        nz = nzmin;
+        double dz = hn[nz];
+        tr[nz] = -((b[nz] - dz) * T[nz]) - c[nz] * T[nz + 1];
+        for (nz = nzmin + 1; nz <= nzmax - 2; nz++) {
+            dz = hn[nz];
+            tr[nz] = -(a[nz] * T[nz - 1]) - (b[nz] - dz) * T[nz] - c[nz] * T[nz + 1];
+        }
+        nz = nzmax - 1;
+        dz = hn[nz];
+        tr[nz] = -(a[nz] * T[nz - 1]) - (b[nz] - dz) * T[nz];
+        tr[nzmin] = tr[nzmin] + bc_surf[n];
+        cp[nzmin] = c[nzmin] / b[nzmin];
+        tp[nzmin] = tr[nzmin] / b[nzmin];
+        for (nz = nzmin + 1; nz <= nzmax - 1; nz++) {
+            double mm = b[nz] - cp[nz - 1] * a[nz];
+            cp[nz] = c[nz] / mm;
+            tp[nz] = (tr[nz] - tp[nz - 1] * a[nz]) / mm;
+        }
+        tr[nzmax - 1] = tp[nzmax - 1];
+        for (nz = nzmax - 2; nz >= nzmin; nz--) tr[nz] = tp[nz] - cp[nz] * tr[nz + 1];
+        for (nz = nzmin; nz <= nzmax - 1; nz++) T[nz] = T[nz] + tr[nz];
+    }
+}
+
+/* ========================================================================== */
+/* per-tracer body of solve_tracers_ale (src/oce_ale_tracer.F90:303-351,       */
+/* 743-772)                                                                    */
+/* ========================================================================== */
+int or_tracer_step(const or_mesh *m, const or_tra_cfg *c, double dt, const double *vel, const double *W,
+                   const double *WI, const double *WE, const double *Kv, const double *bc_surf,
+                   double *values, double *valuesAB, double *valuesold, or_work *w) {
+    const int L1 = m->nl - 1;
+    if (c->ab_order != 2 && c->ab_order != 3) return 2;
+    or_init_tracers_AB(m, c, values, valuesAB, valuesold, w);
+    int rc = or_do_oce_adv_tra(m, dt, vel, W, WI, WE, c, values, valuesAB, w);
+    if (rc) return rc;
+    const size_t N = (size_t)L1 * (size_t)m->nod2D;
+    OMP_FOR
+    for (long i = 0; i < (long)N; i++) w->del_ttf[i] = w->del_ttf[i] + w->del_ttf_advhoriz[i] + w->del_ttf_advvert[i];
+    OMP_FOR
+    for (int n = 0; n < m->nod2D; n++) {
+        int nzmax = m->nlevels_nod2D[n] - 1, nzmin = m->ulevels_nod2D[n];
+        for (int nz = nzmin; nz <= nzmax; nz++) {
+            size_t i = IX1(nz, n);
+            w->del_ttf[i] = w->del_ttf[i] + values[i] * (m->hnode[i] - m->hnode_new[i]);
+            values[i] = values[i] + w->del_ttf[i] / m->hnode_new[i];
+        }
+    }
+    if (c->i_vert_diff) or_diff_ver_part_impl_ale(m, dt, Kv, bc_surf, values);
+    return 0;
+}

@@ -1,0 +1,126 @@
+/*
+ * tracer_oracle.h -- FP64 CPU restatement of FESOM2's tracer-transport step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the checker for the CUDA path: only the
+ * test suite, the smoke test and the benchmark's CPU-baseline leg may load it.
+ * The product library never links or calls it.
+ *
+ * Parity status: the reference (Fortran + MPI) cannot be compiled in this
+ * image and its own tests hold no golden vectors for this path, so the
+ * restatement is pinned only by the hand-derived known-answer tests under
+ * tests/golden/ ("parity unpinned" against the reference binary itself).
+ *
+ * Layout: every array keeps the reference's Fortran layout a(level, entity),
+ * i.e. index [entity * ld + (level - 1)] with ld = nl-1 or nl.  Entity
+ * indices are 0-based; edge_tri[2*e+1] < 0 marks a boundary edge.  Level
+ * counts (nlevels, ulevels, ...) keep the reference's 1-based values.
+ */
+#ifndef FESOM_TRACER_ORACLE_H
+#define FESOM_TRACER_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct or_mesh {
+    int nod2D, elem2D, edge2D, nl;
+    const int *elem2D_nodes;       /* 3*T2 */
+    const int *edges;              /* 2*E2 */
+    const int *edge_tri;           /* 2*E2 */
+    const int *nod_in_elem2D_ptr;  /* N2+1 */
+    const int *nod_in_elem2D;      /* nnz, ascending element order per node */
+    const int *nlevels, *ulevels;                 /* T2 */
+    const int *nlevels_nod2D, *ulevels_nod2D;     /* N2 */
+    const int *nlevels_nod2D_min, *ulevels_nod2D_max;
+    const double *coord_nod2D;     /* 2*N2 */
+    const double *elem_area, *elem_cos;           /* T2 */
+    const double *edge_dxdy;       /* 2*E2 */
+    const double *edge_cross_dxdy; /* 4*E2 */
+    const double *gradient_sca;    /* 6*T2 */
+    const double *area, *areasvol; /* nl*N2 */
+    const double *hnode, *hnode_new; /* (nl-1)*N2 */
+    const double *helem;           /* (nl-1)*T2 */
+    const double *Z_3d_n;          /* (nl-1)*N2 */
+    const double *zbar_3d_n;       /* nl*N2 */
+    const double *zbar_n_bot;      /* N2 */
+    double cyclic_length;
+} or_mesh;
+
+/* scheme tuple of T_TRACER_DATA (src/MOD_TRACER.F90:10-27) */
+enum { OR_HOR_MUSCL = 0, OR_HOR_MFCT = 1, OR_HOR_UPW1 = 2 };
+enum { OR_VER_QR4C = 0, OR_VER_UPW1 = 1 };
+typedef struct or_tra_cfg {
+    int hor, ver;
+    int lim_fct;       /* 1: 'FCT', 0: no limiter */
+    double ph, pv;     /* tra_adv_ph / tra_adv_pv */
+    int ab_order;      /* 2 or 3 */
+    int i_vert_diff;   /* implicit vertical diffusion on/off */
+} or_tra_cfg;
+
+/* T_TRACER_WORK (src/MOD_TRACER.F90:30-72) plus the module arrays tr_xy/tr_z */
+typedef struct or_work {
+    int *nboundary_lay;        /* N2 */
+    int *edge_up_dn_tri;       /* 2*E2, -1 = none */
+    double *edge_up_dn_grad;   /* 4*(nl-1)*E2 (also the FCT AUX array) */
+    double *tr_xy;             /* 2*(nl-1)*T2 */
+    double *tr_z;              /* nl*N2 */
+    double *fct_LO;            /* (nl-1)*N2 */
+    double *adv_flux_hor;      /* (nl-1)*E2 */
+    double *adv_flux_ver;      /* nl*N2 */
+    double *fct_ttf_max, *fct_ttf_min, *fct_plus, *fct_minus; /* (nl-1)*N2 */
+    double *tvert_max, *tvert_min;                           /* (nl-1)*N2 */
+    double *del_ttf, *del_ttf_advhoriz, *del_ttf_advvert;    /* (nl-1)*N2 */
+} or_work;
+
+/* threads: 1 = serial "exact" mode (edge scatters in ascending edge order);
+ * >1 = OpenMP mode with per-node locks around scatters, as the reference's
+ * default OpenMP build (nondeterministic at round-off level). */
+void or_set_threads(int nthreads);
+int or_get_threads(void);
+
+/* muscl_adv_init + find_up_downwind_triangles (src/oce_muscl_adv.F90:32-352) */
+void or_muscl_adv_init(const or_mesh *m, or_work *w);
+
+/* init_tracers_AB (src/oce_tracer_mod.F90:13-143) incl. gradients and fill_up_dn_grad */
+void or_init_tracers_AB(const or_mesh *m, const or_tra_cfg *c, double *values, double *valuesAB,
+                        double *valuesold, or_work *w);
+void or_tracer_gradient_elements(const or_mesh *m, const double *ttf, double *tr_xy);
+void or_tracer_gradient_z(const or_mesh *m, const double *ttf, double *tr_z);
+void or_fill_up_dn_grad(const or_mesh *m, or_work *w);
+
+/* individual flux routines (o_init_zero as in the reference) */
+void or_adv_tra_hor_upw1(const or_mesh *m, const double *vel, const double *ttf, double *flux, int init_zero);
+void or_adv_tra_hor_muscl(const or_mesh *m, const double *vel, const double *ttf, double num_ord, double *flux,
+                          const double *edge_up_dn_grad, const int *nboundary_lay, int init_zero);
+void or_adv_tra_hor_mfct(const or_mesh *m, const double *vel, const double *ttf, double num_ord, double *flux,
+                         const double *edge_up_dn_grad, int init_zero);
+void or_adv_tra_ver_upw1(const or_mesh *m, const double *W, const double *ttf, double *flux, int init_zero);
+void or_adv_tra_ver_qr4c(const or_mesh *m, const double *W, const double *ttf, double num_ord, double *flux,
+                         int init_zero);
+void or_oce_tra_adv_fct(const or_mesh *m, double dt, const double *ttf, const double *lo, double *adf_h,
+                        double *adf_v, or_work *w);
+void or_oce_tra_adv_flux2dtracer(const or_mesh *m, double dt, double *dttf_h, double *dttf_v,
+                                 const double *flux_h, const double *flux_v, int use_lo, const double *ttf,
+                                 const double *lo);
+
+/* do_oce_adv_tra (src/oce_adv_tra_driver.F90:46-490), use_wsplit = .false. */
+int or_do_oce_adv_tra(const or_mesh *m, double dt, const double *vel, const double *W, const double *WI,
+                      const double *WE, const or_tra_cfg *c, const double *ttf, const double *ttfAB,
+                      or_work *w);
+
+/* diff_ver_part_impl_ale (src/oce_ale_tracer.F90:907-1435), Redi/KPP/SW/icebergs off;
+ * bc_surf(n) is the bc_surface() value added at nzmin. */
+void or_diff_ver_part_impl_ale(const or_mesh *m, double dt, const double *Kv, const double *bc_surf,
+                               double *values);
+
+/* The per-tracer body of solve_tracers_ale (src/oce_ale_tracer.F90:303-351):
+ * init_tracers_AB, do_oce_adv_tra, del_ttf sum, diff_tracers_ale (T* update,
+ * implicit vertical diffusion).  Horizontal (Redi) diffusion is off. */
+int or_tracer_step(const or_mesh *m, const or_tra_cfg *c, double dt, const double *vel, const double *W,
+                   const double *WI, const double *WE, const double *Kv, const double *bc_surf,
+                   double *values, double *valuesAB, double *valuesold, or_work *w);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
