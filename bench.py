@@ -1,0 +1,413 @@
+#!/usr/bin/env python
+"""Tracer-step benchmark: tracer DOF-steps/s of the FESOM2 tracer transport step
+(init_tracers_AB + MUSCL/QR4C/FCT advection + T* update + implicit vertical
+diffusion) on one GB300, FP32 batched form vs FP64 plain form.
+
+Default workload: configuration 4 (icosahedral sphere, 9 subdivisions, 30%
+land, 70 z-levels 5->250 m with partial cells, 24 tracers: T, S and 22
+lognormal passive tracers), seeded synthetic inputs.  One "step" advances all
+tracers by dt.  The timed region replays the captured CUDA graph of the FP32
+batched step with every input resident in HBM (the working set, tens of GB,
+is far larger than L2, so no flush is needed).
+
+Also reported: the FP64 plain form (one tracer per launch), the end-to-end
+rate through the host-buffer C ABI (host->device copies of forcing and tracer
+state and device->host copies of the results inside the timed region), the
+roofline of the dominant kernel, and the CPU baseline (the FP64 oracle port,
+OpenMP on the host cores, on a bounded sample of the same workload).
+
+``--impl reference`` times the reference's CPU algorithm (the FP64 oracle
+restatement; the Fortran reference cannot be built here) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from fesom2_gb300 import mesh as M  # noqa: E402
+
+METRIC = "tracer DOF-steps/s, FP32-batched vs FP64-plain on 1 GB300; % of HBM BW"
+UNIT = "DOF-steps/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--config", type=int, default=4)
+    p.add_argument("--scale", type=float, default=1.0, help="shrink the mesh (tests only)")
+    p.add_argument("--tracers", type=int, default=None)
+    p.add_argument("--fp64-steps", type=int, default=2)
+    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--profile-only", action="store_true", help="one warm step + one profiled step (for ncu)")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def workload(cfg: int, scale: float, ntr_override):
+    t0 = time.time()
+    mesh = M.config_mesh(cfg, scale=scale)
+    kind = "channel" if cfg in (1, 2) else "sphere"
+    ntr = {1: 2, 2: 2, 3: 2, 4: 24}.get(cfg, 2) if ntr_override is None else ntr_override
+    dt = 600.0
+    forcing = M.make_forcing(mesh, kind, seed=11, dt=dt, kv_profile="const" if cfg == 1 else "surface")
+    tracers = M.make_tracers(mesh, kind, ntr=ntr, seed=5, dtype=np.float32)
+    gen_s = time.time() - t0
+    names = {1: "channel 100x400, 40 levels, 2 tracers", 2: "channel 400x1600, 60 levels, seamounts, 2 tracers",
+             3: "sphere 7 subdivisions, 48 levels, 2 tracers",
+             4: "sphere 9 subdivisions, 70 levels, 24 tracers (T, S, 22 lognormal)"}
+    return mesh, kind, forcing, tracers, dt, names.get(cfg, f"config {cfg}"), gen_s
+
+
+def algorithmic_bytes(counts, ntr, s):
+    """FCT-minimal dataflow bytes per step: s*[Ntr*(18 N3 + 3 E3) + 3 T3 + 14 N3]."""
+    N3, E3, T3 = counts["N3"], counts["E3"], counts["T3"]
+    return s * (ntr * (18 * N3 + 3 * E3) + 3 * T3 + 14 * N3)
+
+
+def stage_bytes(counts, ntr, s):
+    """Compulsory bytes per launch of each stage kernel of this implementation
+    (every input read once, every output written once, for ntr tracers):
+      ab:        read T, Told; write TAB, Told                      4 N3 per tracer
+      trxy:      read T; write 2 gradient components per element    N3 + 2 T3
+      edge_flux: read T, TAB (N3 each), gradients (2 T3); write FLO, ADh (2 E3); shared uv, helem (3 T3)
+      node_lo:   read T, TAB, FLO (E3); write LO, ADv;  shared w, we, area, hnode, hnode_new, areasvol, Z, zbar (8 N3)
+      bounds:    read T, LO; write bmax, bmin                       4 N3
+      rpm:       read ADv, ADh (E3), bmax, bmin; write R+, R-       5 N3 + E3; shared areasvol, hnode_new (2 N3)
+      update:    read T, LO, ADv, ADh (E3), R+, R-; write T         6 N3 + E3; shared hnode, hnode_new, areasvol (3 N3)
+      vdiff:     read T, write T (FP32: 4+4); shared Kv, area, areasvol, hnode_new (4 N3), FP64 scratch 3 x 2 x 8 B
+    """
+    N3, E3, T3 = counts["N3"], counts["E3"], counts["T3"]
+    return {
+        "ab": s * ntr * 4 * N3,
+        "trxy": s * ntr * (N3 + 2 * T3),
+        "edge_flux": s * (ntr * (2 * N3 + 2 * T3 + 2 * E3) + 3 * T3),
+        "node_lo": s * (ntr * (3 * N3 + E3) + 8 * N3),
+        "bounds": s * ntr * 4 * N3,
+        "rpm": s * (ntr * (5 * N3 + E3) + 2 * N3),
+        "update": s * (ntr * (6 * N3 + E3) + 3 * N3),
+        "vdiff": s * (ntr * 2 * N3 + 4 * N3) + ntr * 48 * N3,
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    def __init__(self, idx: int):
+        self.idx = idx
+        self.proc = None
+        self.out = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.out), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.out, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={q}", "--format=csv,noheader",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [l.strip().split(",") for l in open(self.out) if l.strip()]
+        except Exception:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1].split()[0]))
+                smax = float(r[2].split()[0])
+                for k, n in enumerate(names):
+                    if "Active" in r[5 + k] and "Not" not in r[5 + k]:
+                        reasons.add(n)
+            except Exception:
+                continue
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def cpu_rate(mesh, forcing, tracer64, dt, threads: int, max_dofs: float = 2.0e8):
+    """FP64 oracle (OpenMP, per-node locks as the reference's OpenMP build) on one
+    tracer step of the workload's mesh: DOF-steps/s."""
+    from oracle import oracle as O
+    O.set_threads(threads)
+    f = O.ensure_f64(M.Forcing(uv=forcing.uv, w=forcing.w, w_e=forcing.w_e, w_i=forcing.w_i, Kv=forcing.Kv,
+                               bc_surface=forcing.bc_surface, dt=dt))
+    om = O.OracleMesh(mesh)
+    T = np.ascontiguousarray(tracer64, dtype=np.float64)
+    Told = T.copy()
+    cfg = O.cfg_struct()
+    t0 = time.perf_counter()
+    om.tracer_step(f, cfg, T, np.zeros_like(T), Told)
+    el = time.perf_counter() - t0
+    N3 = mesh.counts()["N3"]
+    return N3 / el, el
+
+
+def run_reference(args, rank, world):
+    """Reference arm: the reference's CPU algorithm (FP64 oracle port, OpenMP on all
+    host cores), one tracer step of the workload's mesh per bench step."""
+    if rank != 0:
+        return
+    mesh, kind, forcing, tracers, dt, wname, _ = workload(args.config, args.scale, args.tracers)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_rate(mesh, forcing, tracers[0], dt, threads)
+    t = 0.0
+    rates = []
+    for _ in range(args.steps):
+        r, el = cpu_rate(mesh, forcing, tracers[0], dt, threads)
+        rates.append(r)
+        t += el
+    N3 = mesh.counts()["N3"]
+    value = N3 * args.steps / t
+    sample = f"1 tracer step of the {wname} mesh (N3 = {N3} DOF) per bench step"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wname, "cfg": args.config},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    from fesom2_gb300 import gpu as G
+    torch.cuda.set_device(local_rank)
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+
+    def barrier():
+        if dist:
+            tdist.barrier()
+        torch.cuda.synchronize()
+
+    mesh, kind, forcing, tracers, dt, wname, gen_s = workload(args.config, args.scale, args.tracers)
+    ntr = tracers.shape[0]
+    counts = mesh.counts()
+    N3 = counts["N3"]
+    cfgs = [G.tra_cfg("MUSCL", "QR4C", "FCT", 0.0, 1.0, id=(k + 1 if k < 2 else 100 + k)) for k in range(ntr)]
+    f32 = M.Forcing(uv=forcing.uv.astype(np.float32), w=forcing.w.astype(np.float32),
+                    w_e=forcing.w_e.astype(np.float32), w_i=forcing.w_i.astype(np.float32),
+                    Kv=forcing.Kv.astype(np.float32), bc_surface=None, dt=dt)
+    stream = torch.cuda.Stream()
+    res = {}
+
+    # ---------------- FP32 batched form, device-resident -------------------
+    ctx = G.Context(mesh, G.PREC_FP32, max_tracers=ntr)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.state_setup(cfgs)
+    ctx.forcing_upload(f32)
+    for k in range(ntr):
+        ctx.tracer_upload(k, tracers[k], tracers[k])
+    torch.cuda.synchronize()
+    launches = ctx.launches_per_step()
+    if args.profile_only:
+        ctx.run_steps(dt, 1, use_graph=True)
+        torch.cuda.synchronize()
+        prof = ctx.profile_step(dt)
+        if rank == 0:
+            print(json.dumps({"profile": prof}), flush=True)
+        return
+    ctx.run_steps(dt, args.warmup, use_graph=True)
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        barrier()
+        ev0.record(stream)
+        ctx.run_steps(dt, args.steps, use_graph=True)
+        ev1.record(stream)
+        barrier()
+    ms = ev0.elapsed_time(ev1)
+    st = ctx.status()
+    # per-stage times from profiled steps on the same stream
+    prof_steps = 2
+    agg = {}
+    for _ in range(prof_steps):
+        p = ctx.profile_step(dt)
+        for k, (t, n) in p.items():
+            a = agg.setdefault(k, [0.0, 0])
+            a[0] += t
+            a[1] += n
+    content = ctx.content()
+    ctx.close()
+    del ctx
+    torch.cuda.synchronize()
+
+    ms_t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if dist:
+        tdist.all_reduce(ms_t, op=tdist.ReduceOp.MAX)
+    ms_max = float(ms_t.item())
+    units = ntr * N3 * args.steps * world
+    value = units / (ms_max / 1e3)
+
+    # roofline of the dominant kernel
+    from json import load as jload
+    peaks = {}
+    try:
+        peaks = jload(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    sb = stage_bytes(counts, ntr, 4)
+    shares = {k: v[0] for k, v in agg.items() if v[1] > 0}
+    tot = sum(shares.values())
+    dom = max(shares, key=shares.get)
+    dom_ms = agg[dom][0] / agg[dom][1]
+    # bytes per launch: the stage model is per step; a step issues agg[dom][1]/prof_steps launches
+    per_launch_bytes = sb[dom] / (agg[dom][1] / prof_steps)
+    achieved = per_launch_bytes / (dom_ms / 1e3) / 1e9
+    step_bytes = algorithmic_bytes(counts, ntr, 4)
+    res["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                       "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_src,
+                       "share": shares[dom] / tot,
+                       "stage_ms_per_step": {k: v / prof_steps for k, v in shares.items()},
+                       "step_algorithmic_bytes": step_bytes,
+                       "step_achieved_gbs": step_bytes / (ms / args.steps / 1e3) / 1e9,
+                       "step_frac": step_bytes / (ms / args.steps / 1e3) / 1e9 / hbm_peak}
+
+    # ---------------- FP64 plain form (one tracer per launch) ---------------
+    if not args.no_fp64:
+        f64 = M.Forcing(uv=forcing.uv, w=forcing.w, w_e=forcing.w_e, w_i=forcing.w_i, Kv=forcing.Kv,
+                        bc_surface=None, dt=dt)
+        c64 = G.Context(mesh, G.PREC_FP64, max_tracers=ntr)
+        c64.set_stream(stream.cuda_stream)
+        c64.state_setup(cfgs)
+        c64.set_tracers_per_launch(1)
+        c64.forcing_upload(f64)
+        for k in range(ntr):
+            t64 = tracers[k].astype(np.float64)
+            c64.tracer_upload(k, t64, t64)
+        c64.run_steps(dt, 1, use_graph=True)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        c64.run_steps(dt, args.fp64_steps, use_graph=True)
+        e1.record(stream)
+        barrier()
+        ms64 = e0.elapsed_time(e1)
+        c64.close()
+        del c64
+        res["fp64_plain"] = {"value": ntr * N3 * args.fp64_steps / (ms64 / 1e3), "unit": UNIT,
+                             "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps,
+                             "tracers_per_launch": 1}
+        res["fp32_over_fp64"] = value / res["fp64_plain"]["value"]
+
+    # ---------------- end to end through host buffers -----------------------
+    if not args.no_e2e:
+        ce = G.Context(mesh, G.PREC_FP32, max_tracers=ntr)
+        ce.set_stream(stream.cuda_stream)
+        ce.state_setup(cfgs)
+        L1 = mesh.nl - 1
+        pin = lambda shape: torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy()
+        h_uv = pin(f32.uv.shape); h_uv[...] = f32.uv
+        h_w = pin(f32.w.shape); h_w[...] = f32.w
+        h_we = pin(f32.w_e.shape); h_we[...] = f32.w_e
+        h_kv = pin(f32.Kv.shape); h_kv[...] = f32.Kv
+        h_T = pin((ntr, mesh.nod2D, L1)); h_T[...] = tracers
+        h_O = pin((ntr, mesh.nod2D, L1)); h_O[...] = tracers
+        fe = M.Forcing(uv=h_uv, w=h_w, w_e=h_we, w_i=None, Kv=h_kv, bc_surface=None, dt=dt)
+
+        def e2e_step():
+            ce.forcing_upload(fe)
+            for k in range(ntr):
+                ce.tracer_upload(k, h_T[k], h_O[k])
+            ce.run_steps(dt, 1, use_graph=True)
+            for k in range(ntr):
+                ce._chk(ce.L.fesom_gpu_tracer_download_f32(ce.h, k, G._p(h_T[k]), G._p(h_O[k])))
+
+        e2e_step()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        e1.record(stream)
+        barrier()
+        mse = e0.elapsed_time(e1)
+        ce.close()
+        del ce
+        h2d = 4 * (h_uv.size + h_w.size + h_we.size + h_kv.size + 2 * ntr * mesh.nod2D * L1)
+        d2h = 4 * 2 * ntr * mesh.nod2D * L1
+        res["e2e"] = {"value": ntr * N3 * args.e2e_steps * world / (mse / 1e3), "unit": UNIT,
+                      "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                      "ms_per_step": mse / args.e2e_steps}
+
+    # ---------------- CPU baseline (rank 0, N = 1) ---------------------------
+    if not args.no_cpu and rank == 0 and world == 1:
+        threads = os.cpu_count() or 1
+        rate, el = cpu_rate(mesh, forcing, tracers[0], dt, threads)
+        res["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": f"1 tracer step of the full workload mesh (N3 = {N3}), "
+                                         f"FP64 oracle with OpenMP, {el:.1f} s"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": wname, "cfg": args.config, "tracers": ntr, "N3_per_tracer": N3,
+                           "E3": counts["E3"], "T3": counts["T3"], "nodes": counts["N2"], "levels": mesh.nl,
+                           "dt_s": dt, "l2": "inputs larger than L2 (no flush)",
+                           "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                           "mesh_generation_s": gen_s},
+                "gpu_launches": launches * args.steps,
+                "clocks": clk.summary(), "status_word": st,
+                "content_fp64": [float(c) for c in content[:2]]}
+        line.update(res)
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(local_rank)
+        tdist.init_process_group("nccl")
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,903 @@
+// capi.cu -- context management and the C ABI (include/fesom_gpu.h).
+//
+// The context owns every device allocation: topology and geometry copied at
+// fesom_gpu_init, forcing buffers, the tracer state and the per-stage work
+// arrays (sized once; no allocation per step).  All work goes to one stream.
+// The device-resident step is captured once into a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/fesom_gpu.h"
+#include "fesom_internal.h"
+#include "mesh_prep.h"
+
+using namespace fesom;
+
+struct fesom_gpu_ctx {
+    int prec = FESOM_PREC_FP64;
+    int max_tr = 1;
+    HostTopo ht;
+    int N2 = 0, E2 = 0, T2 = 0, nl = 0, L1 = 0, ibase = 1;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    std::vector<void *> allocs;
+    DTopo tp{};
+    DGeom<double> g64{};
+    DGeom<float> g32{};
+    // forcing (context precision)
+    void *uv = nullptr, *w = nullptr, *wi = nullptr, *we = nullptr, *Kv = nullptr, *bc = nullptr;
+    double *stage = nullptr;   // FP64 staging chunk for conversions
+    size_t stage_n = 0;
+    // tracer state
+    int ntr = 0;
+    int group = 0;             // tracers per launch (work arrays are sized for one group)
+    int group_cap = 0;         // tracers the work arrays can hold
+    int ab_max = 2;
+    std::vector<fesom_tra_cfg> cfgs;
+    DCfg *d_cfg = nullptr;
+    void *T = nullptr, *Told = nullptr;
+    void *TAB = nullptr, *trxy = nullptr, *FLO = nullptr, *ADh = nullptr, *LO = nullptr, *ADv = nullptr;
+    void *bmax = nullptr, *bmin = nullptr, *dttf_h = nullptr, *dttf_v = nullptr;
+    double *scratch = nullptr, *partials = nullptr, *content_out = nullptr;
+    int content_blocks = 0;
+    unsigned *status = nullptr;
+    bool forcing_ready = false;
+    bool state_ready = false;
+    cudaGraphExec_t gexec = nullptr;
+    double g_dt = 0.0;
+};
+
+namespace {
+
+size_t rsize(const fesom_gpu_ctx *c) { return c->prec == FESOM_PREC_FP32 ? sizeof(float) : sizeof(double); }
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) {                                                                  \
+            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                        \
+            return FESOM_ERR_CUDA;                                                                \
+        }                                                                                         \
+    } while (0)
+
+int dalloc(fesom_gpu_ctx *ctx, void **p, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        ctx->err = std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e);
+        *p = nullptr;
+        return FESOM_ERR_NOMEM;
+    }
+    ctx->allocs.push_back(*p);
+    return FESOM_OK;
+}
+
+void dfree(fesom_gpu_ctx *ctx, void *&p) {
+    if (!p) return;
+    cudaFree(p);
+    ctx->allocs.erase(std::remove(ctx->allocs.begin(), ctx->allocs.end(), p), ctx->allocs.end());
+    p = nullptr;
+}
+
+int upload_int(fesom_gpu_ctx *ctx, const int **dst, const std::vector<int> &v) {
+    void *p;
+    int rc = dalloc(ctx, &p, v.size() * sizeof(int));
+    if (rc) return rc;
+    CK(cudaMemcpy(p, v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice));
+    *dst = (const int *)p;
+    return FESOM_OK;
+}
+
+__global__ void k_d2f(const double *in, float *out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
+}
+__global__ void k_f2d(const float *in, double *out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
+}
+
+// host FP64 -> device array of the context precision (chunked through the stage buffer)
+int put(fesom_gpu_ctx *ctx, void *dst, const double *src, size_t n) {
+    if (!src) return FESOM_OK;
+    if (ctx->prec == FESOM_PREC_FP64) {
+        CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        return FESOM_OK;
+    }
+    for (size_t off = 0; off < n; off += ctx->stage_n) {
+        size_t m = std::min(ctx->stage_n, n - off);
+        CK(cudaMemcpyAsync(ctx->stage, src + off, m * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        k_d2f<<<(int)std::min<size_t>((m + 255) / 256, 152 * 32), 256, 0, ctx->stream>>>(ctx->stage, (float *)dst + off, m);
+        CK(cudaGetLastError());
+    }
+    return FESOM_OK;
+}
+
+// device array of the context precision -> host FP64
+int get(fesom_gpu_ctx *ctx, double *dst, const void *src, size_t n) {
+    if (!dst) return FESOM_OK;
+    if (ctx->prec == FESOM_PREC_FP64) {
+        CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        return FESOM_OK;
+    }
+    for (size_t off = 0; off < n; off += ctx->stage_n) {
+        size_t m = std::min(ctx->stage_n, n - off);
+        k_f2d<<<(int)std::min<size_t>((m + 255) / 256, 152 * 32), 256, 0, ctx->stream>>>((const float *)src + off, ctx->stage, m);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(dst + off, ctx->stage, m * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    return FESOM_OK;
+}
+
+// geometry upload in the context precision
+template <typename R>
+int upload_geom(fesom_gpu_ctx *ctx, const R **dst, const double *src, size_t n) {
+    void *p;
+    int rc = dalloc(ctx, &p, n * sizeof(R));
+    if (rc) return rc;
+    rc = put(ctx, p, src, n);
+    if (rc) return rc;
+    *dst = (const R *)p;
+    return FESOM_OK;
+}
+
+template <typename R>
+int init_geom(fesom_gpu_ctx *ctx, const fesom_mesh_desc *d, DGeom<R> &g) {
+    const size_t N2 = ctx->N2, E2 = ctx->E2, T2 = ctx->T2, nl = ctx->nl, L1 = ctx->L1;
+    int rc = 0;
+    if ((rc = upload_geom<R>(ctx, &g.elem_area, d->elem_area, T2))) return rc;
+    if ((rc = upload_geom<R>(ctx, &g.elem_cos, d->elem_cos, T2))) return rc;
+    if ((rc = upload_geom<R>(ctx, &g.gs, d->gradient_sca, 6 * T2))) return rc;
+    if ((rc = upload_geom<R>(ctx, &g.ecd, d->edge_cross_dxdy, 4 * E2))) return rc;
+    if ((rc = upload_geom<R>(ctx, &g.edxy, d->edge_dxdy, 2 * E2))) return rc;
+    if ((rc = upload_geom<R>(ctx, &g.area, d->area, nl * N2))) return rc;
+    if ((rc = upload_geom<R>(ctx, &g.areasvol, d->areasvol, nl * N2))) return rc;
+    if ((rc = upload_geom<R>(ctx, &g.hnode, d->hnode, L1 * N2))) return rc;
+    if ((rc = upload_geom<R>(ctx, &g.hnode_new, d->hnode_new, L1 * N2))) return rc;
+    if ((rc = upload_geom<R>(ctx, &g.helem, d->helem, L1 * T2))) return rc;
+    if ((rc = upload_geom<R>(ctx, &g.Z3, d->Z_3d_n, L1 * N2))) return rc;
+    if ((rc = upload_geom<R>(ctx, &g.zbar3, d->zbar_3d_n, nl * N2))) return rc;
+    if ((rc = upload_geom<R>(ctx, &g.zbar_n_bot, d->zbar_n_bot, N2))) return rc;
+    return FESOM_OK;
+}
+
+int check_cfg(fesom_gpu_ctx *ctx, const fesom_tra_cfg *c) {
+    if (!c) { ctx->err = "null tracer configuration"; return FESOM_ERR_ARG; }
+    if (c->adv_hor < 0 || c->adv_hor > 2) { ctx->err = "unknown horizontal advection scheme"; return FESOM_ERR_SCHEME; }
+    if (c->adv_ver == FESOM_ADV_VER_CDIFF || c->adv_ver == FESOM_ADV_VER_PPM) {
+        ctx->err = "vertical scheme CDIFF/PPM is not implemented on the device";
+        return FESOM_ERR_SCHEME;
+    }
+    if (c->adv_ver < 0 || c->adv_ver > 1) { ctx->err = "unknown vertical advection scheme"; return FESOM_ERR_SCHEME; }
+    if (c->adv_lim != 0 && c->adv_lim != 1) { ctx->err = "unknown limiter"; return FESOM_ERR_SCHEME; }
+    if (c->ab_order != 2 && c->ab_order != 3) {
+        ctx->err = "Adams-Bashforth tracer order must be 2 or 3";
+        return FESOM_ERR_ARG;
+    }
+    return FESOM_OK;
+}
+
+DCfg to_dcfg(const fesom_tra_cfg &c) {
+    DCfg d{};
+    d.hor = c.adv_hor;
+    d.ver = c.adv_ver;
+    d.lim = c.adv_lim;
+    d.ab = c.ab_order;
+    d.ph = c.adv_ph;
+    d.pv = c.adv_pv;
+    d.ivd = c.i_vert_diff;
+    return d;
+}
+
+// Allocate tracer state for ntr tracers (values/valuesold) and work arrays for
+// one group of tracers; the group size is the largest that fits in 85% of the
+// free device memory (at least 1).
+int alloc_state(fesom_gpu_ctx *ctx, int ntr, int ab_max) {
+    const size_t rs = rsize(ctx);
+    const size_t sN = (size_t)ctx->L1 * ctx->N2, sNI = (size_t)ctx->nl * ctx->N2;
+    const size_t sE = (size_t)ctx->L1 * ctx->E2, sT = 2 * (size_t)ctx->L1 * ctx->T2;
+    if (ctx->state_ready && ctx->ntr >= ntr && ctx->ab_max >= ab_max) return FESOM_OK;
+    void *bufs[] = {ctx->T, ctx->Told, ctx->TAB, ctx->trxy, ctx->FLO, ctx->ADh, ctx->LO, ctx->ADv,
+                    ctx->bmax, ctx->bmin, ctx->dttf_h, ctx->dttf_v, ctx->d_cfg, ctx->bc};
+    for (void *b : bufs) { void *p = b; dfree(ctx, p); }
+    ctx->T = ctx->Told = ctx->TAB = ctx->trxy = ctx->FLO = ctx->ADh = ctx->LO = ctx->ADv = nullptr;
+    ctx->bmax = ctx->bmin = ctx->dttf_h = ctx->dttf_v = ctx->bc = nullptr;
+    ctx->d_cfg = nullptr;
+    if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
+    int rc;
+    if ((rc = dalloc(ctx, &ctx->T, rs * sN * ntr))) return rc;
+    if ((rc = dalloc(ctx, &ctx->Told, rs * sN * ntr * (ab_max - 1)))) return rc;
+    CK(cudaMemset(ctx->Told, 0, rs * sN * ntr * (ab_max - 1)));
+    if ((rc = dalloc(ctx, &ctx->bc, rs * (size_t)ctx->N2 * ntr))) return rc;
+    CK(cudaMemset(ctx->bc, 0, rs * (size_t)ctx->N2 * ntr));
+    if ((rc = dalloc(ctx, (void **)&ctx->d_cfg, sizeof(DCfg) * ntr))) return rc;
+    const size_t per_tracer = rs * (4 * sN + sNI + sT + 2 * sE);
+    size_t fr = 0, tot = 0;
+    CK(cudaMemGetInfo(&fr, &tot));
+    int g = (int)std::min<size_t>((size_t)ntr, std::max<size_t>(1, (size_t)(0.85 * fr) / per_tracer));
+    ctx->group = g;
+    ctx->group_cap = g;
+    if ((rc = dalloc(ctx, &ctx->TAB, rs * sN * g))) return rc;
+    if ((rc = dalloc(ctx, &ctx->trxy, rs * sT * g))) return rc;
+    if ((rc = dalloc(ctx, &ctx->FLO, rs * sE * g))) return rc;
+    if ((rc = dalloc(ctx, &ctx->ADh, rs * sE * g))) return rc;
+    if ((rc = dalloc(ctx, &ctx->LO, rs * sN * g))) return rc;
+    if ((rc = dalloc(ctx, &ctx->ADv, rs * sNI * g))) return rc;
+    if ((rc = dalloc(ctx, &ctx->bmax, rs * sN * g))) return rc;
+    if ((rc = dalloc(ctx, &ctx->bmin, rs * sN * g))) return rc;
+    // the advective increments are outputs of the single-tracer drop-in only
+    if ((rc = dalloc(ctx, &ctx->dttf_h, rs * sN))) return rc;
+    if ((rc = dalloc(ctx, &ctx->dttf_v, rs * sN))) return rc;
+    ctx->ntr = ntr;
+    ctx->ab_max = ab_max;
+    ctx->state_ready = true;
+    return FESOM_OK;
+}
+
+template <typename R>
+DTracers<R> group_view(fesom_gpu_ctx *ctx, int t0, int nt) {
+    DTracers<R> v{};
+    v.ntr = nt;
+    v.sN = (size_t)ctx->L1 * ctx->N2;
+    v.sNI = (size_t)ctx->nl * ctx->N2;
+    v.sE = (size_t)ctx->L1 * ctx->E2;
+    v.sT = 2 * (size_t)ctx->L1 * ctx->T2;
+    v.T = (R *)ctx->T + t0 * v.sN;
+    v.Told = (R *)ctx->Told + t0 * v.sN * (ctx->ab_max - 1);
+    v.TAB = (R *)ctx->TAB;
+    v.trxy = (R *)ctx->trxy;
+    v.FLO = (R *)ctx->FLO;
+    v.ADh = (R *)ctx->ADh;
+    v.LO = (R *)ctx->LO;
+    v.ADv = (R *)ctx->ADv;
+    v.bmax = (R *)ctx->bmax;
+    v.bmin = (R *)ctx->bmin;
+    v.dttf_h = (R *)ctx->dttf_h;
+    v.dttf_v = (R *)ctx->dttf_v;
+    v.cfg = ctx->d_cfg + t0;
+    v.status = ctx->status;
+    return v;
+}
+
+template <typename R>
+DForcing<R> forcing_view(fesom_gpu_ctx *ctx, int t0) {
+    DForcing<R> f{};
+    f.uv = (const R *)ctx->uv;
+    f.w = (const R *)ctx->w;
+    f.wi = (const R *)ctx->wi;
+    f.we = (const R *)ctx->we;
+    f.Kv = (const R *)ctx->Kv;
+    f.bc = ctx->bc ? (const R *)ctx->bc + (size_t)t0 * ctx->N2 : nullptr;
+    return f;
+}
+
+template <typename R>
+const DGeom<R> &geom(fesom_gpu_ctx *ctx);
+template <>
+const DGeom<double> &geom<double>(fesom_gpu_ctx *ctx) { return ctx->g64; }
+template <>
+const DGeom<float> &geom<float>(fesom_gpu_ctx *ctx) { return ctx->g32; }
+
+// One tracer step for tracers [0, ntr): per group init_tracers_AB, gradients,
+// edge fluxes, LO + vertical fluxes, FCT bounds, R+/R-, limited update with
+// T*, implicit vertical diffusion.  Stream-ordered, capturable.
+struct StageTimer {
+    cudaEvent_t ev[2 * FESOM_NUM_STAGES * 64];
+    int stage[FESOM_NUM_STAGES * 64];
+    int n = 0;
+};
+
+template <typename R>
+int enqueue_step(fesom_gpu_ctx *ctx, double dt, StageTimer *tm = nullptr) {
+    const DGeom<R> &g = geom<R>(ctx);
+#define STAGE(id, call)                                                                  \
+    do {                                                                                 \
+        if (tm && tm->n < FESOM_NUM_STAGES * 64) {                                       \
+            cudaEventRecord(tm->ev[2 * tm->n], ctx->stream);                             \
+            call;                                                                        \
+            cudaEventRecord(tm->ev[2 * tm->n + 1], ctx->stream);                         \
+            tm->stage[tm->n++] = id;                                                     \
+        } else {                                                                         \
+            call;                                                                        \
+        }                                                                                \
+    } while (0)
+    for (int t0 = 0; t0 < ctx->ntr; t0 += ctx->group) {
+        const int nt = std::min(ctx->group, ctx->ntr - t0);
+        DTracers<R> tr = group_view<R>(ctx, t0, nt);
+        DForcing<R> f = forcing_view<R>(ctx, t0);
+        bool any_fct = false, any_ho = false, any_vd = false;
+        int ab = 2;
+        for (int t = t0; t < t0 + nt; t++) {
+            any_fct |= ctx->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
+            any_ho |= ctx->cfgs[t].adv_hor != FESOM_ADV_HOR_UPW1;
+            any_vd |= ctx->cfgs[t].i_vert_diff != 0;
+            ab = std::max(ab, (int)ctx->cfgs[t].ab_order);
+        }
+        // all tracers of a group share the valuesold depth of the context
+        STAGE(0, Launch<R>::ab(ctx->tp, tr, ctx->ab_max, ctx->stream));
+        if (any_ho) STAGE(1, Launch<R>::trxy(ctx->tp, g, tr, ctx->stream));
+        STAGE(2, Launch<R>::edge_flux(ctx->tp, g, f, tr, any_fct, ctx->stream));
+        STAGE(3, Launch<R>::node_lo(ctx->tp, g, f, tr, dt, any_fct, ctx->stream));
+        if (any_fct) {
+            STAGE(4, Launch<R>::bounds(ctx->tp, tr, ctx->stream));
+            STAGE(5, Launch<R>::rpm(ctx->tp, g, tr, dt, ctx->stream));
+        }
+        STAGE(6, Launch<R>::update(ctx->tp, g, tr, dt, any_fct, 1, ctx->stream));
+        if (any_vd) STAGE(7, Launch<R>::vdiff(ctx->tp, g, f, tr, dt, ctx->scratch, ctx->stream));
+    }
+#undef STAGE
+    CK(cudaGetLastError());
+    return FESOM_OK;
+}
+
+int launches_per_step(fesom_gpu_ctx *ctx) {
+    int n = 0;
+    for (int t0 = 0; t0 < ctx->ntr; t0 += ctx->group) {
+        const int nt = std::min(ctx->group, ctx->ntr - t0);
+        bool any_fct = false, any_ho = false, any_vd = false;
+        for (int t = t0; t < t0 + nt; t++) {
+            any_fct |= ctx->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
+            any_ho |= ctx->cfgs[t].adv_hor != FESOM_ADV_HOR_UPW1;
+            any_vd |= ctx->cfgs[t].i_vert_diff != 0;
+        }
+        n += 4 + (any_ho ? 1 : 0) + (any_fct ? 2 : 0) + (any_vd ? 1 : 0);
+    }
+    return n;
+}
+
+int enqueue_step_any(fesom_gpu_ctx *ctx, double dt) {
+    return ctx->prec == FESOM_PREC_FP32 ? enqueue_step<float>(ctx, dt) : enqueue_step<double>(ctx, dt);
+}
+
+int wait_stream(fesom_gpu_ctx *ctx, int timeout_ms) {
+    cudaEvent_t ev;
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    CK(cudaEventRecord(ev, ctx->stream));
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t q = cudaEventQuery(ev);
+        if (q == cudaSuccess) break;
+        if (q != cudaErrorNotReady) {
+            cudaEventDestroy(ev);
+            ctx->err = std::string("stream error: ") + cudaGetErrorString(q);
+            return FESOM_ERR_CUDA;
+        }
+        auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+        if (timeout_ms >= 0 && ms > timeout_ms) {
+            cudaEventDestroy(ev);
+            ctx->err = "device work did not finish within the time limit";
+            return FESOM_ERR_TIMEOUT;
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(ms < 10 ? 20 : 500));
+    }
+    cudaEventDestroy(ev);
+    return FESOM_OK;
+}
+
+int need_fp64(fesom_gpu_ctx *ctx) {
+    if (ctx->prec != FESOM_PREC_FP64) {
+        ctx->err = "the per-routine drop-ins run in FESOM_PREC_FP64 contexts";
+        return FESOM_ERR_STATE;
+    }
+    return FESOM_OK;
+}
+
+int ensure_one(fesom_gpu_ctx *ctx, const fesom_tra_cfg *cfg) {
+    int rc = check_cfg(ctx, cfg);
+    if (rc) return rc;
+    if (!ctx->state_ready || ctx->ab_max < cfg->ab_order) {
+        rc = alloc_state(ctx, std::max(1, ctx->ntr), std::max(ctx->ab_max, (int)cfg->ab_order));
+        if (rc) return rc;
+        if (ctx->cfgs.size() < (size_t)ctx->ntr) ctx->cfgs.resize(ctx->ntr, *cfg);
+    }
+    DCfg d = to_dcfg(*cfg);
+    CK(cudaMemcpyAsync(ctx->d_cfg, &d, sizeof(DCfg), cudaMemcpyHostToDevice, ctx->stream));
+    return FESOM_OK;
+}
+
+}  // namespace
+
+// =============================================================================
+// C ABI
+// =============================================================================
+extern "C" {
+
+int fesom_gpu_abi_version(void) { return FESOM_GPU_ABI_VERSION; }
+
+const char *fesom_gpu_last_error(const fesom_gpu_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int fesom_gpu_init(const fesom_mesh_desc *mesh, int32_t precision, int32_t max_tracers, fesom_gpu_ctx **out) {
+    if (!mesh || !out) return FESOM_ERR_ARG;
+    *out = nullptr;
+    if (precision != FESOM_PREC_FP64 && precision != FESOM_PREC_FP32) return FESOM_ERR_ARG;
+    fesom_gpu_ctx *ctx = new fesom_gpu_ctx();
+    ctx->prec = precision;
+    ctx->max_tr = std::max(1, (int)max_tracers);
+    std::string perr;
+    if (!prepare_mesh(*mesh, ctx->ht, perr)) {
+        ctx->err = perr;
+        *out = ctx;  // the caller can read the message, then finalize
+        return FESOM_ERR_MESH;
+    }
+    ctx->N2 = mesh->nod2D;
+    ctx->E2 = mesh->edge2D;
+    ctx->T2 = mesh->elem2D;
+    ctx->nl = mesh->nl;
+    ctx->L1 = mesh->nl - 1;
+    ctx->ibase = mesh->index_base;
+    *out = ctx;
+    int rc;
+    const HostTopo &h = ctx->ht;
+    DTopo &tp = ctx->tp;
+    tp.N2 = ctx->N2; tp.E2 = ctx->E2; tp.T2 = ctx->T2; tp.nl = ctx->nl; tp.L1 = ctx->L1;
+    if ((rc = upload_int(ctx, &tp.e_n1, h.e_n1)) || (rc = upload_int(ctx, &tp.e_n2, h.e_n2)) ||
+        (rc = upload_int(ctx, &tp.e_t1, h.e_t1)) || (rc = upload_int(ctx, &tp.e_t2, h.e_t2)) ||
+        (rc = upload_int(ctx, &tp.e_up, h.e_up)) || (rc = upload_int(ctx, &tp.e_dn, h.e_dn)) ||
+        (rc = upload_int(ctx, &tp.e_lo, h.e_lo)) || (rc = upload_int(ctx, &tp.e_hi, h.e_hi)) ||
+        (rc = upload_int(ctx, &tp.t_n, h.t_n)) || (rc = upload_int(ctx, &tp.t_nlev, h.t_nlev)) ||
+        (rc = upload_int(ctx, &tp.t_ulev, h.t_ulev)) || (rc = upload_int(ctx, &tp.n_nlev, h.n_nlev)) ||
+        (rc = upload_int(ctx, &tp.n_ulev, h.n_ulev)) || (rc = upload_int(ctx, &tp.n_nlevmin, h.n_nlevmin)) ||
+        (rc = upload_int(ctx, &tp.n_ulevmax, h.n_ulevmax)) || (rc = upload_int(ctx, &tp.n_nbl, h.n_nbl)) ||
+        (rc = upload_int(ctx, &tp.ne_ptr, h.ne_ptr)) || (rc = upload_int(ctx, &tp.ne_idx, h.ne_idx)) ||
+        (rc = upload_int(ctx, &tp.nie_ptr, h.nie_ptr)) || (rc = upload_int(ctx, &tp.nie_idx, h.nie_idx)))
+        return rc;
+    ctx->stage_n = std::min<size_t>((size_t)16 << 20, std::max<size_t>(2 * (size_t)ctx->L1 * ctx->T2, (size_t)ctx->nl * ctx->N2));
+    if ((rc = dalloc(ctx, (void **)&ctx->stage, ctx->stage_n * sizeof(double)))) return rc;
+    if (precision == FESOM_PREC_FP32) rc = init_geom<float>(ctx, mesh, ctx->g32);
+    else rc = init_geom<double>(ctx, mesh, ctx->g64);
+    if (rc) return rc;
+    const size_t rs = rsize(ctx);
+    if ((rc = dalloc(ctx, &ctx->uv, rs * 2 * (size_t)ctx->L1 * ctx->T2))) return rc;
+    if ((rc = dalloc(ctx, &ctx->w, rs * (size_t)ctx->nl * ctx->N2))) return rc;
+    if ((rc = dalloc(ctx, &ctx->wi, rs * (size_t)ctx->nl * ctx->N2))) return rc;
+    if ((rc = dalloc(ctx, &ctx->we, rs * (size_t)ctx->nl * ctx->N2))) return rc;
+    if ((rc = dalloc(ctx, &ctx->Kv, rs * (size_t)ctx->nl * ctx->N2))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->scratch, sizeof(double) * 3 * (size_t)(ctx->L1 + 1) * ctx->N2))) return rc;
+    ctx->content_blocks = 152 * 4;
+    if ((rc = dalloc(ctx, (void **)&ctx->partials, sizeof(double) * (size_t)ctx->content_blocks * ctx->max_tr))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->content_out, sizeof(double) * ctx->max_tr))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->status, sizeof(unsigned)))) return rc;
+    CK(cudaMemset(ctx->status, 0, sizeof(unsigned)));
+    CK(cudaDeviceSynchronize());
+    return FESOM_OK;
+}
+
+int fesom_gpu_mesh_check(const fesom_mesh_desc *mesh, int32_t *nbl, int32_t *updn, char *errbuf, int32_t errlen) {
+    if (!mesh) return FESOM_ERR_ARG;
+    HostTopo h;
+    std::string perr;
+    if (!prepare_mesh(*mesh, h, perr)) {
+        if (errbuf && errlen > 0) {
+            std::strncpy(errbuf, perr.c_str(), (size_t)errlen - 1);
+            errbuf[errlen - 1] = 0;
+        }
+        return FESOM_ERR_MESH;
+    }
+    const int b = mesh->index_base;
+    if (nbl) std::memcpy(nbl, h.n_nbl.data(), sizeof(int) * h.N2);
+    if (updn)
+        for (int e = 0; e < h.E2; e++) {
+            updn[2 * e] = h.e_up[e] < 0 ? b - 1 : h.e_up[e] + b;
+            updn[2 * e + 1] = h.e_dn[e] < 0 ? b - 1 : h.e_dn[e] + b;
+        }
+    return FESOM_OK;
+}
+
+int fesom_gpu_finalize(fesom_gpu_ctx *ctx) {
+    if (!ctx) return FESOM_OK;
+    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+    for (void *p : ctx->allocs) cudaFree(p);
+    delete ctx;
+    return FESOM_OK;
+}
+
+int fesom_gpu_set_stream(fesom_gpu_ctx *ctx, void *stream) {
+    if (!ctx) return FESOM_ERR_ARG;
+    ctx->stream = (cudaStream_t)stream;
+    if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
+    return FESOM_OK;
+}
+
+int fesom_gpu_get_muscl_init(fesom_gpu_ctx *ctx, int32_t *nbl, int32_t *updn) {
+    if (!ctx) return FESOM_ERR_ARG;
+    if (nbl) std::memcpy(nbl, ctx->ht.n_nbl.data(), sizeof(int) * ctx->N2);
+    if (updn)
+        for (int e = 0; e < ctx->E2; e++) {
+            updn[2 * e] = ctx->ht.e_up[e] < 0 ? ctx->ibase - 1 : ctx->ht.e_up[e] + ctx->ibase;
+            updn[2 * e + 1] = ctx->ht.e_dn[e] < 0 ? ctx->ibase - 1 : ctx->ht.e_dn[e] + ctx->ibase;
+        }
+    return FESOM_OK;
+}
+
+int fesom_gpu_status(fesom_gpu_ctx *ctx, uint32_t *status, int32_t timeout_ms) {
+    if (!ctx || !status) return FESOM_ERR_ARG;
+    int rc = wait_stream(ctx, timeout_ms);
+    if (rc) return rc;
+    unsigned s = 0;
+    CK(cudaMemcpy(&s, ctx->status, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    CK(cudaMemset(ctx->status, 0, sizeof(unsigned)));
+    *status = s;
+    return FESOM_OK;
+}
+
+int fesom_gpu_update_thickness(fesom_gpu_ctx *ctx, const double *hnode, const double *hnode_new, const double *helem,
+                               const double *Z_3d_n, const double *zbar_3d_n) {
+    if (!ctx) return FESOM_ERR_ARG;
+    const size_t N2 = ctx->N2, T2 = ctx->T2, L1 = ctx->L1, nl = ctx->nl;
+    int rc;
+    if (ctx->prec == FESOM_PREC_FP32) {
+        DGeom<float> &g = ctx->g32;
+        if ((rc = put(ctx, (void *)g.hnode, hnode, L1 * N2)) || (rc = put(ctx, (void *)g.hnode_new, hnode_new, L1 * N2)) ||
+            (rc = put(ctx, (void *)g.helem, helem, L1 * T2)) || (rc = put(ctx, (void *)g.Z3, Z_3d_n, L1 * N2)) ||
+            (rc = put(ctx, (void *)g.zbar3, zbar_3d_n, nl * N2)))
+            return rc;
+    } else {
+        DGeom<double> &g = ctx->g64;
+        if ((rc = put(ctx, (void *)g.hnode, hnode, L1 * N2)) || (rc = put(ctx, (void *)g.hnode_new, hnode_new, L1 * N2)) ||
+            (rc = put(ctx, (void *)g.helem, helem, L1 * T2)) || (rc = put(ctx, (void *)g.Z3, Z_3d_n, L1 * N2)) ||
+            (rc = put(ctx, (void *)g.zbar3, zbar_3d_n, nl * N2)))
+            return rc;
+    }
+    return wait_stream(ctx, -1);
+}
+
+// ---- per-routine drop-ins ----------------------------------------------------
+int fesom_gpu_init_tracers_ab(fesom_gpu_ctx *ctx, const fesom_tra_cfg *cfg, const double *values, double *valuesAB,
+                              double *valuesold) {
+    if (!ctx || !values || !valuesAB || !valuesold) return FESOM_ERR_ARG;
+    int rc;
+    if ((rc = need_fp64(ctx)) || (rc = ensure_one(ctx, cfg))) return rc;
+    const size_t sN = (size_t)ctx->L1 * ctx->N2;
+    const int ab = cfg->ab_order;
+    if ((rc = put(ctx, ctx->T, values, sN))) return rc;
+    if (ab == ctx->ab_max) {
+        if ((rc = put(ctx, ctx->Told, valuesold, sN * (ab - 1)))) return rc;
+    } else {
+        ctx->err = "valuesold depth differs from the context's Adams-Bashforth order";
+        return FESOM_ERR_STATE;
+    }
+    DTracers<double> tr = group_view<double>(ctx, 0, 1);
+    Launch<double>::ab(ctx->tp, tr, ab, ctx->stream);
+    Launch<double>::trxy(ctx->tp, ctx->g64, tr, ctx->stream);
+    CK(cudaGetLastError());
+    if ((rc = get(ctx, valuesAB, ctx->TAB, sN))) return rc;
+    if ((rc = get(ctx, valuesold, ctx->Told, sN * (ab - 1)))) return rc;
+    return wait_stream(ctx, -1);
+}
+
+int fesom_gpu_adv_tra(fesom_gpu_ctx *ctx, double dt, const double *vel, const double *w, const double *wi,
+                      const double *we, const fesom_tra_cfg *cfg, const double *ttf, const double *ttfAB,
+                      double *dttf_h, double *dttf_v) {
+    if (!ctx || !vel || !w || !we || !ttf || !ttfAB || !dttf_h || !dttf_v) return FESOM_ERR_ARG;
+    int rc;
+    if ((rc = need_fp64(ctx)) || (rc = ensure_one(ctx, cfg))) return rc;
+    const size_t sN = (size_t)ctx->L1 * ctx->N2, sNI = (size_t)ctx->nl * ctx->N2;
+    if ((rc = put(ctx, ctx->uv, vel, 2 * (size_t)ctx->L1 * ctx->T2))) return rc;
+    if ((rc = put(ctx, ctx->w, w, sNI))) return rc;
+    if ((rc = put(ctx, ctx->wi, wi, sNI))) return rc;
+    if ((rc = put(ctx, ctx->we, we, sNI))) return rc;
+    if ((rc = put(ctx, ctx->T, ttf, sN))) return rc;
+    if ((rc = put(ctx, ctx->TAB, ttfAB, sN))) return rc;
+    DTracers<double> tr = group_view<double>(ctx, 0, 1);
+    DForcing<double> f = forcing_view<double>(ctx, 0);
+    const int fct = cfg->adv_lim == FESOM_ADV_LIM_FCT;
+    if (cfg->adv_hor != FESOM_ADV_HOR_UPW1) Launch<double>::trxy(ctx->tp, ctx->g64, tr, ctx->stream);
+    Launch<double>::edge_flux(ctx->tp, ctx->g64, f, tr, fct, ctx->stream);
+    Launch<double>::node_lo(ctx->tp, ctx->g64, f, tr, dt, fct, ctx->stream);
+    if (fct) {
+        Launch<double>::bounds(ctx->tp, tr, ctx->stream);
+        Launch<double>::rpm(ctx->tp, ctx->g64, tr, dt, ctx->stream);
+    }
+    Launch<double>::update(ctx->tp, ctx->g64, tr, dt, fct, 0, ctx->stream);
+    CK(cudaGetLastError());
+    if ((rc = get(ctx, dttf_h, ctx->dttf_h, sN))) return rc;
+    if ((rc = get(ctx, dttf_v, ctx->dttf_v, sN))) return rc;
+    return wait_stream(ctx, -1);
+}
+
+int fesom_gpu_vdiff_impl(fesom_gpu_ctx *ctx, double dt, const fesom_tra_cfg *cfg, const double *Kv,
+                         const double *bc_surf, double *values) {
+    if (!ctx || !Kv || !values) return FESOM_ERR_ARG;
+    int rc;
+    if ((rc = need_fp64(ctx)) || (rc = ensure_one(ctx, cfg))) return rc;
+    const size_t sN = (size_t)ctx->L1 * ctx->N2, sNI = (size_t)ctx->nl * ctx->N2;
+    if ((rc = put(ctx, ctx->Kv, Kv, sNI))) return rc;
+    if (bc_surf) {
+        if ((rc = put(ctx, ctx->bc, bc_surf, ctx->N2))) return rc;
+    } else {
+        CK(cudaMemsetAsync(ctx->bc, 0, sizeof(double) * ctx->N2, ctx->stream));
+    }
+    if ((rc = put(ctx, ctx->T, values, sN))) return rc;
+    DTracers<double> tr = group_view<double>(ctx, 0, 1);
+    DForcing<double> f = forcing_view<double>(ctx, 0);
+    fesom_tra_cfg c = *cfg;
+    c.i_vert_diff = 1;
+    DCfg d = to_dcfg(c);
+    CK(cudaMemcpyAsync(ctx->d_cfg, &d, sizeof(DCfg), cudaMemcpyHostToDevice, ctx->stream));
+    Launch<double>::vdiff(ctx->tp, ctx->g64, f, tr, dt, ctx->scratch, ctx->stream);
+    CK(cudaGetLastError());
+    if ((rc = get(ctx, values, ctx->T, sN))) return rc;
+    return wait_stream(ctx, -1);
+}
+
+// ---- device-resident stepping ---------------------------------------------------
+int fesom_gpu_state_setup(fesom_gpu_ctx *ctx, int32_t ntr, const fesom_tra_cfg *cfgs) {
+    if (!ctx || ntr < 1 || !cfgs) return FESOM_ERR_ARG;
+    if (ntr > ctx->max_tr) { ctx->err = "ntr exceeds max_tracers given to fesom_gpu_init"; return FESOM_ERR_ARG; }
+    int ab_max = 2, rc;
+    for (int t = 0; t < ntr; t++) {
+        if ((rc = check_cfg(ctx, &cfgs[t]))) return rc;
+        ab_max = std::max(ab_max, (int)cfgs[t].ab_order);
+    }
+    for (int t = 0; t < ntr; t++)
+        if (cfgs[t].ab_order != ab_max) {
+            ctx->err = "all tracers of a batch must use the same Adams-Bashforth order";
+            return FESOM_ERR_ARG;
+        }
+    if ((rc = alloc_state(ctx, ntr, ab_max))) return rc;
+    ctx->ntr = ntr;
+    ctx->cfgs.assign(cfgs, cfgs + ntr);
+    std::vector<DCfg> d(ntr);
+    for (int t = 0; t < ntr; t++) d[t] = to_dcfg(cfgs[t]);
+    CK(cudaMemcpy(ctx->d_cfg, d.data(), sizeof(DCfg) * ntr, cudaMemcpyHostToDevice));
+    if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
+    return FESOM_OK;
+}
+
+int fesom_gpu_forcing_upload(fesom_gpu_ctx *ctx, const double *uv, const double *w, const double *wi,
+                             const double *we, const double *Kv, const double *bc_surf) {
+    if (!ctx || !uv || !w || !we || !Kv) return FESOM_ERR_ARG;
+    if (!ctx->state_ready) { ctx->err = "call fesom_gpu_state_setup first"; return FESOM_ERR_STATE; }
+    const size_t sNI = (size_t)ctx->nl * ctx->N2;
+    int rc;
+    if ((rc = put(ctx, ctx->uv, uv, 2 * (size_t)ctx->L1 * ctx->T2)) || (rc = put(ctx, ctx->w, w, sNI)) ||
+        (rc = put(ctx, ctx->we, we, sNI)) || (rc = put(ctx, ctx->Kv, Kv, sNI)))
+        return rc;
+    if (wi && (rc = put(ctx, ctx->wi, wi, sNI))) return rc;
+    if (bc_surf) {
+        if ((rc = put(ctx, ctx->bc, bc_surf, (size_t)ctx->N2 * ctx->ntr))) return rc;
+    } else {
+        CK(cudaMemsetAsync(ctx->bc, 0, rsize(ctx) * (size_t)ctx->N2 * ctx->ntr, ctx->stream));
+    }
+    ctx->forcing_ready = true;
+    return FESOM_OK;
+}
+
+int fesom_gpu_forcing_upload_f32(fesom_gpu_ctx *ctx, const float *uv, const float *w, const float *wi, const float *we,
+                                 const float *Kv, const float *bc_surf) {
+    if (!ctx || !uv || !w || !we || !Kv) return FESOM_ERR_ARG;
+    if (ctx->prec != FESOM_PREC_FP32) { ctx->err = "FP32 buffers need a FESOM_PREC_FP32 context"; return FESOM_ERR_STATE; }
+    if (!ctx->state_ready) { ctx->err = "call fesom_gpu_state_setup first"; return FESOM_ERR_STATE; }
+    const size_t sNI = (size_t)ctx->nl * ctx->N2;
+    CK(cudaMemcpyAsync(ctx->uv, uv, 4 * 2 * (size_t)ctx->L1 * ctx->T2, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->w, w, 4 * sNI, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->we, we, 4 * sNI, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->Kv, Kv, 4 * sNI, cudaMemcpyHostToDevice, ctx->stream));
+    if (wi) CK(cudaMemcpyAsync(ctx->wi, wi, 4 * sNI, cudaMemcpyHostToDevice, ctx->stream));
+    if (bc_surf) CK(cudaMemcpyAsync(ctx->bc, bc_surf, 4 * (size_t)ctx->N2 * ctx->ntr, cudaMemcpyHostToDevice, ctx->stream));
+    else CK(cudaMemsetAsync(ctx->bc, 0, 4 * (size_t)ctx->N2 * ctx->ntr, ctx->stream));
+    ctx->forcing_ready = true;
+    return FESOM_OK;
+}
+
+static int tracer_check(fesom_gpu_ctx *ctx, int32_t tr) {
+    if (!ctx) return FESOM_ERR_ARG;
+    if (!ctx->state_ready || tr < 0 || tr >= ctx->ntr) {
+        ctx->err = "tracer index outside the state set up by fesom_gpu_state_setup";
+        return FESOM_ERR_STATE;
+    }
+    return FESOM_OK;
+}
+
+int fesom_gpu_tracer_upload(fesom_gpu_ctx *ctx, int32_t tr, const double *values, const double *valuesold) {
+    int rc = tracer_check(ctx, tr);
+    if (rc) return rc;
+    const size_t sN = (size_t)ctx->L1 * ctx->N2, rs = rsize(ctx);
+    if ((rc = put(ctx, (char *)ctx->T + rs * sN * tr, values, sN))) return rc;
+    return put(ctx, (char *)ctx->Told + rs * sN * (ctx->ab_max - 1) * tr, valuesold, sN * (ctx->ab_max - 1));
+}
+
+int fesom_gpu_tracer_download(fesom_gpu_ctx *ctx, int32_t tr, double *values, double *valuesold) {
+    int rc = tracer_check(ctx, tr);
+    if (rc) return rc;
+    const size_t sN = (size_t)ctx->L1 * ctx->N2, rs = rsize(ctx);
+    if ((rc = get(ctx, values, (char *)ctx->T + rs * sN * tr, sN))) return rc;
+    if ((rc = get(ctx, valuesold, (char *)ctx->Told + rs * sN * (ctx->ab_max - 1) * tr, sN * (ctx->ab_max - 1))))
+        return rc;
+    return wait_stream(ctx, -1);
+}
+
+int fesom_gpu_tracer_upload_f32(fesom_gpu_ctx *ctx, int32_t tr, const float *values, const float *valuesold) {
+    int rc = tracer_check(ctx, tr);
+    if (rc) return rc;
+    if (ctx->prec != FESOM_PREC_FP32) { ctx->err = "FP32 buffers need a FESOM_PREC_FP32 context"; return FESOM_ERR_STATE; }
+    const size_t sN = (size_t)ctx->L1 * ctx->N2;
+    if (values) CK(cudaMemcpyAsync((float *)ctx->T + sN * tr, values, 4 * sN, cudaMemcpyHostToDevice, ctx->stream));
+    if (valuesold)
+        CK(cudaMemcpyAsync((float *)ctx->Told + sN * (ctx->ab_max - 1) * tr, valuesold, 4 * sN * (ctx->ab_max - 1),
+                           cudaMemcpyHostToDevice, ctx->stream));
+    return FESOM_OK;
+}
+
+int fesom_gpu_tracer_download_f32(fesom_gpu_ctx *ctx, int32_t tr, float *values, float *valuesold) {
+    int rc = tracer_check(ctx, tr);
+    if (rc) return rc;
+    if (ctx->prec != FESOM_PREC_FP32) { ctx->err = "FP32 buffers need a FESOM_PREC_FP32 context"; return FESOM_ERR_STATE; }
+    const size_t sN = (size_t)ctx->L1 * ctx->N2;
+    if (values) CK(cudaMemcpyAsync(values, (float *)ctx->T + sN * tr, 4 * sN, cudaMemcpyDeviceToHost, ctx->stream));
+    if (valuesold)
+        CK(cudaMemcpyAsync(valuesold, (float *)ctx->Told + sN * (ctx->ab_max - 1) * tr, 4 * sN * (ctx->ab_max - 1),
+                           cudaMemcpyDeviceToHost, ctx->stream));
+    return FESOM_OK;
+}
+
+int fesom_gpu_run_steps(fesom_gpu_ctx *ctx, double dt, int32_t nsteps, int32_t use_graph) {
+    if (!ctx || nsteps < 0) return FESOM_ERR_ARG;
+    if (!ctx->state_ready || !ctx->forcing_ready) {
+        ctx->err = "state and forcing must be set up before stepping";
+        return FESOM_ERR_STATE;
+    }
+    int rc;
+    if (!use_graph) {
+        for (int s = 0; s < nsteps; s++)
+            if ((rc = enqueue_step_any(ctx, dt))) return rc;
+        return FESOM_OK;
+    }
+    if (!ctx->gexec || ctx->g_dt != dt) {
+        if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
+        cudaStream_t cap = ctx->stream;
+        bool own = false;
+        if (!cap) {  // the legacy stream cannot be captured: capture on a private stream
+            CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+            own = true;
+        }
+        cudaStream_t keep = ctx->stream;
+        ctx->stream = cap;
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        rc = enqueue_step_any(ctx, dt);
+        cudaError_t e = cudaStreamEndCapture(cap, &graph);
+        ctx->stream = keep;
+        if (own) cudaStreamDestroy(cap);
+        if (rc) return rc;
+        if (e != cudaSuccess) { ctx->err = std::string("graph capture: ") + cudaGetErrorString(e); return FESOM_ERR_CUDA; }
+        e = cudaGraphInstantiate(&ctx->gexec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) { ctx->err = std::string("graph instantiate: ") + cudaGetErrorString(e); return FESOM_ERR_CUDA; }
+        ctx->g_dt = dt;
+    }
+    for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(ctx->gexec, ctx->stream));
+    return FESOM_OK;
+}
+
+int fesom_gpu_tracer_step(fesom_gpu_ctx *ctx, int32_t ntr, const fesom_tra_cfg *cfgs, double dt, const double *uv,
+                          const double *w, const double *wi, const double *we, const double *Kv, const double *bc_surf,
+                          double *const *values, double *const *valuesold) {
+    if (!ctx || !values || !valuesold) return FESOM_ERR_ARG;
+    int rc;
+    bool same = ctx->state_ready && ctx->ntr == ntr && (int)ctx->cfgs.size() == ntr;
+    for (int t = 0; same && t < ntr; t++) same = std::memcmp(&ctx->cfgs[t], &cfgs[t], sizeof(fesom_tra_cfg)) == 0;
+    if (!same && (rc = fesom_gpu_state_setup(ctx, ntr, cfgs))) return rc;
+    if ((rc = fesom_gpu_forcing_upload(ctx, uv, w, wi, we, Kv, bc_surf))) return rc;
+    for (int t = 0; t < ntr; t++)
+        if ((rc = fesom_gpu_tracer_upload(ctx, t, values[t], valuesold[t]))) return rc;
+    if ((rc = fesom_gpu_run_steps(ctx, dt, 1, 0))) return rc;
+    const size_t sN = (size_t)ctx->L1 * ctx->N2, rs = rsize(ctx);
+    for (int t = 0; t < ntr; t++) {
+        if ((rc = get(ctx, values[t], (char *)ctx->T + rs * sN * t, sN))) return rc;
+        if ((rc = get(ctx, valuesold[t], (char *)ctx->Told + rs * sN * (ctx->ab_max - 1) * t, sN * (ctx->ab_max - 1))))
+            return rc;
+    }
+    rc = wait_stream(ctx, -1);
+    if (rc) return rc;
+    unsigned s = 0;
+    CK(cudaMemcpy(&s, ctx->status, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (s & FESOM_STATUS_NAN) {
+        CK(cudaMemset(ctx->status, 0, sizeof(unsigned)));
+        ctx->err = "non-finite tracer value produced";
+        return FESOM_ERR_NUMERIC;
+    }
+    return FESOM_OK;
+}
+
+int fesom_gpu_set_tracers_per_launch(fesom_gpu_ctx *ctx, int32_t n) {
+    if (!ctx || n < 0) return FESOM_ERR_ARG;
+    if (!ctx->state_ready) { ctx->err = "call fesom_gpu_state_setup first"; return FESOM_ERR_STATE; }
+    ctx->group = n == 0 ? ctx->group_cap : std::min((int)n, ctx->group_cap);
+    if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
+    return FESOM_OK;
+}
+
+int fesom_gpu_debug_fetch(fesom_gpu_ctx *ctx, const char *name, int32_t tr, double *out, size_t count) {
+    if (!ctx || !name || !out) return FESOM_ERR_ARG;
+    if (!ctx->state_ready) { ctx->err = "no tracer state"; return FESOM_ERR_STATE; }
+    const size_t sN = (size_t)ctx->L1 * ctx->N2, sNI = (size_t)ctx->nl * ctx->N2;
+    const size_t sE = (size_t)ctx->L1 * ctx->E2, sT = 2 * (size_t)ctx->L1 * ctx->T2;
+    const std::string n(name);
+    const void *src = nullptr;
+    size_t len = 0;
+    const bool work = !(n == "T" || n == "Told");
+    if (work && tr >= ctx->group) { ctx->err = "work arrays hold one launch group"; return FESOM_ERR_ARG; }
+    const size_t rs = rsize(ctx);
+    if (n == "T") { src = (char *)ctx->T + rs * sN * tr; len = sN; }
+    else if (n == "Told") { src = (char *)ctx->Told + rs * sN * (ctx->ab_max - 1) * tr; len = sN * (ctx->ab_max - 1); }
+    else if (n == "TAB") { src = (char *)ctx->TAB + rs * sN * tr; len = sN; }
+    else if (n == "trxy") { src = (char *)ctx->trxy + rs * sT * tr; len = sT; }
+    else if (n == "FLO") { src = (char *)ctx->FLO + rs * sE * tr; len = sE; }
+    else if (n == "ADh") { src = (char *)ctx->ADh + rs * sE * tr; len = sE; }
+    else if (n == "LO") { src = (char *)ctx->LO + rs * sN * tr; len = sN; }
+    else if (n == "ADv") { src = (char *)ctx->ADv + rs * sNI * tr; len = sNI; }
+    else if (n == "bmax") { src = (char *)ctx->bmax + rs * sN * tr; len = sN; }
+    else if (n == "bmin") { src = (char *)ctx->bmin + rs * sN * tr; len = sN; }
+    else if (n == "dttf_h" && tr == 0) { src = ctx->dttf_h; len = sN; }
+    else if (n == "dttf_v" && tr == 0) { src = ctx->dttf_v; len = sN; }
+    else { ctx->err = "unknown work array " + n; return FESOM_ERR_ARG; }
+    if (count < len) { ctx->err = "output buffer too small"; return FESOM_ERR_ARG; }
+    int rc = get(ctx, out, src, len);
+    if (rc) return rc;
+    return wait_stream(ctx, -1);
+}
+
+int fesom_gpu_launches_per_step(fesom_gpu_ctx *ctx, int32_t *launches) {
+    if (!ctx || !launches) return FESOM_ERR_ARG;
+    if (!ctx->state_ready) { ctx->err = "no tracer state"; return FESOM_ERR_STATE; }
+    *launches = launches_per_step(ctx);
+    return FESOM_OK;
+}
+
+int fesom_gpu_profile_step(fesom_gpu_ctx *ctx, double dt, float *stage_ms, int32_t *launches) {
+    if (!ctx || !stage_ms || !launches) return FESOM_ERR_ARG;
+    if (!ctx->state_ready || !ctx->forcing_ready) {
+        ctx->err = "state and forcing must be set up before stepping";
+        return FESOM_ERR_STATE;
+    }
+    StageTimer *tm = new StageTimer();
+    const int nev = 2 * FESOM_NUM_STAGES * 64;
+    for (int i = 0; i < nev; i++) cudaEventCreate(&tm->ev[i]);
+    int rc = ctx->prec == FESOM_PREC_FP32 ? enqueue_step<float>(ctx, dt, tm) : enqueue_step<double>(ctx, dt, tm);
+    if (!rc) rc = wait_stream(ctx, -1);
+    for (int i = 0; i < FESOM_NUM_STAGES; i++) { stage_ms[i] = 0.f; launches[i] = 0; }
+    if (!rc)
+        for (int k = 0; k < tm->n; k++) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, tm->ev[2 * k], tm->ev[2 * k + 1]);
+            stage_ms[tm->stage[k]] += ms;
+            launches[tm->stage[k]] += 1;
+        }
+    for (int i = 0; i < nev; i++) cudaEventDestroy(tm->ev[i]);
+    delete tm;
+    return rc;
+}
+
+int fesom_gpu_tracer_content(fesom_gpu_ctx *ctx, double *content) {
+    if (!ctx || !content) return FESOM_ERR_ARG;
+    if (!ctx->state_ready) { ctx->err = "no tracer state"; return FESOM_ERR_STATE; }
+    if (ctx->prec == FESOM_PREC_FP32) {
+        DTracers<float> tr = group_view<float>(ctx, 0, ctx->ntr);
+        Launch<float>::content(ctx->tp, ctx->g32, tr, ctx->partials, ctx->content_blocks, ctx->content_out, ctx->stream);
+    } else {
+        DTracers<double> tr = group_view<double>(ctx, 0, ctx->ntr);
+        Launch<double>::content(ctx->tp, ctx->g64, tr, ctx->partials, ctx->content_blocks, ctx->content_out, ctx->stream);
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(content, ctx->content_out, sizeof(double) * ctx->ntr, cudaMemcpyDeviceToHost, ctx->stream));
+    return wait_stream(ctx, -1);
+}
+
+int fesom_gpu_tracer_device_ptr(fesom_gpu_ctx *ctx, int32_t tr, void **values, void **valuesold) {
+    int rc = tracer_check(ctx, tr);
+    if (rc) return rc;
+    const size_t sN = (size_t)ctx->L1 * ctx->N2, rs = rsize(ctx);
+    if (values) *values = (char *)ctx->T + rs * sN * tr;
+    if (valuesold) *valuesold = (char *)ctx->Told + rs * sN * (ctx->ab_max - 1) * tr;
+    return FESOM_OK;
+}
+
+}  // extern "C"

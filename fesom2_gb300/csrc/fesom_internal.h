@@ -1,0 +1,97 @@
+// fesom_internal.h -- device-side data structures shared by the host library
+// and the kernels of the GB300 tracer-transport step.
+//
+// Layout in HBM: every 3-D field keeps the reference's Fortran layout
+// a(level, entity): column-contiguous, stride nl-1 (layer fields) or nl
+// (interface fields) per entity; all tracers of a batch share one allocation
+// with a fixed per-tracer stride.  Topology is 0-based int32; gather lists are
+// CSR arrays in ascending edge (element) order so that every node sum adds its
+// terms in the order of the reference's serial edge scatter.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace fesom {
+
+constexpr double kREarth = 6367500.0;  // src/oce_modules.F90:29
+constexpr double kABEpsilon = 0.1;     // src/oce_modules.F90:105
+constexpr double kFluxEps = 1e-16;     // src/oce_adv_tra_fct.F90:99 (double under -fdefault-real-8)
+constexpr double kBigNumber = 1e3;     // src/oce_adv_tra_fct.F90:100
+
+struct DTopo {
+    int N2, E2, T2, nl, L1;
+    const int *e_n1, *e_n2;   // edges(1:2, e)
+    const int *e_t1, *e_t2;   // edge_tri(1:2, e), -1 = none
+    const int *e_up, *e_dn;   // edge_up_dn_tri(1:2, e), -1 = none
+    const int *e_lo, *e_hi;   // level range [nu12, nl12] of the edge scatters (1-based)
+    const int *t_n;           // 3 * T2 element nodes
+    const int *t_nlev, *t_ulev;
+    const int *n_nlev, *n_ulev, *n_nlevmin, *n_ulevmax, *n_nbl;
+    const int *ne_ptr, *ne_idx;    // node -> edge, idx >= 0: node is edges(1,e); ~e: node is edges(2,e)
+    const int *nie_ptr, *nie_idx;  // node -> element, ascending element order
+};
+
+template <typename R>
+struct DGeom {
+    const R *elem_area, *elem_cos, *gs;  // gs: 6 per element
+    const R *ecd, *edxy;                 // 4 / 2 per edge
+    const R *area, *areasvol;            // nl per node
+    const R *hnode, *hnode_new;          // nl-1 per node
+    const R *helem;                      // nl-1 per element
+    const R *Z3, *zbar3;                 // nl-1 / nl per node
+    const R *zbar_n_bot;                 // per node
+};
+
+template <typename R>
+struct DForcing {
+    const R *uv;              // 2*(nl-1) per element
+    const R *w, *wi, *we;     // nl per node
+    const R *Kv;              // nl per node
+    const R *bc;              // ntr per node (may be null)
+};
+
+// Per-tracer scheme on the device (fesom_tra_cfg without the id).
+struct DCfg {
+    int hor, ver, lim, ab;
+    double ph, pv;
+    int ivd, pad;
+};
+
+template <typename R>
+struct DTracers {
+    int ntr;
+    size_t sN;    // stride of a layer field per tracer: (nl-1) * N2
+    size_t sNI;   // stride of an interface field per tracer: nl * N2
+    size_t sE;    // stride of an edge field: (nl-1) * E2
+    size_t sT;    // stride of tr_xy: 2 * (nl-1) * T2
+    R *T, *Told, *TAB;   // Told holds (ab-1) interleaved previous levels
+    R *trxy;
+    R *FLO, *ADh;        // low-order / antidiffusive edge fluxes
+    R *LO, *ADv;         // low-order solution / antidiffusive vertical flux
+    R *bmax, *bmin;      // FCT bound increments, then R+ / R- in place
+    R *dttf_h, *dttf_v;  // advective increments (drop-in outputs)
+    const DCfg *cfg;
+    unsigned *status;
+};
+
+// launch wrappers (kernels_fp64.cu / kernels_fp32.cu)
+template <typename R>
+struct Launch {
+    static void ab(const DTopo &, DTracers<R> &, int ab_order, cudaStream_t);
+    static void trxy(const DTopo &, const DGeom<R> &, DTracers<R> &, cudaStream_t);
+    static void edge_flux(const DTopo &, const DGeom<R> &, const DForcing<R> &, DTracers<R> &, int fct, cudaStream_t);
+    static void node_lo(const DTopo &, const DGeom<R> &, const DForcing<R> &, DTracers<R> &, double dt, int fct,
+                        cudaStream_t);
+    static void bounds(const DTopo &, DTracers<R> &, cudaStream_t);
+    static void rpm(const DTopo &, const DGeom<R> &, DTracers<R> &, double dt, cudaStream_t);
+    // mode 0: write dttf_h/dttf_v only; mode 1: del_ttf sum + T* update into T
+    static void update(const DTopo &, const DGeom<R> &, DTracers<R> &, double dt, int fct, int mode, cudaStream_t);
+    static void vdiff(const DTopo &, const DGeom<R> &, const DForcing<R> &, DTracers<R> &, double dt,
+                      double *scratch, cudaStream_t);
+    static void content(const DTopo &, const DGeom<R> &, const DTracers<R> &, double *partials, int nblk,
+                        double *out, cudaStream_t);
+};
+
+}  // namespace fesom

@@ -1,0 +1,716 @@
+// tracer_kernels.cuh -- sm_103a kernels of the FESOM2 tracer-transport step.
+//
+// One template, two instantiations:
+//   R = double  (kernels_fp64.cu, built with --fmad=false): the reference's
+//               FP64 arithmetic in the reference's evaluation order, so the
+//               results match the serial Fortran loops bit for bit;
+//   R = float   (kernels_fp32.cu): FP32 storage and arithmetic, compensated
+//               node sums, FP64 Thomas solve and FP64 content sums.
+//
+// Mapping: edge and node kernels run one warp per entity with the lanes over
+// the levels of the column (the reference's arrays are level-contiguous, so
+// every lane load is coalesced).  Node sums are gathers over the node's
+// ascending edge list instead of the reference's edge scatters: the terms are
+// added in the same order, without atomics, so sums are deterministic.  The
+// tridiagonal solve runs one thread per column (GB300's FP64 pipe is narrow;
+// a full warp of columns keeps every lane busy).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "fesom_internal.h"
+
+namespace fesom {
+
+constexpr int kWarpsPerBlock = 4;
+constexpr int kThreads = 32 * kWarpsPerBlock;
+
+template <typename R> __device__ __forceinline__ R rmax(R a, R b) { return a > b ? a : b; }
+template <typename R> __device__ __forceinline__ R rmin(R a, R b) { return a < b ? a : b; }
+template <typename R> __device__ __forceinline__ R rabs(R a) { return fabs(a); }
+template <> __device__ __forceinline__ float rabs<float>(float a) { return fabsf(a); }
+
+__device__ __forceinline__ size_t ix1(int nz, int n, int L1) { return (size_t)n * L1 + (nz - 1); }
+__device__ __forceinline__ size_t ixn(int nz, int n, int nl) { return (size_t)n * nl + (nz - 1); }
+
+// ---------------------------------------------------------------------------
+// Node-sum accumulator: plain for FP64 (the reference's order and rounding),
+// Neumaier-compensated for FP32.
+// ---------------------------------------------------------------------------
+template <typename R>
+struct Acc {
+    R s;
+    __device__ __forceinline__ Acc() : s(R(0)) {}
+    __device__ __forceinline__ void add(R x) { s = s + x; }
+    __device__ __forceinline__ void sub(R x) { s = s - x; }
+    __device__ __forceinline__ R get() const { return s; }
+};
+template <>
+struct Acc<float> {
+    float s, c;
+    __device__ __forceinline__ Acc() : s(0.f), c(0.f) {}
+    __device__ __forceinline__ void add(float x) {
+        float t = s + x;
+        c += (fabsf(s) >= fabsf(x)) ? ((s - t) + x) : ((x - t) + s);
+        s = t;
+    }
+    __device__ __forceinline__ void sub(float x) { add(-x); }
+    __device__ __forceinline__ float get() const { return s + c; }
+};
+
+// ===========================================================================
+// init_tracers_AB: valuesAB and the valuesold shift (src/oce_tracer_mod.F90:46-123)
+// ===========================================================================
+template <typename R>
+__global__ void k_ab(DTracers<R> tr, size_t n, int ab) {
+    const R ca = R(0.5 + kABEpsilon), cb = R(1.5 + kABEpsilon);
+    for (int t = 0; t < tr.ntr; t++) {
+        R *T = tr.T + t * tr.sN, *TAB = tr.TAB + t * tr.sN;
+        R *O = tr.Told + t * tr.sN * (ab - 1);
+        for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+            R v = T[i];
+            if (ab == 2) {
+                TAB[i] = -(ca * O[i]) + cb * v;
+                O[i] = v;
+            } else {
+                R o1 = O[2 * i], o2 = O[2 * i + 1];
+                R x = R(5.0) * o2 - R(16.0) * o1 + R(23.0) * v;
+                TAB[i] = x / R(12.0);
+                O[2 * i + 1] = o1;
+                O[2 * i] = v;
+            }
+        }
+    }
+}
+
+// ===========================================================================
+// tracer_gradient_elements (src/oce_tracer_mod.F90:147-188): warp per element
+// ===========================================================================
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_trxy(DTopo tp, DGeom<R> g, DTracers<R> tr) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int L1 = tp.L1;
+    for (int el = blockIdx.x * kWarpsPerBlock + warp; el < tp.T2; el += gridDim.x * kWarpsPerBlock) {
+        const int a = tp.t_n[3 * el], b = tp.t_n[3 * el + 1], c = tp.t_n[3 * el + 2];
+        const R *gs = g.gs + 6 * (size_t)el;
+        const R g0 = gs[0], g1 = gs[1], g2 = gs[2], g3 = gs[3], g4 = gs[4], g5 = gs[5];
+        const int nzmin = tp.t_ulev[el], nzmax = tp.t_nlev[el];
+        for (int t = 0; t < tr.ntr; t++) {
+            const R *T = tr.T + t * tr.sN;
+            R *out = tr.trxy + t * tr.sT;
+            for (int nz = nzmin + lane; nz <= nzmax - 1; nz += 32) {
+                R ta = T[ix1(nz, a, L1)], tb = T[ix1(nz, b, L1)], tc = T[ix1(nz, c, L1)];
+                R s = R(0);
+                s = s + g0 * ta;
+                s = s + g1 * tb;
+                s = s + g2 * tc;
+                R s2 = R(0);
+                s2 = s2 + g3 * ta;
+                s2 = s2 + g4 * tb;
+                s2 = s2 + g5 * tc;
+                out[2 * ix1(nz, el, L1)] = s;
+                out[2 * ix1(nz, el, L1) + 1] = s2;
+            }
+        }
+    }
+}
+
+// area-weighted mean of tr_xy over the node's elements wet at level nz
+// (fill_up_dn_grad, src/oce_muscl_adv.F90:388-405)
+template <typename R>
+__device__ __forceinline__ void node_mean_grad(const DTopo &tp, const DGeom<R> &g, const R *trxy, int node, int nz,
+                                               R &gx, R &gy) {
+    const int L1 = tp.L1;
+    R tvol = R(0), tx = R(0), ty = R(0);
+    for (int k = tp.nie_ptr[node]; k < tp.nie_ptr[node + 1]; k++) {
+        const int el = tp.nie_idx[k];
+        if (tp.t_nlev[el] - 1 < nz || nz < tp.t_ulev[el]) continue;
+        const R ea = g.elem_area[el];
+        tvol = tvol + ea;
+        tx = tx + trxy[2 * ix1(nz, el, L1)] * ea;
+        ty = ty + trxy[2 * ix1(nz, el, L1) + 1] * ea;
+    }
+    gx = tx / tvol;
+    gy = ty / tvol;
+}
+
+// ===========================================================================
+// Edge fluxes: adv_tra_hor_upw1 (LO, values) and adv_tra_hor_muscl / _mfct /
+// _upw1 (HO, valuesAB) with fill_up_dn_grad inlined
+// (src/oce_adv_tra_hor.F90:64-834, src/oce_muscl_adv.F90:356-525).
+// Writes FLO (FCT only) and ADh = HO - LO (FCT) or HO (no limiter).
+// ===========================================================================
+template <typename R>
+__global__ void __launch_bounds__(kThreads)
+k_edge_flux(DTopo tp, DGeom<R> g, DForcing<R> f, DTracers<R> tr) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int L1 = tp.L1;
+    const R RE = R(kREarth);
+    for (int e = blockIdx.x * kWarpsPerBlock + warp; e < tp.E2; e += gridDim.x * kWarpsPerBlock) {
+        const int n1 = tp.e_n1[e], n2 = tp.e_n2[e];
+        const int el1 = tp.e_t1[e], el2 = tp.e_t2[e];
+        const int nl1 = tp.t_nlev[el1] - 1, nu1 = tp.t_ulev[el1];
+        const R dX1 = g.ecd[4 * (size_t)e], dY1 = g.ecd[4 * (size_t)e + 1];
+        R a = RE * g.elem_cos[el1];
+        int nl2 = 0, nu2 = 0;
+        R dX2 = R(0), dY2 = R(0);
+        if (el2 >= 0) {
+            dX2 = g.ecd[4 * (size_t)e + 2];
+            dY2 = g.ecd[4 * (size_t)e + 3];
+            nl2 = tp.t_nlev[el2] - 1;
+            nu2 = tp.t_ulev[el2];
+            a = R(0.5) * (a + RE * g.elem_cos[el2]);
+        }
+        const int fnl12 = nl1 < nl2 ? nl1 : nl2;
+        const int fnu12 = nu1 > nu2 ? nu1 : nu2;
+        const int lo = tp.e_lo[e], hi = tp.e_hi[e];
+        const R ex = g.edxy[2 * (size_t)e], ey = g.edxy[2 * (size_t)e + 1];
+        const int up = tp.e_up[e], dn = tp.e_dn[e];
+        const bool inner = (up >= 0) && (dn >= 0);
+        int gzmin = 0, gzmax = 0;
+        if (inner) {
+            gzmin = max(tp.n_ulevmax[n1], tp.n_ulevmax[n2]);
+            gzmax = min(tp.n_nlevmin[n1], tp.n_nlevmin[n2]);
+        }
+        const int nbl1 = tp.n_nbl[n1], nbl2 = tp.n_nbl[n2];
+        for (int nz = lo + lane; nz <= hi; nz += 32) {
+            // segment rule of the reference's five loops (A..E)
+            int seg = 0;
+            if (nz >= nu1 && nz <= fnu12 - 1) seg = 1;
+            else if (nu2 > 0 && nz >= nu2 && nz <= fnu12 - 1) seg = 2;
+            else if (nz >= fnu12 && nz <= fnl12) seg = 3;
+            else if (nz >= fnl12 + 1 && nz <= nl1) seg = 1;
+            else if (nz >= fnl12 + 1 && nz <= nl2) seg = 2;
+            R vf = R(0);
+            if (seg & 1) {
+                const R u = f.uv[2 * ix1(nz, el1, L1)], v = f.uv[2 * ix1(nz, el1, L1) + 1];
+                vf = (-(v * dX1) + u * dY1) * g.helem[ix1(nz, el1, L1)];
+            }
+            if (seg & 2) {
+                const R u = f.uv[2 * ix1(nz, el2, L1)], v = f.uv[2 * ix1(nz, el2, L1) + 1];
+                const R v2 = (v * dX2 - u * dY2) * g.helem[ix1(nz, el2, L1)];
+                vf = (seg == 3) ? vf + v2 : v2;
+            }
+            const R avf = rabs(vf);
+            for (int t = 0; t < tr.ntr; t++) {
+                const DCfg c = tr.cfg[t];
+                const int fct = c.lim;
+                const R *T = tr.T + t * tr.sN;
+                const R *TA = tr.TAB + t * tr.sN;
+                R flo = R(0);
+                if (fct && seg)
+                    flo = -(R(0.5) * (T[ix1(nz, n1, L1)] * (vf + avf) + T[ix1(nz, n2, L1)] * (vf - avf))) - R(0);
+                const R fin = fct ? flo : R(0);
+                R ad = fin;
+                if (seg) {
+                    const R t1 = TA[ix1(nz, n1, L1)], t2 = TA[ix1(nz, n2, L1)];
+                    if (c.hor == 2) {
+                        ad = -(R(0.5) * (t1 * (vf + avf) + t2 * (vf - avf))) - fin;
+                    } else {
+                        const R *txy = tr.trxy + t * tr.sT;
+                        R g1, g2, g3, g4;
+                        if (inner && nz >= gzmin && nz <= gzmax - 1) {
+                            g1 = txy[2 * ix1(nz, up, L1)];
+                            g3 = txy[2 * ix1(nz, up, L1) + 1];
+                            g2 = txy[2 * ix1(nz, dn, L1)];
+                            g4 = txy[2 * ix1(nz, dn, L1) + 1];
+                        } else {
+                            node_mean_grad(tp, g, txy, n1, nz, g1, g3);
+                            node_mean_grad(tp, g, txy, n2, nz, g2, g4);
+                        }
+                        R Tm2, Tm1;
+                        if (c.hor == 0) {
+                            const R clo1 = (nbl1 - nz) >= 0 ? R(1) : R(0);
+                            const R clo2 = (nbl2 - nz) >= 0 ? R(1) : R(0);
+                            Tm2 = t2 - (R(2.0) * (t2 - t1) + ex * a * g2 + ey * RE * g4) / R(6.0) * clo2;
+                            Tm1 = t1 + (R(2.0) * (t2 - t1) + ex * a * g1 + ey * RE * g3) / R(6.0) * clo1;
+                        } else {
+                            Tm2 = t2 - (R(2.0) * (t2 - t1) + ex * a * g2 + ey * RE * g4) / R(6.0);
+                            Tm1 = t1 + (R(2.0) * (t2 - t1) + ex * a * g1 + ey * RE * g3) / R(6.0);
+                        }
+                        const R no = R(c.ph);
+                        const R cHO = (vf + avf) * Tm1 + (vf - avf) * Tm2;
+                        ad = -(R(0.5) * (R(1.0) - no) * cHO) - vf * no * R(0.5) * (Tm1 + Tm2) - fin;
+                    }
+                }
+                if (fct) tr.FLO[t * tr.sE + ix1(nz, e, L1)] = flo;
+                tr.ADh[t * tr.sE + ix1(nz, e, L1)] = ad;
+            }
+        }
+    }
+}
+
+// ===========================================================================
+// Node columns, stage 1: LO solution (edge gather of the upwind fluxes,
+// adv_tra_ver_upw1 with w_e, src/oce_adv_tra_driver.F90:122-250) and the
+// vertical high-order flux minus the LO flux (adv_tra_ver_qr4c / _upw1 with w,
+// src/oce_adv_tra_ver.F90:244-434).  Without a limiter only the HO vertical
+// flux (with w_e) is formed.
+// ===========================================================================
+template <typename R>
+__device__ __forceinline__ R ver_upw1_flux(const R *T, const R *W, const R *area, int nz, int n, int nzmin, int nzmax,
+                                           int L1, int nl, R fin) {
+    // statement order of the reference: surface, bottom, interior
+    R v = fin;
+    if (nz == nzmin) v = -(W[ixn(nz, n, nl)] * T[ix1(nz, n, L1)] * area[ixn(nz, n, nl)]) - v;
+    if (nz == nzmax) v = R(0.0) - v;
+    if (nz >= nzmin + 1 && nz <= nzmax - 1) {
+        const R Wv = W[ixn(nz, n, nl)], aW = rabs(Wv);
+        v = -(R(0.5) * (T[ix1(nz, n, L1)] * (Wv + aW) + T[ix1(nz - 1, n, L1)] * (Wv - aW)) * area[ixn(nz, n, nl)]) - v;
+    }
+    return v;
+}
+
+template <typename R>
+__device__ __forceinline__ R ver_qr4c_flux(const R *T, const R *W, const R *area, const R *Z3, const R *zb3, int nz,
+                                           int n, int nzmin, int nzmax, int L1, int nl, R no, R fin) {
+    // statement order of the reference: nzmin, nzmin+1, nzmax-1, nzmax, interior
+    R v = fin;
+    if (nz == nzmin) v = -(T[ix1(nz, n, L1)] * W[ixn(nz, n, nl)] * area[ixn(nz, n, nl)]) - v;
+    if (nz == nzmin + 1)
+        v = -(R(0.5) * (T[ix1(nz - 1, n, L1)] + T[ix1(nz, n, L1)]) * W[ixn(nz, n, nl)] * area[ixn(nz, n, nl)]) - v;
+    if (nz == nzmax - 1)
+        v = -(R(0.5) * (T[ix1(nz - 1, n, L1)] + T[ix1(nz, n, L1)]) * W[ixn(nz, n, nl)] * area[ixn(nz, n, nl)]) - v;
+    if (nz == nzmax) v = R(0.0) - v;
+    if (nz >= nzmin + 2 && nz <= nzmax - 2) {
+        const R tm2 = T[ix1(nz - 2, n, L1)], tm1 = T[ix1(nz - 1, n, L1)], t0 = T[ix1(nz, n, L1)],
+                tp1 = T[ix1(nz + 1, n, L1)];
+        const R zm2 = Z3[ix1(nz - 2, n, L1)], zm1 = Z3[ix1(nz - 1, n, L1)], z0 = Z3[ix1(nz, n, L1)],
+                zp1 = Z3[ix1(nz + 1, n, L1)];
+        const R qc = (tm1 - t0) / (zm1 - z0);
+        const R qu = (t0 - tp1) / (z0 - zp1);
+        const R qd = (tm2 - tm1) / (zm2 - zm1);
+        const R zb = zb3[ixn(nz, n, nl)];
+        const R Tm1 = t0 + (R(2.0) * qc + qu) * (zb - z0) / R(3.0);
+        const R Tm2 = tm1 + (R(2.0) * qc + qd) * (zb - zm1) / R(3.0);
+        const R Wv = W[ixn(nz, n, nl)], aW = rabs(Wv);
+        const R Tmean = (Wv + aW) * Tm1 + (Wv - aW) * Tm2;
+        v = (-(R(0.5) * (R(1.0) - no) * Tmean) - no * (R(0.5) * (Tm1 + Tm2)) * Wv) * area[ixn(nz, n, nl)] - v;
+    }
+    return v;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kThreads)
+k_node_lo(DTopo tp, DGeom<R> g, DForcing<R> f, DTracers<R> tr, R dt) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int L1 = tp.L1, nl = tp.nl;
+    for (int n = blockIdx.x * kWarpsPerBlock + warp; n < tp.N2; n += gridDim.x * kWarpsPerBlock) {
+        const int nzmin = tp.n_ulev[n], nzmax = tp.n_nlev[n];
+        const int k0 = tp.ne_ptr[n], k1 = tp.ne_ptr[n + 1];
+        for (int t = 0; t < tr.ntr; t++) {
+            const DCfg c = tr.cfg[t];
+            const int fct = c.lim;
+            const R *T = tr.T + t * tr.sN;
+            const R *TA = tr.TAB + t * tr.sN;
+            const R *FLO = tr.FLO + t * tr.sE;
+            for (int nz = nzmin + lane; nz <= nzmax; nz += 32) {
+                R fv0 = R(0);
+                if (fct) {
+                    fv0 = ver_upw1_flux(T, f.we, g.area, nz, n, nzmin, nzmax, L1, nl, R(0));
+                    if (nz <= nzmax - 1) {
+                        const R fv1 = ver_upw1_flux(T, f.we, g.area, nz + 1, n, nzmin, nzmax, L1, nl, R(0));
+                        R acc = R(0);
+                        for (int k = k0; k < k1; k++) {
+                            const int code = tp.ne_idx[k];
+                            const int e = code >= 0 ? code : ~code;
+                            if (nz < tp.e_lo[e] || nz > tp.e_hi[e]) continue;
+                            const R x = FLO[ix1(nz, e, L1)];
+                            acc = code >= 0 ? acc + x : acc - x;
+                        }
+                        const size_t i = ix1(nz, n, L1);
+                        tr.LO[t * tr.sN + i] =
+                            (T[i] * g.hnode[i] + (acc + (fv0 - fv1)) * dt / g.areasvol[ixn(nz, n, nl)]) / g.hnode_new[i];
+                    }
+                }
+                const R *pw = fct ? f.w : f.we;
+                R v;
+                if (c.ver == 0)
+                    v = ver_qr4c_flux(TA, pw, g.area, g.Z3, g.zbar3, nz, n, nzmin, nzmax, L1, nl, R(c.pv), fv0);
+                else
+                    v = ver_upw1_flux(TA, pw, g.area, nz, n, nzmin, nzmax, L1, nl, fv0);
+                tr.ADv[t * tr.sNI + ixn(nz, n, nl)] = v;
+            }
+        }
+    }
+}
+
+// ===========================================================================
+// FCT bounds a1-a3 and bound increments (src/oce_adv_tra_fct.F90:124-248).
+// The element max/min (AUX) is recomputed per node from the element's three
+// nodes (max/min are exact, so this equals the reference's two passes).
+// ===========================================================================
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_bounds(DTopo tp, DTracers<R> tr) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R *sm = reinterpret_cast<R *>(smem_raw);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int L1 = tp.L1;
+    R *tvmax = sm + (size_t)warp * 2 * (L1 + 2);
+    R *tvmin = tvmax + (L1 + 2);
+    const R big = R(kBigNumber);
+    for (int n = blockIdx.x * kWarpsPerBlock + warp; n < tp.N2; n += gridDim.x * kWarpsPerBlock) {
+        const int nzmin = tp.n_ulev[n], nzmax = tp.n_nlev[n];
+        const int k0 = tp.nie_ptr[n], k1 = tp.nie_ptr[n + 1];
+        for (int t = 0; t < tr.ntr; t++) {
+            if (!tr.cfg[t].lim) continue;
+            const R *T = tr.T + t * tr.sN;
+            const R *LO = tr.LO + t * tr.sN;
+            for (int nz = nzmin + lane; nz <= nzmax - 1; nz += 32) {
+                R mx = R(0), mn = R(0);
+                for (int k = k0; k < k1; k++) {
+                    const int el = tp.nie_idx[k];
+                    R amx, amn;
+                    if (nz >= tp.t_ulev[el] && nz <= tp.t_nlev[el] - 1) {
+                        const int a = tp.t_n[3 * el], b = tp.t_n[3 * el + 1], cc = tp.t_n[3 * el + 2];
+                        const R la = LO[ix1(nz, a, L1)], ta = T[ix1(nz, a, L1)];
+                        const R lb = LO[ix1(nz, b, L1)], tb = T[ix1(nz, b, L1)];
+                        const R lc = LO[ix1(nz, cc, L1)], tc = T[ix1(nz, cc, L1)];
+                        amx = rmax(rmax(rmax(la, ta), rmax(lb, tb)), rmax(lc, tc));
+                        amn = rmin(rmin(rmin(la, ta), rmin(lb, tb)), rmin(lc, tc));
+                    } else {
+                        amx = -big;
+                        amn = big;
+                    }
+                    if (k == k0) { mx = amx; mn = amn; }
+                    else { mx = rmax(mx, amx); mn = rmin(mn, amn); }
+                }
+                tvmax[nz] = mx;
+                tvmin[nz] = mn;
+            }
+            __syncwarp();
+            R *bmx = tr.bmax + t * tr.sN, *bmn = tr.bmin + t * tr.sN;
+            for (int nz = nzmin + lane; nz <= nzmax - 1; nz += 32) {
+                const R lo = LO[ix1(nz, n, L1)];
+                R vmx, vmn;
+                if (nz == nzmin || nz == nzmax - 1) {
+                    vmx = tvmax[nz] - lo;
+                    vmn = tvmin[nz] - lo;
+                } else {
+                    vmx = rmax(rmax(tvmax[nz - 1], tvmax[nz]), tvmax[nz + 1]) - lo;
+                    vmn = rmin(rmin(tvmin[nz - 1], tvmin[nz]), tvmin[nz + 1]) - lo;
+                }
+                bmx[ix1(nz, n, L1)] = vmx;
+                bmn[ix1(nz, n, L1)] = vmn;
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// ===========================================================================
+// FCT b1 + b2: sums of positive / negative antidiffusive fluxes into each
+// node-layer (vertical, then edges in ascending order) and the ratios R+ / R-
+// (src/oce_adv_tra_fct.F90:265-405).  R+ / R- overwrite bmax / bmin.
+// ===========================================================================
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_rpm(DTopo tp, DGeom<R> g, DTracers<R> tr, R dt) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int L1 = tp.L1, nl = tp.nl;
+    const R eps = R(kFluxEps);
+    for (int n = blockIdx.x * kWarpsPerBlock + warp; n < tp.N2; n += gridDim.x * kWarpsPerBlock) {
+        const int nzmin = tp.n_ulev[n], nzmax = tp.n_nlev[n];
+        const int k0 = tp.ne_ptr[n], k1 = tp.ne_ptr[n + 1];
+        for (int t = 0; t < tr.ntr; t++) {
+            if (!tr.cfg[t].lim) continue;
+            const R *ADv = tr.ADv + t * tr.sNI;
+            const R *ADh = tr.ADh + t * tr.sE;
+            for (int nz = nzmin + lane; nz <= nzmax - 1; nz += 32) {
+                const R v0 = ADv[ixn(nz, n, nl)], v1 = ADv[ixn(nz + 1, n, nl)];
+                Acc<R> P, M;
+                P.add(rmax(R(0), v0) + rmax(R(0), -v1));
+                M.add(rmin(R(0), v0) + rmin(R(0), -v1));
+                for (int k = k0; k < k1; k++) {
+                    const int code = tp.ne_idx[k];
+                    const int e = code >= 0 ? code : ~code;
+                    if (nz < tp.e_lo[e] || nz > tp.e_hi[e]) continue;
+                    const R x = ADh[ix1(nz, e, L1)];
+                    if (code >= 0) { P.add(rmax(R(0), x)); M.add(rmin(R(0), x)); }
+                    else { P.add(rmax(R(0), -x)); M.add(rmin(R(0), -x)); }
+                }
+                const size_t i = ix1(nz, n, L1);
+                const R av = g.areasvol[ixn(nz, n, nl)], hn = g.hnode_new[i];
+                R fl = P.get() * dt / av / hn + eps;
+                const R rp = rmin(R(1.0), tr.bmax[t * tr.sN + i] / fl);
+                fl = M.get() * dt / av / hn - eps;
+                const R rm = rmin(R(1.0), tr.bmin[t * tr.sN + i] / fl);
+                tr.bmax[t * tr.sN + i] = rp;
+                tr.bmin[t * tr.sN + i] = rm;
+            }
+        }
+    }
+}
+
+// ===========================================================================
+// FCT b3 limiting + oce_tra_adv_flux2dtracer (src/oce_adv_tra_fct.F90:425-500,
+// src/oce_adv_tra_driver.F90:494-646) + (mode 1) the del_ttf sum and the T*
+// update of diff_tracers_ale (src/oce_ale_tracer.F90:319-321, 743-754).
+// The limited edge flux is formed at each end node from R+/R- of both ends.
+// ===========================================================================
+template <typename R>
+__device__ __forceinline__ R limited_adv(const R *ADv, const R *Rp, const R *Rm, int nz, int n, int nzmin, int nzmax,
+                                         int L1, int nl) {
+    const R x = ADv[ixn(nz, n, nl)];
+    if (nz == nzmax) return x;
+    R ae = R(1.0);
+    if (nz == nzmin) {
+        ae = x >= R(0) ? rmin(ae, Rp[ix1(nz, n, L1)]) : rmin(ae, Rm[ix1(nz, n, L1)]);
+    } else if (x >= R(0)) {
+        ae = rmin(ae, Rm[ix1(nz - 1, n, L1)]);
+        ae = rmin(ae, Rp[ix1(nz, n, L1)]);
+    } else {
+        ae = rmin(ae, Rp[ix1(nz - 1, n, L1)]);
+        ae = rmin(ae, Rm[ix1(nz, n, L1)]);
+    }
+    return ae * x;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_update(DTopo tp, DGeom<R> g, DTracers<R> tr, R dt, int mode) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int L1 = tp.L1, nl = tp.nl;
+    for (int n = blockIdx.x * kWarpsPerBlock + warp; n < tp.N2; n += gridDim.x * kWarpsPerBlock) {
+        const int nzmin = tp.n_ulev[n], nzmax = tp.n_nlev[n];
+        const int k0 = tp.ne_ptr[n], k1 = tp.ne_ptr[n + 1];
+        for (int t = 0; t < tr.ntr; t++) {
+            const int fct = tr.cfg[t].lim;
+            R *T = tr.T + t * tr.sN;
+            const R *ADv = tr.ADv + t * tr.sNI;
+            const R *ADh = tr.ADh + t * tr.sE;
+            const R *Rp = tr.bmax + t * tr.sN, *Rm = tr.bmin + t * tr.sN;
+            for (int nz = nzmin + lane; nz <= nzmax - 1; nz += 32) {
+                const size_t i = ix1(nz, n, L1);
+                const R av = g.areasvol[ixn(nz, n, nl)];
+                R dv = R(0.0);
+                R f0, f1;
+                if (fct) {
+                    dv = dv - T[i] * g.hnode[i] + tr.LO[t * tr.sN + i] * g.hnode_new[i];
+                    f0 = limited_adv(ADv, Rp, Rm, nz, n, nzmin, nzmax, L1, nl);
+                    f1 = limited_adv(ADv, Rp, Rm, nz + 1, n, nzmin, nzmax, L1, nl);
+                } else {
+                    f0 = ADv[ixn(nz, n, nl)];
+                    f1 = ADv[ixn(nz + 1, n, nl)];
+                }
+                dv = dv + (f0 - f1) * dt / av;
+                Acc<R> dh;
+                for (int k = k0; k < k1; k++) {
+                    const int code = tp.ne_idx[k];
+                    const int e = code >= 0 ? code : ~code;
+                    if (nz < tp.e_lo[e] || nz > tp.e_hi[e]) continue;
+                    R x = ADh[ix1(nz, e, L1)];
+                    if (fct) {
+                        const int a = tp.e_n1[e], b = tp.e_n2[e];
+                        R ae = R(1.0);
+                        if (x >= R(0)) {
+                            ae = rmin(ae, Rp[ix1(nz, a, L1)]);
+                            ae = rmin(ae, Rm[ix1(nz, b, L1)]);
+                        } else {
+                            ae = rmin(ae, Rm[ix1(nz, a, L1)]);
+                            ae = rmin(ae, Rp[ix1(nz, b, L1)]);
+                        }
+                        x = ae * x;
+                    }
+                    if (code >= 0) dh.add(x * dt / av);
+                    else dh.sub(x * dt / av);
+                }
+                const R dhv = dh.get();
+                if (mode == 0) {
+                    tr.dttf_h[t * tr.sN + i] = dhv;
+                    tr.dttf_v[t * tr.sN + i] = dv;
+                } else {
+                    R del = R(0.0) + dhv + dv;
+                    del = del + T[i] * (g.hnode[i] - g.hnode_new[i]);
+                    const R tn = T[i] + del / g.hnode_new[i];
+                    T[i] = tn;
+                    if (!isfinite(tn)) atomicOr(tr.status, 1u);
+                }
+            }
+        }
+    }
+}
+
+// ===========================================================================
+// diff_ver_part_impl_ale (src/oce_ale_tracer.F90:1071-1430): one thread per
+// column, arithmetic in A (double for both forms).  Scratch holds Z_n, cp and
+// tp level-major ([level][node]) so that a warp's accesses are coalesced.
+// ===========================================================================
+template <typename R>
+__global__ void __launch_bounds__(128) k_vdiff(DTopo tp, DGeom<R> g, DForcing<R> f, DTracers<R> tr, double dt,
+                                               double *scratch) {
+    typedef double A;
+    const int L1 = tp.L1, nl = tp.nl;
+    const size_t N2 = tp.N2;
+    A *Zs = scratch, *cps = scratch + (size_t)(L1 + 1) * N2, *tps = cps + (size_t)(L1 + 1) * N2;
+#define ZN(k) Zs[(size_t)(k) * N2 + n]
+#define CP(k) cps[(size_t)(k) * N2 + n]
+#define TP(k) tps[(size_t)(k) * N2 + n]
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < tp.N2; n += gridDim.x * blockDim.x) {
+        const int nzmax = tp.n_nlev[n], nzmin = tp.n_ulev[n];
+        const R *hn = g.hnode_new + (size_t)n * L1 - 1;  // hn[nz], 1-based
+        const R *ar = g.area + (size_t)n * nl - 1;
+        const R *av = g.areasvol + (size_t)n * nl - 1;
+        const R *kv = f.Kv + (size_t)n * nl - 1;
+        // Z_n bottom-up (:1088-1096); ZN(k) = Z_n(k)
+        A zb = (A)g.zbar_n_bot[n];
+        ZN(nzmax - 1) = zb + (A)hn[nzmax - 1] / 2.0;
+        for (int nz = nzmax - 1; nz >= nzmin + 1; nz--) {
+            zb = zb + (A)hn[nz];
+            ZN(nz - 1) = zb + (A)hn[nz - 1] / 2.0;
+        }
+        for (int t = 0; t < tr.ntr; t++) {
+            R *Tc = tr.T + t * tr.sN + (size_t)n * L1 - 1;
+            if (!tr.cfg[t].ivd) continue;
+            const A bc = f.bc ? (A)f.bc[(size_t)t * N2 + n] : 0.0;
+            // forward elimination, coefficients built on the fly (:1099-1229, 1406-1414)
+            int nz = nzmin;
+            A zinv2 = 1.0 / (ZN(nz) - ZN(nz + 1));
+            const A zinv = 1.0 * dt;
+            A c = -((A)kv[nz + 1] * zinv2 * zinv * (A)ar[nz + 1] / (A)av[nz]);
+            A b = -c + (A)hn[nz];
+            A Tm = (A)Tc[nz], T0 = Tm, Tp1 = (A)Tc[nz + 1];
+            A dz = (A)hn[nz];
+            A rhs = -((b - dz) * T0) - c * Tp1;
+            rhs = rhs + bc;
+            A cp = c / b, tpv = rhs / b;
+            CP(nz) = cp;
+            TP(nz) = tpv;
+            A zinv1 = zinv2;
+            for (nz = nzmin + 1; nz <= nzmax - 2; nz++) {
+                zinv2 = 1.0 / (ZN(nz) - ZN(nz + 1));
+                const A a = -((A)kv[nz] * zinv1 * zinv * ((A)ar[nz] / (A)av[nz]));
+                c = -((A)kv[nz + 1] * zinv2 * zinv * (A)ar[nz + 1] / (A)av[nz]);
+                b = -a - c + (A)hn[nz];
+                zinv1 = zinv2;
+                Tm = T0;
+                T0 = Tp1;
+                Tp1 = (A)Tc[nz + 1];
+                dz = (A)hn[nz];
+                rhs = -(a * Tm) - (b - dz) * T0 - c * Tp1;
+                const A m = b - cp * a;
+                cp = c / m;
+                tpv = (rhs - tpv * a) / m;
+                CP(nz) = cp;
+                TP(nz) = tpv;
+            }
+            nz = nzmax - 1;
+            {
+                const A a = -((A)kv[nz] * zinv1 * zinv * ((A)ar[nz] / (A)av[nz]));
+                b = -a + (A)hn[nz];
+                Tm = T0;
+                T0 = Tp1;
+                dz = (A)hn[nz];
+                rhs = -(a * Tm) - (b - dz) * T0;
+                const A m = b - cp * a;
+                tpv = (rhs - tpv * a) / m;
+            }
+            // back substitution (:1417-1430)
+            A trv = tpv;
+            Tc[nzmax - 1] = (R)((A)Tc[nzmax - 1] + trv);
+            for (nz = nzmax - 2; nz >= nzmin; nz--) {
+                trv = TP(nz) - CP(nz) * trv;
+                Tc[nz] = (R)((A)Tc[nz] + trv);
+            }
+        }
+    }
+#undef ZN
+#undef CP
+#undef TP
+}
+
+// ===========================================================================
+// Global content sum over wet node-layers of T * hnode_new * areasvol (FP64),
+// deterministic: fixed per-block partials, then one ordered pass.
+// ===========================================================================
+template <typename R>
+__global__ void __launch_bounds__(256) k_content_partial(DTopo tp, DGeom<R> g, DTracers<R> tr, double *partials) {
+    __shared__ double red[256];
+    const int L1 = tp.L1, nl = tp.nl;
+    for (int t = 0; t < tr.ntr; t++) {
+        const R *T = tr.T + t * tr.sN;
+        double s = 0.0;
+        for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < tp.N2; n += gridDim.x * blockDim.x) {
+            for (int nz = tp.n_ulev[n]; nz <= tp.n_nlev[n] - 1; nz++) {
+                const size_t i = ix1(nz, n, L1);
+                s += (double)T[i] * (double)g.hnode_new[i] * (double)g.areasvol[ixn(nz, n, nl)];
+            }
+        }
+        red[threadIdx.x] = s;
+        __syncthreads();
+        for (int o = 128; o > 0; o >>= 1) {
+            if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) partials[(size_t)t * gridDim.x + blockIdx.x] = red[0];
+        __syncthreads();
+    }
+}
+
+static __global__ void k_content_final(const double *partials, int nblk, int ntr, double *out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntr) return;
+    double s = 0.0;
+    for (int b = 0; b < nblk; b++) s += partials[(size_t)t * nblk + b];
+    out[t] = s;
+}
+
+// ===========================================================================
+// launch wrappers
+// ===========================================================================
+static inline int grid_for(int nent, int per_block) {
+    int b = (nent + per_block - 1) / per_block;
+    const int cap = 152 * 64;
+    if (b > cap) b = cap;
+    return b < 1 ? 1 : b;
+}
+
+template <typename R>
+void Launch<R>::ab(const DTopo &tp, DTracers<R> &tr, int ab, cudaStream_t s) {
+    const size_t n = (size_t)tp.L1 * tp.N2;
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_ab<R><<<blocks, 256, 0, s>>>(tr, n, ab);
+}
+template <typename R>
+void Launch<R>::trxy(const DTopo &tp, const DGeom<R> &g, DTracers<R> &tr, cudaStream_t s) {
+    k_trxy<R><<<grid_for(tp.T2, kWarpsPerBlock), kThreads, 0, s>>>(tp, g, tr);
+}
+template <typename R>
+void Launch<R>::edge_flux(const DTopo &tp, const DGeom<R> &g, const DForcing<R> &f, DTracers<R> &tr, int fct,
+                          cudaStream_t s) {
+    (void)fct;
+    k_edge_flux<R><<<grid_for(tp.E2, kWarpsPerBlock), kThreads, 0, s>>>(tp, g, f, tr);
+}
+template <typename R>
+void Launch<R>::node_lo(const DTopo &tp, const DGeom<R> &g, const DForcing<R> &f, DTracers<R> &tr, double dt, int fct,
+                        cudaStream_t s) {
+    (void)fct;
+    k_node_lo<R><<<grid_for(tp.N2, kWarpsPerBlock), kThreads, 0, s>>>(tp, g, f, tr, (R)dt);
+}
+template <typename R>
+void Launch<R>::bounds(const DTopo &tp, DTracers<R> &tr, cudaStream_t s) {
+    const size_t sm = sizeof(R) * 2 * (tp.L1 + 2) * kWarpsPerBlock;
+    k_bounds<R><<<grid_for(tp.N2, kWarpsPerBlock), kThreads, sm, s>>>(tp, tr);
+}
+template <typename R>
+void Launch<R>::rpm(const DTopo &tp, const DGeom<R> &g, DTracers<R> &tr, double dt, cudaStream_t s) {
+    k_rpm<R><<<grid_for(tp.N2, kWarpsPerBlock), kThreads, 0, s>>>(tp, g, tr, (R)dt);
+}
+template <typename R>
+void Launch<R>::update(const DTopo &tp, const DGeom<R> &g, DTracers<R> &tr, double dt, int fct, int mode,
+                       cudaStream_t s) {
+    (void)fct;
+    k_update<R><<<grid_for(tp.N2, kWarpsPerBlock), kThreads, 0, s>>>(tp, g, tr, (R)dt, mode);
+}
+template <typename R>
+void Launch<R>::vdiff(const DTopo &tp, const DGeom<R> &g, const DForcing<R> &f, DTracers<R> &tr, double dt,
+                      double *scratch, cudaStream_t s) {
+    int blocks = (tp.N2 + 127) / 128;
+    k_vdiff<R><<<blocks, 128, 0, s>>>(tp, g, f, tr, dt, scratch);
+}
+template <typename R>
+void Launch<R>::content(const DTopo &tp, const DGeom<R> &g, const DTracers<R> &tr, double *partials, int nblk,
+                        double *out, cudaStream_t s) {
+    k_content_partial<R><<<nblk, 256, 0, s>>>(tp, g, tr, partials);
+    k_content_final<<<(tr.ntr + 63) / 64, 64, 0, s>>>(partials, nblk, tr.ntr, out);
+}
+
+}  // namespace fesom

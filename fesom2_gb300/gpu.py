@@ -1,0 +1,320 @@
+"""ctypes binding of libfesom_gpu.so (the C ABI in include/fesom_gpu.h).
+
+This module is the Python face of the library: it fills a
+``fesom_mesh_desc`` from a :class:`fesom2_gb300.mesh.Mesh` and exposes each
+entry point.  There is no CPU fallback: if the shared library cannot be
+loaded, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import build as _build
+
+_P = C.c_void_p
+LIB_PATH = _build.LIB
+
+PREC_FP64, PREC_FP32 = 0, 1
+HOR = {"MUSCL": 0, "MFCT": 1, "UPW1": 2}
+VER = {"QR4C": 0, "UPW1": 1, "CDIFF": 2, "PPM": 3}
+LIM = {"NON": 0, "FCT": 1}
+ERRORS = {1: "ARG", 2: "SCHEME", 3: "MESH", 4: "CUDA", 5: "NOMEM", 6: "TIMEOUT", 7: "NUMERIC", 8: "STATE"}
+STATUS_NAN, STATUS_FCT_BOUND, STATUS_INDEX = 1, 2, 4
+STAGES = ["ab", "trxy", "edge_flux", "node_lo", "bounds", "rpm", "update", "vdiff"]
+STAGES_N = len(STAGES)
+
+
+class TraCfg(C.Structure):
+    _fields_ = [("adv_hor", C.c_int32), ("adv_ver", C.c_int32), ("adv_lim", C.c_int32), ("ab_order", C.c_int32),
+                ("adv_ph", C.c_double), ("adv_pv", C.c_double), ("i_vert_diff", C.c_int32), ("id", C.c_int32)]
+
+
+def tra_cfg(hor="MUSCL", ver="QR4C", lim="FCT", ph=0.0, pv=1.0, ab_order=2, i_vert_diff=True, id=1) -> TraCfg:
+    """One nml_tracer_list row of namelist.tra (plus AB_order and i_vert_diff)."""
+    return TraCfg(HOR[hor], VER[ver], LIM[lim.strip()], int(ab_order), float(ph), float(pv),
+                  1 if i_vert_diff else 0, int(id))
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("nod2D", C.c_int32), ("elem2D", C.c_int32), ("edge2D", C.c_int32), ("nl", C.c_int32),
+                ("index_base", C.c_int32), ("ld_nie", C.c_int32)] + \
+        [(n, _P) for n in ("elem2D_nodes", "edges", "edge_tri", "nod_in_elem2D_num", "nod_in_elem2D",
+                           "nlevels", "ulevels", "nlevels_nod2D", "ulevels_nod2D", "nlevels_nod2D_min",
+                           "ulevels_nod2D_max", "coord_nod2D", "elem_area", "elem_cos", "edge_dxdy",
+                           "edge_cross_dxdy", "gradient_sca", "area", "areasvol", "hnode", "hnode_new", "helem",
+                           "Z_3d_n", "zbar_3d_n", "zbar_n_bot")] + \
+        [("cyclic_length", C.c_double), ("nboundary_lay", _P), ("edge_up_dn_tri", _P)]
+
+
+class FesomGpuError(RuntimeError):
+    def __init__(self, rc: int, msg: str):
+        super().__init__(f"FESOM_ERR_{ERRORS.get(rc, rc)}: {msg}")
+        self.rc = rc
+
+
+_lib: Optional[C.CDLL] = None
+
+_SIGS = {
+    "fesom_gpu_abi_version": ([], C.c_int),
+    "fesom_gpu_last_error": ([_P], C.c_char_p),
+    "fesom_gpu_init": ([C.POINTER(MeshDesc), C.c_int32, C.c_int32, C.POINTER(_P)], C.c_int),
+    "fesom_gpu_finalize": ([_P], C.c_int),
+    "fesom_gpu_mesh_check": ([C.POINTER(MeshDesc), _P, _P, C.c_char_p, C.c_int32], C.c_int),
+    "fesom_gpu_set_stream": ([_P, _P], C.c_int),
+    "fesom_gpu_get_muscl_init": ([_P, _P, _P], C.c_int),
+    "fesom_gpu_status": ([_P, C.POINTER(C.c_uint32), C.c_int32], C.c_int),
+    "fesom_gpu_update_thickness": ([_P, _P, _P, _P, _P, _P], C.c_int),
+    "fesom_gpu_init_tracers_ab": ([_P, C.POINTER(TraCfg), _P, _P, _P], C.c_int),
+    "fesom_gpu_adv_tra": ([_P, C.c_double, _P, _P, _P, _P, C.POINTER(TraCfg), _P, _P, _P, _P], C.c_int),
+    "fesom_gpu_vdiff_impl": ([_P, C.c_double, C.POINTER(TraCfg), _P, _P, _P], C.c_int),
+    "fesom_gpu_tracer_step": ([_P, C.c_int32, C.POINTER(TraCfg), C.c_double, _P, _P, _P, _P, _P, _P,
+                               C.POINTER(_P), C.POINTER(_P)], C.c_int),
+    "fesom_gpu_state_setup": ([_P, C.c_int32, C.POINTER(TraCfg)], C.c_int),
+    "fesom_gpu_forcing_upload": ([_P, _P, _P, _P, _P, _P, _P], C.c_int),
+    "fesom_gpu_forcing_upload_f32": ([_P, _P, _P, _P, _P, _P, _P], C.c_int),
+    "fesom_gpu_tracer_upload": ([_P, C.c_int32, _P, _P], C.c_int),
+    "fesom_gpu_tracer_download": ([_P, C.c_int32, _P, _P], C.c_int),
+    "fesom_gpu_tracer_upload_f32": ([_P, C.c_int32, _P, _P], C.c_int),
+    "fesom_gpu_tracer_download_f32": ([_P, C.c_int32, _P, _P], C.c_int),
+    "fesom_gpu_run_steps": ([_P, C.c_double, C.c_int32, C.c_int32], C.c_int),
+    "fesom_gpu_tracer_content": ([_P, _P], C.c_int),
+    "fesom_gpu_set_tracers_per_launch": ([_P, C.c_int32], C.c_int),
+    "fesom_gpu_profile_step": ([_P, C.c_double, _P, _P], C.c_int),
+    "fesom_gpu_launches_per_step": ([_P, C.POINTER(C.c_int32)], C.c_int),
+    "fesom_gpu_debug_fetch": ([_P, C.c_char_p, C.c_int32, _P, C.c_size_t], C.c_int),
+    "fesom_gpu_tracer_device_ptr": ([_P, C.c_int32, C.POINTER(_P), C.POINTER(_P)], C.c_int),
+}
+
+
+def load(path: Optional[str] = None) -> C.CDLL:
+    """Load the shared library (raises if it is missing; no fallback)."""
+    global _lib
+    if _lib is None:
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise FileNotFoundError(f"{p} is missing: build it with `python -m fesom2_gb300.build`")
+        L = C.CDLL(p)
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def _p(a: Optional[np.ndarray]):
+    if a is None:
+        return None
+    return C.c_void_p(a.ctypes.data)
+
+
+def _c64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+def mesh_desc(mesh, pass_muscl_init=None):
+    """Build a ``fesom_mesh_desc`` (and the arrays it points to) for a Mesh."""
+    i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+    f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    nie_num = mesh.nod_in_elem2D_num()
+    ld = int(nie_num.max())
+    nie2 = np.zeros((mesh.nod2D, ld), dtype=np.int32)
+    rows = np.repeat(np.arange(mesh.nod2D), nie_num)
+    cols = np.arange(mesh.nod_in_elem2D.size) - np.repeat(mesh.nod_in_elem2D_ptr[:-1], nie_num)
+    nie2[rows, cols] = mesh.nod_in_elem2D
+    keep = dict(
+            elem2D_nodes=i32(mesh.elem2D_nodes), edges=i32(mesh.edges), edge_tri=i32(mesh.edge_tri),
+            nod_in_elem2D_num=i32(nie_num), nod_in_elem2D=nie2, nlevels=i32(mesh.nlevels),
+            ulevels=i32(mesh.ulevels), nlevels_nod2D=i32(mesh.nlevels_nod2D), ulevels_nod2D=i32(mesh.ulevels_nod2D),
+            nlevels_nod2D_min=i32(mesh.nlevels_nod2D_min), ulevels_nod2D_max=i32(mesh.ulevels_nod2D_max),
+            coord_nod2D=f64(mesh.coord_nod2D), elem_area=f64(mesh.elem_area), elem_cos=f64(mesh.elem_cos),
+            edge_dxdy=f64(mesh.edge_dxdy), edge_cross_dxdy=f64(mesh.edge_cross_dxdy),
+            gradient_sca=f64(mesh.gradient_sca), area=f64(mesh.area), areasvol=f64(mesh.areasvol),
+            hnode=f64(mesh.hnode), hnode_new=f64(mesh.hnode_new), helem=f64(mesh.helem), Z_3d_n=f64(mesh.Z_3d_n),
+            zbar_3d_n=f64(mesh.zbar_3d_n), zbar_n_bot=f64(mesh.zbar_n_bot))
+    d = MeshDesc()
+    d.nod2D, d.elem2D, d.edge2D, d.nl = mesh.nod2D, mesh.elem2D, mesh.edge2D, mesh.nl
+    d.index_base = 0
+    d.ld_nie = ld
+    for k, v in keep.items():
+        setattr(d, k, v.ctypes.data)
+    d.cyclic_length = float(mesh.cyclic_length)
+    if pass_muscl_init is not None:
+        nbl, updn = pass_muscl_init
+        keep["nbl"] = i32(nbl)
+        keep["updn"] = i32(updn)
+        d.nboundary_lay = keep["nbl"].ctypes.data
+        d.edge_up_dn_tri = keep["updn"].ctypes.data
+    return d, keep
+
+
+def mesh_check(mesh, pass_muscl_init=None):
+    """Host-only validation; returns (nboundary_lay, edge_up_dn_tri) 0-based (-1 = none)."""
+    L = load()
+    d, keep = mesh_desc(mesh, pass_muscl_init)
+    nbl = np.zeros(mesh.nod2D, np.int32)
+    updn = np.zeros((mesh.edge2D, 2), np.int32)
+    buf = C.create_string_buffer(512)
+    rc = L.fesom_gpu_mesh_check(C.byref(d), _p(nbl), _p(updn), buf, 512)
+    if rc != 0:
+        raise FesomGpuError(rc, buf.value.decode())
+    return nbl, updn
+
+
+class Context:
+    """One ``fesom_gpu_ctx``: a mesh on the current CUDA device."""
+
+    def __init__(self, mesh, precision: int = PREC_FP64, max_tracers: int = 1, pass_muscl_init=None):
+        L = load()
+        self.mesh = mesh
+        self.prec = precision
+        d, self._keep = mesh_desc(mesh, pass_muscl_init)
+        self.desc = d
+        h = _P()
+        rc = L.fesom_gpu_init(C.byref(d), int(precision), int(max_tracers), C.byref(h))
+        self.h = h
+        if rc != 0:
+            msg = L.fesom_gpu_last_error(h).decode() if h.value else "init failed"
+            L.fesom_gpu_finalize(h)
+            self.h = _P()
+            raise FesomGpuError(rc, msg)
+        self.L = L
+
+    # -- plumbing -------------------------------------------------------------
+    def _chk(self, rc: int):
+        if rc != 0:
+            raise FesomGpuError(rc, self.L.fesom_gpu_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.fesom_gpu_finalize(self.h)
+            self.h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int):
+        self._chk(self.L.fesom_gpu_set_stream(self.h, C.c_void_p(stream_handle)))
+
+    def muscl_init(self):
+        nbl = np.zeros(self.mesh.nod2D, np.int32)
+        updn = np.zeros((self.mesh.edge2D, 2), np.int32)
+        self._chk(self.L.fesom_gpu_get_muscl_init(self.h, _p(nbl), _p(updn)))
+        return nbl, updn
+
+    def status(self, timeout_ms: int = 60000) -> int:
+        s = C.c_uint32(0)
+        self._chk(self.L.fesom_gpu_status(self.h, C.byref(s), int(timeout_ms)))
+        return int(s.value)
+
+    # -- per-routine drop-ins (FP64) ---------------------------------------------
+    def init_tracers_ab(self, cfg: TraCfg, values, valuesAB, valuesold):
+        self._chk(self.L.fesom_gpu_init_tracers_ab(self.h, C.byref(cfg), _p(values), _p(valuesAB), _p(valuesold)))
+
+    def adv_tra(self, forcing, cfg: TraCfg, ttf, ttfAB, dt=None):
+        N2, L1 = self.mesh.nod2D, self.mesh.nl - 1
+        dh = np.zeros((N2, L1))
+        dv = np.zeros((N2, L1))
+        uv, w, wi, we = _c64(forcing.uv), _c64(forcing.w), _c64(forcing.w_i), _c64(forcing.w_e)
+        self._chk(self.L.fesom_gpu_adv_tra(self.h, float(forcing.dt if dt is None else dt), _p(uv), _p(w), _p(wi),
+                                           _p(we), C.byref(cfg), _p(_c64(ttf)), _p(_c64(ttfAB)), _p(dh), _p(dv)))
+        return dh, dv
+
+    def vdiff_impl(self, forcing, cfg: TraCfg, values, dt=None, bc=None):
+        Kv = _c64(forcing.Kv)
+        bcs = _c64(forcing.bc_surface if bc is None else bc)
+        self._chk(self.L.fesom_gpu_vdiff_impl(self.h, float(forcing.dt if dt is None else dt), C.byref(cfg), _p(Kv),
+                                              _p(bcs), _p(values)))
+
+    # -- whole step ------------------------------------------------------------
+    def tracer_step(self, forcing, cfgs: Sequence[TraCfg], values: Sequence[np.ndarray],
+                    valuesold: Sequence[np.ndarray], dt=None, bc=None):
+        n = len(cfgs)
+        arr = (TraCfg * n)(*cfgs)
+        vp = (_P * n)(*[C.c_void_p(v.ctypes.data) for v in values])
+        op = (_P * n)(*[C.c_void_p(v.ctypes.data) for v in valuesold])
+        for v in list(values) + list(valuesold):
+            assert v.dtype == np.float64 and v.flags.c_contiguous
+        uv, w, wi, we, Kv = (_c64(forcing.uv), _c64(forcing.w), _c64(forcing.w_i), _c64(forcing.w_e),
+                             _c64(forcing.Kv))
+        bcs = None if bc is None else _c64(bc)
+        self._chk(self.L.fesom_gpu_tracer_step(self.h, n, arr, float(forcing.dt if dt is None else dt), _p(uv),
+                                               _p(w), _p(wi), _p(we), _p(Kv), _p(bcs), vp, op))
+
+    # -- device-resident stepping --------------------------------------------------
+    def state_setup(self, cfgs: Sequence[TraCfg]):
+        n = len(cfgs)
+        self._cfgs = (TraCfg * n)(*cfgs)
+        self._chk(self.L.fesom_gpu_state_setup(self.h, n, self._cfgs))
+        self.ntr = n
+
+    def forcing_upload(self, forcing, bc=None):
+        if self.prec == PREC_FP32 and forcing.uv.dtype == np.float32:
+            f = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float32)
+            self._fk = [f(forcing.uv), f(forcing.w), f(forcing.w_i), f(forcing.w_e), f(forcing.Kv), f(bc)]
+            self._chk(self.L.fesom_gpu_forcing_upload_f32(self.h, *[_p(a) for a in self._fk]))
+        else:
+            self._fk = [_c64(forcing.uv), _c64(forcing.w), _c64(forcing.w_i), _c64(forcing.w_e), _c64(forcing.Kv),
+                        _c64(bc)]
+            self._chk(self.L.fesom_gpu_forcing_upload(self.h, *[_p(a) for a in self._fk]))
+
+    def tracer_upload(self, tr: int, values, valuesold):
+        if values.dtype == np.float32:
+            self._chk(self.L.fesom_gpu_tracer_upload_f32(self.h, tr, _p(values), _p(valuesold)))
+        else:
+            self._chk(self.L.fesom_gpu_tracer_upload(self.h, tr, _p(_c64(values)), _p(_c64(valuesold))))
+
+    def tracer_download(self, tr: int, dtype=np.float64):
+        N2, L1 = self.mesh.nod2D, self.mesh.nl - 1
+        v = np.zeros((N2, L1), dtype=dtype)
+        o = np.zeros((N2, L1), dtype=dtype)
+        if dtype == np.float32:
+            self._chk(self.L.fesom_gpu_tracer_download_f32(self.h, tr, _p(v), _p(o)))
+            self.status()
+        else:
+            self._chk(self.L.fesom_gpu_tracer_download(self.h, tr, _p(v), _p(o)))
+        return v, o
+
+    def run_steps(self, dt: float, nsteps: int, use_graph: bool = True):
+        self._chk(self.L.fesom_gpu_run_steps(self.h, float(dt), int(nsteps), 1 if use_graph else 0))
+
+    def set_tracers_per_launch(self, n: int):
+        self._chk(self.L.fesom_gpu_set_tracers_per_launch(self.h, int(n)))
+
+    def launches_per_step(self) -> int:
+        n = C.c_int32(0)
+        self._chk(self.L.fesom_gpu_launches_per_step(self.h, C.byref(n)))
+        return int(n.value)
+
+    def profile_step(self, dt: float):
+        """One non-graph step with events around each stage: {stage: (ms, launches)}."""
+        ms = np.zeros(STAGES_N, np.float32)
+        nl = np.zeros(STAGES_N, np.int32)
+        self._chk(self.L.fesom_gpu_profile_step(self.h, float(dt), _p(ms), _p(nl)))
+        return {STAGES[i]: (float(ms[i]), int(nl[i])) for i in range(STAGES_N)}
+
+    def debug_fetch(self, name: str, tr: int = 0) -> np.ndarray:
+        """Internal work array of a tracer slot (FP64 contexts; testing aid)."""
+        m = self.mesh
+        L1, nl = m.nl - 1, m.nl
+        shapes = {"T": (m.nod2D, L1), "Told": (m.nod2D, L1, -1), "TAB": (m.nod2D, L1), "trxy": (m.elem2D, L1, 2),
+                  "FLO": (m.edge2D, L1), "ADh": (m.edge2D, L1), "LO": (m.nod2D, L1), "ADv": (m.nod2D, nl),
+                  "bmax": (m.nod2D, L1), "bmin": (m.nod2D, L1), "dttf_h": (m.nod2D, L1), "dttf_v": (m.nod2D, L1)}
+        n = int(np.prod([abs(x) for x in shapes[name]])) * (3 if name == "Told" else 1)
+        out = np.zeros(n)
+        self._chk(self.L.fesom_gpu_debug_fetch(self.h, name.encode(), int(tr), _p(out), n))
+        if name == "Told":
+            return out
+        return out.reshape(shapes[name])
+
+    def content(self) -> np.ndarray:
+        out = np.zeros(self.ntr)
+        self._chk(self.L.fesom_gpu_tracer_content(self.h, _p(out)))
+        return out

@@ -34,6 +34,7 @@ from __future__ import annotations
 
 import dataclasses
 import math
+import os
 from typing import Optional
 
 import numpy as np
@@ -318,18 +319,26 @@ def _levels_from_depth(tri: np.ndarray, depth_nod: np.ndarray, zbar: np.ndarray,
     nbr = np.full((T2, 3), -1, dtype=np.int64)
     nbr[u, rank] = v
     for nz in range(thers_zbar_lev + 1, nl + 1):
+        # only elements open at nz with a closed (or missing) neighbour can fail the test
+        nb_lev = np.where(nbr >= 0, nlev[np.maximum(nbr, 0)], -1)
+        cand = np.flatnonzero((nlev >= nz) & (nb_lev < nz).any(axis=1))
         for _ in range(1000):
-            openn = np.where(nbr >= 0, nlev[np.maximum(nbr, 0)] >= nz, False).sum(axis=1)
-            bad = (nlev >= nz) & (openn < 2)
-            if not bad.any():
+            if cand.size == 0:
+                break
+            nbc = nbr[cand]
+            openn = np.where(nbc >= 0, nlev[np.maximum(nbc, 0)] >= nz, False).sum(axis=1)
+            bad = cand[(nlev[cand] >= nz) & (openn < 2)]
+            if bad.size == 0:
                 break
             if nz - 1 < thers_zbar_lev:
-                for k in range(3):
-                    idx = nbr[bad, k]
-                    idx = idx[idx >= 0]
-                    nlev[idx] = np.maximum(nlev[idx], nz)
+                idx = nbr[bad].reshape(-1)
+                idx = idx[idx >= 0]
+                nlev[idx] = np.maximum(nlev[idx], nz)
+                cand = np.unique(np.concatenate([idx, bad]))
             else:
                 nlev[bad] = nz - 1
+                nb = nbr[bad].reshape(-1)
+                cand = np.unique(nb[nb >= 0])
     return nlev.astype(np.int32)
 
 
@@ -439,14 +448,13 @@ def _finish_mesh(coord: np.ndarray, tri: np.ndarray, cyc: float, cartesian: bool
     helem[np.arange(T2), nle - 2] = bottom_elem_thickness
 
     # area / areasvol (oce_mesh.F90:2277-2340)
-    # area(nz, n) = sum over wet elements (ascending element order) of elem_area/3
-    area = np.zeros((N2, nl))
+    # area(nz, n) = sum over the node's elements wet at layer nz of elem_area/3: every
+    # element contributes to layers 1..nlevels-1, so accumulate at the layer where it
+    # stops and take a reverse cumulative sum over levels
     a3 = (elem_area_rad / 3.0)[nie]
-    nlev_p = nle[nie]
-    for nz in range(nl - 1):
-        wsel = nz < (nlev_p - 1)
-        area[:, nz] = np.bincount(nie_node, weights=np.where(wsel, a3, 0.0), minlength=N2)
-    area = area * R_EARTH * R_EARTH
+    stop = nle[nie] - 2                     # last wet layer (0-based)
+    D = np.bincount(nie_node.astype(np.int64) * nl + stop, weights=a3, minlength=N2 * nl).reshape(N2, nl)
+    area = np.flip(np.cumsum(np.flip(D, axis=1), axis=1), axis=1) * (R_EARTH * R_EARTH)
     wet_n = np.arange(nl)[None, :] < (nln - 1)[:, None]
     areasvol = np.where(wet_n, area, 0.0)
 
@@ -645,12 +653,19 @@ def vert_vel(mesh: Mesh, uv: np.ndarray) -> np.ndarray:
     wet2 = (lev >= (mesh.ulevels[e2] - 1)[:, None]) & (lev < (mesh.nlevels[e2] - 1)[:, None]) & has2[:, None]
     c2 = -(uv[e2, :, 1] * ecd[:, 2:3] - uv[e2, :, 0] * ecd[:, 3:4]) * mesh.helem[e2]
     c2 = np.where(wet2, c2, 0.0)
-    # scatter in the reference order: per edge +c1 -> n1, -c1 -> n2, +c2 -> n1, -c2 -> n2
-    idx = np.stack([e[:, 0], e[:, 1], e[:, 0], e[:, 1]], axis=1).reshape(-1)
+    # edge scatter (+ to edges(1,e), - to edges(2,e)) as a segmented sum over
+    # edges sorted by node
+    c = c1 + c2
+    del c1, c2
+    nodes = np.concatenate([e[:, 0], e[:, 1]])
+    sign = np.concatenate([np.ones(e.shape[0]), -np.ones(e.shape[0])])
+    order = np.argsort(nodes, kind="stable")
+    rows = np.where(order < e.shape[0], order, order - e.shape[0])
+    vals = c[rows] * sign[order][:, None]
+    starts = np.flatnonzero(np.r_[True, nodes[order][1:] != nodes[order][:-1]])
     acc = np.zeros((N2, nl - 1))
-    for nz in range(nl - 1):
-        wts = np.stack([c1[:, nz], -c1[:, nz], c2[:, nz], -c2[:, nz]], axis=1).reshape(-1)
-        acc[:, nz] = np.bincount(idx, weights=wts, minlength=N2)
+    acc[nodes[order][starts]] = np.add.reduceat(vals, starts, axis=0)
+    del vals
     W[:, :nl - 1] = acc
     # bottom-up cumulative sum over wet levels
     nln = mesh.nlevels_nod2D.astype(np.int64)
@@ -658,6 +673,38 @@ def vert_vel(mesh: Mesh, uv: np.ndarray) -> np.ndarray:
     W = np.where(wetn, W, 0.0)
     W = np.flip(np.cumsum(np.flip(W, axis=1), axis=1), axis=1)
     W = np.where(wetn, W, 0.0)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        W = np.where(wetn, W / np.where(mesh.area > 0, mesh.area, 1.0), 0.0)
+    return W
+
+
+def vert_vel_separable(mesh: Mesh, base: np.ndarray, prof: np.ndarray) -> np.ndarray:
+    """vert_vel for uv(:, nz, el) = base(:, el) * prof(nz) on wet layers: the
+    edge-segment fluxes factor into per-(node, element) coefficients times
+    prof*helem, so the node divergence is one sparse product."""
+    import scipy.sparse as sp
+    nl, N2, T2 = mesh.nl, mesh.nod2D, mesh.elem2D
+    e = mesh.edges.astype(np.int64)
+    el1 = mesh.edge_tri[:, 0].astype(np.int64)
+    el2 = mesh.edge_tri[:, 1].astype(np.int64)
+    ecd = mesh.edge_cross_dxdy
+    s1 = base[el1, 1] * ecd[:, 0] - base[el1, 0] * ecd[:, 1]
+    has2 = el2 >= 0
+    e2 = np.maximum(el2, 0)
+    s2 = np.where(has2, -(base[e2, 1] * ecd[:, 2] - base[e2, 0] * ecd[:, 3]), 0.0)
+    rows = np.concatenate([e[:, 0], e[:, 1], e[:, 0], e[:, 1]])
+    cols = np.concatenate([el1, el1, e2, e2])
+    vals = np.concatenate([s1, -s1, s2, -s2])
+    A = sp.csr_matrix((vals, (rows, cols)), shape=(N2, T2))
+    q = mesh.helem * prof[None, :]          # helem is 0 below each element's bottom
+    acc = np.asarray(A @ q)
+    W = np.zeros((N2, nl))
+    W[:, :nl - 1] = acc
+    nln = mesh.nlevels_nod2D.astype(np.int64)
+    wetn = np.arange(nl)[None, :] < (nln - 1)[:, None]
+    W *= wetn
+    W = np.flip(np.cumsum(np.flip(W, axis=1), axis=1), axis=1)
+    W *= wetn
     with np.errstate(divide="ignore", invalid="ignore"):
         W = np.where(wetn, W / np.where(mesh.area > 0, mesh.area, 1.0), 0.0)
     return W
@@ -702,12 +749,12 @@ def make_forcing(mesh: Mesh, kind: str, seed: int = 11, dt: float = 600.0,
         s = np.sqrt(np.mean(np.sum(base ** 2, axis=1)))
         base *= rms / max(s, 1e-300)
         prof = 0.4 + 0.6 * np.exp(Zm / 800.0)
-    uv = base[:, None, :] * prof[None, :, None]
     lev = np.arange(nl - 1)[None, :]
     wet = (lev >= (mesh.ulevels - 1)[:, None]) & (lev < (mesh.nlevels - 1)[:, None])
-    uv = np.where(wet[:, :, None], uv, 0.0)
-    uv = np.ascontiguousarray(uv)
-    W = vert_vel(mesh, uv)
+    uv = np.empty((mesh.elem2D, nl - 1, 2))
+    np.multiply(base[:, None, :], prof[None, :, None], out=uv)
+    uv *= wet[:, :, None]
+    W = vert_vel_separable(mesh, base, prof)
     if surface_w_zero:
         W[np.arange(mesh.nod2D), mesh.ulevels_nod2D - 1] = 0.0
     if kv_profile == "const":
@@ -729,29 +776,41 @@ def make_tracers(mesh: Mesh, kind: str, ntr: int = 2, seed: int = 5, Lj: float =
     """Initial tracer values, shape (ntr, N2, nl-1); dry levels are 0.
 
     Tracer 0 is temperature, 1 salinity, the rest lognormal(0, 1) passive
-    tracers (strictly positive)."""
-    rng = np.random.default_rng(seed)
+    tracers (strictly positive).  Each tracer draws from its own seeded stream
+    (seed, k), so the values do not depend on the thread that makes them."""
+    import concurrent.futures as cf
     N2, nl = mesh.nod2D, mesh.nl
     d = node_depth_mid(mesh)
     out = np.zeros((ntr, N2, nl - 1), dtype=dtype)
     lev = np.arange(nl - 1)[None, :]
     wet = (lev >= (mesh.ulevels_nod2D - 1)[:, None]) & (lev < (mesh.nlevels_nod2D - 1)[:, None])
-    if kind == "channel":
-        y = mesh.coord_nod2D[:, 1] * R_EARTH
-        yp = y - 0.5 * (y.min() + y.max())
-        sig = 0.01 if noise is None else noise
-        T = 20.0 - 0.005 * d + 2.0 * np.tanh(yp / Lj)[:, None] + rng.normal(0, sig, d.shape)
-        S = 35.0 + rng.normal(0, sig, d.shape)
-    else:
-        lat = mesh.coord_nod2D[:, 1]
-        sig = 0.1 if noise is None else noise
-        T = 2.0 + 26.0 * (np.cos(lat) ** 2)[:, None] * np.exp(-d / 1000.0) + rng.normal(0, sig, d.shape)
-        S = 34.0 + 1.5 * np.cos(2 * lat)[:, None] + rng.normal(0, sig, d.shape)
-    fields = [T, S]
-    for k in range(2, ntr):
-        fields.append(np.exp(rng.normal(0.0, 1.0, d.shape)))
-    for k in range(ntr):
-        out[k] = np.where(wet, fields[k], 0.0)
+
+    def one(k):
+        rng = np.random.default_rng([seed, k])
+        if k == 0:
+            if kind == "channel":
+                y = mesh.coord_nod2D[:, 1] * R_EARTH
+                yp = y - 0.5 * (y.min() + y.max())
+                sig = 0.01 if noise is None else noise
+                v = 20.0 - 0.005 * d + 2.0 * np.tanh(yp / Lj)[:, None] + rng.normal(0, sig, d.shape)
+            else:
+                lat = mesh.coord_nod2D[:, 1]
+                sig = 0.1 if noise is None else noise
+                v = 2.0 + 26.0 * (np.cos(lat) ** 2)[:, None] * np.exp(-d / 1000.0) + rng.normal(0, sig, d.shape)
+        elif k == 1:
+            sig = (0.01 if kind == "channel" else 0.1) if noise is None else noise
+            if kind == "channel":
+                v = 35.0 + rng.normal(0, sig, d.shape)
+            else:
+                lat = mesh.coord_nod2D[:, 1]
+                v = 34.0 + 1.5 * np.cos(2 * lat)[:, None] + rng.normal(0, sig, d.shape)
+        else:
+            z = rng.standard_normal(d.shape, dtype=np.float32)
+            v = np.exp(z, out=z)
+        np.copyto(out[k], np.where(wet, v, 0.0).astype(dtype, copy=False))
+
+    with cf.ThreadPoolExecutor(max_workers=min(ntr, os.cpu_count() or 4)) as ex:
+        list(ex.map(one, range(ntr)))
     return out
 
 

@@ -1,0 +1,223 @@
+/*
+ * fesom_gpu.h -- C ABI of the GB300 (sm_103a) FESOM2 tracer-transport step.
+ *
+ * The library replaces, call for call, the tracer-transport routines of
+ * FESOM2 (reference paths are relative to the FESOM2 source tree):
+ *
+ *   fesom_gpu_init_tracers_ab   init_tracers_AB          src/oce_tracer_mod.F90:13-143
+ *   fesom_gpu_adv_tra           do_oce_adv_tra           src/oce_adv_tra_driver.F90:46-490
+ *   fesom_gpu_vdiff_impl        diff_ver_part_impl_ale   src/oce_ale_tracer.F90:907-1435
+ *   fesom_gpu_tracer_step       body of the tracer loop  src/oce_ale_tracer.F90:280-351
+ *                               (init_tracers_AB, do_oce_adv_tra, del_ttf sum,
+ *                               diff_tracers_ale's T* update and implicit
+ *                               vertical diffusion) for all tracers at once
+ *   fesom_gpu_init              setup of the mesh-derived work arrays:
+ *                               oce_adv_tra_fct_init  src/oce_adv_tra_fct.F90:35-67,
+ *                               muscl_adv_init        src/oce_muscl_adv.F90:32-352,
+ *                               find_levels_min_e2n   src/oce_mesh.F90:1656-1694
+ *
+ * All arrays are passed by address in the reference's Fortran layout
+ * a(level, entity) (column-major, level-contiguous), exactly as the derived
+ * types t_mesh / t_tracer / t_dyn hold them, so a Fortran caller passes
+ * c_loc() of its arrays with no copy.  Host pointers are copied to the device
+ * inside the call; the *_dev variants take device pointers.
+ *
+ * Error convention: every entry point returns 0 on success and a FESOM_ERR_*
+ * code otherwise (the reference aborts through par_ex on the same conditions);
+ * fesom_gpu_last_error() gives a message.  No call blocks without a bound and
+ * no kernel traps.
+ */
+#ifndef FESOM_GPU_H
+#define FESOM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FESOM_GPU_ABI_VERSION 1
+
+/* status codes */
+#define FESOM_OK 0
+#define FESOM_ERR_ARG 1          /* bad argument / null pointer / size mismatch */
+#define FESOM_ERR_SCHEME 2       /* unknown or unsupported advection scheme (PPM, CDIFF, w-split) */
+#define FESOM_ERR_MESH 3         /* mesh fails validation (index out of range, < 2 layers, ...) */
+#define FESOM_ERR_CUDA 4         /* a CUDA runtime call failed */
+#define FESOM_ERR_NOMEM 5        /* device allocation failed */
+#define FESOM_ERR_TIMEOUT 6      /* a bounded wait on the device expired */
+#define FESOM_ERR_NUMERIC 7      /* device status word reports NaN/Inf in a result */
+#define FESOM_ERR_STATE 8        /* call order violated (e.g. step before forcing upload) */
+
+/* precision of the device-side step */
+#define FESOM_PREC_FP64 0        /* plain form: the reference's FP64 arithmetic, bit-for-bit order */
+#define FESOM_PREC_FP32 1        /* batched form: FP32 storage/arithmetic, FP64 Thomas solve and sums */
+
+/* tra_adv_hor / tra_adv_ver / tra_adv_lim strings of namelist.tra */
+#define FESOM_ADV_HOR_MUSCL 0
+#define FESOM_ADV_HOR_MFCT 1
+#define FESOM_ADV_HOR_UPW1 2
+#define FESOM_ADV_VER_QR4C 0
+#define FESOM_ADV_VER_UPW1 1
+#define FESOM_ADV_VER_CDIFF 2    /* rejected with FESOM_ERR_SCHEME */
+#define FESOM_ADV_VER_PPM 3      /* rejected with FESOM_ERR_SCHEME */
+#define FESOM_ADV_LIM_NONE 0
+#define FESOM_ADV_LIM_FCT 1
+
+/* device status word bits (fesom_gpu_status) */
+#define FESOM_STATUS_NAN 0x1u        /* a non-finite tracer value was produced */
+#define FESOM_STATUS_FCT_BOUND 0x2u  /* (FP32 form) an advected value left its FCT bounds */
+#define FESOM_STATUS_INDEX 0x4u      /* a kernel met an index outside its array and skipped it */
+
+/* Per-tracer scheme tuple of T_TRACER_DATA (src/MOD_TRACER.F90:10-27). */
+typedef struct fesom_tra_cfg {
+    int32_t adv_hor;      /* FESOM_ADV_HOR_* */
+    int32_t adv_ver;      /* FESOM_ADV_VER_* */
+    int32_t adv_lim;      /* FESOM_ADV_LIM_* */
+    int32_t ab_order;     /* 2 or 3 */
+    double adv_ph;        /* tra_adv_ph: fourth-order fraction of the horizontal scheme */
+    double adv_pv;        /* tra_adv_pv: fourth-order fraction of QR4C */
+    int32_t i_vert_diff;  /* 1: implicit vertical diffusion */
+    int32_t id;           /* tracer ID (1 = temperature, 2 = salinity, ...), informational */
+} fesom_tra_cfg;
+
+/*
+ * Mesh description: the t_mesh members the path reads (src/MOD_MESH.F90:22-160),
+ * in Fortran layout.  Integer indices are index_base-based (1 for Fortran
+ * callers); edge_tri(2,e) <= index_base-1 marks a boundary edge (the reference
+ * stores -999).  nod_in_elem2D is the reference's 2-D array (ld_nie, nod2D)
+ * with nod_in_elem2D_num(nod2D) valid entries per node.  nboundary_lay and
+ * edge_up_dn_tri (t_tracer_work, filled by muscl_adv_init) are optional: when
+ * NULL the library computes them as muscl_adv_init does.
+ *
+ * Thicknesses (hnode, hnode_new, helem, Z_3d_n, zbar_3d_n) change with ALE;
+ * fesom_gpu_update_thickness() refreshes them between steps.
+ */
+typedef struct fesom_mesh_desc {
+    int32_t nod2D, elem2D, edge2D, nl;
+    int32_t index_base;
+    int32_t ld_nie;
+    const int32_t *elem2D_nodes;       /* (3, elem2D) */
+    const int32_t *edges;              /* (2, edge2D) */
+    const int32_t *edge_tri;           /* (2, edge2D) */
+    const int32_t *nod_in_elem2D_num;  /* (nod2D) */
+    const int32_t *nod_in_elem2D;      /* (ld_nie, nod2D) */
+    const int32_t *nlevels, *ulevels;                  /* (elem2D) */
+    const int32_t *nlevels_nod2D, *ulevels_nod2D;      /* (nod2D) */
+    const int32_t *nlevels_nod2D_min, *ulevels_nod2D_max; /* (nod2D) */
+    const double *coord_nod2D;         /* (2, nod2D), rotated lon/lat in radians */
+    const double *elem_area, *elem_cos;                /* (elem2D) */
+    const double *edge_dxdy;           /* (2, edge2D) */
+    const double *edge_cross_dxdy;     /* (4, edge2D) */
+    const double *gradient_sca;        /* (6, elem2D) */
+    const double *area, *areasvol;     /* (nl, nod2D) */
+    const double *hnode, *hnode_new;   /* (nl-1, nod2D) */
+    const double *helem;               /* (nl-1, elem2D) */
+    const double *Z_3d_n;              /* (nl-1, nod2D) */
+    const double *zbar_3d_n;           /* (nl, nod2D) */
+    const double *zbar_n_bot;          /* (nod2D) */
+    double cyclic_length;
+    const int32_t *nboundary_lay;      /* optional (nod2D) */
+    const int32_t *edge_up_dn_tri;     /* optional (2, edge2D), <= index_base-1 = none */
+} fesom_mesh_desc;
+
+typedef struct fesom_gpu_ctx fesom_gpu_ctx;
+
+/* ---- lifetime ------------------------------------------------------------ */
+/* Validates the mesh, builds the node->edge and node->element gather lists
+ * (ascending edge / element order, so every node sum adds its terms in the
+ * reference's serial scatter order) and copies topology and geometry to the
+ * current CUDA device.  max_tracers bounds the batched entry points. */
+int fesom_gpu_init(const fesom_mesh_desc *mesh, int32_t precision, int32_t max_tracers, fesom_gpu_ctx **ctx);
+int fesom_gpu_finalize(fesom_gpu_ctx *ctx);
+/* Host-only: validates the mesh and returns the derived muscl_adv_init arrays
+ * (index_base-based, either output may be NULL) without touching the GPU; on
+ * failure the message is written to errbuf (errlen bytes, NUL-terminated). */
+int fesom_gpu_mesh_check(const fesom_mesh_desc *mesh, int32_t *nboundary_lay, int32_t *edge_up_dn_tri, char *errbuf,
+                         int32_t errlen);
+/* Launch everything on this stream (a cudaStream_t); NULL = the legacy default stream. */
+int fesom_gpu_set_stream(fesom_gpu_ctx *ctx, void *stream);
+const char *fesom_gpu_last_error(const fesom_gpu_ctx *ctx);
+int fesom_gpu_abi_version(void);
+/* Copies of the derived init arrays, index_base-based: nboundary_lay (nod2D),
+ * edge_up_dn_tri (2, edge2D).  Either pointer may be NULL. */
+int fesom_gpu_get_muscl_init(fesom_gpu_ctx *ctx, int32_t *nboundary_lay, int32_t *edge_up_dn_tri);
+/* Reads and clears the device status word (FESOM_STATUS_* bits); waits at
+ * most timeout_ms for the stream, returns FESOM_ERR_TIMEOUT beyond. */
+int fesom_gpu_status(fesom_gpu_ctx *ctx, uint32_t *status, int32_t timeout_ms);
+/* ALE: new hnode/hnode_new/helem/Z_3d_n/zbar_3d_n (any may be NULL = unchanged). */
+int fesom_gpu_update_thickness(fesom_gpu_ctx *ctx, const double *hnode, const double *hnode_new,
+                               const double *helem, const double *Z_3d_n, const double *zbar_3d_n);
+
+/* ---- per-routine drop-ins (FP64, host arrays, one tracer per call) ------- */
+/* init_tracers_AB: valuesAB from values/valuesold (AB2/AB3), valuesold shift,
+ * element gradients (tr_xy) and edge_up_dn_grad kept on the device.
+ * valuesold is (ab_order-1, nl-1, nod2D). */
+int fesom_gpu_init_tracers_ab(fesom_gpu_ctx *ctx, const fesom_tra_cfg *cfg, const double *values,
+                              double *valuesAB, double *valuesold);
+/* do_oce_adv_tra with use_wsplit = .false.: vel (2, nl-1, elem2D), w/wi/we
+ * (nl, nod2D), ttf = values, ttfAB = valuesAB (nl-1, nod2D).  Writes
+ * dttf_h / dttf_v (del_ttf_advhoriz / del_ttf_advvert, (nl-1, nod2D)); they
+ * are overwritten (the reference adds to arrays that init_tracers_AB zeroed). */
+int fesom_gpu_adv_tra(fesom_gpu_ctx *ctx, double dt, const double *vel, const double *w, const double *wi,
+                      const double *we, const fesom_tra_cfg *cfg, const double *ttf, const double *ttfAB,
+                      double *dttf_h, double *dttf_v);
+/* diff_ver_part_impl_ale (Redi, KPP non-local, shortwave and iceberg terms
+ * off): Kv (nl, nod2D), bc_surf (nod2D) = the bc_surface() term added at
+ * nzmin; values (nl-1, nod2D) updated in place. */
+int fesom_gpu_vdiff_impl(fesom_gpu_ctx *ctx, double dt, const fesom_tra_cfg *cfg, const double *Kv,
+                         const double *bc_surf, double *values);
+
+/* ---- the whole tracer step for all tracers (host arrays) ----------------- */
+/* values[t] (nl-1, nod2D), valuesold[t] (ab_order-1, nl-1, nod2D) updated in
+ * place; bc_surf is (nod2D, ntr) or NULL (zero).  In FESOM_PREC_FP32 the data
+ * are rounded to FP32 on the device and the results widened back. */
+int fesom_gpu_tracer_step(fesom_gpu_ctx *ctx, int32_t ntr, const fesom_tra_cfg *cfgs, double dt,
+                          const double *uv, const double *w, const double *wi, const double *we,
+                          const double *Kv, const double *bc_surf, double *const *values,
+                          double *const *valuesold);
+
+/* ---- device-resident stepping (the form a time loop uses) ---------------- */
+/* Tracer state lives on the device in the context's precision.  Forcing
+ * (uv, w, wi, we, Kv, bc_surf) is uploaded once per model step; steps then run
+ * from a captured CUDA graph with no host traffic.  FP64 host arrays are
+ * converted on the device in FESOM_PREC_FP32. */
+int fesom_gpu_state_setup(fesom_gpu_ctx *ctx, int32_t ntr, const fesom_tra_cfg *cfgs);
+int fesom_gpu_forcing_upload(fesom_gpu_ctx *ctx, const double *uv, const double *w, const double *wi,
+                             const double *we, const double *Kv, const double *bc_surf);
+int fesom_gpu_tracer_upload(fesom_gpu_ctx *ctx, int32_t tr, const double *values, const double *valuesold);
+int fesom_gpu_tracer_download(fesom_gpu_ctx *ctx, int32_t tr, double *values, double *valuesold);
+/* FP32 host buffers (FESOM_PREC_FP32 only): no widening on the way. */
+int fesom_gpu_tracer_upload_f32(fesom_gpu_ctx *ctx, int32_t tr, const float *values, const float *valuesold);
+int fesom_gpu_tracer_download_f32(fesom_gpu_ctx *ctx, int32_t tr, float *values, float *valuesold);
+int fesom_gpu_forcing_upload_f32(fesom_gpu_ctx *ctx, const float *uv, const float *w, const float *wi,
+                                 const float *we, const float *Kv, const float *bc_surf);
+/* Runs nsteps tracer steps of dt on the device (graph replay when use_graph). */
+int fesom_gpu_run_steps(fesom_gpu_ctx *ctx, double dt, int32_t nsteps, int32_t use_graph);
+/* Tracers per launch of each stage (0 = as many as the work arrays hold; the
+ * FP64 plain form uses 1, one tracer per launch as the reference loops). */
+int fesom_gpu_set_tracers_per_launch(fesom_gpu_ctx *ctx, int32_t n);
+/* One step without the graph, with CUDA events around every stage on the
+ * context stream; stage_ms[i] receives the summed time of stage i over all
+ * tracer groups and launches[i] the number of launches (arrays of
+ * FESOM_NUM_STAGES entries, stage order: ab, trxy, edge_flux, node_lo,
+ * bounds, rpm, update, vdiff). */
+#define FESOM_NUM_STAGES 8
+int fesom_gpu_profile_step(fesom_gpu_ctx *ctx, double dt, float *stage_ms, int32_t *launches);
+/* Copy of an internal per-tracer work array of tracer slot tr (FP64 contexts,
+ * for testing): name is one of "T", "Told", "TAB", "trxy", "FLO", "ADh", "LO",
+ * "ADv", "bmax", "bmin" (bmax/bmin hold R+/R- after a step), "dttf_h",
+ * "dttf_v"; count is the number of doubles out can hold. */
+int fesom_gpu_debug_fetch(fesom_gpu_ctx *ctx, const char *name, int32_t tr, double *out, size_t count);
+/* Kernel launches one device-resident step issues. */
+int fesom_gpu_launches_per_step(fesom_gpu_ctx *ctx, int32_t *launches);
+/* Global content sum_nodes sum_levels values*hnode_new*areasvol per tracer, in FP64. */
+int fesom_gpu_tracer_content(fesom_gpu_ctx *ctx, double *content);
+/* Device pointer of tracer tr's values (context precision), for zero-copy users. */
+int fesom_gpu_tracer_device_ptr(fesom_gpu_ctx *ctx, int32_t tr, void **values, void **valuesold);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FESOM_GPU_H */

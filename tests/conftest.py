@@ -1,0 +1,67 @@
+"""Shared fixtures: small seeded meshes and forcings; the `gpu` marker."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from fesom2_gb300 import mesh as M  # noqa: E402
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+def _cuda_available() -> bool:
+    """True when the CUDA driver reports a device (checked through libcuda, no torch import)."""
+    import ctypes
+    try:
+        cu = ctypes.CDLL("libcuda.so.1")
+        if cu.cuInit(0) != 0:
+            return False
+        n = ctypes.c_int(0)
+        return cu.cuDeviceGetCount(ctypes.byref(n)) == 0 and n.value > 0
+    except OSError:
+        return False
+
+
+def pytest_collection_modifyitems(config, items):
+    if _cuda_available():
+        return
+    skip = pytest.mark.skip(reason="no CUDA device")
+    for it in items:
+        if "gpu" in it.keywords:
+            it.add_marker(skip)
+
+
+@pytest.fixture(scope="session")
+def channel_small():
+    """12 x 16 channel, 40 x 100 m levels, flat (configuration 1 layout, shrunk)."""
+    return M.channel_mesh(12, 16, 5000.0, -np.arange(41) * 100.0)
+
+
+@pytest.fixture(scope="session")
+def channel_seamount():
+    """16 x 24 channel, 60 stretched levels, seamounts and partial cells (configuration 2 layout, shrunk)."""
+    return M.channel_mesh(16, 24, 5000.0, M.stretched_zbar(60, 10.0, 200.0), seamounts=3, seed=4,
+                          partial_cells=True)
+
+
+@pytest.fixture(scope="session")
+def sphere_small():
+    """Icosahedral sphere, 4 subdivisions, 30% land, 48 levels, partial cells (configuration 3 layout, shrunk)."""
+    return M.sphere_mesh(4, M.stretched_zbar(48, 5.0, 250.0), seed=9)
+
+
+def wet_mask(mesh):
+    lev = np.arange(mesh.nl - 1)[None, :]
+    return (lev >= (mesh.ulevels_nod2D - 1)[:, None]) & (lev < (mesh.nlevels_nod2D - 1)[:, None])
+
+
+def perturbed_old(T, rng, scale=1e-3):
+    """valuesold for the first AB step: T plus a small seeded perturbation."""
+    return np.ascontiguousarray(T * (1.0 + scale * rng.standard_normal(T.shape)))

@@ -1,0 +1,214 @@
+"""Parity of the CUDA path (through the C ABI) with the FP64 CPU oracle.
+
+FP64 plain form: bit-for-bit equality with the oracle (the kernels add every
+sum in the reference's serial scatter order and are built without FMA
+contraction).  FP32 form: max relative error per step <= 1e-5 against the
+FP64 oracle started from the same state, content conserved, FCT bounds kept.
+"""
+import numpy as np
+import pytest
+
+from fesom2_gb300 import gpu as G
+from fesom2_gb300 import mesh as M
+from oracle import oracle as O
+from tests.conftest import perturbed_old, wet_mask
+
+pytestmark = pytest.mark.gpu
+
+SCHEMES = [("MUSCL", "QR4C", "FCT"), ("MFCT", "QR4C", "FCT"), ("UPW1", "UPW1", "FCT"),
+           ("MUSCL", "QR4C", "NON"), ("UPW1", "QR4C", "NON"), ("MFCT", "UPW1", "FCT")]
+
+
+def _setup(mesh, kind, seed=3, ntr=2, surface_w_zero=False):
+    f = O.ensure_f64(M.make_forcing(mesh, kind, seed=seed, dt=600.0, surface_w_zero=surface_w_zero))
+    tr = M.make_tracers(mesh, kind, ntr=ntr, seed=seed + 1)
+    return f, tr
+
+
+@pytest.mark.parametrize("meshname", ["channel_small", "channel_seamount", "sphere_small"])
+def test_muscl_init_matches_oracle(meshname, request):
+    mesh = request.getfixturevalue(meshname)
+    ctx = G.Context(mesh, G.PREC_FP64)
+    om = O.OracleMesh(mesh)
+    nbl, updn = ctx.muscl_init()
+    assert np.array_equal(nbl, om.work["nboundary_lay"])
+    assert np.array_equal(updn, om.work["edge_up_dn_tri"])
+
+
+@pytest.mark.parametrize("meshname,kind", [("channel_small", "channel"), ("sphere_small", "sphere")])
+@pytest.mark.parametrize("ab", [2, 3])
+def test_init_tracers_ab_bitwise(meshname, kind, ab, request):
+    mesh = request.getfixturevalue(meshname)
+    f, tr = _setup(mesh, kind)
+    rng = np.random.default_rng(7)
+    T = np.ascontiguousarray(tr[0])
+    old = np.ascontiguousarray(np.stack([perturbed_old(T, rng) for _ in range(ab - 1)], axis=-1))
+    ocfg = O.cfg_struct(ab_order=ab)
+    gcfg = G.tra_cfg(ab_order=ab)
+    om = O.OracleMesh(mesh)
+    o_old, o_ab = old.copy(), np.zeros_like(T)
+    om.init_tracers_AB(ocfg, T.copy(), o_ab, o_old)
+    ctx = G.Context(mesh, G.PREC_FP64)
+    g_old, g_ab = old.copy(), np.zeros_like(T)
+    ctx.init_tracers_ab(gcfg, T.copy(), g_ab, g_old)
+    assert np.array_equal(g_ab, o_ab)
+    assert np.array_equal(g_old, o_old)
+
+
+@pytest.mark.parametrize("scheme", SCHEMES, ids=["-".join(s) for s in SCHEMES])
+@pytest.mark.parametrize("meshname,kind", [("channel_seamount", "channel"), ("sphere_small", "sphere")])
+def test_adv_tra_bitwise(scheme, meshname, kind, request):
+    """do_oce_adv_tra: del_ttf_advhoriz / del_ttf_advvert equal the oracle's bit for bit."""
+    mesh = request.getfixturevalue(meshname)
+    hor, ver, lim = scheme
+    f, tr = _setup(mesh, kind)
+    rng = np.random.default_rng(11)
+    T = np.ascontiguousarray(tr[0])
+    TAB = np.ascontiguousarray(T * (1.0 + 1e-3 * rng.standard_normal(T.shape)))
+    om = O.OracleMesh(mesh)
+    ocfg = O.cfg_struct(hor, ver, lim, ph=0.0, pv=1.0)
+    om.init_tracers_AB(ocfg, T.copy(), np.zeros_like(T), T.copy())  # zero del_ttf*, gradients of T
+    om.do_oce_adv_tra(f, ocfg, T, TAB)
+    ctx = G.Context(mesh, G.PREC_FP64)
+    dh, dv = ctx.adv_tra(f, G.tra_cfg(hor, ver, lim, ph=0.0, pv=1.0), T, TAB)
+    wet = wet_mask(mesh)
+    assert np.array_equal(dh[wet], om.work["del_ttf_advhoriz"][wet])
+    assert np.array_equal(dv[wet], om.work["del_ttf_advvert"][wet])
+
+
+@pytest.mark.parametrize("meshname,kind", [("channel_seamount", "channel"), ("sphere_small", "sphere")])
+def test_vdiff_bitwise(meshname, kind, request):
+    mesh = request.getfixturevalue(meshname)
+    f, tr = _setup(mesh, kind)
+    f.bc_surface = np.linspace(-1e-3, 1e-3, mesh.nod2D)
+    T = np.ascontiguousarray(tr[1])
+    om = O.OracleMesh(mesh)
+    To = T.copy()
+    om.diff_ver_part_impl_ale(f, To)
+    ctx = G.Context(mesh, G.PREC_FP64)
+    Tg = T.copy()
+    ctx.vdiff_impl(f, G.tra_cfg(), Tg)
+    assert np.array_equal(Tg, To)
+
+
+@pytest.mark.parametrize("meshname,kind", [("channel_small", "channel"), ("channel_seamount", "channel"),
+                                           ("sphere_small", "sphere")])
+def test_tracer_step_bitwise_multi_step(meshname, kind, request):
+    """Whole per-tracer body (AB2, MUSCL+QR4C+FCT, T*, implicit diffusion), 3 steps, 2 tracers."""
+    mesh = request.getfixturevalue(meshname)
+    f, tr = _setup(mesh, kind)
+    om = O.OracleMesh(mesh)
+    ctx = G.Context(mesh, G.PREC_FP64, max_tracers=2)
+    ocfg = O.cfg_struct("MUSCL", "QR4C", "FCT", 0.0, 1.0)
+    gcfgs = [G.tra_cfg("MUSCL", "QR4C", "FCT", 0.0, 1.0, id=1), G.tra_cfg("MUSCL", "QR4C", "FCT", 0.0, 1.0, id=2)]
+    rng = np.random.default_rng(2)
+    To = [np.array(t, copy=True) for t in tr]
+    Oo = [perturbed_old(t, rng) for t in To]
+    Tg = [t.copy() for t in To]
+    Og = [o.copy() for o in Oo]
+    for step in range(3):
+        for k in range(2):
+            om.tracer_step(f, ocfg, To[k], np.zeros_like(To[k]), Oo[k])
+        ctx.tracer_step(f, gcfgs, Tg, Og)
+        for k in range(2):
+            assert np.array_equal(Tg[k], To[k]), f"step {step} tracer {k}"
+            assert np.array_equal(Og[k], Oo[k])
+
+
+def test_device_resident_graph_matches_host_calls(channel_seamount):
+    """run_steps (CUDA graph replay) equals the same steps through the host-array entry point."""
+    mesh = channel_seamount
+    f, tr = _setup(mesh, "channel")
+    cfgs = [G.tra_cfg(id=1), G.tra_cfg(id=2)]
+    a = G.Context(mesh, G.PREC_FP64, max_tracers=2)
+    Ta = [np.array(t, copy=True) for t in tr]
+    Oa = [t.copy() for t in Ta]
+    for _ in range(4):
+        a.tracer_step(f, cfgs, Ta, Oa)
+    b = G.Context(mesh, G.PREC_FP64, max_tracers=2)
+    b.state_setup(cfgs)
+    b.forcing_upload(f)
+    for k in range(2):
+        b.tracer_upload(k, np.array(tr[k], copy=True), np.array(tr[k], copy=True))
+    b.run_steps(f.dt, 4, use_graph=True)
+    for k in range(2):
+        v, o = b.tracer_download(k)
+        assert np.array_equal(v, Ta[k])
+        assert np.array_equal(o, Oa[k])
+
+
+@pytest.mark.parametrize("meshname,kind", [("channel_seamount", "channel"), ("sphere_small", "sphere")])
+def test_fp32_error_vs_fp64_oracle(meshname, kind, request):
+    """FP32 form, one step from the same state: max relative error <= 1e-5."""
+    mesh = request.getfixturevalue(meshname)
+    ntr = 4
+    f, tr = _setup(mesh, kind, ntr=ntr)
+    cfgs = [G.tra_cfg(id=k + 1) for k in range(ntr)]
+    ctx = G.Context(mesh, G.PREC_FP32, max_tracers=ntr)
+    ctx.state_setup(cfgs)
+    ctx.forcing_upload(f)
+    om = O.OracleMesh(mesh)
+    wet = wet_mask(mesh)
+    ocfg = O.cfg_struct()
+    for k in range(ntr):
+        T32 = tr[k].astype(np.float32)
+        ctx.tracer_upload(k, T32, T32)
+    ctx.run_steps(f.dt, 1, use_graph=False)
+    for k in range(ntr):
+        T64 = tr[k].astype(np.float32).astype(np.float64)
+        O64 = T64.copy()
+        om.tracer_step(f, ocfg, T64, np.zeros_like(T64), O64)
+        v, _ = ctx.tracer_download(k)
+        rel = np.abs(v[wet] - T64[wet]) / np.maximum(np.abs(T64[wet]), 1e-30)
+        assert rel.max() <= 1e-5, (k, rel.max())
+    assert ctx.status() == 0
+
+
+@pytest.mark.parametrize("prec,tol", [(G.PREC_FP64, 1e-12), (G.PREC_FP32, 1e-5)])
+def test_content_conservation(channel_seamount, prec, tol):
+    """Rigid lid (w = 0 at the surface), linfs: sum T*hnode_new*areasvol is conserved."""
+    mesh = channel_seamount
+    f, tr = _setup(mesh, "channel", surface_w_zero=True)
+    cfgs = [G.tra_cfg(id=1), G.tra_cfg(id=2)]
+    ctx = G.Context(mesh, prec, max_tracers=2)
+    ctx.state_setup(cfgs)
+    ctx.forcing_upload(f)
+    for k in range(2):
+        ctx.tracer_upload(k, np.ascontiguousarray(tr[k]), np.ascontiguousarray(tr[k]))
+    c0 = ctx.content()
+    ctx.run_steps(f.dt, 5)
+    c1 = ctx.content()
+    assert np.all(np.abs(c1 - c0) / np.abs(c0) <= tol), (c0, c1)
+
+
+def test_lognormal_positivity_fp32(sphere_small):
+    mesh = sphere_small
+    ntr = 6
+    f, tr = _setup(mesh, "sphere", ntr=ntr)
+    cfgs = [G.tra_cfg(id=100 + k) for k in range(ntr)]
+    ctx = G.Context(mesh, G.PREC_FP32, max_tracers=ntr)
+    ctx.state_setup(cfgs)
+    ctx.forcing_upload(f)
+    for k in range(ntr):
+        ctx.tracer_upload(k, tr[k].astype(np.float32), tr[k].astype(np.float32))
+    ctx.run_steps(f.dt, 5)
+    wet = wet_mask(mesh)
+    for k in range(2, ntr):
+        v, _ = ctx.tracer_download(k, dtype=np.float32)
+        assert v[wet].min() >= 0.0
+
+
+def test_errors_are_reported(channel_small):
+    ctx = G.Context(channel_small, G.PREC_FP64)
+    f, tr = _setup(channel_small, "channel")
+    T = np.ascontiguousarray(tr[0])
+    with pytest.raises(G.FesomGpuError) as e:
+        ctx.adv_tra(f, G.tra_cfg("MUSCL", "PPM", "FCT"), T, T)
+    assert e.value.rc == 2
+    bad = G.tra_cfg()
+    bad.ab_order = 4
+    with pytest.raises(G.FesomGpuError):
+        ctx.adv_tra(f, bad, T, T)
+    with pytest.raises(G.FesomGpuError) as e:
+        ctx.run_steps(600.0, 1)
+    assert e.value.rc == 8

@@ -1,0 +1,229 @@
+"""The FP64 CPU oracle, pinned by known-answer properties and by an independent
+numpy restatement of the same reference loops (tests/refimpl.py)."""
+import numpy as np
+import pytest
+
+from fesom2_gb300 import mesh as M
+from oracle import oracle as O
+from tests.conftest import perturbed_old, wet_mask
+from tests.refimpl import Ref
+
+SCHEMES = [("MUSCL", "QR4C", "FCT"), ("MFCT", "QR4C", "FCT"), ("UPW1", "UPW1", "FCT"),
+           ("MUSCL", "QR4C", "NON"), ("UPW1", "QR4C", "NON")]
+
+
+def _forcing(mesh, kind, **kw):
+    return O.ensure_f64(M.make_forcing(mesh, kind, seed=3, dt=600.0, **kw))
+
+
+@pytest.mark.parametrize("meshname,kind", [("channel_small", "channel"), ("channel_seamount", "channel"),
+                                           ("sphere_small", "sphere")])
+def test_gradients_match_restatement(meshname, kind, request):
+    mesh = request.getfixturevalue(meshname)
+    tr = M.make_tracers(mesh, kind, ntr=1, seed=4)
+    T = np.ascontiguousarray(tr[0])
+    om = O.OracleMesh(mesh)
+    om.init_tracers_AB(O.cfg_struct(), T.copy(), np.zeros_like(T), T.copy())
+    ref = Ref(mesh)
+    trxy = ref.tr_xy(T)
+    ewet = (ref.lev >= mesh.ulevels[:, None]) & (ref.lev <= mesh.nlevels[:, None] - 1)
+    assert np.array_equal(trxy[ewet], om.work["tr_xy"][ewet])
+    G = ref.fill_up_dn_grad(trxy, om.work["edge_up_dn_tri"])
+    assert np.array_equal(G[ref.smask], om.work["edge_up_dn_grad"][ref.smask])
+
+
+@pytest.mark.parametrize("scheme", SCHEMES, ids=["-".join(s) for s in SCHEMES])
+@pytest.mark.parametrize("meshname,kind", [("channel_seamount", "channel"), ("sphere_small", "sphere")])
+def test_adv_tra_matches_restatement(scheme, meshname, kind, request):
+    mesh = request.getfixturevalue(meshname)
+    hor, ver, lim = scheme
+    f = _forcing(mesh, kind)
+    tr = M.make_tracers(mesh, kind, ntr=1, seed=4)
+    T = np.ascontiguousarray(tr[0])
+    rng = np.random.default_rng(5)
+    TAB = np.ascontiguousarray(T * (1 + 1e-3 * rng.standard_normal(T.shape)))
+    om = O.OracleMesh(mesh)
+    ocfg = O.cfg_struct(hor, ver, lim)
+    om.init_tracers_AB(ocfg, T.copy(), np.zeros_like(T), T.copy())
+    G = om.work["edge_up_dn_grad"].copy()
+    om.do_oce_adv_tra(f, ocfg, T, TAB)
+    ref = Ref(mesh)
+    dh, dv, aux = ref.adv_tra(f.dt, f.uv, f.w, f.w_e, T, TAB, hor, ver, lim, 0.0, 1.0, G, om.work["nboundary_lay"])
+    wet = wet_mask(mesh)
+    assert np.array_equal(dh[wet], om.work["del_ttf_advhoriz"][wet])
+    assert np.array_equal(dv[wet], om.work["del_ttf_advvert"][wet])
+    if lim == "FCT":
+        assert np.array_equal(aux["LO"][wet], om.work["fct_LO"][wet])
+
+
+@pytest.mark.parametrize("meshname,kind", [("channel_small", "channel"), ("sphere_small", "sphere")])
+def test_vdiff_matches_restatement(meshname, kind, request):
+    mesh = request.getfixturevalue(meshname)
+    f = _forcing(mesh, kind)
+    f.bc_surface = np.linspace(-2e-3, 1e-3, mesh.nod2D)
+    T = np.ascontiguousarray(M.make_tracers(mesh, kind, ntr=1, seed=2)[0])
+    om = O.OracleMesh(mesh)
+    To = T.copy()
+    om.diff_ver_part_impl_ale(f, To)
+    Tr = Ref(mesh).vdiff(f.dt, f.Kv, f.bc_surface, T)
+    assert np.array_equal(To, Tr)
+
+
+@pytest.mark.parametrize("meshname,kind", [("channel_seamount", "channel"), ("sphere_small", "sphere")])
+def test_tracer_step_matches_restatement(meshname, kind, request):
+    mesh = request.getfixturevalue(meshname)
+    f = _forcing(mesh, kind)
+    T = np.ascontiguousarray(M.make_tracers(mesh, kind, ntr=1, seed=6)[0])
+    Told = perturbed_old(T, np.random.default_rng(1))
+    om = O.OracleMesh(mesh)
+    To, Oo = T.copy(), Told.copy()
+    om.tracer_step(f, O.cfg_struct(), To, np.zeros_like(To), Oo)
+    Tr, Or = Ref(mesh).tracer_step(f, T, Told, om.work["edge_up_dn_tri"], om.work["nboundary_lay"])
+    assert np.array_equal(To, Tr)
+    assert np.array_equal(Oo, Or)
+
+
+# ---- known-answer properties ----------------------------------------------------
+@pytest.mark.parametrize("scheme", SCHEMES, ids=["-".join(s) for s in SCHEMES])
+def test_constant_tracer_is_preserved(sphere_small, scheme):
+    """With w from the discrete divergence, a constant tracer stays constant (LO = HO = c, AD = 0)."""
+    mesh = sphere_small
+    f = _forcing(mesh, "sphere")
+    wet = wet_mask(mesh)
+    T = np.where(wet, 7.25, 0.0)
+    Told = T.copy()
+    om = O.OracleMesh(mesh)
+    cfg = O.cfg_struct(*scheme)
+    for _ in range(3):
+        om.tracer_step(f, cfg, T, np.zeros_like(T), Told)
+    assert np.abs(T[wet] - 7.25).max() < 1e-12
+
+
+@pytest.mark.parametrize("meshname,kind", [("channel_seamount", "channel"), ("sphere_small", "sphere")])
+def test_content_conserved(meshname, kind, request):
+    """Rigid lid (w(nzmin) = 0), linfs: sum T*hnode_new*areasvol conserved to 1e-12 relative."""
+    mesh = request.getfixturevalue(meshname)
+    f = _forcing(mesh, kind, surface_w_zero=True)
+    wet = wet_mask(mesh)
+    V = mesh.areasvol[:, :mesh.nl - 1]
+    om = O.OracleMesh(mesh)
+    for k, T in enumerate(M.make_tracers(mesh, kind, ntr=3, seed=8)):
+        T = np.ascontiguousarray(T)
+        Told = T.copy()
+        c0 = np.sum(np.where(wet, T * mesh.hnode * V, 0.0))
+        for _ in range(4):
+            om.tracer_step(f, O.cfg_struct(), T, np.zeros_like(T), Told)
+        c1 = np.sum(np.where(wet, T * mesh.hnode_new * V, 0.0))
+        assert abs(c1 - c0) / abs(c0) < 1e-12, k
+
+
+def test_fct_result_within_bounds(sphere_small):
+    """After limited advection every value lies in [min, max] of max/min(LO, T) over the
+    node's elements and the adjacent layers (the FCT bounds), up to round-off."""
+    mesh = sphere_small
+    f = _forcing(mesh, "sphere")
+    om = O.OracleMesh(mesh)
+    wet = wet_mask(mesh)
+    T = np.ascontiguousarray(M.make_tracers(mesh, "sphere", ntr=3, seed=12)[2])  # lognormal: sharp
+    TAB = np.zeros_like(T)
+    Told = T.copy()
+    cfg = O.cfg_struct()
+    om.init_tracers_AB(cfg, T, TAB, Told)
+    om.do_oce_adv_tra(f, cfg, T, TAB)
+    w = om.work
+    Tadv = T + (w["del_ttf_advhoriz"] + w["del_ttf_advvert"] + T * (mesh.hnode - mesh.hnode_new)) / mesh.hnode_new
+    tmax, tmin = w["tvert_max"], w["tvert_min"]
+    up = np.concatenate([tmax[:, :1], tmax[:, :-1]], 1); dn = np.concatenate([tmax[:, 1:], tmax[:, -1:]], 1)
+    upm = np.concatenate([tmin[:, :1], tmin[:, :-1]], 1); dnm = np.concatenate([tmin[:, 1:], tmin[:, -1:]], 1)
+    lev = np.arange(1, mesh.nl)[None, :]
+    inner = (lev >= mesh.ulevels_nod2D[:, None] + 1) & (lev <= mesh.nlevels_nod2D[:, None] - 2)
+    hi = np.where(inner, np.maximum(np.maximum(up, tmax), dn), tmax)
+    lo = np.where(inner, np.minimum(np.minimum(upm, tmin), dnm), tmin)
+    tol = 1e-12 * np.abs(T).max()
+    assert np.all(Tadv[wet] <= hi[wet] + tol)
+    assert np.all(Tadv[wet] >= lo[wet] - tol)
+
+
+def test_vertical_diffusion_solves_the_tridiagonal_system(channel_seamount):
+    """The Thomas sweep equals a dense solve of the reference's tridiagonal system
+    (coefficients rebuilt here from oce_ale_tracer.F90:1099-1229)."""
+    mesh = channel_seamount
+    f = _forcing(mesh, "channel")
+    T = np.ascontiguousarray(M.make_tracers(mesh, "channel", ntr=1, seed=3)[0])
+    om = O.OracleMesh(mesh)
+    To = T.copy()
+    om.diff_ver_part_impl_ale(f, To)
+    dt = f.dt
+    for n in [0, 7, mesh.nod2D // 2, mesh.nod2D - 1]:
+        nzmin, nzmax = mesh.ulevels_nod2D[n], mesh.nlevels_nod2D[n]
+        hn = mesh.hnode_new[n]
+        z = np.zeros(mesh.nl + 1)
+        zb = mesh.zbar_n_bot[n]
+        z[nzmax - 1] = zb + hn[nzmax - 2] / 2
+        for k in range(nzmax - 1, nzmin, -1):
+            zb += hn[k - 1]
+            z[k - 1] = zb + hn[k - 2] / 2
+        K = np.arange(nzmin, nzmax)
+        nlay = K.size
+        A = np.zeros((nlay, nlay))
+        for i, k in enumerate(K):
+            ar, av, kv = mesh.area[n], mesh.areasvol[n], f.Kv[n]
+            if k > nzmin:
+                A[i, i - 1] = -kv[k - 1] * dt / (z[k - 1] - z[k]) * ar[k - 1] / av[k - 1]
+            if k < nzmax - 1:
+                A[i, i + 1] = -kv[k] * dt / (z[k] - z[k + 1]) * ar[k] / av[k - 1]
+            A[i, i] = -A[i].sum() + hn[k - 1]
+        rhs = hn[K - 1] * T[n, K - 1]
+        sol = np.linalg.solve(A, rhs)
+        assert np.allclose(To[n, K - 1], sol, rtol=1e-12, atol=1e-12)
+        # column content conserved by the diffusion
+        V = mesh.areasvol[n, K - 1] * hn[K - 1]
+        assert abs(np.sum(V * To[n, K - 1]) - np.sum(V * T[n, K - 1])) <= 1e-12 * abs(np.sum(V * T[n, K - 1]))
+
+
+def test_upwind_edge_flux_by_hand(channel_small):
+    """One interior edge: F = -0.5*(T1*(v+|v|) + T2*(v-|v|)) with v the two-segment
+    volume flux (oce_adv_tra_hor.F90:211-216), written out from the formula."""
+    mesh = channel_small
+    f = _forcing(mesh, "channel")
+    T = np.ascontiguousarray(M.make_tracers(mesh, "channel", ntr=1, seed=3)[0])
+    flux = np.zeros((mesh.edge2D, mesh.nl - 1))
+    import ctypes as C
+    O.lib().or_adv_tra_hor_upw1(C.byref(O.OracleMesh(mesh).s), O._ptr(f.uv), O._ptr(T), O._ptr(flux), 1)
+    e = int(np.flatnonzero(mesh.edge_tri[:, 1] >= 0)[5])
+    n1, n2 = mesh.edges[e]
+    el1, el2 = mesh.edge_tri[e]
+    dx1, dy1, dx2, dy2 = mesh.edge_cross_dxdy[e]
+    for nz in range(3):
+        u1, v1 = f.uv[el1, nz]
+        u2, v2 = f.uv[el2, nz]
+        vf = (-v1 * dx1 + u1 * dy1) * mesh.helem[el1, nz] + (v2 * dx2 - u2 * dy2) * mesh.helem[el2, nz]
+        want = -0.5 * (T[n1, nz] * (vf + abs(vf)) + T[n2, nz] * (vf - abs(vf)))
+        assert flux[e, nz] == want
+
+
+def test_qr4c_interior_flux_by_hand(channel_seamount):
+    """QR4C at an interior interface (oce_adv_tra_ver.F90:415-425), written out."""
+    mesh = channel_seamount
+    f = _forcing(mesh, "channel")
+    n = 3
+    rng = np.random.default_rng(0)
+    T = np.ascontiguousarray(rng.uniform(1, 2, (mesh.nod2D, mesh.nl - 1)))
+    W = np.ascontiguousarray(rng.uniform(-1e-4, 1e-4, (mesh.nod2D, mesh.nl)))
+    flux = np.zeros((mesh.nod2D, mesh.nl))
+    import ctypes as C
+    pv = 0.7
+    O.lib().or_adv_tra_ver_qr4c(C.byref(O.OracleMesh(mesh).s), O._ptr(W), O._ptr(T), C.c_double(pv), O._ptr(flux), 1)
+    Z, zb = mesh.Z_3d_n[n], mesh.zbar_3d_n[n]
+    nz = 5  # 1-based interface, interior
+    t = lambda k: T[n, k - 1]
+    zz = lambda k: Z[k - 1]
+    qc = (t(nz - 1) - t(nz)) / (zz(nz - 1) - zz(nz))
+    qu = (t(nz) - t(nz + 1)) / (zz(nz) - zz(nz + 1))
+    qd = (t(nz - 2) - t(nz - 1)) / (zz(nz - 2) - zz(nz - 1))
+    Tm1 = t(nz) + (2 * qc + qu) * (zb[nz - 1] - zz(nz)) / 3.0
+    Tm2 = t(nz - 1) + (2 * qc + qd) * (zb[nz - 1] - zz(nz - 1)) / 3.0
+    w = W[n, nz - 1]
+    Tmean = (w + abs(w)) * Tm1 + (w - abs(w)) * Tm2
+    want = (-0.5 * (1 - pv) * Tmean - pv * (0.5 * (Tm1 + Tm2)) * w) * mesh.area[n, nz - 1]
+    assert flux[n, nz - 1] == want
