@@ -326,7 +326,7 @@ int enqueue_step(fesom_gpu_ctx *ctx, double dt, StageTimer *tm = nullptr) {
         STAGE(2, Launch<R>::edge_flux(ctx->tp, g, f, tr, any_fct, ctx->stream));
         STAGE(3, Launch<R>::node_lo(ctx->tp, g, f, tr, dt, any_fct, ctx->stream));
         if (any_fct) {
-            STAGE(4, Launch<R>::bounds(ctx->tp, tr, ctx->stream));
+            STAGE(4, Launch<R>::bounds(ctx->tp, g, tr, ctx->stream));
             STAGE(5, Launch<R>::rpm(ctx->tp, g, tr, dt, ctx->stream));
         }
         STAGE(6, Launch<R>::update(ctx->tp, g, tr, dt, any_fct, 1, ctx->stream));
@@ -592,7 +592,7 @@ int fesom_gpu_adv_tra(fesom_gpu_ctx *ctx, double dt, const double *vel, const do
     Launch<double>::edge_flux(ctx->tp, ctx->g64, f, tr, fct, ctx->stream);
     Launch<double>::node_lo(ctx->tp, ctx->g64, f, tr, dt, fct, ctx->stream);
     if (fct) {
-        Launch<double>::bounds(ctx->tp, tr, ctx->stream);
+        Launch<double>::bounds(ctx->tp, ctx->g64, tr, ctx->stream);
         Launch<double>::rpm(ctx->tp, ctx->g64, tr, dt, ctx->stream);
     }
     Launch<double>::update(ctx->tp, ctx->g64, tr, dt, fct, 0, ctx->stream);

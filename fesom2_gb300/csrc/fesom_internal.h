@@ -84,7 +84,7 @@ struct Launch {
     static void edge_flux(const DTopo &, const DGeom<R> &, const DForcing<R> &, DTracers<R> &, int fct, cudaStream_t);
     static void node_lo(const DTopo &, const DGeom<R> &, const DForcing<R> &, DTracers<R> &, double dt, int fct,
                         cudaStream_t);
-    static void bounds(const DTopo &, DTracers<R> &, cudaStream_t);
+    static void bounds(const DTopo &, const DGeom<R> &, DTracers<R> &, cudaStream_t);
     static void rpm(const DTopo &, const DGeom<R> &, DTracers<R> &, double dt, cudaStream_t);
     // mode 0: write dttf_h/dttf_v only; mode 1: del_ttf sum + T* update into T
     static void update(const DTopo &, const DGeom<R> &, DTracers<R> &, double dt, int fct, int mode, cudaStream_t);

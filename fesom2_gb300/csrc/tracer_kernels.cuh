@@ -29,6 +29,15 @@ template <typename R> __device__ __forceinline__ R rmin(R a, R b) { return a < b
 template <typename R> __device__ __forceinline__ R rabs(R a) { return fabs(a); }
 template <> __device__ __forceinline__ float rabs<float>(float a) { return fabsf(a); }
 
+// The FP64 form keeps the reference's statements and evaluation order.  The FP32
+// form keeps LO's increment (the low-order flux divergence times dt/areasvol)
+// in the LO buffer instead of LO itself, so the final update is a compensated
+// sum of flux terms rather than the difference LO*hnode_new - T*hnode of two
+// nearly equal products (which loses most FP32 bits); LO is rebuilt where the
+// FCT bounds need it.
+template <typename R> struct Exact { static constexpr bool value = false; };
+template <> struct Exact<double> { static constexpr bool value = true; };
+
 __device__ __forceinline__ size_t ix1(int nz, int n, int L1) { return (size_t)n * L1 + (nz - 1); }
 __device__ __forceinline__ size_t ixn(int nz, int n, int nl) { return (size_t)n * nl + (nz - 1); }
 
@@ -309,17 +318,24 @@ k_node_lo(DTopo tp, DGeom<R> g, DForcing<R> f, DTracers<R> tr, R dt) {
                     fv0 = ver_upw1_flux(T, f.we, g.area, nz, n, nzmin, nzmax, L1, nl, R(0));
                     if (nz <= nzmax - 1) {
                         const R fv1 = ver_upw1_flux(T, f.we, g.area, nz + 1, n, nzmin, nzmax, L1, nl, R(0));
-                        R acc = R(0);
+                        Acc<R> acc;
                         for (int k = k0; k < k1; k++) {
                             const int code = tp.ne_idx[k];
                             const int e = code >= 0 ? code : ~code;
                             if (nz < tp.e_lo[e] || nz > tp.e_hi[e]) continue;
                             const R x = FLO[ix1(nz, e, L1)];
-                            acc = code >= 0 ? acc + x : acc - x;
+                            if (code >= 0) acc.add(x);
+                            else acc.sub(x);
                         }
                         const size_t i = ix1(nz, n, L1);
-                        tr.LO[t * tr.sN + i] =
-                            (T[i] * g.hnode[i] + (acc + (fv0 - fv1)) * dt / g.areasvol[ixn(nz, n, nl)]) / g.hnode_new[i];
+                        if (Exact<R>::value) {
+                            tr.LO[t * tr.sN + i] = (T[i] * g.hnode[i] + (acc.get() + (fv0 - fv1)) * dt /
+                                                    g.areasvol[ixn(nz, n, nl)]) / g.hnode_new[i];
+                        } else {
+                            acc.add(fv0);
+                            acc.sub(fv1);
+                            tr.LO[t * tr.sN + i] = acc.get() * dt / g.areasvol[ixn(nz, n, nl)];
+                        }
                     }
                 }
                 const R *pw = fct ? f.w : f.we;
@@ -339,8 +355,16 @@ k_node_lo(DTopo tp, DGeom<R> g, DForcing<R> f, DTracers<R> tr, R dt) {
 // The element max/min (AUX) is recomputed per node from the element's three
 // nodes (max/min are exact, so this equals the reference's two passes).
 // ===========================================================================
+// LO of node x at layer nz (the FP32 form stores the increment, see Exact)
 template <typename R>
-__global__ void __launch_bounds__(kThreads) k_bounds(DTopo tp, DTracers<R> tr) {
+__device__ __forceinline__ R lo_value(const R *LO, const R *T, const DGeom<R> &g, int nz, int x, int L1) {
+    const size_t i = ix1(nz, x, L1);
+    if (Exact<R>::value) return LO[i];
+    return (T[i] * g.hnode[i] + LO[i]) / g.hnode_new[i];
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_bounds(DTopo tp, DGeom<R> g, DTracers<R> tr) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R *sm = reinterpret_cast<R *>(smem_raw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -362,9 +386,9 @@ __global__ void __launch_bounds__(kThreads) k_bounds(DTopo tp, DTracers<R> tr) {
                     R amx, amn;
                     if (nz >= tp.t_ulev[el] && nz <= tp.t_nlev[el] - 1) {
                         const int a = tp.t_n[3 * el], b = tp.t_n[3 * el + 1], cc = tp.t_n[3 * el + 2];
-                        const R la = LO[ix1(nz, a, L1)], ta = T[ix1(nz, a, L1)];
-                        const R lb = LO[ix1(nz, b, L1)], tb = T[ix1(nz, b, L1)];
-                        const R lc = LO[ix1(nz, cc, L1)], tc = T[ix1(nz, cc, L1)];
+                        const R la = lo_value(LO, T, g, nz, a, L1), ta = T[ix1(nz, a, L1)];
+                        const R lb = lo_value(LO, T, g, nz, b, L1), tb = T[ix1(nz, b, L1)];
+                        const R lc = lo_value(LO, T, g, nz, cc, L1), tc = T[ix1(nz, cc, L1)];
                         amx = rmax(rmax(rmax(la, ta), rmax(lb, tb)), rmax(lc, tc));
                         amn = rmin(rmin(rmin(la, ta), rmin(lb, tb)), rmin(lc, tc));
                     } else {
@@ -380,7 +404,7 @@ __global__ void __launch_bounds__(kThreads) k_bounds(DTopo tp, DTracers<R> tr) {
             __syncwarp();
             R *bmx = tr.bmax + t * tr.sN, *bmn = tr.bmin + t * tr.sN;
             for (int nz = nzmin + lane; nz <= nzmax - 1; nz += 32) {
-                const R lo = LO[ix1(nz, n, L1)];
+                const R lo = lo_value(LO, T, g, nz, n, L1);
                 R vmx, vmn;
                 if (nz == nzmin || nz == nzmax - 1) {
                     vmx = tvmax[nz] - lo;
@@ -483,15 +507,22 @@ __global__ void __launch_bounds__(kThreads) k_update(DTopo tp, DGeom<R> g, DTrac
                 R dv = R(0.0);
                 R f0, f1;
                 if (fct) {
-                    dv = dv - T[i] * g.hnode[i] + tr.LO[t * tr.sN + i] * g.hnode_new[i];
+                    if (Exact<R>::value) dv = dv - T[i] * g.hnode[i] + tr.LO[t * tr.sN + i] * g.hnode_new[i];
                     f0 = limited_adv(ADv, Rp, Rm, nz, n, nzmin, nzmax, L1, nl);
                     f1 = limited_adv(ADv, Rp, Rm, nz + 1, n, nzmin, nzmax, L1, nl);
                 } else {
                     f0 = ADv[ixn(nz, n, nl)];
                     f1 = ADv[ixn(nz + 1, n, nl)];
                 }
-                dv = dv + (f0 - f1) * dt / av;
                 Acc<R> dh;
+                if (!Exact<R>::value) {
+                    // FP32: one compensated sum of LO increment, vertical and horizontal terms
+                    if (fct) dh.add(tr.LO[t * tr.sN + i]);
+                    dh.add(f0 * dt / av);
+                    dh.sub(f1 * dt / av);
+                } else {
+                    dv = dv + (f0 - f1) * dt / av;
+                }
                 for (int k = k0; k < k1; k++) {
                     const int code = tp.ne_idx[k];
                     const int e = code >= 0 ? code : ~code;
@@ -512,13 +543,17 @@ __global__ void __launch_bounds__(kThreads) k_update(DTopo tp, DGeom<R> g, DTrac
                     if (code >= 0) dh.add(x * dt / av);
                     else dh.sub(x * dt / av);
                 }
+                if (!Exact<R>::value) dh.add(T[i] * (g.hnode[i] - g.hnode_new[i]));
                 const R dhv = dh.get();
                 if (mode == 0) {
                     tr.dttf_h[t * tr.sN + i] = dhv;
                     tr.dttf_v[t * tr.sN + i] = dv;
                 } else {
-                    R del = R(0.0) + dhv + dv;
-                    del = del + T[i] * (g.hnode[i] - g.hnode_new[i]);
+                    R del = dhv;
+                    if (Exact<R>::value) {
+                        del = R(0.0) + dhv + dv;
+                        del = del + T[i] * (g.hnode[i] - g.hnode_new[i]);
+                    }
                     const R tn = T[i] + del / g.hnode_new[i];
                     T[i] = tn;
                     if (!isfinite(tn)) atomicOr(tr.status, 1u);
@@ -686,9 +721,9 @@ void Launch<R>::node_lo(const DTopo &tp, const DGeom<R> &g, const DForcing<R> &f
     k_node_lo<R><<<grid_for(tp.N2, kWarpsPerBlock), kThreads, 0, s>>>(tp, g, f, tr, (R)dt);
 }
 template <typename R>
-void Launch<R>::bounds(const DTopo &tp, DTracers<R> &tr, cudaStream_t s) {
+void Launch<R>::bounds(const DTopo &tp, const DGeom<R> &g, DTracers<R> &tr, cudaStream_t s) {
     const size_t sm = sizeof(R) * 2 * (tp.L1 + 2) * kWarpsPerBlock;
-    k_bounds<R><<<grid_for(tp.N2, kWarpsPerBlock), kThreads, sm, s>>>(tp, tr);
+    k_bounds<R><<<grid_for(tp.N2, kWarpsPerBlock), kThreads, sm, s>>>(tp, g, tr);
 }
 template <typename R>
 void Launch<R>::rpm(const DTopo &tp, const DGeom<R> &g, DTracers<R> &tr, double dt, cudaStream_t s) {

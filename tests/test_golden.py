@@ -1,0 +1,44 @@
+"""Committed golden fixtures (tests/golden/*.npz, made by tests/golden/make_golden.py):
+the oracle (CPU) and the FP64 CUDA path (GPU, through the C ABI) reproduce the
+stored results of three tracer steps bit for bit."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.golden.make_golden import CASES, load
+
+NAMES = sorted(CASES)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_reproduces_golden(name):
+    mesh, f, d = load(name)
+    om = O.OracleMesh(mesh)
+    assert np.array_equal(om.work["nboundary_lay"], d["muscl_nbl"])
+    assert np.array_equal(om.work["edge_up_dn_tri"], d["muscl_updn"])
+    hor, ver, lim = [str(x) for x in d["scheme"]]
+    cfg = O.cfg_struct(hor, ver, lim, ph=0.0, pv=1.0, ab_order=int(d["ab"]))
+    for k in range(2):
+        T, old = d[f"T0_{k}"].copy(), d[f"old0_{k}"].copy()
+        for s in range(3):
+            om.tracer_step(f, cfg, T, np.zeros_like(T), old)
+            assert np.array_equal(T, d[f"T{s + 1}_{k}"]), (name, k, s)
+            assert np.array_equal(old, d[f"old{s + 1}_{k}"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", NAMES)
+def test_gpu_fp64_reproduces_golden(name):
+    from fesom2_gb300 import gpu as G
+    mesh, f, d = load(name)
+    hor, ver, lim = [str(x) for x in d["scheme"]]
+    ab = int(d["ab"])
+    cfgs = [G.tra_cfg(hor, ver, lim, 0.0, 1.0, ab_order=ab, id=k + 1) for k in range(2)]
+    ctx = G.Context(mesh, G.PREC_FP64, max_tracers=2)
+    T = [d[f"T0_{k}"].copy() for k in range(2)]
+    old = [np.ascontiguousarray(d[f"old0_{k}"]).copy() for k in range(2)]
+    for s in range(3):
+        ctx.tracer_step(f, cfgs, T, old)
+        for k in range(2):
+            assert np.array_equal(T[k], d[f"T{s + 1}_{k}"]), (name, k, s)
+            assert np.array_equal(old[k].reshape(-1), d[f"old{s + 1}_{k}"].reshape(-1))
