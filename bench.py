@@ -80,27 +80,36 @@ def algorithmic_bytes(counts, ntr, s):
     return s * (ntr * (18 * N3 + 3 * E3) + 3 * T3 + 14 * N3)
 
 
-def stage_bytes(counts, ntr, s):
-    """Compulsory bytes per launch of each stage kernel of this implementation
-    (every input read once, every output written once, for ntr tracers):
-      ab:        read T, Told; write TAB, Told                      4 N3 per tracer
-      trxy:      read T; write 2 gradient components per element    N3 + 2 T3
-      edge_flux: read T, TAB (N3 each), gradients (2 T3); write FLO, ADh (2 E3); shared uv, helem (3 T3)
-      node_lo:   read T, TAB, FLO (E3); write LO, ADv;  shared w, we, area, hnode, hnode_new, areasvol, Z, zbar (8 N3)
-      bounds:    read T, LO; write bmax, bmin                       4 N3
-      rpm:       read ADv, ADh (E3), bmax, bmin; write R+, R-       5 N3 + E3; shared areasvol, hnode_new (2 N3)
-      update:    read T, LO, ADv, ADh (E3), R+, R-; write T         6 N3 + E3; shared hnode, hnode_new, areasvol (3 N3)
-      vdiff:     read T, write T (FP32: 4+4); shared Kv, area, areasvol, hnode_new (4 N3), FP64 scratch 3 x 2 x 8 B
+def stage_bytes(counts, ntr, s, ab=2):
+    """Compulsory bytes per step of each stage kernel (every input read once, every
+    output written once) for ntr tracers, s bytes per value.
+
+    FP32 batched form:
+      vflux:    read uv (2 T3), helem (T3); write the edge volume flux VF (E3)           shared
+      vfactors: read Kv, area, areasvol, hnode_new (4 N3); write a, c, 1/m, c/m (4 N3)   shared
+      lo_ad:    per tracer read T, T_old (2 N3; 3 with AB3); write LO increment, ADv (2 N3),
+                ADh (E3); shared VF (E3), w, w_e, area, Z, zbar, areasvol (6 N3)
+      bounds:   per tracer read T, LO increment, ADv (3 N3), ADh (E3); write R+, R- and the
+                bounds T_up, T_lo (4 N3); shared hnode, hnode_new, areasvol (3 N3)
+      update:   per tracer read T, LO increment, ADv, R+, R-, T_up, T_lo (7 N3), ADh (E3); write
+                T (N3); shared factors (4 N3), hnode, hnode_new, areasvol (3 N3)
+    FP64 plain form (per tracer, one tracer per launch):
+      ab 4 N3; trxy N3 + 2 T3; edge_flux 2 N3 + 2 T3 + 2 E3 (+3 T3 shared); node_lo 3 N3 + E3
+      (+8 N3); bounds 4 N3; rpm 5 N3 + E3 (+2 N3); update 6 N3 + E3 (+3 N3); vdiff 2 N3 (+4 N3)
+      plus 48 B per DOF of FP64 scratch.
     """
     N3, E3, T3 = counts["N3"], counts["E3"], counts["T3"]
     return {
+        "vflux": s * (3 * T3 + E3),
+        "vfactors": s * 8 * N3,
+        "lo_ad": s * (ntr * ((ab + 2) * N3 + E3) + E3 + 6 * N3),
+        "bounds": s * (ntr * (7 * N3 + E3) + 3 * N3),
+        "update": s * (ntr * (8 * N3 + E3) + 7 * N3),
         "ab": s * ntr * 4 * N3,
         "trxy": s * ntr * (N3 + 2 * T3),
         "edge_flux": s * (ntr * (2 * N3 + 2 * T3 + 2 * E3) + 3 * T3),
         "node_lo": s * (ntr * (3 * N3 + E3) + 8 * N3),
-        "bounds": s * ntr * 4 * N3,
         "rpm": s * (ntr * (5 * N3 + E3) + 2 * N3),
-        "update": s * (ntr * (6 * N3 + E3) + 3 * N3),
         "vdiff": s * (ntr * 2 * N3 + 4 * N3) + ntr * 48 * N3,
     }
 
@@ -234,6 +243,21 @@ def run_ours(args, rank, world, local_rank):
         ctx.tracer_upload(k, tracers[k], tracers[k])
     torch.cuda.synchronize()
     launches = ctx.launches_per_step()
+    # one step from the initial state for the error report against the FP64 oracle,
+    # then the initial state again for the timing
+    err_tracers = [k for k in (0, 1, ntr - 1) if k < ntr]
+    err_tracers = sorted(set(err_tracers))
+    first_step = {}
+    if not args.profile_only and not args.no_cpu:
+        c0 = ctx.content()
+        ctx.run_steps(dt, 1, use_graph=False)
+        c1 = ctx.content()
+        for k in err_tracers:
+            first_step[k] = ctx.tracer_download(k, dtype=np.float32)[0]
+        res["content_drift_fp32"] = [float(abs(c1[k] - c0[k]) / abs(c0[k])) for k in range(min(ntr, 2))]
+        for k in range(ntr):
+            ctx.tracer_upload(k, tracers[k], tracers[k])
+        torch.cuda.synchronize()
     if args.profile_only:
         ctx.run_steps(dt, 1, use_graph=True)
         torch.cuda.synchronize()
@@ -373,6 +397,22 @@ def run_ours(args, rank, world, local_rank):
         res["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                                "sample": f"1 tracer step of the full workload mesh (N3 = {N3}), "
                                          f"FP64 oracle with OpenMP, {el:.1f} s"}
+        # error of the FP32 batched step against the FP64 oracle (same FP32-rounded start)
+        from oracle import oracle as O
+        lev = np.arange(mesh.nl - 1)[None, :]
+        wet = (lev >= (mesh.ulevels_nod2D - 1)[:, None]) & (lev < (mesh.nlevels_nod2D - 1)[:, None])
+        om = O.OracleMesh(mesh)
+        fo = O.ensure_f64(M.Forcing(uv=forcing.uv, w=forcing.w, w_e=forcing.w_e, w_i=forcing.w_i, Kv=forcing.Kv,
+                                    bc_surface=forcing.bc_surface, dt=dt))
+        errs = {}
+        for k, got in first_step.items():
+            T64 = tracers[k].astype(np.float64)
+            O64 = T64.copy()
+            om.tracer_step(fo, O.cfg_struct(), T64, np.zeros_like(T64), O64)
+            d = np.abs(got[wet].astype(np.float64) - T64[wet])
+            errs[f"tracer{k}"] = {"normwise": float(d.max() / np.abs(T64[wet]).max()),
+                                  "pointwise_rel": float((d / np.maximum(np.abs(T64[wet]), 1e-30)).max())}
+        res["error_vs_fp64_oracle_one_step"] = errs
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

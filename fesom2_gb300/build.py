@@ -23,6 +23,7 @@ UNITS = {
     # FP64 kernels: no FMA contraction, so the arithmetic matches the reference bit for bit
     "kernels_fp64.cu": ["--fmad=false"],
     "kernels_fp32.cu": [],
+    "kernels_fp32_batched.cu": [],
     "capi.cu": [],
 }
 HOST_UNITS = ["mesh_prep.cpp"]

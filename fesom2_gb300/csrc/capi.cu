@@ -52,6 +52,15 @@ struct fesom_gpu_ctx {
     bool state_ready = false;
     cudaGraphExec_t gexec = nullptr;
     double g_dt = 0.0;
+    // FP32 batched form: rotating time-level buffers and its work arrays
+    float *Bf[3] = {nullptr, nullptr, nullptr};
+    int rot = 0;
+    float *VF = nullptr;
+    VFactors vfac{};
+    float *LOi = nullptr, *ADv32 = nullptr, *ADh32 = nullptr, *Rp = nullptr, *Rm = nullptr;
+    float *Tup = nullptr, *Tlo = nullptr;
+    cudaGraphExec_t gexec32[3] = {nullptr, nullptr, nullptr};
+    double g32_dt[3] = {0.0, 0.0, 0.0};
 };
 
 namespace {
@@ -132,6 +141,77 @@ int get(fesom_gpu_ctx *ctx, double *dst, const void *src, size_t n) {
         k_f2d<<<(int)std::min<size_t>((m + 255) / 256, 152 * 32), 256, 0, ctx->stream>>>((const float *)src + off, ctx->stage, m);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(dst + off, ctx->stage, m * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    return FESOM_OK;
+}
+
+// valuesold of AB3 interleaves its two levels, valuesold(k, nz, n): split into / join
+// from the two level buffers of the FP32 form (through the stage buffer)
+__global__ void k_deint_d2f(const double *in, float *o1, float *o2, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        o1[i] = (float)in[2 * i];
+        o2[i] = (float)in[2 * i + 1];
+    }
+}
+__global__ void k_int_f2d(const float *o1, const float *o2, double *out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        out[2 * i] = (double)o1[i];
+        out[2 * i + 1] = (double)o2[i];
+    }
+}
+__global__ void k_deint_f(const float *in, float *o1, float *o2, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        o1[i] = in[2 * i];
+        o2[i] = in[2 * i + 1];
+    }
+}
+__global__ void k_int_f(const float *o1, const float *o2, float *out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        out[2 * i] = o1[i];
+        out[2 * i + 1] = o2[i];
+    }
+}
+static int nblk(size_t m) { return (int)std::min<size_t>((m + 255) / 256, 152 * 32); }
+
+int put_deint(fesom_gpu_ctx *ctx, float *o1, float *o2, const double *src, size_t n) {
+    const size_t ch = ctx->stage_n / 2;
+    for (size_t off = 0; off < n; off += ch) {
+        size_t m = std::min(ch, n - off);
+        CK(cudaMemcpyAsync(ctx->stage, src + 2 * off, 2 * m * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        k_deint_d2f<<<nblk(m), 256, 0, ctx->stream>>>(ctx->stage, o1 + off, o2 + off, m);
+        CK(cudaGetLastError());
+    }
+    return FESOM_OK;
+}
+int get_int(fesom_gpu_ctx *ctx, double *dst, const float *o1, const float *o2, size_t n) {
+    const size_t ch = ctx->stage_n / 2;
+    for (size_t off = 0; off < n; off += ch) {
+        size_t m = std::min(ch, n - off);
+        k_int_f2d<<<nblk(m), 256, 0, ctx->stream>>>(o1 + off, o2 + off, ctx->stage, m);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(dst + 2 * off, ctx->stage, 2 * m * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    return FESOM_OK;
+}
+int put_deint_f(fesom_gpu_ctx *ctx, float *o1, float *o2, const float *src, size_t n) {
+    float *st = (float *)ctx->stage;
+    const size_t ch = ctx->stage_n;  // 2*ch floats fit the stage
+    for (size_t off = 0; off < n; off += ch) {
+        size_t m = std::min(ch, n - off);
+        CK(cudaMemcpyAsync(st, src + 2 * off, 2 * m * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+        k_deint_f<<<nblk(m), 256, 0, ctx->stream>>>(st, o1 + off, o2 + off, m);
+        CK(cudaGetLastError());
+    }
+    return FESOM_OK;
+}
+int get_int_f(fesom_gpu_ctx *ctx, float *dst, const float *o1, const float *o2, size_t n) {
+    float *st = (float *)ctx->stage;
+    const size_t ch = ctx->stage_n;
+    for (size_t off = 0; off < n; off += ch) {
+        size_t m = std::min(ch, n - off);
+        k_int_f<<<nblk(m), 256, 0, ctx->stream>>>(o1 + off, o2 + off, st, m);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(dst + 2 * off, st, 2 * m * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     }
     return FESOM_OK;
 }
@@ -288,6 +368,84 @@ const DGeom<float> &geom<float>(fesom_gpu_ctx *ctx) { return ctx->g32; }
 // One tracer step for tracers [0, ntr): per group init_tracers_AB, gradients,
 // edge fluxes, LO + vertical fluxes, FCT bounds, R+/R-, limited update with
 // T*, implicit vertical diffusion.  Stream-ordered, capturable.
+// ---- FP32 batched form ---------------------------------------------------------
+// time level k (0 = current values, 1 = previous, 2 = the one before) of the rotation
+float *level32(fesom_gpu_ctx *ctx, int k) {
+    if (ctx->ab_max == 2) return ctx->Bf[k == 0 ? ctx->rot : ctx->rot ^ 1];
+    const int r = ctx->rot;
+    return ctx->Bf[k == 0 ? r : (k == 1 ? (r + 2) % 3 : (r + 1) % 3)];
+}
+void rotate32(fesom_gpu_ctx *ctx) { ctx->rot = ctx->ab_max == 2 ? ctx->rot ^ 1 : (ctx->rot + 1) % 3; }
+
+void free_graphs32(fesom_gpu_ctx *ctx) {
+    for (auto &g : ctx->gexec32)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+}
+
+int alloc_state32(fesom_gpu_ctx *ctx, int ntr, int ab) {
+    const size_t sN = (size_t)ctx->L1 * ctx->N2, sNI = (size_t)ctx->nl * ctx->N2, sE = (size_t)ctx->L1 * ctx->E2;
+    void *old[] = {ctx->Bf[0], ctx->Bf[1], ctx->Bf[2], ctx->VF, ctx->vfac.a, ctx->vfac.c, ctx->vfac.inv, ctx->vfac.cp,
+                   ctx->LOi, ctx->ADv32, ctx->ADh32, ctx->Rp, ctx->Rm, ctx->Tup, ctx->Tlo, ctx->d_cfg, ctx->bc};
+    for (void *b : old) { void *p = b; dfree(ctx, p); }
+    ctx->Bf[0] = ctx->Bf[1] = ctx->Bf[2] = nullptr;
+    ctx->VF = ctx->LOi = ctx->ADv32 = ctx->ADh32 = ctx->Rp = ctx->Rm = ctx->Tup = ctx->Tlo = nullptr;
+    ctx->vfac = VFactors{};
+    ctx->d_cfg = nullptr;
+    ctx->bc = nullptr;
+    free_graphs32(ctx);
+    int rc;
+    for (int k = 0; k < ab; k++)
+        if ((rc = dalloc(ctx, (void **)&ctx->Bf[k], 4 * sN * ntr))) return rc;
+    for (int k = 0; k < ab; k++) CK(cudaMemset(ctx->Bf[k], 0, 4 * sN * ntr));
+    if ((rc = dalloc(ctx, &ctx->bc, 4 * (size_t)ctx->N2 * ntr))) return rc;
+    CK(cudaMemset(ctx->bc, 0, 4 * (size_t)ctx->N2 * ntr));
+    if ((rc = dalloc(ctx, (void **)&ctx->d_cfg, sizeof(DCfg) * ntr))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->VF, 4 * sE))) return rc;
+    float **fac[] = {&ctx->vfac.a, &ctx->vfac.c, &ctx->vfac.inv, &ctx->vfac.cp};
+    for (float **f : fac)
+        if ((rc = dalloc(ctx, (void **)f, 4 * sN))) return rc;
+    const size_t per_tracer = 4 * (5 * sN + sNI + sE);
+    size_t fr = 0, tot = 0;
+    CK(cudaMemGetInfo(&fr, &tot));
+    const int g = (int)std::min<size_t>((size_t)ntr, std::max<size_t>(1, (size_t)(0.85 * fr) / per_tracer));
+    ctx->group = ctx->group_cap = g;
+    if ((rc = dalloc(ctx, (void **)&ctx->LOi, 4 * sN * g))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->ADv32, 4 * sNI * g))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->ADh32, 4 * sE * g))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->Rp, 4 * sN * g))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->Rm, 4 * sN * g))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->Tup, 4 * sN * g))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->Tlo, 4 * sN * g))) return rc;
+    ctx->rot = 0;
+    ctx->ntr = ntr;
+    ctx->ab_max = ab;
+    ctx->state_ready = true;
+    return FESOM_OK;
+}
+
+B32View view32(fesom_gpu_ctx *ctx, int t0, int nt) {
+    B32View v{};
+    v.ntr = nt;
+    v.ab = ctx->ab_max;
+    v.sN = (size_t)ctx->L1 * ctx->N2;
+    v.sNI = (size_t)ctx->nl * ctx->N2;
+    v.sE = (size_t)ctx->L1 * ctx->E2;
+    v.T = level32(ctx, 0) + t0 * v.sN;
+    v.O1 = level32(ctx, 1) + t0 * v.sN;
+    v.O2 = ctx->ab_max == 3 ? level32(ctx, 2) + t0 * v.sN : nullptr;
+    v.Tnew = level32(ctx, ctx->ab_max - 1) + t0 * v.sN;
+    v.LOi = ctx->LOi;
+    v.ADv = ctx->ADv32;
+    v.ADh = ctx->ADh32;
+    v.Rp = ctx->Rp;
+    v.Rm = ctx->Rm;
+    v.Tup = ctx->Tup;
+    v.Tlo = ctx->Tlo;
+    v.cfg = ctx->d_cfg + t0;
+    v.status = ctx->status;
+    return v;
+}
+
 struct StageTimer {
     cudaEvent_t ev[2 * FESOM_NUM_STAGES * 64];
     int stage[FESOM_NUM_STAGES * 64];
@@ -332,13 +490,46 @@ int enqueue_step(fesom_gpu_ctx *ctx, double dt, StageTimer *tm = nullptr) {
         STAGE(6, Launch<R>::update(ctx->tp, g, tr, dt, any_fct, 1, ctx->stream));
         if (any_vd) STAGE(7, Launch<R>::vdiff(ctx->tp, g, f, tr, dt, ctx->scratch, ctx->stream));
     }
-#undef STAGE
     CK(cudaGetLastError());
     return FESOM_OK;
 }
 
+int enqueue_step32(fesom_gpu_ctx *ctx, double dt, StageTimer *tm = nullptr) {
+    const DGeom<float> &g = ctx->g32;
+    DForcing<float> f = forcing_view<float>(ctx, 0);
+    bool any_vd = false;
+    for (int t = 0; t < ctx->ntr; t++) any_vd |= ctx->cfgs[t].i_vert_diff != 0;
+    STAGE(8, b32_vflux(ctx->tp, g, f, ctx->VF, ctx->stream));
+    if (any_vd) STAGE(9, b32_vfactors(ctx->tp, g, f, dt, ctx->vfac, ctx->stream));
+    for (int t0 = 0; t0 < ctx->ntr; t0 += ctx->group) {
+        const int nt = std::min(ctx->group, ctx->ntr - t0);
+        B32View B = view32(ctx, t0, nt);
+        DForcing<float> fg = forcing_view<float>(ctx, t0);
+        bool any_fct = false;
+        for (int t = t0; t < t0 + nt; t++) any_fct |= ctx->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
+        STAGE(10, b32_lo_ad(ctx->tp, g, fg, B, ctx->VF, dt, ctx->stream));
+        if (any_fct) STAGE(4, b32_bounds(ctx->tp, g, B, dt, ctx->stream));
+        STAGE(6, b32_update(ctx->tp, g, fg, B, ctx->vfac, dt, ctx->stream));
+    }
+    CK(cudaGetLastError());
+    return FESOM_OK;
+}
+#undef STAGE
+
 int launches_per_step(fesom_gpu_ctx *ctx) {
     int n = 0;
+    if (ctx->prec == FESOM_PREC_FP32) {
+        bool any_vd = false;
+        for (int t = 0; t < ctx->ntr; t++) any_vd |= ctx->cfgs[t].i_vert_diff != 0;
+        n = 1 + (any_vd ? 1 : 0);
+        for (int t0 = 0; t0 < ctx->ntr; t0 += ctx->group) {
+            const int nt = std::min(ctx->group, ctx->ntr - t0);
+            bool any_fct = false;
+            for (int t = t0; t < t0 + nt; t++) any_fct |= ctx->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
+            n += 2 + (any_fct ? 1 : 0);
+        }
+        return n;
+    }
     for (int t0 = 0; t0 < ctx->ntr; t0 += ctx->group) {
         const int nt = std::min(ctx->group, ctx->ntr - t0);
         bool any_fct = false, any_ho = false, any_vd = false;
@@ -353,7 +544,7 @@ int launches_per_step(fesom_gpu_ctx *ctx) {
 }
 
 int enqueue_step_any(fesom_gpu_ctx *ctx, double dt) {
-    return ctx->prec == FESOM_PREC_FP32 ? enqueue_step<float>(ctx, dt) : enqueue_step<double>(ctx, dt);
+    return ctx->prec == FESOM_PREC_FP32 ? enqueue_step32(ctx, dt) : enqueue_step<double>(ctx, dt);
 }
 
 int wait_stream(fesom_gpu_ctx *ctx, int timeout_ms) {
@@ -426,6 +617,11 @@ int fesom_gpu_init(const fesom_mesh_desc *mesh, int32_t precision, int32_t max_t
         *out = ctx;  // the caller can read the message, then finalize
         return FESOM_ERR_MESH;
     }
+    if (precision == FESOM_PREC_FP32 && mesh->nl - 1 > 128) {
+        ctx->err = "the FP32 form handles columns of up to 128 layers";
+        *out = ctx;
+        return FESOM_ERR_MESH;
+    }
     ctx->N2 = mesh->nod2D;
     ctx->E2 = mesh->edge2D;
     ctx->T2 = mesh->elem2D;
@@ -493,6 +689,7 @@ int fesom_gpu_mesh_check(const fesom_mesh_desc *mesh, int32_t *nbl, int32_t *upd
 int fesom_gpu_finalize(fesom_gpu_ctx *ctx) {
     if (!ctx) return FESOM_OK;
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+    free_graphs32(ctx);
     for (void *p : ctx->allocs) cudaFree(p);
     delete ctx;
     return FESOM_OK;
@@ -502,6 +699,7 @@ int fesom_gpu_set_stream(fesom_gpu_ctx *ctx, void *stream) {
     if (!ctx) return FESOM_ERR_ARG;
     ctx->stream = (cudaStream_t)stream;
     if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
+    free_graphs32(ctx);
     return FESOM_OK;
 }
 
@@ -641,7 +839,13 @@ int fesom_gpu_state_setup(fesom_gpu_ctx *ctx, int32_t ntr, const fesom_tra_cfg *
             ctx->err = "all tracers of a batch must use the same Adams-Bashforth order";
             return FESOM_ERR_ARG;
         }
-    if ((rc = alloc_state(ctx, ntr, ab_max))) return rc;
+    if (ctx->prec == FESOM_PREC_FP32) {
+        if (!(ctx->state_ready && ctx->ntr == ntr && ctx->ab_max == ab_max) && (rc = alloc_state32(ctx, ntr, ab_max)))
+            return rc;
+        free_graphs32(ctx);
+    } else if ((rc = alloc_state(ctx, ntr, ab_max))) {
+        return rc;
+    }
     ctx->ntr = ntr;
     ctx->cfgs.assign(cfgs, cfgs + ntr);
     std::vector<DCfg> d(ntr);
@@ -700,6 +904,12 @@ int fesom_gpu_tracer_upload(fesom_gpu_ctx *ctx, int32_t tr, const double *values
     int rc = tracer_check(ctx, tr);
     if (rc) return rc;
     const size_t sN = (size_t)ctx->L1 * ctx->N2, rs = rsize(ctx);
+    if (ctx->prec == FESOM_PREC_FP32) {
+        if ((rc = put(ctx, level32(ctx, 0) + sN * tr, values, sN))) return rc;
+        if (!valuesold) return FESOM_OK;
+        if (ctx->ab_max == 2) return put(ctx, level32(ctx, 1) + sN * tr, valuesold, sN);
+        return put_deint(ctx, level32(ctx, 1) + sN * tr, level32(ctx, 2) + sN * tr, valuesold, sN);
+    }
     if ((rc = put(ctx, (char *)ctx->T + rs * sN * tr, values, sN))) return rc;
     return put(ctx, (char *)ctx->Told + rs * sN * (ctx->ab_max - 1) * tr, valuesold, sN * (ctx->ab_max - 1));
 }
@@ -708,6 +918,15 @@ int fesom_gpu_tracer_download(fesom_gpu_ctx *ctx, int32_t tr, double *values, do
     int rc = tracer_check(ctx, tr);
     if (rc) return rc;
     const size_t sN = (size_t)ctx->L1 * ctx->N2, rs = rsize(ctx);
+    if (ctx->prec == FESOM_PREC_FP32) {
+        if ((rc = get(ctx, values, level32(ctx, 0) + sN * tr, sN))) return rc;
+        if (valuesold) {
+            if (ctx->ab_max == 2) rc = get(ctx, valuesold, level32(ctx, 1) + sN * tr, sN);
+            else rc = get_int(ctx, valuesold, level32(ctx, 1) + sN * tr, level32(ctx, 2) + sN * tr, sN);
+            if (rc) return rc;
+        }
+        return wait_stream(ctx, -1);
+    }
     if ((rc = get(ctx, values, (char *)ctx->T + rs * sN * tr, sN))) return rc;
     if ((rc = get(ctx, valuesold, (char *)ctx->Told + rs * sN * (ctx->ab_max - 1) * tr, sN * (ctx->ab_max - 1))))
         return rc;
@@ -719,10 +938,13 @@ int fesom_gpu_tracer_upload_f32(fesom_gpu_ctx *ctx, int32_t tr, const float *val
     if (rc) return rc;
     if (ctx->prec != FESOM_PREC_FP32) { ctx->err = "FP32 buffers need a FESOM_PREC_FP32 context"; return FESOM_ERR_STATE; }
     const size_t sN = (size_t)ctx->L1 * ctx->N2;
-    if (values) CK(cudaMemcpyAsync((float *)ctx->T + sN * tr, values, 4 * sN, cudaMemcpyHostToDevice, ctx->stream));
-    if (valuesold)
-        CK(cudaMemcpyAsync((float *)ctx->Told + sN * (ctx->ab_max - 1) * tr, valuesold, 4 * sN * (ctx->ab_max - 1),
-                           cudaMemcpyHostToDevice, ctx->stream));
+    if (values) CK(cudaMemcpyAsync(level32(ctx, 0) + sN * tr, values, 4 * sN, cudaMemcpyHostToDevice, ctx->stream));
+    if (valuesold) {
+        if (ctx->ab_max == 2)
+            CK(cudaMemcpyAsync(level32(ctx, 1) + sN * tr, valuesold, 4 * sN, cudaMemcpyHostToDevice, ctx->stream));
+        else if ((rc = put_deint_f(ctx, level32(ctx, 1) + sN * tr, level32(ctx, 2) + sN * tr, valuesold, sN)))
+            return rc;
+    }
     return FESOM_OK;
 }
 
@@ -731,10 +953,40 @@ int fesom_gpu_tracer_download_f32(fesom_gpu_ctx *ctx, int32_t tr, float *values,
     if (rc) return rc;
     if (ctx->prec != FESOM_PREC_FP32) { ctx->err = "FP32 buffers need a FESOM_PREC_FP32 context"; return FESOM_ERR_STATE; }
     const size_t sN = (size_t)ctx->L1 * ctx->N2;
-    if (values) CK(cudaMemcpyAsync(values, (float *)ctx->T + sN * tr, 4 * sN, cudaMemcpyDeviceToHost, ctx->stream));
-    if (valuesold)
-        CK(cudaMemcpyAsync(valuesold, (float *)ctx->Told + sN * (ctx->ab_max - 1) * tr, 4 * sN * (ctx->ab_max - 1),
-                           cudaMemcpyDeviceToHost, ctx->stream));
+    if (values) CK(cudaMemcpyAsync(values, level32(ctx, 0) + sN * tr, 4 * sN, cudaMemcpyDeviceToHost, ctx->stream));
+    if (valuesold) {
+        if (ctx->ab_max == 2)
+            CK(cudaMemcpyAsync(valuesold, level32(ctx, 1) + sN * tr, 4 * sN, cudaMemcpyDeviceToHost, ctx->stream));
+        else if ((rc = get_int_f(ctx, valuesold, level32(ctx, 1) + sN * tr, level32(ctx, 2) + sN * tr, sN)))
+            return rc;
+    }
+    return FESOM_OK;
+}
+
+// capture one step (stream-ordered launches) into an executable graph
+static int capture_graph(fesom_gpu_ctx *ctx, double dt, cudaGraphExec_t *out) {
+    cudaStream_t cap = ctx->stream;
+    bool own = false;
+    if (!cap) {  // the legacy stream cannot be captured: capture on a private stream
+        CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        own = true;
+    }
+    cudaStream_t keep = ctx->stream;
+    ctx->stream = cap;
+    cudaGraph_t graph;
+    cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    int rc = FESOM_OK;
+    if (e == cudaSuccess) {
+        rc = enqueue_step_any(ctx, dt);
+        e = cudaStreamEndCapture(cap, &graph);
+    }
+    ctx->stream = keep;
+    if (own) cudaStreamDestroy(cap);
+    if (rc) return rc;
+    if (e != cudaSuccess) { ctx->err = std::string("graph capture: ") + cudaGetErrorString(e); return FESOM_ERR_CUDA; }
+    e = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) { ctx->err = std::string("graph instantiate: ") + cudaGetErrorString(e); return FESOM_ERR_CUDA; }
     return FESOM_OK;
 }
 
@@ -745,6 +997,23 @@ int fesom_gpu_run_steps(fesom_gpu_ctx *ctx, double dt, int32_t nsteps, int32_t u
         return FESOM_ERR_STATE;
     }
     int rc;
+    if (ctx->prec == FESOM_PREC_FP32) {
+        for (int s = 0; s < nsteps; s++) {
+            if (!use_graph) {
+                if ((rc = enqueue_step32(ctx, dt))) return rc;
+            } else {
+                const int r = ctx->rot;
+                if (!ctx->gexec32[r] || ctx->g32_dt[r] != dt) {
+                    if (ctx->gexec32[r]) { cudaGraphExecDestroy(ctx->gexec32[r]); ctx->gexec32[r] = nullptr; }
+                    if ((rc = capture_graph(ctx, dt, &ctx->gexec32[r]))) return rc;
+                    ctx->g32_dt[r] = dt;
+                }
+                CK(cudaGraphLaunch(ctx->gexec32[r], ctx->stream));
+            }
+            rotate32(ctx);
+        }
+        return FESOM_OK;
+    }
     if (!use_graph) {
         for (int s = 0; s < nsteps; s++)
             if ((rc = enqueue_step_any(ctx, dt))) return rc;
@@ -752,25 +1021,7 @@ int fesom_gpu_run_steps(fesom_gpu_ctx *ctx, double dt, int32_t nsteps, int32_t u
     }
     if (!ctx->gexec || ctx->g_dt != dt) {
         if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
-        cudaStream_t cap = ctx->stream;
-        bool own = false;
-        if (!cap) {  // the legacy stream cannot be captured: capture on a private stream
-            CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-            own = true;
-        }
-        cudaStream_t keep = ctx->stream;
-        ctx->stream = cap;
-        cudaGraph_t graph;
-        CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-        rc = enqueue_step_any(ctx, dt);
-        cudaError_t e = cudaStreamEndCapture(cap, &graph);
-        ctx->stream = keep;
-        if (own) cudaStreamDestroy(cap);
-        if (rc) return rc;
-        if (e != cudaSuccess) { ctx->err = std::string("graph capture: ") + cudaGetErrorString(e); return FESOM_ERR_CUDA; }
-        e = cudaGraphInstantiate(&ctx->gexec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (e != cudaSuccess) { ctx->err = std::string("graph instantiate: ") + cudaGetErrorString(e); return FESOM_ERR_CUDA; }
+        if ((rc = capture_graph(ctx, dt, &ctx->gexec))) return rc;
         ctx->g_dt = dt;
     }
     for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(ctx->gexec, ctx->stream));
@@ -812,12 +1063,14 @@ int fesom_gpu_set_tracers_per_launch(fesom_gpu_ctx *ctx, int32_t n) {
     if (!ctx->state_ready) { ctx->err = "call fesom_gpu_state_setup first"; return FESOM_ERR_STATE; }
     ctx->group = n == 0 ? ctx->group_cap : std::min((int)n, ctx->group_cap);
     if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
+    free_graphs32(ctx);
     return FESOM_OK;
 }
 
 int fesom_gpu_debug_fetch(fesom_gpu_ctx *ctx, const char *name, int32_t tr, double *out, size_t count) {
     if (!ctx || !name || !out) return FESOM_ERR_ARG;
     if (!ctx->state_ready) { ctx->err = "no tracer state"; return FESOM_ERR_STATE; }
+    if (ctx->prec != FESOM_PREC_FP64) { ctx->err = "work arrays are exposed for FP64 contexts"; return FESOM_ERR_STATE; }
     const size_t sN = (size_t)ctx->L1 * ctx->N2, sNI = (size_t)ctx->nl * ctx->N2;
     const size_t sE = (size_t)ctx->L1 * ctx->E2, sT = 2 * (size_t)ctx->L1 * ctx->T2;
     const std::string n(name);
@@ -861,7 +1114,8 @@ int fesom_gpu_profile_step(fesom_gpu_ctx *ctx, double dt, float *stage_ms, int32
     StageTimer *tm = new StageTimer();
     const int nev = 2 * FESOM_NUM_STAGES * 64;
     for (int i = 0; i < nev; i++) cudaEventCreate(&tm->ev[i]);
-    int rc = ctx->prec == FESOM_PREC_FP32 ? enqueue_step<float>(ctx, dt, tm) : enqueue_step<double>(ctx, dt, tm);
+    int rc = ctx->prec == FESOM_PREC_FP32 ? enqueue_step32(ctx, dt, tm) : enqueue_step<double>(ctx, dt, tm);
+    if (!rc && ctx->prec == FESOM_PREC_FP32) rotate32(ctx);
     if (!rc) rc = wait_stream(ctx, -1);
     for (int i = 0; i < FESOM_NUM_STAGES; i++) { stage_ms[i] = 0.f; launches[i] = 0; }
     if (!rc)
@@ -880,7 +1134,10 @@ int fesom_gpu_tracer_content(fesom_gpu_ctx *ctx, double *content) {
     if (!ctx || !content) return FESOM_ERR_ARG;
     if (!ctx->state_ready) { ctx->err = "no tracer state"; return FESOM_ERR_STATE; }
     if (ctx->prec == FESOM_PREC_FP32) {
-        DTracers<float> tr = group_view<float>(ctx, 0, ctx->ntr);
+        DTracers<float> tr{};
+        tr.ntr = ctx->ntr;
+        tr.sN = (size_t)ctx->L1 * ctx->N2;
+        tr.T = level32(ctx, 0);
         Launch<float>::content(ctx->tp, ctx->g32, tr, ctx->partials, ctx->content_blocks, ctx->content_out, ctx->stream);
     } else {
         DTracers<double> tr = group_view<double>(ctx, 0, ctx->ntr);
@@ -895,6 +1152,11 @@ int fesom_gpu_tracer_device_ptr(fesom_gpu_ctx *ctx, int32_t tr, void **values, v
     int rc = tracer_check(ctx, tr);
     if (rc) return rc;
     const size_t sN = (size_t)ctx->L1 * ctx->N2, rs = rsize(ctx);
+    if (ctx->prec == FESOM_PREC_FP32) {
+        if (values) *values = level32(ctx, 0) + sN * tr;
+        if (valuesold) *valuesold = level32(ctx, 1) + sN * tr;
+        return FESOM_OK;
+    }
     if (values) *values = (char *)ctx->T + rs * sN * tr;
     if (valuesold) *valuesold = (char *)ctx->Told + rs * sN * (ctx->ab_max - 1) * tr;
     return FESOM_OK;

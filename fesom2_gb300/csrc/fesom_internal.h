@@ -76,6 +76,35 @@ struct DTracers {
     unsigned *status;
 };
 
+// FP32 batched form (kernels_fp32_batched.cu): one step's view of the tracer state.
+// T / O1 / O2 are the current and previous time levels (rotated each step, no copy);
+// the step writes the new values into Tnew (the buffer of the oldest level).
+struct B32View {
+    int ntr, ab;
+    size_t sN, sNI, sE;
+    const float *T, *O1, *O2;
+    float *Tnew;
+    float *LOi;      // LO increment: low-order flux divergence * dt / areasvol
+    float *ADv;      // antidiffusive (or, without limiter, high-order) vertical flux
+    float *ADh;      // the same for edges, written by the edge's first node
+    float *Rp, *Rm;  // FCT ratios R+ / R-
+    float *Tup, *Tlo;  // FCT bounds of the advected value (LO + bmax, LO + bmin)
+    const DCfg *cfg;
+    unsigned *status;
+};
+// FP32 copies of the FP64 factorisation of each column's vertical-diffusion matrix
+struct VFactors {
+    float *a, *c, *inv, *cp;
+};
+void b32_vflux(const DTopo &, const DGeom<float> &, const DForcing<float> &, float *VF, cudaStream_t);
+void b32_vfactors(const DTopo &, const DGeom<float> &, const DForcing<float> &, double dt, const VFactors &,
+                  cudaStream_t);
+void b32_lo_ad(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, const float *VF,
+               double dt, cudaStream_t);
+void b32_bounds(const DTopo &, const DGeom<float> &, const B32View &, double dt, cudaStream_t);
+void b32_update(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, const VFactors &,
+                double dt, cudaStream_t);
+
 // launch wrappers (kernels_fp64.cu / kernels_fp32.cu)
 template <typename R>
 struct Launch {

@@ -24,7 +24,7 @@ VER = {"QR4C": 0, "UPW1": 1, "CDIFF": 2, "PPM": 3}
 LIM = {"NON": 0, "FCT": 1}
 ERRORS = {1: "ARG", 2: "SCHEME", 3: "MESH", 4: "CUDA", 5: "NOMEM", 6: "TIMEOUT", 7: "NUMERIC", 8: "STATE"}
 STATUS_NAN, STATUS_FCT_BOUND, STATUS_INDEX = 1, 2, 4
-STAGES = ["ab", "trxy", "edge_flux", "node_lo", "bounds", "rpm", "update", "vdiff"]
+STAGES = ["ab", "trxy", "edge_flux", "node_lo", "bounds", "rpm", "update", "vdiff", "vflux", "vfactors", "lo_ad"]
 STAGES_N = len(STAGES)
 
 
@@ -266,15 +266,22 @@ class Context:
             self._chk(self.L.fesom_gpu_forcing_upload(self.h, *[_p(a) for a in self._fk]))
 
     def tracer_upload(self, tr: int, values, valuesold):
+        ab = int(self._cfgs[0].ab_order) if getattr(self, "_cfgs", None) else 2
+        N2, L1 = self.mesh.nod2D, self.mesh.nl - 1
+        if values.size != N2 * L1 or valuesold.size != N2 * L1 * (ab - 1):
+            raise ValueError("values must hold (nod2D, nl-1) and valuesold (ab_order-1)*(nod2D, nl-1) entries")
         if values.dtype == np.float32:
             self._chk(self.L.fesom_gpu_tracer_upload_f32(self.h, tr, _p(values), _p(valuesold)))
         else:
             self._chk(self.L.fesom_gpu_tracer_upload(self.h, tr, _p(_c64(values)), _p(_c64(valuesold))))
 
     def tracer_download(self, tr: int, dtype=np.float64):
+        """values (nod2D, nl-1) and valuesold in the reference's layout: (nod2D, nl-1)
+        for AB2, (nod2D, nl-1, 2) for AB3 (valuesold(1:2, nz, n))."""
         N2, L1 = self.mesh.nod2D, self.mesh.nl - 1
+        ab = int(self._cfgs[0].ab_order) if getattr(self, "_cfgs", None) else 2
         v = np.zeros((N2, L1), dtype=dtype)
-        o = np.zeros((N2, L1), dtype=dtype)
+        o = np.zeros((N2, L1) if ab == 2 else (N2, L1, ab - 1), dtype=dtype)
         if dtype == np.float32:
             self._chk(self.L.fesom_gpu_tracer_download_f32(self.h, tr, _p(v), _p(o)))
             self.status()

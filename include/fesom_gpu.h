@@ -202,8 +202,9 @@ int fesom_gpu_set_tracers_per_launch(fesom_gpu_ctx *ctx, int32_t n);
  * context stream; stage_ms[i] receives the summed time of stage i over all
  * tracer groups and launches[i] the number of launches (arrays of
  * FESOM_NUM_STAGES entries, stage order: ab, trxy, edge_flux, node_lo,
- * bounds, rpm, update, vdiff). */
-#define FESOM_NUM_STAGES 8
+ * bounds, rpm, update, vdiff, vflux, vfactors, lo_ad; the FP64 form uses the
+ * first eight, the FP32 form vflux, vfactors, lo_ad, bounds, update). */
+#define FESOM_NUM_STAGES 11
 int fesom_gpu_profile_step(fesom_gpu_ctx *ctx, double dt, float *stage_ms, int32_t *launches);
 /* Copy of an internal per-tracer work array of tracer slot tr (FP64 contexts,
  * for testing): name is one of "T", "Told", "TAB", "trxy", "FLO", "ADh", "LO",

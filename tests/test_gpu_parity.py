@@ -218,3 +218,62 @@ def test_errors_are_reported(channel_small):
     with pytest.raises(G.FesomGpuError) as e:
         ctx.run_steps(600.0, 1)
     assert e.value.rc == 8
+
+
+FP32_SCHEMES = [("MUSCL", "QR4C", "FCT", 2), ("MFCT", "UPW1", "FCT", 3), ("UPW1", "QR4C", "NON", 2),
+                ("MUSCL", "QR4C", "NON", 3)]
+
+
+@pytest.mark.parametrize("scheme", FP32_SCHEMES, ids=["-".join(map(str, s)) for s in FP32_SCHEMES])
+def test_fp32_schemes_and_ab_orders_vs_oracle(sphere_small, scheme):
+    """FP32 batched form, 3 steps of every scheme family and AB order, against the
+    FP64 oracle started from the same (FP32-rounded) state: normwise error <= 1e-5."""
+    hor, ver, lim, ab = scheme
+    mesh = sphere_small
+    f, tr = _setup(mesh, "sphere", ntr=3)
+    rng = np.random.default_rng(4)
+    cfgs = [G.tra_cfg(hor, ver, lim, 0.0, 1.0, ab_order=ab, id=k + 1) for k in range(3)]
+    ocfg = O.cfg_struct(hor, ver, lim, 0.0, 1.0, ab_order=ab)
+    om = O.OracleMesh(mesh)
+    wet = wet_mask(mesh)
+    ctx = G.Context(mesh, G.PREC_FP32, max_tracers=3)
+    ctx.state_setup(cfgs)
+    ctx.forcing_upload(f)
+    T64, O64 = [], []
+    for k in range(3):
+        T = tr[k].astype(np.float32).astype(np.float64)
+        old = np.stack([T * (1 + 1e-3 * rng.standard_normal(T.shape)) for _ in range(ab - 1)], axis=-1)
+        old = np.ascontiguousarray(old.astype(np.float32).astype(np.float64))
+        ctx.tracer_upload(k, T, old)
+        T64.append(T.copy())
+        O64.append(old.copy())
+    for step in range(3):
+        ctx.run_steps(f.dt, 1, use_graph=(step % 2 == 1))
+        for k in range(3):
+            om.tracer_step(f, ocfg, T64[k], np.zeros_like(T64[k]), O64[k])
+    for k in range(3):
+        v, o = ctx.tracer_download(k)
+        err = np.abs(v[wet] - T64[k][wet]).max() / np.abs(T64[k][wet]).max()
+        assert err <= 1e-5, (k, err)
+        # the previous time levels come back in the caller's valuesold layout
+        assert np.abs(o.reshape(-1)[:8] - O64[k].reshape(-1)[:8]).max() <= 1e-5 * np.abs(O64[k]).max()
+    assert ctx.status() == 0
+
+
+def test_fp32_graph_replay_equals_direct_launches(channel_seamount):
+    mesh = channel_seamount
+    f, tr = _setup(mesh, "channel", ntr=2)
+    cfgs = [G.tra_cfg(id=1), G.tra_cfg(id=2)]
+    out = []
+    for use_graph in (False, True):
+        ctx = G.Context(mesh, G.PREC_FP32, max_tracers=2)
+        ctx.state_setup(cfgs)
+        ctx.forcing_upload(f)
+        for k in range(2):
+            ctx.tracer_upload(k, tr[k].astype(np.float32), tr[k].astype(np.float32))
+        ctx.run_steps(f.dt, 5, use_graph=use_graph)
+        out.append([ctx.tracer_download(k, dtype=np.float32) for k in range(2)])
+        ctx.close()
+    for k in range(2):
+        assert np.array_equal(out[0][k][0], out[1][k][0])
+        assert np.array_equal(out[0][k][1], out[1][k][1])
