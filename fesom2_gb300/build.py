@@ -25,6 +25,8 @@ UNITS = {
     "kernels_fp32.cu": [],
     "kernels_fp32_batched.cu": [],
     "capi.cu": [],
+    # allocation-free vertical diffusion: FP64, same rounding as kernels_fp64.cu
+    "vdiff_noalloc.cu": ["--fmad=false"],
 }
 HOST_UNITS = ["mesh_prep.cpp"]
 

@@ -213,6 +213,29 @@ int fesom_gpu_profile_step(fesom_gpu_ctx *ctx, double dt, float *stage_ms, int32
 int fesom_gpu_debug_fetch(fesom_gpu_ctx *ctx, const char *name, int32_t tr, double *out, size_t count);
 /* Kernel launches one device-resident step issues. */
 int fesom_gpu_launches_per_step(fesom_gpu_ctx *ctx, int32_t *launches);
+/* ---- allocation-free vertical diffusion ----------------------------------- */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc:
+ * FESOM2's OpenACC build, whose `!$ACC DATA` regions own every device array
+ * and pass them out as device addresses (`!$ACC HOST_DATA USE_DEVICE`), and
+ * codes held to a fixed device-memory budget.  Same computation as
+ * fesom_gpu_vdiff_impl (diff_ver_part_impl_ale, FP64, bit-identical results)
+ * on arrays the caller already holds on the current device -- every pointer is
+ * a DEVICE pointer in the layout of fesom_mesh_desc -- with no context and no
+ * allocation: the column-solve scratch is a fixed device array inside the
+ * library, FESOM_GPU_NOALLOC_SCRATCH_DOUBLES doubles (32 MiB, held by every
+ * GPU that loads the library until the process exits).  Meshes with
+ * 3*nl*nod2D above that are rejected with FESOM_ERR_ARG and a message in
+ * errbuf.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * All calls share the scratch: calls that overlap on the GPU race.  The work
+ * is queued on `stream` (a cudaStream_t, NULL = legacy stream); the caller
+ * synchronizes. */
+#define FESOM_GPU_NOALLOC_SCRATCH_DOUBLES ((size_t)4194304)
+int fesom_gpu_vdiff_impl_noalloc(int32_t nod2D, int32_t nl, const int32_t *nlevels_nod2D,
+                                 const int32_t *ulevels_nod2D, const double *zbar_n_bot, const double *hnode_new,
+                                 const double *area, const double *areasvol, const double *Kv, const double *bc_surf,
+                                 double dt, double *values, void *stream, char *errbuf, int32_t errlen);
+
 /* Global content sum_nodes sum_levels values*hnode_new*areasvol per tracer, in FP64. */
 int fesom_gpu_tracer_content(fesom_gpu_ctx *ctx, double *content);
 /* Device pointer of tracer tr's values (context precision), for zero-copy users. */
