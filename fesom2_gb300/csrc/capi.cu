@@ -57,8 +57,9 @@ struct fesom_gpu_ctx {
     int rot = 0;
     float *VF = nullptr;
     VFactors vfac{};
-    float *LOi = nullptr, *ADv32 = nullptr, *ADh32 = nullptr, *Rp = nullptr, *Rm = nullptr;
-    float *Tup = nullptr, *Tlo = nullptr;
+    float *LOi = nullptr, *ADv32 = nullptr, *ADh32 = nullptr;
+    float2 *R2 = nullptr, *TB2 = nullptr;
+    MusclW mw{};
     cudaGraphExec_t gexec32[3] = {nullptr, nullptr, nullptr};
     double g32_dt[3] = {0.0, 0.0, 0.0};
 };
@@ -248,6 +249,62 @@ int init_geom(fesom_gpu_ctx *ctx, const fesom_mesh_desc *d, DGeom<R> &g) {
     return FESOM_OK;
 }
 
+// Per-edge reconstruction data of the FP32 form (see MusclW): the triangle gradient
+// projected on the edge, edge_dxdy(1)*a*gx + edge_dxdy(2)*r_earth*gy, as weights of the
+// triangle's three node values (gradient_sca, src/oce_mesh.F90:2644-2666), in FP64.
+int init_muscl_weights(fesom_gpu_ctx *ctx, const fesom_mesh_desc *d) {
+    const HostTopo &h = ctx->ht;
+    const int E2 = ctx->E2;
+    for (int n = 0; n < ctx->N2; n++)
+        if (h.ne_ptr[n + 1] - h.ne_ptr[n] > kMaxDeg) {
+            ctx->err = "the FP32 form handles nodes with at most 16 edges";
+            return FESOM_ERR_MESH;
+        }
+    std::vector<int4> un(E2), dn(E2);
+    std::vector<float4> wu(E2), wd(E2);
+    for (int e = 0; e < E2; e++) {
+        const int n1 = h.e_n1[e], n2 = h.e_n2[e], el1 = h.e_t1[e], el2 = h.e_t2[e];
+        double a = kREarth * d->elem_cos[el1];
+        if (el2 >= 0) a = 0.5 * (a + kREarth * d->elem_cos[el2]);
+        const double ex = d->edge_dxdy[2 * (size_t)e], ey = d->edge_dxdy[2 * (size_t)e + 1];
+        const int up = h.e_up[e], dw = h.e_dn[e];
+        int gzmin = 1, gzmax = 0;
+        if (up >= 0 && dw >= 0) {
+            gzmin = std::max(h.n_ulevmax[n1], h.n_ulevmax[n2]);
+            gzmax = std::min(h.n_nlevmin[n1], h.n_nlevmin[n2]);
+        }
+        auto tri = [&](int el, int node, int4 &nn, float4 &ww) {
+            if (el < 0) {
+                nn = make_int4(node, node, node, 0);
+                ww = make_float4(0.f, 0.f, 0.f, (float)a);
+                return;
+            }
+            const double *gs = d->gradient_sca + 6 * (size_t)el;
+            nn = make_int4(h.t_n[3 * (size_t)el], h.t_n[3 * (size_t)el + 1], h.t_n[3 * (size_t)el + 2], 0);
+            ww = make_float4((float)(ex * a * gs[0] + ey * kREarth * gs[3]), (float)(ex * a * gs[1] + ey * kREarth * gs[4]),
+                             (float)(ex * a * gs[2] + ey * kREarth * gs[5]), (float)a);
+        };
+        tri(up, n1, un[e], wu[e]);
+        tri(dw, n2, dn[e], wd[e]);
+        un[e].w = gzmin | (gzmax << 16);
+    }
+    int rc;
+    void *p;
+    if ((rc = dalloc(ctx, &p, sizeof(int4) * E2))) return rc;
+    CK(cudaMemcpy(p, un.data(), sizeof(int4) * E2, cudaMemcpyHostToDevice));
+    ctx->mw.un = (const int4 *)p;
+    if ((rc = dalloc(ctx, &p, sizeof(int4) * E2))) return rc;
+    CK(cudaMemcpy(p, dn.data(), sizeof(int4) * E2, cudaMemcpyHostToDevice));
+    ctx->mw.dn = (const int4 *)p;
+    if ((rc = dalloc(ctx, &p, sizeof(float4) * E2))) return rc;
+    CK(cudaMemcpy(p, wu.data(), sizeof(float4) * E2, cudaMemcpyHostToDevice));
+    ctx->mw.wu = (const float4 *)p;
+    if ((rc = dalloc(ctx, &p, sizeof(float4) * E2))) return rc;
+    CK(cudaMemcpy(p, wd.data(), sizeof(float4) * E2, cudaMemcpyHostToDevice));
+    ctx->mw.wd = (const float4 *)p;
+    return FESOM_OK;
+}
+
 int check_cfg(fesom_gpu_ctx *ctx, const fesom_tra_cfg *c) {
     if (!c) { ctx->err = "null tracer configuration"; return FESOM_ERR_ARG; }
     if (c->adv_hor < 0 || c->adv_hor > 2) { ctx->err = "unknown horizontal advection scheme"; return FESOM_ERR_SCHEME; }
@@ -385,10 +442,11 @@ void free_graphs32(fesom_gpu_ctx *ctx) {
 int alloc_state32(fesom_gpu_ctx *ctx, int ntr, int ab) {
     const size_t sN = (size_t)ctx->L1 * ctx->N2, sNI = (size_t)ctx->nl * ctx->N2, sE = (size_t)ctx->L1 * ctx->E2;
     void *old[] = {ctx->Bf[0], ctx->Bf[1], ctx->Bf[2], ctx->VF, ctx->vfac.a, ctx->vfac.c, ctx->vfac.inv, ctx->vfac.cp,
-                   ctx->LOi, ctx->ADv32, ctx->ADh32, ctx->Rp, ctx->Rm, ctx->Tup, ctx->Tlo, ctx->d_cfg, ctx->bc};
+                   ctx->LOi, ctx->ADv32, ctx->ADh32, ctx->R2, ctx->TB2, ctx->d_cfg, ctx->bc};
     for (void *b : old) { void *p = b; dfree(ctx, p); }
     ctx->Bf[0] = ctx->Bf[1] = ctx->Bf[2] = nullptr;
-    ctx->VF = ctx->LOi = ctx->ADv32 = ctx->ADh32 = ctx->Rp = ctx->Rm = ctx->Tup = ctx->Tlo = nullptr;
+    ctx->VF = ctx->LOi = ctx->ADv32 = ctx->ADh32 = nullptr;
+    ctx->R2 = ctx->TB2 = nullptr;
     ctx->vfac = VFactors{};
     ctx->d_cfg = nullptr;
     ctx->bc = nullptr;
@@ -404,7 +462,7 @@ int alloc_state32(fesom_gpu_ctx *ctx, int ntr, int ab) {
     float **fac[] = {&ctx->vfac.a, &ctx->vfac.c, &ctx->vfac.inv, &ctx->vfac.cp};
     for (float **f : fac)
         if ((rc = dalloc(ctx, (void **)f, 4 * sN))) return rc;
-    const size_t per_tracer = 4 * (5 * sN + sNI + sE);
+    const size_t per_tracer = 4 * (5 * sN + sNI + sE);  // LO increment, (R+,R-), bounds, ADv, ADh
     size_t fr = 0, tot = 0;
     CK(cudaMemGetInfo(&fr, &tot));
     const int g = (int)std::min<size_t>((size_t)ntr, std::max<size_t>(1, (size_t)(0.85 * fr) / per_tracer));
@@ -412,10 +470,8 @@ int alloc_state32(fesom_gpu_ctx *ctx, int ntr, int ab) {
     if ((rc = dalloc(ctx, (void **)&ctx->LOi, 4 * sN * g))) return rc;
     if ((rc = dalloc(ctx, (void **)&ctx->ADv32, 4 * sNI * g))) return rc;
     if ((rc = dalloc(ctx, (void **)&ctx->ADh32, 4 * sE * g))) return rc;
-    if ((rc = dalloc(ctx, (void **)&ctx->Rp, 4 * sN * g))) return rc;
-    if ((rc = dalloc(ctx, (void **)&ctx->Rm, 4 * sN * g))) return rc;
-    if ((rc = dalloc(ctx, (void **)&ctx->Tup, 4 * sN * g))) return rc;
-    if ((rc = dalloc(ctx, (void **)&ctx->Tlo, 4 * sN * g))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->R2, 8 * sN * g))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->TB2, 8 * sN * g))) return rc;
     ctx->rot = 0;
     ctx->ntr = ntr;
     ctx->ab_max = ab;
@@ -437,10 +493,8 @@ B32View view32(fesom_gpu_ctx *ctx, int t0, int nt) {
     v.LOi = ctx->LOi;
     v.ADv = ctx->ADv32;
     v.ADh = ctx->ADh32;
-    v.Rp = ctx->Rp;
-    v.Rm = ctx->Rm;
-    v.Tup = ctx->Tup;
-    v.Tlo = ctx->Tlo;
+    v.R = ctx->R2;
+    v.TB = ctx->TB2;
     v.cfg = ctx->d_cfg + t0;
     v.status = ctx->status;
     return v;
@@ -507,7 +561,7 @@ int enqueue_step32(fesom_gpu_ctx *ctx, double dt, StageTimer *tm = nullptr) {
         DForcing<float> fg = forcing_view<float>(ctx, t0);
         bool any_fct = false;
         for (int t = t0; t < t0 + nt; t++) any_fct |= ctx->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
-        STAGE(10, b32_lo_ad(ctx->tp, g, fg, B, ctx->VF, dt, ctx->stream));
+        STAGE(10, b32_lo_ad(ctx->tp, g, fg, B, ctx->mw, ctx->VF, dt, ctx->stream));
         if (any_fct) STAGE(4, b32_bounds(ctx->tp, g, B, dt, ctx->stream));
         STAGE(6, b32_update(ctx->tp, g, fg, B, ctx->vfac, dt, ctx->stream));
     }
@@ -649,6 +703,7 @@ int fesom_gpu_init(const fesom_mesh_desc *mesh, int32_t precision, int32_t max_t
     if (precision == FESOM_PREC_FP32) rc = init_geom<float>(ctx, mesh, ctx->g32);
     else rc = init_geom<double>(ctx, mesh, ctx->g64);
     if (rc) return rc;
+    if (precision == FESOM_PREC_FP32 && (rc = init_muscl_weights(ctx, mesh))) return rc;
     const size_t rs = rsize(ctx);
     if ((rc = dalloc(ctx, &ctx->uv, rs * 2 * (size_t)ctx->L1 * ctx->T2))) return rc;
     if ((rc = dalloc(ctx, &ctx->w, rs * (size_t)ctx->nl * ctx->N2))) return rc;

@@ -87,10 +87,21 @@ struct B32View {
     float *LOi;      // LO increment: low-order flux divergence * dt / areasvol
     float *ADv;      // antidiffusive (or, without limiter, high-order) vertical flux
     float *ADh;      // the same for edges, written by the edge's first node
-    float *Rp, *Rm;  // FCT ratios R+ / R-
-    float *Tup, *Tlo;  // FCT bounds of the advected value (LO + bmax, LO + bmin)
+    float2 *R;       // FCT ratios (R+, R-)
+    float2 *TB;      // FCT bounds of the advected value (LO + bmax, LO + bmin)
     const DCfg *cfg;
     unsigned *status;
+};
+// Node degree bound of the FP32 form (the node's edge list is staged in shared memory)
+constexpr int kMaxDeg = 16;
+// Per-edge MUSCL/MFCT reconstruction data of the FP32 form, precomputed at init:
+// un / dn = nodes of the up (of edges(1,e)) and down (of edges(2,e)) triangle, with
+// un.w = gzmin | gzmax << 16 (levels where the triangle gradients apply, 0 if none);
+// wu / wd = weights so that sum_k wu_k T(un_k) = edge_dxdy(1)*a*gx + edge_dxdy(2)*r_earth*gy
+// of the triangle gradient (oce_adv_tra_hor.F90:446-461), wu.w = a (r_earth * mean elem_cos)
+struct MusclW {
+    const int4 *un, *dn;
+    const float4 *wu, *wd;
 };
 // FP32 copies of the FP64 factorisation of each column's vertical-diffusion matrix
 struct VFactors {
@@ -99,8 +110,8 @@ struct VFactors {
 void b32_vflux(const DTopo &, const DGeom<float> &, const DForcing<float> &, float *VF, cudaStream_t);
 void b32_vfactors(const DTopo &, const DGeom<float> &, const DForcing<float> &, double dt, const VFactors &,
                   cudaStream_t);
-void b32_lo_ad(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, const float *VF,
-               double dt, cudaStream_t);
+void b32_lo_ad(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, const MusclW &,
+               const float *VF, double dt, cudaStream_t);
 void b32_bounds(const DTopo &, const DGeom<float> &, const B32View &, double dt, cudaStream_t);
 void b32_update(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, const VFactors &,
                 double dt, cudaStream_t);

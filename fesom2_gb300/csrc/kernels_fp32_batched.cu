@@ -38,6 +38,8 @@ namespace {
 constexpr int kW = 4;                 // warps per block
 constexpr int kT = 32 * kW;
 constexpr unsigned kFull = 0xffffffffu;
+constexpr int kU = 8;                 // neighbours per unrolled group
+constexpr int kMaxChunks = 4;         // columns up to 128 layers
 
 __device__ __forceinline__ size_t i1(int nz, int n, int L1) { return (size_t)n * L1 + (nz - 1); }
 __device__ __forceinline__ size_t iN(int nz, int n, int nl) { return (size_t)n * nl + (nz - 1); }
@@ -51,12 +53,6 @@ struct Kahan {
     }
     __device__ __forceinline__ float get() const { return s + c; }
 };
-
-__device__ __forceinline__ float ab_value(const B32View &B, size_t i, int t) {
-    const float v = B.T[t * B.sN + i];
-    if (B.ab == 2) return -(0.6f * B.O1[t * B.sN + i]) + 1.6f * v;
-    return (5.0f * B.O2[t * B.sN + i] - 16.0f * B.O1[t * B.sN + i] + 23.0f * v) * (1.0f / 12.0f);
-}
 
 // upwind vertical flux with velocity W at interface nz (statement order of
 // adv_tra_ver_upw1: surface, bottom, interior), fin = 0
@@ -153,155 +149,181 @@ __global__ void __launch_bounds__(128) k32_vfactors(DTopo tp, DGeom<float> g, DF
 }
 
 // ---------------------------------------------------------------------------
-// gradients of the element tracer field for the MUSCL / MFCT reconstruction
+// per-node staging: the node's edge list in shared memory, once per node
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void tri_grad(const DTopo &tp, const DGeom<float> &g, const float *T, int el, int nz,
-                                         float &gx, float &gy) {
-    const int L1 = tp.L1;
-    const int a = tp.t_n[3 * el], b = tp.t_n[3 * el + 1], c = tp.t_n[3 * el + 2];
-    const float *gs = g.gs + 6 * (size_t)el;
-    const float ta = T[i1(nz, a, L1)], tb = T[i1(nz, b, L1)], tc = T[i1(nz, c, L1)];
-    gx = gs[0] * ta + gs[1] * tb + gs[2] * tc;
-    gy = gs[3] * ta + gs[4] * tb + gs[5] * tc;
+struct NodeEdges {
+    int e[kMaxDeg], m[kMaxDeg], lo[kMaxDeg], hi[kMaxDeg];
+    unsigned own;  // bit j: the node is edges(1, e_j) (it owns the edge flux)
+    int deg, nzmin, nzmax;
+};
+
+__device__ __forceinline__ void stage_node(const DTopo &tp, int n, NodeEdges &S) {
+    const int k0 = tp.ne_ptr[n];
+    const int deg = tp.ne_ptr[n + 1] - k0;
+    if (threadIdx.x < deg && threadIdx.x < kMaxDeg) {
+        const int j = threadIdx.x;
+        const int code = tp.ne_idx[k0 + j];
+        const int e = code >= 0 ? code : ~code;
+        S.e[j] = e;
+        S.m[j] = code >= 0 ? tp.e_n2[e] : tp.e_n1[e];
+        S.lo[j] = tp.e_lo[e];
+        S.hi[j] = tp.e_hi[e];
+    }
+    if (threadIdx.x == 32) {
+        unsigned own = 0;
+        for (int j = 0; j < deg && j < kMaxDeg; j++)
+            if (tp.ne_idx[k0 + j] >= 0) own |= 1u << j;
+        S.own = own;
+        S.deg = deg;
+        S.nzmin = tp.n_ulev[n];
+        S.nzmax = tp.n_nlev[n];
+    }
 }
 
-__device__ __forceinline__ void node_grad(const DTopo &tp, const DGeom<float> &g, const float *T, int node, int nz,
-                                          float &gx, float &gy) {
+// area-weighted mean over the node's wet elements of the element gradient,
+// projected on the edge: ex*a*gx + ey*R*gy (fill_up_dn_grad node means)
+__device__ __noinline__ float node_grad_proj(const DTopo &tp, const DGeom<float> &g, const float *T, int node, int nz,
+                                             float exa, float eyr) {
+    const int L1 = tp.L1;
     float tvol = 0.f, tx = 0.f, ty = 0.f;
     for (int k = tp.nie_ptr[node]; k < tp.nie_ptr[node + 1]; k++) {
         const int el = tp.nie_idx[k];
         if (tp.t_nlev[el] - 1 < nz || nz < tp.t_ulev[el]) continue;
-        float ex, ey;
-        tri_grad(tp, g, T, el, nz, ex, ey);
+        const int a = tp.t_n[3 * el], b = tp.t_n[3 * el + 1], c = tp.t_n[3 * el + 2];
+        const float *gs = g.gs + 6 * (size_t)el;
+        const float ta = T[i1(nz, a, L1)], tb = T[i1(nz, b, L1)], tc = T[i1(nz, c, L1)];
         const float ea = g.elem_area[el];
         tvol += ea;
-        tx += ex * ea;
-        ty += ey * ea;
+        tx += (gs[0] * ta + gs[1] * tb + gs[2] * tc) * ea;
+        ty += (gs[3] * ta + gs[4] * tb + gs[5] * tc) * ea;
     }
-    gx = tx / tvol;
-    gy = ty / tvol;
+    return exa * (tx / tvol) + eyr * (ty / tvol);
 }
 
 // ---------------------------------------------------------------------------
 // k32_lo_ad
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kT)
-k32_lo_ad(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, const float *VF, float dt) {
+k32_lo_ad(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, MusclW mw, const float *VF, float dt) {
+    __shared__ NodeEdges S;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int L1 = tp.L1, nl = tp.nl;
     const float RE = (float)kREarth;
-    for (int n = blockIdx.x * kW + warp; n < tp.N2; n += gridDim.x * kW) {
-        const int nzmin = tp.n_ulev[n], nzmax = tp.n_nlev[n];
-        const int k0 = tp.ne_ptr[n], k1 = tp.ne_ptr[n + 1];
-        for (int t = 0; t < B.ntr; t++) {
+    for (int n = blockIdx.x; n < tp.N2; n += gridDim.x) {
+        __syncthreads();
+        stage_node(tp, n, S);
+        __syncthreads();
+        const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
+        for (int t = warp; t < B.ntr; t += kW) {
             const DCfg c = B.cfg[t];
             const int fct = c.lim;
             const float *T = B.T + t * B.sN;
+            const float *O1 = B.O1 + t * B.sN;
+            const float *O2 = B.ab == 3 ? B.O2 + t * B.sN : nullptr;
+            auto tab = [&](size_t i) {
+                const float v = T[i];
+                return B.ab == 2 ? -(0.6f * O1[i]) + 1.6f * v : (5.0f * O2[i] - 16.0f * O1[i] + 23.0f * v) * (1.0f / 12.0f);
+            };
             for (int nz = nzmin + lane; nz <= nzmax; nz += 32) {
-                // vertical: LO flux with w_e at nz and nz+1, HO flux with w (FCT) / w_e on AB values
                 float fv0 = 0.f, fv1 = 0.f;
                 if (fct) {
                     fv0 = vupw(T, f.we, g.area, nz, n, nzmin, nzmax, L1, nl);
                     if (nz <= nzmax - 1) fv1 = vupw(T, f.we, g.area, nz + 1, n, nzmin, nzmax, L1, nl);
                 }
                 const float *pw = fct ? f.w : f.we;
+                const float ar = g.area[iN(nz, n, nl)];
                 float ho;
-                if (c.ver == 0) {
-                    // QR4C (adv_tra_ver_qr4c statement order)
-                    if (nz == nzmin) {
-                        ho = -(ab_value(B, i1(nz, n, L1), t) * pw[iN(nz, n, nl)] * g.area[iN(nz, n, nl)]);
-                    } else if (nz == nzmax) {
-                        ho = 0.f;
-                    } else if (nz == nzmin + 1 || nz == nzmax - 1) {
-                        ho = -(0.5f * (ab_value(B, i1(nz - 1, n, L1), t) + ab_value(B, i1(nz, n, L1), t)) *
-                               pw[iN(nz, n, nl)] * g.area[iN(nz, n, nl)]);
+                if (nz == nzmax) {
+                    ho = 0.f;
+                } else if (nz == nzmin) {
+                    ho = -(tab(i1(nz, n, L1)) * pw[iN(nz, n, nl)] * ar);
+                } else if (c.ver != 0 || nz == nzmin + 1 || nz == nzmax - 1) {
+                    const float w = pw[iN(nz, n, nl)];
+                    const float t0 = tab(i1(nz, n, L1)), tm1 = tab(i1(nz - 1, n, L1));
+                    if (c.ver == 0) {
+                        ho = -(0.5f * (tm1 + t0) * w * ar);
                         // a two-layer column writes this row twice: flux = C - (C - flux_in)
                         if (nzmin + 1 == nzmax - 1) ho = ho - (ho - fv0) + fv0;
                     } else {
-                        const float tm2 = ab_value(B, i1(nz - 2, n, L1), t), tm1 = ab_value(B, i1(nz - 1, n, L1), t);
-                        const float t0 = ab_value(B, i1(nz, n, L1), t), tp1 = ab_value(B, i1(nz + 1, n, L1), t);
-                        const float zm2 = g.Z3[i1(nz - 2, n, L1)], zm1 = g.Z3[i1(nz - 1, n, L1)];
-                        const float z0 = g.Z3[i1(nz, n, L1)], zp1 = g.Z3[i1(nz + 1, n, L1)];
-                        const float qc = (tm1 - t0) / (zm1 - z0);
-                        const float qu = (t0 - tp1) / (z0 - zp1);
-                        const float qd = (tm2 - tm1) / (zm2 - zm1);
-                        const float zb = g.zbar3[iN(nz, n, nl)];
-                        const float Tm1 = t0 + (2.f * qc + qu) * (zb - z0) * (1.f / 3.f);
-                        const float Tm2 = tm1 + (2.f * qc + qd) * (zb - zm1) * (1.f / 3.f);
-                        const float w = pw[iN(nz, n, nl)], aw = fabsf(w);
-                        const float no = (float)c.pv;
-                        const float Tmean = (w + aw) * Tm1 + (w - aw) * Tm2;
-                        ho = (-(0.5f * (1.f - no) * Tmean) - no * (0.5f * (Tm1 + Tm2)) * w) * g.area[iN(nz, n, nl)];
+                        const float aw = fabsf(w);
+                        ho = -(0.5f * (t0 * (w + aw) + tm1 * (w - aw)) * ar);
                     }
                 } else {
-                    if (nz == nzmin) {
-                        ho = -(pw[iN(nz, n, nl)] * ab_value(B, i1(nz, n, L1), t) * g.area[iN(nz, n, nl)]);
-                    } else if (nz == nzmax) {
-                        ho = 0.f;
-                    } else {
-                        const float w = pw[iN(nz, n, nl)], aw = fabsf(w);
-                        ho = -(0.5f * (ab_value(B, i1(nz, n, L1), t) * (w + aw) +
-                                       ab_value(B, i1(nz - 1, n, L1), t) * (w - aw)) *
-                               g.area[iN(nz, n, nl)]);
-                    }
+                    const float tm2 = tab(i1(nz - 2, n, L1)), tm1 = tab(i1(nz - 1, n, L1));
+                    const float t0 = tab(i1(nz, n, L1)), tp1 = tab(i1(nz + 1, n, L1));
+                    const float zm2 = g.Z3[i1(nz - 2, n, L1)], zm1 = g.Z3[i1(nz - 1, n, L1)];
+                    const float z0 = g.Z3[i1(nz, n, L1)], zp1 = g.Z3[i1(nz + 1, n, L1)];
+                    const float qc = (tm1 - t0) / (zm1 - z0);
+                    const float qu = (t0 - tp1) / (z0 - zp1);
+                    const float qd = (tm2 - tm1) / (zm2 - zm1);
+                    const float zb = g.zbar3[iN(nz, n, nl)];
+                    const float Tm1 = t0 + (2.f * qc + qu) * (zb - z0) * (1.f / 3.f);
+                    const float Tm2 = tm1 + (2.f * qc + qd) * (zb - zm1) * (1.f / 3.f);
+                    const float w = pw[iN(nz, n, nl)], aw = fabsf(w);
+                    const float no = (float)c.pv;
+                    const float Tmean = (w + aw) * Tm1 + (w - aw) * Tm2;
+                    ho = (-(0.5f * (1.f - no) * Tmean) - no * (0.5f * (Tm1 + Tm2)) * w) * ar;
                 }
                 B.ADv[t * B.sNI + iN(nz, n, nl)] = ho - fv0;
                 if (nz > nzmax - 1) continue;
-                // horizontal: LO gather over all edges, antidiffusive flux of owned edges
                 const size_t i = i1(nz, n, L1);
                 const float Tn = T[i];
-                const float TAn = ab_value(B, i, t);
+                const float TAn = tab(i);
                 Kahan acc;
-                for (int k = k0; k < k1; k++) {
-                    const int code = tp.ne_idx[k];
-                    const bool own = code >= 0;
-                    const int e = own ? code : ~code;
-                    if (nz < tp.e_lo[e] || nz > tp.e_hi[e]) continue;
-                    const int m = own ? tp.e_n2[e] : tp.e_n1[e];
-                    const float vf = VF[i1(nz, e, L1)], avf = fabsf(vf);
-                    const float Tm = T[i1(nz, m, L1)];
-                    const float T1 = own ? Tn : Tm, T2 = own ? Tm : Tn;
-                    const float flo = fct ? -(0.5f * (T1 * (vf + avf) + T2 * (vf - avf))) : 0.f;
-                    if (fct) acc.add(own ? flo : -flo);
-                    if (!own) continue;
-                    // owned edge: high-order flux on the AB values
-                    const float t1 = TAn, t2 = ab_value(B, i1(nz, m, L1), t);
-                    float hf;
-                    if (c.hor == 2) {
-                        hf = -(0.5f * (t1 * (vf + avf) + t2 * (vf - avf)));
-                    } else {
-                        const int up = tp.e_up[e], dn = tp.e_dn[e];
-                        float g1, g2, g3, g4;
-                        bool tri = false;
-                        if (up >= 0 && dn >= 0) {
-                            const int gzmin = max(tp.n_ulevmax[n], tp.n_ulevmax[m]);
-                            const int gzmax = min(tp.n_nlevmin[n], tp.n_nlevmin[m]);
-                            tri = nz >= gzmin && nz <= gzmax - 1;
-                        }
-                        if (tri) {
-                            tri_grad(tp, g, T, up, nz, g1, g3);
-                            tri_grad(tp, g, T, dn, nz, g2, g4);
-                        } else {
-                            node_grad(tp, g, T, n, nz, g1, g3);
-                            node_grad(tp, g, T, m, nz, g2, g4);
-                        }
-                        const int el1 = tp.e_t1[e], el2 = tp.e_t2[e];
-                        float a = RE * g.elem_cos[el1];
-                        if (el2 >= 0) a = 0.5f * (a + RE * g.elem_cos[el2]);
-                        const float ex = g.edxy[2 * (size_t)e], ey = g.edxy[2 * (size_t)e + 1];
-                        float clo1 = 1.f, clo2 = 1.f;
-                        if (c.hor == 0) {
-                            clo1 = (tp.n_nbl[n] - nz) >= 0 ? 1.f : 0.f;
-                            clo2 = (tp.n_nbl[m] - nz) >= 0 ? 1.f : 0.f;
-                        }
-                        const float d2 = 2.f * (t2 - t1);
-                        const float Tm2 = t2 - (d2 + ex * a * g2 + ey * RE * g4) * (1.f / 6.f) * clo2;
-                        const float Tm1 = t1 + (d2 + ex * a * g1 + ey * RE * g3) * (1.f / 6.f) * clo1;
-                        const float no = (float)c.ph;
-                        const float cHO = (vf + avf) * Tm1 + (vf - avf) * Tm2;
-                        hf = -(0.5f * (1.f - no) * cHO) - vf * no * 0.5f * (Tm1 + Tm2);
+                for (int g0 = 0; g0 < deg; g0 += kU) {
+                    float vf[kU], tm[kU];
+                    bool ok[kU];
+#pragma unroll
+                    for (int u = 0; u < kU; u++) {
+                        const int j = g0 + u;
+                        ok[u] = j < deg && nz >= S.lo[j] && nz <= S.hi[j];
+                        vf[u] = ok[u] ? VF[i1(nz, S.e[j], L1)] : 0.f;
+                        tm[u] = ok[u] ? T[i1(nz, S.m[j], L1)] : 0.f;
                     }
-                    B.ADh[t * B.sE + i1(nz, e, L1)] = hf - flo;
+#pragma unroll
+                    for (int u = 0; u < kU; u++) {
+                        if (!ok[u]) continue;
+                        const int j = g0 + u;
+                        const bool own = (S.own >> j) & 1u;
+                        const float v = vf[u], av = fabsf(v);
+                        const float T1 = own ? Tn : tm[u], T2 = own ? tm[u] : Tn;
+                        const float flo = fct ? -(0.5f * (T1 * (v + av) + T2 * (v - av))) : 0.f;
+                        if (fct) acc.add(own ? flo : -flo);
+                        if (!own) continue;
+                        // owned edge: high-order flux on the AB values
+                        const int e = S.e[j], m = S.m[j];
+                        const float t1 = TAn, t2 = tab(i1(nz, m, L1));
+                        float hf;
+                        if (c.hor == 2) {
+                            hf = -(0.5f * (t1 * (v + av) + t2 * (v - av)));
+                        } else {
+                            const int4 un = mw.un[e], dn = mw.dn[e];
+                            const float4 wu = mw.wu[e], wd = mw.wd[e];
+                            const int gzmin = un.w & 0xffff, gzmax = un.w >> 16;
+                            float s1, s2;
+                            if (nz >= gzmin && nz <= gzmax - 1) {
+                                s1 = wu.x * T[i1(nz, un.x, L1)] + wu.y * T[i1(nz, un.y, L1)] + wu.z * T[i1(nz, un.z, L1)];
+                                s2 = wd.x * T[i1(nz, dn.x, L1)] + wd.y * T[i1(nz, dn.y, L1)] + wd.z * T[i1(nz, dn.z, L1)];
+                            } else {
+                                const float exa = g.edxy[2 * (size_t)e] * wu.w;
+                                const float eyr = g.edxy[2 * (size_t)e + 1] * RE;
+                                s1 = node_grad_proj(tp, g, T, n, nz, exa, eyr);
+                                s2 = node_grad_proj(tp, g, T, m, nz, exa, eyr);
+                            }
+                            float clo1 = 1.f, clo2 = 1.f;
+                            if (c.hor == 0) {
+                                clo1 = (tp.n_nbl[n] - nz) >= 0 ? 1.f : 0.f;
+                                clo2 = (tp.n_nbl[m] - nz) >= 0 ? 1.f : 0.f;
+                            }
+                            const float d2 = 2.f * (t2 - t1);
+                            const float Tm2 = t2 - (d2 + s2) * (1.f / 6.f) * clo2;
+                            const float Tm1 = t1 + (d2 + s1) * (1.f / 6.f) * clo1;
+                            const float no = (float)c.ph;
+                            const float cHO = (v + av) * Tm1 + (v - av) * Tm2;
+                            hf = -(0.5f * (1.f - no) * cHO) - v * no * 0.5f * (Tm1 + Tm2);
+                        }
+                        B.ADh[t * B.sE + i1(nz, e, L1)] = hf - flo;
+                    }
                 }
                 if (fct) {
                     acc.add(fv0);
@@ -316,37 +338,48 @@ k32_lo_ad(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, const float *V
 // ---------------------------------------------------------------------------
 // k32_bounds: FCT bounds and R+ / R- (FCT tracers only)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float lo_at(const float *T, const float *LOi, const DGeom<float> &g, size_t i) {
-    return (T[i] * g.hnode[i] + LOi[i]) / g.hnode_new[i];
-}
-
 __global__ void __launch_bounds__(kT) k32_bounds(DTopo tp, DGeom<float> g, B32View B, float dt) {
+    __shared__ NodeEdges S;
     extern __shared__ __align__(16) float sm32[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int L1 = tp.L1, nl = tp.nl;
     float *tvmax = sm32 + (size_t)warp * 2 * (L1 + 2);
     float *tvmin = tvmax + (L1 + 2);
     const float eps = (float)kFluxEps;
-    for (int n = blockIdx.x * kW + warp; n < tp.N2; n += gridDim.x * kW) {
-        const int nzmin = tp.n_ulev[n], nzmax = tp.n_nlev[n];
-        const int k0 = tp.ne_ptr[n], k1 = tp.ne_ptr[n + 1];
-        for (int t = 0; t < B.ntr; t++) {
+    for (int n = blockIdx.x; n < tp.N2; n += gridDim.x) {
+        __syncthreads();
+        stage_node(tp, n, S);
+        __syncthreads();
+        const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
+        for (int t = warp; t < B.ntr; t += kW) {
             if (!B.cfg[t].lim) continue;
             const float *T = B.T + t * B.sN;
             const float *LOi = B.LOi + t * B.sN;
             for (int nz = nzmin + lane; nz <= nzmax - 1; nz += 32) {
                 const size_t i = i1(nz, n, L1);
-                const float lo = lo_at(T, LOi, g, i), tt = T[i];
+                const float tt = T[i];
+                const float lo = (tt * g.hnode[i] + LOi[i]) / g.hnode_new[i];
                 float mx = fmaxf(lo, tt), mn = fminf(lo, tt);
-                for (int k = k0; k < k1; k++) {
-                    const int code = tp.ne_idx[k];
-                    const int e = code >= 0 ? code : ~code;
-                    if (nz < tp.e_lo[e] || nz > tp.e_hi[e]) continue;
-                    const int m = code >= 0 ? tp.e_n2[e] : tp.e_n1[e];
-                    const size_t j = i1(nz, m, L1);
-                    const float lm = lo_at(T, LOi, g, j), tm = T[j];
-                    mx = fmaxf(mx, fmaxf(lm, tm));
-                    mn = fminf(mn, fminf(lm, tm));
+                for (int g0 = 0; g0 < deg; g0 += kU) {
+                    float tm[kU], li[kU], hm[kU], hnm[kU];
+                    bool ok[kU];
+#pragma unroll
+                    for (int u = 0; u < kU; u++) {
+                        const int j = g0 + u;
+                        ok[u] = j < deg && nz >= S.lo[j] && nz <= S.hi[j];
+                        const size_t jj = ok[u] ? i1(nz, S.m[j], L1) : i;
+                        tm[u] = T[jj];
+                        li[u] = LOi[jj];
+                        hm[u] = g.hnode[jj];
+                        hnm[u] = g.hnode_new[jj];
+                    }
+#pragma unroll
+                    for (int u = 0; u < kU; u++) {
+                        if (!ok[u]) continue;
+                        const float lm = (tm[u] * hm[u] + li[u]) / hnm[u];
+                        mx = fmaxf(mx, fmaxf(lm, tm[u]));
+                        mn = fminf(mn, fminf(lm, tm[u]));
+                    }
                 }
                 tvmax[nz] = mx;
                 tvmin[nz] = mn;
@@ -356,35 +389,42 @@ __global__ void __launch_bounds__(kT) k32_bounds(DTopo tp, DGeom<float> g, B32Vi
             const float *ADh = B.ADh + t * B.sE;
             for (int nz = nzmin + lane; nz <= nzmax - 1; nz += 32) {
                 const size_t i = i1(nz, n, L1);
-                const float lo = lo_at(T, LOi, g, i);
-                float bmx, bmn;
+                const float lo = (T[i] * g.hnode[i] + LOi[i]) / g.hnode_new[i];
+                float tup, tlo;
                 if (nz == nzmin || nz == nzmax - 1) {
-                    bmx = tvmax[nz] - lo;
-                    bmn = tvmin[nz] - lo;
+                    tup = tvmax[nz];
+                    tlo = tvmin[nz];
                 } else {
-                    bmx = fmaxf(fmaxf(tvmax[nz - 1], tvmax[nz]), tvmax[nz + 1]) - lo;
-                    bmn = fminf(fminf(tvmin[nz - 1], tvmin[nz]), tvmin[nz + 1]) - lo;
+                    tup = fmaxf(fmaxf(tvmax[nz - 1], tvmax[nz]), tvmax[nz + 1]);
+                    tlo = fminf(fminf(tvmin[nz - 1], tvmin[nz]), tvmin[nz + 1]);
                 }
+                const float bmx = tup - lo, bmn = tlo - lo;
                 const float v0 = ADv[iN(nz, n, nl)], v1 = ADv[iN(nz + 1, n, nl)];
                 Kahan P, M;
                 P.add(fmaxf(0.f, v0) + fmaxf(0.f, -v1));
                 M.add(fminf(0.f, v0) + fminf(0.f, -v1));
-                for (int k = k0; k < k1; k++) {
-                    const int code = tp.ne_idx[k];
-                    const int e = code >= 0 ? code : ~code;
-                    if (nz < tp.e_lo[e] || nz > tp.e_hi[e]) continue;
-                    float x = ADh[i1(nz, e, L1)];
-                    if (code < 0) x = -x;
-                    P.add(fmaxf(0.f, x));
-                    M.add(fminf(0.f, x));
+                for (int g0 = 0; g0 < deg; g0 += kU) {
+                    float x[kU];
+                    bool ok[kU];
+#pragma unroll
+                    for (int u = 0; u < kU; u++) {
+                        const int j = g0 + u;
+                        ok[u] = j < deg && nz >= S.lo[j] && nz <= S.hi[j];
+                        x[u] = ok[u] ? ADh[i1(nz, S.e[j], L1)] : 0.f;
+                    }
+#pragma unroll
+                    for (int u = 0; u < kU; u++) {
+                        if (!ok[u]) continue;
+                        const float xv = ((S.own >> (g0 + u)) & 1u) ? x[u] : -x[u];
+                        P.add(fmaxf(0.f, xv));
+                        M.add(fminf(0.f, xv));
+                    }
                 }
                 const float s = dt / (g.areasvol[iN(nz, n, nl)] * g.hnode_new[i]);
-                B.Rp[t * B.sN + i] = fminf(1.f, bmx / (P.get() * s + eps));
-                B.Rm[t * B.sN + i] = fminf(1.f, bmn / (M.get() * s - eps));
+                B.R[t * B.sN + i] = make_float2(fminf(1.f, bmx / (P.get() * s + eps)), fminf(1.f, bmn / (M.get() * s - eps)));
                 // the bounds themselves: the update clamps the advected value into them, so
                 // FP32 rounding in the limiter can never create a new extremum
-                B.Tup[t * B.sN + i] = bmx + lo;
-                B.Tlo[t * B.sN + i] = bmn + lo;
+                B.TB[t * B.sN + i] = make_float2(tup, tlo);
             }
             __syncwarp();
         }
@@ -417,25 +457,26 @@ __device__ __forceinline__ void scan_down(float &A, float &B, int lane) {
     }
 }
 
-constexpr int kMaxChunks = 4;  // columns up to 128 layers
-
 __global__ void __launch_bounds__(kT)
 k32_update(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, VFactors vf, float dt) {
+    __shared__ NodeEdges S;
     extern __shared__ __align__(16) float sm32[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int L1 = tp.L1, nl = tp.nl;
     float *Ta = sm32 + (size_t)warp * (L1 + 2);
-    for (int n = blockIdx.x * kW + warp; n < tp.N2; n += gridDim.x * kW) {
-        const int nzmin = tp.n_ulev[n], nzmax = tp.n_nlev[n];
-        const int k0 = tp.ne_ptr[n], k1 = tp.ne_ptr[n + 1];
+    for (int n = blockIdx.x; n < tp.N2; n += gridDim.x) {
+        __syncthreads();
+        stage_node(tp, n, S);
+        __syncthreads();
+        const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
         const int nch = (nzmax - nzmin + 31) / 32;
-        for (int t = 0; t < B.ntr; t++) {
+        for (int t = warp; t < B.ntr; t += kW) {
             const DCfg c = B.cfg[t];
             const int fct = c.lim;
             const float *T = B.T + t * B.sN;
             const float *ADv = B.ADv + t * B.sNI;
             const float *ADh = B.ADh + t * B.sE;
-            const float *Rp = B.Rp + t * B.sN, *Rm = B.Rm + t * B.sN;
+            const float2 *R = B.R + t * B.sN;
             float tadv[kMaxChunks];
 #pragma unroll
             for (int ch = 0; ch < kMaxChunks; ch++) {
@@ -443,43 +484,58 @@ k32_update(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, VFactors vf, 
                 tadv[ch] = 0.f;
                 if (ch >= nch || nz > nzmax - 1) continue;
                 const size_t i = i1(nz, n, L1);
-                const float av = g.areasvol[iN(nz, n, nl)];
-                const float sdt = dt / av;
+                const float sdt = dt / g.areasvol[iN(nz, n, nl)];
                 Kahan del;
                 float f0 = ADv[iN(nz, n, nl)], f1 = ADv[iN(nz + 1, n, nl)];
+                float2 r0 = make_float2(1.f, 1.f);
                 if (fct) {
                     del.add(B.LOi[t * B.sN + i]);
+                    r0 = R[i];
                     // vertical limiting (oce_adv_tra_fct.F90:425-456); the bottom interface is not limited
-                    float ae = 1.f;
-                    if (nz == nzmin) ae = f0 >= 0.f ? fminf(ae, Rp[i]) : fminf(ae, Rm[i]);
-                    else ae = f0 >= 0.f ? fminf(fminf(ae, Rm[i - 1]), Rp[i]) : fminf(fminf(ae, Rp[i - 1]), Rm[i]);
-                    f0 *= ae;
+                    if (nz == nzmin) {
+                        f0 *= f0 >= 0.f ? fminf(1.f, r0.x) : fminf(1.f, r0.y);
+                    } else {
+                        const float2 rm = R[i - 1];
+                        f0 *= f0 >= 0.f ? fminf(fminf(1.f, rm.y), r0.x) : fminf(fminf(1.f, rm.x), r0.y);
+                    }
                     if (nz + 1 <= nzmax - 1) {
-                        ae = f1 >= 0.f ? fminf(fminf(1.f, Rm[i]), Rp[i + 1]) : fminf(fminf(1.f, Rp[i]), Rm[i + 1]);
-                        f1 *= ae;
+                        const float2 rp = R[i + 1];
+                        f1 *= f1 >= 0.f ? fminf(fminf(1.f, r0.y), rp.x) : fminf(fminf(1.f, r0.x), rp.y);
                     }
                 }
                 del.add(f0 * sdt);
                 del.add(-(f1 * sdt));
-                for (int k = k0; k < k1; k++) {
-                    const int code = tp.ne_idx[k];
-                    const int e = code >= 0 ? code : ~code;
-                    if (nz < tp.e_lo[e] || nz > tp.e_hi[e]) continue;
-                    float x = ADh[i1(nz, e, L1)];
-                    if (fct) {
-                        const size_t ia = i1(nz, tp.e_n1[e], L1), ib = i1(nz, tp.e_n2[e], L1);
-                        const float ae = x >= 0.f ? fminf(fminf(1.f, Rp[ia]), Rm[ib]) : fminf(fminf(1.f, Rm[ia]), Rp[ib]);
-                        x *= ae;
+                for (int g0 = 0; g0 < deg; g0 += kU) {
+                    float x[kU];
+                    float2 rm[kU];
+                    bool ok[kU];
+#pragma unroll
+                    for (int u = 0; u < kU; u++) {
+                        const int j = g0 + u;
+                        ok[u] = j < deg && nz >= S.lo[j] && nz <= S.hi[j];
+                        x[u] = ok[u] ? ADh[i1(nz, S.e[j], L1)] : 0.f;
+                        rm[u] = (ok[u] && fct) ? R[i1(nz, S.m[j], L1)] : make_float2(1.f, 1.f);
                     }
-                    del.add(code >= 0 ? x * sdt : -(x * sdt));
+#pragma unroll
+                    for (int u = 0; u < kU; u++) {
+                        if (!ok[u]) continue;
+                        const bool own = (S.own >> (g0 + u)) & 1u;
+                        float xv = x[u];
+                        if (fct) {
+                            // R of edges(1,e) and edges(2,e)
+                            const float2 ra = own ? r0 : rm[u], rb = own ? rm[u] : r0;
+                            xv *= xv >= 0.f ? fminf(fminf(1.f, ra.x), rb.y) : fminf(fminf(1.f, ra.y), rb.x);
+                        }
+                        del.add(own ? xv * sdt : -(xv * sdt));
+                    }
                 }
                 del.add(T[i] * (g.hnode[i] - g.hnode_new[i]));
                 float v = T[i] + del.get() / g.hnode_new[i];
                 if (fct) {
-                    const float hi = B.Tup[t * B.sN + i], lo = B.Tlo[t * B.sN + i];
-                    const float vc = fminf(fmaxf(v, lo), hi);
+                    const float2 tb = B.TB[t * B.sN + i];
+                    const float vc = fminf(fmaxf(v, tb.y), tb.x);
                     // a clamp beyond round-off means the limiter itself failed
-                    if (fabsf(vc - v) > 1e-5f * (hi - lo) + 1e-6f * fabsf(vc)) atomicOr(B.status, 2u);
+                    if (fabsf(vc - v) > 1e-5f * (tb.x - tb.y) + 1e-6f * fabsf(vc)) atomicOr(B.status, 2u);
                     v = vc;
                 }
                 tadv[ch] = v;
@@ -505,7 +561,8 @@ k32_update(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, VFactors vf, 
             const float bc = f.bc ? f.bc[(size_t)t * tp.N2 + n] : 0.f;
 #pragma unroll
             for (int ch = 0; ch < kMaxChunks; ch++) {
-                if (ch >= nch) break;
+                tpv[ch] = 0.f;
+                if (ch >= nch) continue;
                 const int nz = nzmin + 32 * ch + lane;
                 float A = 1.f, Bv = 0.f;
                 if (nz <= nzmax - 1) {
@@ -565,18 +622,21 @@ void b32_vfactors(const DTopo &tp, const DGeom<float> &g, const DForcing<float> 
                   cudaStream_t s) {
     k32_vfactors<<<(tp.N2 + 127) / 128, 128, 0, s>>>(tp, g, f, dt, v);
 }
-void b32_lo_ad(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B, const float *VF,
-               double dt, cudaStream_t s) {
-    k32_lo_ad<<<grid32(tp.N2, kW), kT, 0, s>>>(tp, g, f, B, VF, (float)dt);
+// node kernels: one block per node (grid-stride), the tracers split over the block's warps
+static int grid_nodes(int n2) { return n2 < 152 * 32 ? n2 : 152 * 32; }
+
+void b32_lo_ad(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B, const MusclW &mw,
+               const float *VF, double dt, cudaStream_t s) {
+    k32_lo_ad<<<grid_nodes(tp.N2), kT, 0, s>>>(tp, g, f, B, mw, VF, (float)dt);
 }
 void b32_bounds(const DTopo &tp, const DGeom<float> &g, const B32View &B, double dt, cudaStream_t s) {
     const size_t sm = sizeof(float) * 2 * (tp.L1 + 2) * kW;
-    k32_bounds<<<grid32(tp.N2, kW), kT, sm, s>>>(tp, g, B, (float)dt);
+    k32_bounds<<<grid_nodes(tp.N2), kT, sm, s>>>(tp, g, B, (float)dt);
 }
 void b32_update(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B,
                 const VFactors &v, double dt, cudaStream_t s) {
     const size_t sm = sizeof(float) * (tp.L1 + 2) * kW;
-    k32_update<<<grid32(tp.N2, kW), kT, sm, s>>>(tp, g, f, B, v, (float)dt);
+    k32_update<<<grid_nodes(tp.N2), kT, sm, s>>>(tp, g, f, B, v, (float)dt);
 }
 
 }  // namespace fesom

@@ -116,6 +116,17 @@ def _c64(a):
     return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
 
 
+def _bc_all(forcing, bc, ntr):
+    """Surface term of every tracer, (ntr, nod2D): bc as given, else forcing.bc_surface
+    (one term per node) applied to every tracer, else None (zero)."""
+    if bc is not None:
+        return bc
+    b = getattr(forcing, "bc_surface", None)
+    if b is None:
+        return None
+    return np.ascontiguousarray(np.broadcast_to(np.asarray(b), (ntr, np.asarray(b).shape[-1])))
+
+
 def mesh_desc(mesh, pass_muscl_init=None):
     """Build a ``fesom_mesh_desc`` (and the arrays it points to) for a Mesh."""
     i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
@@ -244,7 +255,7 @@ class Context:
             assert v.dtype == np.float64 and v.flags.c_contiguous
         uv, w, wi, we, Kv = (_c64(forcing.uv), _c64(forcing.w), _c64(forcing.w_i), _c64(forcing.w_e),
                              _c64(forcing.Kv))
-        bcs = None if bc is None else _c64(bc)
+        bcs = _c64(_bc_all(forcing, bc, n))
         self._chk(self.L.fesom_gpu_tracer_step(self.h, n, arr, float(forcing.dt if dt is None else dt), _p(uv),
                                                _p(w), _p(wi), _p(we), _p(Kv), _p(bcs), vp, op))
 
@@ -256,6 +267,7 @@ class Context:
         self.ntr = n
 
     def forcing_upload(self, forcing, bc=None):
+        bc = _bc_all(forcing, bc, getattr(self, "ntr", 1))
         if self.prec == PREC_FP32 and forcing.uv.dtype == np.float32:
             f = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float32)
             self._fk = [f(forcing.uv), f(forcing.w), f(forcing.w_i), f(forcing.w_e), f(forcing.Kv), f(bc)]
