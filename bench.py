@@ -80,36 +80,43 @@ def algorithmic_bytes(counts, ntr, s):
     return s * (ntr * (18 * N3 + 3 * E3) + 3 * T3 + 14 * N3)
 
 
-def stage_bytes(counts, ntr, s, ab=2):
+def stage_bytes(counts, ntr, s, ab=2, form="fp32"):
     """Compulsory bytes per step of each stage kernel (every input read once, every
     output written once) for ntr tracers, s bytes per value.
 
     FP32 batched form:
-      vflux:    read uv (2 T3), helem (T3); write the edge volume flux VF (E3)           shared
-      vfactors: read Kv, area, areasvol, hnode_new (4 N3); write a, c, 1/m, c/m (4 N3)   shared
-      lo_ad:    per tracer read T, T_old (2 N3; 3 with AB3); write LO increment, ADv (2 N3),
-                ADh (E3); shared VF (E3), w, w_e, area, Z, zbar, areasvol (6 N3)
-      bounds:   per tracer read T, LO increment, ADv (3 N3), ADh (E3); write R+, R- and the
-                bounds T_up, T_lo (4 N3); shared hnode, hnode_new, areasvol (3 N3)
-      update:   per tracer read T, LO increment, ADv, R+, R-, T_up, T_lo (7 N3), ADh (E3); write
-                T (N3); shared factors (4 N3), hnode, hnode_new, areasvol (3 N3)
+      vflux:     read uv (2 T3), helem (T3); write the edge volume flux VF (E3)           shared
+      vfactors:  read Kv, area, areasvol, hnode_new (4 N3); write a, c, 1/m, c/m (4 N3)   shared
+      lo_ad:     per tracer read T and the previous levels (ab N3); write LO, ADv (2 N3);
+                 shared VF (E3), w, w_e, area, Z, zbar, areasvol, hnode, hnode_new (8 N3)
+      edge_flux: per tracer read T and the previous levels (ab N3); write ADh (E3); shared VF (E3)
+      bounds:    per tracer read T, LO, ADv (3 N3), ADh (E3); write R+, R- and the bounds
+                 T_up, T_lo (4 N3); shared hnode_new, areasvol (2 N3)
+      update:    per tracer read LO, ADv, R+, R-, T_up, T_lo (6 N3), ADh (E3); write T (N3);
+                 shared factors (4 N3), hnode_new, areasvol (2 N3)
     FP64 plain form (per tracer, one tracer per launch):
       ab 4 N3; trxy N3 + 2 T3; edge_flux 2 N3 + 2 T3 + 2 E3 (+3 T3 shared); node_lo 3 N3 + E3
       (+8 N3); bounds 4 N3; rpm 5 N3 + E3 (+2 N3); update 6 N3 + E3 (+3 N3); vdiff 2 N3 (+4 N3)
       plus 48 B per DOF of FP64 scratch.
     """
     N3, E3, T3 = counts["N3"], counts["E3"], counts["T3"]
+    if form == "fp32":
+        return {
+            "vflux": s * (3 * T3 + E3),
+            "vfactors": s * 8 * N3,
+            "lo_ad": s * (ntr * (ab + 2) * N3 + E3 + 8 * N3),
+            "edge_flux": s * (ntr * (ab * N3 + E3) + E3),
+            "bounds": s * (ntr * (7 * N3 + E3) + 2 * N3),
+            "update": s * (ntr * (7 * N3 + E3) + 6 * N3),
+        }
     return {
-        "vflux": s * (3 * T3 + E3),
-        "vfactors": s * 8 * N3,
-        "lo_ad": s * (ntr * ((ab + 2) * N3 + E3) + E3 + 6 * N3),
-        "bounds": s * (ntr * (7 * N3 + E3) + 3 * N3),
-        "update": s * (ntr * (8 * N3 + E3) + 7 * N3),
         "ab": s * ntr * 4 * N3,
         "trxy": s * ntr * (N3 + 2 * T3),
         "edge_flux": s * (ntr * (2 * N3 + 2 * T3 + 2 * E3) + 3 * T3),
         "node_lo": s * (ntr * (3 * N3 + E3) + 8 * N3),
+        "bounds": s * ntr * 4 * N3,
         "rpm": s * (ntr * (5 * N3 + E3) + 2 * N3),
+        "update": s * (ntr * (6 * N3 + E3) + 3 * N3),
         "vdiff": s * (ntr * 2 * N3 + 4 * N3) + ntr * 48 * N3,
     }
 

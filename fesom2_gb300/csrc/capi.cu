@@ -57,7 +57,7 @@ struct fesom_gpu_ctx {
     int rot = 0;
     float *VF = nullptr;
     VFactors vfac{};
-    float *LOi = nullptr, *ADv32 = nullptr, *ADh32 = nullptr;
+    float *LO32 = nullptr, *ADv32 = nullptr, *ADh32 = nullptr;
     float2 *R2 = nullptr, *TB2 = nullptr;
     MusclW mw{};
     cudaGraphExec_t gexec32[3] = {nullptr, nullptr, nullptr};
@@ -442,10 +442,10 @@ void free_graphs32(fesom_gpu_ctx *ctx) {
 int alloc_state32(fesom_gpu_ctx *ctx, int ntr, int ab) {
     const size_t sN = (size_t)ctx->L1 * ctx->N2, sNI = (size_t)ctx->nl * ctx->N2, sE = (size_t)ctx->L1 * ctx->E2;
     void *old[] = {ctx->Bf[0], ctx->Bf[1], ctx->Bf[2], ctx->VF, ctx->vfac.a, ctx->vfac.c, ctx->vfac.inv, ctx->vfac.cp,
-                   ctx->LOi, ctx->ADv32, ctx->ADh32, ctx->R2, ctx->TB2, ctx->d_cfg, ctx->bc};
+                   ctx->LO32, ctx->ADv32, ctx->ADh32, ctx->R2, ctx->TB2, ctx->d_cfg, ctx->bc};
     for (void *b : old) { void *p = b; dfree(ctx, p); }
     ctx->Bf[0] = ctx->Bf[1] = ctx->Bf[2] = nullptr;
-    ctx->VF = ctx->LOi = ctx->ADv32 = ctx->ADh32 = nullptr;
+    ctx->VF = ctx->LO32 = ctx->ADv32 = ctx->ADh32 = nullptr;
     ctx->R2 = ctx->TB2 = nullptr;
     ctx->vfac = VFactors{};
     ctx->d_cfg = nullptr;
@@ -467,7 +467,7 @@ int alloc_state32(fesom_gpu_ctx *ctx, int ntr, int ab) {
     CK(cudaMemGetInfo(&fr, &tot));
     const int g = (int)std::min<size_t>((size_t)ntr, std::max<size_t>(1, (size_t)(0.85 * fr) / per_tracer));
     ctx->group = ctx->group_cap = g;
-    if ((rc = dalloc(ctx, (void **)&ctx->LOi, 4 * sN * g))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->LO32, 4 * sN * g))) return rc;
     if ((rc = dalloc(ctx, (void **)&ctx->ADv32, 4 * sNI * g))) return rc;
     if ((rc = dalloc(ctx, (void **)&ctx->ADh32, 4 * sE * g))) return rc;
     if ((rc = dalloc(ctx, (void **)&ctx->R2, 8 * sN * g))) return rc;
@@ -490,7 +490,7 @@ B32View view32(fesom_gpu_ctx *ctx, int t0, int nt) {
     v.O1 = level32(ctx, 1) + t0 * v.sN;
     v.O2 = ctx->ab_max == 3 ? level32(ctx, 2) + t0 * v.sN : nullptr;
     v.Tnew = level32(ctx, ctx->ab_max - 1) + t0 * v.sN;
-    v.LOi = ctx->LOi;
+    v.LO = ctx->LO32;
     v.ADv = ctx->ADv32;
     v.ADh = ctx->ADh32;
     v.R = ctx->R2;
@@ -561,9 +561,12 @@ int enqueue_step32(fesom_gpu_ctx *ctx, double dt, StageTimer *tm = nullptr) {
         DForcing<float> fg = forcing_view<float>(ctx, t0);
         bool any_fct = false;
         for (int t = t0; t < t0 + nt; t++) any_fct |= ctx->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
-        STAGE(10, b32_lo_ad(ctx->tp, g, fg, B, ctx->mw, ctx->VF, dt, ctx->stream));
+        STAGE(10, b32_lo_ad(ctx->tp, g, fg, B, ctx->VF, dt, ctx->stream));
+        STAGE(2, b32_ho(ctx->tp, g, B, ctx->mw, ctx->VF, ctx->stream));
         if (any_fct) STAGE(4, b32_bounds(ctx->tp, g, B, dt, ctx->stream));
-        STAGE(6, b32_update(ctx->tp, g, fg, B, ctx->vfac, dt, ctx->stream));
+        bool grp_vd = false;
+        for (int t = t0; t < t0 + nt; t++) grp_vd |= ctx->cfgs[t].i_vert_diff != 0;
+        STAGE(6, b32_update(ctx->tp, g, fg, B, ctx->vfac, dt, grp_vd ? 1 : 0, ctx->stream));
     }
     CK(cudaGetLastError());
     return FESOM_OK;
@@ -580,7 +583,9 @@ int launches_per_step(fesom_gpu_ctx *ctx) {
             const int nt = std::min(ctx->group, ctx->ntr - t0);
             bool any_fct = false;
             for (int t = t0; t < t0 + nt; t++) any_fct |= ctx->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
-            n += 2 + (any_fct ? 1 : 0);
+            // lo_ad, ho, update (+ bounds); the node kernels launch again for the wide nodes
+            const int wide = ctx->tp.n_wide ? 2 : 1;
+            n += 1 + wide * (2 + (any_fct ? 1 : 0));
         }
         return n;
     }
@@ -676,6 +681,13 @@ int fesom_gpu_init(const fesom_mesh_desc *mesh, int32_t precision, int32_t max_t
         *out = ctx;
         return FESOM_ERR_MESH;
     }
+    // the FP32 kernels index a tracer's columns and edge layers with 32-bit offsets
+    if (precision == FESOM_PREC_FP32 &&
+        std::max((size_t)mesh->nl * (size_t)mesh->nod2D, (size_t)mesh->nl * (size_t)mesh->edge2D) >= ((size_t)1 << 31)) {
+        ctx->err = "the FP32 form handles meshes with nl * max(nod2D, edge2D) below 2^31";
+        *out = ctx;
+        return FESOM_ERR_MESH;
+    }
     ctx->N2 = mesh->nod2D;
     ctx->E2 = mesh->edge2D;
     ctx->T2 = mesh->elem2D;
@@ -698,6 +710,15 @@ int fesom_gpu_init(const fesom_mesh_desc *mesh, int32_t precision, int32_t max_t
         (rc = upload_int(ctx, &tp.ne_ptr, h.ne_ptr)) || (rc = upload_int(ctx, &tp.ne_idx, h.ne_idx)) ||
         (rc = upload_int(ctx, &tp.nie_ptr, h.nie_ptr)) || (rc = upload_int(ctx, &tp.nie_idx, h.nie_idx)))
         return rc;
+    // nodes of more than 8 edges: the FP32 node kernels give them a launch of their own
+    {
+        std::vector<int> wide;
+        for (int n = 0; n < ctx->N2; n++)
+            if (h.ne_ptr[n + 1] - h.ne_ptr[n] > 8) wide.push_back(n);
+        tp.n_wide = (int)wide.size();
+        tp.wide_nodes = nullptr;
+        if (!wide.empty() && (rc = upload_int(ctx, &tp.wide_nodes, wide))) return rc;
+    }
     ctx->stage_n = std::min<size_t>((size_t)16 << 20, std::max<size_t>(2 * (size_t)ctx->L1 * ctx->T2, (size_t)ctx->nl * ctx->N2));
     if ((rc = dalloc(ctx, (void **)&ctx->stage, ctx->stage_n * sizeof(double)))) return rc;
     if (precision == FESOM_PREC_FP32) rc = init_geom<float>(ctx, mesh, ctx->g32);

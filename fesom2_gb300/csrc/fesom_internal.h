@@ -31,6 +31,8 @@ struct DTopo {
     const int *n_nlev, *n_ulev, *n_nlevmin, *n_ulevmax, *n_nbl;
     const int *ne_ptr, *ne_idx;    // node -> edge, idx >= 0: node is edges(1,e); ~e: node is edges(2,e)
     const int *nie_ptr, *nie_idx;  // node -> element, ascending element order
+    int n_wide;                    // nodes of more than 8 edges (FP32 form: their own launch)
+    const int *wide_nodes;
 };
 
 template <typename R>
@@ -84,15 +86,15 @@ struct B32View {
     size_t sN, sNI, sE;
     const float *T, *O1, *O2;
     float *Tnew;
-    float *LOi;      // LO increment: low-order flux divergence * dt / areasvol
-    float *ADv;      // antidiffusive (or, without limiter, high-order) vertical flux
+    float *LO;       // low-order (upwind) solution
+    float *ADv;      // vertical flux high order minus low order (the antidiffusive flux)
     float *ADh;      // the same for edges, written by the edge's first node
     float2 *R;       // FCT ratios (R+, R-)
     float2 *TB;      // FCT bounds of the advected value (LO + bmax, LO + bmin)
     const DCfg *cfg;
     unsigned *status;
 };
-// Node degree bound of the FP32 form (the node's edge list is staged in shared memory)
+// Node degree bound of the FP32 form (the node's edge list is staged per warp)
 constexpr int kMaxDeg = 16;
 // Per-edge MUSCL/MFCT reconstruction data of the FP32 form, precomputed at init:
 // un / dn = nodes of the up (of edges(1,e)) and down (of edges(2,e)) triangle, with
@@ -110,11 +112,12 @@ struct VFactors {
 void b32_vflux(const DTopo &, const DGeom<float> &, const DForcing<float> &, float *VF, cudaStream_t);
 void b32_vfactors(const DTopo &, const DGeom<float> &, const DForcing<float> &, double dt, const VFactors &,
                   cudaStream_t);
-void b32_lo_ad(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, const MusclW &,
-               const float *VF, double dt, cudaStream_t);
+void b32_lo_ad(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, const float *VF,
+               double dt, cudaStream_t);
+void b32_ho(const DTopo &, const DGeom<float> &, const B32View &, const MusclW &, const float *VF, cudaStream_t);
 void b32_bounds(const DTopo &, const DGeom<float> &, const B32View &, double dt, cudaStream_t);
 void b32_update(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, const VFactors &,
-                double dt, cudaStream_t);
+                double dt, int any_ivd, cudaStream_t);
 
 // launch wrappers (kernels_fp64.cu / kernels_fp32.cu)
 template <typename R>

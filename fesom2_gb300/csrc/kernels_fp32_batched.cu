@@ -1,6 +1,6 @@
 // kernels_fp32_batched.cu -- the FP32 batched form of the tracer step.
 //
-// All tracers of a step in one launch per stage; four tracer stages, two
+// All tracers of a step in one launch per stage; three tracer stages and two
 // tracer-independent set-up stages:
 //
 //   k32_vflux     edge volume fluxes per edge-layer (oce_adv_tra_hor.F90:159-250
@@ -11,22 +11,35 @@
 //                 cause, so they are formed in FP64; stored as FP32 a, c, 1/m, c/m
 //   k32_lo_ad     per node: the LO solution's increment (edge gather of upwind
 //                 fluxes + upwind vertical flux with w_e), the vertical
-//                 antidiffusive flux (QR4C/UPW1 with w on the AB values) and the
+//                 antidiffusive flux (QR4C/UPW1 on the AB values) and the
 //                 antidiffusive flux of the edges the node owns (edges(1,e) == n):
 //                 MUSCL/MFCT/UPW1 on the AB values with fill_up_dn_grad inlined
-//   k32_bounds    per node: FCT bounds (max/min of LO and T over the node's wet
-//                 elements and the adjacent layers) and R+/R- (oce_adv_tra_fct.F90)
-//   k32_update    per node: limited fluxes, flux divergence, T* update and the
+//   k32_bounds    per node: FCT bounds (max/min of LO and T over the node's
+//                 neighbours and the adjacent layers) and R+/R- (oce_adv_tra_fct.F90)
+//   k32_update    per node: limited fluxes, flux divergence, T* update, then the
 //                 implicit vertical diffusion as two warp scans of affine maps over
 //                 the column (the forward and back substitution with the FP64
-//                 factors), written to the buffer of the oldest time level
+//                 factors); written to the buffer of the oldest time level
+//
+// Every tracer carries the same three quantities whatever its limiter: the LO
+// increment and the antidiffusive fluxes "high order minus low order" of the
+// edges and interfaces.  Without FCT the update adds them unlimited, which is
+// the high-order flux divergence; with FCT it scales them by R+/R- first.
+//
+// Mapping: one warp per node for ALL tracers of the launch.  The lanes cover a
+// chunk of the node's column (one level per lane); consecutive chunks overlap
+// by the halo levels each stage needs (the level above/below comes from the
+// neighbouring lane through a shuffle), and the halo lanes compute but do not
+// store.  The node's edge list, the neighbour offsets and the tracer-
+// independent geometry of a chunk sit in registers and serve every tracer, so
+// per tracer a lane does only the gathers and the arithmetic of that tracer.
+// Eight consecutive nodes per block (the node order is spatially local), so
+// the neighbour columns a block gathers are mostly shared between its warps.
 //
 // Layout: tracer-major, column-contiguous per tracer (the reference's
-// a(level, node) per tracer).  One warp per node with the lanes over the levels
-// of the column: every column access is coalesced, neighbour columns come
-// through L1/L2.  No atomics: each edge flux is written by its owner node only,
-// every node sum is a gather.  The Adams-Bashforth shift is a rotation of the
-// time-level buffers (no copy).
+// a(level, node) per tracer).  No atomics on values: each edge flux is written
+// by its owner node only and every node sum is a gather.  The Adams-Bashforth
+// shift is a rotation of the time-level buffers (no copy).
 #include <cuda_runtime.h>
 
 #include "fesom_internal.h"
@@ -35,44 +48,23 @@ namespace fesom {
 
 namespace {
 
-constexpr int kW = 4;                 // warps per block
-constexpr int kT = 32 * kW;
+constexpr int kWB = 8;                // warps (= nodes) per block
+constexpr int kTB = 32 * kWB;
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kU = 8;                 // neighbours per unrolled group
-constexpr int kMaxChunks = 4;         // columns up to 128 layers
+constexpr int kMaxChunks = 5;         // columns of up to 128 layers, 30 levels per chunk
+constexpr int kMinBlocks = 3;         // resident blocks per SM the tracer kernels are built for (<= 80 registers)
 
 __device__ __forceinline__ size_t i1(int nz, int n, int L1) { return (size_t)n * L1 + (nz - 1); }
-__device__ __forceinline__ size_t iN(int nz, int n, int nl) { return (size_t)n * nl + (nz - 1); }
-
-struct Kahan {
-    float s = 0.f, c = 0.f;
-    __device__ __forceinline__ void add(float x) {
-        float t = s + x;
-        c += (fabsf(s) >= fabsf(x)) ? ((s - t) + x) : ((x - t) + s);
-        s = t;
-    }
-    __device__ __forceinline__ float get() const { return s + c; }
-};
-
-// upwind vertical flux with velocity W at interface nz (statement order of
-// adv_tra_ver_upw1: surface, bottom, interior), fin = 0
-__device__ __forceinline__ float vupw(const float *T, const float *W, const float *area, int nz, int n, int nzmin,
-                                      int nzmax, int L1, int nl) {
-    if (nz == nzmin) return -(W[iN(nz, n, nl)] * T[i1(nz, n, L1)] * area[iN(nz, n, nl)]);
-    if (nz == nzmax) return 0.f;
-    const float w = W[iN(nz, n, nl)], aw = fabsf(w);
-    return -(0.5f * (T[i1(nz, n, L1)] * (w + aw) + T[i1(nz - 1, n, L1)] * (w - aw)) * area[iN(nz, n, nl)]);
-}
 
 }  // namespace
 
 // ---------------------------------------------------------------------------
 // k32_vflux: volume flux of every edge-layer (shared by all tracers)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kT) k32_vflux(DTopo tp, DGeom<float> g, DForcing<float> f, float *VF) {
+__global__ void __launch_bounds__(kTB) k32_vflux(DTopo tp, DGeom<float> g, DForcing<float> f, float *VF) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int L1 = tp.L1;
-    for (int e = blockIdx.x * kW + warp; e < tp.E2; e += gridDim.x * kW) {
+    for (int e = blockIdx.x * kWB + warp; e < tp.E2; e += gridDim.x * kWB) {
         const int el1 = tp.e_t1[e], el2 = tp.e_t2[e];
         const int nl1 = tp.t_nlev[el1] - 1, nu1 = tp.t_ulev[el1];
         int nl2 = 0, nu2 = 0;
@@ -148,36 +140,59 @@ __global__ void __launch_bounds__(128) k32_vfactors(DTopo tp, DGeom<float> g, DF
     }
 }
 
+
 // ---------------------------------------------------------------------------
-// per-node staging: the node's edge list in shared memory, once per node
+// per-warp staging of the node's edge list (one warp per node)
 // ---------------------------------------------------------------------------
-struct NodeEdges {
+struct WEdges {
     int e[kMaxDeg], m[kMaxDeg], lo[kMaxDeg], hi[kMaxDeg];
     unsigned own;  // bit j: the node is edges(1, e_j) (it owns the edge flux)
     int deg, nzmin, nzmax;
 };
 
-__device__ __forceinline__ void stage_node(const DTopo &tp, int n, NodeEdges &S) {
+__device__ __forceinline__ void stage_edges(const DTopo &tp, int n, int lane, WEdges &S) {
     const int k0 = tp.ne_ptr[n];
-    const int deg = tp.ne_ptr[n + 1] - k0;
-    if (threadIdx.x < deg && threadIdx.x < kMaxDeg) {
-        const int j = threadIdx.x;
-        const int code = tp.ne_idx[k0 + j];
+    const int deg = min(tp.ne_ptr[n + 1] - k0, kMaxDeg);
+    int code = 0;
+    if (lane < deg) {
+        code = tp.ne_idx[k0 + lane];
         const int e = code >= 0 ? code : ~code;
-        S.e[j] = e;
-        S.m[j] = code >= 0 ? tp.e_n2[e] : tp.e_n1[e];
-        S.lo[j] = tp.e_lo[e];
-        S.hi[j] = tp.e_hi[e];
+        S.e[lane] = e;
+        S.m[lane] = code >= 0 ? tp.e_n2[e] : tp.e_n1[e];
+        S.lo[lane] = tp.e_lo[e];
+        S.hi[lane] = tp.e_hi[e];
     }
-    if (threadIdx.x == 32) {
-        unsigned own = 0;
-        for (int j = 0; j < deg && j < kMaxDeg; j++)
-            if (tp.ne_idx[k0 + j] >= 0) own |= 1u << j;
+    const unsigned own = __ballot_sync(kFull, lane < deg && code >= 0);
+    if (lane == 0) {
         S.own = own;
         S.deg = deg;
         S.nzmin = tp.n_ulev[n];
         S.nzmax = tp.n_nlev[n];
     }
+    __syncwarp();
+}
+
+// chunk ch of a column, HU halo levels above and HD below the stored levels
+template <int HU, int HD>
+struct Chunk {
+    static constexpr int OUT = 32 - HU - HD;
+    int nz;
+    bool lvl, out;
+    __device__ __forceinline__ Chunk(int nzmin, int nzmax, int ch, int lane) {
+        nz = nzmin - HU + OUT * ch + lane;
+        lvl = nz >= nzmin && nz <= nzmax - 1;
+        out = lvl && lane >= HU && lane < 32 - HD;
+    }
+    static __device__ __forceinline__ int count(int nzmin, int nzmax) { return (nzmax - nzmin + OUT - 1) / OUT; }
+};
+
+__device__ __forceinline__ float sh_up(float v, int d) { return __shfl_up_sync(kFull, v, d); }
+__device__ __forceinline__ float sh_dn(float v, int d) { return __shfl_down_sync(kFull, v, d); }
+
+// Adams-Bashforth value minus the current value: AB2 -(0.5+eps) T^{n-1} + (1.5+eps) T^n,
+// AB3 (23 T^n - 16 T^{n-1} + 5 T^{n-2}) / 12 (oce_tracer_mod.F90:53, 67-68), eps = 0.1
+__device__ __forceinline__ float ab_delta(int ab, float t, float o1, float o2) {
+    return ab == 2 ? 0.6f * (t - o1) : (11.f * (t - o1) - 5.f * (o1 - o2)) * (1.f / 12.f);
 }
 
 // area-weighted mean over the node's wet elements of the element gradient,
@@ -200,137 +215,218 @@ __device__ __noinline__ float node_grad_proj(const DTopo &tp, const DGeom<float>
     return exa * (tx / tvol) + eyr * (ty / tvol);
 }
 
+
 // ---------------------------------------------------------------------------
 // k32_lo_ad
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kT)
-k32_lo_ad(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, MusclW mw, const float *VF, float dt) {
-    __shared__ NodeEdges S;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+template <int KD>
+__device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
+                                           const B32View &B, const float *__restrict__ VF, float dt, int n, int lane,
+                                           const WEdges &S) {
+    using C = Chunk<2, 1>;
     const int L1 = tp.L1, nl = tp.nl;
-    const float RE = (float)kREarth;
-    for (int n = blockIdx.x; n < tp.N2; n += gridDim.x) {
-        __syncthreads();
-        stage_node(tp, n, S);
-        __syncthreads();
-        const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
-        for (int t = warp; t < B.ntr; t += kW) {
+    const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
+    const unsigned own = S.own;
+    const int nch = C::count(nzmin, nzmax);
+    for (int ch = 0; ch < nch; ch++) {
+        const C k(nzmin, nzmax, ch, lane);
+        const int nz = k.nz;
+        const int i = n * L1 + nz - 1;   // layer nz of the node (valid where k.lvl)
+        const int iv = n * nl + nz - 1;  // interface nz
+        // ---- tracer-independent part of the chunk ----
+        int off[KD];
+        float v[KD];
+        unsigned okm = 0;
+        float Dh = 0.f;  // net horizontal volume flux into the node
+#pragma unroll
+        for (int u = 0; u < KD; u++) {
+            const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
+            off[u] = S.m[u] * L1 + nz - 1;
+            v[u] = ok ? VF[S.e[u] * L1 + nz - 1] : 0.f;
+            okm |= ok ? 1u << u : 0u;
+            Dh += ((own >> u) & 1u) ? -v[u] : v[u];
+        }
+        float ar0 = 0.f, we0 = 0.f, w0 = 0.f, sdt = 0.f, Z0 = 0.f, hr = 0.f;
+        if (k.lvl) {
+            ar0 = g.area[iv];
+            we0 = f.we[iv];
+            w0 = f.w[iv];
+            const float ihn = 1.f / g.hnode_new[i];
+            sdt = dt / g.areasvol[iv] * ihn;
+            hr = g.hnode[i] * ihn;
+            Z0 = g.Z3[i];
+        }
+        const float Zm1 = sh_up(Z0, 1), Zm2 = sh_up(Z0, 2), Zp1 = sh_dn(Z0, 1);
+        // QR4C interior geometry, nzmin+2 <= nz <= nzmax-2 (oce_adv_tra_ver.F90:409-425)
+        const bool qint = k.out && nz >= nzmin + 2 && nz <= nzmax - 2;
+        float idz0 = 0.f, idzp = 0.f, idzm = 0.f, g1 = 0.f, g2 = 0.f;
+        if (qint) {
+            const float zb = g.zbar3[iv];
+            idz0 = 1.f / (Zm1 - Z0);
+            idzp = 1.f / (Z0 - Zp1);
+            idzm = 1.f / (Zm2 - Zm1);
+            g1 = (zb - Z0) * (1.f / 3.f);
+            g2 = (zb - Zm1) * (1.f / 3.f);
+        }
+        const bool twolayer = nzmin + 1 == nzmax - 1;
+        // ---- per tracer ----
+#pragma unroll 1
+        for (int t = 0; t < B.ntr; t++) {
             const DCfg c = B.cfg[t];
-            const int fct = c.lim;
-            const float *T = B.T + t * B.sN;
-            const float *O1 = B.O1 + t * B.sN;
-            const float *O2 = B.ab == 3 ? B.O2 + t * B.sN : nullptr;
-            auto tab = [&](size_t i) {
-                const float v = T[i];
-                return B.ab == 2 ? -(0.6f * O1[i]) + 1.6f * v : (5.0f * O2[i] - 16.0f * O1[i] + 23.0f * v) * (1.0f / 12.0f);
-            };
-            for (int nz = nzmin + lane; nz <= nzmax; nz += 32) {
-                float fv0 = 0.f, fv1 = 0.f;
-                if (fct) {
-                    fv0 = vupw(T, f.we, g.area, nz, n, nzmin, nzmax, L1, nl);
-                    if (nz <= nzmax - 1) fv1 = vupw(T, f.we, g.area, nz + 1, n, nzmin, nzmax, L1, nl);
-                }
-                const float *pw = fct ? f.w : f.we;
-                const float ar = g.area[iN(nz, n, nl)];
-                float ho;
-                if (nz == nzmax) {
-                    ho = 0.f;
-                } else if (nz == nzmin) {
-                    ho = -(tab(i1(nz, n, L1)) * pw[iN(nz, n, nl)] * ar);
-                } else if (c.ver != 0 || nz == nzmin + 1 || nz == nzmax - 1) {
-                    const float w = pw[iN(nz, n, nl)];
-                    const float t0 = tab(i1(nz, n, L1)), tm1 = tab(i1(nz - 1, n, L1));
-                    if (c.ver == 0) {
-                        ho = -(0.5f * (tm1 + t0) * w * ar);
-                        // a two-layer column writes this row twice: flux = C - (C - flux_in)
-                        if (nzmin + 1 == nzmax - 1) ho = ho - (ho - fv0) + fv0;
-                    } else {
-                        const float aw = fabsf(w);
-                        ho = -(0.5f * (t0 * (w + aw) + tm1 * (w - aw)) * ar);
-                    }
+            const size_t to = (size_t)t * B.sN;
+            const float *__restrict__ T = B.T + to;
+            const float *__restrict__ O1 = B.O1 + to;
+            const float *__restrict__ O2 = B.ab == 3 ? B.O2 + to : O1;
+            float Tn = 0.f, dab = 0.f;
+            if (k.lvl) {
+                Tn = T[i];
+                dab = ab_delta(B.ab, Tn, O1[i], B.ab == 3 ? O2[i] : 0.f);
+            }
+            const float tab = Tn + dab;
+            const float Tu = sh_up(Tn, 1);
+            const float tabu = sh_up(tab, 1), tabu2 = sh_up(tab, 2), tabd = sh_dn(tab, 1);
+            float tm[KD];
+#pragma unroll
+            for (int u = 0; u < KD; u++) tm[u] = ((okm >> u) & 1u) ? T[off[u]] : 0.f;
+            // LO: upwind edge fluxes in difference form, sum_j am_j (T_j - T_n) + Dh T_n
+            float hs = Dh * Tn;
+#pragma unroll
+            for (int u = 0; u < KD; u++) {
+                if (!((okm >> u) & 1u)) continue;
+                const float am = ((own >> u) & 1u) ? -fminf(v[u], 0.f) : fmaxf(v[u], 0.f);
+                hs += am * (tm[u] - Tn);
+            }
+            // upwind vertical flux with w_e at interface nz (adv_tra_ver_upw1)
+            float fv0 = 0.f;
+            if (k.lvl) {
+                if (nz == nzmin) {
+                    fv0 = -(we0 * Tn * ar0);
                 } else {
-                    const float tm2 = tab(i1(nz - 2, n, L1)), tm1 = tab(i1(nz - 1, n, L1));
-                    const float t0 = tab(i1(nz, n, L1)), tp1 = tab(i1(nz + 1, n, L1));
-                    const float zm2 = g.Z3[i1(nz - 2, n, L1)], zm1 = g.Z3[i1(nz - 1, n, L1)];
-                    const float z0 = g.Z3[i1(nz, n, L1)], zp1 = g.Z3[i1(nz + 1, n, L1)];
-                    const float qc = (tm1 - t0) / (zm1 - z0);
-                    const float qu = (t0 - tp1) / (z0 - zp1);
-                    const float qd = (tm2 - tm1) / (zm2 - zm1);
-                    const float zb = g.zbar3[iN(nz, n, nl)];
-                    const float Tm1 = t0 + (2.f * qc + qu) * (zb - z0) * (1.f / 3.f);
-                    const float Tm2 = tm1 + (2.f * qc + qd) * (zb - zm1) * (1.f / 3.f);
-                    const float w = pw[iN(nz, n, nl)], aw = fabsf(w);
-                    const float no = (float)c.pv;
-                    const float Tmean = (w + aw) * Tm1 + (w - aw) * Tm2;
-                    ho = (-(0.5f * (1.f - no) * Tmean) - no * (0.5f * (Tm1 + Tm2)) * w) * ar;
-                }
-                B.ADv[t * B.sNI + iN(nz, n, nl)] = ho - fv0;
-                if (nz > nzmax - 1) continue;
-                const size_t i = i1(nz, n, L1);
-                const float Tn = T[i];
-                const float TAn = tab(i);
-                Kahan acc;
-                for (int g0 = 0; g0 < deg; g0 += kU) {
-                    float vf[kU], tm[kU];
-                    bool ok[kU];
-#pragma unroll
-                    for (int u = 0; u < kU; u++) {
-                        const int j = g0 + u;
-                        ok[u] = j < deg && nz >= S.lo[j] && nz <= S.hi[j];
-                        vf[u] = ok[u] ? VF[i1(nz, S.e[j], L1)] : 0.f;
-                        tm[u] = ok[u] ? T[i1(nz, S.m[j], L1)] : 0.f;
-                    }
-#pragma unroll
-                    for (int u = 0; u < kU; u++) {
-                        if (!ok[u]) continue;
-                        const int j = g0 + u;
-                        const bool own = (S.own >> j) & 1u;
-                        const float v = vf[u], av = fabsf(v);
-                        const float T1 = own ? Tn : tm[u], T2 = own ? tm[u] : Tn;
-                        const float flo = fct ? -(0.5f * (T1 * (v + av) + T2 * (v - av))) : 0.f;
-                        if (fct) acc.add(own ? flo : -flo);
-                        if (!own) continue;
-                        // owned edge: high-order flux on the AB values
-                        const int e = S.e[j], m = S.m[j];
-                        const float t1 = TAn, t2 = tab(i1(nz, m, L1));
-                        float hf;
-                        if (c.hor == 2) {
-                            hf = -(0.5f * (t1 * (v + av) + t2 * (v - av)));
-                        } else {
-                            const int4 un = mw.un[e], dn = mw.dn[e];
-                            const float4 wu = mw.wu[e], wd = mw.wd[e];
-                            const int gzmin = un.w & 0xffff, gzmax = un.w >> 16;
-                            float s1, s2;
-                            if (nz >= gzmin && nz <= gzmax - 1) {
-                                s1 = wu.x * T[i1(nz, un.x, L1)] + wu.y * T[i1(nz, un.y, L1)] + wu.z * T[i1(nz, un.z, L1)];
-                                s2 = wd.x * T[i1(nz, dn.x, L1)] + wd.y * T[i1(nz, dn.y, L1)] + wd.z * T[i1(nz, dn.z, L1)];
-                            } else {
-                                const float exa = g.edxy[2 * (size_t)e] * wu.w;
-                                const float eyr = g.edxy[2 * (size_t)e + 1] * RE;
-                                s1 = node_grad_proj(tp, g, T, n, nz, exa, eyr);
-                                s2 = node_grad_proj(tp, g, T, m, nz, exa, eyr);
-                            }
-                            float clo1 = 1.f, clo2 = 1.f;
-                            if (c.hor == 0) {
-                                clo1 = (tp.n_nbl[n] - nz) >= 0 ? 1.f : 0.f;
-                                clo2 = (tp.n_nbl[m] - nz) >= 0 ? 1.f : 0.f;
-                            }
-                            const float d2 = 2.f * (t2 - t1);
-                            const float Tm2 = t2 - (d2 + s2) * (1.f / 6.f) * clo2;
-                            const float Tm1 = t1 + (d2 + s1) * (1.f / 6.f) * clo1;
-                            const float no = (float)c.ph;
-                            const float cHO = (v + av) * Tm1 + (v - av) * Tm2;
-                            hf = -(0.5f * (1.f - no) * cHO) - v * no * 0.5f * (Tm1 + Tm2);
-                        }
-                        B.ADh[t * B.sE + i1(nz, e, L1)] = hf - flo;
-                    }
-                }
-                if (fct) {
-                    acc.add(fv0);
-                    acc.add(-fv1);
-                    B.LOi[t * B.sN + i] = acc.get() * dt / g.areasvol[iN(nz, n, nl)];
+                    const float aw = fabsf(we0);
+                    fv0 = -(0.5f * (Tn * (we0 + aw) + Tu * (we0 - aw)) * ar0);
                 }
             }
+            float fv1 = sh_dn(fv0, 1);
+            if (nz == nzmax - 1) fv1 = 0.f;
+            // LO = (T hnode + flux divergence dt / areasvol) / hnode_new (oce_adv_tra_driver.F90:249)
+            if (k.out) B.LO[to + i] = Tn * hr + (hs + fv0 - fv1) * sdt;
+            // vertical high-order flux on the AB values (QR4C / UPW1), minus the LO flux
+            if (k.out) {
+                const float pw = c.lim ? w0 : we0;
+                float Cf;
+                if (nz == nzmin) {
+                    Cf = -(tab * pw * ar0);
+                } else if (c.ver != 0 || nz == nzmin + 1 || nz == nzmax - 1) {
+                    if (c.ver == 0) {
+                        Cf = -(0.5f * (tabu + tab) * pw * ar0);
+                    } else {
+                        const float aw = fabsf(pw);
+                        Cf = -(0.5f * (tab * (pw + aw) + tabu * (pw - aw)) * ar0);
+                    }
+                } else {
+                    const float qc = (tabu - tab) * idz0;
+                    const float qu = (tab - tabd) * idzp;
+                    const float qd = (tabu2 - tabu) * idzm;
+                    const float Tm1 = tab + (2.f * qc + qu) * g1;
+                    const float Tm2 = tabu + (2.f * qc + qd) * g2;
+                    const float aw = fabsf(pw), no = (float)c.pv;
+                    const float Tmean = (pw + aw) * Tm1 + (pw - aw) * Tm2;
+                    Cf = (-(0.5f * (1.f - no) * Tmean) - no * (0.5f * (Tm1 + Tm2)) * pw) * ar0;
+                }
+                // flux = C - flux_in; FCT passes the LO flux in, otherwise zero
+                const float fin = c.lim ? fv0 : 0.f;
+                float F = Cf - fin;
+                // a two-layer column writes its middle interface twice (statements nzmin+1, nzmax-1)
+                if (c.ver == 0 && twolayer && nz == nzmin + 1) F = Cf - F;
+                B.ADv[(size_t)t * B.sNI + iv] = c.lim ? F : F - fv0;
+            }
+        }
+    }
+}
+
+// the node of a warp: consecutive nodes, or (WIDE) the listed nodes of more than 8 edges
+template <bool WIDE>
+__device__ __forceinline__ int warp_node(const DTopo &tp, int warp) {
+    const int j = blockIdx.x * kWB + warp;
+    if (WIDE) return j < tp.n_wide ? tp.wide_nodes[j] : -1;
+    return j < tp.N2 ? j : -1;
+}
+
+template <bool WIDE>
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : kMinBlocks)
+k32_lo_ad(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, const float *__restrict__ VF, float dt) {
+    __shared__ WEdges Se[kWB];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int n = warp_node<WIDE>(tp, warp);
+    if (n < 0) return;
+    WEdges &S = Se[warp];
+    stage_edges(tp, n, lane, S);
+    if ((S.deg > 8) != WIDE) return;
+    lo_ad_node<WIDE ? kMaxDeg : 8>(tp, g, f, B, VF, dt, n, lane, S);
+}
+
+// ---------------------------------------------------------------------------
+// k32_ho: high-order minus low-order flux of every edge-layer
+// ---------------------------------------------------------------------------
+// One warp per edge, the lanes over the edge's levels [nu12, nl12].  MUSCL / MFCT
+// (adv_tra_hor_muscl / _mfct, oce_adv_tra_hor.F90:261-834) on the AB values with the
+// gradients of fill_up_dn_grad (oce_muscl_adv.F90:356-525) folded into per-edge
+// weights of the up / down triangles' node values; UPW1 (:64-257).  The LO flux is
+// the upwind flux of the current values (oce_adv_tra_driver.F90:131-190).
+__global__ void __launch_bounds__(kTB, kMinBlocks)
+k32_ho(DTopo tp, DGeom<float> g, B32View B, MusclW mw, const float *__restrict__ VF) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int e = blockIdx.x * kWB + warp;
+    if (e >= tp.E2) return;
+    const int L1 = tp.L1;
+    const int n1 = tp.e_n1[e], n2 = tp.e_n2[e];
+    const int elo = tp.e_lo[e], ehi = tp.e_hi[e];
+    const int nbl1 = tp.n_nbl[n1], nbl2 = tp.n_nbl[n2];
+    const int4 un = mw.un[e], dn = mw.dn[e];
+    const float4 wu = mw.wu[e], wd = mw.wd[e];
+    const int gzmin = un.w & 0xffff, gzmax = un.w >> 16;
+    const float exa = g.edxy[2 * (size_t)e] * wu.w, eyr = g.edxy[2 * (size_t)e + 1] * (float)kREarth;
+    for (int nz0 = elo; nz0 <= ehi; nz0 += 32) {
+        const int nz = nz0 + lane;
+        const bool ok = nz <= ehi;
+        const int ie = e * L1 + nz - 1, ia = n1 * L1 + nz - 1, ib = n2 * L1 + nz - 1;
+        const float v = ok ? VF[ie] : 0.f, vp = fmaxf(v, 0.f), vm = fminf(v, 0.f);
+        const bool tri = nz >= gzmin && nz <= gzmax - 1;
+        const float cl1 = (nbl1 - nz) >= 0 ? 1.f : 0.f, cl2 = (nbl2 - nz) >= 0 ? 1.f : 0.f;
+#pragma unroll 1
+        for (int t = 0; t < B.ntr; t++) {
+            if (!ok) continue;
+            const DCfg c = B.cfg[t];
+            const size_t to = (size_t)t * B.sN;
+            const float *__restrict__ T = B.T + to;
+            const float *__restrict__ O1 = B.O1 + to;
+            const float *__restrict__ O2 = B.ab == 3 ? B.O2 + to : O1;
+            const float T1 = T[ia], T2 = T[ib];
+            const float t1 = T1 + ab_delta(B.ab, T1, O1[ia], B.ab == 3 ? O2[ia] : 0.f);
+            const float t2 = T2 + ab_delta(B.ab, T2, O1[ib], B.ab == 3 ? O2[ib] : 0.f);
+            const float flo = -(T1 * vp + T2 * vm);
+            float hf;
+            if (c.hor == 2) {
+                hf = -(t1 * vp + t2 * vm);
+            } else {
+                float s1, s2;
+                if (tri) {
+                    s1 = wu.x * T[un.x * L1 + nz - 1] + wu.y * T[un.y * L1 + nz - 1] + wu.z * T[un.z * L1 + nz - 1];
+                    s2 = wd.x * T[dn.x * L1 + nz - 1] + wd.y * T[dn.y * L1 + nz - 1] + wd.z * T[dn.z * L1 + nz - 1];
+                } else {
+                    s1 = node_grad_proj(tp, g, T, n1, nz, exa, eyr);
+                    s2 = node_grad_proj(tp, g, T, n2, nz, exa, eyr);
+                }
+                // c_lo = 1 up to nboundary_lay (MUSCL), always 1 (MFCT)
+                const float clo1 = c.hor == 0 ? cl1 : 1.f, clo2 = c.hor == 0 ? cl2 : 1.f;
+                const float d2 = 2.f * (t2 - t1);
+                const float Tm2 = t2 - (d2 + s2) * (1.f / 6.f) * clo2;
+                const float Tm1 = t1 + (d2 + s1) * (1.f / 6.f) * clo1;
+                const float no = (float)c.ph;
+                const float cHO = 2.f * (vp * Tm1 + vm * Tm2);
+                hf = -(0.5f * (1.f - no) * cHO) - v * no * 0.5f * (Tm1 + Tm2);
+            }
+            B.ADh[(size_t)t * B.sE + ie] = hf - flo;
         }
     }
 }
@@ -338,97 +434,89 @@ k32_lo_ad(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, MusclW mw, con
 // ---------------------------------------------------------------------------
 // k32_bounds: FCT bounds and R+ / R- (FCT tracers only)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kT) k32_bounds(DTopo tp, DGeom<float> g, B32View B, float dt) {
-    __shared__ NodeEdges S;
-    extern __shared__ __align__(16) float sm32[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+template <int KD>
+__device__ __forceinline__ void bounds_node(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int n,
+                                            int lane, const WEdges &S) {
+    using C = Chunk<1, 1>;
     const int L1 = tp.L1, nl = tp.nl;
-    float *tvmax = sm32 + (size_t)warp * 2 * (L1 + 2);
-    float *tvmin = tvmax + (L1 + 2);
+    const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
+    const unsigned own = S.own;
     const float eps = (float)kFluxEps;
-    for (int n = blockIdx.x; n < tp.N2; n += gridDim.x) {
-        __syncthreads();
-        stage_node(tp, n, S);
-        __syncthreads();
-        const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
-        for (int t = warp; t < B.ntr; t += kW) {
+    const int nch = C::count(nzmin, nzmax);
+    for (int ch = 0; ch < nch; ch++) {
+        const C k(nzmin, nzmax, ch, lane);
+        const int nz = k.nz;
+        const int i = n * L1 + nz - 1, iv = n * nl + nz - 1;
+        int off[KD];
+        unsigned okm = 0;
+#pragma unroll
+        for (int u = 0; u < KD; u++) {
+            const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
+            off[u] = S.m[u] * L1 + nz - 1;
+            okm |= ok ? 1u << u : 0u;
+        }
+        const float s = k.lvl ? dt / (g.areasvol[iv] * g.hnode_new[i]) : 0.f;
+#pragma unroll 1
+        for (int t = 0; t < B.ntr; t++) {
             if (!B.cfg[t].lim) continue;
-            const float *T = B.T + t * B.sN;
-            const float *LOi = B.LOi + t * B.sN;
-            for (int nz = nzmin + lane; nz <= nzmax - 1; nz += 32) {
-                const size_t i = i1(nz, n, L1);
-                const float tt = T[i];
-                const float lo = (tt * g.hnode[i] + LOi[i]) / g.hnode_new[i];
-                float mx = fmaxf(lo, tt), mn = fminf(lo, tt);
-                for (int g0 = 0; g0 < deg; g0 += kU) {
-                    float tm[kU], li[kU], hm[kU], hnm[kU];
-                    bool ok[kU];
-#pragma unroll
-                    for (int u = 0; u < kU; u++) {
-                        const int j = g0 + u;
-                        ok[u] = j < deg && nz >= S.lo[j] && nz <= S.hi[j];
-                        const size_t jj = ok[u] ? i1(nz, S.m[j], L1) : i;
-                        tm[u] = T[jj];
-                        li[u] = LOi[jj];
-                        hm[u] = g.hnode[jj];
-                        hnm[u] = g.hnode_new[jj];
-                    }
-#pragma unroll
-                    for (int u = 0; u < kU; u++) {
-                        if (!ok[u]) continue;
-                        const float lm = (tm[u] * hm[u] + li[u]) / hnm[u];
-                        mx = fmaxf(mx, fmaxf(lm, tm[u]));
-                        mn = fminf(mn, fminf(lm, tm[u]));
-                    }
-                }
-                tvmax[nz] = mx;
-                tvmin[nz] = mn;
+            const size_t to = (size_t)t * B.sN;
+            const float *__restrict__ T = B.T + to;
+            const float *__restrict__ LO = B.LO + to;
+            const float *__restrict__ ADh = B.ADh + (size_t)t * B.sE;
+            float Tn = 0.f, lo = 0.f, v0 = 0.f;
+            if (k.lvl) {
+                Tn = T[i];
+                lo = LO[i];
+                v0 = B.ADv[(size_t)t * B.sNI + iv];
             }
-            __syncwarp();
-            const float *ADv = B.ADv + t * B.sNI;
-            const float *ADh = B.ADh + t * B.sE;
-            for (int nz = nzmin + lane; nz <= nzmax - 1; nz += 32) {
-                const size_t i = i1(nz, n, L1);
-                const float lo = (T[i] * g.hnode[i] + LOi[i]) / g.hnode_new[i];
-                float tup, tlo;
-                if (nz == nzmin || nz == nzmax - 1) {
-                    tup = tvmax[nz];
-                    tlo = tvmin[nz];
-                } else {
-                    tup = fmaxf(fmaxf(tvmax[nz - 1], tvmax[nz]), tvmax[nz + 1]);
-                    tlo = fminf(fminf(tvmin[nz - 1], tvmin[nz]), tvmin[nz + 1]);
-                }
+            // bounds over the node, its neighbours and the layers above and below
+            // (oce_adv_tra_fct.F90:124-248)
+            float mx = fmaxf(lo, Tn), mn = fminf(lo, Tn);
+            float P = 0.f, M = 0.f;
+#pragma unroll
+            for (int u = 0; u < KD; u++) {
+                const bool ok = (okm >> u) & 1u;
+                const float tm = ok ? T[off[u]] : Tn;
+                const float lm = ok ? LO[off[u]] : lo;
+                const float x = ok ? ADh[S.e[u] * L1 + nz - 1] : 0.f;
+                mx = fmaxf(mx, fmaxf(lm, tm));
+                mn = fminf(mn, fminf(lm, tm));
+                const float xv = ((own >> u) & 1u) ? x : -x;
+                P += fmaxf(0.f, xv);
+                M += fminf(0.f, xv);
+            }
+            const float mxu = sh_up(mx, 1), mxd = sh_dn(mx, 1), mnu = sh_up(mn, 1), mnd = sh_dn(mn, 1);
+            float tup = mx, tlo = mn;
+            if (nz != nzmin && nz != nzmax - 1) {
+                tup = fmaxf(fmaxf(mxu, mx), mxd);
+                tlo = fminf(fminf(mnu, mn), mnd);
+            }
+            // P / M: sums of the positive / negative antidiffusive fluxes into the node
+            float v1 = sh_dn(v0, 1);
+            if (nz == nzmax - 1) v1 = 0.f;
+            P += fmaxf(0.f, v0) + fmaxf(0.f, -v1);
+            M += fminf(0.f, v0) + fminf(0.f, -v1);
+            if (k.out) {
                 const float bmx = tup - lo, bmn = tlo - lo;
-                const float v0 = ADv[iN(nz, n, nl)], v1 = ADv[iN(nz + 1, n, nl)];
-                Kahan P, M;
-                P.add(fmaxf(0.f, v0) + fmaxf(0.f, -v1));
-                M.add(fminf(0.f, v0) + fminf(0.f, -v1));
-                for (int g0 = 0; g0 < deg; g0 += kU) {
-                    float x[kU];
-                    bool ok[kU];
-#pragma unroll
-                    for (int u = 0; u < kU; u++) {
-                        const int j = g0 + u;
-                        ok[u] = j < deg && nz >= S.lo[j] && nz <= S.hi[j];
-                        x[u] = ok[u] ? ADh[i1(nz, S.e[j], L1)] : 0.f;
-                    }
-#pragma unroll
-                    for (int u = 0; u < kU; u++) {
-                        if (!ok[u]) continue;
-                        const float xv = ((S.own >> (g0 + u)) & 1u) ? x[u] : -x[u];
-                        P.add(fmaxf(0.f, xv));
-                        M.add(fminf(0.f, xv));
-                    }
-                }
-                const float s = dt / (g.areasvol[iN(nz, n, nl)] * g.hnode_new[i]);
-                B.R[t * B.sN + i] = make_float2(fminf(1.f, bmx / (P.get() * s + eps)), fminf(1.f, bmn / (M.get() * s - eps)));
+                B.R[to + i] = make_float2(fminf(1.f, bmx / (P * s + eps)), fminf(1.f, bmn / (M * s - eps)));
                 // the bounds themselves: the update clamps the advected value into them, so
                 // FP32 rounding in the limiter can never create a new extremum
-                B.TB[t * B.sN + i] = make_float2(tup, tlo);
+                B.TB[to + i] = make_float2(tup, tlo);
             }
-            __syncwarp();
         }
     }
+}
+
+template <bool WIDE>
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : kMinBlocks) k32_bounds(DTopo tp, DGeom<float> g, B32View B, float dt) {
+    __shared__ WEdges Se[kWB];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int n = warp_node<WIDE>(tp, warp);
+    if (n < 0) return;
+    WEdges &S = Se[warp];
+    stage_edges(tp, n, lane, S);
+    if ((S.deg > 8) != WIDE) return;
+    bounds_node<WIDE ? kMaxDeg : 8>(tp, g, B, dt, n, lane, S);
 }
 
 // ---------------------------------------------------------------------------
@@ -457,152 +545,160 @@ __device__ __forceinline__ void scan_down(float &A, float &B, int lane) {
     }
 }
 
-__global__ void __launch_bounds__(kT)
-k32_update(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, VFactors vf, float dt) {
-    __shared__ NodeEdges S;
-    extern __shared__ __align__(16) float sm32[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+template <int KD>
+__device__ __forceinline__ void advect_node(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int n,
+                                            int lane, const WEdges &S) {
+    using C = Chunk<1, 1>;
     const int L1 = tp.L1, nl = tp.nl;
-    float *Ta = sm32 + (size_t)warp * (L1 + 2);
-    for (int n = blockIdx.x; n < tp.N2; n += gridDim.x) {
-        __syncthreads();
-        stage_node(tp, n, S);
-        __syncthreads();
-        const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
-        const int nch = (nzmax - nzmin + 31) / 32;
-        for (int t = warp; t < B.ntr; t += kW) {
-            const DCfg c = B.cfg[t];
-            const int fct = c.lim;
-            const float *T = B.T + t * B.sN;
-            const float *ADv = B.ADv + t * B.sNI;
-            const float *ADh = B.ADh + t * B.sE;
-            const float2 *R = B.R + t * B.sN;
-            float tadv[kMaxChunks];
+    const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
+    const unsigned own = S.own;
+    const int nch = C::count(nzmin, nzmax);
+    for (int ch = 0; ch < nch; ch++) {
+        const C k(nzmin, nzmax, ch, lane);
+        const int nz = k.nz;
+        const int i = n * L1 + nz - 1, iv = n * nl + nz - 1;
+        int off[KD];
+        unsigned okm = 0;
 #pragma unroll
-            for (int ch = 0; ch < kMaxChunks; ch++) {
-                const int nz = nzmin + 32 * ch + lane;
-                tadv[ch] = 0.f;
-                if (ch >= nch || nz > nzmax - 1) continue;
-                const size_t i = i1(nz, n, L1);
-                const float sdt = dt / g.areasvol[iN(nz, n, nl)];
-                Kahan del;
-                float f0 = ADv[iN(nz, n, nl)], f1 = ADv[iN(nz + 1, n, nl)];
-                float2 r0 = make_float2(1.f, 1.f);
-                if (fct) {
-                    del.add(B.LOi[t * B.sN + i]);
-                    r0 = R[i];
-                    // vertical limiting (oce_adv_tra_fct.F90:425-456); the bottom interface is not limited
-                    if (nz == nzmin) {
-                        f0 *= f0 >= 0.f ? fminf(1.f, r0.x) : fminf(1.f, r0.y);
-                    } else {
-                        const float2 rm = R[i - 1];
-                        f0 *= f0 >= 0.f ? fminf(fminf(1.f, rm.y), r0.x) : fminf(fminf(1.f, rm.x), r0.y);
-                    }
-                    if (nz + 1 <= nzmax - 1) {
-                        const float2 rp = R[i + 1];
-                        f1 *= f1 >= 0.f ? fminf(fminf(1.f, r0.y), rp.x) : fminf(fminf(1.f, r0.x), rp.y);
-                    }
-                }
-                del.add(f0 * sdt);
-                del.add(-(f1 * sdt));
-                for (int g0 = 0; g0 < deg; g0 += kU) {
-                    float x[kU];
-                    float2 rm[kU];
-                    bool ok[kU];
-#pragma unroll
-                    for (int u = 0; u < kU; u++) {
-                        const int j = g0 + u;
-                        ok[u] = j < deg && nz >= S.lo[j] && nz <= S.hi[j];
-                        x[u] = ok[u] ? ADh[i1(nz, S.e[j], L1)] : 0.f;
-                        rm[u] = (ok[u] && fct) ? R[i1(nz, S.m[j], L1)] : make_float2(1.f, 1.f);
-                    }
-#pragma unroll
-                    for (int u = 0; u < kU; u++) {
-                        if (!ok[u]) continue;
-                        const bool own = (S.own >> (g0 + u)) & 1u;
-                        float xv = x[u];
-                        if (fct) {
-                            // R of edges(1,e) and edges(2,e)
-                            const float2 ra = own ? r0 : rm[u], rb = own ? rm[u] : r0;
-                            xv *= xv >= 0.f ? fminf(fminf(1.f, ra.x), rb.y) : fminf(fminf(1.f, ra.y), rb.x);
-                        }
-                        del.add(own ? xv * sdt : -(xv * sdt));
-                    }
-                }
-                del.add(T[i] * (g.hnode[i] - g.hnode_new[i]));
-                float v = T[i] + del.get() / g.hnode_new[i];
-                if (fct) {
-                    const float2 tb = B.TB[t * B.sN + i];
-                    const float vc = fminf(fmaxf(v, tb.y), tb.x);
-                    // a clamp beyond round-off means the limiter itself failed
-                    if (fabsf(vc - v) > 1e-5f * (tb.x - tb.y) + 1e-6f * fabsf(vc)) atomicOr(B.status, 2u);
-                    v = vc;
-                }
-                tadv[ch] = v;
-                Ta[nz] = v;
-            }
-            float *Tout = B.Tnew + t * B.sN;
-            if (!c.ivd) {
-#pragma unroll
-                for (int ch = 0; ch < kMaxChunks; ch++) {
-                    const int nz = nzmin + 32 * ch + lane;
-                    if (ch < nch && nz <= nzmax - 1) {
-                        Tout[i1(nz, n, L1)] = tadv[ch];
-                        if (!isfinite(tadv[ch])) atomicOr(B.status, 1u);
-                    }
-                }
-                __syncwarp();
-                continue;
-            }
-            __syncwarp();
-            // forward substitution: tp_k = inv_k*rhs_k - a_k*inv_k*tp_{k-1}
-            float tpv[kMaxChunks];
-            float carry = 0.f;
-            const float bc = f.bc ? f.bc[(size_t)t * tp.N2 + n] : 0.f;
-#pragma unroll
-            for (int ch = 0; ch < kMaxChunks; ch++) {
-                tpv[ch] = 0.f;
-                if (ch >= nch) continue;
-                const int nz = nzmin + 32 * ch + lane;
-                float A = 1.f, Bv = 0.f;
-                if (nz <= nzmax - 1) {
-                    const size_t i = i1(nz, n, L1);
-                    const float a = vf.a[i], cc = vf.c[i], inv = vf.inv[i];
-                    const float t0 = tadv[ch];
-                    float rhs = 0.f;
-                    if (nz > nzmin) rhs -= a * (Ta[nz - 1] - t0);
-                    if (nz < nzmax - 1) rhs -= cc * (Ta[nz + 1] - t0);
-                    if (nz == nzmin) rhs += bc;
-                    A = -(a * inv);
-                    Bv = rhs * inv;
-                }
-                scan_up(A, Bv, lane);
-                const float y = A * carry + Bv;
-                tpv[ch] = y;
-                carry = __shfl_sync(kFull, y, 31);
-            }
-            // back substitution: x_k = tp_k - cp_k * x_{k+1}
-            carry = 0.f;
-#pragma unroll
-            for (int ch = kMaxChunks - 1; ch >= 0; ch--) {
-                if (ch >= nch) continue;
-                const int nz = nzmin + 32 * ch + lane;
-                float A = 1.f, Bv = 0.f;
-                if (nz <= nzmax - 1) {
-                    A = -vf.cp[i1(nz, n, L1)];
-                    Bv = tpv[ch];
-                }
-                scan_down(A, Bv, lane);
-                const float x = A * carry + Bv;
-                carry = __shfl_sync(kFull, x, 0);
-                if (nz <= nzmax - 1) {
-                    const float v = tadv[ch] + x;
-                    Tout[i1(nz, n, L1)] = v;
-                    if (!isfinite(v)) atomicOr(B.status, 1u);
-                }
-            }
-            __syncwarp();
+        for (int u = 0; u < KD; u++) {
+            const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
+            off[u] = S.m[u] * L1 + nz - 1;
+            okm |= ok ? 1u << u : 0u;
         }
+        const float sdt = k.lvl ? dt / (g.areasvol[iv] * g.hnode_new[i]) : 0.f;
+#pragma unroll 1
+        for (int t = 0; t < B.ntr; t++) {
+            const int fct = B.cfg[t].lim;
+            const size_t to = (size_t)t * B.sN;
+            const float *__restrict__ ADh = B.ADh + (size_t)t * B.sE;
+            const float2 *__restrict__ R = B.R + to;
+            float lo = 0.f, f0 = 0.f;
+            float2 r0 = make_float2(1.f, 1.f);
+            if (k.lvl) {
+                lo = B.LO[to + i];
+                f0 = B.ADv[(size_t)t * B.sNI + iv];
+                if (fct) r0 = R[i];
+            }
+            // vertical limiting (oce_adv_tra_fct.F90:425-456): interface nz by R of layers
+            // nz-1 and nz; the next interface is the lane below's
+            const float rux = sh_up(r0.x, 1), ruy = sh_up(r0.y, 1);
+            if (fct) {
+                if (nz == nzmin) f0 *= f0 >= 0.f ? r0.x : r0.y;
+                else f0 *= f0 >= 0.f ? fminf(ruy, r0.x) : fminf(rux, r0.y);
+            }
+            float f1 = sh_dn(f0, 1);
+            if (nz == nzmax - 1) f1 = 0.f;
+            // horizontal limiting (oce_adv_tra_fct.F90:468-500): R of edges(1,e) and edges(2,e)
+            float hs = 0.f;
+#pragma unroll
+            for (int u = 0; u < KD; u++) {
+                const bool ok = (okm >> u) & 1u;
+                float xv = ok ? ADh[S.e[u] * L1 + nz - 1] : 0.f;
+                if (fct) {
+                    const float2 rm = ok ? R[off[u]] : make_float2(1.f, 1.f);
+                    const bool o = (own >> u) & 1u;
+                    const float2 ra = o ? r0 : rm, rb = o ? rm : r0;
+                    xv *= xv >= 0.f ? fminf(ra.x, rb.y) : fminf(ra.y, rb.x);
+                }
+                hs += ((own >> u) & 1u) ? xv : -xv;
+            }
+            // del_ttf = (LO hnode_new - T hnode) + limited flux divergence dt / areasvol;
+            // T* = T + (del_ttf + T (hnode - hnode_new)) / hnode_new = LO + fluxes dt / areasvol / hnode_new
+            // (oce_adv_tra_driver.F90:535-620, oce_ale_tracer.F90:319-321, 743-754)
+            float val = lo + (f0 - f1 + hs) * sdt;
+            if (k.out) {
+                if (fct) {
+                    const float2 tb = B.TB[to + i];
+                    const float vc = fminf(fmaxf(val, tb.y), tb.x);
+                    // a clamp beyond round-off means the limiter itself failed
+                    if (fabsf(vc - val) > 1e-5f * (tb.x - tb.y) + 1e-6f * fabsf(vc)) atomicOr(B.status, 2u);
+                    val = vc;
+                }
+                B.Tnew[to + i] = val;
+                if (!isfinite(val)) atomicOr(B.status, 1u);
+            }
+        }
+    }
+}
+
+// implicit vertical diffusion of the advected column (already in Tnew) for every
+// tracer with i_vert_diff: forward substitution tp_k = inv_k rhs_k - a_k inv_k tp_{k-1}
+// and back substitution x_k = tp_k - cp_k x_{k+1} as scans of affine maps
+__device__ __forceinline__ void vdiff_node(const DTopo &tp, const DForcing<float> &f, const B32View &B,
+                                           const VFactors &vf, int n, int lane, int nzmin, int nzmax) {
+    using C = Chunk<1, 1>;
+    const int L1 = tp.L1;
+    const int nch = C::count(nzmin, nzmax);
+#pragma unroll 1
+    for (int t = 0; t < B.ntr; t++) {
+        if (!B.cfg[t].ivd) continue;
+        float *__restrict__ Tout = B.Tnew + (size_t)t * B.sN;
+        const float bc = f.bc ? f.bc[(size_t)t * tp.N2 + n] : 0.f;
+        float tpv[kMaxChunks], tad[kMaxChunks];
+        float carry = 0.f;
+#pragma unroll
+        for (int ch = 0; ch < kMaxChunks; ch++) {
+            tpv[ch] = 0.f;
+            tad[ch] = 0.f;
+            if (ch >= nch) continue;
+            const C k(nzmin, nzmax, ch, lane);
+            const int nz = k.nz;
+            const int i = n * L1 + nz - 1;
+            const float t0 = k.lvl ? Tout[i] : 0.f;
+            const float tu = sh_up(t0, 1), td = sh_dn(t0, 1);
+            float A = 1.f, Bv = 0.f;
+            if (k.out) {
+                const float a = vf.a[i], cc = vf.c[i], inv = vf.inv[i];
+                float rhs = 0.f;
+                if (nz > nzmin) rhs -= a * (tu - t0);
+                if (nz < nzmax - 1) rhs -= cc * (td - t0);
+                if (nz == nzmin) rhs += bc;
+                A = -(a * inv);
+                Bv = rhs * inv;
+            }
+            scan_up(A, Bv, lane);
+            const float y = A * carry + Bv;
+            tpv[ch] = y;
+            tad[ch] = t0;
+            carry = __shfl_sync(kFull, y, 30);
+        }
+        carry = 0.f;
+#pragma unroll
+        for (int ch = kMaxChunks - 1; ch >= 0; ch--) {
+            if (ch >= nch) continue;
+            const C k(nzmin, nzmax, ch, lane);
+            const int i = n * L1 + k.nz - 1;
+            float A = 1.f, Bv = 0.f;
+            if (k.out) {
+                A = -vf.cp[i];
+                Bv = tpv[ch];
+            }
+            scan_down(A, Bv, lane);
+            const float x = A * carry + Bv;
+            carry = __shfl_sync(kFull, x, 1);
+            if (k.out) {
+                const float val = tad[ch] + x;
+                Tout[i] = val;
+                if (!isfinite(val)) atomicOr(B.status, 1u);
+            }
+        }
+    }
+}
+
+template <bool WIDE>
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : kMinBlocks)
+k32_update(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, VFactors vf, float dt, int any_ivd) {
+    __shared__ WEdges Se[kWB];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int n = warp_node<WIDE>(tp, warp);
+    if (n < 0) return;
+    WEdges &S = Se[warp];
+    stage_edges(tp, n, lane, S);
+    if ((S.deg > 8) != WIDE) return;
+    advect_node<WIDE ? kMaxDeg : 8>(tp, g, B, dt, n, lane, S);
+    if (any_ivd) {
+        __syncwarp();
+        vdiff_node(tp, f, B, vf, n, lane, S.nzmin, S.nzmax);
     }
 }
 
@@ -616,27 +712,33 @@ static int grid32(int nent, int per_block) {
 }
 
 void b32_vflux(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, float *VF, cudaStream_t s) {
-    k32_vflux<<<grid32(tp.E2, kW), kT, 0, s>>>(tp, g, f, VF);
+    k32_vflux<<<grid32(tp.E2, kWB), kTB, 0, s>>>(tp, g, f, VF);
 }
 void b32_vfactors(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, double dt, const VFactors &v,
                   cudaStream_t s) {
     k32_vfactors<<<(tp.N2 + 127) / 128, 128, 0, s>>>(tp, g, f, dt, v);
 }
-// node kernels: one block per node (grid-stride), the tracers split over the block's warps
-static int grid_nodes(int n2) { return n2 < 152 * 32 ? n2 : 152 * 32; }
+// node kernels: one warp per node, kWB consecutive nodes per block; the nodes of more
+// than 8 edges (listed at init) take a second, small launch with 16 edge slots
+static int grid_nodes(int n) { return (n + kWB - 1) / kWB; }
 
-void b32_lo_ad(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B, const MusclW &mw,
-               const float *VF, double dt, cudaStream_t s) {
-    k32_lo_ad<<<grid_nodes(tp.N2), kT, 0, s>>>(tp, g, f, B, mw, VF, (float)dt);
+void b32_lo_ad(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B, const float *VF,
+               double dt, cudaStream_t s) {
+    k32_lo_ad<false><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
+    if (tp.n_wide) k32_lo_ad<true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
+}
+void b32_ho(const DTopo &tp, const DGeom<float> &g, const B32View &B, const MusclW &mw, const float *VF,
+            cudaStream_t s) {
+    k32_ho<<<grid_nodes(tp.E2), kTB, 0, s>>>(tp, g, B, mw, VF);
 }
 void b32_bounds(const DTopo &tp, const DGeom<float> &g, const B32View &B, double dt, cudaStream_t s) {
-    const size_t sm = sizeof(float) * 2 * (tp.L1 + 2) * kW;
-    k32_bounds<<<grid_nodes(tp.N2), kT, sm, s>>>(tp, g, B, (float)dt);
+    k32_bounds<false><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, B, (float)dt);
+    if (tp.n_wide) k32_bounds<true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
 }
 void b32_update(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B,
-                const VFactors &v, double dt, cudaStream_t s) {
-    const size_t sm = sizeof(float) * (tp.L1 + 2) * kW;
-    k32_update<<<grid_nodes(tp.N2), kT, sm, s>>>(tp, g, f, B, v, (float)dt);
+                const VFactors &v, double dt, int any_ivd, cudaStream_t s) {
+    k32_update<false><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, f, B, v, (float)dt, any_ivd);
+    if (tp.n_wide) k32_update<true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, f, B, v, (float)dt, any_ivd);
 }
 
 }  // namespace fesom

@@ -513,25 +513,66 @@ def channel_mesh(nx: int = 100, ny: int = 400, dx: float = 5000.0, zbar: Optiona
             tris.append(np.stack([nid(ii, jj), nid(ii + 1, jj + 1), nid(ii, jj + 1)], axis=1))
             tris.append(np.stack([nid(ii, jj), nid(ii + 1, jj), nid(ii + 1, jj + 1)], axis=1))
     tri = np.concatenate(tris, axis=0)
-    H = -zbar[-1]
-    depth = np.full(coord.shape[0], -H)
+    depth = _seamount_depth(x.reshape(-1), y.reshape(-1), nx * dx, ny * dy, -zbar[-1], seamounts, seed, True)
+    m = _finish_mesh(coord, tri, cyc, True, zbar, depth, partial_cells, name=f"channel_{nx}x{ny}")
+    return m
+
+
+def _seamount_depth(x, y, Lx, Ly, H, seamounts, seed, periodic):
+    """Node depth (negative, metres): flat bottom at H minus seeded Gaussian seamounts."""
+    depth = np.full(x.shape[0], -H)
     if seamounts > 0:
         rng = np.random.default_rng(seed + 7)
-        Lx, Ly = nx * dx, ny * dy
         cxs = rng.uniform(0, Lx, seamounts)
         cys = rng.uniform(0.1 * Ly, 0.9 * Ly, seamounts)
         rad = rng.uniform(0.04, 0.12, seamounts) * Ly
         amp = rng.uniform(0.5, 0.82, seamounts) * H
-        xm = x.reshape(-1)
-        ym = y.reshape(-1)
-        bump = np.zeros_like(xm)
+        bump = np.zeros_like(x)
         for k in range(seamounts):
-            ddx = np.abs(xm - cxs[k])
-            ddx = np.minimum(ddx, Lx - ddx)
-            bump = np.maximum(bump, amp[k] * np.exp(-(ddx ** 2 + (ym - cys[k]) ** 2) / (2 * rad[k] ** 2)))
+            ddx = np.abs(x - cxs[k])
+            if periodic:
+                ddx = np.minimum(ddx, Lx - ddx)
+            bump = np.maximum(bump, amp[k] * np.exp(-(ddx ** 2 + (y - cys[k]) ** 2) / (2 * rad[k] ** 2)))
         depth = -(H - bump) - 1e-3
-    m = _finish_mesh(coord, tri, cyc, True, zbar, depth, partial_cells, name=f"channel_{nx}x{ny}")
-    return m
+    return depth
+
+
+def delaunay_mesh(npts: int = 400, Lx: float = 100e3, Ly: float = 80e3, zbar: Optional[np.ndarray] = None,
+                  seamounts: int = 0, seed: int = 1, partial_cells: bool = False) -> Mesh:
+    """Closed rectangular basin meshed by the Delaunay triangulation of seeded random
+    points (plus points along the walls): an irregular mesh whose node degrees spread
+    from 3 to 10 and more, unlike the regular channel and icosahedral meshes.
+    Cartesian metric, not periodic."""
+    from scipy.spatial import Delaunay
+    if zbar is None:
+        zbar = -np.arange(41) * 100.0
+    rng = np.random.default_rng(seed)
+    nb = max(4, int(round(math.sqrt(npts))))
+    side = np.linspace(0.0, 1.0, nb, endpoint=False)
+    wall = np.concatenate([np.stack([side * Lx, np.zeros(nb)], 1), np.stack([np.full(nb, Lx), side * Ly], 1),
+                           np.stack([Lx - side * Lx, np.full(nb, Ly)], 1), np.stack([np.zeros(nb), Ly - side * Ly], 1)])
+    inner = np.stack([rng.uniform(0.02, 0.98, npts) * Lx, rng.uniform(0.02, 0.98, npts) * Ly], 1)
+    pts = np.concatenate([wall, inner])
+    tri = Delaunay(pts).simplices
+    # drop slivers along the walls (three wall points in a row)
+    a, b, c = pts[tri[:, 0]], pts[tri[:, 1]], pts[tri[:, 2]]
+    area2 = np.abs((b[:, 0] - a[:, 0]) * (c[:, 1] - a[:, 1]) - (b[:, 1] - a[:, 1]) * (c[:, 0] - a[:, 0]))
+    tri = tri[area2 > 1e-6 * Lx * Ly / npts]
+    used = np.zeros(pts.shape[0], bool)
+    used[tri.reshape(-1)] = True
+    remap = np.cumsum(used) - 1
+    pts = pts[used]
+    tri = remap[tri]
+    order = np.argsort(_morton_key(np.stack([2 * pts[:, 0] / Lx - 1, 2 * pts[:, 1] / Ly - 1, np.zeros(len(pts))], 1)),
+                       kind="stable")
+    inv = np.empty_like(order)
+    inv[order] = np.arange(order.size)
+    pts = pts[order]
+    tri = inv[tri]
+    coord = pts / R_EARTH
+    cyc = 1e3 * max(Lx, Ly) / R_EARTH  # never reached: no cyclic wrap
+    depth = _seamount_depth(pts[:, 0], pts[:, 1], Lx, Ly, -zbar[-1], seamounts, seed, False)
+    return _finish_mesh(coord, tri, cyc, True, zbar, depth, partial_cells, name=f"delaunay_{npts}")
 
 
 def _icosphere(nsub: int):
@@ -716,7 +757,7 @@ def make_forcing(mesh: Mesh, kind: str, seed: int = 11, dt: float = 600.0,
     """Seeded velocity / Kv for a mesh.
 
     ``kind='channel'``: psi = U0*L*tanh(y'/L) + 0.05*U0*L*(Fourier modes k<=8),
-    multiplied by a vertical profile; ``kind='sphere'``: smooth random psi scaled
+    multiplied by a vertical profile; ``kind='basin'``: a closed gyre, psi zero on the walls; ``kind='sphere'``: smooth random psi scaled
     to ``rms`` m/s, tapered to zero on coasts.  Element velocity is the discrete
     rot-grad of psi (divergence-free in the edge-flux form where the dual cell is
     closed), w comes from the discrete divergence.  ``surface_w_zero`` sets
@@ -737,6 +778,19 @@ def make_forcing(mesh: Mesh, kind: str, seed: int = 11, dt: float = 600.0,
             a, ph, mm = rng.normal(), rng.uniform(0, 2 * np.pi), rng.integers(1, 5)
             modes += a / k * np.sin(2 * np.pi * k * x / Lx + ph) * np.sin(np.pi * mm * (y - y.min()) / Ly)
         psi = psi + 0.05 * U0 * Lj * modes
+        prof = 0.3 + 0.7 * np.exp(Zm / 1000.0)
+        base = _rot_grad(mesh, psi)
+    elif kind == "basin":
+        # closed basin: psi vanishes on every wall, a gyre plus seeded modes
+        x = mesh.coord_nod2D[:, 0] * R_EARTH
+        y = mesh.coord_nod2D[:, 1] * R_EARTH
+        Lx, Ly = x.max() - x.min(), y.max() - y.min()
+        xs, ys = (x - x.min()) / Lx, (y - y.min()) / Ly
+        psi = np.sin(np.pi * xs) * np.sin(np.pi * ys)
+        for k in range(1, 5):
+            a, mm = rng.normal(), rng.integers(1, 4)
+            psi = psi + 0.2 * a / k * np.sin(np.pi * (k + 1) * xs) * np.sin(np.pi * mm * ys)
+        psi *= U0 * min(Lx, Ly) / np.pi
         prof = 0.3 + 0.7 * np.exp(Zm / 1000.0)
         base = _rot_grad(mesh, psi)
     else:
@@ -788,7 +842,7 @@ def make_tracers(mesh: Mesh, kind: str, ntr: int = 2, seed: int = 5, Lj: float =
     def one(k):
         rng = np.random.default_rng([seed, k])
         if k == 0:
-            if kind == "channel":
+            if kind in ("channel", "basin"):
                 y = mesh.coord_nod2D[:, 1] * R_EARTH
                 yp = y - 0.5 * (y.min() + y.max())
                 sig = 0.01 if noise is None else noise
@@ -798,8 +852,8 @@ def make_tracers(mesh: Mesh, kind: str, ntr: int = 2, seed: int = 5, Lj: float =
                 sig = 0.1 if noise is None else noise
                 v = 2.0 + 26.0 * (np.cos(lat) ** 2)[:, None] * np.exp(-d / 1000.0) + rng.normal(0, sig, d.shape)
         elif k == 1:
-            sig = (0.01 if kind == "channel" else 0.1) if noise is None else noise
-            if kind == "channel":
+            sig = (0.01 if kind in ("channel", "basin") else 0.1) if noise is None else noise
+            if kind in ("channel", "basin"):
                 v = 35.0 + rng.normal(0, sig, d.shape)
             else:
                 lat = mesh.coord_nod2D[:, 1]

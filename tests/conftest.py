@@ -57,6 +57,13 @@ def sphere_small():
     return M.sphere_mesh(4, M.stretched_zbar(48, 5.0, 250.0), seed=9)
 
 
+@pytest.fixture(scope="session")
+def basin_irregular():
+    """Closed basin, Delaunay triangulation of 400 random points (node degrees 2 to 10),
+    30 stretched levels, seamounts and partial cells."""
+    return M.delaunay_mesh(400, zbar=M.stretched_zbar(30, 10.0, 200.0), seamounts=2, seed=3, partial_cells=True)
+
+
 def wet_mask(mesh):
     lev = np.arange(mesh.nl - 1)[None, :]
     return (lev >= (mesh.ulevels_nod2D - 1)[:, None]) & (lev < (mesh.nlevels_nod2D - 1)[:, None])

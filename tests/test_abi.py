@@ -47,7 +47,7 @@ def test_nm_shows_symbols_as_text(lib):
     assert set(declared_functions()) <= exported
 
 
-@pytest.mark.parametrize("meshname", ["channel_small", "channel_seamount", "sphere_small"])
+@pytest.mark.parametrize("meshname", ["channel_small", "channel_seamount", "sphere_small", "basin_irregular"])
 def test_mesh_check_matches_oracle_muscl_init(lib, meshname, request):
     mesh = request.getfixturevalue(meshname)
     nbl, updn = G.mesh_check(mesh)

@@ -25,7 +25,7 @@ def _setup(mesh, kind, seed=3, ntr=2, surface_w_zero=False):
     return f, tr
 
 
-@pytest.mark.parametrize("meshname", ["channel_small", "channel_seamount", "sphere_small"])
+@pytest.mark.parametrize("meshname", ["channel_small", "channel_seamount", "sphere_small", "basin_irregular"])
 def test_muscl_init_matches_oracle(meshname, request):
     mesh = request.getfixturevalue(meshname)
     ctx = G.Context(mesh, G.PREC_FP64)
@@ -56,7 +56,8 @@ def test_init_tracers_ab_bitwise(meshname, kind, ab, request):
 
 
 @pytest.mark.parametrize("scheme", SCHEMES, ids=["-".join(s) for s in SCHEMES])
-@pytest.mark.parametrize("meshname,kind", [("channel_seamount", "channel"), ("sphere_small", "sphere")])
+@pytest.mark.parametrize("meshname,kind", [("channel_seamount", "channel"), ("sphere_small", "sphere"),
+                                           ("basin_irregular", "basin")])
 def test_adv_tra_bitwise(scheme, meshname, kind, request):
     """do_oce_adv_tra: del_ttf_advhoriz / del_ttf_advvert equal the oracle's bit for bit."""
     mesh = request.getfixturevalue(meshname)
@@ -92,7 +93,7 @@ def test_vdiff_bitwise(meshname, kind, request):
 
 
 @pytest.mark.parametrize("meshname,kind", [("channel_small", "channel"), ("channel_seamount", "channel"),
-                                           ("sphere_small", "sphere")])
+                                           ("sphere_small", "sphere"), ("basin_irregular", "basin")])
 def test_tracer_step_bitwise_multi_step(meshname, kind, request):
     """Whole per-tracer body (AB2, MUSCL+QR4C+FCT, T*, implicit diffusion), 3 steps, 2 tracers."""
     mesh = request.getfixturevalue(meshname)
@@ -137,7 +138,8 @@ def test_device_resident_graph_matches_host_calls(channel_seamount):
         assert np.array_equal(o, Oa[k])
 
 
-@pytest.mark.parametrize("meshname,kind", [("channel_seamount", "channel"), ("sphere_small", "sphere")])
+@pytest.mark.parametrize("meshname,kind", [("channel_seamount", "channel"), ("sphere_small", "sphere"),
+                                           ("basin_irregular", "basin")])
 def test_fp32_error_vs_fp64_oracle(meshname, kind, request):
     """FP32 form, one step from the same state: error against the FP64 oracle <= 1e-5,
     normwise (max |dT| / max |T|) for every tracer and pointwise relative for T and S.
@@ -225,12 +227,13 @@ FP32_SCHEMES = [("MUSCL", "QR4C", "FCT", 2), ("MFCT", "UPW1", "FCT", 3), ("UPW1"
 
 
 @pytest.mark.parametrize("scheme", FP32_SCHEMES, ids=["-".join(map(str, s)) for s in FP32_SCHEMES])
-def test_fp32_schemes_and_ab_orders_vs_oracle(sphere_small, scheme):
+@pytest.mark.parametrize("meshname,kind", [("sphere_small", "sphere"), ("basin_irregular", "basin")])
+def test_fp32_schemes_and_ab_orders_vs_oracle(meshname, kind, scheme, request):
     """FP32 batched form, 3 steps of every scheme family and AB order, against the
     FP64 oracle started from the same (FP32-rounded) state: normwise error <= 1e-5."""
     hor, ver, lim, ab = scheme
-    mesh = sphere_small
-    f, tr = _setup(mesh, "sphere", ntr=3)
+    mesh = request.getfixturevalue(meshname)
+    f, tr = _setup(mesh, kind, ntr=3)
     rng = np.random.default_rng(4)
     cfgs = [G.tra_cfg(hor, ver, lim, 0.0, 1.0, ab_order=ab, id=k + 1) for k in range(3)]
     ocfg = O.cfg_struct(hor, ver, lim, 0.0, 1.0, ab_order=ab)
@@ -277,3 +280,38 @@ def test_fp32_graph_replay_equals_direct_launches(channel_seamount):
     for k in range(2):
         assert np.array_equal(out[0][k][0], out[1][k][0])
         assert np.array_equal(out[0][k][1], out[1][k][1])
+
+
+def test_fp32_mixed_schemes_in_one_batch(basin_irregular):
+    """Tracers of different schemes, limiters and vertical-diffusion switches share one
+    FP32 launch per stage; each must match the oracle run with its own configuration."""
+    mesh = basin_irregular
+    f, tr = _setup(mesh, "basin", ntr=4)
+    specs = [("MUSCL", "QR4C", "FCT", 1), ("UPW1", "UPW1", "NON", 1), ("MFCT", "QR4C", "FCT", 0),
+             ("MUSCL", "UPW1", "NON", 0)]
+    cfgs, ocfgs = [], []
+    for k, (hor, ver, lim, ivd) in enumerate(specs):
+        c = G.tra_cfg(hor, ver, lim, 0.0, 1.0, id=k + 1)
+        c.i_vert_diff = ivd
+        cfgs.append(c)
+        ocfgs.append(O.cfg_struct(hor, ver, lim, 0.0, 1.0, i_vert_diff=ivd))
+    om = O.OracleMesh(mesh)
+    wet = wet_mask(mesh)
+    ctx = G.Context(mesh, G.PREC_FP32, max_tracers=4)
+    ctx.state_setup(cfgs)
+    ctx.forcing_upload(f)
+    T64, O64 = [], []
+    for k in range(4):
+        T = tr[k].astype(np.float32).astype(np.float64)
+        ctx.tracer_upload(k, T, T)
+        T64.append(T.copy())
+        O64.append(T.copy())
+    for step in range(2):
+        ctx.run_steps(f.dt, 1, use_graph=(step == 1))
+        for k in range(4):
+            om.tracer_step(f, ocfgs[k], T64[k], np.zeros_like(T64[k]), O64[k])
+    for k in range(4):
+        v, _ = ctx.tracer_download(k)
+        err = np.abs(v[wet] - T64[k][wet]).max() / np.abs(T64[k][wet]).max()
+        assert err <= 1e-5, (specs[k], err)
+    assert ctx.status() == 0

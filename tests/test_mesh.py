@@ -32,8 +32,8 @@ def test_elements_are_clockwise_and_edge_tri_left(sphere_small):
     assert inner[:m.edge2D_in].all() and not inner[m.edge2D_in:].any()
 
 
-def test_levels(channel_seamount, sphere_small):
-    for m in (channel_seamount, sphere_small):
+def test_levels(channel_seamount, sphere_small, basin_irregular):
+    for m in (channel_seamount, sphere_small, basin_irregular):
         assert np.all(m.nlevels >= 5) and np.all(m.nlevels <= m.nl)
         assert np.all(m.nlevels_nod2D - m.ulevels_nod2D >= 4)
         # node levels are the max over the node's elements
@@ -61,3 +61,13 @@ def test_tracers_are_seeded_and_positive(sphere_small):
     lev = np.arange(sphere_small.nl - 1)[None, :]
     wet = lev < (sphere_small.nlevels_nod2D - 1)[:, None]
     assert a[2][wet].min() > 0 and a[3][wet].min() > 0
+
+
+def test_irregular_basin_has_high_degree_nodes(basin_irregular):
+    """The Delaunay basin carries nodes of more than 8 edges (the FP32 form's second
+    launch) and its gyre has no flow through the walls: w vanishes on a flat bottom."""
+    m = basin_irregular
+    deg = np.bincount(m.edges.reshape(-1), minlength=m.nod2D)
+    assert deg.max() > 8 and deg.min() >= 2
+    flat = M.delaunay_mesh(400, zbar=M.stretched_zbar(30, 10.0, 200.0), seed=3)
+    assert np.abs(M.make_forcing(flat, "basin").w).max() < 1e-12
