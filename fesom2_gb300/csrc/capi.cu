@@ -62,6 +62,10 @@ struct fesom_gpu_ctx {
     MusclW mw{};
     cudaGraphExec_t gexec32[3] = {nullptr, nullptr, nullptr};
     double g32_dt[3] = {0.0, 0.0, 0.0};
+    // second stream: the tracer-independent vertical-diffusion factors run beside the
+    // advection stages and join before the update
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 namespace {
@@ -262,6 +266,8 @@ int init_muscl_weights(fesom_gpu_ctx *ctx, const fesom_mesh_desc *d) {
         }
     std::vector<int4> un(E2), dn(E2);
     std::vector<float4> wu(E2), wd(E2);
+    std::vector<int> fb;
+    int rc;
     for (int e = 0; e < E2; e++) {
         const int n1 = h.e_n1[e], n2 = h.e_n2[e], el1 = h.e_t1[e], el2 = h.e_t2[e];
         double a = kREarth * d->elem_cos[el1];
@@ -273,6 +279,7 @@ int init_muscl_weights(fesom_gpu_ctx *ctx, const fesom_mesh_desc *d) {
             gzmin = std::max(h.n_ulevmax[n1], h.n_ulevmax[n2]);
             gzmax = std::min(h.n_nlevmin[n1], h.n_nlevmin[n2]);
         }
+        // the triangle's nodes from the edge node on (prepare_mesh checked that the triangle holds it)
         auto tri = [&](int el, int node, int4 &nn, float4 &ww) {
             if (el < 0) {
                 nn = make_int4(node, node, node, 0);
@@ -280,15 +287,26 @@ int init_muscl_weights(fesom_gpu_ctx *ctx, const fesom_mesh_desc *d) {
                 return;
             }
             const double *gs = d->gradient_sca + 6 * (size_t)el;
-            nn = make_int4(h.t_n[3 * (size_t)el], h.t_n[3 * (size_t)el + 1], h.t_n[3 * (size_t)el + 2], 0);
-            ww = make_float4((float)(ex * a * gs[0] + ey * kREarth * gs[3]), (float)(ex * a * gs[1] + ey * kREarth * gs[4]),
-                             (float)(ex * a * gs[2] + ey * kREarth * gs[5]), (float)a);
+            const int *tn = &h.t_n[3 * (size_t)el];
+            const int p = tn[0] == node ? 0 : (tn[1] == node ? 1 : 2);
+            int q[3];
+            float w[3];
+            for (int k = 0; k < 3; k++) {
+                const int r = (p + k) % 3;
+                q[k] = tn[r];
+                w[k] = (float)(ex * a * gs[r] + ey * kREarth * gs[r + 3]);
+            }
+            nn = make_int4(q[0], q[1], q[2], 0);
+            ww = make_float4(w[0], w[1], w[2], (float)a);
         };
         tri(up, n1, un[e], wu[e]);
         tri(dw, n2, dn[e], wd[e]);
         un[e].w = gzmin | (gzmax << 16);
+        if (h.e_lo[e] < gzmin || h.e_hi[e] > gzmax - 1) fb.push_back(e);
     }
-    int rc;
+    ctx->tp.n_fb = (int)fb.size();
+    ctx->tp.fb_edges = nullptr;
+    if (!fb.empty() && (rc = upload_int(ctx, &ctx->tp.fb_edges, fb))) return rc;
     void *p;
     if ((rc = dalloc(ctx, &p, sizeof(int4) * E2))) return rc;
     CK(cudaMemcpy(p, un.data(), sizeof(int4) * E2, cudaMemcpyHostToDevice));
@@ -462,16 +480,24 @@ int alloc_state32(fesom_gpu_ctx *ctx, int ntr, int ab) {
     float **fac[] = {&ctx->vfac.a, &ctx->vfac.c, &ctx->vfac.inv, &ctx->vfac.cp};
     for (float **f : fac)
         if ((rc = dalloc(ctx, (void **)f, 4 * sN))) return rc;
-    const size_t per_tracer = 4 * (5 * sN + sNI + sE);  // LO increment, (R+,R-), bounds, ADv, ADh
+    const size_t per_tracer = 4 * (5 * sN + sNI + sE);  // LO, (R+,R-), bounds, ADv, ADh
     size_t fr = 0, tot = 0;
     CK(cudaMemGetInfo(&fr, &tot));
-    const int g = (int)std::min<size_t>((size_t)ntr, std::max<size_t>(1, (size_t)(0.85 * fr) / per_tracer));
+    // at most 64 tracers per launch: the kernels take per-tracer switches as 64-bit masks
+    const int g = (int)std::min<size_t>(std::min<size_t>((size_t)ntr, 64),
+                                        std::max<size_t>(1, (size_t)(0.85 * fr) / per_tracer));
     ctx->group = ctx->group_cap = g;
     if ((rc = dalloc(ctx, (void **)&ctx->LO32, 4 * sN * g))) return rc;
     if ((rc = dalloc(ctx, (void **)&ctx->ADv32, 4 * sNI * g))) return rc;
     if ((rc = dalloc(ctx, (void **)&ctx->ADh32, 4 * sE * g))) return rc;
     if ((rc = dalloc(ctx, (void **)&ctx->R2, 8 * sN * g))) return rc;
     if ((rc = dalloc(ctx, (void **)&ctx->TB2, 8 * sN * g))) return rc;
+    // created here, not on first use: a first step may run inside a stream capture
+    if (!ctx->side) {
+        CK(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+    }
     ctx->rot = 0;
     ctx->ntr = ntr;
     ctx->ab_max = ab;
@@ -497,6 +523,16 @@ B32View view32(fesom_gpu_ctx *ctx, int t0, int nt) {
     v.TB = ctx->TB2;
     v.cfg = ctx->d_cfg + t0;
     v.status = ctx->status;
+    v.fct_mask = v.ivd_mask = 0;
+    for (int t = 0; t < nt; t++) {
+        const fesom_tra_cfg &c = ctx->cfgs[t0 + t];
+        if (c.adv_lim == FESOM_ADV_LIM_FCT) v.fct_mask |= 1ull << t;
+        if (c.i_vert_diff) v.ivd_mask |= 1ull << t;
+        v.hor[t] = (signed char)c.adv_hor;
+        v.ver[t] = (signed char)c.adv_ver;
+        v.ph[t] = (float)c.adv_ph;
+        v.pv[t] = (float)c.adv_pv;
+    }
     return v;
 }
 
@@ -554,7 +590,17 @@ int enqueue_step32(fesom_gpu_ctx *ctx, double dt, StageTimer *tm = nullptr) {
     bool any_vd = false;
     for (int t = 0; t < ctx->ntr; t++) any_vd |= ctx->cfgs[t].i_vert_diff != 0;
     STAGE(8, b32_vflux(ctx->tp, g, f, ctx->VF, ctx->stream));
-    if (any_vd) STAGE(9, b32_vfactors(ctx->tp, g, f, dt, ctx->vfac, ctx->stream));
+    // the factors depend on the forcing only: outside profiled steps they run on the side
+    // stream while the advection stages of the first group run, and join before its update
+    const bool fork = any_vd && !tm;
+    if (fork) {
+        CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
+        CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+        b32_vfactors(ctx->tp, g, f, dt, ctx->vfac, ctx->side);
+        CK(cudaEventRecord(ctx->ev_join, ctx->side));
+    } else if (any_vd) {
+        STAGE(9, b32_vfactors(ctx->tp, g, f, dt, ctx->vfac, ctx->stream));
+    }
     for (int t0 = 0; t0 < ctx->ntr; t0 += ctx->group) {
         const int nt = std::min(ctx->group, ctx->ntr - t0);
         B32View B = view32(ctx, t0, nt);
@@ -564,9 +610,8 @@ int enqueue_step32(fesom_gpu_ctx *ctx, double dt, StageTimer *tm = nullptr) {
         STAGE(10, b32_lo_ad(ctx->tp, g, fg, B, ctx->VF, dt, ctx->stream));
         STAGE(2, b32_ho(ctx->tp, g, B, ctx->mw, ctx->VF, ctx->stream));
         if (any_fct) STAGE(4, b32_bounds(ctx->tp, g, B, dt, ctx->stream));
-        bool grp_vd = false;
-        for (int t = t0; t < t0 + nt; t++) grp_vd |= ctx->cfgs[t].i_vert_diff != 0;
-        STAGE(6, b32_update(ctx->tp, g, fg, B, ctx->vfac, dt, grp_vd ? 1 : 0, ctx->stream));
+        if (fork && t0 == 0) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+        STAGE(6, b32_update(ctx->tp, g, fg, B, ctx->vfac, dt, ctx->stream));
     }
     CK(cudaGetLastError());
     return FESOM_OK;
@@ -583,9 +628,9 @@ int launches_per_step(fesom_gpu_ctx *ctx) {
             const int nt = std::min(ctx->group, ctx->ntr - t0);
             bool any_fct = false;
             for (int t = t0; t < t0 + nt; t++) any_fct |= ctx->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
-            // lo_ad, ho, update (+ bounds); the node kernels launch again for the wide nodes
+            // lo_ad, update (+ bounds), launched again for the wide nodes; ho (+ its fallback edges)
             const int wide = ctx->tp.n_wide ? 2 : 1;
-            n += 1 + wide * (2 + (any_fct ? 1 : 0));
+            n += wide * (2 + (any_fct ? 1 : 0)) + (ctx->tp.n_fb ? 2 : 1);
         }
         return n;
     }
@@ -766,6 +811,9 @@ int fesom_gpu_finalize(fesom_gpu_ctx *ctx) {
     if (!ctx) return FESOM_OK;
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
     free_graphs32(ctx);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     for (void *p : ctx->allocs) cudaFree(p);
     delete ctx;
     return FESOM_OK;

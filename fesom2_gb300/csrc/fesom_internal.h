@@ -33,6 +33,8 @@ struct DTopo {
     const int *nie_ptr, *nie_idx;  // node -> element, ascending element order
     int n_wide;                    // nodes of more than 8 edges (FP32 form: their own launch)
     const int *wide_nodes;
+    int n_fb;                      // edges with levels outside their triangles' shared range
+    const int *fb_edges;           // (FP32 form: the node-mean MUSCL gradients, own launch)
 };
 
 template <typename R>
@@ -93,14 +95,20 @@ struct B32View {
     float2 *TB;      // FCT bounds of the advected value (LO + bmax, LO + bmin)
     const DCfg *cfg;
     unsigned *status;
+    unsigned long long fct_mask;  // bit t: tracer t of the launch uses the FCT limiter
+    unsigned long long ivd_mask;  // bit t: tracer t takes the implicit vertical diffusion
+    // per-tracer schemes in the kernel parameters (constant bank), at most 64 tracers
+    signed char hor[64], ver[64];
+    float ph[64], pv[64];
 };
 // Node degree bound of the FP32 form (the node's edge list is staged per warp)
 constexpr int kMaxDeg = 16;
 // Per-edge MUSCL/MFCT reconstruction data of the FP32 form, precomputed at init:
-// un / dn = nodes of the up (of edges(1,e)) and down (of edges(2,e)) triangle, with
-// un.w = gzmin | gzmax << 16 (levels where the triangle gradients apply, 0 if none);
-// wu / wd = weights so that sum_k wu_k T(un_k) = edge_dxdy(1)*a*gx + edge_dxdy(2)*r_earth*gy
-// of the triangle gradient (oce_adv_tra_hor.F90:446-461), wu.w = a (r_earth * mean elem_cos)
+// un / dn = nodes of the up (of edges(1,e)) and down (of edges(2,e)) triangle, the edge
+// node first (un.x = edges(1,e), dn.x = edges(2,e)), with un.w = gzmin | gzmax << 16
+// (levels where the triangle gradients apply, 0 if none); wu / wd = weights so that
+// sum_k wu_k T(un_k) = edge_dxdy(1)*a*gx + edge_dxdy(2)*r_earth*gy of the triangle
+// gradient (oce_adv_tra_hor.F90:446-461), wu.w = a (r_earth * mean elem_cos)
 struct MusclW {
     const int4 *un, *dn;
     const float4 *wu, *wd;
@@ -117,7 +125,7 @@ void b32_lo_ad(const DTopo &, const DGeom<float> &, const DForcing<float> &, con
 void b32_ho(const DTopo &, const DGeom<float> &, const B32View &, const MusclW &, const float *VF, cudaStream_t);
 void b32_bounds(const DTopo &, const DGeom<float> &, const B32View &, double dt, cudaStream_t);
 void b32_update(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, const VFactors &,
-                double dt, int any_ivd, cudaStream_t);
+                double dt, cudaStream_t);
 
 // launch wrappers (kernels_fp64.cu / kernels_fp32.cu)
 template <typename R>

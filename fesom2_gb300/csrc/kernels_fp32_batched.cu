@@ -272,22 +272,22 @@ __device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &
         // ---- per tracer ----
 #pragma unroll 1
         for (int t = 0; t < B.ntr; t++) {
-            const DCfg c = B.cfg[t];
+            const bool lim = (B.fct_mask >> t) & 1ull;
+            const int ver = B.ver[t];
             const size_t to = (size_t)t * B.sN;
             const float *__restrict__ T = B.T + to;
             const float *__restrict__ O1 = B.O1 + to;
             const float *__restrict__ O2 = B.ab == 3 ? B.O2 + to : O1;
-            float Tn = 0.f, dab = 0.f;
-            if (k.lvl) {
-                Tn = T[i];
-                dab = ab_delta(B.ab, Tn, O1[i], B.ab == 3 ? O2[i] : 0.f);
-            }
-            const float tab = Tn + dab;
-            const float Tu = sh_up(Tn, 1);
-            const float tabu = sh_up(tab, 1), tabu2 = sh_up(tab, 2), tabd = sh_dn(tab, 1);
+            // every load of the tracer's chunk first
+            const float Tn = k.lvl ? T[i] : 0.f;
+            const float o1 = k.lvl ? O1[i] : 0.f;
+            const float o2 = (k.lvl && B.ab == 3) ? O2[i] : 0.f;
             float tm[KD];
 #pragma unroll
             for (int u = 0; u < KD; u++) tm[u] = ((okm >> u) & 1u) ? T[off[u]] : 0.f;
+            const float tab = Tn + (k.lvl ? ab_delta(B.ab, Tn, o1, o2) : 0.f);
+            const float Tu = sh_up(Tn, 1);
+            const float tabu = sh_up(tab, 1), tabu2 = sh_up(tab, 2), tabd = sh_dn(tab, 1);
             // LO: upwind edge fluxes in difference form, sum_j am_j (T_j - T_n) + Dh T_n
             float hs = Dh * Tn;
 #pragma unroll
@@ -312,12 +312,12 @@ __device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &
             if (k.out) B.LO[to + i] = Tn * hr + (hs + fv0 - fv1) * sdt;
             // vertical high-order flux on the AB values (QR4C / UPW1), minus the LO flux
             if (k.out) {
-                const float pw = c.lim ? w0 : we0;
+                const float pw = lim ? w0 : we0;
                 float Cf;
                 if (nz == nzmin) {
                     Cf = -(tab * pw * ar0);
-                } else if (c.ver != 0 || nz == nzmin + 1 || nz == nzmax - 1) {
-                    if (c.ver == 0) {
+                } else if (ver != 0 || nz == nzmin + 1 || nz == nzmax - 1) {
+                    if (ver == 0) {
                         Cf = -(0.5f * (tabu + tab) * pw * ar0);
                     } else {
                         const float aw = fabsf(pw);
@@ -329,16 +329,16 @@ __device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &
                     const float qd = (tabu2 - tabu) * idzm;
                     const float Tm1 = tab + (2.f * qc + qu) * g1;
                     const float Tm2 = tabu + (2.f * qc + qd) * g2;
-                    const float aw = fabsf(pw), no = (float)c.pv;
+                    const float aw = fabsf(pw), no = B.pv[t];
                     const float Tmean = (pw + aw) * Tm1 + (pw - aw) * Tm2;
                     Cf = (-(0.5f * (1.f - no) * Tmean) - no * (0.5f * (Tm1 + Tm2)) * pw) * ar0;
                 }
                 // flux = C - flux_in; FCT passes the LO flux in, otherwise zero
-                const float fin = c.lim ? fv0 : 0.f;
+                const float fin = lim ? fv0 : 0.f;
                 float F = Cf - fin;
                 // a two-layer column writes its middle interface twice (statements nzmin+1, nzmax-1)
-                if (c.ver == 0 && twolayer && nz == nzmin + 1) F = Cf - F;
-                B.ADv[(size_t)t * B.sNI + iv] = c.lim ? F : F - fv0;
+                if (ver == 0 && twolayer && nz == nzmin + 1) F = Cf - F;
+                B.ADv[(size_t)t * B.sNI + iv] = lim ? F : F - fv0;
             }
         }
     }
@@ -362,7 +362,9 @@ k32_lo_ad(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, const float *_
     WEdges &S = Se[warp];
     stage_edges(tp, n, lane, S);
     if ((S.deg > 8) != WIDE) return;
-    lo_ad_node<WIDE ? kMaxDeg : 8>(tp, g, f, B, VF, dt, n, lane, S);
+    if (WIDE) lo_ad_node<kMaxDeg>(tp, g, f, B, VF, dt, n, lane, S);
+    else if (S.deg <= 6) lo_ad_node<6>(tp, g, f, B, VF, dt, n, lane, S);
+    else lo_ad_node<8>(tp, g, f, B, VF, dt, n, lane, S);
 }
 
 // ---------------------------------------------------------------------------
@@ -370,14 +372,22 @@ k32_lo_ad(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, const float *_
 // ---------------------------------------------------------------------------
 // One warp per edge, the lanes over the edge's levels [nu12, nl12].  MUSCL / MFCT
 // (adv_tra_hor_muscl / _mfct, oce_adv_tra_hor.F90:261-834) on the AB values with the
-// gradients of fill_up_dn_grad (oce_muscl_adv.F90:356-525) folded into per-edge
-// weights of the up / down triangles' node values; UPW1 (:64-257).  The LO flux is
-// the upwind flux of the current values (oce_adv_tra_driver.F90:131-190).
-__global__ void __launch_bounds__(kTB, kMinBlocks)
+// gradients of fill_up_dn_grad (oce_muscl_adv.F90:356-525); UPW1 (:64-257).  The LO
+// flux is the upwind flux of the current values (oce_adv_tra_driver.F90:131-190).
+//
+// The up triangle holds edges(1,e) and the down triangle edges(2,e); their gradients,
+// projected on the edge, are wu.y (T(un.y) - T1) + wu.z (T(un.z) - T1) and the same
+// for the down triangle (the three weights of a triangle sum to zero).  Those apply
+// at the levels where every element around both nodes is wet, [gzmin, gzmax); the
+// other levels take the area-weighted node means and run in the FALLBACK launch over
+// the edges listed at init (under one percent of the edge-layers of an ocean mesh).
+template <bool FALLBACK>
+__global__ void __launch_bounds__(kTB, FALLBACK ? 1 : kMinBlocks)
 k32_ho(DTopo tp, DGeom<float> g, B32View B, MusclW mw, const float *__restrict__ VF) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int e = blockIdx.x * kWB + warp;
-    if (e >= tp.E2) return;
+    const int j = blockIdx.x * kWB + warp;
+    if (j >= (FALLBACK ? tp.n_fb : tp.E2)) return;
+    const int e = FALLBACK ? tp.fb_edges[j] : j;
     const int L1 = tp.L1;
     const int n1 = tp.e_n1[e], n2 = tp.e_n2[e];
     const int elo = tp.e_lo[e], ehi = tp.e_hi[e];
@@ -385,44 +395,51 @@ k32_ho(DTopo tp, DGeom<float> g, B32View B, MusclW mw, const float *__restrict__
     const int4 un = mw.un[e], dn = mw.dn[e];
     const float4 wu = mw.wu[e], wd = mw.wd[e];
     const int gzmin = un.w & 0xffff, gzmax = un.w >> 16;
-    const float exa = g.edxy[2 * (size_t)e] * wu.w, eyr = g.edxy[2 * (size_t)e + 1] * (float)kREarth;
     for (int nz0 = elo; nz0 <= ehi; nz0 += 32) {
         const int nz = nz0 + lane;
-        const bool ok = nz <= ehi;
+        const bool tri = nz >= gzmin && nz <= gzmax - 1;
+        const bool ok = nz <= ehi && (FALLBACK ? !tri : true);
         const int ie = e * L1 + nz - 1, ia = n1 * L1 + nz - 1, ib = n2 * L1 + nz - 1;
         const float v = ok ? VF[ie] : 0.f, vp = fmaxf(v, 0.f), vm = fminf(v, 0.f);
-        const bool tri = nz >= gzmin && nz <= gzmax - 1;
         const float cl1 = (nbl1 - nz) >= 0 ? 1.f : 0.f, cl2 = (nbl2 - nz) >= 0 ? 1.f : 0.f;
+        const int ua = un.y * L1 + nz - 1, ub = un.z * L1 + nz - 1;
+        const int da = dn.y * L1 + nz - 1, db = dn.z * L1 + nz - 1;
 #pragma unroll 1
         for (int t = 0; t < B.ntr; t++) {
             if (!ok) continue;
-            const DCfg c = B.cfg[t];
+            const int hor = B.hor[t];
+            if (FALLBACK && hor == 2) continue;  // UPW1 has no gradients: the main launch wrote it
             const size_t to = (size_t)t * B.sN;
             const float *__restrict__ T = B.T + to;
             const float *__restrict__ O1 = B.O1 + to;
             const float *__restrict__ O2 = B.ab == 3 ? B.O2 + to : O1;
             const float T1 = T[ia], T2 = T[ib];
+            const bool grad = !FALLBACK && hor != 2 && tri;
+            const float ga = grad ? T[ua] : 0.f, gb = grad ? T[ub] : 0.f;
+            const float gc = grad ? T[da] : 0.f, gd = grad ? T[db] : 0.f;
             const float t1 = T1 + ab_delta(B.ab, T1, O1[ia], B.ab == 3 ? O2[ia] : 0.f);
             const float t2 = T2 + ab_delta(B.ab, T2, O1[ib], B.ab == 3 ? O2[ib] : 0.f);
             const float flo = -(T1 * vp + T2 * vm);
             float hf;
-            if (c.hor == 2) {
+            if (hor == 2) {
                 hf = -(t1 * vp + t2 * vm);
             } else {
                 float s1, s2;
-                if (tri) {
-                    s1 = wu.x * T[un.x * L1 + nz - 1] + wu.y * T[un.y * L1 + nz - 1] + wu.z * T[un.z * L1 + nz - 1];
-                    s2 = wd.x * T[dn.x * L1 + nz - 1] + wd.y * T[dn.y * L1 + nz - 1] + wd.z * T[dn.z * L1 + nz - 1];
-                } else {
+                if (FALLBACK) {
+                    const float exa = g.edxy[2 * (size_t)e] * wu.w, eyr = g.edxy[2 * (size_t)e + 1] * (float)kREarth;
                     s1 = node_grad_proj(tp, g, T, n1, nz, exa, eyr);
                     s2 = node_grad_proj(tp, g, T, n2, nz, exa, eyr);
+                } else {
+                    if (!tri) continue;  // written by the fallback launch
+                    s1 = wu.y * (ga - T1) + wu.z * (gb - T1);
+                    s2 = wd.y * (gc - T2) + wd.z * (gd - T2);
                 }
                 // c_lo = 1 up to nboundary_lay (MUSCL), always 1 (MFCT)
-                const float clo1 = c.hor == 0 ? cl1 : 1.f, clo2 = c.hor == 0 ? cl2 : 1.f;
+                const float clo1 = hor == 0 ? cl1 : 1.f, clo2 = hor == 0 ? cl2 : 1.f;
                 const float d2 = 2.f * (t2 - t1);
                 const float Tm2 = t2 - (d2 + s2) * (1.f / 6.f) * clo2;
                 const float Tm1 = t1 + (d2 + s1) * (1.f / 6.f) * clo1;
-                const float no = (float)c.ph;
+                const float no = B.ph[t];
                 const float cHO = 2.f * (vp * Tm1 + vm * Tm2);
                 hf = -(0.5f * (1.f - no) * cHO) - v * no * 0.5f * (Tm1 + Tm2);
             }
@@ -458,16 +475,22 @@ __device__ __forceinline__ void bounds_node(const DTopo &tp, const DGeom<float> 
         const float s = k.lvl ? dt / (g.areasvol[iv] * g.hnode_new[i]) : 0.f;
 #pragma unroll 1
         for (int t = 0; t < B.ntr; t++) {
-            if (!B.cfg[t].lim) continue;
+            if (!((B.fct_mask >> t) & 1ull)) continue;
             const size_t to = (size_t)t * B.sN;
             const float *__restrict__ T = B.T + to;
             const float *__restrict__ LO = B.LO + to;
             const float *__restrict__ ADh = B.ADh + (size_t)t * B.sE;
-            float Tn = 0.f, lo = 0.f, v0 = 0.f;
-            if (k.lvl) {
-                Tn = T[i];
-                lo = LO[i];
-                v0 = B.ADv[(size_t)t * B.sNI + iv];
+            // every load of the tracer's chunk first
+            const float Tn = k.lvl ? T[i] : 0.f;
+            const float lo = k.lvl ? LO[i] : 0.f;
+            const float v0 = k.lvl ? B.ADv[(size_t)t * B.sNI + iv] : 0.f;
+            float tm[KD], lm[KD], x[KD];
+#pragma unroll
+            for (int u = 0; u < KD; u++) {
+                const bool ok = (okm >> u) & 1u;
+                tm[u] = ok ? T[off[u]] : 0.f;
+                lm[u] = ok ? LO[off[u]] : 0.f;
+                x[u] = ok ? ADh[S.e[u] * L1 + nz - 1] : 0.f;
             }
             // bounds over the node, its neighbours and the layers above and below
             // (oce_adv_tra_fct.F90:124-248)
@@ -476,12 +499,10 @@ __device__ __forceinline__ void bounds_node(const DTopo &tp, const DGeom<float> 
 #pragma unroll
             for (int u = 0; u < KD; u++) {
                 const bool ok = (okm >> u) & 1u;
-                const float tm = ok ? T[off[u]] : Tn;
-                const float lm = ok ? LO[off[u]] : lo;
-                const float x = ok ? ADh[S.e[u] * L1 + nz - 1] : 0.f;
-                mx = fmaxf(mx, fmaxf(lm, tm));
-                mn = fminf(mn, fminf(lm, tm));
-                const float xv = ((own >> u) & 1u) ? x : -x;
+                const float a = ok ? tm[u] : Tn, b = ok ? lm[u] : lo;
+                mx = fmaxf(mx, fmaxf(a, b));
+                mn = fminf(mn, fminf(a, b));
+                const float xv = ((own >> u) & 1u) ? x[u] : -x[u];
                 P += fmaxf(0.f, xv);
                 M += fminf(0.f, xv);
             }
@@ -516,7 +537,9 @@ __global__ void __launch_bounds__(kTB, WIDE ? 1 : kMinBlocks) k32_bounds(DTopo t
     WEdges &S = Se[warp];
     stage_edges(tp, n, lane, S);
     if ((S.deg > 8) != WIDE) return;
-    bounds_node<WIDE ? kMaxDeg : 8>(tp, g, B, dt, n, lane, S);
+    if (WIDE) bounds_node<kMaxDeg>(tp, g, B, dt, n, lane, S);
+    else if (S.deg <= 6) bounds_node<6>(tp, g, B, dt, n, lane, S);
+    else bounds_node<8>(tp, g, B, dt, n, lane, S);
 }
 
 // ---------------------------------------------------------------------------
@@ -545,39 +568,54 @@ __device__ __forceinline__ void scan_down(float &A, float &B, int lane) {
     }
 }
 
+// One tracer's column: advected values chunk by chunk (kept in registers), then the
+// implicit vertical diffusion as forward and back substitution with the FP64 factors:
+// tp_k = inv_k rhs_k - a_k inv_k tp_{k-1}, x_k = tp_k - cp_k x_{k+1}, each a scan of
+// affine maps over the lanes with the carry passed from chunk to chunk.  Every load of a
+// chunk is issued before any of its arithmetic; the column's factors sit in shared memory.
 template <int KD>
-__device__ __forceinline__ void advect_node(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int n,
-                                            int lane, const WEdges &S) {
+__device__ __forceinline__ void update_node(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
+                                            const B32View &B, float dt, int n, int lane, const WEdges &S,
+                                            const float4 *__restrict__ fac) {
     using C = Chunk<1, 1>;
     const int L1 = tp.L1, nl = tp.nl;
     const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
     const unsigned own = S.own;
     const int nch = C::count(nzmin, nzmax);
-    for (int ch = 0; ch < nch; ch++) {
-        const C k(nzmin, nzmax, ch, lane);
-        const int nz = k.nz;
-        const int i = n * L1 + nz - 1, iv = n * nl + nz - 1;
-        int off[KD];
-        unsigned okm = 0;
-#pragma unroll
-        for (int u = 0; u < KD; u++) {
-            const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
-            off[u] = S.m[u] * L1 + nz - 1;
-            okm |= ok ? 1u << u : 0u;
-        }
-        const float sdt = k.lvl ? dt / (g.areasvol[iv] * g.hnode_new[i]) : 0.f;
 #pragma unroll 1
-        for (int t = 0; t < B.ntr; t++) {
-            const int fct = B.cfg[t].lim;
-            const size_t to = (size_t)t * B.sN;
-            const float *__restrict__ ADh = B.ADh + (size_t)t * B.sE;
-            const float2 *__restrict__ R = B.R + to;
-            float lo = 0.f, f0 = 0.f;
-            float2 r0 = make_float2(1.f, 1.f);
-            if (k.lvl) {
-                lo = B.LO[to + i];
-                f0 = B.ADv[(size_t)t * B.sNI + iv];
-                if (fct) r0 = R[i];
+    for (int t = 0; t < B.ntr; t++) {
+        const bool fct = (B.fct_mask >> t) & 1ull;
+        const bool ivd = (B.ivd_mask >> t) & 1ull;
+        const size_t to = (size_t)t * B.sN;
+        const float *__restrict__ ADh = B.ADh + (size_t)t * B.sE;
+        const float *__restrict__ ADv = B.ADv + (size_t)t * B.sNI;
+        const float *__restrict__ LO = B.LO + to;
+        const float2 *__restrict__ R = B.R + to;
+        const float2 *__restrict__ TB = B.TB + to;
+        float *__restrict__ Tout = B.Tnew + to;
+        float tad[kMaxChunks];
+#pragma unroll
+        for (int ch = 0; ch < kMaxChunks; ch++) {
+            tad[ch] = 0.f;
+            if (ch >= nch) continue;
+            const C k(nzmin, nzmax, ch, lane);
+            const int nz = k.nz;
+            const int i = n * L1 + nz - 1, iv = n * nl + nz - 1;
+            const bool lf = k.lvl && fct;
+            const float lo = k.lvl ? LO[i] : 0.f;
+            float f0 = k.lvl ? ADv[iv] : 0.f;
+            const float2 r0 = lf ? R[i] : make_float2(1.f, 1.f);
+            const float2 tb = lf ? TB[i] : make_float2(0.f, 0.f);
+            const float sdt = k.lvl ? dt / (g.areasvol[iv] * g.hnode_new[i]) : 0.f;
+            float x[KD];
+            float2 rm[KD];
+            unsigned okm = 0;
+#pragma unroll
+            for (int u = 0; u < KD; u++) {
+                const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
+                okm |= ok ? 1u << u : 0u;
+                x[u] = ok ? ADh[S.e[u] * L1 + nz - 1] : 0.f;
+                rm[u] = (ok && fct) ? R[S.m[u] * L1 + nz - 1] : make_float2(1.f, 1.f);
             }
             // vertical limiting (oce_adv_tra_fct.F90:425-456): interface nz by R of layers
             // nz-1 and nz; the next interface is the lane below's
@@ -588,97 +626,75 @@ __device__ __forceinline__ void advect_node(const DTopo &tp, const DGeom<float> 
             }
             float f1 = sh_dn(f0, 1);
             if (nz == nzmax - 1) f1 = 0.f;
-            // horizontal limiting (oce_adv_tra_fct.F90:468-500): R of edges(1,e) and edges(2,e)
+            // horizontal limiting (oce_adv_tra_fct.F90:468-500) seen from the node: with G the
+            // antidiffusive flux into the node and m the other end, G >= 0 takes
+            // min(R+(n), R-(m)), G < 0 takes min(R-(n), R+(m))
             float hs = 0.f;
 #pragma unroll
             for (int u = 0; u < KD; u++) {
-                const bool ok = (okm >> u) & 1u;
-                float xv = ok ? ADh[S.e[u] * L1 + nz - 1] : 0.f;
-                if (fct) {
-                    const float2 rm = ok ? R[off[u]] : make_float2(1.f, 1.f);
-                    const bool o = (own >> u) & 1u;
-                    const float2 ra = o ? r0 : rm, rb = o ? rm : r0;
-                    xv *= xv >= 0.f ? fminf(ra.x, rb.y) : fminf(ra.y, rb.x);
-                }
-                hs += ((own >> u) & 1u) ? xv : -xv;
+                float G = ((own >> u) & 1u) ? x[u] : -x[u];
+                if (fct) G *= G >= 0.f ? fminf(r0.x, rm[u].y) : fminf(r0.y, rm[u].x);
+                hs += G;
             }
             // del_ttf = (LO hnode_new - T hnode) + limited flux divergence dt / areasvol;
             // T* = T + (del_ttf + T (hnode - hnode_new)) / hnode_new = LO + fluxes dt / areasvol / hnode_new
             // (oce_adv_tra_driver.F90:535-620, oce_ale_tracer.F90:319-321, 743-754)
             float val = lo + (f0 - f1 + hs) * sdt;
-            if (k.out) {
-                if (fct) {
-                    const float2 tb = B.TB[to + i];
-                    const float vc = fminf(fmaxf(val, tb.y), tb.x);
-                    // a clamp beyond round-off means the limiter itself failed
-                    if (fabsf(vc - val) > 1e-5f * (tb.x - tb.y) + 1e-6f * fabsf(vc)) atomicOr(B.status, 2u);
-                    val = vc;
-                }
-                B.Tnew[to + i] = val;
+            if (fct && k.out) {
+                const float vc = fminf(fmaxf(val, tb.y), tb.x);
+                // a clamp beyond round-off means the limiter itself failed
+                if (fabsf(vc - val) > 1e-5f * (tb.x - tb.y) + 1e-6f * fabsf(vc)) atomicOr(B.status, 2u);
+                val = vc;
+            }
+            tad[ch] = val;
+            if (!ivd && k.out) {
+                Tout[i] = val;
                 if (!isfinite(val)) atomicOr(B.status, 1u);
             }
         }
-    }
-}
-
-// implicit vertical diffusion of the advected column (already in Tnew) for every
-// tracer with i_vert_diff: forward substitution tp_k = inv_k rhs_k - a_k inv_k tp_{k-1}
-// and back substitution x_k = tp_k - cp_k x_{k+1} as scans of affine maps
-__device__ __forceinline__ void vdiff_node(const DTopo &tp, const DForcing<float> &f, const B32View &B,
-                                           const VFactors &vf, int n, int lane, int nzmin, int nzmax) {
-    using C = Chunk<1, 1>;
-    const int L1 = tp.L1;
-    const int nch = C::count(nzmin, nzmax);
-#pragma unroll 1
-    for (int t = 0; t < B.ntr; t++) {
-        if (!B.cfg[t].ivd) continue;
-        float *__restrict__ Tout = B.Tnew + (size_t)t * B.sN;
+        if (!ivd) continue;
         const float bc = f.bc ? f.bc[(size_t)t * tp.N2 + n] : 0.f;
-        float tpv[kMaxChunks], tad[kMaxChunks];
+        float tpv[kMaxChunks];
         float carry = 0.f;
 #pragma unroll
         for (int ch = 0; ch < kMaxChunks; ch++) {
             tpv[ch] = 0.f;
-            tad[ch] = 0.f;
             if (ch >= nch) continue;
             const C k(nzmin, nzmax, ch, lane);
             const int nz = k.nz;
-            const int i = n * L1 + nz - 1;
-            const float t0 = k.lvl ? Tout[i] : 0.f;
+            const float t0 = tad[ch];
             const float tu = sh_up(t0, 1), td = sh_dn(t0, 1);
             float A = 1.f, Bv = 0.f;
             if (k.out) {
-                const float a = vf.a[i], cc = vf.c[i], inv = vf.inv[i];
+                const float4 fz = fac[nz];  // (a, c, 1/m, c/m)
                 float rhs = 0.f;
-                if (nz > nzmin) rhs -= a * (tu - t0);
-                if (nz < nzmax - 1) rhs -= cc * (td - t0);
+                if (nz > nzmin) rhs -= fz.x * (tu - t0);
+                if (nz < nzmax - 1) rhs -= fz.y * (td - t0);
                 if (nz == nzmin) rhs += bc;
-                A = -(a * inv);
-                Bv = rhs * inv;
+                A = -(fz.x * fz.z);
+                Bv = rhs * fz.z;
             }
             scan_up(A, Bv, lane);
             const float y = A * carry + Bv;
             tpv[ch] = y;
-            tad[ch] = t0;
-            carry = __shfl_sync(kFull, y, 30);
+            carry = __shfl_sync(kFull, y, 30);  // last stored lane (Chunk<1, 1>)
         }
         carry = 0.f;
 #pragma unroll
         for (int ch = kMaxChunks - 1; ch >= 0; ch--) {
             if (ch >= nch) continue;
             const C k(nzmin, nzmax, ch, lane);
-            const int i = n * L1 + k.nz - 1;
             float A = 1.f, Bv = 0.f;
             if (k.out) {
-                A = -vf.cp[i];
+                A = -fac[k.nz].w;
                 Bv = tpv[ch];
             }
             scan_down(A, Bv, lane);
-            const float x = A * carry + Bv;
-            carry = __shfl_sync(kFull, x, 1);
+            const float xx = A * carry + Bv;
+            carry = __shfl_sync(kFull, xx, 1);  // first stored lane (Chunk<1, 1>)
             if (k.out) {
-                const float val = tad[ch] + x;
-                Tout[i] = val;
+                const float val = tad[ch] + xx;
+                Tout[n * L1 + k.nz - 1] = val;
                 if (!isfinite(val)) atomicOr(B.status, 1u);
             }
         }
@@ -687,19 +703,26 @@ __device__ __forceinline__ void vdiff_node(const DTopo &tp, const DForcing<float
 
 template <bool WIDE>
 __global__ void __launch_bounds__(kTB, WIDE ? 1 : kMinBlocks)
-k32_update(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, VFactors vf, float dt, int any_ivd) {
+k32_update(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, VFactors vf, float dt) {
     __shared__ WEdges Se[kWB];
+    extern __shared__ __align__(16) float4 fac_sm[];  // kWB columns of (a, c, 1/m, c/m), 1-based levels
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int n = warp_node<WIDE>(tp, warp);
     if (n < 0) return;
     WEdges &S = Se[warp];
     stage_edges(tp, n, lane, S);
     if ((S.deg > 8) != WIDE) return;
-    advect_node<WIDE ? kMaxDeg : 8>(tp, g, B, dt, n, lane, S);
-    if (any_ivd) {
+    float4 *fac = fac_sm + (size_t)warp * (tp.L1 + 1);
+    if (B.ivd_mask) {
+        for (int nz = S.nzmin + lane; nz <= S.nzmax - 1; nz += 32) {
+            const int i = n * tp.L1 + nz - 1;
+            fac[nz] = make_float4(vf.a[i], vf.c[i], vf.inv[i], vf.cp[i]);
+        }
         __syncwarp();
-        vdiff_node(tp, f, B, vf, n, lane, S.nzmin, S.nzmax);
     }
+    if (WIDE) update_node<kMaxDeg>(tp, g, f, B, dt, n, lane, S, fac);
+    else if (S.deg <= 6) update_node<6>(tp, g, f, B, dt, n, lane, S, fac);
+    else update_node<8>(tp, g, f, B, dt, n, lane, S, fac);
 }
 
 // ---------------------------------------------------------------------------
@@ -729,16 +752,18 @@ void b32_lo_ad(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
 }
 void b32_ho(const DTopo &tp, const DGeom<float> &g, const B32View &B, const MusclW &mw, const float *VF,
             cudaStream_t s) {
-    k32_ho<<<grid_nodes(tp.E2), kTB, 0, s>>>(tp, g, B, mw, VF);
+    k32_ho<false><<<grid_nodes(tp.E2), kTB, 0, s>>>(tp, g, B, mw, VF);
+    if (tp.n_fb) k32_ho<true><<<grid_nodes(tp.n_fb), kTB, 0, s>>>(tp, g, B, mw, VF);
 }
 void b32_bounds(const DTopo &tp, const DGeom<float> &g, const B32View &B, double dt, cudaStream_t s) {
     k32_bounds<false><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, B, (float)dt);
     if (tp.n_wide) k32_bounds<true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
 }
 void b32_update(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B,
-                const VFactors &v, double dt, int any_ivd, cudaStream_t s) {
-    k32_update<false><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, f, B, v, (float)dt, any_ivd);
-    if (tp.n_wide) k32_update<true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, f, B, v, (float)dt, any_ivd);
+                const VFactors &v, double dt, cudaStream_t s) {
+    const size_t sm = sizeof(float4) * (tp.L1 + 1) * kWB;
+    k32_update<false><<<grid_nodes(tp.N2), kTB, sm, s>>>(tp, g, f, B, v, (float)dt);
+    if (tp.n_wide) k32_update<true><<<grid_nodes(tp.n_wide), kTB, sm, s>>>(tp, g, f, B, v, (float)dt);
 }
 
 }  // namespace fesom
