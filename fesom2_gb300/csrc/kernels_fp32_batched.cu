@@ -381,6 +381,29 @@ k32_lo_ad(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, const float *_
 // at the levels where every element around both nodes is wet, [gzmin, gzmax); the
 // other levels take the area-weighted node means and run in the FALLBACK launch over
 // the edges listed at init (under one percent of the edge-layers of an ocean mesh).
+// high-order minus low-order flux of one edge-layer from the two end values, their
+// previous time levels and the projected gradients s1 (up) / s2 (down)
+__device__ __forceinline__ float ho_minus_lo(int hor, float ph, int ab, float T1, float T2, float o1a, float o1b,
+                                             float o2a, float o2b, float s1, float s2, float v, float cl1, float cl2) {
+    const float vp = fmaxf(v, 0.f), vm = fminf(v, 0.f);
+    const float t1 = T1 + ab_delta(ab, T1, o1a, o2a);
+    const float t2 = T2 + ab_delta(ab, T2, o1b, o2b);
+    const float flo = -(T1 * vp + T2 * vm);
+    float hf;
+    if (hor == 2) {
+        hf = -(t1 * vp + t2 * vm);
+    } else {
+        // c_lo = 1 up to nboundary_lay (MUSCL), always 1 (MFCT)
+        const float clo1 = hor == 0 ? cl1 : 1.f, clo2 = hor == 0 ? cl2 : 1.f;
+        const float d2 = 2.f * (t2 - t1);
+        const float Tm2 = t2 - (d2 + s2) * (1.f / 6.f) * clo2;
+        const float Tm1 = t1 + (d2 + s1) * (1.f / 6.f) * clo1;
+        const float cHO = 2.f * (vp * Tm1 + vm * Tm2);
+        hf = -(0.5f * (1.f - ph) * cHO) - v * ph * 0.5f * (Tm1 + Tm2);
+    }
+    return hf - flo;
+}
+
 template <bool FALLBACK>
 __global__ void __launch_bounds__(kTB, FALLBACK ? 1 : kMinBlocks)
 k32_ho(DTopo tp, DGeom<float> g, B32View B, MusclW mw, const float *__restrict__ VF) {
@@ -400,50 +423,64 @@ k32_ho(DTopo tp, DGeom<float> g, B32View B, MusclW mw, const float *__restrict__
         const bool tri = nz >= gzmin && nz <= gzmax - 1;
         const bool ok = nz <= ehi && (FALLBACK ? !tri : true);
         const int ie = e * L1 + nz - 1, ia = n1 * L1 + nz - 1, ib = n2 * L1 + nz - 1;
-        const float v = ok ? VF[ie] : 0.f, vp = fmaxf(v, 0.f), vm = fminf(v, 0.f);
+        const float v = ok ? VF[ie] : 0.f;
         const float cl1 = (nbl1 - nz) >= 0 ? 1.f : 0.f, cl2 = (nbl2 - nz) >= 0 ? 1.f : 0.f;
         const int ua = un.y * L1 + nz - 1, ub = un.z * L1 + nz - 1;
         const int da = dn.y * L1 + nz - 1, db = dn.z * L1 + nz - 1;
+        if (!ok) continue;
+        if (FALLBACK) {
 #pragma unroll 1
-        for (int t = 0; t < B.ntr; t++) {
-            if (!ok) continue;
-            const int hor = B.hor[t];
-            if (FALLBACK && hor == 2) continue;  // UPW1 has no gradients: the main launch wrote it
-            const size_t to = (size_t)t * B.sN;
-            const float *__restrict__ T = B.T + to;
-            const float *__restrict__ O1 = B.O1 + to;
-            const float *__restrict__ O2 = B.ab == 3 ? B.O2 + to : O1;
-            const float T1 = T[ia], T2 = T[ib];
-            const bool grad = !FALLBACK && hor != 2 && tri;
-            const float ga = grad ? T[ua] : 0.f, gb = grad ? T[ub] : 0.f;
-            const float gc = grad ? T[da] : 0.f, gd = grad ? T[db] : 0.f;
-            const float t1 = T1 + ab_delta(B.ab, T1, O1[ia], B.ab == 3 ? O2[ia] : 0.f);
-            const float t2 = T2 + ab_delta(B.ab, T2, O1[ib], B.ab == 3 ? O2[ib] : 0.f);
-            const float flo = -(T1 * vp + T2 * vm);
-            float hf;
-            if (hor == 2) {
-                hf = -(t1 * vp + t2 * vm);
-            } else {
-                float s1, s2;
-                if (FALLBACK) {
-                    const float exa = g.edxy[2 * (size_t)e] * wu.w, eyr = g.edxy[2 * (size_t)e + 1] * (float)kREarth;
-                    s1 = node_grad_proj(tp, g, T, n1, nz, exa, eyr);
-                    s2 = node_grad_proj(tp, g, T, n2, nz, exa, eyr);
-                } else {
-                    if (!tri) continue;  // written by the fallback launch
-                    s1 = wu.y * (ga - T1) + wu.z * (gb - T1);
-                    s2 = wd.y * (gc - T2) + wd.z * (gd - T2);
-                }
-                // c_lo = 1 up to nboundary_lay (MUSCL), always 1 (MFCT)
-                const float clo1 = hor == 0 ? cl1 : 1.f, clo2 = hor == 0 ? cl2 : 1.f;
-                const float d2 = 2.f * (t2 - t1);
-                const float Tm2 = t2 - (d2 + s2) * (1.f / 6.f) * clo2;
-                const float Tm1 = t1 + (d2 + s1) * (1.f / 6.f) * clo1;
-                const float no = B.ph[t];
-                const float cHO = 2.f * (vp * Tm1 + vm * Tm2);
-                hf = -(0.5f * (1.f - no) * cHO) - v * no * 0.5f * (Tm1 + Tm2);
+            for (int t = 0; t < B.ntr; t++) {
+                const int hor = B.hor[t];
+                if (hor == 2) continue;  // UPW1 has no gradients: the main launch wrote it
+                const size_t to = (size_t)t * B.sN;
+                const float *__restrict__ T = B.T + to;
+                const float exa = g.edxy[2 * (size_t)e] * wu.w, eyr = g.edxy[2 * (size_t)e + 1] * (float)kREarth;
+                const float T1 = T[ia], T2 = T[ib];
+                const float o1a = B.O1[to + ia], o1b = B.O1[to + ib];
+                const float o2a = B.ab == 3 ? B.O2[to + ia] : 0.f, o2b = B.ab == 3 ? B.O2[to + ib] : 0.f;
+                const float s1 = node_grad_proj(tp, g, T, n1, nz, exa, eyr);
+                const float s2 = node_grad_proj(tp, g, T, n2, nz, exa, eyr);
+                B.ADh[(size_t)t * B.sE + ie] =
+                    ho_minus_lo(hor, B.ph[t], B.ab, T1, T2, o1a, o1b, o2a, o2b, s1, s2, v, cl1, cl2);
             }
-            B.ADh[(size_t)t * B.sE + ie] = hf - flo;
+            continue;
+        }
+        // two tracers per pass: their gathers in flight together
+#pragma unroll 1
+        for (int t = 0; t < B.ntr; t += 2) {
+            const bool two = t + 1 < B.ntr;
+            float T1[2], T2[2], o1a[2], o1b[2], o2a[2], o2b[2], ga[2], gb[2], gc[2], gd[2];
+            bool grad[2];
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const bool on = q == 0 || two;
+                const int tq = on ? t + q : t;
+                const size_t to = (size_t)tq * B.sN;
+                const float *__restrict__ T = B.T + to;
+                grad[q] = on && B.hor[tq] != 2 && tri;
+                T1[q] = on ? T[ia] : 0.f;
+                T2[q] = on ? T[ib] : 0.f;
+                o1a[q] = on ? B.O1[to + ia] : 0.f;
+                o1b[q] = on ? B.O1[to + ib] : 0.f;
+                o2a[q] = (on && B.ab == 3) ? B.O2[to + ia] : 0.f;
+                o2b[q] = (on && B.ab == 3) ? B.O2[to + ib] : 0.f;
+                ga[q] = grad[q] ? T[ua] : 0.f;
+                gb[q] = grad[q] ? T[ub] : 0.f;
+                gc[q] = grad[q] ? T[da] : 0.f;
+                gd[q] = grad[q] ? T[db] : 0.f;
+            }
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                if (q == 1 && !two) continue;
+                const int hor = B.hor[t + q];
+                // MUSCL / MFCT levels outside the triangles' range: the fallback launch
+                if (hor != 2 && !tri) continue;
+                const float s1 = wu.y * (ga[q] - T1[q]) + wu.z * (gb[q] - T1[q]);
+                const float s2 = wd.y * (gc[q] - T2[q]) + wd.z * (gd[q] - T2[q]);
+                B.ADh[(size_t)(t + q) * B.sE + ie] = ho_minus_lo(hor, B.ph[t + q], B.ab, T1[q], T2[q], o1a[q], o1b[q],
+                                                                 o2a[q], o2b[q], s1, s2, v, cl1, cl2);
+            }
         }
     }
 }
