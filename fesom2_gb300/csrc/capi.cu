@@ -266,7 +266,9 @@ int init_muscl_weights(fesom_gpu_ctx *ctx, const fesom_mesh_desc *d) {
         }
     std::vector<int4> un(E2), dn(E2);
     std::vector<float4> wu(E2), wd(E2);
-    std::vector<int> fb;
+    std::vector<int> it_e, it_nz, it_ptr(1, 0), it_n1, wn;
+    std::vector<double> ww;
+    std::vector<int2> pairs;
     int rc;
     for (int e = 0; e < E2; e++) {
         const int n1 = h.e_n1[e], n2 = h.e_n2[e], el1 = h.e_t1[e], el2 = h.e_t2[e];
@@ -302,11 +304,64 @@ int init_muscl_weights(fesom_gpu_ctx *ctx, const fesom_mesh_desc *d) {
         tri(up, n1, un[e], wu[e]);
         tri(dw, n2, dn[e], wd[e]);
         un[e].w = gzmin | (gzmax << 16);
-        if (h.e_lo[e] < gzmin || h.e_hi[e] > gzmax - 1) fb.push_back(e);
+        // edge-layers outside [gzmin, gzmax): the projected node-mean gradient at each end
+        // node as weights of its neighbours' values (difference form: the weights of an
+        // element sum to zero, so the end node's own weight drops out)
+        for (int nz = h.e_lo[e]; nz <= h.e_hi[e]; nz++) {
+            if (nz >= gzmin && nz <= gzmax - 1) continue;
+            it_e.push_back(e);
+            it_nz.push_back(nz);
+            for (int side = 0; side < 2; side++) {
+                const int node = side == 0 ? n1 : n2;
+                wn.clear();
+                ww.clear();
+                double tvol = 0.0;
+                for (int k = h.nie_ptr[node]; k < h.nie_ptr[node + 1]; k++) {
+                    const int el = h.nie_idx[k];
+                    if (h.t_nlev[el] - 1 < nz || nz < h.t_ulev[el]) continue;
+                    const double ea = d->elem_area[el];
+                    const double *gs = d->gradient_sca + 6 * (size_t)el;
+                    tvol += ea;
+                    for (int q = 0; q < 3; q++) {
+                        const int vtx = h.t_n[3 * (size_t)el + q];
+                        const double wq = ea * (ex * a * gs[q] + ey * kREarth * gs[q + 3]);
+                        size_t j = 0;
+                        while (j < wn.size() && wn[j] != vtx) j++;
+                        if (j == wn.size()) { wn.push_back(vtx); ww.push_back(0.0); }
+                        ww[j] += wq;
+                    }
+                }
+                int cnt = 0;
+                for (size_t j = 0; j < wn.size(); j++) {
+                    if (wn[j] == node || tvol <= 0.0) continue;
+                    const float wf = (float)(ww[j] / tvol);
+                    int wb;
+                    std::memcpy(&wb, &wf, sizeof(int));
+                    pairs.push_back(make_int2(wn[j], wb));
+                    cnt++;
+                }
+                if (side == 0) it_n1.push_back(cnt);
+            }
+            it_ptr.push_back((int)pairs.size());
+        }
     }
-    ctx->tp.n_fb = (int)fb.size();
-    ctx->tp.fb_edges = nullptr;
-    if (!fb.empty() && (rc = upload_int(ctx, &ctx->tp.fb_edges, fb))) return rc;
+    MusclW &mw = ctx->mw;
+    mw.n_items = (int)it_e.size();
+    if (mw.n_items) {
+        const int *q;
+        if ((rc = upload_int(ctx, &q, it_e))) return rc;
+        mw.it_e = q;
+        if ((rc = upload_int(ctx, &q, it_nz))) return rc;
+        mw.it_nz = q;
+        if ((rc = upload_int(ctx, &q, it_ptr))) return rc;
+        mw.it_ptr = q;
+        if ((rc = upload_int(ctx, &q, it_n1))) return rc;
+        mw.it_n1 = q;
+        void *pp;
+        if ((rc = dalloc(ctx, &pp, sizeof(int2) * std::max<size_t>(1, pairs.size())))) return rc;
+        if (!pairs.empty()) CK(cudaMemcpy(pp, pairs.data(), sizeof(int2) * pairs.size(), cudaMemcpyHostToDevice));
+        mw.pairs = (const int2 *)pp;
+    }
     void *p;
     if ((rc = dalloc(ctx, &p, sizeof(int4) * E2))) return rc;
     CK(cudaMemcpy(p, un.data(), sizeof(int4) * E2, cudaMemcpyHostToDevice));
@@ -630,7 +685,7 @@ int launches_per_step(fesom_gpu_ctx *ctx) {
             for (int t = t0; t < t0 + nt; t++) any_fct |= ctx->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
             // lo_ad, update (+ bounds), launched again for the wide nodes; ho (+ its fallback edges)
             const int wide = ctx->tp.n_wide ? 2 : 1;
-            n += wide * (2 + (any_fct ? 1 : 0)) + (ctx->tp.n_fb ? 2 : 1);
+            n += wide * (2 + (any_fct ? 1 : 0)) + (ctx->mw.n_items ? 2 : 1);
         }
         return n;
     }

@@ -33,8 +33,6 @@ struct DTopo {
     const int *nie_ptr, *nie_idx;  // node -> element, ascending element order
     int n_wide;                    // nodes of more than 8 edges (FP32 form: their own launch)
     const int *wide_nodes;
-    int n_fb;                      // edges with levels outside their triangles' shared range
-    const int *fb_edges;           // (FP32 form: the node-mean MUSCL gradients, own launch)
 };
 
 template <typename R>
@@ -112,6 +110,14 @@ constexpr int kMaxDeg = 16;
 struct MusclW {
     const int4 *un, *dn;
     const float4 *wu, *wd;
+    // edge-layers outside their triangles' shared range (and every layer of an edge
+    // without an up or down triangle) take the area-weighted node means of the element
+    // gradients (oce_muscl_adv.F90:388-405, 441-521): per item (edge e, level nz) the
+    // projected mean gradient at edges(1,e) is sum_j w_j (T(node_j) - T(edges(1,e)))
+    // over pairs [ptr, ptr + n1), at edges(2,e) over [ptr + n1, next ptr)
+    int n_items;
+    const int *it_e, *it_nz, *it_ptr, *it_n1;
+    const int2 *pairs;  // (node, weight as float bits)
 };
 // FP32 copies of the FP64 factorisation of each column's vertical-diffusion matrix
 struct VFactors {

@@ -195,25 +195,6 @@ __device__ __forceinline__ float ab_delta(int ab, float t, float o1, float o2) {
     return ab == 2 ? 0.6f * (t - o1) : (11.f * (t - o1) - 5.f * (o1 - o2)) * (1.f / 12.f);
 }
 
-// area-weighted mean over the node's wet elements of the element gradient,
-// projected on the edge: ex*a*gx + ey*R*gy (fill_up_dn_grad node means)
-__device__ __noinline__ float node_grad_proj(const DTopo &tp, const DGeom<float> &g, const float *T, int node, int nz,
-                                             float exa, float eyr) {
-    const int L1 = tp.L1;
-    float tvol = 0.f, tx = 0.f, ty = 0.f;
-    for (int k = tp.nie_ptr[node]; k < tp.nie_ptr[node + 1]; k++) {
-        const int el = tp.nie_idx[k];
-        if (tp.t_nlev[el] - 1 < nz || nz < tp.t_ulev[el]) continue;
-        const int a = tp.t_n[3 * el], b = tp.t_n[3 * el + 1], c = tp.t_n[3 * el + 2];
-        const float *gs = g.gs + 6 * (size_t)el;
-        const float ta = T[i1(nz, a, L1)], tb = T[i1(nz, b, L1)], tc = T[i1(nz, c, L1)];
-        const float ea = g.elem_area[el];
-        tvol += ea;
-        tx += (gs[0] * ta + gs[1] * tb + gs[2] * tc) * ea;
-        ty += (gs[3] * ta + gs[4] * tb + gs[5] * tc) * ea;
-    }
-    return exa * (tx / tvol) + eyr * (ty / tvol);
-}
 
 
 // ---------------------------------------------------------------------------
@@ -367,20 +348,6 @@ k32_lo_ad(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, const float *_
     else lo_ad_node<8>(tp, g, f, B, VF, dt, n, lane, S);
 }
 
-// ---------------------------------------------------------------------------
-// k32_ho: high-order minus low-order flux of every edge-layer
-// ---------------------------------------------------------------------------
-// One warp per edge, the lanes over the edge's levels [nu12, nl12].  MUSCL / MFCT
-// (adv_tra_hor_muscl / _mfct, oce_adv_tra_hor.F90:261-834) on the AB values with the
-// gradients of fill_up_dn_grad (oce_muscl_adv.F90:356-525); UPW1 (:64-257).  The LO
-// flux is the upwind flux of the current values (oce_adv_tra_driver.F90:131-190).
-//
-// The up triangle holds edges(1,e) and the down triangle edges(2,e); their gradients,
-// projected on the edge, are wu.y (T(un.y) - T1) + wu.z (T(un.z) - T1) and the same
-// for the down triangle (the three weights of a triangle sum to zero).  Those apply
-// at the levels where every element around both nodes is wet, [gzmin, gzmax); the
-// other levels take the area-weighted node means and run in the FALLBACK launch over
-// the edges listed at init (under one percent of the edge-layers of an ocean mesh).
 // high-order minus low-order flux of one edge-layer from the two end values, their
 // previous time levels and the projected gradients s1 (up) / s2 (down)
 __device__ __forceinline__ float ho_minus_lo(int hor, float ph, int ab, float T1, float T2, float o1a, float o1b,
@@ -404,13 +371,25 @@ __device__ __forceinline__ float ho_minus_lo(int hor, float ph, int ab, float T1
     return hf - flo;
 }
 
-template <bool FALLBACK>
-__global__ void __launch_bounds__(kTB, FALLBACK ? 1 : kMinBlocks)
-k32_ho(DTopo tp, DGeom<float> g, B32View B, MusclW mw, const float *__restrict__ VF) {
+// ---------------------------------------------------------------------------
+// k32_ho: high-order minus low-order flux of every edge-layer
+// ---------------------------------------------------------------------------
+// One warp per edge, the lanes over the edge's levels [nu12, nl12].  MUSCL / MFCT
+// (adv_tra_hor_muscl / _mfct, oce_adv_tra_hor.F90:261-834) on the AB values with the
+// gradients of fill_up_dn_grad (oce_muscl_adv.F90:356-525); UPW1 (:64-257).  The LO
+// flux is the upwind flux of the current values (oce_adv_tra_driver.F90:131-190).
+//
+// The up triangle holds edges(1,e) and the down triangle edges(2,e); their gradients,
+// projected on the edge, are wu.y (T(un.y) - T1) + wu.z (T(un.z) - T1) and the same
+// for the down triangle (the three weights of a triangle sum to zero).  Those apply
+// at the levels where every element around both nodes is wet, [gzmin, gzmax); the
+// other edge-layers (under one percent of an ocean mesh's) take the node means in
+// k32_ho_nodemean.
+__global__ void __launch_bounds__(kTB, kMinBlocks)
+k32_ho(DTopo tp, B32View B, MusclW mw, const float *__restrict__ VF) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int j = blockIdx.x * kWB + warp;
-    if (j >= (FALLBACK ? tp.n_fb : tp.E2)) return;
-    const int e = FALLBACK ? tp.fb_edges[j] : j;
+    const int e = blockIdx.x * kWB + warp;
+    if (e >= tp.E2) return;
     const int L1 = tp.L1;
     const int n1 = tp.e_n1[e], n2 = tp.e_n2[e];
     const int elo = tp.e_lo[e], ehi = tp.e_hi[e];
@@ -421,31 +400,13 @@ k32_ho(DTopo tp, DGeom<float> g, B32View B, MusclW mw, const float *__restrict__
     for (int nz0 = elo; nz0 <= ehi; nz0 += 32) {
         const int nz = nz0 + lane;
         const bool tri = nz >= gzmin && nz <= gzmax - 1;
-        const bool ok = nz <= ehi && (FALLBACK ? !tri : true);
+        const bool ok = nz <= ehi;
         const int ie = e * L1 + nz - 1, ia = n1 * L1 + nz - 1, ib = n2 * L1 + nz - 1;
         const float v = ok ? VF[ie] : 0.f;
         const float cl1 = (nbl1 - nz) >= 0 ? 1.f : 0.f, cl2 = (nbl2 - nz) >= 0 ? 1.f : 0.f;
         const int ua = un.y * L1 + nz - 1, ub = un.z * L1 + nz - 1;
         const int da = dn.y * L1 + nz - 1, db = dn.z * L1 + nz - 1;
         if (!ok) continue;
-        if (FALLBACK) {
-#pragma unroll 1
-            for (int t = 0; t < B.ntr; t++) {
-                const int hor = B.hor[t];
-                if (hor == 2) continue;  // UPW1 has no gradients: the main launch wrote it
-                const size_t to = (size_t)t * B.sN;
-                const float *__restrict__ T = B.T + to;
-                const float exa = g.edxy[2 * (size_t)e] * wu.w, eyr = g.edxy[2 * (size_t)e + 1] * (float)kREarth;
-                const float T1 = T[ia], T2 = T[ib];
-                const float o1a = B.O1[to + ia], o1b = B.O1[to + ib];
-                const float o2a = B.ab == 3 ? B.O2[to + ia] : 0.f, o2b = B.ab == 3 ? B.O2[to + ib] : 0.f;
-                const float s1 = node_grad_proj(tp, g, T, n1, nz, exa, eyr);
-                const float s2 = node_grad_proj(tp, g, T, n2, nz, exa, eyr);
-                B.ADh[(size_t)t * B.sE + ie] =
-                    ho_minus_lo(hor, B.ph[t], B.ab, T1, T2, o1a, o1b, o2a, o2b, s1, s2, v, cl1, cl2);
-            }
-            continue;
-        }
         // two tracers per pass: their gathers in flight together
 #pragma unroll 1
         for (int t = 0; t < B.ntr; t += 2) {
@@ -481,6 +442,40 @@ k32_ho(DTopo tp, DGeom<float> g, B32View B, MusclW mw, const float *__restrict__
                 B.ADh[(size_t)(t + q) * B.sE + ie] = ho_minus_lo(hor, B.ph[t + q], B.ab, T1[q], T2[q], o1a[q], o1b[q],
                                                                  o2a[q], o2b[q], s1, s2, v, cl1, cl2);
             }
+        }
+    }
+}
+
+// The edge-layers of the node-mean gradients: one thread per (edge, level) item, every
+// tracer, with the projected mean gradients as precomputed neighbour weights.
+__global__ void __launch_bounds__(256) k32_ho_nodemean(DTopo tp, B32View B, MusclW mw, const float *__restrict__ VF) {
+    const int L1 = tp.L1;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < mw.n_items; j += gridDim.x * blockDim.x) {
+        const int e = mw.it_e[j], nz = mw.it_nz[j];
+        const int p0 = mw.it_ptr[j], p1 = p0 + mw.it_n1[j], p2 = mw.it_ptr[j + 1];
+        const int n1 = tp.e_n1[e], n2 = tp.e_n2[e];
+        const int ie = e * L1 + nz - 1, ia = n1 * L1 + nz - 1, ib = n2 * L1 + nz - 1;
+        const float v = VF[ie];
+        const float cl1 = (tp.n_nbl[n1] - nz) >= 0 ? 1.f : 0.f, cl2 = (tp.n_nbl[n2] - nz) >= 0 ? 1.f : 0.f;
+#pragma unroll 1
+        for (int t = 0; t < B.ntr; t++) {
+            const int hor = B.hor[t];
+            if (hor == 2) continue;  // UPW1 has no gradients: k32_ho wrote it
+            const size_t to = (size_t)t * B.sN;
+            const float *__restrict__ T = B.T + to;
+            const float T1 = T[ia], T2 = T[ib];
+            const float o1a = B.O1[to + ia], o1b = B.O1[to + ib];
+            const float o2a = B.ab == 3 ? B.O2[to + ia] : 0.f, o2b = B.ab == 3 ? B.O2[to + ib] : 0.f;
+            float s1 = 0.f, s2 = 0.f;
+            for (int p = p0; p < p1; p++) {
+                const int2 q = mw.pairs[p];
+                s1 += __int_as_float(q.y) * (T[q.x * L1 + nz - 1] - T1);
+            }
+            for (int p = p1; p < p2; p++) {
+                const int2 q = mw.pairs[p];
+                s2 += __int_as_float(q.y) * (T[q.x * L1 + nz - 1] - T2);
+            }
+            B.ADh[(size_t)t * B.sE + ie] = ho_minus_lo(hor, B.ph[t], B.ab, T1, T2, o1a, o1b, o2a, o2b, s1, s2, v, cl1, cl2);
         }
     }
 }
@@ -789,8 +784,12 @@ void b32_lo_ad(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
 }
 void b32_ho(const DTopo &tp, const DGeom<float> &g, const B32View &B, const MusclW &mw, const float *VF,
             cudaStream_t s) {
-    k32_ho<false><<<grid_nodes(tp.E2), kTB, 0, s>>>(tp, g, B, mw, VF);
-    if (tp.n_fb) k32_ho<true><<<grid_nodes(tp.n_fb), kTB, 0, s>>>(tp, g, B, mw, VF);
+    k32_ho<<<grid_nodes(tp.E2), kTB, 0, s>>>(tp, B, mw, VF);
+    if (mw.n_items) {
+        int blocks = (mw.n_items + 255) / 256;
+        if (blocks > 152 * 8) blocks = 152 * 8;
+        k32_ho_nodemean<<<blocks, 256, 0, s>>>(tp, B, mw, VF);
+    }
 }
 void b32_bounds(const DTopo &tp, const DGeom<float> &g, const B32View &B, double dt, cudaStream_t s) {
     k32_bounds<false><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, B, (float)dt);
