@@ -52,7 +52,19 @@ constexpr int kWB = 8;                // warps (= nodes) per block
 constexpr int kTB = 32 * kWB;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kMaxChunks = 5;         // columns of up to 128 layers, 30 levels per chunk
-constexpr int kMinBlocks = 3;         // resident blocks per SM the tracer kernels are built for (<= 80 registers)
+// resident blocks per SM each tracer kernel is built for (3: <= 80 registers, 4: <= 64)
+#ifndef FESOM_MINB_LO
+#define FESOM_MINB_LO 3
+#endif
+#ifndef FESOM_MINB_HO
+#define FESOM_MINB_HO 4
+#endif
+#ifndef FESOM_MINB_BOUNDS
+#define FESOM_MINB_BOUNDS 4
+#endif
+#ifndef FESOM_MINB_UPDATE
+#define FESOM_MINB_UPDATE 4
+#endif
 
 __device__ __forceinline__ size_t i1(int nz, int n, int L1) { return (size_t)n * L1 + (nz - 1); }
 
@@ -101,45 +113,109 @@ __global__ void __launch_bounds__(kTB) k32_vflux(DTopo tp, DGeom<float> g, DForc
 // ---------------------------------------------------------------------------
 // k32_vfactors: FP64 factorisation of each column's tridiagonal system
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k32_vfactors(DTopo tp, DGeom<float> g, DForcing<float> f, double dt,
-                                                    VFactors vf) {
-    // a(k) = -Kv(k) dt/(Z_n(k-1)-Z_n(k)) area(k)/areasvol(k), c(k) = -Kv(k+1) dt/(Z_n(k)-Z_n(k+1))
-    // area(k+1)/areasvol(k), b = -a - c + hnode_new (oce_ale_tracer.F90:1099-1204), with
-    // Z_n(k)-Z_n(k+1) = (hnode_new(k) + hnode_new(k+1))/2 (the mid-depths of :1088-1096);
-    // Thomas pivots m(k) = b(k) - cp(k-1) a(k), cp(k) = c(k)/m(k) (:1406-1414)
+// a(k) = -Kv(k) dt/(Z_n(k-1)-Z_n(k)) area(k)/areasvol(k), c(k) = -Kv(k+1) dt/(Z_n(k)-Z_n(k+1))
+// area(k+1)/areasvol(k), b = -a - c + hnode_new (oce_ale_tracer.F90:1099-1204), with
+// Z_n(k)-Z_n(k+1) = (hnode_new(k) + hnode_new(k+1))/2 (the mid-depths of :1088-1096);
+// Thomas pivots m(k) = b(k) - cp(k-1) a(k), cp(k) = c(k)/m(k) (:1406-1414).
+// One thread per column runs the recurrence; the block's columns move through shared
+// memory in tiles of kVfK levels, loaded and stored with the lanes over the levels of a
+// column (each column's tile is one contiguous run), so no thread walks its own column
+// through the cache.
+constexpr int kVfCols = 128;  // columns per block
+constexpr int kVfK = 8;       // levels per tile
+__global__ void __launch_bounds__(kVfCols) k32_vfactors(DTopo tp, DGeom<float> g, DForcing<float> f, double dt,
+                                                        VFactors vf) {
+    // inputs for levels lev0 .. lev0 + kVfK (one extra: the next level's h, Kv, area);
+    // outputs for levels lev0 .. lev0 + kVfK - 1
+    __shared__ float s_hn[kVfCols][kVfK + 1], s_ar[kVfCols][kVfK + 1], s_av[kVfCols][kVfK + 1],
+        s_kv[kVfCols][kVfK + 1];
+    __shared__ float s_a[kVfCols][kVfK], s_c[kVfCols][kVfK], s_i[kVfCols][kVfK], s_p[kVfCols][kVfK];
+    __shared__ int s_lmax;
     const int L1 = tp.L1, nl = tp.nl;
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < tp.N2; n += gridDim.x * blockDim.x) {
-        const int nzmax = tp.n_nlev[n], nzmin = tp.n_ulev[n];
-        const float *hn = g.hnode_new + (size_t)n * L1 - 1;
-        const float *ar = g.area + (size_t)n * nl - 1;
-        const float *av = g.areasvol + (size_t)n * nl - 1;
-        const float *kv = f.Kv + (size_t)n * nl - 1;
-        float *oa = vf.a + (size_t)n * L1 - 1, *oc = vf.c + (size_t)n * L1 - 1;
-        float *oi = vf.inv + (size_t)n * L1 - 1, *ocp = vf.cp + (size_t)n * L1 - 1;
-        double cp = 0.0, zinv1 = 0.0;
-        double hcur = (double)hn[nzmin];
-        for (int nz = nzmin; nz <= nzmax - 1; nz++) {
-            const double hnext = nz < nzmax - 1 ? (double)hn[nz + 1] : 0.0;
-            const double avz = (double)av[nz];
-            const double a = nz > nzmin ? -((double)kv[nz] * zinv1 * dt * ((double)ar[nz] / avz)) : 0.0;
-            double c = 0.0, zinv2 = 0.0;
-            if (nz < nzmax - 1) {
-                zinv2 = 2.0 / (hcur + hnext);
-                c = -((double)kv[nz + 1] * zinv2 * dt * (double)ar[nz + 1] / avz);
+    const int c0 = blockIdx.x * kVfCols, tid = threadIdx.x;
+    const int ncol = min(kVfCols, tp.N2 - c0);
+    const int n = c0 + tid;
+    const bool mine = tid < ncol;
+    const int nzmin = mine ? tp.n_ulev[n] : 1, nzmax = mine ? tp.n_nlev[n] : 1;
+    if (tid == 0) s_lmax = 0;
+    __syncthreads();
+    if (mine) atomicMax(&s_lmax, nzmax - 1);
+    __syncthreads();
+    const int lmax = s_lmax;
+    int lmin = 1 << 30;
+    // the first tile starts at the block's shallowest top layer
+    {
+        __shared__ int s_lmin;
+        if (tid == 0) s_lmin = 1 << 30;
+        __syncthreads();
+        if (mine) atomicMin(&s_lmin, nzmin);
+        __syncthreads();
+        lmin = s_lmin;
+    }
+    double cp = 0.0, zinv1 = 0.0, hcur = 0.0;
+    for (int lev0 = lmin; lev0 <= lmax; lev0 += kVfK) {
+        // load: item q = column * (kVfK + 1) + k, consecutive threads on consecutive levels
+        for (int q = tid; q < ncol * (kVfK + 1); q += kVfCols) {
+            const int col = q / (kVfK + 1), k = q - col * (kVfK + 1);
+            const int lev = lev0 + k, cn = c0 + col;
+            float hv = 0.f, arv = 0.f, avv = 0.f, kvv = 0.f;
+            if (lev <= L1) hv = g.hnode_new[(size_t)cn * L1 + lev - 1];
+            if (lev <= nl) {
+                const size_t iv = (size_t)cn * nl + lev - 1;
+                arv = g.area[iv];
+                avv = g.areasvol[iv];
+                kvv = f.Kv[iv];
             }
-            const double b = -a - c + hcur;
-            const double inv = 1.0 / (b - cp * a);
-            cp = c * inv;
-            oa[nz] = (float)a;
-            oc[nz] = (float)c;
-            oi[nz] = (float)inv;
-            ocp[nz] = (float)cp;
-            zinv1 = zinv2;
-            hcur = hnext;
+            s_hn[col][k] = hv;
+            s_ar[col][k] = arv;
+            s_av[col][k] = avv;
+            s_kv[col][k] = kvv;
         }
+        __syncthreads();
+        if (mine) {
+            for (int k = 0; k < kVfK; k++) {
+                const int nz = lev0 + k;
+                float oa = 0.f, oc = 0.f, oi = 0.f, ocp = 0.f;
+                if (nz >= nzmin && nz <= nzmax - 1) {
+                    if (nz == nzmin) hcur = (double)s_hn[tid][k];
+                    const double hnext = nz < nzmax - 1 ? (double)s_hn[tid][k + 1] : 0.0;
+                    const double avz = (double)s_av[tid][k];
+                    const double a = nz > nzmin ? -((double)s_kv[tid][k] * zinv1 * dt * ((double)s_ar[tid][k] / avz)) : 0.0;
+                    double c = 0.0, zinv2 = 0.0;
+                    if (nz < nzmax - 1) {
+                        zinv2 = 2.0 / (hcur + hnext);
+                        c = -((double)s_kv[tid][k + 1] * zinv2 * dt * (double)s_ar[tid][k + 1] / avz);
+                    }
+                    const double b = -a - c + hcur;
+                    const double inv = 1.0 / (b - cp * a);
+                    cp = c * inv;
+                    oa = (float)a;
+                    oc = (float)c;
+                    oi = (float)inv;
+                    ocp = (float)cp;
+                    zinv1 = zinv2;
+                    hcur = hnext;
+                }
+                s_a[tid][k] = oa;
+                s_c[tid][k] = oc;
+                s_i[tid][k] = oi;
+                s_p[tid][k] = ocp;
+            }
+        }
+        __syncthreads();
+        for (int q = tid; q < ncol * kVfK; q += kVfCols) {
+            const int col = q / kVfK, k = q - col * kVfK;
+            const int lev = lev0 + k, cn = c0 + col;
+            if (lev > L1) continue;
+            const size_t i = (size_t)cn * L1 + lev - 1;
+            vf.a[i] = s_a[col][k];
+            vf.c[i] = s_c[col][k];
+            vf.inv[i] = s_i[col][k];
+            vf.cp[i] = s_p[col][k];
+        }
+        __syncthreads();
     }
 }
-
 
 // ---------------------------------------------------------------------------
 // per-warp staging of the node's edge list (one warp per node)
@@ -334,7 +410,7 @@ __device__ __forceinline__ int warp_node(const DTopo &tp, int warp) {
 }
 
 template <bool WIDE>
-__global__ void __launch_bounds__(kTB, WIDE ? 1 : kMinBlocks)
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_LO)
 k32_lo_ad(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, const float *__restrict__ VF, float dt) {
     __shared__ WEdges Se[kWB];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -385,7 +461,7 @@ __device__ __forceinline__ float ho_minus_lo(int hor, float ph, int ab, float T1
 // at the levels where every element around both nodes is wet, [gzmin, gzmax); the
 // other edge-layers (under one percent of an ocean mesh's) take the node means in
 // k32_ho_nodemean.
-__global__ void __launch_bounds__(kTB, kMinBlocks)
+__global__ void __launch_bounds__(kTB, FESOM_MINB_HO)
 k32_ho(DTopo tp, B32View B, MusclW mw, const float *__restrict__ VF) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int e = blockIdx.x * kWB + warp;
@@ -561,7 +637,7 @@ __device__ __forceinline__ void bounds_node(const DTopo &tp, const DGeom<float> 
 }
 
 template <bool WIDE>
-__global__ void __launch_bounds__(kTB, WIDE ? 1 : kMinBlocks) k32_bounds(DTopo tp, DGeom<float> g, B32View B, float dt) {
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_BOUNDS) k32_bounds(DTopo tp, DGeom<float> g, B32View B, float dt) {
     __shared__ WEdges Se[kWB];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int n = warp_node<WIDE>(tp, warp);
@@ -734,7 +810,7 @@ __device__ __forceinline__ void update_node(const DTopo &tp, const DGeom<float> 
 }
 
 template <bool WIDE>
-__global__ void __launch_bounds__(kTB, WIDE ? 1 : kMinBlocks)
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_UPDATE)
 k32_update(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, VFactors vf, float dt) {
     __shared__ WEdges Se[kWB];
     extern __shared__ __align__(16) float4 fac_sm[];  // kWB columns of (a, c, 1/m, c/m), 1-based levels
@@ -771,7 +847,7 @@ void b32_vflux(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
 }
 void b32_vfactors(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, double dt, const VFactors &v,
                   cudaStream_t s) {
-    k32_vfactors<<<(tp.N2 + 127) / 128, 128, 0, s>>>(tp, g, f, dt, v);
+    k32_vfactors<<<(tp.N2 + kVfCols - 1) / kVfCols, kVfCols, 0, s>>>(tp, g, f, dt, v);
 }
 // node kernels: one warp per node, kWB consecutive nodes per block; the nodes of more
 // than 8 edges (listed at init) take a second, small launch with 16 edge slots
