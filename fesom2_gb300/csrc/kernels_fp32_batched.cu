@@ -117,7 +117,9 @@ __global__ void __launch_bounds__(kTB) k32_vflux(DTopo tp, DGeom<float> g, DForc
 // area(k+1)/areasvol(k), b = -a - c + hnode_new (oce_ale_tracer.F90:1099-1204), with
 // Z_n(k)-Z_n(k+1) = (hnode_new(k) + hnode_new(k+1))/2 (the mid-depths of :1088-1096);
 // Thomas pivots m(k) = b(k) - cp(k-1) a(k), cp(k) = c(k)/m(k) (:1406-1414).
-// One thread per column runs the recurrence; the block's columns move through shared
+// a, b, c are formed in FP32 and used with those rounded values throughout, so all
+// factors belong to one consistent system; the pivot recurrence, where thin bottom
+// cells cancel most bits, runs in FP64.  One thread per column runs the recurrence; the block's columns move through shared
 // memory in tiles of kVfK levels, loaded and stored with the lanes over the levels of a
 // column (each column's tile is one contiguous run), so no thread walks its own column
 // through the cache.
@@ -152,7 +154,9 @@ __global__ void __launch_bounds__(kVfCols) k32_vfactors(DTopo tp, DGeom<float> g
         __syncthreads();
         lmin = s_lmin;
     }
-    double cp = 0.0, zinv1 = 0.0, hcur = 0.0;
+    const float dtf = (float)dt;
+    double cp = 0.0;
+    float zinv1 = 0.f, hcur = 0.f;
     for (int lev0 = lmin; lev0 <= lmax; lev0 += kVfK) {
         // load: item q = column * (kVfK + 1) + k, consecutive threads on consecutive levels
         for (int q = tid; q < ncol * (kVfK + 1); q += kVfCols) {
@@ -177,21 +181,25 @@ __global__ void __launch_bounds__(kVfCols) k32_vfactors(DTopo tp, DGeom<float> g
                 const int nz = lev0 + k;
                 float oa = 0.f, oc = 0.f, oi = 0.f, ocp = 0.f;
                 if (nz >= nzmin && nz <= nzmax - 1) {
-                    if (nz == nzmin) hcur = (double)s_hn[tid][k];
-                    const double hnext = nz < nzmax - 1 ? (double)s_hn[tid][k + 1] : 0.0;
-                    const double avz = (double)s_av[tid][k];
-                    const double a = nz > nzmin ? -((double)s_kv[tid][k] * zinv1 * dt * ((double)s_ar[tid][k] / avz)) : 0.0;
-                    double c = 0.0, zinv2 = 0.0;
+                    if (nz == nzmin) hcur = s_hn[tid][k];
+                    const float hnext = nz < nzmax - 1 ? s_hn[tid][k + 1] : 0.f;
+                    const float ravz = 1.f / s_av[tid][k];
+                    const float a = nz > nzmin ? -(s_kv[tid][k] * zinv1 * dtf * (s_ar[tid][k] * ravz)) : 0.f;
+                    float c = 0.f, zinv2 = 0.f;
                     if (nz < nzmax - 1) {
-                        zinv2 = 2.0 / (hcur + hnext);
-                        c = -((double)s_kv[tid][k + 1] * zinv2 * dt * (double)s_ar[tid][k + 1] / avz);
+                        zinv2 = 2.f / (hcur + hnext);
+                        c = -(s_kv[tid][k + 1] * zinv2 * dtf * s_ar[tid][k + 1] * ravz);
                     }
-                    const double b = -a - c + hcur;
-                    const double inv = 1.0 / (b - cp * a);
-                    cp = c * inv;
-                    oa = (float)a;
-                    oc = (float)c;
-                    oi = (float)inv;
+                    // pivot recurrence in FP64 on the FP32-rounded coefficients; 1/m from an FP32
+                    // reciprocal and one Newton-Raphson step r = r0 (2 - m r0)
+                    const double ad = (double)a;
+                    const double m = ((double)(-a - c) + (double)hcur) - cp * ad;
+                    const double r0 = (double)__frcp_rn((float)m);
+                    const double r = r0 * (2.0 - m * r0);
+                    cp = (double)c * r;
+                    oa = a;
+                    oc = c;
+                    oi = (float)r;
                     ocp = (float)cp;
                     zinv1 = zinv2;
                     hcur = hnext;
@@ -682,9 +690,9 @@ __device__ __forceinline__ void scan_down(float &A, float &B, int lane) {
 // affine maps over the lanes with the carry passed from chunk to chunk.  Every load of a
 // chunk is issued before any of its arithmetic; the column's factors sit in shared memory.
 template <int KD>
-__device__ __forceinline__ void update_node(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
-                                            const B32View &B, float dt, int n, int lane, const WEdges &S,
-                                            const float4 *__restrict__ fac) {
+__device__ __forceinline__ void update_node(const DTopo &tp, const DForcing<float> &f, const B32View &B, int n,
+                                            int lane, const WEdges &S, const float4 *__restrict__ fac,
+                                            const float *__restrict__ sdtv) {
     using C = Chunk<1, 1>;
     const int L1 = tp.L1, nl = tp.nl;
     const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
@@ -714,7 +722,7 @@ __device__ __forceinline__ void update_node(const DTopo &tp, const DGeom<float> 
             float f0 = k.lvl ? ADv[iv] : 0.f;
             const float2 r0 = lf ? R[i] : make_float2(1.f, 1.f);
             const float2 tb = lf ? TB[i] : make_float2(0.f, 0.f);
-            const float sdt = k.lvl ? dt / (g.areasvol[iv] * g.hnode_new[i]) : 0.f;
+            const float sdt = k.lvl ? sdtv[nz] : 0.f;
             float x[KD];
             float2 rm[KD];
             unsigned okm = 0;
@@ -813,7 +821,8 @@ template <bool WIDE>
 __global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_UPDATE)
 k32_update(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, VFactors vf, float dt) {
     __shared__ WEdges Se[kWB];
-    extern __shared__ __align__(16) float4 fac_sm[];  // kWB columns of (a, c, 1/m, c/m), 1-based levels
+    // kWB columns of (a, c, 1/m, c/m), then kWB columns of dt / (areasvol hnode_new); 1-based levels
+    extern __shared__ __align__(16) float4 fac_sm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int n = warp_node<WIDE>(tp, warp);
     if (n < 0) return;
@@ -821,16 +830,18 @@ k32_update(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, VFactors vf, 
     stage_edges(tp, n, lane, S);
     if ((S.deg > 8) != WIDE) return;
     float4 *fac = fac_sm + (size_t)warp * (tp.L1 + 1);
-    if (B.ivd_mask) {
-        for (int nz = S.nzmin + lane; nz <= S.nzmax - 1; nz += 32) {
-            const int i = n * tp.L1 + nz - 1;
-            fac[nz] = make_float4(vf.a[i], vf.c[i], vf.inv[i], vf.cp[i]);
-        }
-        __syncwarp();
+    float *sdtv = reinterpret_cast<float *>(fac_sm + (size_t)kWB * (tp.L1 + 1)) + (size_t)warp * (tp.L1 + 1);
+    // the column's tracer-independent factors, once per node: dt / (areasvol hnode_new) and
+    // the implicit-diffusion factors
+    for (int nz = S.nzmin + lane; nz <= S.nzmax - 1; nz += 32) {
+        const int i = n * tp.L1 + nz - 1;
+        sdtv[nz] = dt / (g.areasvol[n * tp.nl + nz - 1] * g.hnode_new[i]);
+        if (B.ivd_mask) fac[nz] = make_float4(vf.a[i], vf.c[i], vf.inv[i], vf.cp[i]);
     }
-    if (WIDE) update_node<kMaxDeg>(tp, g, f, B, dt, n, lane, S, fac);
-    else if (S.deg <= 6) update_node<6>(tp, g, f, B, dt, n, lane, S, fac);
-    else update_node<8>(tp, g, f, B, dt, n, lane, S, fac);
+    __syncwarp();
+    if (WIDE) update_node<kMaxDeg>(tp, f, B, n, lane, S, fac, sdtv);
+    else if (S.deg <= 6) update_node<6>(tp, f, B, n, lane, S, fac, sdtv);
+    else update_node<8>(tp, f, B, n, lane, S, fac, sdtv);
 }
 
 // ---------------------------------------------------------------------------
@@ -873,7 +884,7 @@ void b32_bounds(const DTopo &tp, const DGeom<float> &g, const B32View &B, double
 }
 void b32_update(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B,
                 const VFactors &v, double dt, cudaStream_t s) {
-    const size_t sm = sizeof(float4) * (tp.L1 + 1) * kWB;
+    const size_t sm = (sizeof(float4) + sizeof(float)) * (tp.L1 + 1) * kWB;
     k32_update<false><<<grid_nodes(tp.N2), kTB, sm, s>>>(tp, g, f, B, v, (float)dt);
     if (tp.n_wide) k32_update<true><<<grid_nodes(tp.n_wide), kTB, sm, s>>>(tp, g, f, B, v, (float)dt);
 }
