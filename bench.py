@@ -55,6 +55,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--profile-only", action="store_true", help="one warm step + one profiled step (for ncu)")
+    p.add_argument("--no-tune", action="store_true", help="configuration 5: keep the generators' node order")
     return p.parse_args()
 
 
@@ -78,6 +79,12 @@ def algorithmic_bytes(counts, ntr, s):
     """FCT-minimal dataflow bytes per step: s*[Ntr*(18 N3 + 3 E3) + 3 T3 + 14 N3]."""
     N3, E3, T3 = counts["N3"], counts["E3"], counts["T3"]
     return s * (ntr * (18 * N3 + 3 * E3) + 3 * T3 + 14 * N3)
+
+
+# DRAM bytes (read + write) per tracer-DOF of each FP32 stage, measured with one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum) of `--profile-only --scale 0.25`; the traffic
+# of a full-size launch is this figure times the tracer-DOF it processes
+MEASURED_DRAM_B_PER_TRACER_DOF = {"update": 51.26, "bounds": 82.69, "edge_flux": 31.43, "lo_ad": 30.65}
 
 
 def stage_bytes(counts, ntr, s, ab=2, form="fp32"):
@@ -322,8 +329,12 @@ def run_ours(args, rank, world, local_rank):
     per_launch_bytes = sb[dom] / (agg[dom][1] / prof_steps)
     achieved = per_launch_bytes / (dom_ms / 1e3) / 1e9
     step_bytes = algorithmic_bytes(counts, ntr, 4)
+    traffic = None
+    if dom in MEASURED_DRAM_B_PER_TRACER_DOF:
+        traffic = MEASURED_DRAM_B_PER_TRACER_DOF[dom] * ntr * N3 / (agg[dom][1] / prof_steps)
     res["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                       "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_src,
+                       "frac": achieved / hbm_peak, "traffic": traffic, "traffic_unit": "B per launch",
+                       "algorithmic_bytes_per_launch": per_launch_bytes, "peak_source": peak_src,
                        "share": shares[dom] / tot,
                        "stage_ms_per_step": {k: v / prof_steps for k, v in shares.items()},
                        "step_algorithmic_bytes": step_bytes,
@@ -437,6 +448,119 @@ def run_ours(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def run_batch(args, rank, world, local_rank):
+    """Configuration 5: sixteen independent meshes of uneven size stepped together through
+    one multi-instance batch (one launch per stage over all of them); with several ranks
+    each rank takes its share of the instances (greedy packing of their work), no exchange."""
+    import torch
+    from fesom2_gb300 import batch as Bt
+    from fesom2_gb300 import gpu as G
+    torch.cuda.set_device(local_rank)
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+
+    def barrier():
+        if dist:
+            tdist.barrier()
+        torch.cuda.synchronize()
+
+    specs = Bt.instance_specs()
+    mine = Bt.partition([s.nodes_target * s.layers * s.tracers for s in specs], world)[rank]
+    stream = torch.cuda.Stream()
+    t_gen = time.time()
+    ctxs, info, init_state = [], [], []
+    for i in mine:
+        sp = specs[i]
+        mesh, kind, forcing, tracers = Bt.make_instance(sp, node_scale=args.scale)
+        cfgs = Bt.scheme_configs(sp.tracers, G.tra_cfg, sp.seed)
+        name, order, tune_ms = ("morton", None, {})
+        if not args.no_tune:
+            name, order, tune_ms = Bt.autotune_order(mesh, forcing, tracers, cfgs, stream=stream)
+        if name != "morton":
+            mesh = Bt.permute_nodes(mesh, order)
+            forcing = Bt.permute_forcing(forcing, order)
+            tracers = np.ascontiguousarray(tracers[:, order])
+        f32 = M.Forcing(uv=forcing.uv.astype(np.float32), w=forcing.w.astype(np.float32),
+                        w_e=forcing.w_e.astype(np.float32), w_i=forcing.w_i.astype(np.float32),
+                        Kv=forcing.Kv.astype(np.float32), bc_surface=None, dt=forcing.dt)
+        ctx = G.Context(mesh, G.PREC_FP32, max_tracers=sp.tracers)
+        ctx.set_stream(stream.cuda_stream)
+        ctx.state_setup(cfgs)
+        ctx.forcing_upload(f32)
+        for k in range(sp.tracers):
+            ctx.tracer_upload(k, tracers[k], tracers[k])
+        ctxs.append(ctx)
+        init_state.append((mesh, forcing, tracers))
+        c = mesh.counts()
+        info.append({"instance": i, "kind": sp.kind, "nodes": c["N2"], "layers": mesh.nl - 1, "tracers": sp.tracers,
+                     "N3": c["N3"], "order": name, "tune_ms_per_step": tune_ms})
+    gen_s = time.time() - t_gen
+    b = G.Batch(ctxs)
+    b.set_stream(stream.cuda_stream)
+    dt = 600.0
+    units_step = sum(x["N3"] * x["tracers"] for x in info)
+    # one batched step from the initial state: error of tracers 0 and 1 against the FP64 oracle
+    errs = {}
+    if not args.no_cpu:
+        b.run_steps(dt, 1, use_graph=False)
+        torch.cuda.synchronize()
+        from oracle import oracle as O
+        for ctx, x, (mesh, forcing, tracers) in zip(ctxs, info, init_state):
+            om = O.OracleMesh(mesh)
+            fo = O.ensure_f64(forcing)
+            lev = np.arange(mesh.nl - 1)[None, :]
+            wet = (lev >= (mesh.ulevels_nod2D - 1)[:, None]) & (lev < (mesh.nlevels_nod2D - 1)[:, None])
+            e = []
+            for k in range(min(2, x["tracers"])):
+                got = ctx.tracer_download(k, dtype=np.float32)[0]
+                T64 = tracers[k].astype(np.float64)
+                om.tracer_step(fo, O.cfg_struct(), T64, np.zeros_like(T64), T64.copy())
+                e.append(float(np.abs(got[wet].astype(np.float64) - T64[wet]).max() / np.abs(T64[wet]).max()))
+            errs[str(x["instance"])] = e
+            for k in range(x["tracers"]):
+                ctx.tracer_upload(k, tracers[k], tracers[k])
+        torch.cuda.synchronize()
+    b.run_steps(dt, args.warmup, use_graph=True)
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        barrier()
+        ev0.record(stream)
+        b.run_steps(dt, args.steps, use_graph=True)
+        ev1.record(stream)
+        barrier()
+    ms = ev0.elapsed_time(ev1)
+    st = [c.status() for c in ctxs]
+    units = torch.tensor([float(units_step * args.steps)], dtype=torch.float64, device="cuda")
+    ms_t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if dist:
+        tdist.all_reduce(units, op=tdist.ReduceOp.SUM)
+        tdist.all_reduce(ms_t, op=tdist.ReduceOp.MAX)
+        gathered = [None] * world
+        tdist.all_gather_object(gathered, {"info": info, "errs": errs})
+    else:
+        gathered = [{"info": info, "errs": errs}]
+    if rank == 0:
+        all_info = [x for g in gathered for x in g["info"]]
+        all_errs = {k: v for g in gathered for k, v in g["errs"].items()}
+        ms_max = float(ms_t.item())
+        line = {"metric": METRIC, "value": float(units.item()) / (ms_max / 1e3), "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "16 independent channel/sphere meshes, 20k-800k nodes (log-uniform), "
+                                       "20-80 layers, 2-24 tracers each, one launch per stage over all of them",
+                           "cfg": 5, "instances": sorted(all_info, key=lambda x: x["instance"]),
+                           "parallelism": f"instances split over {world} ranks" if world > 1 else "single GPU",
+                           "l2": "inputs larger than L2 (no flush)", "mesh_generation_and_tuning_s": gen_s},
+                "gpu_launches": b.launches_per_step() * args.steps, "clocks": clk.summary(),
+                "status_words": st, "error_vs_fp64_oracle_one_step": all_errs}
+        print(json.dumps(line), flush=True)
+    b.close()
+    for c in ctxs:
+        c.close()
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -450,7 +574,10 @@ def main():
         import torch.distributed as tdist
         torch.cuda.set_device(local_rank)
         tdist.init_process_group("nccl")
-    run_ours(args, rank, world, local_rank)
+    if args.config == 5:
+        run_batch(args, rank, world, local_rank)
+    else:
+        run_ours(args, rank, world, local_rank)
     if world > 1:
         import torch.distributed as tdist
         tdist.destroy_process_group()

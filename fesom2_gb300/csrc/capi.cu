@@ -1341,4 +1341,205 @@ int fesom_gpu_tracer_device_ptr(fesom_gpu_ctx *ctx, int32_t tr, void **values, v
     return FESOM_OK;
 }
 
+// ---------------------------------------------------------------------------
+// multi-instance batch of the FP32 form (no counterpart in the reference, which runs
+// one mesh per process)
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+struct fesom_gpu_batch {
+    std::vector<fesom_gpu_ctx *> inst;
+    int ab = 2, phase = 0;
+    cudaStream_t stream = nullptr;
+    Inst32 *d_inst = nullptr;  // ab descriptor sets (one per rotation phase), inst.size() each
+    double d_dt = -1.0;
+    MultiIdx ix_e{}, ix_vfb{}, ix_n{}, ix_w{}, ix_it{};
+    int maxL1 = 0;
+    bool any_vd = false, any_fct = false;
+    cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};
+    double g_dt[3] = {0.0, 0.0, 0.0};
+    std::string err;
+};
+
+namespace {
+
+#define BCK(call)                                                                                 \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) {                                                                  \
+            b->err = std::string(#call) + ": " + cudaGetErrorString(e_);                          \
+            return FESOM_ERR_CUDA;                                                                \
+        }                                                                                         \
+    } while (0)
+
+void set_prefix(MultiIdx &ix, const std::vector<int> &count) {
+    ix.n = (int)count.size();
+    ix.start[0] = 0;
+    for (int i = 0; i < ix.n; i++) ix.start[i + 1] = ix.start[i] + count[i];
+}
+
+// descriptors of every instance for each rotation phase, for time step dt
+int batch_descriptors(fesom_gpu_batch *b, double dt) {
+    const int n = (int)b->inst.size();
+    std::vector<Inst32> h((size_t)n * b->ab);
+    for (int p = 0; p < b->ab; p++)
+        for (int i = 0; i < n; i++) {
+            fesom_gpu_ctx *c = b->inst[i];
+            const int keep = c->rot;
+            for (int k = 0; k < p; k++) rotate32(c);
+            Inst32 &d = h[(size_t)p * n + i];
+            d.tp = c->tp;
+            d.g = c->g32;
+            d.f = forcing_view<float>(c, 0);
+            d.B = view32(c, 0, c->ntr);
+            d.mw = c->mw;
+            d.VF = c->VF;
+            d.vf = c->vfac;
+            d.dt = (float)dt;
+            d.dtd = dt;
+            c->rot = keep;
+        }
+    BCK(cudaMemcpy(b->d_inst, h.data(), sizeof(Inst32) * h.size(), cudaMemcpyHostToDevice));
+    b->d_dt = dt;
+    return FESOM_OK;
+}
+
+void enqueue_batch_step(fesom_gpu_batch *b, cudaStream_t s) {
+    const Inst32 *I = b->d_inst + (size_t)b->phase * b->inst.size();
+    const bool wide = b->ix_w.start[b->ix_w.n] > 0;
+    bm32_vflux(I, b->ix_e, s);
+    if (b->any_vd) bm32_vfactors(I, b->ix_vfb, s);
+    bm32_lo_ad(I, b->ix_n, false, s);
+    if (wide) bm32_lo_ad(I, b->ix_w, true, s);
+    bm32_ho(I, b->ix_e, b->ix_it, s);
+    if (b->any_fct) {
+        bm32_bounds(I, b->ix_n, false, s);
+        if (wide) bm32_bounds(I, b->ix_w, true, s);
+    }
+    bm32_update(I, b->ix_n, false, b->maxL1, s);
+    if (wide) bm32_update(I, b->ix_w, true, b->maxL1, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+int fesom_gpu_batch_create(fesom_gpu_ctx *const *ctxs, int32_t n, fesom_gpu_batch **out) {
+    if (!out) return FESOM_ERR_ARG;
+    *out = nullptr;
+    fesom_gpu_batch *b = new fesom_gpu_batch();
+    *out = b;
+    if (!ctxs || n < 1 || n > kMaxInst) {
+        b->err = "a batch holds 1 to 64 FP32 contexts";
+        return FESOM_ERR_ARG;
+    }
+    std::vector<int> ce, cvb, cn, cw, cit;
+    for (int i = 0; i < n; i++) {
+        fesom_gpu_ctx *c = ctxs[i];
+        if (!c || c->prec != FESOM_PREC_FP32) { b->err = "batch instances must be FP32 contexts"; return FESOM_ERR_ARG; }
+        if (!c->state_ready || !c->forcing_ready) {
+            b->err = "every batch instance needs its tracer state and forcing set up";
+            return FESOM_ERR_STATE;
+        }
+        if (c->group != c->ntr) {
+            b->err = "every batch instance must hold all its tracers in one launch group";
+            return FESOM_ERR_STATE;
+        }
+        if (i > 0 && c->ab_max != b->ab) { b->err = "batch instances must share one Adams-Bashforth order"; return FESOM_ERR_ARG; }
+        b->ab = c->ab_max;
+        for (int t = 0; t < c->ntr; t++) {
+            b->any_vd |= c->cfgs[t].i_vert_diff != 0;
+            b->any_fct |= c->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
+        }
+        b->maxL1 = std::max(b->maxL1, c->L1);
+        b->inst.push_back(c);
+        ce.push_back(c->E2);
+        cvb.push_back((c->N2 + kVfCols - 1) / kVfCols);
+        cn.push_back(c->N2);
+        cw.push_back(c->tp.n_wide);
+        cit.push_back(c->mw.n_items);
+    }
+    set_prefix(b->ix_e, ce);
+    set_prefix(b->ix_vfb, cvb);
+    set_prefix(b->ix_n, cn);
+    set_prefix(b->ix_w, cw);
+    set_prefix(b->ix_it, cit);
+    BCK(cudaMalloc((void **)&b->d_inst, sizeof(Inst32) * (size_t)n * b->ab));
+    return FESOM_OK;
+}
+
+int fesom_gpu_batch_set_stream(fesom_gpu_batch *b, void *stream) {
+    if (!b) return FESOM_ERR_ARG;
+    b->stream = (cudaStream_t)stream;
+    for (auto &g : b->gexec)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    return FESOM_OK;
+}
+
+int fesom_gpu_batch_run_steps(fesom_gpu_batch *b, double dt, int32_t nsteps, int32_t use_graph) {
+    if (!b || nsteps < 0) return FESOM_ERR_ARG;
+    int rc;
+    if (b->d_dt != dt) {
+        BCK(cudaStreamSynchronize(b->stream));
+        if ((rc = batch_descriptors(b, dt))) return rc;
+    }
+    for (int s = 0; s < nsteps; s++) {
+        if (!use_graph) {
+            enqueue_batch_step(b, b->stream);
+            BCK(cudaGetLastError());
+        } else {
+            const int p = b->phase;
+            if (!b->gexec[p] || b->g_dt[p] != dt) {
+                if (b->gexec[p]) { cudaGraphExecDestroy(b->gexec[p]); b->gexec[p] = nullptr; }
+                cudaStream_t cap = b->stream;
+                bool own = false;
+                if (!cap) {  // the legacy stream cannot be captured: capture on a private stream
+                    BCK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+                    own = true;
+                }
+                cudaGraph_t graph;
+                cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+                if (e == cudaSuccess) {
+                    enqueue_batch_step(b, cap);
+                    e = cudaStreamEndCapture(cap, &graph);
+                }
+                if (own) cudaStreamDestroy(cap);
+                if (e != cudaSuccess) { b->err = std::string("graph capture: ") + cudaGetErrorString(e); return FESOM_ERR_CUDA; }
+                e = cudaGraphInstantiate(&b->gexec[p], graph, 0);
+                cudaGraphDestroy(graph);
+                if (e != cudaSuccess) { b->err = std::string("graph instantiate: ") + cudaGetErrorString(e); return FESOM_ERR_CUDA; }
+                b->g_dt[p] = dt;
+            }
+            BCK(cudaGraphLaunch(b->gexec[p], b->stream));
+        }
+        b->phase = (b->phase + 1) % b->ab;
+        for (fesom_gpu_ctx *c : b->inst) {
+            rotate32(c);
+            // a context's own graphs were captured for its own rotation: its next
+            // single-context step picks the graph of the new rotation
+        }
+    }
+    return FESOM_OK;
+}
+
+int fesom_gpu_batch_launches_per_step(fesom_gpu_batch *b, int32_t *launches) {
+    if (!b || !launches) return FESOM_ERR_ARG;
+    const bool wide = b->ix_w.start[b->ix_w.n] > 0;
+    const int k = wide ? 2 : 1;
+    int n = 1 + (b->any_vd ? 1 : 0) + k * (2 + (b->any_fct ? 1 : 0)) + 1 + (b->ix_it.start[b->ix_it.n] ? 1 : 0);
+    *launches = n;
+    return FESOM_OK;
+}
+
+const char *fesom_gpu_batch_last_error(const fesom_gpu_batch *b) { return b ? b->err.c_str() : "null batch"; }
+
+int fesom_gpu_batch_destroy(fesom_gpu_batch *b) {
+    if (!b) return FESOM_OK;
+    for (auto &g : b->gexec)
+        if (g) cudaGraphExecDestroy(g);
+    if (b->d_inst) cudaFree(b->d_inst);
+    delete b;
+    return FESOM_OK;
+}
+
 }  // extern "C"

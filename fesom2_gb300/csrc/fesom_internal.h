@@ -133,6 +133,32 @@ void b32_bounds(const DTopo &, const DGeom<float> &, const B32View &, double dt,
 void b32_update(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, const VFactors &,
                 double dt, cudaStream_t);
 
+// Multi-instance batch of the FP32 form: one descriptor per instance (device memory) and,
+// per stage, the offsets of each instance's units in the launch
+struct Inst32 {
+    DTopo tp;
+    DGeom<float> g;
+    DForcing<float> f;
+    B32View B;
+    MusclW mw;
+    float *VF;
+    VFactors vf;
+    float dt;
+    double dtd;
+};
+constexpr int kMaxInst = 64;
+constexpr int kVfCols = 128;  // columns per block of the diffusion-factor kernel
+struct MultiIdx {
+    int n;
+    int start[kMaxInst + 1];
+};
+void bm32_vflux(const Inst32 *, const MultiIdx &, cudaStream_t);
+void bm32_vfactors(const Inst32 *, const MultiIdx &, cudaStream_t);
+void bm32_lo_ad(const Inst32 *, const MultiIdx &, bool wide, cudaStream_t);
+void bm32_ho(const Inst32 *, const MultiIdx &edges, const MultiIdx &items, cudaStream_t);
+void bm32_bounds(const Inst32 *, const MultiIdx &, bool wide, cudaStream_t);
+void bm32_update(const Inst32 *, const MultiIdx &, bool wide, int maxL1, cudaStream_t);
+
 // launch wrappers (kernels_fp64.cu / kernels_fp32.cu)
 template <typename R>
 struct Launch {

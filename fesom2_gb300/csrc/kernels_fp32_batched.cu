@@ -73,10 +73,10 @@ __device__ __forceinline__ size_t i1(int nz, int n, int L1) { return (size_t)n *
 // ---------------------------------------------------------------------------
 // k32_vflux: volume flux of every edge-layer (shared by all tracers)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kTB) k32_vflux(DTopo tp, DGeom<float> g, DForcing<float> f, float *VF) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+__device__ __forceinline__ void vflux_edge(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, float *VF,
+                                           int e, int lane) {
     const int L1 = tp.L1;
-    for (int e = blockIdx.x * kWB + warp; e < tp.E2; e += gridDim.x * kWB) {
+    {
         const int el1 = tp.e_t1[e], el2 = tp.e_t2[e];
         const int nl1 = tp.t_nlev[el1] - 1, nu1 = tp.t_ulev[el1];
         int nl2 = 0, nu2 = 0;
@@ -110,6 +110,11 @@ __global__ void __launch_bounds__(kTB) k32_vflux(DTopo tp, DGeom<float> g, DForc
     }
 }
 
+__global__ void __launch_bounds__(kTB) k32_vflux(DTopo tp, DGeom<float> g, DForcing<float> f, float *VF) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int e = blockIdx.x * kWB + warp; e < tp.E2; e += gridDim.x * kWB) vflux_edge(tp, g, f, VF, e, lane);
+}
+
 // ---------------------------------------------------------------------------
 // k32_vfactors: FP64 factorisation of each column's tridiagonal system
 // ---------------------------------------------------------------------------
@@ -123,10 +128,9 @@ __global__ void __launch_bounds__(kTB) k32_vflux(DTopo tp, DGeom<float> g, DForc
 // memory in tiles of kVfK levels, loaded and stored with the lanes over the levels of a
 // column (each column's tile is one contiguous run), so no thread walks its own column
 // through the cache.
-constexpr int kVfCols = 128;  // columns per block
 constexpr int kVfK = 8;       // levels per tile
-__global__ void __launch_bounds__(kVfCols) k32_vfactors(DTopo tp, DGeom<float> g, DForcing<float> f, double dt,
-                                                        VFactors vf) {
+__device__ __forceinline__ void vfactors_block(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
+                                               double dt, const VFactors &vf, int blk) {
     // inputs for levels lev0 .. lev0 + kVfK (one extra: the next level's h, Kv, area);
     // outputs for levels lev0 .. lev0 + kVfK - 1
     __shared__ float s_hn[kVfCols][kVfK + 1], s_ar[kVfCols][kVfK + 1], s_av[kVfCols][kVfK + 1],
@@ -134,7 +138,7 @@ __global__ void __launch_bounds__(kVfCols) k32_vfactors(DTopo tp, DGeom<float> g
     __shared__ float s_a[kVfCols][kVfK], s_c[kVfCols][kVfK], s_i[kVfCols][kVfK], s_p[kVfCols][kVfK];
     __shared__ int s_lmax;
     const int L1 = tp.L1, nl = tp.nl;
-    const int c0 = blockIdx.x * kVfCols, tid = threadIdx.x;
+    const int c0 = blk * kVfCols, tid = threadIdx.x;
     const int ncol = min(kVfCols, tp.N2 - c0);
     const int n = c0 + tid;
     const bool mine = tid < ncol;
@@ -223,6 +227,11 @@ __global__ void __launch_bounds__(kVfCols) k32_vfactors(DTopo tp, DGeom<float> g
         }
         __syncthreads();
     }
+}
+
+__global__ void __launch_bounds__(kVfCols) k32_vfactors(DTopo tp, DGeom<float> g, DForcing<float> f, double dt,
+                                                        VFactors vf) {
+    vfactors_block(tp, g, f, dt, vf, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -409,20 +418,18 @@ __device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &
     }
 }
 
-// the node of a warp: consecutive nodes, or (WIDE) the listed nodes of more than 8 edges
+// the node of warp unit j: consecutive nodes, or (WIDE) the listed nodes of more than 8 edges
 template <bool WIDE>
-__device__ __forceinline__ int warp_node(const DTopo &tp, int warp) {
-    const int j = blockIdx.x * kWB + warp;
+__device__ __forceinline__ int unit_node(const DTopo &tp, int j) {
     if (WIDE) return j < tp.n_wide ? tp.wide_nodes[j] : -1;
     return j < tp.N2 ? j : -1;
 }
 
 template <bool WIDE>
-__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_LO)
-k32_lo_ad(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, const float *__restrict__ VF, float dt) {
-    __shared__ WEdges Se[kWB];
+__device__ __forceinline__ void lo_ad_unit(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
+                                           const B32View &B, const float *__restrict__ VF, float dt, int j, WEdges *Se) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int n = warp_node<WIDE>(tp, warp);
+    const int n = unit_node<WIDE>(tp, j);
     if (n < 0) return;
     WEdges &S = Se[warp];
     stage_edges(tp, n, lane, S);
@@ -430,6 +437,13 @@ k32_lo_ad(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, const float *_
     if (WIDE) lo_ad_node<kMaxDeg>(tp, g, f, B, VF, dt, n, lane, S);
     else if (S.deg <= 6) lo_ad_node<6>(tp, g, f, B, VF, dt, n, lane, S);
     else lo_ad_node<8>(tp, g, f, B, VF, dt, n, lane, S);
+}
+
+template <bool WIDE>
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_LO)
+k32_lo_ad(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, const float *__restrict__ VF, float dt) {
+    __shared__ WEdges Se[kWB];
+    lo_ad_unit<WIDE>(tp, g, f, B, VF, dt, blockIdx.x * kWB + (threadIdx.x >> 5), Se);
 }
 
 // high-order minus low-order flux of one edge-layer from the two end values, their
@@ -469,10 +483,9 @@ __device__ __forceinline__ float ho_minus_lo(int hor, float ph, int ab, float T1
 // at the levels where every element around both nodes is wet, [gzmin, gzmax); the
 // other edge-layers (under one percent of an ocean mesh's) take the node means in
 // k32_ho_nodemean.
-__global__ void __launch_bounds__(kTB, FESOM_MINB_HO)
-k32_ho(DTopo tp, B32View B, MusclW mw, const float *__restrict__ VF) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int e = blockIdx.x * kWB + warp;
+__device__ __forceinline__ void ho_unit(const DTopo &tp, const B32View &B, const MusclW &mw,
+                                        const float *__restrict__ VF, int e) {
+    const int lane = threadIdx.x & 31;
     if (e >= tp.E2) return;
     const int L1 = tp.L1;
     const int n1 = tp.e_n1[e], n2 = tp.e_n2[e];
@@ -530,11 +543,17 @@ k32_ho(DTopo tp, B32View B, MusclW mw, const float *__restrict__ VF) {
     }
 }
 
+__global__ void __launch_bounds__(kTB, FESOM_MINB_HO)
+k32_ho(DTopo tp, B32View B, MusclW mw, const float *__restrict__ VF) {
+    ho_unit(tp, B, mw, VF, blockIdx.x * kWB + (threadIdx.x >> 5));
+}
+
 // The edge-layers of the node-mean gradients: one thread per (edge, level) item, every
 // tracer, with the projected mean gradients as precomputed neighbour weights.
-__global__ void __launch_bounds__(256) k32_ho_nodemean(DTopo tp, B32View B, MusclW mw, const float *__restrict__ VF) {
+__device__ __forceinline__ void nodemean_item(const DTopo &tp, const B32View &B, const MusclW &mw,
+                                              const float *__restrict__ VF, int j) {
     const int L1 = tp.L1;
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < mw.n_items; j += gridDim.x * blockDim.x) {
+    {
         const int e = mw.it_e[j], nz = mw.it_nz[j];
         const int p0 = mw.it_ptr[j], p1 = p0 + mw.it_n1[j], p2 = mw.it_ptr[j + 1];
         const int n1 = tp.e_n1[e], n2 = tp.e_n2[e];
@@ -562,6 +581,11 @@ __global__ void __launch_bounds__(256) k32_ho_nodemean(DTopo tp, B32View B, Musc
             B.ADh[(size_t)t * B.sE + ie] = ho_minus_lo(hor, B.ph[t], B.ab, T1, T2, o1a, o1b, o2a, o2b, s1, s2, v, cl1, cl2);
         }
     }
+}
+
+__global__ void __launch_bounds__(256) k32_ho_nodemean(DTopo tp, B32View B, MusclW mw, const float *__restrict__ VF) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < mw.n_items; j += gridDim.x * blockDim.x)
+        nodemean_item(tp, B, mw, VF, j);
 }
 
 // ---------------------------------------------------------------------------
@@ -645,10 +669,10 @@ __device__ __forceinline__ void bounds_node(const DTopo &tp, const DGeom<float> 
 }
 
 template <bool WIDE>
-__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_BOUNDS) k32_bounds(DTopo tp, DGeom<float> g, B32View B, float dt) {
-    __shared__ WEdges Se[kWB];
+__device__ __forceinline__ void bounds_unit(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int j,
+                                            WEdges *Se) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int n = warp_node<WIDE>(tp, warp);
+    const int n = unit_node<WIDE>(tp, j);
     if (n < 0) return;
     WEdges &S = Se[warp];
     stage_edges(tp, n, lane, S);
@@ -656,6 +680,12 @@ __global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_BOUNDS) k32_bounds(
     if (WIDE) bounds_node<kMaxDeg>(tp, g, B, dt, n, lane, S);
     else if (S.deg <= 6) bounds_node<6>(tp, g, B, dt, n, lane, S);
     else bounds_node<8>(tp, g, B, dt, n, lane, S);
+}
+
+template <bool WIDE>
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_BOUNDS) k32_bounds(DTopo tp, DGeom<float> g, B32View B, float dt) {
+    __shared__ WEdges Se[kWB];
+    bounds_unit<WIDE>(tp, g, B, dt, blockIdx.x * kWB + (threadIdx.x >> 5), Se);
 }
 
 // ---------------------------------------------------------------------------
@@ -817,20 +847,20 @@ __device__ __forceinline__ void update_node(const DTopo &tp, const DForcing<floa
     }
 }
 
+// fac_sm: kWB columns of (a, c, 1/m, c/m), then kWB columns of dt / (areasvol hnode_new),
+// colstride entries each (1-based levels)
 template <bool WIDE>
-__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_UPDATE)
-k32_update(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, VFactors vf, float dt) {
-    __shared__ WEdges Se[kWB];
-    // kWB columns of (a, c, 1/m, c/m), then kWB columns of dt / (areasvol hnode_new); 1-based levels
-    extern __shared__ __align__(16) float4 fac_sm[];
+__device__ __forceinline__ void update_unit(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
+                                            const B32View &B, const VFactors &vf, float dt, int j, WEdges *Se,
+                                            float4 *fac_sm, int colstride) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int n = warp_node<WIDE>(tp, warp);
+    const int n = unit_node<WIDE>(tp, j);
     if (n < 0) return;
     WEdges &S = Se[warp];
     stage_edges(tp, n, lane, S);
     if ((S.deg > 8) != WIDE) return;
-    float4 *fac = fac_sm + (size_t)warp * (tp.L1 + 1);
-    float *sdtv = reinterpret_cast<float *>(fac_sm + (size_t)kWB * (tp.L1 + 1)) + (size_t)warp * (tp.L1 + 1);
+    float4 *fac = fac_sm + (size_t)warp * colstride;
+    float *sdtv = reinterpret_cast<float *>(fac_sm + (size_t)kWB * colstride) + (size_t)warp * colstride;
     // the column's tracer-independent factors, once per node: dt / (areasvol hnode_new) and
     // the implicit-diffusion factors
     for (int nz = S.nzmin + lane; nz <= S.nzmax - 1; nz += 32) {
@@ -842,6 +872,81 @@ k32_update(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, VFactors vf, 
     if (WIDE) update_node<kMaxDeg>(tp, f, B, n, lane, S, fac, sdtv);
     else if (S.deg <= 6) update_node<6>(tp, f, B, n, lane, S, fac, sdtv);
     else update_node<8>(tp, f, B, n, lane, S, fac, sdtv);
+}
+
+template <bool WIDE>
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_UPDATE)
+k32_update(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, VFactors vf, float dt) {
+    __shared__ WEdges Se[kWB];
+    extern __shared__ __align__(16) float4 fac_sm[];
+    update_unit<WIDE>(tp, g, f, B, vf, dt, blockIdx.x * kWB + (threadIdx.x >> 5), Se, fac_sm, tp.L1 + 1);
+}
+
+// ---------------------------------------------------------------------------
+// multi-instance launches: every stage over all instances of a batch at once
+// ---------------------------------------------------------------------------
+// Units (edges, column blocks, nodes, items) of all instances are numbered one after
+// another; ix.start[i] is instance i's first unit.  A warp (or thread, or block) finds
+// its instance by binary search over those offsets (kernel parameters, warp-uniform)
+// and runs the single-instance body with that instance's descriptor.
+__device__ __forceinline__ int find_inst(const MultiIdx &ix, int u) {
+    int lo = 0, hi = ix.n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (ix.start[mid] <= u) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(kTB) k32m_vflux(const Inst32 *__restrict__ I, MultiIdx ix) {
+    const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
+    if (u >= ix.start[ix.n]) return;
+    const int i = find_inst(ix, u);
+    vflux_edge(I[i].tp, I[i].g, I[i].f, I[i].VF, u - ix.start[i], threadIdx.x & 31);
+}
+__global__ void __launch_bounds__(kVfCols) k32m_vfactors(const Inst32 *__restrict__ I, MultiIdx ix) {
+    const int u = blockIdx.x;
+    const int i = find_inst(ix, u);
+    vfactors_block(I[i].tp, I[i].g, I[i].f, I[i].dtd, I[i].vf, u - ix.start[i]);
+}
+template <bool WIDE>
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_LO) k32m_lo_ad(const Inst32 *__restrict__ I, MultiIdx ix) {
+    __shared__ WEdges Se[kWB];
+    const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
+    if (u >= ix.start[ix.n]) return;
+    const int i = find_inst(ix, u);
+    lo_ad_unit<WIDE>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].VF, I[i].dt, u - ix.start[i], Se);
+}
+__global__ void __launch_bounds__(kTB, FESOM_MINB_HO) k32m_ho(const Inst32 *__restrict__ I, MultiIdx ix) {
+    const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
+    if (u >= ix.start[ix.n]) return;
+    const int i = find_inst(ix, u);
+    ho_unit(I[i].tp, I[i].B, I[i].mw, I[i].VF, u - ix.start[i]);
+}
+__global__ void __launch_bounds__(256) k32m_ho_nodemean(const Inst32 *__restrict__ I, MultiIdx ix) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= ix.start[ix.n]) return;
+    const int i = find_inst(ix, u);
+    nodemean_item(I[i].tp, I[i].B, I[i].mw, I[i].VF, u - ix.start[i]);
+}
+template <bool WIDE>
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_BOUNDS) k32m_bounds(const Inst32 *__restrict__ I, MultiIdx ix) {
+    __shared__ WEdges Se[kWB];
+    const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
+    if (u >= ix.start[ix.n]) return;
+    const int i = find_inst(ix, u);
+    bounds_unit<WIDE>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
+}
+template <bool WIDE>
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_UPDATE)
+k32m_update(const Inst32 *__restrict__ I, MultiIdx ix, int colstride) {
+    __shared__ WEdges Se[kWB];
+    extern __shared__ __align__(16) float4 fac_sm[];
+    const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
+    if (u >= ix.start[ix.n]) return;
+    const int i = find_inst(ix, u);
+    update_unit<WIDE>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].vf, I[i].dt, u - ix.start[i], Se, fac_sm, colstride);
 }
 
 // ---------------------------------------------------------------------------
@@ -887,6 +992,40 @@ void b32_update(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f
     const size_t sm = (sizeof(float4) + sizeof(float)) * (tp.L1 + 1) * kWB;
     k32_update<false><<<grid_nodes(tp.N2), kTB, sm, s>>>(tp, g, f, B, v, (float)dt);
     if (tp.n_wide) k32_update<true><<<grid_nodes(tp.n_wide), kTB, sm, s>>>(tp, g, f, B, v, (float)dt);
+}
+
+// multi-instance launch wrappers: ix_* hold the per-instance unit offsets of each stage
+void bm32_vflux(const Inst32 *I, const MultiIdx &ix, cudaStream_t s) {
+    const int u = ix.start[ix.n];
+    if (u) k32m_vflux<<<grid_nodes(u), kTB, 0, s>>>(I, ix);
+}
+void bm32_vfactors(const Inst32 *I, const MultiIdx &ix, cudaStream_t s) {
+    const int u = ix.start[ix.n];
+    if (u) k32m_vfactors<<<u, kVfCols, 0, s>>>(I, ix);
+}
+void bm32_lo_ad(const Inst32 *I, const MultiIdx &ix, bool wide, cudaStream_t s) {
+    const int u = ix.start[ix.n];
+    if (!u) return;
+    if (wide) k32m_lo_ad<true><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
+    else k32m_lo_ad<false><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
+}
+void bm32_ho(const Inst32 *I, const MultiIdx &ix_e, const MultiIdx &ix_items, cudaStream_t s) {
+    if (ix_e.start[ix_e.n]) k32m_ho<<<grid_nodes(ix_e.start[ix_e.n]), kTB, 0, s>>>(I, ix_e);
+    const int u = ix_items.start[ix_items.n];
+    if (u) k32m_ho_nodemean<<<(u + 255) / 256, 256, 0, s>>>(I, ix_items);
+}
+void bm32_bounds(const Inst32 *I, const MultiIdx &ix, bool wide, cudaStream_t s) {
+    const int u = ix.start[ix.n];
+    if (!u) return;
+    if (wide) k32m_bounds<true><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
+    else k32m_bounds<false><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
+}
+void bm32_update(const Inst32 *I, const MultiIdx &ix, bool wide, int maxL1, cudaStream_t s) {
+    const int u = ix.start[ix.n];
+    if (!u) return;
+    const size_t sm = (sizeof(float4) + sizeof(float)) * (maxL1 + 1) * kWB;
+    if (wide) k32m_update<true><<<grid_nodes(u), kTB, sm, s>>>(I, ix, maxL1 + 1);
+    else k32m_update<false><<<grid_nodes(u), kTB, sm, s>>>(I, ix, maxL1 + 1);
 }
 
 }  // namespace fesom

@@ -87,6 +87,12 @@ _SIGS = {
     "fesom_gpu_launches_per_step": ([_P, C.POINTER(C.c_int32)], C.c_int),
     "fesom_gpu_debug_fetch": ([_P, C.c_char_p, C.c_int32, _P, C.c_size_t], C.c_int),
     "fesom_gpu_tracer_device_ptr": ([_P, C.c_int32, C.POINTER(_P), C.POINTER(_P)], C.c_int),
+    "fesom_gpu_batch_create": ([C.POINTER(_P), C.c_int32, C.POINTER(_P)], C.c_int),
+    "fesom_gpu_batch_set_stream": ([_P, _P], C.c_int),
+    "fesom_gpu_batch_run_steps": ([_P, C.c_double, C.c_int32, C.c_int32], C.c_int),
+    "fesom_gpu_batch_launches_per_step": ([_P, C.POINTER(C.c_int32)], C.c_int),
+    "fesom_gpu_batch_last_error": ([_P], C.c_char_p),
+    "fesom_gpu_batch_destroy": ([_P], C.c_int),
 }
 
 
@@ -337,3 +343,49 @@ class Context:
         out = np.zeros(self.ntr)
         self._chk(self.L.fesom_gpu_tracer_content(self.h, _p(out)))
         return out
+
+
+class Batch:
+    """``fesom_gpu_batch``: FP32 contexts stepped together, one launch per stage over all of
+    them (each context set up with ``state_setup`` and ``forcing_upload`` first)."""
+
+    def __init__(self, contexts):
+        L = load()
+        self.L = L
+        self.contexts = list(contexts)  # the batch points into them: keep them alive
+        arr = (_P * len(self.contexts))(*[c.h for c in self.contexts])
+        h = _P()
+        rc = L.fesom_gpu_batch_create(arr, len(self.contexts), C.byref(h))
+        self.h = h
+        if rc != 0:
+            msg = L.fesom_gpu_batch_last_error(h).decode() if h.value else "batch create failed"
+            L.fesom_gpu_batch_destroy(h)
+            self.h = _P()
+            raise FesomGpuError(rc, msg)
+
+    def _chk(self, rc: int):
+        if rc != 0:
+            raise FesomGpuError(rc, self.L.fesom_gpu_batch_last_error(self.h).decode())
+
+    def set_stream(self, stream: int):
+        self._chk(self.L.fesom_gpu_batch_set_stream(self.h, _P(stream)))
+
+    def run_steps(self, dt: float, nsteps: int, use_graph: bool = True):
+        self._chk(self.L.fesom_gpu_batch_run_steps(self.h, float(dt), int(nsteps), 1 if use_graph else 0))
+
+    def launches_per_step(self) -> int:
+        n = C.c_int32(0)
+        self._chk(self.L.fesom_gpu_batch_launches_per_step(self.h, C.byref(n)))
+        return int(n.value)
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.fesom_gpu_batch_destroy(self.h)
+            self.h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+

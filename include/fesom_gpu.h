@@ -241,6 +241,25 @@ int fesom_gpu_tracer_content(fesom_gpu_ctx *ctx, double *content);
 /* Device pointer of tracer tr's values (context precision), for zero-copy users. */
 int fesom_gpu_tracer_device_ptr(fesom_gpu_ctx *ctx, int32_t tr, void **values, void **valuesold);
 
+/* ---- multi-instance batch of the FP32 form --------------------------------------------
+ * No counterpart in the reference: FESOM2 steps one mesh per MPI rank.  Independent FP32
+ * contexts -- each with its own mesh, tracer state (fesom_gpu_state_setup, all tracers in
+ * one launch group) and forcing uploaded, all with one Adams-Bashforth order -- step
+ * together with one kernel launch per stage over all of them.  The results agree with
+ * stepping each context alone (fesom_gpu_run_steps) to FP32 rounding; afterwards each
+ * context is read with its own calls (fesom_gpu_tracer_download_f32, fesom_gpu_tracer_content).
+ * At most 64 contexts per batch.  The batch keeps pointers to the contexts: destroy it
+ * before them. */
+typedef struct fesom_gpu_batch fesom_gpu_batch;
+int fesom_gpu_batch_create(fesom_gpu_ctx *const *ctxs, int32_t n, fesom_gpu_batch **out);
+/* stream of the batch launches (NULL = legacy stream); the contexts' own streams are not used */
+int fesom_gpu_batch_set_stream(fesom_gpu_batch *b, void *stream);
+/* nsteps steps of every instance; use_graph != 0 replays a captured CUDA graph per step */
+int fesom_gpu_batch_run_steps(fesom_gpu_batch *b, double dt, int32_t nsteps, int32_t use_graph);
+int fesom_gpu_batch_launches_per_step(fesom_gpu_batch *b, int32_t *launches);
+const char *fesom_gpu_batch_last_error(const fesom_gpu_batch *b);
+int fesom_gpu_batch_destroy(fesom_gpu_batch *b);
+
 #ifdef __cplusplus
 }
 #endif
