@@ -100,7 +100,8 @@ def stage_bytes(counts, ntr, s, ab=2, form="fp32"):
       bounds:    per tracer read T, LO, ADv (3 N3), ADh (E3); write R+, R- and the bounds
                  T_up, T_lo (4 N3); shared hnode_new, areasvol (2 N3)
       update:    per tracer read LO, ADv, R+, R-, T_up, T_lo (6 N3), ADh (E3); write T (N3);
-                 shared factors (4 N3), hnode_new, areasvol (2 N3)
+                 shared hnode_new, areasvol (2 N3)
+      vdiff:     per tracer read and write T (2 N3); shared factors (4 N3)
     FP64 plain form (per tracer, one tracer per launch):
       ab 4 N3; trxy N3 + 2 T3; edge_flux 2 N3 + 2 T3 + 2 E3 (+3 T3 shared); node_lo 3 N3 + E3
       (+8 N3); bounds 4 N3; rpm 5 N3 + E3 (+2 N3); update 6 N3 + E3 (+3 N3); vdiff 2 N3 (+4 N3)
@@ -114,7 +115,8 @@ def stage_bytes(counts, ntr, s, ab=2, form="fp32"):
             "lo_ad": s * (ntr * (ab + 2) * N3 + E3 + 8 * N3),
             "edge_flux": s * (ntr * (ab * N3 + E3) + E3),
             "bounds": s * (ntr * (7 * N3 + E3) + 2 * N3),
-            "update": s * (ntr * (7 * N3 + E3) + 6 * N3),
+            "update": s * (ntr * (7 * N3 + E3) + 2 * N3),
+            "vdiff": s * (ntr * 2 * N3 + 4 * N3),
         }
     return {
         "ab": s * ntr * 4 * N3,

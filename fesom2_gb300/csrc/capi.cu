@@ -591,6 +591,37 @@ B32View view32(fesom_gpu_ctx *ctx, int t0, int nt) {
     return v;
 }
 
+// tracers [s0, s0 + ns) of a launch group
+B32View sub32(const B32View &B, int s0, int ns) {
+    B32View v = B;
+    v.ntr = ns;
+    v.T += s0 * B.sN;
+    v.O1 += s0 * B.sN;
+    if (v.O2) v.O2 += s0 * B.sN;
+    v.Tnew += s0 * B.sN;
+    v.LO += s0 * B.sN;
+    v.ADv += s0 * B.sNI;
+    v.ADh += s0 * B.sE;
+    v.R += s0 * B.sN;
+    v.TB += s0 * B.sN;
+    v.cfg += s0;
+    v.fct_mask = B.fct_mask >> s0;
+    v.ivd_mask = B.ivd_mask >> s0;
+    for (int t = 0; t < ns; t++) {
+        v.hor[t] = B.hor[s0 + t];
+        v.ver[t] = B.ver[s0 + t];
+        v.ph[t] = B.ph[s0 + t];
+        v.pv[t] = B.pv[s0 + t];
+    }
+    return v;
+}
+
+// tracers per bounds launch: the bounds stage gathers two fields of every neighbour, so
+// fewer tracers per pass keep the neighbour columns of the nodes in flight inside L2
+#ifndef FESOM_BOUNDS_GROUP
+#define FESOM_BOUNDS_GROUP 6  // 0: the whole launch group
+#endif
+
 struct StageTimer {
     cudaEvent_t ev[2 * FESOM_NUM_STAGES * 64];
     int stage[FESOM_NUM_STAGES * 64];
@@ -664,9 +695,16 @@ int enqueue_step32(fesom_gpu_ctx *ctx, double dt, StageTimer *tm = nullptr) {
         for (int t = t0; t < t0 + nt; t++) any_fct |= ctx->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
         STAGE(10, b32_lo_ad(ctx->tp, g, fg, B, ctx->VF, dt, ctx->stream));
         STAGE(2, b32_ho(ctx->tp, g, B, ctx->mw, ctx->VF, ctx->stream));
-        if (any_fct) STAGE(4, b32_bounds(ctx->tp, g, B, dt, ctx->stream));
-        if (fork && t0 == 0) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
-        STAGE(6, b32_update(ctx->tp, g, fg, B, ctx->vfac, dt, ctx->stream));
+        if (any_fct) {
+            const int bg = FESOM_BOUNDS_GROUP > 0 ? FESOM_BOUNDS_GROUP : nt;
+            for (int s0 = 0; s0 < nt; s0 += bg)
+                STAGE(4, b32_bounds(ctx->tp, g, sub32(B, s0, std::min(bg, nt - s0)), dt, ctx->stream));
+        }
+        STAGE(6, b32_update(ctx->tp, g, B, dt, ctx->stream));
+        if (B.ivd_mask) {
+            if (fork && t0 == 0) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+            STAGE(7, b32_vdiff(ctx->tp, fg, B, ctx->vfac, ctx->stream));
+        }
     }
     CK(cudaGetLastError());
     return FESOM_OK;
@@ -683,9 +721,13 @@ int launches_per_step(fesom_gpu_ctx *ctx) {
             const int nt = std::min(ctx->group, ctx->ntr - t0);
             bool any_fct = false;
             for (int t = t0; t < t0 + nt; t++) any_fct |= ctx->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
-            // lo_ad, update (+ bounds), launched again for the wide nodes; ho (+ its fallback edges)
+            bool grp_vd = false;
+            for (int t = t0; t < t0 + nt; t++) grp_vd |= ctx->cfgs[t].i_vert_diff != 0;
+            // lo_ad, update (+ bounds), launched again for the wide nodes; ho (+ its fallback
+            // edges); vdiff
             const int wide = ctx->tp.n_wide ? 2 : 1;
-            n += wide * (2 + (any_fct ? 1 : 0)) + (ctx->mw.n_items ? 2 : 1);
+            const int bg = FESOM_BOUNDS_GROUP > 0 ? FESOM_BOUNDS_GROUP : nt;
+            n += wide * (2 + (any_fct ? (nt + bg - 1) / bg : 0)) + (ctx->mw.n_items ? 2 : 1) + (grp_vd ? 1 : 0);
         }
         return n;
     }
@@ -1416,8 +1458,9 @@ void enqueue_batch_step(fesom_gpu_batch *b, cudaStream_t s) {
         bm32_bounds(I, b->ix_n, false, s);
         if (wide) bm32_bounds(I, b->ix_w, true, s);
     }
-    bm32_update(I, b->ix_n, false, b->maxL1, s);
-    if (wide) bm32_update(I, b->ix_w, true, b->maxL1, s);
+    bm32_update(I, b->ix_n, false, s);
+    if (wide) bm32_update(I, b->ix_w, true, s);
+    if (b->any_vd) bm32_vdiff(I, b->ix_n, s);
 }
 
 }  // namespace
@@ -1526,7 +1569,7 @@ int fesom_gpu_batch_launches_per_step(fesom_gpu_batch *b, int32_t *launches) {
     if (!b || !launches) return FESOM_ERR_ARG;
     const bool wide = b->ix_w.start[b->ix_w.n] > 0;
     const int k = wide ? 2 : 1;
-    int n = 1 + (b->any_vd ? 1 : 0) + k * (2 + (b->any_fct ? 1 : 0)) + 1 + (b->ix_it.start[b->ix_it.n] ? 1 : 0);
+    int n = 1 + (b->any_vd ? 2 : 0) + k * (2 + (b->any_fct ? 1 : 0)) + 1 + (b->ix_it.start[b->ix_it.n] ? 1 : 0);
     *launches = n;
     return FESOM_OK;
 }

@@ -130,8 +130,8 @@ void b32_lo_ad(const DTopo &, const DGeom<float> &, const DForcing<float> &, con
                double dt, cudaStream_t);
 void b32_ho(const DTopo &, const DGeom<float> &, const B32View &, const MusclW &, const float *VF, cudaStream_t);
 void b32_bounds(const DTopo &, const DGeom<float> &, const B32View &, double dt, cudaStream_t);
-void b32_update(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, const VFactors &,
-                double dt, cudaStream_t);
+void b32_update(const DTopo &, const DGeom<float> &, const B32View &, double dt, cudaStream_t);
+void b32_vdiff(const DTopo &, const DForcing<float> &, const B32View &, const VFactors &, cudaStream_t);
 
 // Multi-instance batch of the FP32 form: one descriptor per instance (device memory) and,
 // per stage, the offsets of each instance's units in the launch
@@ -157,7 +157,8 @@ void bm32_vfactors(const Inst32 *, const MultiIdx &, cudaStream_t);
 void bm32_lo_ad(const Inst32 *, const MultiIdx &, bool wide, cudaStream_t);
 void bm32_ho(const Inst32 *, const MultiIdx &edges, const MultiIdx &items, cudaStream_t);
 void bm32_bounds(const Inst32 *, const MultiIdx &, bool wide, cudaStream_t);
-void bm32_update(const Inst32 *, const MultiIdx &, bool wide, int maxL1, cudaStream_t);
+void bm32_update(const Inst32 *, const MultiIdx &, bool wide, cudaStream_t);
+void bm32_vdiff(const Inst32 *, const MultiIdx &, cudaStream_t);
 
 // launch wrappers (kernels_fp64.cu / kernels_fp32.cu)
 template <typename R>

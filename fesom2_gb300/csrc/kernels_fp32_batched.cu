@@ -714,52 +714,45 @@ __device__ __forceinline__ void scan_down(float &A, float &B, int lane) {
     }
 }
 
-// One tracer's column: advected values chunk by chunk (kept in registers), then the
-// implicit vertical diffusion as forward and back substitution with the FP64 factors:
-// tp_k = inv_k rhs_k - a_k inv_k tp_{k-1}, x_k = tp_k - cp_k x_{k+1}, each a scan of
-// affine maps over the lanes with the carry passed from chunk to chunk.  Every load of a
-// chunk is issued before any of its arithmetic; the column's factors sit in shared memory.
+// Limited update of every tracer of a node: per chunk the tracer-independent part
+// (which edge slots are wet, dt / (areasvol hnode_new)) once, then per tracer every gather
+// of the chunk, the limiter and the T* value, written to the buffer of the oldest time level.
 template <int KD>
-__device__ __forceinline__ void update_node(const DTopo &tp, const DForcing<float> &f, const B32View &B, int n,
-                                            int lane, const WEdges &S, const float4 *__restrict__ fac,
-                                            const float *__restrict__ sdtv) {
+__device__ __forceinline__ void update_node(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt,
+                                            int n, int lane, const WEdges &S) {
     using C = Chunk<1, 1>;
     const int L1 = tp.L1, nl = tp.nl;
     const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
     const unsigned own = S.own;
     const int nch = C::count(nzmin, nzmax);
-#pragma unroll 1
-    for (int t = 0; t < B.ntr; t++) {
-        const bool fct = (B.fct_mask >> t) & 1ull;
-        const bool ivd = (B.ivd_mask >> t) & 1ull;
-        const size_t to = (size_t)t * B.sN;
-        const float *__restrict__ ADh = B.ADh + (size_t)t * B.sE;
-        const float *__restrict__ ADv = B.ADv + (size_t)t * B.sNI;
-        const float *__restrict__ LO = B.LO + to;
-        const float2 *__restrict__ R = B.R + to;
-        const float2 *__restrict__ TB = B.TB + to;
-        float *__restrict__ Tout = B.Tnew + to;
-        float tad[kMaxChunks];
+    for (int ch = 0; ch < nch; ch++) {
+        const C k(nzmin, nzmax, ch, lane);
+        const int nz = k.nz;
+        const int i = n * L1 + nz - 1, iv = n * nl + nz - 1;
+        const float sdt = k.lvl ? dt / (g.areasvol[iv] * g.hnode_new[i]) : 0.f;
+        unsigned okm = 0;
 #pragma unroll
-        for (int ch = 0; ch < kMaxChunks; ch++) {
-            tad[ch] = 0.f;
-            if (ch >= nch) continue;
-            const C k(nzmin, nzmax, ch, lane);
-            const int nz = k.nz;
-            const int i = n * L1 + nz - 1, iv = n * nl + nz - 1;
+        for (int u = 0; u < KD; u++) {
+            const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
+            okm |= ok ? 1u << u : 0u;
+        }
+#pragma unroll 1
+        for (int t = 0; t < B.ntr; t++) {
+            const bool fct = (B.fct_mask >> t) & 1ull;
+            const size_t to = (size_t)t * B.sN;
+            const float *__restrict__ ADh = B.ADh + (size_t)t * B.sE;
+            const float2 *__restrict__ R = B.R + to;
             const bool lf = k.lvl && fct;
-            const float lo = k.lvl ? LO[i] : 0.f;
-            float f0 = k.lvl ? ADv[iv] : 0.f;
+            // every load of the tracer's chunk first
+            const float lo = k.lvl ? B.LO[to + i] : 0.f;
+            float f0 = k.lvl ? B.ADv[(size_t)t * B.sNI + iv] : 0.f;
             const float2 r0 = lf ? R[i] : make_float2(1.f, 1.f);
-            const float2 tb = lf ? TB[i] : make_float2(0.f, 0.f);
-            const float sdt = k.lvl ? sdtv[nz] : 0.f;
+            const float2 tb = lf ? B.TB[to + i] : make_float2(0.f, 0.f);
             float x[KD];
             float2 rm[KD];
-            unsigned okm = 0;
 #pragma unroll
             for (int u = 0; u < KD; u++) {
-                const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
-                okm |= ok ? 1u << u : 0u;
+                const bool ok = (okm >> u) & 1u;
                 x[u] = ok ? ADh[S.e[u] * L1 + nz - 1] : 0.f;
                 rm[u] = (ok && fct) ? R[S.m[u] * L1 + nz - 1] : make_float2(1.f, 1.f);
             }
@@ -786,100 +779,218 @@ __device__ __forceinline__ void update_node(const DTopo &tp, const DForcing<floa
             // T* = T + (del_ttf + T (hnode - hnode_new)) / hnode_new = LO + fluxes dt / areasvol / hnode_new
             // (oce_adv_tra_driver.F90:535-620, oce_ale_tracer.F90:319-321, 743-754)
             float val = lo + (f0 - f1 + hs) * sdt;
-            if (fct && k.out) {
-                const float vc = fminf(fmaxf(val, tb.y), tb.x);
-                // a clamp beyond round-off means the limiter itself failed
-                if (fabsf(vc - val) > 1e-5f * (tb.x - tb.y) + 1e-6f * fabsf(vc)) atomicOr(B.status, 2u);
-                val = vc;
-            }
-            tad[ch] = val;
-            if (!ivd && k.out) {
-                Tout[i] = val;
-                if (!isfinite(val)) atomicOr(B.status, 1u);
-            }
-        }
-        if (!ivd) continue;
-        const float bc = f.bc ? f.bc[(size_t)t * tp.N2 + n] : 0.f;
-        float tpv[kMaxChunks];
-        float carry = 0.f;
-#pragma unroll
-        for (int ch = 0; ch < kMaxChunks; ch++) {
-            tpv[ch] = 0.f;
-            if (ch >= nch) continue;
-            const C k(nzmin, nzmax, ch, lane);
-            const int nz = k.nz;
-            const float t0 = tad[ch];
-            const float tu = sh_up(t0, 1), td = sh_dn(t0, 1);
-            float A = 1.f, Bv = 0.f;
             if (k.out) {
-                const float4 fz = fac[nz];  // (a, c, 1/m, c/m)
-                float rhs = 0.f;
-                if (nz > nzmin) rhs -= fz.x * (tu - t0);
-                if (nz < nzmax - 1) rhs -= fz.y * (td - t0);
-                if (nz == nzmin) rhs += bc;
-                A = -(fz.x * fz.z);
-                Bv = rhs * fz.z;
-            }
-            scan_up(A, Bv, lane);
-            const float y = A * carry + Bv;
-            tpv[ch] = y;
-            carry = __shfl_sync(kFull, y, 30);  // last stored lane (Chunk<1, 1>)
-        }
-        carry = 0.f;
-#pragma unroll
-        for (int ch = kMaxChunks - 1; ch >= 0; ch--) {
-            if (ch >= nch) continue;
-            const C k(nzmin, nzmax, ch, lane);
-            float A = 1.f, Bv = 0.f;
-            if (k.out) {
-                A = -fac[k.nz].w;
-                Bv = tpv[ch];
-            }
-            scan_down(A, Bv, lane);
-            const float xx = A * carry + Bv;
-            carry = __shfl_sync(kFull, xx, 1);  // first stored lane (Chunk<1, 1>)
-            if (k.out) {
-                const float val = tad[ch] + xx;
-                Tout[n * L1 + k.nz - 1] = val;
+                if (fct) {
+                    const float vc = fminf(fmaxf(val, tb.y), tb.x);
+                    // a clamp beyond round-off means the limiter itself failed
+                    if (fabsf(vc - val) > 1e-5f * (tb.x - tb.y) + 1e-6f * fabsf(vc)) atomicOr(B.status, 2u);
+                    val = vc;
+                }
+                B.Tnew[to + i] = val;
                 if (!isfinite(val)) atomicOr(B.status, 1u);
             }
         }
     }
 }
 
-// fac_sm: kWB columns of (a, c, 1/m, c/m), then kWB columns of dt / (areasvol hnode_new),
-// colstride entries each (1-based levels)
 template <bool WIDE>
-__device__ __forceinline__ void update_unit(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
-                                            const B32View &B, const VFactors &vf, float dt, int j, WEdges *Se,
-                                            float4 *fac_sm, int colstride) {
+__device__ __forceinline__ void update_unit(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int j,
+                                            WEdges *Se) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int n = unit_node<WIDE>(tp, j);
     if (n < 0) return;
     WEdges &S = Se[warp];
     stage_edges(tp, n, lane, S);
     if ((S.deg > 8) != WIDE) return;
-    float4 *fac = fac_sm + (size_t)warp * colstride;
-    float *sdtv = reinterpret_cast<float *>(fac_sm + (size_t)kWB * colstride) + (size_t)warp * colstride;
-    // the column's tracer-independent factors, once per node: dt / (areasvol hnode_new) and
-    // the implicit-diffusion factors
-    for (int nz = S.nzmin + lane; nz <= S.nzmax - 1; nz += 32) {
-        const int i = n * tp.L1 + nz - 1;
-        sdtv[nz] = dt / (g.areasvol[n * tp.nl + nz - 1] * g.hnode_new[i]);
-        if (B.ivd_mask) fac[nz] = make_float4(vf.a[i], vf.c[i], vf.inv[i], vf.cp[i]);
-    }
-    __syncwarp();
-    if (WIDE) update_node<kMaxDeg>(tp, f, B, n, lane, S, fac, sdtv);
-    else if (S.deg <= 6) update_node<6>(tp, f, B, n, lane, S, fac, sdtv);
-    else update_node<8>(tp, f, B, n, lane, S, fac, sdtv);
+    if (WIDE) update_node<kMaxDeg>(tp, g, B, dt, n, lane, S);
+    else if (S.deg <= 6) update_node<6>(tp, g, B, dt, n, lane, S);
+    else update_node<8>(tp, g, B, dt, n, lane, S);
 }
 
 template <bool WIDE>
 __global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_UPDATE)
-k32_update(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, VFactors vf, float dt) {
+k32_update(DTopo tp, DGeom<float> g, B32View B, float dt) {
     __shared__ WEdges Se[kWB];
-    extern __shared__ __align__(16) float4 fac_sm[];
-    update_unit<WIDE>(tp, g, f, B, vf, dt, blockIdx.x * kWB + (threadIdx.x >> 5), Se, fac_sm, tp.L1 + 1);
+    update_unit<WIDE>(tp, g, B, dt, blockIdx.x * kWB + (threadIdx.x >> 5), Se);
+}
+
+// ---------------------------------------------------------------------------
+// k32_vdiff: implicit vertical diffusion of the advected columns (in Tnew)
+// ---------------------------------------------------------------------------
+// Forward substitution tp_k = inv_k rhs_k - a_k inv_k tp_{k-1} and back substitution
+// x_k = tp_k - cp_k x_{k+1} (oce_ale_tracer.F90:1406-1422) with the column's FP64-derived
+// factors, as scans of affine maps y -> A y + B over the lanes of each chunk with the carry
+// passed from chunk to chunk.  The multipliers A depend on the column only: their partial
+// products at each scan step are formed once per node into shared memory, so a tracer's
+// scan step is one shuffle and one multiply-add.  rhs_k = -a_k (T_{k-1} - T_k)
+// - c_k (T_{k+1} - T_k) (+ bc_surface at the top, :1216-1229, 1377-1383); T += x.
+constexpr int kWV = 4;                    // warps (nodes) per block of the diffusion kernel
+constexpr int kScan = 5;                  // steps of a 32-lane scan
+constexpr int kVdiffMaxChunks = kMaxChunks;
+
+struct VdiffWarp {
+    float4 fac[130];                                  // (a, c, 1/m, c/m), 1-based levels
+    float af[kVdiffMaxChunks][kScan + 1][32];         // forward: A at each step (0 below the offset), then the total
+    float ab[kVdiffMaxChunks][kScan + 1][32];         // backward
+};
+
+// forward and back substitution of tracers t1 and t2 (t2 < 0: none) of a column of NCH
+// chunks: the chunks' scans are independent straight-line code; only the carries between
+// chunks are serial
+template <int NCH>
+__device__ __forceinline__ void vdiff_pair(const DTopo &tp, const DForcing<float> &f, const B32View &B, int n,
+                                           int lane, int nzmin, int nzmax, int t1, int t2, VdiffWarp &W) {
+    using C = Chunk<1, 1>;
+    const int L1 = tp.L1;
+    const bool two = t2 >= 0;
+    float *__restrict__ T1 = B.Tnew + (size_t)t1 * B.sN;
+    float *__restrict__ T2 = B.Tnew + (size_t)(two ? t2 : t1) * B.sN;
+    const float bc1 = f.bc ? f.bc[(size_t)t1 * tp.N2 + n] : 0.f;
+    const float bc2 = (f.bc && two) ? f.bc[(size_t)t2 * tp.N2 + n] : 0.f;
+    float a1[NCH], a2[NCH], y1[NCH], y2[NCH];
+#pragma unroll
+    for (int ch = 0; ch < NCH; ch++) {
+        const C k(nzmin, nzmax, ch, lane);
+        const int nz = k.nz, i = n * L1 + nz - 1;
+        a1[ch] = k.lvl ? T1[i] : 0.f;
+        a2[ch] = (k.lvl && two) ? T2[i] : 0.f;
+    }
+#pragma unroll
+    for (int ch = 0; ch < NCH; ch++) {
+        const C k(nzmin, nzmax, ch, lane);
+        const int nz = k.nz;
+        const float u1 = sh_up(a1[ch], 1), d1 = sh_dn(a1[ch], 1);
+        const float u2 = sh_up(a2[ch], 1), d2 = sh_dn(a2[ch], 1);
+        float b1 = 0.f, b2 = 0.f;
+        if (k.out) {
+            const float4 fz = W.fac[nz];
+            float r1 = 0.f, r2 = 0.f;
+            if (nz > nzmin) {
+                r1 -= fz.x * (u1 - a1[ch]);
+                r2 -= fz.x * (u2 - a2[ch]);
+            }
+            if (nz < nzmax - 1) {
+                r1 -= fz.y * (d1 - a1[ch]);
+                r2 -= fz.y * (d2 - a2[ch]);
+            }
+            if (nz == nzmin) {
+                r1 += bc1;
+                r2 += bc2;
+            }
+            b1 = r1 * fz.z;
+            b2 = r2 * fz.z;
+        }
+#pragma unroll
+        for (int s = 0, off = 1; s < kScan; s++, off <<= 1) {
+            const float w = W.af[ch][s][lane];
+            b1 = fmaf(w, __shfl_up_sync(kFull, b1, off), b1);
+            b2 = fmaf(w, __shfl_up_sync(kFull, b2, off), b2);
+        }
+        y1[ch] = b1;
+        y2[ch] = b2;
+    }
+    float c1 = 0.f, c2 = 0.f;
+#pragma unroll
+    for (int ch = 0; ch < NCH; ch++) {
+        const float w = W.af[ch][kScan][lane];
+        y1[ch] = fmaf(w, c1, y1[ch]);
+        y2[ch] = fmaf(w, c2, y2[ch]);
+        c1 = __shfl_sync(kFull, y1[ch], 30);  // last stored lane (Chunk<1, 1>)
+        c2 = __shfl_sync(kFull, y2[ch], 30);
+    }
+#pragma unroll
+    for (int ch = 0; ch < NCH; ch++) {
+        const C k(nzmin, nzmax, ch, lane);
+        float b1 = k.out ? y1[ch] : 0.f, b2 = k.out ? y2[ch] : 0.f;
+#pragma unroll
+        for (int s = 0, off = 1; s < kScan; s++, off <<= 1) {
+            const float w = W.ab[ch][s][lane];
+            b1 = fmaf(w, __shfl_down_sync(kFull, b1, off), b1);
+            b2 = fmaf(w, __shfl_down_sync(kFull, b2, off), b2);
+        }
+        y1[ch] = b1;
+        y2[ch] = b2;
+    }
+    c1 = c2 = 0.f;
+#pragma unroll
+    for (int ch = NCH - 1; ch >= 0; ch--) {
+        const C k(nzmin, nzmax, ch, lane);
+        const float w = W.ab[ch][kScan][lane];
+        const float x1 = fmaf(w, c1, y1[ch]), x2 = fmaf(w, c2, y2[ch]);
+        c1 = __shfl_sync(kFull, x1, 1);  // first stored lane (Chunk<1, 1>)
+        c2 = __shfl_sync(kFull, x2, 1);
+        if (k.out) {
+            const int i = n * L1 + k.nz - 1;
+            const float v1 = a1[ch] + x1;
+            T1[i] = v1;
+            if (!isfinite(v1)) atomicOr(B.status, 1u);
+            if (two) {
+                const float v2 = a2[ch] + x2;
+                T2[i] = v2;
+                if (!isfinite(v2)) atomicOr(B.status, 1u);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void vdiff_unit(const DTopo &tp, const DForcing<float> &f, const B32View &B,
+                                           const VFactors &vf, int n, VdiffWarp &W) {
+    using C = Chunk<1, 1>;
+    const int lane = threadIdx.x & 31;
+    if (n >= tp.N2) return;
+    const int L1 = tp.L1;
+    const int nzmin = tp.n_ulev[n], nzmax = tp.n_nlev[n];
+    const int nch = C::count(nzmin, nzmax);
+    for (int nz = nzmin + lane; nz <= nzmax - 1; nz += 32) {
+        const int i = n * L1 + nz - 1;
+        W.fac[nz] = make_float4(vf.a[i], vf.c[i], vf.inv[i], vf.cp[i]);
+    }
+    __syncwarp();
+    // the column's scan multipliers
+    for (int ch = 0; ch < nch; ch++) {
+        const C k(nzmin, nzmax, ch, lane);
+        float A = 1.f, Ad = 1.f;
+        if (k.out) {
+            const float4 fz = W.fac[k.nz];
+            A = -(fz.x * fz.z);
+            Ad = -fz.w;
+        }
+#pragma unroll
+        for (int s = 0, off = 1; s < kScan; s++, off <<= 1) {
+            W.af[ch][s][lane] = lane >= off ? A : 0.f;
+            W.ab[ch][s][lane] = lane + off < 32 ? Ad : 0.f;
+            const float Ap = __shfl_up_sync(kFull, A, off), An = __shfl_down_sync(kFull, Ad, off);
+            if (lane >= off) A *= Ap;
+            if (lane + off < 32) Ad *= An;
+        }
+        W.af[ch][kScan][lane] = A;
+        W.ab[ch][kScan][lane] = Ad;
+    }
+    __syncwarp();
+    // the tracers with implicit diffusion, two per pass: their scan chains interleave
+    unsigned long long todo = B.ivd_mask & (B.ntr >= 64 ? ~0ull : ((1ull << B.ntr) - 1));
+    while (todo) {
+        const int t1 = __ffsll((long long)todo) - 1;
+        todo &= todo - 1;
+        int t2 = -1;
+        if (todo) {
+            t2 = __ffsll((long long)todo) - 1;
+            todo &= todo - 1;
+        }
+        switch (nch) {
+            case 1: vdiff_pair<1>(tp, f, B, n, lane, nzmin, nzmax, t1, t2, W); break;
+            case 2: vdiff_pair<2>(tp, f, B, n, lane, nzmin, nzmax, t1, t2, W); break;
+            case 3: vdiff_pair<3>(tp, f, B, n, lane, nzmin, nzmax, t1, t2, W); break;
+            case 4: vdiff_pair<4>(tp, f, B, n, lane, nzmin, nzmax, t1, t2, W); break;
+            default: vdiff_pair<5>(tp, f, B, n, lane, nzmin, nzmax, t1, t2, W); break;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(32 * kWV) k32_vdiff(DTopo tp, DForcing<float> f, B32View B, VFactors vf) {
+    __shared__ VdiffWarp Wsm[kWV];
+    const int warp = threadIdx.x >> 5;
+    vdiff_unit(tp, f, B, vf, blockIdx.x * kWV + warp, Wsm[warp]);
 }
 
 // ---------------------------------------------------------------------------
@@ -939,14 +1050,19 @@ __global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_BOUNDS) k32m_bounds
     bounds_unit<WIDE>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
 }
 template <bool WIDE>
-__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_UPDATE)
-k32m_update(const Inst32 *__restrict__ I, MultiIdx ix, int colstride) {
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_UPDATE) k32m_update(const Inst32 *__restrict__ I, MultiIdx ix) {
     __shared__ WEdges Se[kWB];
-    extern __shared__ __align__(16) float4 fac_sm[];
     const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
     if (u >= ix.start[ix.n]) return;
     const int i = find_inst(ix, u);
-    update_unit<WIDE>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].vf, I[i].dt, u - ix.start[i], Se, fac_sm, colstride);
+    update_unit<WIDE>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
+}
+__global__ void __launch_bounds__(32 * kWV) k32m_vdiff(const Inst32 *__restrict__ I, MultiIdx ix) {
+    __shared__ VdiffWarp Wsm[kWV];
+    const int u = blockIdx.x * kWV + (threadIdx.x >> 5);
+    if (u >= ix.start[ix.n]) return;
+    const int i = find_inst(ix, u);
+    vdiff_unit(I[i].tp, I[i].f, I[i].B, I[i].vf, u - ix.start[i], Wsm[threadIdx.x >> 5]);
 }
 
 // ---------------------------------------------------------------------------
@@ -987,11 +1103,12 @@ void b32_bounds(const DTopo &tp, const DGeom<float> &g, const B32View &B, double
     k32_bounds<false><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, B, (float)dt);
     if (tp.n_wide) k32_bounds<true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
 }
-void b32_update(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B,
-                const VFactors &v, double dt, cudaStream_t s) {
-    const size_t sm = (sizeof(float4) + sizeof(float)) * (tp.L1 + 1) * kWB;
-    k32_update<false><<<grid_nodes(tp.N2), kTB, sm, s>>>(tp, g, f, B, v, (float)dt);
-    if (tp.n_wide) k32_update<true><<<grid_nodes(tp.n_wide), kTB, sm, s>>>(tp, g, f, B, v, (float)dt);
+void b32_update(const DTopo &tp, const DGeom<float> &g, const B32View &B, double dt, cudaStream_t s) {
+    k32_update<false><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, B, (float)dt);
+    if (tp.n_wide) k32_update<true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
+}
+void b32_vdiff(const DTopo &tp, const DForcing<float> &f, const B32View &B, const VFactors &v, cudaStream_t s) {
+    k32_vdiff<<<(tp.N2 + kWV - 1) / kWV, 32 * kWV, 0, s>>>(tp, f, B, v);
 }
 
 // multi-instance launch wrappers: ix_* hold the per-instance unit offsets of each stage
@@ -1020,12 +1137,15 @@ void bm32_bounds(const Inst32 *I, const MultiIdx &ix, bool wide, cudaStream_t s)
     if (wide) k32m_bounds<true><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
     else k32m_bounds<false><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
 }
-void bm32_update(const Inst32 *I, const MultiIdx &ix, bool wide, int maxL1, cudaStream_t s) {
+void bm32_update(const Inst32 *I, const MultiIdx &ix, bool wide, cudaStream_t s) {
     const int u = ix.start[ix.n];
     if (!u) return;
-    const size_t sm = (sizeof(float4) + sizeof(float)) * (maxL1 + 1) * kWB;
-    if (wide) k32m_update<true><<<grid_nodes(u), kTB, sm, s>>>(I, ix, maxL1 + 1);
-    else k32m_update<false><<<grid_nodes(u), kTB, sm, s>>>(I, ix, maxL1 + 1);
+    if (wide) k32m_update<true><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
+    else k32m_update<false><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
+}
+void bm32_vdiff(const Inst32 *I, const MultiIdx &ix, cudaStream_t s) {
+    const int u = ix.start[ix.n];
+    if (u) k32m_vdiff<<<(u + kWV - 1) / kWV, 32 * kWV, 0, s>>>(I, ix);
 }
 
 }  // namespace fesom
