@@ -66,6 +66,11 @@ struct fesom_gpu_ctx {
     // advection stages and join before the update
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // host-array step with overlapped transfers: copy-in and copy-out streams, an event per
+    // tracer group for "resident" and "computed"
+    cudaStream_t h2d = nullptr, d2h = nullptr;
+    cudaEvent_t ev_forcing = nullptr;
+    std::vector<cudaEvent_t> ev_in, ev_done;
 };
 
 namespace {
@@ -552,6 +557,9 @@ int alloc_state32(fesom_gpu_ctx *ctx, int ntr, int ab) {
         CK(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+        CK(cudaStreamCreateWithFlags(&ctx->h2d, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&ctx->d2h, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&ctx->ev_forcing, cudaEventDisableTiming));
     }
     ctx->rot = 0;
     ctx->ntr = ntr;
@@ -670,15 +678,15 @@ int enqueue_step(fesom_gpu_ctx *ctx, double dt, StageTimer *tm = nullptr) {
     return FESOM_OK;
 }
 
-int enqueue_step32(fesom_gpu_ctx *ctx, double dt, StageTimer *tm = nullptr) {
+// the tracer-independent stages of a step: edge volume fluxes, then the vertical-diffusion
+// factors (outside profiled steps on the side stream, joined before the first diffusion)
+int enqueue_shared32(fesom_gpu_ctx *ctx, double dt, StageTimer *tm, bool &fork) {
     const DGeom<float> &g = ctx->g32;
     DForcing<float> f = forcing_view<float>(ctx, 0);
     bool any_vd = false;
     for (int t = 0; t < ctx->ntr; t++) any_vd |= ctx->cfgs[t].i_vert_diff != 0;
     STAGE(8, b32_vflux(ctx->tp, g, f, ctx->VF, ctx->stream));
-    // the factors depend on the forcing only: outside profiled steps they run on the side
-    // stream while the advection stages of the first group run, and join before its update
-    const bool fork = any_vd && !tm;
+    fork = any_vd && !tm;
     if (fork) {
         CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
         CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
@@ -687,25 +695,43 @@ int enqueue_step32(fesom_gpu_ctx *ctx, double dt, StageTimer *tm = nullptr) {
     } else if (any_vd) {
         STAGE(9, b32_vfactors(ctx->tp, g, f, dt, ctx->vfac, ctx->stream));
     }
-    for (int t0 = 0; t0 < ctx->ntr; t0 += ctx->group) {
-        const int nt = std::min(ctx->group, ctx->ntr - t0);
-        B32View B = view32(ctx, t0, nt);
-        DForcing<float> fg = forcing_view<float>(ctx, t0);
-        bool any_fct = false;
-        for (int t = t0; t < t0 + nt; t++) any_fct |= ctx->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
-        STAGE(10, b32_lo_ad(ctx->tp, g, fg, B, ctx->VF, dt, ctx->stream));
-        STAGE(2, b32_ho(ctx->tp, g, B, ctx->mw, ctx->VF, ctx->stream));
-        if (any_fct) {
-            const int bg = FESOM_BOUNDS_GROUP > 0 ? FESOM_BOUNDS_GROUP : nt;
-            for (int s0 = 0; s0 < nt; s0 += bg)
-                STAGE(4, b32_bounds(ctx->tp, g, sub32(B, s0, std::min(bg, nt - s0)), dt, ctx->stream));
-        }
-        STAGE(6, b32_update(ctx->tp, g, B, dt, ctx->stream));
-        if (B.ivd_mask) {
-            if (fork && t0 == 0) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
-            STAGE(7, b32_vdiff(ctx->tp, fg, B, ctx->vfac, ctx->stream));
-        }
+    return FESOM_OK;
+}
+
+// the stages of tracers [t0, t0 + nt); `joined` records that the stream already waited
+// for the factors of the side stream
+int enqueue_group32(fesom_gpu_ctx *ctx, double dt, int t0, int nt, StageTimer *tm, bool fork, bool &joined) {
+    const DGeom<float> &g = ctx->g32;
+    B32View B = view32(ctx, t0, nt);
+    DForcing<float> fg = forcing_view<float>(ctx, t0);
+    bool any_fct = false;
+    for (int t = t0; t < t0 + nt; t++) any_fct |= ctx->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
+    STAGE(10, b32_lo_ad(ctx->tp, g, fg, B, ctx->VF, dt, ctx->stream));
+    STAGE(2, b32_ho(ctx->tp, g, B, ctx->mw, ctx->VF, ctx->stream));
+    if (any_fct) {
+        const int bg = FESOM_BOUNDS_GROUP > 0 ? FESOM_BOUNDS_GROUP : nt;
+        for (int s0 = 0; s0 < nt; s0 += bg)
+            STAGE(4, b32_bounds(ctx->tp, g, sub32(B, s0, std::min(bg, nt - s0)), dt, ctx->stream));
     }
+    STAGE(6, b32_update(ctx->tp, g, B, dt, ctx->stream));
+    if (B.ivd_mask) {
+        if (fork && !joined) {
+            CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+            joined = true;
+        }
+        STAGE(7, b32_vdiff(ctx->tp, fg, B, ctx->vfac, ctx->stream));
+    }
+    return FESOM_OK;
+}
+
+int enqueue_step32(fesom_gpu_ctx *ctx, double dt, StageTimer *tm = nullptr) {
+    bool fork = false, joined = false;
+    int rc = enqueue_shared32(ctx, dt, tm, fork);
+    if (rc) return rc;
+    for (int t0 = 0; t0 < ctx->ntr; t0 += ctx->group)
+        if ((rc = enqueue_group32(ctx, dt, t0, std::min(ctx->group, ctx->ntr - t0), tm, fork, joined))) return rc;
+    // a side-stream branch must rejoin the stream (a captured graph requires it)
+    if (fork && !joined) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
     CK(cudaGetLastError());
     return FESOM_OK;
 }
@@ -911,6 +937,11 @@ int fesom_gpu_finalize(fesom_gpu_ctx *ctx) {
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->side) cudaStreamDestroy(ctx->side);
+    if (ctx->ev_forcing) cudaEventDestroy(ctx->ev_forcing);
+    for (cudaEvent_t e : ctx->ev_in) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->ev_done) cudaEventDestroy(e);
+    if (ctx->h2d) cudaStreamDestroy(ctx->h2d);
+    if (ctx->d2h) cudaStreamDestroy(ctx->d2h);
     for (void *p : ctx->allocs) cudaFree(p);
     delete ctx;
     return FESOM_OK;
@@ -1367,6 +1398,93 @@ int fesom_gpu_tracer_content(fesom_gpu_ctx *ctx, double *content) {
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(content, ctx->content_out, sizeof(double) * ctx->ntr, cudaMemcpyDeviceToHost, ctx->stream));
     return wait_stream(ctx, -1);
+}
+
+int fesom_gpu_step_host_f32(fesom_gpu_ctx *ctx, double dt, const float *uv, const float *w, const float *wi,
+                            const float *we, const float *Kv, const float *bc_surf, const float *const *values_in,
+                            const float *const *valuesold_in, float *const *values_out, float *const *valuesold_out) {
+    if (!ctx || !uv || !w || !we || !Kv || !values_in || !valuesold_in || !values_out) return FESOM_ERR_ARG;
+    if (ctx->prec != FESOM_PREC_FP32) { ctx->err = "FP32 buffers need a FESOM_PREC_FP32 context"; return FESOM_ERR_STATE; }
+    if (!ctx->state_ready) { ctx->err = "call fesom_gpu_state_setup first"; return FESOM_ERR_STATE; }
+    int rc;
+    const int ntr = ctx->ntr;
+    const size_t sN = (size_t)ctx->L1 * ctx->N2;
+    if (ctx->ab_max != 2) {
+        // AB3 interleaves its two previous levels on the host: the serial path
+        if ((rc = fesom_gpu_forcing_upload_f32(ctx, uv, w, wi, we, Kv, bc_surf))) return rc;
+        for (int t = 0; t < ntr; t++)
+            if ((rc = fesom_gpu_tracer_upload_f32(ctx, t, values_in[t], valuesold_in[t]))) return rc;
+        if ((rc = fesom_gpu_run_steps(ctx, dt, 1, 0))) return rc;
+        for (int t = 0; t < ntr; t++)
+            if ((rc = fesom_gpu_tracer_download_f32(ctx, t, values_out[t], valuesold_out ? valuesold_out[t] : nullptr)))
+                return rc;
+        return wait_stream(ctx, -1);
+    }
+    const int G = ctx->group, ng = (ntr + G - 1) / G;
+    while ((int)ctx->ev_in.size() < ng) {
+        cudaEvent_t a, b;
+        CK(cudaEventCreateWithFlags(&a, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&b, cudaEventDisableTiming));
+        ctx->ev_in.push_back(a);
+        ctx->ev_done.push_back(b);
+    }
+    // the previous step's kernels are done with the buffers the copies fill
+    CK(cudaEventRecord(ctx->ev_forcing, ctx->stream));
+    CK(cudaStreamWaitEvent(ctx->h2d, ctx->ev_forcing, 0));
+    // forcing, then the tracer groups, on the copy-in stream
+    const size_t sNI = (size_t)ctx->nl * ctx->N2;
+    CK(cudaMemcpyAsync(ctx->uv, uv, 4 * 2 * (size_t)ctx->L1 * ctx->T2, cudaMemcpyHostToDevice, ctx->h2d));
+    CK(cudaMemcpyAsync(ctx->w, w, 4 * sNI, cudaMemcpyHostToDevice, ctx->h2d));
+    CK(cudaMemcpyAsync(ctx->we, we, 4 * sNI, cudaMemcpyHostToDevice, ctx->h2d));
+    CK(cudaMemcpyAsync(ctx->Kv, Kv, 4 * sNI, cudaMemcpyHostToDevice, ctx->h2d));
+    if (wi) CK(cudaMemcpyAsync(ctx->wi, wi, 4 * sNI, cudaMemcpyHostToDevice, ctx->h2d));
+    if (bc_surf) CK(cudaMemcpyAsync(ctx->bc, bc_surf, 4 * (size_t)ctx->N2 * ntr, cudaMemcpyHostToDevice, ctx->h2d));
+    else CK(cudaMemsetAsync(ctx->bc, 0, 4 * (size_t)ctx->N2 * ntr, ctx->h2d));
+    ctx->forcing_ready = true;
+    CK(cudaEventRecord(ctx->ev_forcing, ctx->h2d));
+    float *Tcur = level32(ctx, 0), *Told = level32(ctx, 1);  // the step writes Tnew into Told's buffer
+    for (int gi = 0; gi < ng; gi++) {
+        for (int t = gi * G; t < std::min(ntr, (gi + 1) * G); t++) {
+            CK(cudaMemcpyAsync(Tcur + sN * t, values_in[t], 4 * sN, cudaMemcpyHostToDevice, ctx->h2d));
+            CK(cudaMemcpyAsync(Told + sN * t, valuesold_in[t], 4 * sN, cudaMemcpyHostToDevice, ctx->h2d));
+        }
+        CK(cudaEventRecord(ctx->ev_in[gi], ctx->h2d));
+    }
+    // compute each group as soon as its tracers are resident
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_forcing, 0));
+    bool fork = false, joined = false;
+    if ((rc = enqueue_shared32(ctx, dt, nullptr, fork))) return rc;
+    for (int gi = 0; gi < ng; gi++) {
+        CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_in[gi], 0));
+        const int t0 = gi * G;
+        if ((rc = enqueue_group32(ctx, dt, t0, std::min(G, ntr - t0), nullptr, fork, joined))) return rc;
+        CK(cudaEventRecord(ctx->ev_done[gi], ctx->stream));
+    }
+    if (fork && !joined) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+    CK(cudaGetLastError());
+    // copy each group out as soon as it is computed: the new values (Told's buffer) and the
+    // new previous level (the values the step started from)
+    for (int gi = 0; gi < ng; gi++) {
+        CK(cudaStreamWaitEvent(ctx->d2h, ctx->ev_done[gi], 0));
+        for (int t = gi * G; t < std::min(ntr, (gi + 1) * G); t++) {
+            CK(cudaMemcpyAsync(values_out[t], Told + sN * t, 4 * sN, cudaMemcpyDeviceToHost, ctx->d2h));
+            if (valuesold_out)
+                CK(cudaMemcpyAsync(valuesold_out[t], Tcur + sN * t, 4 * sN, cudaMemcpyDeviceToHost, ctx->d2h));
+        }
+    }
+    rotate32(ctx);
+    // the context's stream follows the copies out, so later calls see a quiet context
+    CK(cudaEventRecord(ctx->ev_forcing, ctx->d2h));
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_forcing, 0));
+    if ((rc = wait_stream(ctx, -1))) return rc;
+    unsigned st = 0;
+    CK(cudaMemcpy(&st, ctx->status, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (st) {
+        CK(cudaMemset(ctx->status, 0, sizeof(unsigned)));
+        ctx->err = st & FESOM_STATUS_NAN ? "NaN in the tracer step" : "FCT limiter needed more than round-off clamping";
+        return FESOM_ERR_NUMERIC;
+    }
+    return FESOM_OK;
 }
 
 int fesom_gpu_tracer_device_ptr(fesom_gpu_ctx *ctx, int32_t tr, void **values, void **valuesold) {

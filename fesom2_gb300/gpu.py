@@ -87,6 +87,8 @@ _SIGS = {
     "fesom_gpu_launches_per_step": ([_P, C.POINTER(C.c_int32)], C.c_int),
     "fesom_gpu_debug_fetch": ([_P, C.c_char_p, C.c_int32, _P, C.c_size_t], C.c_int),
     "fesom_gpu_tracer_device_ptr": ([_P, C.c_int32, C.POINTER(_P), C.POINTER(_P)], C.c_int),
+    "fesom_gpu_step_host_f32": ([_P, C.c_double, _P, _P, _P, _P, _P, _P, C.POINTER(_P), C.POINTER(_P),
+                                 C.POINTER(_P), C.POINTER(_P)], C.c_int),
     "fesom_gpu_batch_create": ([C.POINTER(_P), C.c_int32, C.POINTER(_P)], C.c_int),
     "fesom_gpu_batch_set_stream": ([_P, _P], C.c_int),
     "fesom_gpu_batch_run_steps": ([_P, C.c_double, C.c_int32, C.c_int32], C.c_int),
@@ -312,6 +314,26 @@ class Context:
 
     def set_tracers_per_launch(self, n: int):
         self._chk(self.L.fesom_gpu_set_tracers_per_launch(self.h, int(n)))
+
+    def step_host_f32(self, forcing, values_in, valuesold_in, values_out=None, valuesold_out=None):
+        """One FP32 step from and to host float32 arrays with the transfers overlapped with the
+        compute (``fesom_gpu_step_host_f32``); the outputs default to the inputs (in place)."""
+        f = forcing
+        for a in (f.uv, f.w, f.w_e, f.Kv):
+            if a.dtype != np.float32 or not a.flags.c_contiguous:
+                raise ValueError("forcing arrays must be C-contiguous float32")
+        n = len(values_in)
+        values_out = values_in if values_out is None else values_out
+        arrs = [values_in, valuesold_in, values_out] + ([valuesold_out] if valuesold_out is not None else [])
+        for lst in arrs:
+            for a in lst:
+                if a.dtype != np.float32 or not a.flags.c_contiguous:
+                    raise ValueError("tracer arrays must be C-contiguous float32")
+        mk = lambda lst: (_P * n)(*[a.ctypes.data for a in lst])
+        self._chk(self.L.fesom_gpu_step_host_f32(
+            self.h, float(f.dt), _p(f.uv), _p(f.w), _p(getattr(f, "w_i", None)), _p(f.w_e), _p(f.Kv),
+            _p(f.bc_surface), mk(values_in), mk(valuesold_in), mk(values_out),
+            mk(valuesold_out) if valuesold_out is not None else None))
 
     def launches_per_step(self) -> int:
         n = C.c_int32(0)

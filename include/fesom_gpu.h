@@ -241,6 +241,18 @@ int fesom_gpu_tracer_content(fesom_gpu_ctx *ctx, double *content);
 /* Device pointer of tracer tr's values (context precision), for zero-copy users. */
 int fesom_gpu_tracer_device_ptr(fesom_gpu_ctx *ctx, int32_t tr, void **values, void **valuesold);
 
+/* One step of an FP32 context from and to host arrays (FP32, the caller's layout), with the
+ * transfers overlapped with the compute: the tracers move in launch groups
+ * (fesom_gpu_set_tracers_per_launch) -- a group computes as soon as its values and previous
+ * level are resident, and is copied back as soon as it is done, while later groups upload
+ * and earlier ones download.  values_out / valuesold_out may be the input arrays (in-place
+ * update, as the reference's tracer arrays); valuesold_out may be NULL.  Blocks until the
+ * results are in host memory; page-locked host arrays give the full transfer rate.  AB3
+ * contexts take the serial path (their previous levels are interleaved on the host). */
+int fesom_gpu_step_host_f32(fesom_gpu_ctx *ctx, double dt, const float *uv, const float *w, const float *wi,
+                            const float *we, const float *Kv, const float *bc_surf, const float *const *values_in,
+                            const float *const *valuesold_in, float *const *values_out, float *const *valuesold_out);
+
 /* ---- multi-instance batch of the FP32 form --------------------------------------------
  * No counterpart in the reference: FESOM2 steps one mesh per MPI rank.  Independent FP32
  * contexts -- each with its own mesh, tracer state (fesom_gpu_state_setup, all tracers in
