@@ -27,6 +27,8 @@ UNITS = {
     "capi.cu": [],
     # allocation-free vertical diffusion: FP64, same rounding as kernels_fp64.cu
     "vdiff_noalloc.cu": ["--fmad=false"],
+    # tail of the tracer loop (decay, climatology relaxation, clamps): FP64, no contraction
+    "kernels_tail.cu": ["--fmad=false"],
 }
 HOST_UNITS = ["mesh_prep.cpp"]
 

@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -71,6 +72,10 @@ struct fesom_gpu_ctx {
     cudaStream_t h2d = nullptr, d2h = nullptr;
     cudaEvent_t ev_forcing = nullptr;
     std::vector<cudaEvent_t> ev_in, ev_done;
+    // tail of the tracer loop: node y coordinates (relax_zonal_temp) and work arrays
+    double *coord_y = nullptr;
+    double *tail_v = nullptr, *tail_r2c = nullptr, *tail_T = nullptr, *tail_S = nullptr, *tail_z = nullptr;
+    int tail_nbins = 0;
 };
 
 namespace {
@@ -893,6 +898,12 @@ int fesom_gpu_init(const fesom_mesh_desc *mesh, int32_t precision, int32_t max_t
     else rc = init_geom<double>(ctx, mesh, ctx->g64);
     if (rc) return rc;
     if (precision == FESOM_PREC_FP32 && (rc = init_muscl_weights(ctx, mesh))) return rc;
+    {
+        std::vector<double> y(ctx->N2);
+        for (int n = 0; n < ctx->N2; n++) y[n] = mesh->coord_nod2D[2 * (size_t)n + 1];
+        if ((rc = dalloc(ctx, (void **)&ctx->coord_y, sizeof(double) * ctx->N2))) return rc;
+        CK(cudaMemcpy(ctx->coord_y, y.data(), sizeof(double) * ctx->N2, cudaMemcpyHostToDevice));
+    }
     const size_t rs = rsize(ctx);
     if ((rc = dalloc(ctx, &ctx->uv, rs * 2 * (size_t)ctx->L1 * ctx->T2))) return rc;
     if ((rc = dalloc(ctx, &ctx->w, rs * (size_t)ctx->nl * ctx->N2))) return rc;
@@ -1397,6 +1408,76 @@ int fesom_gpu_tracer_content(fesom_gpu_ctx *ctx, double *content) {
     }
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(content, ctx->content_out, sizeof(double) * ctx->ntr, cudaMemcpyDeviceToHost, ctx->stream));
+    return wait_stream(ctx, -1);
+}
+
+int fesom_gpu_tracer_tail(fesom_gpu_ctx *ctx, int32_t ntr, const fesom_tra_cfg *cfgs, double dt,
+                          const fesom_tail_cfg *tc, const double *relax2clim, const double *Tclim, const double *Sclim,
+                          const double *ztem, double *const *values) {
+    if (!ctx || !cfgs || !tc || !values || ntr < 1) return FESOM_ERR_ARG;
+    int rc = need_fp64(ctx);
+    if (rc) return rc;
+    const bool clim = tc->clim_relax > 1.0e-8 && !tc->zonal_relax;
+    if (clim && (!relax2clim || !Tclim || !Sclim)) {
+        ctx->err = "relax_to_clim needs relax2clim, Tclim and Sclim";
+        return FESOM_ERR_ARG;
+    }
+    if (tc->zonal_relax && (!Tclim || !ztem || tc->nbins < 1 || !(tc->dy > 0.0))) {
+        ctx->err = "relax_zonal_temp needs Tclim, ztem, nbins >= 1 and dy > 0";
+        return FESOM_ERR_ARG;
+    }
+    const size_t sN = (size_t)ctx->L1 * ctx->N2;
+    if (!ctx->tail_v) {
+        if ((rc = dalloc(ctx, (void **)&ctx->tail_v, sizeof(double) * sN)) ||
+            (rc = dalloc(ctx, (void **)&ctx->tail_r2c, sizeof(double) * ctx->N2)) ||
+            (rc = dalloc(ctx, (void **)&ctx->tail_T, sizeof(double) * sN)) ||
+            (rc = dalloc(ctx, (void **)&ctx->tail_S, sizeof(double) * sN)))
+            return rc;
+    }
+    if (tc->zonal_relax && ctx->tail_nbins < tc->nbins) {
+        if (ctx->tail_z) { void *p = ctx->tail_z; dfree(ctx, p); ctx->tail_z = nullptr; }
+        if ((rc = dalloc(ctx, (void **)&ctx->tail_z, sizeof(double) * (size_t)tc->nbins * ctx->L1))) return rc;
+        ctx->tail_nbins = tc->nbins;
+    }
+    if (clim) {
+        CK(cudaMemcpyAsync(ctx->tail_r2c, relax2clim, sizeof(double) * ctx->N2, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->tail_S, Sclim, sizeof(double) * sN, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    if (clim || tc->zonal_relax) CK(cudaMemcpyAsync(ctx->tail_T, Tclim, sizeof(double) * sN, cudaMemcpyHostToDevice, ctx->stream));
+    if (tc->zonal_relax)
+        CK(cudaMemcpyAsync(ctx->tail_z, ztem, sizeof(double) * (size_t)tc->nbins * ctx->L1, cudaMemcpyHostToDevice,
+                           ctx->stream));
+    // decay constants of 14C and 39Ar (src/mod_transit.F90:49-50), factors formed on the host
+    const double k14 = 3.8561e-12, k39 = 8.1708e-11;
+    for (int t = 0; t < ntr; t++) {
+        TailArgs a{};
+        a.decay = cfgs[t].id == 14 || cfgs[t].id == 39;
+        a.decay_f = a.decay ? std::exp(-(cfgs[t].id == 14 ? k14 : k39) * dt) : 1.0;
+        a.dt = dt;
+        if (tc->zonal_relax) {
+            // relax_zonal_temp of tracer 1 runs at every iteration of the tracer loop
+            if (t == 0) {
+                a.relax = 2;
+                a.repeat = ntr;
+                a.clim = ctx->tail_T;
+                a.ztem = ctx->tail_z;
+                a.lat0 = tc->lat0;
+                a.dy = tc->dy;
+                a.tau_inv = tc->tau_inv;
+                a.nbins = tc->nbins;
+            }
+        } else if (clim && (cfgs[t].id == 1 || cfgs[t].id == 2)) {
+            a.relax = 1;
+            a.r2c = ctx->tail_r2c;
+            a.clim = cfgs[t].id == 1 ? ctx->tail_T : ctx->tail_S;
+        }
+        a.clamp = t == tc->salt_index ? 1 : (t == tc->age_index ? 2 : 0);
+        if (!a.decay && !a.relax && !a.clamp) continue;
+        CK(cudaMemcpyAsync(ctx->tail_v, values[t], sizeof(double) * sN, cudaMemcpyHostToDevice, ctx->stream));
+        launch_tracer_tail(ctx->tp, ctx->coord_y, ctx->tail_v, a, ctx->stream);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(values[t], ctx->tail_v, sizeof(double) * sN, cudaMemcpyDeviceToHost, ctx->stream));
+    }
     return wait_stream(ctx, -1);
 }
 

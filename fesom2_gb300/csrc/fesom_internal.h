@@ -160,6 +160,19 @@ void bm32_bounds(const Inst32 *, const MultiIdx &, bool wide, cudaStream_t);
 void bm32_update(const Inst32 *, const MultiIdx &, bool wide, cudaStream_t);
 void bm32_vdiff(const Inst32 *, const MultiIdx &, cudaStream_t);
 
+// tail of the tracer loop (kernels_tail.cu): one tracer's decay, relaxation and clamp
+struct TailArgs {
+    int decay;            // multiply the whole field by decay_f
+    double decay_f;
+    int relax;            // 0 none, 1 relax_to_clim (r2c, clim), 2 relax_zonal_temp (clim = Tclim, ztem)
+    int repeat;           // applications of relax_zonal_temp (once per tracer of the loop)
+    const double *r2c, *clim, *ztem;
+    double dt, lat0, dy, tau_inv;
+    int nbins;
+    int clamp;            // 0 none, 1 salinity to [3, 45], 2 age tracer >= 0
+};
+void launch_tracer_tail(const DTopo &, const double *coord_y, double *v, const TailArgs &, cudaStream_t);
+
 // launch wrappers (kernels_fp64.cu / kernels_fp32.cu)
 template <typename R>
 struct Launch {

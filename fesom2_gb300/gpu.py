@@ -87,6 +87,7 @@ _SIGS = {
     "fesom_gpu_launches_per_step": ([_P, C.POINTER(C.c_int32)], C.c_int),
     "fesom_gpu_debug_fetch": ([_P, C.c_char_p, C.c_int32, _P, C.c_size_t], C.c_int),
     "fesom_gpu_tracer_device_ptr": ([_P, C.c_int32, C.POINTER(_P), C.POINTER(_P)], C.c_int),
+    "fesom_gpu_tracer_tail": ([_P, C.c_int32, _P, C.c_double, _P, _P, _P, _P, _P, C.POINTER(_P)], C.c_int),
     "fesom_gpu_step_host_f32": ([_P, C.c_double, _P, _P, _P, _P, _P, _P, C.POINTER(_P), C.POINTER(_P),
                                  C.POINTER(_P), C.POINTER(_P)], C.c_int),
     "fesom_gpu_batch_create": ([C.POINTER(_P), C.c_int32, C.POINTER(_P)], C.c_int),
@@ -242,8 +243,9 @@ class Context:
         dh = np.zeros((N2, L1))
         dv = np.zeros((N2, L1))
         uv, w, wi, we = _c64(forcing.uv), _c64(forcing.w), _c64(forcing.w_i), _c64(forcing.w_e)
+        t64, tab64 = _c64(ttf), _c64(ttfAB)  # alive through the call
         self._chk(self.L.fesom_gpu_adv_tra(self.h, float(forcing.dt if dt is None else dt), _p(uv), _p(w), _p(wi),
-                                           _p(we), C.byref(cfg), _p(_c64(ttf)), _p(_c64(ttfAB)), _p(dh), _p(dv)))
+                                           _p(we), C.byref(cfg), _p(t64), _p(tab64), _p(dh), _p(dv)))
         return dh, dv
 
     def vdiff_impl(self, forcing, cfg: TraCfg, values, dt=None, bc=None):
@@ -293,7 +295,8 @@ class Context:
         if values.dtype == np.float32:
             self._chk(self.L.fesom_gpu_tracer_upload_f32(self.h, tr, _p(values), _p(valuesold)))
         else:
-            self._chk(self.L.fesom_gpu_tracer_upload(self.h, tr, _p(_c64(values)), _p(_c64(valuesold))))
+            v64, o64 = _c64(values), _c64(valuesold)  # alive through the call
+            self._chk(self.L.fesom_gpu_tracer_upload(self.h, tr, _p(v64), _p(o64)))
 
     def tracer_download(self, tr: int, dtype=np.float64):
         """values (nod2D, nl-1) and valuesold in the reference's layout: (nod2D, nl-1)
@@ -335,6 +338,18 @@ class Context:
             _p(f.bc_surface), mk(values_in), mk(valuesold_in), mk(values_out),
             mk(valuesold_out) if valuesold_out is not None else None))
 
+    def tracer_tail(self, cfgs, dt, tc: "TailCfg", relax2clim, Tclim, Sclim, ztem, values):
+        """Tail of the tracer loop (``fesom_gpu_tracer_tail``) on the FP64 arrays ``values`` in place."""
+        for a in values:
+            if a.dtype != np.float64 or not a.flags.c_contiguous:
+                raise ValueError("tracer arrays must be C-contiguous float64")
+        n = len(values)
+        arr = (TraCfg * n)(*cfgs)
+        vp = (_P * n)(*[a.ctypes.data for a in values])
+        keep = [_c64(relax2clim), _c64(Tclim), _c64(Sclim), _c64(ztem)]  # alive through the call
+        self._chk(self.L.fesom_gpu_tracer_tail(self.h, n, C.cast(arr, _P), float(dt), C.cast(C.pointer(tc), _P),
+                                               *[_p(a) for a in keep], vp))
+
     def launches_per_step(self) -> int:
         n = C.c_int32(0)
         self._chk(self.L.fesom_gpu_launches_per_step(self.h, C.byref(n)))
@@ -365,6 +380,19 @@ class Context:
         out = np.zeros(self.ntr)
         self._chk(self.L.fesom_gpu_tracer_content(self.h, _p(out)))
         return out
+
+
+class TailCfg(C.Structure):
+    """``fesom_tail_cfg``: decay, climatology relaxation and clamps after the tracer loop."""
+    _fields_ = [("clim_relax", C.c_double), ("salt_index", C.c_int32), ("age_index", C.c_int32),
+                ("zonal_relax", C.c_int32), ("nbins", C.c_int32), ("lat0", C.c_double), ("dy", C.c_double),
+                ("tau_inv", C.c_double)]
+
+
+def tail_cfg(clim_relax=1.0 / (10 * 3600.0 * 24), salt_index=1, age_index=-1, zonal_relax=0, nbins=100,
+             lat0=0.0, dy=1.0, tau_inv=0.0) -> TailCfg:
+    return TailCfg(float(clim_relax), int(salt_index), int(age_index), int(zonal_relax), int(nbins), float(lat0),
+                   float(dy), float(tau_inv))
 
 
 class Batch:

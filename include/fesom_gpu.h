@@ -241,6 +241,24 @@ int fesom_gpu_tracer_content(fesom_gpu_ctx *ctx, double *content);
 /* Device pointer of tracer tr's values (context precision), for zero-copy users. */
 int fesom_gpu_tracer_device_ptr(fesom_gpu_ctx *ctx, int32_t tr, void **values, void **valuesold);
 
+/* Tail of the tracer loop of solve_tracers_ale (src/oce_ale_tracer.F90:353-375, 497-525):
+ * radioactive decay of the tracers with ID 14 and 39; relax_to_clim (src/oce_tracer_mod.F90:
+ * 236-298) of the tracers with ID 1 and 2 when clim_relax > 1e-8 -- or, with zonal_relax,
+ * the Soufflet channel's relax_zonal_temp (src/toy_channel_soufflet.F90:91-121) of tracer 1,
+ * applied once per tracer of the loop as the reference does; then the salinity tracer
+ * clamped to [3, 45] and the age tracer floored at 0.  FP64 contexts, host arrays in place. */
+typedef struct fesom_tail_cfg {
+    double clim_relax;     /* namelist clim_relax (src/oce_modules.F90:46) */
+    int32_t salt_index;    /* 0-based tracer clamped to [3, 45] (the reference: tracer 2); -1: none */
+    int32_t age_index;     /* 0-based age tracer (use_age_tracer); -1: none */
+    int32_t zonal_relax;   /* 1: relax_zonal_temp instead of relax_to_clim */
+    int32_t nbins;         /* relax_zonal_temp: bins of ztem(nl-1, nbins) */
+    double lat0, dy, tau_inv;
+} fesom_tail_cfg;
+int fesom_gpu_tracer_tail(fesom_gpu_ctx *ctx, int32_t ntr, const fesom_tra_cfg *cfgs, double dt,
+                          const fesom_tail_cfg *tc, const double *relax2clim, const double *Tclim, const double *Sclim,
+                          const double *ztem, double *const *values);
+
 /* One step of an FP32 context from and to host arrays (FP32, the caller's layout), with the
  * transfers overlapped with the compute: the tracers move in launch groups
  * (fesom_gpu_set_tracers_per_launch) -- a group computes as soon as its values and previous

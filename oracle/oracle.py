@@ -64,7 +64,7 @@ def lib() -> C.CDLL:
                      "or_fill_up_dn_grad", "or_adv_tra_hor_upw1", "or_adv_tra_hor_muscl", "or_adv_tra_hor_mfct",
                      "or_adv_tra_ver_upw1", "or_adv_tra_ver_qr4c", "or_oce_tra_adv_fct",
                      "or_oce_tra_adv_flux2dtracer", "or_do_oce_adv_tra", "or_diff_ver_part_impl_ale",
-                     "or_tracer_step", "or_set_threads", "or_get_threads"):
+                     "or_tracer_step", "or_set_threads", "or_get_threads", "or_tracer_tail"):
             getattr(L, name)
         L.or_tracer_step.restype = C.c_int
         L.or_do_oce_adv_tra.restype = C.c_int
@@ -154,6 +154,30 @@ class OracleMesh:
     def diff_ver_part_impl_ale(self, forcing, values, dt=None) -> None:
         lib().or_diff_ver_part_impl_ale(C.byref(self.s), C.c_double(forcing.dt if dt is None else dt),
                                         _ptr(forcing.Kv), _ptr(forcing.bc_surface), _ptr(values))
+
+
+class TailCfg(C.Structure):
+    """or_tail_cfg: the tail of solve_tracers_ale (decay, climatology relaxation, clamps)."""
+    _fields_ = [("clim_relax", C.c_double), ("salt_index", C.c_int), ("age_index", C.c_int),
+                ("zonal_relax", C.c_int), ("nbins", C.c_int), ("lat0", C.c_double), ("dy", C.c_double),
+                ("tau_inv", C.c_double)]
+
+
+def tail_cfg(clim_relax=1.0 / (10 * 3600.0 * 24), salt_index=1, age_index=-1, zonal_relax=0, nbins=100,
+             lat0=0.0, dy=1.0, tau_inv=0.0) -> TailCfg:
+    return TailCfg(float(clim_relax), int(salt_index), int(age_index), int(zonal_relax), int(nbins), float(lat0),
+                   float(dy), float(tau_inv))
+
+
+def tracer_tail(om, ids, dt, tc: TailCfg, relax2clim, Tclim, Sclim, ztem, values) -> None:
+    """The tail of solve_tracers_ale on the list ``values`` (in place)."""
+    for a in values:
+        assert a.flags.c_contiguous and a.dtype == np.float64
+    n = len(values)
+    arr = (_P * n)(*[a.ctypes.data_as(_P) for a in values])
+    idv = np.ascontiguousarray(ids, dtype=np.int32)
+    lib().or_tracer_tail(C.byref(om.s), C.c_int(n), idv.ctypes.data_as(_P), C.c_double(dt), C.byref(tc),
+                         _ptr(relax2clim), _ptr(Tclim), _ptr(Sclim), _ptr(ztem), arr)
 
 
 def ensure_f64(forcing):

@@ -784,3 +784,80 @@ int or_tracer_step(const or_mesh *m, const or_tra_cfg *c, double dt, const doubl
     if (c->i_vert_diff) or_diff_ver_part_impl_ale(m, dt, Kv, bc_surf, values);
     return 0;
 }
+
+/* ========================================================================== */
+/* tail of solve_tracers_ale (src/oce_ale_tracer.F90:353-375, 497-525)         */
+/* ========================================================================== */
+static const double kDecay14 = 3.8561e-12, kDecay39 = 8.1708e-11; /* src/mod_transit.F90:49-50 */
+
+/* relax_to_clim (src/oce_tracer_mod.F90:236-298) for tracer values of ID id */
+static void relax_to_clim(const or_mesh *m, double dt, int id, double clim_relax, const double *relax2clim,
+                          const double *Tclim, const double *Sclim, double *values) {
+    const int L1 = m->nl - 1;
+    const double *clim = id == 1 ? Tclim : (id == 2 ? Sclim : NULL);
+    if (!(clim_relax > 1.0e-8) || !clim) return;
+    for (int n = 0; n < m->nod2D; n++) {
+        int nzmin = m->ulevels_nod2D[n], nzmax = m->nlevels_nod2D[n];
+        for (int nz = nzmin; nz <= nzmax - 1; nz++) {
+            size_t i = IX1(nz, n);
+            values[i] = values[i] + relax2clim[n] * dt * (clim[i] - values[i]);
+        }
+    }
+}
+
+/* relax_zonal_temp (src/toy_channel_soufflet.F90:91-121) */
+static void relax_zonal_temp(const or_mesh *m, double dt, const or_tail_cfg *tc, const double *Tclim,
+                             const double *ztem, double *values) {
+    const int L1 = m->nl - 1;
+    for (int n = 0; n < m->nod2D; n++) {
+        double yy = m->coord_nod2D[2 * n + 1] - tc->lat0, a = 0.0;
+        int nn, nn1;
+        if (yy < tc->dy / 2.0) {
+            nn = 1;
+            nn1 = 1;
+        } else {
+            nn = (int)floor(yy / tc->dy - 0.5) + 1;
+            if (nn > tc->nbins) nn = tc->nbins;  /* outside the table (the reference reads past it) */
+            nn1 = nn + 1;
+            if (nn1 > tc->nbins) nn1 = nn;
+            a = yy / tc->dy + 0.5 - nn;
+        }
+        for (int nz = 1; nz <= m->nlevels_nod2D[n] - 1; nz++) {
+            double Tzon = (1.0 - a) * ztem[(nz - 1) + (size_t)(nn - 1) * L1] + a * ztem[(nz - 1) + (size_t)(nn1 - 1) * L1];
+            size_t i = IX1(nz, n);
+            values[i] = values[i] + dt * tc->tau_inv * (Tclim[i] - Tzon);
+        }
+    }
+}
+
+void or_tracer_tail(const or_mesh *m, int ntr, const int *ids, double dt, const or_tail_cfg *tc,
+                    const double *relax2clim, const double *Tclim, const double *Sclim, const double *ztem,
+                    double **values) {
+    const int L1 = m->nl - 1;
+    const size_t N = (size_t)L1 * (size_t)m->nod2D;
+    for (int t = 0; t < ntr; t++) {
+        /* radioactive decay of the whole field (:355-356) */
+        if (ids[t] == 14 || ids[t] == 39) {
+            const double f = exp(-(ids[t] == 14 ? kDecay14 : kDecay39) * dt);
+            for (size_t i = 0; i < N; i++) values[t][i] = values[t][i] * f;
+        }
+        if (tc->zonal_relax) relax_zonal_temp(m, dt, tc, Tclim, ztem, values[0]);
+        else relax_to_clim(m, dt, ids[t], tc->clim_relax, relax2clim, Tclim, Sclim, values[t]);
+    }
+    for (int k = 0; k < 2; k++) {
+        int t = k == 0 ? tc->salt_index : tc->age_index;
+        if (t < 0 || t >= ntr) continue;
+        for (int n = 0; n < m->nod2D; n++) {
+            int nzmax = m->nlevels_nod2D[n] - 1, nzmin = m->ulevels_nod2D[n];
+            for (int nz = nzmin; nz <= nzmax; nz++) {
+                double *v = &values[t][IX1(nz, n)];
+                if (k == 0) {
+                    if (*v > 45.0) *v = 45.0;
+                    if (*v < 3.0) *v = 3.0;
+                } else if (*v < 0.0) {
+                    *v = 0.0;
+                }
+            }
+        }
+    }
+}

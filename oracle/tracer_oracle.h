@@ -120,6 +120,23 @@ int or_tracer_step(const or_mesh *m, const or_tra_cfg *c, double dt, const doubl
                    const double *WI, const double *WE, const double *Kv, const double *bc_surf,
                    double *values, double *valuesAB, double *valuesold, or_work *w);
 
+/* Tail of the tracer loop of solve_tracers_ale (src/oce_ale_tracer.F90:353-375) and of the
+ * routine (:497-525): radioactive decay of IDs 14 and 39 (decay constants of
+ * src/mod_transit.F90:49-50), relax_to_clim (src/oce_tracer_mod.F90:236-298) or, in the
+ * Soufflet channel, relax_zonal_temp of tracer 1 (src/toy_channel_soufflet.F90:91-121) at
+ * every tracer iteration, then the salinity clamp to [3, 45] and the age-tracer floor. */
+typedef struct or_tail_cfg {
+    double clim_relax;
+    int salt_index;   /* 0-based, -1: none */
+    int age_index;    /* 0-based, -1: none */
+    int zonal_relax;  /* 1: relax_zonal_temp of tracer 0 instead of relax_to_clim */
+    int nbins;        /* bins of ztem (ztem(nl-1, nbins)) */
+    double lat0, dy, tau_inv;
+} or_tail_cfg;
+void or_tracer_tail(const or_mesh *m, int ntr, const int *ids, double dt, const or_tail_cfg *tc,
+                    const double *relax2clim, const double *Tclim, const double *Sclim, const double *ztem,
+                    double **values);
+
 #ifdef __cplusplus
 }
 #endif

@@ -227,3 +227,56 @@ def test_qr4c_interior_flux_by_hand(channel_seamount):
     Tmean = (w + abs(w)) * Tm1 + (w - abs(w)) * Tm2
     want = (-0.5 * (1 - pv) * Tmean - pv * (0.5 * (Tm1 + Tm2)) * w) * mesh.area[n, nz - 1]
     assert flux[n, nz - 1] == want
+
+
+def _tail_inputs(mesh, ntr, seed):
+    rng = np.random.default_rng(seed)
+    L1 = mesh.nl - 1
+    vals = [np.ascontiguousarray(30.0 + 20.0 * rng.standard_normal((mesh.nod2D, L1))) for _ in range(ntr)]
+    vals[-1][:] = 0.2 * rng.standard_normal((mesh.nod2D, L1))  # age tracer with negatives
+    r2c = np.ascontiguousarray(rng.uniform(0.0, 1e-5, mesh.nod2D))
+    Tclim = np.ascontiguousarray(10.0 + rng.standard_normal((mesh.nod2D, L1)))
+    Sclim = np.ascontiguousarray(35.0 + rng.standard_normal((mesh.nod2D, L1)))
+    ztem = np.ascontiguousarray(rng.standard_normal((12, L1)))
+    return vals, r2c, Tclim, Sclim, ztem
+
+
+def test_oracle_tail_matches_numpy(channel_small):
+    """Decay, relax_to_clim and the clamps written out in numpy from the reference's formulas."""
+    mesh = channel_small
+    ids = [1, 2, 14, 39, 101]
+    vals, r2c, Tclim, Sclim, ztem = _tail_inputs(mesh, len(ids), 3)
+    dt = 600.0
+    tc = O.tail_cfg(salt_index=1, age_index=4)
+    got = [v.copy() for v in vals]
+    O.tracer_tail(O.OracleMesh(mesh), ids, dt, tc, r2c, Tclim, Sclim, ztem, got)
+    want = [v.copy() for v in vals]
+    lev = np.arange(mesh.nl - 1)[None, :] + 1
+    wet = (lev >= mesh.ulevels_nod2D[:, None]) & (lev <= mesh.nlevels_nod2D[:, None] - 1)
+    want[2] = want[2] * np.exp(-3.8561e-12 * dt)
+    want[3] = want[3] * np.exp(-8.1708e-11 * dt)
+    for k, clim in ((0, Tclim), (1, Sclim)):
+        upd = want[k] + r2c[:, None] * dt * (clim - want[k])
+        want[k] = np.where(wet, upd, want[k])
+    want[1] = np.where(wet, np.minimum(np.maximum(np.minimum(want[1], 45.0), 3.0), 45.0), want[1])
+    want[4] = np.where(wet & (want[4] < 0.0), 0.0, want[4])
+    for k in range(len(ids)):
+        assert np.array_equal(got[k], want[k]), k
+
+
+def test_oracle_tail_zonal_relax_repeats_per_tracer(channel_small):
+    """relax_zonal_temp acts on tracer 1 once per tracer of the loop (the reference calls it
+    inside the loop with tracers%data(1)): three tracers give three increments."""
+    mesh = channel_small
+    vals, r2c, Tclim, Sclim, ztem = _tail_inputs(mesh, 3, 4)
+    y = mesh.coord_nod2D[:, 1]
+    tc = O.tail_cfg(salt_index=-1, age_index=-1, zonal_relax=1, nbins=12, lat0=float(y.min()),
+                    dy=float((y.max() - y.min()) / 12), tau_inv=1.0 / 86400.0)
+    got = [v.copy() for v in vals]
+    O.tracer_tail(O.OracleMesh(mesh), [1, 2, 101], 600.0, tc, r2c, Tclim, Sclim, ztem, got)
+    assert np.array_equal(got[1], vals[1]) and np.array_equal(got[2], vals[2])
+    one = [vals[0].copy()]
+    O.tracer_tail(O.OracleMesh(mesh), [1], 600.0, tc, r2c, Tclim, Sclim, ztem, one)
+    inc = one[0] - vals[0]
+    assert np.allclose(got[0] - vals[0], 3 * inc, rtol=1e-12, atol=1e-12)
+    assert np.abs(inc).max() > 0
