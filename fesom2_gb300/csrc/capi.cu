@@ -59,6 +59,7 @@ struct fesom_gpu_ctx {
     float *VF = nullptr;
     VFactors vfac{};
     float *LO32 = nullptr, *ADv32 = nullptr, *ADh32 = nullptr;
+    float *HD32 = nullptr;  // horizontal diffusion flux per edge-layer and tracer of a launch group
     float2 *R2 = nullptr, *TB2 = nullptr;
     MusclW mw{};
     cudaGraphExec_t gexec32[3] = {nullptr, nullptr, nullptr};
@@ -73,6 +74,7 @@ struct fesom_gpu_ctx {
     cudaEvent_t ev_forcing = nullptr;
     std::vector<cudaEvent_t> ev_in, ev_done;
     // tail of the tracer loop: node y coordinates (relax_zonal_temp) and work arrays
+    void *Ki = nullptr;        // horizontal diffusivity (context precision), null: none
     double *coord_y = nullptr;
     double *tail_v = nullptr, *tail_r2c = nullptr, *tail_T = nullptr, *tail_S = nullptr, *tail_z = nullptr;
     int tail_nbins = 0;
@@ -438,7 +440,7 @@ int alloc_state(fesom_gpu_ctx *ctx, int ntr, int ab_max) {
     if ((rc = dalloc(ctx, &ctx->bc, rs * (size_t)ctx->N2 * ntr))) return rc;
     CK(cudaMemset(ctx->bc, 0, rs * (size_t)ctx->N2 * ntr));
     if ((rc = dalloc(ctx, (void **)&ctx->d_cfg, sizeof(DCfg) * ntr))) return rc;
-    const size_t per_tracer = rs * (4 * sN + sNI + sT + 2 * sE);
+    const size_t per_tracer = rs * (5 * sN + sNI + sT + 2 * sE);
     size_t fr = 0, tot = 0;
     CK(cudaMemGetInfo(&fr, &tot));
     int g = (int)std::min<size_t>((size_t)ntr, std::max<size_t>(1, (size_t)(0.85 * fr) / per_tracer));
@@ -452,9 +454,10 @@ int alloc_state(fesom_gpu_ctx *ctx, int ntr, int ab_max) {
     if ((rc = dalloc(ctx, &ctx->ADv, rs * sNI * g))) return rc;
     if ((rc = dalloc(ctx, &ctx->bmax, rs * sN * g))) return rc;
     if ((rc = dalloc(ctx, &ctx->bmin, rs * sN * g))) return rc;
-    // the advective increments are outputs of the single-tracer drop-in only
+    // the advective increments are outputs of the single-tracer drop-in only; in a step
+    // dttf_v holds the explicit vertical diffusion increments of every tracer of a group
     if ((rc = dalloc(ctx, &ctx->dttf_h, rs * sN))) return rc;
-    if ((rc = dalloc(ctx, &ctx->dttf_v, rs * sN))) return rc;
+    if ((rc = dalloc(ctx, &ctx->dttf_v, rs * sN * g))) return rc;
     ctx->ntr = ntr;
     ctx->ab_max = ab_max;
     ctx->state_ready = true;
@@ -483,6 +486,11 @@ DTracers<R> group_view(fesom_gpu_ctx *ctx, int t0, int nt) {
     v.dttf_v = (R *)ctx->dttf_v;
     v.cfg = ctx->d_cfg + t0;
     v.status = ctx->status;
+    // diff_tracers_ale: the edge diffusion fluxes reuse FLO (dead after the LO stage), the
+    // explicit vertical increments reuse dttf_v (unused by the step)
+    v.Ki = (const R *)ctx->Ki;
+    v.HD = ctx->Ki ? (R *)ctx->FLO : nullptr;
+    v.VX = (R *)ctx->dttf_v;
     return v;
 }
 
@@ -525,10 +533,10 @@ void free_graphs32(fesom_gpu_ctx *ctx) {
 int alloc_state32(fesom_gpu_ctx *ctx, int ntr, int ab) {
     const size_t sN = (size_t)ctx->L1 * ctx->N2, sNI = (size_t)ctx->nl * ctx->N2, sE = (size_t)ctx->L1 * ctx->E2;
     void *old[] = {ctx->Bf[0], ctx->Bf[1], ctx->Bf[2], ctx->VF, ctx->vfac.a, ctx->vfac.c, ctx->vfac.inv, ctx->vfac.cp,
-                   ctx->LO32, ctx->ADv32, ctx->ADh32, ctx->R2, ctx->TB2, ctx->d_cfg, ctx->bc};
+                   ctx->LO32, ctx->ADv32, ctx->ADh32, ctx->R2, ctx->TB2, ctx->d_cfg, ctx->bc, ctx->HD32};
     for (void *b : old) { void *p = b; dfree(ctx, p); }
     ctx->Bf[0] = ctx->Bf[1] = ctx->Bf[2] = nullptr;
-    ctx->VF = ctx->LO32 = ctx->ADv32 = ctx->ADh32 = nullptr;
+    ctx->VF = ctx->LO32 = ctx->ADv32 = ctx->ADh32 = ctx->HD32 = nullptr;
     ctx->R2 = ctx->TB2 = nullptr;
     ctx->vfac = VFactors{};
     ctx->d_cfg = nullptr;
@@ -545,7 +553,8 @@ int alloc_state32(fesom_gpu_ctx *ctx, int ntr, int ab) {
     float **fac[] = {&ctx->vfac.a, &ctx->vfac.c, &ctx->vfac.inv, &ctx->vfac.cp};
     for (float **f : fac)
         if ((rc = dalloc(ctx, (void **)f, 4 * sN))) return rc;
-    const size_t per_tracer = 4 * (5 * sN + sNI + sE);  // LO, (R+,R-), bounds, ADv, ADh
+    // LO, (R+,R-), bounds, ADv, ADh (+ the horizontal diffusion fluxes)
+    const size_t per_tracer = 4 * (5 * sN + sNI + sE + (ctx->Ki ? sE : 0));
     size_t fr = 0, tot = 0;
     CK(cudaMemGetInfo(&fr, &tot));
     // at most 64 tracers per launch: the kernels take per-tracer switches as 64-bit masks
@@ -557,6 +566,7 @@ int alloc_state32(fesom_gpu_ctx *ctx, int ntr, int ab) {
     if ((rc = dalloc(ctx, (void **)&ctx->ADh32, 4 * sE * g))) return rc;
     if ((rc = dalloc(ctx, (void **)&ctx->R2, 8 * sN * g))) return rc;
     if ((rc = dalloc(ctx, (void **)&ctx->TB2, 8 * sN * g))) return rc;
+    if (ctx->Ki && (rc = dalloc(ctx, (void **)&ctx->HD32, 4 * sE * g))) return rc;
     // created here, not on first use: a first step may run inside a stream capture
     if (!ctx->side) {
         CK(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
@@ -591,11 +601,17 @@ B32View view32(fesom_gpu_ctx *ctx, int t0, int nt) {
     v.TB = ctx->TB2;
     v.cfg = ctx->d_cfg + t0;
     v.status = ctx->status;
-    v.fct_mask = v.ivd_mask = 0;
+    v.fct_mask = v.ivd_mask = v.diff_mask = 0;
+    v.Ki = (const float *)ctx->Ki;
+    v.HD = ctx->Ki ? ctx->HD32 : nullptr;
+    v.Kv = (const float *)ctx->Kv;
+    v.sF = ctx->N2;
+    v.fsurf = ctx->bc ? (const float *)ctx->bc + (size_t)t0 * ctx->N2 : nullptr;
     for (int t = 0; t < nt; t++) {
         const fesom_tra_cfg &c = ctx->cfgs[t0 + t];
         if (c.adv_lim == FESOM_ADV_LIM_FCT) v.fct_mask |= 1ull << t;
         if (c.i_vert_diff) v.ivd_mask |= 1ull << t;
+        if (ctx->Ki || !c.i_vert_diff) v.diff_mask |= 1ull << t;
         v.hor[t] = (signed char)c.adv_hor;
         v.ver[t] = (signed char)c.adv_ver;
         v.ph[t] = (float)c.adv_ph;
@@ -620,6 +636,9 @@ B32View sub32(const B32View &B, int s0, int ns) {
     v.cfg += s0;
     v.fct_mask = B.fct_mask >> s0;
     v.ivd_mask = B.ivd_mask >> s0;
+    v.diff_mask = B.diff_mask >> s0;
+    if (v.HD) v.HD += s0 * B.sE;
+    if (v.fsurf) v.fsurf += s0 * B.sF;
     for (int t = 0; t < ns; t++) {
         v.hor[t] = B.hor[s0 + t];
         v.ver[t] = B.ver[s0 + t];
@@ -659,19 +678,24 @@ int enqueue_step(fesom_gpu_ctx *ctx, double dt, StageTimer *tm = nullptr) {
         const int nt = std::min(ctx->group, ctx->ntr - t0);
         DTracers<R> tr = group_view<R>(ctx, t0, nt);
         DForcing<R> f = forcing_view<R>(ctx, t0);
-        bool any_fct = false, any_ho = false, any_vd = false;
+        bool any_fct = false, any_ho = false, any_vd = false, any_ex = false;
         int ab = 2;
         for (int t = t0; t < t0 + nt; t++) {
             any_fct |= ctx->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
             any_ho |= ctx->cfgs[t].adv_hor != FESOM_ADV_HOR_UPW1;
             any_vd |= ctx->cfgs[t].i_vert_diff != 0;
+            any_ex |= ctx->cfgs[t].i_vert_diff == 0;
             ab = std::max(ab, (int)ctx->cfgs[t].ab_order);
         }
         // all tracers of a group share the valuesold depth of the context
         STAGE(0, Launch<R>::ab(ctx->tp, tr, ctx->ab_max, ctx->stream));
-        if (any_ho) STAGE(1, Launch<R>::trxy(ctx->tp, g, tr, ctx->stream));
+        if (any_ho || ctx->Ki) STAGE(1, Launch<R>::trxy(ctx->tp, g, tr, ctx->stream));
         STAGE(2, Launch<R>::edge_flux(ctx->tp, g, f, tr, any_fct, ctx->stream));
         STAGE(3, Launch<R>::node_lo(ctx->tp, g, f, tr, dt, any_fct, ctx->stream));
+        // diff_tracers_ale: horizontal diffusion fluxes, explicit vertical increments (both from
+        // the values before the update)
+        if (ctx->Ki) STAGE(2, Launch<R>::hdiff(ctx->tp, g, tr, ctx->stream));
+        if (any_ex) STAGE(7, Launch<R>::vexpl(ctx->tp, g, f, tr, dt, tr.VX, 0, 0, ctx->stream));
         if (any_fct) {
             STAGE(4, Launch<R>::bounds(ctx->tp, g, tr, ctx->stream));
             STAGE(5, Launch<R>::rpm(ctx->tp, g, tr, dt, ctx->stream));
@@ -713,6 +737,10 @@ int enqueue_group32(fesom_gpu_ctx *ctx, double dt, int t0, int nt, StageTimer *t
     for (int t = t0; t < t0 + nt; t++) any_fct |= ctx->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
     STAGE(10, b32_lo_ad(ctx->tp, g, fg, B, ctx->VF, dt, ctx->stream));
     STAGE(2, b32_ho(ctx->tp, g, B, ctx->mw, ctx->VF, ctx->stream));
+    // diff_tracers_ale from the values before the update; the increment waits in Tnew (the
+    // oldest level, read by lo_ad and ho only) for the update to add it after the limiter
+    if (B.Ki) STAGE(2, b32_hdiff(ctx->tp, g, B, ctx->stream));
+    if (B.diff_mask) STAGE(7, b32_diff(ctx->tp, g, B, dt, ctx->stream));
     if (any_fct) {
         const int bg = FESOM_BOUNDS_GROUP > 0 ? FESOM_BOUNDS_GROUP : nt;
         for (int s0 = 0; s0 < nt; s0 += bg)
@@ -758,7 +786,10 @@ int launches_per_step(fesom_gpu_ctx *ctx) {
             // edges); vdiff
             const int wide = ctx->tp.n_wide ? 2 : 1;
             const int bg = FESOM_BOUNDS_GROUP > 0 ? FESOM_BOUNDS_GROUP : nt;
-            n += wide * (2 + (any_fct ? (nt + bg - 1) / bg : 0)) + (ctx->mw.n_items ? 2 : 1) + (grp_vd ? 1 : 0);
+            bool grp_diff = ctx->Ki != nullptr;
+            for (int t = t0; t < t0 + nt; t++) grp_diff |= ctx->cfgs[t].i_vert_diff == 0;
+            n += wide * (2 + (any_fct ? (nt + bg - 1) / bg : 0) + (grp_diff ? 1 : 0)) + (ctx->mw.n_items ? 2 : 1) +
+                 (grp_vd ? 1 : 0) + (ctx->Ki ? 1 : 0);
         }
         return n;
     }
@@ -770,7 +801,10 @@ int launches_per_step(fesom_gpu_ctx *ctx) {
             any_ho |= ctx->cfgs[t].adv_hor != FESOM_ADV_HOR_UPW1;
             any_vd |= ctx->cfgs[t].i_vert_diff != 0;
         }
-        n += 4 + (any_ho ? 1 : 0) + (any_fct ? 2 : 0) + (any_vd ? 1 : 0);
+        bool any_ex = false;
+        for (int t = t0; t < t0 + nt; t++) any_ex |= ctx->cfgs[t].i_vert_diff == 0;
+        n += 4 + ((any_ho || ctx->Ki) ? 1 : 0) + (any_fct ? 2 : 0) + (any_vd ? 1 : 0) + (ctx->Ki ? 1 : 0) +
+             (any_ex ? 1 : 0);
     }
     return n;
 }
@@ -1411,6 +1445,71 @@ int fesom_gpu_tracer_content(fesom_gpu_ctx *ctx, double *content) {
     return wait_stream(ctx, -1);
 }
 
+int fesom_gpu_set_hdiff(fesom_gpu_ctx *ctx, const double *Ki) {
+    if (!ctx) return FESOM_ERR_ARG;
+    if (!Ki) {
+        if (ctx->Ki) { void *p = ctx->Ki; dfree(ctx, p); ctx->Ki = nullptr; }
+        if (ctx->HD32) { void *p = ctx->HD32; dfree(ctx, p); ctx->HD32 = nullptr; }
+    } else {
+        int rc;
+        const size_t sN = (size_t)ctx->L1 * ctx->N2;
+        if (!ctx->Ki && (rc = dalloc(ctx, &ctx->Ki, rsize(ctx) * sN))) return rc;
+        if ((rc = put(ctx, ctx->Ki, Ki, sN))) return rc;
+        // the FP32 form keeps the edge fluxes of a launch group apart from the advective ones
+        if (ctx->prec == FESOM_PREC_FP32 && ctx->state_ready && !ctx->HD32 &&
+            (rc = dalloc(ctx, (void **)&ctx->HD32, 4 * (size_t)ctx->L1 * ctx->E2 * ctx->group_cap)))
+            return rc;
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
+    free_graphs32(ctx);
+    return FESOM_OK;
+}
+
+int fesom_gpu_diff_hor(fesom_gpu_ctx *ctx, double dt, const double *Ki, const double *values, double *del_ttf) {
+    if (!ctx || !Ki || !values || !del_ttf) return FESOM_ERR_ARG;
+    fesom_tra_cfg cfg{};
+    cfg.adv_hor = FESOM_ADV_HOR_MUSCL;
+    cfg.ab_order = 2;
+    int rc = need_fp64(ctx);
+    if (rc || (rc = ensure_one(ctx, &cfg))) return rc;
+    const size_t sN = (size_t)ctx->L1 * ctx->N2;
+    if (!ctx->tail_v && (rc = dalloc(ctx, (void **)&ctx->tail_v, sizeof(double) * sN))) return rc;
+    DTracers<double> tr = group_view<double>(ctx, 0, 1);
+    tr.Ki = ctx->tail_v;
+    tr.HD = (double *)ctx->FLO;
+    if ((rc = put(ctx, ctx->tail_v, Ki, sN)) || (rc = put(ctx, tr.T, values, sN)) ||
+        (rc = put(ctx, tr.dttf_h, del_ttf, sN)))
+        return rc;
+    Launch<double>::trxy(ctx->tp, ctx->g64, tr, ctx->stream);
+    Launch<double>::hdiff(ctx->tp, ctx->g64, tr, ctx->stream);
+    Launch<double>::hdiff_gather(ctx->tp, ctx->g64, tr, dt, tr.dttf_h, ctx->stream);
+    CK(cudaGetLastError());
+    if ((rc = get(ctx, del_ttf, tr.dttf_h, sN))) return rc;
+    return wait_stream(ctx, -1);
+}
+
+int fesom_gpu_diff_ver_expl(fesom_gpu_ctx *ctx, double dt, const double *Kv, const double *flux_surf,
+                            const double *values, double *del_ttf) {
+    if (!ctx || !Kv || !values || !del_ttf) return FESOM_ERR_ARG;
+    fesom_tra_cfg cfg{};
+    cfg.ab_order = 2;
+    int rc = need_fp64(ctx);
+    if (rc || (rc = ensure_one(ctx, &cfg))) return rc;
+    const size_t sN = (size_t)ctx->L1 * ctx->N2;
+    DTracers<double> tr = group_view<double>(ctx, 0, 1);
+    if ((rc = put(ctx, ctx->Kv, Kv, (size_t)ctx->nl * ctx->N2)) || (rc = put(ctx, tr.T, values, sN)) ||
+        (rc = put(ctx, tr.dttf_h, del_ttf, sN)))
+        return rc;
+    if (flux_surf) CK(cudaMemcpyAsync(ctx->bc, flux_surf, sizeof(double) * ctx->N2, cudaMemcpyHostToDevice, ctx->stream));
+    else CK(cudaMemsetAsync(ctx->bc, 0, sizeof(double) * ctx->N2, ctx->stream));
+    DForcing<double> f = forcing_view<double>(ctx, 0);
+    Launch<double>::vexpl(ctx->tp, ctx->g64, f, tr, dt, tr.dttf_h, 1, 1, ctx->stream);
+    CK(cudaGetLastError());
+    if ((rc = get(ctx, del_ttf, tr.dttf_h, sN))) return rc;
+    return wait_stream(ctx, -1);
+}
+
 int fesom_gpu_tracer_tail(fesom_gpu_ctx *ctx, int32_t ntr, const fesom_tra_cfg *cfgs, double dt,
                           const fesom_tail_cfg *tc, const double *relax2clim, const double *Tclim, const double *Sclim,
                           const double *ztem, double *const *values) {
@@ -1596,7 +1695,7 @@ struct fesom_gpu_batch {
     double d_dt = -1.0;
     MultiIdx ix_e{}, ix_vfb{}, ix_n{}, ix_w{}, ix_it{};
     int maxL1 = 0;
-    bool any_vd = false, any_fct = false;
+    bool any_vd = false, any_fct = false, any_hd = false, any_diff = false;
     cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};
     double g_dt[3] = {0.0, 0.0, 0.0};
     std::string err;
@@ -1653,6 +1752,11 @@ void enqueue_batch_step(fesom_gpu_batch *b, cudaStream_t s) {
     bm32_lo_ad(I, b->ix_n, false, s);
     if (wide) bm32_lo_ad(I, b->ix_w, true, s);
     bm32_ho(I, b->ix_e, b->ix_it, s);
+    if (b->any_hd) bm32_hdiff(I, b->ix_e, s);
+    if (b->any_diff) {
+        bm32_diff(I, b->ix_n, false, s);
+        if (wide) bm32_diff(I, b->ix_w, true, s);
+    }
     if (b->any_fct) {
         bm32_bounds(I, b->ix_n, false, s);
         if (wide) bm32_bounds(I, b->ix_w, true, s);
@@ -1692,7 +1796,10 @@ int fesom_gpu_batch_create(fesom_gpu_ctx *const *ctxs, int32_t n, fesom_gpu_batc
         for (int t = 0; t < c->ntr; t++) {
             b->any_vd |= c->cfgs[t].i_vert_diff != 0;
             b->any_fct |= c->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
+            b->any_diff |= c->cfgs[t].i_vert_diff == 0;
         }
+        b->any_hd |= c->Ki != nullptr;
+        b->any_diff |= c->Ki != nullptr;
         b->maxL1 = std::max(b->maxL1, c->L1);
         b->inst.push_back(c);
         ce.push_back(c->E2);
@@ -1768,7 +1875,8 @@ int fesom_gpu_batch_launches_per_step(fesom_gpu_batch *b, int32_t *launches) {
     if (!b || !launches) return FESOM_ERR_ARG;
     const bool wide = b->ix_w.start[b->ix_w.n] > 0;
     const int k = wide ? 2 : 1;
-    int n = 1 + (b->any_vd ? 2 : 0) + k * (2 + (b->any_fct ? 1 : 0)) + 1 + (b->ix_it.start[b->ix_it.n] ? 1 : 0);
+    int n = 1 + (b->any_vd ? 2 : 0) + k * (2 + (b->any_fct ? 1 : 0) + (b->any_diff ? 1 : 0)) + 1 +
+            (b->ix_it.start[b->ix_it.n] ? 1 : 0) + (b->any_hd ? 1 : 0);
     *launches = n;
     return FESOM_OK;
 }

@@ -76,6 +76,9 @@ struct DTracers {
     R *dttf_h, *dttf_v;  // advective increments (drop-in outputs)
     const DCfg *cfg;
     unsigned *status;
+    const R *Ki;         // horizontal diffusivity (nl-1 per node), null: no horizontal diffusion
+    R *HD;               // horizontal diffusion flux per edge-layer (diff_part_hor_redi's c)
+    R *VX;               // explicit vertical diffusion increment per node-layer
 };
 
 // FP32 batched form (kernels_fp32_batched.cu): one step's view of the tracer state.
@@ -98,6 +101,15 @@ struct B32View {
     // per-tracer schemes in the kernel parameters (constant bank), at most 64 tracers
     signed char hor[64], ver[64];
     float ph[64], pv[64];
+    // diffusion of diff_tracers_ale: bit t of diff_mask: tracer t gets horizontal (Ki set) or
+    // explicit vertical (no implicit diffusion) terms; k32_diff parks their increment to T* in
+    // Tnew and the update adds it after the FCT clamp
+    unsigned long long diff_mask;
+    const float *Ki;   // horizontal diffusivity, nl-1 per node; null: none
+    float *HD;         // horizontal diffusion flux per edge-layer
+    const float *Kv;   // vertical diffusivity (explicit part), nl per node
+    const float *fsurf;  // surface flux per tracer and node (explicit vertical diffusion)
+    size_t sF;           // tracer stride of fsurf (nodes)
 };
 // Node degree bound of the FP32 form (the node's edge list is staged per warp)
 constexpr int kMaxDeg = 16;
@@ -130,6 +142,8 @@ void b32_lo_ad(const DTopo &, const DGeom<float> &, const DForcing<float> &, con
                double dt, cudaStream_t);
 void b32_ho(const DTopo &, const DGeom<float> &, const B32View &, const MusclW &, const float *VF, cudaStream_t);
 void b32_bounds(const DTopo &, const DGeom<float> &, const B32View &, double dt, cudaStream_t);
+void b32_hdiff(const DTopo &, const DGeom<float> &, const B32View &, cudaStream_t);
+void b32_diff(const DTopo &, const DGeom<float> &, const B32View &, double dt, cudaStream_t);
 void b32_update(const DTopo &, const DGeom<float> &, const B32View &, double dt, cudaStream_t);
 void b32_vdiff(const DTopo &, const DForcing<float> &, const B32View &, const VFactors &, cudaStream_t);
 
@@ -159,6 +173,8 @@ void bm32_ho(const Inst32 *, const MultiIdx &edges, const MultiIdx &items, cudaS
 void bm32_bounds(const Inst32 *, const MultiIdx &, bool wide, cudaStream_t);
 void bm32_update(const Inst32 *, const MultiIdx &, bool wide, cudaStream_t);
 void bm32_vdiff(const Inst32 *, const MultiIdx &, cudaStream_t);
+void bm32_hdiff(const Inst32 *, const MultiIdx &edges, cudaStream_t);
+void bm32_diff(const Inst32 *, const MultiIdx &nodes, bool wide, cudaStream_t);
 
 // tail of the tracer loop (kernels_tail.cu): one tracer's decay, relaxation and clamp
 struct TailArgs {
@@ -189,6 +205,13 @@ struct Launch {
                       double *scratch, cudaStream_t);
     static void content(const DTopo &, const DGeom<R> &, const DTracers<R> &, double *partials, int nblk,
                         double *out, cudaStream_t);
+    // diff_part_hor_redi: edge fluxes into tr.HD; hdiff_gather adds them to del (ascending edges)
+    static void hdiff(const DTopo &, const DGeom<R> &, DTracers<R> &, cudaStream_t);
+    static void hdiff_gather(const DTopo &, const DGeom<R> &, DTracers<R> &, double dt, R *del, cudaStream_t);
+    // diff_ver_part_expl_ale: increments of the tracers without implicit vertical diffusion (or of
+    // every tracer with all != 0) into out (add == 0) or added to out (add != 0)
+    static void vexpl(const DTopo &, const DGeom<R> &, const DForcing<R> &, DTracers<R> &, double dt, R *out,
+                      int all, int add, cudaStream_t);
 };
 
 }  // namespace fesom

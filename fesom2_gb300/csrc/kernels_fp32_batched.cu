@@ -786,6 +786,8 @@ __device__ __forceinline__ void update_node(const DTopo &tp, const DGeom<float> 
                     if (fabsf(vc - val) > 1e-5f * (tb.x - tb.y) + 1e-6f * fabsf(vc)) atomicOr(B.status, 2u);
                     val = vc;
                 }
+                // the diffusion increment k32_diff parked in Tnew (the limiter acts on advection only)
+                if ((B.diff_mask >> t) & 1ull) val += B.Tnew[to + i];
                 B.Tnew[to + i] = val;
                 if (!isfinite(val)) atomicOr(B.status, 1u);
             }
@@ -812,6 +814,153 @@ __global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_UPDATE)
 k32_update(DTopo tp, DGeom<float> g, B32View B, float dt) {
     __shared__ WEdges Se[kWB];
     update_unit<WIDE>(tp, g, B, dt, blockIdx.x * kWB + (threadIdx.x >> 5), Se);
+}
+
+// ---------------------------------------------------------------------------
+// diffusion of diff_tracers_ale (oce_ale_tracer.F90:560-772) in the FP32 form
+// ---------------------------------------------------------------------------
+// k32_hdiff: diff_part_hor_redi (:1526-1689, Redi off) flux c of every edge-layer from the
+// element gradients of the current values: segments A/D (element 1), B/E (element 2), C (both)
+__device__ __forceinline__ void hdiff_edge32(const DTopo &tp, const DGeom<float> &g, const B32View &B, int e) {
+    const int lane = threadIdx.x & 31;
+    if (e >= tp.E2 || !B.Ki) return;
+    const int L1 = tp.L1;
+    const int el1 = tp.e_t1[e], el2 = tp.e_t2[e], n1 = tp.e_n1[e], n2 = tp.e_n2[e];
+    const int nl1 = tp.t_nlev[el1] - 1, ul1 = tp.t_ulev[el1];
+    int nl2 = 0, ul2 = 0;
+    const float dX1 = g.ecd[4 * (size_t)e], dY1 = g.ecd[4 * (size_t)e + 1];
+    float dX2 = 0.f, dY2 = 0.f;
+    const int a0 = tp.t_n[3 * el1], a1 = tp.t_n[3 * el1 + 1], a2 = tp.t_n[3 * el1 + 2];
+    const float *gs1 = g.gs + 6 * (size_t)el1;
+    int b0 = a0, b1 = a1, b2 = a2;
+    const float *gs2 = gs1;
+    if (el2 >= 0) {
+        nl2 = tp.t_nlev[el2] - 1;
+        ul2 = tp.t_ulev[el2];
+        dX2 = g.ecd[4 * (size_t)e + 2];
+        dY2 = g.ecd[4 * (size_t)e + 3];
+        b0 = tp.t_n[3 * el2];
+        b1 = tp.t_n[3 * el2 + 1];
+        b2 = tp.t_n[3 * el2 + 2];
+        gs2 = g.gs + 6 * (size_t)el2;
+    }
+    const float p0 = gs1[0], p1 = gs1[1], p2 = gs1[2], p3 = gs1[3], p4 = gs1[4], p5 = gs1[5];
+    const float q0 = gs2[0], q1 = gs2[1], q2 = gs2[2], q3 = gs2[3], q4 = gs2[4], q5 = gs2[5];
+    const int nl12 = min(nl1, nl2), ul12 = max(ul1, ul2);
+    for (int nz0 = tp.e_lo[e]; nz0 <= tp.e_hi[e]; nz0 += 32) {
+        const int nz = nz0 + lane;
+        if (nz > tp.e_hi[e]) continue;
+        int seg = 0;
+        if (nz >= ul1 && nz <= ul12 - 1) seg = 1;
+        else if (ul2 > 0 && nz >= ul2 && nz <= ul12 - 1) seg = 2;
+        else if (nz >= ul12 && nz <= nl12) seg = 3;
+        else if (nz >= nl12 + 1 && nz <= nl1) seg = 1;
+        else if (nz >= nl12 + 1 && nz <= nl2) seg = 2;
+        const float Kh = (B.Ki[n1 * L1 + nz - 1] + B.Ki[n2 * L1 + nz - 1]) * 0.5f;
+        const float h1 = g.helem[el1 * L1 + nz - 1], h2 = seg >= 2 ? g.helem[el2 * L1 + nz - 1] : 0.f;
+        const bool u1 = seg == 1 || seg == 3, u2 = seg >= 2;
+#pragma unroll 1
+        for (int t = 0; t < B.ntr; t++) {
+            const float *__restrict__ T = B.T + (size_t)t * B.sN;
+            float tx1 = 0.f, ty1 = 0.f, tx2 = 0.f, ty2 = 0.f;
+            if (u1) {
+                const float va = T[a0 * L1 + nz - 1], vb = T[a1 * L1 + nz - 1], vc = T[a2 * L1 + nz - 1];
+                tx1 = p0 * va + p1 * vb + p2 * vc;
+                ty1 = p3 * va + p4 * vb + p5 * vc;
+            }
+            if (u2) {
+                const float va = T[b0 * L1 + nz - 1], vb = T[b1 * L1 + nz - 1], vc = T[b2 * L1 + nz - 1];
+                tx2 = q0 * va + q1 * vb + q2 * vc;
+                ty2 = q3 * va + q4 * vb + q5 * vc;
+            }
+            float c = 0.f;
+            if (seg == 1) c = (-dX1 * (Kh * ty1) + dY1 * (Kh * tx1)) * h1;
+            else if (seg == 2) c = (dX2 * (Kh * ty2) - dY2 * (Kh * tx2)) * h2;
+            else if (seg == 3)
+                c = ((dX2 - dX1) * (Kh * (0.5f * (ty1 + ty2))) - (dY2 - dY1) * (Kh * (0.5f * (tx1 + tx2)))) *
+                    ((h1 + h2) * 0.5f);
+            B.HD[(size_t)t * B.sE + e * L1 + nz - 1] = c;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kTB) k32_hdiff(DTopo tp, DGeom<float> g, B32View B) {
+    hdiff_edge32(tp, g, B, blockIdx.x * kWB + (threadIdx.x >> 5));
+}
+
+// k32_diff: the diffusion increment to T* of every tracer in diff_mask, parked in Tnew:
+// (sum of the node's edge fluxes +- c) dt / (areasvol hnode_new) and, without implicit vertical
+// diffusion, diff_ver_part_expl_ale (:841-902): vd(ul) = surface flux, vd(nz) = Kv (T(nz-1)
+// - T(nz)) / (Z(nz-1) - Z(nz)) area, increment (vd(nz) - vd(nz+1)) / (zbar(nz) - zbar(nz+1))
+// dt / (areasvol hnode_new)
+template <int KD>
+__device__ __forceinline__ void diff_node32(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int n,
+                                            int lane, const WEdges &S) {
+    using C = Chunk<1, 1>;
+    const int L1 = tp.L1, nl = tp.nl;
+    const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
+    const unsigned own = S.own;
+    const int nch = C::count(nzmin, nzmax);
+    for (int ch = 0; ch < nch; ch++) {
+        const C k(nzmin, nzmax, ch, lane);
+        const int nz = k.nz;
+        const int i = n * L1 + nz - 1, iv = n * nl + nz - 1;
+        float sdt = 0.f, kz = 0.f, q = 0.f;
+        if (k.lvl) {
+            sdt = dt / (g.areasvol[iv] * g.hnode_new[i]);
+            if (nz > nzmin) kz = B.Kv[iv] / (g.Z3[i - 1] - g.Z3[i]) * g.area[iv];
+            q = sdt / (g.zbar3[iv] - g.zbar3[iv + 1]);
+        }
+        const float kzd = sh_dn(kz, 1);
+        unsigned okm = 0;
+#pragma unroll
+        for (int u = 0; u < KD; u++) {
+            const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
+            okm |= ok ? 1u << u : 0u;
+        }
+#pragma unroll 1
+        for (int t = 0; t < B.ntr; t++) {
+            if (!((B.diff_mask >> t) & 1ull)) continue;
+            float d = 0.f;
+            if (B.Ki) {
+                const float *__restrict__ HD = B.HD + (size_t)t * B.sE;
+#pragma unroll
+                for (int u = 0; u < KD; u++) {
+                    const float x = ((okm >> u) & 1u) ? HD[S.e[u] * L1 + nz - 1] : 0.f;
+                    d += ((own >> u) & 1u) ? x : -x;
+                }
+                d *= sdt;
+            }
+            if (!((B.ivd_mask >> t) & 1ull)) {
+                const float Tn = k.lvl ? B.T[(size_t)t * B.sN + i] : 0.f;
+                const float Tu = sh_up(Tn, 1), Td = sh_dn(Tn, 1);
+                const float fs = B.fsurf ? B.fsurf[t * B.sF + n] : 0.f;
+                const float vd0 = nz == nzmin ? fs : kz * (Tu - Tn);
+                const float vd1 = nz == nzmax - 1 ? 0.f : kzd * (Tn - Td);
+                d += (vd0 - vd1) * q;
+            }
+            if (k.out) B.Tnew[(size_t)t * B.sN + i] = d;
+        }
+    }
+}
+
+template <bool WIDE>
+__device__ __forceinline__ void diff_unit(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int j,
+                                          WEdges *Se) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int n = unit_node<WIDE>(tp, j);
+    if (n < 0 || !B.diff_mask) return;
+    WEdges &S = Se[warp];
+    stage_edges(tp, n, lane, S);
+    if ((S.deg > 8) != WIDE) return;
+    if (WIDE) diff_node32<kMaxDeg>(tp, g, B, dt, n, lane, S);
+    else diff_node32<8>(tp, g, B, dt, n, lane, S);
+}
+
+template <bool WIDE>
+__global__ void __launch_bounds__(kTB) k32_diff(DTopo tp, DGeom<float> g, B32View B, float dt) {
+    __shared__ WEdges Se[kWB];
+    diff_unit<WIDE>(tp, g, B, dt, blockIdx.x * kWB + (threadIdx.x >> 5), Se);
 }
 
 // ---------------------------------------------------------------------------
@@ -1065,6 +1214,21 @@ __global__ void __launch_bounds__(32 * kWV) k32m_vdiff(const Inst32 *__restrict_
     vdiff_unit(I[i].tp, I[i].f, I[i].B, I[i].vf, u - ix.start[i], Wsm[threadIdx.x >> 5]);
 }
 
+__global__ void __launch_bounds__(kTB) k32m_hdiff(const Inst32 *__restrict__ I, MultiIdx ix) {
+    const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
+    if (u >= ix.start[ix.n]) return;
+    const int i = find_inst(ix, u);
+    hdiff_edge32(I[i].tp, I[i].g, I[i].B, u - ix.start[i]);
+}
+template <bool WIDE>
+__global__ void __launch_bounds__(kTB) k32m_diff(const Inst32 *__restrict__ I, MultiIdx ix) {
+    __shared__ WEdges Se[kWB];
+    const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
+    if (u >= ix.start[ix.n]) return;
+    const int i = find_inst(ix, u);
+    diff_unit<WIDE>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
+}
+
 // ---------------------------------------------------------------------------
 // launch wrappers
 // ---------------------------------------------------------------------------
@@ -1107,6 +1271,13 @@ void b32_update(const DTopo &tp, const DGeom<float> &g, const B32View &B, double
     k32_update<false><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, B, (float)dt);
     if (tp.n_wide) k32_update<true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
 }
+void b32_hdiff(const DTopo &tp, const DGeom<float> &g, const B32View &B, cudaStream_t s) {
+    k32_hdiff<<<grid_nodes(tp.E2), kTB, 0, s>>>(tp, g, B);
+}
+void b32_diff(const DTopo &tp, const DGeom<float> &g, const B32View &B, double dt, cudaStream_t s) {
+    k32_diff<false><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, B, (float)dt);
+    if (tp.n_wide) k32_diff<true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
+}
 void b32_vdiff(const DTopo &tp, const DForcing<float> &f, const B32View &B, const VFactors &v, cudaStream_t s) {
     k32_vdiff<<<(tp.N2 + kWV - 1) / kWV, 32 * kWV, 0, s>>>(tp, f, B, v);
 }
@@ -1142,6 +1313,16 @@ void bm32_update(const Inst32 *I, const MultiIdx &ix, bool wide, cudaStream_t s)
     if (!u) return;
     if (wide) k32m_update<true><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
     else k32m_update<false><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
+}
+void bm32_hdiff(const Inst32 *I, const MultiIdx &ix, cudaStream_t s) {
+    const int u = ix.start[ix.n];
+    if (u) k32m_hdiff<<<grid_nodes(u), kTB, 0, s>>>(I, ix);
+}
+void bm32_diff(const Inst32 *I, const MultiIdx &ix, bool wide, cudaStream_t s) {
+    const int u = ix.start[ix.n];
+    if (!u) return;
+    if (wide) k32m_diff<true><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
+    else k32m_diff<false><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
 }
 void bm32_vdiff(const Inst32 *I, const MultiIdx &ix, cudaStream_t s) {
     const int u = ix.start[ix.n];

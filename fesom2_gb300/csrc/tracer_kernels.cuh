@@ -552,6 +552,9 @@ __global__ void __launch_bounds__(kThreads) k_update(DTopo tp, DGeom<R> g, DTrac
                     R del = dhv;
                     if (Exact<R>::value) {
                         del = R(0.0) + dhv + dv;
+                        // diff_tracers_ale: horizontal, then explicit vertical diffusion
+                        if (tr.HD) del = hdiff_add(tp, tr.HD + t * tr.sE, del, n, nz, L1, dt, av);
+                        if (tr.VX && !tr.cfg[t].ivd) del = del + tr.VX[t * tr.sN + i];
                         del = del + T[i] * (g.hnode[i] - g.hnode_new[i]);
                     }
                     const R tn = T[i] + del / g.hnode_new[i];
@@ -568,6 +571,134 @@ __global__ void __launch_bounds__(kThreads) k_update(DTopo tp, DGeom<R> g, DTrac
 // column, arithmetic in A (double for both forms).  Scratch holds Z_n, cp and
 // tp level-major ([level][node]) so that a warp's accesses are coalesced.
 // ===========================================================================
+// ---------------------------------------------------------------------------
+// diff_part_hor_redi (oce_ale_tracer.F90:1526-1689), Redi off: per edge-layer the flux
+// c of the segment (A/D: element 1, B/E: element 2, C: both), Kh = (Ki(n1) + Ki(n2)) / 2
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_hdiff(DTopo tp, DGeom<R> g, DTracers<R> tr) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int L1 = tp.L1;
+    for (int e = blockIdx.x * kWarpsPerBlock + warp; e < tp.E2; e += gridDim.x * kWarpsPerBlock) {
+        const int el1 = tp.e_t1[e], el2 = tp.e_t2[e], n1 = tp.e_n1[e], n2 = tp.e_n2[e];
+        const int nl1 = tp.t_nlev[el1] - 1, ul1 = tp.t_ulev[el1];
+        int nl2 = 0, ul2 = 0;
+        const R dX1 = g.ecd[4 * (size_t)e], dY1 = g.ecd[4 * (size_t)e + 1];
+        R dX2 = R(0), dY2 = R(0);
+        if (el2 >= 0) {
+            nl2 = tp.t_nlev[el2] - 1;
+            ul2 = tp.t_ulev[el2];
+            dX2 = g.ecd[4 * (size_t)e + 2];
+            dY2 = g.ecd[4 * (size_t)e + 3];
+        }
+        const int nl12 = nl1 < nl2 ? nl1 : nl2, ul12 = ul1 > ul2 ? ul1 : ul2;
+        for (int nz = tp.e_lo[e] + lane; nz <= tp.e_hi[e]; nz += 32) {
+            int seg = 0;
+            if (nz >= ul1 && nz <= ul12 - 1) seg = 1;                    // (A)
+            else if (ul2 > 0 && nz >= ul2 && nz <= ul12 - 1) seg = 2;    // (B)
+            else if (nz >= ul12 && nz <= nl12) seg = 3;                 // (C)
+            else if (nz >= nl12 + 1 && nz <= nl1) seg = 1;              // (D)
+            else if (nz >= nl12 + 1 && nz <= nl2) seg = 2;              // (E)
+            for (int t = 0; t < tr.ntr; t++) {
+                const R *Ki = tr.Ki;
+                const R *xy = tr.trxy + t * tr.sT;
+                const R Kh = (Ki[ix1(nz, n1, L1)] + Ki[ix1(nz, n2, L1)]) / R(2.0);
+                R c = R(0);
+                if (seg == 1) {
+                    const R dz = g.helem[ix1(nz, el1, L1)];
+                    const R Fx = Kh * xy[2 * ix1(nz, el1, L1)], Fy = Kh * xy[2 * ix1(nz, el1, L1) + 1];
+                    c = (-dX1 * Fy + dY1 * Fx) * dz;
+                } else if (seg == 2) {
+                    const R dz = g.helem[ix1(nz, el2, L1)];
+                    const R Fx = Kh * xy[2 * ix1(nz, el2, L1)], Fy = Kh * xy[2 * ix1(nz, el2, L1) + 1];
+                    c = (dX2 * Fy - dY2 * Fx) * dz;
+                } else if (seg == 3) {
+                    const R dz = (g.helem[ix1(nz, el1, L1)] + g.helem[ix1(nz, el2, L1)]) / R(2.0);
+                    const R Tx = R(0.5) * (xy[2 * ix1(nz, el1, L1)] + xy[2 * ix1(nz, el2, L1)]);
+                    const R Ty = R(0.5) * (xy[2 * ix1(nz, el1, L1) + 1] + xy[2 * ix1(nz, el2, L1) + 1]);
+                    const R Fx = Kh * Tx, Fy = Kh * Ty;
+                    c = ((dX2 - dX1) * Fy - (dY2 - dY1) * Fx) * dz;
+                }
+                tr.HD[t * tr.sE + ix1(nz, e, L1)] = c;
+            }
+        }
+    }
+}
+
+// del(n) += rhs * dt / areasvol(n) for each edge of n in ascending edge order; rhs = 0 + c at
+// edges(1,e), 0 - c at edges(2,e) (oce_ale_tracer.F90:1677-1684)
+template <typename R>
+__device__ __forceinline__ R hdiff_add(const DTopo &tp, const R *HD, R del, int n, int nz, int L1, R dt, R av) {
+    for (int k = tp.ne_ptr[n]; k < tp.ne_ptr[n + 1]; k++) {
+        const int code = tp.ne_idx[k];
+        const int e = code >= 0 ? code : ~code;
+        if (nz < tp.e_lo[e] || nz > tp.e_hi[e]) continue;
+        const R c = HD[ix1(nz, e, L1)];
+        const R rhs = code >= 0 ? R(0) + c : R(0) - c;
+        del = del + rhs * dt / av;
+    }
+    return del;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_hdiff_gather(DTopo tp, DGeom<R> g, DTracers<R> tr, R dt, R *del) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int L1 = tp.L1, nl = tp.nl;
+    for (int n = blockIdx.x * kWarpsPerBlock + warp; n < tp.N2; n += gridDim.x * kWarpsPerBlock) {
+        const int nzmin = tp.n_ulev[n], nzmax = tp.n_nlev[n];
+        for (int t = 0; t < tr.ntr; t++)
+            for (int nz = nzmin + lane; nz <= nzmax - 1; nz += 32) {
+                const size_t i = ix1(nz, n, L1);
+                del[t * tr.sN + i] =
+                    hdiff_add(tp, tr.HD + t * tr.sE, del[t * tr.sN + i], n, nz, L1, dt, g.areasvol[ixn(nz, n, nl)]);
+            }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// diff_ver_part_expl_ale (oce_ale_tracer.F90:841-902): vd(ul) = surface flux (f.bc),
+// vd(nz) = Kv (T(nz-1) - T(nz)) / (Z(nz-1) - Z(nz)) area; increment of layer nz
+// (vd(nz) - vd(nz+1)) / (zbar(nz) - zbar(nz+1)) dt / areasvol, at the bottom layer
+// (vd(nl1) / (zbar(nl1) - zbar(nl1+1))) dt / areasvol
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ R vexpl_vd(const DTopo &tp, const DGeom<R> &g, const R *Kv, const R *T, R fsurf, int n,
+                                      int nz, int ul1, int nl1, int L1, int nl) {
+    if (nz == ul1) return fsurf;
+    if (nz > nl1) return R(0);
+    const R zinv1 = R(1.0) / (g.Z3[ix1(nz - 1, n, L1)] - g.Z3[ix1(nz, n, L1)]);
+    return Kv[ixn(nz, n, nl)] * (T[ix1(nz - 1, n, L1)] - T[ix1(nz, n, L1)]) * zinv1 * g.area[ixn(nz, n, nl)];
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_vexpl(DTopo tp, DGeom<R> g, DForcing<R> f, DTracers<R> tr, R dt,
+                                                    R *out, int all, int add) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int L1 = tp.L1, nl = tp.nl;
+    for (int n = blockIdx.x * kWarpsPerBlock + warp; n < tp.N2; n += gridDim.x * kWarpsPerBlock) {
+        const int nl1 = tp.n_nlev[n] - 1, ul1 = tp.n_ulev[n];
+        for (int t = 0; t < tr.ntr; t++) {
+            if (!all && tr.cfg[t].ivd) continue;
+            const R *T = tr.T + t * tr.sN;
+            const R fs = f.bc ? f.bc[(size_t)t * tp.N2 + n] : R(0);
+            for (int nz = ul1 + lane; nz <= nl1; nz += 32) {
+                const size_t i = ix1(nz, n, L1);
+                const R av = g.areasvol[ixn(nz, n, nl)];
+                const R v0 = vexpl_vd(tp, g, f.Kv, T, fs, n, nz, ul1, nl1, L1, nl);
+                R inc;
+                if (nz <= nl1 - 1) {
+                    const R v1 = vexpl_vd(tp, g, f.Kv, T, fs, n, nz + 1, ul1, nl1, L1, nl);
+                    inc = (v0 - v1) / (g.zbar3[ixn(nz, n, nl)] - g.zbar3[ixn(nz + 1, n, nl)]) * dt / av;
+                } else {
+                    inc = (v0 / (g.zbar3[ixn(nz, n, nl)] - g.zbar3[ixn(nz + 1, n, nl)])) * dt / av;
+                }
+                R *o = out + t * tr.sN;
+                o[i] = add ? o[i] + inc : inc;
+            }
+        }
+    }
+}
+
 template <typename R>
 __global__ void __launch_bounds__(128) k_vdiff(DTopo tp, DGeom<R> g, DForcing<R> f, DTracers<R> tr, double dt,
                                                double *scratch) {
@@ -746,6 +877,20 @@ void Launch<R>::content(const DTopo &tp, const DGeom<R> &g, const DTracers<R> &t
                         double *out, cudaStream_t s) {
     k_content_partial<R><<<nblk, 256, 0, s>>>(tp, g, tr, partials);
     k_content_final<<<(tr.ntr + 63) / 64, 64, 0, s>>>(partials, nblk, tr.ntr, out);
+}
+
+template <typename R>
+void Launch<R>::hdiff(const DTopo &tp, const DGeom<R> &g, DTracers<R> &tr, cudaStream_t s) {
+    k_hdiff<R><<<grid_for(tp.E2, kWarpsPerBlock), kThreads, 0, s>>>(tp, g, tr);
+}
+template <typename R>
+void Launch<R>::hdiff_gather(const DTopo &tp, const DGeom<R> &g, DTracers<R> &tr, double dt, R *del, cudaStream_t s) {
+    k_hdiff_gather<R><<<grid_for(tp.N2, kWarpsPerBlock), kThreads, 0, s>>>(tp, g, tr, (R)dt, del);
+}
+template <typename R>
+void Launch<R>::vexpl(const DTopo &tp, const DGeom<R> &g, const DForcing<R> &f, DTracers<R> &tr, double dt, R *out,
+                      int all, int add, cudaStream_t s) {
+    k_vexpl<R><<<grid_for(tp.N2, kWarpsPerBlock), kThreads, 0, s>>>(tp, g, f, tr, (R)dt, out, all, add);
 }
 
 }  // namespace fesom

@@ -88,6 +88,9 @@ _SIGS = {
     "fesom_gpu_debug_fetch": ([_P, C.c_char_p, C.c_int32, _P, C.c_size_t], C.c_int),
     "fesom_gpu_tracer_device_ptr": ([_P, C.c_int32, C.POINTER(_P), C.POINTER(_P)], C.c_int),
     "fesom_gpu_tracer_tail": ([_P, C.c_int32, _P, C.c_double, _P, _P, _P, _P, _P, C.POINTER(_P)], C.c_int),
+    "fesom_gpu_set_hdiff": ([_P, _P], C.c_int),
+    "fesom_gpu_diff_hor": ([_P, C.c_double, _P, _P, _P], C.c_int),
+    "fesom_gpu_diff_ver_expl": ([_P, C.c_double, _P, _P, _P, _P], C.c_int),
     "fesom_gpu_step_host_f32": ([_P, C.c_double, _P, _P, _P, _P, _P, _P, C.POINTER(_P), C.POINTER(_P),
                                  C.POINTER(_P), C.POINTER(_P)], C.c_int),
     "fesom_gpu_batch_create": ([C.POINTER(_P), C.c_int32, C.POINTER(_P)], C.c_int),
@@ -349,6 +352,28 @@ class Context:
         keep = [_c64(relax2clim), _c64(Tclim), _c64(Sclim), _c64(ztem)]  # alive through the call
         self._chk(self.L.fesom_gpu_tracer_tail(self.h, n, C.cast(arr, _P), float(dt), C.cast(C.pointer(tc), _P),
                                                *[_p(a) for a in keep], vp))
+
+    def set_hdiff(self, Ki):
+        """Horizontal diffusivity Ki(nod2D, nl-1) for every later step (``None``: no horizontal
+        diffusion)."""
+        self._Ki = None if Ki is None else _c64(Ki)
+        self._chk(self.L.fesom_gpu_set_hdiff(self.h, None if self._Ki is None else _p(self._Ki)))
+
+    def diff_hor(self, dt, Ki, values, del_ttf):
+        """diff_part_hor_redi alone (FP64): ``del_ttf`` (float64, in place) += the horizontal
+        diffusion of ``values``."""
+        if del_ttf.dtype != np.float64 or not del_ttf.flags.c_contiguous:
+            raise ValueError("del_ttf must be C-contiguous float64")
+        keep = [_c64(Ki), _c64(values)]
+        self._chk(self.L.fesom_gpu_diff_hor(self.h, float(dt), _p(keep[0]), _p(keep[1]), _p(del_ttf)))
+
+    def diff_ver_expl(self, dt, Kv, flux_surf, values, del_ttf):
+        """diff_ver_part_expl_ale alone (FP64): ``del_ttf`` (float64, in place) += the explicit
+        vertical diffusion of ``values``."""
+        if del_ttf.dtype != np.float64 or not del_ttf.flags.c_contiguous:
+            raise ValueError("del_ttf must be C-contiguous float64")
+        keep = [_c64(Kv), _c64(flux_surf), _c64(values)]
+        self._chk(self.L.fesom_gpu_diff_ver_expl(self.h, float(dt), *[_p(a) for a in keep], _p(del_ttf)))
 
     def launches_per_step(self) -> int:
         n = C.c_int32(0)

@@ -241,6 +241,22 @@ int fesom_gpu_tracer_content(fesom_gpu_ctx *ctx, double *content);
 /* Device pointer of tracer tr's values (context precision), for zero-copy users. */
 int fesom_gpu_tracer_device_ptr(fesom_gpu_ctx *ctx, int32_t tr, void **values, void **valuesold);
 
+/* Horizontal diffusion of diff_tracers_ale (diff_part_hor_redi, src/oce_ale_tracer.F90:1526-1689,
+ * Redi off): Ki(nl-1, nod2D) = K_hor (mesh_resolution / 100 km)^2 (src/oce_setup_step.F90:968-972).
+ * fesom_gpu_set_hdiff makes every later step of the context add it (NULL: none, as K_hor = 0);
+ * the FP64 and FP32 forms both take it. */
+int fesom_gpu_set_hdiff(fesom_gpu_ctx *ctx, const double *Ki);
+/* The routine alone (FP64 contexts): del_ttf += the edge diffusion fluxes of the element
+ * gradients of values, in ascending edge order. */
+int fesom_gpu_diff_hor(fesom_gpu_ctx *ctx, double dt, const double *Ki, const double *values, double *del_ttf);
+/* diff_ver_part_expl_ale (src/oce_ale_tracer.F90:841-902, FP64 contexts): del_ttf += the explicit
+ * vertical diffusion of values with Kv(nl, nod2D); flux_surf(nod2D) is the surface flux
+ * vd_flux(ulevels) (-heat_flux/vcpw for temperature, the salt fluxes for salinity; NULL: 0).
+ * The steps apply it to the tracers with i_vert_diff = 0, with the bc_surf entries of those
+ * tracers as their surface flux. */
+int fesom_gpu_diff_ver_expl(fesom_gpu_ctx *ctx, double dt, const double *Kv, const double *flux_surf,
+                            const double *values, double *del_ttf);
+
 /* Tail of the tracer loop of solve_tracers_ale (src/oce_ale_tracer.F90:353-375, 497-525):
  * radioactive decay of the tracers with ID 14 and 39; relax_to_clim (src/oce_tracer_mod.F90:
  * 236-298) of the tracers with ID 1 and 2 when clim_relax > 1e-8 -- or, with zonal_relax,

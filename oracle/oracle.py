@@ -64,9 +64,11 @@ def lib() -> C.CDLL:
                      "or_fill_up_dn_grad", "or_adv_tra_hor_upw1", "or_adv_tra_hor_muscl", "or_adv_tra_hor_mfct",
                      "or_adv_tra_ver_upw1", "or_adv_tra_ver_qr4c", "or_oce_tra_adv_fct",
                      "or_oce_tra_adv_flux2dtracer", "or_do_oce_adv_tra", "or_diff_ver_part_impl_ale",
-                     "or_tracer_step", "or_set_threads", "or_get_threads", "or_tracer_tail"):
+                     "or_tracer_step", "or_set_threads", "or_get_threads", "or_tracer_tail",
+                     "or_diff_part_hor_redi", "or_diff_ver_part_expl_ale", "or_tracer_step_ex"):
             getattr(L, name)
         L.or_tracer_step.restype = C.c_int
+        L.or_tracer_step_ex.restype = C.c_int
         L.or_do_oce_adv_tra.restype = C.c_int
         L.or_set_threads.argtypes = [C.c_int]
         _lib = L
@@ -150,6 +152,26 @@ class OracleMesh:
                                      C.byref(cfg), _ptr(values), _ptr(valuesAB), C.byref(self.w))
         if rc != 0:
             raise RuntimeError(f"oracle do_oce_adv_tra failed with status {rc}")
+
+    def tracer_step_ex(self, forcing, cfg: _OrCfg, values, valuesAB, valuesold, Ki=None, dt=None) -> None:
+        """tracer_step with the horizontal diffusion of Ki (None: K_hor = 0)."""
+        for a in (values, valuesAB, valuesold):
+            assert a.flags.c_contiguous and a.dtype == np.float64
+        ki = None if Ki is None else np.ascontiguousarray(Ki, dtype=np.float64)
+        rc = lib().or_tracer_step_ex(C.byref(self.s), C.byref(cfg), C.c_double(forcing.dt if dt is None else dt),
+                                     _ptr(forcing.uv), _ptr(forcing.w), _ptr(forcing.w_i), _ptr(forcing.w_e),
+                                     _ptr(forcing.Kv), _ptr(forcing.bc_surface), _ptr(ki), _ptr(values),
+                                     _ptr(valuesAB), _ptr(valuesold), C.byref(self.w))
+        if rc != 0:
+            raise RuntimeError(f"oracle tracer step failed with status {rc}")
+
+    def diff_part_hor_redi(self, dt, Ki, tr_xy, del_ttf) -> None:
+        ki = np.ascontiguousarray(Ki, dtype=np.float64)
+        lib().or_diff_part_hor_redi(C.byref(self.s), C.c_double(dt), _ptr(ki), _ptr(tr_xy), _ptr(del_ttf))
+
+    def diff_ver_part_expl_ale(self, dt, Kv, flux, values, del_ttf) -> None:
+        lib().or_diff_ver_part_expl_ale(C.byref(self.s), C.c_double(dt), _ptr(Kv), _ptr(flux), _ptr(values),
+                                        _ptr(del_ttf))
 
     def diff_ver_part_impl_ale(self, forcing, values, dt=None) -> None:
         lib().or_diff_ver_part_impl_ale(C.byref(self.s), C.c_double(forcing.dt if dt is None else dt),

@@ -761,9 +761,111 @@ void or_diff_ver_part_impl_ale(const or_mesh *m, double dt, const double *Kv, co
 /* per-tracer body of solve_tracers_ale (src/oce_ale_tracer.F90:303-351,       */
 /* 743-772)                                                                    */
 /* ========================================================================== */
+/* ========================================================================== */
+/* diffusion parts of diff_tracers_ale (src/oce_ale_tracer.F90:560-772)        */
+/* ========================================================================== */
+void or_diff_part_hor_redi(const or_mesh *m, double dt, const double *Ki, const double *tr_xy, double *del_ttf) {
+    const int NL = m->nl, L1 = NL - 1;
+    double rhs1[NL + 1], rhs2[NL + 1];
+    for (int edge = 0; edge < m->edge2D; edge++) {
+        for (int k = 0; k <= NL; k++) rhs1[k] = rhs2[k] = 0.0;
+        const double dX1 = m->edge_cross_dxdy[4 * (size_t)edge], dY1 = m->edge_cross_dxdy[4 * (size_t)edge + 1];
+        double dX2 = 0.0, dY2 = 0.0;
+        const int el1 = m->edge_tri[2 * edge], el2 = m->edge_tri[2 * edge + 1];
+        const int n1 = m->edges[2 * edge], n2 = m->edges[2 * edge + 1];
+        const int nl1 = m->nlevels[el1] - 1, ul1 = m->ulevels[el1];
+        int nl2 = 0, ul2 = 0;
+        if (el2 >= 0) {
+            nl2 = m->nlevels[el2] - 1;
+            ul2 = m->ulevels[el2];
+            dX2 = m->edge_cross_dxdy[4 * (size_t)edge + 2];
+            dY2 = m->edge_cross_dxdy[4 * (size_t)edge + 3];
+        }
+        int nl12 = nl1 < nl2 ? nl1 : nl2, ul12 = ul1 > ul2 ? ul1 : ul2;
+        /* fluxes Kh grad T of one element (segments A/D: el1, B/E: el2, C: mean of both) */
+#define KH(nz) ((Ki[IX1(nz, n1)] + Ki[IX1(nz, n2)]) / 2.0)
+#define TXY(k, nz, el) (tr_xy[2 * IX1(nz, el) + (k)])
+        for (int nz = ul1; nz <= ul12 - 1; nz++) { /* (A) */
+            double Kh = KH(nz), dz = m->helem[IX1(nz, el1)];
+            double Fx = Kh * TXY(0, nz, el1), Fy = Kh * TXY(1, nz, el1);
+            double cc = (-dX1 * Fy + dY1 * Fx) * dz;
+            rhs1[nz] = rhs1[nz] + cc;
+            rhs2[nz] = rhs2[nz] - cc;
+        }
+        if (ul2 > 0)
+            for (int nz = ul2; nz <= ul12 - 1; nz++) { /* (B) */
+                double Kh = KH(nz), dz = m->helem[IX1(nz, el2)];
+                double Fx = Kh * TXY(0, nz, el2), Fy = Kh * TXY(1, nz, el2);
+                double cc = (dX2 * Fy - dY2 * Fx) * dz;
+                rhs1[nz] = rhs1[nz] + cc;
+                rhs2[nz] = rhs2[nz] - cc;
+            }
+        for (int nz = ul12; nz <= nl12; nz++) { /* (C) */
+            double Kh = KH(nz), dz = (m->helem[IX1(nz, el1)] + m->helem[IX1(nz, el2)]) / 2.0;
+            double Tx = 0.5 * (TXY(0, nz, el1) + TXY(0, nz, el2)), Ty = 0.5 * (TXY(1, nz, el1) + TXY(1, nz, el2));
+            double Fx = Kh * Tx, Fy = Kh * Ty;
+            double cc = ((dX2 - dX1) * Fy - (dY2 - dY1) * Fx) * dz;
+            rhs1[nz] = rhs1[nz] + cc;
+            rhs2[nz] = rhs2[nz] - cc;
+        }
+        for (int nz = nl12 + 1; nz <= nl1; nz++) { /* (D) */
+            double Kh = KH(nz), dz = m->helem[IX1(nz, el1)];
+            double Fx = Kh * TXY(0, nz, el1), Fy = Kh * TXY(1, nz, el1);
+            double cc = (-dX1 * Fy + dY1 * Fx) * dz;
+            rhs1[nz] = rhs1[nz] + cc;
+            rhs2[nz] = rhs2[nz] - cc;
+        }
+        for (int nz = nl12 + 1; nz <= nl2; nz++) { /* (E) */
+            double Kh = KH(nz), dz = m->helem[IX1(nz, el2)];
+            double Fx = Kh * TXY(0, nz, el2), Fy = Kh * TXY(1, nz, el2);
+            double cc = (dX2 * Fy - dY2 * Fx) * dz;
+            rhs1[nz] = rhs1[nz] + cc;
+            rhs2[nz] = rhs2[nz] - cc;
+        }
+#undef KH
+#undef TXY
+        nl12 = nl1 > nl2 ? nl1 : nl2;
+        ul12 = ul1;
+        if (ul2 > 0) ul12 = ul1 < ul2 ? ul1 : ul2;
+        for (int nz = ul12; nz <= nl12; nz++) {
+            del_ttf[IX1(nz, n1)] = del_ttf[IX1(nz, n1)] + rhs1[nz] * dt / m->areasvol[IXN(nz, n1)];
+            del_ttf[IX1(nz, n2)] = del_ttf[IX1(nz, n2)] + rhs2[nz] * dt / m->areasvol[IXN(nz, n2)];
+        }
+    }
+}
+
+void or_diff_ver_part_expl_ale(const or_mesh *m, double dt, const double *Kv, const double *flux_surf,
+                               const double *values, double *del_ttf) {
+    const int NL = m->nl, L1 = NL - 1;
+    OMP_FOR
+    for (int n = 0; n < m->nod2D; n++) {
+        double vd[NL + 1];
+        for (int k = 0; k <= NL; k++) vd[k] = 0.0;
+        const int nl1 = m->nlevels_nod2D[n] - 1, ul1 = m->ulevels_nod2D[n];
+        vd[ul1] = flux_surf ? flux_surf[n] : 0.0;
+        for (int nz = ul1 + 1; nz <= nl1; nz++) {
+            double zinv1 = 1.0 / (m->Z_3d_n[IX1(nz - 1, n)] - m->Z_3d_n[IX1(nz, n)]);
+            vd[nz] = Kv[IXN(nz, n)] * (values[IX1(nz - 1, n)] - values[IX1(nz, n)]) * zinv1 * m->area[IXN(nz, n)];
+        }
+        for (int nz = ul1; nz <= nl1 - 1; nz++)
+            del_ttf[IX1(nz, n)] = del_ttf[IX1(nz, n)] + (vd[nz] - vd[nz + 1]) /
+                                                            (m->zbar_3d_n[IXN(nz, n)] - m->zbar_3d_n[IXN(nz + 1, n)]) *
+                                                            dt / m->areasvol[IXN(nz, n)];
+        del_ttf[IX1(nl1, n)] = del_ttf[IX1(nl1, n)] +
+                               (vd[nl1] / (m->zbar_3d_n[IXN(nl1, n)] - m->zbar_3d_n[IXN(nl1 + 1, n)])) * dt /
+                                   m->areasvol[IXN(nl1, n)];
+    }
+}
+
 int or_tracer_step(const or_mesh *m, const or_tra_cfg *c, double dt, const double *vel, const double *W,
                    const double *WI, const double *WE, const double *Kv, const double *bc_surf,
                    double *values, double *valuesAB, double *valuesold, or_work *w) {
+    return or_tracer_step_ex(m, c, dt, vel, W, WI, WE, Kv, bc_surf, NULL, values, valuesAB, valuesold, w);
+}
+
+int or_tracer_step_ex(const or_mesh *m, const or_tra_cfg *c, double dt, const double *vel, const double *W,
+                      const double *WI, const double *WE, const double *Kv, const double *bc_surf, const double *Ki,
+                      double *values, double *valuesAB, double *valuesold, or_work *w) {
     const int L1 = m->nl - 1;
     if (c->ab_order != 2 && c->ab_order != 3) return 2;
     or_init_tracers_AB(m, c, values, valuesAB, valuesold, w);
@@ -772,6 +874,9 @@ int or_tracer_step(const or_mesh *m, const or_tra_cfg *c, double dt, const doubl
     const size_t N = (size_t)L1 * (size_t)m->nod2D;
     OMP_FOR
     for (long i = 0; i < (long)N; i++) w->del_ttf[i] = w->del_ttf[i] + w->del_ttf_advhoriz[i] + w->del_ttf_advvert[i];
+    /* diff_tracers_ale (:595-607): horizontal diffusion, then the explicit vertical one */
+    if (Ki) or_diff_part_hor_redi(m, dt, Ki, w->tr_xy, w->del_ttf);
+    if (!c->i_vert_diff) or_diff_ver_part_expl_ale(m, dt, Kv, bc_surf, values, w->del_ttf);
     OMP_FOR
     for (int n = 0; n < m->nod2D; n++) {
         int nzmax = m->nlevels_nod2D[n] - 1, nzmin = m->ulevels_nod2D[n];

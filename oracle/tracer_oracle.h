@@ -113,6 +113,21 @@ int or_do_oce_adv_tra(const or_mesh *m, double dt, const double *vel, const doub
 void or_diff_ver_part_impl_ale(const or_mesh *m, double dt, const double *Kv, const double *bc_surf,
                                double *values);
 
+/* diff_part_hor_redi (src/oce_ale_tracer.F90:1526-1689) with Redi off: edge fluxes of
+ * Ki-weighted element gradients tr_xy, scattered into del_ttf in ascending edge order. */
+void or_diff_part_hor_redi(const or_mesh *m, double dt, const double *Ki, const double *tr_xy, double *del_ttf);
+/* diff_ver_part_expl_ale (src/oce_ale_tracer.F90:841-902): explicit vertical diffusion of
+ * values into del_ttf; flux_surf(n) is the surface flux vd_flux(ulevels) (NULL: zero). */
+void or_diff_ver_part_expl_ale(const or_mesh *m, double dt, const double *Kv, const double *flux_surf,
+                               const double *values, double *del_ttf);
+
+/* The per-tracer body of solve_tracers_ale with the horizontal diffusion of diff_tracers_ale
+ * (Ki = NULL: K_hor = 0) and, for tracers without implicit vertical diffusion, the explicit
+ * one (bc_surf then holds its surface flux). */
+int or_tracer_step_ex(const or_mesh *m, const or_tra_cfg *c, double dt, const double *vel, const double *W,
+                      const double *WI, const double *WE, const double *Kv, const double *bc_surf, const double *Ki,
+                      double *values, double *valuesAB, double *valuesold, or_work *w);
+
 /* The per-tracer body of solve_tracers_ale (src/oce_ale_tracer.F90:303-351):
  * init_tracers_AB, do_oce_adv_tra, del_ttf sum, diff_tracers_ale (T* update,
  * implicit vertical diffusion).  Horizontal (Redi) diffusion is off. */

@@ -80,6 +80,61 @@ class Ref:
         v2 = (vel[self.e2, :, 1] * ecd[:, 2:3] - vel[self.e2, :, 0] * ecd[:, 3:4]) * h2
         return {1: v1, 2: v2, 3: v1 + v2}[which]
 
+    # ---- oce_ale_tracer.F90:1526-1689 (diff_part_hor_redi, Redi off) --------
+    def diff_part_hor_redi(self, dt, Ki, trxy, del_ttf):
+        """Edge fluxes Kh grad T of the segments A..E, scattered in ascending edge order."""
+        m = self.m
+        Kh = (Ki[self.n1] + Ki[self.n2]) / 2.0
+        ecd = m.edge_cross_dxdy
+        dX1, dY1 = ecd[:, 0:1], ecd[:, 1:2]
+        dX2 = np.where(self.has2[:, None], ecd[:, 2:3], 0.0)
+        dY2 = np.where(self.has2[:, None], ecd[:, 3:4], 0.0)
+        h1, h2 = m.helem[self.el1], m.helem[self.e2]
+        t1, t2 = trxy[self.el1], trxy[self.e2]
+        c1 = (-dX1 * (Kh * t1[:, :, 1]) + dY1 * (Kh * t1[:, :, 0])) * h1
+        c2 = (dX2 * (Kh * t2[:, :, 1]) - dY2 * (Kh * t2[:, :, 0])) * h2
+        Tx = 0.5 * (t1[:, :, 0] + t2[:, :, 0])
+        Ty = 0.5 * (t1[:, :, 1] + t2[:, :, 1])
+        c3 = ((dX2 - dX1) * (Kh * Ty) - (dY2 - dY1) * (Kh * Tx)) * ((h1 + h2) / 2.0)
+        c = np.zeros_like(Kh)
+        for mask, typ in self.segs:
+            c = np.where(mask, {1: c1, 2: c2, 3: c3}[typ], c)
+        rhs1, rhs2 = 0.0 + c, 0.0 - c
+        av = m.areasvol[:, :-1]
+        v1 = np.where(self.smask, rhs1 * dt / av[self.n1], 0.0)
+        v2 = np.where(self.smask, rhs2 * dt / av[self.n2], 0.0)
+        vals = np.stack([v1, v2], axis=1).reshape(-1, self.L1)
+        out = del_ttf.copy()
+        np.add.at(out, self.sc_rows, vals)
+        return out
+
+    # ---- oce_ale_tracer.F90:841-902 (diff_ver_part_expl_ale) ----------------
+    def diff_ver_part_expl_ale(self, dt, Kv, flux, T, del_ttf):
+        m = self.m
+        N2, L1 = m.nod2D, self.L1
+        nl1 = (m.nlevels_nod2D - 1)[:, None]
+        ul1 = m.ulevels_nod2D[:, None]
+        lev = self.lev
+        vd = np.zeros((N2, L1 + 2))  # vd[:, nz], nz 1-based
+        Tm = np.concatenate([np.zeros((N2, 1)), T[:, :-1]], axis=1)   # T(nz-1)
+        zm = np.concatenate([np.ones((N2, 1)), m.Z_3d_n[:, :-1]], axis=1)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            zinv1 = 1.0 / (zm - m.Z_3d_n)
+            inner = Kv[:, :L1] * (Tm - T) * zinv1 * m.area[:, :L1]
+        vdl = np.where((lev >= ul1 + 1) & (lev <= nl1), inner, 0.0)
+        vdl = np.where(lev == ul1, (np.zeros(N2) if flux is None else flux)[:, None], vdl)
+        vd[:, 1:L1 + 1] = vdl
+        vnext = vd[:, 2:L1 + 2]
+        zb = m.zbar_3d_n
+        av = m.areasvol[:, :L1]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            mid = (vdl - vnext) / (zb[:, :L1] - zb[:, 1:L1 + 1]) * dt / av
+            bot = (vdl / (zb[:, :L1] - zb[:, 1:L1 + 1])) * dt / av
+        out = del_ttf.copy()
+        out = np.where((lev >= ul1) & (lev <= nl1 - 1), out + mid, out)
+        out = np.where(lev == nl1, out + bot, out)
+        return out
+
     # ---- oce_tracer_mod.F90:147-188 -----------------------------------------
     def tr_xy(self, T):
         m = self.m
