@@ -344,18 +344,29 @@ def _levels_from_depth(tri: np.ndarray, depth_nod: np.ndarray, zbar: np.ndarray,
 
 def _finish_mesh(coord: np.ndarray, tri: np.ndarray, cyc: float, cartesian: bool,
                  zbar: np.ndarray, depth_nod: np.ndarray, partial_cells: bool,
-                 name: str) -> Mesh:
+                 name: str, nlevels: Optional[np.ndarray] = None, edge_set=None) -> Mesh:
+    """Derived arrays of a mesh from node coordinates (radians), triangles (0-based), levels
+    and node depths.  ``nlevels`` (element level counts) and ``edge_set`` = (edges, edge_tri,
+    edge2D_in), 0-based with -1 for a missing triangle, are taken as given when passed (as
+    the reference takes them from the partitioner's files), else built here."""
     nl = zbar.size
     Z = 0.5 * (zbar[:-1] + zbar[1:])
     tri = _orient_clockwise(coord, tri.astype(np.int64), cyc)
     N2 = coord.shape[0]
     T2 = tri.shape[0]
-    edges, edge_tri, edge2D_in = _build_edges(coord, tri, cyc)
+    if edge_set is None:
+        edges, edge_tri, edge2D_in = _build_edges(coord, tri, cyc)
+    else:
+        edges, edge_tri, edge2D_in = edge_set
+        edges = np.ascontiguousarray(edges, dtype=np.int32)
+        edge_tri = np.ascontiguousarray(edge_tri, dtype=np.int32)
     ptr, nie = _nod_in_elem(tri, N2)
     nie_node = np.repeat(np.arange(N2), np.diff(ptr))
 
     # --- levels --------------------------------------------------------------
-    nlevels = _levels_from_depth(tri, depth_nod, zbar, Z)
+    if nlevels is None:
+        nlevels = _levels_from_depth(tri, depth_nod, zbar, Z)
+    nlevels = np.ascontiguousarray(nlevels, dtype=np.int32)
     ulevels = np.ones(T2, dtype=np.int32)
     nlevels_nod2D = np.zeros(N2, dtype=np.int32)
     np.maximum.at(nlevels_nod2D, tri.reshape(-1), np.repeat(nlevels, 3))

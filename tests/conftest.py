@@ -72,3 +72,23 @@ def wet_mask(mesh):
 def perturbed_old(T, rng, scale=1e-3):
     """valuesold for the first AB step: T plus a small seeded perturbation."""
     return np.ascontiguousarray(T * (1.0 + scale * rng.standard_normal(T.shape)))
+
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="session")
+def soufflet_file_mesh():
+    """The Soufflet channel of the reference's test data (2875 nodes, 41 levels, Cartesian,
+    cyclic over 4.5 degrees), built from the copy of its .out files in tests/golden."""
+    from fesom2_gb300 import meshio as MI
+    return MI.mesh_from_files(MI.load_files(os.path.join(GOLDEN, "mesh_soufflet.npz")), name="soufflet",
+                              **MI.SOUFFLET)
+
+
+@pytest.fixture(scope="session")
+def pi_file_mesh():
+    """The PI mesh of the reference's test data (3140 nodes, 48 levels, global, rotated by
+    the Euler angles 50, 15, -90), built from the copy of its .out files in tests/golden."""
+    from fesom2_gb300 import meshio as MI
+    return MI.mesh_from_files(MI.load_files(os.path.join(GOLDEN, "mesh_pi.npz")), name="pi", **MI.PI)
