@@ -51,6 +51,7 @@ struct fesom_gpu_ctx {
     unsigned *status = nullptr;
     bool forcing_ready = false;
     bool state_ready = false;
+    int wsplit = 0;            // dynamics%use_wsplit (fesom_gpu_set_wsplit)
     cudaGraphExec_t gexec = nullptr;
     double g_dt = 0.0;
     // FP32 batched form: rotating time-level buffers and its work arrays
@@ -393,11 +394,7 @@ int init_muscl_weights(fesom_gpu_ctx *ctx, const fesom_mesh_desc *d) {
 int check_cfg(fesom_gpu_ctx *ctx, const fesom_tra_cfg *c) {
     if (!c) { ctx->err = "null tracer configuration"; return FESOM_ERR_ARG; }
     if (c->adv_hor < 0 || c->adv_hor > 2) { ctx->err = "unknown horizontal advection scheme"; return FESOM_ERR_SCHEME; }
-    if (c->adv_ver == FESOM_ADV_VER_CDIFF || c->adv_ver == FESOM_ADV_VER_PPM) {
-        ctx->err = "vertical scheme CDIFF/PPM is not implemented on the device";
-        return FESOM_ERR_SCHEME;
-    }
-    if (c->adv_ver < 0 || c->adv_ver > 1) { ctx->err = "unknown vertical advection scheme"; return FESOM_ERR_SCHEME; }
+    if (c->adv_ver < 0 || c->adv_ver > 3) { ctx->err = "unknown vertical advection scheme"; return FESOM_ERR_SCHEME; }
     if (c->adv_lim != 0 && c->adv_lim != 1) { ctx->err = "unknown limiter"; return FESOM_ERR_SCHEME; }
     if (c->ab_order != 2 && c->ab_order != 3) {
         ctx->err = "Adams-Bashforth tracer order must be 2 or 3";
@@ -503,6 +500,7 @@ DForcing<R> forcing_view(fesom_gpu_ctx *ctx, int t0) {
     f.we = (const R *)ctx->we;
     f.Kv = (const R *)ctx->Kv;
     f.bc = ctx->bc ? (const R *)ctx->bc + (size_t)t0 * ctx->N2 : nullptr;
+    f.wsplit = ctx->wsplit;
     return f;
 }
 
@@ -601,7 +599,7 @@ B32View view32(fesom_gpu_ctx *ctx, int t0, int nt) {
     v.TB = ctx->TB2;
     v.cfg = ctx->d_cfg + t0;
     v.status = ctx->status;
-    v.fct_mask = v.ivd_mask = v.diff_mask = 0;
+    v.fct_mask = v.ivd_mask = v.diff_mask = v.ppm_mask = v.wimpl_mask = 0;
     v.Ki = (const float *)ctx->Ki;
     v.HD = ctx->Ki ? ctx->HD32 : nullptr;
     v.Kv = (const float *)ctx->Kv;
@@ -612,6 +610,8 @@ B32View view32(fesom_gpu_ctx *ctx, int t0, int nt) {
         if (c.adv_lim == FESOM_ADV_LIM_FCT) v.fct_mask |= 1ull << t;
         if (c.i_vert_diff) v.ivd_mask |= 1ull << t;
         if (ctx->Ki || !c.i_vert_diff) v.diff_mask |= 1ull << t;
+        if (c.adv_ver == FESOM_ADV_VER_PPM) v.ppm_mask |= 1ull << t;
+        if (ctx->wsplit && c.i_vert_diff && c.adv_lim != FESOM_ADV_LIM_FCT) v.wimpl_mask |= 1ull << t;
         v.hor[t] = (signed char)c.adv_hor;
         v.ver[t] = (signed char)c.adv_ver;
         v.ph[t] = (float)c.adv_ph;
@@ -637,6 +637,8 @@ B32View sub32(const B32View &B, int s0, int ns) {
     v.fct_mask = B.fct_mask >> s0;
     v.ivd_mask = B.ivd_mask >> s0;
     v.diff_mask = B.diff_mask >> s0;
+    v.ppm_mask = B.ppm_mask >> s0;
+    v.wimpl_mask = B.wimpl_mask >> s0;
     if (v.HD) v.HD += s0 * B.sE;
     if (v.fsurf) v.fsurf += s0 * B.sF;
     for (int t = 0; t < ns; t++) {
@@ -692,6 +694,8 @@ int enqueue_step(fesom_gpu_ctx *ctx, double dt, StageTimer *tm = nullptr) {
         if (any_ho || ctx->Ki) STAGE(1, Launch<R>::trxy(ctx->tp, g, tr, ctx->stream));
         STAGE(2, Launch<R>::edge_flux(ctx->tp, g, f, tr, any_fct, ctx->stream));
         STAGE(3, Launch<R>::node_lo(ctx->tp, g, f, tr, dt, any_fct, ctx->stream));
+        // split vertical velocity: w_i advects the LO values implicitly (oce_adv_tra_driver.F90:323-334)
+        if (ctx->wsplit && any_fct) STAGE(3, Launch<R>::lo_impl(ctx->tp, g, f, tr, dt, ctx->scratch, ctx->stream));
         // diff_tracers_ale: horizontal diffusion fluxes, explicit vertical increments (both from
         // the values before the update)
         if (ctx->Ki) STAGE(2, Launch<R>::hdiff(ctx->tp, g, tr, ctx->stream));
@@ -736,6 +740,9 @@ int enqueue_group32(fesom_gpu_ctx *ctx, double dt, int t0, int nt, StageTimer *t
     bool any_fct = false;
     for (int t = t0; t < t0 + nt; t++) any_fct |= ctx->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
     STAGE(10, b32_lo_ad(ctx->tp, g, fg, B, ctx->VF, dt, ctx->stream));
+    if (B.ppm_mask) STAGE(10, b32_vppm(ctx->tp, g, fg, B, dt, ctx->stream));
+    // split vertical velocity: w_i advects the LO values implicitly (oce_adv_tra_driver.F90:323-334)
+    if (ctx->wsplit && any_fct) STAGE(10, b32_lo_impl(ctx->tp, g, fg, B, dt, ctx->scratch, ctx->stream));
     STAGE(2, b32_ho(ctx->tp, g, B, ctx->mw, ctx->VF, ctx->stream));
     // diff_tracers_ale from the values before the update; the increment waits in Tnew (the
     // oldest level, read by lo_ad and ho only) for the update to add it after the limiter
@@ -754,6 +761,7 @@ int enqueue_group32(fesom_gpu_ctx *ctx, double dt, int t0, int nt, StageTimer *t
         }
         STAGE(7, b32_vdiff(ctx->tp, fg, B, ctx->vfac, ctx->stream));
     }
+    if (B.wimpl_mask) STAGE(7, b32_vdiff_w(ctx->tp, g, fg, B, dt, ctx->scratch, ctx->stream));
     return FESOM_OK;
 }
 
@@ -788,8 +796,14 @@ int launches_per_step(fesom_gpu_ctx *ctx) {
             const int bg = FESOM_BOUNDS_GROUP > 0 ? FESOM_BOUNDS_GROUP : nt;
             bool grp_diff = ctx->Ki != nullptr;
             for (int t = t0; t < t0 + nt; t++) grp_diff |= ctx->cfgs[t].i_vert_diff == 0;
+            bool grp_ppm = false, grp_wimpl = false;
+            for (int t = t0; t < t0 + nt; t++) {
+                grp_ppm |= ctx->cfgs[t].adv_ver == FESOM_ADV_VER_PPM;
+                grp_wimpl |= ctx->wsplit && ctx->cfgs[t].i_vert_diff && ctx->cfgs[t].adv_lim != FESOM_ADV_LIM_FCT;
+            }
             n += wide * (2 + (any_fct ? (nt + bg - 1) / bg : 0) + (grp_diff ? 1 : 0)) + (ctx->mw.n_items ? 2 : 1) +
-                 (grp_vd ? 1 : 0) + (ctx->Ki ? 1 : 0);
+                 (grp_vd ? 1 : 0) + (ctx->Ki ? 1 : 0) + (grp_ppm ? 1 : 0) + ((ctx->wsplit && any_fct) ? 1 : 0) +
+                 (grp_wimpl ? 1 : 0);
         }
         return n;
     }
@@ -804,7 +818,7 @@ int launches_per_step(fesom_gpu_ctx *ctx) {
         bool any_ex = false;
         for (int t = t0; t < t0 + nt; t++) any_ex |= ctx->cfgs[t].i_vert_diff == 0;
         n += 4 + ((any_ho || ctx->Ki) ? 1 : 0) + (any_fct ? 2 : 0) + (any_vd ? 1 : 0) + (ctx->Ki ? 1 : 0) +
-             (any_ex ? 1 : 0);
+             (any_ex ? 1 : 0) + ((ctx->wsplit && any_fct) ? 1 : 0);
     }
     return n;
 }
@@ -1071,6 +1085,10 @@ int fesom_gpu_adv_tra(fesom_gpu_ctx *ctx, double dt, const double *vel, const do
                       const double *we, const fesom_tra_cfg *cfg, const double *ttf, const double *ttfAB,
                       double *dttf_h, double *dttf_v) {
     if (!ctx || !vel || !w || !we || !ttf || !ttfAB || !dttf_h || !dttf_v) return FESOM_ERR_ARG;
+    if (ctx->wsplit && !wi) {
+        ctx->err = "the split vertical velocity needs w_i";
+        return FESOM_ERR_ARG;
+    }
     int rc;
     if ((rc = need_fp64(ctx)) || (rc = ensure_one(ctx, cfg))) return rc;
     const size_t sN = (size_t)ctx->L1 * ctx->N2, sNI = (size_t)ctx->nl * ctx->N2;
@@ -1086,6 +1104,7 @@ int fesom_gpu_adv_tra(fesom_gpu_ctx *ctx, double dt, const double *vel, const do
     if (cfg->adv_hor != FESOM_ADV_HOR_UPW1) Launch<double>::trxy(ctx->tp, ctx->g64, tr, ctx->stream);
     Launch<double>::edge_flux(ctx->tp, ctx->g64, f, tr, fct, ctx->stream);
     Launch<double>::node_lo(ctx->tp, ctx->g64, f, tr, dt, fct, ctx->stream);
+    if (fct && ctx->wsplit) Launch<double>::lo_impl(ctx->tp, ctx->g64, f, tr, dt, ctx->scratch, ctx->stream);
     if (fct) {
         Launch<double>::bounds(ctx->tp, ctx->g64, tr, ctx->stream);
         Launch<double>::rpm(ctx->tp, ctx->g64, tr, dt, ctx->stream);
@@ -1099,9 +1118,15 @@ int fesom_gpu_adv_tra(fesom_gpu_ctx *ctx, double dt, const double *vel, const do
 
 int fesom_gpu_vdiff_impl(fesom_gpu_ctx *ctx, double dt, const fesom_tra_cfg *cfg, const double *Kv,
                          const double *bc_surf, double *values) {
+    return fesom_gpu_vdiff_impl_wi(ctx, dt, cfg, Kv, bc_surf, nullptr, values);
+}
+
+int fesom_gpu_vdiff_impl_wi(fesom_gpu_ctx *ctx, double dt, const fesom_tra_cfg *cfg, const double *Kv,
+                            const double *bc_surf, const double *wi, double *values) {
     if (!ctx || !Kv || !values) return FESOM_ERR_ARG;
     int rc;
     if ((rc = need_fp64(ctx)) || (rc = ensure_one(ctx, cfg))) return rc;
+    if (wi && (rc = put(ctx, ctx->wi, wi, (size_t)ctx->nl * ctx->N2))) return rc;
     const size_t sN = (size_t)ctx->L1 * ctx->N2, sNI = (size_t)ctx->nl * ctx->N2;
     if ((rc = put(ctx, ctx->Kv, Kv, sNI))) return rc;
     if (bc_surf) {
@@ -1112,6 +1137,7 @@ int fesom_gpu_vdiff_impl(fesom_gpu_ctx *ctx, double dt, const fesom_tra_cfg *cfg
     if ((rc = put(ctx, ctx->T, values, sN))) return rc;
     DTracers<double> tr = group_view<double>(ctx, 0, 1);
     DForcing<double> f = forcing_view<double>(ctx, 0);
+    f.wsplit = wi != nullptr;  // do_wimpl: w_i given and no limiter (the kernel checks the limiter)
     fesom_tra_cfg c = *cfg;
     c.i_vert_diff = 1;
     DCfg d = to_dcfg(c);
@@ -1443,6 +1469,14 @@ int fesom_gpu_tracer_content(fesom_gpu_ctx *ctx, double *content) {
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(content, ctx->content_out, sizeof(double) * ctx->ntr, cudaMemcpyDeviceToHost, ctx->stream));
     return wait_stream(ctx, -1);
+}
+
+int fesom_gpu_set_wsplit(fesom_gpu_ctx *ctx, int32_t on) {
+    if (!ctx) return FESOM_ERR_ARG;
+    ctx->wsplit = on ? 1 : 0;
+    if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
+    free_graphs32(ctx);
+    return FESOM_OK;
 }
 
 int fesom_gpu_set_hdiff(fesom_gpu_ctx *ctx, const double *Ki) {
@@ -1792,6 +1826,12 @@ int fesom_gpu_batch_create(fesom_gpu_ctx *const *ctxs, int32_t n, fesom_gpu_batc
             return FESOM_ERR_STATE;
         }
         if (i > 0 && c->ab_max != b->ab) { b->err = "batch instances must share one Adams-Bashforth order"; return FESOM_ERR_ARG; }
+        bool ppm = false;
+        for (int t = 0; t < c->ntr; t++) ppm |= c->cfgs[t].adv_ver == FESOM_ADV_VER_PPM;
+        if (ppm || c->wsplit) {
+            b->err = "the PPM vertical scheme and the split vertical velocity step in single contexts only";
+            return FESOM_ERR_SCHEME;
+        }
         b->ab = c->ab_max;
         for (int t = 0; t < c->ntr; t++) {
             b->any_vd |= c->cfgs[t].i_vert_diff != 0;

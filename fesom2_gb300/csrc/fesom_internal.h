@@ -52,6 +52,7 @@ struct DForcing {
     const R *w, *wi, *we;     // nl per node
     const R *Kv;              // nl per node
     const R *bc;              // ntr per node (may be null)
+    int wsplit;               // dynamics%use_wsplit: w = w_e + w_i, w_i advected implicitly
 };
 
 // Per-tracer scheme on the device (fesom_tra_cfg without the id).
@@ -110,6 +111,8 @@ struct B32View {
     const float *Kv;   // vertical diffusivity (explicit part), nl per node
     const float *fsurf;  // surface flux per tracer and node (explicit vertical diffusion)
     size_t sF;           // tracer stride of fsurf (nodes)
+    unsigned long long ppm_mask;    // tracers with the PPM vertical scheme (k32_vppm writes their ADv)
+    unsigned long long wimpl_mask;  // split velocity: implicit diffusion with the w_i terms (k32_vdiff_w)
 };
 // Node degree bound of the FP32 form (the node's edge list is staged per warp)
 constexpr int kMaxDeg = 16;
@@ -142,6 +145,11 @@ void b32_lo_ad(const DTopo &, const DGeom<float> &, const DForcing<float> &, con
                double dt, cudaStream_t);
 void b32_ho(const DTopo &, const DGeom<float> &, const B32View &, const MusclW &, const float *VF, cudaStream_t);
 void b32_bounds(const DTopo &, const DGeom<float> &, const B32View &, double dt, cudaStream_t);
+void b32_vppm(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, double dt, cudaStream_t);
+void b32_lo_impl(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, double dt,
+                 double *scratch, cudaStream_t);
+void b32_vdiff_w(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, double dt,
+                 double *scratch, cudaStream_t);
 void b32_hdiff(const DTopo &, const DGeom<float> &, const B32View &, cudaStream_t);
 void b32_diff(const DTopo &, const DGeom<float> &, const B32View &, double dt, cudaStream_t);
 void b32_update(const DTopo &, const DGeom<float> &, const B32View &, double dt, cudaStream_t);
@@ -203,6 +211,9 @@ struct Launch {
     static void update(const DTopo &, const DGeom<R> &, DTracers<R> &, double dt, int fct, int mode, cudaStream_t);
     static void vdiff(const DTopo &, const DGeom<R> &, const DForcing<R> &, DTracers<R> &, double dt,
                       double *scratch, cudaStream_t);
+    // adv_tra_vert_impl by w_i on the LO values of the FCT tracers (split vertical velocity)
+    static void lo_impl(const DTopo &, const DGeom<R> &, const DForcing<R> &, DTracers<R> &, double dt,
+                        double *scratch, cudaStream_t);
     static void content(const DTopo &, const DGeom<R> &, const DTracers<R> &, double *partials, int nblk,
                         double *out, cudaStream_t);
     // diff_part_hor_redi: edge fluxes into tr.HD; hdiff_gather adds them to del (ascending edges)

@@ -384,14 +384,26 @@ __device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &
             if (nz == nzmax - 1) fv1 = 0.f;
             // LO = (T hnode + flux divergence dt / areasvol) / hnode_new (oce_adv_tra_driver.F90:249)
             if (k.out) B.LO[to + i] = Tn * hr + (hs + fv0 - fv1) * sdt;
-            // vertical high-order flux on the AB values (QR4C / UPW1), minus the LO flux
-            if (k.out) {
+            // with the split vertical velocity the LO part of the antidiffusive flux is the upwind
+            // flux of the full w (oce_adv_tra_driver.F90:323-334)
+            float fw0 = fv0;
+            if (f.wsplit && k.lvl) {
+                if (nz == nzmin) {
+                    fw0 = -(w0 * Tn * ar0);
+                } else {
+                    const float aw = fabsf(w0);
+                    fw0 = -(0.5f * (Tn * (w0 + aw) + Tu * (w0 - aw)) * ar0);
+                }
+            }
+            // vertical high-order flux on the AB values (QR4C / UPW1 / CDIFF; PPM in k32_vppm),
+            // minus the LO flux
+            if (k.out && ver != 3) {
                 const float pw = lim ? w0 : we0;
                 float Cf;
                 if (nz == nzmin) {
                     Cf = -(tab * pw * ar0);
                 } else if (ver != 0 || nz == nzmin + 1 || nz == nzmax - 1) {
-                    if (ver == 0) {
+                    if (ver != 1) {  // QR4C next to the ends, CDIFF everywhere
                         Cf = -(0.5f * (tabu + tab) * pw * ar0);
                     } else {
                         const float aw = fabsf(pw);
@@ -408,7 +420,7 @@ __device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &
                     Cf = (-(0.5f * (1.f - no) * Tmean) - no * (0.5f * (Tm1 + Tm2)) * pw) * ar0;
                 }
                 // flux = C - flux_in; FCT passes the LO flux in, otherwise zero
-                const float fin = lim ? fv0 : 0.f;
+                const float fin = lim ? fw0 : 0.f;
                 float F = Cf - fin;
                 // a two-layer column writes its middle interface twice (statements nzmin+1, nzmax-1)
                 if (ver == 0 && twolayer && nz == nzmin + 1) F = Cf - F;
@@ -817,6 +829,252 @@ k32_update(DTopo tp, DGeom<float> g, B32View B, float dt) {
 }
 
 // ---------------------------------------------------------------------------
+// k32_vppm: adv_tra_vert_ppm (oce_adv_tra_ver.F90:438-631) on the AB values of the tracers
+// in ppm_mask, minus the LO flux, into ADv.  A warp per node over chunks of 27 interfaces
+// with 3 levels of halo above and 2 below: the interface value tv(k) needs the layers
+// k-2..k+1, the flux of interface nz the parabola of layer nz or nz-1.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void vppm_node(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
+                                          const B32View &B, float dt, int n, int lane) {
+    using C = Chunk<3, 2>;
+    const int L1 = tp.L1, nl = tp.nl;
+    const int nzmin = tp.n_ulev[n], nzmax = tp.n_nlev[n];
+    const int nch = C::count(nzmin, nzmax);
+    for (int ch = 0; ch < nch; ch++) {
+        const C k(nzmin, nzmax, ch, lane);
+        const int nz = k.nz;
+        const int i = n * L1 + nz - 1, iv = n * nl + nz - 1;
+        float hn0 = 0.f, ho0 = 0.f, ar0 = 0.f, w0 = 0.f, we0 = 0.f;
+        if (k.lvl) {
+            hn0 = g.hnode_new[i];
+            ho0 = g.hnode[i];
+            ar0 = g.area[iv];
+            w0 = f.w[iv];
+            we0 = f.we[iv];
+        }
+        const float hm1 = sh_up(hn0, 1), hm2 = sh_up(hn0, 2), hp1 = sh_dn(hn0, 1);
+        const float hom1 = sh_up(ho0, 1);
+        unsigned long long todo = B.ppm_mask;
+        while (todo) {
+            const int t = __ffsll((long long)todo) - 1;
+            todo &= todo - 1;
+            const bool lim = (B.fct_mask >> t) & 1ull;
+            const size_t to = (size_t)t * B.sN;
+            const float Tn = k.lvl ? B.T[to + i] : 0.f;
+            const float o1 = k.lvl ? B.O1[to + i] : 0.f;
+            const float o2 = (k.lvl && B.ab == 3) ? B.O2[to + i] : 0.f;
+            const float tab = Tn + (k.lvl ? ab_delta(B.ab, Tn, o1, o2) : 0.f);
+            const float tm1 = sh_up(tab, 1), tm2 = sh_up(tab, 2), tp1 = sh_dn(tab, 1);
+            const float Tu = sh_up(Tn, 1);
+            // tv(nz) (:488-562): centred next to the ends, the non-uniform PPM value between
+            float tv;
+            if (nz == nzmax) {
+                tv = tm1;
+            } else if (nz == nzmin) {
+                tv = tab;
+            } else if (nz == nzmax - 1 || nz == nzmin + 1) {
+                tv = 0.5f * (tm1 + tab);
+            } else {
+                // layer j = nz-1: dzjm1 = h(nz-2), dzj = h(nz-1), dzjp1 = h(nz), dzjp2 = h(nz+1)
+                const float a0 = hm2, a1 = hm1, a2 = hn0, a3 = hp1;
+                const float d10 = tab - tm1, d0m = tm1 - tm2, d21 = tp1 - tab;
+                float dj = a1 / (a0 + a1 + a2) * ((2.f * a0 + a1) / (a2 + a1) * d10 + (a1 + 2.f * a2) / (a0 + a1) * d0m);
+                float dj1 = a2 / (a1 + a2 + a3) * ((2.f * a1 + a2) / (a3 + a2) * d21 + (a2 + 2.f * a3) / (a1 + a2) * d10);
+                dj = d10 * d0m > 0.f ? copysignf(fminf(fminf(fabsf(dj), 2.f * fabsf(d10)), 2.f * fabsf(d0m)), dj) : 0.f;
+                dj1 = d21 * d10 > 0.f ? copysignf(fminf(fminf(fabsf(dj1), 2.f * fabsf(d21)), 2.f * fabsf(d10)), dj1) : 0.f;
+                tv = tm1 + a1 / (a1 + a2) * d10 +
+                     1.f / (a0 + a1 + a2 + a3) *
+                         ((2.f * a2 * a1) / (a1 + a2) * ((a0 + a1) / (2.f * a1 + a2) - (a3 + a2) / (2.f * a2 + a1)) * d10 -
+                          a1 * (a0 + a1) / (2.f * a1 + a2) * dj1 + a2 * (a2 + a3) / (a1 + 2.f * a2) * dj);
+            }
+            const float tvu = sh_up(tv, 1), tvd = sh_dn(tv, 1);
+            if (!k.out) continue;
+            const float pw = lim ? w0 : we0;
+            float Cf = 0.f;
+            if (nz == nzmin) {
+                Cf = -(tv * pw * ar0);
+            } else if (pw > 0.f || pw < 0.f) {
+                // the parabola of the upwind layer (:564-620)
+                const bool top = pw > 0.f;
+                float aL = top ? tv : tvu, aR = top ? tvd : tv;
+                const float tt = top ? tab : tm1, dz = top ? ho0 : hom1;
+                if ((aR - tt) * (tt - aL) <= 0.f) aL = aR = tt;
+                if ((aR - aL) * (tt - 0.5f * (aL + aR)) > (aR - aL) * (aR - aL) * (1.f / 6.f)) aL = 3.f * tt - 2.f * aR;
+                if ((aR - aL) * (tt - 0.5f * (aR + aL)) < -((aR - aL) * (aR - aL) * (1.f / 6.f))) aR = 3.f * tt - 2.f * aL;
+                const float aj = 6.f * (tt - 0.5f * (aL + aR));
+                const float x = fminf(fabsf(pw) * dt / dz, 1.f);
+                const float v = top ? -aL - 0.5f * x * (aR - aL + (1.f - (2.f / 3.f) * x) * aj)
+                                    : -aR + 0.5f * x * (aR - aL - (1.f - (2.f / 3.f) * x) * aj);
+                Cf = v * ar0 * pw;
+            }
+            // minus the upwind LO flux: of w_e, or of the full w for FCT with the split velocity
+            const float wl = (lim && f.wsplit) ? w0 : we0;
+            float fl;
+            if (nz == nzmin) {
+                fl = -(wl * Tn * ar0);
+            } else {
+                const float aw = fabsf(wl);
+                fl = -(0.5f * (Tn * (wl + aw) + Tu * (wl - aw)) * ar0);
+            }
+            B.ADv[(size_t)t * B.sNI + iv] = Cf - fl;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kTB) k32_vppm(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, float dt) {
+    const int n = blockIdx.x * kWB + (threadIdx.x >> 5);
+    if (n >= tp.N2) return;
+    vppm_node(tp, g, f, B, dt, n, threadIdx.x & 31);
+}
+
+// ---------------------------------------------------------------------------
+// split vertical velocity, FP32 form: adv_tra_vert_impl by w_i on the LO values of the FCT
+// tracers (oce_adv_tra_ver.F90:90-240), and the implicit vertical diffusion with the w_i
+// terms for the tracers without the limiter (oce_ale_tracer.F90:907-1435, do_wimpl).  One
+// thread per column, FP64 arithmetic; scratch holds Z_n, cp and tp level-major.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k32_lo_impl(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B,
+                                                   double dt, double *scratch) {
+    const int L1 = tp.L1, nl = tp.nl;
+    const size_t N2 = tp.N2;
+    double *cps = scratch, *tps = scratch + (size_t)(L1 + 1) * N2;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= tp.N2) return;
+#define CP(k) cps[(size_t)(k) * N2 + n]
+#define TP(k) tps[(size_t)(k) * N2 + n]
+    const int nzmax = tp.n_nlev[n], nzmin = tp.n_ulev[n];
+    const float *hn = g.hnode_new + (size_t)n * L1 - 1;
+    const float *ar = g.area + (size_t)n * nl - 1, *av = g.areasvol + (size_t)n * nl - 1;
+    const float *wi = f.wi + (size_t)n * nl - 1;
+    unsigned long long todo = B.fct_mask & (B.ntr >= 64 ? ~0ull : ((1ull << B.ntr) - 1));
+    while (todo) {
+        const int t = __ffsll((long long)todo) - 1;
+        todo &= todo - 1;
+        float *Tc = B.LO + (size_t)t * B.sN + (size_t)n * L1 - 1;
+        int nz = nzmin;
+        double v = dt * ar[nz] / av[nz];
+        double b = (double)hn[nz] + (double)wi[nz] * v;
+        v = dt * ar[nz + 1] / av[nz];
+        b = b - fmin(0.0, (double)wi[nz + 1]) * v;
+        double c = -(fmax(0.0, (double)wi[nz + 1]) * v);
+        double T0 = Tc[nz], Tp1 = Tc[nz + 1], Tm;
+        double rhs = -((b - hn[nz]) * T0) - c * Tp1;
+        double cp = c / b, tpv = rhs / b;
+        CP(nz) = cp;
+        TP(nz) = tpv;
+        for (nz = nzmin + 1; nz <= nzmax - 1; nz++) {
+            v = dt * ar[nz] / av[nz];
+            const double a = fmin(0.0, (double)wi[nz]) * v;
+            b = (double)hn[nz] + fmax(0.0, (double)wi[nz]) * v;
+            c = 0.0;
+            if (nz <= nzmax - 2) {
+                v = dt * ar[nz + 1] / av[nz];
+                b = b - fmin(0.0, (double)wi[nz + 1]) * v;
+                c = -(fmax(0.0, (double)wi[nz + 1]) * v);
+            }
+            Tm = T0;
+            T0 = Tp1;
+            Tp1 = nz <= nzmax - 2 ? (double)Tc[nz + 1] : 0.0;
+            rhs = -(a * Tm) - (b - hn[nz]) * T0 - c * Tp1;
+            const double m = b - cp * a;
+            cp = c / m;
+            tpv = (rhs - tpv * a) / m;
+            CP(nz) = cp;
+            TP(nz) = tpv;
+        }
+        double x = tpv;
+        Tc[nzmax - 1] = (float)(Tc[nzmax - 1] + x);
+        for (nz = nzmax - 2; nz >= nzmin; nz--) {
+            x = TP(nz) - CP(nz) * x;
+            Tc[nz] = (float)(Tc[nz] + x);
+        }
+    }
+#undef CP
+#undef TP
+}
+
+__global__ void __launch_bounds__(128) k32_vdiff_w(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B,
+                                                   double dt, double *scratch) {
+    const int L1 = tp.L1, nl = tp.nl;
+    const size_t N2 = tp.N2;
+    double *Zs = scratch, *cps = scratch + (size_t)(L1 + 1) * N2, *tps = cps + (size_t)(L1 + 1) * N2;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= tp.N2) return;
+#define ZN(k) Zs[(size_t)(k) * N2 + n]
+#define CP(k) cps[(size_t)(k) * N2 + n]
+#define TP(k) tps[(size_t)(k) * N2 + n]
+    const int nzmax = tp.n_nlev[n], nzmin = tp.n_ulev[n];
+    const float *hn = g.hnode_new + (size_t)n * L1 - 1;
+    const float *ar = g.area + (size_t)n * nl - 1, *av = g.areasvol + (size_t)n * nl - 1;
+    const float *kv = f.Kv + (size_t)n * nl - 1, *wi = f.wi + (size_t)n * nl - 1;
+    double zb = g.zbar_n_bot[n];
+    ZN(nzmax - 1) = zb + (double)hn[nzmax - 1] / 2.0;
+    for (int nz = nzmax - 1; nz >= nzmin + 1; nz--) {
+        zb = zb + (double)hn[nz];
+        ZN(nz - 1) = zb + (double)hn[nz - 1] / 2.0;
+    }
+    unsigned long long todo = B.wimpl_mask & (B.ntr >= 64 ? ~0ull : ((1ull << B.ntr) - 1));
+    while (todo) {
+        const int t = __ffsll((long long)todo) - 1;
+        todo &= todo - 1;
+        float *Tc = B.Tnew + (size_t)t * B.sN + (size_t)n * L1 - 1;
+        const double bc = B.fsurf ? (double)B.fsurf[t * B.sF + n] : 0.0;
+        int nz = nzmin;
+        double zinv2 = 1.0 / (ZN(nz) - ZN(nz + 1)), zinv1;
+        double c = -((double)kv[nz + 1] * zinv2 * dt * ar[nz + 1] / av[nz]);
+        double b = -c + hn[nz];
+        double v = dt * ((double)ar[nz] / av[nz]);
+        b = b + (double)wi[nz] * v;
+        v = dt * ar[nz + 1] / av[nz];
+        b = b - fmin(0.0, (double)wi[nz + 1]) * v;
+        c = c - fmax(0.0, (double)wi[nz + 1]) * v;
+        double T0 = Tc[nz], Tp1 = Tc[nz + 1], Tm;
+        double rhs = -((b - hn[nz]) * T0) - c * Tp1 + bc;
+        double cp = c / b, tpv = rhs / b;
+        CP(nz) = cp;
+        TP(nz) = tpv;
+        zinv1 = zinv2;
+        for (nz = nzmin + 1; nz <= nzmax - 1; nz++) {
+            const bool bot = nz == nzmax - 1;
+            double a = -((double)kv[nz] * zinv1 * dt * ((double)ar[nz] / av[nz]));
+            c = 0.0;
+            if (!bot) {
+                zinv2 = 1.0 / (ZN(nz) - ZN(nz + 1));
+                c = -((double)kv[nz + 1] * zinv2 * dt * ar[nz + 1] / av[nz]);
+            }
+            b = -a - c + hn[nz];
+            zinv1 = zinv2;
+            v = dt * ((double)ar[nz] / av[nz]);
+            a = a + fmin(0.0, (double)wi[nz]) * v;
+            b = b + fmax(0.0, (double)wi[nz]) * v;
+            if (!bot) {
+                v = dt * ar[nz + 1] / av[nz];
+                b = b - fmin(0.0, (double)wi[nz + 1]) * v;
+                c = c - fmax(0.0, (double)wi[nz + 1]) * v;
+            }
+            Tm = T0;
+            T0 = Tp1;
+            Tp1 = bot ? 0.0 : (double)Tc[nz + 1];
+            rhs = -(a * Tm) - (b - hn[nz]) * T0 - c * Tp1;
+            const double m = b - cp * a;
+            cp = c / m;
+            tpv = (rhs - tpv * a) / m;
+            CP(nz) = cp;
+            TP(nz) = tpv;
+        }
+        double x = tpv;
+        Tc[nzmax - 1] = (float)(Tc[nzmax - 1] + x);
+        for (nz = nzmax - 2; nz >= nzmin; nz--) {
+            x = TP(nz) - CP(nz) * x;
+            Tc[nz] = (float)(Tc[nz] + x);
+        }
+    }
+#undef ZN
+#undef CP
+#undef TP
+}
+
+// ---------------------------------------------------------------------------
 // diffusion of diff_tracers_ale (oce_ale_tracer.F90:560-772) in the FP32 form
 // ---------------------------------------------------------------------------
 // k32_hdiff: diff_part_hor_redi (:1526-1689, Redi off) flux c of every edge-layer from the
@@ -1117,7 +1375,7 @@ __device__ __forceinline__ void vdiff_unit(const DTopo &tp, const DForcing<float
     }
     __syncwarp();
     // the tracers with implicit diffusion, two per pass: their scan chains interleave
-    unsigned long long todo = B.ivd_mask & (B.ntr >= 64 ? ~0ull : ((1ull << B.ntr) - 1));
+    unsigned long long todo = (B.ivd_mask & ~B.wimpl_mask) & (B.ntr >= 64 ? ~0ull : ((1ull << B.ntr) - 1));
     while (todo) {
         const int t1 = __ffsll((long long)todo) - 1;
         todo &= todo - 1;
@@ -1270,6 +1528,18 @@ void b32_bounds(const DTopo &tp, const DGeom<float> &g, const B32View &B, double
 void b32_update(const DTopo &tp, const DGeom<float> &g, const B32View &B, double dt, cudaStream_t s) {
     k32_update<false><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, B, (float)dt);
     if (tp.n_wide) k32_update<true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
+}
+void b32_vppm(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B, double dt,
+              cudaStream_t s) {
+    k32_vppm<<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, f, B, (float)dt);
+}
+void b32_lo_impl(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B, double dt,
+                 double *scratch, cudaStream_t s) {
+    k32_lo_impl<<<(tp.N2 + 127) / 128, 128, 0, s>>>(tp, g, f, B, dt, scratch);
+}
+void b32_vdiff_w(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B, double dt,
+                 double *scratch, cudaStream_t s) {
+    k32_vdiff_w<<<(tp.N2 + 127) / 128, 128, 0, s>>>(tp, g, f, B, dt, scratch);
 }
 void b32_hdiff(const DTopo &tp, const DGeom<float> &g, const B32View &B, cudaStream_t s) {
     k32_hdiff<<<grid_nodes(tp.E2), kTB, 0, s>>>(tp, g, B);

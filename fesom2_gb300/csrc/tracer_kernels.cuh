@@ -298,6 +298,89 @@ __device__ __forceinline__ R ver_qr4c_flux(const R *T, const R *W, const R *area
     return v;
 }
 
+// adv_tra_ver_cdiff (src/oce_adv_tra_ver.F90:635-695): the bottom interface keeps its input
+template <typename R>
+__device__ __forceinline__ R ver_cdiff_flux(const R *T, const R *W, const R *area, int nz, int n, int nzmin, int nzmax,
+                                            int L1, int nl, R fin) {
+    if (nz == nzmin) return -(W[ixn(nz, n, nl)] * T[ix1(nz, n, L1)] * area[ixn(nz, n, nl)]) - fin;
+    if (nz == nzmax) return fin;
+    const R tv = R(0.5) * (T[ix1(nz - 1, n, L1)] + T[ix1(nz, n, L1)]);
+    return -(tv * W[ixn(nz, n, nl)] * area[ixn(nz, n, nl)]) - fin;
+}
+
+template <typename R>
+__device__ __forceinline__ R min3r(R a, R b, R c) { return rmin(rmin(a, b), c); }
+// Fortran sign(1, b)
+template <typename R>
+__device__ __forceinline__ R sign1(R b) { return signbit(b) ? R(-1.0) : R(1.0); }
+
+// interface value tv(k) of adv_tra_vert_ppm (src/oce_adv_tra_ver.F90:488-562) on a column:
+// Tc, hc 1-based views of the layer values and the new thicknesses
+template <typename R>
+__device__ R ppm_tv(const R *Tc, const R *hc, int k, int nzmin, int nzmax) {
+    if (k == nzmax) return Tc[nzmax - 1];
+    if (k == nzmin) return Tc[nzmin];
+    if (k == nzmax - 1) return R(0.5) * (Tc[nzmax - 2] + Tc[nzmax - 1]);
+    if (k == nzmin + 1) return R(0.5) * (Tc[nzmin] + Tc[nzmin + 1]);
+    const int nz = k - 1;
+    const R dzjm1 = hc[nz - 1], dzj = hc[nz], dzjp1 = hc[nz + 1], dzjp2 = hc[nz + 2];
+    const R tm1 = Tc[nz - 1], t0 = Tc[nz], tp1 = Tc[nz + 1], tp2 = Tc[nz + 2];
+    R deltaj = dzj / (dzjm1 + dzj + dzjp1) *
+               ((R(2.0) * dzjm1 + dzj) / (dzjp1 + dzj) * (tp1 - t0) + (dzj + R(2.0) * dzjp1) / (dzjm1 + dzj) * (t0 - tm1));
+    R deltajp1 = dzjp1 / (dzj + dzjp1 + dzjp2) *
+                 ((R(2.0) * dzj + dzjp1) / (dzjp2 + dzjp1) * (tp2 - tp1) +
+                  (dzjp1 + R(2.0) * dzjp2) / (dzj + dzjp1) * (tp1 - t0));
+    if ((tp1 - t0) * (t0 - tm1) > R(0.0))
+        deltaj = min3r(rabs(deltaj), R(2.0) * rabs(tp1 - t0), R(2.0) * rabs(t0 - tm1)) * sign1(deltaj);
+    else
+        deltaj = R(0.0);
+    if ((tp2 - tp1) * (tp1 - t0) > R(0.0))
+        deltajp1 = min3r(rabs(deltajp1), R(2.0) * rabs(tp2 - tp1), R(2.0) * rabs(tp1 - t0)) * sign1(deltajp1);
+    else
+        deltajp1 = R(0.0);
+    return t0 + dzj / (dzj + dzjp1) * (tp1 - t0) +
+           R(1.0) / (dzjm1 + dzj + dzjp1 + dzjp2) *
+               ((R(2.0) * dzjp1 * dzj) / (dzj + dzjp1) *
+                    ((dzjm1 + dzj) / (R(2.0) * dzj + dzjp1) - (dzjp2 + dzjp1) / (R(2.0) * dzjp1 + dzj)) * (tp1 - t0) -
+                dzj * (dzjm1 + dzj) / (R(2.0) * dzj + dzjp1) * deltajp1 +
+                dzjp1 * (dzjp1 + dzjp2) / (dzj + R(2.0) * dzjp1) * deltaj);
+}
+
+// the PPM flux of interface nz (:564-620): the monotonised parabola of the upwind layer (nz
+// when w(nz) > 0, nz-1 when w(nz) < 0) integrated over the part swept in dt (old thickness);
+// the surface takes -tv w area, the bottom 0; minus the input flux
+template <typename R>
+__device__ R ver_ppm_flux(const R *T, const R *W, const R *area, const R *hn, const R *ho, R dt, int nz, int n,
+                          int nzmin, int nzmax, int L1, int nl, R fin) {
+    const R *Tc = T + (size_t)n * L1 - 1, *hc = hn + (size_t)n * L1 - 1, *oc = ho + (size_t)n * L1 - 1;
+    const R *Wc = W + (size_t)n * nl - 1, *ac = area + (size_t)n * nl - 1;
+    if (nz == nzmin) return -(ppm_tv(Tc, hc, nzmin, nzmin, nzmax) * Wc[nzmin] * ac[nzmin]) - fin;
+    if (nz == nzmax) return R(0.0) - fin;
+    const R w = Wc[nz];
+    if (!(w > R(0.0)) && !(w < R(0.0))) return R(0.0) - fin;
+    const bool top = w > R(0.0);
+    const int j = top ? nz : nz - 1;  // the upwind layer
+    R aL = ppm_tv(Tc, hc, j, nzmin, nzmax), aR = ppm_tv(Tc, hc, j + 1, nzmin, nzmax);
+    const R t = Tc[j];
+    if ((aR - t) * (t - aL) <= R(0.0)) {
+        aL = t;
+        aR = t;
+    }
+    if ((aR - aL) * (t - R(0.5) * (aL + aR)) > (aR - aL) * (aR - aL) / R(6.0)) aL = R(3.0) * t - R(2.0) * aR;
+    if ((aR - aL) * (t - R(0.5) * (aR + aL)) < -((aR - aL) * (aR - aL) / R(6.0))) aR = R(3.0) * t - R(2.0) * aL;
+    const R dzj = oc[j];
+    const R aj = R(6.0) * (t - R(0.5) * (aL + aR));
+    R v;
+    if (top) {
+        const R x = rmin(w * dt / dzj, R(1.0));
+        v = -aL - R(0.5) * x * (aR - aL + (R(1.0) - R(2.0) / R(3.0) * x) * aj);
+    } else {
+        const R x = rmin(-(w * dt / dzj), R(1.0));
+        v = -aR + R(0.5) * x * (aR - aL - (R(1.0) - R(2.0) / R(3.0) * x) * aj);
+    }
+    return v * ac[nz] * w - fin;
+}
+
 template <typename R>
 __global__ void __launch_bounds__(kThreads)
 k_node_lo(DTopo tp, DGeom<R> g, DForcing<R> f, DTracers<R> tr, R dt) {
@@ -339,11 +422,18 @@ k_node_lo(DTopo tp, DGeom<R> g, DForcing<R> f, DTracers<R> tr, R dt) {
                     }
                 }
                 const R *pw = fct ? f.w : f.we;
+                // with the split vertical velocity the LO part of the antidiffusive flux is the
+                // upwind flux of the full w (oce_adv_tra_driver.F90:323-334)
+                const R fin = (fct && f.wsplit) ? ver_upw1_flux(T, f.w, g.area, nz, n, nzmin, nzmax, L1, nl, R(0)) : fv0;
                 R v;
                 if (c.ver == 0)
-                    v = ver_qr4c_flux(TA, pw, g.area, g.Z3, g.zbar3, nz, n, nzmin, nzmax, L1, nl, R(c.pv), fv0);
+                    v = ver_qr4c_flux(TA, pw, g.area, g.Z3, g.zbar3, nz, n, nzmin, nzmax, L1, nl, R(c.pv), fin);
+                else if (c.ver == 2)
+                    v = ver_cdiff_flux(TA, pw, g.area, nz, n, nzmin, nzmax, L1, nl, fin);
+                else if (c.ver == 3)
+                    v = ver_ppm_flux(TA, pw, g.area, g.hnode_new, g.hnode, dt, nz, n, nzmin, nzmax, L1, nl, fin);
                 else
-                    v = ver_upw1_flux(TA, pw, g.area, nz, n, nzmin, nzmax, L1, nl, fv0);
+                    v = ver_upw1_flux(TA, pw, g.area, nz, n, nzmin, nzmax, L1, nl, fin);
                 tr.ADv[t * tr.sNI + ixn(nz, n, nl)] = v;
             }
         }
@@ -699,6 +789,81 @@ __global__ void __launch_bounds__(kThreads) k_vexpl(DTopo tp, DGeom<R> g, DForci
     }
 }
 
+// ===========================================================================
+// adv_tra_vert_impl (src/oce_adv_tra_ver.F90:90-240) on the LO values of the FCT tracers:
+// implicit upwind advection by w_i, one thread per column, arithmetic in A (double); scratch
+// holds cp and tp level-major
+// ===========================================================================
+template <typename R>
+__global__ void __launch_bounds__(128) k_lo_impl(DTopo tp, DGeom<R> g, DForcing<R> f, DTracers<R> tr, double dt,
+                                                 double *scratch) {
+    typedef double A;
+    const int L1 = tp.L1, nl = tp.nl;
+    const size_t N2 = tp.N2;
+    A *cps = scratch, *tps = scratch + (size_t)(L1 + 1) * N2;
+#define CP(k) cps[(size_t)(k) * N2 + n]
+#define TP(k) tps[(size_t)(k) * N2 + n]
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < tp.N2; n += gridDim.x * blockDim.x) {
+        const int nzmax = tp.n_nlev[n], nzmin = tp.n_ulev[n];
+        const R *hn = g.hnode_new + (size_t)n * L1 - 1;
+        const R *ar = g.area + (size_t)n * nl - 1;
+        const R *av = g.areasvol + (size_t)n * nl - 1;
+        const R *wi = f.wi + (size_t)n * nl - 1;
+        for (int t = 0; t < tr.ntr; t++) {
+            if (!tr.cfg[t].lim) continue;
+            R *Tc = tr.LO + t * tr.sN + (size_t)n * L1 - 1;
+            const A zinv = 1.0 * dt;
+            int nz = nzmin;
+            A v = zinv * (A)ar[nz] / (A)av[nz];
+            A b = (A)hn[nz] + (A)wi[nz] * v;
+            v = zinv * (A)ar[nz + 1] / (A)av[nz];
+            b = b - fmin(0.0, (A)wi[nz + 1]) * v;
+            A c = -(fmax(0.0, (A)wi[nz + 1]) * v);
+            A T0 = (A)Tc[nz], Tp1 = (A)Tc[nz + 1], Tm;
+            A rhs = -((b - (A)hn[nz]) * T0) - c * Tp1;
+            A cp = c / b, tpv = rhs / b;
+            CP(nz) = cp;
+            TP(nz) = tpv;
+            for (nz = nzmin + 1; nz <= nzmax - 2; nz++) {
+                v = zinv * (A)ar[nz] / (A)av[nz];
+                const A a = fmin(0.0, (A)wi[nz]) * v;
+                b = (A)hn[nz] + fmax(0.0, (A)wi[nz]) * v;
+                v = zinv * (A)ar[nz + 1] / (A)av[nz];
+                b = b - fmin(0.0, (A)wi[nz + 1]) * v;
+                c = -(fmax(0.0, (A)wi[nz + 1]) * v);
+                Tm = T0;
+                T0 = Tp1;
+                Tp1 = (A)Tc[nz + 1];
+                rhs = -(a * Tm) - (b - (A)hn[nz]) * T0 - c * Tp1;
+                const A m = b - cp * a;
+                cp = c / m;
+                tpv = (rhs - tpv * a) / m;
+                CP(nz) = cp;
+                TP(nz) = tpv;
+            }
+            nz = nzmax - 1;
+            {
+                v = zinv * (A)ar[nz] / (A)av[nz];
+                const A a = fmin(0.0, (A)wi[nz]) * v;
+                b = (A)hn[nz] + fmax(0.0, (A)wi[nz]) * v;
+                Tm = T0;
+                T0 = Tp1;
+                rhs = -(a * Tm) - (b - (A)hn[nz]) * T0;
+                const A m = b - cp * a;
+                tpv = (rhs - tpv * a) / m;
+            }
+            A trv = tpv;
+            Tc[nzmax - 1] = (R)((A)Tc[nzmax - 1] + trv);
+            for (nz = nzmax - 2; nz >= nzmin; nz--) {
+                trv = TP(nz) - CP(nz) * trv;
+                Tc[nz] = (R)((A)Tc[nz] + trv);
+            }
+        }
+    }
+#undef CP
+#undef TP
+}
+
 template <typename R>
 __global__ void __launch_bounds__(128) k_vdiff(DTopo tp, DGeom<R> g, DForcing<R> f, DTracers<R> tr, double dt,
                                                double *scratch) {
@@ -725,6 +890,9 @@ __global__ void __launch_bounds__(128) k_vdiff(DTopo tp, DGeom<R> g, DForcing<R>
         for (int t = 0; t < tr.ntr; t++) {
             R *Tc = tr.T + t * tr.sN + (size_t)n * L1 - 1;
             if (!tr.cfg[t].ivd) continue;
+            // the implicit part of a split vertical velocity joins the solve without a limiter (:961)
+            const bool wimpl = f.wsplit && !tr.cfg[t].lim;
+            const R *wi = f.wi + (size_t)n * nl - 1;
             const A bc = f.bc ? (A)f.bc[(size_t)t * N2 + n] : 0.0;
             // forward elimination, coefficients built on the fly (:1099-1229, 1406-1414)
             int nz = nzmin;
@@ -732,6 +900,13 @@ __global__ void __launch_bounds__(128) k_vdiff(DTopo tp, DGeom<R> g, DForcing<R>
             const A zinv = 1.0 * dt;
             A c = -((A)kv[nz + 1] * zinv2 * zinv * (A)ar[nz + 1] / (A)av[nz]);
             A b = -c + (A)hn[nz];
+            if (wimpl) {  // :1134-1147
+                A v = zinv * ((A)ar[nz] / (A)av[nz]);
+                b = b + (A)wi[nz] * v;
+                v = zinv * (A)ar[nz + 1] / (A)av[nz];
+                b = b - fmin(0.0, (A)wi[nz + 1]) * v;
+                c = c - fmax(0.0, (A)wi[nz + 1]) * v;
+            }
             A Tm = (A)Tc[nz], T0 = Tm, Tp1 = (A)Tc[nz + 1];
             A dz = (A)hn[nz];
             A rhs = -((b - dz) * T0) - c * Tp1;
@@ -742,10 +917,18 @@ __global__ void __launch_bounds__(128) k_vdiff(DTopo tp, DGeom<R> g, DForcing<R>
             A zinv1 = zinv2;
             for (nz = nzmin + 1; nz <= nzmax - 2; nz++) {
                 zinv2 = 1.0 / (ZN(nz) - ZN(nz + 1));
-                const A a = -((A)kv[nz] * zinv1 * zinv * ((A)ar[nz] / (A)av[nz]));
+                A a = -((A)kv[nz] * zinv1 * zinv * ((A)ar[nz] / (A)av[nz]));
                 c = -((A)kv[nz + 1] * zinv2 * zinv * (A)ar[nz + 1] / (A)av[nz]);
                 b = -a - c + (A)hn[nz];
                 zinv1 = zinv2;
+                if (wimpl) {  // :1176-1189
+                    A v = zinv * ((A)ar[nz] / (A)av[nz]);
+                    a = a + fmin(0.0, (A)wi[nz]) * v;
+                    b = b + fmax(0.0, (A)wi[nz]) * v;
+                    v = zinv * (A)ar[nz + 1] / (A)av[nz];
+                    b = b - fmin(0.0, (A)wi[nz + 1]) * v;
+                    c = c - fmax(0.0, (A)wi[nz + 1]) * v;
+                }
                 Tm = T0;
                 T0 = Tp1;
                 Tp1 = (A)Tc[nz + 1];
@@ -759,8 +942,13 @@ __global__ void __launch_bounds__(128) k_vdiff(DTopo tp, DGeom<R> g, DForcing<R>
             }
             nz = nzmax - 1;
             {
-                const A a = -((A)kv[nz] * zinv1 * zinv * ((A)ar[nz] / (A)av[nz]));
+                A a = -((A)kv[nz] * zinv1 * zinv * ((A)ar[nz] / (A)av[nz]));
                 b = -a + (A)hn[nz];
+                if (wimpl) {  // :1207-1216
+                    const A v = zinv * ((A)ar[nz] / (A)av[nz]);
+                    a = a + fmin(0.0, (A)wi[nz]) * v;
+                    b = b + fmax(0.0, (A)wi[nz]) * v;
+                }
                 Tm = T0;
                 T0 = Tp1;
                 dz = (A)hn[nz];
@@ -865,6 +1053,11 @@ void Launch<R>::update(const DTopo &tp, const DGeom<R> &g, DTracers<R> &tr, doub
                        cudaStream_t s) {
     (void)fct;
     k_update<R><<<grid_for(tp.N2, kWarpsPerBlock), kThreads, 0, s>>>(tp, g, tr, (R)dt, mode);
+}
+template <typename R>
+void Launch<R>::lo_impl(const DTopo &tp, const DGeom<R> &g, const DForcing<R> &f, DTracers<R> &tr, double dt,
+                        double *scratch, cudaStream_t s) {
+    k_lo_impl<R><<<(tp.N2 + 127) / 128, 128, 0, s>>>(tp, g, f, tr, dt, scratch);
 }
 template <typename R>
 void Launch<R>::vdiff(const DTopo &tp, const DGeom<R> &g, const DForcing<R> &f, DTracers<R> &tr, double dt,

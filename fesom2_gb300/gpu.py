@@ -89,6 +89,8 @@ _SIGS = {
     "fesom_gpu_tracer_device_ptr": ([_P, C.c_int32, C.POINTER(_P), C.POINTER(_P)], C.c_int),
     "fesom_gpu_tracer_tail": ([_P, C.c_int32, _P, C.c_double, _P, _P, _P, _P, _P, C.POINTER(_P)], C.c_int),
     "fesom_gpu_set_hdiff": ([_P, _P], C.c_int),
+    "fesom_gpu_set_wsplit": ([_P, C.c_int32], C.c_int),
+    "fesom_gpu_vdiff_impl_wi": ([_P, C.c_double, C.POINTER(TraCfg), _P, _P, _P, _P], C.c_int),
     "fesom_gpu_diff_hor": ([_P, C.c_double, _P, _P, _P], C.c_int),
     "fesom_gpu_diff_ver_expl": ([_P, C.c_double, _P, _P, _P, _P], C.c_int),
     "fesom_gpu_step_host_f32": ([_P, C.c_double, _P, _P, _P, _P, _P, _P, C.POINTER(_P), C.POINTER(_P),
@@ -251,11 +253,18 @@ class Context:
                                            _p(we), C.byref(cfg), _p(t64), _p(tab64), _p(dh), _p(dv)))
         return dh, dv
 
-    def vdiff_impl(self, forcing, cfg: TraCfg, values, dt=None, bc=None):
+    def vdiff_impl(self, forcing, cfg: TraCfg, values, dt=None, bc=None, wimpl=False):
+        """diff_ver_part_impl_ale on ``values`` in place; ``wimpl``: with the w_i terms of a split
+        vertical velocity (forcing.w_i)."""
         Kv = _c64(forcing.Kv)
         bcs = _c64(forcing.bc_surface if bc is None else bc)
-        self._chk(self.L.fesom_gpu_vdiff_impl(self.h, float(forcing.dt if dt is None else dt), C.byref(cfg), _p(Kv),
-                                              _p(bcs), _p(values)))
+        wi = _c64(forcing.w_i) if wimpl else None
+        self._chk(self.L.fesom_gpu_vdiff_impl_wi(self.h, float(forcing.dt if dt is None else dt), C.byref(cfg),
+                                                 _p(Kv), _p(bcs), _p(wi), _p(values)))
+
+    def set_wsplit(self, on: bool):
+        """dynamics%use_wsplit for every later step (fesom_gpu_set_wsplit)."""
+        self._chk(self.L.fesom_gpu_set_wsplit(self.h, 1 if on else 0))
 
     # -- whole step ------------------------------------------------------------
     def tracer_step(self, forcing, cfgs: Sequence[TraCfg], values: Sequence[np.ndarray],

@@ -831,6 +831,26 @@ def make_forcing(mesh: Mesh, kind: str, seed: int = 11, dt: float = 600.0,
                    bc_surface=np.zeros(mesh.nod2D), dt=float(dt))
 
 
+def split_vertical_velocity(mesh: Mesh, forcing: Forcing, maxcfl: float) -> Forcing:
+    """The forcing with w split into an explicit part w_e and an implicit part w_i as
+    compute_Wvel_split does (src/oce_ale.F90:3034-3047): where the vertical Courant number
+    exceeds maxcfl, dd = (CFL - maxcfl) / maxcfl, w_e = w / (1 + dd), w_i = dd w / (1 + dd).
+    The Courant number of an interface here is |w| dt over the thinner adjacent layer (a
+    stand-in for the model's CFL_z diagnostic)."""
+    W = forcing.w
+    N2, nl = W.shape
+    h = np.where(mesh.hnode > 0, mesh.hnode, np.inf)
+    up = np.concatenate([np.full((N2, 1), np.inf), h], axis=1)      # layer above interface k
+    dn = np.concatenate([h, np.full((N2, 1), np.inf)], axis=1)      # layer below interface k
+    hmin = np.minimum(up, dn)
+    cfl = np.where(np.isfinite(hmin), np.abs(W) * forcing.dt / hmin, 0.0)
+    dd = np.maximum(cfl - maxcfl, 0.0) / max(maxcfl, 1e-12)
+    split = cfl > maxcfl
+    we = np.where(split, (1.0 / (1.0 + dd)) * W, W)
+    wi = np.where(split, (dd / (1.0 + dd)) * W, 0.0)
+    return dataclasses.replace(forcing, w_e=np.ascontiguousarray(we), w_i=np.ascontiguousarray(wi))
+
+
 def node_depth_mid(mesh: Mesh) -> np.ndarray:
     """Layer mid-depth (positive down, metres) per node-layer."""
     return -mesh.Z_3d_n

@@ -42,7 +42,7 @@ extern "C" {
 /* status codes */
 #define FESOM_OK 0
 #define FESOM_ERR_ARG 1          /* bad argument / null pointer / size mismatch */
-#define FESOM_ERR_SCHEME 2       /* unknown or unsupported advection scheme (PPM, CDIFF, w-split) */
+#define FESOM_ERR_SCHEME 2       /* unknown advection scheme or limiter */
 #define FESOM_ERR_MESH 3         /* mesh fails validation (index out of range, < 2 layers, ...) */
 #define FESOM_ERR_CUDA 4         /* a CUDA runtime call failed */
 #define FESOM_ERR_NOMEM 5        /* device allocation failed */
@@ -60,8 +60,8 @@ extern "C" {
 #define FESOM_ADV_HOR_UPW1 2
 #define FESOM_ADV_VER_QR4C 0
 #define FESOM_ADV_VER_UPW1 1
-#define FESOM_ADV_VER_CDIFF 2    /* rejected with FESOM_ERR_SCHEME */
-#define FESOM_ADV_VER_PPM 3      /* rejected with FESOM_ERR_SCHEME */
+#define FESOM_ADV_VER_CDIFF 2    /* adv_tra_ver_cdiff, src/oce_adv_tra_ver.F90:635-695 */
+#define FESOM_ADV_VER_PPM 3      /* adv_tra_vert_ppm, src/oce_adv_tra_ver.F90:438-631 */
 #define FESOM_ADV_LIM_NONE 0
 #define FESOM_ADV_LIM_FCT 1
 
@@ -168,6 +168,10 @@ int fesom_gpu_adv_tra(fesom_gpu_ctx *ctx, double dt, const double *vel, const do
  * nzmin; values (nl-1, nod2D) updated in place. */
 int fesom_gpu_vdiff_impl(fesom_gpu_ctx *ctx, double dt, const fesom_tra_cfg *cfg, const double *Kv,
                          const double *bc_surf, double *values);
+/* The same with the w_i terms of a split vertical velocity (wi(nl, nod2D); NULL: none) for a
+ * tracer without the limiter, as diff_ver_part_impl_ale with do_wimpl. */
+int fesom_gpu_vdiff_impl_wi(fesom_gpu_ctx *ctx, double dt, const fesom_tra_cfg *cfg, const double *Kv,
+                            const double *bc_surf, const double *wi, double *values);
 
 /* ---- the whole tracer step for all tracers (host arrays) ----------------- */
 /* values[t] (nl-1, nod2D), valuesold[t] (ab_order-1, nl-1, nod2D) updated in
@@ -246,6 +250,14 @@ int fesom_gpu_tracer_device_ptr(fesom_gpu_ctx *ctx, int32_t tr, void **values, v
  * fesom_gpu_set_hdiff makes every later step of the context add it (NULL: none, as K_hor = 0);
  * the FP64 and FP32 forms both take it. */
 int fesom_gpu_set_hdiff(fesom_gpu_ctx *ctx, const double *Ki);
+/* dynamics%use_wsplit (src/MOD_DYN.F90:156, off by default): the vertical velocity is split
+ * into the explicit w_e and the implicit w_i (the forcing's we / wi).  With it on, FCT tracers
+ * advect their LO values implicitly by w_i (adv_tra_vert_impl, src/oce_adv_tra_ver.F90:90-240)
+ * and take the upwind flux of the full w as the LO part of the antidiffusive vertical flux
+ * (src/oce_adv_tra_driver.F90:323-334); tracers without the limiter add w_i to the implicit
+ * vertical solve (src/oce_ale_tracer.F90:961, 1134-1216).  Applies to every later step and to
+ * fesom_gpu_adv_tra, which then needs wi. */
+int fesom_gpu_set_wsplit(fesom_gpu_ctx *ctx, int32_t on);
 /* The routine alone (FP64 contexts): del_ttf += the edge diffusion fluxes of the element
  * gradients of values, in ascending edge order. */
 int fesom_gpu_diff_hor(fesom_gpu_ctx *ctx, double dt, const double *Ki, const double *values, double *del_ttf);

@@ -18,7 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
 HOR = {"MUSCL": 0, "MFCT": 1, "UPW1": 2}
-VER = {"QR4C": 0, "UPW1": 1}
+VER = {"QR4C": 0, "UPW1": 1, "CDIFF": 2, "PPM": 3}
 
 _P = C.c_void_p
 
@@ -35,7 +35,7 @@ class _OrMesh(C.Structure):
 
 class _OrCfg(C.Structure):
     _fields_ = [("hor", C.c_int), ("ver", C.c_int), ("lim_fct", C.c_int), ("ph", C.c_double),
-                ("pv", C.c_double), ("ab_order", C.c_int), ("i_vert_diff", C.c_int)]
+                ("pv", C.c_double), ("ab_order", C.c_int), ("i_vert_diff", C.c_int), ("wsplit", C.c_int)]
 
 
 class _OrWork(C.Structure):
@@ -83,9 +83,10 @@ def _ptr(a: Optional[np.ndarray]):
     return None if a is None else a.ctypes.data_as(_P)
 
 
-def cfg_struct(hor="MUSCL", ver="QR4C", lim="FCT", ph=0.0, pv=1.0, ab_order=2, i_vert_diff=True) -> _OrCfg:
+def cfg_struct(hor="MUSCL", ver="QR4C", lim="FCT", ph=0.0, pv=1.0, ab_order=2, i_vert_diff=True,
+               wsplit=False) -> _OrCfg:
     return _OrCfg(HOR[hor], VER[ver], 1 if lim == "FCT" else 0, float(ph), float(pv), int(ab_order),
-                  1 if i_vert_diff else 0)
+                  1 if i_vert_diff else 0, 1 if wsplit else 0)
 
 
 class OracleMesh:
@@ -173,9 +174,32 @@ class OracleMesh:
         lib().or_diff_ver_part_expl_ale(C.byref(self.s), C.c_double(dt), _ptr(Kv), _ptr(flux), _ptr(values),
                                         _ptr(del_ttf))
 
-    def diff_ver_part_impl_ale(self, forcing, values, dt=None) -> None:
-        lib().or_diff_ver_part_impl_ale(C.byref(self.s), C.c_double(forcing.dt if dt is None else dt),
-                                        _ptr(forcing.Kv), _ptr(forcing.bc_surface), _ptr(values))
+    def diff_ver_part_impl_ale(self, forcing, values, dt=None, wimpl=False) -> None:
+        """In place on ``values``; ``wimpl``: with the implicit advection by forcing.w_i."""
+        lib().or_diff_ver_part_impl_ale_w(C.byref(self.s), C.c_double(forcing.dt if dt is None else dt),
+                                          _ptr(forcing.Kv), _ptr(forcing.bc_surface),
+                                          _ptr(forcing.w_i) if wimpl else None, 1 if wimpl else 0, _ptr(values))
+
+    def adv_tra_vert_impl(self, W, values, dt) -> None:
+        """adv_tra_vert_impl in place on ``values``."""
+        lib().or_adv_tra_vert_impl(C.byref(self.s), C.c_double(dt), _ptr(W), _ptr(values))
+
+    def ver_flux(self, scheme, W, values, dt, flux=None, init_zero=True) -> np.ndarray:
+        """One vertical flux routine (UPW1, QR4C with pv = 1, CDIFF, PPM) into flux(nod2D, nl)."""
+        m = self.mesh
+        out = np.zeros((m.nod2D, m.nl)) if flux is None else flux
+        z = 1 if init_zero else 0
+        if scheme == "UPW1":
+            lib().or_adv_tra_ver_upw1(C.byref(self.s), _ptr(W), _ptr(values), _ptr(out), z)
+        elif scheme == "QR4C":
+            lib().or_adv_tra_ver_qr4c(C.byref(self.s), _ptr(W), _ptr(values), C.c_double(1.0), _ptr(out), z)
+        elif scheme == "CDIFF":
+            lib().or_adv_tra_ver_cdiff(C.byref(self.s), _ptr(W), _ptr(values), _ptr(out), z)
+        elif scheme == "PPM":
+            lib().or_adv_tra_vert_ppm(C.byref(self.s), C.c_double(dt), _ptr(W), _ptr(values), _ptr(out), z)
+        else:
+            raise ValueError(scheme)
+        return out
 
 
 class TailCfg(C.Structure):

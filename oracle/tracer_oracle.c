@@ -444,6 +444,153 @@ void or_adv_tra_ver_qr4c(const or_mesh *m, const double *W, const double *ttf, d
     }
 }
 
+/* adv_tra_ver_cdiff (src/oce_adv_tra_ver.F90:635-695): centred interface values; the flux
+ * of the bottom interface is left as it was (only nzmin..nlevels-1 are written) */
+void or_adv_tra_ver_cdiff(const or_mesh *m, const double *W, const double *ttf, double *flux, int init_zero) {
+    const int NL = m->nl, L1 = NL - 1;
+    if (init_zero) memset(flux, 0, sizeof(double) * (size_t)NL * (size_t)m->nod2D);
+    OMP_FOR
+    for (int n = 0; n < m->nod2D; n++) {
+        double tvert[NL + 2];
+        const int nzmax = m->nlevels_nod2D[n] - 1, nzmin = m->ulevels_nod2D[n];
+        tvert[nzmin] = -(W[IXN(nzmin, n)] * ttf[IX1(nzmin, n)] * m->area[IXN(nzmin, n)]);
+        tvert[nzmax + 1] = 0.0;
+        for (int nz = nzmin + 1; nz <= nzmax; nz++) {
+            double tv = 0.5 * (ttf[IX1(nz - 1, n)] + ttf[IX1(nz, n)]);
+            tvert[nz] = -(tv * W[IXN(nz, n)] * m->area[IXN(nz, n)]);
+        }
+        for (int nz = nzmin; nz <= nzmax; nz++) flux[IXN(nz, n)] = tvert[nz] - flux[IXN(nz, n)];
+    }
+}
+
+/* Fortran sign(1.0, b): the sign of b, -1 for -0.0 as well */
+static inline double sign1(double b) { return signbit(b) ? -1.0 : 1.0; }
+static inline double min3(double a, double b, double c) { double x = a < b ? a : b; return x < c ? x : c; }
+
+/* adv_tra_vert_ppm (src/oce_adv_tra_ver.F90:438-631): interface values of the non-uniform
+ * piecewise parabolic reconstruction on the new thicknesses (Colella and Woodward 1984,
+ * eqs. 1.6-1.8; centred values next to the surface and the bottom), then per layer a
+ * monotonised parabola integrated over the part swept upwind in dt (old thickness) */
+void or_adv_tra_vert_ppm(const or_mesh *m, double dt, const double *W, const double *ttf, double *flux,
+                         int init_zero) {
+    const int NL = m->nl, L1 = NL - 1;
+    if (init_zero) memset(flux, 0, sizeof(double) * (size_t)NL * (size_t)m->nod2D);
+    OMP_FOR
+    for (int n = 0; n < m->nod2D; n++) {
+        double tvert[NL + 2], tv[NL + 2];
+        const int nzmax = m->nlevels_nod2D[n], nzmin = m->ulevels_nod2D[n];
+        const double *T = &ttf[IX1(1, n)] - 1, *hn = &m->hnode_new[IX1(1, n)] - 1, *ho = &m->hnode[IX1(1, n)] - 1;
+        const double *w = &W[IXN(1, n)] - 1, *ar = &m->area[IXN(1, n)] - 1;
+        tv[nzmin] = T[nzmin];
+        tv[nzmin + 1] = 0.5 * (T[nzmin] + T[nzmin + 1]);
+        tv[nzmax - 1] = 0.5 * (T[nzmax - 2] + T[nzmax - 1]);
+        tv[nzmax] = T[nzmax - 1];
+        for (int nz = nzmin + 1; nz <= nzmax - 3; nz++) {
+            const double dzjm1 = hn[nz - 1], dzj = hn[nz], dzjp1 = hn[nz + 1], dzjp2 = hn[nz + 2];
+            double deltaj = dzj / (dzjm1 + dzj + dzjp1) *
+                            ((2.0 * dzjm1 + dzj) / (dzjp1 + dzj) * (T[nz + 1] - T[nz]) +
+                             (dzj + 2.0 * dzjp1) / (dzjm1 + dzj) * (T[nz] - T[nz - 1]));
+            double deltajp1 = dzjp1 / (dzj + dzjp1 + dzjp2) *
+                              ((2.0 * dzj + dzjp1) / (dzjp2 + dzjp1) * (T[nz + 2] - T[nz + 1]) +
+                               (dzjp1 + 2.0 * dzjp2) / (dzj + dzjp1) * (T[nz + 1] - T[nz]));
+            if ((T[nz + 1] - T[nz]) * (T[nz] - T[nz - 1]) > 0.0)
+                deltaj = min3(fabs(deltaj), 2.0 * fabs(T[nz + 1] - T[nz]), 2.0 * fabs(T[nz] - T[nz - 1])) * sign1(deltaj);
+            else
+                deltaj = 0.0;
+            if ((T[nz + 2] - T[nz + 1]) * (T[nz + 1] - T[nz]) > 0.0)
+                deltajp1 = min3(fabs(deltajp1), 2.0 * fabs(T[nz + 2] - T[nz + 1]), 2.0 * fabs(T[nz + 1] - T[nz])) *
+                           sign1(deltajp1);
+            else
+                deltajp1 = 0.0;
+            tv[nz + 1] = T[nz] + dzj / (dzj + dzjp1) * (T[nz + 1] - T[nz]) +
+                         1.0 / (dzjm1 + dzj + dzjp1 + dzjp2) *
+                             ((2.0 * dzjp1 * dzj) / (dzj + dzjp1) *
+                                  ((dzjm1 + dzj) / (2.0 * dzj + dzjp1) - (dzjp2 + dzjp1) / (2.0 * dzjp1 + dzj)) *
+                                  (T[nz + 1] - T[nz]) -
+                              dzj * (dzjm1 + dzj) / (2.0 * dzj + dzjp1) * deltajp1 +
+                              dzjp1 * (dzjp1 + dzjp2) / (dzj + 2.0 * dzjp1) * deltaj);
+        }
+        for (int k = 1; k <= nzmax; k++) tvert[k] = 0.0;
+        for (int nz = nzmin; nz <= nzmax - 1; nz++) {
+            if (w[nz] <= 0.0 && w[nz + 1] >= 0.0) continue;
+            double aL = tv[nz], aR = tv[nz + 1];
+            if ((aR - T[nz]) * (T[nz] - aL) <= 0.0) {
+                aL = T[nz];
+                aR = T[nz];
+            }
+            if ((aR - aL) * (T[nz] - 0.5 * (aL + aR)) > (aR - aL) * (aR - aL) / 6.0) aL = 3.0 * T[nz] - 2.0 * aR;
+            if ((aR - aL) * (T[nz] - 0.5 * (aR + aL)) < -((aR - aL) * (aR - aL) / 6.0)) aR = 3.0 * T[nz] - 2.0 * aL;
+            const double dzj = ho[nz];
+            const double aj = 6.0 * (T[nz] - 0.5 * (aL + aR));
+            if (w[nz] > 0.0) {
+                double x = fmin(w[nz] * dt / dzj, 1.0);
+                tvert[nz] = -aL - 0.5 * x * (aR - aL + (1.0 - 2.0 / 3.0 * x) * aj);
+                tvert[nz] = tvert[nz] * ar[nz] * w[nz];
+            }
+            if (w[nz + 1] < 0.0) {
+                double x = fmin(-(w[nz + 1] * dt / dzj), 1.0);
+                tvert[nz + 1] = -aR + 0.5 * x * (aR - aL - (1.0 - 2.0 / 3.0 * x) * aj);
+                tvert[nz + 1] = tvert[nz + 1] * ar[nz + 1] * w[nz + 1];
+            }
+        }
+        tvert[nzmin] = -(tv[nzmin] * w[nzmin] * ar[nzmin]);
+        tvert[nzmax] = 0.0;
+        for (int nz = nzmin; nz <= nzmax; nz++) flux[IXN(nz, n)] = tvert[nz] - flux[IXN(nz, n)];
+    }
+}
+
+/* adv_tra_vert_impl (src/oce_adv_tra_ver.F90:90-240): implicit upwind advection by W of a
+ * column field, in place (a tridiagonal solve per column on the new thicknesses) */
+void or_adv_tra_vert_impl(const or_mesh *m, double dt, const double *W, double *ttf) {
+    const int NL = m->nl, L1 = NL - 1;
+    OMP_FOR
+    for (int n = 0; n < m->nod2D; n++) {
+        double a[NL + 1], b[NL + 1], c[NL + 1], tr[NL + 1], cp[NL + 1], tp[NL + 1];
+        for (int k = 0; k <= NL; k++) a[k] = b[k] = c[k] = tr[k] = cp[k] = tp[k] = 0.0;
+        const int nzmax = m->nlevels_nod2D[n], nzmin = m->ulevels_nod2D[n];
+        const double *hn = &m->hnode_new[IX1(1, n)] - 1, *w = &W[IXN(1, n)] - 1;
+        const double *ar = &m->area[IXN(1, n)] - 1, *av = &m->areasvol[IXN(1, n)] - 1;
+        double *T = &ttf[IX1(1, n)] - 1;
+        const double zinv = 1.0 * dt;
+        int nz = nzmin;
+        a[nz] = 0.0;
+        double v_adv = zinv * ar[nz] / av[nz];
+        b[nz] = hn[nz] + w[nz] * v_adv;
+        v_adv = zinv * ar[nz + 1] / av[nz];
+        b[nz] = b[nz] - fmin(0.0, w[nz + 1]) * v_adv;
+        c[nz] = -(fmax(0.0, w[nz + 1]) * v_adv);
+        for (nz = nzmin + 1; nz <= nzmax - 2; nz++) {
+            v_adv = zinv * ar[nz] / av[nz];
+            a[nz] = fmin(0.0, w[nz]) * v_adv;
+            b[nz] = hn[nz] + fmax(0.0, w[nz]) * v_adv;
+            v_adv = zinv * ar[nz + 1] / av[nz];
+            b[nz] = b[nz] - fmin(0.0, w[nz + 1]) * v_adv;
+            c[nz] = -(fmax(0.0, w[nz + 1]) * v_adv);
+        }
+        nz = nzmax - 1;
+        v_adv = zinv * ar[nz] / av[nz];
+        a[nz] = fmin(0.0, w[nz]) * v_adv;
+        b[nz] = hn[nz] + fmax(0.0, w[nz]) * v_adv;
+        c[nz] = 0.0;
+        nz = nzmin;
+        tr[nz] = -((b[nz] - hn[nz]) * T[nz]) - c[nz] * T[nz + 1];
+        for (nz = nzmin + 1; nz <= nzmax - 2; nz++)
+            tr[nz] = -(a[nz] * T[nz - 1]) - (b[nz] - hn[nz]) * T[nz] - c[nz] * T[nz + 1];
+        nz = nzmax - 1;
+        tr[nz] = -(a[nz] * T[nz - 1]) - (b[nz] - hn[nz]) * T[nz];
+        cp[nzmin] = c[nzmin] / b[nzmin];
+        tp[nzmin] = tr[nzmin] / b[nzmin];
+        for (nz = nzmin + 1; nz <= nzmax - 1; nz++) {
+            double mm = b[nz] - cp[nz - 1] * a[nz];
+            cp[nz] = c[nz] / mm;
+            tp[nz] = (tr[nz] - tp[nz - 1] * a[nz]) / mm;
+        }
+        tr[nzmax - 1] = tp[nzmax - 1];
+        for (nz = nzmax - 2; nz >= nzmin; nz--) tr[nz] = tp[nz] - cp[nz] * tr[nz + 1];
+        for (nz = nzmin; nz <= nzmax - 1; nz++) T[nz] = T[nz] + tr[nz];
+    }
+}
+
 /* ========================================================================== */
 /* FCT limiter (src/oce_adv_tra_fct.F90:72-512)                                */
 /* ========================================================================== */
@@ -640,10 +787,9 @@ void or_oce_tra_adv_flux2dtracer(const or_mesh *m, double dt, double *dttf_h, do
 int or_do_oce_adv_tra(const or_mesh *m, double dt, const double *vel, const double *W, const double *WI,
                       const double *WE, const or_tra_cfg *c, const double *ttf, const double *ttfAB,
                       or_work *w) {
-    (void)WI;
     const int NL = m->nl, L1 = NL - 1;
     locks_ensure(m->nod2D);
-    if (c->hor < 0 || c->hor > 2 || c->ver < 0 || c->ver > 1) return 1;
+    if (c->hor < 0 || c->hor > 2 || c->ver < 0 || c->ver > 3) return 1;
     double *fct_LO = w->fct_LO, *afh = w->adv_flux_hor, *afv = w->adv_flux_ver;
     if (c->lim_fct) {
         or_adv_tra_hor_upw1(m, vel, ttf, afh, 1);
@@ -668,6 +814,12 @@ int or_do_oce_adv_tra(const or_mesh *m, double dt, const double *vel, const doub
                                       (fct_LO[IX1(nz, n)] + (afv[IXN(nz, n)] - afv[IXN(nz + 1, n)])) * dt /
                                           m->areasvol[IXN(nz, n)]) /
                                      m->hnode_new[IX1(nz, n)];
+        if (c->wsplit) {
+            /* w split (:323-334): the implicit part w_i advects LO implicitly; the LO part of
+             * the antidiffusive vertical flux is the upwind flux of the full w */
+            or_adv_tra_vert_impl(m, dt, WI, fct_LO);
+            or_adv_tra_ver_upw1(m, W, ttf, afv, 1);
+        }
     }
     int zero = c->lim_fct ? 0 : 1;
     if (c->hor == OR_HOR_MUSCL)
@@ -679,6 +831,10 @@ int or_do_oce_adv_tra(const or_mesh *m, double dt, const double *vel, const doub
     const double *pw = c->lim_fct ? W : WE;
     if (c->ver == OR_VER_QR4C)
         or_adv_tra_ver_qr4c(m, pw, ttfAB, c->pv, afv, zero);
+    else if (c->ver == OR_VER_CDIFF)
+        or_adv_tra_ver_cdiff(m, pw, ttfAB, afv, zero);
+    else if (c->ver == OR_VER_PPM)
+        or_adv_tra_vert_ppm(m, dt, pw, ttfAB, afv, zero);
     else
         or_adv_tra_ver_upw1(m, pw, ttfAB, afv, zero);
     if (c->lim_fct) {
@@ -695,6 +851,11 @@ int or_do_oce_adv_tra(const or_mesh *m, double dt, const double *vel, const doub
 /* ========================================================================== */
 void or_diff_ver_part_impl_ale(const or_mesh *m, double dt, const double *Kv, const double *bc_surf,
                                double *values) {
+    or_diff_ver_part_impl_ale_w(m, dt, Kv, bc_surf, NULL, 0, values);
+}
+
+void or_diff_ver_part_impl_ale_w(const or_mesh *m, double dt, const double *Kv, const double *bc_surf,
+                                 const double *WI, int do_wimpl, double *values) {
     const int NL = m->nl, L1 = NL - 1;
     OMP_FOR
     for (int n = 0; n < m->nod2D; n++) {
@@ -717,9 +878,18 @@ void or_diff_ver_part_impl_ale(const or_mesh *m, double dt, const double *Kv, co
         int nz = nzmin;
         double zinv2 = 1.0 / (Z_n[nz] - Z_n[nz + 1]);
         double zinv = 1.0 * dt;
+        const double *wi = WI ? &WI[IXN(1, n)] - 1 : NULL;
+        double v_adv;
         a[nz] = 0.0;
         c[nz] = -(kv[nz + 1] * zinv2 * zinv * ar[nz + 1] / av[nz]);
         b[nz] = -c[nz] + hn[nz];
+        if (do_wimpl) { /* implicit part of the split vertical velocity (:1134-1147) */
+            v_adv = zinv * (ar[nz] / av[nz]);
+            b[nz] = b[nz] + wi[nz] * v_adv;
+            v_adv = zinv * ar[nz + 1] / av[nz];
+            b[nz] = b[nz] - fmin(0.0, wi[nz + 1]) * v_adv;
+            c[nz] = c[nz] - fmax(0.0, wi[nz + 1]) * v_adv;
+        }
         double zinv1 = zinv2;
         for (nz = nzmin + 1; nz <= nzmax - 2; nz++) {
             zinv2 = 1.0 / (Z_n[nz] - Z_n[nz + 1]);
@@ -727,12 +897,25 @@ void or_diff_ver_part_impl_ale(const or_mesh *m, double dt, const double *Kv, co
             c[nz] = -(kv[nz + 1] * zinv2 * zinv * ar[nz + 1] / av[nz]);
             b[nz] = -a[nz] - c[nz] + hn[nz];
             zinv1 = zinv2;
+            if (do_wimpl) { /* :1176-1189 */
+                v_adv = zinv * (ar[nz] / av[nz]);
+                a[nz] = a[nz] + fmin(0.0, wi[nz]) * v_adv;
+                b[nz] = b[nz] + fmax(0.0, wi[nz]) * v_adv;
+                v_adv = zinv * ar[nz + 1] / av[nz];
+                b[nz] = b[nz] - fmin(0.0, wi[nz + 1]) * v_adv;
+                c[nz] = c[nz] - fmax(0.0, wi[nz + 1]) * v_adv;
+            }
         }
         nz = nzmax - 1;
         zinv = 1.0 * dt;
         a[nz] = -(kv[nz] * zinv1 * zinv * (ar[nz] / av[nz]));
         c[nz] = 0.0;
         b[nz] = -a[nz] + hn[nz];
+        if (do_wimpl) { /* :1207-1216 */
+            v_adv = zinv * (ar[nz] / av[nz]);
+            a[nz] = a[nz] + fmin(0.0, wi[nz]) * v_adv;
+            b[nz] = b[nz] + fmax(0.0, wi[nz]) * v_adv;
+        }
         nz = nzmin;
         double dz = hn[nz];
         tr[nz] = -((b[nz] - dz) * T[nz]) - c[nz] * T[nz + 1];
@@ -886,7 +1069,8 @@ int or_tracer_step_ex(const or_mesh *m, const or_tra_cfg *c, double dt, const do
             values[i] = values[i] + w->del_ttf[i] / m->hnode_new[i];
         }
     }
-    if (c->i_vert_diff) or_diff_ver_part_impl_ale(m, dt, Kv, bc_surf, values);
+    /* the w_i part goes into the implicit solve only without the limiter (:961) */
+    if (c->i_vert_diff) or_diff_ver_part_impl_ale_w(m, dt, Kv, bc_surf, WI, c->wsplit && !c->lim_fct, values);
     return 0;
 }
 

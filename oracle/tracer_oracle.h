@@ -48,13 +48,14 @@ typedef struct or_mesh {
 
 /* scheme tuple of T_TRACER_DATA (src/MOD_TRACER.F90:10-27) */
 enum { OR_HOR_MUSCL = 0, OR_HOR_MFCT = 1, OR_HOR_UPW1 = 2 };
-enum { OR_VER_QR4C = 0, OR_VER_UPW1 = 1 };
+enum { OR_VER_QR4C = 0, OR_VER_UPW1 = 1, OR_VER_CDIFF = 2, OR_VER_PPM = 3 };
 typedef struct or_tra_cfg {
     int hor, ver;
     int lim_fct;       /* 1: 'FCT', 0: no limiter */
     double ph, pv;     /* tra_adv_ph / tra_adv_pv */
     int ab_order;      /* 2 or 3 */
     int i_vert_diff;   /* implicit vertical diffusion on/off */
+    int wsplit;        /* dynamics%use_wsplit: vertical velocity split into w_e + w_i */
 } or_tra_cfg;
 
 /* T_TRACER_WORK (src/MOD_TRACER.F90:30-72) plus the module arrays tr_xy/tr_z */
@@ -95,6 +96,10 @@ void or_adv_tra_hor_muscl(const or_mesh *m, const double *vel, const double *ttf
 void or_adv_tra_hor_mfct(const or_mesh *m, const double *vel, const double *ttf, double num_ord, double *flux,
                          const double *edge_up_dn_grad, int init_zero);
 void or_adv_tra_ver_upw1(const or_mesh *m, const double *W, const double *ttf, double *flux, int init_zero);
+void or_adv_tra_ver_cdiff(const or_mesh *m, const double *W, const double *ttf, double *flux, int init_zero);
+void or_adv_tra_vert_ppm(const or_mesh *m, double dt, const double *W, const double *ttf, double *flux,
+                         int init_zero);
+void or_adv_tra_vert_impl(const or_mesh *m, double dt, const double *W, double *ttf);
 void or_adv_tra_ver_qr4c(const or_mesh *m, const double *W, const double *ttf, double num_ord, double *flux,
                          int init_zero);
 void or_oce_tra_adv_fct(const or_mesh *m, double dt, const double *ttf, const double *lo, double *adf_h,
@@ -112,6 +117,10 @@ int or_do_oce_adv_tra(const or_mesh *m, double dt, const double *vel, const doub
  * bc_surf(n) is the bc_surface() value added at nzmin. */
 void or_diff_ver_part_impl_ale(const or_mesh *m, double dt, const double *Kv, const double *bc_surf,
                                double *values);
+/* the same with the implicit advection by the w_i part of a split vertical velocity
+ * (do_wimpl: split velocity and no limiter, :961, 1134-1216) */
+void or_diff_ver_part_impl_ale_w(const or_mesh *m, double dt, const double *Kv, const double *bc_surf,
+                                 const double *WI, int do_wimpl, double *values);
 
 /* diff_part_hor_redi (src/oce_ale_tracer.F90:1526-1689) with Redi off: edge fluxes of
  * Ki-weighted element gradients tr_xy, scattered into del_ttf in ascending edge order. */

@@ -9,6 +9,8 @@ fesom2_gb300.mesh; level numbers are 1-based as in the Fortran.
 """
 from __future__ import annotations
 
+import math
+
 import numpy as np
 
 R_EARTH = 6367500.0
@@ -345,7 +347,7 @@ class Ref:
         return adf_h, adf_v, {"tvert_max": tmax, "tvert_min": tmin}
 
     # ---- oce_adv_tra_driver.F90 ----------------------------------------------
-    def adv_tra(self, dt, vel, W, WE, T, TAB, hor, ver, lim, ph, pv, G, nbl):
+    def adv_tra(self, dt, vel, W, WE, T, TAB, hor, ver, lim, ph, pv, G, nbl, WI=None, wsplit=False):
         m = self.m
         N2, L1, nl = m.nod2D, self.L1, self.nl
         wet = self.wet
@@ -357,6 +359,9 @@ class Ref:
             LOs = self._scatter(fh, self.smask)
             fv = self.ver_upw1(WE, T, np.zeros((N2, nl)))
             LO = np.where(wet, (T * m.hnode + (LOs + (fv[:, :L1] - fv[:, 1:])) * dt / av) / m.hnode_new, LOs)
+            if wsplit:
+                LO = vert_impl(m, dt, WI, LO)
+                fv = self.ver_upw1(W, T, np.zeros((N2, nl)))
             flux_h, flux_v = fh, fv
             pw = W
         else:
@@ -370,6 +375,10 @@ class Ref:
             flux_h = self.hor_upw1(vel, TAB, flux_h)
         if ver == "QR4C":
             flux_v = self.ver_qr4c(pw, TAB, pv, flux_v)
+        elif ver == "CDIFF":
+            flux_v = ver_cdiff(m, pw, TAB, flux_v)
+        elif ver == "PPM":
+            flux_v = ver_ppm(m, dt, pw, TAB, flux_v)
         else:
             flux_v = self.ver_upw1(pw, TAB, flux_v)
         dv = np.zeros((N2, L1))
@@ -459,16 +468,225 @@ class Ref:
         return T
 
     # ---- whole per-tracer body ----------------------------------------------------
-    def tracer_step(self, forcing, T, Told, updn, nbl, hor="MUSCL", ver="QR4C", lim="FCT", ph=0.0, pv=1.0):
+    def tracer_step(self, forcing, T, Told, updn, nbl, hor="MUSCL", ver="QR4C", lim="FCT", ph=0.0, pv=1.0,
+                    wsplit=False):
         m = self.m
         dt = forcing.dt
         TAB = -((0.5 + EPS_AB) * Told) + (1.5 + EPS_AB) * T
         Told_new = T.copy()
         G = self.fill_up_dn_grad(self.tr_xy(T), updn)
-        dh, dv, _ = self.adv_tra(dt, forcing.uv, forcing.w, forcing.w_e, T, TAB, hor, ver, lim, ph, pv, G, nbl)
+        dh, dv, _ = self.adv_tra(dt, forcing.uv, forcing.w, forcing.w_e, T, TAB, hor, ver, lim, ph, pv, G, nbl,
+                                 WI=forcing.w_i, wsplit=wsplit)
         wet = self.wet
         dl = 0.0 + dh + dv
         dl = np.where(wet, dl + T * (m.hnode - m.hnode_new), dl)
         Tn = np.where(wet, T + dl / m.hnode_new, T)
-        Tn = self.vdiff(dt, forcing.Kv, forcing.bc_surface, Tn)
+        if wsplit and lim != "FCT":
+            Tn = vdiff_wimpl(m, dt, forcing.Kv, forcing.bc_surface, forcing.w_i, Tn)
+        else:
+            Tn = self.vdiff(dt, forcing.Kv, forcing.bc_surface, Tn)
         return Tn, Told_new
+
+
+# ---------------------------------------------------------------------------
+# column routines as plain loops (small meshes): vertical schemes CDIFF and PPM,
+# implicit advection by the w_i part of a split vertical velocity
+# ---------------------------------------------------------------------------
+def ver_cdiff(m, W, T, flux):
+    """adv_tra_ver_cdiff (oce_adv_tra_ver.F90:635-695); flux (nod2D, nl) updated and returned."""
+    flux = flux.copy()
+    for n in range(m.nod2D):
+        nzmax = int(m.nlevels_nod2D[n]) - 1
+        nzmin = int(m.ulevels_nod2D[n])
+        tvert = {nzmin: -(W[n, nzmin - 1] * T[n, nzmin - 1] * m.area[n, nzmin - 1]), nzmax + 1: 0.0}
+        for nz in range(nzmin + 1, nzmax + 1):
+            tv = 0.5 * (T[n, nz - 2] + T[n, nz - 1])
+            tvert[nz] = -(tv * W[n, nz - 1] * m.area[n, nz - 1])
+        for nz in range(nzmin, nzmax + 1):
+            flux[n, nz - 1] = tvert[nz] - flux[n, nz - 1]
+    return flux
+
+
+def _sign1(x):
+    return -1.0 if math.copysign(1.0, x) < 0 else 1.0
+
+
+def ver_ppm(m, dt, W, T, flux):
+    """adv_tra_vert_ppm (oce_adv_tra_ver.F90:438-631)."""
+    flux = flux.copy()
+    for n in range(m.nod2D):
+        nzmax = int(m.nlevels_nod2D[n])
+        nzmin = int(m.ulevels_nod2D[n])
+        t = lambda k: T[n, k - 1]
+        h = lambda k: m.hnode_new[n, k - 1]
+        w = lambda k: W[n, k - 1]
+        tv = {}
+        tv[nzmin] = t(nzmin)
+        tv[nzmin + 1] = 0.5 * (t(nzmin) + t(nzmin + 1))
+        tv[nzmax - 1] = 0.5 * (t(nzmax - 2) + t(nzmax - 1))
+        tv[nzmax] = t(nzmax - 1)
+        for nz in range(nzmin + 1, nzmax - 2):
+            a0, a1, a2, a3 = h(nz - 1), h(nz), h(nz + 1), h(nz + 2)
+            dj = a1 / (a0 + a1 + a2) * ((2.0 * a0 + a1) / (a2 + a1) * (t(nz + 1) - t(nz))
+                                        + (a1 + 2.0 * a2) / (a0 + a1) * (t(nz) - t(nz - 1)))
+            dj1 = a2 / (a1 + a2 + a3) * ((2.0 * a1 + a2) / (a3 + a2) * (t(nz + 2) - t(nz + 1))
+                                         + (a2 + 2.0 * a3) / (a1 + a2) * (t(nz + 1) - t(nz)))
+            if (t(nz + 1) - t(nz)) * (t(nz) - t(nz - 1)) > 0.0:
+                dj = min(abs(dj), 2.0 * abs(t(nz + 1) - t(nz)), 2.0 * abs(t(nz) - t(nz - 1))) * _sign1(dj)
+            else:
+                dj = 0.0
+            if (t(nz + 2) - t(nz + 1)) * (t(nz + 1) - t(nz)) > 0.0:
+                dj1 = min(abs(dj1), 2.0 * abs(t(nz + 2) - t(nz + 1)), 2.0 * abs(t(nz + 1) - t(nz))) * _sign1(dj1)
+            else:
+                dj1 = 0.0
+            tv[nz + 1] = (t(nz) + a1 / (a1 + a2) * (t(nz + 1) - t(nz))
+                          + 1.0 / (a0 + a1 + a2 + a3)
+                          * ((2.0 * a2 * a1) / (a1 + a2) * ((a0 + a1) / (2.0 * a1 + a2) - (a3 + a2) / (2.0 * a2 + a1))
+                             * (t(nz + 1) - t(nz))
+                             - a1 * (a0 + a1) / (2.0 * a1 + a2) * dj1
+                             + a2 * (a2 + a3) / (a1 + 2.0 * a2) * dj))
+        tvert = {k: 0.0 for k in range(1, nzmax + 1)}
+        for nz in range(nzmin, nzmax):
+            if w(nz) <= 0.0 and w(nz + 1) >= 0.0:
+                continue
+            aL, aR = tv[nz], tv[nz + 1]
+            if (aR - t(nz)) * (t(nz) - aL) <= 0.0:
+                aL = aR = t(nz)
+            if (aR - aL) * (t(nz) - 0.5 * (aL + aR)) > (aR - aL) * (aR - aL) / 6.0:
+                aL = 3.0 * t(nz) - 2.0 * aR
+            if (aR - aL) * (t(nz) - 0.5 * (aR + aL)) < -((aR - aL) * (aR - aL) / 6.0):
+                aR = 3.0 * t(nz) - 2.0 * aL
+            dz = m.hnode[n, nz - 1]
+            aj = 6.0 * (t(nz) - 0.5 * (aL + aR))
+            if w(nz) > 0.0:
+                x = min(w(nz) * dt / dz, 1.0)
+                v = -aL - 0.5 * x * (aR - aL + (1.0 - 2.0 / 3.0 * x) * aj)
+                tvert[nz] = v * m.area[n, nz - 1] * w(nz)
+            if w(nz + 1) < 0.0:
+                x = min(-(w(nz + 1) * dt / dz), 1.0)
+                v = -aR + 0.5 * x * (aR - aL - (1.0 - 2.0 / 3.0 * x) * aj)
+                tvert[nz + 1] = v * m.area[n, nz] * w(nz + 1)
+        tvert[nzmin] = -(tv[nzmin] * w(nzmin) * m.area[n, nzmin - 1])
+        tvert[nzmax] = 0.0
+        for nz in range(nzmin, nzmax + 1):
+            flux[n, nz - 1] = tvert[nz] - flux[n, nz - 1]
+    return flux
+
+
+def _thomas(a, b, c, tr, lo, hi):
+    cp, tp = {}, {}
+    cp[lo] = c[lo] / b[lo]
+    tp[lo] = tr[lo] / b[lo]
+    for nz in range(lo + 1, hi + 1):
+        mm = b[nz] - cp[nz - 1] * a[nz]
+        cp[nz] = c[nz] / mm
+        tp[nz] = (tr[nz] - tp[nz - 1] * a[nz]) / mm
+    x = {hi: tp[hi]}
+    for nz in range(hi - 1, lo - 1, -1):
+        x[nz] = tp[nz] - cp[nz] * x[nz + 1]
+    return x
+
+
+def vert_impl(m, dt, W, T):
+    """adv_tra_vert_impl (oce_adv_tra_ver.F90:90-240) on a copy of T."""
+    T = T.copy()
+    for n in range(m.nod2D):
+        nzmax = int(m.nlevels_nod2D[n])
+        nzmin = int(m.ulevels_nod2D[n])
+        hn = lambda k: m.hnode_new[n, k - 1]
+        ar = lambda k: m.area[n, k - 1]
+        av = lambda k: m.areasvol[n, k - 1]
+        w = lambda k: W[n, k - 1]
+        a, b, c, tr = {}, {}, {}, {}
+        zinv = 1.0 * dt
+        nz = nzmin
+        a[nz] = 0.0
+        v = zinv * ar(nz) / av(nz)
+        b[nz] = hn(nz) + w(nz) * v
+        v = zinv * ar(nz + 1) / av(nz)
+        b[nz] = b[nz] - min(0.0, w(nz + 1)) * v
+        c[nz] = -(max(0.0, w(nz + 1)) * v)
+        for nz in range(nzmin + 1, nzmax - 1):
+            v = zinv * ar(nz) / av(nz)
+            a[nz] = min(0.0, w(nz)) * v
+            b[nz] = hn(nz) + max(0.0, w(nz)) * v
+            v = zinv * ar(nz + 1) / av(nz)
+            b[nz] = b[nz] - min(0.0, w(nz + 1)) * v
+            c[nz] = -(max(0.0, w(nz + 1)) * v)
+        nz = nzmax - 1
+        v = zinv * ar(nz) / av(nz)
+        a[nz] = min(0.0, w(nz)) * v
+        b[nz] = hn(nz) + max(0.0, w(nz)) * v
+        c[nz] = 0.0
+        t = lambda k: T[n, k - 1]
+        tr[nzmin] = -((b[nzmin] - hn(nzmin)) * t(nzmin)) - c[nzmin] * t(nzmin + 1)
+        for nz in range(nzmin + 1, nzmax - 1):
+            tr[nz] = -(a[nz] * t(nz - 1)) - (b[nz] - hn(nz)) * t(nz) - c[nz] * t(nz + 1)
+        nz = nzmax - 1
+        tr[nz] = -(a[nz] * t(nz - 1)) - (b[nz] - hn(nz)) * t(nz)
+        x = _thomas(a, b, c, tr, nzmin, nzmax - 1)
+        for nz in range(nzmin, nzmax):
+            T[n, nz - 1] = T[n, nz - 1] + x[nz]
+    return T
+
+
+def vdiff_wimpl(m, dt, Kv, bc, WI, T):
+    """diff_ver_part_impl_ale (oce_ale_tracer.F90:907-1435) with do_wimpl, on a copy of T."""
+    T = T.copy()
+    for n in range(m.nod2D):
+        nzmax = int(m.nlevels_nod2D[n])
+        nzmin = int(m.ulevels_nod2D[n])
+        hn = lambda k: m.hnode_new[n, k - 1]
+        ar = lambda k: m.area[n, k - 1]
+        av = lambda k: m.areasvol[n, k - 1]
+        kv = lambda k: Kv[n, k - 1]
+        wi = lambda k: WI[n, k - 1]
+        zbar, Z = {}, {}
+        zbar[nzmax] = m.zbar_n_bot[n]
+        Z[nzmax - 1] = zbar[nzmax] + hn(nzmax - 1) / 2.0
+        for nz in range(nzmax - 1, nzmin, -1):
+            zbar[nz] = zbar[nz + 1] + hn(nz)
+            Z[nz - 1] = zbar[nz] + hn(nz - 1) / 2.0
+        a, b, c, tr = {}, {}, {}, {}
+        nz = nzmin
+        zinv2 = 1.0 / (Z[nz] - Z[nz + 1])
+        zinv = 1.0 * dt
+        a[nz] = 0.0
+        c[nz] = -(kv(nz + 1) * zinv2 * zinv * ar(nz + 1) / av(nz))
+        b[nz] = -c[nz] + hn(nz)
+        v = zinv * (ar(nz) / av(nz))
+        b[nz] = b[nz] + wi(nz) * v
+        v = zinv * ar(nz + 1) / av(nz)
+        b[nz] = b[nz] - min(0.0, wi(nz + 1)) * v
+        c[nz] = c[nz] - max(0.0, wi(nz + 1)) * v
+        zinv1 = zinv2
+        for nz in range(nzmin + 1, nzmax - 1):
+            zinv2 = 1.0 / (Z[nz] - Z[nz + 1])
+            a[nz] = -(kv(nz) * zinv1 * zinv * (ar(nz) / av(nz)))
+            c[nz] = -(kv(nz + 1) * zinv2 * zinv * ar(nz + 1) / av(nz))
+            b[nz] = -a[nz] - c[nz] + hn(nz)
+            zinv1 = zinv2
+            v = zinv * (ar(nz) / av(nz))
+            a[nz] = a[nz] + min(0.0, wi(nz)) * v
+            b[nz] = b[nz] + max(0.0, wi(nz)) * v
+            v = zinv * ar(nz + 1) / av(nz)
+            b[nz] = b[nz] - min(0.0, wi(nz + 1)) * v
+            c[nz] = c[nz] - max(0.0, wi(nz + 1)) * v
+        nz = nzmax - 1
+        a[nz] = -(kv(nz) * zinv1 * zinv * (ar(nz) / av(nz)))
+        c[nz] = 0.0
+        b[nz] = -a[nz] + hn(nz)
+        v = zinv * (ar(nz) / av(nz))
+        a[nz] = a[nz] + min(0.0, wi(nz)) * v
+        b[nz] = b[nz] + max(0.0, wi(nz)) * v
+        t = lambda k: T[n, k - 1]
+        tr[nzmin] = -((b[nzmin] - hn(nzmin)) * t(nzmin)) - c[nzmin] * t(nzmin + 1)
+        for nz in range(nzmin + 1, nzmax - 1):
+            tr[nz] = -(a[nz] * t(nz - 1)) - (b[nz] - hn(nz)) * t(nz) - c[nz] * t(nz + 1)
+        nz = nzmax - 1
+        tr[nz] = -(a[nz] * t(nz - 1)) - (b[nz] - hn(nz)) * t(nz)
+        tr[nzmin] = tr[nzmin] + (0.0 if bc is None else bc[n])
+        x = _thomas(a, b, c, tr, nzmin, nzmax - 1)
+        for nz in range(nzmin, nzmax):
+            T[n, nz - 1] = T[n, nz - 1] + x[nz]
+    return T

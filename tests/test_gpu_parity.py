@@ -210,8 +210,10 @@ def test_errors_are_reported(channel_small):
     ctx = G.Context(channel_small, G.PREC_FP64)
     f, tr = _setup(channel_small, "channel")
     T = np.ascontiguousarray(tr[0])
+    unknown = G.tra_cfg()
+    unknown.adv_ver = 7
     with pytest.raises(G.FesomGpuError) as e:
-        ctx.adv_tra(f, G.tra_cfg("MUSCL", "PPM", "FCT"), T, T)
+        ctx.adv_tra(f, unknown, T, T)
     assert e.value.rc == 2
     bad = G.tra_cfg()
     bad.ab_order = 4

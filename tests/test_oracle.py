@@ -331,3 +331,130 @@ def test_horizontal_diffusion_conserves_and_smooths(channel_seamount):
     assert abs(np.sum(d * av)) <= 1e-9 * np.sum(np.abs(d * av))
     Tn = T + d / np.where(wet, mesh.hnode_new, 1.0)
     assert np.var(Tn[wet]) < np.var(T[wet])
+
+
+# ---- vertical schemes CDIFF and PPM, split vertical velocity ----------------------
+from tests import refimpl as RI  # noqa: E402
+
+
+@pytest.mark.parametrize("meshname,kind", [("channel_seamount", "channel"), ("basin_irregular", "basin")])
+@pytest.mark.parametrize("scheme", ["CDIFF", "PPM"])
+@pytest.mark.parametrize("wscale", [1.0, 400.0])
+def test_vertical_schemes_match_restatement(meshname, kind, scheme, wscale, request):
+    """adv_tra_ver_cdiff / adv_tra_vert_ppm: oracle and loop restatement agree bit for bit,
+    from zero and from a given flux (the FCT form subtracts the LO flux); a large w makes
+    the PPM sweep fraction reach its cap of 1."""
+    mesh = request.getfixturevalue(meshname)
+    f = _forcing(mesh, kind)
+    W = np.ascontiguousarray(f.w * wscale)
+    T = np.ascontiguousarray(M.make_tracers(mesh, kind, ntr=1, seed=4)[0])
+    om = O.OracleMesh(mesh)
+    rng = np.random.default_rng(3)
+    F0 = np.ascontiguousarray(rng.standard_normal((mesh.nod2D, mesh.nl)))
+    for zero in (True, False):
+        got = om.ver_flux(scheme, W, T, f.dt, flux=F0.copy(), init_zero=zero)
+        start = np.zeros_like(F0) if zero else F0
+        want = RI.ver_cdiff(mesh, W, T, start) if scheme == "CDIFF" else RI.ver_ppm(mesh, f.dt, W, T, start)
+        assert np.array_equal(got, want), zero
+
+
+def test_ppm_reconstruction_properties(channel_seamount):
+    """PPM keeps a linear profile on uniform layers exactly away from the ends, and a
+    constant one everywhere: the flux is then the upwind value times w area."""
+    mesh = channel_seamount
+    f = _forcing(mesh, "channel")
+    om = O.OracleMesh(mesh)
+    wet = wet_mask(mesh)
+    T = np.ascontiguousarray(np.where(wet, 3.5, 0.0))
+    F = om.ver_flux("PPM", f.w, T, f.dt)
+    Fu = om.ver_flux("UPW1", f.w, T, f.dt)
+    assert np.allclose(F, Fu, rtol=1e-14, atol=1e-30)
+
+
+@pytest.mark.parametrize("meshname,kind", [("channel_seamount", "channel"), ("basin_irregular", "basin")])
+def test_vert_impl_and_wimpl_match_restatement(meshname, kind, request):
+    """adv_tra_vert_impl and the w_i terms of diff_ver_part_impl_ale: oracle and loop
+    restatement agree bit for bit; the implicit advection of a constant column changes it
+    only by the column divergence of w_i."""
+    mesh = request.getfixturevalue(meshname)
+    f = M.split_vertical_velocity(mesh, _forcing(mesh, kind), maxcfl=0.01)
+    assert np.abs(f.w_i).max() > 0
+    f.bc_surface = np.linspace(-2e-3, 1e-3, mesh.nod2D)
+    T = np.ascontiguousarray(M.make_tracers(mesh, kind, ntr=1, seed=2)[0])
+    om = O.OracleMesh(mesh)
+    To = T.copy()
+    om.adv_tra_vert_impl(f.w_i, To, f.dt)
+    assert np.array_equal(To, RI.vert_impl(mesh, f.dt, f.w_i, T))
+    assert np.abs(To - T).max() > 0
+    To = T.copy()
+    om.diff_ver_part_impl_ale(f, To, wimpl=True)
+    assert np.array_equal(To, RI.vdiff_wimpl(mesh, f.dt, f.Kv, f.bc_surface, f.w_i, T))
+    # without w_i terms the same routine is the plain implicit diffusion
+    To = T.copy()
+    om.diff_ver_part_impl_ale(f, To)
+    assert np.array_equal(To, Ref(mesh).vdiff(f.dt, f.Kv, f.bc_surface, T))
+
+
+NEW_SCHEMES = [("MUSCL", "CDIFF", "FCT", False), ("MFCT", "PPM", "FCT", False), ("UPW1", "PPM", "NON", False),
+               ("MUSCL", "QR4C", "FCT", True), ("MFCT", "PPM", "FCT", True), ("MUSCL", "CDIFF", "NON", True)]
+
+
+@pytest.mark.parametrize("scheme", NEW_SCHEMES, ids=["-".join(map(str, s)) for s in NEW_SCHEMES])
+@pytest.mark.parametrize("meshname,kind", [("channel_seamount", "channel"), ("basin_irregular", "basin")])
+def test_new_vertical_options_match_restatement(scheme, meshname, kind, request):
+    """do_oce_adv_tra and the whole step with CDIFF / PPM and with the split vertical
+    velocity: oracle and restatement agree bit for bit."""
+    hor, ver, lim, wsplit = scheme
+    mesh = request.getfixturevalue(meshname)
+    f = M.split_vertical_velocity(mesh, _forcing(mesh, kind), maxcfl=0.01) if wsplit else _forcing(mesh, kind)
+    T = np.ascontiguousarray(M.make_tracers(mesh, kind, ntr=1, seed=4)[0])
+    rng = np.random.default_rng(5)
+    TAB = np.ascontiguousarray(T * (1 + 1e-3 * rng.standard_normal(T.shape)))
+    om = O.OracleMesh(mesh)
+    ocfg = O.cfg_struct(hor, ver, lim, wsplit=wsplit)
+    om.init_tracers_AB(ocfg, T.copy(), np.zeros_like(T), T.copy())
+    G = om.work["edge_up_dn_grad"].copy()
+    om.do_oce_adv_tra(f, ocfg, T, TAB)
+    ref = Ref(mesh)
+    dh, dv, aux = ref.adv_tra(f.dt, f.uv, f.w, f.w_e, T, TAB, hor, ver, lim, 0.0, 1.0, G, om.work["nboundary_lay"],
+                              WI=f.w_i, wsplit=wsplit)
+    wet = wet_mask(mesh)
+    assert np.array_equal(dh[wet], om.work["del_ttf_advhoriz"][wet])
+    assert np.array_equal(dv[wet], om.work["del_ttf_advvert"][wet])
+    if lim == "FCT":
+        assert np.array_equal(aux["LO"][wet], om.work["fct_LO"][wet])
+    Told = perturbed_old(T, np.random.default_rng(1))
+    To, Oo = T.copy(), Told.copy()
+    om.tracer_step(f, ocfg, To, np.zeros_like(To), Oo)
+    Tr, _ = ref.tracer_step(f, T, Told, om.work["edge_up_dn_tri"], om.work["nboundary_lay"], hor, ver, lim,
+                            wsplit=wsplit)
+    assert np.array_equal(To, Tr)
+
+
+def test_wsplit_without_implicit_part_is_the_plain_step(channel_seamount):
+    """With w_i = 0 the split path (implicit LO advection, LO flux of the full w) reduces to
+    the plain one exactly; with w_i != 0 it does not."""
+    mesh = channel_seamount
+    f = _forcing(mesh, "channel")
+    T = np.ascontiguousarray(M.make_tracers(mesh, "channel", ntr=1, seed=4)[0])
+    om = O.OracleMesh(mesh)
+    outs = []
+    for ff, ws in ((f, False), (f, True), (M.split_vertical_velocity(mesh, f, maxcfl=0.01), True)):
+        Tx, Ox = T.copy(), T.copy()
+        om.tracer_step(ff, O.cfg_struct("MUSCL", "QR4C", "FCT", wsplit=ws), Tx, np.zeros_like(Tx), Ox)
+        outs.append(Tx)
+    assert np.array_equal(outs[0], outs[1])
+    assert not np.array_equal(outs[0], outs[2])
+
+
+@pytest.mark.parametrize("ver", ["CDIFF", "PPM"])
+@pytest.mark.parametrize("lim", ["FCT", "NON"])
+def test_constant_tracer_new_vertical_schemes(sphere_small, ver, lim):
+    mesh = sphere_small
+    f = _forcing(mesh, "sphere")
+    wet = wet_mask(mesh)
+    T = np.ascontiguousarray(np.where(wet, 7.25, 0.0))
+    Told = T.copy()
+    om = O.OracleMesh(mesh)
+    om.tracer_step(f, O.cfg_struct("MUSCL", ver, lim), T, np.zeros_like(T), Told)
+    assert np.abs(T[wet] - 7.25).max() < 1e-12
