@@ -52,6 +52,10 @@ struct fesom_gpu_ctx {
     bool forcing_ready = false;
     bool state_ready = false;
     int wsplit = 0;            // dynamics%use_wsplit (fesom_gpu_set_wsplit)
+    // FP32 form: tracers per launch of the node stages (lo_ad, ho, bounds, update); 0 = the
+    // whole launch group.  Fewer tracers per pass keep the neighbour columns of the nodes in
+    // flight inside L2 (fesom_gpu_set_stage_tracers)
+    int stage_tr[4] = {0, 0, 6, 6};
     cudaGraphExec_t gexec = nullptr;
     double g_dt = 0.0;
     // FP32 batched form: rotating time-level buffers and its work arrays
@@ -650,11 +654,11 @@ B32View sub32(const B32View &B, int s0, int ns) {
     return v;
 }
 
-// tracers per bounds launch: the bounds stage gathers two fields of every neighbour, so
-// fewer tracers per pass keep the neighbour columns of the nodes in flight inside L2
-#ifndef FESOM_BOUNDS_GROUP
-#define FESOM_BOUNDS_GROUP 6  // 0: the whole launch group
-#endif
+// tracers per launch of node stage k of a launch group of nt tracers
+inline int stage_group(const fesom_gpu_ctx *ctx, int k, int nt) {
+    const int g = ctx->stage_tr[k];
+    return g > 0 && g < nt ? g : nt;
+}
 
 struct StageTimer {
     cudaEvent_t ev[2 * FESOM_NUM_STAGES * 64];
@@ -739,21 +743,33 @@ int enqueue_group32(fesom_gpu_ctx *ctx, double dt, int t0, int nt, StageTimer *t
     DForcing<float> fg = forcing_view<float>(ctx, t0);
     bool any_fct = false;
     for (int t = t0; t < t0 + nt; t++) any_fct |= ctx->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
-    STAGE(10, b32_lo_ad(ctx->tp, g, fg, B, ctx->VF, dt, ctx->stream));
+    {
+        const int sg = stage_group(ctx, 0, nt);
+        for (int s0 = 0; s0 < nt; s0 += sg)
+            STAGE(10, b32_lo_ad(ctx->tp, g, fg, sub32(B, s0, std::min(sg, nt - s0)), ctx->VF, dt, ctx->stream));
+    }
     if (B.ppm_mask) STAGE(10, b32_vppm(ctx->tp, g, fg, B, dt, ctx->stream));
     // split vertical velocity: w_i advects the LO values implicitly (oce_adv_tra_driver.F90:323-334)
     if (ctx->wsplit && any_fct) STAGE(10, b32_lo_impl(ctx->tp, g, fg, B, dt, ctx->scratch, ctx->stream));
-    STAGE(2, b32_ho(ctx->tp, g, B, ctx->mw, ctx->VF, ctx->stream));
+    {
+        const int sg = stage_group(ctx, 1, nt);
+        for (int s0 = 0; s0 < nt; s0 += sg)
+            STAGE(2, b32_ho(ctx->tp, g, sub32(B, s0, std::min(sg, nt - s0)), ctx->mw, ctx->VF, ctx->stream));
+    }
     // diff_tracers_ale from the values before the update; the increment waits in Tnew (the
     // oldest level, read by lo_ad and ho only) for the update to add it after the limiter
     if (B.Ki) STAGE(2, b32_hdiff(ctx->tp, g, B, ctx->stream));
     if (B.diff_mask) STAGE(7, b32_diff(ctx->tp, g, B, dt, ctx->stream));
     if (any_fct) {
-        const int bg = FESOM_BOUNDS_GROUP > 0 ? FESOM_BOUNDS_GROUP : nt;
+        const int bg = stage_group(ctx, 2, nt);
         for (int s0 = 0; s0 < nt; s0 += bg)
             STAGE(4, b32_bounds(ctx->tp, g, sub32(B, s0, std::min(bg, nt - s0)), dt, ctx->stream));
     }
-    STAGE(6, b32_update(ctx->tp, g, B, dt, ctx->stream));
+    {
+        const int sg = stage_group(ctx, 3, nt);
+        for (int s0 = 0; s0 < nt; s0 += sg)
+            STAGE(6, b32_update(ctx->tp, g, sub32(B, s0, std::min(sg, nt - s0)), dt, ctx->stream));
+    }
     if (B.ivd_mask) {
         if (fork && !joined) {
             CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
@@ -793,7 +809,10 @@ int launches_per_step(fesom_gpu_ctx *ctx) {
             // lo_ad, update (+ bounds), launched again for the wide nodes; ho (+ its fallback
             // edges); vdiff
             const int wide = ctx->tp.n_wide ? 2 : 1;
-            const int bg = FESOM_BOUNDS_GROUP > 0 ? FESOM_BOUNDS_GROUP : nt;
+            const int nlo = (nt + stage_group(ctx, 0, nt) - 1) / stage_group(ctx, 0, nt);
+            const int nho = (nt + stage_group(ctx, 1, nt) - 1) / stage_group(ctx, 1, nt);
+            const int nbo = (nt + stage_group(ctx, 2, nt) - 1) / stage_group(ctx, 2, nt);
+            const int nup = (nt + stage_group(ctx, 3, nt) - 1) / stage_group(ctx, 3, nt);
             bool grp_diff = ctx->Ki != nullptr;
             for (int t = t0; t < t0 + nt; t++) grp_diff |= ctx->cfgs[t].i_vert_diff == 0;
             bool grp_ppm = false, grp_wimpl = false;
@@ -801,7 +820,7 @@ int launches_per_step(fesom_gpu_ctx *ctx) {
                 grp_ppm |= ctx->cfgs[t].adv_ver == FESOM_ADV_VER_PPM;
                 grp_wimpl |= ctx->wsplit && ctx->cfgs[t].i_vert_diff && ctx->cfgs[t].adv_lim != FESOM_ADV_LIM_FCT;
             }
-            n += wide * (2 + (any_fct ? (nt + bg - 1) / bg : 0) + (grp_diff ? 1 : 0)) + (ctx->mw.n_items ? 2 : 1) +
+            n += wide * (nlo + nup + (any_fct ? nbo : 0) + (grp_diff ? 1 : 0)) + nho * (ctx->mw.n_items ? 2 : 1) +
                  (grp_vd ? 1 : 0) + (ctx->Ki ? 1 : 0) + (grp_ppm ? 1 : 0) + ((ctx->wsplit && any_fct) ? 1 : 0) +
                  (grp_wimpl ? 1 : 0);
         }
@@ -1469,6 +1488,13 @@ int fesom_gpu_tracer_content(fesom_gpu_ctx *ctx, double *content) {
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(content, ctx->content_out, sizeof(double) * ctx->ntr, cudaMemcpyDeviceToHost, ctx->stream));
     return wait_stream(ctx, -1);
+}
+
+int fesom_gpu_set_stage_tracers(fesom_gpu_ctx *ctx, int32_t stage, int32_t tracers) {
+    if (!ctx || stage < 0 || stage > 3 || tracers < 0) return FESOM_ERR_ARG;
+    ctx->stage_tr[stage] = tracers;
+    free_graphs32(ctx);
+    return FESOM_OK;
 }
 
 int fesom_gpu_set_wsplit(fesom_gpu_ctx *ctx, int32_t on) {

@@ -90,6 +90,7 @@ _SIGS = {
     "fesom_gpu_tracer_tail": ([_P, C.c_int32, _P, C.c_double, _P, _P, _P, _P, _P, C.POINTER(_P)], C.c_int),
     "fesom_gpu_set_hdiff": ([_P, _P], C.c_int),
     "fesom_gpu_set_wsplit": ([_P, C.c_int32], C.c_int),
+    "fesom_gpu_set_stage_tracers": ([_P, C.c_int32, C.c_int32], C.c_int),
     "fesom_gpu_vdiff_impl_wi": ([_P, C.c_double, C.POINTER(TraCfg), _P, _P, _P, _P], C.c_int),
     "fesom_gpu_diff_hor": ([_P, C.c_double, _P, _P, _P], C.c_int),
     "fesom_gpu_diff_ver_expl": ([_P, C.c_double, _P, _P, _P, _P], C.c_int),
@@ -261,6 +262,10 @@ class Context:
         wi = _c64(forcing.w_i) if wimpl else None
         self._chk(self.L.fesom_gpu_vdiff_impl_wi(self.h, float(forcing.dt if dt is None else dt), C.byref(cfg),
                                                  _p(Kv), _p(bcs), _p(wi), _p(values)))
+
+    def set_stage_tracers(self, stage: int, tracers: int):
+        """FP32 form: tracers per launch of stage 0 lo_ad, 1 ho, 2 bounds, 3 update (0: all)."""
+        self._chk(self.L.fesom_gpu_set_stage_tracers(self.h, int(stage), int(tracers)))
 
     def set_wsplit(self, on: bool):
         """dynamics%use_wsplit for every later step (fesom_gpu_set_wsplit)."""

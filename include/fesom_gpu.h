@@ -258,6 +258,11 @@ int fesom_gpu_set_hdiff(fesom_gpu_ctx *ctx, const double *Ki);
  * vertical solve (src/oce_ale_tracer.F90:961, 1134-1216).  Applies to every later step and to
  * fesom_gpu_adv_tra, which then needs wi. */
 int fesom_gpu_set_wsplit(fesom_gpu_ctx *ctx, int32_t on);
+/* Performance setting of the FP32 form (results do not change): tracers per launch of the
+ * node/edge stages, stage 0 = LO and vertical fluxes, 1 = horizontal high-order fluxes,
+ * 2 = FCT bounds, 3 = limited update; 0 = every tracer of the launch group in one pass.
+ * Fewer tracers per pass keep the neighbour columns of the nodes in flight inside L2. */
+int fesom_gpu_set_stage_tracers(fesom_gpu_ctx *ctx, int32_t stage, int32_t tracers);
 /* The routine alone (FP64 contexts): del_ttf += the edge diffusion fluxes of the element
  * gradients of values, in ascending edge order. */
 int fesom_gpu_diff_hor(fesom_gpu_ctx *ctx, double dt, const double *Ki, const double *values, double *del_ttf);
