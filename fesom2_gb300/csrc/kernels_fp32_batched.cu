@@ -293,7 +293,7 @@ __device__ __forceinline__ float ab_delta(int ab, float t, float o1, float o2) {
 // ---------------------------------------------------------------------------
 // k32_lo_ad
 // ---------------------------------------------------------------------------
-template <int KD>
+template <int KD, bool WS>
 __device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
                                            const B32View &B, const float *__restrict__ VF, float dt, int n, int lane,
                                            const WEdges &S) {
@@ -387,7 +387,7 @@ __device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &
             // with the split vertical velocity the LO part of the antidiffusive flux is the upwind
             // flux of the full w (oce_adv_tra_driver.F90:323-334)
             float fw0 = fv0;
-            if (f.wsplit && k.lvl) {
+            if (WS && k.lvl) {
                 if (nz == nzmin) {
                     fw0 = -(w0 * Tn * ar0);
                 } else {
@@ -437,7 +437,8 @@ __device__ __forceinline__ int unit_node(const DTopo &tp, int j) {
     return j < tp.N2 ? j : -1;
 }
 
-template <bool WIDE>
+// WS: the split vertical velocity (a separate instantiation keeps the default path unchanged)
+template <bool WIDE, bool WS>
 __device__ __forceinline__ void lo_ad_unit(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
                                            const B32View &B, const float *__restrict__ VF, float dt, int j, WEdges *Se) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -446,16 +447,16 @@ __device__ __forceinline__ void lo_ad_unit(const DTopo &tp, const DGeom<float> &
     WEdges &S = Se[warp];
     stage_edges(tp, n, lane, S);
     if ((S.deg > 8) != WIDE) return;
-    if (WIDE) lo_ad_node<kMaxDeg>(tp, g, f, B, VF, dt, n, lane, S);
-    else if (S.deg <= 6) lo_ad_node<6>(tp, g, f, B, VF, dt, n, lane, S);
-    else lo_ad_node<8>(tp, g, f, B, VF, dt, n, lane, S);
+    if (WIDE) lo_ad_node<kMaxDeg, WS>(tp, g, f, B, VF, dt, n, lane, S);
+    else if (S.deg <= 6) lo_ad_node<6, WS>(tp, g, f, B, VF, dt, n, lane, S);
+    else lo_ad_node<8, WS>(tp, g, f, B, VF, dt, n, lane, S);
 }
 
-template <bool WIDE>
+template <bool WIDE, bool WS>
 __global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_LO)
 k32_lo_ad(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, const float *__restrict__ VF, float dt) {
     __shared__ WEdges Se[kWB];
-    lo_ad_unit<WIDE>(tp, g, f, B, VF, dt, blockIdx.x * kWB + (threadIdx.x >> 5), Se);
+    lo_ad_unit<WIDE, WS>(tp, g, f, B, VF, dt, blockIdx.x * kWB + (threadIdx.x >> 5), Se);
 }
 
 // high-order minus low-order flux of one edge-layer from the two end values, their
@@ -1434,7 +1435,8 @@ __global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_LO) k32m_lo_ad(cons
     const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
     if (u >= ix.start[ix.n]) return;
     const int i = find_inst(ix, u);
-    lo_ad_unit<WIDE>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].VF, I[i].dt, u - ix.start[i], Se);
+    // batches take no split vertical velocity
+    lo_ad_unit<WIDE, false>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].VF, I[i].dt, u - ix.start[i], Se);
 }
 __global__ void __launch_bounds__(kTB, FESOM_MINB_HO) k32m_ho(const Inst32 *__restrict__ I, MultiIdx ix) {
     const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
@@ -1509,8 +1511,13 @@ static int grid_nodes(int n) { return (n + kWB - 1) / kWB; }
 
 void b32_lo_ad(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B, const float *VF,
                double dt, cudaStream_t s) {
-    k32_lo_ad<false><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
-    if (tp.n_wide) k32_lo_ad<true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
+    if (f.wsplit) {
+        k32_lo_ad<false, true><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
+        if (tp.n_wide) k32_lo_ad<true, true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
+    } else {
+        k32_lo_ad<false, false><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
+        if (tp.n_wide) k32_lo_ad<true, false><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
+    }
 }
 void b32_ho(const DTopo &tp, const DGeom<float> &g, const B32View &B, const MusclW &mw, const float *VF,
             cudaStream_t s) {
