@@ -84,7 +84,7 @@ def algorithmic_bytes(counts, ntr, s):
 # DRAM bytes (read + write) per tracer-DOF of each FP32 stage, measured with one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum) of `--profile-only --scale 0.25`; the traffic
 # of a full-size launch is this figure times the tracer-DOF it processes
-MEASURED_DRAM_B_PER_TRACER_DOF = {"update": 51.26, "bounds": 82.69, "edge_flux": 31.43, "lo_ad": 30.65}
+MEASURED_DRAM_B_PER_TRACER_DOF = {"update": 55.04, "bounds": 53.25, "edge_flux": 31.48, "lo_ad": 30.68}
 
 
 def stage_bytes(counts, ntr, s, ab=2, form="fp32"):
