@@ -384,16 +384,20 @@ def run_ours(args, rank, world, local_rank):
         h_T = pin((ntr, mesh.nod2D, L1)); h_T[...] = tracers
         h_O = pin((ntr, mesh.nod2D, L1)); h_O[...] = tracers
         fe = M.Forcing(uv=h_uv, w=h_w, w_e=h_we, w_i=None, Kv=h_kv, bc_surface=None, dt=dt)
-        vals = [h_T[k] for k in range(ntr)]
-        olds = [h_O[k] for k in range(ntr)]
+        # two host time levels that swap roles every step, as a model keeps values and
+        # valuesold: the new values are written over the previous level, which the step has
+        # consumed, and the values it started from become the previous level
+        levels = [[h_T[k] for k in range(ntr)], [h_O[k] for k in range(ntr)]]
         # tracer groups of 6: a group computes while the next uploads and the previous downloads
         e2e_group = min(6, ntr)
         ce.set_tracers_per_launch(e2e_group)
 
         def e2e_step():
-            # the public host-array step: forcing and tracer state in, new values and the new
-            # previous level out, every step (fesom_gpu_step_host_f32)
-            ce.step_host_f32(fe, vals, olds, vals, olds)
+            # the public host-array step: forcing and tracer state in, the new values out,
+            # every step (fesom_gpu_step_host_f32)
+            cur, old = levels
+            ce.step_host_f32(fe, cur, old, old, None)
+            levels.reverse()
 
         e2e_step()
         barrier()
@@ -407,7 +411,7 @@ def run_ours(args, rank, world, local_rank):
         ce.close()
         del ce
         h2d = 4 * (h_uv.size + h_w.size + h_we.size + h_kv.size + 2 * ntr * mesh.nod2D * L1)
-        d2h = 4 * 2 * ntr * mesh.nod2D * L1
+        d2h = 4 * ntr * mesh.nod2D * L1
         res["e2e"] = {"value": ntr * N3 * args.e2e_steps * world / (mse / 1e3), "unit": UNIT,
                       "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                       "ms_per_step": mse / args.e2e_steps, "api": "fesom_gpu_step_host_f32",

@@ -1660,7 +1660,12 @@ int fesom_gpu_step_host_f32(fesom_gpu_ctx *ctx, double dt, const float *uv, cons
                 return rc;
         return wait_stream(ctx, -1);
     }
-    const int G = ctx->group, ng = (ntr + G - 1) / G;
+    // tracer groups of ctx->group tracers
+    const int G = ctx->group;
+    std::vector<int> gs;  // first tracer of each group, and ntr at the end
+    for (int t = 0; t < ntr; t += G) gs.push_back(t);
+    gs.push_back(ntr);
+    const int ng = (int)gs.size() - 1;
     while ((int)ctx->ev_in.size() < ng) {
         cudaEvent_t a, b;
         CK(cudaEventCreateWithFlags(&a, cudaEventDisableTiming));
@@ -1684,7 +1689,7 @@ int fesom_gpu_step_host_f32(fesom_gpu_ctx *ctx, double dt, const float *uv, cons
     CK(cudaEventRecord(ctx->ev_forcing, ctx->h2d));
     float *Tcur = level32(ctx, 0), *Told = level32(ctx, 1);  // the step writes Tnew into Told's buffer
     for (int gi = 0; gi < ng; gi++) {
-        for (int t = gi * G; t < std::min(ntr, (gi + 1) * G); t++) {
+        for (int t = gs[gi]; t < gs[gi + 1]; t++) {
             CK(cudaMemcpyAsync(Tcur + sN * t, values_in[t], 4 * sN, cudaMemcpyHostToDevice, ctx->h2d));
             CK(cudaMemcpyAsync(Told + sN * t, valuesold_in[t], 4 * sN, cudaMemcpyHostToDevice, ctx->h2d));
         }
@@ -1696,8 +1701,7 @@ int fesom_gpu_step_host_f32(fesom_gpu_ctx *ctx, double dt, const float *uv, cons
     if ((rc = enqueue_shared32(ctx, dt, nullptr, fork))) return rc;
     for (int gi = 0; gi < ng; gi++) {
         CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_in[gi], 0));
-        const int t0 = gi * G;
-        if ((rc = enqueue_group32(ctx, dt, t0, std::min(G, ntr - t0), nullptr, fork, joined))) return rc;
+        if ((rc = enqueue_group32(ctx, dt, gs[gi], gs[gi + 1] - gs[gi], nullptr, fork, joined))) return rc;
         CK(cudaEventRecord(ctx->ev_done[gi], ctx->stream));
     }
     if (fork && !joined) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
@@ -1706,7 +1710,7 @@ int fesom_gpu_step_host_f32(fesom_gpu_ctx *ctx, double dt, const float *uv, cons
     // new previous level (the values the step started from)
     for (int gi = 0; gi < ng; gi++) {
         CK(cudaStreamWaitEvent(ctx->d2h, ctx->ev_done[gi], 0));
-        for (int t = gi * G; t < std::min(ntr, (gi + 1) * G); t++) {
+        for (int t = gs[gi]; t < gs[gi + 1]; t++) {
             CK(cudaMemcpyAsync(values_out[t], Told + sN * t, 4 * sN, cudaMemcpyDeviceToHost, ctx->d2h));
             if (valuesold_out)
                 CK(cudaMemcpyAsync(valuesold_out[t], Tcur + sN * t, 4 * sN, cudaMemcpyDeviceToHost, ctx->d2h));

@@ -297,9 +297,12 @@ int fesom_gpu_tracer_tail(fesom_gpu_ctx *ctx, int32_t ntr, const fesom_tra_cfg *
  * (fesom_gpu_set_tracers_per_launch) -- a group computes as soon as its values and previous
  * level are resident, and is copied back as soon as it is done, while later groups upload
  * and earlier ones download.  values_out / valuesold_out may be the input arrays (in-place
- * update, as the reference's tracer arrays); valuesold_out may be NULL.  Blocks until the
- * results are in host memory; page-locked host arrays give the full transfer rate.  AB3
- * contexts take the serial path (their previous levels are interleaved on the host). */
+ * update, as the reference's tracer arrays); valuesold_out may be NULL: the previous level
+ * after the step is the values the step started from, so a caller that keeps two time-level
+ * arrays and swaps them (values_out = valuesold_in, then exchange the roles) moves only the new
+ * values back.  Blocks until the results are in host memory; page-locked host arrays give
+ * the full transfer rate.  AB3 contexts take the serial path (their previous levels are interleaved on
+ * the host). */
 int fesom_gpu_step_host_f32(fesom_gpu_ctx *ctx, double dt, const float *uv, const float *w, const float *wi,
                             const float *we, const float *Kv, const float *bc_surf, const float *const *values_in,
                             const float *const *valuesold_in, float *const *values_out, float *const *valuesold_out);

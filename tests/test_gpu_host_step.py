@@ -57,3 +57,31 @@ def test_host_step_equals_device_resident_steps(channel_seamount, ab):
         assert np.array_equal(vals[k], want[k][0]), k
         assert np.array_equal(olds[k].reshape(-1), want[k][1].reshape(-1)), k
     assert b.status() == 0
+
+
+def test_host_step_with_swapped_time_levels(channel_seamount):
+    """Two host time levels that swap roles (new values written over the consumed previous
+    level, no previous level copied back) give the device-resident steps' values."""
+    mesh = channel_seamount
+    f32, tr, cfgs = _setup(mesh, "channel", 2)
+    n = len(cfgs)
+    a = G.Context(mesh, G.PREC_FP32, max_tracers=n)
+    a.state_setup(cfgs)
+    a.set_tracers_per_launch(3)
+    a.forcing_upload(f32)
+    for k in range(n):
+        a.tracer_upload(k, np.array(tr[k], copy=True), np.array(tr[k], copy=True))
+    a.run_steps(600.0, 4, use_graph=True)
+    want = [a.tracer_download(k, dtype=np.float32) for k in range(n)]
+    b = G.Context(mesh, G.PREC_FP32, max_tracers=n)
+    b.state_setup(cfgs)
+    b.set_tracers_per_launch(3)
+    levels = [[np.array(tr[k], copy=True) for k in range(n)], [np.array(tr[k], copy=True) for k in range(n)]]
+    for _ in range(4):
+        cur, old = levels
+        b.step_host_f32(f32, cur, old, old, None)
+        levels.reverse()
+    for k in range(n):
+        assert np.array_equal(levels[0][k], want[k][0]), k
+        assert np.array_equal(levels[1][k], want[k][1]), k
+    assert b.status() == 0
