@@ -1760,6 +1760,7 @@ struct fesom_gpu_batch {
     MultiIdx ix_e{}, ix_vfb{}, ix_n{}, ix_w{}, ix_it{};
     int maxL1 = 0;
     bool any_vd = false, any_fct = false, any_hd = false, any_diff = false;
+    bool any_ws = false, any_ppm = false, any_lo_impl = false, any_wimpl = false;
     cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};
     double g_dt[3] = {0.0, 0.0, 0.0};
     std::string err;
@@ -1801,6 +1802,7 @@ int batch_descriptors(fesom_gpu_batch *b, double dt) {
             d.vf = c->vfac;
             d.dt = (float)dt;
             d.dtd = dt;
+            d.scratch = c->scratch;
             c->rot = keep;
         }
     BCK(cudaMemcpy(b->d_inst, h.data(), sizeof(Inst32) * h.size(), cudaMemcpyHostToDevice));
@@ -1813,8 +1815,10 @@ void enqueue_batch_step(fesom_gpu_batch *b, cudaStream_t s) {
     const bool wide = b->ix_w.start[b->ix_w.n] > 0;
     bm32_vflux(I, b->ix_e, s);
     if (b->any_vd) bm32_vfactors(I, b->ix_vfb, s);
-    bm32_lo_ad(I, b->ix_n, false, s);
-    if (wide) bm32_lo_ad(I, b->ix_w, true, s);
+    bm32_lo_ad(I, b->ix_n, false, b->any_ws, s);
+    if (wide) bm32_lo_ad(I, b->ix_w, true, b->any_ws, s);
+    if (b->any_ppm) bm32_vppm(I, b->ix_n, s);
+    if (b->any_lo_impl) bm32_lo_impl(I, b->ix_n, s);
     bm32_ho(I, b->ix_e, b->ix_it, s);
     if (b->any_hd) bm32_hdiff(I, b->ix_e, s);
     if (b->any_diff) {
@@ -1828,6 +1832,7 @@ void enqueue_batch_step(fesom_gpu_batch *b, cudaStream_t s) {
     bm32_update(I, b->ix_n, false, s);
     if (wide) bm32_update(I, b->ix_w, true, s);
     if (b->any_vd) bm32_vdiff(I, b->ix_n, s);
+    if (b->any_wimpl) bm32_vdiff_w(I, b->ix_n, s);
 }
 
 }  // namespace
@@ -1856,12 +1861,14 @@ int fesom_gpu_batch_create(fesom_gpu_ctx *const *ctxs, int32_t n, fesom_gpu_batc
             return FESOM_ERR_STATE;
         }
         if (i > 0 && c->ab_max != b->ab) { b->err = "batch instances must share one Adams-Bashforth order"; return FESOM_ERR_ARG; }
-        bool ppm = false;
-        for (int t = 0; t < c->ntr; t++) ppm |= c->cfgs[t].adv_ver == FESOM_ADV_VER_PPM;
-        if (ppm || c->wsplit) {
-            b->err = "the PPM vertical scheme and the split vertical velocity step in single contexts only";
-            return FESOM_ERR_SCHEME;
+        bool fct = false;
+        for (int t = 0; t < c->ntr; t++) {
+            b->any_ppm |= c->cfgs[t].adv_ver == FESOM_ADV_VER_PPM;
+            b->any_wimpl |= c->wsplit && c->cfgs[t].i_vert_diff && c->cfgs[t].adv_lim != FESOM_ADV_LIM_FCT;
+            fct |= c->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
         }
+        b->any_ws |= c->wsplit != 0;
+        b->any_lo_impl |= c->wsplit && fct;
         b->ab = c->ab_max;
         for (int t = 0; t < c->ntr; t++) {
             b->any_vd |= c->cfgs[t].i_vert_diff != 0;
@@ -1946,7 +1953,8 @@ int fesom_gpu_batch_launches_per_step(fesom_gpu_batch *b, int32_t *launches) {
     const bool wide = b->ix_w.start[b->ix_w.n] > 0;
     const int k = wide ? 2 : 1;
     int n = 1 + (b->any_vd ? 2 : 0) + k * (2 + (b->any_fct ? 1 : 0) + (b->any_diff ? 1 : 0)) + 1 +
-            (b->ix_it.start[b->ix_it.n] ? 1 : 0) + (b->any_hd ? 1 : 0);
+            (b->ix_it.start[b->ix_it.n] ? 1 : 0) + (b->any_hd ? 1 : 0) + (b->any_ppm ? 1 : 0) +
+            (b->any_lo_impl ? 1 : 0) + (b->any_wimpl ? 1 : 0);
     *launches = n;
     return FESOM_OK;
 }

@@ -167,6 +167,7 @@ struct Inst32 {
     VFactors vf;
     float dt;
     double dtd;
+    double *scratch;  // the instance's column scratch (split vertical velocity)
 };
 constexpr int kMaxInst = 64;
 constexpr int kVfCols = 128;  // columns per block of the diffusion-factor kernel
@@ -176,7 +177,10 @@ struct MultiIdx {
 };
 void bm32_vflux(const Inst32 *, const MultiIdx &, cudaStream_t);
 void bm32_vfactors(const Inst32 *, const MultiIdx &, cudaStream_t);
-void bm32_lo_ad(const Inst32 *, const MultiIdx &, bool wide, cudaStream_t);
+void bm32_lo_ad(const Inst32 *, const MultiIdx &nodes, bool wide, bool ws, cudaStream_t);
+void bm32_vppm(const Inst32 *, const MultiIdx &nodes, cudaStream_t);
+void bm32_lo_impl(const Inst32 *, const MultiIdx &nodes, cudaStream_t);
+void bm32_vdiff_w(const Inst32 *, const MultiIdx &nodes, cudaStream_t);
 void bm32_ho(const Inst32 *, const MultiIdx &edges, const MultiIdx &items, cudaStream_t);
 void bm32_bounds(const Inst32 *, const MultiIdx &, bool wide, cudaStream_t);
 void bm32_update(const Inst32 *, const MultiIdx &, bool wide, cudaStream_t);

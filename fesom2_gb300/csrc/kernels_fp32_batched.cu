@@ -387,7 +387,7 @@ __device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &
             // with the split vertical velocity the LO part of the antidiffusive flux is the upwind
             // flux of the full w (oce_adv_tra_driver.F90:323-334)
             float fw0 = fv0;
-            if (WS && k.lvl) {
+            if (WS && f.wsplit && k.lvl) {
                 if (nz == nzmin) {
                     fw0 = -(w0 * Tn * ar0);
                 } else {
@@ -934,13 +934,11 @@ __global__ void __launch_bounds__(kTB) k32_vppm(DTopo tp, DGeom<float> g, DForci
 // terms for the tracers without the limiter (oce_ale_tracer.F90:907-1435, do_wimpl).  One
 // thread per column, FP64 arithmetic; scratch holds Z_n, cp and tp level-major.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k32_lo_impl(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B,
-                                                   double dt, double *scratch) {
+__device__ __forceinline__ void lo_impl_column(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
+                                               const B32View &B, double dt, double *scratch, int n) {
     const int L1 = tp.L1, nl = tp.nl;
     const size_t N2 = tp.N2;
     double *cps = scratch, *tps = scratch + (size_t)(L1 + 1) * N2;
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= tp.N2) return;
 #define CP(k) cps[(size_t)(k) * N2 + n]
 #define TP(k) tps[(size_t)(k) * N2 + n]
     const int nzmax = tp.n_nlev[n], nzmin = tp.n_ulev[n];
@@ -994,13 +992,11 @@ __global__ void __launch_bounds__(128) k32_lo_impl(DTopo tp, DGeom<float> g, DFo
 #undef TP
 }
 
-__global__ void __launch_bounds__(128) k32_vdiff_w(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B,
-                                                   double dt, double *scratch) {
+__device__ __forceinline__ void vdiff_w_column(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
+                                               const B32View &B, double dt, double *scratch, int n) {
     const int L1 = tp.L1, nl = tp.nl;
     const size_t N2 = tp.N2;
     double *Zs = scratch, *cps = scratch + (size_t)(L1 + 1) * N2, *tps = cps + (size_t)(L1 + 1) * N2;
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= tp.N2) return;
 #define ZN(k) Zs[(size_t)(k) * N2 + n]
 #define CP(k) cps[(size_t)(k) * N2 + n]
 #define TP(k) tps[(size_t)(k) * N2 + n]
@@ -1073,6 +1069,17 @@ __global__ void __launch_bounds__(128) k32_vdiff_w(DTopo tp, DGeom<float> g, DFo
 #undef ZN
 #undef CP
 #undef TP
+}
+
+__global__ void __launch_bounds__(128) k32_lo_impl(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, double dt,
+                                                   double *scratch) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n < tp.N2) lo_impl_column(tp, g, f, B, dt, scratch, n);
+}
+__global__ void __launch_bounds__(128) k32_vdiff_w(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, double dt,
+                                                   double *scratch) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n < tp.N2) vdiff_w_column(tp, g, f, B, dt, scratch, n);
 }
 
 // ---------------------------------------------------------------------------
@@ -1429,14 +1436,14 @@ __global__ void __launch_bounds__(kVfCols) k32m_vfactors(const Inst32 *__restric
     const int i = find_inst(ix, u);
     vfactors_block(I[i].tp, I[i].g, I[i].f, I[i].dtd, I[i].vf, u - ix.start[i]);
 }
-template <bool WIDE>
+// WS: some instance has the split vertical velocity (each instance checks its own switch)
+template <bool WIDE, bool WS>
 __global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_LO) k32m_lo_ad(const Inst32 *__restrict__ I, MultiIdx ix) {
     __shared__ WEdges Se[kWB];
     const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
     if (u >= ix.start[ix.n]) return;
     const int i = find_inst(ix, u);
-    // batches take no split vertical velocity
-    lo_ad_unit<WIDE, false>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].VF, I[i].dt, u - ix.start[i], Se);
+    lo_ad_unit<WIDE, WS>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].VF, I[i].dt, u - ix.start[i], Se);
 }
 __global__ void __launch_bounds__(kTB, FESOM_MINB_HO) k32m_ho(const Inst32 *__restrict__ I, MultiIdx ix) {
     const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
@@ -1472,6 +1479,25 @@ __global__ void __launch_bounds__(32 * kWV) k32m_vdiff(const Inst32 *__restrict_
     if (u >= ix.start[ix.n]) return;
     const int i = find_inst(ix, u);
     vdiff_unit(I[i].tp, I[i].f, I[i].B, I[i].vf, u - ix.start[i], Wsm[threadIdx.x >> 5]);
+}
+
+__global__ void __launch_bounds__(kTB) k32m_vppm(const Inst32 *__restrict__ I, MultiIdx ix) {
+    const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
+    if (u >= ix.start[ix.n]) return;
+    const int i = find_inst(ix, u);
+    if (I[i].B.ppm_mask) vppm_node(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].dt, u - ix.start[i], threadIdx.x & 31);
+}
+__global__ void __launch_bounds__(128) k32m_lo_impl(const Inst32 *__restrict__ I, MultiIdx ix) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= ix.start[ix.n]) return;
+    const int i = find_inst(ix, u);
+    if (I[i].f.wsplit) lo_impl_column(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].dtd, I[i].scratch, u - ix.start[i]);
+}
+__global__ void __launch_bounds__(128) k32m_vdiff_w(const Inst32 *__restrict__ I, MultiIdx ix) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= ix.start[ix.n]) return;
+    const int i = find_inst(ix, u);
+    if (I[i].B.wimpl_mask) vdiff_w_column(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].dtd, I[i].scratch, u - ix.start[i]);
 }
 
 __global__ void __launch_bounds__(kTB) k32m_hdiff(const Inst32 *__restrict__ I, MultiIdx ix) {
@@ -1568,11 +1594,28 @@ void bm32_vfactors(const Inst32 *I, const MultiIdx &ix, cudaStream_t s) {
     const int u = ix.start[ix.n];
     if (u) k32m_vfactors<<<u, kVfCols, 0, s>>>(I, ix);
 }
-void bm32_lo_ad(const Inst32 *I, const MultiIdx &ix, bool wide, cudaStream_t s) {
+void bm32_lo_ad(const Inst32 *I, const MultiIdx &ix, bool wide, bool ws, cudaStream_t s) {
     const int u = ix.start[ix.n];
     if (!u) return;
-    if (wide) k32m_lo_ad<true><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
-    else k32m_lo_ad<false><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
+    if (ws) {
+        if (wide) k32m_lo_ad<true, true><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
+        else k32m_lo_ad<false, true><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
+    } else {
+        if (wide) k32m_lo_ad<true, false><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
+        else k32m_lo_ad<false, false><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
+    }
+}
+void bm32_vppm(const Inst32 *I, const MultiIdx &ix, cudaStream_t s) {
+    const int u = ix.start[ix.n];
+    if (u) k32m_vppm<<<grid_nodes(u), kTB, 0, s>>>(I, ix);
+}
+void bm32_lo_impl(const Inst32 *I, const MultiIdx &ix, cudaStream_t s) {
+    const int u = ix.start[ix.n];
+    if (u) k32m_lo_impl<<<(u + 127) / 128, 128, 0, s>>>(I, ix);
+}
+void bm32_vdiff_w(const Inst32 *I, const MultiIdx &ix, cudaStream_t s) {
+    const int u = ix.start[ix.n];
+    if (u) k32m_vdiff_w<<<(u + 127) / 128, 128, 0, s>>>(I, ix);
 }
 void bm32_ho(const Inst32 *I, const MultiIdx &ix_e, const MultiIdx &ix_items, cudaStream_t s) {
     if (ix_e.start[ix_e.n]) k32m_ho<<<grid_nodes(ix_e.start[ix_e.n]), kTB, 0, s>>>(I, ix_e);

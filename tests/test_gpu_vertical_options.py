@@ -138,15 +138,38 @@ def test_split_velocity_changes_the_step(channel_seamount):
     assert np.abs(outs[1][wet] - outs[0][wet]).max() > 1e-4 * np.abs(outs[0][wet]).max()
 
 
-def test_batch_rejects_single_context_options(channel_small):
-    f = _forcing(channel_small, "channel", False)
-    T = M.make_tracers(channel_small, "channel", ntr=1, seed=4)[0].astype(np.float32)
-    for cfg, ws in ((G.tra_cfg("MUSCL", "PPM", "FCT"), False), (G.tra_cfg(), True)):
-        ctx = G.Context(channel_small, G.PREC_FP32, max_tracers=1)
-        ctx.state_setup([cfg])
-        ctx.forcing_upload(f)
-        ctx.set_wsplit(ws)
-        ctx.tracer_upload(0, T, T)
-        with pytest.raises(G.FesomGpuError) as e:
-            G.Batch([ctx])
-        assert e.value.rc == 2
+def test_batch_with_vertical_options_equals_alone(channel_seamount, sphere_small):
+    """A batch of an instance with PPM and CDIFF tracers and an instance with the split
+    vertical velocity steps as the instances do alone (FP32 rounding: the batch kernels are
+    separate compilations)."""
+    setups = [(channel_seamount, "channel", False, [("MFCT", "PPM", "FCT"), ("MUSCL", "CDIFF", "NON")]),
+              (sphere_small, "sphere", True, [("MUSCL", "QR4C", "FCT"), ("UPW1", "PPM", "NON"),
+                                              ("MUSCL", "CDIFF", "NON")])]
+    runs = []
+    for batched in (False, True):
+        ctxs = []
+        for mesh, kind, ws, opts in setups:
+            f = _forcing(mesh, kind, ws)
+            tr = M.make_tracers(mesh, kind, ntr=len(opts), seed=4)
+            ctx = G.Context(mesh, G.PREC_FP32, max_tracers=len(opts))
+            ctx.state_setup([G.tra_cfg(h, v, l, id=k + 1) for k, (h, v, l) in enumerate(opts)])
+            ctx.forcing_upload(f)
+            ctx.set_wsplit(ws)
+            for k in range(len(opts)):
+                t32 = tr[k].astype(np.float32)
+                ctx.tracer_upload(k, t32, t32)
+            ctxs.append(ctx)
+        if batched:
+            b = G.Batch(ctxs)
+            b.run_steps(600.0, 3, use_graph=True)
+            b.close()
+        else:
+            for c in ctxs:
+                c.run_steps(600.0, 3, use_graph=True)
+        runs.append([[c.tracer_download(k)[0] for k in range(c.ntr)] for c in ctxs])
+        for c in ctxs:
+            assert c.status() == 0
+    for i in range(len(setups)):
+        for k in range(len(runs[0][i])):
+            a, b = runs[0][i][k], runs[1][i][k]
+            assert np.abs(a - b).max() <= 1e-6 * np.abs(a).max(), (i, k)
