@@ -92,3 +92,21 @@ def pi_file_mesh():
     the Euler angles 50, 15, -90), built from the copy of its .out files in tests/golden."""
     from fesom2_gb300 import meshio as MI
     return MI.mesh_from_files(MI.load_files(os.path.join(GOLDEN, "mesh_pi.npz")), name="pi", **MI.PI)
+
+
+def shallow_mesh(nl: int = 5, seed: int = 7):
+    """A 10 x 12 channel whose element columns hold 2 to nl-1 layers at random (2-layer,
+    3-layer and deeper columns side by side): the shortest columns the path accepts."""
+    base = M.channel_mesh(10, 12, 5000.0, -np.arange(nl) * 40.0)
+    rng = np.random.default_rng(seed)
+    p = np.r_[0.7, np.full(nl - 3, 0.3 / (nl - 3))]
+    nlev = rng.choice(np.arange(3, nl + 1), size=base.elem2D, p=p).astype(np.int32)
+    depth = np.full(base.nod2D, -40.0 * (nl - 1))
+    return M._finish_mesh(base.coord_nod2D, base.elem2D_nodes.astype(np.int64), base.cyclic_length, True,
+                          base.zbar, depth, False, "shallow", nlevels=nlev)
+
+
+@pytest.fixture(scope="session")
+def shallow_channel():
+    return shallow_mesh()
+
