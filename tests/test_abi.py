@@ -85,3 +85,19 @@ def test_missing_library_fails_loudly(tmp_path):
     with pytest.raises(FileNotFoundError):
         G2.load(str(tmp_path / "nope.so"))
     importlib.reload(G)
+
+
+@pytest.mark.parametrize("field,index,value", [("elem2D_nodes", (0, 1), -1), ("elem2D_nodes", (5, 2), 10 ** 6),
+                                               ("edge_tri", (0, 0), 10 ** 6), ("nlevels", (2,), 99),
+                                               ("ulevels_nod2D", (0,), 40), ("edges", (1, 1), -3)])
+def test_mesh_check_rejects_out_of_range_entries(lib, channel_small, field, index, value):
+    """Index and level validation on the host, before any device work: every out-of-range
+    entry is a FESOM_ERR_MESH with a message."""
+    import copy
+    m = copy.deepcopy(channel_small)
+    a = getattr(m, field).copy()
+    a[index] = value
+    setattr(m, field, a)
+    with pytest.raises(G.FesomGpuError) as e:
+        G.mesh_check(m)
+    assert e.value.rc == 3 and len(str(e.value)) > 20
