@@ -26,6 +26,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 
@@ -136,7 +137,9 @@ class ClockSampler:
     def __init__(self, idx: int):
         self.idx = idx
         self.proc = None
-        self.out = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        # raw samples: FESOM_BENCH_CLOCKS_DIR if set, else the temporary directory
+        d = os.environ.get("FESOM_BENCH_CLOCKS_DIR") or tempfile.gettempdir()
+        self.out = os.path.join(d, f"clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         os.makedirs(os.path.dirname(self.out), exist_ok=True)
