@@ -11,16 +11,25 @@
  *                               (init_tracers_AB, do_oce_adv_tra, del_ttf sum,
  *                               diff_tracers_ale's T* update and implicit
  *                               vertical diffusion) for all tracers at once
+ *   fesom_gpu_diff_hor          diff_part_hor_redi       src/oce_ale_tracer.F90:1526-1689 (Redi off)
+ *   fesom_gpu_diff_ver_expl     diff_ver_part_expl_ale   src/oce_ale_tracer.F90:841-902
+ *   fesom_gpu_tracer_tail       tail of solve_tracers_ale src/oce_ale_tracer.F90:353-375, 497-525
  *   fesom_gpu_init              setup of the mesh-derived work arrays:
  *                               oce_adv_tra_fct_init  src/oce_adv_tra_fct.F90:35-67,
  *                               muscl_adv_init        src/oce_muscl_adv.F90:32-352,
  *                               find_levels_min_e2n   src/oce_mesh.F90:1656-1694
  *
+ * and adds device-resident stepping (fesom_gpu_state_setup / _forcing_upload /
+ * _run_steps, CUDA-graph replay), a host-array FP32 step with the transfers
+ * overlapped (fesom_gpu_step_host_f32) and a batch of independent meshes
+ * (fesom_gpu_batch_*).
+ *
  * All arrays are passed by address in the reference's Fortran layout
  * a(level, entity) (column-major, level-contiguous), exactly as the derived
  * types t_mesh / t_tracer / t_dyn hold them, so a Fortran caller passes
  * c_loc() of its arrays with no copy.  Host pointers are copied to the device
- * inside the call; the *_dev variants take device pointers.
+ * inside the call; fesom_gpu_tracer_device_ptr and fesom_gpu_vdiff_impl_noalloc
+ * work on device memory.
  *
  * Error convention: every entry point returns 0 on success and a FESOM_ERR_*
  * code otherwise (the reference aborts through par_ex on the same conditions);
