@@ -16,7 +16,8 @@ import numpy as np
 from . import build as _build
 
 _P = C.c_void_p
-LIB_PATH = _build.LIB
+# the in-tree build, or another build of the same sources named by FESOM_GPU_LIB
+LIB_PATH = os.path.abspath(os.environ["FESOM_GPU_LIB"]) if os.environ.get("FESOM_GPU_LIB") else _build.LIB
 
 PREC_FP64, PREC_FP32 = 0, 1
 HOR = {"MUSCL": 0, "MFCT": 1, "UPW1": 2}
