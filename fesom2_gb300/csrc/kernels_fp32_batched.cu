@@ -1252,97 +1252,99 @@ struct VdiffWarp {
 // forward and back substitution of tracers t1 and t2 (t2 < 0: none) of a column of NCH
 // chunks: the chunks' scans are independent straight-line code; only the carries between
 // chunks are serial
-template <int NCH>
-__device__ __forceinline__ void vdiff_pair(const DTopo &tp, const DForcing<float> &f, const B32View &B, int n,
-                                           int lane, int nzmin, int nzmax, int t1, int t2, VdiffWarp &W) {
+#ifndef FESOM_VDIFF_NT
+#define FESOM_VDIFF_NT 3  // tracers whose scan chains interleave in one pass (2: 12.8 ms, 3: 11.4, 4: 12.5 on the 24-tracer sphere)
+#endif
+
+// the forward and backward scans of NT tracers (the first nt of them real), interleaved
+template <int NCH, int NT>
+__device__ __forceinline__ void vdiff_multi(const DTopo &tp, const DForcing<float> &f, const B32View &B, int n,
+                                            int lane, int nzmin, int nzmax, const int (&tt)[NT], int nt,
+                                            VdiffWarp &W) {
     using C = Chunk<1, 1>;
     const int L1 = tp.L1;
-    const bool two = t2 >= 0;
-    float *__restrict__ T1 = B.Tnew + (size_t)t1 * B.sN;
-    float *__restrict__ T2 = B.Tnew + (size_t)(two ? t2 : t1) * B.sN;
-    const float bc1 = f.bc ? f.bc[(size_t)t1 * tp.N2 + n] : 0.f;
-    const float bc2 = (f.bc && two) ? f.bc[(size_t)t2 * tp.N2 + n] : 0.f;
-    float a1[NCH], a2[NCH], y1[NCH], y2[NCH];
+    float *__restrict__ Tq[NT];
+    float bc[NT];
+#pragma unroll
+    for (int q = 0; q < NT; q++) {
+        const int t = q < nt ? tt[q] : tt[0];
+        Tq[q] = B.Tnew + (size_t)t * B.sN;
+        bc[q] = (f.bc && q < nt) ? f.bc[(size_t)t * tp.N2 + n] : 0.f;
+    }
+    float a[NT][NCH], y[NT][NCH];
 #pragma unroll
     for (int ch = 0; ch < NCH; ch++) {
         const C k(nzmin, nzmax, ch, lane);
-        const int nz = k.nz, i = n * L1 + nz - 1;
-        a1[ch] = k.lvl ? T1[i] : 0.f;
-        a2[ch] = (k.lvl && two) ? T2[i] : 0.f;
+        const int i = n * L1 + k.nz - 1;
+#pragma unroll
+        for (int q = 0; q < NT; q++) a[q][ch] = (k.lvl && q < nt) ? Tq[q][i] : 0.f;
     }
 #pragma unroll
     for (int ch = 0; ch < NCH; ch++) {
         const C k(nzmin, nzmax, ch, lane);
         const int nz = k.nz;
-        const float u1 = sh_up(a1[ch], 1), d1 = sh_dn(a1[ch], 1);
-        const float u2 = sh_up(a2[ch], 1), d2 = sh_dn(a2[ch], 1);
-        float b1 = 0.f, b2 = 0.f;
-        if (k.out) {
-            const float4 fz = W.fac[nz];
-            float r1 = 0.f, r2 = 0.f;
-            if (nz > nzmin) {
-                r1 -= fz.x * (u1 - a1[ch]);
-                r2 -= fz.x * (u2 - a2[ch]);
-            }
-            if (nz < nzmax - 1) {
-                r1 -= fz.y * (d1 - a1[ch]);
-                r2 -= fz.y * (d2 - a2[ch]);
-            }
-            if (nz == nzmin) {
-                r1 += bc1;
-                r2 += bc2;
-            }
-            b1 = r1 * fz.z;
-            b2 = r2 * fz.z;
+        float b[NT];
+        const float4 fz = k.out ? W.fac[nz] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q < NT; q++) {
+            const float u = sh_up(a[q][ch], 1), d = sh_dn(a[q][ch], 1);
+            float r = 0.f;
+            if (nz > nzmin) r -= fz.x * (u - a[q][ch]);
+            if (nz < nzmax - 1) r -= fz.y * (d - a[q][ch]);
+            if (nz == nzmin) r += bc[q];
+            b[q] = k.out ? r * fz.z : 0.f;
         }
 #pragma unroll
         for (int s = 0, off = 1; s < kScan; s++, off <<= 1) {
             const float w = W.af[ch][s][lane];
-            b1 = fmaf(w, __shfl_up_sync(kFull, b1, off), b1);
-            b2 = fmaf(w, __shfl_up_sync(kFull, b2, off), b2);
+#pragma unroll
+            for (int q = 0; q < NT; q++) b[q] = fmaf(w, __shfl_up_sync(kFull, b[q], off), b[q]);
         }
-        y1[ch] = b1;
-        y2[ch] = b2;
+#pragma unroll
+        for (int q = 0; q < NT; q++) y[q][ch] = b[q];
     }
-    float c1 = 0.f, c2 = 0.f;
+    float c[NT];
+#pragma unroll
+    for (int q = 0; q < NT; q++) c[q] = 0.f;
 #pragma unroll
     for (int ch = 0; ch < NCH; ch++) {
         const float w = W.af[ch][kScan][lane];
-        y1[ch] = fmaf(w, c1, y1[ch]);
-        y2[ch] = fmaf(w, c2, y2[ch]);
-        c1 = __shfl_sync(kFull, y1[ch], 30);  // last stored lane (Chunk<1, 1>)
-        c2 = __shfl_sync(kFull, y2[ch], 30);
+#pragma unroll
+        for (int q = 0; q < NT; q++) {
+            y[q][ch] = fmaf(w, c[q], y[q][ch]);
+            c[q] = __shfl_sync(kFull, y[q][ch], 30);  // last stored lane (Chunk<1, 1>)
+        }
     }
 #pragma unroll
     for (int ch = 0; ch < NCH; ch++) {
         const C k(nzmin, nzmax, ch, lane);
-        float b1 = k.out ? y1[ch] : 0.f, b2 = k.out ? y2[ch] : 0.f;
+        float b[NT];
+#pragma unroll
+        for (int q = 0; q < NT; q++) b[q] = k.out ? y[q][ch] : 0.f;
 #pragma unroll
         for (int s = 0, off = 1; s < kScan; s++, off <<= 1) {
             const float w = W.ab[ch][s][lane];
-            b1 = fmaf(w, __shfl_down_sync(kFull, b1, off), b1);
-            b2 = fmaf(w, __shfl_down_sync(kFull, b2, off), b2);
+#pragma unroll
+            for (int q = 0; q < NT; q++) b[q] = fmaf(w, __shfl_down_sync(kFull, b[q], off), b[q]);
         }
-        y1[ch] = b1;
-        y2[ch] = b2;
+#pragma unroll
+        for (int q = 0; q < NT; q++) y[q][ch] = b[q];
     }
-    c1 = c2 = 0.f;
+#pragma unroll
+    for (int q = 0; q < NT; q++) c[q] = 0.f;
 #pragma unroll
     for (int ch = NCH - 1; ch >= 0; ch--) {
         const C k(nzmin, nzmax, ch, lane);
         const float w = W.ab[ch][kScan][lane];
-        const float x1 = fmaf(w, c1, y1[ch]), x2 = fmaf(w, c2, y2[ch]);
-        c1 = __shfl_sync(kFull, x1, 1);  // first stored lane (Chunk<1, 1>)
-        c2 = __shfl_sync(kFull, x2, 1);
-        if (k.out) {
-            const int i = n * L1 + k.nz - 1;
-            const float v1 = a1[ch] + x1;
-            T1[i] = v1;
-            if (!isfinite(v1)) atomicOr(B.status, 1u);
-            if (two) {
-                const float v2 = a2[ch] + x2;
-                T2[i] = v2;
-                if (!isfinite(v2)) atomicOr(B.status, 1u);
+        const int i = n * L1 + k.nz - 1;
+#pragma unroll
+        for (int q = 0; q < NT; q++) {
+            const float x = fmaf(w, c[q], y[q][ch]);
+            c[q] = __shfl_sync(kFull, x, 1);  // first stored lane (Chunk<1, 1>)
+            if (k.out && q < nt) {
+                const float v = a[q][ch] + x;
+                Tq[q][i] = v;
+                if (!isfinite(v)) atomicOr(B.status, 1u);
             }
         }
     }
@@ -1382,22 +1384,25 @@ __device__ __forceinline__ void vdiff_unit(const DTopo &tp, const DForcing<float
         W.ab[ch][kScan][lane] = Ad;
     }
     __syncwarp();
-    // the tracers with implicit diffusion, two per pass: their scan chains interleave
+    // the tracers with implicit diffusion, FESOM_VDIFF_NT per pass: their scan chains interleave
+    constexpr int NT = FESOM_VDIFF_NT;
     unsigned long long todo = (B.ivd_mask & ~B.wimpl_mask) & (B.ntr >= 64 ? ~0ull : ((1ull << B.ntr) - 1));
     while (todo) {
-        const int t1 = __ffsll((long long)todo) - 1;
-        todo &= todo - 1;
-        int t2 = -1;
-        if (todo) {
-            t2 = __ffsll((long long)todo) - 1;
-            todo &= todo - 1;
+        int tt[NT], nt = 0;
+#pragma unroll
+        for (int q = 0; q < NT; q++) {
+            tt[q] = todo ? __ffsll((long long)todo) - 1 : (q ? tt[0] : 0);
+            if (todo) {
+                todo &= todo - 1;
+                nt++;
+            }
         }
         switch (nch) {
-            case 1: vdiff_pair<1>(tp, f, B, n, lane, nzmin, nzmax, t1, t2, W); break;
-            case 2: vdiff_pair<2>(tp, f, B, n, lane, nzmin, nzmax, t1, t2, W); break;
-            case 3: vdiff_pair<3>(tp, f, B, n, lane, nzmin, nzmax, t1, t2, W); break;
-            case 4: vdiff_pair<4>(tp, f, B, n, lane, nzmin, nzmax, t1, t2, W); break;
-            default: vdiff_pair<5>(tp, f, B, n, lane, nzmin, nzmax, t1, t2, W); break;
+            case 1: vdiff_multi<1, NT>(tp, f, B, n, lane, nzmin, nzmax, tt, nt, W); break;
+            case 2: vdiff_multi<2, NT>(tp, f, B, n, lane, nzmin, nzmax, tt, nt, W); break;
+            case 3: vdiff_multi<3, NT>(tp, f, B, n, lane, nzmin, nzmax, tt, nt, W); break;
+            case 4: vdiff_multi<4, NT>(tp, f, B, n, lane, nzmin, nzmax, tt, nt, W); break;
+            default: vdiff_multi<5, NT>(tp, f, B, n, lane, nzmin, nzmax, tt, nt, W); break;
         }
     }
 }
