@@ -309,16 +309,18 @@ __device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &
         const int iv = n * nl + nz - 1;  // interface nz
         // ---- tracer-independent part of the chunk ----
         int off[KD];
-        float v[KD];
+        float am[KD];  // upwind inflow weight of each edge slot (0 where the slot is dry)
         unsigned okm = 0;
         float Dh = 0.f;  // net horizontal volume flux into the node
 #pragma unroll
         for (int u = 0; u < KD; u++) {
             const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
             off[u] = S.m[u] * L1 + nz - 1;
-            v[u] = ok ? VF[S.e[u] * L1 + nz - 1] : 0.f;
+            const float v = ok ? VF[S.e[u] * L1 + nz - 1] : 0.f;
             okm |= ok ? 1u << u : 0u;
-            Dh += ((own >> u) & 1u) ? -v[u] : v[u];
+            const bool ow = (own >> u) & 1u;
+            Dh += ow ? -v : v;
+            am[u] = ow ? -fminf(v, 0.f) : fmaxf(v, 0.f);
         }
         float ar0 = 0.f, we0 = 0.f, w0 = 0.f, sdt = 0.f, Z0 = 0.f, hr = 0.f;
         if (k.lvl) {
@@ -365,11 +367,8 @@ __device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &
             // LO: upwind edge fluxes in difference form, sum_j am_j (T_j - T_n) + Dh T_n
             float hs = Dh * Tn;
 #pragma unroll
-            for (int u = 0; u < KD; u++) {
-                if (!((okm >> u) & 1u)) continue;
-                const float am = ((own >> u) & 1u) ? -fminf(v[u], 0.f) : fmaxf(v[u], 0.f);
-                hs += am * (tm[u] - Tn);
-            }
+            for (int u = 0; u < KD; u++)
+                if ((okm >> u) & 1u) hs += am[u] * (tm[u] - Tn);
             // upwind vertical flux with w_e at interface nz (adv_tra_ver_upw1)
             float fv0 = 0.f;
             if (k.lvl) {
