@@ -317,3 +317,28 @@ def test_fp32_mixed_schemes_in_one_batch(basin_irregular):
         err = np.abs(v[wet] - T64[k][wet]).max() / np.abs(T64[k][wet]).max()
         assert err <= 1e-5, (specs[k], err)
     assert ctx.status() == 0
+
+
+def test_fp32_stage_passes_do_not_change_results(basin_irregular):
+    """Tracers per launch of each node stage (fesom_gpu_set_stage_tracers) is a performance
+    setting: any split of the 7 tracers gives the same bits."""
+    mesh = basin_irregular
+    f, tr = _setup(mesh, "basin", ntr=7)
+    cfgs = [G.tra_cfg(["MUSCL", "MFCT", "UPW1"][k % 3], ["QR4C", "UPW1", "PPM", "CDIFF"][k % 4],
+                      "FCT" if k % 3 else "NON", id=k + 1) for k in range(7)]
+    outs = []
+    for split in ([0, 0, 0, 0], [3, 2, 5, 1], [1, 7, 2, 4]):
+        ctx = G.Context(mesh, G.PREC_FP32, max_tracers=7)
+        ctx.state_setup(cfgs)
+        ctx.forcing_upload(f)
+        for st, v in enumerate(split):
+            ctx.set_stage_tracers(st, v)
+        for k in range(7):
+            t32 = tr[k].astype(np.float32)
+            ctx.tracer_upload(k, t32, t32)
+        ctx.run_steps(f.dt, 3, use_graph=True)
+        outs.append([ctx.tracer_download(k, dtype=np.float32)[0] for k in range(7)])
+        assert ctx.status() == 0
+    for o in outs[1:]:
+        for k in range(7):
+            assert np.array_equal(o[k], outs[0][k]), k
