@@ -344,11 +344,13 @@ def _levels_from_depth(tri: np.ndarray, depth_nod: np.ndarray, zbar: np.ndarray,
 
 def _finish_mesh(coord: np.ndarray, tri: np.ndarray, cyc: float, cartesian: bool,
                  zbar: np.ndarray, depth_nod: np.ndarray, partial_cells: bool,
-                 name: str, nlevels: Optional[np.ndarray] = None, edge_set=None) -> Mesh:
+                 name: str, nlevels: Optional[np.ndarray] = None, edge_set=None,
+                 ulevels: Optional[np.ndarray] = None) -> Mesh:
     """Derived arrays of a mesh from node coordinates (radians), triangles (0-based), levels
     and node depths.  ``nlevels`` (element level counts) and ``edge_set`` = (edges, edge_tri,
     edge2D_in), 0-based with -1 for a missing triangle, are taken as given when passed (as
-    the reference takes them from the partitioner's files), else built here."""
+    the reference takes them from the partitioner's files), else built here.  ``ulevels``
+    (element first wet levels, cavities under ice shelves) defaults to 1 everywhere."""
     nl = zbar.size
     Z = 0.5 * (zbar[:-1] + zbar[1:])
     tri = _orient_clockwise(coord, tri.astype(np.int64), cyc)
@@ -367,10 +369,12 @@ def _finish_mesh(coord: np.ndarray, tri: np.ndarray, cyc: float, cartesian: bool
     if nlevels is None:
         nlevels = _levels_from_depth(tri, depth_nod, zbar, Z)
     nlevels = np.ascontiguousarray(nlevels, dtype=np.int32)
-    ulevels = np.ones(T2, dtype=np.int32)
+    ulevels = np.ones(T2, dtype=np.int32) if ulevels is None else np.ascontiguousarray(ulevels, dtype=np.int32)
+    cavity = bool((ulevels > 1).any())
     nlevels_nod2D = np.zeros(N2, dtype=np.int32)
     np.maximum.at(nlevels_nod2D, tri.reshape(-1), np.repeat(nlevels, 3))
-    ulevels_nod2D = np.ones(N2, dtype=np.int32)
+    ulevels_nod2D = np.full(N2, nl + 1, dtype=np.int32)
+    np.minimum.at(ulevels_nod2D, nie_node, ulevels[nie])
     nlevels_nod2D_min = np.full(N2, nl + 1, dtype=np.int32)
     np.minimum.at(nlevels_nod2D_min, nie_node, nlevels[nie])
     ulevels_nod2D_max = np.zeros(N2, dtype=np.int32)
@@ -453,9 +457,12 @@ def _finish_mesh(coord: np.ndarray, tri: np.ndarray, cyc: float, cartesian: bool
 
     Lh = np.arange(nl - 1)[None, :]
     dz = (zbar[:-1] - zbar[1:])[None, :]
-    hnode = np.where(Lh < (nln - 2)[:, None], dz, 0.0)
+    uln = ulevels_nod2D.astype(np.int64)
+    ule = ulevels.astype(np.int64)
+    # layers above the first wet level (under an ice shelf) have no thickness
+    hnode = np.where((Lh < (nln - 2)[:, None]) & (Lh >= (uln - 1)[:, None]), dz, 0.0)
     hnode[np.arange(N2), nln - 2] = bottom_node_thickness
-    helem = np.where(Lh < (nle - 2)[:, None], dz, 0.0)
+    helem = np.where((Lh < (nle - 2)[:, None]) & (Lh >= (ule - 1)[:, None]), dz, 0.0)
     helem[np.arange(T2), nle - 2] = bottom_elem_thickness
 
     # area / areasvol (oce_mesh.F90:2277-2340)
@@ -464,10 +471,29 @@ def _finish_mesh(coord: np.ndarray, tri: np.ndarray, cyc: float, cartesian: bool
     # stops and take a reverse cumulative sum over levels
     a3 = (elem_area_rad / 3.0)[nie]
     stop = nle[nie] - 2                     # last wet layer (0-based)
-    D = np.bincount(nie_node.astype(np.int64) * nl + stop, weights=a3, minlength=N2 * nl).reshape(N2, nl)
-    area = np.flip(np.cumsum(np.flip(D, axis=1), axis=1), axis=1) * (R_EARTH * R_EARTH)
-    wet_n = np.arange(nl)[None, :] < (nln - 1)[:, None]
-    areasvol = np.where(wet_n, area, 0.0)
+    if not cavity:
+        D = np.bincount(nie_node.astype(np.int64) * nl + stop, weights=a3, minlength=N2 * nl).reshape(N2, nl)
+        area = np.flip(np.cumsum(np.flip(D, axis=1), axis=1), axis=1) * (R_EARTH * R_EARTH)
+        wet_n = np.arange(nl)[None, :] < (nln - 1)[:, None]
+        areasvol = np.where(wet_n, area, 0.0)
+    else:
+        # an element counts at levels ulevels..nlevels-1 only; areasvol of a level with an
+        # element still under the shelf takes the area of the level below
+        # (oce_mesh.F90:2277-2330, use_cavity)
+        start = ule[nie] - 1
+        area = np.zeros((N2, nl))
+        cav = np.zeros((N2, nl), dtype=np.int64)
+        nn = nie_node.astype(np.int64)
+        for k in range(nl):
+            on = (start <= k) & (k <= stop)
+            area[:, k] = np.bincount(nn, weights=np.where(on, a3, 0.0), minlength=N2)
+            cav[:, k] = np.bincount(nn, weights=(k < start).astype(np.float64), minlength=N2).astype(np.int64)
+        lev = np.arange(nl)[None, :]
+        wet_n = (lev >= (uln - 1)[:, None]) & (lev < (nln - 1)[:, None])
+        below = np.minimum(lev + 1, (nln - 2)[:, None])
+        area_below = np.take_along_axis(area, np.broadcast_to(below, area.shape), axis=1)
+        areasvol = np.where(wet_n, np.where(cav > 0, area_below, area), 0.0) * (R_EARTH * R_EARTH)
+        area = area * (R_EARTH * R_EARTH)
 
     return Mesh(
         nl=nl, coord_nod2D=np.ascontiguousarray(coord), elem2D_nodes=tri.astype(np.int32),

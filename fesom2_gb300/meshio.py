@@ -14,7 +14,9 @@ What the reference does on load, and this reader with it (src/oce_mesh.F90):
     triangle index <= 0 marking a boundary edge (:1791-1930);
   * triangle orientation made clockwise (``test_tri``, :1721-1742), then the derived
     geometry as for the generated meshes.
-Cavities (``cavity_*.out``) are not read: every column starts at level 1.
+Cavities: ``cavity_elvls.out`` gives each element's first wet level (ulevels) and
+``cavity_nlvls.out`` each node's, the smallest of its elements' (checked); without them every
+column starts at level 1.  The top cell under an ice shelf is a full cell.
 """
 from __future__ import annotations
 
@@ -87,7 +89,8 @@ def read_files(path: str) -> dict:
     zbar = aux[1:1 + nl].copy()
     depth = aux[1 + nl:].copy()
     out = {"xy_deg": xy, "flag": flag, "tri": tri, "zbar": zbar, "depth": depth, "N2": N2, "T2": T2}
-    for name, key in (("elvls.out", "elvls"), ("nlvls.out", "nlvls")):
+    for name, key in (("elvls.out", "elvls"), ("nlvls.out", "nlvls"), ("cavity_elvls.out", "cavity_elvls"),
+                      ("cavity_nlvls.out", "cavity_nlvls")):
         if os.path.exists(f(name)):
             out[key] = _tokens(f(name)).astype(np.int32)
     if os.path.exists(f("edges.out")):
@@ -143,8 +146,13 @@ def mesh_from_files(r: dict, cartesian: bool = False, cyclic_length_deg: float =
     if nlevels is not None and nlevels.size != T2:
         raise ValueError("elvls.out does not hold one level count per element")
     edge_set = (r["edges"], r["edge_tri"], int(r["edge2D_in"])) if "edges" in r else None
+    ulevels = r.get("cavity_elvls")
+    if ulevels is not None and ulevels.size != T2:
+        raise ValueError("cavity_elvls.out does not hold one level per element")
     mesh = M._finish_mesh(coord, r["tri"], cyclic_length_deg * RAD, cartesian, zbar, depth, partial_cells,
-                          name, nlevels=nlevels, edge_set=edge_set)
+                          name, nlevels=nlevels, edge_set=edge_set, ulevels=ulevels)
+    if "cavity_nlvls" in r and not np.array_equal(np.asarray(r["cavity_nlvls"]), mesh.ulevels_nod2D):
+        raise ValueError("cavity_nlvls.out disagrees with the shallowest element level around each node")
     if "nlvls" in r and not np.array_equal(np.asarray(r["nlvls"]), mesh.nlevels_nod2D):
         raise ValueError("nlvls.out disagrees with the deepest element level around each node")
     return mesh
@@ -153,6 +161,8 @@ def mesh_from_files(r: dict, cartesian: bool = False, cyclic_length_deg: float =
 # the namelist.config switches of the two meshes the reference's tests carry
 SOUFFLET = dict(cartesian=True, cyclic_length_deg=4.5, rotation=None)
 PI = dict(cartesian=False, cyclic_length_deg=360.0, rotation=(50.0, 15.0, -90.0))
+# the PI mesh with cavities: the default namelist.config switches, as for PI
+PI_CAVITY = dict(PI)
 
 
 def save_files(r: dict, path: str) -> None:

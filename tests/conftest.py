@@ -94,6 +94,15 @@ def pi_file_mesh():
     return MI.mesh_from_files(MI.load_files(os.path.join(GOLDEN, "mesh_pi.npz")), name="pi", **MI.PI)
 
 
+@pytest.fixture(scope="session")
+def pi_cavity_file_mesh():
+    """The PI mesh with ice-shelf cavities of the reference's test data (6808 nodes, 48 levels,
+    170 elements whose columns start below the surface), from the copy in tests/golden."""
+    from fesom2_gb300 import meshio as MI
+    return MI.mesh_from_files(MI.load_files(os.path.join(GOLDEN, "mesh_pi_cavity.npz")), name="pi_cavity",
+                              **MI.PI_CAVITY)
+
+
 def shallow_mesh(nl: int = 5, seed: int = 7):
     """A 10 x 12 channel whose element columns hold 2 to nl-1 layers at random (2-layer,
     3-layer and deeper columns side by side): the shortest columns the path accepts."""

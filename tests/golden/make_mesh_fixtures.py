@@ -1,5 +1,6 @@
-"""Copy the two FESOM2 mesh folders the reference's tests carry (Soufflet channel and the
-PI mesh, tests/data/MESHES/{soufflet,pi}) into tests/golden/mesh_*.npz, as the raw arrays
+"""Copy the FESOM2 mesh folders the reference's tests carry (Soufflet channel, the PI mesh and
+PI with ice-shelf cavities, tests/data/MESHES/{soufflet,pi,pi_cavity}) into
+tests/golden/mesh_*.npz, as the raw arrays
 of their .out files, so that tests can build those meshes where the reference tree is
 absent.  Run from the repository root:  python tests/golden/make_mesh_fixtures.py [ref]
 (ref: the reference checkout, default /root/reference).
@@ -14,7 +15,7 @@ from fesom2_gb300 import meshio as MI  # noqa: E402
 
 
 def main(ref: str = "/root/reference") -> None:
-    for name in ("soufflet", "pi"):
+    for name in ("soufflet", "pi", "pi_cavity"):
         r = MI.read_files(os.path.join(ref, "tests", "data", "MESHES", name))
         out = os.path.join(ROOT, "tests", "golden", f"mesh_{name}.npz")
         MI.save_files(r, out)

@@ -1,4 +1,5 @@
-"""The GPU step on the two meshes of the reference's test data (Soufflet channel, PI),
+"""The GPU step on the meshes of the reference's test data (Soufflet channel, PI, PI with
+ice-shelf cavities),
 through the C ABI: FP64 bit for bit with the oracle over several steps (with the
 Soufflet namelist's horizontal diffusion, K_hor = 10), FP32 within 1e-5 normwise."""
 import numpy as np
@@ -12,7 +13,8 @@ from tests.test_oracle import _ki
 
 pytestmark = pytest.mark.gpu
 
-CASES = [("soufflet_file_mesh", "channel", 10.0), ("pi_file_mesh", "sphere", None)]
+CASES = [("soufflet_file_mesh", "channel", 10.0), ("pi_file_mesh", "sphere", None),
+         ("pi_cavity_file_mesh", "sphere", None)]
 
 
 @pytest.mark.parametrize("meshname,kind,khor", CASES)

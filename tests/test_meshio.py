@@ -14,7 +14,7 @@ from tests.conftest import GOLDEN, wet_mask
 REF_MESHES = "/root/reference/tests/data/MESHES"
 
 
-@pytest.mark.parametrize("name", ["soufflet", "pi"])
+@pytest.mark.parametrize("name", ["soufflet", "pi", "pi_cavity"])
 def test_fixture_is_the_mesh_folder(name):
     """tests/golden/mesh_*.npz holds exactly the arrays of the reference's mesh folder."""
     folder = os.path.join(REF_MESHES, name)
@@ -28,7 +28,8 @@ def test_fixture_is_the_mesh_folder(name):
 
 
 @pytest.mark.parametrize("meshname,E2,E2in,nl", [("soufflet_file_mesh", 8575, 8525, 41),
-                                                 ("pi_file_mesh", 8986, 8531, 48)])
+                                                 ("pi_file_mesh", 8986, 8531, 48),
+                                                 ("pi_cavity_file_mesh", 19267, 18089, 48)])
 def test_file_topology(meshname, E2, E2in, nl, request):
     """Edges in file order: internal ones first, the same set as the edges of the triangles,
     the first triangle left of n1 -> n2; node levels the deepest of their elements."""
@@ -82,7 +83,8 @@ def test_pi_rotation(pi_file_mesh):
     assert 0.6 < frac < 0.75
 
 
-@pytest.mark.parametrize("meshname,kind", [("soufflet_file_mesh", "channel"), ("pi_file_mesh", "sphere")])
+@pytest.mark.parametrize("meshname,kind", [("soufflet_file_mesh", "channel"), ("pi_file_mesh", "sphere"),
+                                           ("pi_cavity_file_mesh", "sphere")])
 def test_oracle_keeps_a_constant_tracer(meshname, kind, request):
     """Constant-tracer preservation on the file meshes (the vertical velocity closes the
     discrete divergence of the horizontal flow)."""
@@ -107,3 +109,36 @@ def test_reader_rejects_inconsistent_levels(tmp_path):
     r["elvls"] = r["elvls"][:-1]
     with pytest.raises(ValueError):
         MI.mesh_from_files(r, **MI.SOUFFLET)
+
+
+def test_cavity_levels(pi_cavity_file_mesh):
+    """Under the ice shelves the columns start below the surface: node first levels are the
+    shallowest of their elements', the layers above have no thickness, and areasvol of a level
+    with an element still under the shelf is the area of the level below."""
+    m = pi_cavity_file_mesh
+    assert (m.ulevels > 1).sum() == 170 and (m.ulevels_nod2D > 1).sum() == 95
+    umin = np.full(m.nod2D, 99)
+    np.minimum.at(umin, m.elem2D_nodes.reshape(-1), np.repeat(m.ulevels, 3))
+    assert np.array_equal(umin, m.ulevels_nod2D)
+    lev = np.arange(m.nl - 1)[None, :]
+    above = lev < (m.ulevels_nod2D - 1)[:, None]
+    assert np.all(m.hnode[above] == 0.0)
+    wet = wet_mask(m)
+    assert np.all(m.hnode[wet] > 0.0) and np.all(m.areasvol[:, :-1][wet] > 0.0)
+
+
+@pytest.mark.parametrize("scheme", [("MUSCL", "QR4C", "FCT"), ("MFCT", "PPM", "NON"), ("UPW1", "CDIFF", "FCT")])
+def test_cavity_step_matches_restatement(pi_cavity_file_mesh, scheme):
+    """Both restatements agree bit for bit on columns that start below the surface."""
+    from tests.conftest import perturbed_old
+    from tests.refimpl import Ref
+    m = pi_cavity_file_mesh
+    f = O.ensure_f64(M.make_forcing(m, "sphere", seed=3, dt=600.0))
+    T = np.ascontiguousarray(M.make_tracers(m, "sphere", ntr=1, seed=6)[0])
+    Told = perturbed_old(T, np.random.default_rng(1))
+    om = O.OracleMesh(m)
+    To, Oo = T.copy(), Told.copy()
+    om.tracer_step(f, O.cfg_struct(*scheme), To, np.zeros_like(To), Oo)
+    Tr, _ = Ref(m).tracer_step(f, T, Told, om.work["edge_up_dn_tri"], om.work["nboundary_lay"], *scheme)
+    assert np.array_equal(To, Tr)
+
