@@ -56,6 +56,9 @@ struct fesom_gpu_ctx {
     // whole launch group.  Fewer tracers per pass keep the neighbour columns of the nodes in
     // flight inside L2 (fesom_gpu_set_stage_tracers)
     int stage_tr[4] = {0, 0, 6, 6};
+    // tracer groups of fesom_gpu_step_host_f32, in order (fesom_gpu_set_host_groups);
+    // empty: the automatic ramp of host_groups()
+    std::vector<int> host_groups;
     cudaGraphExec_t gexec = nullptr;
     double g_dt = 0.0;
     // FP32 batched form: rotating time-level buffers and its work arrays
@@ -1188,6 +1191,7 @@ int fesom_gpu_state_setup(fesom_gpu_ctx *ctx, int32_t ntr, const fesom_tra_cfg *
     } else if ((rc = alloc_state(ctx, ntr, ab_max))) {
         return rc;
     }
+    if (ctx->ntr != ntr) ctx->host_groups.clear();
     ctx->ntr = ntr;
     ctx->cfgs.assign(cfgs, cfgs + ntr);
     std::vector<DCfg> d(ntr);
@@ -1404,6 +1408,7 @@ int fesom_gpu_set_tracers_per_launch(fesom_gpu_ctx *ctx, int32_t n) {
     if (!ctx || n < 0) return FESOM_ERR_ARG;
     if (!ctx->state_ready) { ctx->err = "call fesom_gpu_state_setup first"; return FESOM_ERR_STATE; }
     ctx->group = n == 0 ? ctx->group_cap : std::min((int)n, ctx->group_cap);
+    ctx->host_groups.clear();
     if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
     free_graphs32(ctx);
     return FESOM_OK;
@@ -1640,6 +1645,49 @@ int fesom_gpu_tracer_tail(fesom_gpu_ctx *ctx, int32_t ntr, const fesom_tra_cfg *
     return wait_stream(ctx, -1);
 }
 
+}  // extern "C"
+
+// Tracer groups of the host-array step: the first group's upload and the last group's
+// download are the parts of the step no compute hides, so both are small; between them the
+// groups double up to the launch group.  With G tracers per launch the first group holds
+// max(1, G/3) tracers and so does the last (24 tracers, G = 6: 2, 4, 6, 6, 4, 2).
+static std::vector<int> host_groups(const fesom_gpu_ctx *ctx) {
+    if (!ctx->host_groups.empty()) return ctx->host_groups;
+    const int G = std::max(1, ctx->group), s0 = std::max(1, G / 3);
+    std::vector<int> out;
+    for (int rem = ctx->ntr, s = s0; rem > 0; s = std::min(G, 2 * s)) {
+        const int x = std::min(std::min(s, rem), G);
+        out.push_back(x);
+        rem -= x;
+    }
+    if (out.size() > 1 && out.back() > s0) {
+        const int last = out.back();
+        out.back() = last - s0;
+        out.push_back(s0);
+    }
+    return out;
+}
+
+extern "C" {
+
+int fesom_gpu_set_host_groups(fesom_gpu_ctx *ctx, int32_t n, const int32_t *sizes) {
+    if (!ctx || n < 0 || (n > 0 && !sizes)) return FESOM_ERR_ARG;
+    if (!ctx->state_ready) { ctx->err = "call fesom_gpu_state_setup first"; return FESOM_ERR_STATE; }
+    std::vector<int> gs;
+    int sum = 0;
+    for (int i = 0; i < n; i++) {
+        if (sizes[i] < 1 || sizes[i] > ctx->group) {
+            ctx->err = "a host group holds 1 to tracers-per-launch tracers";
+            return FESOM_ERR_ARG;
+        }
+        gs.push_back(sizes[i]);
+        sum += sizes[i];
+    }
+    if (n > 0 && sum != ctx->ntr) { ctx->err = "the host groups must hold every tracer once"; return FESOM_ERR_ARG; }
+    ctx->host_groups = gs;
+    return FESOM_OK;
+}
+
 int fesom_gpu_step_host_f32(fesom_gpu_ctx *ctx, double dt, const float *uv, const float *w, const float *wi,
                             const float *we, const float *Kv, const float *bc_surf, const float *const *values_in,
                             const float *const *valuesold_in, float *const *values_out, float *const *valuesold_out) {
@@ -1660,11 +1708,13 @@ int fesom_gpu_step_host_f32(fesom_gpu_ctx *ctx, double dt, const float *uv, cons
                 return rc;
         return wait_stream(ctx, -1);
     }
-    // tracer groups of ctx->group tracers
-    const int G = ctx->group;
-    std::vector<int> gs;  // first tracer of each group, and ntr at the end
-    for (int t = 0; t < ntr; t += G) gs.push_back(t);
-    gs.push_back(ntr);
+    // tracer groups: first tracer of each group, and ntr at the end
+    std::vector<int> gs(1, 0);
+    for (int x : host_groups(ctx)) gs.push_back(gs.back() + x);
+    if (gs.back() != ntr || (int)gs.size() < 2) {
+        ctx->err = "the host groups must hold every tracer once";
+        return FESOM_ERR_ARG;
+    }
     const int ng = (int)gs.size() - 1;
     while ((int)ctx->ev_in.size() < ng) {
         cudaEvent_t a, b;

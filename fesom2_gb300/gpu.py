@@ -84,6 +84,7 @@ _SIGS = {
     "fesom_gpu_run_steps": ([_P, C.c_double, C.c_int32, C.c_int32], C.c_int),
     "fesom_gpu_tracer_content": ([_P, _P], C.c_int),
     "fesom_gpu_set_tracers_per_launch": ([_P, C.c_int32], C.c_int),
+    "fesom_gpu_set_host_groups": ([_P, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
     "fesom_gpu_profile_step": ([_P, C.c_double, _P, _P], C.c_int),
     "fesom_gpu_launches_per_step": ([_P, C.POINTER(C.c_int32)], C.c_int),
     "fesom_gpu_debug_fetch": ([_P, C.c_char_p, C.c_int32, _P, C.c_size_t], C.c_int),
@@ -335,6 +336,12 @@ class Context:
 
     def set_tracers_per_launch(self, n: int):
         self._chk(self.L.fesom_gpu_set_tracers_per_launch(self.h, int(n)))
+
+    def set_host_groups(self, sizes=()):
+        """Group sizes of ``step_host_f32`` in order (``fesom_gpu_set_host_groups``); an empty
+        sequence restores the default ramp."""
+        a = (C.c_int32 * max(1, len(sizes)))(*[int(x) for x in sizes])
+        self._chk(self.L.fesom_gpu_set_host_groups(self.h, len(sizes), a))
 
     def step_host_f32(self, forcing, values_in, valuesold_in, values_out=None, valuesold_out=None):
         """One FP32 step from and to host float32 arrays with the transfers overlapped with the

@@ -302,16 +302,24 @@ int fesom_gpu_tracer_tail(fesom_gpu_ctx *ctx, int32_t ntr, const fesom_tra_cfg *
                           const double *ztem, double *const *values);
 
 /* One step of an FP32 context from and to host arrays (FP32, the caller's layout), with the
- * transfers overlapped with the compute: the tracers move in launch groups
- * (fesom_gpu_set_tracers_per_launch) -- a group computes as soon as its values and previous
- * level are resident, and is copied back as soon as it is done, while later groups upload
- * and earlier ones download.  values_out / valuesold_out may be the input arrays (in-place
+ * transfers overlapped with the compute: the tracers move in groups of at most the tracers
+ * per launch (fesom_gpu_set_tracers_per_launch) -- a group computes as soon as its values and
+ * previous level are resident, and is copied back as soon as it is done, while later groups
+ * upload and earlier ones download.  The first group's upload and the last group's download
+ * are not hidden, so by default both groups are small and the groups between double up to the
+ * launch group (G tracers per launch: max(1, G/3) tracers first and last; 24 tracers, G = 6:
+ * 2, 4, 6, 6, 4, 2); fesom_gpu_set_host_groups sets another order.  values_out / valuesold_out may be the input arrays (in-place
  * update, as the reference's tracer arrays); valuesold_out may be NULL: the previous level
  * after the step is the values the step started from, so a caller that keeps two time-level
  * arrays and swaps them (values_out = valuesold_in, then exchange the roles) moves only the new
  * values back.  Blocks until the results are in host memory; page-locked host arrays give
  * the full transfer rate.  AB3 contexts take the serial path (their previous levels are interleaved on
  * the host). */
+/* Group sizes of fesom_gpu_step_host_f32, in order: n sizes of 1 to the tracers per launch
+ * each, summing to the context's tracer count (FESOM_ERR_ARG otherwise); n = 0 restores the
+ * default.  Cleared by fesom_gpu_set_tracers_per_launch and by a state setup with another
+ * tracer count. */
+int fesom_gpu_set_host_groups(fesom_gpu_ctx *ctx, int32_t n, const int32_t *sizes);
 int fesom_gpu_step_host_f32(fesom_gpu_ctx *ctx, double dt, const float *uv, const float *w, const float *wi,
                             const float *we, const float *Kv, const float *bc_surf, const float *const *values_in,
                             const float *const *valuesold_in, float *const *values_out, float *const *valuesold_out);

@@ -85,3 +85,31 @@ def test_host_step_with_swapped_time_levels(channel_seamount):
         assert np.array_equal(levels[0][k], want[k][0]), k
         assert np.array_equal(levels[1][k], want[k][1]), k
     assert b.status() == 0
+
+
+def test_host_step_with_explicit_groups(channel_seamount):
+    """Group orders set by fesom_gpu_set_host_groups give the same values as the default ramp;
+    orders that miss or repeat a tracer, or exceed the tracers per launch, are rejected."""
+    mesh = channel_seamount
+    f32, tr, cfgs = _setup(mesh, "channel", 2)
+    n = len(cfgs)
+    results = []
+    for sizes in ((), (3, 2), (1, 1, 1, 1, 1), (2, 3)):
+        b = G.Context(mesh, G.PREC_FP32, max_tracers=n)
+        b.state_setup(cfgs)
+        b.set_tracers_per_launch(3)
+        b.set_host_groups(sizes)
+        levels = [[np.array(tr[k], copy=True) for k in range(n)], [np.array(tr[k], copy=True) for k in range(n)]]
+        for _ in range(2):
+            cur, old = levels
+            b.step_host_f32(f32, cur, old, old, None)
+            levels.reverse()
+        results.append(levels[0])
+        assert b.status() == 0
+        for bad in ((3, 1), (4, 1), (3, 3), (0, 3, 2)):
+            with pytest.raises(G.FesomGpuError):
+                b.set_host_groups(bad)
+        b.close()
+    for r in results[1:]:
+        for k in range(n):
+            assert np.array_equal(r[k], results[0][k]), k
