@@ -305,6 +305,14 @@ def run_ours(args, rank, world, local_rank):
             a[0] += t
             a[1] += n
     content = ctx.content()
+    # FCT positivity of the lognormal passive tracers after every step run so far: the
+    # smallest wet value of the last tracer (its initial values are strictly positive)
+    pos_min = None
+    if ntr > 2:
+        lev = np.arange(mesh.nl - 1)[None, :]
+        wet_l = (lev >= (mesh.ulevels_nod2D - 1)[:, None]) & (lev < (mesh.nlevels_nod2D - 1)[:, None])
+        pos_min = float(ctx.tracer_download(ntr - 1, dtype=np.float32)[0][wet_l].min())
+        del wet_l
     ctx.close()
     del ctx
     torch.cuda.synchronize()
@@ -454,7 +462,7 @@ def run_ours(args, rank, world, local_rank):
                            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                            "mesh_generation_s": gen_s},
                 "gpu_launches": launches * args.steps,
-                "clocks": clk.summary(), "status_word": st,
+                "clocks": clk.summary(), "status_word": st, "lognormal_tracer_min_after_steps": pos_min,
                 "content_fp64": [float(c) for c in content[:2]]}
         line.update(res)
         print(json.dumps(line), flush=True)
