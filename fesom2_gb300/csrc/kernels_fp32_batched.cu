@@ -270,14 +270,36 @@ template <int HU, int HD>
 struct Chunk {
     static constexpr int OUT = 32 - HU - HD;
     int nz;
+    int q = 0;  // tracer slot of the lane (packed chunks)
     bool lvl, out;
     __device__ __forceinline__ Chunk(int nzmin, int nzmax, int ch, int lane) {
         nz = nzmin - HU + OUT * ch + lane;
         lvl = nz >= nzmin && nz <= nzmax - 1;
         out = lvl && lane >= HU && lane < 32 - HD;
     }
+    // the last chunk of a column in P segments of W = (its levels + HU + HD) lanes, one
+    // tracer per segment: segment q holds the lanes [q W, (q + 1) W), laid out as a whole
+    // chunk, so the vertical shuffles of a stored lane stay inside its segment
+    __device__ __forceinline__ Chunk(int nzmin, int nzmax, int ch, int lane, int W, int P) {
+        q = lane / W;
+        const int l = lane - q * W;
+        nz = nzmin - HU + OUT * ch + l;
+        lvl = q < P && nz >= nzmin && nz <= nzmax - 1;
+        out = lvl && l >= HU && l < W - HD;
+    }
     static __device__ __forceinline__ int count(int nzmin, int nzmax) { return (nzmax - nzmin + OUT - 1) / OUT; }
+    // segments of the last chunk: its width, and how many fit a warp (1: not packed)
+    static __device__ __forceinline__ int last_width(int nzmin, int nzmax) {
+        const int nl = nzmax - nzmin;
+        return nl - OUT * (count(nzmin, nzmax) - 1) + HU + HD;
+    }
 };
+
+// the q-th set bit of m, -1 when m has fewer than q + 1 set bits
+__device__ __forceinline__ int nth_bit(unsigned long long m, int q) {
+    for (int j = 0; j < q && m; j++) m &= m - 1;
+    return m ? __ffsll((long long)m) - 1 : -1;
+}
 
 __device__ __forceinline__ float sh_up(float v, int d) { return __shfl_up_sync(kFull, v, d); }
 __device__ __forceinline__ float sh_dn(float v, int d) { return __shfl_down_sync(kFull, v, d); }
@@ -603,81 +625,112 @@ __global__ void __launch_bounds__(256) k32_ho_nodemean(DTopo tp, B32View B, Musc
 // ---------------------------------------------------------------------------
 // k32_bounds: FCT bounds and R+ / R- (FCT tracers only)
 // ---------------------------------------------------------------------------
-template <int KD>
-__device__ __forceinline__ void bounds_node(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int n,
-                                            int lane, const WEdges &S) {
+// One chunk of a node's column for the FCT tracers of the launch.  PACK: the column's last
+// chunk with P tracers side by side in segments of W lanes (its few levels would leave most
+// lanes idle); otherwise one tracer at a time over the whole warp.
+template <int KD, bool PACK>
+__device__ __forceinline__ void bounds_chunk(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int n,
+                                             int lane, const WEdges &S, int ch, int W, int P) {
     using C = Chunk<1, 1>;
     const int L1 = tp.L1, nl = tp.nl;
     const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
     const unsigned own = S.own;
     const float eps = (float)kFluxEps;
-    const int nch = C::count(nzmin, nzmax);
-    for (int ch = 0; ch < nch; ch++) {
-        const C k(nzmin, nzmax, ch, lane);
-        const int nz = k.nz;
-        const int i = n * L1 + nz - 1, iv = n * nl + nz - 1;
-        int off[KD];
-        unsigned okm = 0;
+    const C k = PACK ? C(nzmin, nzmax, ch, lane, W, P) : C(nzmin, nzmax, ch, lane);
+    const int nz = k.nz;
+    const int i = n * L1 + nz - 1, iv = n * nl + nz - 1;
+    int off[KD];
+    unsigned okm = 0;
+#pragma unroll
+    for (int u = 0; u < KD; u++) {
+        const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
+        off[u] = S.m[u] * L1 + nz - 1;
+        okm |= ok ? 1u << u : 0u;
+    }
+    const float s = k.lvl ? dt / (g.areasvol[iv] * g.hnode_new[i]) : 0.f;
+    unsigned long long todo = B.fct_mask & (B.ntr >= 64 ? ~0ull : ((1ull << B.ntr) - 1));
+    while (todo) {
+        // the lane's tracer: the next FCT tracer, or (packed) the q-th next one
+        int t;
+        if (PACK) {
+            t = nth_bit(todo, k.q);
+            for (int j = 0; j < P && todo; j++) todo &= todo - 1;
+        } else {
+            t = __ffsll((long long)todo) - 1;
+            todo &= todo - 1;
+        }
+        const bool lv = k.lvl && t >= 0;
+        const unsigned okt = lv ? okm : 0u;
+        const size_t to = (size_t)(t < 0 ? 0 : t) * B.sN;
+        const float *__restrict__ T = B.T + to;
+        const float *__restrict__ LO = B.LO + to;
+        const float *__restrict__ ADh = B.ADh + (size_t)(t < 0 ? 0 : t) * B.sE;
+        // every load of the tracer's chunk first
+        const float Tn = lv ? T[i] : 0.f;
+        const float lo = lv ? LO[i] : 0.f;
+        const float v0 = lv ? B.ADv[(size_t)(t < 0 ? 0 : t) * B.sNI + iv] : 0.f;
+        float tm[KD], lm[KD], x[KD];
 #pragma unroll
         for (int u = 0; u < KD; u++) {
-            const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
-            off[u] = S.m[u] * L1 + nz - 1;
-            okm |= ok ? 1u << u : 0u;
+            const bool ok = (okt >> u) & 1u;
+            tm[u] = ok ? T[off[u]] : 0.f;
+            lm[u] = ok ? LO[off[u]] : 0.f;
+            // packed chunks: the edge fluxes after the bounds (fewer values live at once)
+            if (!PACK) x[u] = ok ? ADh[S.e[u] * L1 + nz - 1] : 0.f;
         }
-        const float s = k.lvl ? dt / (g.areasvol[iv] * g.hnode_new[i]) : 0.f;
-#pragma unroll 1
-        for (int t = 0; t < B.ntr; t++) {
-            if (!((B.fct_mask >> t) & 1ull)) continue;
-            const size_t to = (size_t)t * B.sN;
-            const float *__restrict__ T = B.T + to;
-            const float *__restrict__ LO = B.LO + to;
-            const float *__restrict__ ADh = B.ADh + (size_t)t * B.sE;
-            // every load of the tracer's chunk first
-            const float Tn = k.lvl ? T[i] : 0.f;
-            const float lo = k.lvl ? LO[i] : 0.f;
-            const float v0 = k.lvl ? B.ADv[(size_t)t * B.sNI + iv] : 0.f;
-            float tm[KD], lm[KD], x[KD];
+        // bounds over the node, its neighbours and the layers above and below
+        // (oce_adv_tra_fct.F90:124-248)
+        float mx = fmaxf(lo, Tn), mn = fminf(lo, Tn);
+        float Pp = 0.f, M = 0.f;
 #pragma unroll
-            for (int u = 0; u < KD; u++) {
-                const bool ok = (okm >> u) & 1u;
-                tm[u] = ok ? T[off[u]] : 0.f;
-                lm[u] = ok ? LO[off[u]] : 0.f;
-                x[u] = ok ? ADh[S.e[u] * L1 + nz - 1] : 0.f;
-            }
-            // bounds over the node, its neighbours and the layers above and below
-            // (oce_adv_tra_fct.F90:124-248)
-            float mx = fmaxf(lo, Tn), mn = fminf(lo, Tn);
-            float P = 0.f, M = 0.f;
+        for (int u = 0; u < KD; u++) {
+            const bool ok = (okt >> u) & 1u;
+            const float a = ok ? tm[u] : Tn, b = ok ? lm[u] : lo;
+            mx = fmaxf(mx, fmaxf(a, b));
+            mn = fminf(mn, fminf(a, b));
+        }
+        if (PACK) {
 #pragma unroll
-            for (int u = 0; u < KD; u++) {
-                const bool ok = (okm >> u) & 1u;
-                const float a = ok ? tm[u] : Tn, b = ok ? lm[u] : lo;
-                mx = fmaxf(mx, fmaxf(a, b));
-                mn = fminf(mn, fminf(a, b));
-                const float xv = ((own >> u) & 1u) ? x[u] : -x[u];
-                P += fmaxf(0.f, xv);
-                M += fminf(0.f, xv);
-            }
-            const float mxu = sh_up(mx, 1), mxd = sh_dn(mx, 1), mnu = sh_up(mn, 1), mnd = sh_dn(mn, 1);
-            float tup = mx, tlo = mn;
-            if (nz != nzmin && nz != nzmax - 1) {
-                tup = fmaxf(fmaxf(mxu, mx), mxd);
-                tlo = fminf(fminf(mnu, mn), mnd);
-            }
-            // P / M: sums of the positive / negative antidiffusive fluxes into the node
-            float v1 = sh_dn(v0, 1);
-            if (nz == nzmax - 1) v1 = 0.f;
-            P += fmaxf(0.f, v0) + fmaxf(0.f, -v1);
-            M += fminf(0.f, v0) + fminf(0.f, -v1);
-            if (k.out) {
-                const float bmx = tup - lo, bmn = tlo - lo;
-                B.R[to + i] = make_float2(fminf(1.f, bmx / (P * s + eps)), fminf(1.f, bmn / (M * s - eps)));
-                // the bounds themselves: the update clamps the advected value into them, so
-                // FP32 rounding in the limiter can never create a new extremum
-                B.TB[to + i] = make_float2(tup, tlo);
-            }
+            for (int u = 0; u < KD; u++) x[u] = ((okt >> u) & 1u) ? ADh[S.e[u] * L1 + nz - 1] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < KD; u++) {
+            const float xv = ((own >> u) & 1u) ? x[u] : -x[u];
+            Pp += fmaxf(0.f, xv);
+            M += fminf(0.f, xv);
+        }
+        const float mxu = sh_up(mx, 1), mxd = sh_dn(mx, 1), mnu = sh_up(mn, 1), mnd = sh_dn(mn, 1);
+        float tup = mx, tlo = mn;
+        if (nz != nzmin && nz != nzmax - 1) {
+            tup = fmaxf(fmaxf(mxu, mx), mxd);
+            tlo = fminf(fminf(mnu, mn), mnd);
+        }
+        // P / M: sums of the positive / negative antidiffusive fluxes into the node
+        float v1 = sh_dn(v0, 1);
+        if (nz == nzmax - 1) v1 = 0.f;
+        Pp += fmaxf(0.f, v0) + fmaxf(0.f, -v1);
+        M += fminf(0.f, v0) + fminf(0.f, -v1);
+        if (k.out && t >= 0) {
+            const float bmx = tup - lo, bmn = tlo - lo;
+            B.R[to + i] = make_float2(fminf(1.f, bmx / (Pp * s + eps)), fminf(1.f, bmn / (M * s - eps)));
+            // the bounds themselves: the update clamps the advected value into them, so
+            // FP32 rounding in the limiter can never create a new extremum
+            B.TB[to + i] = make_float2(tup, tlo);
         }
     }
+}
+
+template <int KD>
+__device__ __forceinline__ void bounds_node(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int n,
+                                            int lane, const WEdges &S) {
+    using C = Chunk<1, 1>;
+    const int nch = C::count(S.nzmin, S.nzmax);
+    for (int ch = 0; ch < nch - 1; ch++) bounds_chunk<KD, false>(tp, g, B, dt, n, lane, S, ch, 32, 1);
+    const int W = C::last_width(S.nzmin, S.nzmax), P = 32 / W;
+    // packed only for nodes of at most 6 edges (nearly all of an ocean mesh's): the wider
+    // packed body would spill registers
+    if (KD <= 6 && P > 1) bounds_chunk<KD, true>(tp, g, B, dt, n, lane, S, nch - 1, W, P);
+    else bounds_chunk<KD, false>(tp, g, B, dt, n, lane, S, nch - 1, 32, 1);
 }
 
 template <bool WIDE>
@@ -726,6 +779,87 @@ __device__ __forceinline__ void scan_down(float &A, float &B, int lane) {
     }
 }
 
+template <int KD, bool PACK>
+__device__ __forceinline__ void update_chunk(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt,
+                                             int n, int lane, const WEdges &S, int ch, int W, int P) {
+    using C = Chunk<1, 1>;
+    const int L1 = tp.L1, nl = tp.nl;
+    const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
+    const unsigned own = S.own;
+    const C k = PACK ? C(nzmin, nzmax, ch, lane, W, P) : C(nzmin, nzmax, ch, lane);
+    const int nz = k.nz;
+    const int i = n * L1 + nz - 1, iv = n * nl + nz - 1;
+    const float sdt = k.lvl ? dt / (g.areasvol[iv] * g.hnode_new[i]) : 0.f;
+    unsigned okm = 0;
+#pragma unroll
+    for (int u = 0; u < KD; u++) {
+        const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
+        okm |= ok ? 1u << u : 0u;
+    }
+#pragma unroll 1
+    for (int t0 = 0; t0 < B.ntr; t0 += PACK ? P : 1) {
+        // the lane's tracer (packed: the tracer of its segment)
+        const int t = t0 + k.q;
+        const bool on = t < B.ntr;
+        const int tc = on ? t : t0;
+        const bool fct = (B.fct_mask >> tc) & 1ull;
+        const size_t to = (size_t)tc * B.sN;
+        const float *__restrict__ ADh = B.ADh + (size_t)tc * B.sE;
+        const float2 *__restrict__ R = B.R + to;
+        const bool lv = k.lvl && on;
+        const bool lf = lv && fct;
+        const unsigned okt = lv ? okm : 0u;
+        // every load of the tracer's chunk first
+        const float lo = lv ? B.LO[to + i] : 0.f;
+        float f0 = lv ? B.ADv[(size_t)tc * B.sNI + iv] : 0.f;
+        const float2 r0 = lf ? R[i] : make_float2(1.f, 1.f);
+        const float2 tb = lf ? B.TB[to + i] : make_float2(0.f, 0.f);
+        float x[KD];
+        float2 rm[KD];
+#pragma unroll
+        for (int u = 0; u < KD; u++) {
+            const bool ok = (okt >> u) & 1u;
+            x[u] = ok ? ADh[S.e[u] * L1 + nz - 1] : 0.f;
+            rm[u] = (ok && fct) ? R[S.m[u] * L1 + nz - 1] : make_float2(1.f, 1.f);
+        }
+        // vertical limiting (oce_adv_tra_fct.F90:425-456): interface nz by R of layers
+        // nz-1 and nz; the next interface is the lane below's
+        const float rux = sh_up(r0.x, 1), ruy = sh_up(r0.y, 1);
+        if (fct) {
+            if (nz == nzmin) f0 *= f0 >= 0.f ? r0.x : r0.y;
+            else f0 *= f0 >= 0.f ? fminf(ruy, r0.x) : fminf(rux, r0.y);
+        }
+        float f1 = sh_dn(f0, 1);
+        if (nz == nzmax - 1) f1 = 0.f;
+        // horizontal limiting (oce_adv_tra_fct.F90:468-500) seen from the node: with G the
+        // antidiffusive flux into the node and m the other end, G >= 0 takes
+        // min(R+(n), R-(m)), G < 0 takes min(R-(n), R+(m))
+        float hs = 0.f;
+#pragma unroll
+        for (int u = 0; u < KD; u++) {
+            float G = ((own >> u) & 1u) ? x[u] : -x[u];
+            if (fct) G *= G >= 0.f ? fminf(r0.x, rm[u].y) : fminf(r0.y, rm[u].x);
+            hs += G;
+        }
+        // del_ttf = (LO hnode_new - T hnode) + limited flux divergence dt / areasvol;
+        // T* = T + (del_ttf + T (hnode - hnode_new)) / hnode_new = LO + fluxes dt / areasvol / hnode_new
+        // (oce_adv_tra_driver.F90:535-620, oce_ale_tracer.F90:319-321, 743-754)
+        float val = lo + (f0 - f1 + hs) * sdt;
+        if (k.out && on) {
+            if (fct) {
+                const float vc = fminf(fmaxf(val, tb.y), tb.x);
+                // a clamp beyond round-off means the limiter itself failed
+                if (fabsf(vc - val) > 1e-5f * (tb.x - tb.y) + 1e-6f * fabsf(vc)) atomicOr(B.status, 2u);
+                val = vc;
+            }
+            // the diffusion increment k32_diff parked in Tnew (the limiter acts on advection only)
+            if ((B.diff_mask >> tc) & 1ull) val += B.Tnew[to + i];
+            B.Tnew[to + i] = val;
+            if (!isfinite(val)) atomicOr(B.status, 1u);
+        }
+    }
+}
+
 // Limited update of every tracer of a node: per chunk the tracer-independent part
 // (which edge slots are wet, dt / (areasvol hnode_new)) once, then per tracer every gather
 // of the chunk, the limiter and the T* value, written to the buffer of the oldest time level.
@@ -733,78 +867,12 @@ template <int KD>
 __device__ __forceinline__ void update_node(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt,
                                             int n, int lane, const WEdges &S) {
     using C = Chunk<1, 1>;
-    const int L1 = tp.L1, nl = tp.nl;
-    const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
-    const unsigned own = S.own;
-    const int nch = C::count(nzmin, nzmax);
-    for (int ch = 0; ch < nch; ch++) {
-        const C k(nzmin, nzmax, ch, lane);
-        const int nz = k.nz;
-        const int i = n * L1 + nz - 1, iv = n * nl + nz - 1;
-        const float sdt = k.lvl ? dt / (g.areasvol[iv] * g.hnode_new[i]) : 0.f;
-        unsigned okm = 0;
-#pragma unroll
-        for (int u = 0; u < KD; u++) {
-            const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
-            okm |= ok ? 1u << u : 0u;
-        }
-#pragma unroll 1
-        for (int t = 0; t < B.ntr; t++) {
-            const bool fct = (B.fct_mask >> t) & 1ull;
-            const size_t to = (size_t)t * B.sN;
-            const float *__restrict__ ADh = B.ADh + (size_t)t * B.sE;
-            const float2 *__restrict__ R = B.R + to;
-            const bool lf = k.lvl && fct;
-            // every load of the tracer's chunk first
-            const float lo = k.lvl ? B.LO[to + i] : 0.f;
-            float f0 = k.lvl ? B.ADv[(size_t)t * B.sNI + iv] : 0.f;
-            const float2 r0 = lf ? R[i] : make_float2(1.f, 1.f);
-            const float2 tb = lf ? B.TB[to + i] : make_float2(0.f, 0.f);
-            float x[KD];
-            float2 rm[KD];
-#pragma unroll
-            for (int u = 0; u < KD; u++) {
-                const bool ok = (okm >> u) & 1u;
-                x[u] = ok ? ADh[S.e[u] * L1 + nz - 1] : 0.f;
-                rm[u] = (ok && fct) ? R[S.m[u] * L1 + nz - 1] : make_float2(1.f, 1.f);
-            }
-            // vertical limiting (oce_adv_tra_fct.F90:425-456): interface nz by R of layers
-            // nz-1 and nz; the next interface is the lane below's
-            const float rux = sh_up(r0.x, 1), ruy = sh_up(r0.y, 1);
-            if (fct) {
-                if (nz == nzmin) f0 *= f0 >= 0.f ? r0.x : r0.y;
-                else f0 *= f0 >= 0.f ? fminf(ruy, r0.x) : fminf(rux, r0.y);
-            }
-            float f1 = sh_dn(f0, 1);
-            if (nz == nzmax - 1) f1 = 0.f;
-            // horizontal limiting (oce_adv_tra_fct.F90:468-500) seen from the node: with G the
-            // antidiffusive flux into the node and m the other end, G >= 0 takes
-            // min(R+(n), R-(m)), G < 0 takes min(R-(n), R+(m))
-            float hs = 0.f;
-#pragma unroll
-            for (int u = 0; u < KD; u++) {
-                float G = ((own >> u) & 1u) ? x[u] : -x[u];
-                if (fct) G *= G >= 0.f ? fminf(r0.x, rm[u].y) : fminf(r0.y, rm[u].x);
-                hs += G;
-            }
-            // del_ttf = (LO hnode_new - T hnode) + limited flux divergence dt / areasvol;
-            // T* = T + (del_ttf + T (hnode - hnode_new)) / hnode_new = LO + fluxes dt / areasvol / hnode_new
-            // (oce_adv_tra_driver.F90:535-620, oce_ale_tracer.F90:319-321, 743-754)
-            float val = lo + (f0 - f1 + hs) * sdt;
-            if (k.out) {
-                if (fct) {
-                    const float vc = fminf(fmaxf(val, tb.y), tb.x);
-                    // a clamp beyond round-off means the limiter itself failed
-                    if (fabsf(vc - val) > 1e-5f * (tb.x - tb.y) + 1e-6f * fabsf(vc)) atomicOr(B.status, 2u);
-                    val = vc;
-                }
-                // the diffusion increment k32_diff parked in Tnew (the limiter acts on advection only)
-                if ((B.diff_mask >> t) & 1ull) val += B.Tnew[to + i];
-                B.Tnew[to + i] = val;
-                if (!isfinite(val)) atomicOr(B.status, 1u);
-            }
-        }
-    }
+    const int nch = C::count(S.nzmin, S.nzmax);
+    for (int ch = 0; ch < nch - 1; ch++) update_chunk<KD, false>(tp, g, B, dt, n, lane, S, ch, 32, 1);
+    const int W = C::last_width(S.nzmin, S.nzmax), P = 32 / W;
+    // packed only for nodes of at most 6 edges, as in k32_bounds
+    if (KD <= 6 && P > 1) update_chunk<KD, true>(tp, g, B, dt, n, lane, S, nch - 1, W, P);
+    else update_chunk<KD, false>(tp, g, B, dt, n, lane, S, nch - 1, 32, 1);
 }
 
 template <bool WIDE>
