@@ -65,6 +65,10 @@ constexpr int kMaxChunks = 5;         // columns of up to 128 layers, 30 levels 
 #ifndef FESOM_MINB_UPDATE
 #define FESOM_MINB_UPDATE 4
 #endif
+// tracers side by side in the last level chunk of a column in the multi-instance kernels too
+#ifndef FESOM_PACK_MULTI
+#define FESOM_PACK_MULTI true
+#endif
 
 __device__ __forceinline__ size_t i1(int nz, int n, int L1) { return (size_t)n * L1 + (nz - 1); }
 
@@ -295,12 +299,6 @@ struct Chunk {
     }
 };
 
-// the q-th set bit of m, -1 when m has fewer than q + 1 set bits
-__device__ __forceinline__ int nth_bit(unsigned long long m, int q) {
-    for (int j = 0; j < q && m; j++) m &= m - 1;
-    return m ? __ffsll((long long)m) - 1 : -1;
-}
-
 __device__ __forceinline__ float sh_up(float v, int d) { return __shfl_up_sync(kFull, v, d); }
 __device__ __forceinline__ float sh_dn(float v, int d) { return __shfl_down_sync(kFull, v, d); }
 
@@ -315,17 +313,19 @@ __device__ __forceinline__ float ab_delta(int ab, float t, float o1, float o2) {
 // ---------------------------------------------------------------------------
 // k32_lo_ad
 // ---------------------------------------------------------------------------
-template <int KD, bool WS>
-__device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
-                                           const B32View &B, const float *__restrict__ VF, float dt, int n, int lane,
-                                           const WEdges &S) {
+// One chunk of a node's column for every tracer of the launch.  PACK: the column's last
+// chunk with P tracers side by side in segments of W lanes; otherwise one tracer at a time
+// over the whole warp.
+template <int KD, bool WS, bool PACK>
+__device__ __forceinline__ void lo_ad_chunk(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
+                                            const B32View &B, const float *__restrict__ VF, float dt, int n, int lane,
+                                            const WEdges &S, int ch, int W, int P) {
     using C = Chunk<2, 1>;
     const int L1 = tp.L1, nl = tp.nl;
     const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
     const unsigned own = S.own;
-    const int nch = C::count(nzmin, nzmax);
-    for (int ch = 0; ch < nch; ch++) {
-        const C k(nzmin, nzmax, ch, lane);
+    {
+        const C k = PACK ? C(nzmin, nzmax, ch, lane, W, P) : C(nzmin, nzmax, ch, lane);
         const int nz = k.nz;
         const int i = n * L1 + nz - 1;   // layer nz of the node (valid where k.lvl)
         const int iv = n * nl + nz - 1;  // interface nz
@@ -369,7 +369,13 @@ __device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &
         const bool twolayer = nzmin + 1 == nzmax - 1;
         // ---- per tracer ----
 #pragma unroll 1
-        for (int t = 0; t < B.ntr; t++) {
+        for (int t0 = 0; t0 < B.ntr; t0 += PACK ? P : 1) {
+            // the lane's tracer (packed: the tracer of its segment; idle past the last)
+            const int tt = t0 + k.q;
+            const bool on = tt < B.ntr;
+            const int t = on ? tt : t0;
+            const bool lvt = k.lvl && on;
+            const unsigned okt = lvt ? okm : 0u;
             const bool lim = (B.fct_mask >> t) & 1ull;
             const int ver = B.ver[t];
             const size_t to = (size_t)t * B.sN;
@@ -377,23 +383,23 @@ __device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &
             const float *__restrict__ O1 = B.O1 + to;
             const float *__restrict__ O2 = B.ab == 3 ? B.O2 + to : O1;
             // every load of the tracer's chunk first
-            const float Tn = k.lvl ? T[i] : 0.f;
-            const float o1 = k.lvl ? O1[i] : 0.f;
-            const float o2 = (k.lvl && B.ab == 3) ? O2[i] : 0.f;
+            const float Tn = lvt ? T[i] : 0.f;
+            const float o1 = lvt ? O1[i] : 0.f;
+            const float o2 = (lvt && B.ab == 3) ? O2[i] : 0.f;
             float tm[KD];
 #pragma unroll
-            for (int u = 0; u < KD; u++) tm[u] = ((okm >> u) & 1u) ? T[off[u]] : 0.f;
-            const float tab = Tn + (k.lvl ? ab_delta(B.ab, Tn, o1, o2) : 0.f);
+            for (int u = 0; u < KD; u++) tm[u] = ((okt >> u) & 1u) ? T[off[u]] : 0.f;
+            const float tab = Tn + (lvt ? ab_delta(B.ab, Tn, o1, o2) : 0.f);
             const float Tu = sh_up(Tn, 1);
             const float tabu = sh_up(tab, 1), tabu2 = sh_up(tab, 2), tabd = sh_dn(tab, 1);
             // LO: upwind edge fluxes in difference form, sum_j am_j (T_j - T_n) + Dh T_n
             float hs = Dh * Tn;
 #pragma unroll
             for (int u = 0; u < KD; u++)
-                if ((okm >> u) & 1u) hs += am[u] * (tm[u] - Tn);
+                if ((okt >> u) & 1u) hs += am[u] * (tm[u] - Tn);
             // upwind vertical flux with w_e at interface nz (adv_tra_ver_upw1)
             float fv0 = 0.f;
-            if (k.lvl) {
+            if (lvt) {
                 if (nz == nzmin) {
                     fv0 = -(we0 * Tn * ar0);
                 } else {
@@ -404,11 +410,11 @@ __device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &
             float fv1 = sh_dn(fv0, 1);
             if (nz == nzmax - 1) fv1 = 0.f;
             // LO = (T hnode + flux divergence dt / areasvol) / hnode_new (oce_adv_tra_driver.F90:249)
-            if (k.out) B.LO[to + i] = Tn * hr + (hs + fv0 - fv1) * sdt;
+            if (k.out && on) B.LO[to + i] = Tn * hr + (hs + fv0 - fv1) * sdt;
             // with the split vertical velocity the LO part of the antidiffusive flux is the upwind
             // flux of the full w (oce_adv_tra_driver.F90:323-334)
             float fw0 = fv0;
-            if (WS && f.wsplit && k.lvl) {
+            if (WS && f.wsplit && lvt) {
                 if (nz == nzmin) {
                     fw0 = -(w0 * Tn * ar0);
                 } else {
@@ -418,7 +424,7 @@ __device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &
             }
             // vertical high-order flux on the AB values (QR4C / UPW1 / CDIFF; PPM in k32_vppm),
             // minus the LO flux
-            if (k.out && ver != 3) {
+            if (k.out && on && ver != 3) {
                 const float pw = lim ? w0 : we0;
                 float Cf;
                 if (nz == nzmin) {
@@ -451,6 +457,19 @@ __device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &
     }
 }
 
+template <int KD, bool WS, bool PK>
+__device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
+                                           const B32View &B, const float *__restrict__ VF, float dt, int n, int lane,
+                                           const WEdges &S) {
+    using C = Chunk<2, 1>;
+    const int nch = C::count(S.nzmin, S.nzmax);
+    for (int ch = 0; ch < nch - 1; ch++) lo_ad_chunk<KD, WS, false>(tp, g, f, B, VF, dt, n, lane, S, ch, 32, 1);
+    const int W = C::last_width(S.nzmin, S.nzmax), P = 32 / W;
+    // packed only for nodes of at most 6 edges, as in k32_bounds
+    if (PK && KD <= 6 && P > 1) lo_ad_chunk<KD, WS, true>(tp, g, f, B, VF, dt, n, lane, S, nch - 1, W, P);
+    else lo_ad_chunk<KD, WS, false>(tp, g, f, B, VF, dt, n, lane, S, nch - 1, 32, 1);
+}
+
 // the node of warp unit j: consecutive nodes, or (WIDE) the listed nodes of more than 8 edges
 template <bool WIDE>
 __device__ __forceinline__ int unit_node(const DTopo &tp, int j) {
@@ -459,7 +478,7 @@ __device__ __forceinline__ int unit_node(const DTopo &tp, int j) {
 }
 
 // WS: the split vertical velocity (a separate instantiation keeps the default path unchanged)
-template <bool WIDE, bool WS>
+template <bool WIDE, bool WS, bool PK>
 __device__ __forceinline__ void lo_ad_unit(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
                                            const B32View &B, const float *__restrict__ VF, float dt, int j, WEdges *Se) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -468,16 +487,16 @@ __device__ __forceinline__ void lo_ad_unit(const DTopo &tp, const DGeom<float> &
     WEdges &S = Se[warp];
     stage_edges(tp, n, lane, S);
     if ((S.deg > 8) != WIDE) return;
-    if (WIDE) lo_ad_node<kMaxDeg, WS>(tp, g, f, B, VF, dt, n, lane, S);
-    else if (S.deg <= 6) lo_ad_node<6, WS>(tp, g, f, B, VF, dt, n, lane, S);
-    else lo_ad_node<8, WS>(tp, g, f, B, VF, dt, n, lane, S);
+    if (WIDE) lo_ad_node<kMaxDeg, WS, PK>(tp, g, f, B, VF, dt, n, lane, S);
+    else if (S.deg <= 6) lo_ad_node<6, WS, PK>(tp, g, f, B, VF, dt, n, lane, S);
+    else lo_ad_node<8, WS, PK>(tp, g, f, B, VF, dt, n, lane, S);
 }
 
 template <bool WIDE, bool WS>
 __global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_LO)
 k32_lo_ad(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, const float *__restrict__ VF, float dt) {
     __shared__ WEdges Se[kWB];
-    lo_ad_unit<WIDE, WS>(tp, g, f, B, VF, dt, blockIdx.x * kWB + (threadIdx.x >> 5), Se);
+    lo_ad_unit<WIDE, WS, true>(tp, g, f, B, VF, dt, blockIdx.x * kWB + (threadIdx.x >> 5), Se);
 }
 
 // high-order minus low-order flux of one edge-layer from the two end values, their
@@ -517,69 +536,88 @@ __device__ __forceinline__ float ho_minus_lo(int hor, float ph, int ab, float T1
 // at the levels where every element around both nodes is wet, [gzmin, gzmax); the
 // other edge-layers (under one percent of an ocean mesh's) take the node means in
 // k32_ho_nodemean.
-__device__ __forceinline__ void ho_unit(const DTopo &tp, const B32View &B, const MusclW &mw,
-                                        const float *__restrict__ VF, int e) {
-    const int lane = threadIdx.x & 31;
-    if (e >= tp.E2) return;
+//
+// A pass covers 32 levels of the edge; the last pass, when its levels fill at most half a
+// warp, carries P tracers side by side in segments of W lanes (PACK).
+template <bool PACK>
+__device__ __forceinline__ void ho_pass(const DTopo &tp, const B32View &B, const MusclW &mw,
+                                        const float *__restrict__ VF, int e, int nz0, int W, int P, int lane) {
     const int L1 = tp.L1;
     const int n1 = tp.e_n1[e], n2 = tp.e_n2[e];
-    const int elo = tp.e_lo[e], ehi = tp.e_hi[e];
+    const int ehi = tp.e_hi[e];
     const int nbl1 = tp.n_nbl[n1], nbl2 = tp.n_nbl[n2];
     const int4 un = mw.un[e], dn = mw.dn[e];
     const float4 wu = mw.wu[e], wd = mw.wd[e];
     const int gzmin = un.w & 0xffff, gzmax = un.w >> 16;
-    for (int nz0 = elo; nz0 <= ehi; nz0 += 32) {
-        const int nz = nz0 + lane;
-        const bool tri = nz >= gzmin && nz <= gzmax - 1;
-        const bool ok = nz <= ehi;
-        const int ie = e * L1 + nz - 1, ia = n1 * L1 + nz - 1, ib = n2 * L1 + nz - 1;
-        const float v = ok ? VF[ie] : 0.f;
-        const float cl1 = (nbl1 - nz) >= 0 ? 1.f : 0.f, cl2 = (nbl2 - nz) >= 0 ? 1.f : 0.f;
-        const int ua = un.y * L1 + nz - 1, ub = un.z * L1 + nz - 1;
-        const int da = dn.y * L1 + nz - 1, db = dn.z * L1 + nz - 1;
-        if (!ok) continue;
-        // two tracers per pass: their gathers in flight together
+    const int q = PACK ? lane / W : 0;
+    const int nz = nz0 + lane - q * W;
+    const bool tri = nz >= gzmin && nz <= gzmax - 1;
+    const bool ok = nz <= ehi && q < P;
+    const int ie = e * L1 + nz - 1, ia = n1 * L1 + nz - 1, ib = n2 * L1 + nz - 1;
+    const float v = ok ? VF[ie] : 0.f;
+    const float cl1 = (nbl1 - nz) >= 0 ? 1.f : 0.f, cl2 = (nbl2 - nz) >= 0 ? 1.f : 0.f;
+    const int ua = un.y * L1 + nz - 1, ub = un.z * L1 + nz - 1;
+    const int da = dn.y * L1 + nz - 1, db = dn.z * L1 + nz - 1;
+    if (!ok) return;
+    // two tracers per pass: their gathers in flight together (packed: tracers t0 + q and
+    // t0 + P + q of the segment)
+    const int step = PACK ? P : 1;
 #pragma unroll 1
-        for (int t = 0; t < B.ntr; t += 2) {
-            const bool two = t + 1 < B.ntr;
-            float T1[2], T2[2], o1a[2], o1b[2], o2a[2], o2b[2], ga[2], gb[2], gc[2], gd[2];
-            bool grad[2];
+    for (int t0 = 0; t0 < B.ntr; t0 += 2 * step) {
+        float T1[2], T2[2], o1a[2], o1b[2], o2a[2], o2b[2], ga[2], gb[2], gc[2], gd[2];
+        bool grad[2], on[2];
+        int tt[2];
 #pragma unroll
-            for (int q = 0; q < 2; q++) {
-                const bool on = q == 0 || two;
-                const int tq = on ? t + q : t;
-                const size_t to = (size_t)tq * B.sN;
-                const float *__restrict__ T = B.T + to;
-                grad[q] = on && B.hor[tq] != 2 && tri;
-                T1[q] = on ? T[ia] : 0.f;
-                T2[q] = on ? T[ib] : 0.f;
-                o1a[q] = on ? B.O1[to + ia] : 0.f;
-                o1b[q] = on ? B.O1[to + ib] : 0.f;
-                o2a[q] = (on && B.ab == 3) ? B.O2[to + ia] : 0.f;
-                o2b[q] = (on && B.ab == 3) ? B.O2[to + ib] : 0.f;
-                ga[q] = grad[q] ? T[ua] : 0.f;
-                gb[q] = grad[q] ? T[ub] : 0.f;
-                gc[q] = grad[q] ? T[da] : 0.f;
-                gd[q] = grad[q] ? T[db] : 0.f;
-            }
+        for (int r = 0; r < 2; r++) {
+            const int tq = t0 + r * step + q;
+            on[r] = tq < B.ntr;
+            tt[r] = on[r] ? tq : t0;
+            const size_t to = (size_t)tt[r] * B.sN;
+            const float *__restrict__ T = B.T + to;
+            grad[r] = on[r] && B.hor[tt[r]] != 2 && tri;
+            T1[r] = on[r] ? T[ia] : 0.f;
+            T2[r] = on[r] ? T[ib] : 0.f;
+            o1a[r] = on[r] ? B.O1[to + ia] : 0.f;
+            o1b[r] = on[r] ? B.O1[to + ib] : 0.f;
+            o2a[r] = (on[r] && B.ab == 3) ? B.O2[to + ia] : 0.f;
+            o2b[r] = (on[r] && B.ab == 3) ? B.O2[to + ib] : 0.f;
+            ga[r] = grad[r] ? T[ua] : 0.f;
+            gb[r] = grad[r] ? T[ub] : 0.f;
+            gc[r] = grad[r] ? T[da] : 0.f;
+            gd[r] = grad[r] ? T[db] : 0.f;
+        }
 #pragma unroll
-            for (int q = 0; q < 2; q++) {
-                if (q == 1 && !two) continue;
-                const int hor = B.hor[t + q];
-                // MUSCL / MFCT levels outside the triangles' range: the fallback launch
-                if (hor != 2 && !tri) continue;
-                const float s1 = wu.y * (ga[q] - T1[q]) + wu.z * (gb[q] - T1[q]);
-                const float s2 = wd.y * (gc[q] - T2[q]) + wd.z * (gd[q] - T2[q]);
-                B.ADh[(size_t)(t + q) * B.sE + ie] = ho_minus_lo(hor, B.ph[t + q], B.ab, T1[q], T2[q], o1a[q], o1b[q],
-                                                                 o2a[q], o2b[q], s1, s2, v, cl1, cl2);
-            }
+        for (int r = 0; r < 2; r++) {
+            if (!on[r]) continue;
+            const int hor = B.hor[tt[r]];
+            // MUSCL / MFCT levels outside the triangles' range: the fallback launch
+            if (hor != 2 && !tri) continue;
+            const float s1 = wu.y * (ga[r] - T1[r]) + wu.z * (gb[r] - T1[r]);
+            const float s2 = wd.y * (gc[r] - T2[r]) + wd.z * (gd[r] - T2[r]);
+            B.ADh[(size_t)tt[r] * B.sE + ie] = ho_minus_lo(hor, B.ph[tt[r]], B.ab, T1[r], T2[r], o1a[r], o1b[r],
+                                                           o2a[r], o2b[r], s1, s2, v, cl1, cl2);
         }
     }
 }
 
+template <bool PK>
+__device__ __forceinline__ void ho_unit(const DTopo &tp, const B32View &B, const MusclW &mw,
+                                        const float *__restrict__ VF, int e) {
+    const int lane = threadIdx.x & 31;
+    if (e >= tp.E2) return;
+    const int elo = tp.e_lo[e], ehi = tp.e_hi[e];
+    int nz0 = elo;
+    for (; nz0 + 32 <= ehi; nz0 += 32) ho_pass<false>(tp, B, mw, VF, e, nz0, 32, 1, lane);
+    const int W = ehi - nz0 + 1;
+    if (W < 1) return;
+    const int P = 32 / W;
+    if (PK && P > 1) ho_pass<true>(tp, B, mw, VF, e, nz0, W, P, lane);
+    else ho_pass<false>(tp, B, mw, VF, e, nz0, 32, 1, lane);
+}
+
 __global__ void __launch_bounds__(kTB, FESOM_MINB_HO)
 k32_ho(DTopo tp, B32View B, MusclW mw, const float *__restrict__ VF) {
-    ho_unit(tp, B, mw, VF, blockIdx.x * kWB + (threadIdx.x >> 5));
+    ho_unit<true>(tp, B, mw, VF, blockIdx.x * kWB + (threadIdx.x >> 5));
 }
 
 // The edge-layers of the node-mean gradients: one thread per (edge, level) item, every
@@ -649,12 +687,15 @@ __device__ __forceinline__ void bounds_chunk(const DTopo &tp, const DGeom<float>
     }
     const float s = k.lvl ? dt / (g.areasvol[iv] * g.hnode_new[i]) : 0.f;
     unsigned long long todo = B.fct_mask & (B.ntr >= 64 ? ~0ull : ((1ull << B.ntr) - 1));
-    while (todo) {
-        // the lane's tracer: the next FCT tracer, or (packed) the q-th next one
+    int t0 = 0;
+    while (PACK ? t0 < B.ntr : todo != 0ull) {
+        // the lane's tracer: the next FCT tracer, or (packed) tracer t0 + q of the segment,
+        // idle where that tracer has no FCT
         int t;
         if (PACK) {
-            t = nth_bit(todo, k.q);
-            for (int j = 0; j < P && todo; j++) todo &= todo - 1;
+            t = t0 + k.q;
+            if (t >= B.ntr || !((B.fct_mask >> t) & 1ull)) t = -1;
+            t0 += P;
         } else {
             t = __ffsll((long long)todo) - 1;
             todo &= todo - 1;
@@ -720,7 +761,7 @@ __device__ __forceinline__ void bounds_chunk(const DTopo &tp, const DGeom<float>
     }
 }
 
-template <int KD>
+template <int KD, bool PK>
 __device__ __forceinline__ void bounds_node(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int n,
                                             int lane, const WEdges &S) {
     using C = Chunk<1, 1>;
@@ -729,11 +770,11 @@ __device__ __forceinline__ void bounds_node(const DTopo &tp, const DGeom<float> 
     const int W = C::last_width(S.nzmin, S.nzmax), P = 32 / W;
     // packed only for nodes of at most 6 edges (nearly all of an ocean mesh's): the wider
     // packed body would spill registers
-    if (KD <= 6 && P > 1) bounds_chunk<KD, true>(tp, g, B, dt, n, lane, S, nch - 1, W, P);
+    if (PK && KD <= 6 && P > 1) bounds_chunk<KD, true>(tp, g, B, dt, n, lane, S, nch - 1, W, P);
     else bounds_chunk<KD, false>(tp, g, B, dt, n, lane, S, nch - 1, 32, 1);
 }
 
-template <bool WIDE>
+template <bool WIDE, bool PK>
 __device__ __forceinline__ void bounds_unit(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int j,
                                             WEdges *Se) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -742,15 +783,15 @@ __device__ __forceinline__ void bounds_unit(const DTopo &tp, const DGeom<float> 
     WEdges &S = Se[warp];
     stage_edges(tp, n, lane, S);
     if ((S.deg > 8) != WIDE) return;
-    if (WIDE) bounds_node<kMaxDeg>(tp, g, B, dt, n, lane, S);
-    else if (S.deg <= 6) bounds_node<6>(tp, g, B, dt, n, lane, S);
-    else bounds_node<8>(tp, g, B, dt, n, lane, S);
+    if (WIDE) bounds_node<kMaxDeg, PK>(tp, g, B, dt, n, lane, S);
+    else if (S.deg <= 6) bounds_node<6, PK>(tp, g, B, dt, n, lane, S);
+    else bounds_node<8, PK>(tp, g, B, dt, n, lane, S);
 }
 
 template <bool WIDE>
 __global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_BOUNDS) k32_bounds(DTopo tp, DGeom<float> g, B32View B, float dt) {
     __shared__ WEdges Se[kWB];
-    bounds_unit<WIDE>(tp, g, B, dt, blockIdx.x * kWB + (threadIdx.x >> 5), Se);
+    bounds_unit<WIDE, true>(tp, g, B, dt, blockIdx.x * kWB + (threadIdx.x >> 5), Se);
 }
 
 // ---------------------------------------------------------------------------
@@ -863,7 +904,7 @@ __device__ __forceinline__ void update_chunk(const DTopo &tp, const DGeom<float>
 // Limited update of every tracer of a node: per chunk the tracer-independent part
 // (which edge slots are wet, dt / (areasvol hnode_new)) once, then per tracer every gather
 // of the chunk, the limiter and the T* value, written to the buffer of the oldest time level.
-template <int KD>
+template <int KD, bool PK>
 __device__ __forceinline__ void update_node(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt,
                                             int n, int lane, const WEdges &S) {
     using C = Chunk<1, 1>;
@@ -871,11 +912,11 @@ __device__ __forceinline__ void update_node(const DTopo &tp, const DGeom<float> 
     for (int ch = 0; ch < nch - 1; ch++) update_chunk<KD, false>(tp, g, B, dt, n, lane, S, ch, 32, 1);
     const int W = C::last_width(S.nzmin, S.nzmax), P = 32 / W;
     // packed only for nodes of at most 6 edges, as in k32_bounds
-    if (KD <= 6 && P > 1) update_chunk<KD, true>(tp, g, B, dt, n, lane, S, nch - 1, W, P);
+    if (PK && KD <= 6 && P > 1) update_chunk<KD, true>(tp, g, B, dt, n, lane, S, nch - 1, W, P);
     else update_chunk<KD, false>(tp, g, B, dt, n, lane, S, nch - 1, 32, 1);
 }
 
-template <bool WIDE>
+template <bool WIDE, bool PK>
 __device__ __forceinline__ void update_unit(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int j,
                                             WEdges *Se) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -884,16 +925,16 @@ __device__ __forceinline__ void update_unit(const DTopo &tp, const DGeom<float> 
     WEdges &S = Se[warp];
     stage_edges(tp, n, lane, S);
     if ((S.deg > 8) != WIDE) return;
-    if (WIDE) update_node<kMaxDeg>(tp, g, B, dt, n, lane, S);
-    else if (S.deg <= 6) update_node<6>(tp, g, B, dt, n, lane, S);
-    else update_node<8>(tp, g, B, dt, n, lane, S);
+    if (WIDE) update_node<kMaxDeg, PK>(tp, g, B, dt, n, lane, S);
+    else if (S.deg <= 6) update_node<6, PK>(tp, g, B, dt, n, lane, S);
+    else update_node<8, PK>(tp, g, B, dt, n, lane, S);
 }
 
 template <bool WIDE>
 __global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_UPDATE)
 k32_update(DTopo tp, DGeom<float> g, B32View B, float dt) {
     __shared__ WEdges Se[kWB];
-    update_unit<WIDE>(tp, g, B, dt, blockIdx.x * kWB + (threadIdx.x >> 5), Se);
+    update_unit<WIDE, true>(tp, g, B, dt, blockIdx.x * kWB + (threadIdx.x >> 5), Se);
 }
 
 // ---------------------------------------------------------------------------
@@ -1515,13 +1556,13 @@ __global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_LO) k32m_lo_ad(cons
     const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
     if (u >= ix.start[ix.n]) return;
     const int i = find_inst(ix, u);
-    lo_ad_unit<WIDE, WS>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].VF, I[i].dt, u - ix.start[i], Se);
+    lo_ad_unit<WIDE, WS, FESOM_PACK_MULTI>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].VF, I[i].dt, u - ix.start[i], Se);
 }
 __global__ void __launch_bounds__(kTB, FESOM_MINB_HO) k32m_ho(const Inst32 *__restrict__ I, MultiIdx ix) {
     const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
     if (u >= ix.start[ix.n]) return;
     const int i = find_inst(ix, u);
-    ho_unit(I[i].tp, I[i].B, I[i].mw, I[i].VF, u - ix.start[i]);
+    ho_unit<FESOM_PACK_MULTI>(I[i].tp, I[i].B, I[i].mw, I[i].VF, u - ix.start[i]);
 }
 __global__ void __launch_bounds__(256) k32m_ho_nodemean(const Inst32 *__restrict__ I, MultiIdx ix) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1535,7 +1576,7 @@ __global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_BOUNDS) k32m_bounds
     const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
     if (u >= ix.start[ix.n]) return;
     const int i = find_inst(ix, u);
-    bounds_unit<WIDE>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
+    bounds_unit<WIDE, FESOM_PACK_MULTI>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
 }
 template <bool WIDE>
 __global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_UPDATE) k32m_update(const Inst32 *__restrict__ I, MultiIdx ix) {
@@ -1543,7 +1584,7 @@ __global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_UPDATE) k32m_update
     const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
     if (u >= ix.start[ix.n]) return;
     const int i = find_inst(ix, u);
-    update_unit<WIDE>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
+    update_unit<WIDE, FESOM_PACK_MULTI>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
 }
 __global__ void __launch_bounds__(32 * kWV) k32m_vdiff(const Inst32 *__restrict__ I, MultiIdx ix) {
     __shared__ VdiffWarp Wsm[kWV];
