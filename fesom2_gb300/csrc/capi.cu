@@ -1103,6 +1103,24 @@ int fesom_gpu_init_tracers_ab(fesom_gpu_ctx *ctx, const fesom_tra_cfg *cfg, cons
     return wait_stream(ctx, -1);
 }
 
+int fesom_gpu_tracer_gradient_z(fesom_gpu_ctx *ctx, const double *values, double *tr_z) {
+    if (!ctx || !values || !tr_z) return FESOM_ERR_ARG;
+    int rc;
+    if ((rc = need_fp64(ctx))) return rc;
+    if (!ctx->state_ready) {  // the work arrays of one tracer
+        fesom_tra_cfg c{};
+        c.ab_order = 2;
+        if ((rc = ensure_one(ctx, &c))) return rc;
+    }
+    const size_t sN = (size_t)ctx->L1 * ctx->N2, sNI = (size_t)ctx->nl * ctx->N2;
+    // tr_z travels both ways: the interfaces outside a column keep the caller's values
+    if ((rc = put(ctx, ctx->T, values, sN)) || (rc = put(ctx, ctx->ADv, tr_z, sNI))) return rc;
+    Launch<double>::trz(ctx->tp, ctx->g64, (const double *)ctx->T, (double *)ctx->ADv, ctx->stream);
+    CK(cudaGetLastError());
+    if ((rc = get(ctx, tr_z, ctx->ADv, sNI))) return rc;
+    return wait_stream(ctx, -1);
+}
+
 int fesom_gpu_adv_tra(fesom_gpu_ctx *ctx, double dt, const double *vel, const double *w, const double *wi,
                       const double *we, const fesom_tra_cfg *cfg, const double *ttf, const double *ttfAB,
                       double *dttf_h, double *dttf_v) {

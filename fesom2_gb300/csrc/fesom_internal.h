@@ -206,6 +206,8 @@ template <typename R>
 struct Launch {
     static void ab(const DTopo &, DTracers<R> &, int ab_order, cudaStream_t);
     static void trxy(const DTopo &, const DGeom<R> &, DTracers<R> &, cudaStream_t);
+    // tracer_gradient_z of T into trz (nl per node)
+    static void trz(const DTopo &, const DGeom<R> &, const R *T, R *trz, cudaStream_t);
     static void edge_flux(const DTopo &, const DGeom<R> &, const DForcing<R> &, DTracers<R> &, int fct, cudaStream_t);
     static void node_lo(const DTopo &, const DGeom<R> &, const DForcing<R> &, DTracers<R> &, double dt, int fct,
                         cudaStream_t);

@@ -123,6 +123,28 @@ __global__ void __launch_bounds__(kThreads) k_trxy(DTopo tp, DGeom<R> g, DTracer
     }
 }
 
+// ===========================================================================
+// tracer_gradient_z (src/oce_tracer_mod.F90:192-232): warp per node, lanes over levels;
+// tr_z(nz) = (T(nz-1) - T(nz)) / (0.5 (hnode(nz-1) + hnode(nz))) inside the column, zero at
+// the first and last interface; the interfaces outside [nzmin, nzmax] are left as they are
+// ===========================================================================
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_trz(DTopo tp, DGeom<R> g, const R *__restrict__ T, R *__restrict__ trz) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int L1 = tp.L1, nl = tp.nl;
+    for (int n = blockIdx.x * kWarpsPerBlock + warp; n < tp.N2; n += gridDim.x * kWarpsPerBlock) {
+        const int nzmin = tp.n_ulev[n], nzmax = tp.n_nlev[n];
+        for (int nz = nzmin + 1 + lane; nz <= nzmax - 1; nz += 32) {
+            const R dz = R(0.5) * (g.hnode[ix1(nz - 1, n, L1)] + g.hnode[ix1(nz, n, L1)]);
+            trz[ixn(nz, n, nl)] = (T[ix1(nz - 1, n, L1)] - T[ix1(nz, n, L1)]) / dz;
+        }
+        if (lane == 0) {
+            trz[ixn(nzmin, n, nl)] = R(0);
+            trz[ixn(nzmax, n, nl)] = R(0);
+        }
+    }
+}
+
 // area-weighted mean of tr_xy over the node's elements wet at level nz
 // (fill_up_dn_grad, src/oce_muscl_adv.F90:388-405)
 template <typename R>
@@ -1026,6 +1048,10 @@ void Launch<R>::ab(const DTopo &tp, DTracers<R> &tr, int ab, cudaStream_t s) {
 template <typename R>
 void Launch<R>::trxy(const DTopo &tp, const DGeom<R> &g, DTracers<R> &tr, cudaStream_t s) {
     k_trxy<R><<<grid_for(tp.T2, kWarpsPerBlock), kThreads, 0, s>>>(tp, g, tr);
+}
+template <typename R>
+void Launch<R>::trz(const DTopo &tp, const DGeom<R> &g, const R *T, R *trz, cudaStream_t s) {
+    k_trz<R><<<grid_for(tp.N2, kWarpsPerBlock), kThreads, 0, s>>>(tp, g, T, trz);
 }
 template <typename R>
 void Launch<R>::edge_flux(const DTopo &tp, const DGeom<R> &g, const DForcing<R> &f, DTracers<R> &tr, int fct,

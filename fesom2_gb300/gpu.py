@@ -85,6 +85,7 @@ _SIGS = {
     "fesom_gpu_tracer_content": ([_P, _P], C.c_int),
     "fesom_gpu_set_tracers_per_launch": ([_P, C.c_int32], C.c_int),
     "fesom_gpu_set_host_groups": ([_P, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
+    "fesom_gpu_tracer_gradient_z": ([_P, _P, _P], C.c_int),
     "fesom_gpu_profile_step": ([_P, C.c_double, _P, _P], C.c_int),
     "fesom_gpu_launches_per_step": ([_P, C.POINTER(C.c_int32)], C.c_int),
     "fesom_gpu_debug_fetch": ([_P, C.c_char_p, C.c_int32, _P, C.c_size_t], C.c_int),
@@ -245,6 +246,17 @@ class Context:
     # -- per-routine drop-ins (FP64) ---------------------------------------------
     def init_tracers_ab(self, cfg: TraCfg, values, valuesAB, valuesold):
         self._chk(self.L.fesom_gpu_init_tracers_ab(self.h, C.byref(cfg), _p(values), _p(valuesAB), _p(valuesold)))
+
+    def tracer_gradient_z(self, values, tr_z=None):
+        """tracer_gradient_z of values (nod2D, nl-1) (``fesom_gpu_tracer_gradient_z``); tr_z
+        (nod2D, nl) is updated in place (a new zero array when None) and returned."""
+        N2, nl = self.mesh.nod2D, self.mesh.nl
+        out = np.zeros((N2, nl)) if tr_z is None else tr_z
+        if out.dtype != np.float64 or not out.flags.c_contiguous or out.shape != (N2, nl):
+            raise ValueError("tr_z must be a C-contiguous float64 (nod2D, nl) array")
+        v = _c64(values)
+        self._chk(self.L.fesom_gpu_tracer_gradient_z(self.h, _p(v), _p(out)))
+        return out
 
     def adv_tra(self, forcing, cfg: TraCfg, ttf, ttfAB, dt=None):
         N2, L1 = self.mesh.nod2D, self.mesh.nl - 1

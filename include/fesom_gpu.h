@@ -5,6 +5,7 @@
  * FESOM2 (reference paths are relative to the FESOM2 source tree):
  *
  *   fesom_gpu_init_tracers_ab   init_tracers_AB          src/oce_tracer_mod.F90:13-143
+ *   fesom_gpu_tracer_gradient_z tracer_gradient_z        src/oce_tracer_mod.F90:192-232
  *   fesom_gpu_adv_tra           do_oce_adv_tra           src/oce_adv_tra_driver.F90:46-490
  *   fesom_gpu_vdiff_impl        diff_ver_part_impl_ale   src/oce_ale_tracer.F90:907-1435
  *   fesom_gpu_tracer_step       body of the tracer loop  src/oce_ale_tracer.F90:280-351
@@ -21,7 +22,7 @@
  *
  * and adds device-resident stepping (fesom_gpu_state_setup / _forcing_upload /
  * _run_steps, CUDA-graph replay), a host-array FP32 step with the transfers
- * overlapped (fesom_gpu_step_host_f32) and a batch of independent meshes
+ * overlapped (fesom_gpu_step_host_f32, group order fesom_gpu_set_host_groups) and a batch of independent meshes
  * (fesom_gpu_batch_*).
  *
  * All arrays are passed by address in the reference's Fortran layout
@@ -165,6 +166,12 @@ int fesom_gpu_update_thickness(fesom_gpu_ctx *ctx, const double *hnode, const do
  * valuesold is (ab_order-1, nl-1, nod2D). */
 int fesom_gpu_init_tracers_ab(fesom_gpu_ctx *ctx, const fesom_tra_cfg *cfg, const double *values,
                               double *valuesAB, double *valuesold);
+/* tracer_gradient_z (src/oce_tracer_mod.F90:192-232), FP64 contexts: tr_z(nz, n) of values
+ * (nl-1, nod2D) into tr_z (nl, nod2D) -- (T(nz-1) - T(nz)) / (0.5 (hnode(nz-1) + hnode(nz)))
+ * for nzmin < nz < nzmax, zero at nzmin and nzmax; the other entries of tr_z keep their
+ * values.  The reference computes it in init_tracers_AB for the modules outside the tracer
+ * step (the step itself does not read it). */
+int fesom_gpu_tracer_gradient_z(fesom_gpu_ctx *ctx, const double *values, double *tr_z);
 /* do_oce_adv_tra with use_wsplit = .false.: vel (2, nl-1, elem2D), w/wi/we
  * (nl, nod2D), ttf = values, ttfAB = valuesAB (nl-1, nod2D).  Writes
  * dttf_h / dttf_v (del_ttf_advhoriz / del_ttf_advvert, (nl-1, nod2D)); they

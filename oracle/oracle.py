@@ -65,7 +65,8 @@ def lib() -> C.CDLL:
                      "or_adv_tra_ver_upw1", "or_adv_tra_ver_qr4c", "or_oce_tra_adv_fct",
                      "or_oce_tra_adv_flux2dtracer", "or_do_oce_adv_tra", "or_diff_ver_part_impl_ale",
                      "or_tracer_step", "or_set_threads", "or_get_threads", "or_tracer_tail",
-                     "or_diff_part_hor_redi", "or_diff_ver_part_expl_ale", "or_tracer_step_ex"):
+                     "or_diff_part_hor_redi", "or_diff_ver_part_expl_ale", "or_tracer_step_ex",
+                     "or_tracer_gradient_z"):
             getattr(L, name)
         L.or_tracer_step.restype = C.c_int
         L.or_tracer_step_ex.restype = C.c_int
@@ -142,6 +143,12 @@ class OracleMesh:
                                   _ptr(valuesold), C.byref(self.w))
         if rc != 0:
             raise RuntimeError(f"oracle tracer step failed with status {rc}")
+
+    def tracer_gradient_z(self, values, tr_z) -> None:
+        """tracer_gradient_z (src/oce_tracer_mod.F90:192-232) of values into tr_z (nod2D, nl), in place."""
+        for a in (values, tr_z):
+            assert a.flags.c_contiguous and a.dtype == np.float64
+        lib().or_tracer_gradient_z(C.byref(self.s), _ptr(values), _ptr(tr_z))
 
     def init_tracers_AB(self, cfg, values, valuesAB, valuesold) -> None:
         lib().or_init_tracers_AB(C.byref(self.s), C.byref(cfg), _ptr(values), _ptr(valuesAB), _ptr(valuesold),

@@ -55,6 +55,23 @@ def test_init_tracers_ab_bitwise(meshname, kind, ab, request):
     assert np.array_equal(g_old, o_old)
 
 
+@pytest.mark.parametrize("meshname,kind", [("channel_seamount", "channel"), ("sphere_small", "sphere"),
+                                           ("pi_cavity_file_mesh", "sphere")])
+def test_tracer_gradient_z_bitwise(meshname, kind, request):
+    """fesom_gpu_tracer_gradient_z equals the oracle bit for bit, the interfaces outside each
+    column (above a cavity's first wet level, below the bottom) keeping the caller's values."""
+    mesh = request.getfixturevalue(meshname)
+    _, tr = _setup(mesh, kind)
+    T = np.ascontiguousarray(tr[0])
+    trz0 = np.full((mesh.nod2D, mesh.nl), 7.25)
+    want = trz0.copy()
+    O.OracleMesh(mesh).tracer_gradient_z(T, want)
+    ctx = G.Context(mesh, G.PREC_FP64)
+    got = ctx.tracer_gradient_z(T, trz0.copy())
+    assert np.array_equal(got, want)
+    assert (want == 7.25).any()  # entries outside the columns exist and were kept
+
+
 @pytest.mark.parametrize("scheme", SCHEMES, ids=["-".join(s) for s in SCHEMES])
 @pytest.mark.parametrize("meshname,kind", [("channel_seamount", "channel"), ("sphere_small", "sphere"),
                                            ("basin_irregular", "basin")])

@@ -32,6 +32,37 @@ def test_gradients_match_restatement(meshname, kind, request):
     assert np.array_equal(G[ref.smask], om.work["edge_up_dn_grad"][ref.smask])
 
 
+def trz_restatement(mesh, T, trz0):
+    """tracer_gradient_z (src/oce_tracer_mod.F90:192-232) in numpy: tr_z(nz) = (T(nz-1) - T(nz)) /
+    (0.5 (hnode(nz-1) + hnode(nz))) for nzmin < nz < nzmax, zero at nzmin and nzmax, other entries kept."""
+    out = trz0.copy()
+    for n in range(mesh.nod2D):
+        lo, hi = int(mesh.ulevels_nod2D[n]), int(mesh.nlevels_nod2D[n])
+        for nz in range(lo + 1, hi):
+            dz = 0.5 * (mesh.hnode[n, nz - 2] + mesh.hnode[n, nz - 1])
+            out[n, nz - 1] = (T[n, nz - 2] - T[n, nz - 1]) / dz
+        out[n, lo - 1] = 0.0
+        out[n, hi - 1] = 0.0
+    return out
+
+
+@pytest.mark.parametrize("meshname,kind", [("channel_seamount", "channel"), ("pi_cavity_file_mesh", "sphere")])
+def test_vertical_gradient_matches_restatement(meshname, kind, request):
+    """tr_z of the oracle (also filled by init_tracers_AB) against the loop restatement, on a mesh
+    with partial cells and one with ice-shelf cavities (columns starting below the surface)."""
+    mesh = request.getfixturevalue(meshname)
+    T = np.ascontiguousarray(M.make_tracers(mesh, kind, ntr=1, seed=4)[0])
+    trz0 = np.full((mesh.nod2D, mesh.nl), 7.25)
+    want = trz_restatement(mesh, T, trz0)
+    om = O.OracleMesh(mesh)
+    got = trz0.copy()
+    om.tracer_gradient_z(T, got)
+    assert np.array_equal(got, want)
+    om.work["tr_z"][...] = trz0
+    om.init_tracers_AB(O.cfg_struct(), T.copy(), np.zeros_like(T), T.copy())
+    assert np.array_equal(om.work["tr_z"], want)
+
+
 @pytest.mark.parametrize("scheme", SCHEMES, ids=["-".join(s) for s in SCHEMES])
 @pytest.mark.parametrize("meshname,kind", [("channel_seamount", "channel"), ("sphere_small", "sphere")])
 def test_adv_tra_matches_restatement(scheme, meshname, kind, request):
