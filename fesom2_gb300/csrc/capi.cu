@@ -142,12 +142,12 @@ __global__ void k_f2d(const float *in, double *out, size_t n) {
 int put(fesom_gpu_ctx *ctx, void *dst, const double *src, size_t n) {
     if (!src) return FESOM_OK;
     if (ctx->prec == FESOM_PREC_FP64) {
-        CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDefault, ctx->stream));
         return FESOM_OK;
     }
     for (size_t off = 0; off < n; off += ctx->stage_n) {
         size_t m = std::min(ctx->stage_n, n - off);
-        CK(cudaMemcpyAsync(ctx->stage, src + off, m * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->stage, src + off, m * sizeof(double), cudaMemcpyDefault, ctx->stream));
         k_d2f<<<(int)std::min<size_t>((m + 255) / 256, 152 * 32), 256, 0, ctx->stream>>>(ctx->stage, (float *)dst + off, m);
         CK(cudaGetLastError());
     }
@@ -158,14 +158,14 @@ int put(fesom_gpu_ctx *ctx, void *dst, const double *src, size_t n) {
 int get(fesom_gpu_ctx *ctx, double *dst, const void *src, size_t n) {
     if (!dst) return FESOM_OK;
     if (ctx->prec == FESOM_PREC_FP64) {
-        CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDefault, ctx->stream));
         return FESOM_OK;
     }
     for (size_t off = 0; off < n; off += ctx->stage_n) {
         size_t m = std::min(ctx->stage_n, n - off);
         k_f2d<<<(int)std::min<size_t>((m + 255) / 256, 152 * 32), 256, 0, ctx->stream>>>((const float *)src + off, ctx->stage, m);
         CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(dst + off, ctx->stage, m * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(dst + off, ctx->stage, m * sizeof(double), cudaMemcpyDefault, ctx->stream));
     }
     return FESOM_OK;
 }
@@ -202,7 +202,7 @@ int put_deint(fesom_gpu_ctx *ctx, float *o1, float *o2, const double *src, size_
     const size_t ch = ctx->stage_n / 2;
     for (size_t off = 0; off < n; off += ch) {
         size_t m = std::min(ch, n - off);
-        CK(cudaMemcpyAsync(ctx->stage, src + 2 * off, 2 * m * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->stage, src + 2 * off, 2 * m * sizeof(double), cudaMemcpyDefault, ctx->stream));
         k_deint_d2f<<<nblk(m), 256, 0, ctx->stream>>>(ctx->stage, o1 + off, o2 + off, m);
         CK(cudaGetLastError());
     }
@@ -214,7 +214,7 @@ int get_int(fesom_gpu_ctx *ctx, double *dst, const float *o1, const float *o2, s
         size_t m = std::min(ch, n - off);
         k_int_f2d<<<nblk(m), 256, 0, ctx->stream>>>(o1 + off, o2 + off, ctx->stage, m);
         CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(dst + 2 * off, ctx->stage, 2 * m * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(dst + 2 * off, ctx->stage, 2 * m * sizeof(double), cudaMemcpyDefault, ctx->stream));
     }
     return FESOM_OK;
 }
@@ -223,7 +223,7 @@ int put_deint_f(fesom_gpu_ctx *ctx, float *o1, float *o2, const float *src, size
     const size_t ch = ctx->stage_n;  // 2*ch floats fit the stage
     for (size_t off = 0; off < n; off += ch) {
         size_t m = std::min(ch, n - off);
-        CK(cudaMemcpyAsync(st, src + 2 * off, 2 * m * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(st, src + 2 * off, 2 * m * sizeof(float), cudaMemcpyDefault, ctx->stream));
         k_deint_f<<<nblk(m), 256, 0, ctx->stream>>>(st, o1 + off, o2 + off, m);
         CK(cudaGetLastError());
     }
@@ -236,7 +236,7 @@ int get_int_f(fesom_gpu_ctx *ctx, float *dst, const float *o1, const float *o2, 
         size_t m = std::min(ch, n - off);
         k_int_f<<<nblk(m), 256, 0, ctx->stream>>>(o1 + off, o2 + off, st, m);
         CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(dst + 2 * off, st, 2 * m * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(dst + 2 * off, st, 2 * m * sizeof(float), cudaMemcpyDefault, ctx->stream));
     }
     return FESOM_OK;
 }
@@ -891,7 +891,7 @@ int ensure_one(fesom_gpu_ctx *ctx, const fesom_tra_cfg *cfg) {
         if (ctx->cfgs.size() < (size_t)ctx->ntr) ctx->cfgs.resize(ctx->ntr, *cfg);
     }
     DCfg d = to_dcfg(*cfg);
-    CK(cudaMemcpyAsync(ctx->d_cfg, &d, sizeof(DCfg), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_cfg, &d, sizeof(DCfg), cudaMemcpyDefault, ctx->stream));
     return FESOM_OK;
 }
 
@@ -1181,7 +1181,7 @@ int fesom_gpu_vdiff_impl_wi(fesom_gpu_ctx *ctx, double dt, const fesom_tra_cfg *
     fesom_tra_cfg c = *cfg;
     c.i_vert_diff = 1;
     DCfg d = to_dcfg(c);
-    CK(cudaMemcpyAsync(ctx->d_cfg, &d, sizeof(DCfg), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_cfg, &d, sizeof(DCfg), cudaMemcpyDefault, ctx->stream));
     Launch<double>::vdiff(ctx->tp, ctx->g64, f, tr, dt, ctx->scratch, ctx->stream);
     CK(cudaGetLastError());
     if ((rc = get(ctx, values, ctx->T, sN))) return rc;
@@ -1244,12 +1244,12 @@ int fesom_gpu_forcing_upload_f32(fesom_gpu_ctx *ctx, const float *uv, const floa
     if (ctx->prec != FESOM_PREC_FP32) { ctx->err = "FP32 buffers need a FESOM_PREC_FP32 context"; return FESOM_ERR_STATE; }
     if (!ctx->state_ready) { ctx->err = "call fesom_gpu_state_setup first"; return FESOM_ERR_STATE; }
     const size_t sNI = (size_t)ctx->nl * ctx->N2;
-    CK(cudaMemcpyAsync(ctx->uv, uv, 4 * 2 * (size_t)ctx->L1 * ctx->T2, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(ctx->w, w, 4 * sNI, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(ctx->we, we, 4 * sNI, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(ctx->Kv, Kv, 4 * sNI, cudaMemcpyHostToDevice, ctx->stream));
-    if (wi) CK(cudaMemcpyAsync(ctx->wi, wi, 4 * sNI, cudaMemcpyHostToDevice, ctx->stream));
-    if (bc_surf) CK(cudaMemcpyAsync(ctx->bc, bc_surf, 4 * (size_t)ctx->N2 * ctx->ntr, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->uv, uv, 4 * 2 * (size_t)ctx->L1 * ctx->T2, cudaMemcpyDefault, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->w, w, 4 * sNI, cudaMemcpyDefault, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->we, we, 4 * sNI, cudaMemcpyDefault, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->Kv, Kv, 4 * sNI, cudaMemcpyDefault, ctx->stream));
+    if (wi) CK(cudaMemcpyAsync(ctx->wi, wi, 4 * sNI, cudaMemcpyDefault, ctx->stream));
+    if (bc_surf) CK(cudaMemcpyAsync(ctx->bc, bc_surf, 4 * (size_t)ctx->N2 * ctx->ntr, cudaMemcpyDefault, ctx->stream));
     else CK(cudaMemsetAsync(ctx->bc, 0, 4 * (size_t)ctx->N2 * ctx->ntr, ctx->stream));
     ctx->forcing_ready = true;
     return FESOM_OK;
@@ -1302,10 +1302,10 @@ int fesom_gpu_tracer_upload_f32(fesom_gpu_ctx *ctx, int32_t tr, const float *val
     if (rc) return rc;
     if (ctx->prec != FESOM_PREC_FP32) { ctx->err = "FP32 buffers need a FESOM_PREC_FP32 context"; return FESOM_ERR_STATE; }
     const size_t sN = (size_t)ctx->L1 * ctx->N2;
-    if (values) CK(cudaMemcpyAsync(level32(ctx, 0) + sN * tr, values, 4 * sN, cudaMemcpyHostToDevice, ctx->stream));
+    if (values) CK(cudaMemcpyAsync(level32(ctx, 0) + sN * tr, values, 4 * sN, cudaMemcpyDefault, ctx->stream));
     if (valuesold) {
         if (ctx->ab_max == 2)
-            CK(cudaMemcpyAsync(level32(ctx, 1) + sN * tr, valuesold, 4 * sN, cudaMemcpyHostToDevice, ctx->stream));
+            CK(cudaMemcpyAsync(level32(ctx, 1) + sN * tr, valuesold, 4 * sN, cudaMemcpyDefault, ctx->stream));
         else if ((rc = put_deint_f(ctx, level32(ctx, 1) + sN * tr, level32(ctx, 2) + sN * tr, valuesold, sN)))
             return rc;
     }
@@ -1317,10 +1317,10 @@ int fesom_gpu_tracer_download_f32(fesom_gpu_ctx *ctx, int32_t tr, float *values,
     if (rc) return rc;
     if (ctx->prec != FESOM_PREC_FP32) { ctx->err = "FP32 buffers need a FESOM_PREC_FP32 context"; return FESOM_ERR_STATE; }
     const size_t sN = (size_t)ctx->L1 * ctx->N2;
-    if (values) CK(cudaMemcpyAsync(values, level32(ctx, 0) + sN * tr, 4 * sN, cudaMemcpyDeviceToHost, ctx->stream));
+    if (values) CK(cudaMemcpyAsync(values, level32(ctx, 0) + sN * tr, 4 * sN, cudaMemcpyDefault, ctx->stream));
     if (valuesold) {
         if (ctx->ab_max == 2)
-            CK(cudaMemcpyAsync(valuesold, level32(ctx, 1) + sN * tr, 4 * sN, cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaMemcpyAsync(valuesold, level32(ctx, 1) + sN * tr, 4 * sN, cudaMemcpyDefault, ctx->stream));
         else if ((rc = get_int_f(ctx, valuesold, level32(ctx, 1) + sN * tr, level32(ctx, 2) + sN * tr, sN)))
             return rc;
     }
@@ -1509,7 +1509,7 @@ int fesom_gpu_tracer_content(fesom_gpu_ctx *ctx, double *content) {
         Launch<double>::content(ctx->tp, ctx->g64, tr, ctx->partials, ctx->content_blocks, ctx->content_out, ctx->stream);
     }
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(content, ctx->content_out, sizeof(double) * ctx->ntr, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(content, ctx->content_out, sizeof(double) * ctx->ntr, cudaMemcpyDefault, ctx->stream));
     return wait_stream(ctx, -1);
 }
 
@@ -1584,7 +1584,7 @@ int fesom_gpu_diff_ver_expl(fesom_gpu_ctx *ctx, double dt, const double *Kv, con
     if ((rc = put(ctx, ctx->Kv, Kv, (size_t)ctx->nl * ctx->N2)) || (rc = put(ctx, tr.T, values, sN)) ||
         (rc = put(ctx, tr.dttf_h, del_ttf, sN)))
         return rc;
-    if (flux_surf) CK(cudaMemcpyAsync(ctx->bc, flux_surf, sizeof(double) * ctx->N2, cudaMemcpyHostToDevice, ctx->stream));
+    if (flux_surf) CK(cudaMemcpyAsync(ctx->bc, flux_surf, sizeof(double) * ctx->N2, cudaMemcpyDefault, ctx->stream));
     else CK(cudaMemsetAsync(ctx->bc, 0, sizeof(double) * ctx->N2, ctx->stream));
     DForcing<double> f = forcing_view<double>(ctx, 0);
     Launch<double>::vexpl(ctx->tp, ctx->g64, f, tr, dt, tr.dttf_h, 1, 1, ctx->stream);
@@ -1622,12 +1622,12 @@ int fesom_gpu_tracer_tail(fesom_gpu_ctx *ctx, int32_t ntr, const fesom_tra_cfg *
         ctx->tail_nbins = tc->nbins;
     }
     if (clim) {
-        CK(cudaMemcpyAsync(ctx->tail_r2c, relax2clim, sizeof(double) * ctx->N2, cudaMemcpyHostToDevice, ctx->stream));
-        CK(cudaMemcpyAsync(ctx->tail_S, Sclim, sizeof(double) * sN, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->tail_r2c, relax2clim, sizeof(double) * ctx->N2, cudaMemcpyDefault, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->tail_S, Sclim, sizeof(double) * sN, cudaMemcpyDefault, ctx->stream));
     }
-    if (clim || tc->zonal_relax) CK(cudaMemcpyAsync(ctx->tail_T, Tclim, sizeof(double) * sN, cudaMemcpyHostToDevice, ctx->stream));
+    if (clim || tc->zonal_relax) CK(cudaMemcpyAsync(ctx->tail_T, Tclim, sizeof(double) * sN, cudaMemcpyDefault, ctx->stream));
     if (tc->zonal_relax)
-        CK(cudaMemcpyAsync(ctx->tail_z, ztem, sizeof(double) * (size_t)tc->nbins * ctx->L1, cudaMemcpyHostToDevice,
+        CK(cudaMemcpyAsync(ctx->tail_z, ztem, sizeof(double) * (size_t)tc->nbins * ctx->L1, cudaMemcpyDefault,
                            ctx->stream));
     // decay constants of 14C and 39Ar (src/mod_transit.F90:49-50), factors formed on the host
     const double k14 = 3.8561e-12, k39 = 8.1708e-11;
@@ -1655,10 +1655,10 @@ int fesom_gpu_tracer_tail(fesom_gpu_ctx *ctx, int32_t ntr, const fesom_tra_cfg *
         }
         a.clamp = t == tc->salt_index ? 1 : (t == tc->age_index ? 2 : 0);
         if (!a.decay && !a.relax && !a.clamp) continue;
-        CK(cudaMemcpyAsync(ctx->tail_v, values[t], sizeof(double) * sN, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->tail_v, values[t], sizeof(double) * sN, cudaMemcpyDefault, ctx->stream));
         launch_tracer_tail(ctx->tp, ctx->coord_y, ctx->tail_v, a, ctx->stream);
         CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(values[t], ctx->tail_v, sizeof(double) * sN, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(values[t], ctx->tail_v, sizeof(double) * sN, cudaMemcpyDefault, ctx->stream));
     }
     return wait_stream(ctx, -1);
 }
@@ -1746,20 +1746,20 @@ int fesom_gpu_step_host_f32(fesom_gpu_ctx *ctx, double dt, const float *uv, cons
     CK(cudaStreamWaitEvent(ctx->h2d, ctx->ev_forcing, 0));
     // forcing, then the tracer groups, on the copy-in stream
     const size_t sNI = (size_t)ctx->nl * ctx->N2;
-    CK(cudaMemcpyAsync(ctx->uv, uv, 4 * 2 * (size_t)ctx->L1 * ctx->T2, cudaMemcpyHostToDevice, ctx->h2d));
-    CK(cudaMemcpyAsync(ctx->w, w, 4 * sNI, cudaMemcpyHostToDevice, ctx->h2d));
-    CK(cudaMemcpyAsync(ctx->we, we, 4 * sNI, cudaMemcpyHostToDevice, ctx->h2d));
-    CK(cudaMemcpyAsync(ctx->Kv, Kv, 4 * sNI, cudaMemcpyHostToDevice, ctx->h2d));
-    if (wi) CK(cudaMemcpyAsync(ctx->wi, wi, 4 * sNI, cudaMemcpyHostToDevice, ctx->h2d));
-    if (bc_surf) CK(cudaMemcpyAsync(ctx->bc, bc_surf, 4 * (size_t)ctx->N2 * ntr, cudaMemcpyHostToDevice, ctx->h2d));
+    CK(cudaMemcpyAsync(ctx->uv, uv, 4 * 2 * (size_t)ctx->L1 * ctx->T2, cudaMemcpyDefault, ctx->h2d));
+    CK(cudaMemcpyAsync(ctx->w, w, 4 * sNI, cudaMemcpyDefault, ctx->h2d));
+    CK(cudaMemcpyAsync(ctx->we, we, 4 * sNI, cudaMemcpyDefault, ctx->h2d));
+    CK(cudaMemcpyAsync(ctx->Kv, Kv, 4 * sNI, cudaMemcpyDefault, ctx->h2d));
+    if (wi) CK(cudaMemcpyAsync(ctx->wi, wi, 4 * sNI, cudaMemcpyDefault, ctx->h2d));
+    if (bc_surf) CK(cudaMemcpyAsync(ctx->bc, bc_surf, 4 * (size_t)ctx->N2 * ntr, cudaMemcpyDefault, ctx->h2d));
     else CK(cudaMemsetAsync(ctx->bc, 0, 4 * (size_t)ctx->N2 * ntr, ctx->h2d));
     ctx->forcing_ready = true;
     CK(cudaEventRecord(ctx->ev_forcing, ctx->h2d));
     float *Tcur = level32(ctx, 0), *Told = level32(ctx, 1);  // the step writes Tnew into Told's buffer
     for (int gi = 0; gi < ng; gi++) {
         for (int t = gs[gi]; t < gs[gi + 1]; t++) {
-            CK(cudaMemcpyAsync(Tcur + sN * t, values_in[t], 4 * sN, cudaMemcpyHostToDevice, ctx->h2d));
-            CK(cudaMemcpyAsync(Told + sN * t, valuesold_in[t], 4 * sN, cudaMemcpyHostToDevice, ctx->h2d));
+            CK(cudaMemcpyAsync(Tcur + sN * t, values_in[t], 4 * sN, cudaMemcpyDefault, ctx->h2d));
+            CK(cudaMemcpyAsync(Told + sN * t, valuesold_in[t], 4 * sN, cudaMemcpyDefault, ctx->h2d));
         }
         CK(cudaEventRecord(ctx->ev_in[gi], ctx->h2d));
     }
@@ -1779,9 +1779,9 @@ int fesom_gpu_step_host_f32(fesom_gpu_ctx *ctx, double dt, const float *uv, cons
     for (int gi = 0; gi < ng; gi++) {
         CK(cudaStreamWaitEvent(ctx->d2h, ctx->ev_done[gi], 0));
         for (int t = gs[gi]; t < gs[gi + 1]; t++) {
-            CK(cudaMemcpyAsync(values_out[t], Told + sN * t, 4 * sN, cudaMemcpyDeviceToHost, ctx->d2h));
+            CK(cudaMemcpyAsync(values_out[t], Told + sN * t, 4 * sN, cudaMemcpyDefault, ctx->d2h));
             if (valuesold_out)
-                CK(cudaMemcpyAsync(valuesold_out[t], Tcur + sN * t, 4 * sN, cudaMemcpyDeviceToHost, ctx->d2h));
+                CK(cudaMemcpyAsync(valuesold_out[t], Tcur + sN * t, 4 * sN, cudaMemcpyDefault, ctx->d2h));
         }
     }
     rotate32(ctx);

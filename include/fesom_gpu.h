@@ -28,9 +28,13 @@
  * All arrays are passed by address in the reference's Fortran layout
  * a(level, entity) (column-major, level-contiguous), exactly as the derived
  * types t_mesh / t_tracer / t_dyn hold them, so a Fortran caller passes
- * c_loc() of its arrays with no copy.  Host pointers are copied to the device
- * inside the call; fesom_gpu_tracer_device_ptr and fesom_gpu_vdiff_impl_noalloc
- * work on device memory.
+ * c_loc() of its arrays with no copy.  An array argument may be a host or a
+ * device pointer: the copies inside each call take their direction from the
+ * pointer (unified addressing), so a caller whose arrays already live on the
+ * GPU (an OpenACC build passing `host_data use_device` addresses) moves nothing
+ * over the host link.  fesom_gpu_tracer_device_ptr gives the device-resident
+ * state; fesom_gpu_vdiff_impl_noalloc works on the caller's device arrays in
+ * place.
  *
  * Error convention: every entry point returns 0 on success and a FESOM_ERR_*
  * code otherwise (the reference aborts through par_ex on the same conditions);

@@ -5,6 +5,8 @@ sum in the reference's serial scatter order and are built without FMA
 contraction).  FP32 form: max relative error per step <= 1e-5 against the
 FP64 oracle started from the same state, content conserved, FCT bounds kept.
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -359,3 +361,30 @@ def test_fp32_stage_passes_do_not_change_results(basin_irregular):
     for o in outs[1:]:
         for k in range(7):
             assert np.array_equal(o[k], outs[0][k]), k
+
+
+def test_device_pointers_give_the_host_results(channel_seamount):
+    """Array arguments may live in device memory (an OpenACC caller's `host_data use_device`
+    addresses): the copies inside each call take their direction from the pointer, and the
+    results equal those of the same calls on host arrays bit for bit."""
+    torch = pytest.importorskip("torch")
+    mesh = channel_seamount
+    f, tr = _setup(mesh, "channel")
+    T = np.ascontiguousarray(tr[0])
+    cfg = G.tra_cfg()
+    ctx = G.Context(mesh, G.PREC_FP64)
+    # host arrays
+    want_z = ctx.tracer_gradient_z(T, np.full((mesh.nod2D, mesh.nl), 3.5))
+    want_v = T.copy()
+    ctx.vdiff_impl(f, cfg, want_v)
+    # the same calls on device arrays
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to("cuda")
+    T_d, z_d = dev(T), dev(np.full((mesh.nod2D, mesh.nl), 3.5))
+    kv_d, v_d = dev(f.Kv), dev(T)
+    bc_d = None if f.bc_surface is None else dev(np.asarray(f.bc_surface, dtype=np.float64))
+    p = lambda t: None if t is None else G._P(t.data_ptr())
+    assert ctx.L.fesom_gpu_tracer_gradient_z(ctx.h, p(T_d), p(z_d)) == 0
+    assert ctx.L.fesom_gpu_vdiff_impl_wi(ctx.h, float(f.dt), C.byref(cfg), p(kv_d), p(bc_d), None, p(v_d)) == 0
+    torch.cuda.synchronize()
+    assert np.array_equal(z_d.cpu().numpy(), want_z)
+    assert np.array_equal(v_d.cpu().numpy(), want_v)
