@@ -1,45 +1,50 @@
 // kernels_fp32_batched.cu -- the FP32 batched form of the tracer step.
 //
-// All tracers of a step in one launch per stage; three tracer stages and two
-// tracer-independent set-up stages:
+// All tracers of a launch group in one launch per stage, the whole step in one CUDA graph:
 //
-//   k32_vflux     edge volume fluxes per edge-layer (oce_adv_tra_hor.F90:159-250
-//                 segment rule); shared by every tracer
-//   k32_vfactors  FP64 factorisation of the implicit vertical-diffusion matrix of
-//                 every column (oce_ale_tracer.F90:1088-1204, 1406-1414): the
-//                 pivots m = b - cp*a carry the cancellation that thin bottom cells
-//                 cause, so they are formed in FP64; stored as FP32 a, c, 1/m, c/m
-//   k32_lo_ad     per node: the LO solution's increment (edge gather of upwind
-//                 fluxes + upwind vertical flux with w_e), the vertical
-//                 antidiffusive flux (QR4C/UPW1 on the AB values) and the
-//                 antidiffusive flux of the edges the node owns (edges(1,e) == n):
-//                 MUSCL/MFCT/UPW1 on the AB values with fill_up_dn_grad inlined
-//   k32_bounds    per node: FCT bounds (max/min of LO and T over the node's
-//                 neighbours and the adjacent layers) and R+/R- (oce_adv_tra_fct.F90)
-//   k32_update    per node: limited fluxes, flux divergence, T* update, then the
-//                 implicit vertical diffusion as two warp scans of affine maps over
-//                 the column (the forward and back substitution with the FP64
-//                 factors); written to the buffer of the oldest time level
+//   k32_vflux        edge volume fluxes per edge-layer (oce_adv_tra_hor.F90:159-250
+//                    segment rule); shared by every tracer
+//   k32_vfactors     FP64 factorisation of the implicit vertical-diffusion matrix of
+//                    every column (oce_ale_tracer.F90:1088-1204, 1406-1414): the
+//                    pivots m = b - cp*a carry the cancellation that thin bottom cells
+//                    cause, so they are formed in FP64; stored as FP32 a, c, 1/m, c/m
+//   k32_lo_ad        per node: the LO solution (edge gather of upwind fluxes + upwind
+//                    vertical flux with w_e) and the vertical antidiffusive flux
+//                    (QR4C / UPW1 / CDIFF on the AB values; PPM in k32_vppm)
+//   k32_ho           per edge: the horizontal antidiffusive flux, MUSCL / MFCT / UPW1 on
+//                    the AB values minus the upwind LO flux (k32_ho_nodemean: the few
+//                    edge-layers whose gradients are node means)
+//   k32_bounds       per node: FCT bounds (max/min of LO and T over the node's
+//                    neighbours and the adjacent layers) and R+/R- (oce_adv_tra_fct.F90)
+//   k32_update       per node: limited fluxes, flux divergence, T* update, written to
+//                    the buffer of the oldest time level
+//   k32_vdiff        per node: the implicit vertical diffusion as two warp scans of
+//                    affine maps over the column (forward and back substitution with
+//                    the FP64-formed factors)
+//   k32_vppm, k32_lo_impl, k32_vdiff_w, k32_hdiff, k32_diff
+//                    the optional parts: PPM vertical fluxes, the split vertical
+//                    velocity, horizontal and explicit vertical diffusion
 //
-// Every tracer carries the same three quantities whatever its limiter: the LO
-// increment and the antidiffusive fluxes "high order minus low order" of the
-// edges and interfaces.  Without FCT the update adds them unlimited, which is
-// the high-order flux divergence; with FCT it scales them by R+/R- first.
+// Every tracer carries the same quantities whatever its limiter: the LO solution and
+// the antidiffusive fluxes "high order minus low order" of the edges and interfaces.
+// Without FCT the update adds them unlimited, which is the high-order flux divergence;
+// with FCT it scales them by R+/R- first.
 //
-// Mapping: one warp per node for ALL tracers of the launch.  The lanes cover a
-// chunk of the node's column (one level per lane); consecutive chunks overlap
-// by the halo levels each stage needs (the level above/below comes from the
-// neighbouring lane through a shuffle), and the halo lanes compute but do not
-// store.  The node's edge list, the neighbour offsets and the tracer-
-// independent geometry of a chunk sit in registers and serve every tracer, so
-// per tracer a lane does only the gathers and the arithmetic of that tracer.
-// Eight consecutive nodes per block (the node order is spatially local), so
-// the neighbour columns a block gathers are mostly shared between its warps.
+// Mapping of the node stages: one warp per node for all tracers of the launch.  The
+// lanes cover a chunk of the node's column (one level per lane); consecutive chunks
+// overlap by the halo levels each stage needs (the level above/below comes from the
+// neighbouring lane through a shuffle), and the halo lanes compute but do not store.
+// The last chunk of a column, when its levels fill at most half a warp, carries several
+// tracers side by side in lane segments.  The node's edge list, the neighbour offsets
+// and the tracer-independent geometry of a chunk sit in registers and serve every
+// tracer, so per tracer a lane does only the gathers and the arithmetic of that tracer.
+// Eight consecutive nodes per block (the node order is spatially local), so the
+// neighbour columns a block gathers are mostly shared between its warps.
 //
-// Layout: tracer-major, column-contiguous per tracer (the reference's
-// a(level, node) per tracer).  No atomics on values: each edge flux is written
-// by its owner node only and every node sum is a gather.  The Adams-Bashforth
-// shift is a rotation of the time-level buffers (no copy).
+// Layout: tracer-major, column-contiguous per tracer (the reference's a(level, node)
+// per tracer).  No atomics on values: each edge flux is written once and every node
+// sum is a gather.  The Adams-Bashforth shift is a rotation of the time-level buffers
+// (no copy).
 #include <cuda_runtime.h>
 
 #include "fesom_internal.h"
