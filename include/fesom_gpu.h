@@ -164,7 +164,11 @@ int fesom_gpu_status(fesom_gpu_ctx *ctx, uint32_t *status, int32_t timeout_ms);
 int fesom_gpu_update_thickness(fesom_gpu_ctx *ctx, const double *hnode, const double *hnode_new,
                                const double *helem, const double *Z_3d_n, const double *zbar_3d_n);
 
-/* ---- per-routine drop-ins (FP64, host arrays, one tracer per call) ------- */
+/* ---- per-routine drop-ins (FP64, host arrays, one tracer per call) -------
+ * They stage their arrays in the buffers of the context's first tracer slot,
+ * so between them and device-resident stepping (fesom_gpu_state_setup /
+ * fesom_gpu_run_steps) of the same context, slot 0's device state is not
+ * kept: a caller mixing the two re-uploads it (fesom_gpu_tracer_upload). */
 /* init_tracers_AB: valuesAB from values/valuesold (AB2/AB3), valuesold shift,
  * element gradients (tr_xy) and edge_up_dn_grad kept on the device.
  * valuesold is (ab_order-1, nl-1, nod2D). */
