@@ -452,7 +452,8 @@ def mesh_from_dump(tm: Dict[str, object], partit: Optional[Dict[str, object]] = 
     nie = i32(tm["nod_in_elem2D"])  # (nod2D, maxK) row-major view of nod_in_elem2D(maxK, nod2D)
     ptr = np.zeros(N2 + 1, np.int32)
     ptr[1:] = np.cumsum(num)
-    lists = np.concatenate([nie[n, :num[n]] for n in range(N2)]) - 1 if N2 else np.zeros(0, np.int32)
+    # the first num(n) entries of every column nod_in_elem2D(:, n), in order
+    lists = nie[:N2][np.arange(nie.shape[1])[None, :] < num[:, None]] - 1
     return M.Mesh(
         nl=nl, coord_nod2D=np.zeros((N2, 2)), elem2D_nodes=i32(tri), edges=i32(edges), edge_tri=etri,
         edge2D_in=int(tm["edge2D_in"]), nod_in_elem2D_ptr=ptr, nod_in_elem2D=i32(lists),
@@ -475,8 +476,7 @@ def dump_from_mesh(mesh) -> Dict[str, object]:
     num = mesh.nod_in_elem2D_num()
     maxk = int(num.max()) if N2 else 0
     nie = np.zeros((N2, maxk), np.int32)
-    for n in range(N2):
-        nie[n, :num[n]] = mesh.nod_in_elem2D[mesh.nod_in_elem2D_ptr[n]:mesh.nod_in_elem2D_ptr[n + 1]] + 1
+    nie[np.arange(maxk)[None, :] < num[:, None]] = mesh.nod_in_elem2D + 1
     etri = np.where(mesh.edge_tri < 0, 0, mesh.edge_tri + 1).astype(np.int32)
     out: Dict[str, object] = {
         "nod2D": N2, "ocean_area": float(np.sum(mesh.area[:, 0])), "ocean_areawithcav": float(np.sum(mesh.area[:, 0])),
