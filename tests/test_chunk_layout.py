@@ -72,3 +72,28 @@ def test_packing_factor_on_deep_columns():
     assert (nch, W, P) == (3, 14, 2)
     # a 13-layer column: one chunk of 15 lanes -> 2 tracers side by side
     assert layout(1, 14, 1, 1)[1:] == (1, 15, 2)
+
+
+def test_edge_passes_store_every_level_once():
+    """k32_ho: passes of 32 levels over an edge's range [elo, ehi]; the last pass, when its W
+    levels fill at most half a warp, carries floor(32 / W) tracers in segments of W lanes."""
+    for elo in (1, 4):
+        for nlev in range(1, 129):
+            ehi = elo + nlev - 1
+            per_tracer = {}
+            nz0 = elo
+            while nz0 + 32 <= ehi:  # full passes: one tracer per pass
+                per_tracer.setdefault(0, []).extend(range(nz0, nz0 + 32))
+                nz0 += 32
+            W = ehi - nz0 + 1
+            P = 32 // W
+            for lane in range(32):
+                q = lane // W if P > 1 else 0
+                nz = nz0 + lane - q * W
+                if nz <= ehi and q < P:
+                    per_tracer.setdefault(q, [])
+                    per_tracer[q].append(nz)
+            full = [z for z in per_tracer.get(0, []) if z < nz0]
+            for q in range(P):
+                levels = full + [z for z in per_tracer.get(q, []) if z >= nz0]
+                assert sorted(levels) == list(range(elo, ehi + 1)), (elo, nlev, q)
