@@ -242,3 +242,54 @@ def test_partit_dump_and_the_whole_mesh_rule(tmp_path, channel_small):
     with pytest.raises(ValueError):
         D.mesh_from_dump(r["mesh"], dict(r["partit"], npes=2, eDim_nod2D=5))
     assert D.rank_suffix(3, 1) == "3" and D.rank_suffix(3, 8) == "3" and D.rank_suffix(3, 16) == "03"
+
+
+def test_payload_round_trip_random_fields(tmp_path, monkeypatch):
+    """Random field sequences (scalars, logicals, characters, arrays of rank 1-4 with zero and
+    unallocated extents) read back as written, with records split into subrecords."""
+    hyp = pytest.importorskip("hypothesis")
+    from hypothesis import given, settings, strategies as st
+
+    monkeypatch.setattr(D, "_MAX_SUB", 64)
+    kinds = st.sampled_from(["i4", "f8", "L4", "c", ("i4", 1), ("f8", 2), ("i4", 3), ("f8", 4)])
+
+    @settings(max_examples=60, deadline=None)
+    @given(st.lists(st.tuples(kinds, st.integers(0, 2 ** 31 - 1)), min_size=1, max_size=12))
+    def check(spec):
+        rng = np.random.default_rng(spec[0][1])
+        w = D.PayloadWriter()
+        want = []
+        for kind, seed in spec:
+            r = np.random.default_rng(seed)
+            if kind == "c":
+                v = "".join(r.choice(list("ABCDEFGH"), size=int(r.integers(0, 20))))
+                w.chars(v, 20)
+            elif isinstance(kind, str):
+                v = {"i4": int(r.integers(-2 ** 31, 2 ** 31)), "f8": float(r.standard_normal()),
+                     "L4": bool(r.integers(0, 2))}[kind]
+                w.scalar(kind, v)
+            else:
+                dt, rank = kind
+                if r.random() < 0.2:
+                    v = None
+                else:
+                    shape = tuple(int(x) for x in r.integers(0, 4, rank))
+                    v = (r.integers(-9, 9, shape).astype(np.int32) if dt == "i4" else r.standard_normal(shape))
+                    if v.size == 0 and all(d == 0 for d in shape):
+                        v = None
+                w.array(v, dt, rank)
+            want.append((kind, v))
+        p = str(tmp_path / f"rand{rng.integers(1 << 30)}.bin")
+        w.write(p)
+        rd = D.read_dump(p)
+        for kind, v in want:
+            if kind == "c":
+                assert rd.chars(20) == v.rstrip()
+            elif isinstance(kind, str):
+                assert rd.scalar(kind) == v
+            else:
+                got = rd.array(*kind)
+                assert (got is None and v is None) or np.array_equal(got, v)
+        rd.done()
+
+    check()
