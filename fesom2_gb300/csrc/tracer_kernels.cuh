@@ -1,11 +1,10 @@
-// tracer_kernels.cuh -- sm_103a kernels of the FESOM2 tracer-transport step.
+// tracer_kernels.cuh -- sm_103a kernels of the FESOM2 tracer-transport step, FP64 form.
 //
-// One template, two instantiations:
-//   R = double  (kernels_fp64.cu, built with --fmad=false): the reference's
-//               FP64 arithmetic in the reference's evaluation order, so the
-//               results match the serial Fortran loops bit for bit;
-//   R = float   (kernels_fp32.cu): FP32 storage and arithmetic, compensated
-//               node sums, FP64 Thomas solve and FP64 content sums.
+// Instantiated with R = double (kernels_fp64.cu, built with --fmad=false): the
+// reference's FP64 arithmetic in the reference's evaluation order, so the results
+// match the serial Fortran loops bit for bit.  The FP32 form has its own kernels
+// (kernels_fp32_batched.cu) and takes only the content sums from here
+// (kernels_fp32.cu).
 //
 // Mapping: edge and node kernels run one warp per entity with the lanes over
 // the levels of the column (the reference's arrays are level-contiguous, so
@@ -18,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include "fesom_internal.h"
+#include "vdiff_column.cuh"
 
 namespace fesom {
 
@@ -889,107 +889,26 @@ __global__ void __launch_bounds__(128) k_lo_impl(DTopo tp, DGeom<R> g, DForcing<
 template <typename R>
 __global__ void __launch_bounds__(128) k_vdiff(DTopo tp, DGeom<R> g, DForcing<R> f, DTracers<R> tr, double dt,
                                                double *scratch) {
-    typedef double A;
     const int L1 = tp.L1, nl = tp.nl;
     const size_t N2 = tp.N2;
-    A *Zs = scratch, *cps = scratch + (size_t)(L1 + 1) * N2, *tps = cps + (size_t)(L1 + 1) * N2;
-#define ZN(k) Zs[(size_t)(k) * N2 + n]
-#define CP(k) cps[(size_t)(k) * N2 + n]
-#define TP(k) tps[(size_t)(k) * N2 + n]
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < tp.N2; n += gridDim.x * blockDim.x) {
         const int nzmax = tp.n_nlev[n], nzmin = tp.n_ulev[n];
         const R *hn = g.hnode_new + (size_t)n * L1 - 1;  // hn[nz], 1-based
         const R *ar = g.area + (size_t)n * nl - 1;
         const R *av = g.areasvol + (size_t)n * nl - 1;
         const R *kv = f.Kv + (size_t)n * nl - 1;
-        // Z_n bottom-up (:1088-1096); ZN(k) = Z_n(k)
-        A zb = (A)g.zbar_n_bot[n];
-        ZN(nzmax - 1) = zb + (A)hn[nzmax - 1] / 2.0;
-        for (int nz = nzmax - 1; nz >= nzmin + 1; nz--) {
-            zb = zb + (A)hn[nz];
-            ZN(nz - 1) = zb + (A)hn[nz - 1] / 2.0;
-        }
+        const R *wi = f.wi + (size_t)n * nl - 1;
+        const ColScratch cs{scratch + n, scratch + (size_t)(L1 + 1) * N2 + n, scratch + 2 * (size_t)(L1 + 1) * N2 + n,
+                            N2};
+        vdiff_col_z<R>(cs, nzmin, nzmax, (double)g.zbar_n_bot[n], hn);
         for (int t = 0; t < tr.ntr; t++) {
-            R *Tc = tr.T + t * tr.sN + (size_t)n * L1 - 1;
             if (!tr.cfg[t].ivd) continue;
             // the implicit part of a split vertical velocity joins the solve without a limiter (:961)
             const bool wimpl = f.wsplit && !tr.cfg[t].lim;
-            const R *wi = f.wi + (size_t)n * nl - 1;
-            const A bc = f.bc ? (A)f.bc[(size_t)t * N2 + n] : 0.0;
-            // forward elimination, coefficients built on the fly (:1099-1229, 1406-1414)
-            int nz = nzmin;
-            A zinv2 = 1.0 / (ZN(nz) - ZN(nz + 1));
-            const A zinv = 1.0 * dt;
-            A c = -((A)kv[nz + 1] * zinv2 * zinv * (A)ar[nz + 1] / (A)av[nz]);
-            A b = -c + (A)hn[nz];
-            if (wimpl) {  // :1134-1147
-                A v = zinv * ((A)ar[nz] / (A)av[nz]);
-                b = b + (A)wi[nz] * v;
-                v = zinv * (A)ar[nz + 1] / (A)av[nz];
-                b = b - fmin(0.0, (A)wi[nz + 1]) * v;
-                c = c - fmax(0.0, (A)wi[nz + 1]) * v;
-            }
-            A Tm = (A)Tc[nz], T0 = Tm, Tp1 = (A)Tc[nz + 1];
-            A dz = (A)hn[nz];
-            A rhs = -((b - dz) * T0) - c * Tp1;
-            rhs = rhs + bc;
-            A cp = c / b, tpv = rhs / b;
-            CP(nz) = cp;
-            TP(nz) = tpv;
-            A zinv1 = zinv2;
-            for (nz = nzmin + 1; nz <= nzmax - 2; nz++) {
-                zinv2 = 1.0 / (ZN(nz) - ZN(nz + 1));
-                A a = -((A)kv[nz] * zinv1 * zinv * ((A)ar[nz] / (A)av[nz]));
-                c = -((A)kv[nz + 1] * zinv2 * zinv * (A)ar[nz + 1] / (A)av[nz]);
-                b = -a - c + (A)hn[nz];
-                zinv1 = zinv2;
-                if (wimpl) {  // :1176-1189
-                    A v = zinv * ((A)ar[nz] / (A)av[nz]);
-                    a = a + fmin(0.0, (A)wi[nz]) * v;
-                    b = b + fmax(0.0, (A)wi[nz]) * v;
-                    v = zinv * (A)ar[nz + 1] / (A)av[nz];
-                    b = b - fmin(0.0, (A)wi[nz + 1]) * v;
-                    c = c - fmax(0.0, (A)wi[nz + 1]) * v;
-                }
-                Tm = T0;
-                T0 = Tp1;
-                Tp1 = (A)Tc[nz + 1];
-                dz = (A)hn[nz];
-                rhs = -(a * Tm) - (b - dz) * T0 - c * Tp1;
-                const A m = b - cp * a;
-                cp = c / m;
-                tpv = (rhs - tpv * a) / m;
-                CP(nz) = cp;
-                TP(nz) = tpv;
-            }
-            nz = nzmax - 1;
-            {
-                A a = -((A)kv[nz] * zinv1 * zinv * ((A)ar[nz] / (A)av[nz]));
-                b = -a + (A)hn[nz];
-                if (wimpl) {  // :1207-1216
-                    const A v = zinv * ((A)ar[nz] / (A)av[nz]);
-                    a = a + fmin(0.0, (A)wi[nz]) * v;
-                    b = b + fmax(0.0, (A)wi[nz]) * v;
-                }
-                Tm = T0;
-                T0 = Tp1;
-                dz = (A)hn[nz];
-                rhs = -(a * Tm) - (b - dz) * T0;
-                const A m = b - cp * a;
-                tpv = (rhs - tpv * a) / m;
-            }
-            // back substitution (:1417-1430)
-            A trv = tpv;
-            Tc[nzmax - 1] = (R)((A)Tc[nzmax - 1] + trv);
-            for (nz = nzmax - 2; nz >= nzmin; nz--) {
-                trv = TP(nz) - CP(nz) * trv;
-                Tc[nz] = (R)((A)Tc[nz] + trv);
-            }
+            const double bc = f.bc ? (double)f.bc[(size_t)t * N2 + n] : 0.0;
+            vdiff_col_solve<R>(cs, nzmin, nzmax, hn, ar, av, kv, wimpl, wi, bc, dt, tr.T + t * tr.sN + (size_t)n * L1 - 1);
         }
     }
-#undef ZN
-#undef CP
-#undef TP
 }
 
 // ===========================================================================

@@ -13,28 +13,49 @@
 //
 // The scratch holds, per column, Z_n and the Thomas factors cp/tp, level-major;
 // every entry a call reads is written by the same call first, so nothing has to
-// start at zero.  All calls share the array: calls that overlap on the GPU
-// (different streams, or different host threads) race on it.
+// start at zero.  A status word beside it records columns whose level bounds the
+// kernel refused (it is cleared at the start of every call).  All calls share both:
+// calls that overlap on the GPU (different streams, or different host threads) race
+// on them.  A call waits, with a time limit, for its kernel and reads the status word
+// back, so it returns only when the values are final.
 //
-// Built with --fmad=false like the FP64 kernels, so the results equal those of
-// fesom_gpu_vdiff_impl bit for bit.
+// The column solve is the one k_vdiff<double> runs (vdiff_column.cuh), built with
+// --fmad=false in both places, so the results equal those of fesom_gpu_vdiff_impl bit
+// for bit.
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <thread>
 
 #include "../../include/fesom_gpu.h"
+#include "vdiff_column.cuh"
 
 namespace {
 
-// 3 arrays of (nl+1) levels per column: nod2D * (nl+1) * 3 <= this bound.
+using fesom::ColScratch;
+using fesom::vdiff_col_solve;
+using fesom::vdiff_col_z;
+
+// 3 arrays of nl levels per column (Z_n, cp, tp at levels 0 .. nl-1): nod2D * nl * 3 <= this bound.
 constexpr size_t kScratchDoubles = FESOM_GPU_NOALLOC_SCRATCH_DOUBLES;
 static __device__ __align__(256) double g_vdiff_scratch[kScratchDoubles];
+// FESOM_STATUS_* bits of the last call (cleared at the start of each call)
+static __device__ unsigned g_status;
 
 constexpr int kMaxDevices = 64;
+constexpr int kWaitLimitMs = 60000;
 std::mutex g_mu;
-double *g_scratch_addr[kMaxDevices] = {nullptr};
+// per device, looked up once with the device current: the device addresses of the two arrays
+// above, and an event the call waits on
+struct DevState {
+    double *scratch = nullptr;
+    unsigned *status = nullptr;
+    cudaEvent_t done = nullptr;
+};
+DevState g_dev[kMaxDevices];
 
 void set_err(char *errbuf, int32_t errlen, const char *msg) {
     if (errbuf && errlen > 0) {
@@ -43,85 +64,33 @@ void set_err(char *errbuf, int32_t errlen, const char *msg) {
     }
 }
 
-// diff_ver_part_impl_ale (src/oce_ale_tracer.F90:1071-1430) for one column per
-// thread; same statements and evaluation order as k_vdiff<double>.
+// diff_ver_part_impl_ale (src/oce_ale_tracer.F90:1071-1430) for one column per thread, the
+// column solve k_vdiff<double> uses.  The level arrays come from the caller and are not
+// validated on the host: a column outside 1 <= ulevels_nod2D, nlevels_nod2D <= nl with at least
+// two wet layers is skipped (its values untouched, nothing read or written outside the arrays)
+// and raises FESOM_STATUS_INDEX in g_status.
 __global__ void __launch_bounds__(128)
 k_vdiff_noalloc(int N2_, int nl, const int *__restrict__ nlev, const int *__restrict__ ulev,
                 const double *__restrict__ zbar_n_bot, const double *__restrict__ hnode_new,
                 const double *__restrict__ area, const double *__restrict__ areasvol, const double *__restrict__ Kv,
-                const double *__restrict__ bc_surf, double dt, double *__restrict__ values, double *scratch) {
-    typedef double A;
+                const double *__restrict__ bc_surf, double dt, double *__restrict__ values, double *scratch,
+                unsigned *status) {
     const int L1 = nl - 1;
     const size_t N2 = (size_t)N2_;
-    A *Zs = scratch, *cps = scratch + (size_t)(L1 + 1) * N2, *tps = cps + (size_t)(L1 + 1) * N2;
-#define ZN(k) Zs[(size_t)(k) * N2 + n]
-#define CP(k) cps[(size_t)(k) * N2 + n]
-#define TP(k) tps[(size_t)(k) * N2 + n]
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N2_; n += gridDim.x * blockDim.x) {
         const int nzmax = nlev[n], nzmin = ulev[n];
-        const A *hn = hnode_new + (size_t)n * L1 - 1;
-        const A *ar = area + (size_t)n * nl - 1;
-        const A *av = areasvol + (size_t)n * nl - 1;
-        const A *kv = Kv + (size_t)n * nl - 1;
-        A *Tc = values + (size_t)n * L1 - 1;
-        A zb = zbar_n_bot[n];
-        ZN(nzmax - 1) = zb + hn[nzmax - 1] / 2.0;
-        for (int nz = nzmax - 1; nz >= nzmin + 1; nz--) {
-            zb = zb + hn[nz];
-            ZN(nz - 1) = zb + hn[nz - 1] / 2.0;
+        if (nzmin < 1 || nzmax > nl || nzmax - nzmin < 2) {
+            atomicOr(status, FESOM_STATUS_INDEX);
+            continue;
         }
-        const A bc = bc_surf ? bc_surf[n] : 0.0;
-        int nz = nzmin;
-        A zinv2 = 1.0 / (ZN(nz) - ZN(nz + 1));
-        const A zinv = 1.0 * dt;
-        A c = -(kv[nz + 1] * zinv2 * zinv * ar[nz + 1] / av[nz]);
-        A b = -c + hn[nz];
-        A Tm = Tc[nz], T0 = Tm, Tp1 = Tc[nz + 1];
-        A dz = hn[nz];
-        A rhs = -((b - dz) * T0) - c * Tp1;
-        rhs = rhs + bc;
-        A cp = c / b, tpv = rhs / b;
-        CP(nz) = cp;
-        TP(nz) = tpv;
-        A zinv1 = zinv2;
-        for (nz = nzmin + 1; nz <= nzmax - 2; nz++) {
-            zinv2 = 1.0 / (ZN(nz) - ZN(nz + 1));
-            const A a = -(kv[nz] * zinv1 * zinv * (ar[nz] / av[nz]));
-            c = -(kv[nz + 1] * zinv2 * zinv * ar[nz + 1] / av[nz]);
-            b = -a - c + hn[nz];
-            zinv1 = zinv2;
-            Tm = T0;
-            T0 = Tp1;
-            Tp1 = Tc[nz + 1];
-            dz = hn[nz];
-            rhs = -(a * Tm) - (b - dz) * T0 - c * Tp1;
-            const A m = b - cp * a;
-            cp = c / m;
-            tpv = (rhs - tpv * a) / m;
-            CP(nz) = cp;
-            TP(nz) = tpv;
-        }
-        nz = nzmax - 1;
-        {
-            const A a = -(kv[nz] * zinv1 * zinv * (ar[nz] / av[nz]));
-            b = -a + hn[nz];
-            Tm = T0;
-            T0 = Tp1;
-            dz = hn[nz];
-            rhs = -(a * Tm) - (b - dz) * T0;
-            const A m = b - cp * a;
-            tpv = (rhs - tpv * a) / m;
-        }
-        A trv = tpv;
-        Tc[nzmax - 1] = Tc[nzmax - 1] + trv;
-        for (nz = nzmax - 2; nz >= nzmin; nz--) {
-            trv = TP(nz) - CP(nz) * trv;
-            Tc[nz] = Tc[nz] + trv;
-        }
+        const ColScratch cs{scratch + n, scratch + (size_t)(L1 + 1) * N2 + n, scratch + 2 * (size_t)(L1 + 1) * N2 + n,
+                            N2};
+        const double *hn = hnode_new + (size_t)n * L1 - 1;
+        vdiff_col_z<double>(cs, nzmin, nzmax, zbar_n_bot[n], hn);
+        vdiff_col_solve<double>(cs, nzmin, nzmax, hn, area + (size_t)n * nl - 1, areasvol + (size_t)n * nl - 1,
+                                Kv + (size_t)n * nl - 1, false, nullptr, bc_surf ? bc_surf[n] : 0.0, dt,
+                                values + (size_t)n * L1 - 1);
     }
-#undef ZN
-#undef CP
-#undef TP
 }
 
 }  // namespace
@@ -152,31 +121,70 @@ extern "C" int fesom_gpu_vdiff_impl_noalloc(int32_t nod2D, int32_t nl, const int
         set_err(errbuf, errlen, "fesom_gpu_vdiff_impl_noalloc: no current CUDA device");
         return FESOM_ERR_CUDA;
     }
-    double *scratch;
+    DevState st;
     {
-        // one-time set-up per device, with that device current: the host-side name of
-        // the array is not a device address, so fetch the address the kernel must use
+        // one-time set-up per device, with that device current: the host-side names of the
+        // arrays are not device addresses, so fetch the addresses the kernel must use
         std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_scratch_addr[dev]) {
-            void *p = nullptr;
+        DevState &d = g_dev[dev];
+        if (!d.scratch) {
+            void *p = nullptr, *q = nullptr;
             e = cudaGetSymbolAddress(&p, g_vdiff_scratch);
-            if (e != cudaSuccess || !p) {
+            if (e == cudaSuccess) e = cudaGetSymbolAddress(&q, g_status);
+            if (e == cudaSuccess && !d.done) e = cudaEventCreateWithFlags(&d.done, cudaEventDisableTiming);
+            if (e != cudaSuccess || !p || !q) {
                 set_err(errbuf, errlen, cudaGetErrorString(e));
                 return FESOM_ERR_CUDA;
             }
-            g_scratch_addr[dev] = (double *)p;
+            d.status = (unsigned *)q;
+            d.scratch = (double *)p;
         }
-        scratch = g_scratch_addr[dev];
+        st = d;
     }
-    const int threads = 128;
-    int blocks = (nod2D + threads - 1) / threads;
-    k_vdiff_noalloc<<<blocks, threads, 0, (cudaStream_t)stream>>>(nod2D, nl, nlevels_nod2D, ulevels_nod2D, zbar_n_bot,
-                                                                   hnode_new, area, areasvol, Kv, bc_surf, dt, values,
-                                                                   scratch);
-    e = cudaGetLastError();
+    cudaStream_t s = (cudaStream_t)stream;
+    e = cudaMemsetAsync(st.status, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) {
         set_err(errbuf, errlen, cudaGetErrorString(e));
         return FESOM_ERR_CUDA;
+    }
+    const int threads = 128;
+    int blocks = (nod2D + threads - 1) / threads;
+    k_vdiff_noalloc<<<blocks, threads, 0, s>>>(nod2D, nl, nlevels_nod2D, ulevels_nod2D, zbar_n_bot, hnode_new, area,
+                                               areasvol, Kv, bc_surf, dt, values, st.scratch, st.status);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventRecord(st.done, s);
+    if (e != cudaSuccess) {
+        set_err(errbuf, errlen, cudaGetErrorString(e));
+        return FESOM_ERR_CUDA;
+    }
+    // wait, with a time limit, for the kernel, then read its status word
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        e = cudaEventQuery(st.done);
+        if (e == cudaSuccess) break;
+        if (e != cudaErrorNotReady) {
+            set_err(errbuf, errlen, cudaGetErrorString(e));
+            return FESOM_ERR_CUDA;
+        }
+        const auto ms =
+            std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+        if (ms > kWaitLimitMs) {
+            set_err(errbuf, errlen, "fesom_gpu_vdiff_impl_noalloc: the solve did not finish within the time limit");
+            return FESOM_ERR_TIMEOUT;
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(ms < 10 ? 20 : 500));
+    }
+    unsigned bits = 0;
+    e = cudaMemcpy(&bits, st.status, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        set_err(errbuf, errlen, cudaGetErrorString(e));
+        return FESOM_ERR_CUDA;
+    }
+    if (bits & FESOM_STATUS_INDEX) {
+        set_err(errbuf, errlen,
+                "fesom_gpu_vdiff_impl_noalloc: a column outside 1 <= ulevels_nod2D, nlevels_nod2D <= nl with at least "
+                "two wet layers was skipped");
+        return FESOM_ERR_MESH;
     }
     return FESOM_OK;
 }

@@ -255,9 +255,14 @@ int fesom_gpu_launches_per_step(fesom_gpu_ctx *ctx, int32_t *launches);
  * 3*nl*nod2D above that are rejected with FESOM_ERR_ARG and a message in
  * errbuf.  The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress), so make that first call before any stream capture.
- * All calls share the scratch: calls that overlap on the GPU race.  The work
- * is queued on `stream` (a cudaStream_t, NULL = legacy stream); the caller
- * synchronizes. */
+ * Columns must satisfy 1 <= ulevels_nod2D(n), nlevels_nod2D(n) <= nl and
+ * nlevels_nod2D(n) - ulevels_nod2D(n) >= 2 (two wet layers); the kernel skips
+ * any other column, leaving its values untouched, and the call returns
+ * FESOM_ERR_MESH.  The work runs on `stream` (a cudaStream_t, NULL = legacy
+ * stream); the call waits for it (at most 60 s, else FESOM_ERR_TIMEOUT) and
+ * reads the kernel's status word back, so the values are final on return.
+ * All calls share the scratch and the status word: calls that overlap on the
+ * GPU (other streams, other host threads) race on them. */
 #define FESOM_GPU_NOALLOC_SCRATCH_DOUBLES ((size_t)4194304)
 int fesom_gpu_vdiff_impl_noalloc(int32_t nod2D, int32_t nl, const int32_t *nlevels_nod2D,
                                  const int32_t *ulevels_nod2D, const double *zbar_n_bot, const double *hnode_new,

@@ -8,6 +8,11 @@ calls the entry point through the C ABI twice in a row, and checks each result
 against the regular entry point (fesom_gpu_vdiff_impl) applied the same number
 of times: equal bit for bit, the tolerance of the other FP64 tests.
 
+The level arrays are the caller's and the entry point cannot check them on the
+host; a column with bad level bounds is skipped on the device and the call
+returns FESOM_ERR_MESH, which the last test checks on a values array with a
+sentinel tail inside its own allocation.
+
 This file is collected last, so a run that stops at the first failure has run
 every other test before it.
 """
@@ -89,3 +94,50 @@ def test_noalloc_vdiff_rejects_meshes_beyond_its_scratch():
                   one.data_ptr(), one.data_ptr(), None, 600.0, one.data_ptr(), None, err, 256)
     assert rc == 1
     assert b"too large" in err.value
+
+
+def test_noalloc_vdiff_skips_columns_with_bad_level_bounds():
+    """A one-layer column, a bottom level past nl and a top level below 1 are skipped and
+    reported as FESOM_ERR_MESH; the other columns equal the regular entry point's result,
+    the skipped ones and a sentinel tail behind the values are unchanged."""
+    torch = pytest.importorskip("torch")
+    mesh, f, T0 = _case()
+    ctx = G.Context(mesh, G.PREC_FP64)
+    want = T0.copy()
+    ctx.vdiff_impl(f, G.tra_cfg(), want)
+    ctx.close()
+
+    nlev = np.array(mesh.nlevels_nod2D, dtype=np.int32, copy=True)
+    ulev = np.array(mesh.ulevels_nod2D, dtype=np.int32, copy=True)
+    last = mesh.nod2D - 1
+    bad = {last: "one layer", 3: "below nl", 7: "top"}
+    nlev[last] = ulev[last] + 1          # one wet layer: the solve would read past the column
+    nlev[3] = mesh.nl + 1                # bottom level past nl
+    ulev[7] = 0                          # top level below 1
+    L1 = mesh.nl - 1
+    sentinel = 12345.5
+    tail = 4 * L1
+    vals = np.concatenate([np.ravel(T0), np.full(tail, sentinel)])  # T0[n, :] is column n
+
+    dev = torch.device("cuda:0")
+
+    def on_device(a, dtype):
+        return torch.from_numpy(np.ascontiguousarray(a, dtype=dtype)).to(dev)
+
+    dv = on_device(vals, np.float64)
+    args = [on_device(nlev, np.int32), on_device(ulev, np.int32), on_device(mesh.zbar_n_bot, np.float64),
+            on_device(mesh.hnode_new, np.float64), on_device(mesh.area, np.float64),
+            on_device(mesh.areasvol, np.float64), on_device(f.Kv, np.float64), on_device(f.bc_surface, np.float64)]
+    torch.cuda.synchronize()
+    err = C.create_string_buffer(256)
+    rc = _entry()(mesh.nod2D, mesh.nl, *[a.data_ptr() for a in args], float(f.dt), dv.data_ptr(), None, err, 256)
+    assert rc == 3, (rc, err.value)
+    assert b"skipped" in err.value
+    got = dv.cpu().numpy()
+    assert np.all(got[-tail:] == sentinel)
+    got = got[:-tail].reshape(np.shape(T0))
+    for n in range(mesh.nod2D):
+        if n in bad:
+            assert np.array_equal(got[n], T0[n]), bad[n]
+        else:
+            assert np.array_equal(got[n], want[n])
