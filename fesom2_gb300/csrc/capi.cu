@@ -52,23 +52,33 @@ struct fesom_gpu_ctx {
     bool forcing_ready = false;
     bool state_ready = false;
     int wsplit = 0;            // dynamics%use_wsplit (fesom_gpu_set_wsplit)
-    // FP32 form: tracers per launch of the node stages (lo_ad, ho, bounds, update); 0 = the
-    // whole launch group.  Fewer tracers per pass keep the neighbour columns of the nodes in
-    // flight inside L2 (fesom_gpu_set_stage_tracers)
-    int stage_tr[4] = {0, 0, 6, 6};
+    // FP32 form: tracers per launch of the node stages (lo_ad, ho, bounds, update), rounded up
+    // to whole tracer groups; 0 = the whole launch group in one launch
+    // (fesom_gpu_set_stage_tracers)
+    int stage_tr[4] = {0, 0, 0, 0};
     // tracer groups of fesom_gpu_step_host_f32, in order (fesom_gpu_set_host_groups);
     // empty: the automatic ramp of host_groups()
     std::vector<int> host_groups;
     cudaGraphExec_t gexec = nullptr;
     double g_dt = 0.0;
-    // FP32 batched form: rotating time-level buffers and its work arrays
+    // FP32 batched form: tracers in groups of gw slots of one scheme (B32View), rotating
+    // time-level buffers and the work arrays of one launch group
+    int gw = 4;                          // slots per tracer group
+    int gw_req = 0;                      // width asked for by fesom_gpu_set_tracer_width (0: automatic)
+    int ngr = 0;                         // tracer groups
+    std::vector<int> slot_g, slot_c;     // tracer t -> its group and slot in the group
+    std::vector<int> gfirst;             // a tracer of each group (the group's scheme)
+    std::vector<int> slot_tr;            // tracer of each slot (ngr * gw, -1: empty)
     float *Bf[3] = {nullptr, nullptr, nullptr};
     int rot = 0;
     float *VF = nullptr;
     VFactors vfac{};
     float *LO32 = nullptr, *ADv32 = nullptr, *ADh32 = nullptr;
-    float *HD32 = nullptr;  // horizontal diffusion flux per edge-layer and tracer of a launch group
-    float2 *R2 = nullptr, *TB2 = nullptr;
+    float *HD32 = nullptr;  // horizontal diffusion flux per edge-layer of a launch group
+    float *Rp32 = nullptr, *Rm32 = nullptr, *Bp32 = nullptr, *Bm32 = nullptr;
+    float *pack_in = nullptr, *pack_out = nullptr;  // staging of the host-array step (FP32 columns)
+    size_t pack_n = 0;                   // floats each staging buffer holds
+    LaunchShape shape[4];                // lo_ad, ho, bounds, update (the autotuner's choice)
     MusclW mw{};
     cudaGraphExec_t gexec32[3] = {nullptr, nullptr, nullptr};
     double g32_dt[3] = {0.0, 0.0, 0.0};
@@ -170,71 +180,97 @@ int get(fesom_gpu_ctx *ctx, double *dst, const void *src, size_t n) {
     return FESOM_OK;
 }
 
-// valuesold of AB3 interleaves its two levels, valuesold(k, nz, n): split into / join
-// from the two level buffers of the FP32 form (through the stage buffer)
-__global__ void k_deint_d2f(const double *in, float *o1, float *o2, size_t n) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        o1[i] = (float)in[2 * i];
-        o2[i] = (float)in[2 * i + 1];
-    }
-}
-__global__ void k_int_f2d(const float *o1, const float *o2, double *out, size_t n) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        out[2 * i] = (double)o1[i];
-        out[2 * i + 1] = (double)o2[i];
-    }
-}
-__global__ void k_deint_f(const float *in, float *o1, float *o2, size_t n) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        o1[i] = in[2 * i];
-        o2[i] = in[2 * i + 1];
-    }
-}
-__global__ void k_int_f(const float *o1, const float *o2, float *out, size_t n) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        out[2 * i] = o1[i];
-        out[2 * i + 1] = o2[i];
-    }
-}
 static int nblk(size_t m) { return (int)std::min<size_t>((m + 255) / 256, 152 * 32); }
 
-int put_deint(fesom_gpu_ctx *ctx, float *o1, float *o2, const double *src, size_t n) {
-    const size_t ch = ctx->stage_n / 2;
-    for (size_t off = 0; off < n; off += ch) {
-        size_t m = std::min(ch, n - off);
-        CK(cudaMemcpyAsync(ctx->stage, src + 2 * off, 2 * m * sizeof(double), cudaMemcpyDefault, ctx->stream));
-        k_deint_d2f<<<nblk(m), 256, 0, ctx->stream>>>(ctx->stage, o1 + off, o2 + off, m);
+// One tracer's column-major array (host or device; FP64 or FP32) into / out of its slot of a
+// group field of the FP32 form, through the stage buffer (chunks of stage_n doubles or
+// 2 stage_n floats).  `count` entries; pair: AB3's interleaved valuesold(2, level, node) into
+// / out of the group fields g1 (k = 1) and g2 (k = 2).
+int put_slot(fesom_gpu_ctx *ctx, float *grpf, int c, const double *src, size_t count) {
+    if (!src) return FESOM_OK;
+    for (size_t off = 0; off < count; off += ctx->stage_n) {
+        const size_t m = std::min(ctx->stage_n, count - off);
+        CK(cudaMemcpyAsync(ctx->stage, src + off, m * sizeof(double), cudaMemcpyDefault, ctx->stream));
+        b32_put_slot(ctx->stage, grpf + off * ctx->gw, ctx->gw, c, m, ctx->stream);
         CK(cudaGetLastError());
     }
     return FESOM_OK;
 }
-int get_int(fesom_gpu_ctx *ctx, double *dst, const float *o1, const float *o2, size_t n) {
+int put_slot_f(fesom_gpu_ctx *ctx, float *grpf, int c, const float *src, size_t count) {
+    if (!src) return FESOM_OK;
+    float *st = (float *)ctx->stage;
+    const size_t ch = 2 * ctx->stage_n;
+    for (size_t off = 0; off < count; off += ch) {
+        const size_t m = std::min(ch, count - off);
+        CK(cudaMemcpyAsync(st, src + off, m * sizeof(float), cudaMemcpyDefault, ctx->stream));
+        b32_put_slot_f(st, grpf + off * ctx->gw, ctx->gw, c, m, ctx->stream);
+        CK(cudaGetLastError());
+    }
+    return FESOM_OK;
+}
+int get_slot(fesom_gpu_ctx *ctx, double *dst, const float *grpf, int c, size_t count) {
+    if (!dst) return FESOM_OK;
+    for (size_t off = 0; off < count; off += ctx->stage_n) {
+        const size_t m = std::min(ctx->stage_n, count - off);
+        b32_get_slot(grpf + off * ctx->gw, ctx->gw, c, m, ctx->stage, ctx->stream);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(dst + off, ctx->stage, m * sizeof(double), cudaMemcpyDefault, ctx->stream));
+    }
+    return FESOM_OK;
+}
+int get_slot_f(fesom_gpu_ctx *ctx, float *dst, const float *grpf, int c, size_t count) {
+    if (!dst) return FESOM_OK;
+    float *st = (float *)ctx->stage;
+    const size_t ch = 2 * ctx->stage_n;
+    for (size_t off = 0; off < count; off += ch) {
+        const size_t m = std::min(ch, count - off);
+        b32_get_slot_f(grpf + off * ctx->gw, ctx->gw, c, m, st, ctx->stream);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(dst + off, st, m * sizeof(float), cudaMemcpyDefault, ctx->stream));
+    }
+    return FESOM_OK;
+}
+int put_slot_pair(fesom_gpu_ctx *ctx, float *g1, float *g2, int c, const double *src, size_t count) {
+    if (!src) return FESOM_OK;
     const size_t ch = ctx->stage_n / 2;
-    for (size_t off = 0; off < n; off += ch) {
-        size_t m = std::min(ch, n - off);
-        k_int_f2d<<<nblk(m), 256, 0, ctx->stream>>>(o1 + off, o2 + off, ctx->stage, m);
+    for (size_t off = 0; off < count; off += ch) {
+        const size_t m = std::min(ch, count - off);
+        CK(cudaMemcpyAsync(ctx->stage, src + 2 * off, 2 * m * sizeof(double), cudaMemcpyDefault, ctx->stream));
+        b32_put_slot_pair(ctx->stage, g1 + off * ctx->gw, g2 + off * ctx->gw, ctx->gw, c, m, ctx->stream);
+        CK(cudaGetLastError());
+    }
+    return FESOM_OK;
+}
+int put_slot_pair_f(fesom_gpu_ctx *ctx, float *g1, float *g2, int c, const float *src, size_t count) {
+    if (!src) return FESOM_OK;
+    float *st = (float *)ctx->stage;
+    const size_t ch = ctx->stage_n;
+    for (size_t off = 0; off < count; off += ch) {
+        const size_t m = std::min(ch, count - off);
+        CK(cudaMemcpyAsync(st, src + 2 * off, 2 * m * sizeof(float), cudaMemcpyDefault, ctx->stream));
+        b32_put_slot_pair_f(st, g1 + off * ctx->gw, g2 + off * ctx->gw, ctx->gw, c, m, ctx->stream);
+        CK(cudaGetLastError());
+    }
+    return FESOM_OK;
+}
+int get_slot_pair(fesom_gpu_ctx *ctx, double *dst, const float *g1, const float *g2, int c, size_t count) {
+    if (!dst) return FESOM_OK;
+    const size_t ch = ctx->stage_n / 2;
+    for (size_t off = 0; off < count; off += ch) {
+        const size_t m = std::min(ch, count - off);
+        b32_get_slot_pair(g1 + off * ctx->gw, g2 + off * ctx->gw, ctx->gw, c, m, ctx->stage, ctx->stream);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(dst + 2 * off, ctx->stage, 2 * m * sizeof(double), cudaMemcpyDefault, ctx->stream));
     }
     return FESOM_OK;
 }
-int put_deint_f(fesom_gpu_ctx *ctx, float *o1, float *o2, const float *src, size_t n) {
-    float *st = (float *)ctx->stage;
-    const size_t ch = ctx->stage_n;  // 2*ch floats fit the stage
-    for (size_t off = 0; off < n; off += ch) {
-        size_t m = std::min(ch, n - off);
-        CK(cudaMemcpyAsync(st, src + 2 * off, 2 * m * sizeof(float), cudaMemcpyDefault, ctx->stream));
-        k_deint_f<<<nblk(m), 256, 0, ctx->stream>>>(st, o1 + off, o2 + off, m);
-        CK(cudaGetLastError());
-    }
-    return FESOM_OK;
-}
-int get_int_f(fesom_gpu_ctx *ctx, float *dst, const float *o1, const float *o2, size_t n) {
+int get_slot_pair_f(fesom_gpu_ctx *ctx, float *dst, const float *g1, const float *g2, int c, size_t count) {
+    if (!dst) return FESOM_OK;
     float *st = (float *)ctx->stage;
     const size_t ch = ctx->stage_n;
-    for (size_t off = 0; off < n; off += ch) {
-        size_t m = std::min(ch, n - off);
-        k_int_f<<<nblk(m), 256, 0, ctx->stream>>>(o1 + off, o2 + off, st, m);
+    for (size_t off = 0; off < count; off += ch) {
+        const size_t m = std::min(ch, count - off);
+        b32_get_slot_pair_f(g1 + off * ctx->gw, g2 + off * ctx->gw, ctx->gw, c, m, st, ctx->stream);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(dst + 2 * off, st, 2 * m * sizeof(float), cudaMemcpyDefault, ctx->stream));
     }
@@ -515,8 +551,6 @@ template <typename R>
 const DGeom<R> &geom(fesom_gpu_ctx *ctx);
 template <>
 const DGeom<double> &geom<double>(fesom_gpu_ctx *ctx) { return ctx->g64; }
-template <>
-const DGeom<float> &geom<float>(fesom_gpu_ctx *ctx) { return ctx->g32; }
 
 // One tracer step for tracers [0, ntr): per group init_tracers_AB, gradients,
 // edge fluxes, LO + vertical fluxes, FCT bounds, R+/R-, limited update with
@@ -535,43 +569,93 @@ void free_graphs32(fesom_gpu_ctx *ctx) {
         if (g) { cudaGraphExecDestroy(g); g = nullptr; }
 }
 
-int alloc_state32(fesom_gpu_ctx *ctx, int ntr, int ab) {
+// Tracer groups of the FP32 form: tracers of one scheme (limiter, horizontal and vertical
+// scheme, implicit vertical diffusion) share a group of G slots, filled in tracer order.
+bool same_scheme(const fesom_tra_cfg &a, const fesom_tra_cfg &b) {
+    return a.adv_hor == b.adv_hor && a.adv_ver == b.adv_ver && a.adv_lim == b.adv_lim &&
+           a.i_vert_diff == b.i_vert_diff;
+}
+// groups of width G for the tracer schemes cf; slot (group, place) of each tracer
+int place_tracers(const std::vector<fesom_tra_cfg> &cf, int G, std::vector<int> *sg, std::vector<int> *sc,
+                  std::vector<int> *first) {
+    std::vector<int> fill, gf;
+    if (sg) sg->assign(cf.size(), 0);
+    if (sc) sc->assign(cf.size(), 0);
+    for (size_t t = 0; t < cf.size(); t++) {
+        int g = -1;
+        for (size_t k = 0; k < gf.size() && g < 0; k++)
+            if (fill[k] < G && same_scheme(cf[gf[k]], cf[t])) g = (int)k;
+        if (g < 0) {
+            g = (int)gf.size();
+            gf.push_back((int)t);
+            fill.push_back(0);
+        }
+        if (sg) (*sg)[t] = g;
+        if (sc) (*sc)[t] = fill[g];
+        fill[g]++;
+    }
+    if (first) *first = gf;
+    return (int)gf.size();
+}
+// the group width: as asked, else the one with the fewest slots (4 on a tie)
+void assign_groups(fesom_gpu_ctx *ctx, const std::vector<fesom_tra_cfg> &cf) {
+    int G = ctx->gw_req;
+    if (G != 2 && G != 4) G = 2 * place_tracers(cf, 2, nullptr, nullptr, nullptr) < 4 * place_tracers(cf, 4, nullptr, nullptr, nullptr) ? 2 : 4;
+    ctx->gw = G;
+    ctx->ngr = place_tracers(cf, G, &ctx->slot_g, &ctx->slot_c, &ctx->gfirst);
+    ctx->slot_tr.assign((size_t)ctx->ngr * G, -1);
+    for (size_t t = 0; t < cf.size(); t++) ctx->slot_tr[(size_t)ctx->slot_g[t] * G + ctx->slot_c[t]] = (int)t;
+}
+
+int alloc_state32(fesom_gpu_ctx *ctx, int ab) {
     const size_t sN = (size_t)ctx->L1 * ctx->N2, sNI = (size_t)ctx->nl * ctx->N2, sE = (size_t)ctx->L1 * ctx->E2;
+    const int G = ctx->gw, ngr = ctx->ngr;
     void *old[] = {ctx->Bf[0], ctx->Bf[1], ctx->Bf[2], ctx->VF, ctx->vfac.a, ctx->vfac.c, ctx->vfac.inv, ctx->vfac.cp,
-                   ctx->LO32, ctx->ADv32, ctx->ADh32, ctx->R2, ctx->TB2, ctx->d_cfg, ctx->bc, ctx->HD32};
+                   ctx->LO32, ctx->ADv32, ctx->ADh32, ctx->Rp32, ctx->Rm32, ctx->Bp32, ctx->Bm32, ctx->d_cfg, ctx->bc,
+                   ctx->HD32, ctx->partials, ctx->content_out, ctx->pack_in, ctx->pack_out};
     for (void *b : old) { void *p = b; dfree(ctx, p); }
     ctx->Bf[0] = ctx->Bf[1] = ctx->Bf[2] = nullptr;
     ctx->VF = ctx->LO32 = ctx->ADv32 = ctx->ADh32 = ctx->HD32 = nullptr;
-    ctx->R2 = ctx->TB2 = nullptr;
+    ctx->Rp32 = ctx->Rm32 = ctx->Bp32 = ctx->Bm32 = nullptr;
+    ctx->pack_in = ctx->pack_out = nullptr;
+    ctx->pack_n = 0;
+    ctx->partials = ctx->content_out = nullptr;
     ctx->vfac = VFactors{};
     ctx->d_cfg = nullptr;
     ctx->bc = nullptr;
     free_graphs32(ctx);
     int rc;
+    const size_t lev = 4 * sN * G * (size_t)ngr;  // bytes of one time level of every group
     for (int k = 0; k < ab; k++)
-        if ((rc = dalloc(ctx, (void **)&ctx->Bf[k], 4 * sN * ntr))) return rc;
-    for (int k = 0; k < ab; k++) CK(cudaMemset(ctx->Bf[k], 0, 4 * sN * ntr));
-    if ((rc = dalloc(ctx, &ctx->bc, 4 * (size_t)ctx->N2 * ntr))) return rc;
-    CK(cudaMemset(ctx->bc, 0, 4 * (size_t)ctx->N2 * ntr));
-    if ((rc = dalloc(ctx, (void **)&ctx->d_cfg, sizeof(DCfg) * ntr))) return rc;
+        if ((rc = dalloc(ctx, (void **)&ctx->Bf[k], lev))) return rc;
+    for (int k = 0; k < ab; k++) CK(cudaMemset(ctx->Bf[k], 0, lev));
+    if ((rc = dalloc(ctx, &ctx->bc, 4 * (size_t)ctx->N2 * G * ngr))) return rc;
+    CK(cudaMemset(ctx->bc, 0, 4 * (size_t)ctx->N2 * G * ngr));
+    if ((rc = dalloc(ctx, (void **)&ctx->d_cfg, sizeof(DCfg) * std::max<size_t>(1, ctx->cfgs.size())))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->partials, sizeof(double) * (size_t)ctx->content_blocks * ngr * G))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->content_out, sizeof(double) * (size_t)ngr * G))) return rc;
     if ((rc = dalloc(ctx, (void **)&ctx->VF, 4 * sE))) return rc;
     float **fac[] = {&ctx->vfac.a, &ctx->vfac.c, &ctx->vfac.inv, &ctx->vfac.cp};
     for (float **f : fac)
         if ((rc = dalloc(ctx, (void **)f, 4 * sN))) return rc;
-    // LO, (R+,R-), bounds, ADv, ADh (+ the horizontal diffusion fluxes)
-    const size_t per_tracer = 4 * (5 * sN + sNI + sE + (ctx->Ki ? sE : 0));
+    // LO, R+, R-, the two bounds, ADv, ADh (+ the horizontal diffusion fluxes) per group
+    const size_t per_group = 4 * (size_t)G * (5 * sN + sNI + sE + (ctx->Ki ? sE : 0));
     size_t fr = 0, tot = 0;
     CK(cudaMemGetInfo(&fr, &tot));
-    // at most 64 tracers per launch: the kernels take per-tracer switches as 64-bit masks
-    const int g = (int)std::min<size_t>(std::min<size_t>((size_t)ntr, 64),
-                                        std::max<size_t>(1, (size_t)(0.85 * fr) / per_tracer));
+    // at most kMaxSlots slots and kMaxGroups groups per launch (per-slot kernel parameters)
+    const int gmax = std::min(kMaxGroups, kMaxSlots / G);
+    const int g = (int)std::min<size_t>(std::min<size_t>((size_t)ngr, (size_t)gmax),
+                                        std::max<size_t>(1, (size_t)(0.85 * fr) / per_group));
     ctx->group = ctx->group_cap = g;
-    if ((rc = dalloc(ctx, (void **)&ctx->LO32, 4 * sN * g))) return rc;
-    if ((rc = dalloc(ctx, (void **)&ctx->ADv32, 4 * sNI * g))) return rc;
-    if ((rc = dalloc(ctx, (void **)&ctx->ADh32, 4 * sE * g))) return rc;
-    if ((rc = dalloc(ctx, (void **)&ctx->R2, 8 * sN * g))) return rc;
-    if ((rc = dalloc(ctx, (void **)&ctx->TB2, 8 * sN * g))) return rc;
-    if (ctx->Ki && (rc = dalloc(ctx, (void **)&ctx->HD32, 4 * sE * g))) return rc;
+    const size_t wg = 4 * (size_t)G * g;
+    if ((rc = dalloc(ctx, (void **)&ctx->LO32, wg * sN))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->ADv32, wg * sNI))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->ADh32, wg * sE))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->Rp32, wg * sN))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->Rm32, wg * sN))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->Bp32, wg * sN))) return rc;
+    if ((rc = dalloc(ctx, (void **)&ctx->Bm32, wg * sN))) return rc;
+    if (ctx->Ki && (rc = dalloc(ctx, (void **)&ctx->HD32, wg * sE))) return rc;
     // created here, not on first use: a first step may run inside a stream capture
     if (!ctx->side) {
         CK(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
@@ -582,85 +666,97 @@ int alloc_state32(fesom_gpu_ctx *ctx, int ntr, int ab) {
         CK(cudaEventCreateWithFlags(&ctx->ev_forcing, cudaEventDisableTiming));
     }
     ctx->rot = 0;
-    ctx->ntr = ntr;
     ctx->ab_max = ab;
     ctx->state_ready = true;
     return FESOM_OK;
 }
 
-B32View view32(fesom_gpu_ctx *ctx, int t0, int nt) {
+// groups [g0, g0 + ng) of the tracer state; the work arrays hold the launch group from 0
+B32View view32(fesom_gpu_ctx *ctx, int g0, int ng) {
+    const int G = ctx->gw;
     B32View v{};
-    v.ntr = nt;
+    v.ng = ng;
     v.ab = ctx->ab_max;
+    v.G = G;
     v.sN = (size_t)ctx->L1 * ctx->N2;
     v.sNI = (size_t)ctx->nl * ctx->N2;
     v.sE = (size_t)ctx->L1 * ctx->E2;
-    v.T = level32(ctx, 0) + t0 * v.sN;
-    v.O1 = level32(ctx, 1) + t0 * v.sN;
-    v.O2 = ctx->ab_max == 3 ? level32(ctx, 2) + t0 * v.sN : nullptr;
-    v.Tnew = level32(ctx, ctx->ab_max - 1) + t0 * v.sN;
+    const size_t go = (size_t)g0 * v.sN * G;
+    v.T = level32(ctx, 0) + go;
+    v.O1 = level32(ctx, 1) + go;
+    v.O2 = ctx->ab_max == 3 ? level32(ctx, 2) + go : nullptr;
+    v.Tnew = level32(ctx, ctx->ab_max - 1) + go;
     v.LO = ctx->LO32;
     v.ADv = ctx->ADv32;
     v.ADh = ctx->ADh32;
-    v.R = ctx->R2;
-    v.TB = ctx->TB2;
-    v.cfg = ctx->d_cfg + t0;
+    v.Rp = ctx->Rp32;
+    v.Rm = ctx->Rm32;
+    v.Bp = ctx->Bp32;
+    v.Bm = ctx->Bm32;
     v.status = ctx->status;
-    v.fct_mask = v.ivd_mask = v.diff_mask = v.ppm_mask = v.wimpl_mask = 0;
+    v.fct = v.ivd = v.diff = v.ppm = v.wimpl = 0;
     v.Ki = (const float *)ctx->Ki;
     v.HD = ctx->Ki ? ctx->HD32 : nullptr;
     v.Kv = (const float *)ctx->Kv;
     v.sF = ctx->N2;
-    v.fsurf = ctx->bc ? (const float *)ctx->bc + (size_t)t0 * ctx->N2 : nullptr;
-    for (int t = 0; t < nt; t++) {
-        const fesom_tra_cfg &c = ctx->cfgs[t0 + t];
-        if (c.adv_lim == FESOM_ADV_LIM_FCT) v.fct_mask |= 1ull << t;
-        if (c.i_vert_diff) v.ivd_mask |= 1ull << t;
-        if (ctx->Ki || !c.i_vert_diff) v.diff_mask |= 1ull << t;
-        if (c.adv_ver == FESOM_ADV_VER_PPM) v.ppm_mask |= 1ull << t;
-        if (ctx->wsplit && c.i_vert_diff && c.adv_lim != FESOM_ADV_LIM_FCT) v.wimpl_mask |= 1ull << t;
-        v.hor[t] = (signed char)c.adv_hor;
-        v.ver[t] = (signed char)c.adv_ver;
-        v.ph[t] = (float)c.adv_ph;
-        v.pv[t] = (float)c.adv_pv;
+    v.fsurf = ctx->bc ? (const float *)ctx->bc + (size_t)g0 * ctx->N2 * G : nullptr;
+    for (int g = 0; g < ng; g++) {
+        const fesom_tra_cfg &c = ctx->cfgs[ctx->gfirst[g0 + g]];
+        if (c.adv_lim == FESOM_ADV_LIM_FCT) v.fct |= 1ull << g;
+        if (c.i_vert_diff) v.ivd |= 1ull << g;
+        if (ctx->Ki || !c.i_vert_diff) v.diff |= 1ull << g;
+        if (c.adv_ver == FESOM_ADV_VER_PPM) v.ppm |= 1ull << g;
+        if (ctx->wsplit && c.i_vert_diff && c.adv_lim != FESOM_ADV_LIM_FCT) v.wimpl |= 1ull << g;
+        v.hor[g] = (signed char)c.adv_hor;
+        v.ver[g] = (signed char)c.adv_ver;
+        for (int k = 0; k < G; k++) {
+            const int t = ctx->slot_tr[(size_t)(g0 + g) * G + k];
+            v.ph[g * G + k] = t >= 0 ? (float)ctx->cfgs[t].adv_ph : 0.f;
+            v.pv[g * G + k] = t >= 0 ? (float)ctx->cfgs[t].adv_pv : 0.f;
+        }
     }
     return v;
 }
 
-// tracers [s0, s0 + ns) of a launch group
+// groups [s0, s0 + ns) of a launch group
 B32View sub32(const B32View &B, int s0, int ns) {
     B32View v = B;
-    v.ntr = ns;
-    v.T += s0 * B.sN;
-    v.O1 += s0 * B.sN;
-    if (v.O2) v.O2 += s0 * B.sN;
-    v.Tnew += s0 * B.sN;
-    v.LO += s0 * B.sN;
-    v.ADv += s0 * B.sNI;
-    v.ADh += s0 * B.sE;
-    v.R += s0 * B.sN;
-    v.TB += s0 * B.sN;
-    v.cfg += s0;
-    v.fct_mask = B.fct_mask >> s0;
-    v.ivd_mask = B.ivd_mask >> s0;
-    v.diff_mask = B.diff_mask >> s0;
-    v.ppm_mask = B.ppm_mask >> s0;
-    v.wimpl_mask = B.wimpl_mask >> s0;
-    if (v.HD) v.HD += s0 * B.sE;
-    if (v.fsurf) v.fsurf += s0 * B.sF;
-    for (int t = 0; t < ns; t++) {
-        v.hor[t] = B.hor[s0 + t];
-        v.ver[t] = B.ver[s0 + t];
-        v.ph[t] = B.ph[s0 + t];
-        v.pv[t] = B.pv[s0 + t];
+    const size_t G = B.G;
+    v.ng = ns;
+    v.T += s0 * B.sN * G;
+    v.O1 += s0 * B.sN * G;
+    if (v.O2) v.O2 += s0 * B.sN * G;
+    v.Tnew += s0 * B.sN * G;
+    v.LO += s0 * B.sN * G;
+    v.ADv += s0 * B.sNI * G;
+    v.ADh += s0 * B.sE * G;
+    v.Rp += s0 * B.sN * G;
+    v.Rm += s0 * B.sN * G;
+    v.Bp += s0 * B.sN * G;
+    v.Bm += s0 * B.sN * G;
+    v.fct = B.fct >> s0;
+    v.ivd = B.ivd >> s0;
+    v.diff = B.diff >> s0;
+    v.ppm = B.ppm >> s0;
+    v.wimpl = B.wimpl >> s0;
+    if (v.HD) v.HD += s0 * B.sE * G;
+    if (v.fsurf) v.fsurf += s0 * B.sF * G;
+    for (int g = 0; g < ns; g++) {
+        v.hor[g] = B.hor[s0 + g];
+        v.ver[g] = B.ver[s0 + g];
+    }
+    for (int k = 0; k < ns * B.G; k++) {
+        v.ph[k] = B.ph[s0 * B.G + k];
+        v.pv[k] = B.pv[s0 * B.G + k];
     }
     return v;
 }
 
-// tracers per launch of node stage k of a launch group of nt tracers
-inline int stage_group(const fesom_gpu_ctx *ctx, int k, int nt) {
-    const int g = ctx->stage_tr[k];
-    return g > 0 && g < nt ? g : nt;
+// groups per launch of node stage k of a launch group of ng groups (stage_tr in tracers)
+inline int stage_group(const fesom_gpu_ctx *ctx, int k, int ng) {
+    const int t = ctx->stage_tr[k];
+    const int g = t > 0 ? (t + ctx->gw - 1) / ctx->gw : ng;
+    return g < ng ? g : ng;
 }
 
 struct StageTimer {
@@ -738,49 +834,50 @@ int enqueue_shared32(fesom_gpu_ctx *ctx, double dt, StageTimer *tm, bool &fork) 
     return FESOM_OK;
 }
 
-// the stages of tracers [t0, t0 + nt); `joined` records that the stream already waited
-// for the factors of the side stream
-int enqueue_group32(fesom_gpu_ctx *ctx, double dt, int t0, int nt, StageTimer *tm, bool fork, bool &joined) {
+// the stages of groups [g0, g0 + ng); `joined` records that the stream already waited for
+// the factors of the side stream
+int enqueue_group32(fesom_gpu_ctx *ctx, double dt, int g0, int ng, StageTimer *tm, bool fork, bool &joined) {
     const DGeom<float> &g = ctx->g32;
-    B32View B = view32(ctx, t0, nt);
-    DForcing<float> fg = forcing_view<float>(ctx, t0);
-    bool any_fct = false;
-    for (int t = t0; t < t0 + nt; t++) any_fct |= ctx->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
+    B32View B = view32(ctx, g0, ng);
+    DForcing<float> fg = forcing_view<float>(ctx, 0);
+    const bool any_fct = B.fct != 0;
     {
-        const int sg = stage_group(ctx, 0, nt);
-        for (int s0 = 0; s0 < nt; s0 += sg)
-            STAGE(10, b32_lo_ad(ctx->tp, g, fg, sub32(B, s0, std::min(sg, nt - s0)), ctx->VF, dt, ctx->stream));
+        const int sg = stage_group(ctx, 0, ng);
+        for (int s0 = 0; s0 < ng; s0 += sg)
+            STAGE(10, b32_lo_ad(ctx->tp, g, fg, sub32(B, s0, std::min(sg, ng - s0)), ctx->VF, dt, ctx->shape[0],
+                                ctx->stream));
     }
-    if (B.ppm_mask) STAGE(10, b32_vppm(ctx->tp, g, fg, B, dt, ctx->stream));
+    if (B.ppm) STAGE(10, b32_vppm(ctx->tp, g, fg, B, dt, ctx->stream));
     // split vertical velocity: w_i advects the LO values implicitly (oce_adv_tra_driver.F90:323-334)
     if (ctx->wsplit && any_fct) STAGE(10, b32_lo_impl(ctx->tp, g, fg, B, dt, ctx->scratch, ctx->stream));
     {
-        const int sg = stage_group(ctx, 1, nt);
-        for (int s0 = 0; s0 < nt; s0 += sg)
-            STAGE(2, b32_ho(ctx->tp, g, sub32(B, s0, std::min(sg, nt - s0)), ctx->mw, ctx->VF, ctx->stream));
+        const int sg = stage_group(ctx, 1, ng);
+        for (int s0 = 0; s0 < ng; s0 += sg)
+            STAGE(2, b32_ho(ctx->tp, g, sub32(B, s0, std::min(sg, ng - s0)), ctx->mw, ctx->VF, ctx->shape[1],
+                            ctx->stream));
     }
     // diff_tracers_ale from the values before the update; the increment waits in Tnew (the
     // oldest level, read by lo_ad and ho only) for the update to add it after the limiter
     if (B.Ki) STAGE(2, b32_hdiff(ctx->tp, g, B, ctx->stream));
-    if (B.diff_mask) STAGE(7, b32_diff(ctx->tp, g, B, dt, ctx->stream));
+    if (B.diff) STAGE(7, b32_diff(ctx->tp, g, B, dt, ctx->stream));
     if (any_fct) {
-        const int bg = stage_group(ctx, 2, nt);
-        for (int s0 = 0; s0 < nt; s0 += bg)
-            STAGE(4, b32_bounds(ctx->tp, g, sub32(B, s0, std::min(bg, nt - s0)), dt, ctx->stream));
+        const int bg = stage_group(ctx, 2, ng);
+        for (int s0 = 0; s0 < ng; s0 += bg)
+            STAGE(4, b32_bounds(ctx->tp, g, sub32(B, s0, std::min(bg, ng - s0)), dt, ctx->shape[2], ctx->stream));
     }
     {
-        const int sg = stage_group(ctx, 3, nt);
-        for (int s0 = 0; s0 < nt; s0 += sg)
-            STAGE(6, b32_update(ctx->tp, g, sub32(B, s0, std::min(sg, nt - s0)), dt, ctx->stream));
+        const int sg = stage_group(ctx, 3, ng);
+        for (int s0 = 0; s0 < ng; s0 += sg)
+            STAGE(6, b32_update(ctx->tp, g, sub32(B, s0, std::min(sg, ng - s0)), dt, ctx->shape[3], ctx->stream));
     }
-    if (B.ivd_mask) {
+    if (B.ivd & ~B.wimpl) {
         if (fork && !joined) {
             CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
             joined = true;
         }
         STAGE(7, b32_vdiff(ctx->tp, fg, B, ctx->vfac, ctx->stream));
     }
-    if (B.wimpl_mask) STAGE(7, b32_vdiff_w(ctx->tp, g, fg, B, dt, ctx->scratch, ctx->stream));
+    if (B.wimpl) STAGE(7, b32_vdiff_w(ctx->tp, g, fg, B, dt, ctx->scratch, ctx->stream));
     return FESOM_OK;
 }
 
@@ -788,8 +885,8 @@ int enqueue_step32(fesom_gpu_ctx *ctx, double dt, StageTimer *tm = nullptr) {
     bool fork = false, joined = false;
     int rc = enqueue_shared32(ctx, dt, tm, fork);
     if (rc) return rc;
-    for (int t0 = 0; t0 < ctx->ntr; t0 += ctx->group)
-        if ((rc = enqueue_group32(ctx, dt, t0, std::min(ctx->group, ctx->ntr - t0), tm, fork, joined))) return rc;
+    for (int g0 = 0; g0 < ctx->ngr; g0 += ctx->group)
+        if ((rc = enqueue_group32(ctx, dt, g0, std::min(ctx->group, ctx->ngr - g0), tm, fork, joined))) return rc;
     // a side-stream branch must rejoin the stream (a captured graph requires it)
     if (fork && !joined) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
     CK(cudaGetLastError());
@@ -803,29 +900,16 @@ int launches_per_step(fesom_gpu_ctx *ctx) {
         bool any_vd = false;
         for (int t = 0; t < ctx->ntr; t++) any_vd |= ctx->cfgs[t].i_vert_diff != 0;
         n = 1 + (any_vd ? 1 : 0);
-        for (int t0 = 0; t0 < ctx->ntr; t0 += ctx->group) {
-            const int nt = std::min(ctx->group, ctx->ntr - t0);
-            bool any_fct = false;
-            for (int t = t0; t < t0 + nt; t++) any_fct |= ctx->cfgs[t].adv_lim == FESOM_ADV_LIM_FCT;
-            bool grp_vd = false;
-            for (int t = t0; t < t0 + nt; t++) grp_vd |= ctx->cfgs[t].i_vert_diff != 0;
-            // lo_ad, update (+ bounds), launched again for the wide nodes; ho (+ its fallback
-            // edges); vdiff
+        for (int g0 = 0; g0 < ctx->ngr; g0 += ctx->group) {
+            const int ng = std::min(ctx->group, ctx->ngr - g0);
+            const B32View B = view32(ctx, g0, ng);
+            // lo_ad, update (+ bounds), launched again for the wide nodes; ho (+ its node-mean
+            // edge-layers); vdiff
             const int wide = ctx->tp.n_wide ? 2 : 1;
-            const int nlo = (nt + stage_group(ctx, 0, nt) - 1) / stage_group(ctx, 0, nt);
-            const int nho = (nt + stage_group(ctx, 1, nt) - 1) / stage_group(ctx, 1, nt);
-            const int nbo = (nt + stage_group(ctx, 2, nt) - 1) / stage_group(ctx, 2, nt);
-            const int nup = (nt + stage_group(ctx, 3, nt) - 1) / stage_group(ctx, 3, nt);
-            bool grp_diff = ctx->Ki != nullptr;
-            for (int t = t0; t < t0 + nt; t++) grp_diff |= ctx->cfgs[t].i_vert_diff == 0;
-            bool grp_ppm = false, grp_wimpl = false;
-            for (int t = t0; t < t0 + nt; t++) {
-                grp_ppm |= ctx->cfgs[t].adv_ver == FESOM_ADV_VER_PPM;
-                grp_wimpl |= ctx->wsplit && ctx->cfgs[t].i_vert_diff && ctx->cfgs[t].adv_lim != FESOM_ADV_LIM_FCT;
-            }
-            n += wide * (nlo + nup + (any_fct ? nbo : 0) + (grp_diff ? 1 : 0)) + nho * (ctx->mw.n_items ? 2 : 1) +
-                 (grp_vd ? 1 : 0) + (ctx->Ki ? 1 : 0) + (grp_ppm ? 1 : 0) + ((ctx->wsplit && any_fct) ? 1 : 0) +
-                 (grp_wimpl ? 1 : 0);
+            auto passes = [&](int k) { return (ng + stage_group(ctx, k, ng) - 1) / stage_group(ctx, k, ng); };
+            n += wide * (passes(0) + passes(3) + (B.fct ? passes(2) : 0) + (B.diff ? 1 : 0)) +
+                 passes(1) * (ctx->mw.n_items ? 2 : 1) + ((B.ivd & ~B.wimpl) ? 1 : 0) + (ctx->Ki ? 1 : 0) +
+                 (B.ppm ? 1 : 0) + ((ctx->wsplit && B.fct) ? 1 : 0) + (B.wimpl ? 1 : 0);
         }
         return n;
     }
@@ -900,6 +984,14 @@ int ensure_one(fesom_gpu_ctx *ctx, const fesom_tra_cfg *cfg) {
 // =============================================================================
 // C ABI
 // =============================================================================
+namespace {
+// the pipelined host-array step of the FP32 form (defined with the host-array entry points)
+template <typename S>
+int step_host(fesom_gpu_ctx *ctx, double dt, const S *uv, const S *w, const S *wi, const S *we, const S *Kv,
+              const S *bc_surf, const S *const *values_in, const S *const *valuesold_in, S *const *values_out,
+              S *const *valuesold_out);
+}  // namespace
+
 extern "C" {
 
 int fesom_gpu_abi_version(void) { return FESOM_GPU_ABI_VERSION; }
@@ -1203,8 +1295,18 @@ int fesom_gpu_state_setup(fesom_gpu_ctx *ctx, int32_t ntr, const fesom_tra_cfg *
             return FESOM_ERR_ARG;
         }
     if (ctx->prec == FESOM_PREC_FP32) {
-        if (!(ctx->state_ready && ctx->ntr == ntr && ctx->ab_max == ab_max) && (rc = alloc_state32(ctx, ntr, ab_max)))
-            return rc;
+        // the tracer groups follow the schemes: a new set of schemes may place tracers anew
+        std::vector<fesom_tra_cfg> cf(cfgs, cfgs + ntr);
+        const std::vector<int> keep_g = ctx->slot_g, keep_c = ctx->slot_c;
+        const int keep_w = ctx->gw, keep_n = ctx->ngr;
+        assign_groups(ctx, cf);
+        const bool same = ctx->state_ready && ctx->ntr == ntr && ctx->ab_max == ab_max && keep_g == ctx->slot_g &&
+                          keep_c == ctx->slot_c && keep_w == ctx->gw && keep_n == ctx->ngr;
+        ctx->cfgs = cf;
+        if (!same) {
+            ctx->host_groups.clear();
+            if ((rc = alloc_state32(ctx, ab_max))) return rc;
+        }
         free_graphs32(ctx);
     } else if ((rc = alloc_state(ctx, ntr, ab_max))) {
         return rc;
@@ -1229,7 +1331,14 @@ int fesom_gpu_forcing_upload(fesom_gpu_ctx *ctx, const double *uv, const double 
         (rc = put(ctx, ctx->we, we, sNI)) || (rc = put(ctx, ctx->Kv, Kv, sNI)))
         return rc;
     if (wi && (rc = put(ctx, ctx->wi, wi, sNI))) return rc;
-    if (bc_surf) {
+    if (ctx->prec == FESOM_PREC_FP32) {
+        // the surface flux of tracer t goes to its slot of the group layout
+        CK(cudaMemsetAsync(ctx->bc, 0, 4 * (size_t)ctx->N2 * ctx->gw * ctx->ngr, ctx->stream));
+        for (int t = 0; bc_surf && t < ctx->ntr; t++)
+            if ((rc = put_slot(ctx, (float *)ctx->bc + (size_t)ctx->slot_g[t] * ctx->N2 * ctx->gw, ctx->slot_c[t],
+                               bc_surf + (size_t)t * ctx->N2, ctx->N2)))
+                return rc;
+    } else if (bc_surf) {
         if ((rc = put(ctx, ctx->bc, bc_surf, (size_t)ctx->N2 * ctx->ntr))) return rc;
     } else {
         CK(cudaMemsetAsync(ctx->bc, 0, rsize(ctx) * (size_t)ctx->N2 * ctx->ntr, ctx->stream));
@@ -1249,8 +1358,12 @@ int fesom_gpu_forcing_upload_f32(fesom_gpu_ctx *ctx, const float *uv, const floa
     CK(cudaMemcpyAsync(ctx->we, we, 4 * sNI, cudaMemcpyDefault, ctx->stream));
     CK(cudaMemcpyAsync(ctx->Kv, Kv, 4 * sNI, cudaMemcpyDefault, ctx->stream));
     if (wi) CK(cudaMemcpyAsync(ctx->wi, wi, 4 * sNI, cudaMemcpyDefault, ctx->stream));
-    if (bc_surf) CK(cudaMemcpyAsync(ctx->bc, bc_surf, 4 * (size_t)ctx->N2 * ctx->ntr, cudaMemcpyDefault, ctx->stream));
-    else CK(cudaMemsetAsync(ctx->bc, 0, 4 * (size_t)ctx->N2 * ctx->ntr, ctx->stream));
+    CK(cudaMemsetAsync(ctx->bc, 0, 4 * (size_t)ctx->N2 * ctx->gw * ctx->ngr, ctx->stream));
+    for (int t = 0; bc_surf && t < ctx->ntr; t++) {
+        const int rc = put_slot_f(ctx, (float *)ctx->bc + (size_t)ctx->slot_g[t] * ctx->N2 * ctx->gw, ctx->slot_c[t],
+                                  bc_surf + (size_t)t * ctx->N2, ctx->N2);
+        if (rc) return rc;
+    }
     ctx->forcing_ready = true;
     return FESOM_OK;
 }
@@ -1269,10 +1382,12 @@ int fesom_gpu_tracer_upload(fesom_gpu_ctx *ctx, int32_t tr, const double *values
     if (rc) return rc;
     const size_t sN = (size_t)ctx->L1 * ctx->N2, rs = rsize(ctx);
     if (ctx->prec == FESOM_PREC_FP32) {
-        if ((rc = put(ctx, level32(ctx, 0) + sN * tr, values, sN))) return rc;
+        const size_t go = (size_t)ctx->slot_g[tr] * sN * ctx->gw;
+        const int c = ctx->slot_c[tr];
+        if ((rc = put_slot(ctx, level32(ctx, 0) + go, c, values, sN))) return rc;
         if (!valuesold) return FESOM_OK;
-        if (ctx->ab_max == 2) return put(ctx, level32(ctx, 1) + sN * tr, valuesold, sN);
-        return put_deint(ctx, level32(ctx, 1) + sN * tr, level32(ctx, 2) + sN * tr, valuesold, sN);
+        if (ctx->ab_max == 2) return put_slot(ctx, level32(ctx, 1) + go, c, valuesold, sN);
+        return put_slot_pair(ctx, level32(ctx, 1) + go, level32(ctx, 2) + go, c, valuesold, sN);
     }
     if ((rc = put(ctx, (char *)ctx->T + rs * sN * tr, values, sN))) return rc;
     return put(ctx, (char *)ctx->Told + rs * sN * (ctx->ab_max - 1) * tr, valuesold, sN * (ctx->ab_max - 1));
@@ -1283,10 +1398,12 @@ int fesom_gpu_tracer_download(fesom_gpu_ctx *ctx, int32_t tr, double *values, do
     if (rc) return rc;
     const size_t sN = (size_t)ctx->L1 * ctx->N2, rs = rsize(ctx);
     if (ctx->prec == FESOM_PREC_FP32) {
-        if ((rc = get(ctx, values, level32(ctx, 0) + sN * tr, sN))) return rc;
+        const size_t go = (size_t)ctx->slot_g[tr] * sN * ctx->gw;
+        const int c = ctx->slot_c[tr];
+        if ((rc = get_slot(ctx, values, level32(ctx, 0) + go, c, sN))) return rc;
         if (valuesold) {
-            if (ctx->ab_max == 2) rc = get(ctx, valuesold, level32(ctx, 1) + sN * tr, sN);
-            else rc = get_int(ctx, valuesold, level32(ctx, 1) + sN * tr, level32(ctx, 2) + sN * tr, sN);
+            if (ctx->ab_max == 2) rc = get_slot(ctx, valuesold, level32(ctx, 1) + go, c, sN);
+            else rc = get_slot_pair(ctx, valuesold, level32(ctx, 1) + go, level32(ctx, 2) + go, c, sN);
             if (rc) return rc;
         }
         return wait_stream(ctx, -1);
@@ -1302,12 +1419,12 @@ int fesom_gpu_tracer_upload_f32(fesom_gpu_ctx *ctx, int32_t tr, const float *val
     if (rc) return rc;
     if (ctx->prec != FESOM_PREC_FP32) { ctx->err = "FP32 buffers need a FESOM_PREC_FP32 context"; return FESOM_ERR_STATE; }
     const size_t sN = (size_t)ctx->L1 * ctx->N2;
-    if (values) CK(cudaMemcpyAsync(level32(ctx, 0) + sN * tr, values, 4 * sN, cudaMemcpyDefault, ctx->stream));
+    const size_t go = (size_t)ctx->slot_g[tr] * sN * ctx->gw;
+    const int c = ctx->slot_c[tr];
+    if ((rc = put_slot_f(ctx, level32(ctx, 0) + go, c, values, sN))) return rc;
     if (valuesold) {
-        if (ctx->ab_max == 2)
-            CK(cudaMemcpyAsync(level32(ctx, 1) + sN * tr, valuesold, 4 * sN, cudaMemcpyDefault, ctx->stream));
-        else if ((rc = put_deint_f(ctx, level32(ctx, 1) + sN * tr, level32(ctx, 2) + sN * tr, valuesold, sN)))
-            return rc;
+        if (ctx->ab_max == 2) return put_slot_f(ctx, level32(ctx, 1) + go, c, valuesold, sN);
+        return put_slot_pair_f(ctx, level32(ctx, 1) + go, level32(ctx, 2) + go, c, valuesold, sN);
     }
     return FESOM_OK;
 }
@@ -1317,12 +1434,12 @@ int fesom_gpu_tracer_download_f32(fesom_gpu_ctx *ctx, int32_t tr, float *values,
     if (rc) return rc;
     if (ctx->prec != FESOM_PREC_FP32) { ctx->err = "FP32 buffers need a FESOM_PREC_FP32 context"; return FESOM_ERR_STATE; }
     const size_t sN = (size_t)ctx->L1 * ctx->N2;
-    if (values) CK(cudaMemcpyAsync(values, level32(ctx, 0) + sN * tr, 4 * sN, cudaMemcpyDefault, ctx->stream));
+    const size_t go = (size_t)ctx->slot_g[tr] * sN * ctx->gw;
+    const int c = ctx->slot_c[tr];
+    if ((rc = get_slot_f(ctx, values, level32(ctx, 0) + go, c, sN))) return rc;
     if (valuesold) {
-        if (ctx->ab_max == 2)
-            CK(cudaMemcpyAsync(valuesold, level32(ctx, 1) + sN * tr, 4 * sN, cudaMemcpyDefault, ctx->stream));
-        else if ((rc = get_int_f(ctx, valuesold, level32(ctx, 1) + sN * tr, level32(ctx, 2) + sN * tr, sN)))
-            return rc;
+        if (ctx->ab_max == 2) return get_slot_f(ctx, valuesold, level32(ctx, 1) + go, c, sN);
+        return get_slot_pair_f(ctx, valuesold, level32(ctx, 1) + go, level32(ctx, 2) + go, c, sN);
     }
     return FESOM_OK;
 }
@@ -1400,6 +1517,12 @@ int fesom_gpu_tracer_step(fesom_gpu_ctx *ctx, int32_t ntr, const fesom_tra_cfg *
     bool same = ctx->state_ready && ctx->ntr == ntr && (int)ctx->cfgs.size() == ntr;
     for (int t = 0; same && t < ntr; t++) same = std::memcmp(&ctx->cfgs[t], &cfgs[t], sizeof(fesom_tra_cfg)) == 0;
     if (!same && (rc = fesom_gpu_state_setup(ctx, ntr, cfgs))) return rc;
+    if (ctx->prec == FESOM_PREC_FP32) {
+        if (!uv || !w || !we || !Kv) return FESOM_ERR_ARG;
+        // the FP64 host arrays go through the pipelined host-array step (converted on the device)
+        std::vector<const double *> vin(values, values + ntr), oin(valuesold, valuesold + ntr);
+        return step_host<double>(ctx, dt, uv, w, wi, we, Kv, bc_surf, vin.data(), oin.data(), values, valuesold);
+    }
     if ((rc = fesom_gpu_forcing_upload(ctx, uv, w, wi, we, Kv, bc_surf))) return rc;
     for (int t = 0; t < ntr; t++)
         if ((rc = fesom_gpu_tracer_upload(ctx, t, values[t], valuesold[t]))) return rc;
@@ -1425,7 +1548,9 @@ int fesom_gpu_tracer_step(fesom_gpu_ctx *ctx, int32_t ntr, const fesom_tra_cfg *
 int fesom_gpu_set_tracers_per_launch(fesom_gpu_ctx *ctx, int32_t n) {
     if (!ctx || n < 0) return FESOM_ERR_ARG;
     if (!ctx->state_ready) { ctx->err = "call fesom_gpu_state_setup first"; return FESOM_ERR_STATE; }
-    ctx->group = n == 0 ? ctx->group_cap : std::min((int)n, ctx->group_cap);
+    // the FP32 form launches whole tracer groups: n tracers round up to groups
+    const int m = ctx->prec == FESOM_PREC_FP32 ? (n + ctx->gw - 1) / ctx->gw : n;
+    ctx->group = m == 0 ? ctx->group_cap : std::min(m, ctx->group_cap);
     ctx->host_groups.clear();
     if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
     free_graphs32(ctx);
@@ -1499,11 +1624,16 @@ int fesom_gpu_tracer_content(fesom_gpu_ctx *ctx, double *content) {
     if (!ctx || !content) return FESOM_ERR_ARG;
     if (!ctx->state_ready) { ctx->err = "no tracer state"; return FESOM_ERR_STATE; }
     if (ctx->prec == FESOM_PREC_FP32) {
-        DTracers<float> tr{};
-        tr.ntr = ctx->ntr;
-        tr.sN = (size_t)ctx->L1 * ctx->N2;
-        tr.T = level32(ctx, 0);
-        Launch<float>::content(ctx->tp, ctx->g32, tr, ctx->partials, ctx->content_blocks, ctx->content_out, ctx->stream);
+        b32_content(ctx->tp, ctx->g32, level32(ctx, 0), ctx->ngr, ctx->gw, ctx->partials, ctx->content_blocks,
+                    ctx->content_out, ctx->stream);
+        CK(cudaGetLastError());
+        std::vector<double> slots((size_t)ctx->ngr * ctx->gw);
+        CK(cudaMemcpyAsync(slots.data(), ctx->content_out, sizeof(double) * slots.size(), cudaMemcpyDefault,
+                           ctx->stream));
+        int rc = wait_stream(ctx, -1);
+        if (rc) return rc;
+        for (int t = 0; t < ctx->ntr; t++) content[t] = slots[(size_t)ctx->slot_g[t] * ctx->gw + ctx->slot_c[t]];
+        return FESOM_OK;
     } else {
         DTracers<double> tr = group_view<double>(ctx, 0, ctx->ntr);
         Launch<double>::content(ctx->tp, ctx->g64, tr, ctx->partials, ctx->content_blocks, ctx->content_out, ctx->stream);
@@ -1540,7 +1670,7 @@ int fesom_gpu_set_hdiff(fesom_gpu_ctx *ctx, const double *Ki) {
         if ((rc = put(ctx, ctx->Ki, Ki, sN))) return rc;
         // the FP32 form keeps the edge fluxes of a launch group apart from the advective ones
         if (ctx->prec == FESOM_PREC_FP32 && ctx->state_ready && !ctx->HD32 &&
-            (rc = dalloc(ctx, (void **)&ctx->HD32, 4 * (size_t)ctx->L1 * ctx->E2 * ctx->group_cap)))
+            (rc = dalloc(ctx, (void **)&ctx->HD32, 4 * (size_t)ctx->L1 * ctx->E2 * ctx->gw * ctx->group_cap)))
             return rc;
         CK(cudaStreamSynchronize(ctx->stream));
     }
@@ -1665,16 +1795,16 @@ int fesom_gpu_tracer_tail(fesom_gpu_ctx *ctx, int32_t ntr, const fesom_tra_cfg *
 
 }  // extern "C"
 
-// Tracer groups of the host-array step: the first group's upload and the last group's
-// download are the parts of the step no compute hides, so both are small; between them the
-// groups double up to the launch group.  With G tracers per launch the first group holds
-// max(1, G/3) tracers and so does the last (24 tracers, G = 6: 2, 4, 6, 6, 4, 2).
+// Pipeline stages of the host-array step, in tracer groups: the first stage's upload and the
+// last stage's download are the parts of the step no compute hides, so both are small;
+// between them the stages double up to the launch group.  With L groups per launch the first
+// stage holds max(1, L/3) groups and so does the last.
 static std::vector<int> host_groups(const fesom_gpu_ctx *ctx) {
     if (!ctx->host_groups.empty()) return ctx->host_groups;
-    const int G = std::max(1, ctx->group), s0 = std::max(1, G / 3);
+    const int L = std::max(1, ctx->group), s0 = std::max(1, L / 3);
     std::vector<int> out;
-    for (int rem = ctx->ntr, s = s0; rem > 0; s = std::min(G, 2 * s)) {
-        const int x = std::min(std::min(s, rem), G);
+    for (int rem = ctx->ngr, s = s0; rem > 0; s = std::min(L, 2 * s)) {
+        const int x = std::min(std::min(s, rem), L);
         out.push_back(x);
         rem -= x;
     }
@@ -1686,104 +1816,168 @@ static std::vector<int> host_groups(const fesom_gpu_ctx *ctx) {
     return out;
 }
 
-extern "C" {
+namespace {
 
-int fesom_gpu_set_host_groups(fesom_gpu_ctx *ctx, int32_t n, const int32_t *sizes) {
-    if (!ctx || n < 0 || (n > 0 && !sizes)) return FESOM_ERR_ARG;
-    if (!ctx->state_ready) { ctx->err = "call fesom_gpu_state_setup first"; return FESOM_ERR_STATE; }
-    std::vector<int> gs;
-    int sum = 0;
-    for (int i = 0; i < n; i++) {
-        if (sizes[i] < 1 || sizes[i] > ctx->group) {
-            ctx->err = "a host group holds 1 to tracers-per-launch tracers";
-            return FESOM_ERR_ARG;
-        }
-        gs.push_back(sizes[i]);
-        sum += sizes[i];
+// forcing of the host-array step on the copy-in stream, FP32 or FP64 host arrays
+int put_on(fesom_gpu_ctx *ctx, cudaStream_t st, float *dst, const float *src, size_t n) {
+    CK(cudaMemcpyAsync(dst, src, 4 * n, cudaMemcpyDefault, st));
+    return FESOM_OK;
+}
+int put_on(fesom_gpu_ctx *ctx, cudaStream_t st, float *dst, const double *src, size_t n) {
+    for (size_t off = 0; off < n; off += ctx->stage_n) {
+        const size_t m = std::min(ctx->stage_n, n - off);
+        CK(cudaMemcpyAsync(ctx->stage, src + off, m * sizeof(double), cudaMemcpyDefault, st));
+        k_d2f<<<nblk(m), 256, 0, st>>>(ctx->stage, dst + off, m);
+        CK(cudaGetLastError());
     }
-    if (n > 0 && sum != ctx->ntr) { ctx->err = "the host groups must hold every tracer once"; return FESOM_ERR_ARG; }
-    ctx->host_groups = gs;
     return FESOM_OK;
 }
 
-int fesom_gpu_step_host_f32(fesom_gpu_ctx *ctx, double dt, const float *uv, const float *w, const float *wi,
-                            const float *we, const float *Kv, const float *bc_surf, const float *const *values_in,
-                            const float *const *valuesold_in, float *const *values_out, float *const *valuesold_out) {
-    if (!ctx || !uv || !w || !we || !Kv || !values_in || !valuesold_in || !values_out) return FESOM_ERR_ARG;
-    if (ctx->prec != FESOM_PREC_FP32) { ctx->err = "FP32 buffers need a FESOM_PREC_FP32 context"; return FESOM_ERR_STATE; }
-    if (!ctx->state_ready) { ctx->err = "call fesom_gpu_state_setup first"; return FESOM_ERR_STATE; }
+// One FP32 step from and to host arrays of type S (FP32 or FP64), the transfers overlapped
+// with the compute: the stages of host_groups() go in on the copy-in stream into a ring of two
+// staging buffers, are packed into the group layout and stepped on the context stream as soon
+// as they are resident, and are unpacked into a ring of two output buffers and copied out on
+// the copy-out stream as soon as they are computed.
+template <typename S>
+int step_host(fesom_gpu_ctx *ctx, double dt, const S *uv, const S *w, const S *wi, const S *we, const S *Kv,
+              const S *bc_surf, const S *const *values_in, const S *const *valuesold_in, S *const *values_out,
+              S *const *valuesold_out) {
     int rc;
-    const int ntr = ctx->ntr;
-    const size_t sN = (size_t)ctx->L1 * ctx->N2;
-    if (ctx->ab_max != 2) {
-        // AB3 interleaves its two previous levels on the host: the serial path
-        if ((rc = fesom_gpu_forcing_upload_f32(ctx, uv, w, wi, we, Kv, bc_surf))) return rc;
-        for (int t = 0; t < ntr; t++)
-            if ((rc = fesom_gpu_tracer_upload_f32(ctx, t, values_in[t], valuesold_in[t]))) return rc;
-        if ((rc = fesom_gpu_run_steps(ctx, dt, 1, 0))) return rc;
-        for (int t = 0; t < ntr; t++)
-            if ((rc = fesom_gpu_tracer_download_f32(ctx, t, values_out[t], valuesold_out ? valuesold_out[t] : nullptr)))
-                return rc;
-        return wait_stream(ctx, -1);
-    }
-    // tracer groups: first tracer of each group, and ntr at the end
+    const int G = ctx->gw, ab = ctx->ab_max, lv = ab - 1;
+    const size_t sN = (size_t)ctx->L1 * ctx->N2, sNI = (size_t)ctx->nl * ctx->N2;
     std::vector<int> gs(1, 0);
     for (int x : host_groups(ctx)) gs.push_back(gs.back() + x);
-    if (gs.back() != ntr || (int)gs.size() < 2) {
-        ctx->err = "the host groups must hold every tracer once";
+    if (gs.back() != ctx->ngr || (int)gs.size() < 2) {
+        ctx->err = "the host groups must hold every tracer group once";
         return FESOM_ERR_ARG;
     }
-    const int ng = (int)gs.size() - 1;
-    while ((int)ctx->ev_in.size() < ng) {
+    const int ns = (int)gs.size() - 1;
+    // staging per slot of the two rings: the largest stage's tracers, values and previous levels
+    size_t need = 0;
+    for (int k = 0; k < ns; k++) need = std::max(need, (size_t)(gs[k + 1] - gs[k]) * G * (1 + lv) * sN * sizeof(S));
+    need = std::max(need, sizeof(S) * (size_t)ctx->N2 * ctx->ntr);  // the surface fluxes pass through slot 0
+    if (ctx->pack_n < need) {
+        for (float **b : {&ctx->pack_in, &ctx->pack_out}) {
+            void *p = *b;
+            dfree(ctx, p);
+            *b = nullptr;
+        }
+        ctx->pack_n = 0;
+        if ((rc = dalloc(ctx, (void **)&ctx->pack_in, 2 * need)) || (rc = dalloc(ctx, (void **)&ctx->pack_out, 2 * need)))
+            return rc;
+        ctx->pack_n = need;
+    }
+    while ((int)ctx->ev_in.size() < 2 * ns) {
         cudaEvent_t a, b;
         CK(cudaEventCreateWithFlags(&a, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&b, cudaEventDisableTiming));
         ctx->ev_in.push_back(a);
         ctx->ev_done.push_back(b);
     }
+    // ev_in[k]: stage k resident in its staging slot; ev_in[ns + k]: stage k packed (its
+    // staging slot free); ev_done[k]: stage k computed and unpacked; ev_done[ns + k]: copied out
+    cudaEvent_t *ev_res = ctx->ev_in.data(), *ev_pack = ctx->ev_in.data() + ns;
+    cudaEvent_t *ev_comp = ctx->ev_done.data(), *ev_out = ctx->ev_done.data() + ns;
     // the previous step's kernels are done with the buffers the copies fill
     CK(cudaEventRecord(ctx->ev_forcing, ctx->stream));
     CK(cudaStreamWaitEvent(ctx->h2d, ctx->ev_forcing, 0));
-    // forcing, then the tracer groups, on the copy-in stream
-    const size_t sNI = (size_t)ctx->nl * ctx->N2;
-    CK(cudaMemcpyAsync(ctx->uv, uv, 4 * 2 * (size_t)ctx->L1 * ctx->T2, cudaMemcpyDefault, ctx->h2d));
-    CK(cudaMemcpyAsync(ctx->w, w, 4 * sNI, cudaMemcpyDefault, ctx->h2d));
-    CK(cudaMemcpyAsync(ctx->we, we, 4 * sNI, cudaMemcpyDefault, ctx->h2d));
-    CK(cudaMemcpyAsync(ctx->Kv, Kv, 4 * sNI, cudaMemcpyDefault, ctx->h2d));
-    if (wi) CK(cudaMemcpyAsync(ctx->wi, wi, 4 * sNI, cudaMemcpyDefault, ctx->h2d));
-    if (bc_surf) CK(cudaMemcpyAsync(ctx->bc, bc_surf, 4 * (size_t)ctx->N2 * ntr, cudaMemcpyDefault, ctx->h2d));
-    else CK(cudaMemsetAsync(ctx->bc, 0, 4 * (size_t)ctx->N2 * ntr, ctx->h2d));
+    if ((rc = put_on(ctx, ctx->h2d, (float *)ctx->uv, uv, 2 * (size_t)ctx->L1 * ctx->T2)) ||
+        (rc = put_on(ctx, ctx->h2d, (float *)ctx->w, w, sNI)) || (rc = put_on(ctx, ctx->h2d, (float *)ctx->we, we, sNI)) ||
+        (rc = put_on(ctx, ctx->h2d, (float *)ctx->Kv, Kv, sNI)))
+        return rc;
+    if (wi && (rc = put_on(ctx, ctx->h2d, (float *)ctx->wi, wi, sNI))) return rc;
+    CK(cudaMemsetAsync(ctx->bc, 0, 4 * (size_t)ctx->N2 * G * ctx->ngr, ctx->h2d));
+    if (bc_surf) {
+        // per tracer into its slot, through the first staging slot (free at this point)
+        S *st = (S *)ctx->pack_in;
+        CK(cudaMemcpyAsync(st, bc_surf, sizeof(S) * (size_t)ctx->N2 * ctx->ntr, cudaMemcpyDefault, ctx->h2d));
+        for (int g = 0; g < ctx->ngr; g++) {
+            SlotSrc<S> src{};
+            for (int c = 0; c < G; c++) {
+                const int t = ctx->slot_tr[(size_t)g * G + c];
+                src.p[c] = t >= 0 ? st + (size_t)t * ctx->N2 : nullptr;
+            }
+            b32_pack_group<S>(src, (float *)ctx->bc + (size_t)g * ctx->N2 * G, G, ctx->N2, 1, 0, ctx->h2d);
+        }
+        CK(cudaGetLastError());
+    }
     ctx->forcing_ready = true;
     CK(cudaEventRecord(ctx->ev_forcing, ctx->h2d));
-    float *Tcur = level32(ctx, 0), *Told = level32(ctx, 1);  // the step writes Tnew into Told's buffer
-    for (int gi = 0; gi < ng; gi++) {
-        for (int t = gs[gi]; t < gs[gi + 1]; t++) {
-            CK(cudaMemcpyAsync(Tcur + sN * t, values_in[t], 4 * sN, cudaMemcpyDefault, ctx->h2d));
-            CK(cudaMemcpyAsync(Told + sN * t, valuesold_in[t], 4 * sN, cudaMemcpyDefault, ctx->h2d));
-        }
-        CK(cudaEventRecord(ctx->ev_in[gi], ctx->h2d));
-    }
-    // compute each group as soon as its tracers are resident
+    float *L0 = level32(ctx, 0), *L1b = level32(ctx, 1), *L2b = ab == 3 ? level32(ctx, 2) : nullptr;
+    float *Lnew = level32(ctx, ab - 1);
     CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_forcing, 0));
     bool fork = false, joined = false;
     if ((rc = enqueue_shared32(ctx, dt, nullptr, fork))) return rc;
-    for (int gi = 0; gi < ng; gi++) {
-        CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_in[gi], 0));
-        if ((rc = enqueue_group32(ctx, dt, gs[gi], gs[gi + 1] - gs[gi], nullptr, fork, joined))) return rc;
-        CK(cudaEventRecord(ctx->ev_done[gi], ctx->stream));
+    const size_t per_tr = (1 + lv) * sN;  // staged elements per tracer: values, then valuesold
+    for (int k = 0; k < ns; k++) {
+        S *in = (S *)((char *)ctx->pack_in + (k & 1) * need);
+        S *out = (S *)((char *)ctx->pack_out + (k & 1) * need);
+        // copy in: stage k's tracers, once stage k-2 has left the slot
+        if (k >= 2) CK(cudaStreamWaitEvent(ctx->h2d, ev_pack[k - 2], 0));
+        int q = 0;
+        for (int g = gs[k]; g < gs[k + 1]; g++)
+            for (int c = 0; c < G; c++, q++) {
+                const int t = ctx->slot_tr[(size_t)g * G + c];
+                if (t < 0) continue;
+                CK(cudaMemcpyAsync(in + q * per_tr, values_in[t], sizeof(S) * sN, cudaMemcpyDefault, ctx->h2d));
+                CK(cudaMemcpyAsync(in + q * per_tr + sN, valuesold_in[t], sizeof(S) * sN * lv, cudaMemcpyDefault,
+                                   ctx->h2d));
+            }
+        CK(cudaEventRecord(ev_res[k], ctx->h2d));
+        // compute: pack into the time levels, the stages of the groups, unpack the results
+        CK(cudaStreamWaitEvent(ctx->stream, ev_res[k], 0));
+        q = 0;
+        for (int g = gs[k]; g < gs[k + 1]; g++, q += G) {
+            SlotSrc<S> v{}, o{};
+            for (int c = 0; c < G; c++) {
+                const bool has = ctx->slot_tr[(size_t)g * G + c] >= 0;
+                v.p[c] = has ? in + (q + c) * per_tr : nullptr;
+                o.p[c] = has ? in + (q + c) * per_tr + sN : nullptr;
+            }
+            const size_t go = (size_t)g * sN * G;
+            b32_pack_group<S>(v, L0 + go, G, sN, 1, 0, ctx->stream);
+            b32_pack_group<S>(o, L1b + go, G, sN, lv, 0, ctx->stream);
+            if (ab == 3) b32_pack_group<S>(o, L2b + go, G, sN, 2, 1, ctx->stream);
+        }
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(ev_pack[k], ctx->stream));
+        for (int g0 = gs[k]; g0 < gs[k + 1]; g0 += ctx->group)
+            if ((rc = enqueue_group32(ctx, dt, g0, std::min(ctx->group, gs[k + 1] - g0), nullptr, fork, joined)))
+                return rc;
+        if (k >= 2) CK(cudaStreamWaitEvent(ctx->stream, ev_out[k - 2], 0));
+        q = 0;
+        for (int g = gs[k]; g < gs[k + 1]; g++, q += G) {
+            SlotDst<S> v{}, o{};
+            for (int c = 0; c < G; c++) {
+                const bool has = ctx->slot_tr[(size_t)g * G + c] >= 0;
+                v.p[c] = has ? out + (q + c) * per_tr : nullptr;
+                o.p[c] = (has && valuesold_out) ? out + (q + c) * per_tr + sN : nullptr;
+            }
+            const size_t go = (size_t)g * sN * G;
+            b32_unpack_group<S>(Lnew + go, G, sN, v, 1, 0, ctx->stream);
+            if (valuesold_out) {
+                // the new previous levels: the values the step started from (and, AB3, the level before)
+                b32_unpack_group<S>(L0 + go, G, sN, o, lv, 0, ctx->stream);
+                if (ab == 3) b32_unpack_group<S>(L1b + go, G, sN, o, 2, 1, ctx->stream);
+            }
+        }
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(ev_comp[k], ctx->stream));
+        // copy out
+        CK(cudaStreamWaitEvent(ctx->d2h, ev_comp[k], 0));
+        q = 0;
+        for (int g = gs[k]; g < gs[k + 1]; g++)
+            for (int c = 0; c < G; c++, q++) {
+                const int t = ctx->slot_tr[(size_t)g * G + c];
+                if (t < 0) continue;
+                CK(cudaMemcpyAsync(values_out[t], out + q * per_tr, sizeof(S) * sN, cudaMemcpyDefault, ctx->d2h));
+                if (valuesold_out)
+                    CK(cudaMemcpyAsync(valuesold_out[t], out + q * per_tr + sN, sizeof(S) * sN * lv, cudaMemcpyDefault,
+                                       ctx->d2h));
+            }
+        CK(cudaEventRecord(ev_out[k], ctx->d2h));
     }
     if (fork && !joined) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
-    CK(cudaGetLastError());
-    // copy each group out as soon as it is computed: the new values (Told's buffer) and the
-    // new previous level (the values the step started from)
-    for (int gi = 0; gi < ng; gi++) {
-        CK(cudaStreamWaitEvent(ctx->d2h, ctx->ev_done[gi], 0));
-        for (int t = gs[gi]; t < gs[gi + 1]; t++) {
-            CK(cudaMemcpyAsync(values_out[t], Told + sN * t, 4 * sN, cudaMemcpyDefault, ctx->d2h));
-            if (valuesold_out)
-                CK(cudaMemcpyAsync(valuesold_out[t], Tcur + sN * t, 4 * sN, cudaMemcpyDefault, ctx->d2h));
-        }
-    }
     rotate32(ctx);
     // the context's stream follows the copies out, so later calls see a quiet context
     CK(cudaEventRecord(ctx->ev_forcing, ctx->d2h));
@@ -1799,14 +1993,67 @@ int fesom_gpu_step_host_f32(fesom_gpu_ctx *ctx, double dt, const float *uv, cons
     return FESOM_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+int fesom_gpu_set_host_groups(fesom_gpu_ctx *ctx, int32_t n, const int32_t *sizes) {
+    if (!ctx || n < 0 || (n > 0 && !sizes)) return FESOM_ERR_ARG;
+    if (!ctx->state_ready) { ctx->err = "call fesom_gpu_state_setup first"; return FESOM_ERR_STATE; }
+    if (ctx->prec != FESOM_PREC_FP32) { ctx->err = "host groups belong to the FP32 form"; return FESOM_ERR_STATE; }
+    std::vector<int> gs;
+    int sum = 0;
+    for (int i = 0; i < n; i++) {
+        if (sizes[i] < 1 || sizes[i] > ctx->group) {
+            ctx->err = "a host group holds 1 to groups-per-launch tracer groups";
+            return FESOM_ERR_ARG;
+        }
+        gs.push_back(sizes[i]);
+        sum += sizes[i];
+    }
+    if (n > 0 && sum != ctx->ngr) { ctx->err = "the host groups must hold every tracer group once"; return FESOM_ERR_ARG; }
+    ctx->host_groups = gs;
+    return FESOM_OK;
+}
+
+int fesom_gpu_tracer_groups(fesom_gpu_ctx *ctx, int32_t *groups, int32_t *width, int32_t *group_of,
+                            int32_t *slot_of) {
+    if (!ctx) return FESOM_ERR_ARG;
+    if (!ctx->state_ready) { ctx->err = "call fesom_gpu_state_setup first"; return FESOM_ERR_STATE; }
+    if (ctx->prec != FESOM_PREC_FP32) { ctx->err = "tracer groups belong to the FP32 form"; return FESOM_ERR_STATE; }
+    if (groups) *groups = ctx->ngr;
+    if (width) *width = ctx->gw;
+    for (int t = 0; t < ctx->ntr; t++) {
+        if (group_of) group_of[t] = ctx->slot_g[t];
+        if (slot_of) slot_of[t] = ctx->slot_c[t];
+    }
+    return FESOM_OK;
+}
+
+int fesom_gpu_set_tracer_width(fesom_gpu_ctx *ctx, int32_t width) {
+    if (!ctx || (width != 0 && width != 2 && width != 4)) return FESOM_ERR_ARG;
+    ctx->gw_req = width;
+    // the next fesom_gpu_state_setup places the tracers with it
+    return FESOM_OK;
+}
+
+int fesom_gpu_step_host_f32(fesom_gpu_ctx *ctx, double dt, const float *uv, const float *w, const float *wi,
+                            const float *we, const float *Kv, const float *bc_surf, const float *const *values_in,
+                            const float *const *valuesold_in, float *const *values_out, float *const *valuesold_out) {
+    if (!ctx || !uv || !w || !we || !Kv || !values_in || !valuesold_in || !values_out) return FESOM_ERR_ARG;
+    if (ctx->prec != FESOM_PREC_FP32) { ctx->err = "FP32 buffers need a FESOM_PREC_FP32 context"; return FESOM_ERR_STATE; }
+    if (!ctx->state_ready) { ctx->err = "call fesom_gpu_state_setup first"; return FESOM_ERR_STATE; }
+    return step_host<float>(ctx, dt, uv, w, wi, we, Kv, bc_surf, values_in, valuesold_in, values_out, valuesold_out);
+}
+
 int fesom_gpu_tracer_device_ptr(fesom_gpu_ctx *ctx, int32_t tr, void **values, void **valuesold) {
     int rc = tracer_check(ctx, tr);
     if (rc) return rc;
     const size_t sN = (size_t)ctx->L1 * ctx->N2, rs = rsize(ctx);
     if (ctx->prec == FESOM_PREC_FP32) {
-        if (values) *values = level32(ctx, 0) + sN * tr;
-        if (valuesold) *valuesold = level32(ctx, 1) + sN * tr;
-        return FESOM_OK;
+        ctx->err = "the FP32 form stores tracers in interleaved groups (fesom_gpu_tracer_groups): use the upload and "
+                   "download calls";
+        return FESOM_ERR_STATE;
     }
     if (values) *values = (char *)ctx->T + rs * sN * tr;
     if (valuesold) *valuesold = (char *)ctx->Told + rs * sN * (ctx->ab_max - 1) * tr;
@@ -1864,7 +2111,7 @@ int batch_descriptors(fesom_gpu_batch *b, double dt) {
             d.tp = c->tp;
             d.g = c->g32;
             d.f = forcing_view<float>(c, 0);
-            d.B = view32(c, 0, c->ntr);
+            d.B = view32(c, 0, c->ngr);
             d.mw = c->mw;
             d.VF = c->VF;
             d.vf = c->vfac;
@@ -1924,7 +2171,7 @@ int fesom_gpu_batch_create(fesom_gpu_ctx *const *ctxs, int32_t n, fesom_gpu_batc
             b->err = "every batch instance needs its tracer state and forcing set up";
             return FESOM_ERR_STATE;
         }
-        if (c->group != c->ntr) {
+        if (c->group != c->ngr) {
             b->err = "every batch instance must hold all its tracers in one launch group";
             return FESOM_ERR_STATE;
         }

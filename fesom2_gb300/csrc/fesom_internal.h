@@ -83,36 +83,39 @@ struct DTracers {
 };
 
 // FP32 batched form (kernels_fp32_batched.cu): one step's view of the tracer state.
-// T / O1 / O2 are the current and previous time levels (rotated each step, no copy);
-// the step writes the new values into Tnew (the buffer of the oldest level).
+//
+// Tracer groups: the tracers of the form sit in groups of G (4, or 2 for small tracer
+// counts) "slots" of one scheme, side by side in every entry: a field of a group is an
+// array of G-float entries in the reference's a(level, entity) order, entry
+// (g, entity, level) at ((g * count + entity) * levels + level - 1) * G floats.  A lane's
+// 16-byte (8-byte) load of one entry brings the values of all G tracers, so every
+// address, predicate and gather serves G tracers.  Slots a group does not fill hold zeros
+// and compute zeros.  T / O1 / O2 are the current and previous time levels (rotated
+// each step, no copy); the step writes the new values into Tnew (the oldest level).
+constexpr int kMaxSlots = 64;   // tracer slots of one launch group (per-slot parameters)
+constexpr int kMaxGroups = 32;  // tracer groups of one launch group (G >= 2)
 struct B32View {
-    int ntr, ab;
-    size_t sN, sNI, sE;
+    int ng, ab, G;          // tracer groups of the launch, Adams-Bashforth order, slots per group
+    size_t sN, sNI, sE;     // entries per group: layer (nl-1)*N2, interface nl*N2, edge (nl-1)*E2
     const float *T, *O1, *O2;
     float *Tnew;
-    float *LO;       // low-order (upwind) solution
-    float *ADv;      // vertical flux high order minus low order (the antidiffusive flux)
-    float *ADh;      // the same for edges, written by the edge's first node
-    float2 *R;       // FCT ratios (R+, R-)
-    float2 *TB;      // FCT bounds of the advected value (LO + bmax, LO + bmin)
-    const DCfg *cfg;
+    float *LO;              // low-order (upwind) solution
+    float *ADv;             // vertical flux high order minus low order (the antidiffusive flux)
+    float *ADh;             // the same for edges, in the direction edges(1,e) -> edges(2,e)
+    float *Rp, *Rm;         // FCT ratios R+ and R-
+    float *Bp, *Bm;         // FCT bounds of the advected value (LO + bmax, LO + bmin)
     unsigned *status;
-    unsigned long long fct_mask;  // bit t: tracer t of the launch uses the FCT limiter
-    unsigned long long ivd_mask;  // bit t: tracer t takes the implicit vertical diffusion
-    // per-tracer schemes in the kernel parameters (constant bank), at most 64 tracers
-    signed char hor[64], ver[64];
-    float ph[64], pv[64];
-    // diffusion of diff_tracers_ale: bit t of diff_mask: tracer t gets horizontal (Ki set) or
-    // explicit vertical (no implicit diffusion) terms; k32_diff parks their increment to T* in
-    // Tnew and the update adds it after the FCT clamp
-    unsigned long long diff_mask;
-    const float *Ki;   // horizontal diffusivity, nl-1 per node; null: none
-    float *HD;         // horizontal diffusion flux per edge-layer
-    const float *Kv;   // vertical diffusivity (explicit part), nl per node
-    const float *fsurf;  // surface flux per tracer and node (explicit vertical diffusion)
-    size_t sF;           // tracer stride of fsurf (nodes)
-    unsigned long long ppm_mask;    // tracers with the PPM vertical scheme (k32_vppm writes their ADv)
-    unsigned long long wimpl_mask;  // split velocity: implicit diffusion with the w_i terms (k32_vdiff_w)
+    // bit g: group g of the launch uses the FCT limiter / takes the implicit vertical
+    // diffusion / gets horizontal or explicit vertical diffusion (k32_diff) / the PPM vertical
+    // scheme (k32_vppm) / the implicit diffusion with the w_i terms of the split velocity
+    unsigned long long fct, ivd, diff, ppm, wimpl;
+    signed char hor[kMaxGroups], ver[kMaxGroups];  // per group, in the kernel parameters
+    float ph[kMaxSlots], pv[kMaxSlots];            // per slot (slot = g * G + c)
+    const float *Ki;        // horizontal diffusivity, nl-1 per node; null: none
+    float *HD;              // horizontal diffusion flux per edge-layer (group layout)
+    const float *Kv;        // vertical diffusivity (explicit part), nl per node
+    const float *fsurf;     // surface flux per group entry (g, node), G floats each; null: none
+    size_t sF;              // entries per group of fsurf (nodes)
 };
 // Node degree bound of the FP32 form (the node's edge list is staged per warp)
 constexpr int kMaxDeg = 16;
@@ -141,10 +144,18 @@ struct VFactors {
 void b32_vflux(const DTopo &, const DGeom<float> &, const DForcing<float> &, float *VF, cudaStream_t);
 void b32_vfactors(const DTopo &, const DGeom<float> &, const DForcing<float> &, double dt, const VFactors &,
                   cudaStream_t);
+// launch shape of the node/edge stages (the autotuner's choices): blocks of 8 warps, at most
+// `blocks_per_sm` x 152 blocks (grid-stride loops over the units); 0: one warp per unit
+struct LaunchShape {
+    int blocks_per_sm = 0;
+};
 void b32_lo_ad(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, const float *VF,
-               double dt, cudaStream_t);
-void b32_ho(const DTopo &, const DGeom<float> &, const B32View &, const MusclW &, const float *VF, cudaStream_t);
-void b32_bounds(const DTopo &, const DGeom<float> &, const B32View &, double dt, cudaStream_t);
+               double dt, const LaunchShape &, cudaStream_t);
+void b32_ho(const DTopo &, const DGeom<float> &, const B32View &, const MusclW &, const float *VF,
+            const LaunchShape &, cudaStream_t);
+void b32_bounds(const DTopo &, const DGeom<float> &, const B32View &, double dt, const LaunchShape &, cudaStream_t);
+void b32_update(const DTopo &, const DGeom<float> &, const B32View &, double dt, const LaunchShape &, cudaStream_t);
+void b32_vdiff(const DTopo &, const DForcing<float> &, const B32View &, const VFactors &, cudaStream_t);
 void b32_vppm(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, double dt, cudaStream_t);
 void b32_lo_impl(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, double dt,
                  double *scratch, cudaStream_t);
@@ -152,8 +163,36 @@ void b32_vdiff_w(const DTopo &, const DGeom<float> &, const DForcing<float> &, c
                  double *scratch, cudaStream_t);
 void b32_hdiff(const DTopo &, const DGeom<float> &, const B32View &, cudaStream_t);
 void b32_diff(const DTopo &, const DGeom<float> &, const B32View &, double dt, cudaStream_t);
-void b32_update(const DTopo &, const DGeom<float> &, const B32View &, double dt, cudaStream_t);
-void b32_vdiff(const DTopo &, const DForcing<float> &, const B32View &, const VFactors &, cudaStream_t);
+// FP64 content sum_nodes sum_levels T hnode_new areasvol of every slot of the ng groups at T
+// (out[slot]); partials: nblk * ng * G doubles
+void b32_content(const DTopo &, const DGeom<float> &, const float *T, int ng, int G, double *partials, int nblk,
+                 double *out, cudaStream_t);
+// layout conversions of the FP32 form: one tracer's column-major array (FP64 or FP32, host
+// values staged on the device) into / out of slot c of a group field of `count` entries
+void b32_put_slot(const double *src, float *grp, int G, int c, size_t count, cudaStream_t);
+void b32_put_slot_f(const float *src, float *grp, int G, int c, size_t count, cudaStream_t);
+void b32_get_slot(const float *grp, int G, int c, size_t count, double *dst, cudaStream_t);
+void b32_get_slot_f(const float *grp, int G, int c, size_t count, float *dst, cudaStream_t);
+// the same for AB3's interleaved valuesold(2, level, node): into / out of two group fields
+void b32_put_slot_pair(const double *src, float *g1, float *g2, int G, int c, size_t count, cudaStream_t);
+void b32_put_slot_pair_f(const float *src, float *g1, float *g2, int G, int c, size_t count, cudaStream_t);
+void b32_get_slot_pair(const float *g1, const float *g2, int G, int c, size_t count, double *dst, cudaStream_t);
+void b32_get_slot_pair_f(const float *g1, const float *g2, int G, int c, size_t count, float *dst, cudaStream_t);
+// a whole group at once: G staged column-major arrays (FP64 or FP32; p[c] of slot c, null:
+// zeros) into / out of one group field, full G-float entries; element i of slot c is
+// p[c][i * stride + off]
+template <typename S>
+struct SlotSrc {
+    const S *p[4];
+};
+template <typename S>
+struct SlotDst {
+    S *p[4];
+};
+template <typename S>
+void b32_pack_group(const SlotSrc<S> &src, float *grp, int G, size_t count, int stride, int off, cudaStream_t);
+template <typename S>
+void b32_unpack_group(const float *grp, int G, size_t count, const SlotDst<S> &dst, int stride, int off, cudaStream_t);
 
 // Multi-instance batch of the FP32 form: one descriptor per instance (device memory) and,
 // per stage, the offsets of each instance's units in the launch

@@ -25,27 +25,40 @@
 //                    the optional parts: PPM vertical fluxes, the split vertical
 //                    velocity, horizontal and explicit vertical diffusion
 //
-// Every tracer carries the same quantities whatever its limiter: the LO solution and
-// the antidiffusive fluxes "high order minus low order" of the edges and interfaces.
-// Without FCT the update adds them unlimited, which is the high-order flux divergence;
-// with FCT it scales them by R+/R- first.
+// Tracer groups: the tracers sit in groups of G slots (G = 4, or 2) of one scheme, side by
+// side in every (level, entity) entry of a field.  A lane's load of one entry is one 16-byte
+// (8-byte) vector load that brings all G tracers, so the address, the wet-level predicate
+// and the load of every gather are formed once for G tracers, and G independent chains of
+// arithmetic follow each load.  Slots a group does not fill hold zeros and compute zeros.
 //
-// Mapping of the node stages: one warp per node for all tracers of the launch.  The
-// lanes cover a chunk of the node's column (one level per lane); consecutive chunks
-// overlap by the halo levels each stage needs (the level above/below comes from the
-// neighbouring lane through a shuffle), and the halo lanes compute but do not store.
-// The last chunk of a column, when its levels fill at most half a warp, carries several
-// tracers side by side in lane segments.  The node's edge list, the neighbour offsets
-// and the tracer-independent geometry of a chunk sit in registers and serve every
-// tracer, so per tracer a lane does only the gathers and the arithmetic of that tracer.
-// Eight consecutive nodes per block (the node order is spatially local), so the
-// neighbour columns a block gathers are mostly shared between its warps.
+// Every tracer carries the same quantities whatever its limiter: the LO solution and the
+// antidiffusive fluxes "high order minus low order" of the edges and interfaces.  Without
+// FCT the update adds them unlimited, which is the high-order flux divergence; with FCT it
+// scales them by R+/R- first.
 //
-// Layout: tracer-major, column-contiguous per tracer (the reference's a(level, node)
-// per tracer).  No atomics on values: each edge flux is written once and every node
-// sum is a gather.  The Adams-Bashforth shift is a rotation of the time-level buffers
-// (no copy).
+// Conservation: every horizontal flux a node sums is formed from the edge's own data in the
+// edge's direction (edges(1,e) -> edges(2,e)) and added at one end and subtracted at the
+// other, so both ends use the same bits (the upwind LO flux is recomputed at each end by the
+// same expression; the antidiffusive flux is stored once per edge-layer and its limiter
+// factor min(R+, R-) is the same seen from either end); a vertical flux is one value shuffled
+// between the two layers it joins.  With hnode = hnode_new the LO solution is T plus the flux
+// divergence (no rescaling of T that would round every value of the column).
+//
+// Mapping of the node stages: one warp per node for all groups of the launch.  The lanes
+// cover a chunk of the node's column (one level per lane); consecutive chunks overlap by the
+// halo levels each stage needs (the level above/below comes from the neighbouring lane
+// through a shuffle), and the halo lanes compute but do not store.  The last chunk of a
+// column, when its levels fill at most half a warp, carries several groups side by side in
+// lane segments.  The node's edge list, the neighbour offsets and the tracer-independent
+// geometry of a chunk sit in registers and serve every group.  Blocks of eight warps take
+// consecutive nodes (the node order is spatially local), so the neighbour columns a block
+// gathers are mostly shared between its warps.
+//
+// No atomics on values: each edge flux is written once and every node sum is a gather.  The
+// Adams-Bashforth shift is a rotation of the time-level buffers (no copy).
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "fesom_internal.h"
 
@@ -57,30 +70,22 @@ constexpr int kWB = 8;                // warps (= nodes) per block
 constexpr int kTB = 32 * kWB;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kMaxChunks = 5;         // columns of up to 128 layers, 30 levels per chunk
-// resident blocks per SM each tracer kernel is built for (3: <= 80 registers, 4: <= 64)
-#ifndef FESOM_MINB_LO
-#define FESOM_MINB_LO 3
-#endif
-#ifndef FESOM_MINB_HO
-#define FESOM_MINB_HO 4
-#endif
-#ifndef FESOM_MINB_BOUNDS
-#define FESOM_MINB_BOUNDS 4
-#endif
-#ifndef FESOM_MINB_UPDATE
-#define FESOM_MINB_UPDATE 4
-#endif
-// tracers side by side in the last level chunk of a column in the multi-instance kernels too
-#ifndef FESOM_PACK_MULTI
-#define FESOM_PACK_MULTI true
-#endif
+
+// resident blocks per SM each group kernel is built for (registers: 65536 / (256 * blocks))
+template <int G>
+struct MinB {
+    static constexpr int lo = 2;
+    static constexpr int ho = G == 4 ? 3 : 4;
+    static constexpr int bounds = G == 4 ? 2 : 3;
+    static constexpr int update = G == 4 ? 2 : 3;
+};
 
 __device__ __forceinline__ size_t i1(int nz, int n, int L1) { return (size_t)n * L1 + (nz - 1); }
 
 // FP32 quotients of the node stages (geometry factors, limiter ratios): the fast division
-// (2 ulp) instead of the correctly rounded one, 4-6 % of the bounds and lo_ad kernels' time;
-// far inside the FP32 form's 1e-5, and the FCT clamp into the stored bounds keeps every
-// result inside its bounds whatever the last bits of R+/R-
+// (2 ulp) instead of the correctly rounded one; far inside the FP32 form's 1e-5, and the FCT
+// clamp into the stored bounds keeps every result inside its bounds whatever the last bits
+// of R+/R-
 __device__ __forceinline__ float qdiv(float a, float b) { return __fdividef(a, b); }
 
 }  // namespace
@@ -259,6 +264,7 @@ struct WEdges {
 };
 
 __device__ __forceinline__ void stage_edges(const DTopo &tp, int n, int lane, WEdges &S) {
+    __syncwarp();  // every lane is done with the previous node's list (grid-stride loops)
     const int k0 = tp.ne_ptr[n];
     const int deg = min(tp.ne_ptr[n + 1] - k0, kMaxDeg);
     int code = 0;
@@ -285,7 +291,7 @@ template <int HU, int HD>
 struct Chunk {
     static constexpr int OUT = 32 - HU - HD;
     int nz;
-    int q = 0;  // tracer slot of the lane (packed chunks)
+    int q = 0;  // segment of the lane (packed chunks): its group is the pass's first plus q
     bool lvl, out;
     __device__ __forceinline__ Chunk(int nzmin, int nzmax, int ch, int lane) {
         nz = nzmin - HU + OUT * ch + lane;
@@ -293,7 +299,7 @@ struct Chunk {
         out = lvl && lane >= HU && lane < 32 - HD;
     }
     // the last chunk of a column in P segments of W = (its levels + HU + HD) lanes, one
-    // tracer per segment: segment q holds the lanes [q W, (q + 1) W), laid out as a whole
+    // tracer group per segment: segment q holds the lanes [q W, (q + 1) W), laid out as a whole
     // chunk, so the vertical shuffles of a stored lane stay inside its segment
     __device__ __forceinline__ Chunk(int nzmin, int nzmax, int ch, int lane, int W, int P) {
         q = lane / W;
@@ -313,21 +319,112 @@ struct Chunk {
 __device__ __forceinline__ float sh_up(float v, int d) { return __shfl_up_sync(kFull, v, d); }
 __device__ __forceinline__ float sh_dn(float v, int d) { return __shfl_down_sync(kFull, v, d); }
 
+
+// ---------------------------------------------------------------------------
+// entries of G floats
+// ---------------------------------------------------------------------------
+template <int G>
+struct Vec {
+    float c[G];
+};
+template <int G>
+__device__ __forceinline__ Vec<G> vfill(float x) {
+    Vec<G> r;
+#pragma unroll
+    for (int k = 0; k < G; k++) r.c[k] = x;
+    return r;
+}
+template <int G>
+__device__ __forceinline__ Vec<G> vld(const float *__restrict__ p, int i);
+template <>
+__device__ __forceinline__ Vec<4> vld<4>(const float *__restrict__ p, int i) {
+    const float4 q = reinterpret_cast<const float4 *>(p)[i];
+    return Vec<4>{{q.x, q.y, q.z, q.w}};
+}
+template <>
+__device__ __forceinline__ Vec<2> vld<2>(const float *__restrict__ p, int i) {
+    const float2 q = reinterpret_cast<const float2 *>(p)[i];
+    return Vec<2>{{q.x, q.y}};
+}
+// entry i where ok, zeros elsewhere (no load issued where !ok)
+template <int G>
+__device__ __forceinline__ Vec<G> vldc(bool ok, const float *__restrict__ p, int i) {
+    Vec<G> r = vfill<G>(0.f);
+    if (ok) r = vld<G>(p, i);
+    return r;
+}
+template <int G>
+__device__ __forceinline__ void vst(float *p, int i, const Vec<G> &v);
+template <>
+__device__ __forceinline__ void vst<4>(float *p, int i, const Vec<4> &v) {
+    reinterpret_cast<float4 *>(p)[i] = make_float4(v.c[0], v.c[1], v.c[2], v.c[3]);
+}
+template <>
+__device__ __forceinline__ void vst<2>(float *p, int i, const Vec<2> &v) {
+    reinterpret_cast<float2 *>(p)[i] = make_float2(v.c[0], v.c[1]);
+}
+// group g of a field of `count` entries per group
+template <int G>
+__device__ __forceinline__ const float *grp(const float *base, int g, size_t count) {
+    return base + (size_t)g * count * G;
+}
+template <int G>
+__device__ __forceinline__ float *grp(float *base, int g, size_t count) {
+    return base + (size_t)g * count * G;
+}
+
 // Adams-Bashforth value minus the current value: AB2 -(0.5+eps) T^{n-1} + (1.5+eps) T^n,
 // AB3 (23 T^n - 16 T^{n-1} + 5 T^{n-2}) / 12 (oce_tracer_mod.F90:53, 67-68), eps = 0.1
 __device__ __forceinline__ float ab_delta(int ab, float t, float o1, float o2) {
     return ab == 2 ? 0.6f * (t - o1) : (11.f * (t - o1) - 5.f * (o1 - o2)) * (1.f / 12.f);
 }
 
+// upwind flux of an edge-layer in the edge's direction, -(T1 v+ + T2 v-)
+// (oce_adv_tra_hor.F90:174-177, 0.5 (v +- |v|) = v+ / v-); rounded the same way wherever it
+// is formed, so the two end nodes of an edge add and subtract the same value
+__device__ __forceinline__ float upw_flux(float T1, float T2, float v) {
+    return -__fmaf_rn(T1, fmaxf(v, 0.f), __fmul_rn(T2, fminf(v, 0.f)));
+}
 
+// vertical high-order flux of interface nz on the AB values (QR4C / UPW1 / CDIFF,
+// oce_adv_tra_ver.F90:332-434, 635-695) minus the LO flux, for one slot
+__device__ __forceinline__ float ver_ad(int ver, bool lim, float pv, int nz, int nzmin, int nzmax, bool twolayer,
+                                        float tab, float tabu, float tabu2, float tabd, float pw, float ar0, float fv0,
+                                        float fw0, float idz0, float idzp, float idzm, float g1, float g2) {
+    float Cf;
+    if (nz == nzmin) {
+        Cf = -(tab * pw * ar0);
+    } else if (ver != 0 || nz == nzmin + 1 || nz == nzmax - 1) {
+        if (ver != 1) {  // QR4C next to the ends, CDIFF everywhere
+            Cf = -(0.5f * (tabu + tab) * pw * ar0);
+        } else {
+            const float aw = fabsf(pw);
+            Cf = -(0.5f * (tab * (pw + aw) + tabu * (pw - aw)) * ar0);
+        }
+    } else {
+        const float qc = (tabu - tab) * idz0;
+        const float qu = (tab - tabd) * idzp;
+        const float qd = (tabu2 - tabu) * idzm;
+        const float Tm1 = tab + (2.f * qc + qu) * g1;
+        const float Tm2 = tabu + (2.f * qc + qd) * g2;
+        const float aw = fabsf(pw);
+        const float Tmean = (pw + aw) * Tm1 + (pw - aw) * Tm2;
+        Cf = (-(0.5f * (1.f - pv) * Tmean) - pv * (0.5f * (Tm1 + Tm2)) * pw) * ar0;
+    }
+    // flux = C - flux_in; FCT passes the LO flux in, otherwise zero
+    float F = Cf - (lim ? fw0 : 0.f);
+    // a two-layer column writes its middle interface twice (statements nzmin+1, nzmax-1)
+    if (ver == 0 && twolayer && nz == nzmin + 1) F = Cf - F;
+    return lim ? F : F - fv0;
+}
 
 // ---------------------------------------------------------------------------
 // k32_lo_ad
 // ---------------------------------------------------------------------------
-// One chunk of a node's column for every tracer of the launch.  PACK: the column's last
-// chunk with P tracers side by side in segments of W lanes; otherwise one tracer at a time
+// One chunk of a node's column for every group of the launch.  PACK: the column's last
+// chunk with P groups side by side in segments of W lanes; otherwise one group at a time
 // over the whole warp.
-template <int KD, bool WS, bool PACK>
+template <int G, int KD, bool WS, bool PACK>
 __device__ __forceinline__ void lo_ad_chunk(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
                                             const B32View &B, const float *__restrict__ VF, float dt, int n, int lane,
                                             const WEdges &S, int ch, int W, int P) {
@@ -335,150 +432,130 @@ __device__ __forceinline__ void lo_ad_chunk(const DTopo &tp, const DGeom<float> 
     const int L1 = tp.L1, nl = tp.nl;
     const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
     const unsigned own = S.own;
-    {
-        const C k = PACK ? C(nzmin, nzmax, ch, lane, W, P) : C(nzmin, nzmax, ch, lane);
-        const int nz = k.nz;
-        const int i = n * L1 + nz - 1;   // layer nz of the node (valid where k.lvl)
-        const int iv = n * nl + nz - 1;  // interface nz
-        // ---- tracer-independent part of the chunk ----
-        int off[KD];
-        float am[KD];  // upwind inflow weight of each edge slot (0 where the slot is dry)
-        unsigned okm = 0;
-        float Dh = 0.f;  // net horizontal volume flux into the node
+    const C k = PACK ? C(nzmin, nzmax, ch, lane, W, P) : C(nzmin, nzmax, ch, lane);
+    const int nz = k.nz;
+    const int i = n * L1 + nz - 1;   // layer nz of the node (valid where k.lvl)
+    const int iv = n * nl + nz - 1;  // interface nz
+    // ---- tracer-independent part of the chunk ----
+    int off[KD];
+    float vf[KD];  // volume flux of each edge slot (0 where the slot is dry)
+    unsigned okm = 0;
 #pragma unroll
-        for (int u = 0; u < KD; u++) {
-            const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
-            off[u] = S.m[u] * L1 + nz - 1;
-            const float v = ok ? VF[S.e[u] * L1 + nz - 1] : 0.f;
-            okm |= ok ? 1u << u : 0u;
-            const bool ow = (own >> u) & 1u;
-            Dh += ow ? -v : v;
-            am[u] = ow ? -fminf(v, 0.f) : fmaxf(v, 0.f);
-        }
-        float ar0 = 0.f, we0 = 0.f, w0 = 0.f, sdt = 0.f, Z0 = 0.f, hr = 0.f;
-        if (k.lvl) {
-            ar0 = g.area[iv];
-            we0 = f.we[iv];
-            w0 = f.w[iv];
-            const float ihn = qdiv(1.f, g.hnode_new[i]);
-            sdt = qdiv(dt, g.areasvol[iv]) * ihn;
-            hr = g.hnode[i] * ihn;
-            Z0 = g.Z3[i];
-        }
-        const float Zm1 = sh_up(Z0, 1), Zm2 = sh_up(Z0, 2), Zp1 = sh_dn(Z0, 1);
-        // QR4C interior geometry, nzmin+2 <= nz <= nzmax-2 (oce_adv_tra_ver.F90:409-425)
-        const bool qint = k.out && nz >= nzmin + 2 && nz <= nzmax - 2;
-        float idz0 = 0.f, idzp = 0.f, idzm = 0.f, g1 = 0.f, g2 = 0.f;
-        if (qint) {
-            const float zb = g.zbar3[iv];
-            idz0 = qdiv(1.f, Zm1 - Z0);
-            idzp = qdiv(1.f, Z0 - Zp1);
-            idzm = qdiv(1.f, Zm2 - Zm1);
-            g1 = (zb - Z0) * (1.f / 3.f);
-            g2 = (zb - Zm1) * (1.f / 3.f);
-        }
-        const bool twolayer = nzmin + 1 == nzmax - 1;
-        // ---- per tracer ----
+    for (int u = 0; u < KD; u++) {
+        const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
+        off[u] = S.m[u] * L1 + nz - 1;
+        vf[u] = ok ? VF[S.e[u] * L1 + nz - 1] : 0.f;
+        okm |= ok ? 1u << u : 0u;
+    }
+    float ar0 = 0.f, we0 = 0.f, w0 = 0.f, sdt = 0.f, Z0 = 0.f, dhr = 0.f;
+    if (k.lvl) {
+        ar0 = g.area[iv];
+        we0 = f.we[iv];
+        w0 = f.w[iv];
+        const float hn = g.hnode_new[i];
+        sdt = qdiv(dt, g.areasvol[iv] * hn);
+        dhr = qdiv(g.hnode[i] - hn, hn);
+        Z0 = g.Z3[i];
+    }
+    const float Zm1 = sh_up(Z0, 1), Zm2 = sh_up(Z0, 2), Zp1 = sh_dn(Z0, 1);
+    // QR4C interior geometry, nzmin+2 <= nz <= nzmax-2 (oce_adv_tra_ver.F90:409-425)
+    const bool qint = k.out && nz >= nzmin + 2 && nz <= nzmax - 2;
+    float idz0 = 0.f, idzp = 0.f, idzm = 0.f, g1 = 0.f, g2 = 0.f;
+    if (qint) {
+        const float zb = g.zbar3[iv];
+        idz0 = qdiv(1.f, Zm1 - Z0);
+        idzp = qdiv(1.f, Z0 - Zp1);
+        idzm = qdiv(1.f, Zm2 - Zm1);
+        g1 = (zb - Z0) * (1.f / 3.f);
+        g2 = (zb - Zm1) * (1.f / 3.f);
+    }
+    const bool twolayer = nzmin + 1 == nzmax - 1;
+    // ---- per group ----
 #pragma unroll 1
-        for (int t0 = 0; t0 < B.ntr; t0 += PACK ? P : 1) {
-            // the lane's tracer (packed: the tracer of its segment; idle past the last)
-            const int tt = t0 + k.q;
-            const bool on = tt < B.ntr;
-            const int t = on ? tt : t0;
-            const bool lvt = k.lvl && on;
-            const unsigned okt = lvt ? okm : 0u;
-            const bool lim = (B.fct_mask >> t) & 1ull;
-            const int ver = B.ver[t];
-            const size_t to = (size_t)t * B.sN;
-            const float *__restrict__ T = B.T + to;
-            const float *__restrict__ O1 = B.O1 + to;
-            const float *__restrict__ O2 = B.ab == 3 ? B.O2 + to : O1;
-            // every load of the tracer's chunk first
-            const float Tn = lvt ? T[i] : 0.f;
-            const float o1 = lvt ? O1[i] : 0.f;
-            const float o2 = (lvt && B.ab == 3) ? O2[i] : 0.f;
-            float tm[KD];
+    for (int g0 = 0; g0 < B.ng; g0 += PACK ? P : 1) {
+        // the lane's group (packed: the group of its segment; idle past the last)
+        const int gg = g0 + k.q;
+        const bool on = gg < B.ng;
+        const int gi = on ? gg : g0;
+        const bool lvt = k.lvl && on;
+        const unsigned okt = lvt ? okm : 0u;
+        const bool lim = (B.fct >> gi) & 1ull;
+        const int ver = B.ver[gi];
+        const float *__restrict__ T = grp<G>(B.T, gi, B.sN);
+        const float *__restrict__ O1 = grp<G>(B.O1, gi, B.sN);
+        const float *__restrict__ O2 = B.ab == 3 ? grp<G>(B.O2, gi, B.sN) : O1;
+        // every load of the group's chunk first
+        const Vec<G> Tn = vldc<G>(lvt, T, i);
+        const Vec<G> o1 = vldc<G>(lvt, O1, i);
+        const Vec<G> o2 = vldc<G>(lvt && B.ab == 3, O2, i);
+        Vec<G> tm[KD];
 #pragma unroll
-            for (int u = 0; u < KD; u++) tm[u] = ((okt >> u) & 1u) ? T[off[u]] : 0.f;
-            const float tab = Tn + (lvt ? ab_delta(B.ab, Tn, o1, o2) : 0.f);
-            const float Tu = sh_up(Tn, 1);
+        for (int u = 0; u < KD; u++) tm[u] = vldc<G>((okt >> u) & 1u, T, off[u]);
+        Vec<G> lo, ad;
+#pragma unroll
+        for (int c = 0; c < G; c++) {
+            const float tn = Tn.c[c];
+            const float tab = tn + (lvt ? ab_delta(B.ab, tn, o1.c[c], o2.c[c]) : 0.f);
+            const float Tu = sh_up(tn, 1);
             const float tabu = sh_up(tab, 1), tabu2 = sh_up(tab, 2), tabd = sh_dn(tab, 1);
-            // LO: upwind edge fluxes in difference form, sum_j am_j (T_j - T_n) + Dh T_n
-            float hs = Dh * Tn;
+            // LO: the upwind edge fluxes, + at edges(1,e), - at edges(2,e), in ascending edge
+            // order (oce_adv_tra_driver.F90:131-190)
+            float hs = 0.f;
 #pragma unroll
-            for (int u = 0; u < KD; u++)
-                if ((okt >> u) & 1u) hs += am[u] * (tm[u] - Tn);
+            for (int u = 0; u < KD; u++) {
+                const bool ow = (own >> u) & 1u;
+                const float tmv = tm[u].c[c];
+                const float F = upw_flux(ow ? tn : tmv, ow ? tmv : tn, vf[u]);
+                hs += ((okt >> u) & 1u) ? (ow ? F : -F) : 0.f;
+            }
             // upwind vertical flux with w_e at interface nz (adv_tra_ver_upw1)
             float fv0 = 0.f;
             if (lvt) {
                 if (nz == nzmin) {
-                    fv0 = -(we0 * Tn * ar0);
+                    fv0 = -(we0 * tn * ar0);
                 } else {
                     const float aw = fabsf(we0);
-                    fv0 = -(0.5f * (Tn * (we0 + aw) + Tu * (we0 - aw)) * ar0);
+                    fv0 = -(0.5f * (tn * (we0 + aw) + Tu * (we0 - aw)) * ar0);
                 }
             }
             float fv1 = sh_dn(fv0, 1);
             if (nz == nzmax - 1) fv1 = 0.f;
-            // LO = (T hnode + flux divergence dt / areasvol) / hnode_new (oce_adv_tra_driver.F90:249)
-            if (k.out && on) B.LO[to + i] = Tn * hr + (hs + fv0 - fv1) * sdt;
+            // LO = (T hnode + flux divergence dt / areasvol) / hnode_new (oce_adv_tra_driver.F90:249),
+            // as T + T (hnode - hnode_new) / hnode_new + flux divergence dt / (areasvol hnode_new)
+            lo.c[c] = tn + fmaf(tn, dhr, (hs + (fv0 - fv1)) * sdt);
             // with the split vertical velocity the LO part of the antidiffusive flux is the upwind
             // flux of the full w (oce_adv_tra_driver.F90:323-334)
             float fw0 = fv0;
             if (WS && f.wsplit && lvt) {
                 if (nz == nzmin) {
-                    fw0 = -(w0 * Tn * ar0);
+                    fw0 = -(w0 * tn * ar0);
                 } else {
                     const float aw = fabsf(w0);
-                    fw0 = -(0.5f * (Tn * (w0 + aw) + Tu * (w0 - aw)) * ar0);
+                    fw0 = -(0.5f * (tn * (w0 + aw) + Tu * (w0 - aw)) * ar0);
                 }
             }
-            // vertical high-order flux on the AB values (QR4C / UPW1 / CDIFF; PPM in k32_vppm),
-            // minus the LO flux
-            if (k.out && on && ver != 3) {
-                const float pw = lim ? w0 : we0;
-                float Cf;
-                if (nz == nzmin) {
-                    Cf = -(tab * pw * ar0);
-                } else if (ver != 0 || nz == nzmin + 1 || nz == nzmax - 1) {
-                    if (ver != 1) {  // QR4C next to the ends, CDIFF everywhere
-                        Cf = -(0.5f * (tabu + tab) * pw * ar0);
-                    } else {
-                        const float aw = fabsf(pw);
-                        Cf = -(0.5f * (tab * (pw + aw) + tabu * (pw - aw)) * ar0);
-                    }
-                } else {
-                    const float qc = (tabu - tab) * idz0;
-                    const float qu = (tab - tabd) * idzp;
-                    const float qd = (tabu2 - tabu) * idzm;
-                    const float Tm1 = tab + (2.f * qc + qu) * g1;
-                    const float Tm2 = tabu + (2.f * qc + qd) * g2;
-                    const float aw = fabsf(pw), no = B.pv[t];
-                    const float Tmean = (pw + aw) * Tm1 + (pw - aw) * Tm2;
-                    Cf = (-(0.5f * (1.f - no) * Tmean) - no * (0.5f * (Tm1 + Tm2)) * pw) * ar0;
-                }
-                // flux = C - flux_in; FCT passes the LO flux in, otherwise zero
-                const float fin = lim ? fw0 : 0.f;
-                float F = Cf - fin;
-                // a two-layer column writes its middle interface twice (statements nzmin+1, nzmax-1)
-                if (ver == 0 && twolayer && nz == nzmin + 1) F = Cf - F;
-                B.ADv[(size_t)t * B.sNI + iv] = lim ? F : F - fv0;
-            }
+            ad.c[c] = ver_ad(ver, lim, B.pv[gi * G + c], nz, nzmin, nzmax, twolayer, tab, tabu, tabu2, tabd,
+                             lim ? w0 : we0, ar0, fv0, fw0, idz0, idzp, idzm, g1, g2);
+        }
+        if (k.out && on) {
+            vst<G>(grp<G>(B.LO, gi, B.sN), i, lo);
+            // PPM fluxes come from k32_vppm
+            if (ver != 3) vst<G>(grp<G>(B.ADv, gi, B.sNI), iv, ad);
         }
     }
 }
 
-template <int KD, bool WS, bool PK>
+template <int G, int KD, bool WS, bool PK>
 __device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
                                            const B32View &B, const float *__restrict__ VF, float dt, int n, int lane,
                                            const WEdges &S) {
     using C = Chunk<2, 1>;
     const int nch = C::count(S.nzmin, S.nzmax);
-    for (int ch = 0; ch < nch - 1; ch++) lo_ad_chunk<KD, WS, false>(tp, g, f, B, VF, dt, n, lane, S, ch, 32, 1);
+    for (int ch = 0; ch < nch - 1; ch++) lo_ad_chunk<G, KD, WS, false>(tp, g, f, B, VF, dt, n, lane, S, ch, 32, 1);
     const int W = C::last_width(S.nzmin, S.nzmax), P = 32 / W;
-    // packed only for nodes of at most 6 edges, as in k32_bounds
-    if (PK && KD <= 6 && P > 1) lo_ad_chunk<KD, WS, true>(tp, g, f, B, VF, dt, n, lane, S, nch - 1, W, P);
-    else lo_ad_chunk<KD, WS, false>(tp, g, f, B, VF, dt, n, lane, S, nch - 1, 32, 1);
+    // packed only for nodes of at most 6 edges (the wider packed bodies would spill)
+    if (PK && KD <= 6 && P > 1) lo_ad_chunk<G, KD, WS, true>(tp, g, f, B, VF, dt, n, lane, S, nch - 1, W, P);
+    else lo_ad_chunk<G, KD, WS, false>(tp, g, f, B, VF, dt, n, lane, S, nch - 1, 32, 1);
 }
 
 // the node of warp unit j: consecutive nodes, or (WIDE) the listed nodes of more than 8 edges
@@ -487,9 +564,13 @@ __device__ __forceinline__ int unit_node(const DTopo &tp, int j) {
     if (WIDE) return j < tp.n_wide ? tp.wide_nodes[j] : -1;
     return j < tp.N2 ? j : -1;
 }
+template <bool WIDE>
+__device__ __forceinline__ int node_units(const DTopo &tp) {
+    return WIDE ? tp.n_wide : tp.N2;
+}
 
 // WS: the split vertical velocity (a separate instantiation keeps the default path unchanged)
-template <bool WIDE, bool WS, bool PK>
+template <int G, bool WIDE, bool WS, bool PK>
 __device__ __forceinline__ void lo_ad_unit(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
                                            const B32View &B, const float *__restrict__ VF, float dt, int j, WEdges *Se) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -498,16 +579,20 @@ __device__ __forceinline__ void lo_ad_unit(const DTopo &tp, const DGeom<float> &
     WEdges &S = Se[warp];
     stage_edges(tp, n, lane, S);
     if ((S.deg > 8) != WIDE) return;
-    if (WIDE) lo_ad_node<kMaxDeg, WS, PK>(tp, g, f, B, VF, dt, n, lane, S);
-    else if (S.deg <= 6) lo_ad_node<6, WS, PK>(tp, g, f, B, VF, dt, n, lane, S);
-    else lo_ad_node<8, WS, PK>(tp, g, f, B, VF, dt, n, lane, S);
+    if (WIDE) lo_ad_node<G, kMaxDeg, WS, PK>(tp, g, f, B, VF, dt, n, lane, S);
+    else if (S.deg <= 6) lo_ad_node<G, 6, WS, PK>(tp, g, f, B, VF, dt, n, lane, S);
+    else lo_ad_node<G, 8, WS, PK>(tp, g, f, B, VF, dt, n, lane, S);
 }
 
-template <bool WIDE, bool WS>
-__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_LO)
+// grid-stride loop of the warps over the units (one launch may hold fewer blocks than units)
+#define FOR_WARP_UNITS(j, count)                                                               \
+    for (int j = blockIdx.x * kWB + (threadIdx.x >> 5); j < (count); j += gridDim.x * kWB)
+
+template <int G, bool WIDE, bool WS>
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : MinB<G>::lo)
 k32_lo_ad(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, const float *__restrict__ VF, float dt) {
     __shared__ WEdges Se[kWB];
-    lo_ad_unit<WIDE, WS, true>(tp, g, f, B, VF, dt, blockIdx.x * kWB + (threadIdx.x >> 5), Se);
+    FOR_WARP_UNITS(j, node_units<WIDE>(tp)) lo_ad_unit<G, WIDE, WS, true>(tp, g, f, B, VF, dt, j, Se);
 }
 
 // high-order minus low-order flux of one edge-layer from the two end values, their
@@ -517,10 +602,10 @@ __device__ __forceinline__ float ho_minus_lo(int hor, float ph, int ab, float T1
     const float vp = fmaxf(v, 0.f), vm = fminf(v, 0.f);
     const float t1 = T1 + ab_delta(ab, T1, o1a, o2a);
     const float t2 = T2 + ab_delta(ab, T2, o1b, o2b);
-    const float flo = -(T1 * vp + T2 * vm);
+    const float flo = upw_flux(T1, T2, v);
     float hf;
     if (hor == 2) {
-        hf = -(t1 * vp + t2 * vm);
+        hf = upw_flux(t1, t2, v);
     } else {
         // c_lo = 1 up to nboundary_lay (MUSCL), always 1 (MFCT)
         const float clo1 = hor == 0 ? cl1 : 1.f, clo2 = hor == 0 ? cl2 : 1.f;
@@ -549,8 +634,8 @@ __device__ __forceinline__ float ho_minus_lo(int hor, float ph, int ab, float T1
 // k32_ho_nodemean.
 //
 // A pass covers 32 levels of the edge; the last pass, when its levels fill at most half a
-// warp, carries P tracers side by side in segments of W lanes (PACK).
-template <bool PACK>
+// warp, carries P groups side by side in segments of W lanes (PACK).
+template <int G, bool PACK>
 __device__ __forceinline__ void ho_pass(const DTopo &tp, const B32View &B, const MusclW &mw,
                                         const float *__restrict__ VF, int e, int nz0, int W, int P, int lane) {
     const int L1 = tp.L1;
@@ -564,120 +649,117 @@ __device__ __forceinline__ void ho_pass(const DTopo &tp, const B32View &B, const
     const int nz = nz0 + lane - q * W;
     const bool tri = nz >= gzmin && nz <= gzmax - 1;
     const bool ok = nz <= ehi && q < P;
+    if (!ok) return;
     const int ie = e * L1 + nz - 1, ia = n1 * L1 + nz - 1, ib = n2 * L1 + nz - 1;
-    const float v = ok ? VF[ie] : 0.f;
+    const float v = VF[ie];
     const float cl1 = (nbl1 - nz) >= 0 ? 1.f : 0.f, cl2 = (nbl2 - nz) >= 0 ? 1.f : 0.f;
     const int ua = un.y * L1 + nz - 1, ub = un.z * L1 + nz - 1;
     const int da = dn.y * L1 + nz - 1, db = dn.z * L1 + nz - 1;
-    if (!ok) return;
-    // two tracers per pass: their gathers in flight together (packed: tracers t0 + q and
-    // t0 + P + q of the segment)
-    const int step = PACK ? P : 1;
 #pragma unroll 1
-    for (int t0 = 0; t0 < B.ntr; t0 += 2 * step) {
-        float T1[2], T2[2], o1a[2], o1b[2], o2a[2], o2b[2], ga[2], gb[2], gc[2], gd[2];
-        bool grad[2], on[2];
-        int tt[2];
+    for (int g0 = 0; g0 < B.ng; g0 += PACK ? P : 1) {
+        const int gq = g0 + q;
+        if (gq >= B.ng) break;
+        const int hor = B.hor[gq];
+        // MUSCL / MFCT levels outside the triangles' range: the node-mean launch
+        if (hor != 2 && !tri) continue;
+        const bool grad = hor != 2;
+        const float *__restrict__ T = grp<G>(B.T, gq, B.sN);
+        const float *__restrict__ O1 = grp<G>(B.O1, gq, B.sN);
+        const float *__restrict__ O2 = B.ab == 3 ? grp<G>(B.O2, gq, B.sN) : O1;
+        const Vec<G> T1 = vld<G>(T, ia), T2 = vld<G>(T, ib);
+        const Vec<G> o1a = vld<G>(O1, ia), o1b = vld<G>(O1, ib);
+        const Vec<G> o2a = vldc<G>(B.ab == 3, O2, ia), o2b = vldc<G>(B.ab == 3, O2, ib);
+        const Vec<G> ga = vldc<G>(grad, T, ua), gb = vldc<G>(grad, T, ub);
+        const Vec<G> gc = vldc<G>(grad, T, da), gd = vldc<G>(grad, T, db);
+        Vec<G> out;
 #pragma unroll
-        for (int r = 0; r < 2; r++) {
-            const int tq = t0 + r * step + q;
-            on[r] = tq < B.ntr;
-            tt[r] = on[r] ? tq : t0;
-            const size_t to = (size_t)tt[r] * B.sN;
-            const float *__restrict__ T = B.T + to;
-            grad[r] = on[r] && B.hor[tt[r]] != 2 && tri;
-            T1[r] = on[r] ? T[ia] : 0.f;
-            T2[r] = on[r] ? T[ib] : 0.f;
-            o1a[r] = on[r] ? B.O1[to + ia] : 0.f;
-            o1b[r] = on[r] ? B.O1[to + ib] : 0.f;
-            o2a[r] = (on[r] && B.ab == 3) ? B.O2[to + ia] : 0.f;
-            o2b[r] = (on[r] && B.ab == 3) ? B.O2[to + ib] : 0.f;
-            ga[r] = grad[r] ? T[ua] : 0.f;
-            gb[r] = grad[r] ? T[ub] : 0.f;
-            gc[r] = grad[r] ? T[da] : 0.f;
-            gd[r] = grad[r] ? T[db] : 0.f;
+        for (int c = 0; c < G; c++) {
+            const float s1 = wu.y * (ga.c[c] - T1.c[c]) + wu.z * (gb.c[c] - T1.c[c]);
+            const float s2 = wd.y * (gc.c[c] - T2.c[c]) + wd.z * (gd.c[c] - T2.c[c]);
+            out.c[c] = ho_minus_lo(hor, B.ph[gq * G + c], B.ab, T1.c[c], T2.c[c], o1a.c[c], o1b.c[c], o2a.c[c],
+                                   o2b.c[c], s1, s2, v, cl1, cl2);
         }
-#pragma unroll
-        for (int r = 0; r < 2; r++) {
-            if (!on[r]) continue;
-            const int hor = B.hor[tt[r]];
-            // MUSCL / MFCT levels outside the triangles' range: the fallback launch
-            if (hor != 2 && !tri) continue;
-            const float s1 = wu.y * (ga[r] - T1[r]) + wu.z * (gb[r] - T1[r]);
-            const float s2 = wd.y * (gc[r] - T2[r]) + wd.z * (gd[r] - T2[r]);
-            B.ADh[(size_t)tt[r] * B.sE + ie] = ho_minus_lo(hor, B.ph[tt[r]], B.ab, T1[r], T2[r], o1a[r], o1b[r],
-                                                           o2a[r], o2b[r], s1, s2, v, cl1, cl2);
-        }
+        vst<G>(grp<G>(B.ADh, gq, B.sE), ie, out);
     }
 }
 
-template <bool PK>
+template <int G, bool PK>
 __device__ __forceinline__ void ho_unit(const DTopo &tp, const B32View &B, const MusclW &mw,
                                         const float *__restrict__ VF, int e) {
     const int lane = threadIdx.x & 31;
     if (e >= tp.E2) return;
     const int elo = tp.e_lo[e], ehi = tp.e_hi[e];
     int nz0 = elo;
-    for (; nz0 + 32 <= ehi; nz0 += 32) ho_pass<false>(tp, B, mw, VF, e, nz0, 32, 1, lane);
+    for (; nz0 + 32 <= ehi; nz0 += 32) ho_pass<G, false>(tp, B, mw, VF, e, nz0, 32, 1, lane);
     const int W = ehi - nz0 + 1;
     if (W < 1) return;
     const int P = 32 / W;
-    if (PK && P > 1) ho_pass<true>(tp, B, mw, VF, e, nz0, W, P, lane);
-    else ho_pass<false>(tp, B, mw, VF, e, nz0, 32, 1, lane);
+    if (PK && P > 1) ho_pass<G, true>(tp, B, mw, VF, e, nz0, W, P, lane);
+    else ho_pass<G, false>(tp, B, mw, VF, e, nz0, 32, 1, lane);
 }
 
-__global__ void __launch_bounds__(kTB, FESOM_MINB_HO)
-k32_ho(DTopo tp, B32View B, MusclW mw, const float *__restrict__ VF) {
-    ho_unit<true>(tp, B, mw, VF, blockIdx.x * kWB + (threadIdx.x >> 5));
+template <int G>
+__global__ void __launch_bounds__(kTB, MinB<G>::ho) k32_ho(DTopo tp, B32View B, MusclW mw, const float *__restrict__ VF) {
+    FOR_WARP_UNITS(e, tp.E2) ho_unit<G, true>(tp, B, mw, VF, e);
 }
 
 // The edge-layers of the node-mean gradients: one thread per (edge, level) item, every
-// tracer, with the projected mean gradients as precomputed neighbour weights.
+// group, with the projected mean gradients as precomputed neighbour weights.
+template <int G>
 __device__ __forceinline__ void nodemean_item(const DTopo &tp, const B32View &B, const MusclW &mw,
                                               const float *__restrict__ VF, int j) {
     const int L1 = tp.L1;
-    {
-        const int e = mw.it_e[j], nz = mw.it_nz[j];
-        const int p0 = mw.it_ptr[j], p1 = p0 + mw.it_n1[j], p2 = mw.it_ptr[j + 1];
-        const int n1 = tp.e_n1[e], n2 = tp.e_n2[e];
-        const int ie = e * L1 + nz - 1, ia = n1 * L1 + nz - 1, ib = n2 * L1 + nz - 1;
-        const float v = VF[ie];
-        const float cl1 = (tp.n_nbl[n1] - nz) >= 0 ? 1.f : 0.f, cl2 = (tp.n_nbl[n2] - nz) >= 0 ? 1.f : 0.f;
+    const int e = mw.it_e[j], nz = mw.it_nz[j];
+    const int p0 = mw.it_ptr[j], p1 = p0 + mw.it_n1[j], p2 = mw.it_ptr[j + 1];
+    const int n1 = tp.e_n1[e], n2 = tp.e_n2[e];
+    const int ie = e * L1 + nz - 1, ia = n1 * L1 + nz - 1, ib = n2 * L1 + nz - 1;
+    const float v = VF[ie];
+    const float cl1 = (tp.n_nbl[n1] - nz) >= 0 ? 1.f : 0.f, cl2 = (tp.n_nbl[n2] - nz) >= 0 ? 1.f : 0.f;
 #pragma unroll 1
-        for (int t = 0; t < B.ntr; t++) {
-            const int hor = B.hor[t];
-            if (hor == 2) continue;  // UPW1 has no gradients: k32_ho wrote it
-            const size_t to = (size_t)t * B.sN;
-            const float *__restrict__ T = B.T + to;
-            const float T1 = T[ia], T2 = T[ib];
-            const float o1a = B.O1[to + ia], o1b = B.O1[to + ib];
-            const float o2a = B.ab == 3 ? B.O2[to + ia] : 0.f, o2b = B.ab == 3 ? B.O2[to + ib] : 0.f;
-            float s1 = 0.f, s2 = 0.f;
-            for (int p = p0; p < p1; p++) {
-                const int2 q = mw.pairs[p];
-                s1 += __int_as_float(q.y) * (T[q.x * L1 + nz - 1] - T1);
-            }
-            for (int p = p1; p < p2; p++) {
-                const int2 q = mw.pairs[p];
-                s2 += __int_as_float(q.y) * (T[q.x * L1 + nz - 1] - T2);
-            }
-            B.ADh[(size_t)t * B.sE + ie] = ho_minus_lo(hor, B.ph[t], B.ab, T1, T2, o1a, o1b, o2a, o2b, s1, s2, v, cl1, cl2);
+    for (int gq = 0; gq < B.ng; gq++) {
+        const int hor = B.hor[gq];
+        if (hor == 2) continue;  // UPW1 has no gradients: k32_ho wrote it
+        const float *__restrict__ T = grp<G>(B.T, gq, B.sN);
+        const float *__restrict__ O1 = grp<G>(B.O1, gq, B.sN);
+        const Vec<G> T1 = vld<G>(T, ia), T2 = vld<G>(T, ib);
+        const Vec<G> o1a = vld<G>(O1, ia), o1b = vld<G>(O1, ib);
+        const Vec<G> o2a = vldc<G>(B.ab == 3, grp<G>(B.O2, gq, B.sN), ia);
+        const Vec<G> o2b = vldc<G>(B.ab == 3, grp<G>(B.O2, gq, B.sN), ib);
+        Vec<G> s1 = vfill<G>(0.f), s2 = vfill<G>(0.f);
+        for (int p = p0; p < p1; p++) {
+            const int2 q = mw.pairs[p];
+            const Vec<G> t = vld<G>(T, q.x * L1 + nz - 1);
+#pragma unroll
+            for (int c = 0; c < G; c++) s1.c[c] += __int_as_float(q.y) * (t.c[c] - T1.c[c]);
         }
+        for (int p = p1; p < p2; p++) {
+            const int2 q = mw.pairs[p];
+            const Vec<G> t = vld<G>(T, q.x * L1 + nz - 1);
+#pragma unroll
+            for (int c = 0; c < G; c++) s2.c[c] += __int_as_float(q.y) * (t.c[c] - T2.c[c]);
+        }
+        Vec<G> out;
+#pragma unroll
+        for (int c = 0; c < G; c++)
+            out.c[c] = ho_minus_lo(hor, B.ph[gq * G + c], B.ab, T1.c[c], T2.c[c], o1a.c[c], o1b.c[c], o2a.c[c],
+                                   o2b.c[c], s1.c[c], s2.c[c], v, cl1, cl2);
+        vst<G>(grp<G>(B.ADh, gq, B.sE), ie, out);
     }
 }
 
+template <int G>
 __global__ void __launch_bounds__(256) k32_ho_nodemean(DTopo tp, B32View B, MusclW mw, const float *__restrict__ VF) {
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < mw.n_items; j += gridDim.x * blockDim.x)
-        nodemean_item(tp, B, mw, VF, j);
+        nodemean_item<G>(tp, B, mw, VF, j);
 }
 
 // ---------------------------------------------------------------------------
-// k32_bounds: FCT bounds and R+ / R- (FCT tracers only)
+// k32_bounds: FCT bounds and R+ / R- (FCT groups only)
 // ---------------------------------------------------------------------------
-// One chunk of a node's column for the FCT tracers of the launch.  PACK: the column's last
-// chunk with P tracers side by side in segments of W lanes (its few levels would leave most
-// lanes idle); otherwise one tracer at a time over the whole warp.
-template <int KD, bool PACK>
+// One chunk of a node's column for the FCT groups of the launch.  PACK: the column's last
+// chunk with P groups side by side in segments of W lanes; otherwise one group at a time
+// over the whole warp.
+template <int G, int KD, bool PACK>
 __device__ __forceinline__ void bounds_chunk(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int n,
                                              int lane, const WEdges &S, int ch, int W, int P) {
     using C = Chunk<1, 1>;
@@ -688,104 +770,115 @@ __device__ __forceinline__ void bounds_chunk(const DTopo &tp, const DGeom<float>
     const C k = PACK ? C(nzmin, nzmax, ch, lane, W, P) : C(nzmin, nzmax, ch, lane);
     const int nz = k.nz;
     const int i = n * L1 + nz - 1, iv = n * nl + nz - 1;
-    int off[KD];
+    int off[KD], eo[KD];
     unsigned okm = 0;
 #pragma unroll
     for (int u = 0; u < KD; u++) {
         const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
         off[u] = S.m[u] * L1 + nz - 1;
+        eo[u] = S.e[u] * L1 + nz - 1;
         okm |= ok ? 1u << u : 0u;
     }
     const float s = k.lvl ? qdiv(dt, g.areasvol[iv] * g.hnode_new[i]) : 0.f;
-    unsigned long long todo = B.fct_mask & (B.ntr >= 64 ? ~0ull : ((1ull << B.ntr) - 1));
-    int t0 = 0;
-    while (PACK ? t0 < B.ntr : todo != 0ull) {
-        // the lane's tracer: the next FCT tracer, or (packed) tracer t0 + q of the segment,
-        // idle where that tracer has no FCT
-        int t;
+    unsigned long long todo = B.fct & (B.ng >= 64 ? ~0ull : ((1ull << B.ng) - 1));
+    int g0 = 0;
+    while (PACK ? g0 < B.ng : todo != 0ull) {
+        // the lane's group: the next FCT group, or (packed) group g0 + q of the segment, idle
+        // where that group has no FCT
+        int gq;
         if (PACK) {
-            t = t0 + k.q;
-            if (t >= B.ntr || !((B.fct_mask >> t) & 1ull)) t = -1;
-            t0 += P;
+            gq = g0 + k.q;
+            if (gq >= B.ng || !((B.fct >> gq) & 1ull)) gq = -1;
+            g0 += P;
         } else {
-            t = __ffsll((long long)todo) - 1;
+            gq = __ffsll((long long)todo) - 1;
             todo &= todo - 1;
         }
-        const bool lv = k.lvl && t >= 0;
+        const bool lv = k.lvl && gq >= 0;
         const unsigned okt = lv ? okm : 0u;
-        const size_t to = (size_t)(t < 0 ? 0 : t) * B.sN;
-        const float *__restrict__ T = B.T + to;
-        const float *__restrict__ LO = B.LO + to;
-        const float *__restrict__ ADh = B.ADh + (size_t)(t < 0 ? 0 : t) * B.sE;
-        // every load of the tracer's chunk first
-        const float Tn = lv ? T[i] : 0.f;
-        const float lo = lv ? LO[i] : 0.f;
-        const float v0 = lv ? B.ADv[(size_t)(t < 0 ? 0 : t) * B.sNI + iv] : 0.f;
-        float tm[KD], lm[KD], x[KD];
-#pragma unroll
-        for (int u = 0; u < KD; u++) {
-            const bool ok = (okt >> u) & 1u;
-            tm[u] = ok ? T[off[u]] : 0.f;
-            lm[u] = ok ? LO[off[u]] : 0.f;
-            // packed chunks: the edge fluxes after the bounds (fewer values live at once)
-            if (!PACK) x[u] = ok ? ADh[S.e[u] * L1 + nz - 1] : 0.f;
-        }
+        const int gs = gq < 0 ? 0 : gq;
+        const float *__restrict__ T = grp<G>(B.T, gs, B.sN);
+        const float *__restrict__ LO = grp<G>(B.LO, gs, B.sN);
+        const float *__restrict__ ADh = grp<G>(B.ADh, gs, B.sE);
+        const Vec<G> Tn = vldc<G>(lv, T, i);
+        const Vec<G> lo = vldc<G>(lv, LO, i);
+        const Vec<G> v0 = vldc<G>(lv, grp<G>(B.ADv, gs, B.sNI), iv);
         // bounds over the node, its neighbours and the layers above and below
         // (oce_adv_tra_fct.F90:124-248)
-        float mx = fmaxf(lo, Tn), mn = fminf(lo, Tn);
-        float Pp = 0.f, M = 0.f;
+        Vec<G> mx, mn;
+#pragma unroll
+        for (int c = 0; c < G; c++) {
+            mx.c[c] = fmaxf(lo.c[c], Tn.c[c]);
+            mn.c[c] = fminf(lo.c[c], Tn.c[c]);
+        }
 #pragma unroll
         for (int u = 0; u < KD; u++) {
             const bool ok = (okt >> u) & 1u;
-            const float a = ok ? tm[u] : Tn, b = ok ? lm[u] : lo;
-            mx = fmaxf(mx, fmaxf(a, b));
-            mn = fminf(mn, fminf(a, b));
-        }
-        if (PACK) {
+            const Vec<G> tm = vldc<G>(ok, T, off[u]);
+            const Vec<G> lm = vldc<G>(ok, LO, off[u]);
 #pragma unroll
-            for (int u = 0; u < KD; u++) x[u] = ((okt >> u) & 1u) ? ADh[S.e[u] * L1 + nz - 1] : 0.f;
-        }
-#pragma unroll
-        for (int u = 0; u < KD; u++) {
-            const float xv = ((own >> u) & 1u) ? x[u] : -x[u];
-            Pp += fmaxf(0.f, xv);
-            M += fminf(0.f, xv);
-        }
-        const float mxu = sh_up(mx, 1), mxd = sh_dn(mx, 1), mnu = sh_up(mn, 1), mnd = sh_dn(mn, 1);
-        float tup = mx, tlo = mn;
-        if (nz != nzmin && nz != nzmax - 1) {
-            tup = fmaxf(fmaxf(mxu, mx), mxd);
-            tlo = fminf(fminf(mnu, mn), mnd);
+            for (int c = 0; c < G; c++) {
+                const float a = ok ? tm.c[c] : Tn.c[c], b = ok ? lm.c[c] : lo.c[c];
+                mx.c[c] = fmaxf(mx.c[c], fmaxf(a, b));
+                mn.c[c] = fminf(mn.c[c], fminf(a, b));
+            }
         }
         // P / M: sums of the positive / negative antidiffusive fluxes into the node
-        float v1 = sh_dn(v0, 1);
-        if (nz == nzmax - 1) v1 = 0.f;
-        Pp += fmaxf(0.f, v0) + fmaxf(0.f, -v1);
-        M += fminf(0.f, v0) + fminf(0.f, -v1);
-        if (k.out && t >= 0) {
-            const float bmx = tup - lo, bmn = tlo - lo;
-            B.R[to + i] = make_float2(fminf(1.f, qdiv(bmx, Pp * s + eps)), fminf(1.f, qdiv(bmn, M * s - eps)));
-            // the bounds themselves: the update clamps the advected value into them, so
-            // FP32 rounding in the limiter can never create a new extremum
-            B.TB[to + i] = make_float2(tup, tlo);
+        Vec<G> Pp = vfill<G>(0.f), M = vfill<G>(0.f);
+#pragma unroll
+        for (int u = 0; u < KD; u++) {
+            const Vec<G> x = vldc<G>((okt >> u) & 1u, ADh, eo[u]);
+            const bool ow = (own >> u) & 1u;
+#pragma unroll
+            for (int c = 0; c < G; c++) {
+                const float xv = ow ? x.c[c] : -x.c[c];
+                Pp.c[c] += fmaxf(0.f, xv);
+                M.c[c] += fminf(0.f, xv);
+            }
+        }
+        Vec<G> rp, rm, bp, bm;
+#pragma unroll
+        for (int c = 0; c < G; c++) {
+            const float mxu = sh_up(mx.c[c], 1), mxd = sh_dn(mx.c[c], 1);
+            const float mnu = sh_up(mn.c[c], 1), mnd = sh_dn(mn.c[c], 1);
+            float tup = mx.c[c], tlo = mn.c[c];
+            if (nz != nzmin && nz != nzmax - 1) {
+                tup = fmaxf(fmaxf(mxu, mx.c[c]), mxd);
+                tlo = fminf(fminf(mnu, mn.c[c]), mnd);
+            }
+            float v1 = sh_dn(v0.c[c], 1);
+            if (nz == nzmax - 1) v1 = 0.f;
+            const float pp = Pp.c[c] + (fmaxf(0.f, v0.c[c]) + fmaxf(0.f, -v1));
+            const float mm = M.c[c] + (fminf(0.f, v0.c[c]) + fminf(0.f, -v1));
+            const float bmx = tup - lo.c[c], bmn = tlo - lo.c[c];
+            rp.c[c] = fminf(1.f, qdiv(bmx, pp * s + eps));
+            rm.c[c] = fminf(1.f, qdiv(bmn, mm * s - eps));
+            // the bounds themselves: the update clamps the advected value into them, so FP32
+            // rounding in the limiter can never create a new extremum
+            bp.c[c] = tup;
+            bm.c[c] = tlo;
+        }
+        if (k.out && gq >= 0) {
+            vst<G>(grp<G>(B.Rp, gq, B.sN), i, rp);
+            vst<G>(grp<G>(B.Rm, gq, B.sN), i, rm);
+            vst<G>(grp<G>(B.Bp, gq, B.sN), i, bp);
+            vst<G>(grp<G>(B.Bm, gq, B.sN), i, bm);
         }
     }
 }
 
-template <int KD, bool PK>
+template <int G, int KD, bool PK>
 __device__ __forceinline__ void bounds_node(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int n,
                                             int lane, const WEdges &S) {
     using C = Chunk<1, 1>;
     const int nch = C::count(S.nzmin, S.nzmax);
-    for (int ch = 0; ch < nch - 1; ch++) bounds_chunk<KD, false>(tp, g, B, dt, n, lane, S, ch, 32, 1);
+    for (int ch = 0; ch < nch - 1; ch++) bounds_chunk<G, KD, false>(tp, g, B, dt, n, lane, S, ch, 32, 1);
     const int W = C::last_width(S.nzmin, S.nzmax), P = 32 / W;
-    // packed only for nodes of at most 6 edges (nearly all of an ocean mesh's): the wider
-    // packed body would spill registers
-    if (PK && KD <= 6 && P > 1) bounds_chunk<KD, true>(tp, g, B, dt, n, lane, S, nch - 1, W, P);
-    else bounds_chunk<KD, false>(tp, g, B, dt, n, lane, S, nch - 1, 32, 1);
+    if (PK && KD <= 6 && P > 1) bounds_chunk<G, KD, true>(tp, g, B, dt, n, lane, S, nch - 1, W, P);
+    else bounds_chunk<G, KD, false>(tp, g, B, dt, n, lane, S, nch - 1, 32, 1);
 }
 
-template <bool WIDE, bool PK>
+template <int G, bool WIDE, bool PK>
 __device__ __forceinline__ void bounds_unit(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int j,
                                             WEdges *Se) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -794,44 +887,22 @@ __device__ __forceinline__ void bounds_unit(const DTopo &tp, const DGeom<float> 
     WEdges &S = Se[warp];
     stage_edges(tp, n, lane, S);
     if ((S.deg > 8) != WIDE) return;
-    if (WIDE) bounds_node<kMaxDeg, PK>(tp, g, B, dt, n, lane, S);
-    else if (S.deg <= 6) bounds_node<6, PK>(tp, g, B, dt, n, lane, S);
-    else bounds_node<8, PK>(tp, g, B, dt, n, lane, S);
+    if (WIDE) bounds_node<G, kMaxDeg, PK>(tp, g, B, dt, n, lane, S);
+    else if (S.deg <= 6) bounds_node<G, 6, PK>(tp, g, B, dt, n, lane, S);
+    else bounds_node<G, 8, PK>(tp, g, B, dt, n, lane, S);
 }
 
-template <bool WIDE>
-__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_BOUNDS) k32_bounds(DTopo tp, DGeom<float> g, B32View B, float dt) {
+template <int G, bool WIDE>
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : MinB<G>::bounds)
+k32_bounds(DTopo tp, DGeom<float> g, B32View B, float dt) {
     __shared__ WEdges Se[kWB];
-    bounds_unit<WIDE, true>(tp, g, B, dt, blockIdx.x * kWB + (threadIdx.x >> 5), Se);
+    FOR_WARP_UNITS(j, node_units<WIDE>(tp)) bounds_unit<G, WIDE, true>(tp, g, B, dt, j, Se);
 }
 
 // ---------------------------------------------------------------------------
-// k32_update: limited update, T*, implicit vertical diffusion (warp scans)
+// k32_update: limited update, T*
 // ---------------------------------------------------------------------------
-// inclusive scan over lanes of affine maps y -> A*y + B, composed in lane order
-__device__ __forceinline__ void scan_up(float &A, float &B, int lane) {
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-        const float Ap = __shfl_up_sync(kFull, A, off), Bp = __shfl_up_sync(kFull, B, off);
-        if (lane >= off) {
-            B = A * Bp + B;
-            A = A * Ap;
-        }
-    }
-}
-// the same, composed in reverse lane order (lane 31 first)
-__device__ __forceinline__ void scan_down(float &A, float &B, int lane) {
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-        const float An = __shfl_down_sync(kFull, A, off), Bn = __shfl_down_sync(kFull, B, off);
-        if (lane + off < 32) {
-            B = A * Bn + B;
-            A = A * An;
-        }
-    }
-}
-
-template <int KD, bool PACK>
+template <int G, int KD, bool PACK>
 __device__ __forceinline__ void update_chunk(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt,
                                              int n, int lane, const WEdges &S, int ch, int W, int P) {
     using C = Chunk<1, 1>;
@@ -842,92 +913,104 @@ __device__ __forceinline__ void update_chunk(const DTopo &tp, const DGeom<float>
     const int nz = k.nz;
     const int i = n * L1 + nz - 1, iv = n * nl + nz - 1;
     const float sdt = k.lvl ? qdiv(dt, g.areasvol[iv] * g.hnode_new[i]) : 0.f;
+    int off[KD], eo[KD];
     unsigned okm = 0;
 #pragma unroll
     for (int u = 0; u < KD; u++) {
         const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
+        off[u] = S.m[u] * L1 + nz - 1;
+        eo[u] = S.e[u] * L1 + nz - 1;
         okm |= ok ? 1u << u : 0u;
     }
 #pragma unroll 1
-    for (int t0 = 0; t0 < B.ntr; t0 += PACK ? P : 1) {
-        // the lane's tracer (packed: the tracer of its segment)
-        const int t = t0 + k.q;
-        const bool on = t < B.ntr;
-        const int tc = on ? t : t0;
-        const bool fct = (B.fct_mask >> tc) & 1ull;
-        const size_t to = (size_t)tc * B.sN;
-        const float *__restrict__ ADh = B.ADh + (size_t)tc * B.sE;
-        const float2 *__restrict__ R = B.R + to;
+    for (int g0 = 0; g0 < B.ng; g0 += PACK ? P : 1) {
+        // the lane's group (packed: the group of its segment)
+        const int gq = g0 + k.q;
+        const bool on = gq < B.ng;
+        const int gc = on ? gq : g0;
+        const bool fct = (B.fct >> gc) & 1ull;
+        const bool dif = (B.diff >> gc) & 1ull;
         const bool lv = k.lvl && on;
         const bool lf = lv && fct;
         const unsigned okt = lv ? okm : 0u;
-        // every load of the tracer's chunk first
-        const float lo = lv ? B.LO[to + i] : 0.f;
-        float f0 = lv ? B.ADv[(size_t)tc * B.sNI + iv] : 0.f;
-        const float2 r0 = lf ? R[i] : make_float2(1.f, 1.f);
-        const float2 tb = lf ? B.TB[to + i] : make_float2(0.f, 0.f);
-        float x[KD];
-        float2 rm[KD];
+        const float *__restrict__ Rp = grp<G>(B.Rp, gc, B.sN);
+        const float *__restrict__ Rm = grp<G>(B.Rm, gc, B.sN);
+        const float *__restrict__ ADh = grp<G>(B.ADh, gc, B.sE);
+        float *__restrict__ Tn = grp<G>(B.Tnew, gc, B.sN);
+        // every load of the group's chunk first
+        const Vec<G> lo = vldc<G>(lv, grp<G>(B.LO, gc, B.sN), i);
+        const Vec<G> f0 = vldc<G>(lv, grp<G>(B.ADv, gc, B.sNI), iv);
+        const Vec<G> r0p = lf ? vld<G>(Rp, i) : vfill<G>(1.f);
+        const Vec<G> r0m = lf ? vld<G>(Rm, i) : vfill<G>(1.f);
+        const Vec<G> tbp = vldc<G>(lf, grp<G>(B.Bp, gc, B.sN), i);
+        const Vec<G> tbm = vldc<G>(lf, grp<G>(B.Bm, gc, B.sN), i);
+        // the diffusion increment k32_diff parked in Tnew (the limiter acts on advection only)
+        const Vec<G> dd = vldc<G>(lv && dif, Tn, i);
+        Vec<G> hs = vfill<G>(0.f);
 #pragma unroll
         for (int u = 0; u < KD; u++) {
             const bool ok = (okt >> u) & 1u;
-            x[u] = ok ? ADh[S.e[u] * L1 + nz - 1] : 0.f;
-            rm[u] = (ok && fct) ? R[S.m[u] * L1 + nz - 1] : make_float2(1.f, 1.f);
-        }
-        // vertical limiting (oce_adv_tra_fct.F90:425-456): interface nz by R of layers
-        // nz-1 and nz; the next interface is the lane below's
-        const float rux = sh_up(r0.x, 1), ruy = sh_up(r0.y, 1);
-        if (fct) {
-            if (nz == nzmin) f0 *= f0 >= 0.f ? r0.x : r0.y;
-            else f0 *= f0 >= 0.f ? fminf(ruy, r0.x) : fminf(rux, r0.y);
-        }
-        float f1 = sh_dn(f0, 1);
-        if (nz == nzmax - 1) f1 = 0.f;
-        // horizontal limiting (oce_adv_tra_fct.F90:468-500) seen from the node: with G the
-        // antidiffusive flux into the node and m the other end, G >= 0 takes
-        // min(R+(n), R-(m)), G < 0 takes min(R-(n), R+(m))
-        float hs = 0.f;
+            const Vec<G> x = vldc<G>(ok, ADh, eo[u]);
+            const Vec<G> rmp = (ok && fct) ? vld<G>(Rp, off[u]) : vfill<G>(1.f);
+            const Vec<G> rmm = (ok && fct) ? vld<G>(Rm, off[u]) : vfill<G>(1.f);
+            const bool ow = (own >> u) & 1u;
+            // horizontal limiting (oce_adv_tra_fct.F90:468-500) seen from the node: with G the
+            // antidiffusive flux into the node and m the other end, G >= 0 takes
+            // min(R+(n), R-(m)), G < 0 takes min(R-(n), R+(m))
 #pragma unroll
-        for (int u = 0; u < KD; u++) {
-            float G = ((own >> u) & 1u) ? x[u] : -x[u];
-            if (fct) G *= G >= 0.f ? fminf(r0.x, rm[u].y) : fminf(r0.y, rm[u].x);
-            hs += G;
+            for (int c = 0; c < G; c++) {
+                float Gf = ow ? x.c[c] : -x.c[c];
+                if (fct) Gf *= Gf >= 0.f ? fminf(r0p.c[c], rmm.c[c]) : fminf(r0m.c[c], rmp.c[c]);
+                hs.c[c] += Gf;
+            }
         }
-        // del_ttf = (LO hnode_new - T hnode) + limited flux divergence dt / areasvol;
-        // T* = T + (del_ttf + T (hnode - hnode_new)) / hnode_new = LO + fluxes dt / areasvol / hnode_new
-        // (oce_adv_tra_driver.F90:535-620, oce_ale_tracer.F90:319-321, 743-754)
-        float val = lo + (f0 - f1 + hs) * sdt;
-        if (k.out && on) {
+        Vec<G> out;
+#pragma unroll
+        for (int c = 0; c < G; c++) {
+            // vertical limiting (oce_adv_tra_fct.F90:425-456): interface nz by R of layers
+            // nz-1 and nz; the next interface is the lane below's
+            const float rux = sh_up(r0p.c[c], 1), ruy = sh_up(r0m.c[c], 1);
+            float fz = f0.c[c];
             if (fct) {
-                const float vc = fminf(fmaxf(val, tb.y), tb.x);
+                if (nz == nzmin) fz *= fz >= 0.f ? r0p.c[c] : r0m.c[c];
+                else fz *= fz >= 0.f ? fminf(ruy, r0p.c[c]) : fminf(rux, r0m.c[c]);
+            }
+            float f1 = sh_dn(fz, 1);
+            if (nz == nzmax - 1) f1 = 0.f;
+            // del_ttf = (LO hnode_new - T hnode) + limited flux divergence dt / areasvol;
+            // T* = T + (del_ttf + T (hnode - hnode_new)) / hnode_new = LO + fluxes dt / areasvol / hnode_new
+            // (oce_adv_tra_driver.F90:535-620, oce_ale_tracer.F90:319-321, 743-754)
+            float val = lo.c[c] + ((fz - f1) + hs.c[c]) * sdt;
+            if (k.out && on && fct) {
+                const float vc = fminf(fmaxf(val, tbm.c[c]), tbp.c[c]);
                 // a clamp beyond round-off means the limiter itself failed
-                if (fabsf(vc - val) > 1e-5f * (tb.x - tb.y) + 1e-6f * fabsf(vc)) atomicOr(B.status, 2u);
+                if (fabsf(vc - val) > 1e-5f * (tbp.c[c] - tbm.c[c]) + 1e-6f * fabsf(vc)) atomicOr(B.status, 2u);
                 val = vc;
             }
-            // the diffusion increment k32_diff parked in Tnew (the limiter acts on advection only)
-            if ((B.diff_mask >> tc) & 1ull) val += B.Tnew[to + i];
-            B.Tnew[to + i] = val;
-            if (!isfinite(val)) atomicOr(B.status, 1u);
+            if (dif) val += dd.c[c];
+            out.c[c] = val;
+        }
+        if (k.out && on) {
+            vst<G>(Tn, i, out);
+#pragma unroll
+            for (int c = 0; c < G; c++)
+                if (!isfinite(out.c[c])) atomicOr(B.status, 1u);
         }
     }
 }
 
-// Limited update of every tracer of a node: per chunk the tracer-independent part
-// (which edge slots are wet, dt / (areasvol hnode_new)) once, then per tracer every gather
-// of the chunk, the limiter and the T* value, written to the buffer of the oldest time level.
-template <int KD, bool PK>
+template <int G, int KD, bool PK>
 __device__ __forceinline__ void update_node(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt,
                                             int n, int lane, const WEdges &S) {
     using C = Chunk<1, 1>;
     const int nch = C::count(S.nzmin, S.nzmax);
-    for (int ch = 0; ch < nch - 1; ch++) update_chunk<KD, false>(tp, g, B, dt, n, lane, S, ch, 32, 1);
+    for (int ch = 0; ch < nch - 1; ch++) update_chunk<G, KD, false>(tp, g, B, dt, n, lane, S, ch, 32, 1);
     const int W = C::last_width(S.nzmin, S.nzmax), P = 32 / W;
-    // packed only for nodes of at most 6 edges, as in k32_bounds
-    if (PK && KD <= 6 && P > 1) update_chunk<KD, true>(tp, g, B, dt, n, lane, S, nch - 1, W, P);
-    else update_chunk<KD, false>(tp, g, B, dt, n, lane, S, nch - 1, 32, 1);
+    if (PK && KD <= 6 && P > 1) update_chunk<G, KD, true>(tp, g, B, dt, n, lane, S, nch - 1, W, P);
+    else update_chunk<G, KD, false>(tp, g, B, dt, n, lane, S, nch - 1, 32, 1);
 }
 
-template <bool WIDE, bool PK>
+template <int G, bool WIDE, bool PK>
 __device__ __forceinline__ void update_unit(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int j,
                                             WEdges *Se) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -936,24 +1019,25 @@ __device__ __forceinline__ void update_unit(const DTopo &tp, const DGeom<float> 
     WEdges &S = Se[warp];
     stage_edges(tp, n, lane, S);
     if ((S.deg > 8) != WIDE) return;
-    if (WIDE) update_node<kMaxDeg, PK>(tp, g, B, dt, n, lane, S);
-    else if (S.deg <= 6) update_node<6, PK>(tp, g, B, dt, n, lane, S);
-    else update_node<8, PK>(tp, g, B, dt, n, lane, S);
+    if (WIDE) update_node<G, kMaxDeg, PK>(tp, g, B, dt, n, lane, S);
+    else if (S.deg <= 6) update_node<G, 6, PK>(tp, g, B, dt, n, lane, S);
+    else update_node<G, 8, PK>(tp, g, B, dt, n, lane, S);
 }
 
-template <bool WIDE>
-__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_UPDATE)
+template <int G, bool WIDE>
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : MinB<G>::update)
 k32_update(DTopo tp, DGeom<float> g, B32View B, float dt) {
     __shared__ WEdges Se[kWB];
-    update_unit<WIDE, true>(tp, g, B, dt, blockIdx.x * kWB + (threadIdx.x >> 5), Se);
+    FOR_WARP_UNITS(j, node_units<WIDE>(tp)) update_unit<G, WIDE, true>(tp, g, B, dt, j, Se);
 }
 
 // ---------------------------------------------------------------------------
-// k32_vppm: adv_tra_vert_ppm (oce_adv_tra_ver.F90:438-631) on the AB values of the tracers
-// in ppm_mask, minus the LO flux, into ADv.  A warp per node over chunks of 27 interfaces
+// k32_vppm: adv_tra_vert_ppm (oce_adv_tra_ver.F90:438-631) on the AB values of the groups
+// in the ppm mask, minus the LO flux, into ADv.  A warp per node over chunks of 27 interfaces
 // with 3 levels of halo above and 2 below: the interface value tv(k) needs the layers
 // k-2..k+1, the flux of interface nz the parabola of layer nz or nz-1.
 // ---------------------------------------------------------------------------
+template <int G>
 __device__ __forceinline__ void vppm_node(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
                                           const B32View &B, float dt, int n, int lane) {
     using C = Chunk<3, 2>;
@@ -974,143 +1058,169 @@ __device__ __forceinline__ void vppm_node(const DTopo &tp, const DGeom<float> &g
         }
         const float hm1 = sh_up(hn0, 1), hm2 = sh_up(hn0, 2), hp1 = sh_dn(hn0, 1);
         const float hom1 = sh_up(ho0, 1);
-        unsigned long long todo = B.ppm_mask;
+        unsigned long long todo = B.ppm & (B.ng >= 64 ? ~0ull : ((1ull << B.ng) - 1));
         while (todo) {
-            const int t = __ffsll((long long)todo) - 1;
+            const int gq = __ffsll((long long)todo) - 1;
             todo &= todo - 1;
-            const bool lim = (B.fct_mask >> t) & 1ull;
-            const size_t to = (size_t)t * B.sN;
-            const float Tn = k.lvl ? B.T[to + i] : 0.f;
-            const float o1 = k.lvl ? B.O1[to + i] : 0.f;
-            const float o2 = (k.lvl && B.ab == 3) ? B.O2[to + i] : 0.f;
-            const float tab = Tn + (k.lvl ? ab_delta(B.ab, Tn, o1, o2) : 0.f);
-            const float tm1 = sh_up(tab, 1), tm2 = sh_up(tab, 2), tp1 = sh_dn(tab, 1);
-            const float Tu = sh_up(Tn, 1);
-            // tv(nz) (:488-562): centred next to the ends, the non-uniform PPM value between
-            float tv;
-            if (nz == nzmax) {
-                tv = tm1;
-            } else if (nz == nzmin) {
-                tv = tab;
-            } else if (nz == nzmax - 1 || nz == nzmin + 1) {
-                tv = 0.5f * (tm1 + tab);
-            } else {
-                // layer j = nz-1: dzjm1 = h(nz-2), dzj = h(nz-1), dzjp1 = h(nz), dzjp2 = h(nz+1)
-                const float a0 = hm2, a1 = hm1, a2 = hn0, a3 = hp1;
-                const float d10 = tab - tm1, d0m = tm1 - tm2, d21 = tp1 - tab;
-                float dj = a1 / (a0 + a1 + a2) * ((2.f * a0 + a1) / (a2 + a1) * d10 + (a1 + 2.f * a2) / (a0 + a1) * d0m);
-                float dj1 = a2 / (a1 + a2 + a3) * ((2.f * a1 + a2) / (a3 + a2) * d21 + (a2 + 2.f * a3) / (a1 + a2) * d10);
-                dj = d10 * d0m > 0.f ? copysignf(fminf(fminf(fabsf(dj), 2.f * fabsf(d10)), 2.f * fabsf(d0m)), dj) : 0.f;
-                dj1 = d21 * d10 > 0.f ? copysignf(fminf(fminf(fabsf(dj1), 2.f * fabsf(d21)), 2.f * fabsf(d10)), dj1) : 0.f;
-                tv = tm1 + a1 / (a1 + a2) * d10 +
-                     1.f / (a0 + a1 + a2 + a3) *
-                         ((2.f * a2 * a1) / (a1 + a2) * ((a0 + a1) / (2.f * a1 + a2) - (a3 + a2) / (2.f * a2 + a1)) * d10 -
-                          a1 * (a0 + a1) / (2.f * a1 + a2) * dj1 + a2 * (a2 + a3) / (a1 + 2.f * a2) * dj);
+            const bool lim = (B.fct >> gq) & 1ull;
+            const Vec<G> Tv = vldc<G>(k.lvl, grp<G>(B.T, gq, B.sN), i);
+            const Vec<G> o1 = vldc<G>(k.lvl, grp<G>(B.O1, gq, B.sN), i);
+            const Vec<G> o2 = vldc<G>(k.lvl && B.ab == 3, grp<G>(B.O2, gq, B.sN), i);
+            Vec<G> out;
+#pragma unroll
+            for (int c = 0; c < G; c++) {
+                const float Tn = Tv.c[c];
+                const float tab = Tn + (k.lvl ? ab_delta(B.ab, Tn, o1.c[c], o2.c[c]) : 0.f);
+                const float tm1 = sh_up(tab, 1), tm2 = sh_up(tab, 2), tp1 = sh_dn(tab, 1);
+                const float Tu = sh_up(Tn, 1);
+                // tv(nz) (:488-562): centred next to the ends, the non-uniform PPM value between
+                float tv;
+                if (nz == nzmax) {
+                    tv = tm1;
+                } else if (nz == nzmin) {
+                    tv = tab;
+                } else if (nz == nzmax - 1 || nz == nzmin + 1) {
+                    tv = 0.5f * (tm1 + tab);
+                } else {
+                    // layer j = nz-1: dzjm1 = h(nz-2), dzj = h(nz-1), dzjp1 = h(nz), dzjp2 = h(nz+1)
+                    const float a0 = hm2, a1 = hm1, a2 = hn0, a3 = hp1;
+                    const float d10 = tab - tm1, d0m = tm1 - tm2, d21 = tp1 - tab;
+                    float dj = a1 / (a0 + a1 + a2) *
+                               ((2.f * a0 + a1) / (a2 + a1) * d10 + (a1 + 2.f * a2) / (a0 + a1) * d0m);
+                    float dj1 = a2 / (a1 + a2 + a3) *
+                                ((2.f * a1 + a2) / (a3 + a2) * d21 + (a2 + 2.f * a3) / (a1 + a2) * d10);
+                    dj = d10 * d0m > 0.f ? copysignf(fminf(fminf(fabsf(dj), 2.f * fabsf(d10)), 2.f * fabsf(d0m)), dj)
+                                         : 0.f;
+                    dj1 = d21 * d10 > 0.f
+                              ? copysignf(fminf(fminf(fabsf(dj1), 2.f * fabsf(d21)), 2.f * fabsf(d10)), dj1)
+                              : 0.f;
+                    tv = tm1 + a1 / (a1 + a2) * d10 +
+                         1.f / (a0 + a1 + a2 + a3) *
+                             ((2.f * a2 * a1) / (a1 + a2) * ((a0 + a1) / (2.f * a1 + a2) - (a3 + a2) / (2.f * a2 + a1)) *
+                                  d10 -
+                              a1 * (a0 + a1) / (2.f * a1 + a2) * dj1 + a2 * (a2 + a3) / (a1 + 2.f * a2) * dj);
+                }
+                const float tvu = sh_up(tv, 1), tvd = sh_dn(tv, 1);
+                const float pw = lim ? w0 : we0;
+                float Cf = 0.f;
+                if (nz == nzmin) {
+                    Cf = -(tv * pw * ar0);
+                } else if (pw > 0.f || pw < 0.f) {
+                    // the parabola of the upwind layer (:564-620)
+                    const bool top = pw > 0.f;
+                    float aL = top ? tv : tvu, aR = top ? tvd : tv;
+                    const float tt = top ? tab : tm1, dz = top ? ho0 : hom1;
+                    if ((aR - tt) * (tt - aL) <= 0.f) aL = aR = tt;
+                    if ((aR - aL) * (tt - 0.5f * (aL + aR)) > (aR - aL) * (aR - aL) * (1.f / 6.f)) aL = 3.f * tt - 2.f * aR;
+                    if ((aR - aL) * (tt - 0.5f * (aR + aL)) < -((aR - aL) * (aR - aL) * (1.f / 6.f)))
+                        aR = 3.f * tt - 2.f * aL;
+                    const float aj = 6.f * (tt - 0.5f * (aL + aR));
+                    const float x = fminf(fabsf(pw) * dt / dz, 1.f);
+                    const float v = top ? -aL - 0.5f * x * (aR - aL + (1.f - (2.f / 3.f) * x) * aj)
+                                        : -aR + 0.5f * x * (aR - aL - (1.f - (2.f / 3.f) * x) * aj);
+                    Cf = v * ar0 * pw;
+                }
+                // minus the upwind LO flux: of w_e, or of the full w for FCT with the split velocity
+                const float wl = (lim && f.wsplit) ? w0 : we0;
+                float fl;
+                if (nz == nzmin) {
+                    fl = -(wl * Tn * ar0);
+                } else {
+                    const float aw = fabsf(wl);
+                    fl = -(0.5f * (Tn * (wl + aw) + Tu * (wl - aw)) * ar0);
+                }
+                out.c[c] = Cf - fl;
             }
-            const float tvu = sh_up(tv, 1), tvd = sh_dn(tv, 1);
-            if (!k.out) continue;
-            const float pw = lim ? w0 : we0;
-            float Cf = 0.f;
-            if (nz == nzmin) {
-                Cf = -(tv * pw * ar0);
-            } else if (pw > 0.f || pw < 0.f) {
-                // the parabola of the upwind layer (:564-620)
-                const bool top = pw > 0.f;
-                float aL = top ? tv : tvu, aR = top ? tvd : tv;
-                const float tt = top ? tab : tm1, dz = top ? ho0 : hom1;
-                if ((aR - tt) * (tt - aL) <= 0.f) aL = aR = tt;
-                if ((aR - aL) * (tt - 0.5f * (aL + aR)) > (aR - aL) * (aR - aL) * (1.f / 6.f)) aL = 3.f * tt - 2.f * aR;
-                if ((aR - aL) * (tt - 0.5f * (aR + aL)) < -((aR - aL) * (aR - aL) * (1.f / 6.f))) aR = 3.f * tt - 2.f * aL;
-                const float aj = 6.f * (tt - 0.5f * (aL + aR));
-                const float x = fminf(fabsf(pw) * dt / dz, 1.f);
-                const float v = top ? -aL - 0.5f * x * (aR - aL + (1.f - (2.f / 3.f) * x) * aj)
-                                    : -aR + 0.5f * x * (aR - aL - (1.f - (2.f / 3.f) * x) * aj);
-                Cf = v * ar0 * pw;
-            }
-            // minus the upwind LO flux: of w_e, or of the full w for FCT with the split velocity
-            const float wl = (lim && f.wsplit) ? w0 : we0;
-            float fl;
-            if (nz == nzmin) {
-                fl = -(wl * Tn * ar0);
-            } else {
-                const float aw = fabsf(wl);
-                fl = -(0.5f * (Tn * (wl + aw) + Tu * (wl - aw)) * ar0);
-            }
-            B.ADv[(size_t)t * B.sNI + iv] = Cf - fl;
+            if (k.out) vst<G>(grp<G>(B.ADv, gq, B.sNI), iv, out);
         }
     }
 }
 
+template <int G>
 __global__ void __launch_bounds__(kTB) k32_vppm(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, float dt) {
-    const int n = blockIdx.x * kWB + (threadIdx.x >> 5);
-    if (n >= tp.N2) return;
-    vppm_node(tp, g, f, B, dt, n, threadIdx.x & 31);
+    FOR_WARP_UNITS(n, tp.N2) vppm_node<G>(tp, g, f, B, dt, n, threadIdx.x & 31);
 }
 
 // ---------------------------------------------------------------------------
 // split vertical velocity, FP32 form: adv_tra_vert_impl by w_i on the LO values of the FCT
-// tracers (oce_adv_tra_ver.F90:90-240), and the implicit vertical diffusion with the w_i
-// terms for the tracers without the limiter (oce_ale_tracer.F90:907-1435, do_wimpl).  One
+// groups (oce_adv_tra_ver.F90:90-240), and the implicit vertical diffusion with the w_i
+// terms for the groups without the limiter (oce_ale_tracer.F90:907-1435, do_wimpl).  One
 // thread per column, FP64 arithmetic; scratch holds Z_n, cp and tp level-major.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void lo_impl_column(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
-                                               const B32View &B, double dt, double *scratch, int n) {
-    const int L1 = tp.L1, nl = tp.nl;
-    const size_t N2 = tp.N2;
-    double *cps = scratch, *tps = scratch + (size_t)(L1 + 1) * N2;
+// one slot's column of a group field (1-based levels)
+struct SlotCol {
+    float *p;
+    int G;
+    __device__ __forceinline__ float &operator[](int nz) const { return p[(size_t)(nz - 1) * G]; }
+};
+
+__device__ __forceinline__ void lo_impl_slot(const float *hn, const float *ar, const float *av, const float *wi,
+                                             double dt, double *cps, double *tps, size_t N2, int n, int nzmin,
+                                             int nzmax, SlotCol Tc) {
 #define CP(k) cps[(size_t)(k) * N2 + n]
 #define TP(k) tps[(size_t)(k) * N2 + n]
-    const int nzmax = tp.n_nlev[n], nzmin = tp.n_ulev[n];
-    const float *hn = g.hnode_new + (size_t)n * L1 - 1;
-    const float *ar = g.area + (size_t)n * nl - 1, *av = g.areasvol + (size_t)n * nl - 1;
-    const float *wi = f.wi + (size_t)n * nl - 1;
-    unsigned long long todo = B.fct_mask & (B.ntr >= 64 ? ~0ull : ((1ull << B.ntr) - 1));
-    while (todo) {
-        const int t = __ffsll((long long)todo) - 1;
-        todo &= todo - 1;
-        float *Tc = B.LO + (size_t)t * B.sN + (size_t)n * L1 - 1;
-        int nz = nzmin;
-        double v = dt * ar[nz] / av[nz];
-        double b = (double)hn[nz] + (double)wi[nz] * v;
-        v = dt * ar[nz + 1] / av[nz];
-        b = b - fmin(0.0, (double)wi[nz + 1]) * v;
-        double c = -(fmax(0.0, (double)wi[nz + 1]) * v);
-        double T0 = Tc[nz], Tp1 = Tc[nz + 1], Tm;
-        double rhs = -((b - hn[nz]) * T0) - c * Tp1;
-        double cp = c / b, tpv = rhs / b;
+    int nz = nzmin;
+    double v = dt * ar[nz] / av[nz];
+    double b = (double)hn[nz] + (double)wi[nz] * v;
+    v = dt * ar[nz + 1] / av[nz];
+    b = b - fmin(0.0, (double)wi[nz + 1]) * v;
+    double c = -(fmax(0.0, (double)wi[nz + 1]) * v);
+    double T0 = Tc[nz], Tp1 = Tc[nz + 1], Tm;
+    double rhs = -((b - hn[nz]) * T0) - c * Tp1;
+    double cp = c / b, tpv = rhs / b;
+    CP(nz) = cp;
+    TP(nz) = tpv;
+    for (nz = nzmin + 1; nz <= nzmax - 1; nz++) {
+        v = dt * ar[nz] / av[nz];
+        const double a = fmin(0.0, (double)wi[nz]) * v;
+        b = (double)hn[nz] + fmax(0.0, (double)wi[nz]) * v;
+        c = 0.0;
+        if (nz <= nzmax - 2) {
+            v = dt * ar[nz + 1] / av[nz];
+            b = b - fmin(0.0, (double)wi[nz + 1]) * v;
+            c = -(fmax(0.0, (double)wi[nz + 1]) * v);
+        }
+        Tm = T0;
+        T0 = Tp1;
+        Tp1 = nz <= nzmax - 2 ? (double)Tc[nz + 1] : 0.0;
+        rhs = -(a * Tm) - (b - hn[nz]) * T0 - c * Tp1;
+        const double m = b - cp * a;
+        cp = c / m;
+        tpv = (rhs - tpv * a) / m;
         CP(nz) = cp;
         TP(nz) = tpv;
-        for (nz = nzmin + 1; nz <= nzmax - 1; nz++) {
-            v = dt * ar[nz] / av[nz];
-            const double a = fmin(0.0, (double)wi[nz]) * v;
-            b = (double)hn[nz] + fmax(0.0, (double)wi[nz]) * v;
-            c = 0.0;
-            if (nz <= nzmax - 2) {
-                v = dt * ar[nz + 1] / av[nz];
-                b = b - fmin(0.0, (double)wi[nz + 1]) * v;
-                c = -(fmax(0.0, (double)wi[nz + 1]) * v);
-            }
-            Tm = T0;
-            T0 = Tp1;
-            Tp1 = nz <= nzmax - 2 ? (double)Tc[nz + 1] : 0.0;
-            rhs = -(a * Tm) - (b - hn[nz]) * T0 - c * Tp1;
-            const double m = b - cp * a;
-            cp = c / m;
-            tpv = (rhs - tpv * a) / m;
-            CP(nz) = cp;
-            TP(nz) = tpv;
-        }
-        double x = tpv;
-        Tc[nzmax - 1] = (float)(Tc[nzmax - 1] + x);
-        for (nz = nzmax - 2; nz >= nzmin; nz--) {
-            x = TP(nz) - CP(nz) * x;
-            Tc[nz] = (float)(Tc[nz] + x);
-        }
+    }
+    double x = tpv;
+    Tc[nzmax - 1] = (float)(Tc[nzmax - 1] + x);
+    for (nz = nzmax - 2; nz >= nzmin; nz--) {
+        x = TP(nz) - CP(nz) * x;
+        Tc[nz] = (float)(Tc[nz] + x);
     }
 #undef CP
 #undef TP
 }
 
+template <int G>
+__device__ __forceinline__ void lo_impl_column(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
+                                               const B32View &B, double dt, double *scratch, int n) {
+    const int L1 = tp.L1, nl = tp.nl;
+    const size_t N2 = tp.N2;
+    double *cps = scratch, *tps = scratch + (size_t)(L1 + 1) * N2;
+    const int nzmax = tp.n_nlev[n], nzmin = tp.n_ulev[n];
+    const float *hn = g.hnode_new + (size_t)n * L1 - 1;
+    const float *ar = g.area + (size_t)n * nl - 1, *av = g.areasvol + (size_t)n * nl - 1;
+    const float *wi = f.wi + (size_t)n * nl - 1;
+    unsigned long long todo = B.fct & (B.ng >= 64 ? ~0ull : ((1ull << B.ng) - 1));
+    while (todo) {
+        const int gq = __ffsll((long long)todo) - 1;
+        todo &= todo - 1;
+        float *base = grp<G>(B.LO, gq, B.sN) + (size_t)n * L1 * G;
+        for (int c = 0; c < G; c++)
+            lo_impl_slot(hn, ar, av, wi, dt, cps, tps, N2, n, nzmin, nzmax, SlotCol{base + c, G});
+    }
+}
+
+template <int G>
 __device__ __forceinline__ void vdiff_w_column(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
                                                const B32View &B, double dt, double *scratch, int n) {
     const int L1 = tp.L1, nl = tp.nl;
@@ -1129,60 +1239,63 @@ __device__ __forceinline__ void vdiff_w_column(const DTopo &tp, const DGeom<floa
         zb = zb + (double)hn[nz];
         ZN(nz - 1) = zb + (double)hn[nz - 1] / 2.0;
     }
-    unsigned long long todo = B.wimpl_mask & (B.ntr >= 64 ? ~0ull : ((1ull << B.ntr) - 1));
+    unsigned long long todo = B.wimpl & (B.ng >= 64 ? ~0ull : ((1ull << B.ng) - 1));
     while (todo) {
-        const int t = __ffsll((long long)todo) - 1;
+        const int gq = __ffsll((long long)todo) - 1;
         todo &= todo - 1;
-        float *Tc = B.Tnew + (size_t)t * B.sN + (size_t)n * L1 - 1;
-        const double bc = B.fsurf ? (double)B.fsurf[t * B.sF + n] : 0.0;
-        int nz = nzmin;
-        double zinv2 = 1.0 / (ZN(nz) - ZN(nz + 1)), zinv1;
-        double c = -((double)kv[nz + 1] * zinv2 * dt * ar[nz + 1] / av[nz]);
-        double b = -c + hn[nz];
-        double v = dt * ((double)ar[nz] / av[nz]);
-        b = b + (double)wi[nz] * v;
-        v = dt * ar[nz + 1] / av[nz];
-        b = b - fmin(0.0, (double)wi[nz + 1]) * v;
-        c = c - fmax(0.0, (double)wi[nz + 1]) * v;
-        double T0 = Tc[nz], Tp1 = Tc[nz + 1], Tm;
-        double rhs = -((b - hn[nz]) * T0) - c * Tp1 + bc;
-        double cp = c / b, tpv = rhs / b;
-        CP(nz) = cp;
-        TP(nz) = tpv;
-        zinv1 = zinv2;
-        for (nz = nzmin + 1; nz <= nzmax - 1; nz++) {
-            const bool bot = nz == nzmax - 1;
-            double a = -((double)kv[nz] * zinv1 * dt * ((double)ar[nz] / av[nz]));
-            c = 0.0;
-            if (!bot) {
-                zinv2 = 1.0 / (ZN(nz) - ZN(nz + 1));
-                c = -((double)kv[nz + 1] * zinv2 * dt * ar[nz + 1] / av[nz]);
-            }
-            b = -a - c + hn[nz];
-            zinv1 = zinv2;
-            v = dt * ((double)ar[nz] / av[nz]);
-            a = a + fmin(0.0, (double)wi[nz]) * v;
-            b = b + fmax(0.0, (double)wi[nz]) * v;
-            if (!bot) {
-                v = dt * ar[nz + 1] / av[nz];
-                b = b - fmin(0.0, (double)wi[nz + 1]) * v;
-                c = c - fmax(0.0, (double)wi[nz + 1]) * v;
-            }
-            Tm = T0;
-            T0 = Tp1;
-            Tp1 = bot ? 0.0 : (double)Tc[nz + 1];
-            rhs = -(a * Tm) - (b - hn[nz]) * T0 - c * Tp1;
-            const double m = b - cp * a;
-            cp = c / m;
-            tpv = (rhs - tpv * a) / m;
+        float *base = grp<G>(B.Tnew, gq, B.sN) + (size_t)n * L1 * G;
+        for (int cs = 0; cs < G; cs++) {
+            const SlotCol Tc{base + cs, G};
+            const double bc = B.fsurf ? (double)B.fsurf[((size_t)gq * N2 + n) * G + cs] : 0.0;
+            int nz = nzmin;
+            double zinv2 = 1.0 / (ZN(nz) - ZN(nz + 1)), zinv1;
+            double c = -((double)kv[nz + 1] * zinv2 * dt * ar[nz + 1] / av[nz]);
+            double b = -c + hn[nz];
+            double v = dt * ((double)ar[nz] / av[nz]);
+            b = b + (double)wi[nz] * v;
+            v = dt * ar[nz + 1] / av[nz];
+            b = b - fmin(0.0, (double)wi[nz + 1]) * v;
+            c = c - fmax(0.0, (double)wi[nz + 1]) * v;
+            double T0 = Tc[nz], Tp1 = Tc[nz + 1], Tm;
+            double rhs = -((b - hn[nz]) * T0) - c * Tp1 + bc;
+            double cp = c / b, tpv = rhs / b;
             CP(nz) = cp;
             TP(nz) = tpv;
-        }
-        double x = tpv;
-        Tc[nzmax - 1] = (float)(Tc[nzmax - 1] + x);
-        for (nz = nzmax - 2; nz >= nzmin; nz--) {
-            x = TP(nz) - CP(nz) * x;
-            Tc[nz] = (float)(Tc[nz] + x);
+            zinv1 = zinv2;
+            for (nz = nzmin + 1; nz <= nzmax - 1; nz++) {
+                const bool bot = nz == nzmax - 1;
+                double a = -((double)kv[nz] * zinv1 * dt * ((double)ar[nz] / av[nz]));
+                c = 0.0;
+                if (!bot) {
+                    zinv2 = 1.0 / (ZN(nz) - ZN(nz + 1));
+                    c = -((double)kv[nz + 1] * zinv2 * dt * ar[nz + 1] / av[nz]);
+                }
+                b = -a - c + hn[nz];
+                zinv1 = zinv2;
+                v = dt * ((double)ar[nz] / av[nz]);
+                a = a + fmin(0.0, (double)wi[nz]) * v;
+                b = b + fmax(0.0, (double)wi[nz]) * v;
+                if (!bot) {
+                    v = dt * ar[nz + 1] / av[nz];
+                    b = b - fmin(0.0, (double)wi[nz + 1]) * v;
+                    c = c - fmax(0.0, (double)wi[nz + 1]) * v;
+                }
+                Tm = T0;
+                T0 = Tp1;
+                Tp1 = bot ? 0.0 : (double)Tc[nz + 1];
+                rhs = -(a * Tm) - (b - hn[nz]) * T0 - c * Tp1;
+                const double m = b - cp * a;
+                cp = c / m;
+                tpv = (rhs - tpv * a) / m;
+                CP(nz) = cp;
+                TP(nz) = tpv;
+            }
+            double x = tpv;
+            Tc[nzmax - 1] = (float)(Tc[nzmax - 1] + x);
+            for (nz = nzmax - 2; nz >= nzmin; nz--) {
+                x = TP(nz) - CP(nz) * x;
+                Tc[nz] = (float)(Tc[nz] + x);
+            }
         }
     }
 #undef ZN
@@ -1190,15 +1303,17 @@ __device__ __forceinline__ void vdiff_w_column(const DTopo &tp, const DGeom<floa
 #undef TP
 }
 
+template <int G>
 __global__ void __launch_bounds__(128) k32_lo_impl(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, double dt,
                                                    double *scratch) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n < tp.N2) lo_impl_column(tp, g, f, B, dt, scratch, n);
+    if (n < tp.N2) lo_impl_column<G>(tp, g, f, B, dt, scratch, n);
 }
+template <int G>
 __global__ void __launch_bounds__(128) k32_vdiff_w(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, double dt,
                                                    double *scratch) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n < tp.N2) vdiff_w_column(tp, g, f, B, dt, scratch, n);
+    if (n < tp.N2) vdiff_w_column<G>(tp, g, f, B, dt, scratch, n);
 }
 
 // ---------------------------------------------------------------------------
@@ -1206,6 +1321,7 @@ __global__ void __launch_bounds__(128) k32_vdiff_w(DTopo tp, DGeom<float> g, DFo
 // ---------------------------------------------------------------------------
 // k32_hdiff: diff_part_hor_redi (:1526-1689, Redi off) flux c of every edge-layer from the
 // element gradients of the current values: segments A/D (element 1), B/E (element 2), C (both)
+template <int G>
 __device__ __forceinline__ void hdiff_edge32(const DTopo &tp, const DGeom<float> &g, const B32View &B, int e) {
     const int lane = threadIdx.x & 31;
     if (e >= tp.E2 || !B.Ki) return;
@@ -1245,40 +1361,48 @@ __device__ __forceinline__ void hdiff_edge32(const DTopo &tp, const DGeom<float>
         const float h1 = g.helem[el1 * L1 + nz - 1], h2 = seg >= 2 ? g.helem[el2 * L1 + nz - 1] : 0.f;
         const bool u1 = seg == 1 || seg == 3, u2 = seg >= 2;
 #pragma unroll 1
-        for (int t = 0; t < B.ntr; t++) {
-            const float *__restrict__ T = B.T + (size_t)t * B.sN;
-            float tx1 = 0.f, ty1 = 0.f, tx2 = 0.f, ty2 = 0.f;
-            if (u1) {
-                const float va = T[a0 * L1 + nz - 1], vb = T[a1 * L1 + nz - 1], vc = T[a2 * L1 + nz - 1];
-                tx1 = p0 * va + p1 * vb + p2 * vc;
-                ty1 = p3 * va + p4 * vb + p5 * vc;
+        for (int gq = 0; gq < B.ng; gq++) {
+            const float *__restrict__ T = grp<G>(B.T, gq, B.sN);
+            const Vec<G> va = vldc<G>(u1, T, a0 * L1 + nz - 1), vb = vldc<G>(u1, T, a1 * L1 + nz - 1),
+                         vc = vldc<G>(u1, T, a2 * L1 + nz - 1);
+            const Vec<G> wa = vldc<G>(u2, T, b0 * L1 + nz - 1), wb = vldc<G>(u2, T, b1 * L1 + nz - 1),
+                         wc = vldc<G>(u2, T, b2 * L1 + nz - 1);
+            Vec<G> out;
+#pragma unroll
+            for (int c = 0; c < G; c++) {
+                float tx1 = 0.f, ty1 = 0.f, tx2 = 0.f, ty2 = 0.f;
+                if (u1) {
+                    tx1 = p0 * va.c[c] + p1 * vb.c[c] + p2 * vc.c[c];
+                    ty1 = p3 * va.c[c] + p4 * vb.c[c] + p5 * vc.c[c];
+                }
+                if (u2) {
+                    tx2 = q0 * wa.c[c] + q1 * wb.c[c] + q2 * wc.c[c];
+                    ty2 = q3 * wa.c[c] + q4 * wb.c[c] + q5 * wc.c[c];
+                }
+                float cf = 0.f;
+                if (seg == 1) cf = (-dX1 * (Kh * ty1) + dY1 * (Kh * tx1)) * h1;
+                else if (seg == 2) cf = (dX2 * (Kh * ty2) - dY2 * (Kh * tx2)) * h2;
+                else if (seg == 3)
+                    cf = ((dX2 - dX1) * (Kh * (0.5f * (ty1 + ty2))) - (dY2 - dY1) * (Kh * (0.5f * (tx1 + tx2)))) *
+                         ((h1 + h2) * 0.5f);
+                out.c[c] = cf;
             }
-            if (u2) {
-                const float va = T[b0 * L1 + nz - 1], vb = T[b1 * L1 + nz - 1], vc = T[b2 * L1 + nz - 1];
-                tx2 = q0 * va + q1 * vb + q2 * vc;
-                ty2 = q3 * va + q4 * vb + q5 * vc;
-            }
-            float c = 0.f;
-            if (seg == 1) c = (-dX1 * (Kh * ty1) + dY1 * (Kh * tx1)) * h1;
-            else if (seg == 2) c = (dX2 * (Kh * ty2) - dY2 * (Kh * tx2)) * h2;
-            else if (seg == 3)
-                c = ((dX2 - dX1) * (Kh * (0.5f * (ty1 + ty2))) - (dY2 - dY1) * (Kh * (0.5f * (tx1 + tx2)))) *
-                    ((h1 + h2) * 0.5f);
-            B.HD[(size_t)t * B.sE + e * L1 + nz - 1] = c;
+            vst<G>(grp<G>(B.HD, gq, B.sE), e * L1 + nz - 1, out);
         }
     }
 }
 
+template <int G>
 __global__ void __launch_bounds__(kTB) k32_hdiff(DTopo tp, DGeom<float> g, B32View B) {
-    hdiff_edge32(tp, g, B, blockIdx.x * kWB + (threadIdx.x >> 5));
+    FOR_WARP_UNITS(e, tp.E2) hdiff_edge32<G>(tp, g, B, e);
 }
 
-// k32_diff: the diffusion increment to T* of every tracer in diff_mask, parked in Tnew:
+// k32_diff: the diffusion increment to T* of every group in the diff mask, parked in Tnew:
 // (sum of the node's edge fluxes +- c) dt / (areasvol hnode_new) and, without implicit vertical
 // diffusion, diff_ver_part_expl_ale (:841-902): vd(ul) = surface flux, vd(nz) = Kv (T(nz-1)
 // - T(nz)) / (Z(nz-1) - Z(nz)) area, increment (vd(nz) - vd(nz+1)) / (zbar(nz) - zbar(nz+1))
 // dt / (areasvol hnode_new)
-template <int KD>
+template <int G, int KD>
 __device__ __forceinline__ void diff_node32(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int n,
                                             int lane, const WEdges &S) {
     using C = Chunk<1, 1>;
@@ -1304,48 +1428,55 @@ __device__ __forceinline__ void diff_node32(const DTopo &tp, const DGeom<float> 
             okm |= ok ? 1u << u : 0u;
         }
 #pragma unroll 1
-        for (int t = 0; t < B.ntr; t++) {
-            if (!((B.diff_mask >> t) & 1ull)) continue;
-            float d = 0.f;
+        for (int gq = 0; gq < B.ng; gq++) {
+            if (!((B.diff >> gq) & 1ull)) continue;
+            Vec<G> d = vfill<G>(0.f);
             if (B.Ki) {
-                const float *__restrict__ HD = B.HD + (size_t)t * B.sE;
+                const float *__restrict__ HD = grp<G>(B.HD, gq, B.sE);
 #pragma unroll
                 for (int u = 0; u < KD; u++) {
-                    const float x = ((okm >> u) & 1u) ? HD[S.e[u] * L1 + nz - 1] : 0.f;
-                    d += ((own >> u) & 1u) ? x : -x;
+                    const Vec<G> x = vldc<G>((okm >> u) & 1u, HD, S.e[u] * L1 + nz - 1);
+                    const bool ow = (own >> u) & 1u;
+#pragma unroll
+                    for (int c = 0; c < G; c++) d.c[c] += ow ? x.c[c] : -x.c[c];
                 }
-                d *= sdt;
+#pragma unroll
+                for (int c = 0; c < G; c++) d.c[c] *= sdt;
             }
-            if (!((B.ivd_mask >> t) & 1ull)) {
-                const float Tn = k.lvl ? B.T[(size_t)t * B.sN + i] : 0.f;
-                const float Tu = sh_up(Tn, 1), Td = sh_dn(Tn, 1);
-                const float fs = B.fsurf ? B.fsurf[t * B.sF + n] : 0.f;
-                const float vd0 = nz == nzmin ? fs : kz * (Tu - Tn);
-                const float vd1 = nz == nzmax - 1 ? 0.f : kzd * (Tn - Td);
-                d += (vd0 - vd1) * q;
+            if (!((B.ivd >> gq) & 1ull)) {
+                const Vec<G> Tv = vldc<G>(k.lvl, grp<G>(B.T, gq, B.sN), i);
+                const Vec<G> fs = B.fsurf ? vld<G>(B.fsurf, gq * tp.N2 + n) : vfill<G>(0.f);
+#pragma unroll
+                for (int c = 0; c < G; c++) {
+                    const float Tn = Tv.c[c];
+                    const float Tu = sh_up(Tn, 1), Td = sh_dn(Tn, 1);
+                    const float vd0 = nz == nzmin ? fs.c[c] : kz * (Tu - Tn);
+                    const float vd1 = nz == nzmax - 1 ? 0.f : kzd * (Tn - Td);
+                    d.c[c] += (vd0 - vd1) * q;
+                }
             }
-            if (k.out) B.Tnew[(size_t)t * B.sN + i] = d;
+            if (k.out) vst<G>(grp<G>(B.Tnew, gq, B.sN), i, d);
         }
     }
 }
 
-template <bool WIDE>
+template <int G, bool WIDE>
 __device__ __forceinline__ void diff_unit(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int j,
                                           WEdges *Se) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int n = unit_node<WIDE>(tp, j);
-    if (n < 0 || !B.diff_mask) return;
+    if (n < 0 || !B.diff) return;
     WEdges &S = Se[warp];
     stage_edges(tp, n, lane, S);
     if ((S.deg > 8) != WIDE) return;
-    if (WIDE) diff_node32<kMaxDeg>(tp, g, B, dt, n, lane, S);
-    else diff_node32<8>(tp, g, B, dt, n, lane, S);
+    if (WIDE) diff_node32<G, kMaxDeg>(tp, g, B, dt, n, lane, S);
+    else diff_node32<G, 8>(tp, g, B, dt, n, lane, S);
 }
 
-template <bool WIDE>
+template <int G, bool WIDE>
 __global__ void __launch_bounds__(kTB) k32_diff(DTopo tp, DGeom<float> g, B32View B, float dt) {
     __shared__ WEdges Se[kWB];
-    diff_unit<WIDE>(tp, g, B, dt, blockIdx.x * kWB + (threadIdx.x >> 5), Se);
+    FOR_WARP_UNITS(j, node_units<WIDE>(tp)) diff_unit<G, WIDE>(tp, g, B, dt, j, Se);
 }
 
 // ---------------------------------------------------------------------------
@@ -1355,9 +1486,10 @@ __global__ void __launch_bounds__(kTB) k32_diff(DTopo tp, DGeom<float> g, B32Vie
 // x_k = tp_k - cp_k x_{k+1} (oce_ale_tracer.F90:1406-1422) with the column's FP64-derived
 // factors, as scans of affine maps y -> A y + B over the lanes of each chunk with the carry
 // passed from chunk to chunk.  The multipliers A depend on the column only: their partial
-// products at each scan step are formed once per node into shared memory, so a tracer's
-// scan step is one shuffle and one multiply-add.  rhs_k = -a_k (T_{k-1} - T_k)
-// - c_k (T_{k+1} - T_k) (+ bc_surface at the top, :1216-1229, 1377-1383); T += x.
+// products at each scan step are formed once per node into shared memory, so a slot's scan
+// step is one shuffle and one multiply-add; the G slots of a group are G interleaved scan
+// chains.  rhs_k = -a_k (T_{k-1} - T_k) - c_k (T_{k+1} - T_k) (+ bc_surface at the top,
+// :1216-1229, 1377-1383); T += x.
 constexpr int kWV = 4;                    // warps (nodes) per block of the diffusion kernel
 constexpr int kScan = 5;                  // steps of a 32-lane scan
 constexpr int kVdiffMaxChunks = kMaxChunks;
@@ -1368,115 +1500,97 @@ struct VdiffWarp {
     float ab[kVdiffMaxChunks][kScan + 1][32];         // backward
 };
 
-// forward and back substitution of tracers t1 and t2 (t2 < 0: none) of a column of NCH
-// chunks: the chunks' scans are independent straight-line code; only the carries between
-// chunks are serial
-#ifndef FESOM_VDIFF_NT
-#define FESOM_VDIFF_NT 3  // tracers whose scan chains interleave in one pass (2: 12.8 ms, 3: 11.4, 4: 12.5 on the 24-tracer sphere)
-#endif
-
-// the forward and backward scans of NT tracers (the first nt of them real), interleaved
-template <int NCH, int NT>
-__device__ __forceinline__ void vdiff_multi(const DTopo &tp, const DForcing<float> &f, const B32View &B, int n,
-                                            int lane, int nzmin, int nzmax, const int (&tt)[NT], int nt,
-                                            VdiffWarp &W) {
+template <int NCH, int G>
+__device__ __forceinline__ void vdiff_group(const DTopo &tp, const B32View &B, int n, int lane, int nzmin, int nzmax,
+                                            int gq, VdiffWarp &W) {
     using C = Chunk<1, 1>;
     const int L1 = tp.L1;
-    float *__restrict__ Tq[NT];
-    float bc[NT];
-#pragma unroll
-    for (int q = 0; q < NT; q++) {
-        const int t = q < nt ? tt[q] : tt[0];
-        Tq[q] = B.Tnew + (size_t)t * B.sN;
-        bc[q] = (f.bc && q < nt) ? f.bc[(size_t)t * tp.N2 + n] : 0.f;
-    }
-    float a[NT][NCH], y[NT][NCH];
+    float *__restrict__ Tg = grp<G>(B.Tnew, gq, B.sN);
+    const Vec<G> bc = B.fsurf ? vld<G>(B.fsurf, gq * tp.N2 + n) : vfill<G>(0.f);
+    Vec<G> a[NCH], y[NCH];
 #pragma unroll
     for (int ch = 0; ch < NCH; ch++) {
         const C k(nzmin, nzmax, ch, lane);
-        const int i = n * L1 + k.nz - 1;
-#pragma unroll
-        for (int q = 0; q < NT; q++) a[q][ch] = (k.lvl && q < nt) ? Tq[q][i] : 0.f;
+        a[ch] = vldc<G>(k.lvl, Tg, n * L1 + k.nz - 1);
     }
 #pragma unroll
     for (int ch = 0; ch < NCH; ch++) {
         const C k(nzmin, nzmax, ch, lane);
         const int nz = k.nz;
-        float b[NT];
+        Vec<G> b;
         const float4 fz = k.out ? W.fac[nz] : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-        for (int q = 0; q < NT; q++) {
-            const float u = sh_up(a[q][ch], 1), d = sh_dn(a[q][ch], 1);
+        for (int c = 0; c < G; c++) {
+            const float u = sh_up(a[ch].c[c], 1), d = sh_dn(a[ch].c[c], 1);
             float r = 0.f;
-            if (nz > nzmin) r -= fz.x * (u - a[q][ch]);
-            if (nz < nzmax - 1) r -= fz.y * (d - a[q][ch]);
-            if (nz == nzmin) r += bc[q];
-            b[q] = k.out ? r * fz.z : 0.f;
+            if (nz > nzmin) r -= fz.x * (u - a[ch].c[c]);
+            if (nz < nzmax - 1) r -= fz.y * (d - a[ch].c[c]);
+            if (nz == nzmin) r += bc.c[c];
+            b.c[c] = k.out ? r * fz.z : 0.f;
         }
 #pragma unroll
         for (int s = 0, off = 1; s < kScan; s++, off <<= 1) {
             const float w = W.af[ch][s][lane];
 #pragma unroll
-            for (int q = 0; q < NT; q++) b[q] = fmaf(w, __shfl_up_sync(kFull, b[q], off), b[q]);
+            for (int c = 0; c < G; c++) b.c[c] = fmaf(w, __shfl_up_sync(kFull, b.c[c], off), b.c[c]);
         }
-#pragma unroll
-        for (int q = 0; q < NT; q++) y[q][ch] = b[q];
+        y[ch] = b;
     }
-    float c[NT];
-#pragma unroll
-    for (int q = 0; q < NT; q++) c[q] = 0.f;
+    Vec<G> cr = vfill<G>(0.f);
 #pragma unroll
     for (int ch = 0; ch < NCH; ch++) {
         const float w = W.af[ch][kScan][lane];
 #pragma unroll
-        for (int q = 0; q < NT; q++) {
-            y[q][ch] = fmaf(w, c[q], y[q][ch]);
-            c[q] = __shfl_sync(kFull, y[q][ch], 30);  // last stored lane (Chunk<1, 1>)
+        for (int c = 0; c < G; c++) {
+            y[ch].c[c] = fmaf(w, cr.c[c], y[ch].c[c]);
+            cr.c[c] = __shfl_sync(kFull, y[ch].c[c], 30);  // last stored lane (Chunk<1, 1>)
         }
     }
 #pragma unroll
     for (int ch = 0; ch < NCH; ch++) {
         const C k(nzmin, nzmax, ch, lane);
-        float b[NT];
+        Vec<G> b;
 #pragma unroll
-        for (int q = 0; q < NT; q++) b[q] = k.out ? y[q][ch] : 0.f;
+        for (int c = 0; c < G; c++) b.c[c] = k.out ? y[ch].c[c] : 0.f;
 #pragma unroll
         for (int s = 0, off = 1; s < kScan; s++, off <<= 1) {
             const float w = W.ab[ch][s][lane];
 #pragma unroll
-            for (int q = 0; q < NT; q++) b[q] = fmaf(w, __shfl_down_sync(kFull, b[q], off), b[q]);
+            for (int c = 0; c < G; c++) b.c[c] = fmaf(w, __shfl_down_sync(kFull, b.c[c], off), b.c[c]);
         }
-#pragma unroll
-        for (int q = 0; q < NT; q++) y[q][ch] = b[q];
+        y[ch] = b;
     }
-#pragma unroll
-    for (int q = 0; q < NT; q++) c[q] = 0.f;
+    cr = vfill<G>(0.f);
 #pragma unroll
     for (int ch = NCH - 1; ch >= 0; ch--) {
         const C k(nzmin, nzmax, ch, lane);
         const float w = W.ab[ch][kScan][lane];
-        const int i = n * L1 + k.nz - 1;
+        Vec<G> o;
+        bool fin = true;
 #pragma unroll
-        for (int q = 0; q < NT; q++) {
-            const float x = fmaf(w, c[q], y[q][ch]);
-            c[q] = __shfl_sync(kFull, x, 1);  // first stored lane (Chunk<1, 1>)
-            if (k.out && q < nt) {
-                const float v = a[q][ch] + x;
-                Tq[q][i] = v;
-                if (!isfinite(v)) atomicOr(B.status, 1u);
-            }
+        for (int c = 0; c < G; c++) {
+            const float x = fmaf(w, cr.c[c], y[ch].c[c]);
+            cr.c[c] = __shfl_sync(kFull, x, 1);  // first stored lane (Chunk<1, 1>)
+            o.c[c] = a[ch].c[c] + x;
+            fin = fin && isfinite(o.c[c]);
+        }
+        if (k.out) {
+            vst<G>(Tg, n * L1 + k.nz - 1, o);
+            if (!fin) atomicOr(B.status, 1u);
         }
     }
 }
 
-__device__ __forceinline__ void vdiff_unit(const DTopo &tp, const DForcing<float> &f, const B32View &B,
-                                           const VFactors &vf, int n, VdiffWarp &W) {
+template <int G>
+__device__ __forceinline__ void vdiff_unit(const DTopo &tp, const B32View &B, const VFactors &vf, int n,
+                                           VdiffWarp &W) {
     using C = Chunk<1, 1>;
     const int lane = threadIdx.x & 31;
     if (n >= tp.N2) return;
     const int L1 = tp.L1;
     const int nzmin = tp.n_ulev[n], nzmax = tp.n_nlev[n];
     const int nch = C::count(nzmin, nzmax);
+    __syncwarp();  // the previous node's reads of W are done
     for (int nz = nzmin + lane; nz <= nzmax - 1; nz += 32) {
         const int i = n * L1 + nz - 1;
         W.fac[nz] = make_float4(vf.a[i], vf.c[i], vf.inv[i], vf.cp[i]);
@@ -1503,33 +1617,117 @@ __device__ __forceinline__ void vdiff_unit(const DTopo &tp, const DForcing<float
         W.ab[ch][kScan][lane] = Ad;
     }
     __syncwarp();
-    // the tracers with implicit diffusion, FESOM_VDIFF_NT per pass: their scan chains interleave
-    constexpr int NT = FESOM_VDIFF_NT;
-    unsigned long long todo = (B.ivd_mask & ~B.wimpl_mask) & (B.ntr >= 64 ? ~0ull : ((1ull << B.ntr) - 1));
+    unsigned long long todo = (B.ivd & ~B.wimpl) & (B.ng >= 64 ? ~0ull : ((1ull << B.ng) - 1));
     while (todo) {
-        int tt[NT], nt = 0;
-#pragma unroll
-        for (int q = 0; q < NT; q++) {
-            tt[q] = todo ? __ffsll((long long)todo) - 1 : (q ? tt[0] : 0);
-            if (todo) {
-                todo &= todo - 1;
-                nt++;
-            }
-        }
+        const int gq = __ffsll((long long)todo) - 1;
+        todo &= todo - 1;
         switch (nch) {
-            case 1: vdiff_multi<1, NT>(tp, f, B, n, lane, nzmin, nzmax, tt, nt, W); break;
-            case 2: vdiff_multi<2, NT>(tp, f, B, n, lane, nzmin, nzmax, tt, nt, W); break;
-            case 3: vdiff_multi<3, NT>(tp, f, B, n, lane, nzmin, nzmax, tt, nt, W); break;
-            case 4: vdiff_multi<4, NT>(tp, f, B, n, lane, nzmin, nzmax, tt, nt, W); break;
-            default: vdiff_multi<5, NT>(tp, f, B, n, lane, nzmin, nzmax, tt, nt, W); break;
+            case 1: vdiff_group<1, G>(tp, B, n, lane, nzmin, nzmax, gq, W); break;
+            case 2: vdiff_group<2, G>(tp, B, n, lane, nzmin, nzmax, gq, W); break;
+            case 3: vdiff_group<3, G>(tp, B, n, lane, nzmin, nzmax, gq, W); break;
+            case 4: vdiff_group<4, G>(tp, B, n, lane, nzmin, nzmax, gq, W); break;
+            default: vdiff_group<5, G>(tp, B, n, lane, nzmin, nzmax, gq, W); break;
         }
     }
 }
 
-__global__ void __launch_bounds__(32 * kWV) k32_vdiff(DTopo tp, DForcing<float> f, B32View B, VFactors vf) {
+template <int G>
+__global__ void __launch_bounds__(32 * kWV) k32_vdiff(DTopo tp, B32View B, VFactors vf) {
     __shared__ VdiffWarp Wsm[kWV];
     const int warp = threadIdx.x >> 5;
-    vdiff_unit(tp, f, B, vf, blockIdx.x * kWV + warp, Wsm[warp]);
+    for (int n = blockIdx.x * kWV + warp; n < tp.N2; n += gridDim.x * kWV) vdiff_unit<G>(tp, B, vf, n, Wsm[warp]);
+}
+
+// ---------------------------------------------------------------------------
+// content sums and layout conversions
+// ---------------------------------------------------------------------------
+// FP64 content of every slot of ng groups: block b sums its nodes [b*per, (b+1)*per) in a
+// fixed order (threads over nodes, then a tree over the block), out = ordered sum of blocks
+template <int G>
+__global__ void __launch_bounds__(256) k32_content_partial(DTopo tp, DGeom<float> g, const float *T, int ng,
+                                                           double *partials) {
+    __shared__ double red[256];
+    const int L1 = tp.L1, nl = tp.nl;
+    const int per = (tp.N2 + gridDim.x - 1) / gridDim.x;
+    const int n0 = blockIdx.x * per, n1 = min(tp.N2, n0 + per);
+    for (int gq = 0; gq < ng; gq++) {
+        double acc[G];
+#pragma unroll
+        for (int c = 0; c < G; c++) acc[c] = 0.0;
+        const float *Tg = grp<G>(T, gq, (size_t)tp.N2 * L1);
+        for (int n = n0 + threadIdx.x; n < n1; n += blockDim.x) {
+            const int nzmin = tp.n_ulev[n], nzmax = tp.n_nlev[n];
+            for (int nz = nzmin; nz <= nzmax - 1; nz++) {
+                const Vec<G> t = vld<G>(Tg, n * L1 + nz - 1);
+                const double w = (double)g.hnode_new[n * L1 + nz - 1] * (double)g.areasvol[n * nl + nz - 1];
+#pragma unroll
+                for (int c = 0; c < G; c++) acc[c] += (double)t.c[c] * w;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < G; c++) {
+            red[threadIdx.x] = acc[c];
+            __syncthreads();
+            for (int s = 128; s > 0; s >>= 1) {
+                if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+                __syncthreads();
+            }
+            if (threadIdx.x == 0) partials[((size_t)blockIdx.x * ng + gq) * G + c] = red[0];
+            __syncthreads();
+        }
+    }
+}
+__global__ void k32_content_final(const double *partials, int nblk, int nslots, double *out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nslots) return;
+    double a = 0.0;
+    for (int b = 0; b < nblk; b++) a += partials[(size_t)b * nslots + s];
+    out[s] = a;
+}
+
+template <typename S>
+__global__ void k32_put_slot(const S *src, float *grpf, int G, int c, size_t count) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
+        grpf[i * G + c] = (float)src[i];
+}
+template <typename S>
+__global__ void k32_get_slot(const float *grpf, int G, int c, size_t count, S *dst) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = (S)grpf[i * G + c];
+}
+template <typename S>
+__global__ void k32_put_slot_pair(const S *src, float *g1, float *g2, int G, int c, size_t count) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
+        g1[i * G + c] = (float)src[2 * i];
+        g2[i * G + c] = (float)src[2 * i + 1];
+    }
+}
+template <typename S>
+__global__ void k32_get_slot_pair(const float *g1, const float *g2, int G, int c, size_t count, S *dst) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
+        dst[2 * i] = (S)g1[i * G + c];
+        dst[2 * i + 1] = (S)g2[i * G + c];
+    }
+}
+// element i of slot c's source is src.p[c][i * stride + off] (stride 2: one level of AB3's
+// interleaved valuesold); a null source fills its slot with zeros
+template <int G, typename S>
+__global__ void k32_pack_group(SlotSrc<S> src, float *grpf, size_t count, int stride, int off) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
+        Vec<G> v;
+#pragma unroll
+        for (int c = 0; c < G; c++) v.c[c] = src.p[c] ? (float)src.p[c][i * stride + off] : 0.f;
+        vst<G>(grpf, (int)i, v);
+    }
+}
+template <int G, typename S>
+__global__ void k32_unpack_group(const float *grpf, size_t count, SlotDst<S> dst, int stride, int off) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
+        const Vec<G> v = vld<G>(grpf, (int)i);
+#pragma unroll
+        for (int c = 0; c < G; c++)
+            if (dst.p[c]) dst.p[c][i * stride + off] = (S)v.c[c];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1538,7 +1736,7 @@ __global__ void __launch_bounds__(32 * kWV) k32_vdiff(DTopo tp, DForcing<float> 
 // Units (edges, column blocks, nodes, items) of all instances are numbered one after
 // another; ix.start[i] is instance i's first unit.  A warp (or thread, or block) finds
 // its instance by binary search over those offsets (kernel parameters, warp-uniform)
-// and runs the single-instance body with that instance's descriptor.
+// and runs the single-instance body with that instance's descriptor and its group width.
 __device__ __forceinline__ int find_inst(const MultiIdx &ix, int u) {
     int lo = 0, hi = ix.n - 1;
     while (lo < hi) {
@@ -1550,10 +1748,10 @@ __device__ __forceinline__ int find_inst(const MultiIdx &ix, int u) {
 }
 
 __global__ void __launch_bounds__(kTB) k32m_vflux(const Inst32 *__restrict__ I, MultiIdx ix) {
-    const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
-    if (u >= ix.start[ix.n]) return;
-    const int i = find_inst(ix, u);
-    vflux_edge(I[i].tp, I[i].g, I[i].f, I[i].VF, u - ix.start[i], threadIdx.x & 31);
+    FOR_WARP_UNITS(u, ix.start[ix.n]) {
+        const int i = find_inst(ix, u);
+        vflux_edge(I[i].tp, I[i].g, I[i].f, I[i].VF, u - ix.start[i], threadIdx.x & 31);
+    }
 }
 __global__ void __launch_bounds__(kVfCols) k32m_vfactors(const Inst32 *__restrict__ I, MultiIdx ix) {
     const int u = blockIdx.x;
@@ -1562,81 +1760,94 @@ __global__ void __launch_bounds__(kVfCols) k32m_vfactors(const Inst32 *__restric
 }
 // WS: some instance has the split vertical velocity (each instance checks its own switch)
 template <bool WIDE, bool WS>
-__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_LO) k32m_lo_ad(const Inst32 *__restrict__ I, MultiIdx ix) {
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : MinB<4>::lo) k32m_lo_ad(const Inst32 *__restrict__ I, MultiIdx ix) {
     __shared__ WEdges Se[kWB];
-    const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
-    if (u >= ix.start[ix.n]) return;
-    const int i = find_inst(ix, u);
-    lo_ad_unit<WIDE, WS, FESOM_PACK_MULTI>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].VF, I[i].dt, u - ix.start[i], Se);
+    FOR_WARP_UNITS(u, ix.start[ix.n]) {
+        const int i = find_inst(ix, u);
+        if (I[i].B.G == 4) lo_ad_unit<4, WIDE, WS, true>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].VF, I[i].dt, u - ix.start[i], Se);
+        else lo_ad_unit<2, WIDE, WS, true>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].VF, I[i].dt, u - ix.start[i], Se);
+    }
 }
-__global__ void __launch_bounds__(kTB, FESOM_MINB_HO) k32m_ho(const Inst32 *__restrict__ I, MultiIdx ix) {
-    const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
-    if (u >= ix.start[ix.n]) return;
-    const int i = find_inst(ix, u);
-    ho_unit<FESOM_PACK_MULTI>(I[i].tp, I[i].B, I[i].mw, I[i].VF, u - ix.start[i]);
+__global__ void __launch_bounds__(kTB, MinB<4>::ho) k32m_ho(const Inst32 *__restrict__ I, MultiIdx ix) {
+    FOR_WARP_UNITS(u, ix.start[ix.n]) {
+        const int i = find_inst(ix, u);
+        if (I[i].B.G == 4) ho_unit<4, true>(I[i].tp, I[i].B, I[i].mw, I[i].VF, u - ix.start[i]);
+        else ho_unit<2, true>(I[i].tp, I[i].B, I[i].mw, I[i].VF, u - ix.start[i]);
+    }
 }
 __global__ void __launch_bounds__(256) k32m_ho_nodemean(const Inst32 *__restrict__ I, MultiIdx ix) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= ix.start[ix.n]) return;
     const int i = find_inst(ix, u);
-    nodemean_item(I[i].tp, I[i].B, I[i].mw, I[i].VF, u - ix.start[i]);
+    if (I[i].B.G == 4) nodemean_item<4>(I[i].tp, I[i].B, I[i].mw, I[i].VF, u - ix.start[i]);
+    else nodemean_item<2>(I[i].tp, I[i].B, I[i].mw, I[i].VF, u - ix.start[i]);
 }
 template <bool WIDE>
-__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_BOUNDS) k32m_bounds(const Inst32 *__restrict__ I, MultiIdx ix) {
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : MinB<4>::bounds) k32m_bounds(const Inst32 *__restrict__ I, MultiIdx ix) {
     __shared__ WEdges Se[kWB];
-    const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
-    if (u >= ix.start[ix.n]) return;
-    const int i = find_inst(ix, u);
-    bounds_unit<WIDE, FESOM_PACK_MULTI>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
+    FOR_WARP_UNITS(u, ix.start[ix.n]) {
+        const int i = find_inst(ix, u);
+        if (I[i].B.G == 4) bounds_unit<4, WIDE, true>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
+        else bounds_unit<2, WIDE, true>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
+    }
 }
 template <bool WIDE>
-__global__ void __launch_bounds__(kTB, WIDE ? 1 : FESOM_MINB_UPDATE) k32m_update(const Inst32 *__restrict__ I, MultiIdx ix) {
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : MinB<4>::update) k32m_update(const Inst32 *__restrict__ I, MultiIdx ix) {
     __shared__ WEdges Se[kWB];
-    const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
-    if (u >= ix.start[ix.n]) return;
-    const int i = find_inst(ix, u);
-    update_unit<WIDE, FESOM_PACK_MULTI>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
+    FOR_WARP_UNITS(u, ix.start[ix.n]) {
+        const int i = find_inst(ix, u);
+        if (I[i].B.G == 4) update_unit<4, WIDE, true>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
+        else update_unit<2, WIDE, true>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
+    }
 }
 __global__ void __launch_bounds__(32 * kWV) k32m_vdiff(const Inst32 *__restrict__ I, MultiIdx ix) {
     __shared__ VdiffWarp Wsm[kWV];
-    const int u = blockIdx.x * kWV + (threadIdx.x >> 5);
-    if (u >= ix.start[ix.n]) return;
-    const int i = find_inst(ix, u);
-    vdiff_unit(I[i].tp, I[i].f, I[i].B, I[i].vf, u - ix.start[i], Wsm[threadIdx.x >> 5]);
+    for (int u = blockIdx.x * kWV + (threadIdx.x >> 5); u < ix.start[ix.n]; u += gridDim.x * kWV) {
+        const int i = find_inst(ix, u);
+        if (I[i].B.G == 4) vdiff_unit<4>(I[i].tp, I[i].B, I[i].vf, u - ix.start[i], Wsm[threadIdx.x >> 5]);
+        else vdiff_unit<2>(I[i].tp, I[i].B, I[i].vf, u - ix.start[i], Wsm[threadIdx.x >> 5]);
+    }
 }
 
 __global__ void __launch_bounds__(kTB) k32m_vppm(const Inst32 *__restrict__ I, MultiIdx ix) {
-    const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
-    if (u >= ix.start[ix.n]) return;
-    const int i = find_inst(ix, u);
-    if (I[i].B.ppm_mask) vppm_node(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].dt, u - ix.start[i], threadIdx.x & 31);
+    FOR_WARP_UNITS(u, ix.start[ix.n]) {
+        const int i = find_inst(ix, u);
+        if (I[i].B.ppm && I[i].B.G == 4) vppm_node<4>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].dt, u - ix.start[i], threadIdx.x & 31);
+        else if (I[i].B.ppm) vppm_node<2>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].dt, u - ix.start[i], threadIdx.x & 31);
+    }
 }
 __global__ void __launch_bounds__(128) k32m_lo_impl(const Inst32 *__restrict__ I, MultiIdx ix) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= ix.start[ix.n]) return;
     const int i = find_inst(ix, u);
-    if (I[i].f.wsplit) lo_impl_column(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].dtd, I[i].scratch, u - ix.start[i]);
+    if (!I[i].f.wsplit) return;
+    if (I[i].B.G == 4) lo_impl_column<4>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].dtd, I[i].scratch, u - ix.start[i]);
+    else lo_impl_column<2>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].dtd, I[i].scratch, u - ix.start[i]);
 }
 __global__ void __launch_bounds__(128) k32m_vdiff_w(const Inst32 *__restrict__ I, MultiIdx ix) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= ix.start[ix.n]) return;
     const int i = find_inst(ix, u);
-    if (I[i].B.wimpl_mask) vdiff_w_column(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].dtd, I[i].scratch, u - ix.start[i]);
+    if (!I[i].B.wimpl) return;
+    if (I[i].B.G == 4) vdiff_w_column<4>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].dtd, I[i].scratch, u - ix.start[i]);
+    else vdiff_w_column<2>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].dtd, I[i].scratch, u - ix.start[i]);
 }
 
 __global__ void __launch_bounds__(kTB) k32m_hdiff(const Inst32 *__restrict__ I, MultiIdx ix) {
-    const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
-    if (u >= ix.start[ix.n]) return;
-    const int i = find_inst(ix, u);
-    hdiff_edge32(I[i].tp, I[i].g, I[i].B, u - ix.start[i]);
+    FOR_WARP_UNITS(u, ix.start[ix.n]) {
+        const int i = find_inst(ix, u);
+        if (I[i].B.G == 4) hdiff_edge32<4>(I[i].tp, I[i].g, I[i].B, u - ix.start[i]);
+        else hdiff_edge32<2>(I[i].tp, I[i].g, I[i].B, u - ix.start[i]);
+    }
 }
 template <bool WIDE>
 __global__ void __launch_bounds__(kTB) k32m_diff(const Inst32 *__restrict__ I, MultiIdx ix) {
     __shared__ WEdges Se[kWB];
-    const int u = blockIdx.x * kWB + (threadIdx.x >> 5);
-    if (u >= ix.start[ix.n]) return;
-    const int i = find_inst(ix, u);
-    diff_unit<WIDE>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
+    FOR_WARP_UNITS(u, ix.start[ix.n]) {
+        const int i = find_inst(ix, u);
+        if (I[i].B.G == 4) diff_unit<4, WIDE>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
+        else diff_unit<2, WIDE>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1647,6 +1858,14 @@ static int grid32(int nent, int per_block) {
     const int cap = 152 * 48;
     return b > cap ? cap : (b < 1 ? 1 : b);
 }
+// warp-per-unit kernels: one warp per unit, or at most blocks_per_sm blocks per SM looping
+static int grid_units(int units, const LaunchShape &sh) {
+    int b = (units + kWB - 1) / kWB;
+    if (sh.blocks_per_sm > 0 && b > 152 * sh.blocks_per_sm) b = 152 * sh.blocks_per_sm;
+    return b < 1 ? 1 : b;
+}
+static int grid_nodes(int n) { return (n + kWB - 1) / kWB; }
+static int grid_flat(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 32); }
 
 void b32_vflux(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, float *VF, cudaStream_t s) {
     k32_vflux<<<grid32(tp.E2, kWB), kTB, 0, s>>>(tp, g, f, VF);
@@ -1655,59 +1874,136 @@ void b32_vfactors(const DTopo &tp, const DGeom<float> &g, const DForcing<float> 
                   cudaStream_t s) {
     k32_vfactors<<<(tp.N2 + kVfCols - 1) / kVfCols, kVfCols, 0, s>>>(tp, g, f, dt, v);
 }
-// node kernels: one warp per node, kWB consecutive nodes per block; the nodes of more
-// than 8 edges (listed at init) take a second, small launch with 16 edge slots
-static int grid_nodes(int n) { return (n + kWB - 1) / kWB; }
 
-void b32_lo_ad(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B, const float *VF,
-               double dt, cudaStream_t s) {
+template <int G>
+static void lo_ad_g(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B, const float *VF,
+                    double dt, const LaunchShape &sh, cudaStream_t s) {
     if (f.wsplit) {
-        k32_lo_ad<false, true><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
-        if (tp.n_wide) k32_lo_ad<true, true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
+        k32_lo_ad<G, false, true><<<grid_units(tp.N2, sh), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
+        if (tp.n_wide) k32_lo_ad<G, true, true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
     } else {
-        k32_lo_ad<false, false><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
-        if (tp.n_wide) k32_lo_ad<true, false><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
+        k32_lo_ad<G, false, false><<<grid_units(tp.N2, sh), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
+        if (tp.n_wide) k32_lo_ad<G, true, false><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
     }
 }
-void b32_ho(const DTopo &tp, const DGeom<float> &g, const B32View &B, const MusclW &mw, const float *VF,
-            cudaStream_t s) {
-    k32_ho<<<grid_nodes(tp.E2), kTB, 0, s>>>(tp, B, mw, VF);
+void b32_lo_ad(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B, const float *VF,
+               double dt, const LaunchShape &sh, cudaStream_t s) {
+    if (B.G == 4) lo_ad_g<4>(tp, g, f, B, VF, dt, sh, s);
+    else lo_ad_g<2>(tp, g, f, B, VF, dt, sh, s);
+}
+template <int G>
+static void ho_g(const DTopo &tp, const B32View &B, const MusclW &mw, const float *VF, const LaunchShape &sh,
+                 cudaStream_t s) {
+    k32_ho<G><<<grid_units(tp.E2, sh), kTB, 0, s>>>(tp, B, mw, VF);
     if (mw.n_items) {
         int blocks = (mw.n_items + 255) / 256;
         if (blocks > 152 * 8) blocks = 152 * 8;
-        k32_ho_nodemean<<<blocks, 256, 0, s>>>(tp, B, mw, VF);
+        k32_ho_nodemean<G><<<blocks, 256, 0, s>>>(tp, B, mw, VF);
     }
 }
-void b32_bounds(const DTopo &tp, const DGeom<float> &g, const B32View &B, double dt, cudaStream_t s) {
-    k32_bounds<false><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, B, (float)dt);
-    if (tp.n_wide) k32_bounds<true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
+void b32_ho(const DTopo &tp, const DGeom<float> &, const B32View &B, const MusclW &mw, const float *VF,
+            const LaunchShape &sh, cudaStream_t s) {
+    if (B.G == 4) ho_g<4>(tp, B, mw, VF, sh, s);
+    else ho_g<2>(tp, B, mw, VF, sh, s);
 }
-void b32_update(const DTopo &tp, const DGeom<float> &g, const B32View &B, double dt, cudaStream_t s) {
-    k32_update<false><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, B, (float)dt);
-    if (tp.n_wide) k32_update<true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
+void b32_bounds(const DTopo &tp, const DGeom<float> &g, const B32View &B, double dt, const LaunchShape &sh,
+                cudaStream_t s) {
+    if (B.G == 4) {
+        k32_bounds<4, false><<<grid_units(tp.N2, sh), kTB, 0, s>>>(tp, g, B, (float)dt);
+        if (tp.n_wide) k32_bounds<4, true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
+    } else {
+        k32_bounds<2, false><<<grid_units(tp.N2, sh), kTB, 0, s>>>(tp, g, B, (float)dt);
+        if (tp.n_wide) k32_bounds<2, true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
+    }
+}
+void b32_update(const DTopo &tp, const DGeom<float> &g, const B32View &B, double dt, const LaunchShape &sh,
+                cudaStream_t s) {
+    if (B.G == 4) {
+        k32_update<4, false><<<grid_units(tp.N2, sh), kTB, 0, s>>>(tp, g, B, (float)dt);
+        if (tp.n_wide) k32_update<4, true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
+    } else {
+        k32_update<2, false><<<grid_units(tp.N2, sh), kTB, 0, s>>>(tp, g, B, (float)dt);
+        if (tp.n_wide) k32_update<2, true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
+    }
+}
+void b32_vdiff(const DTopo &tp, const DForcing<float> &, const B32View &B, const VFactors &v, cudaStream_t s) {
+    if (B.G == 4) k32_vdiff<4><<<(tp.N2 + kWV - 1) / kWV, 32 * kWV, 0, s>>>(tp, B, v);
+    else k32_vdiff<2><<<(tp.N2 + kWV - 1) / kWV, 32 * kWV, 0, s>>>(tp, B, v);
 }
 void b32_vppm(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B, double dt,
               cudaStream_t s) {
-    k32_vppm<<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, f, B, (float)dt);
+    if (B.G == 4) k32_vppm<4><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, f, B, (float)dt);
+    else k32_vppm<2><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, f, B, (float)dt);
 }
 void b32_lo_impl(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B, double dt,
                  double *scratch, cudaStream_t s) {
-    k32_lo_impl<<<(tp.N2 + 127) / 128, 128, 0, s>>>(tp, g, f, B, dt, scratch);
+    if (B.G == 4) k32_lo_impl<4><<<(tp.N2 + 127) / 128, 128, 0, s>>>(tp, g, f, B, dt, scratch);
+    else k32_lo_impl<2><<<(tp.N2 + 127) / 128, 128, 0, s>>>(tp, g, f, B, dt, scratch);
 }
 void b32_vdiff_w(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B, double dt,
                  double *scratch, cudaStream_t s) {
-    k32_vdiff_w<<<(tp.N2 + 127) / 128, 128, 0, s>>>(tp, g, f, B, dt, scratch);
+    if (B.G == 4) k32_vdiff_w<4><<<(tp.N2 + 127) / 128, 128, 0, s>>>(tp, g, f, B, dt, scratch);
+    else k32_vdiff_w<2><<<(tp.N2 + 127) / 128, 128, 0, s>>>(tp, g, f, B, dt, scratch);
 }
 void b32_hdiff(const DTopo &tp, const DGeom<float> &g, const B32View &B, cudaStream_t s) {
-    k32_hdiff<<<grid_nodes(tp.E2), kTB, 0, s>>>(tp, g, B);
+    if (B.G == 4) k32_hdiff<4><<<grid_nodes(tp.E2), kTB, 0, s>>>(tp, g, B);
+    else k32_hdiff<2><<<grid_nodes(tp.E2), kTB, 0, s>>>(tp, g, B);
 }
 void b32_diff(const DTopo &tp, const DGeom<float> &g, const B32View &B, double dt, cudaStream_t s) {
-    k32_diff<false><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, B, (float)dt);
-    if (tp.n_wide) k32_diff<true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
+    if (B.G == 4) {
+        k32_diff<4, false><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, B, (float)dt);
+        if (tp.n_wide) k32_diff<4, true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
+    } else {
+        k32_diff<2, false><<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, B, (float)dt);
+        if (tp.n_wide) k32_diff<2, true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
+    }
 }
-void b32_vdiff(const DTopo &tp, const DForcing<float> &f, const B32View &B, const VFactors &v, cudaStream_t s) {
-    k32_vdiff<<<(tp.N2 + kWV - 1) / kWV, 32 * kWV, 0, s>>>(tp, f, B, v);
+void b32_content(const DTopo &tp, const DGeom<float> &g, const float *T, int ng, int G, double *partials, int nblk,
+                 double *out, cudaStream_t s) {
+    if (G == 4) k32_content_partial<4><<<nblk, 256, 0, s>>>(tp, g, T, ng, partials);
+    else k32_content_partial<2><<<nblk, 256, 0, s>>>(tp, g, T, ng, partials);
+    const int nslots = ng * G;
+    k32_content_final<<<(nslots + 63) / 64, 64, 0, s>>>(partials, nblk, nslots, out);
 }
+void b32_put_slot(const double *src, float *grpf, int G, int c, size_t count, cudaStream_t s) {
+    k32_put_slot<double><<<grid_flat(count), 256, 0, s>>>(src, grpf, G, c, count);
+}
+void b32_put_slot_f(const float *src, float *grpf, int G, int c, size_t count, cudaStream_t s) {
+    k32_put_slot<float><<<grid_flat(count), 256, 0, s>>>(src, grpf, G, c, count);
+}
+void b32_get_slot(const float *grpf, int G, int c, size_t count, double *dst, cudaStream_t s) {
+    k32_get_slot<double><<<grid_flat(count), 256, 0, s>>>(grpf, G, c, count, dst);
+}
+void b32_get_slot_f(const float *grpf, int G, int c, size_t count, float *dst, cudaStream_t s) {
+    k32_get_slot<float><<<grid_flat(count), 256, 0, s>>>(grpf, G, c, count, dst);
+}
+void b32_put_slot_pair(const double *src, float *g1, float *g2, int G, int c, size_t count, cudaStream_t s) {
+    k32_put_slot_pair<double><<<grid_flat(count), 256, 0, s>>>(src, g1, g2, G, c, count);
+}
+void b32_put_slot_pair_f(const float *src, float *g1, float *g2, int G, int c, size_t count, cudaStream_t s) {
+    k32_put_slot_pair<float><<<grid_flat(count), 256, 0, s>>>(src, g1, g2, G, c, count);
+}
+void b32_get_slot_pair(const float *g1, const float *g2, int G, int c, size_t count, double *dst, cudaStream_t s) {
+    k32_get_slot_pair<double><<<grid_flat(count), 256, 0, s>>>(g1, g2, G, c, count, dst);
+}
+void b32_get_slot_pair_f(const float *g1, const float *g2, int G, int c, size_t count, float *dst, cudaStream_t s) {
+    k32_get_slot_pair<float><<<grid_flat(count), 256, 0, s>>>(g1, g2, G, c, count, dst);
+}
+template <typename S>
+void b32_pack_group(const SlotSrc<S> &src, float *grpf, int G, size_t count, int stride, int off, cudaStream_t s) {
+    if (G == 4) k32_pack_group<4, S><<<grid_flat(count), 256, 0, s>>>(src, grpf, count, stride, off);
+    else k32_pack_group<2, S><<<grid_flat(count), 256, 0, s>>>(src, grpf, count, stride, off);
+}
+template <typename S>
+void b32_unpack_group(const float *grpf, int G, size_t count, const SlotDst<S> &dst, int stride, int off,
+                      cudaStream_t s) {
+    if (G == 4) k32_unpack_group<4, S><<<grid_flat(count), 256, 0, s>>>(grpf, count, dst, stride, off);
+    else k32_unpack_group<2, S><<<grid_flat(count), 256, 0, s>>>(grpf, count, dst, stride, off);
+}
+template void b32_pack_group<float>(const SlotSrc<float> &, float *, int, size_t, int, int, cudaStream_t);
+template void b32_pack_group<double>(const SlotSrc<double> &, float *, int, size_t, int, int, cudaStream_t);
+template void b32_unpack_group<float>(const float *, int, size_t, const SlotDst<float> &, int, int, cudaStream_t);
+template void b32_unpack_group<double>(const float *, int, size_t, const SlotDst<double> &, int, int, cudaStream_t);
 
 // multi-instance launch wrappers: ix_* hold the per-instance unit offsets of each stage
 void bm32_vflux(const Inst32 *I, const MultiIdx &ix, cudaStream_t s) {

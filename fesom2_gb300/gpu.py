@@ -85,6 +85,8 @@ _SIGS = {
     "fesom_gpu_tracer_content": ([_P, _P], C.c_int),
     "fesom_gpu_set_tracers_per_launch": ([_P, C.c_int32], C.c_int),
     "fesom_gpu_set_host_groups": ([_P, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
+    "fesom_gpu_set_tracer_width": ([_P, C.c_int32], C.c_int),
+    "fesom_gpu_tracer_groups": ([_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _P, _P], C.c_int),
     "fesom_gpu_tracer_gradient_z": ([_P, _P, _P], C.c_int),
     "fesom_gpu_profile_step": ([_P, C.c_double, _P, _P], C.c_int),
     "fesom_gpu_launches_per_step": ([_P, C.POINTER(C.c_int32)], C.c_int),
@@ -277,6 +279,18 @@ class Context:
         self._chk(self.L.fesom_gpu_vdiff_impl_wi(self.h, float(forcing.dt if dt is None else dt), C.byref(cfg),
                                                  _p(Kv), _p(bcs), _p(wi), _p(values)))
 
+    def set_tracer_width(self, width: int):
+        """FP32 form: slots per tracer group for the next ``state_setup`` (0: automatic, 2, 4)."""
+        self._chk(self.L.fesom_gpu_set_tracer_width(self.h, int(width)))
+
+    def tracer_groups(self):
+        """FP32 form: (group count, width, group of each tracer, slot of each tracer)."""
+        ng, w = C.c_int32(0), C.c_int32(0)
+        g = np.zeros(self.ntr, np.int32)
+        c = np.zeros(self.ntr, np.int32)
+        self._chk(self.L.fesom_gpu_tracer_groups(self.h, C.byref(ng), C.byref(w), _p(g), _p(c)))
+        return int(ng.value), int(w.value), g, c
+
     def set_stage_tracers(self, stage: int, tracers: int):
         """FP32 form: tracers per launch of stage 0 lo_ad, 1 ho, 2 bounds, 3 update (0: all)."""
         self._chk(self.L.fesom_gpu_set_stage_tracers(self.h, int(stage), int(tracers)))
@@ -350,8 +364,8 @@ class Context:
         self._chk(self.L.fesom_gpu_set_tracers_per_launch(self.h, int(n)))
 
     def set_host_groups(self, sizes=()):
-        """Group sizes of ``step_host_f32`` in order (``fesom_gpu_set_host_groups``); an empty
-        sequence restores the default ramp."""
+        """Pipeline stages of ``step_host_f32`` in order, in tracer groups
+        (``fesom_gpu_set_host_groups``); an empty sequence restores the default ramp."""
         a = (C.c_int32 * max(1, len(sizes)))(*[int(x) for x in sizes])
         self._chk(self.L.fesom_gpu_set_host_groups(self.h, len(sizes), a))
 

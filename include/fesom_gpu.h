@@ -33,8 +33,8 @@
  * pointer (unified addressing), so a caller whose arrays already live on the
  * GPU (an OpenACC build passing `host_data use_device` addresses) moves nothing
  * over the host link.  fesom_gpu_tracer_device_ptr gives the device-resident
- * state; fesom_gpu_vdiff_impl_noalloc works on the caller's device arrays in
- * place.
+ * state of an FP64 context; fesom_gpu_vdiff_impl_noalloc works on the caller's
+ * device arrays in place.
  *
  * Error convention: every entry point returns 0 on success and a FESOM_ERR_*
  * code otherwise (the reference aborts through par_ex on the same conditions);
@@ -224,7 +224,8 @@ int fesom_gpu_forcing_upload_f32(fesom_gpu_ctx *ctx, const float *uv, const floa
 /* Runs nsteps tracer steps of dt on the device (graph replay when use_graph). */
 int fesom_gpu_run_steps(fesom_gpu_ctx *ctx, double dt, int32_t nsteps, int32_t use_graph);
 /* Tracers per launch of each stage (0 = as many as the work arrays hold; the
- * FP64 plain form uses 1, one tracer per launch as the reference loops). */
+ * FP64 plain form uses 1, one tracer per launch as the reference loops; the
+ * FP32 form rounds n up to whole tracer groups). */
 int fesom_gpu_set_tracers_per_launch(fesom_gpu_ctx *ctx, int32_t n);
 /* One step without the graph, with CUDA events around every stage on the
  * context stream; stage_ms[i] receives the summed time of stage i over all
@@ -271,7 +272,8 @@ int fesom_gpu_vdiff_impl_noalloc(int32_t nod2D, int32_t nl, const int32_t *nleve
 
 /* Global content sum_nodes sum_levels values*hnode_new*areasvol per tracer, in FP64. */
 int fesom_gpu_tracer_content(fesom_gpu_ctx *ctx, double *content);
-/* Device pointer of tracer tr's values (context precision), for zero-copy users. */
+/* Device pointer of tracer tr's values, for zero-copy users (FP64 contexts; an FP32
+ * context stores its tracers interleaved in groups and returns FESOM_ERR_STATE). */
 int fesom_gpu_tracer_device_ptr(fesom_gpu_ctx *ctx, int32_t tr, void **values, void **valuesold);
 
 /* Horizontal diffusion of diff_tracers_ale (diff_part_hor_redi, src/oce_ale_tracer.F90:1526-1689,
@@ -289,8 +291,8 @@ int fesom_gpu_set_hdiff(fesom_gpu_ctx *ctx, const double *Ki);
 int fesom_gpu_set_wsplit(fesom_gpu_ctx *ctx, int32_t on);
 /* Performance setting of the FP32 form (results do not change): tracers per launch of the
  * node/edge stages, stage 0 = LO and vertical fluxes, 1 = horizontal high-order fluxes,
- * 2 = FCT bounds, 3 = limited update; 0 = every tracer of the launch group in one pass.
- * Fewer tracers per pass keep the neighbour columns of the nodes in flight inside L2. */
+ * 2 = FCT bounds, 3 = limited update, rounded up to whole tracer groups; 0 (the default) =
+ * every group of the launch group in one launch. */
 int fesom_gpu_set_stage_tracers(fesom_gpu_ctx *ctx, int32_t stage, int32_t tracers);
 /* The routine alone (FP64 contexts): del_ttf += the edge diffusion fluxes of the element
  * gradients of values, in ascending edge order. */
@@ -321,24 +323,37 @@ int fesom_gpu_tracer_tail(fesom_gpu_ctx *ctx, int32_t ntr, const fesom_tra_cfg *
                           const fesom_tail_cfg *tc, const double *relax2clim, const double *Tclim, const double *Sclim,
                           const double *ztem, double *const *values);
 
+/* FP32 form, tracer groups (no counterpart in the reference): the tracers sit in groups of
+ * `width` (4, or 2) slots of one scheme (limiter, horizontal and vertical scheme, implicit
+ * vertical diffusion), interleaved in every (level, node) entry of the device arrays, so one
+ * vector load serves a whole group.  fesom_gpu_state_setup places the tracers in order, each
+ * into the first group of its scheme with room; the width is the one with the fewest slots
+ * (4 on a tie) unless fesom_gpu_set_tracer_width (0 = automatic, 2, 4) asked for one before
+ * the setup.  fesom_gpu_tracer_groups reports the placement: the group count, the width and,
+ * per tracer (arrays of the tracer count, NULL to skip), its group and slot. */
+int fesom_gpu_set_tracer_width(fesom_gpu_ctx *ctx, int32_t width);
+int fesom_gpu_tracer_groups(fesom_gpu_ctx *ctx, int32_t *groups, int32_t *width, int32_t *group_of,
+                            int32_t *slot_of);
 /* One step of an FP32 context from and to host arrays (FP32, the caller's layout), with the
- * transfers overlapped with the compute: the tracers move in groups of at most the tracers
- * per launch (fesom_gpu_set_tracers_per_launch) -- a group computes as soon as its values and
- * previous level are resident, and is copied back as soon as it is done, while later groups
- * upload and earlier ones download.  The first group's upload and the last group's download
- * are not hidden, so by default both groups are small and the groups between double up to the
- * launch group (G tracers per launch: max(1, G/3) tracers first and last; 24 tracers, G = 6:
- * 2, 4, 6, 6, 4, 2); fesom_gpu_set_host_groups sets another order.  values_out / valuesold_out may be the input arrays (in-place
- * update, as the reference's tracer arrays); valuesold_out may be NULL: the previous level
- * after the step is the values the step started from, so a caller that keeps two time-level
- * arrays and swaps them (values_out = valuesold_in, then exchange the roles) moves only the new
- * values back.  Blocks until the results are in host memory; page-locked host arrays give
- * the full transfer rate.  AB3 contexts take the serial path (their previous levels are interleaved on
- * the host). */
-/* Group sizes of fesom_gpu_step_host_f32, in order: n sizes of 1 to the tracers per launch
- * each, summing to the context's tracer count (FESOM_ERR_ARG otherwise); n = 0 restores the
- * default.  Cleared by fesom_gpu_set_tracers_per_launch and by a state setup with another
- * tracer count. */
+ * transfers overlapped with the compute: the tracer groups move in pipeline stages -- a stage
+ * is packed into the group layout and computed as soon as its values and previous levels are
+ * resident, and is unpacked and copied back as soon as it is done, while later stages upload
+ * and earlier ones download (two staging buffers each way, allocated on the first call).  The
+ * first stage's upload and the last stage's download are not hidden, so by default both stages
+ * are small and the stages between double up to the groups per launch
+ * (fesom_gpu_set_tracers_per_launch; L groups per launch: max(1, L/3) groups first and last);
+ * fesom_gpu_set_host_groups sets another order.  values_out / valuesold_out may be the input
+ * arrays (in-place update, as the reference's tracer arrays); valuesold_out may be NULL: the
+ * previous level after the step is the values the step started from, so a caller that keeps
+ * two time-level arrays and swaps them (values_out = valuesold_in, then exchange the roles)
+ * moves only the new values back.  AB3 previous levels are interleaved valuesold(2, level,
+ * node) as in the reference.  Blocks until the results are in host memory; page-locked host
+ * arrays give the full transfer rate.  fesom_gpu_tracer_step of an FP32 context runs the same
+ * pipeline on its FP64 host arrays (converted on the device). */
+/* Pipeline stages of fesom_gpu_step_host_f32 / fesom_gpu_tracer_step, in order: n sizes of 1
+ * to the groups per launch each, in tracer groups, summing to the context's group count
+ * (FESOM_ERR_ARG otherwise); n = 0 restores the default.  Cleared by
+ * fesom_gpu_set_tracers_per_launch and by a state setup that places the tracers anew. */
 int fesom_gpu_set_host_groups(fesom_gpu_ctx *ctx, int32_t n, const int32_t *sizes);
 int fesom_gpu_step_host_f32(fesom_gpu_ctx *ctx, double dt, const float *uv, const float *w, const float *wi,
                             const float *we, const float *Kv, const float *bc_surf, const float *const *values_in,

@@ -88,16 +88,20 @@ def test_host_step_with_swapped_time_levels(channel_seamount):
 
 
 def test_host_step_with_explicit_groups(channel_seamount):
-    """Group orders set by fesom_gpu_set_host_groups give the same values as the default ramp;
-    orders that miss or repeat a tracer, or exceed the tracers per launch, are rejected."""
+    """Pipeline stages set by fesom_gpu_set_host_groups (in tracer groups) give the same values
+    as the default ramp; orders that miss or repeat a group, or exceed the groups per launch,
+    are rejected.  The five tracers of four schemes sit in four groups of two slots."""
     mesh = channel_seamount
     f32, tr, cfgs = _setup(mesh, "channel", 2)
     n = len(cfgs)
     results = []
-    for sizes in ((), (3, 2), (1, 1, 1, 1, 1), (2, 3)):
+    for sizes in ((), (2, 2), (1, 1, 1, 1), (1, 2, 1)):
         b = G.Context(mesh, G.PREC_FP32, max_tracers=n)
         b.state_setup(cfgs)
-        b.set_tracers_per_launch(3)
+        ngr, width, grp, slot = b.tracer_groups()
+        assert (ngr, width) == (4, 2)
+        assert list(grp) == [0, 1, 2, 3, 0] and list(slot) == [0, 0, 0, 0, 1]
+        b.set_tracers_per_launch(3)  # two groups per launch
         b.set_host_groups(sizes)
         levels = [[np.array(tr[k], copy=True) for k in range(n)], [np.array(tr[k], copy=True) for k in range(n)]]
         for _ in range(2):
@@ -106,7 +110,7 @@ def test_host_step_with_explicit_groups(channel_seamount):
             levels.reverse()
         results.append(levels[0])
         assert b.status() == 0
-        for bad in ((3, 1), (4, 1), (3, 3), (0, 3, 2)):
+        for bad in ((3, 1), (2, 1), (2, 2, 1), (0, 2, 2)):
             with pytest.raises(G.FesomGpuError):
                 b.set_host_groups(bad)
         b.close()
