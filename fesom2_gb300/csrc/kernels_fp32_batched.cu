@@ -380,10 +380,10 @@ __device__ __forceinline__ float ab_delta(int ab, float t, float o1, float o2) {
 }
 
 // upwind flux of an edge-layer in the edge's direction, -(T1 v+ + T2 v-)
-// (oce_adv_tra_hor.F90:174-177, 0.5 (v +- |v|) = v+ / v-); rounded the same way wherever it
-// is formed, so the two end nodes of an edge add and subtract the same value
+// (oce_adv_tra_hor.F90:174-177, 0.5 (v +- |v|) = v+ / v-), both products rounded and then
+// summed: the rounding k32_lo_ad's node sums use for the same flux
 __device__ __forceinline__ float upw_flux(float T1, float T2, float v) {
-    return -__fmaf_rn(T1, fmaxf(v, 0.f), __fmul_rn(T2, fminf(v, 0.f)));
+    return -__fadd_rn(__fmul_rn(T1, fmaxf(v, 0.f)), __fmul_rn(T2, fminf(v, 0.f)));
 }
 
 // vertical high-order flux of interface nz on the AB values (QR4C / UPW1 / CDIFF,
@@ -437,15 +437,22 @@ __device__ __forceinline__ void lo_ad_chunk(const DTopo &tp, const DGeom<float> 
     const int i = n * L1 + nz - 1;   // layer nz of the node (valid where k.lvl)
     const int iv = n * nl + nz - 1;  // interface nz
     // ---- tracer-independent part of the chunk ----
+    // The node's share of edge slot u's upwind flux F = -(T1 v+ + T2 v-) (+F at edges(1,e),
+    // -F at edges(2,e)) is rn(rn(T_n p_u) + rn(T_m q_u)) with (p, q) = (-v+, -v-) at edges(1,e)
+    // and (v-, v+) at edges(2,e): the same two products and the same sum as at the other end,
+    // so the two ends add exactly opposite values.  A dry slot has p = q = 0 and gathers the
+    // node's own entry, so it adds zero without a per-tracer test.
     int off[KD];
-    float vf[KD];  // volume flux of each edge slot (0 where the slot is dry)
-    unsigned okm = 0;
+    float pq[KD], qq[KD];
 #pragma unroll
     for (int u = 0; u < KD; u++) {
         const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
-        off[u] = S.m[u] * L1 + nz - 1;
-        vf[u] = ok ? VF[S.e[u] * L1 + nz - 1] : 0.f;
-        okm |= ok ? 1u << u : 0u;
+        off[u] = ok ? S.m[u] * L1 + nz - 1 : i;
+        const float v = ok ? VF[S.e[u] * L1 + nz - 1] : 0.f;
+        const float vp = fmaxf(v, 0.f), vm = fminf(v, 0.f);
+        const bool ow = (own >> u) & 1u;
+        pq[u] = ow ? -vp : vm;
+        qq[u] = ow ? -vm : vp;
     }
     float ar0 = 0.f, we0 = 0.f, w0 = 0.f, sdt = 0.f, Z0 = 0.f, dhr = 0.f;
     if (k.lvl) {
@@ -478,7 +485,6 @@ __device__ __forceinline__ void lo_ad_chunk(const DTopo &tp, const DGeom<float> 
         const bool on = gg < B.ng;
         const int gi = on ? gg : g0;
         const bool lvt = k.lvl && on;
-        const unsigned okt = lvt ? okm : 0u;
         const bool lim = (B.fct >> gi) & 1ull;
         const int ver = B.ver[gi];
         const float *__restrict__ T = grp<G>(B.T, gi, B.sN);
@@ -490,7 +496,7 @@ __device__ __forceinline__ void lo_ad_chunk(const DTopo &tp, const DGeom<float> 
         const Vec<G> o2 = vldc<G>(lvt && B.ab == 3, O2, i);
         Vec<G> tm[KD];
 #pragma unroll
-        for (int u = 0; u < KD; u++) tm[u] = vldc<G>((okt >> u) & 1u, T, off[u]);
+        for (int u = 0; u < KD; u++) tm[u] = vldc<G>(lvt, T, off[u]);
         Vec<G> lo, ad;
 #pragma unroll
         for (int c = 0; c < G; c++) {
@@ -502,12 +508,7 @@ __device__ __forceinline__ void lo_ad_chunk(const DTopo &tp, const DGeom<float> 
             // order (oce_adv_tra_driver.F90:131-190)
             float hs = 0.f;
 #pragma unroll
-            for (int u = 0; u < KD; u++) {
-                const bool ow = (own >> u) & 1u;
-                const float tmv = tm[u].c[c];
-                const float F = upw_flux(ow ? tn : tmv, ow ? tmv : tn, vf[u]);
-                hs += ((okt >> u) & 1u) ? (ow ? F : -F) : 0.f;
-            }
+            for (int u = 0; u < KD; u++) hs += __fadd_rn(__fmul_rn(tn, pq[u]), __fmul_rn(tm[u].c[c], qq[u]));
             // upwind vertical flux with w_e at interface nz (adv_tra_ver_upw1)
             float fv0 = 0.f;
             if (lvt) {
@@ -770,14 +771,15 @@ __device__ __forceinline__ void bounds_chunk(const DTopo &tp, const DGeom<float>
     const C k = PACK ? C(nzmin, nzmax, ch, lane, W, P) : C(nzmin, nzmax, ch, lane);
     const int nz = k.nz;
     const int i = n * L1 + nz - 1, iv = n * nl + nz - 1;
+    // a dry slot gathers the node's own T and LO (neutral for the bounds); its ADh is not loaded
     int off[KD], eo[KD];
-    unsigned okm = 0;
+    unsigned okx = 0;
 #pragma unroll
     for (int u = 0; u < KD; u++) {
         const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
-        off[u] = S.m[u] * L1 + nz - 1;
-        eo[u] = S.e[u] * L1 + nz - 1;
-        okm |= ok ? 1u << u : 0u;
+        off[u] = ok ? S.m[u] * L1 + nz - 1 : i;
+        eo[u] = ok ? S.e[u] * L1 + nz - 1 : 0;
+        okx |= ok ? 1u << u : 0u;
     }
     const float s = k.lvl ? qdiv(dt, g.areasvol[iv] * g.hnode_new[i]) : 0.f;
     unsigned long long todo = B.fct & (B.ng >= 64 ? ~0ull : ((1ull << B.ng) - 1));
@@ -795,7 +797,6 @@ __device__ __forceinline__ void bounds_chunk(const DTopo &tp, const DGeom<float>
             todo &= todo - 1;
         }
         const bool lv = k.lvl && gq >= 0;
-        const unsigned okt = lv ? okm : 0u;
         const int gs = gq < 0 ? 0 : gq;
         const float *__restrict__ T = grp<G>(B.T, gs, B.sN);
         const float *__restrict__ LO = grp<G>(B.LO, gs, B.sN);
@@ -813,21 +814,19 @@ __device__ __forceinline__ void bounds_chunk(const DTopo &tp, const DGeom<float>
         }
 #pragma unroll
         for (int u = 0; u < KD; u++) {
-            const bool ok = (okt >> u) & 1u;
-            const Vec<G> tm = vldc<G>(ok, T, off[u]);
-            const Vec<G> lm = vldc<G>(ok, LO, off[u]);
+            const Vec<G> tm = vldc<G>(lv, T, off[u]);
+            const Vec<G> lm = vldc<G>(lv, LO, off[u]);
 #pragma unroll
             for (int c = 0; c < G; c++) {
-                const float a = ok ? tm.c[c] : Tn.c[c], b = ok ? lm.c[c] : lo.c[c];
-                mx.c[c] = fmaxf(mx.c[c], fmaxf(a, b));
-                mn.c[c] = fminf(mn.c[c], fminf(a, b));
+                mx.c[c] = fmaxf(mx.c[c], fmaxf(tm.c[c], lm.c[c]));
+                mn.c[c] = fminf(mn.c[c], fminf(tm.c[c], lm.c[c]));
             }
         }
         // P / M: sums of the positive / negative antidiffusive fluxes into the node
         Vec<G> Pp = vfill<G>(0.f), M = vfill<G>(0.f);
 #pragma unroll
         for (int u = 0; u < KD; u++) {
-            const Vec<G> x = vldc<G>((okt >> u) & 1u, ADh, eo[u]);
+            const Vec<G> x = vldc<G>(lv && ((okx >> u) & 1u), ADh, eo[u]);
             const bool ow = (own >> u) & 1u;
 #pragma unroll
             for (int c = 0; c < G; c++) {
@@ -913,14 +912,15 @@ __device__ __forceinline__ void update_chunk(const DTopo &tp, const DGeom<float>
     const int nz = k.nz;
     const int i = n * L1 + nz - 1, iv = n * nl + nz - 1;
     const float sdt = k.lvl ? qdiv(dt, g.areasvol[iv] * g.hnode_new[i]) : 0.f;
+    // a dry slot gathers the node's own R (finite); its ADh is not loaded (zero)
     int off[KD], eo[KD];
-    unsigned okm = 0;
+    unsigned okx = 0;
 #pragma unroll
     for (int u = 0; u < KD; u++) {
         const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
-        off[u] = S.m[u] * L1 + nz - 1;
-        eo[u] = S.e[u] * L1 + nz - 1;
-        okm |= ok ? 1u << u : 0u;
+        off[u] = ok ? S.m[u] * L1 + nz - 1 : i;
+        eo[u] = ok ? S.e[u] * L1 + nz - 1 : 0;
+        okx |= ok ? 1u << u : 0u;
     }
 #pragma unroll 1
     for (int g0 = 0; g0 < B.ng; g0 += PACK ? P : 1) {
@@ -932,7 +932,6 @@ __device__ __forceinline__ void update_chunk(const DTopo &tp, const DGeom<float>
         const bool dif = (B.diff >> gc) & 1ull;
         const bool lv = k.lvl && on;
         const bool lf = lv && fct;
-        const unsigned okt = lv ? okm : 0u;
         const float *__restrict__ Rp = grp<G>(B.Rp, gc, B.sN);
         const float *__restrict__ Rm = grp<G>(B.Rm, gc, B.sN);
         const float *__restrict__ ADh = grp<G>(B.ADh, gc, B.sE);
@@ -949,10 +948,9 @@ __device__ __forceinline__ void update_chunk(const DTopo &tp, const DGeom<float>
         Vec<G> hs = vfill<G>(0.f);
 #pragma unroll
         for (int u = 0; u < KD; u++) {
-            const bool ok = (okt >> u) & 1u;
-            const Vec<G> x = vldc<G>(ok, ADh, eo[u]);
-            const Vec<G> rmp = (ok && fct) ? vld<G>(Rp, off[u]) : vfill<G>(1.f);
-            const Vec<G> rmm = (ok && fct) ? vld<G>(Rm, off[u]) : vfill<G>(1.f);
+            const Vec<G> x = vldc<G>(lv && ((okx >> u) & 1u), ADh, eo[u]);
+            const Vec<G> rmp = lf ? vld<G>(Rp, off[u]) : vfill<G>(1.f);
+            const Vec<G> rmm = lf ? vld<G>(Rm, off[u]) : vfill<G>(1.f);
             const bool ow = (own >> u) & 1u;
             // horizontal limiting (oce_adv_tra_fct.F90:468-500) seen from the node: with G the
             // antidiffusive flux into the node and m the other end, G >= 0 takes
