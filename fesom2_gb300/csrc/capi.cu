@@ -78,7 +78,9 @@ struct fesom_gpu_ctx {
     float *Rp32 = nullptr, *Rm32 = nullptr, *Bp32 = nullptr, *Bm32 = nullptr;
     float *pack_in = nullptr, *pack_out = nullptr;  // staging of the host-array step (FP32 columns)
     size_t pack_n = 0;                   // floats each staging buffer holds
-    LaunchShape shape[4];                // lo_ad, ho, bounds, update (the autotuner's choice)
+    // lo_ad, ho, bounds, update (the autotuner's choice); lo_ad stages its gathers in shared
+    // memory by default, bounds and update keep them in registers
+    LaunchShape shape[4] = {{0, true}, {0, false}, {0, false}, {0, false}};
     MusclW mw{};
     cudaGraphExec_t gexec32[3] = {nullptr, nullptr, nullptr};
     double g32_dt[3] = {0.0, 0.0, 0.0};
@@ -657,6 +659,7 @@ int alloc_state32(fesom_gpu_ctx *ctx, int ab) {
     if ((rc = dalloc(ctx, (void **)&ctx->Bm32, wg * sN))) return rc;
     if (ctx->Ki && (rc = dalloc(ctx, (void **)&ctx->HD32, wg * sE))) return rc;
     // created here, not on first use: a first step may run inside a stream capture
+    CK(b32_prepare());
     if (!ctx->side) {
         CK(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
@@ -1641,6 +1644,20 @@ int fesom_gpu_tracer_content(fesom_gpu_ctx *ctx, double *content) {
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(content, ctx->content_out, sizeof(double) * ctx->ntr, cudaMemcpyDefault, ctx->stream));
     return wait_stream(ctx, -1);
+}
+
+int fesom_gpu_set_launch_shape(fesom_gpu_ctx *ctx, int32_t stage, int32_t blocks_per_sm) {
+    if (!ctx || stage < 0 || stage > 3 || blocks_per_sm < 0 || blocks_per_sm > 64) return FESOM_ERR_ARG;
+    ctx->shape[stage].blocks_per_sm = blocks_per_sm;
+    free_graphs32(ctx);
+    return FESOM_OK;
+}
+
+int fesom_gpu_set_stage_variant(fesom_gpu_ctx *ctx, int32_t stage, int32_t variant) {
+    if (!ctx || stage < 0 || stage > 3 || stage == 1 || variant < 0 || variant > 1) return FESOM_ERR_ARG;
+    ctx->shape[stage].staged = variant == 1;
+    free_graphs32(ctx);
+    return FESOM_OK;
 }
 
 int fesom_gpu_set_stage_tracers(fesom_gpu_ctx *ctx, int32_t stage, int32_t tracers) {

@@ -141,13 +141,18 @@ struct MusclW {
 struct VFactors {
     float *a, *c, *inv, *cp;
 };
+// once per process, before the first FP32 step (not inside a stream capture): the shared-memory
+// limits of the node kernels that stage their gathers
+cudaError_t b32_prepare();
 void b32_vflux(const DTopo &, const DGeom<float> &, const DForcing<float> &, float *VF, cudaStream_t);
 void b32_vfactors(const DTopo &, const DGeom<float> &, const DForcing<float> &, double dt, const VFactors &,
                   cudaStream_t);
 // launch shape of the node/edge stages (the autotuner's choices): blocks of 8 warps, at most
-// `blocks_per_sm` x 152 blocks (grid-stride loops over the units); 0: one warp per unit
+// `blocks_per_sm` x 152 blocks (grid-stride loops over the units; 0: one warp per unit), and
+// for lo_ad, bounds and update the kernel variant
 struct LaunchShape {
     int blocks_per_sm = 0;
+    bool staged = false;  // node stages: gathers staged in shared memory (cp.async) instead of registers
 };
 void b32_lo_ad(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, const float *VF,
                double dt, const LaunchShape &, cudaStream_t);

@@ -74,10 +74,31 @@ constexpr int kMaxChunks = 5;         // columns of up to 128 layers, 30 levels 
 // resident blocks per SM each group kernel is built for (registers: 65536 / (256 * blocks))
 template <int G>
 struct MinB {
+#ifdef FESOM_MINB_LO
+    static constexpr int lo = FESOM_MINB_LO;
+#else
     static constexpr int lo = 2;
+#endif
+#ifdef FESOM_MINB_HO
+    static constexpr int ho = FESOM_MINB_HO;
+#else
     static constexpr int ho = G == 4 ? 3 : 4;
-    static constexpr int bounds = G == 4 ? 2 : 3;
-    static constexpr int update = G == 4 ? 2 : 3;
+#endif
+    // bounds and update: gathers in registers (three blocks of eight warps per SM measured
+    // faster than two with more registers or one with the whole pass in flight), or staged in
+    // shared memory (which holds one block of the G = 4 staging per SM)
+    static constexpr int node_reg = 3;
+    static constexpr int node_stg = G == 4 ? 1 : 2;
+#ifdef FESOM_MINB_UPDATE_REG
+    static constexpr int update_reg = FESOM_MINB_UPDATE_REG;
+#else
+    static constexpr int update_reg = node_reg;
+#endif
+#ifdef FESOM_MINB_BOUNDS_REG
+    static constexpr int bounds_reg = FESOM_MINB_BOUNDS_REG;
+#else
+    static constexpr int bounds_reg = node_reg;
+#endif
 };
 
 __device__ __forceinline__ size_t i1(int nz, int n, int L1) { return (size_t)n * L1 + (nz - 1); }
@@ -373,6 +394,46 @@ __device__ __forceinline__ float *grp(float *base, int g, size_t count) {
     return base + (size_t)g * count * G;
 }
 
+// ---------------------------------------------------------------------------
+// per-lane asynchronous staging of a pass's gathers in shared memory
+// ---------------------------------------------------------------------------
+// The node stages gather, per pass (one chunk of a column for one tracer group), a few dozen
+// entries per lane: the node's own and every neighbour's.  Held in registers, only a part of
+// them can be in flight at once; staged with cp.async (one G-float copy per lane and entry,
+// zero-filled where the lane has nothing to gather) they all are, and the next pass's copies
+// run while the current pass computes.  Each lane reads back only what it copied, so the
+// staging needs no barrier: cp.async.wait_group orders a lane's copies before its reads.
+// Staging of a warp: [2 buffers][NS entries][32 lanes][G floats].
+template <int G>
+__device__ __forceinline__ void cpa(float *sdst, const float *gsrc, bool pred) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(sdst);
+    const size_t a = __cvta_generic_to_global(gsrc);
+    if constexpr (G == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(a), "r"(pred ? 16 : 0) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(a), "r"(pred ? 8 : 0) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpa_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+// entry s of the lane in a staging buffer
+template <int G>
+__device__ __forceinline__ float *stg(float *buf, int s, int lane) {
+    return buf + ((size_t)s * 32 + lane) * G;
+}
+template <int G>
+__device__ __forceinline__ Vec<G> lds(const float *p) {
+    if constexpr (G == 4) {
+        const float4 q = *reinterpret_cast<const float4 *>(p);
+        return Vec<4>{{q.x, q.y, q.z, q.w}};
+    } else {
+        const float2 q = *reinterpret_cast<const float2 *>(p);
+        return Vec<2>{{q.x, q.y}};
+    }
+}
+
 // Adams-Bashforth value minus the current value: AB2 -(0.5+eps) T^{n-1} + (1.5+eps) T^n,
 // AB3 (23 T^n - 16 T^{n-1} + 5 T^{n-2}) / 12 (oce_tracer_mod.F90:53, 67-68), eps = 0.1
 __device__ __forceinline__ float ab_delta(int ab, float t, float o1, float o2) {
@@ -546,14 +607,160 @@ __device__ __forceinline__ void lo_ad_chunk(const DTopo &tp, const DGeom<float> 
     }
 }
 
+// The same chunk with each pass's gathers staged in shared memory: entries T and the previous
+// levels of the node, then T of every edge slot (a dry slot stages the node's own T).
+constexpr int kNsLoAd = 3 + 6;
+template <int G, int KD, bool WS, bool PACK>
+__device__ __forceinline__ void lo_ad_chunk_pf(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
+                                               const B32View &B, const float *__restrict__ VF, float dt, int n,
+                                               int lane, const WEdges &S, int ch, int W, int P, float *sb) {
+    using C = Chunk<2, 1>;
+    constexpr int NS = 3 + KD;
+    static_assert(NS <= kNsLoAd, "staging sized for six edge slots");
+    const int L1 = tp.L1, nl = tp.nl;
+    const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
+    const unsigned own = S.own;
+    const C k = PACK ? C(nzmin, nzmax, ch, lane, W, P) : C(nzmin, nzmax, ch, lane);
+    const int nz = k.nz;
+    const int i = n * L1 + nz - 1;
+    const int iv = n * nl + nz - 1;
+    // tracer-independent part of the chunk (as in lo_ad_chunk)
+    int off[KD];
+    float pq[KD], qq[KD];
+#pragma unroll
+    for (int u = 0; u < KD; u++) {
+        const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
+        off[u] = ok ? S.m[u] * L1 + nz - 1 : (k.lvl ? i : 0);
+        const float v = ok ? VF[S.e[u] * L1 + nz - 1] : 0.f;
+        const float vp = fmaxf(v, 0.f), vm = fminf(v, 0.f);
+        const bool ow = (own >> u) & 1u;
+        pq[u] = ow ? -vp : vm;
+        qq[u] = ow ? -vm : vp;
+    }
+    float ar0 = 0.f, we0 = 0.f, w0 = 0.f, sdt = 0.f, Z0 = 0.f, dhr = 0.f;
+    if (k.lvl) {
+        ar0 = g.area[iv];
+        we0 = f.we[iv];
+        w0 = f.w[iv];
+        const float hn = g.hnode_new[i];
+        sdt = qdiv(dt, g.areasvol[iv] * hn);
+        dhr = qdiv(g.hnode[i] - hn, hn);
+        Z0 = g.Z3[i];
+    }
+    const float Zm1 = sh_up(Z0, 1), Zm2 = sh_up(Z0, 2), Zp1 = sh_dn(Z0, 1);
+    const bool qint = k.out && nz >= nzmin + 2 && nz <= nzmax - 2;
+    float idz0 = 0.f, idzp = 0.f, idzm = 0.f, g1 = 0.f, g2 = 0.f;
+    if (qint) {
+        const float zb = g.zbar3[iv];
+        idz0 = qdiv(1.f, Zm1 - Z0);
+        idzp = qdiv(1.f, Z0 - Zp1);
+        idzm = qdiv(1.f, Zm2 - Zm1);
+        g1 = (zb - Z0) * (1.f / 3.f);
+        g2 = (zb - Zm1) * (1.f / 3.f);
+    }
+    const bool twolayer = nzmin + 1 == nzmax - 1;
+    const int npass = PACK ? (B.ng + P - 1) / P : B.ng;
+    auto grp_of = [&](int p) { return PACK ? p * P + k.q : p; };
+    auto issue = [&](int p, float *buf) {
+        const int gg = grp_of(p);
+        const bool lvt = k.lvl && gg < B.ng;
+        const int gi = gg < B.ng ? gg : 0;
+        const float *T = grp<G>(B.T, gi, B.sN);
+        const int ii = lvt ? i : 0;
+        cpa<G>(stg<G>(buf, 0, lane), T + (size_t)ii * G, lvt);
+        cpa<G>(stg<G>(buf, 1, lane), grp<G>(B.O1, gi, B.sN) + (size_t)ii * G, lvt);
+        cpa<G>(stg<G>(buf, 2, lane), (B.ab == 3 ? grp<G>(B.O2, gi, B.sN) : T) + (size_t)ii * G, lvt && B.ab == 3);
+#pragma unroll
+        for (int u = 0; u < KD; u++) cpa<G>(stg<G>(buf, 3 + u, lane), T + (size_t)off[u] * G, lvt);
+        cpa_commit();
+    };
+    auto compute = [&](int p, float *buf) {
+        const int gg = grp_of(p);
+        const bool on = gg < B.ng;
+        const int gi = on ? gg : 0;
+        const bool lvt = k.lvl && on;
+        const bool lim = (B.fct >> gi) & 1ull;
+        const int ver = B.ver[gi];
+        const Vec<G> Tn = lds<G>(stg<G>(buf, 0, lane));
+        const Vec<G> o1 = lds<G>(stg<G>(buf, 1, lane));
+        const Vec<G> o2 = lds<G>(stg<G>(buf, 2, lane));
+        Vec<G> hs = vfill<G>(0.f);
+#pragma unroll
+        for (int u = 0; u < KD; u++) {
+            const Vec<G> tm = lds<G>(stg<G>(buf, 3 + u, lane));
+#pragma unroll
+            for (int c = 0; c < G; c++)
+                hs.c[c] += __fadd_rn(__fmul_rn(Tn.c[c], pq[u]), __fmul_rn(tm.c[c], qq[u]));
+        }
+        Vec<G> lo, ad;
+#pragma unroll
+        for (int c = 0; c < G; c++) {
+            const float tn = Tn.c[c];
+            const float tab = tn + (lvt ? ab_delta(B.ab, tn, o1.c[c], o2.c[c]) : 0.f);
+            const float Tu = sh_up(tn, 1);
+            const float tabu = sh_up(tab, 1), tabu2 = sh_up(tab, 2), tabd = sh_dn(tab, 1);
+            float fv0 = 0.f;
+            if (lvt) {
+                if (nz == nzmin) {
+                    fv0 = -(we0 * tn * ar0);
+                } else {
+                    const float aw = fabsf(we0);
+                    fv0 = -(0.5f * (tn * (we0 + aw) + Tu * (we0 - aw)) * ar0);
+                }
+            }
+            float fv1 = sh_dn(fv0, 1);
+            if (nz == nzmax - 1) fv1 = 0.f;
+            lo.c[c] = tn + fmaf(tn, dhr, (hs.c[c] + (fv0 - fv1)) * sdt);
+            float fw0 = fv0;
+            if (WS && f.wsplit && lvt) {
+                if (nz == nzmin) {
+                    fw0 = -(w0 * tn * ar0);
+                } else {
+                    const float aw = fabsf(w0);
+                    fw0 = -(0.5f * (tn * (w0 + aw) + Tu * (w0 - aw)) * ar0);
+                }
+            }
+            ad.c[c] = ver_ad(ver, lim, B.pv[gi * G + c], nz, nzmin, nzmax, twolayer, tab, tabu, tabu2, tabd,
+                             lim ? w0 : we0, ar0, fv0, fw0, idz0, idzp, idzm, g1, g2);
+        }
+        if (k.out && on) {
+            vst<G>(grp<G>(B.LO, gi, B.sN), i, lo);
+            if (ver != 3) vst<G>(grp<G>(B.ADv, gi, B.sNI), iv, ad);
+        }
+    };
+    issue(0, sb);
+    float *cur = sb, *nxt = sb + (size_t)NS * 32 * G;
+    for (int p = 0; p < npass; p++) {
+        if (p + 1 < npass) {
+            issue(p + 1, nxt);
+            cpa_wait<1>();
+        } else {
+            cpa_wait<0>();
+        }
+        compute(p, cur);
+        float *t = cur;
+        cur = nxt;
+        nxt = t;
+    }
+}
+
 template <int G, int KD, bool WS, bool PK>
 __device__ __forceinline__ void lo_ad_node(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
                                            const B32View &B, const float *__restrict__ VF, float dt, int n, int lane,
-                                           const WEdges &S) {
+                                           const WEdges &S, float *sb) {
     using C = Chunk<2, 1>;
     const int nch = C::count(S.nzmin, S.nzmax);
-    for (int ch = 0; ch < nch - 1; ch++) lo_ad_chunk<G, KD, WS, false>(tp, g, f, B, VF, dt, n, lane, S, ch, 32, 1);
     const int W = C::last_width(S.nzmin, S.nzmax), P = 32 / W;
+    if constexpr (KD == 6) {
+        if (sb) {
+            for (int ch = 0; ch < nch - 1; ch++)
+                lo_ad_chunk_pf<G, KD, WS, false>(tp, g, f, B, VF, dt, n, lane, S, ch, 32, 1, sb);
+            if (PK && P > 1) lo_ad_chunk_pf<G, KD, WS, true>(tp, g, f, B, VF, dt, n, lane, S, nch - 1, W, P, sb);
+            else lo_ad_chunk_pf<G, KD, WS, false>(tp, g, f, B, VF, dt, n, lane, S, nch - 1, 32, 1, sb);
+            return;
+        }
+    }
+    for (int ch = 0; ch < nch - 1; ch++) lo_ad_chunk<G, KD, WS, false>(tp, g, f, B, VF, dt, n, lane, S, ch, 32, 1);
     // packed only for nodes of at most 6 edges (the wider packed bodies would spill)
     if (PK && KD <= 6 && P > 1) lo_ad_chunk<G, KD, WS, true>(tp, g, f, B, VF, dt, n, lane, S, nch - 1, W, P);
     else lo_ad_chunk<G, KD, WS, false>(tp, g, f, B, VF, dt, n, lane, S, nch - 1, 32, 1);
@@ -573,27 +780,33 @@ __device__ __forceinline__ int node_units(const DTopo &tp) {
 // WS: the split vertical velocity (a separate instantiation keeps the default path unchanged)
 template <int G, bool WIDE, bool WS, bool PK>
 __device__ __forceinline__ void lo_ad_unit(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
-                                           const B32View &B, const float *__restrict__ VF, float dt, int j, WEdges *Se) {
+                                           const B32View &B, const float *__restrict__ VF, float dt, int j, WEdges *Se,
+                                           float *sb) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int n = unit_node<WIDE>(tp, j);
     if (n < 0) return;
     WEdges &S = Se[warp];
     stage_edges(tp, n, lane, S);
     if ((S.deg > 8) != WIDE) return;
-    if (WIDE) lo_ad_node<G, kMaxDeg, WS, PK>(tp, g, f, B, VF, dt, n, lane, S);
-    else if (S.deg <= 6) lo_ad_node<G, 6, WS, PK>(tp, g, f, B, VF, dt, n, lane, S);
-    else lo_ad_node<G, 8, WS, PK>(tp, g, f, B, VF, dt, n, lane, S);
+    if (WIDE) lo_ad_node<G, kMaxDeg, WS, PK>(tp, g, f, B, VF, dt, n, lane, S, nullptr);
+    else if (S.deg <= 6) lo_ad_node<G, 6, WS, PK>(tp, g, f, B, VF, dt, n, lane, S, sb);
+    else lo_ad_node<G, 8, WS, PK>(tp, g, f, B, VF, dt, n, lane, S, nullptr);
 }
+
+template <int G>
+__host__ __device__ constexpr int stage_bytes_lo_ad() { return 2 * kNsLoAd * 32 * G * 4; }
 
 // grid-stride loop of the warps over the units (one launch may hold fewer blocks than units)
 #define FOR_WARP_UNITS(j, count)                                                               \
     for (int j = blockIdx.x * kWB + (threadIdx.x >> 5); j < (count); j += gridDim.x * kWB)
 
-template <int G, bool WIDE, bool WS>
+template <int G, bool WIDE, bool WS, bool STG>
 __global__ void __launch_bounds__(kTB, WIDE ? 1 : MinB<G>::lo)
 k32_lo_ad(DTopo tp, DGeom<float> g, DForcing<float> f, B32View B, const float *__restrict__ VF, float dt) {
     __shared__ WEdges Se[kWB];
-    FOR_WARP_UNITS(j, node_units<WIDE>(tp)) lo_ad_unit<G, WIDE, WS, true>(tp, g, f, B, VF, dt, j, Se);
+    extern __shared__ __align__(16) float dsm[];
+    float *sb = (WIDE || !STG) ? nullptr : dsm + (size_t)(threadIdx.x >> 5) * (stage_bytes_lo_ad<G>() / 4);
+    FOR_WARP_UNITS(j, node_units<WIDE>(tp)) lo_ad_unit<G, WIDE, WS, true>(tp, g, f, B, VF, dt, j, Se, sb);
 }
 
 // high-order minus low-order flux of one edge-layer from the two end values, their
@@ -866,36 +1079,185 @@ __device__ __forceinline__ void bounds_chunk(const DTopo &tp, const DGeom<float>
     }
 }
 
+// The same chunk with each pass's gathers staged in shared memory (sb: the warp's staging):
+// entries T, LO, ADv of the node, then T, LO, ADh of every edge slot.
+constexpr int kNsBounds = 3 + 3 * 6;
+template <int G, int KD, bool PACK>
+__device__ __forceinline__ void bounds_chunk_pf(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt,
+                                                int n, int lane, const WEdges &S, int ch, int W, int P, float *sb) {
+    using C = Chunk<1, 1>;
+    constexpr int NS = 3 + 3 * KD;
+    static_assert(NS <= kNsBounds, "staging sized for six edge slots");
+    const int L1 = tp.L1, nl = tp.nl;
+    const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
+    const unsigned own = S.own;
+    const float eps = (float)kFluxEps;
+    const C k = PACK ? C(nzmin, nzmax, ch, lane, W, P) : C(nzmin, nzmax, ch, lane);
+    const int nz = k.nz;
+    const int i = n * L1 + nz - 1, iv = n * nl + nz - 1;
+    // a dry slot stages the node's own T and LO (neutral for the bounds) and zeros for ADh
+    int off[KD], eo[KD];
+    unsigned okx = 0;
+#pragma unroll
+    for (int u = 0; u < KD; u++) {
+        const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
+        off[u] = ok ? S.m[u] * L1 + nz - 1 : (k.lvl ? i : 0);
+        eo[u] = ok ? S.e[u] * L1 + nz - 1 : 0;
+        okx |= ok ? 1u << u : 0u;
+    }
+    const float s = k.lvl ? qdiv(dt, g.areasvol[iv] * g.hnode_new[i]) : 0.f;
+    unsigned todo = (unsigned)(B.fct & (B.ng >= 32 ? 0xffffffffull : ((1ull << B.ng) - 1)));
+    int g0 = 0;
+    // the lane's group of the next pass (-1: idle); false when no pass is left
+    auto next = [&](int &gq) -> bool {
+        if (PACK) {
+            if (g0 >= B.ng) return false;
+            gq = g0 + k.q;
+            if (gq >= B.ng || !((B.fct >> gq) & 1ull)) gq = -1;
+            g0 += P;
+            return true;
+        }
+        if (!todo) return false;
+        gq = __ffs(todo) - 1;
+        todo &= todo - 1;
+        return true;
+    };
+    auto issue = [&](int gq, float *buf) {
+        const bool lv = k.lvl && gq >= 0;
+        const int gs = gq < 0 ? 0 : gq;
+        const float *T = grp<G>(B.T, gs, B.sN), *LO = grp<G>(B.LO, gs, B.sN);
+        const float *ADh = grp<G>(B.ADh, gs, B.sE), *ADv = grp<G>(B.ADv, gs, B.sNI);
+        cpa<G>(stg<G>(buf, 0, lane), T + (size_t)(lv ? i : 0) * G, lv);
+        cpa<G>(stg<G>(buf, 1, lane), LO + (size_t)(lv ? i : 0) * G, lv);
+        cpa<G>(stg<G>(buf, 2, lane), ADv + (size_t)(lv ? iv : 0) * G, lv);
+#pragma unroll
+        for (int u = 0; u < KD; u++) {
+            cpa<G>(stg<G>(buf, 3 + 3 * u, lane), T + (size_t)off[u] * G, lv);
+            cpa<G>(stg<G>(buf, 4 + 3 * u, lane), LO + (size_t)off[u] * G, lv);
+            cpa<G>(stg<G>(buf, 5 + 3 * u, lane), ADh + (size_t)eo[u] * G, lv && ((okx >> u) & 1u));
+        }
+        cpa_commit();
+    };
+    auto compute = [&](int gq, float *buf) {
+        const Vec<G> Tn = lds<G>(stg<G>(buf, 0, lane));
+        const Vec<G> lo = lds<G>(stg<G>(buf, 1, lane));
+        const Vec<G> v0 = lds<G>(stg<G>(buf, 2, lane));
+        Vec<G> mx, mn, Pp = vfill<G>(0.f), M = vfill<G>(0.f);
+#pragma unroll
+        for (int c = 0; c < G; c++) {
+            mx.c[c] = fmaxf(lo.c[c], Tn.c[c]);
+            mn.c[c] = fminf(lo.c[c], Tn.c[c]);
+        }
+#pragma unroll
+        for (int u = 0; u < KD; u++) {
+            const Vec<G> tm = lds<G>(stg<G>(buf, 3 + 3 * u, lane));
+            const Vec<G> lm = lds<G>(stg<G>(buf, 4 + 3 * u, lane));
+            const Vec<G> x = lds<G>(stg<G>(buf, 5 + 3 * u, lane));
+            const bool ow = (own >> u) & 1u;
+#pragma unroll
+            for (int c = 0; c < G; c++) {
+                mx.c[c] = fmaxf(mx.c[c], fmaxf(tm.c[c], lm.c[c]));
+                mn.c[c] = fminf(mn.c[c], fminf(tm.c[c], lm.c[c]));
+                const float xv = ow ? x.c[c] : -x.c[c];
+                Pp.c[c] += fmaxf(0.f, xv);
+                M.c[c] += fminf(0.f, xv);
+            }
+        }
+        Vec<G> rp, rm, bp, bm;
+#pragma unroll
+        for (int c = 0; c < G; c++) {
+            const float mxu = sh_up(mx.c[c], 1), mxd = sh_dn(mx.c[c], 1);
+            const float mnu = sh_up(mn.c[c], 1), mnd = sh_dn(mn.c[c], 1);
+            float tup = mx.c[c], tlo = mn.c[c];
+            if (nz != nzmin && nz != nzmax - 1) {
+                tup = fmaxf(fmaxf(mxu, mx.c[c]), mxd);
+                tlo = fminf(fminf(mnu, mn.c[c]), mnd);
+            }
+            float v1 = sh_dn(v0.c[c], 1);
+            if (nz == nzmax - 1) v1 = 0.f;
+            const float pp = Pp.c[c] + (fmaxf(0.f, v0.c[c]) + fmaxf(0.f, -v1));
+            const float mm = M.c[c] + (fminf(0.f, v0.c[c]) + fminf(0.f, -v1));
+            const float bmx = tup - lo.c[c], bmn = tlo - lo.c[c];
+            rp.c[c] = fminf(1.f, qdiv(bmx, pp * s + eps));
+            rm.c[c] = fminf(1.f, qdiv(bmn, mm * s - eps));
+            bp.c[c] = tup;
+            bm.c[c] = tlo;
+        }
+        if (k.out && gq >= 0) {
+            vst<G>(grp<G>(B.Rp, gq, B.sN), i, rp);
+            vst<G>(grp<G>(B.Rm, gq, B.sN), i, rm);
+            vst<G>(grp<G>(B.Bp, gq, B.sN), i, bp);
+            vst<G>(grp<G>(B.Bm, gq, B.sN), i, bm);
+        }
+    };
+    int gq;
+    if (!next(gq)) return;
+    float *cur = sb, *nxt = sb + (size_t)NS * 32 * G;
+    issue(gq, cur);
+    for (;;) {
+        int gn;
+        const bool more = next(gn);
+        if (more) {
+            issue(gn, nxt);
+            cpa_wait<1>();
+        } else {
+            cpa_wait<0>();
+        }
+        compute(gq, cur);
+        if (!more) break;
+        float *t = cur;
+        cur = nxt;
+        nxt = t;
+        gq = gn;
+    }
+}
+
 template <int G, int KD, bool PK>
 __device__ __forceinline__ void bounds_node(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int n,
-                                            int lane, const WEdges &S) {
+                                            int lane, const WEdges &S, float *sb) {
     using C = Chunk<1, 1>;
     const int nch = C::count(S.nzmin, S.nzmax);
-    for (int ch = 0; ch < nch - 1; ch++) bounds_chunk<G, KD, false>(tp, g, B, dt, n, lane, S, ch, 32, 1);
     const int W = C::last_width(S.nzmin, S.nzmax), P = 32 / W;
+    if constexpr (KD == 6) {
+        if (sb) {
+            for (int ch = 0; ch < nch - 1; ch++) bounds_chunk_pf<G, KD, false>(tp, g, B, dt, n, lane, S, ch, 32, 1, sb);
+            if (PK && P > 1) bounds_chunk_pf<G, KD, true>(tp, g, B, dt, n, lane, S, nch - 1, W, P, sb);
+            else bounds_chunk_pf<G, KD, false>(tp, g, B, dt, n, lane, S, nch - 1, 32, 1, sb);
+            return;
+        }
+    }
+    for (int ch = 0; ch < nch - 1; ch++) bounds_chunk<G, KD, false>(tp, g, B, dt, n, lane, S, ch, 32, 1);
     if (PK && KD <= 6 && P > 1) bounds_chunk<G, KD, true>(tp, g, B, dt, n, lane, S, nch - 1, W, P);
     else bounds_chunk<G, KD, false>(tp, g, B, dt, n, lane, S, nch - 1, 32, 1);
 }
 
+// sb: the warp's shared-memory staging (null: the gathers go to registers)
 template <int G, bool WIDE, bool PK>
 __device__ __forceinline__ void bounds_unit(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int j,
-                                            WEdges *Se) {
+                                            WEdges *Se, float *sb) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int n = unit_node<WIDE>(tp, j);
     if (n < 0) return;
     WEdges &S = Se[warp];
     stage_edges(tp, n, lane, S);
     if ((S.deg > 8) != WIDE) return;
-    if (WIDE) bounds_node<G, kMaxDeg, PK>(tp, g, B, dt, n, lane, S);
-    else if (S.deg <= 6) bounds_node<G, 6, PK>(tp, g, B, dt, n, lane, S);
-    else bounds_node<G, 8, PK>(tp, g, B, dt, n, lane, S);
+    if (WIDE) bounds_node<G, kMaxDeg, PK>(tp, g, B, dt, n, lane, S, nullptr);
+    else if (S.deg <= 6) bounds_node<G, 6, PK>(tp, g, B, dt, n, lane, S, sb);
+    else bounds_node<G, 8, PK>(tp, g, B, dt, n, lane, S, nullptr);
 }
 
-template <int G, bool WIDE>
-__global__ void __launch_bounds__(kTB, WIDE ? 1 : MinB<G>::bounds)
+// staging bytes per warp of the bounds kernel (two buffers of NS entries)
+template <int G>
+__host__ __device__ constexpr int stage_bytes_bounds() { return 2 * kNsBounds * 32 * G * 4; }
+
+// STG: each pass's gathers staged in shared memory (fewer resident warps) instead of registers
+template <int G, bool WIDE, bool STG>
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : (STG ? MinB<G>::node_stg : MinB<G>::bounds_reg))
 k32_bounds(DTopo tp, DGeom<float> g, B32View B, float dt) {
     __shared__ WEdges Se[kWB];
-    FOR_WARP_UNITS(j, node_units<WIDE>(tp)) bounds_unit<G, WIDE, true>(tp, g, B, dt, j, Se);
+    extern __shared__ __align__(16) float dsm[];
+    float *sb = (WIDE || !STG) ? nullptr : dsm + (size_t)(threadIdx.x >> 5) * (stage_bytes_bounds<G>() / 4);
+    FOR_WARP_UNITS(j, node_units<WIDE>(tp)) bounds_unit<G, WIDE, true>(tp, g, B, dt, j, Se, sb);
 }
 
 // ---------------------------------------------------------------------------
@@ -997,36 +1359,178 @@ __device__ __forceinline__ void update_chunk(const DTopo &tp, const DGeom<float>
     }
 }
 
+// The same chunk with each pass's gathers staged in shared memory: entries LO, ADv, R+, R-, the
+// two bounds and the parked diffusion increment of the node, then ADh, R+, R- of every slot
+// (a dry slot stages zeros for ADh and the node's own R).
+constexpr int kNsUpdate = 7 + 3 * 6;
+template <int G, int KD, bool PACK>
+__device__ __forceinline__ void update_chunk_pf(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt,
+                                                int n, int lane, const WEdges &S, int ch, int W, int P, float *sb) {
+    using C = Chunk<1, 1>;
+    constexpr int NS = 7 + 3 * KD;
+    static_assert(NS <= kNsUpdate, "staging sized for six edge slots");
+    const int L1 = tp.L1, nl = tp.nl;
+    const int nzmin = S.nzmin, nzmax = S.nzmax, deg = S.deg;
+    const unsigned own = S.own;
+    const C k = PACK ? C(nzmin, nzmax, ch, lane, W, P) : C(nzmin, nzmax, ch, lane);
+    const int nz = k.nz;
+    const int i = n * L1 + nz - 1, iv = n * nl + nz - 1;
+    const float sdt = k.lvl ? qdiv(dt, g.areasvol[iv] * g.hnode_new[i]) : 0.f;
+    int off[KD], eo[KD];
+    unsigned okx = 0;
+#pragma unroll
+    for (int u = 0; u < KD; u++) {
+        const bool ok = u < deg && k.lvl && nz >= S.lo[u] && nz <= S.hi[u];
+        off[u] = ok ? S.m[u] * L1 + nz - 1 : (k.lvl ? i : 0);
+        eo[u] = ok ? S.e[u] * L1 + nz - 1 : 0;
+        okx |= ok ? 1u << u : 0u;
+    }
+    const int npass = PACK ? (B.ng + P - 1) / P : B.ng;
+    // the lane's group in pass p (packed: the group of its segment)
+    auto grp_of = [&](int p) { return PACK ? p * P + k.q : p; };
+    auto issue = [&](int p, float *buf) {
+        const int gq = grp_of(p);
+        const bool on = gq < B.ng;
+        const int gc = on ? gq : 0;
+        const bool lv = k.lvl && on;
+        const bool lf = lv && ((B.fct >> gc) & 1ull);
+        const bool ld = lv && ((B.diff >> gc) & 1ull);
+        const int ii = lv ? i : 0;
+        const float *Rp = grp<G>(B.Rp, gc, B.sN), *Rm = grp<G>(B.Rm, gc, B.sN);
+        const float *ADh = grp<G>(B.ADh, gc, B.sE);
+        cpa<G>(stg<G>(buf, 0, lane), grp<G>(B.LO, gc, B.sN) + (size_t)ii * G, lv);
+        cpa<G>(stg<G>(buf, 1, lane), grp<G>(B.ADv, gc, B.sNI) + (size_t)(lv ? iv : 0) * G, lv);
+        cpa<G>(stg<G>(buf, 2, lane), Rp + (size_t)ii * G, lf);
+        cpa<G>(stg<G>(buf, 3, lane), Rm + (size_t)ii * G, lf);
+        cpa<G>(stg<G>(buf, 4, lane), grp<G>(B.Bp, gc, B.sN) + (size_t)ii * G, lf);
+        cpa<G>(stg<G>(buf, 5, lane), grp<G>(B.Bm, gc, B.sN) + (size_t)ii * G, lf);
+        cpa<G>(stg<G>(buf, 6, lane), grp<G>(B.Tnew, gc, B.sN) + (size_t)ii * G, ld);
+#pragma unroll
+        for (int u = 0; u < KD; u++) {
+            cpa<G>(stg<G>(buf, 7 + 3 * u, lane), ADh + (size_t)eo[u] * G, lv && ((okx >> u) & 1u));
+            cpa<G>(stg<G>(buf, 8 + 3 * u, lane), Rp + (size_t)off[u] * G, lf);
+            cpa<G>(stg<G>(buf, 9 + 3 * u, lane), Rm + (size_t)off[u] * G, lf);
+        }
+        cpa_commit();
+    };
+    auto compute = [&](int p, float *buf) {
+        const int gq = grp_of(p);
+        const bool on = gq < B.ng;
+        const int gc = on ? gq : 0;
+        const bool fct = (B.fct >> gc) & 1ull;
+        const bool dif = (B.diff >> gc) & 1ull;
+        const Vec<G> lo = lds<G>(stg<G>(buf, 0, lane));
+        const Vec<G> f0 = lds<G>(stg<G>(buf, 1, lane));
+        const Vec<G> r0p = lds<G>(stg<G>(buf, 2, lane));
+        const Vec<G> r0m = lds<G>(stg<G>(buf, 3, lane));
+        Vec<G> hs = vfill<G>(0.f);
+#pragma unroll
+        for (int u = 0; u < KD; u++) {
+            const Vec<G> x = lds<G>(stg<G>(buf, 7 + 3 * u, lane));
+            const bool ow = (own >> u) & 1u;
+            if (fct) {
+                const Vec<G> rmp = lds<G>(stg<G>(buf, 8 + 3 * u, lane));
+                const Vec<G> rmm = lds<G>(stg<G>(buf, 9 + 3 * u, lane));
+#pragma unroll
+                for (int c = 0; c < G; c++) {
+                    float Gf = ow ? x.c[c] : -x.c[c];
+                    Gf *= Gf >= 0.f ? fminf(r0p.c[c], rmm.c[c]) : fminf(r0m.c[c], rmp.c[c]);
+                    hs.c[c] += Gf;
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < G; c++) hs.c[c] += ow ? x.c[c] : -x.c[c];
+            }
+        }
+        const Vec<G> tbp = lds<G>(stg<G>(buf, 4, lane));
+        const Vec<G> tbm = lds<G>(stg<G>(buf, 5, lane));
+        const Vec<G> dd = lds<G>(stg<G>(buf, 6, lane));
+        Vec<G> out;
+#pragma unroll
+        for (int c = 0; c < G; c++) {
+            const float rux = sh_up(r0p.c[c], 1), ruy = sh_up(r0m.c[c], 1);
+            float fz = f0.c[c];
+            if (fct) {
+                if (nz == nzmin) fz *= fz >= 0.f ? r0p.c[c] : r0m.c[c];
+                else fz *= fz >= 0.f ? fminf(ruy, r0p.c[c]) : fminf(rux, r0m.c[c]);
+            }
+            float f1 = sh_dn(fz, 1);
+            if (nz == nzmax - 1) f1 = 0.f;
+            float val = lo.c[c] + ((fz - f1) + hs.c[c]) * sdt;
+            if (k.out && on && fct) {
+                const float vc = fminf(fmaxf(val, tbm.c[c]), tbp.c[c]);
+                if (fabsf(vc - val) > 1e-5f * (tbp.c[c] - tbm.c[c]) + 1e-6f * fabsf(vc)) atomicOr(B.status, 2u);
+                val = vc;
+            }
+            if (dif) val += dd.c[c];
+            out.c[c] = val;
+        }
+        if (k.out && on) {
+            vst<G>(grp<G>(B.Tnew, gc, B.sN), i, out);
+#pragma unroll
+            for (int c = 0; c < G; c++)
+                if (!isfinite(out.c[c])) atomicOr(B.status, 1u);
+        }
+    };
+    issue(0, sb);
+    float *cur = sb, *nxt = sb + (size_t)NS * 32 * G;
+    for (int p = 0; p < npass; p++) {
+        if (p + 1 < npass) {
+            issue(p + 1, nxt);
+            cpa_wait<1>();
+        } else {
+            cpa_wait<0>();
+        }
+        compute(p, cur);
+        float *t = cur;
+        cur = nxt;
+        nxt = t;
+    }
+}
+
 template <int G, int KD, bool PK>
 __device__ __forceinline__ void update_node(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt,
-                                            int n, int lane, const WEdges &S) {
+                                            int n, int lane, const WEdges &S, float *sb) {
     using C = Chunk<1, 1>;
     const int nch = C::count(S.nzmin, S.nzmax);
-    for (int ch = 0; ch < nch - 1; ch++) update_chunk<G, KD, false>(tp, g, B, dt, n, lane, S, ch, 32, 1);
     const int W = C::last_width(S.nzmin, S.nzmax), P = 32 / W;
+    if constexpr (KD == 6) {
+        if (sb) {
+            for (int ch = 0; ch < nch - 1; ch++) update_chunk_pf<G, KD, false>(tp, g, B, dt, n, lane, S, ch, 32, 1, sb);
+            if (PK && P > 1) update_chunk_pf<G, KD, true>(tp, g, B, dt, n, lane, S, nch - 1, W, P, sb);
+            else update_chunk_pf<G, KD, false>(tp, g, B, dt, n, lane, S, nch - 1, 32, 1, sb);
+            return;
+        }
+    }
+    for (int ch = 0; ch < nch - 1; ch++) update_chunk<G, KD, false>(tp, g, B, dt, n, lane, S, ch, 32, 1);
     if (PK && KD <= 6 && P > 1) update_chunk<G, KD, true>(tp, g, B, dt, n, lane, S, nch - 1, W, P);
     else update_chunk<G, KD, false>(tp, g, B, dt, n, lane, S, nch - 1, 32, 1);
 }
 
 template <int G, bool WIDE, bool PK>
 __device__ __forceinline__ void update_unit(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int j,
-                                            WEdges *Se) {
+                                            WEdges *Se, float *sb) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int n = unit_node<WIDE>(tp, j);
     if (n < 0) return;
     WEdges &S = Se[warp];
     stage_edges(tp, n, lane, S);
     if ((S.deg > 8) != WIDE) return;
-    if (WIDE) update_node<G, kMaxDeg, PK>(tp, g, B, dt, n, lane, S);
-    else if (S.deg <= 6) update_node<G, 6, PK>(tp, g, B, dt, n, lane, S);
-    else update_node<G, 8, PK>(tp, g, B, dt, n, lane, S);
+    if (WIDE) update_node<G, kMaxDeg, PK>(tp, g, B, dt, n, lane, S, nullptr);
+    else if (S.deg <= 6) update_node<G, 6, PK>(tp, g, B, dt, n, lane, S, sb);
+    else update_node<G, 8, PK>(tp, g, B, dt, n, lane, S, nullptr);
 }
 
-template <int G, bool WIDE>
-__global__ void __launch_bounds__(kTB, WIDE ? 1 : MinB<G>::update)
+template <int G>
+__host__ __device__ constexpr int stage_bytes_update() { return 2 * kNsUpdate * 32 * G * 4; }
+
+template <int G, bool WIDE, bool STG>
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : (STG ? MinB<G>::node_stg : MinB<G>::update_reg))
 k32_update(DTopo tp, DGeom<float> g, B32View B, float dt) {
     __shared__ WEdges Se[kWB];
-    FOR_WARP_UNITS(j, node_units<WIDE>(tp)) update_unit<G, WIDE, true>(tp, g, B, dt, j, Se);
+    extern __shared__ __align__(16) float dsm[];
+    float *sb = (WIDE || !STG) ? nullptr : dsm + (size_t)(threadIdx.x >> 5) * (stage_bytes_update<G>() / 4);
+    FOR_WARP_UNITS(j, node_units<WIDE>(tp)) update_unit<G, WIDE, true>(tp, g, B, dt, j, Se, sb);
 }
 
 // ---------------------------------------------------------------------------
@@ -1762,8 +2266,10 @@ __global__ void __launch_bounds__(kTB, WIDE ? 1 : MinB<4>::lo) k32m_lo_ad(const 
     __shared__ WEdges Se[kWB];
     FOR_WARP_UNITS(u, ix.start[ix.n]) {
         const int i = find_inst(ix, u);
-        if (I[i].B.G == 4) lo_ad_unit<4, WIDE, WS, true>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].VF, I[i].dt, u - ix.start[i], Se);
-        else lo_ad_unit<2, WIDE, WS, true>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].VF, I[i].dt, u - ix.start[i], Se);
+        if (I[i].B.G == 4)
+            lo_ad_unit<4, WIDE, WS, true>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].VF, I[i].dt, u - ix.start[i], Se, nullptr);
+        else
+            lo_ad_unit<2, WIDE, WS, true>(I[i].tp, I[i].g, I[i].f, I[i].B, I[i].VF, I[i].dt, u - ix.start[i], Se, nullptr);
     }
 }
 __global__ void __launch_bounds__(kTB, MinB<4>::ho) k32m_ho(const Inst32 *__restrict__ I, MultiIdx ix) {
@@ -1781,21 +2287,21 @@ __global__ void __launch_bounds__(256) k32m_ho_nodemean(const Inst32 *__restrict
     else nodemean_item<2>(I[i].tp, I[i].B, I[i].mw, I[i].VF, u - ix.start[i]);
 }
 template <bool WIDE>
-__global__ void __launch_bounds__(kTB, WIDE ? 1 : MinB<4>::bounds) k32m_bounds(const Inst32 *__restrict__ I, MultiIdx ix) {
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : MinB<4>::node_reg) k32m_bounds(const Inst32 *__restrict__ I, MultiIdx ix) {
     __shared__ WEdges Se[kWB];
     FOR_WARP_UNITS(u, ix.start[ix.n]) {
         const int i = find_inst(ix, u);
-        if (I[i].B.G == 4) bounds_unit<4, WIDE, true>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
-        else bounds_unit<2, WIDE, true>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
+        if (I[i].B.G == 4) bounds_unit<4, WIDE, true>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se, nullptr);
+        else bounds_unit<2, WIDE, true>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se, nullptr);
     }
 }
 template <bool WIDE>
-__global__ void __launch_bounds__(kTB, WIDE ? 1 : MinB<4>::update) k32m_update(const Inst32 *__restrict__ I, MultiIdx ix) {
+__global__ void __launch_bounds__(kTB, WIDE ? 1 : MinB<4>::node_reg) k32m_update(const Inst32 *__restrict__ I, MultiIdx ix) {
     __shared__ WEdges Se[kWB];
     FOR_WARP_UNITS(u, ix.start[ix.n]) {
         const int i = find_inst(ix, u);
-        if (I[i].B.G == 4) update_unit<4, WIDE, true>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
-        else update_unit<2, WIDE, true>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se);
+        if (I[i].B.G == 4) update_unit<4, WIDE, true>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se, nullptr);
+        else update_unit<2, WIDE, true>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se, nullptr);
     }
 }
 __global__ void __launch_bounds__(32 * kWV) k32m_vdiff(const Inst32 *__restrict__ I, MultiIdx ix) {
@@ -1873,16 +2379,63 @@ void b32_vfactors(const DTopo &tp, const DGeom<float> &g, const DForcing<float> 
     k32_vfactors<<<(tp.N2 + kVfCols - 1) / kVfCols, kVfCols, 0, s>>>(tp, g, f, dt, v);
 }
 
+// dynamic shared memory of the staged node kernels: kWB warps' staging
+template <int G>
+constexpr int smem_lo_ad() { return kWB * stage_bytes_lo_ad<G>(); }
+template <int G>
+constexpr int smem_bounds() { return kWB * stage_bytes_bounds<G>(); }
+template <int G>
+constexpr int smem_update() { return kWB * stage_bytes_update<G>(); }
+
+template <int G>
+static cudaError_t prepare_g() {
+    cudaError_t e = cudaSuccess;
+    auto set = [&](const void *fn, int bytes) {
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    };
+    set((const void *)k32_lo_ad<G, false, false, true>, smem_lo_ad<G>());
+    set((const void *)k32_lo_ad<G, false, true, true>, smem_lo_ad<G>());
+    set((const void *)k32_bounds<G, false, true>, smem_bounds<G>());
+    set((const void *)k32_update<G, false, true>, smem_update<G>());
+    return e;
+}
+cudaError_t b32_prepare() {
+    static cudaError_t done = cudaErrorNotReady;
+    if (done == cudaSuccess) return done;
+    cudaError_t e = prepare_g<4>();
+    if (e == cudaSuccess) e = prepare_g<2>();
+    done = e;
+    return e;
+}
+
+template <int G, bool WS>
+static void lo_ad_gw(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B,
+                     const float *VF, double dt, const LaunchShape &sh, cudaStream_t s) {
+    if (sh.staged)
+        k32_lo_ad<G, false, WS, true><<<grid_units(tp.N2, sh), kTB, smem_lo_ad<G>(), s>>>(tp, g, f, B, VF, (float)dt);
+    else
+        k32_lo_ad<G, false, WS, false><<<grid_units(tp.N2, sh), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
+    if (tp.n_wide) k32_lo_ad<G, true, WS, false><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
+}
 template <int G>
 static void lo_ad_g(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B, const float *VF,
                     double dt, const LaunchShape &sh, cudaStream_t s) {
-    if (f.wsplit) {
-        k32_lo_ad<G, false, true><<<grid_units(tp.N2, sh), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
-        if (tp.n_wide) k32_lo_ad<G, true, true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
-    } else {
-        k32_lo_ad<G, false, false><<<grid_units(tp.N2, sh), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
-        if (tp.n_wide) k32_lo_ad<G, true, false><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, f, B, VF, (float)dt);
-    }
+    if (f.wsplit) lo_ad_gw<G, true>(tp, g, f, B, VF, dt, sh, s);
+    else lo_ad_gw<G, false>(tp, g, f, B, VF, dt, sh, s);
+}
+template <int G>
+static void bounds_g(const DTopo &tp, const DGeom<float> &g, const B32View &B, double dt, const LaunchShape &sh,
+                     cudaStream_t s) {
+    if (sh.staged) k32_bounds<G, false, true><<<grid_units(tp.N2, sh), kTB, smem_bounds<G>(), s>>>(tp, g, B, (float)dt);
+    else k32_bounds<G, false, false><<<grid_units(tp.N2, sh), kTB, 0, s>>>(tp, g, B, (float)dt);
+    if (tp.n_wide) k32_bounds<G, true, false><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
+}
+template <int G>
+static void update_g(const DTopo &tp, const DGeom<float> &g, const B32View &B, double dt, const LaunchShape &sh,
+                     cudaStream_t s) {
+    if (sh.staged) k32_update<G, false, true><<<grid_units(tp.N2, sh), kTB, smem_update<G>(), s>>>(tp, g, B, (float)dt);
+    else k32_update<G, false, false><<<grid_units(tp.N2, sh), kTB, 0, s>>>(tp, g, B, (float)dt);
+    if (tp.n_wide) k32_update<G, true, false><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
 }
 void b32_lo_ad(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B, const float *VF,
                double dt, const LaunchShape &sh, cudaStream_t s) {
@@ -1906,23 +2459,13 @@ void b32_ho(const DTopo &tp, const DGeom<float> &, const B32View &B, const Muscl
 }
 void b32_bounds(const DTopo &tp, const DGeom<float> &g, const B32View &B, double dt, const LaunchShape &sh,
                 cudaStream_t s) {
-    if (B.G == 4) {
-        k32_bounds<4, false><<<grid_units(tp.N2, sh), kTB, 0, s>>>(tp, g, B, (float)dt);
-        if (tp.n_wide) k32_bounds<4, true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
-    } else {
-        k32_bounds<2, false><<<grid_units(tp.N2, sh), kTB, 0, s>>>(tp, g, B, (float)dt);
-        if (tp.n_wide) k32_bounds<2, true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
-    }
+    if (B.G == 4) bounds_g<4>(tp, g, B, dt, sh, s);
+    else bounds_g<2>(tp, g, B, dt, sh, s);
 }
 void b32_update(const DTopo &tp, const DGeom<float> &g, const B32View &B, double dt, const LaunchShape &sh,
                 cudaStream_t s) {
-    if (B.G == 4) {
-        k32_update<4, false><<<grid_units(tp.N2, sh), kTB, 0, s>>>(tp, g, B, (float)dt);
-        if (tp.n_wide) k32_update<4, true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
-    } else {
-        k32_update<2, false><<<grid_units(tp.N2, sh), kTB, 0, s>>>(tp, g, B, (float)dt);
-        if (tp.n_wide) k32_update<2, true><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
-    }
+    if (B.G == 4) update_g<4>(tp, g, B, dt, sh, s);
+    else update_g<2>(tp, g, B, dt, sh, s);
 }
 void b32_vdiff(const DTopo &tp, const DForcing<float> &, const B32View &B, const VFactors &v, cudaStream_t s) {
     if (B.G == 4) k32_vdiff<4><<<(tp.N2 + kWV - 1) / kWV, 32 * kWV, 0, s>>>(tp, B, v);

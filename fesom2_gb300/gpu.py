@@ -96,6 +96,8 @@ _SIGS = {
     "fesom_gpu_set_hdiff": ([_P, _P], C.c_int),
     "fesom_gpu_set_wsplit": ([_P, C.c_int32], C.c_int),
     "fesom_gpu_set_stage_tracers": ([_P, C.c_int32, C.c_int32], C.c_int),
+    "fesom_gpu_set_launch_shape": ([_P, C.c_int32, C.c_int32], C.c_int),
+    "fesom_gpu_set_stage_variant": ([_P, C.c_int32, C.c_int32], C.c_int),
     "fesom_gpu_vdiff_impl_wi": ([_P, C.c_double, C.POINTER(TraCfg), _P, _P, _P, _P], C.c_int),
     "fesom_gpu_diff_hor": ([_P, C.c_double, _P, _P, _P], C.c_int),
     "fesom_gpu_diff_ver_expl": ([_P, C.c_double, _P, _P, _P, _P], C.c_int),
@@ -294,6 +296,16 @@ class Context:
     def set_stage_tracers(self, stage: int, tracers: int):
         """FP32 form: tracers per launch of stage 0 lo_ad, 1 ho, 2 bounds, 3 update (0: all)."""
         self._chk(self.L.fesom_gpu_set_stage_tracers(self.h, int(stage), int(tracers)))
+
+    def set_launch_shape(self, stage: int, blocks_per_sm: int):
+        """FP32 form: at most blocks_per_sm x 152 blocks for stage 0 lo_ad, 1 ho, 2 bounds, 3 update
+        (0: one warp per node or edge)."""
+        self._chk(self.L.fesom_gpu_set_launch_shape(self.h, int(stage), int(blocks_per_sm)))
+
+    def set_stage_variant(self, stage: int, variant: int):
+        """FP32 form: kernel variant of stage 0 lo_ad, 2 bounds, 3 update (0: gathers in registers,
+        1: staged in shared memory)."""
+        self._chk(self.L.fesom_gpu_set_stage_variant(self.h, int(stage), int(variant)))
 
     def set_wsplit(self, on: bool):
         """dynamics%use_wsplit for every later step (fesom_gpu_set_wsplit)."""

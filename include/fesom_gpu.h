@@ -294,6 +294,17 @@ int fesom_gpu_set_wsplit(fesom_gpu_ctx *ctx, int32_t on);
  * 2 = FCT bounds, 3 = limited update, rounded up to whole tracer groups; 0 (the default) =
  * every group of the launch group in one launch. */
 int fesom_gpu_set_stage_tracers(fesom_gpu_ctx *ctx, int32_t stage, int32_t tracers);
+/* Performance setting of the FP32 form (results do not change): grid of the node/edge stage
+ * kernels (stages as in fesom_gpu_set_stage_tracers): blocks_per_sm > 0 launches at most
+ * blocks_per_sm x 152 blocks whose warps loop over the units (nodes, edges); 0 (the default)
+ * launches one warp per unit. */
+int fesom_gpu_set_launch_shape(fesom_gpu_ctx *ctx, int32_t stage, int32_t blocks_per_sm);
+/* Performance setting of the FP32 form: kernel variant of node stage 0 (lo_ad), 2 (bounds) or
+ * 3 (update): 0 gathers each pass's neighbour values into registers, 1 stages them in shared
+ * memory with asynchronous copies while the previous pass computes (fewer resident warps, no
+ * register limit on the gathers in flight).  Defaults: lo_ad 1, bounds 0, update 0.  The two
+ * variants are separate compilations and agree to FP32 round-off. */
+int fesom_gpu_set_stage_variant(fesom_gpu_ctx *ctx, int32_t stage, int32_t variant);
 /* The routine alone (FP64 contexts): del_ttf += the edge diffusion fluxes of the element
  * gradients of values, in ascending edge order. */
 int fesom_gpu_diff_hor(fesom_gpu_ctx *ctx, double dt, const double *Ki, const double *values, double *del_ttf);

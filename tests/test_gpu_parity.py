@@ -338,29 +338,45 @@ def test_fp32_mixed_schemes_in_one_batch(basin_irregular):
     assert ctx.status() == 0
 
 
-def test_fp32_stage_passes_do_not_change_results(basin_irregular):
-    """Tracers per launch of each node stage (fesom_gpu_set_stage_tracers) is a performance
-    setting: any split of the 7 tracers gives the same bits."""
-    mesh = basin_irregular
-    f, tr = _setup(mesh, "basin", ntr=7)
+@pytest.mark.parametrize("meshname,kind", [("basin_irregular", "basin"), ("sphere_small", "sphere")])
+def test_fp32_stage_passes_do_not_change_results(meshname, kind, request):
+    """Tracers per launch of each node stage (fesom_gpu_set_stage_tracers), the grid of the
+    stage kernels (fesom_gpu_set_launch_shape) and their variant (fesom_gpu_set_stage_variant:
+    gathers in registers or staged in shared memory) are performance settings.  Splits and
+    grids run the same code and give the same bits; the two variants of a stage are separate
+    compilations whose products may contract differently, so they agree to FP32 round-off."""
+    mesh = request.getfixturevalue(meshname)
+    f, tr = _setup(mesh, kind, ntr=7)
     cfgs = [G.tra_cfg(["MUSCL", "MFCT", "UPW1"][k % 3], ["QR4C", "UPW1", "PPM", "CDIFF"][k % 4],
                       "FCT" if k % 3 else "NON", id=k + 1) for k in range(7)]
+    combos = (([0, 0, 0, 0], [0, 0, 0, 0], [1, 0, 0]), ([3, 2, 5, 1], [2, 3, 1, 2], [1, 0, 0]),
+              ([1, 7, 2, 4], [0, 0, 0, 0], [1, 0, 0]), ([3, 2, 5, 1], [0, 0, 0, 0], [0, 1, 1]),
+              ([1, 7, 2, 4], [1, 2, 2, 1], [0, 1, 1]))
     outs = []
-    for split in ([0, 0, 0, 0], [3, 2, 5, 1], [1, 7, 2, 4]):
+    for split, shape, variant in combos:
         ctx = G.Context(mesh, G.PREC_FP32, max_tracers=7)
         ctx.state_setup(cfgs)
         ctx.forcing_upload(f)
         for st, v in enumerate(split):
             ctx.set_stage_tracers(st, v)
+        for st, v in enumerate(shape):
+            ctx.set_launch_shape(st, v)
+        for st, v in zip((0, 2, 3), variant):
+            ctx.set_stage_variant(st, v)
         for k in range(7):
             t32 = tr[k].astype(np.float32)
             ctx.tracer_upload(k, t32, t32)
         ctx.run_steps(f.dt, 3, use_graph=True)
         outs.append([ctx.tracer_download(k, dtype=np.float32)[0] for k in range(7)])
         assert ctx.status() == 0
-    for o in outs[1:]:
+        ctx.close()
+    # same variant: bit for bit
+    for i, ref in ((1, 0), (2, 0), (4, 3)):
         for k in range(7):
-            assert np.array_equal(o[k], outs[0][k]), k
+            assert np.array_equal(outs[i][k], outs[ref][k]), (i, k)
+    # other variant: FP32 round-off
+    for k in range(7):
+        assert np.abs(outs[3][k] - outs[0][k]).max() <= 1e-6 * np.abs(outs[0][k]).max(), k
 
 
 def test_device_pointers_give_the_host_results(channel_seamount):
