@@ -925,6 +925,29 @@ def make_tracers(mesh: Mesh, kind: str, ntr: int = 2, seed: int = 5, Lj: float =
     return out
 
 
+def make_slopes(mesh: Mesh, seed: int = 13, smax: float = 2e-3, s_cr: float = 1e-3, s_d: float = 1e-3,
+                dtype=np.float64) -> np.ndarray:
+    """Tapered neutral slopes slope_tapered(3, nl-1, nod2D) as (N2, nl-1, 3); dry levels 0.
+
+    Components 1, 2 are smooth random horizontal slopes of magnitude ~smax, component 3 their
+    norm; all three carry the hyperbolic-tangent taper c = (1 + tanh((s_cr - |S|) / s_d)) / 2 of
+    compute_neutral_slope (src/oce_ale_pressure_bv.F90:3039-3157, ODM95 tapering)."""
+    rng = np.random.default_rng(seed)
+    N2, L1 = mesh.nod2D, mesh.nl - 1
+    lat, lon = mesh.coord_nod2D[:, 1], mesh.coord_nod2D[:, 0]
+    xyz = np.stack([np.cos(lat) * np.cos(lon), np.cos(lat) * np.sin(lon), np.sin(lat)], axis=1)
+    sx = _smooth_field_3d(xyz, rng)[:, None]
+    sy = _smooth_field_3d(xyz, rng)[:, None]
+    prof = np.exp(-node_depth_mid(mesh) / 1500.0) * (0.5 + rng.uniform(0, 1, (1, L1)))
+    S = np.stack([smax * sx * prof, smax * sy * prof], axis=2)
+    s3 = np.sqrt(S[:, :, 0] ** 2 + S[:, :, 1] ** 2)
+    c = 0.5 * (1.0 + np.tanh((s_cr - s3) / s_d))
+    out = np.concatenate([S, s3[:, :, None]], axis=2) * c[:, :, None]
+    lev = np.arange(L1)[None, :]
+    wet = (lev >= (mesh.ulevels_nod2D - 1)[:, None]) & (lev < (mesh.nlevels_nod2D - 1)[:, None])
+    return np.ascontiguousarray(np.where(wet[:, :, None], out, 0.0).astype(dtype))
+
+
 # ---------------------------------------------------------------------------
 # named configurations
 # ---------------------------------------------------------------------------

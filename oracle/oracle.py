@@ -66,10 +66,12 @@ def lib() -> C.CDLL:
                      "or_oce_tra_adv_flux2dtracer", "or_do_oce_adv_tra", "or_diff_ver_part_impl_ale",
                      "or_tracer_step", "or_set_threads", "or_get_threads", "or_tracer_tail",
                      "or_diff_part_hor_redi", "or_diff_ver_part_expl_ale", "or_tracer_step_ex",
-                     "or_tracer_gradient_z"):
+                     "or_tracer_gradient_z", "or_tracer_step_redi", "or_diff_part_hor_redi_s",
+                     "or_diff_ver_part_redi_expl", "or_redi_k33"):
             getattr(L, name)
         L.or_tracer_step.restype = C.c_int
         L.or_tracer_step_ex.restype = C.c_int
+        L.or_tracer_step_redi.restype = C.c_int
         L.or_do_oce_adv_tra.restype = C.c_int
         L.or_set_threads.argtypes = [C.c_int]
         _lib = L
@@ -161,21 +163,42 @@ class OracleMesh:
         if rc != 0:
             raise RuntimeError(f"oracle do_oce_adv_tra failed with status {rc}")
 
-    def tracer_step_ex(self, forcing, cfg: _OrCfg, values, valuesAB, valuesold, Ki=None, dt=None) -> None:
-        """tracer_step with the horizontal diffusion of Ki (None: K_hor = 0)."""
+    def tracer_step_ex(self, forcing, cfg: _OrCfg, values, valuesAB, valuesold, Ki=None, dt=None,
+                       slope=None) -> None:
+        """tracer_step with the horizontal diffusion of Ki (None: K_hor = 0) and, with the tapered
+        neutral slopes ``slope`` (nod2D, nl-1, 3), the Redi terms (Redi = .true.)."""
         for a in (values, valuesAB, valuesold):
             assert a.flags.c_contiguous and a.dtype == np.float64
         ki = None if Ki is None else np.ascontiguousarray(Ki, dtype=np.float64)
-        rc = lib().or_tracer_step_ex(C.byref(self.s), C.byref(cfg), C.c_double(forcing.dt if dt is None else dt),
-                                     _ptr(forcing.uv), _ptr(forcing.w), _ptr(forcing.w_i), _ptr(forcing.w_e),
-                                     _ptr(forcing.Kv), _ptr(forcing.bc_surface), _ptr(ki), _ptr(values),
-                                     _ptr(valuesAB), _ptr(valuesold), C.byref(self.w))
+        sl = None if slope is None else np.ascontiguousarray(slope, dtype=np.float64)
+        rc = lib().or_tracer_step_redi(C.byref(self.s), C.byref(cfg), C.c_double(forcing.dt if dt is None else dt),
+                                       _ptr(forcing.uv), _ptr(forcing.w), _ptr(forcing.w_i), _ptr(forcing.w_e),
+                                       _ptr(forcing.Kv), _ptr(forcing.bc_surface), _ptr(ki), _ptr(sl),
+                                       _ptr(values), _ptr(valuesAB), _ptr(valuesold), C.byref(self.w))
         if rc != 0:
             raise RuntimeError(f"oracle tracer step failed with status {rc}")
 
-    def diff_part_hor_redi(self, dt, Ki, tr_xy, del_ttf) -> None:
+    def diff_part_hor_redi(self, dt, Ki, tr_xy, del_ttf, slope=None, tr_z=None) -> None:
         ki = np.ascontiguousarray(Ki, dtype=np.float64)
-        lib().or_diff_part_hor_redi(C.byref(self.s), C.c_double(dt), _ptr(ki), _ptr(tr_xy), _ptr(del_ttf))
+        sl = None if slope is None else np.ascontiguousarray(slope, dtype=np.float64)
+        lib().or_diff_part_hor_redi_s(C.byref(self.s), C.c_double(dt), _ptr(ki), _ptr(sl), _ptr(tr_xy),
+                                      _ptr(tr_z), _ptr(del_ttf))
+
+    def diff_ver_part_redi_expl(self, dt, Ki, slope, tr_xy, del_ttf) -> None:
+        """diff_ver_part_redi_expl: del_ttf (nod2D, nl-1) += the vertical projection of the
+        isoneutral flux, from the element gradients tr_xy (elem2D, nl-1, 2)."""
+        ki = np.ascontiguousarray(Ki, dtype=np.float64)
+        sl = np.ascontiguousarray(slope, dtype=np.float64)
+        lib().or_diff_ver_part_redi_expl(C.byref(self.s), C.c_double(dt), _ptr(ki), _ptr(sl), _ptr(tr_xy),
+                                         _ptr(del_ttf))
+
+    def redi_k33(self, Kv, Ki, slope) -> np.ndarray:
+        """Kv + Kd s^2 of the implicit solve with Redi, (nod2D, nl)."""
+        out = np.empty((self.mesh.nod2D, self.mesh.nl))
+        lib().or_redi_k33(C.byref(self.s), _ptr(np.ascontiguousarray(Kv, dtype=np.float64)),
+                          _ptr(np.ascontiguousarray(Ki, dtype=np.float64)),
+                          _ptr(np.ascontiguousarray(slope, dtype=np.float64)), _ptr(out))
+        return out
 
     def diff_ver_part_expl_ale(self, dt, Kv, flux, values, del_ttf) -> None:
         lib().or_diff_ver_part_expl_ale(C.byref(self.s), C.c_double(dt), _ptr(Kv), _ptr(flux), _ptr(values),

@@ -947,7 +947,12 @@ void or_diff_ver_part_impl_ale_w(const or_mesh *m, double dt, const double *Kv, 
 /* ========================================================================== */
 /* diffusion parts of diff_tracers_ale (src/oce_ale_tracer.F90:560-772)        */
 /* ========================================================================== */
-void or_diff_part_hor_redi(const or_mesh *m, double dt, const double *Ki, const double *tr_xy, double *del_ttf) {
+/* The isoneutral (Redi) parts take the tapered neutral slopes slope(3, nl-1, nod2D) and the
+ * vertical gradient tr_z (nl per node, tracer_gradient_z of the values); slope == NULL is
+ * Redi = .false. (isredi = 0): the flux is Kh grad T alone. */
+#define SLP(k, nz, n) (slope[3 * IX1(nz, n) + (k)])
+void or_diff_part_hor_redi_s(const or_mesh *m, double dt, const double *Ki, const double *slope,
+                             const double *tr_xy, const double *tr_z, double *del_ttf) {
     const int NL = m->nl, L1 = NL - 1;
     double rhs1[NL + 1], rhs2[NL + 1];
     for (int edge = 0; edge < m->edge2D; edge++) {
@@ -965,48 +970,66 @@ void or_diff_part_hor_redi(const or_mesh *m, double dt, const double *Ki, const 
             dY2 = m->edge_cross_dxdy[4 * (size_t)edge + 3];
         }
         int nl12 = nl1 < nl2 ? nl1 : nl2, ul12 = ul1 > ul2 ? ul1 : ul2;
-        /* fluxes Kh grad T of one element (segments A/D: el1, B/E: el2, C: mean of both) */
+        /* Kh (grad T + slope x mean T_z at the edge's nodes) of one element (segments A/D: el1,
+         * B/E: el2, C: mean of both), Tz(j) = (tr_z(nz) + tr_z(nz+1)) / 2 at node j */
 #define KH(nz) ((Ki[IX1(nz, n1)] + Ki[IX1(nz, n2)]) / 2.0)
 #define TXY(k, nz, el) (tr_xy[2 * IX1(nz, el) + (k)])
+#define FLUX(nz, Tx, Ty, Fx, Fy)                                                                          \
+    do {                                                                                                  \
+        const double Kh_ = KH(nz);                                                                        \
+        if (slope) {                                                                                      \
+            const double tz1 = 0.5 * (tr_z[IXN(nz, n1)] + tr_z[IXN(nz + 1, n1)]);                         \
+            const double tz2 = 0.5 * (tr_z[IXN(nz, n2)] + tr_z[IXN(nz + 1, n2)]);                         \
+            const double sx = (tz1 * SLP(0, nz, n1) + tz2 * SLP(0, nz, n2)) / 2.0;                        \
+            const double sy = (tz1 * SLP(1, nz, n1) + tz2 * SLP(1, nz, n2)) / 2.0;                        \
+            Fx = Kh_ * ((Tx) + sx);                                                                       \
+            Fy = Kh_ * ((Ty) + sy);                                                                       \
+        } else {                                                                                          \
+            Fx = Kh_ * (Tx);                                                                              \
+            Fy = Kh_ * (Ty);                                                                              \
+        }                                                                                                 \
+    } while (0)
+        double Fx, Fy;
         for (int nz = ul1; nz <= ul12 - 1; nz++) { /* (A) */
-            double Kh = KH(nz), dz = m->helem[IX1(nz, el1)];
-            double Fx = Kh * TXY(0, nz, el1), Fy = Kh * TXY(1, nz, el1);
+            double dz = m->helem[IX1(nz, el1)];
+            FLUX(nz, TXY(0, nz, el1), TXY(1, nz, el1), Fx, Fy);
             double cc = (-dX1 * Fy + dY1 * Fx) * dz;
             rhs1[nz] = rhs1[nz] + cc;
             rhs2[nz] = rhs2[nz] - cc;
         }
         if (ul2 > 0)
             for (int nz = ul2; nz <= ul12 - 1; nz++) { /* (B) */
-                double Kh = KH(nz), dz = m->helem[IX1(nz, el2)];
-                double Fx = Kh * TXY(0, nz, el2), Fy = Kh * TXY(1, nz, el2);
+                double dz = m->helem[IX1(nz, el2)];
+                FLUX(nz, TXY(0, nz, el2), TXY(1, nz, el2), Fx, Fy);
                 double cc = (dX2 * Fy - dY2 * Fx) * dz;
                 rhs1[nz] = rhs1[nz] + cc;
                 rhs2[nz] = rhs2[nz] - cc;
             }
         for (int nz = ul12; nz <= nl12; nz++) { /* (C) */
-            double Kh = KH(nz), dz = (m->helem[IX1(nz, el1)] + m->helem[IX1(nz, el2)]) / 2.0;
+            double dz = (m->helem[IX1(nz, el1)] + m->helem[IX1(nz, el2)]) / 2.0;
             double Tx = 0.5 * (TXY(0, nz, el1) + TXY(0, nz, el2)), Ty = 0.5 * (TXY(1, nz, el1) + TXY(1, nz, el2));
-            double Fx = Kh * Tx, Fy = Kh * Ty;
+            FLUX(nz, Tx, Ty, Fx, Fy);
             double cc = ((dX2 - dX1) * Fy - (dY2 - dY1) * Fx) * dz;
             rhs1[nz] = rhs1[nz] + cc;
             rhs2[nz] = rhs2[nz] - cc;
         }
         for (int nz = nl12 + 1; nz <= nl1; nz++) { /* (D) */
-            double Kh = KH(nz), dz = m->helem[IX1(nz, el1)];
-            double Fx = Kh * TXY(0, nz, el1), Fy = Kh * TXY(1, nz, el1);
+            double dz = m->helem[IX1(nz, el1)];
+            FLUX(nz, TXY(0, nz, el1), TXY(1, nz, el1), Fx, Fy);
             double cc = (-dX1 * Fy + dY1 * Fx) * dz;
             rhs1[nz] = rhs1[nz] + cc;
             rhs2[nz] = rhs2[nz] - cc;
         }
         for (int nz = nl12 + 1; nz <= nl2; nz++) { /* (E) */
-            double Kh = KH(nz), dz = m->helem[IX1(nz, el2)];
-            double Fx = Kh * TXY(0, nz, el2), Fy = Kh * TXY(1, nz, el2);
+            double dz = m->helem[IX1(nz, el2)];
+            FLUX(nz, TXY(0, nz, el2), TXY(1, nz, el2), Fx, Fy);
             double cc = (dX2 * Fy - dY2 * Fx) * dz;
             rhs1[nz] = rhs1[nz] + cc;
             rhs2[nz] = rhs2[nz] - cc;
         }
 #undef KH
 #undef TXY
+#undef FLUX
         nl12 = nl1 > nl2 ? nl1 : nl2;
         ul12 = ul1;
         if (ul2 > 0) ul12 = ul1 < ul2 ? ul1 : ul2;
@@ -1016,6 +1039,86 @@ void or_diff_part_hor_redi(const or_mesh *m, double dt, const double *Ki, const 
         }
     }
 }
+
+void or_diff_part_hor_redi(const or_mesh *m, double dt, const double *Ki, const double *tr_xy, double *del_ttf) {
+    or_diff_part_hor_redi_s(m, dt, Ki, NULL, tr_xy, NULL, del_ttf);
+}
+
+/* diff_ver_part_redi_expl (src/oce_ale_tracer.F90:1439-1518): the horizontal part of the
+ * isoneutral flux projected on the vertical.  Node gradients tr_xynodes = sum over the node's
+ * elements wet at nz of tr_xy elem_area, / 3 / areasvol (:1470-1487); depths zbar_n / z_n of the
+ * column from hnode, bottom up from zbar_n_bot (:1496-1503); interface flux vd(nz) of the two
+ * layers around it weighted by their half thicknesses (:1506-1511); increment
+ * (vd(nz) - vd(nz+1)) dt / areasvol (:1512-1514). */
+void or_diff_ver_part_redi_expl(const or_mesh *m, double dt, const double *Ki, const double *slope,
+                                const double *tr_xy, double *del_ttf) {
+    const int NL = m->nl, L1 = NL - 1;
+    OMP_FOR
+    for (int n = 0; n < m->nod2D; n++) {
+        double gx[NL + 1], gy[NL + 1], vd[NL + 2], zbar_n[NL + 2], z_n[NL + 1];
+        const int nl1 = m->nlevels_nod2D[n] - 1, ul1 = m->ulevels_nod2D[n];
+        for (int nz = ul1; nz <= nl1; nz++) {
+            double tx = 0.0, ty = 0.0;
+            for (int k = m->nod_in_elem2D_ptr[n]; k < m->nod_in_elem2D_ptr[n + 1]; k++) {
+                const int elem = m->nod_in_elem2D[k];
+                if (nz <= m->nlevels[elem] - 1 && nz >= m->ulevels[elem]) {
+                    tx = tx + tr_xy[2 * IX1(nz, elem)] * m->elem_area[elem];
+                    ty = ty + tr_xy[2 * IX1(nz, elem) + 1] * m->elem_area[elem];
+                }
+            }
+            gx[nz] = tx / 3.0 / m->areasvol[IXN(nz, n)];
+            gy[nz] = ty / 3.0 / m->areasvol[IXN(nz, n)];
+        }
+        for (int k = 0; k <= NL + 1; k++) vd[k] = zbar_n[k] = 0.0;
+        for (int k = 0; k <= NL; k++) z_n[k] = 0.0;
+        const double *hn = &m->hnode[IX1(1, n)] - 1;
+        zbar_n[nl1 + 1] = m->zbar_n_bot[n];
+        z_n[nl1] = zbar_n[nl1 + 1] + hn[nl1] / 2.0;
+        for (int nz = nl1; nz >= ul1 + 1; nz--) {
+            zbar_n[nz] = zbar_n[nz + 1] + hn[nz];
+            z_n[nz - 1] = zbar_n[nz] + hn[nz - 1] / 2.0;
+        }
+        for (int nz = ul1 + 1; nz <= nl1; nz++) {
+            double v = (z_n[nz - 1] - zbar_n[nz]) * (SLP(0, nz - 1, n) * gx[nz - 1] + SLP(1, nz - 1, n) * gy[nz - 1]) *
+                       Ki[IX1(nz - 1, n)];
+            v = v + (zbar_n[nz] - z_n[nz]) * (SLP(0, nz, n) * gx[nz] + SLP(1, nz, n) * gy[nz]) * Ki[IX1(nz, n)];
+            vd[nz] = v / (z_n[nz - 1] - z_n[nz]) * m->area[IXN(nz, n)];
+        }
+        for (int nz = ul1; nz <= nl1; nz++)
+            del_ttf[IX1(nz, n)] = del_ttf[IX1(nz, n)] + (vd[nz] - vd[nz + 1]) * dt / m->areasvol[IXN(nz, n)];
+    }
+}
+
+/* K_33 = Kv + Kd s^2 of diff_ver_part_impl_ale with Redi (src/oce_ale_tracer.F90:1099-1204): at
+ * interface nz of a column (nzmin < nz < nzmax), with zbar_n / Z_n from hnode_new bottom up,
+ * Ty = (zbar_n(nz) - Z_n(nz)) / dZ s3(nz-1)^2 Ki(nz-1) + (Z_n(nz-1) - zbar_n(nz)) / dZ s3(nz)^2
+ * Ki(nz), 1/dZ = 1 / (Z_n(nz-1) - Z_n(nz)) (Ty of the layer below = Ty1 of the layer above);
+ * other interfaces keep Kv.  The implicit solve with K33 in place of Kv is the reference's. */
+void or_redi_k33(const or_mesh *m, const double *Kv, const double *Ki, const double *slope, double *K33) {
+    const int NL = m->nl, L1 = NL - 1;
+    OMP_FOR
+    for (int n = 0; n < m->nod2D; n++) {
+        double zbar_n[NL + 1], Z_n[NL + 1];
+        for (int k = 0; k <= NL; k++) zbar_n[k] = Z_n[k] = 0.0;
+        for (int nz = 1; nz <= NL; nz++) K33[IXN(nz, n)] = Kv[IXN(nz, n)];
+        const double *hn = &m->hnode_new[IX1(1, n)] - 1;
+        const int nzmax = m->nlevels_nod2D[n], nzmin = m->ulevels_nod2D[n];
+        zbar_n[nzmax] = m->zbar_n_bot[n];
+        Z_n[nzmax - 1] = zbar_n[nzmax] + hn[nzmax - 1] / 2.0;
+        for (int nz = nzmax - 1; nz >= nzmin + 1; nz--) {
+            zbar_n[nz] = zbar_n[nz + 1] + hn[nz];
+            Z_n[nz - 1] = zbar_n[nz] + hn[nz - 1] / 2.0;
+        }
+        for (int nz = nzmin + 1; nz <= nzmax - 1; nz++) {
+            const double zinv = 1.0 / (Z_n[nz - 1] - Z_n[nz]);
+            const double sa = SLP(2, nz - 1, n), sb = SLP(2, nz, n);
+            const double Ty = (zbar_n[nz] - Z_n[nz]) * zinv * (sa * sa) * Ki[IX1(nz - 1, n)] +
+                              (Z_n[nz - 1] - zbar_n[nz]) * zinv * (sb * sb) * Ki[IX1(nz, n)];
+            K33[IXN(nz, n)] = Kv[IXN(nz, n)] + Ty;
+        }
+    }
+}
+#undef SLP
 
 void or_diff_ver_part_expl_ale(const or_mesh *m, double dt, const double *Kv, const double *flux_surf,
                                const double *values, double *del_ttf) {
@@ -1049,6 +1152,13 @@ int or_tracer_step(const or_mesh *m, const or_tra_cfg *c, double dt, const doubl
 int or_tracer_step_ex(const or_mesh *m, const or_tra_cfg *c, double dt, const double *vel, const double *W,
                       const double *WI, const double *WE, const double *Kv, const double *bc_surf, const double *Ki,
                       double *values, double *valuesAB, double *valuesold, or_work *w) {
+    return or_tracer_step_redi(m, c, dt, vel, W, WI, WE, Kv, bc_surf, Ki, NULL, values, valuesAB, valuesold, w);
+}
+
+int or_tracer_step_redi(const or_mesh *m, const or_tra_cfg *c, double dt, const double *vel, const double *W,
+                        const double *WI, const double *WE, const double *Kv, const double *bc_surf, const double *Ki,
+                        const double *slope, double *values, double *valuesAB, double *valuesold, or_work *w) {
+    if (slope && !Ki) return 3;
     const int L1 = m->nl - 1;
     if (c->ab_order != 2 && c->ab_order != 3) return 2;
     or_init_tracers_AB(m, c, values, valuesAB, valuesold, w);
@@ -1058,8 +1168,10 @@ int or_tracer_step_ex(const or_mesh *m, const or_tra_cfg *c, double dt, const do
     OMP_FOR
     for (long i = 0; i < (long)N; i++) w->del_ttf[i] = w->del_ttf[i] + w->del_ttf_advhoriz[i] + w->del_ttf_advvert[i];
     /* diff_tracers_ale (:595-607): horizontal diffusion, then the explicit vertical one */
-    if (Ki) or_diff_part_hor_redi(m, dt, Ki, w->tr_xy, w->del_ttf);
+    if (Ki) or_diff_part_hor_redi_s(m, dt, Ki, slope, w->tr_xy, w->tr_z, w->del_ttf);
     if (!c->i_vert_diff) or_diff_ver_part_expl_ale(m, dt, Kv, bc_surf, values, w->del_ttf);
+    /* :623 */
+    if (slope) or_diff_ver_part_redi_expl(m, dt, Ki, slope, w->tr_xy, w->del_ttf);
     OMP_FOR
     for (int n = 0; n < m->nod2D; n++) {
         int nzmax = m->nlevels_nod2D[n] - 1, nzmin = m->ulevels_nod2D[n];
@@ -1070,7 +1182,16 @@ int or_tracer_step_ex(const or_mesh *m, const or_tra_cfg *c, double dt, const do
         }
     }
     /* the w_i part goes into the implicit solve only without the limiter (:961) */
-    if (c->i_vert_diff) or_diff_ver_part_impl_ale_w(m, dt, Kv, bc_surf, WI, c->wsplit && !c->lim_fct, values);
+    if (c->i_vert_diff) {
+        double *K33 = NULL;
+        if (slope) {
+            K33 = (double *)malloc(sizeof(double) * (size_t)m->nl * (size_t)m->nod2D);
+            if (!K33) return 4;
+            or_redi_k33(m, Kv, Ki, slope, K33);
+        }
+        or_diff_ver_part_impl_ale_w(m, dt, K33 ? K33 : Kv, bc_surf, WI, c->wsplit && !c->lim_fct, values);
+        free(K33);
+    }
     return 0;
 }
 

@@ -125,6 +125,16 @@ void or_diff_ver_part_impl_ale_w(const or_mesh *m, double dt, const double *Kv, 
 /* diff_part_hor_redi (src/oce_ale_tracer.F90:1526-1689) with Redi off: edge fluxes of
  * Ki-weighted element gradients tr_xy, scattered into del_ttf in ascending edge order. */
 void or_diff_part_hor_redi(const or_mesh *m, double dt, const double *Ki, const double *tr_xy, double *del_ttf);
+/* Redi = .true.: the isoneutral parts with the tapered neutral slopes slope(3, nl-1, nod2D)
+ * (slope_tapered) as input.  diff_part_hor_redi with the slope terms (tr_z: nl per node,
+ * tracer_gradient_z of the values); diff_ver_part_redi_expl (src/oce_ale_tracer.F90:1439-1518);
+ * K33 (nl per node) = Kv + Kd s^2 of diff_ver_part_impl_ale's Redi terms (:1099-1204), the
+ * diffusivity of the implicit solve. */
+void or_diff_part_hor_redi_s(const or_mesh *m, double dt, const double *Ki, const double *slope,
+                             const double *tr_xy, const double *tr_z, double *del_ttf);
+void or_diff_ver_part_redi_expl(const or_mesh *m, double dt, const double *Ki, const double *slope,
+                                const double *tr_xy, double *del_ttf);
+void or_redi_k33(const or_mesh *m, const double *Kv, const double *Ki, const double *slope, double *K33);
 /* diff_ver_part_expl_ale (src/oce_ale_tracer.F90:841-902): explicit vertical diffusion of
  * values into del_ttf; flux_surf(n) is the surface flux vd_flux(ulevels) (NULL: zero). */
 void or_diff_ver_part_expl_ale(const or_mesh *m, double dt, const double *Kv, const double *flux_surf,
@@ -136,6 +146,12 @@ void or_diff_ver_part_expl_ale(const or_mesh *m, double dt, const double *Kv, co
 int or_tracer_step_ex(const or_mesh *m, const or_tra_cfg *c, double dt, const double *vel, const double *W,
                       const double *WI, const double *WE, const double *Kv, const double *bc_surf, const double *Ki,
                       double *values, double *valuesAB, double *valuesold, or_work *w);
+/* The same with Redi = .true. when slope != NULL (Ki required; returns 3 without it): the slope
+ * terms of the horizontal diffusion, diff_ver_part_redi_expl after the explicit vertical part
+ * (:623), K33 in the implicit solve. */
+int or_tracer_step_redi(const or_mesh *m, const or_tra_cfg *c, double dt, const double *vel, const double *W,
+                        const double *WI, const double *WE, const double *Kv, const double *bc_surf, const double *Ki,
+                        const double *slope, double *values, double *valuesAB, double *valuesold, or_work *w);
 
 /* The per-tracer body of solve_tracers_ale (src/oce_ale_tracer.F90:303-351):
  * init_tracers_AB, do_oce_adv_tra, del_ttf sum, diff_tracers_ale (T* update,

@@ -82,9 +82,10 @@ class Ref:
         v2 = (vel[self.e2, :, 1] * ecd[:, 2:3] - vel[self.e2, :, 0] * ecd[:, 3:4]) * h2
         return {1: v1, 2: v2, 3: v1 + v2}[which]
 
-    # ---- oce_ale_tracer.F90:1526-1689 (diff_part_hor_redi, Redi off) --------
-    def diff_part_hor_redi(self, dt, Ki, trxy, del_ttf):
-        """Edge fluxes Kh grad T of the segments A..E, scattered in ascending edge order."""
+    # ---- oce_ale_tracer.F90:1526-1689 (diff_part_hor_redi) ---------------------
+    def diff_part_hor_redi(self, dt, Ki, trxy, del_ttf, slope=None, trz=None):
+        """Edge fluxes Kh (grad T [+ S T_z with Redi]) of the segments A..E, scattered in
+        ascending edge order; slope (nod2D, nl-1, 3), trz (nod2D, nl) for Redi = .true."""
         m = self.m
         Kh = (Ki[self.n1] + Ki[self.n2]) / 2.0
         ecd = m.edge_cross_dxdy
@@ -93,11 +94,24 @@ class Ref:
         dY2 = np.where(self.has2[:, None], ecd[:, 3:4], 0.0)
         h1, h2 = m.helem[self.el1], m.helem[self.e2]
         t1, t2 = trxy[self.el1], trxy[self.e2]
-        c1 = (-dX1 * (Kh * t1[:, :, 1]) + dY1 * (Kh * t1[:, :, 0])) * h1
-        c2 = (dX2 * (Kh * t2[:, :, 1]) - dY2 * (Kh * t2[:, :, 0])) * h2
+        if slope is None:
+            F = lambda Tx, Ty: (Kh * Tx, Kh * Ty)
+        else:
+            L1 = self.L1
+            # vertical gradient at mid-layer of both edge nodes (:1586-1588)
+            Tz1 = 0.5 * (trz[self.n1][:, :L1] + trz[self.n1][:, 1:L1 + 1])
+            Tz2 = 0.5 * (trz[self.n2][:, :L1] + trz[self.n2][:, 1:L1 + 1])
+            sx = (Tz1 * slope[self.n1][:, :, 0] + Tz2 * slope[self.n2][:, :, 0]) / 2.0
+            sy = (Tz1 * slope[self.n1][:, :, 1] + Tz2 * slope[self.n2][:, :, 1]) / 2.0
+            F = lambda Tx, Ty: (Kh * (Tx + sx), Kh * (Ty + sy))
+        Fx1, Fy1 = F(t1[:, :, 0], t1[:, :, 1])
+        Fx2, Fy2 = F(t2[:, :, 0], t2[:, :, 1])
+        c1 = (-dX1 * Fy1 + dY1 * Fx1) * h1
+        c2 = (dX2 * Fy2 - dY2 * Fx2) * h2
         Tx = 0.5 * (t1[:, :, 0] + t2[:, :, 0])
         Ty = 0.5 * (t1[:, :, 1] + t2[:, :, 1])
-        c3 = ((dX2 - dX1) * (Kh * Ty) - (dY2 - dY1) * (Kh * Tx)) * ((h1 + h2) / 2.0)
+        Fx3, Fy3 = F(Tx, Ty)
+        c3 = ((dX2 - dX1) * Fy3 - (dY2 - dY1) * Fx3) * ((h1 + h2) / 2.0)
         c = np.zeros_like(Kh)
         for mask, typ in self.segs:
             c = np.where(mask, {1: c1, 2: c2, 3: c3}[typ], c)
@@ -486,6 +500,75 @@ class Ref:
         else:
             Tn = self.vdiff(dt, forcing.Kv, forcing.bc_surface, Tn)
         return Tn, Told_new
+
+
+# ---------------------------------------------------------------------------
+# Redi = .true. (isoneutral diffusion with the tapered neutral slopes as input)
+# ---------------------------------------------------------------------------
+def tr_z(m, T):
+    """tracer_gradient_z (oce_tracer_mod.F90:192-232) as (nod2D, nl); 0 outside the columns."""
+    N2, nl = m.nod2D, m.nl
+    out = np.zeros((N2, nl))
+    lev = np.arange(1, nl + 1)[None, :]
+    dz = 0.5 * (m.hnode[:, :-1] + m.hnode[:, 1:])            # interfaces 2 .. nl-1
+    g = (T[:, :-1] - T[:, 1:]) / np.where(dz != 0.0, dz, 1.0)
+    inner = (lev[:, 1:nl - 1] >= m.ulevels_nod2D[:, None] + 1) & (lev[:, 1:nl - 1] <= m.nlevels_nod2D[:, None] - 1)
+    out[:, 1:nl - 1] = np.where(inner, g, 0.0)
+    return out
+
+
+def _depths_bottom_up(m, h, n, top, bottom_interface):
+    """zbar(k), z(k) of column n from the layer thicknesses h, accumulated upward from zbar_n_bot
+    (zbar at bottom_interface; z of the layer above it at its half thickness)."""
+    zbar = {bottom_interface: m.zbar_n_bot[n]}
+    z = {bottom_interface - 1: zbar[bottom_interface] + h[n, bottom_interface - 2] / 2.0}
+    for k in range(bottom_interface - 1, top, -1):
+        zbar[k] = zbar[k + 1] + h[n, k - 1]
+        z[k - 1] = zbar[k] + h[n, k - 2] / 2.0
+    return zbar, z
+
+
+def redi_vexpl(m, dt, Ki, slope, trxy, del_ttf):
+    """diff_ver_part_redi_expl (oce_ale_tracer.F90:1439-1518), column by column."""
+    out = del_ttf.copy()
+    for n in range(m.nod2D):
+        nl1, ul1 = int(m.nlevels_nod2D[n]) - 1, int(m.ulevels_nod2D[n])
+        els = m.nod_in_elem2D[m.nod_in_elem2D_ptr[n]:m.nod_in_elem2D_ptr[n + 1]]
+        gxy = {}
+        for nz in range(ul1, nl1 + 1):
+            tx = ty = 0.0
+            for el in els:
+                if m.ulevels[el] <= nz <= m.nlevels[el] - 1:
+                    tx = tx + trxy[el, nz - 1, 0] * m.elem_area[el]
+                    ty = ty + trxy[el, nz - 1, 1] * m.elem_area[el]
+            av = m.areasvol[n, nz - 1]
+            gxy[nz] = (tx / 3.0 / av, ty / 3.0 / av)
+        zbar, z = _depths_bottom_up(m, m.hnode, n, ul1, nl1 + 1)
+        proj = lambda k: slope[n, k - 1, 0] * gxy[k][0] + slope[n, k - 1, 1] * gxy[k][1]
+        vd = {k: 0.0 for k in range(ul1, nl1 + 2)}
+        for nz in range(ul1 + 1, nl1 + 1):
+            v = (z[nz - 1] - zbar[nz]) * proj(nz - 1) * Ki[n, nz - 2]
+            v = v + (zbar[nz] - z[nz]) * proj(nz) * Ki[n, nz - 1]
+            vd[nz] = v / (z[nz - 1] - z[nz]) * m.area[n, nz - 1]
+        for nz in range(ul1, nl1 + 1):
+            out[n, nz - 1] = out[n, nz - 1] + (vd[nz] - vd[nz + 1]) * dt / m.areasvol[n, nz - 1]
+    return out
+
+
+def redi_k33(m, Kv, Ki, slope):
+    """Kv + Ty of diff_ver_part_impl_ale with Redi (oce_ale_tracer.F90:1099-1204) per interface,
+    (nod2D, nl): the diffusivity K_33 = Kv + Kd s^2 that the implicit solve uses."""
+    K = Kv.copy()
+    for n in range(m.nod2D):
+        nzmax, nzmin = int(m.nlevels_nod2D[n]), int(m.ulevels_nod2D[n])
+        zbar, Z = _depths_bottom_up(m, m.hnode_new, n, nzmin, nzmax)
+        for nz in range(nzmin + 1, nzmax):
+            zinv = 1.0 / (Z[nz - 1] - Z[nz])
+            sa, sb = slope[n, nz - 2, 2], slope[n, nz - 1, 2]
+            Ty = (zbar[nz] - Z[nz]) * zinv * (sa * sa) * Ki[n, nz - 2] + \
+                (Z[nz - 1] - zbar[nz]) * zinv * (sb * sb) * Ki[n, nz - 1]
+            K[n, nz - 1] = Kv[n, nz - 1] + Ty
+    return K
 
 
 # ---------------------------------------------------------------------------
