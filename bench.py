@@ -56,7 +56,10 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--profile-only", action="store_true", help="one warm step + one profiled step (for ncu)")
-    p.add_argument("--no-tune", action="store_true", help="configuration 5: keep the generators' node order")
+    p.add_argument("--no-tune", action="store_true",
+                   help="no autotuning: the library's launch settings and the generators' node order")
+    p.add_argument("--order", default="auto", choices=["auto", "morton", "rcm"],
+                   help="node order of the single-mesh workload (auto: the faster step of the two, timed)")
     p.add_argument("--no-config5", action="store_true", help="skip the configuration-5 sub-run of the default line")
     p.add_argument("--width", type=int, default=0, help="FP32 tracer-group width (0: automatic, 2, 4)")
     p.add_argument("--stage-tr", default="", help="tracers per launch of lo_ad,ho,bounds,update (e.g. 8,0,8,8)")
@@ -305,6 +308,52 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def order_trial(mesh, forcing, tracers, dt, args, steps=2):
+    """ms per FP32 step of the workload on this node order (default launch settings)."""
+    import torch
+    from fesom2_gb300 import gpu as G
+    ntr = tracers.shape[0]
+    cfgs = [G.tra_cfg("MUSCL", "QR4C", "FCT", 0.0, 1.0, id=(k + 1 if k < 2 else 100 + k)) for k in range(ntr)]
+    f32 = M.Forcing(uv=forcing.uv.astype(np.float32), w=forcing.w.astype(np.float32),
+                    w_e=forcing.w_e.astype(np.float32), w_i=forcing.w_i.astype(np.float32),
+                    Kv=forcing.Kv.astype(np.float32), bc_surface=None, dt=dt)
+    stream = torch.cuda.Stream()
+    ctx = G.Context(mesh, G.PREC_FP32, max_tracers=ntr)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_tracer_width(args.width)
+    ctx.state_setup(cfgs)
+    apply_settings(ctx, args)
+    ctx.forcing_upload(f32)
+    for k in range(ntr):
+        ctx.tracer_upload(k, tracers[k], tracers[k])
+    ctx.run_steps(dt, 1, use_graph=False)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ctx.run_steps(dt, steps, use_graph=False)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    ctx.close()
+    return ms
+
+
+def choose_order(args, mesh, forcing, tracers, dt, rank):
+    """Node order of the workload: the generators' Morton order or reverse Cuthill-McKee of the
+    node graph, the faster FP32 step when timed (--order auto, the benchmark mesh at full size)."""
+    if args.order == "morton" or (args.order == "auto" and (args.no_tune or args.scale != 1.0 or args.profile_only)):
+        return {"chosen": "morton", "timed": False}
+    from fesom2_gb300 import batch as Bt
+    order = Bt.rcm_order(mesh)
+    if args.order == "rcm":
+        return {"chosen": "rcm", "timed": False, "_order": order}
+    ms = {"morton": order_trial(mesh, forcing, tracers, dt, args)}
+    pm = Bt.permute_nodes(mesh, order)
+    ms["rcm"] = order_trial(pm, Bt.permute_forcing(forcing, order), np.ascontiguousarray(tracers[:, order]), dt, args)
+    del pm
+    best = min(ms, key=ms.get)
+    return {"chosen": best, "timed": True, "ms_per_step": ms, "_order": order}
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     from fesom2_gb300 import gpu as G
@@ -326,6 +375,14 @@ def run_ours(args, rank, world, local_rank):
 
     mesh, kind, forcing, tracers, dt, wname, gen_s = workload(args.config, args.scale, args.tracers)
     ntr = tracers.shape[0]
+    node_order = choose_order(args, mesh, forcing, tracers, dt, rank)
+    if node_order["chosen"] == "rcm":
+        from fesom2_gb300 import batch as Bt
+        order = node_order.pop("_order")
+        mesh = Bt.permute_nodes(mesh, order)
+        forcing = Bt.permute_forcing(forcing, order)
+        tracers = np.ascontiguousarray(tracers[:, order])
+    node_order.pop("_order", None)
     counts = mesh.counts()
     N3 = counts["N3"]
     cfgs = [G.tra_cfg("MUSCL", "QR4C", "FCT", 0.0, 1.0, id=(k + 1 if k < 2 else 100 + k)) for k in range(ntr)]
@@ -361,6 +418,10 @@ def run_ours(args, rank, world, local_rank):
             first_step[k] = ctx.tracer_download(k, dtype=np.float32)[0]
         upload_initial(ctx)
         torch.cuda.synchronize()
+    # launch settings by timing (the state is left as it was), unless given on the command line
+    tuning = None
+    if not args.no_tune and not args.profile_only and not (args.stage_tr or args.shape or args.variant):
+        tuning = ctx.autotune(dt, steps=2)
     if args.profile_only:
         ctx.run_steps(dt, 1, use_graph=True)
         torch.cuda.synchronize()
@@ -637,7 +698,8 @@ def run_ours(args, rank, world, local_rank):
                 "config": {"workload": wname, "cfg": args.config, "tracers": ntr, "N3_per_tracer": N3,
                            "E3": counts["E3"], "T3": counts["T3"], "nodes": counts["N2"], "levels": mesh.nl,
                            "dt_s": dt, "l2": "inputs larger than L2 (no flush)", "tracer_groups": ngr,
-                           "group_width": width,
+                           "group_width": width, "node_order": node_order,
+                           "launch_settings": tuning if tuning is not None else "defaults or command line",
                            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                            "mesh_generation_s": gen_s},
                 "gpu_launches": launches * args.steps,

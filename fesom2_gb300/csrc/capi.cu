@@ -95,6 +95,11 @@ struct fesom_gpu_ctx {
     std::vector<cudaEvent_t> ev_in, ev_done;
     // tail of the tracer loop: node y coordinates (relax_zonal_temp) and work arrays
     void *Ki = nullptr;        // horizontal diffusivity (context precision), null: none
+    // Redi (fesom_gpu_set_redi): tapered neutral slopes (3 per node-layer) and the K33 of the
+    // implicit solve (nl per node), context precision; active while Ki is set too
+    void *slope = nullptr, *K33 = nullptr;
+    double *redi_tmp = nullptr;   // FP64 scratch of the routine-level Redi entry points
+    size_t redi_tmp_n = 0;
     double *coord_y = nullptr;
     double *tail_v = nullptr, *tail_r2c = nullptr, *tail_T = nullptr, *tail_S = nullptr, *tail_z = nullptr;
     int tail_nbins = 0;
@@ -768,6 +773,8 @@ struct StageTimer {
     int n = 0;
 };
 
+bool redi_on(const fesom_gpu_ctx *ctx) { return ctx->slope && ctx->Ki; }
+
 template <typename R>
 int enqueue_step(fesom_gpu_ctx *ctx, double dt, StageTimer *tm = nullptr) {
     const DGeom<R> &g = geom<R>(ctx);
@@ -782,10 +789,21 @@ int enqueue_step(fesom_gpu_ctx *ctx, double dt, StageTimer *tm = nullptr) {
             call;                                                                        \
         }                                                                                \
     } while (0)
+    const bool redi = redi_on(ctx);
+    if (redi) {
+        bool vd = false;
+        for (int t = 0; t < ctx->ntr; t++) vd |= ctx->cfgs[t].i_vert_diff != 0;
+        if (vd)
+            STAGE(7, Launch<R>::k33(ctx->tp, g, (const R *)ctx->Kv, (const R *)ctx->Ki, (const R *)ctx->slope,
+                                    (R *)ctx->K33, ctx->stream));
+    }
     for (int t0 = 0; t0 < ctx->ntr; t0 += ctx->group) {
         const int nt = std::min(ctx->group, ctx->ntr - t0);
         DTracers<R> tr = group_view<R>(ctx, t0, nt);
         DForcing<R> f = forcing_view<R>(ctx, t0);
+        // Redi: the slopes; the increments of diff_ver_part_redi_expl in TAB (dead after the LO stage)
+        tr.slope = redi ? (const R *)ctx->slope : nullptr;
+        tr.RV = redi ? (R *)ctx->TAB : nullptr;
         bool any_fct = false, any_ho = false, any_vd = false, any_ex = false;
         int ab = 2;
         for (int t = t0; t < t0 + nt; t++) {
@@ -806,12 +824,18 @@ int enqueue_step(fesom_gpu_ctx *ctx, double dt, StageTimer *tm = nullptr) {
         // the values before the update)
         if (ctx->Ki) STAGE(2, Launch<R>::hdiff(ctx->tp, g, tr, ctx->stream));
         if (any_ex) STAGE(7, Launch<R>::vexpl(ctx->tp, g, f, tr, dt, tr.VX, 0, 0, ctx->stream));
+        if (redi) STAGE(7, Launch<R>::redi_v(ctx->tp, g, tr, dt, 0, ctx->stream));
         if (any_fct) {
             STAGE(4, Launch<R>::bounds(ctx->tp, g, tr, ctx->stream));
             STAGE(5, Launch<R>::rpm(ctx->tp, g, tr, dt, ctx->stream));
         }
         STAGE(6, Launch<R>::update(ctx->tp, g, tr, dt, any_fct, 1, ctx->stream));
-        if (any_vd) STAGE(7, Launch<R>::vdiff(ctx->tp, g, f, tr, dt, ctx->scratch, ctx->stream));
+        if (any_vd) {
+            // Redi: the implicit solve diffuses with K33 = Kv + Kd s^2
+            DForcing<R> fv = f;
+            if (redi) fv.Kv = (const R *)ctx->K33;
+            STAGE(7, Launch<R>::vdiff(ctx->tp, g, fv, tr, dt, ctx->scratch, ctx->stream));
+        }
     }
     CK(cudaGetLastError());
     return FESOM_OK;
@@ -825,6 +849,12 @@ int enqueue_shared32(fesom_gpu_ctx *ctx, double dt, StageTimer *tm, bool &fork) 
     bool any_vd = false;
     for (int t = 0; t < ctx->ntr; t++) any_vd |= ctx->cfgs[t].i_vert_diff != 0;
     STAGE(8, b32_vflux(ctx->tp, g, f, ctx->VF, ctx->stream));
+    if (redi_on(ctx) && any_vd) {
+        // Redi: the factors of the implicit solve use K33 = Kv + Kd s^2
+        STAGE(9, b32_k33(ctx->tp, g, (const float *)ctx->Kv, (const float *)ctx->Ki, (const float *)ctx->slope,
+                         (float *)ctx->K33, ctx->stream));
+        f.Kv = (const float *)ctx->K33;
+    }
     fork = any_vd && !tm;
     if (fork) {
         CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
@@ -844,6 +874,10 @@ int enqueue_group32(fesom_gpu_ctx *ctx, double dt, int g0, int ng, StageTimer *t
     B32View B = view32(ctx, g0, ng);
     DForcing<float> fg = forcing_view<float>(ctx, 0);
     const bool any_fct = B.fct != 0;
+    if (redi_on(ctx)) B.slope = (const float *)ctx->slope;
+    // the implicit solve with the w_i terms diffuses with K33 under Redi
+    DForcing<float> fk = fg;
+    if (redi_on(ctx)) fk.Kv = (const float *)ctx->K33;
     {
         const int sg = stage_group(ctx, 0, ng);
         for (int s0 = 0; s0 < ng; s0 += sg)
@@ -880,7 +914,7 @@ int enqueue_group32(fesom_gpu_ctx *ctx, double dt, int g0, int ng, StageTimer *t
         }
         STAGE(7, b32_vdiff(ctx->tp, fg, B, ctx->vfac, ctx->stream));
     }
-    if (B.wimpl) STAGE(7, b32_vdiff_w(ctx->tp, g, fg, B, dt, ctx->scratch, ctx->stream));
+    if (B.wimpl) STAGE(7, b32_vdiff_w(ctx->tp, g, fk, B, dt, ctx->scratch, ctx->stream));
     return FESOM_OK;
 }
 
@@ -902,7 +936,7 @@ int launches_per_step(fesom_gpu_ctx *ctx) {
     if (ctx->prec == FESOM_PREC_FP32) {
         bool any_vd = false;
         for (int t = 0; t < ctx->ntr; t++) any_vd |= ctx->cfgs[t].i_vert_diff != 0;
-        n = 1 + (any_vd ? 1 : 0);
+        n = 1 + (any_vd ? 1 : 0) + ((any_vd && redi_on(ctx)) ? 1 : 0);
         for (int g0 = 0; g0 < ctx->ngr; g0 += ctx->group) {
             const int ng = std::min(ctx->group, ctx->ngr - g0);
             const B32View B = view32(ctx, g0, ng);
@@ -916,6 +950,11 @@ int launches_per_step(fesom_gpu_ctx *ctx) {
         }
         return n;
     }
+    if (redi_on(ctx)) {
+        bool vd = false;
+        for (int t = 0; t < ctx->ntr; t++) vd |= ctx->cfgs[t].i_vert_diff != 0;
+        n += vd ? 1 : 0;
+    }
     for (int t0 = 0; t0 < ctx->ntr; t0 += ctx->group) {
         const int nt = std::min(ctx->group, ctx->ntr - t0);
         bool any_fct = false, any_ho = false, any_vd = false;
@@ -927,7 +966,7 @@ int launches_per_step(fesom_gpu_ctx *ctx) {
         bool any_ex = false;
         for (int t = t0; t < t0 + nt; t++) any_ex |= ctx->cfgs[t].i_vert_diff == 0;
         n += 4 + ((any_ho || ctx->Ki) ? 1 : 0) + (any_fct ? 2 : 0) + (any_vd ? 1 : 0) + (ctx->Ki ? 1 : 0) +
-             (any_ex ? 1 : 0) + ((ctx->wsplit && any_fct) ? 1 : 0);
+             (any_ex ? 1 : 0) + ((ctx->wsplit && any_fct) ? 1 : 0) + (redi_on(ctx) ? 1 : 0);
     }
     return n;
 }
@@ -1667,6 +1706,129 @@ int fesom_gpu_set_stage_tracers(fesom_gpu_ctx *ctx, int32_t stage, int32_t trace
     return FESOM_OK;
 }
 
+// ---- autotuning of the FP32 form's launch settings (results do not change) -----------------
+namespace {
+struct TuneSetting {
+    int stage_tr[4];
+    LaunchShape shape[4];
+    bool operator==(const TuneSetting &o) const {
+        for (int k = 0; k < 4; k++)
+            if (stage_tr[k] != o.stage_tr[k] || shape[k].blocks_per_sm != o.shape[k].blocks_per_sm ||
+                shape[k].staged != o.shape[k].staged)
+                return false;
+        return true;
+    }
+};
+
+TuneSetting get_setting(const fesom_gpu_ctx *ctx) {
+    TuneSetting t;
+    for (int k = 0; k < 4; k++) {
+        t.stage_tr[k] = ctx->stage_tr[k];
+        t.shape[k] = ctx->shape[k];
+    }
+    return t;
+}
+
+void put_setting(fesom_gpu_ctx *ctx, const TuneSetting &t) {
+    for (int k = 0; k < 4; k++) {
+        ctx->stage_tr[k] = t.stage_tr[k];
+        ctx->shape[k] = t.shape[k];
+    }
+    free_graphs32(ctx);
+}
+
+// one untimed step (cold caches, first launches), then `steps` steps between two events on the
+// context's stream, launched directly (no graph: a candidate would otherwise pay the captures)
+int time_setting(fesom_gpu_ctx *ctx, double dt, int steps, cudaEvent_t e0, cudaEvent_t e1, float *ms) {
+    int rc;
+    if ((rc = fesom_gpu_run_steps(ctx, dt, 1, 0))) return rc;
+    CK(cudaEventRecord(e0, ctx->stream));
+    if ((rc = fesom_gpu_run_steps(ctx, dt, steps, 0))) return rc;
+    CK(cudaEventRecord(e1, ctx->stream));
+    CK(cudaEventSynchronize(e1));
+    CK(cudaEventElapsedTime(ms, e0, e1));
+    *ms /= (float)steps;
+    return FESOM_OK;
+}
+}  // namespace
+
+int fesom_gpu_autotune(fesom_gpu_ctx *ctx, double dt, int32_t steps, fesom_tune_result *res) {
+    if (!ctx || steps < 1 || !res) return FESOM_ERR_ARG;
+    if (ctx->prec != FESOM_PREC_FP32) { ctx->err = "the autotuner tunes the FP32 form"; return FESOM_ERR_STATE; }
+    if (!ctx->state_ready || !ctx->forcing_ready) {
+        ctx->err = "state and forcing must be set up before tuning";
+        return FESOM_ERR_STATE;
+    }
+    int rc;
+    // the time levels and their rotation are put back afterwards: tuning leaves the state as it was
+    const int nlev = ctx->ab_max;
+    const size_t lev = 4 * (size_t)ctx->L1 * ctx->N2 * ctx->gw * (size_t)ctx->ngr;
+    void *backup = nullptr;
+    if ((rc = dalloc(ctx, &backup, lev * nlev))) return rc;
+    for (int k = 0; k < nlev; k++)
+        CK(cudaMemcpyAsync((char *)backup + lev * k, ctx->Bf[k], lev, cudaMemcpyDeviceToDevice, ctx->stream));
+    const int rot0 = ctx->rot;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const TuneSetting start = get_setting(ctx);
+    TuneSetting def{};
+    def.shape[0].staged = true;  // the library defaults: lo_ad staged, the rest in registers
+    int ncand = 0;
+    float def_ms = 0.f, best_ms = 0.f;
+    put_setting(ctx, def);
+    rc = time_setting(ctx, dt, steps, e0, e1, &def_ms);
+    TuneSetting best = def;
+    best_ms = def_ms;
+    ncand = 1;
+    if (!rc && !(start == def)) {
+        float ms = 0.f;
+        put_setting(ctx, start);
+        if (!(rc = time_setting(ctx, dt, steps, e0, e1, &ms)) && ms < best_ms) { best = start; best_ms = ms; }
+        ncand++;
+    }
+    // coordinate descent over the stages: kernel variant, blocks per SM, tracers per launch; a
+    // candidate replaces the best when it is faster by more than 1 % (timing noise)
+    const int ntr_slots = ctx->ngr * ctx->gw;
+    const int bps[] = {0, 2, 4};
+    for (int k = 0; k < 4 && !rc; k++) {
+        const int nvar = (k == 1) ? 1 : 2;
+        const int ntrs = (k >= 2 && ntr_slots > 8) ? 2 : 1;
+        for (int v = 0; v < nvar && !rc; v++)
+            for (int b : bps)
+                for (int q = 0; q < ntrs && !rc; q++) {
+                    TuneSetting c = best;
+                    c.shape[k].staged = (k == 1) ? false : v == 1;
+                    c.shape[k].blocks_per_sm = b;
+                    c.stage_tr[k] = q ? 8 : 0;
+                    if (c == best) continue;
+                    float ms = 0.f;
+                    put_setting(ctx, c);
+                    if ((rc = time_setting(ctx, dt, steps, e0, e1, &ms))) break;
+                    ncand++;
+                    if (ms < 0.99f * best_ms) { best = c; best_ms = ms; }
+                }
+    }
+    put_setting(ctx, rc ? start : best);
+    for (int k = 0; k < nlev; k++)
+        cudaMemcpyAsync(ctx->Bf[k], (char *)backup + lev * k, lev, cudaMemcpyDeviceToDevice, ctx->stream);
+    ctx->rot = rot0;
+    cudaStreamSynchronize(ctx->stream);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    dfree(ctx, backup);
+    if (rc) return rc;
+    res->default_ms = def_ms;
+    res->tuned_ms = best_ms;
+    res->candidates = ncand;
+    for (int k = 0; k < 4; k++) {
+        res->stage_tracers[k] = best.stage_tr[k];
+        res->blocks_per_sm[k] = best.shape[k].blocks_per_sm;
+        res->variant[k] = best.shape[k].staged ? 1 : 0;
+    }
+    return FESOM_OK;
+}
+
 int fesom_gpu_set_wsplit(fesom_gpu_ctx *ctx, int32_t on) {
     if (!ctx) return FESOM_ERR_ARG;
     ctx->wsplit = on ? 1 : 0;
@@ -1696,7 +1858,48 @@ int fesom_gpu_set_hdiff(fesom_gpu_ctx *ctx, const double *Ki) {
     return FESOM_OK;
 }
 
+// FP64 scratch of at least n doubles for the routine-level Redi entry points
+int redi_scratch(fesom_gpu_ctx *ctx, size_t n) {
+    if (ctx->redi_tmp_n >= n) return FESOM_OK;
+    if (ctx->redi_tmp) { void *p = ctx->redi_tmp; dfree(ctx, p); ctx->redi_tmp = nullptr; ctx->redi_tmp_n = 0; }
+    int rc = dalloc(ctx, (void **)&ctx->redi_tmp, sizeof(double) * n);
+    if (rc) return rc;
+    ctx->redi_tmp_n = n;
+    return FESOM_OK;
+}
+
+int fesom_gpu_set_redi(fesom_gpu_ctx *ctx, const double *slope) {
+    if (!ctx) return FESOM_ERR_ARG;
+    const bool was = ctx->slope != nullptr;
+    if (!slope) {
+        if (ctx->slope) { void *p = ctx->slope; dfree(ctx, p); ctx->slope = nullptr; }
+        if (ctx->K33) { void *p = ctx->K33; dfree(ctx, p); ctx->K33 = nullptr; }
+    } else {
+        if (!ctx->Ki) {
+            ctx->err = "Redi needs the horizontal diffusivity Ki (fesom_gpu_set_hdiff)";
+            return FESOM_ERR_STATE;
+        }
+        int rc;
+        const size_t sN = (size_t)ctx->L1 * ctx->N2;
+        if (!ctx->slope && (rc = dalloc(ctx, &ctx->slope, rsize(ctx) * 3 * sN))) return rc;
+        if (!ctx->K33 && (rc = dalloc(ctx, &ctx->K33, rsize(ctx) * (size_t)ctx->nl * ctx->N2))) return rc;
+        if ((rc = put(ctx, ctx->slope, slope, 3 * sN))) return rc;
+        // the caller may reuse its array when the call returns
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    if (was != (slope != nullptr)) {
+        if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
+        free_graphs32(ctx);
+    }
+    return FESOM_OK;
+}
+
 int fesom_gpu_diff_hor(fesom_gpu_ctx *ctx, double dt, const double *Ki, const double *values, double *del_ttf) {
+    return fesom_gpu_diff_hor_redi(ctx, dt, Ki, nullptr, values, del_ttf);
+}
+
+int fesom_gpu_diff_hor_redi(fesom_gpu_ctx *ctx, double dt, const double *Ki, const double *slope, const double *values,
+                            double *del_ttf) {
     if (!ctx || !Ki || !values || !del_ttf) return FESOM_ERR_ARG;
     fesom_tra_cfg cfg{};
     cfg.adv_hor = FESOM_ADV_HOR_MUSCL;
@@ -1711,11 +1914,55 @@ int fesom_gpu_diff_hor(fesom_gpu_ctx *ctx, double dt, const double *Ki, const do
     if ((rc = put(ctx, ctx->tail_v, Ki, sN)) || (rc = put(ctx, tr.T, values, sN)) ||
         (rc = put(ctx, tr.dttf_h, del_ttf, sN)))
         return rc;
+    if (slope) {
+        if ((rc = redi_scratch(ctx, 3 * sN))) return rc;
+        if ((rc = put(ctx, ctx->redi_tmp, slope, 3 * sN))) return rc;
+        tr.slope = ctx->redi_tmp;
+    }
     Launch<double>::trxy(ctx->tp, ctx->g64, tr, ctx->stream);
     Launch<double>::hdiff(ctx->tp, ctx->g64, tr, ctx->stream);
     Launch<double>::hdiff_gather(ctx->tp, ctx->g64, tr, dt, tr.dttf_h, ctx->stream);
     CK(cudaGetLastError());
     if ((rc = get(ctx, del_ttf, tr.dttf_h, sN))) return rc;
+    return wait_stream(ctx, -1);
+}
+
+int fesom_gpu_diff_ver_redi_expl(fesom_gpu_ctx *ctx, double dt, const double *Ki, const double *slope,
+                                 const double *values, double *del_ttf) {
+    if (!ctx || !Ki || !slope || !values || !del_ttf) return FESOM_ERR_ARG;
+    fesom_tra_cfg cfg{};
+    cfg.adv_hor = FESOM_ADV_HOR_MUSCL;
+    cfg.ab_order = 2;
+    int rc = need_fp64(ctx);
+    if (rc || (rc = ensure_one(ctx, &cfg))) return rc;
+    const size_t sN = (size_t)ctx->L1 * ctx->N2;
+    if ((rc = redi_scratch(ctx, 4 * sN))) return rc;
+    DTracers<double> tr = group_view<double>(ctx, 0, 1);
+    tr.Ki = ctx->redi_tmp + 3 * sN;
+    tr.slope = ctx->redi_tmp;
+    tr.RV = tr.dttf_h;
+    if ((rc = put(ctx, ctx->redi_tmp, slope, 3 * sN)) || (rc = put(ctx, ctx->redi_tmp + 3 * sN, Ki, sN)) ||
+        (rc = put(ctx, tr.T, values, sN)) || (rc = put(ctx, tr.dttf_h, del_ttf, sN)))
+        return rc;
+    Launch<double>::trxy(ctx->tp, ctx->g64, tr, ctx->stream);
+    Launch<double>::redi_v(ctx->tp, ctx->g64, tr, dt, 1, ctx->stream);
+    CK(cudaGetLastError());
+    if ((rc = get(ctx, del_ttf, tr.dttf_h, sN))) return rc;
+    return wait_stream(ctx, -1);
+}
+
+int fesom_gpu_redi_k33(fesom_gpu_ctx *ctx, const double *Kv, const double *Ki, const double *slope, double *K33) {
+    if (!ctx || !Kv || !Ki || !slope || !K33) return FESOM_ERR_ARG;
+    int rc = need_fp64(ctx);
+    if (rc) return rc;
+    const size_t sN = (size_t)ctx->L1 * ctx->N2, sNI = (size_t)ctx->nl * ctx->N2;
+    if ((rc = redi_scratch(ctx, 4 * sN + 2 * sNI))) return rc;
+    double *d_s = ctx->redi_tmp, *d_ki = d_s + 3 * sN, *d_kv = d_ki + sN, *d_k = d_kv + sNI;
+    if ((rc = put(ctx, d_s, slope, 3 * sN)) || (rc = put(ctx, d_ki, Ki, sN)) || (rc = put(ctx, d_kv, Kv, sNI)))
+        return rc;
+    Launch<double>::k33(ctx->tp, ctx->g64, d_kv, d_ki, d_s, d_k, ctx->stream);
+    CK(cudaGetLastError());
+    if ((rc = get(ctx, K33, d_k, sNI))) return rc;
     return wait_stream(ctx, -1);
 }
 
@@ -2193,6 +2440,7 @@ int fesom_gpu_batch_create(fesom_gpu_ctx *const *ctxs, int32_t n, fesom_gpu_batc
             return FESOM_ERR_STATE;
         }
         if (i > 0 && c->ab_max != b->ab) { b->err = "batch instances must share one Adams-Bashforth order"; return FESOM_ERR_ARG; }
+        if (redi_on(c)) { b->err = "batch instances cannot use Redi (step Redi contexts on their own)"; return FESOM_ERR_STATE; }
         bool fct = false;
         for (int t = 0; t < c->ntr; t++) {
             b->any_ppm |= c->cfgs[t].adv_ver == FESOM_ADV_VER_PPM;

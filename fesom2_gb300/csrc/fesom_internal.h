@@ -80,6 +80,10 @@ struct DTracers {
     const R *Ki;         // horizontal diffusivity (nl-1 per node), null: no horizontal diffusion
     R *HD;               // horizontal diffusion flux per edge-layer (diff_part_hor_redi's c)
     R *VX;               // explicit vertical diffusion increment per node-layer
+    // Redi = .true.: tapered neutral slopes slope_tapered(3, nl-1, nod2D) (null: Redi off) and
+    // the increments of diff_ver_part_redi_expl per node-layer
+    const R *slope;
+    R *RV;
 };
 
 // FP32 batched form (kernels_fp32_batched.cu): one step's view of the tracer state.
@@ -116,6 +120,9 @@ struct B32View {
     const float *Kv;        // vertical diffusivity (explicit part), nl per node
     const float *fsurf;     // surface flux per group entry (g, node), G floats each; null: none
     size_t sF;              // entries per group of fsurf (nodes)
+    // Redi = .true.: tapered neutral slopes, 3 per node-layer (slope_tapered(3, nl-1, nod2D));
+    // null: Redi off
+    const float *slope;
 };
 // Node degree bound of the FP32 form (the node's edge list is staged per warp)
 constexpr int kMaxDeg = 16;
@@ -167,6 +174,9 @@ void b32_lo_impl(const DTopo &, const DGeom<float> &, const DForcing<float> &, c
 void b32_vdiff_w(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, double dt,
                  double *scratch, cudaStream_t);
 void b32_hdiff(const DTopo &, const DGeom<float> &, const B32View &, cudaStream_t);
+// Redi: K33 (nl per node) = Kv + Kd s^2 of the implicit solve (FP64 arithmetic, FP32 result)
+void b32_k33(const DTopo &, const DGeom<float> &, const float *Kv, const float *Ki, const float *slope, float *K33,
+             cudaStream_t);
 void b32_diff(const DTopo &, const DGeom<float> &, const B32View &, double dt, cudaStream_t);
 // FP64 content sum_nodes sum_levels T hnode_new areasvol of every slot of the ng groups at T
 // (out[slot]); partials: nblk * ng * G doubles
@@ -273,6 +283,11 @@ struct Launch {
     // every tracer with all != 0) into out (add == 0) or added to out (add != 0)
     static void vexpl(const DTopo &, const DGeom<R> &, const DForcing<R> &, DTracers<R> &, double dt, R *out,
                       int all, int add, cudaStream_t);
+    // Redi: diff_ver_part_redi_expl increments of the group (from tr.trxy) into tr.RV (add == 0)
+    // or added to it (add != 0)
+    static void redi_v(const DTopo &, const DGeom<R> &, DTracers<R> &, double dt, int add, cudaStream_t);
+    // Redi: K33 (nl per node) = Kv + Kd s^2 of the implicit solve, tracer-independent
+    static void k33(const DTopo &, const DGeom<R> &, const R *Kv, const R *Ki, const R *slope, R *K33, cudaStream_t);
 };
 
 }  // namespace fesom

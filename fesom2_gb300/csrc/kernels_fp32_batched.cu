@@ -1821,8 +1821,19 @@ __global__ void __launch_bounds__(128) k32_vdiff_w(DTopo tp, DGeom<float> g, DFo
 // ---------------------------------------------------------------------------
 // diffusion of diff_tracers_ale (oce_ale_tracer.F90:560-772) in the FP32 form
 // ---------------------------------------------------------------------------
-// k32_hdiff: diff_part_hor_redi (:1526-1689, Redi off) flux c of every edge-layer from the
-// element gradients of the current values: segments A/D (element 1), B/E (element 2), C (both)
+// k32_hdiff: diff_part_hor_redi (:1526-1689) flux c of every edge-layer from the element
+// gradients of the current values: segments A/D (element 1), B/E (element 2), C (both); with
+// Redi the gradient gains S_xy Tz: Tz at each edge node the layer mean of the vertical gradient
+// (tracer_gradient_z, 0 at the column's top and bottom interfaces), S_xy Tz = (Tz(n1) S(n1)
+// + Tz(n2) S(n2)) / 2 (:1583-1595)
+//
+// 1 / dz of the vertical gradient at interface nz of node n (0 where tr_z is 0)
+__device__ __forceinline__ float trz_rdz(const DTopo &tp, const DGeom<float> &g, int n, int nz) {
+    if (nz <= tp.n_ulev[n] || nz >= tp.n_nlev[n]) return 0.f;
+    const int i = n * tp.L1 + nz - 1;
+    return 2.f / (g.hnode[i - 1] + g.hnode[i]);
+}
+
 template <int G>
 __device__ __forceinline__ void hdiff_edge32(const DTopo &tp, const DGeom<float> &g, const B32View &B, int e) {
     const int lane = threadIdx.x & 31;
@@ -1850,9 +1861,23 @@ __device__ __forceinline__ void hdiff_edge32(const DTopo &tp, const DGeom<float>
     const float p0 = gs1[0], p1 = gs1[1], p2 = gs1[2], p3 = gs1[3], p4 = gs1[4], p5 = gs1[5];
     const float q0 = gs2[0], q1 = gs2[1], q2 = gs2[2], q3 = gs2[3], q4 = gs2[4], q5 = gs2[5];
     const int nl12 = min(nl1, nl2), ul12 = max(ul1, ul2);
+    const bool redi = B.slope != nullptr;
     for (int nz0 = tp.e_lo[e]; nz0 <= tp.e_hi[e]; nz0 += 32) {
         const int nz = nz0 + lane;
         if (nz > tp.e_hi[e]) continue;
+        // Redi: 1/dz of the gradients above and below the layer at both nodes, the slopes
+        float ru1 = 0.f, rd1 = 0.f, ru2 = 0.f, rd2 = 0.f, sx1 = 0.f, sy1 = 0.f, sx2 = 0.f, sy2 = 0.f;
+        if (redi) {
+            ru1 = trz_rdz(tp, g, n1, nz);
+            rd1 = trz_rdz(tp, g, n1, nz + 1);
+            ru2 = trz_rdz(tp, g, n2, nz);
+            rd2 = trz_rdz(tp, g, n2, nz + 1);
+            const float *s1 = B.slope + 3 * (size_t)(n1 * L1 + nz - 1), *s2 = B.slope + 3 * (size_t)(n2 * L1 + nz - 1);
+            sx1 = s1[0];
+            sy1 = s1[1];
+            sx2 = s2[0];
+            sy2 = s2[1];
+        }
         int seg = 0;
         if (nz >= ul1 && nz <= ul12 - 1) seg = 1;
         else if (ul2 > 0 && nz >= ul2 && nz <= ul12 - 1) seg = 2;
@@ -1869,6 +1894,20 @@ __device__ __forceinline__ void hdiff_edge32(const DTopo &tp, const DGeom<float>
                          vc = vldc<G>(u1, T, a2 * L1 + nz - 1);
             const Vec<G> wa = vldc<G>(u2, T, b0 * L1 + nz - 1), wb = vldc<G>(u2, T, b1 * L1 + nz - 1),
                          wc = vldc<G>(u2, T, b2 * L1 + nz - 1);
+            Vec<G> tz1 = vfill<G>(0.f), tz2 = vfill<G>(0.f);
+            if (redi) {
+                // the column neighbours of both edge nodes (rd = 0 where nz + 1 is not a gradient
+                // interface, ru = 0 likewise, so the loads stay inside the columns)
+                const Vec<G> m0 = vldc<G>(ru1 != 0.f, T, n1 * L1 + nz - 2), m1 = vld<G>(T, n1 * L1 + nz - 1),
+                             m2 = vldc<G>(rd1 != 0.f, T, n1 * L1 + nz);
+                const Vec<G> o0 = vldc<G>(ru2 != 0.f, T, n2 * L1 + nz - 2), o1 = vld<G>(T, n2 * L1 + nz - 1),
+                             o2 = vldc<G>(rd2 != 0.f, T, n2 * L1 + nz);
+#pragma unroll
+                for (int c = 0; c < G; c++) {
+                    tz1.c[c] = 0.5f * ((m0.c[c] - m1.c[c]) * ru1 + (m1.c[c] - m2.c[c]) * rd1);
+                    tz2.c[c] = 0.5f * ((o0.c[c] - o1.c[c]) * ru2 + (o1.c[c] - o2.c[c]) * rd2);
+                }
+            }
             Vec<G> out;
 #pragma unroll
             for (int c = 0; c < G; c++) {
@@ -1880,6 +1919,14 @@ __device__ __forceinline__ void hdiff_edge32(const DTopo &tp, const DGeom<float>
                 if (u2) {
                     tx2 = q0 * wa.c[c] + q1 * wb.c[c] + q2 * wc.c[c];
                     ty2 = q3 * wa.c[c] + q4 * wb.c[c] + q5 * wc.c[c];
+                }
+                if (redi) {
+                    const float sx = 0.5f * (tz1.c[c] * sx1 + tz2.c[c] * sx2);
+                    const float sy = 0.5f * (tz1.c[c] * sy1 + tz2.c[c] * sy2);
+                    tx1 += sx;
+                    ty1 += sy;
+                    tx2 += sx;
+                    ty2 += sy;
                 }
                 float cf = 0.f;
                 if (seg == 1) cf = (-dX1 * (Kh * ty1) + dY1 * (Kh * tx1)) * h1;
@@ -1903,7 +1950,12 @@ __global__ void __launch_bounds__(kTB) k32_hdiff(DTopo tp, DGeom<float> g, B32Vi
 // (sum of the node's edge fluxes +- c) dt / (areasvol hnode_new) and, without implicit vertical
 // diffusion, diff_ver_part_expl_ale (:841-902): vd(ul) = surface flux, vd(nz) = Kv (T(nz-1)
 // - T(nz)) / (Z(nz-1) - Z(nz)) area, increment (vd(nz) - vd(nz+1)) / (zbar(nz) - zbar(nz+1))
-// dt / (areasvol hnode_new)
+// dt / (areasvol hnode_new).  With Redi, diff_ver_part_redi_expl (:1439-1518): the node
+// gradient g(nz) = sum over the node's elements wet at nz of grad T elem_area / 3 / areasvol,
+// p = S_xy . g, interface flux vd(nz) = (h(nz-1) p(nz-1) Ki(nz-1) + h(nz) p(nz) Ki(nz)) /
+// (h(nz-1) + h(nz)) area(nz) with h = hnode (the reference's depth differences z(nz-1) -
+// zbar(nz) = h(nz-1)/2 etc. in exact arithmetic), increment (vd(nz) - vd(nz+1)) dt / (areasvol
+// hnode_new)
 template <int G, int KD>
 __device__ __forceinline__ void diff_node32(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int n,
                                             int lane, const WEdges &S) {
@@ -1923,6 +1975,19 @@ __device__ __forceinline__ void diff_node32(const DTopo &tp, const DGeom<float> 
             q = sdt / (g.zbar3[iv] - g.zbar3[iv + 1]);
         }
         const float kzd = sh_dn(kz, 1);
+        // Redi: weights of p above and at the interface nz, 1 / (3 areasvol), the slopes
+        float cu = 0.f, cd = 0.f, r3 = 0.f, sx = 0.f, sy = 0.f;
+        if (B.slope && k.lvl) {
+            r3 = 1.f / (3.f * g.areasvol[iv]);
+            sx = B.slope[3 * (size_t)i];
+            sy = B.slope[3 * (size_t)i + 1];
+            if (nz > nzmin) {
+                const float hu = g.hnode[i - 1], hd = g.hnode[i];
+                const float w = g.area[iv] / (hu + hd);
+                cu = hu * B.Ki[i - 1] * w;
+                cd = hd * B.Ki[i] * w;
+            }
+        }
         unsigned okm = 0;
 #pragma unroll
         for (int u = 0; u < KD; u++) {
@@ -1955,6 +2020,31 @@ __device__ __forceinline__ void diff_node32(const DTopo &tp, const DGeom<float> 
                     const float vd0 = nz == nzmin ? fs.c[c] : kz * (Tu - Tn);
                     const float vd1 = nz == nzmax - 1 ? 0.f : kzd * (Tn - Td);
                     d.c[c] += (vd0 - vd1) * q;
+                }
+            }
+            if (B.slope) {
+                const float *__restrict__ T = grp<G>(B.T, gq, B.sN);
+                Vec<G> gx = vfill<G>(0.f), gy = vfill<G>(0.f);
+                for (int kk = tp.nie_ptr[n]; kk < tp.nie_ptr[n + 1]; kk++) {
+                    const int el = tp.nie_idx[kk];
+                    const bool wet = k.lvl && nz >= tp.t_ulev[el] && nz <= tp.t_nlev[el] - 1;
+                    const float *gs = g.gs + 6 * (size_t)el;
+                    const float ea = g.elem_area[el];
+                    const Vec<G> ta = vldc<G>(wet, T, tp.t_n[3 * el] * L1 + nz - 1),
+                                 tb = vldc<G>(wet, T, tp.t_n[3 * el + 1] * L1 + nz - 1),
+                                 tc = vldc<G>(wet, T, tp.t_n[3 * el + 2] * L1 + nz - 1);
+#pragma unroll
+                    for (int c = 0; c < G; c++) {
+                        gx.c[c] += (gs[0] * ta.c[c] + gs[1] * tb.c[c] + gs[2] * tc.c[c]) * ea;
+                        gy.c[c] += (gs[3] * ta.c[c] + gs[4] * tb.c[c] + gs[5] * tc.c[c]) * ea;
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < G; c++) {
+                    const float pz = (sx * gx.c[c] + sy * gy.c[c]) * r3;
+                    const float vd = cu * sh_up(pz, 1) + cd * pz;
+                    const float vdn = sh_dn(vd, 1);
+                    d.c[c] += (vd - vdn) * sdt;
                 }
             }
             if (k.out) vst<G>(grp<G>(B.Tnew, gq, B.sN), i, d);
@@ -2486,6 +2576,38 @@ void b32_vdiff_w(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &
     if (B.G == 4) k32_vdiff_w<4><<<(tp.N2 + 127) / 128, 128, 0, s>>>(tp, g, f, B, dt, scratch);
     else k32_vdiff_w<2><<<(tp.N2 + 127) / 128, 128, 0, s>>>(tp, g, f, B, dt, scratch);
 }
+// Redi K33 = Kv + Ty (oce_ale_tracer.F90:1099-1204) of every interface nzmin < nz < nzmax, one
+// thread per column, in FP64 from the FP32 inputs: Ty = (zbar(nz) - Z(nz)) / dZ s3(nz-1)^2
+// Ki(nz-1) + (Z(nz-1) - zbar(nz)) / dZ s3(nz)^2 Ki(nz), dZ = Z(nz-1) - Z(nz), zbar / Z of
+// hnode_new from zbar_n_bot upward; Kv elsewhere
+__global__ void __launch_bounds__(128) k32_k33(DTopo tp, DGeom<float> g, const float *Kv, const float *Ki,
+                                               const float *slope, float *K33) {
+    const int L1 = tp.L1, nl = tp.nl;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < tp.N2; n += gridDim.x * blockDim.x) {
+        const int nzmax = tp.n_nlev[n], nzmin = tp.n_ulev[n];
+        const size_t b = (size_t)n * nl, c = (size_t)n * L1;
+        for (int nz = 1; nz <= nl; nz++) K33[b + nz - 1] = Kv[b + nz - 1];
+        double zb = g.zbar_n_bot[n];
+        double Zc = zb + (double)g.hnode_new[c + nzmax - 2] / 2.0;
+        for (int nz = nzmax - 1; nz >= nzmin + 1; nz--) {
+            const double zbn = zb + (double)g.hnode_new[c + nz - 1];
+            const double Zu = zbn + (double)g.hnode_new[c + nz - 2] / 2.0;
+            const double zinv = 1.0 / (Zu - Zc);
+            const double sa = slope[3 * (c + nz - 2) + 2], sb = slope[3 * (c + nz - 1) + 2];
+            const double Ty = (zbn - Zc) * zinv * (sa * sa) * (double)Ki[c + nz - 2] +
+                              (Zu - zbn) * zinv * (sb * sb) * (double)Ki[c + nz - 1];
+            K33[b + nz - 1] = (float)((double)Kv[b + nz - 1] + Ty);
+            zb = zbn;
+            Zc = Zu;
+        }
+    }
+}
+
+void b32_k33(const DTopo &tp, const DGeom<float> &g, const float *Kv, const float *Ki, const float *slope, float *K33,
+             cudaStream_t s) {
+    k32_k33<<<(tp.N2 + 127) / 128, 128, 0, s>>>(tp, g, Kv, Ki, slope, K33);
+}
+
 void b32_hdiff(const DTopo &tp, const DGeom<float> &g, const B32View &B, cudaStream_t s) {
     if (B.G == 4) k32_hdiff<4><<<grid_nodes(tp.E2), kTB, 0, s>>>(tp, g, B);
     else k32_hdiff<2><<<grid_nodes(tp.E2), kTB, 0, s>>>(tp, g, B);

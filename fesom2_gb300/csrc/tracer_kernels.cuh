@@ -667,6 +667,8 @@ __global__ void __launch_bounds__(kThreads) k_update(DTopo tp, DGeom<R> g, DTrac
                         // diff_tracers_ale: horizontal, then explicit vertical diffusion
                         if (tr.HD) del = hdiff_add(tp, tr.HD + t * tr.sE, del, n, nz, L1, dt, av);
                         if (tr.VX && !tr.cfg[t].ivd) del = del + tr.VX[t * tr.sN + i];
+                        // Redi: diff_ver_part_redi_expl (:623)
+                        if (tr.RV) del = del + tr.RV[t * tr.sN + i];
                         del = del + T[i] * (g.hnode[i] - g.hnode_new[i]);
                     }
                     const R tn = T[i] + del / g.hnode_new[i];
@@ -684,9 +686,39 @@ __global__ void __launch_bounds__(kThreads) k_update(DTopo tp, DGeom<R> g, DTrac
 // tp level-major ([level][node]) so that a warp's accesses are coalesced.
 // ===========================================================================
 // ---------------------------------------------------------------------------
-// diff_part_hor_redi (oce_ale_tracer.F90:1526-1689), Redi off: per edge-layer the flux
-// c of the segment (A/D: element 1, B/E: element 2, C: both), Kh = (Ki(n1) + Ki(n2)) / 2
+// diff_part_hor_redi (oce_ale_tracer.F90:1526-1689): per edge-layer the flux c of the segment
+// (A/D: element 1, B/E: element 2, C: both), Kh = (Ki(n1) + Ki(n2)) / 2, F = Kh grad T, with
+// Redi F = Kh (grad T + S_xy Tz): Tz = mean over the layer of the vertical gradient at each
+// edge node, S_xy Tz = (Tz(n1) S(n1) + Tz(n2) S(n2)) / 2 (:1583-1595)
 // ---------------------------------------------------------------------------
+// tracer_gradient_z (oce_tracer_mod.F90:192-232) of T at interface nz of node n: 0 at the
+// column's top and bottom interfaces
+template <typename R>
+__device__ __forceinline__ R trz_node(const DTopo &tp, const DGeom<R> &g, const R *T, int n, int nz) {
+    const int L1 = tp.L1;
+    if (nz <= tp.n_ulev[n] || nz >= tp.n_nlev[n]) return R(0);
+    const R dz = R(0.5) * (g.hnode[ix1(nz - 1, n, L1)] + g.hnode[ix1(nz, n, L1)]);
+    return (T[ix1(nz - 1, n, L1)] - T[ix1(nz, n, L1)]) / dz;
+}
+
+template <typename R>
+__device__ __forceinline__ void hdiff_flux(const DTopo &tp, const DGeom<R> &g, const DTracers<R> &tr, const R *T,
+                                          int n1, int n2, int nz, R Kh, R Tx, R Ty, R &Fx, R &Fy) {
+    if (!tr.slope) {
+        Fx = Kh * Tx;
+        Fy = Kh * Ty;
+        return;
+    }
+    const int L1 = tp.L1;
+    const R tz1 = R(0.5) * (trz_node(tp, g, T, n1, nz) + trz_node(tp, g, T, n1, nz + 1));
+    const R tz2 = R(0.5) * (trz_node(tp, g, T, n2, nz) + trz_node(tp, g, T, n2, nz + 1));
+    const R *s1 = tr.slope + 3 * ix1(nz, n1, L1), *s2 = tr.slope + 3 * ix1(nz, n2, L1);
+    const R sx = (tz1 * s1[0] + tz2 * s2[0]) / R(2.0);
+    const R sy = (tz1 * s1[1] + tz2 * s2[1]) / R(2.0);
+    Fx = Kh * (Tx + sx);
+    Fy = Kh * (Ty + sy);
+}
+
 template <typename R>
 __global__ void __launch_bounds__(kThreads) k_hdiff(DTopo tp, DGeom<R> g, DTracers<R> tr) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -714,21 +746,24 @@ __global__ void __launch_bounds__(kThreads) k_hdiff(DTopo tp, DGeom<R> g, DTrace
             for (int t = 0; t < tr.ntr; t++) {
                 const R *Ki = tr.Ki;
                 const R *xy = tr.trxy + t * tr.sT;
+                const R *T = tr.T + t * tr.sN;
                 const R Kh = (Ki[ix1(nz, n1, L1)] + Ki[ix1(nz, n2, L1)]) / R(2.0);
-                R c = R(0);
+                R c = R(0), Fx, Fy;
                 if (seg == 1) {
                     const R dz = g.helem[ix1(nz, el1, L1)];
-                    const R Fx = Kh * xy[2 * ix1(nz, el1, L1)], Fy = Kh * xy[2 * ix1(nz, el1, L1) + 1];
+                    hdiff_flux(tp, g, tr, T, n1, n2, nz, Kh, xy[2 * ix1(nz, el1, L1)], xy[2 * ix1(nz, el1, L1) + 1], Fx,
+                               Fy);
                     c = (-dX1 * Fy + dY1 * Fx) * dz;
                 } else if (seg == 2) {
                     const R dz = g.helem[ix1(nz, el2, L1)];
-                    const R Fx = Kh * xy[2 * ix1(nz, el2, L1)], Fy = Kh * xy[2 * ix1(nz, el2, L1) + 1];
+                    hdiff_flux(tp, g, tr, T, n1, n2, nz, Kh, xy[2 * ix1(nz, el2, L1)], xy[2 * ix1(nz, el2, L1) + 1], Fx,
+                               Fy);
                     c = (dX2 * Fy - dY2 * Fx) * dz;
                 } else if (seg == 3) {
                     const R dz = (g.helem[ix1(nz, el1, L1)] + g.helem[ix1(nz, el2, L1)]) / R(2.0);
                     const R Tx = R(0.5) * (xy[2 * ix1(nz, el1, L1)] + xy[2 * ix1(nz, el2, L1)]);
                     const R Ty = R(0.5) * (xy[2 * ix1(nz, el1, L1) + 1] + xy[2 * ix1(nz, el2, L1) + 1]);
-                    const R Fx = Kh * Tx, Fy = Kh * Ty;
+                    hdiff_flux(tp, g, tr, T, n1, n2, nz, Kh, Tx, Ty, Fx, Fy);
                     c = ((dX2 - dX1) * Fy - (dY2 - dY1) * Fx) * dz;
                 }
                 tr.HD[t * tr.sE + ix1(nz, e, L1)] = c;
@@ -911,6 +946,90 @@ __global__ void __launch_bounds__(128) k_vdiff(DTopo tp, DGeom<R> g, DForcing<R>
     }
 }
 
+// ---------------------------------------------------------------------------
+// diff_ver_part_redi_expl (oce_ale_tracer.F90:1439-1518), one thread per column, walking the
+// column bottom up: node gradients (sum over the node's elements wet at nz of tr_xy
+// elem_area) / 3 / areasvol; depths zbar_n, z_n from hnode and zbar_n_bot; interface flux
+// vd(nz) = ((z(nz-1) - zbar(nz)) S.g(nz-1) Ki(nz-1) + (zbar(nz) - z(nz)) S.g(nz) Ki(nz))
+// / (z(nz-1) - z(nz)) area(nz); increment (vd(nz) - vd(nz+1)) dt / areasvol into RV
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ R redi_proj(const DTopo &tp, const DGeom<R> &g, const R *xy, const R *slope, int n, int nz) {
+    const int L1 = tp.L1;
+    R tx = R(0), ty = R(0);
+    for (int k = tp.nie_ptr[n]; k < tp.nie_ptr[n + 1]; k++) {
+        const int el = tp.nie_idx[k];
+        if (nz <= tp.t_nlev[el] - 1 && nz >= tp.t_ulev[el]) {
+            tx = tx + xy[2 * ix1(nz, el, L1)] * g.elem_area[el];
+            ty = ty + xy[2 * ix1(nz, el, L1) + 1] * g.elem_area[el];
+        }
+    }
+    const R av = g.areasvol[ixn(nz, n, tp.nl)];
+    const R gx = tx / R(3.0) / av, gy = ty / R(3.0) / av;
+    const R *s = slope + 3 * ix1(nz, n, L1);
+    return s[0] * gx + s[1] * gy;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_redi_v(DTopo tp, DGeom<R> g, DTracers<R> tr, R dt, int add) {
+    const int L1 = tp.L1, nl = tp.nl;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < tp.N2; n += gridDim.x * blockDim.x) {
+        const int nl1 = tp.n_nlev[n] - 1, ul1 = tp.n_ulev[n];
+        const R *Ki = tr.Ki;
+        for (int t = 0; t < tr.ntr; t++) {
+            const R *xy = tr.trxy + t * tr.sT;
+            R *out = tr.RV + t * tr.sN;
+            R zb = g.zbar_n_bot[n];                                  // zbar_n(nz + 1)
+            R zc = zb + g.hnode[ix1(nl1, n, L1)] / R(2.0);           // z_n(nz)
+            R pc = redi_proj(tp, g, xy, tr.slope, n, nl1);           // S . grad at nz
+            R below = R(0);                                          // vd(nz + 1)
+            for (int nz = nl1; nz >= ul1; nz--) {
+                R vd = R(0);
+                if (nz >= ul1 + 1) {
+                    const R zbn = zb + g.hnode[ix1(nz, n, L1)];                  // zbar_n(nz)
+                    const R zu = zbn + g.hnode[ix1(nz - 1, n, L1)] / R(2.0);     // z_n(nz - 1)
+                    const R pu = redi_proj(tp, g, xy, tr.slope, n, nz - 1);
+                    R v = (zu - zbn) * pu * Ki[ix1(nz - 1, n, L1)];
+                    v = v + (zbn - zc) * pc * Ki[ix1(nz, n, L1)];
+                    vd = v / (zu - zc) * g.area[ixn(nz, n, nl)];
+                    zb = zbn;
+                    zc = zu;
+                    pc = pu;
+                }
+                const R inc = (vd - below) * dt / g.areasvol[ixn(nz, n, nl)];
+                out[ix1(nz, n, L1)] = add ? out[ix1(nz, n, L1)] + inc : inc;
+                below = vd;
+            }
+        }
+    }
+}
+
+// K33 = Kv + Ty of diff_ver_part_impl_ale with Redi (oce_ale_tracer.F90:1099-1204) at the
+// interfaces nzmin < nz < nzmax, from zbar_n / Z_n of hnode_new bottom up:
+// Ty = (zbar(nz) - Z(nz)) / dZ s3(nz-1)^2 Ki(nz-1) + (Z(nz-1) - zbar(nz)) / dZ s3(nz)^2 Ki(nz),
+// dZ = Z(nz-1) - Z(nz) (the Ty1 of the layer above is the same number); Kv elsewhere
+template <typename R>
+__global__ void __launch_bounds__(128) k_k33(DTopo tp, DGeom<R> g, const R *Kv, const R *Ki, const R *slope, R *K33) {
+    const int L1 = tp.L1, nl = tp.nl;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < tp.N2; n += gridDim.x * blockDim.x) {
+        const int nzmax = tp.n_nlev[n], nzmin = tp.n_ulev[n];
+        for (int nz = 1; nz <= nl; nz++) K33[ixn(nz, n, nl)] = Kv[ixn(nz, n, nl)];
+        R zb = g.zbar_n_bot[n];                                         // zbar_n(nz + 1)
+        R Zc = zb + g.hnode_new[ix1(nzmax - 1, n, L1)] / R(2.0);        // Z_n(nz)
+        for (int nz = nzmax - 1; nz >= nzmin + 1; nz--) {
+            const R zbn = zb + g.hnode_new[ix1(nz, n, L1)];             // zbar_n(nz)
+            const R Zu = zbn + g.hnode_new[ix1(nz - 1, n, L1)] / R(2.0);  // Z_n(nz - 1)
+            const R zinv = R(1.0) / (Zu - Zc);
+            const R sa = slope[3 * ix1(nz - 1, n, L1) + 2], sb = slope[3 * ix1(nz, n, L1) + 2];
+            const R Ty = (zbn - Zc) * zinv * (sa * sa) * Ki[ix1(nz - 1, n, L1)] +
+                         (Zu - zbn) * zinv * (sb * sb) * Ki[ix1(nz, n, L1)];
+            K33[ixn(nz, n, nl)] = Kv[ixn(nz, n, nl)] + Ty;
+            zb = zbn;
+            Zc = Zu;
+        }
+    }
+}
+
 // ===========================================================================
 // Global content sum over wet node-layers of T * hnode_new * areasvol (FP64),
 // deterministic: fixed per-block partials, then one ordered pass.
@@ -1029,6 +1148,15 @@ template <typename R>
 void Launch<R>::vexpl(const DTopo &tp, const DGeom<R> &g, const DForcing<R> &f, DTracers<R> &tr, double dt, R *out,
                       int all, int add, cudaStream_t s) {
     k_vexpl<R><<<grid_for(tp.N2, kWarpsPerBlock), kThreads, 0, s>>>(tp, g, f, tr, (R)dt, out, all, add);
+}
+template <typename R>
+void Launch<R>::redi_v(const DTopo &tp, const DGeom<R> &g, DTracers<R> &tr, double dt, int add, cudaStream_t s) {
+    k_redi_v<R><<<(tp.N2 + 127) / 128, 128, 0, s>>>(tp, g, tr, (R)dt, add);
+}
+template <typename R>
+void Launch<R>::k33(const DTopo &tp, const DGeom<R> &g, const R *Kv, const R *Ki, const R *slope, R *K33,
+                    cudaStream_t s) {
+    k_k33<R><<<(tp.N2 + 127) / 128, 128, 0, s>>>(tp, g, Kv, Ki, slope, K33);
 }
 
 }  // namespace fesom

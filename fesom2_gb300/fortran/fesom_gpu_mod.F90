@@ -44,6 +44,13 @@ module fesom_gpu_mod
      real(c_double)     :: lat0, dy, tau_inv
   end type fesom_tail_cfg
 
+  ! result of the FP32 launch-settings autotuner (fesom_gpu_autotune)
+  type, bind(C) :: fesom_tune_result
+     real(c_float)      :: default_ms, tuned_ms
+     integer(c_int32_t) :: candidates
+     integer(c_int32_t) :: stage_tracers(4), blocks_per_sm(4), variant(4)
+  end type fesom_tune_result
+
   interface
      integer(c_int) function fesom_gpu_abi_version() bind(C, name="fesom_gpu_abi_version")
        import
@@ -145,6 +152,30 @@ module fesom_gpu_mod
        real(c_double), value :: dt
        type(c_ptr), value :: Ki, values, del_ttf
      end function fesom_gpu_diff_hor
+     ! Redi = .true. with slope_tapered(3, nl-1, nod2D) as input (src/oce_ale_tracer.F90:594-623,
+     ! 1099-1204, 1439-1689): set once per change of the slopes; the routines alone (FP64)
+     integer(c_int) function fesom_gpu_set_redi(ctx, slope) bind(C, name="fesom_gpu_set_redi")
+       import
+       type(c_ptr), value :: ctx, slope
+     end function fesom_gpu_set_redi
+     integer(c_int) function fesom_gpu_diff_hor_redi(ctx, dt, Ki, slope, values, del_ttf) &
+          bind(C, name="fesom_gpu_diff_hor_redi")
+       import
+       type(c_ptr), value :: ctx
+       real(c_double), value :: dt
+       type(c_ptr), value :: Ki, slope, values, del_ttf
+     end function fesom_gpu_diff_hor_redi
+     integer(c_int) function fesom_gpu_diff_ver_redi_expl(ctx, dt, Ki, slope, values, del_ttf) &
+          bind(C, name="fesom_gpu_diff_ver_redi_expl")
+       import
+       type(c_ptr), value :: ctx
+       real(c_double), value :: dt
+       type(c_ptr), value :: Ki, slope, values, del_ttf
+     end function fesom_gpu_diff_ver_redi_expl
+     integer(c_int) function fesom_gpu_redi_k33(ctx, Kv, Ki, slope, K33) bind(C, name="fesom_gpu_redi_k33")
+       import
+       type(c_ptr), value :: ctx, Kv, Ki, slope, K33
+     end function fesom_gpu_redi_k33
      integer(c_int) function fesom_gpu_diff_ver_expl(ctx, dt, Kv, flux_surf, values, del_ttf) &
           bind(C, name="fesom_gpu_diff_ver_expl")
        import
@@ -205,6 +236,14 @@ module fesom_gpu_mod
        import
        type(c_ptr), value :: ctx, content
      end function fesom_gpu_tracer_content
+     ! FP32 launch settings chosen by timing the context's own step (state restored afterwards)
+     integer(c_int) function fesom_gpu_autotune(ctx, dt, steps, res) bind(C, name="fesom_gpu_autotune")
+       import
+       type(c_ptr), value :: ctx
+       real(c_double), value :: dt
+       integer(c_int32_t), value :: steps
+       type(fesom_tune_result), intent(out) :: res
+     end function fesom_gpu_autotune
      ! allocation-free implicit vertical diffusion on device arrays the caller holds
      integer(c_int) function fesom_gpu_vdiff_impl_noalloc(nod2D, nl, nlevels_nod2D, ulevels_nod2D, zbar_n_bot, &
           hnode_new, area, areasvol, Kv, bc_surf, dt, values, stream, errbuf, errlen) &

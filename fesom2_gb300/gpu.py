@@ -51,6 +51,12 @@ class MeshDesc(C.Structure):
         [("cyclic_length", C.c_double), ("nboundary_lay", _P), ("edge_up_dn_tri", _P)]
 
 
+class TuneResult(C.Structure):
+    """``fesom_tune_result``: the FP32 launch settings chosen by ``fesom_gpu_autotune``."""
+    _fields_ = [("default_ms", C.c_float), ("tuned_ms", C.c_float), ("candidates", C.c_int32),
+                ("stage_tracers", C.c_int32 * 4), ("blocks_per_sm", C.c_int32 * 4), ("variant", C.c_int32 * 4)]
+
+
 class FesomGpuError(RuntimeError):
     def __init__(self, rc: int, msg: str):
         super().__init__(f"FESOM_ERR_{ERRORS.get(rc, rc)}: {msg}")
@@ -98,8 +104,13 @@ _SIGS = {
     "fesom_gpu_set_stage_tracers": ([_P, C.c_int32, C.c_int32], C.c_int),
     "fesom_gpu_set_launch_shape": ([_P, C.c_int32, C.c_int32], C.c_int),
     "fesom_gpu_set_stage_variant": ([_P, C.c_int32, C.c_int32], C.c_int),
+    "fesom_gpu_autotune": ([_P, C.c_double, C.c_int32, C.POINTER(TuneResult)], C.c_int),
     "fesom_gpu_vdiff_impl_wi": ([_P, C.c_double, C.POINTER(TraCfg), _P, _P, _P, _P], C.c_int),
     "fesom_gpu_diff_hor": ([_P, C.c_double, _P, _P, _P], C.c_int),
+    "fesom_gpu_set_redi": ([_P, _P], C.c_int),
+    "fesom_gpu_diff_hor_redi": ([_P, C.c_double, _P, _P, _P, _P], C.c_int),
+    "fesom_gpu_diff_ver_redi_expl": ([_P, C.c_double, _P, _P, _P, _P], C.c_int),
+    "fesom_gpu_redi_k33": ([_P, _P, _P, _P, _P], C.c_int),
     "fesom_gpu_diff_ver_expl": ([_P, C.c_double, _P, _P, _P, _P], C.c_int),
     "fesom_gpu_step_host_f32": ([_P, C.c_double, _P, _P, _P, _P, _P, _P, C.POINTER(_P), C.POINTER(_P),
                                  C.POINTER(_P), C.POINTER(_P)], C.c_int),
@@ -307,6 +318,16 @@ class Context:
         1: staged in shared memory)."""
         self._chk(self.L.fesom_gpu_set_stage_variant(self.h, int(stage), int(variant)))
 
+    def autotune(self, dt: float, steps: int = 2) -> dict:
+        """FP32 form: time the step under candidate launch settings, keep the fastest
+        (fesom_gpu_autotune); the tracer state is left as it was.  Returns the choice and the
+        ms per step under the defaults and under the choice."""
+        r = TuneResult()
+        self._chk(self.L.fesom_gpu_autotune(self.h, float(dt), int(steps), C.byref(r)))
+        return {"default_ms": float(r.default_ms), "tuned_ms": float(r.tuned_ms), "candidates": int(r.candidates),
+                "stage_tracers": list(r.stage_tracers), "blocks_per_sm": list(r.blocks_per_sm),
+                "variant": list(r.variant)}
+
     def set_wsplit(self, on: bool):
         """dynamics%use_wsplit for every later step (fesom_gpu_set_wsplit)."""
         self._chk(self.L.fesom_gpu_set_wsplit(self.h, 1 if on else 0))
@@ -419,13 +440,39 @@ class Context:
         self._Ki = None if Ki is None else _c64(Ki)
         self._chk(self.L.fesom_gpu_set_hdiff(self.h, None if self._Ki is None else _p(self._Ki)))
 
-    def diff_hor(self, dt, Ki, values, del_ttf):
+    def set_redi(self, slope):
+        """Redi = .true. with the tapered neutral slopes ``slope`` (nod2D, nl-1, 3) for every later
+        step (``None``: Redi off); needs set_hdiff first."""
+        self._slope = None if slope is None else _c64(slope)
+        self._chk(self.L.fesom_gpu_set_redi(self.h, None if self._slope is None else _p(self._slope)))
+
+    def diff_hor(self, dt, Ki, values, del_ttf, slope=None):
         """diff_part_hor_redi alone (FP64): ``del_ttf`` (float64, in place) += the horizontal
-        diffusion of ``values``."""
+        diffusion of ``values`` (with the Redi slope terms when ``slope`` is given)."""
         if del_ttf.dtype != np.float64 or not del_ttf.flags.c_contiguous:
             raise ValueError("del_ttf must be C-contiguous float64")
         keep = [_c64(Ki), _c64(values)]
-        self._chk(self.L.fesom_gpu_diff_hor(self.h, float(dt), _p(keep[0]), _p(keep[1]), _p(del_ttf)))
+        if slope is None:
+            self._chk(self.L.fesom_gpu_diff_hor(self.h, float(dt), _p(keep[0]), _p(keep[1]), _p(del_ttf)))
+        else:
+            sl = _c64(slope)
+            self._chk(self.L.fesom_gpu_diff_hor_redi(self.h, float(dt), _p(keep[0]), _p(sl), _p(keep[1]),
+                                                     _p(del_ttf)))
+
+    def diff_ver_redi_expl(self, dt, Ki, slope, values, del_ttf):
+        """diff_ver_part_redi_expl alone (FP64): ``del_ttf`` (float64, in place) += the vertical
+        projection of the isoneutral flux of ``values``."""
+        if del_ttf.dtype != np.float64 or not del_ttf.flags.c_contiguous:
+            raise ValueError("del_ttf must be C-contiguous float64")
+        keep = [_c64(Ki), _c64(slope), _c64(values)]
+        self._chk(self.L.fesom_gpu_diff_ver_redi_expl(self.h, float(dt), *[_p(a) for a in keep], _p(del_ttf)))
+
+    def redi_k33(self, Kv, Ki, slope):
+        """K33 = Kv + Kd s^2 of the implicit solve with Redi (FP64), (nod2D, nl)."""
+        out = np.empty(np.shape(Kv), np.float64)
+        keep = [_c64(Kv), _c64(Ki), _c64(slope)]
+        self._chk(self.L.fesom_gpu_redi_k33(self.h, *[_p(a) for a in keep], _p(out)))
+        return out
 
     def diff_ver_expl(self, dt, Kv, flux_surf, values, del_ttf):
         """diff_ver_part_expl_ale alone (FP64): ``del_ttf`` (float64, in place) += the explicit

@@ -13,7 +13,11 @@
  *                               diff_tracers_ale's T* update and implicit
  *                               vertical diffusion) for all tracers at once
  *   fesom_gpu_diff_hor          diff_part_hor_redi       src/oce_ale_tracer.F90:1526-1689 (Redi off)
+ *   fesom_gpu_diff_hor_redi     diff_part_hor_redi       src/oce_ale_tracer.F90:1526-1689 (Redi on)
  *   fesom_gpu_diff_ver_expl     diff_ver_part_expl_ale   src/oce_ale_tracer.F90:841-902
+ *   fesom_gpu_diff_ver_redi_expl diff_ver_part_redi_expl src/oce_ale_tracer.F90:1439-1518
+ *   fesom_gpu_redi_k33          K_33 = Kv + Kd s^2 of diff_ver_part_impl_ale with Redi
+ *                               src/oce_ale_tracer.F90:1099-1204
  *   fesom_gpu_tracer_tail       tail of solve_tracers_ale src/oce_ale_tracer.F90:353-375, 497-525
  *   fesom_gpu_init              setup of the mesh-derived work arrays:
  *                               oce_adv_tra_fct_init  src/oce_adv_tra_fct.F90:35-67,
@@ -305,9 +309,42 @@ int fesom_gpu_set_launch_shape(fesom_gpu_ctx *ctx, int32_t stage, int32_t blocks
  * register limit on the gathers in flight).  Defaults: lo_ad 1, bounds 0, update 0.  The two
  * variants are separate compilations and agree to FP32 round-off. */
 int fesom_gpu_set_stage_variant(fesom_gpu_ctx *ctx, int32_t stage, int32_t variant);
+/* Autotuner of the FP32 form's launch settings (results do not change): times the step of the
+ * context's own state under the library defaults, then by coordinate descent over the four node/edge
+ * stages under each kernel variant, blocks per SM (0, 2, 4) and, for bounds and update with more
+ * than 8 tracer slots, 8 tracers per launch; a candidate is kept when it is more than 1 % faster.
+ * Each candidate runs one untimed and `steps` timed steps (CUDA events on the context's stream).
+ * The fastest settings stay on the context; the tracer state and its time levels are restored
+ * afterwards (one extra copy of the time levels on the device while tuning). */
+typedef struct fesom_tune_result {
+    float default_ms, tuned_ms;   /* ms per step under the defaults and under the chosen settings */
+    int32_t candidates;           /* settings timed */
+    int32_t stage_tracers[4];     /* chosen, per stage (fesom_gpu_set_stage_tracers) */
+    int32_t blocks_per_sm[4];     /* (fesom_gpu_set_launch_shape) */
+    int32_t variant[4];           /* (fesom_gpu_set_stage_variant; stage 1 has one variant) */
+} fesom_tune_result;
+int fesom_gpu_autotune(fesom_gpu_ctx *ctx, double dt, int32_t steps, fesom_tune_result *res);
 /* The routine alone (FP64 contexts): del_ttf += the edge diffusion fluxes of the element
  * gradients of values, in ascending edge order. */
 int fesom_gpu_diff_hor(fesom_gpu_ctx *ctx, double dt, const double *Ki, const double *values, double *del_ttf);
+/* Redi = .true. (isoneutral diffusion, src/oce_ale_tracer.F90:594-623, 1099-1204, 1439-1689) with
+ * the tapered neutral slopes slope(3, nl-1, nod2D) (slope_tapered of compute_neutral_slope,
+ * src/oce_ale_pressure_bv.F90:3039-3157) as input.  fesom_gpu_set_redi copies the slopes to the
+ * context (call it again whenever they change, e.g. before every step; NULL: Redi off); every
+ * later step of either form then adds the slope terms to the horizontal diffusion, applies
+ * diff_ver_part_redi_expl after the explicit vertical part, and diffuses implicitly with
+ * K33 = Kv + Kd s^2.  Needs the horizontal diffusivity (fesom_gpu_set_hdiff; FESOM_ERR_STATE
+ * without it); clearing Ki suspends Redi.  The multi-instance batch does not take Redi. */
+int fesom_gpu_set_redi(fesom_gpu_ctx *ctx, const double *slope);
+/* The routines alone (FP64 contexts): diff_part_hor_redi with the slope terms (slope NULL:
+ * fesom_gpu_diff_hor), diff_ver_part_redi_expl (del_ttf += the vertical projection of the
+ * isoneutral flux of values), and K33(nl, nod2D) = Kv + Ty at the interfaces nzmin < nz < nzmax
+ * of each column (Kv elsewhere). */
+int fesom_gpu_diff_hor_redi(fesom_gpu_ctx *ctx, double dt, const double *Ki, const double *slope, const double *values,
+                            double *del_ttf);
+int fesom_gpu_diff_ver_redi_expl(fesom_gpu_ctx *ctx, double dt, const double *Ki, const double *slope,
+                                 const double *values, double *del_ttf);
+int fesom_gpu_redi_k33(fesom_gpu_ctx *ctx, const double *Kv, const double *Ki, const double *slope, double *K33);
 /* diff_ver_part_expl_ale (src/oce_ale_tracer.F90:841-902, FP64 contexts): del_ttf += the explicit
  * vertical diffusion of values with Kv(nl, nod2D); flux_surf(nod2D) is the surface flux
  * vd_flux(ulevels) (-heat_flux/vcpw for temperature, the salt fluxes for salinity; NULL: 0).

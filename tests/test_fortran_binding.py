@@ -42,7 +42,8 @@ def _struct_fields(name):
         if not decl:
             continue
         names = decl.split(None, 1)[1] if not decl.startswith("const") else decl.split(None, 2)[2]
-        fields += [n.strip().lstrip("*") for n in names.split(",")]
+        # arrays: x[4] in C is x(4) in Fortran
+        fields += [re.sub(r"\[(\d+)\]", r"(\1)", n.strip().lstrip("*")) for n in names.split(",")]
     return fields
 
 
@@ -80,5 +81,5 @@ def test_the_drop_in_routines_are_bound():
 
 def test_bind_c_types_follow_the_c_structs():
     for c_name, f_name in (("fesom_tra_cfg", "fesom_tra_cfg"), ("fesom_mesh_desc", "fesom_mesh_desc"),
-                           ("fesom_tail_cfg", "fesom_tail_cfg")):
+                           ("fesom_tail_cfg", "fesom_tail_cfg"), ("fesom_tune_result", "fesom_tune_result")):
         assert [f.lower() for f in _struct_fields(c_name)] == [f.lower() for f in _fortran_type_fields(f_name)]

@@ -191,9 +191,12 @@ def test_fp32_error_vs_fp64_oracle(meshname, kind, request):
     assert ctx.status() == 0
 
 
-@pytest.mark.parametrize("prec,tol", [(G.PREC_FP64, 1e-12), (G.PREC_FP32, 1e-5)])
+@pytest.mark.parametrize("prec,tol", [(G.PREC_FP64, 1e-12), (G.PREC_FP32, 3e-8)])
 def test_content_conservation(channel_seamount, prec, tol):
-    """Rigid lid (w = 0 at the surface), linfs: sum T*hnode_new*areasvol is conserved."""
+    """Rigid lid (w = 0 at the surface), linfs: sum T*hnode_new*areasvol is conserved over 5
+    steps, FP64 to round-off; FP32 to the rounding of FP32 storage (increments of the vertical
+    diffusion below half an ulp of the stored value are lost, with the same sign over most
+    columns: measured -6.2e-9 for T, -5.6e-10 for S; the bound leaves a factor 5)."""
     mesh = channel_seamount
     f, tr = _setup(mesh, "channel", surface_w_zero=True)
     cfgs = [G.tra_cfg(id=1), G.tra_cfg(id=2)]
@@ -404,3 +407,36 @@ def test_device_pointers_give_the_host_results(channel_seamount):
     torch.cuda.synchronize()
     assert np.array_equal(z_d.cpu().numpy(), want_z)
     assert np.array_equal(v_d.cpu().numpy(), want_v)
+
+
+def test_autotune_keeps_the_state_and_the_results(sphere_small):
+    """fesom_gpu_autotune: the chosen settings are among the candidates, the tracer state after
+    tuning is the state before it bit for bit, and steps under the chosen settings agree with
+    steps under the defaults to FP32 round-off (the kernel variants are separate compilations)."""
+    mesh = sphere_small
+    f, tr = _setup(mesh, "sphere", ntr=12)
+    cfgs = [G.tra_cfg(id=k + 1) for k in range(12)]
+    ctxs = []
+    for tune in (False, True):
+        ctx = G.Context(mesh, G.PREC_FP32, max_tracers=12)
+        ctx.state_setup(cfgs)
+        ctx.forcing_upload(f)
+        for k in range(12):
+            ctx.tracer_upload(k, tr[k].astype(np.float32), tr[k].astype(np.float32))
+        if tune:
+            before = [ctx.tracer_download(k, dtype=np.float32) for k in range(12)]
+            res = ctx.autotune(f.dt, steps=1)
+            assert res["candidates"] >= 2 and res["tuned_ms"] <= res["default_ms"]
+            assert all(b in (0, 2, 4) for b in res["blocks_per_sm"])
+            assert all(t in (0, 8) for t in res["stage_tracers"]) and res["variant"][1] == 0
+            for k in range(12):
+                v, o = ctx.tracer_download(k, dtype=np.float32)
+                assert np.array_equal(v, before[k][0]) and np.array_equal(o, before[k][1])
+        ctx.run_steps(f.dt, 2)
+        ctxs.append(ctx)
+    wet = wet_mask(mesh)
+    for k in range(12):
+        a = ctxs[0].tracer_download(k)[0][wet]
+        b = ctxs[1].tracer_download(k)[0][wet]
+        assert np.abs(a - b).max() <= 1e-6 * np.abs(a).max(), k
+    assert ctxs[1].status() == 0
