@@ -91,11 +91,12 @@ def algorithmic_bytes(counts, ntr, s):
 
 
 # DRAM bytes (read + write) per tracer-DOF of each FP32 stage, measured with one ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum) of `--profile-only --scale 0.1 --tracers 6`
-# (sphere of 7 subdivisions, 6 tracers per launch as in the bounds and update passes of the
-# full workload; inputs far above L2); the traffic of a full-size launch is this figure times
-# the tracer-DOF it processes
-MEASURED_DRAM_B_PER_TRACER_DOF = {"update": 52.90, "bounds": 52.39, "edge_flux": 32.78, "lo_ad": 29.43}
+# (dram__bytes_read.sum + dram__bytes_write.sum) of `--profile-only --scale 0.1 --tracers 12`
+# (sphere of 7 subdivisions, 12 tracers in one launch per stage as in the full workload; inputs
+# far above L2); the traffic of a full-size launch is this figure times the tracer-DOF it
+# processes
+MEASURED_DRAM_B_PER_TRACER_DOF = {"update": 50.88, "bounds": 47.54, "edge_flux": 23.84, "lo_ad": 21.41,
+                                  "vdiff": 9.39}
 
 
 def stage_bytes(counts, ntr, s, ab=2, form="fp32"):

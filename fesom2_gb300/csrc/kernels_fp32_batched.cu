@@ -66,6 +66,10 @@ namespace fesom {
 
 namespace {
 
+// packed FP32 pairs (two slots per instruction) in the edge kernel's arithmetic
+#ifndef FESOM_PACKED_PAIRS
+#define FESOM_PACKED_PAIRS 1
+#endif
 constexpr int kWB = 8;                // warps (= nodes) per block
 constexpr int kTB = 32 * kWB;
 constexpr unsigned kFull = 0xffffffffu;
@@ -479,6 +483,85 @@ __device__ __forceinline__ float ver_ad(int ver, bool lim, float pv, int nz, int
     return lim ? F : F - fv0;
 }
 
+// Packed FP32 pairs: two slots of a group in one instruction (Blackwell's two-wide FP32 add,
+// multiply and fused multiply-add).  Each element rounds as the scalar
+// operation does; a - b is formed as fma(b, -1, a), which rounds once, like the subtraction.
+__device__ __forceinline__ float2 pk(float x) { return make_float2(x, x); }
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+template <int G>
+__device__ __forceinline__ float2 pr(const Vec<G> &a, int j) {
+    return make_float2(a.c[2 * j], a.c[2 * j + 1]);
+}
+
+// The per-group arithmetic of k32_lo_ad for two slots at once: the AB value, the upwind
+// vertical flux with w_e, LO from the edge-flux sum hs, and the vertical antidiffusive flux
+// (ver_ad's branches, taken per lane and group, so both slots of a pair share them).
+template <bool WS>
+__device__ __forceinline__ void lo_ad_pair(const DForcing<float> &f, int ab, int ver, bool lim, bool lvt, float2 pv,
+                                           int nz, int nzmin, int nzmax, bool twolayer, float ar0, float we0, float w0,
+                                           float sdt, float dhr, float idz0, float idzp, float idzm, float g1,
+                                           float g2, float2 tn, float2 o1, float2 o2, float2 hs, float2 &lo,
+                                           float2 &ad) {
+    float2 tab = tn;
+    if (lvt)
+        tab = ab == 2 ? pfma(pk(0.6f), psub(tn, o1), tn)
+                      : pfma(pfma(pk(11.f), psub(tn, o1), pmul(pk(-5.f), psub(o1, o2))), pk(1.f / 12.f), tn);
+    const float2 Tu = make_float2(sh_up(tn.x, 1), sh_up(tn.y, 1));
+    const float2 tabu = make_float2(sh_up(tab.x, 1), sh_up(tab.y, 1));
+    const float2 tabu2 = make_float2(sh_up(tab.x, 2), sh_up(tab.y, 2));
+    const float2 tabd = make_float2(sh_dn(tab.x, 1), sh_dn(tab.y, 1));
+    float2 fv0 = pk(0.f);
+    if (lvt) {
+        if (nz == nzmin) {
+            fv0 = pmul(tn, pk(-(we0 * ar0)));
+        } else {
+            const float aw = fabsf(we0);
+            fv0 = pmul(pfma(tn, pk(we0 + aw), pmul(Tu, pk(we0 - aw))), pk(-0.5f * ar0));
+        }
+    }
+    float2 fv1 = make_float2(sh_dn(fv0.x, 1), sh_dn(fv0.y, 1));
+    if (nz == nzmax - 1) fv1 = pk(0.f);
+    lo = padd(tn, pfma(tn, pk(dhr), pmul(padd(hs, psub(fv0, fv1)), pk(sdt))));
+    float2 fw0 = fv0;
+    if (WS && f.wsplit && lvt) {
+        if (nz == nzmin) {
+            fw0 = pmul(tn, pk(-(w0 * ar0)));
+        } else {
+            const float aw = fabsf(w0);
+            fw0 = pmul(pfma(tn, pk(w0 + aw), pmul(Tu, pk(w0 - aw))), pk(-0.5f * ar0));
+        }
+    }
+    const float pw = lim ? w0 : we0;
+    float2 Cf;
+    if (nz == nzmin) {
+        Cf = pmul(tab, pk(-(pw * ar0)));
+    } else if (ver != 0 || nz == nzmin + 1 || nz == nzmax - 1) {
+        if (ver != 1) {
+            Cf = pmul(padd(tabu, tab), pk(-0.5f * pw * ar0));
+        } else {
+            const float aw = fabsf(pw);
+            Cf = pmul(pfma(tab, pk(pw + aw), pmul(tabu, pk(pw - aw))), pk(-0.5f * ar0));
+        }
+    } else {
+        const float2 qc = pmul(psub(tabu, tab), pk(idz0));
+        const float2 qu = pmul(psub(tab, tabd), pk(idzp));
+        const float2 qd = pmul(psub(tabu2, tabu), pk(idzm));
+        const float2 Tm1 = pfma(pfma(pk(2.f), qc, qu), pk(g1), tab);
+        const float2 Tm2 = pfma(pfma(pk(2.f), qc, qd), pk(g2), tabu);
+        const float aw = fabsf(pw);
+        const float2 Tmean = pfma(pk(pw + aw), Tm1, pmul(pk(pw - aw), Tm2));
+        // (-(0.5 (1 - pv) Tmean) - pv (0.5 (Tm1 + Tm2)) pw) ar0
+        const float2 a1 = pmul(pk(-0.5f), psub(pk(1.f), pv)), a2 = pmul(pk(-0.5f * pw), pv);
+        Cf = pmul(pfma(a1, Tmean, pmul(a2, padd(Tm1, Tm2))), pk(ar0));
+    }
+    float2 F = lim ? psub(Cf, fw0) : Cf;
+    if (ver == 0 && twolayer && nz == nzmin + 1) F = psub(Cf, F);
+    ad = lim ? F : psub(F, fv0);
+}
+
 // ---------------------------------------------------------------------------
 // k32_lo_ad
 // ---------------------------------------------------------------------------
@@ -559,6 +642,23 @@ __device__ __forceinline__ void lo_ad_chunk(const DTopo &tp, const DGeom<float> 
 #pragma unroll
         for (int u = 0; u < KD; u++) tm[u] = vldc<G>(lvt, T, off[u]);
         Vec<G> lo, ad;
+#if FESOM_PACKED_PAIRS
+#pragma unroll
+        for (int j = 0; j < G / 2; j++) {
+            const float2 tn = pr(Tn, j);
+            float2 hs = pk(0.f);
+#pragma unroll
+            for (int u = 0; u < KD; u++) hs = padd(hs, padd(pmul(tn, pk(pq[u])), pmul(pr(tm[u], j), pk(qq[u]))));
+            float2 l2, a2;
+            lo_ad_pair<WS>(f, B.ab, ver, lim, lvt, make_float2(B.pv[gi * G + 2 * j], B.pv[gi * G + 2 * j + 1]), nz,
+                           nzmin, nzmax, twolayer, ar0, we0, w0, sdt, dhr, idz0, idzp, idzm, g1, g2, tn, pr(o1, j),
+                           pr(o2, j), hs, l2, a2);
+            lo.c[2 * j] = l2.x;
+            lo.c[2 * j + 1] = l2.y;
+            ad.c[2 * j] = a2.x;
+            ad.c[2 * j + 1] = a2.y;
+        }
+#else
 #pragma unroll
         for (int c = 0; c < G; c++) {
             const float tn = Tn.c[c];
@@ -599,6 +699,7 @@ __device__ __forceinline__ void lo_ad_chunk(const DTopo &tp, const DGeom<float> 
             ad.c[c] = ver_ad(ver, lim, B.pv[gi * G + c], nz, nzmin, nzmax, twolayer, tab, tabu, tabu2, tabd,
                              lim ? w0 : we0, ar0, fv0, fw0, idz0, idzp, idzm, g1, g2);
         }
+#endif
         if (k.out && on) {
             vst<G>(grp<G>(B.LO, gi, B.sN), i, lo);
             // PPM fluxes come from k32_vppm
@@ -684,6 +785,31 @@ __device__ __forceinline__ void lo_ad_chunk_pf(const DTopo &tp, const DGeom<floa
         const Vec<G> Tn = lds<G>(stg<G>(buf, 0, lane));
         const Vec<G> o1 = lds<G>(stg<G>(buf, 1, lane));
         const Vec<G> o2 = lds<G>(stg<G>(buf, 2, lane));
+#if FESOM_PACKED_PAIRS
+        Vec<G> lo, ad;
+        float2 hsp[G / 2];
+#pragma unroll
+        for (int j = 0; j < G / 2; j++) hsp[j] = pk(0.f);
+#pragma unroll
+        for (int u = 0; u < KD; u++) {
+            const Vec<G> tm = lds<G>(stg<G>(buf, 3 + u, lane));
+#pragma unroll
+            for (int j = 0; j < G / 2; j++)
+                hsp[j] = padd(hsp[j], padd(pmul(pr(Tn, j), pk(pq[u])), pmul(pr(tm, j), pk(qq[u]))));
+        }
+#pragma unroll
+        for (int j = 0; j < G / 2; j++) {
+            const float2 tn = pr(Tn, j), hs = hsp[j];
+            float2 l2, a2;
+            lo_ad_pair<WS>(f, B.ab, ver, lim, lvt, make_float2(B.pv[gi * G + 2 * j], B.pv[gi * G + 2 * j + 1]), nz,
+                           nzmin, nzmax, twolayer, ar0, we0, w0, sdt, dhr, idz0, idzp, idzm, g1, g2, tn, pr(o1, j),
+                           pr(o2, j), hs, l2, a2);
+            lo.c[2 * j] = l2.x;
+            lo.c[2 * j + 1] = l2.y;
+            ad.c[2 * j] = a2.x;
+            ad.c[2 * j + 1] = a2.y;
+        }
+#else
         Vec<G> hs = vfill<G>(0.f);
 #pragma unroll
         for (int u = 0; u < KD; u++) {
@@ -723,6 +849,7 @@ __device__ __forceinline__ void lo_ad_chunk_pf(const DTopo &tp, const DGeom<floa
             ad.c[c] = ver_ad(ver, lim, B.pv[gi * G + c], nz, nzmin, nzmax, twolayer, tab, tabu, tabu2, tabd,
                              lim ? w0 : we0, ar0, fv0, fw0, idz0, idzp, idzm, g1, g2);
         }
+#endif
         if (k.out && on) {
             vst<G>(grp<G>(B.LO, gi, B.sN), i, lo);
             if (ver != 3) vst<G>(grp<G>(B.ADv, gi, B.sNI), iv, ad);
@@ -832,6 +959,30 @@ __device__ __forceinline__ float ho_minus_lo(int hor, float ph, int ab, float T1
     return hf - flo;
 }
 
+// hor, ab uniform over the pair; q1 = 1 - ph, q2 = v ph / 2 per slot; vp, vm the upwind parts of v
+__device__ __forceinline__ float2 ho_minus_lo2(int hor, int ab, float2 q1, float2 q2, float2 T1, float2 T2,
+                                               float2 o1a, float2 o1b, float2 o2a, float2 o2b, float2 s1,
+                                               float2 s2, float vp, float vm, float cl1, float cl2) {
+    float2 t1, t2;
+    if (ab == 2) {
+        t1 = pfma(pk(0.6f), psub(T1, o1a), T1);
+        t2 = pfma(pk(0.6f), psub(T2, o1b), T2);
+    } else {
+        t1 = pfma(pfma(pk(11.f), psub(T1, o1a), pmul(pk(-5.f), psub(o1a, o2a))), pk(1.f / 12.f), T1);
+        t2 = pfma(pfma(pk(11.f), psub(T2, o1b), pmul(pk(-5.f), psub(o1b, o2b))), pk(1.f / 12.f), T2);
+    }
+    // minus the LO flux: + (T1 v+ + T2 v-), both products rounded, then summed
+    const float2 lo = padd(pmul(T1, pk(vp)), pmul(T2, pk(vm)));
+    if (hor == 2) return psub(lo, padd(pmul(t1, pk(vp)), pmul(t2, pk(vm))));
+    const float clo1 = hor == 0 ? cl1 : 1.f, clo2 = hor == 0 ? cl2 : 1.f;
+    const float2 d2 = pmul(pk(2.f), psub(t2, t1));
+    const float2 Tm2 = pfma(pmul(padd(d2, s2), pk(1.f / 6.f)), pk(-clo2), t2);
+    const float2 Tm1 = pfma(pmul(padd(d2, s1), pk(1.f / 6.f)), pk(clo1), t1);
+    // hf = -(1 - ph) (v+ Tm1 + v- Tm2) - (v ph / 2) (Tm1 + Tm2)
+    const float2 c = pfma(pk(vp), Tm1, pmul(pk(vm), Tm2));
+    return psub(lo, pfma(q1, c, pmul(q2, padd(Tm1, Tm2))));
+}
+
 // ---------------------------------------------------------------------------
 // k32_ho: high-order minus low-order flux of every edge-layer
 // ---------------------------------------------------------------------------
@@ -886,6 +1037,21 @@ __device__ __forceinline__ void ho_pass(const DTopo &tp, const B32View &B, const
         const Vec<G> ga = vldc<G>(grad, T, ua), gb = vldc<G>(grad, T, ub);
         const Vec<G> gc = vldc<G>(grad, T, da), gd = vldc<G>(grad, T, db);
         Vec<G> out;
+#if FESOM_PACKED_PAIRS
+        const float vp = fmaxf(v, 0.f), vm = fminf(v, 0.f);
+#pragma unroll
+        for (int j = 0; j < G / 2; j++) {
+            const float2 ph = make_float2(B.ph[gq * G + 2 * j], B.ph[gq * G + 2 * j + 1]);
+            const float2 q1 = psub(pk(1.f), ph), q2 = pmul(pk(0.5f * v), ph);
+            const float2 t1 = pr(T1, j), t2 = pr(T2, j);
+            const float2 s1 = pfma(pk(wu.y), psub(pr(ga, j), t1), pmul(pk(wu.z), psub(pr(gb, j), t1)));
+            const float2 s2 = pfma(pk(wd.y), psub(pr(gc, j), t2), pmul(pk(wd.z), psub(pr(gd, j), t2)));
+            const float2 r = ho_minus_lo2(hor, B.ab, q1, q2, t1, t2, pr(o1a, j), pr(o1b, j), pr(o2a, j), pr(o2b, j),
+                                          s1, s2, vp, vm, cl1, cl2);
+            out.c[2 * j] = r.x;
+            out.c[2 * j + 1] = r.y;
+        }
+#else
 #pragma unroll
         for (int c = 0; c < G; c++) {
             const float s1 = wu.y * (ga.c[c] - T1.c[c]) + wu.z * (gb.c[c] - T1.c[c]);
@@ -893,6 +1059,7 @@ __device__ __forceinline__ void ho_pass(const DTopo &tp, const B32View &B, const
             out.c[c] = ho_minus_lo(hor, B.ph[gq * G + c], B.ab, T1.c[c], T2.c[c], o1a.c[c], o1b.c[c], o2a.c[c],
                                    o2b.c[c], s1, s2, v, cl1, cl2);
         }
+#endif
         vst<G>(grp<G>(B.ADh, gq, B.sE), ie, out);
     }
 }
