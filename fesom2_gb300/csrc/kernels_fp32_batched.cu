@@ -66,6 +66,12 @@ namespace fesom {
 
 namespace {
 
+// the FCT clamp of the advected value into its stored bounds (k32_bounds writes them,
+// k32_update reads them)
+#ifndef FESOM_FCT_CLAMP
+#define FESOM_FCT_CLAMP 1
+#endif
+constexpr bool kFctClamp = FESOM_FCT_CLAMP != 0;
 // packed FP32 pairs (two slots per instruction) in the edge kernel's arithmetic
 #ifndef FESOM_PACKED_PAIRS
 #define FESOM_PACKED_PAIRS 1
@@ -1240,8 +1246,10 @@ __device__ __forceinline__ void bounds_chunk(const DTopo &tp, const DGeom<float>
         if (k.out && gq >= 0) {
             vst<G>(grp<G>(B.Rp, gq, B.sN), i, rp);
             vst<G>(grp<G>(B.Rm, gq, B.sN), i, rm);
-            vst<G>(grp<G>(B.Bp, gq, B.sN), i, bp);
-            vst<G>(grp<G>(B.Bm, gq, B.sN), i, bm);
+            if (kFctClamp) {
+                vst<G>(grp<G>(B.Bp, gq, B.sN), i, bp);
+                vst<G>(grp<G>(B.Bm, gq, B.sN), i, bm);
+            }
         }
     }
 }
@@ -1353,8 +1361,10 @@ __device__ __forceinline__ void bounds_chunk_pf(const DTopo &tp, const DGeom<flo
         if (k.out && gq >= 0) {
             vst<G>(grp<G>(B.Rp, gq, B.sN), i, rp);
             vst<G>(grp<G>(B.Rm, gq, B.sN), i, rm);
-            vst<G>(grp<G>(B.Bp, gq, B.sN), i, bp);
-            vst<G>(grp<G>(B.Bm, gq, B.sN), i, bm);
+            if (kFctClamp) {
+                vst<G>(grp<G>(B.Bp, gq, B.sN), i, bp);
+                vst<G>(grp<G>(B.Bm, gq, B.sN), i, bm);
+            }
         }
     };
     int gq;
@@ -1470,8 +1480,8 @@ __device__ __forceinline__ void update_chunk(const DTopo &tp, const DGeom<float>
         const Vec<G> f0 = vldc<G>(lv, grp<G>(B.ADv, gc, B.sNI), iv);
         const Vec<G> r0p = lf ? vld<G>(Rp, i) : vfill<G>(1.f);
         const Vec<G> r0m = lf ? vld<G>(Rm, i) : vfill<G>(1.f);
-        const Vec<G> tbp = vldc<G>(lf, grp<G>(B.Bp, gc, B.sN), i);
-        const Vec<G> tbm = vldc<G>(lf, grp<G>(B.Bm, gc, B.sN), i);
+        const Vec<G> tbp = vldc<G>(lf && kFctClamp, grp<G>(B.Bp, gc, B.sN), i);
+        const Vec<G> tbm = vldc<G>(lf && kFctClamp, grp<G>(B.Bm, gc, B.sN), i);
         // the diffusion increment k32_diff parked in Tnew (the limiter acts on advection only)
         const Vec<G> dd = vldc<G>(lv && dif, Tn, i);
         Vec<G> hs = vfill<G>(0.f);
@@ -1508,7 +1518,7 @@ __device__ __forceinline__ void update_chunk(const DTopo &tp, const DGeom<float>
             // T* = T + (del_ttf + T (hnode - hnode_new)) / hnode_new = LO + fluxes dt / areasvol / hnode_new
             // (oce_adv_tra_driver.F90:535-620, oce_ale_tracer.F90:319-321, 743-754)
             float val = lo.c[c] + ((fz - f1) + hs.c[c]) * sdt;
-            if (k.out && on && fct) {
+            if (kFctClamp && k.out && on && fct) {
                 const float vc = fminf(fmaxf(val, tbm.c[c]), tbp.c[c]);
                 // a clamp beyond round-off means the limiter itself failed
                 if (fabsf(vc - val) > 1e-5f * (tbp.c[c] - tbm.c[c]) + 1e-6f * fabsf(vc)) atomicOr(B.status, 2u);
@@ -1569,8 +1579,8 @@ __device__ __forceinline__ void update_chunk_pf(const DTopo &tp, const DGeom<flo
         cpa<G>(stg<G>(buf, 1, lane), grp<G>(B.ADv, gc, B.sNI) + (size_t)(lv ? iv : 0) * G, lv);
         cpa<G>(stg<G>(buf, 2, lane), Rp + (size_t)ii * G, lf);
         cpa<G>(stg<G>(buf, 3, lane), Rm + (size_t)ii * G, lf);
-        cpa<G>(stg<G>(buf, 4, lane), grp<G>(B.Bp, gc, B.sN) + (size_t)ii * G, lf);
-        cpa<G>(stg<G>(buf, 5, lane), grp<G>(B.Bm, gc, B.sN) + (size_t)ii * G, lf);
+        cpa<G>(stg<G>(buf, 4, lane), grp<G>(B.Bp, gc, B.sN) + (size_t)ii * G, lf && kFctClamp);
+        cpa<G>(stg<G>(buf, 5, lane), grp<G>(B.Bm, gc, B.sN) + (size_t)ii * G, lf && kFctClamp);
         cpa<G>(stg<G>(buf, 6, lane), grp<G>(B.Tnew, gc, B.sN) + (size_t)ii * G, ld);
 #pragma unroll
         for (int u = 0; u < KD; u++) {
@@ -1624,7 +1634,7 @@ __device__ __forceinline__ void update_chunk_pf(const DTopo &tp, const DGeom<flo
             float f1 = sh_dn(fz, 1);
             if (nz == nzmax - 1) f1 = 0.f;
             float val = lo.c[c] + ((fz - f1) + hs.c[c]) * sdt;
-            if (k.out && on && fct) {
+            if (kFctClamp && k.out && on && fct) {
                 const float vc = fminf(fmaxf(val, tbm.c[c]), tbp.c[c]);
                 if (fabsf(vc - val) > 1e-5f * (tbp.c[c] - tbm.c[c]) + 1e-6f * fabsf(vc)) atomicOr(B.status, 2u);
                 val = vc;
@@ -2243,150 +2253,150 @@ __global__ void __launch_bounds__(kTB) k32_diff(DTopo tp, DGeom<float> g, B32Vie
 // ---------------------------------------------------------------------------
 // Forward substitution tp_k = inv_k rhs_k - a_k inv_k tp_{k-1} and back substitution
 // x_k = tp_k - cp_k x_{k+1} (oce_ale_tracer.F90:1406-1422) with the column's FP64-derived
-// factors, as scans of affine maps y -> A y + B over the lanes of each chunk with the carry
-// passed from chunk to chunk.  The multipliers A depend on the column only: their partial
-// products at each scan step are formed once per node into shared memory, so a slot's scan
-// step is one shuffle and one multiply-add; the G slots of a group are G interleaved scan
-// chains.  rhs_k = -a_k (T_{k-1} - T_k) - c_k (T_{k+1} - T_k) (+ bc_surface at the top,
-// :1216-1229, 1377-1383); T += x.
+// factors, as scans of affine maps y -> A y + B.  Each lane holds K consecutive levels of the
+// column (K = ceil(layers / 32): one warp covers the whole column): it composes its K maps in
+// registers, the warp scans the lane maps (five shuffles), and each lane then runs its K
+// levels from the carry it receives.  The multipliers A depend on the column only: the lane
+// products and their partial products at each scan step are formed once per node (shared
+// memory), so a slot's scan step is one shuffle and one multiply-add, and a column costs a slot
+// 14 shuffles whatever its depth.  rhs_k = -a_k (T_{k-1} - T_k) - c_k (T_{k+1} - T_k)
+// (+ bc_surface at the top, :1216-1229, 1377-1383); T += x.
 constexpr int kWV = 4;                    // warps (nodes) per block of the diffusion kernel
 constexpr int kScan = 5;                  // steps of a 32-lane scan
-constexpr int kVdiffMaxChunks = kMaxChunks;
+constexpr int kVdiffMaxK = 4;             // levels per lane: columns of up to 128 layers
 
 struct VdiffWarp {
-    float4 fac[130];                                  // (a, c, 1/m, c/m), 1-based levels
-    float af[kVdiffMaxChunks][kScan + 1][32];         // forward: A at each step (0 below the offset), then the total
-    float ab[kVdiffMaxChunks][kScan + 1][32];         // backward
+    float4 fac[130];                      // (a, c, 1/m, c/m), 1-based levels
+    float af[kScan][32];                  // forward: lane-map product of the window at each step (0 below the offset)
+    float ab[kScan][32];                  // backward (0 past the offset)
 };
 
-template <int NCH, int G>
+// per-lane column data of a node: the factors of the lane's K levels
+template <int K>
+struct VdiffLane {
+    float a[K], c[K], inv[K], A[K], Ad[K];
+    bool ok[K];
+};
+
+template <int K, int G>
 __device__ __forceinline__ void vdiff_group(const DTopo &tp, const B32View &B, int n, int lane, int nzmin, int nzmax,
-                                            int gq, VdiffWarp &W) {
-    using C = Chunk<1, 1>;
+                                            int gq, const VdiffLane<K> &V, const VdiffWarp &W) {
     const int L1 = tp.L1;
+    const int nz0 = nzmin + lane * K;  // the lane's first level
     float *__restrict__ Tg = grp<G>(B.Tnew, gq, B.sN);
     const Vec<G> bc = B.fsurf ? vld<G>(B.fsurf, gq * tp.N2 + n) : vfill<G>(0.f);
-    Vec<G> a[NCH], y[NCH];
+    Vec<G> a[K], y[K];
 #pragma unroll
-    for (int ch = 0; ch < NCH; ch++) {
-        const C k(nzmin, nzmax, ch, lane);
-        a[ch] = vldc<G>(k.lvl, Tg, n * L1 + k.nz - 1);
-    }
+    for (int t = 0; t < K; t++) a[t] = vldc<G>(V.ok[t], Tg, n * L1 + nz0 + t - 1);
 #pragma unroll
-    for (int ch = 0; ch < NCH; ch++) {
-        const C k(nzmin, nzmax, ch, lane);
-        const int nz = k.nz;
-        Vec<G> b;
-        const float4 fz = k.out ? W.fac[nz] : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int c = 0; c < G; c++) {
+        // the levels next to the lane's ends come from the neighbouring lanes
+        const float up = sh_up(a[K - 1].c[c], 1), dn = sh_dn(a[0].c[c], 1);
+        float bl = 0.f;  // the lane's composed forward map applied to 0
 #pragma unroll
-        for (int c = 0; c < G; c++) {
-            const float u = sh_up(a[ch].c[c], 1), d = sh_dn(a[ch].c[c], 1);
+        for (int t = 0; t < K; t++) {
+            const int nz = nz0 + t;
+            const float tu = t > 0 ? a[t - 1].c[c] : up, td = t < K - 1 ? a[t + 1].c[c] : dn;
+            const float tc = a[t].c[c];
             float r = 0.f;
-            if (nz > nzmin) r -= fz.x * (u - a[ch].c[c]);
-            if (nz < nzmax - 1) r -= fz.y * (d - a[ch].c[c]);
+            if (nz > nzmin) r -= V.a[t] * (tu - tc);
+            if (nz < nzmax - 1) r -= V.c[t] * (td - tc);
             if (nz == nzmin) r += bc.c[c];
-            b.c[c] = k.out ? r * fz.z : 0.f;
+            y[t].c[c] = V.ok[t] ? r * V.inv[t] : 0.f;
+            bl = fmaf(V.A[t], bl, y[t].c[c]);
         }
+        // inclusive scan of the lane maps: bl = tp at the lane's last level
 #pragma unroll
-        for (int s = 0, off = 1; s < kScan; s++, off <<= 1) {
-            const float w = W.af[ch][s][lane];
+        for (int s = 0, off = 1; s < kScan; s++, off <<= 1) bl = fmaf(W.af[s][lane], __shfl_up_sync(kFull, bl, off), bl);
+        float yv = __shfl_up_sync(kFull, bl, 1);
+        if (lane == 0) yv = 0.f;
 #pragma unroll
-            for (int c = 0; c < G; c++) b.c[c] = fmaf(w, __shfl_up_sync(kFull, b.c[c], off), b.c[c]);
+        for (int t = 0; t < K; t++) {
+            yv = fmaf(V.A[t], yv, y[t].c[c]);
+            y[t].c[c] = yv;
         }
-        y[ch] = b;
+        // back substitution: the lane's composed backward map, the suffix scan, the lane's levels
+        float xl = 0.f;
+#pragma unroll
+        for (int t = K - 1; t >= 0; t--) xl = fmaf(V.Ad[t], xl, y[t].c[c]);
+#pragma unroll
+        for (int s = 0, off = 1; s < kScan; s++, off <<= 1)
+            xl = fmaf(W.ab[s][lane], __shfl_down_sync(kFull, xl, off), xl);
+        float xv = __shfl_down_sync(kFull, xl, 1);
+        if (lane == 31) xv = 0.f;
+#pragma unroll
+        for (int t = K - 1; t >= 0; t--) {
+            xv = fmaf(V.Ad[t], xv, y[t].c[c]);
+            y[t].c[c] = a[t].c[c] + xv;
+        }
     }
-    Vec<G> cr = vfill<G>(0.f);
 #pragma unroll
-    for (int ch = 0; ch < NCH; ch++) {
-        const float w = W.af[ch][kScan][lane];
-#pragma unroll
-        for (int c = 0; c < G; c++) {
-            y[ch].c[c] = fmaf(w, cr.c[c], y[ch].c[c]);
-            cr.c[c] = __shfl_sync(kFull, y[ch].c[c], 30);  // last stored lane (Chunk<1, 1>)
-        }
-    }
-#pragma unroll
-    for (int ch = 0; ch < NCH; ch++) {
-        const C k(nzmin, nzmax, ch, lane);
-        Vec<G> b;
-#pragma unroll
-        for (int c = 0; c < G; c++) b.c[c] = k.out ? y[ch].c[c] : 0.f;
-#pragma unroll
-        for (int s = 0, off = 1; s < kScan; s++, off <<= 1) {
-            const float w = W.ab[ch][s][lane];
-#pragma unroll
-            for (int c = 0; c < G; c++) b.c[c] = fmaf(w, __shfl_down_sync(kFull, b.c[c], off), b.c[c]);
-        }
-        y[ch] = b;
-    }
-    cr = vfill<G>(0.f);
-#pragma unroll
-    for (int ch = NCH - 1; ch >= 0; ch--) {
-        const C k(nzmin, nzmax, ch, lane);
-        const float w = W.ab[ch][kScan][lane];
-        Vec<G> o;
+    for (int t = 0; t < K; t++) {
+        if (!V.ok[t]) continue;
         bool fin = true;
 #pragma unroll
-        for (int c = 0; c < G; c++) {
-            const float x = fmaf(w, cr.c[c], y[ch].c[c]);
-            cr.c[c] = __shfl_sync(kFull, x, 1);  // first stored lane (Chunk<1, 1>)
-            o.c[c] = a[ch].c[c] + x;
-            fin = fin && isfinite(o.c[c]);
-        }
-        if (k.out) {
-            vst<G>(Tg, n * L1 + k.nz - 1, o);
-            if (!fin) atomicOr(B.status, 1u);
-        }
+        for (int c = 0; c < G; c++) fin = fin && isfinite(y[t].c[c]);
+        vst<G>(Tg, n * L1 + nz0 + t - 1, y[t]);
+        if (!fin) atomicOr(B.status, 1u);
     }
 }
 
-template <int G>
-__device__ __forceinline__ void vdiff_unit(const DTopo &tp, const B32View &B, const VFactors &vf, int n,
+template <int K, int G>
+__device__ __forceinline__ void vdiff_node(const DTopo &tp, const B32View &B, int n, int lane, int nzmin, int nzmax,
                                            VdiffWarp &W) {
-    using C = Chunk<1, 1>;
-    const int lane = threadIdx.x & 31;
-    if (n >= tp.N2) return;
-    const int L1 = tp.L1;
-    const int nzmin = tp.n_ulev[n], nzmax = tp.n_nlev[n];
-    const int nch = C::count(nzmin, nzmax);
-    __syncwarp();  // the previous node's reads of W are done
-    for (int nz = nzmin + lane; nz <= nzmax - 1; nz += 32) {
-        const int i = n * L1 + nz - 1;
-        W.fac[nz] = make_float4(vf.a[i], vf.c[i], vf.inv[i], vf.cp[i]);
-    }
-    __syncwarp();
-    // the column's scan multipliers
-    for (int ch = 0; ch < nch; ch++) {
-        const C k(nzmin, nzmax, ch, lane);
-        float A = 1.f, Ad = 1.f;
-        if (k.out) {
-            const float4 fz = W.fac[k.nz];
-            A = -(fz.x * fz.z);
-            Ad = -fz.w;
-        }
+    VdiffLane<K> V;
+    float A = 1.f, Ad = 1.f;
 #pragma unroll
-        for (int s = 0, off = 1; s < kScan; s++, off <<= 1) {
-            W.af[ch][s][lane] = lane >= off ? A : 0.f;
-            W.ab[ch][s][lane] = lane + off < 32 ? Ad : 0.f;
-            const float Ap = __shfl_up_sync(kFull, A, off), An = __shfl_down_sync(kFull, Ad, off);
-            if (lane >= off) A *= Ap;
-            if (lane + off < 32) Ad *= An;
-        }
-        W.af[ch][kScan][lane] = A;
-        W.ab[ch][kScan][lane] = Ad;
+    for (int t = 0; t < K; t++) {
+        const int nz = nzmin + lane * K + t;
+        V.ok[t] = nz <= nzmax - 1;
+        const float4 fz = V.ok[t] ? W.fac[nz] : make_float4(0.f, 0.f, 0.f, 0.f);
+        V.a[t] = fz.x;
+        V.c[t] = fz.y;
+        V.inv[t] = fz.z;
+        // levels past the column's end are identity maps
+        V.A[t] = V.ok[t] ? -(fz.x * fz.z) : 1.f;
+        V.Ad[t] = V.ok[t] ? -fz.w : 1.f;
+        A *= V.A[t];
+        Ad *= V.Ad[t];
+    }
+    // partial products of the lane maps at each scan step
+#pragma unroll
+    for (int s = 0, off = 1; s < kScan; s++, off <<= 1) {
+        W.af[s][lane] = lane >= off ? A : 0.f;
+        W.ab[s][lane] = lane + off < 32 ? Ad : 0.f;
+        const float Ap = __shfl_up_sync(kFull, A, off), An = __shfl_down_sync(kFull, Ad, off);
+        if (lane >= off) A *= Ap;
+        if (lane + off < 32) Ad *= An;
     }
     __syncwarp();
     unsigned long long todo = (B.ivd & ~B.wimpl) & (B.ng >= 64 ? ~0ull : ((1ull << B.ng) - 1));
     while (todo) {
         const int gq = __ffsll((long long)todo) - 1;
         todo &= todo - 1;
-        switch (nch) {
-            case 1: vdiff_group<1, G>(tp, B, n, lane, nzmin, nzmax, gq, W); break;
-            case 2: vdiff_group<2, G>(tp, B, n, lane, nzmin, nzmax, gq, W); break;
-            case 3: vdiff_group<3, G>(tp, B, n, lane, nzmin, nzmax, gq, W); break;
-            case 4: vdiff_group<4, G>(tp, B, n, lane, nzmin, nzmax, gq, W); break;
-            default: vdiff_group<5, G>(tp, B, n, lane, nzmin, nzmax, gq, W); break;
-        }
+        vdiff_group<K, G>(tp, B, n, lane, nzmin, nzmax, gq, V, W);
+    }
+}
+
+template <int G>
+__device__ __forceinline__ void vdiff_unit(const DTopo &tp, const B32View &B, const VFactors &vf, int n,
+                                           VdiffWarp &W) {
+    const int lane = threadIdx.x & 31;
+    if (n >= tp.N2) return;
+    const int L1 = tp.L1;
+    const int nzmin = tp.n_ulev[n], nzmax = tp.n_nlev[n];
+    const int K = (nzmax - nzmin + 31) / 32;
+    __syncwarp();  // the previous node's reads of W are done
+    for (int nz = nzmin + lane; nz <= nzmax - 1; nz += 32) {
+        const int i = n * L1 + nz - 1;
+        W.fac[nz] = make_float4(vf.a[i], vf.c[i], vf.inv[i], vf.cp[i]);
+    }
+    __syncwarp();
+    switch (K) {
+        case 1: vdiff_node<1, G>(tp, B, n, lane, nzmin, nzmax, W); break;
+        case 2: vdiff_node<2, G>(tp, B, n, lane, nzmin, nzmax, W); break;
+        case 3: vdiff_node<3, G>(tp, B, n, lane, nzmin, nzmax, W); break;
+        default: vdiff_node<4, G>(tp, B, n, lane, nzmin, nzmax, W); break;
     }
 }
 
