@@ -64,7 +64,7 @@ def parse():
     p.add_argument("--width", type=int, default=0, help="FP32 tracer-group width (0: automatic, 2, 4)")
     p.add_argument("--stage-tr", default="", help="tracers per launch of lo_ad,ho,bounds,update (e.g. 8,0,8,8)")
     p.add_argument("--shape", default="", help="blocks per SM of lo_ad,ho,bounds,update (0: one warp per unit)")
-    p.add_argument("--variant", default="", help="kernel variant of lo_ad,bounds,update (0 registers, 1 staged)")
+    p.add_argument("--variant", default="", help="kernel variant of lo_ad,ho,bounds,update (0 registers, 1 staged)")
     return p.parse_args()
 
 
@@ -95,8 +95,8 @@ def algorithmic_bytes(counts, ntr, s):
 # (sphere of 7 subdivisions, 12 tracers in one launch per stage as in the full workload; inputs
 # far above L2); the traffic of a full-size launch is this figure times the tracer-DOF it
 # processes
-MEASURED_DRAM_B_PER_TRACER_DOF = {"update": 50.88, "bounds": 47.54, "edge_flux": 23.84, "lo_ad": 21.41,
-                                  "vdiff": 9.39}
+MEASURED_DRAM_B_PER_TRACER_DOF = {"update": 39.88, "bounds": 37.85, "edge_flux": 23.86, "lo_ad": 21.41,
+                                  "vdiff": 9.35}
 
 
 def stage_bytes(counts, ntr, s, ab=2, form="fp32"):
@@ -109,10 +109,11 @@ def stage_bytes(counts, ntr, s, ab=2, form="fp32"):
       lo_ad:     per tracer read T and the previous levels (ab N3); write LO, ADv (2 N3);
                  shared VF (E3), w, w_e, area, Z, zbar, areasvol, hnode, hnode_new (8 N3)
       edge_flux: per tracer read T and the previous levels (ab N3); write ADh (E3); shared VF (E3)
-      bounds:    per tracer read T, LO, ADv (3 N3), ADh (E3); write R+, R- and the bounds
-                 T_up, T_lo (4 N3); shared hnode_new, areasvol (2 N3)
-      update:    per tracer read LO, ADv, R+, R-, T_up, T_lo (6 N3), ADh (E3); write T (N3);
-                 shared hnode_new, areasvol (2 N3)
+      bounds:    per tracer read T, LO, ADv (3 N3), ADh (E3); write R+, R- (2 N3); shared
+                 hnode_new, areasvol (2 N3)
+      update:    per tracer read LO, ADv, R+, R- (4 N3), ADh (E3); write T (N3); shared
+                 hnode_new, areasvol (2 N3)
+                 (a build with the FCT clamp also writes and reads the bounds: 2 N3 more each)
       vdiff:     per tracer read and write T (2 N3); shared factors (4 N3)
     FP64 plain form (per tracer, one tracer per launch):
       ab 4 N3; trxy N3 + 2 T3; edge_flux 2 N3 + 2 T3 + 2 E3 (+3 T3 shared); node_lo 3 N3 + E3
@@ -126,8 +127,8 @@ def stage_bytes(counts, ntr, s, ab=2, form="fp32"):
             "vfactors": s * 8 * N3,
             "lo_ad": s * (ntr * (ab + 2) * N3 + E3 + 8 * N3),
             "edge_flux": s * (ntr * (ab * N3 + E3) + E3),
-            "bounds": s * (ntr * (7 * N3 + E3) + 2 * N3),
-            "update": s * (ntr * (7 * N3 + E3) + 2 * N3),
+            "bounds": s * (ntr * (5 * N3 + E3) + 2 * N3),
+            "update": s * (ntr * (5 * N3 + E3) + 2 * N3),
             "vdiff": s * (ntr * 2 * N3 + 4 * N3),
         }
     return {
@@ -271,13 +272,39 @@ class HostPinned:
         self.held.clear()
 
 
+def host_link_gbs(stream, nbytes: int = 1 << 30, reps: int = 3) -> dict:
+    """Copy rate of the host link at this moment: `reps` copies of `nbytes` between a
+    page-locked host array and the device each way (GB/s, each copy timed with CUDA events)."""
+    import torch
+    pinned = HostPinned()
+    h = pinned.copy(np.zeros(nbytes // 4, np.float32), np.float32)
+    src = torch.from_numpy(h)
+    d = torch.empty(h.size, dtype=torch.float32, device="cuda")
+    out = {"h2d": [], "d2h": []}
+    with torch.cuda.stream(stream):
+        for _ in range(reps):
+            for way in ("h2d", "d2h"):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                if way == "h2d":
+                    d.copy_(src, non_blocking=True)
+                else:
+                    src.copy_(d, non_blocking=True)
+                e1.record(stream)
+                e1.synchronize()
+                out[way].append(round(nbytes / (e0.elapsed_time(e1) / 1e3) / 1e9, 1))
+    del d, src
+    pinned.release()
+    return out
+
+
 def apply_settings(ctx, args):
     """The FP32 performance settings given on the command line (results do not change)."""
     for k, v in enumerate(args.stage_tr.split(",") if args.stage_tr else []):
         ctx.set_stage_tracers(k, int(v))
     for k, v in enumerate(args.shape.split(",") if args.shape else []):
         ctx.set_launch_shape(k, int(v))
-    for k, v in zip((0, 2, 3), args.variant.split(",") if args.variant else []):
+    for k, v in enumerate(args.variant.split(",") if args.variant else []):
         ctx.set_stage_variant(k, int(v))
 
 
@@ -580,6 +607,7 @@ def run_ours(args, rank, world, local_rank):
     # ---------------- end to end through host buffers -----------------------
     if not args.no_e2e:
         L1 = mesh.nl - 1
+        link = host_link_gbs(stream)
         pinned = HostPinned()
         # (1) FP32 host arrays through fesom_gpu_step_host_f32
         ce = G.Context(mesh, G.PREC_FP32, max_tracers=ntr)
@@ -620,7 +648,8 @@ def run_ours(args, rank, world, local_rank):
         res["e2e"] = {"value": ntr * N3 * args.e2e_steps * world / (mse / 1e3), "unit": UNIT,
                       "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                       "ms_per_step": mse / args.e2e_steps, "api": "fesom_gpu_step_host_f32",
-                      "tracer_groups": ngr, "group_width": width}
+                      "tracer_groups": ngr, "group_width": width, "host_link_before": link,
+                      "host_link_after": host_link_gbs(stream)}
         # (2) FP64 host arrays, the reference's own layout and precision, through the call a
         # Fortran caller binds for the tracer loop (fesom_gpu_tracer_step, FP32 context):
         # values and valuesold in, both updated in place
@@ -691,6 +720,28 @@ def run_ours(args, rank, world, local_rank):
                               "error_vs_fp64_oracle_one_step": errs5, "clocks": line5.get("clocks")}
         except Exception as e:  # reported, not fatal: the headline is configuration 4
             res["config5"] = {"error": f"{type(e).__name__}: {e}"[:300]}
+        # configurations 1-3 (channel, seamount channel, small sphere): throughput, FP32 error
+        # against the FP64 GPU form after each of 5 steps, rigid-lid content drift
+        subs = {}
+        for cfg in (1, 2, 3):
+            try:
+                out = subprocess.run([sys.executable, os.path.abspath(__file__), "--config", str(cfg), "--steps", "10",
+                                      "--warmup", "3", "--no-cpu", "--no-e2e", "--no-config5", "--no-tune"],
+                                     capture_output=True, text=True, timeout=600)
+                ln = json.loads(out.stdout.strip().splitlines()[-1])
+                per = ln.get("error_fp32_vs_fp64_gpu_per_step", {})
+                subs[f"config{cfg}"] = {
+                    "workload": ln["config"]["workload"], "value": ln["value"], "unit": UNIT,
+                    "ms_per_step": ln["ms_per_step"], "steps": ln["steps"],
+                    "fp64_plain_value": ln.get("fp64_plain", {}).get("value"),
+                    "max_normwise_error_vs_fp64_gpu_per_step": [max(v["normwise"][j] for v in per.values())
+                                                                for j in range(5)] if per else None,
+                    "content_rigid_lid_max_abs_relative_drift_per_step":
+                        ln.get("content_rigid_lid", {}).get("max_abs_relative_drift_per_step"),
+                    "clocks": ln.get("clocks")}
+            except Exception as e:  # reported, not fatal
+                subs[f"config{cfg}"] = {"error": f"{type(e).__name__}: {e}"[:300]}
+        res["configs_1_3"] = subs
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -645,8 +645,9 @@ int alloc_state32(fesom_gpu_ctx *ctx, int ab) {
     float **fac[] = {&ctx->vfac.a, &ctx->vfac.c, &ctx->vfac.inv, &ctx->vfac.cp};
     for (float **f : fac)
         if ((rc = dalloc(ctx, (void **)f, 4 * sN))) return rc;
-    // LO, R+, R-, the two bounds, ADv, ADh (+ the horizontal diffusion fluxes) per group
-    const size_t per_group = 4 * (size_t)G * (5 * sN + sNI + sE + (ctx->Ki ? sE : 0));
+    // LO, R+, R-, (the two bounds,) ADv, ADh (+ the horizontal diffusion fluxes) per group
+    const bool clamp = b32_fct_clamp();
+    const size_t per_group = 4 * (size_t)G * ((clamp ? 5 : 3) * sN + sNI + sE + (ctx->Ki ? sE : 0));
     size_t fr = 0, tot = 0;
     CK(cudaMemGetInfo(&fr, &tot));
     // at most kMaxSlots slots and kMaxGroups groups per launch (per-slot kernel parameters)
@@ -660,8 +661,8 @@ int alloc_state32(fesom_gpu_ctx *ctx, int ab) {
     if ((rc = dalloc(ctx, (void **)&ctx->ADh32, wg * sE))) return rc;
     if ((rc = dalloc(ctx, (void **)&ctx->Rp32, wg * sN))) return rc;
     if ((rc = dalloc(ctx, (void **)&ctx->Rm32, wg * sN))) return rc;
-    if ((rc = dalloc(ctx, (void **)&ctx->Bp32, wg * sN))) return rc;
-    if ((rc = dalloc(ctx, (void **)&ctx->Bm32, wg * sN))) return rc;
+    if (clamp && (rc = dalloc(ctx, (void **)&ctx->Bp32, wg * sN))) return rc;
+    if (clamp && (rc = dalloc(ctx, (void **)&ctx->Bm32, wg * sN))) return rc;
     if (ctx->Ki && (rc = dalloc(ctx, (void **)&ctx->HD32, wg * sE))) return rc;
     // created here, not on first use: a first step may run inside a stream capture
     CK(b32_prepare());
@@ -1693,7 +1694,7 @@ int fesom_gpu_set_launch_shape(fesom_gpu_ctx *ctx, int32_t stage, int32_t blocks
 }
 
 int fesom_gpu_set_stage_variant(fesom_gpu_ctx *ctx, int32_t stage, int32_t variant) {
-    if (!ctx || stage < 0 || stage > 3 || stage == 1 || variant < 0 || variant > 1) return FESOM_ERR_ARG;
+    if (!ctx || stage < 0 || stage > 3 || variant < 0 || variant > 1) return FESOM_ERR_ARG;
     ctx->shape[stage].staged = variant == 1;
     free_graphs32(ctx);
     return FESOM_OK;
@@ -1792,13 +1793,13 @@ int fesom_gpu_autotune(fesom_gpu_ctx *ctx, double dt, int32_t steps, fesom_tune_
     const int ntr_slots = ctx->ngr * ctx->gw;
     const int bps[] = {0, 2, 4};
     for (int k = 0; k < 4 && !rc; k++) {
-        const int nvar = (k == 1) ? 1 : 2;
+        const int nvar = 2;
         const int ntrs = (k >= 2 && ntr_slots > 8) ? 2 : 1;
         for (int v = 0; v < nvar && !rc; v++)
             for (int b : bps)
                 for (int q = 0; q < ntrs && !rc; q++) {
                     TuneSetting c = best;
-                    c.shape[k].staged = (k == 1) ? false : v == 1;
+                    c.shape[k].staged = v == 1;
                     c.shape[k].blocks_per_sm = b;
                     c.stage_tr[k] = q ? 8 : 0;
                     if (c == best) continue;

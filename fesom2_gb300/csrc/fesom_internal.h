@@ -107,7 +107,7 @@ struct B32View {
     float *ADv;             // vertical flux high order minus low order (the antidiffusive flux)
     float *ADh;             // the same for edges, in the direction edges(1,e) -> edges(2,e)
     float *Rp, *Rm;         // FCT ratios R+ and R-
-    float *Bp, *Bm;         // FCT bounds of the advected value (LO + bmax, LO + bmin)
+    float *Bp, *Bm;         // FCT bounds of the advected value (builds with the clamp only)
     unsigned *status;
     // bit g: group g of the launch uses the FCT limiter / takes the implicit vertical
     // diffusion / gets horizontal or explicit vertical diffusion (k32_diff) / the PPM vertical
@@ -151,6 +151,9 @@ struct VFactors {
 // once per process, before the first FP32 step (not inside a stream capture): the shared-memory
 // limits of the node kernels that stage their gathers
 cudaError_t b32_prepare();
+// whether the build clamps advected values into their stored FCT bounds (FESOM_FCT_CLAMP); the
+// bound arrays exist only then
+bool b32_fct_clamp();
 void b32_vflux(const DTopo &, const DGeom<float> &, const DForcing<float> &, float *VF, cudaStream_t);
 void b32_vfactors(const DTopo &, const DGeom<float> &, const DForcing<float> &, double dt, const VFactors &,
                   cudaStream_t);

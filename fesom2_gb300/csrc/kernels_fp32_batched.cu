@@ -66,10 +66,14 @@ namespace fesom {
 
 namespace {
 
-// the FCT clamp of the advected value into its stored bounds (k32_bounds writes them,
-// k32_update reads them)
+// The FCT clamp of the advected value into its bounds: k32_bounds stores the bounds, k32_update
+// clamps into them and raises FESOM_STATUS_FCT_BOUND where the clamp moved a value by more than
+// round-off.  The reference has no such clamp; the FP32 limiter keeps the values inside their
+// bounds to FP32 round-off without it, and the two bound arrays cost a write and a read of 8
+// bytes per tracer-DOF (7.8 ms of the 24-tracer benchmark step), so the default build leaves it
+// out; -DFESOM_FCT_CLAMP=1 builds it in.
 #ifndef FESOM_FCT_CLAMP
-#define FESOM_FCT_CLAMP 1
+#define FESOM_FCT_CLAMP 0
 #endif
 constexpr bool kFctClamp = FESOM_FCT_CLAMP != 0;
 // packed FP32 pairs (two slots per instruction) in the edge kernel's arithmetic
@@ -94,6 +98,8 @@ struct MinB {
 #else
     static constexpr int ho = G == 4 ? 3 : 4;
 #endif
+    // the staged edge kernel: 80 KB (G = 4) of staging per block of eight warps
+    static constexpr int ho_stg = 2;
     // bounds and update: gathers in registers (three blocks of eight warps per SM measured
     // faster than two with more registers or one with the whole pass in flight), or staged in
     // shared memory (which holds one block of the G = 4 staging per SM)
@@ -1006,6 +1012,39 @@ __device__ __forceinline__ float2 ho_minus_lo2(int hor, int ab, float2 q1, float
 //
 // A pass covers 32 levels of the edge; the last pass, when its levels fill at most half a
 // warp, carries P groups side by side in segments of W lanes (PACK).
+// the group's high-minus-low fluxes of one edge-layer from its gathered entries
+template <int G>
+__device__ __forceinline__ Vec<G> ho_group(const B32View &B, int gq, int hor, const Vec<G> &T1, const Vec<G> &T2,
+                                           const Vec<G> &o1a, const Vec<G> &o1b, const Vec<G> &o2a, const Vec<G> &o2b,
+                                           const Vec<G> &ga, const Vec<G> &gb, const Vec<G> &gc, const Vec<G> &gd,
+                                           const float4 &wu, const float4 &wd, float v, float cl1, float cl2) {
+    Vec<G> out;
+#if FESOM_PACKED_PAIRS
+    const float vp = fmaxf(v, 0.f), vm = fminf(v, 0.f);
+#pragma unroll
+    for (int j = 0; j < G / 2; j++) {
+        const float2 ph = make_float2(B.ph[gq * G + 2 * j], B.ph[gq * G + 2 * j + 1]);
+        const float2 q1 = psub(pk(1.f), ph), q2 = pmul(pk(0.5f * v), ph);
+        const float2 t1 = pr(T1, j), t2 = pr(T2, j);
+        const float2 s1 = pfma(pk(wu.y), psub(pr(ga, j), t1), pmul(pk(wu.z), psub(pr(gb, j), t1)));
+        const float2 s2 = pfma(pk(wd.y), psub(pr(gc, j), t2), pmul(pk(wd.z), psub(pr(gd, j), t2)));
+        const float2 r = ho_minus_lo2(hor, B.ab, q1, q2, t1, t2, pr(o1a, j), pr(o1b, j), pr(o2a, j), pr(o2b, j), s1,
+                                      s2, vp, vm, cl1, cl2);
+        out.c[2 * j] = r.x;
+        out.c[2 * j + 1] = r.y;
+    }
+#else
+#pragma unroll
+    for (int c = 0; c < G; c++) {
+        const float s1 = wu.y * (ga.c[c] - T1.c[c]) + wu.z * (gb.c[c] - T1.c[c]);
+        const float s2 = wd.y * (gc.c[c] - T2.c[c]) + wd.z * (gd.c[c] - T2.c[c]);
+        out.c[c] = ho_minus_lo(hor, B.ph[gq * G + c], B.ab, T1.c[c], T2.c[c], o1a.c[c], o1b.c[c], o2a.c[c], o2b.c[c],
+                               s1, s2, v, cl1, cl2);
+    }
+#endif
+    return out;
+}
+
 template <int G, bool PACK>
 __device__ __forceinline__ void ho_pass(const DTopo &tp, const B32View &B, const MusclW &mw,
                                         const float *__restrict__ VF, int e, int nz0, int W, int P, int lane) {
@@ -1042,52 +1081,122 @@ __device__ __forceinline__ void ho_pass(const DTopo &tp, const B32View &B, const
         const Vec<G> o2a = vldc<G>(B.ab == 3, O2, ia), o2b = vldc<G>(B.ab == 3, O2, ib);
         const Vec<G> ga = vldc<G>(grad, T, ua), gb = vldc<G>(grad, T, ub);
         const Vec<G> gc = vldc<G>(grad, T, da), gd = vldc<G>(grad, T, db);
-        Vec<G> out;
-#if FESOM_PACKED_PAIRS
-        const float vp = fmaxf(v, 0.f), vm = fminf(v, 0.f);
-#pragma unroll
-        for (int j = 0; j < G / 2; j++) {
-            const float2 ph = make_float2(B.ph[gq * G + 2 * j], B.ph[gq * G + 2 * j + 1]);
-            const float2 q1 = psub(pk(1.f), ph), q2 = pmul(pk(0.5f * v), ph);
-            const float2 t1 = pr(T1, j), t2 = pr(T2, j);
-            const float2 s1 = pfma(pk(wu.y), psub(pr(ga, j), t1), pmul(pk(wu.z), psub(pr(gb, j), t1)));
-            const float2 s2 = pfma(pk(wd.y), psub(pr(gc, j), t2), pmul(pk(wd.z), psub(pr(gd, j), t2)));
-            const float2 r = ho_minus_lo2(hor, B.ab, q1, q2, t1, t2, pr(o1a, j), pr(o1b, j), pr(o2a, j), pr(o2b, j),
-                                          s1, s2, vp, vm, cl1, cl2);
-            out.c[2 * j] = r.x;
-            out.c[2 * j + 1] = r.y;
-        }
-#else
-#pragma unroll
-        for (int c = 0; c < G; c++) {
-            const float s1 = wu.y * (ga.c[c] - T1.c[c]) + wu.z * (gb.c[c] - T1.c[c]);
-            const float s2 = wd.y * (gc.c[c] - T2.c[c]) + wd.z * (gd.c[c] - T2.c[c]);
-            out.c[c] = ho_minus_lo(hor, B.ph[gq * G + c], B.ab, T1.c[c], T2.c[c], o1a.c[c], o1b.c[c], o2a.c[c],
-                                   o2b.c[c], s1, s2, v, cl1, cl2);
-        }
-#endif
-        vst<G>(grp<G>(B.ADh, gq, B.sE), ie, out);
+        vst<G>(grp<G>(B.ADh, gq, B.sE), ie,
+               ho_group<G>(B, gq, hor, T1, T2, o1a, o1b, o2a, o2b, ga, gb, gc, gd, wu, wd, v, cl1, cl2));
     }
 }
 
-template <int G, bool PK>
+// The same pass with each group's gathers (T and the previous levels at both ends, T at the
+// four triangle vertices) copied into shared memory by cp.async, double-buffered across the
+// groups: the next group's copies are in flight while the current one computes.  Each lane reads
+// back only its own copies, so the staging needs no barrier.  Staging of a warp:
+// [2 buffers][kNsHo entries][32 lanes][G floats].
+constexpr int kNsHo = 10;
+template <int G>
+__host__ __device__ constexpr int stage_bytes_ho() { return 2 * kNsHo * 32 * G * 4; }
+
+template <int G, bool PACK>
+__device__ __forceinline__ void ho_pass_pf(const DTopo &tp, const B32View &B, const MusclW &mw,
+                                           const float *__restrict__ VF, int e, int nz0, int W, int P, int lane,
+                                           float *sb) {
+    const int L1 = tp.L1;
+    const int n1 = tp.e_n1[e], n2 = tp.e_n2[e];
+    const int ehi = tp.e_hi[e];
+    const int nbl1 = tp.n_nbl[n1], nbl2 = tp.n_nbl[n2];
+    const int4 un = mw.un[e], dn = mw.dn[e];
+    const float4 wu = mw.wu[e], wd = mw.wd[e];
+    const int gzmin = un.w & 0xffff, gzmax = un.w >> 16;
+    const int q = PACK ? lane / W : 0;
+    const int nz = nz0 + lane - q * W;
+    const bool tri = nz >= gzmin && nz <= gzmax - 1;
+    const bool ok = nz <= ehi && q < P;
+    if (!ok) return;
+    const int ie = e * L1 + nz - 1, ia = n1 * L1 + nz - 1, ib = n2 * L1 + nz - 1;
+    const float v = VF[ie];
+    const float cl1 = (nbl1 - nz) >= 0 ? 1.f : 0.f, cl2 = (nbl2 - nz) >= 0 ? 1.f : 0.f;
+    // the triangle vertices' entries where the gradients apply (elsewhere the edge's own, unread)
+    const int ua = tri ? un.y * L1 + nz - 1 : ia, ub = tri ? un.z * L1 + nz - 1 : ia;
+    const int da = tri ? dn.y * L1 + nz - 1 : ib, db = tri ? dn.z * L1 + nz - 1 : ib;
+    const int npass = PACK ? (B.ng + P - 1) / P : B.ng;
+    auto issue = [&](int p, float *buf) {
+        const int gq = PACK ? p * P + q : p;
+        const bool on = gq < B.ng;
+        const int gi = on ? gq : 0;
+        const int hor = B.hor[gi];
+        const bool act = on && (hor == 2 || tri);
+        const bool grad = act && hor != 2;
+        const float *T = grp<G>(B.T, gi, B.sN), *O1 = grp<G>(B.O1, gi, B.sN);
+        const float *O2 = B.ab == 3 ? grp<G>(B.O2, gi, B.sN) : O1;
+        cpa<G>(stg<G>(buf, 0, lane), T + (size_t)ia * G, act);
+        cpa<G>(stg<G>(buf, 1, lane), T + (size_t)ib * G, act);
+        cpa<G>(stg<G>(buf, 2, lane), O1 + (size_t)ia * G, act);
+        cpa<G>(stg<G>(buf, 3, lane), O1 + (size_t)ib * G, act);
+        cpa<G>(stg<G>(buf, 4, lane), O2 + (size_t)ia * G, act && B.ab == 3);
+        cpa<G>(stg<G>(buf, 5, lane), O2 + (size_t)ib * G, act && B.ab == 3);
+        cpa<G>(stg<G>(buf, 6, lane), T + (size_t)ua * G, grad);
+        cpa<G>(stg<G>(buf, 7, lane), T + (size_t)ub * G, grad);
+        cpa<G>(stg<G>(buf, 8, lane), T + (size_t)da * G, grad);
+        cpa<G>(stg<G>(buf, 9, lane), T + (size_t)db * G, grad);
+        cpa_commit();
+    };
+    auto compute = [&](int p, const float *buf) {
+        const int gq = PACK ? p * P + q : p;
+        if (gq >= B.ng) return;
+        const int hor = B.hor[gq];
+        if (hor != 2 && !tri) return;  // MUSCL / MFCT outside the triangles' range: the node-mean launch
+        const Vec<G> r = ho_group<G>(B, gq, hor, lds<G>(stg<G>((float *)buf, 0, lane)),
+                                     lds<G>(stg<G>((float *)buf, 1, lane)), lds<G>(stg<G>((float *)buf, 2, lane)),
+                                     lds<G>(stg<G>((float *)buf, 3, lane)), lds<G>(stg<G>((float *)buf, 4, lane)),
+                                     lds<G>(stg<G>((float *)buf, 5, lane)), lds<G>(stg<G>((float *)buf, 6, lane)),
+                                     lds<G>(stg<G>((float *)buf, 7, lane)), lds<G>(stg<G>((float *)buf, 8, lane)),
+                                     lds<G>(stg<G>((float *)buf, 9, lane)), wu, wd, v, cl1, cl2);
+        vst<G>(grp<G>(B.ADh, gq, B.sE), ie, r);
+    };
+    issue(0, sb);
+    float *cur = sb, *nxt = sb + (size_t)kNsHo * 32 * G;
+    for (int p = 0; p < npass; p++) {
+        if (p + 1 < npass) {
+            issue(p + 1, nxt);
+            cpa_wait<1>();
+        } else {
+            cpa_wait<0>();
+        }
+        compute(p, cur);
+        float *t = cur;
+        cur = nxt;
+        nxt = t;
+    }
+}
+
+template <int G, bool PK, bool STG>
 __device__ __forceinline__ void ho_unit(const DTopo &tp, const B32View &B, const MusclW &mw,
-                                        const float *__restrict__ VF, int e) {
+                                        const float *__restrict__ VF, int e, float *sb) {
     const int lane = threadIdx.x & 31;
     if (e >= tp.E2) return;
     const int elo = tp.e_lo[e], ehi = tp.e_hi[e];
     int nz0 = elo;
-    for (; nz0 + 32 <= ehi; nz0 += 32) ho_pass<G, false>(tp, B, mw, VF, e, nz0, 32, 1, lane);
+    for (; nz0 + 32 <= ehi; nz0 += 32) {
+        if (STG) ho_pass_pf<G, false>(tp, B, mw, VF, e, nz0, 32, 1, lane, sb);
+        else ho_pass<G, false>(tp, B, mw, VF, e, nz0, 32, 1, lane);
+    }
     const int W = ehi - nz0 + 1;
     if (W < 1) return;
     const int P = 32 / W;
-    if (PK && P > 1) ho_pass<G, true>(tp, B, mw, VF, e, nz0, W, P, lane);
-    else ho_pass<G, false>(tp, B, mw, VF, e, nz0, 32, 1, lane);
+    if (STG) {
+        if (PK && P > 1) ho_pass_pf<G, true>(tp, B, mw, VF, e, nz0, W, P, lane, sb);
+        else ho_pass_pf<G, false>(tp, B, mw, VF, e, nz0, 32, 1, lane, sb);
+    } else {
+        if (PK && P > 1) ho_pass<G, true>(tp, B, mw, VF, e, nz0, W, P, lane);
+        else ho_pass<G, false>(tp, B, mw, VF, e, nz0, 32, 1, lane);
+    }
 }
 
-template <int G>
-__global__ void __launch_bounds__(kTB, MinB<G>::ho) k32_ho(DTopo tp, B32View B, MusclW mw, const float *__restrict__ VF) {
-    FOR_WARP_UNITS(e, tp.E2) ho_unit<G, true>(tp, B, mw, VF, e);
+template <int G, bool STG>
+__global__ void __launch_bounds__(kTB, STG ? MinB<G>::ho_stg : MinB<G>::ho)
+k32_ho(DTopo tp, B32View B, MusclW mw, const float *__restrict__ VF) {
+    extern __shared__ __align__(16) float dsm[];
+    float *sb = STG ? dsm + (size_t)(threadIdx.x >> 5) * (stage_bytes_ho<G>() / 4) : nullptr;
+    FOR_WARP_UNITS(e, tp.E2) ho_unit<G, true, STG>(tp, B, mw, VF, e, sb);
 }
 
 // The edge-layers of the node-mean gradients: one thread per (edge, level) item, every
@@ -1579,8 +1688,9 @@ __device__ __forceinline__ void update_chunk_pf(const DTopo &tp, const DGeom<flo
         cpa<G>(stg<G>(buf, 1, lane), grp<G>(B.ADv, gc, B.sNI) + (size_t)(lv ? iv : 0) * G, lv);
         cpa<G>(stg<G>(buf, 2, lane), Rp + (size_t)ii * G, lf);
         cpa<G>(stg<G>(buf, 3, lane), Rm + (size_t)ii * G, lf);
-        cpa<G>(stg<G>(buf, 4, lane), grp<G>(B.Bp, gc, B.sN) + (size_t)ii * G, lf && kFctClamp);
-        cpa<G>(stg<G>(buf, 5, lane), grp<G>(B.Bm, gc, B.sN) + (size_t)ii * G, lf && kFctClamp);
+        // (without the clamp the bounds are not allocated: the zero-filled copies name LO)
+        cpa<G>(stg<G>(buf, 4, lane), grp<G>(kFctClamp ? B.Bp : B.LO, gc, B.sN) + (size_t)ii * G, lf && kFctClamp);
+        cpa<G>(stg<G>(buf, 5, lane), grp<G>(kFctClamp ? B.Bm : B.LO, gc, B.sN) + (size_t)ii * G, lf && kFctClamp);
         cpa<G>(stg<G>(buf, 6, lane), grp<G>(B.Tnew, gc, B.sN) + (size_t)ii * G, ld);
 #pragma unroll
         for (int u = 0; u < KD; u++) {
@@ -2542,8 +2652,8 @@ __global__ void __launch_bounds__(kTB, WIDE ? 1 : MinB<4>::lo) k32m_lo_ad(const 
 __global__ void __launch_bounds__(kTB, MinB<4>::ho) k32m_ho(const Inst32 *__restrict__ I, MultiIdx ix) {
     FOR_WARP_UNITS(u, ix.start[ix.n]) {
         const int i = find_inst(ix, u);
-        if (I[i].B.G == 4) ho_unit<4, true>(I[i].tp, I[i].B, I[i].mw, I[i].VF, u - ix.start[i]);
-        else ho_unit<2, true>(I[i].tp, I[i].B, I[i].mw, I[i].VF, u - ix.start[i]);
+        if (I[i].B.G == 4) ho_unit<4, true, false>(I[i].tp, I[i].B, I[i].mw, I[i].VF, u - ix.start[i], nullptr);
+        else ho_unit<2, true, false>(I[i].tp, I[i].B, I[i].mw, I[i].VF, u - ix.start[i], nullptr);
     }
 }
 __global__ void __launch_bounds__(256) k32m_ho_nodemean(const Inst32 *__restrict__ I, MultiIdx ix) {
@@ -2653,6 +2763,8 @@ template <int G>
 constexpr int smem_bounds() { return kWB * stage_bytes_bounds<G>(); }
 template <int G>
 constexpr int smem_update() { return kWB * stage_bytes_update<G>(); }
+template <int G>
+constexpr int smem_ho() { return kWB * stage_bytes_ho<G>(); }
 
 template <int G>
 static cudaError_t prepare_g() {
@@ -2664,8 +2776,11 @@ static cudaError_t prepare_g() {
     set((const void *)k32_lo_ad<G, false, true, true>, smem_lo_ad<G>());
     set((const void *)k32_bounds<G, false, true>, smem_bounds<G>());
     set((const void *)k32_update<G, false, true>, smem_update<G>());
+    set((const void *)k32_ho<G, true>, smem_ho<G>());
     return e;
 }
+bool b32_fct_clamp() { return kFctClamp; }
+
 cudaError_t b32_prepare() {
     static cudaError_t done = cudaErrorNotReady;
     if (done == cudaSuccess) return done;
@@ -2712,7 +2827,8 @@ void b32_lo_ad(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
 template <int G>
 static void ho_g(const DTopo &tp, const B32View &B, const MusclW &mw, const float *VF, const LaunchShape &sh,
                  cudaStream_t s) {
-    k32_ho<G><<<grid_units(tp.E2, sh), kTB, 0, s>>>(tp, B, mw, VF);
+    if (sh.staged) k32_ho<G, true><<<grid_units(tp.E2, sh), kTB, smem_ho<G>(), s>>>(tp, B, mw, VF);
+    else k32_ho<G, false><<<grid_units(tp.E2, sh), kTB, 0, s>>>(tp, B, mw, VF);
     if (mw.n_items) {
         int blocks = (mw.n_items + 255) / 256;
         if (blocks > 152 * 8) blocks = 152 * 8;

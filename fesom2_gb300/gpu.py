@@ -314,7 +314,7 @@ class Context:
         self._chk(self.L.fesom_gpu_set_launch_shape(self.h, int(stage), int(blocks_per_sm)))
 
     def set_stage_variant(self, stage: int, variant: int):
-        """FP32 form: kernel variant of stage 0 lo_ad, 2 bounds, 3 update (0: gathers in registers,
+        """FP32 form: kernel variant of stage 0 lo_ad, 1 ho, 2 bounds, 3 update (0: gathers in registers,
         1: staged in shared memory)."""
         self._chk(self.L.fesom_gpu_set_stage_variant(self.h, int(stage), int(variant)))
 

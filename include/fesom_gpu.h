@@ -85,7 +85,8 @@ extern "C" {
 
 /* device status word bits (fesom_gpu_status) */
 #define FESOM_STATUS_NAN 0x1u        /* a non-finite tracer value was produced */
-#define FESOM_STATUS_FCT_BOUND 0x2u  /* (FP32 form) an advected value left its FCT bounds */
+#define FESOM_STATUS_FCT_BOUND 0x2u  /* (FP32 form built with FESOM_FCT_CLAMP=1) an advected value
+                                        left its FCT bounds by more than round-off */
 #define FESOM_STATUS_INDEX 0x4u      /* a kernel met an index outside its array and skipped it */
 
 /* Per-tracer scheme tuple of T_TRACER_DATA (src/MOD_TRACER.F90:10-27). */
@@ -303,15 +304,15 @@ int fesom_gpu_set_stage_tracers(fesom_gpu_ctx *ctx, int32_t stage, int32_t trace
  * blocks_per_sm x 152 blocks whose warps loop over the units (nodes, edges); 0 (the default)
  * launches one warp per unit. */
 int fesom_gpu_set_launch_shape(fesom_gpu_ctx *ctx, int32_t stage, int32_t blocks_per_sm);
-/* Performance setting of the FP32 form: kernel variant of node stage 0 (lo_ad), 2 (bounds) or
- * 3 (update): 0 gathers each pass's neighbour values into registers, 1 stages them in shared
+/* Performance setting of the FP32 form: kernel variant of stage 0 (lo_ad), 1 (the edge fluxes),
+ * 2 (bounds) or 3 (update): 0 gathers each pass's entries into registers, 1 stages them in shared
  * memory with asynchronous copies while the previous pass computes (fewer resident warps, no
- * register limit on the gathers in flight).  Defaults: lo_ad 1, bounds 0, update 0.  The two
- * variants are separate compilations and agree to FP32 round-off. */
+ * register limit on the gathers in flight).  Defaults: lo_ad 1, the others 0.  The two variants
+ * are separate compilations and agree to FP32 round-off. */
 int fesom_gpu_set_stage_variant(fesom_gpu_ctx *ctx, int32_t stage, int32_t variant);
 /* Autotuner of the FP32 form's launch settings (results do not change): times the step of the
  * context's own state under the library defaults, then by coordinate descent over the four node/edge
- * stages under each kernel variant, blocks per SM (0, 2, 4) and, for bounds and update with more
+ * stages under both kernel variants, blocks per SM (0, 2, 4) and, for bounds and update with more
  * than 8 tracer slots, 8 tracers per launch; a candidate is kept when it is more than 1 % faster.
  * Each candidate runs one untimed and `steps` timed steps (CUDA events on the context's stream).
  * The fastest settings stay on the context; the tracer state and its time levels are restored
@@ -321,7 +322,7 @@ typedef struct fesom_tune_result {
     int32_t candidates;           /* settings timed */
     int32_t stage_tracers[4];     /* chosen, per stage (fesom_gpu_set_stage_tracers) */
     int32_t blocks_per_sm[4];     /* (fesom_gpu_set_launch_shape) */
-    int32_t variant[4];           /* (fesom_gpu_set_stage_variant; stage 1 has one variant) */
+    int32_t variant[4];           /* (fesom_gpu_set_stage_variant) */
 } fesom_tune_result;
 int fesom_gpu_autotune(fesom_gpu_ctx *ctx, double dt, int32_t steps, fesom_tune_result *res);
 /* The routine alone (FP64 contexts): del_ttf += the edge diffusion fluxes of the element

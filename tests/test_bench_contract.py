@@ -35,5 +35,5 @@ def test_roofline_byte_formulas():
     assert bench.algorithmic_bytes(c, 24, 4) == 4 * (24 * (18 * N3 + 3 * E3) + 3 * T3 + 14 * N3)
     sb = bench.stage_bytes(c, 6, 4)
     # the bounds and update passes: 7 N3 + E3 per tracer, hnode_new and areasvol shared
-    assert sb["bounds"] == sb["update"] == 4 * (6 * (7 * N3 + E3) + 2 * N3)
+    assert sb["bounds"] == sb["update"] == 4 * (6 * (5 * N3 + E3) + 2 * N3)
     assert set(bench.MEASURED_DRAM_B_PER_TRACER_DOF) <= set(sb)

@@ -352,9 +352,9 @@ def test_fp32_stage_passes_do_not_change_results(meshname, kind, request):
     f, tr = _setup(mesh, kind, ntr=7)
     cfgs = [G.tra_cfg(["MUSCL", "MFCT", "UPW1"][k % 3], ["QR4C", "UPW1", "PPM", "CDIFF"][k % 4],
                       "FCT" if k % 3 else "NON", id=k + 1) for k in range(7)]
-    combos = (([0, 0, 0, 0], [0, 0, 0, 0], [1, 0, 0]), ([3, 2, 5, 1], [2, 3, 1, 2], [1, 0, 0]),
-              ([1, 7, 2, 4], [0, 0, 0, 0], [1, 0, 0]), ([3, 2, 5, 1], [0, 0, 0, 0], [0, 1, 1]),
-              ([1, 7, 2, 4], [1, 2, 2, 1], [0, 1, 1]))
+    combos = (([0, 0, 0, 0], [0, 0, 0, 0], [1, 0, 0, 0]), ([3, 2, 5, 1], [2, 3, 1, 2], [1, 0, 0, 0]),
+              ([1, 7, 2, 4], [0, 0, 0, 0], [1, 0, 0, 0]), ([3, 2, 5, 1], [0, 0, 0, 0], [0, 1, 1, 1]),
+              ([1, 7, 2, 4], [1, 2, 2, 1], [0, 1, 1, 1]))
     outs = []
     for split, shape, variant in combos:
         ctx = G.Context(mesh, G.PREC_FP32, max_tracers=7)
@@ -364,7 +364,7 @@ def test_fp32_stage_passes_do_not_change_results(meshname, kind, request):
             ctx.set_stage_tracers(st, v)
         for st, v in enumerate(shape):
             ctx.set_launch_shape(st, v)
-        for st, v in zip((0, 2, 3), variant):
+        for st, v in enumerate(variant):
             ctx.set_stage_variant(st, v)
         for k in range(7):
             t32 = tr[k].astype(np.float32)
@@ -428,7 +428,7 @@ def test_autotune_keeps_the_state_and_the_results(sphere_small):
             res = ctx.autotune(f.dt, steps=1)
             assert res["candidates"] >= 2 and res["tuned_ms"] <= res["default_ms"]
             assert all(b in (0, 2, 4) for b in res["blocks_per_sm"])
-            assert all(t in (0, 8) for t in res["stage_tracers"]) and res["variant"][1] == 0
+            assert all(t in (0, 8) for t in res["stage_tracers"]) and all(v in (0, 1) for v in res["variant"])
             for k in range(12):
                 v, o = ctx.tracer_download(k, dtype=np.float32)
                 assert np.array_equal(v, before[k][0]) and np.array_equal(o, before[k][1])
