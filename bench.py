@@ -248,27 +248,21 @@ def rigid_lid(mesh, f):
 
 
 class HostPinned:
-    """Host copies page-locked in place (cudaHostRegister) and unlocked together by release():
-    the pages go back to the system when the arrays are dropped, with no pinned-allocator cache
-    holding (and rounding up) tens of GB between the phases that use them."""
+    """Host copies in page-locked memory from the library (fesom_gpu_host_alloc, cudaHostAlloc),
+    given back together by release() once the arrays are dropped: no pinned-allocator cache holds
+    (and rounds up) tens of GB between the phases that use them."""
 
     def __init__(self):
-        import torch
-        self.rt = torch.cuda.cudart()
         self.held = []
 
     def copy(self, src, dtype):
-        a = np.empty(src.shape, dtype)
+        from fesom2_gb300 import gpu as G
+        a = G.host_array(np.shape(src), dtype)
         a[...] = src
-        rc = self.rt.cudaHostRegister(a.ctypes.data, a.nbytes, 0)
-        if int(rc) != 0:
-            raise RuntimeError(f"cudaHostRegister of {a.nbytes} bytes failed: {rc}")
         self.held.append(a)
         return a
 
     def release(self):
-        for a in self.held:
-            self.rt.cudaHostUnregister(a.ctypes.data)
         self.held.clear()
 
 

@@ -1039,6 +1039,21 @@ extern "C" {
 
 int fesom_gpu_abi_version(void) { return FESOM_GPU_ABI_VERSION; }
 
+int fesom_gpu_host_alloc(size_t bytes, void **ptr) {
+    if (!ptr || bytes == 0) return FESOM_ERR_ARG;
+    *ptr = nullptr;
+    if (cudaHostAlloc(ptr, bytes, cudaHostAllocDefault) != cudaSuccess) {
+        *ptr = nullptr;
+        return FESOM_ERR_NOMEM;
+    }
+    return FESOM_OK;
+}
+
+int fesom_gpu_host_free(void *ptr) {
+    if (!ptr) return FESOM_OK;
+    return cudaFreeHost(ptr) == cudaSuccess ? FESOM_OK : FESOM_ERR_CUDA;
+}
+
 const char *fesom_gpu_last_error(const fesom_gpu_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
 int fesom_gpu_init(const fesom_mesh_desc *mesh, int32_t precision, int32_t max_tracers, fesom_gpu_ctx **out) {

@@ -67,6 +67,8 @@ _lib: Optional[C.CDLL] = None
 
 _SIGS = {
     "fesom_gpu_abi_version": ([], C.c_int),
+    "fesom_gpu_host_alloc": ([C.c_size_t, C.POINTER(_P)], C.c_int),
+    "fesom_gpu_host_free": ([_P], C.c_int),
     "fesom_gpu_last_error": ([_P], C.c_char_p),
     "fesom_gpu_init": ([C.POINTER(MeshDesc), C.c_int32, C.c_int32, C.POINTER(_P)], C.c_int),
     "fesom_gpu_finalize": ([_P], C.c_int),
@@ -143,6 +145,21 @@ def _p(a: Optional[np.ndarray]):
     if a is None:
         return None
     return C.c_void_p(a.ctypes.data)
+
+
+def host_array(shape, dtype=np.float32) -> np.ndarray:
+    """A numpy array in page-locked host memory (fesom_gpu_host_alloc), freed when the array and
+    every view of it are gone: the host arrays of the host-array steps."""
+    import weakref
+    L = load()
+    n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+    p = _P()
+    rc = L.fesom_gpu_host_alloc(max(n, 1), C.byref(p))
+    if rc != 0:
+        raise FesomGpuError(rc, f"fesom_gpu_host_alloc of {n} bytes failed")
+    buf = (C.c_char * max(n, 1)).from_address(p.value)
+    weakref.finalize(buf, L.fesom_gpu_host_free, C.c_void_p(p.value))
+    return np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
 
 
 def _c64(a):

@@ -159,6 +159,11 @@ int fesom_gpu_mesh_check(const fesom_mesh_desc *mesh, int32_t *nboundary_lay, in
 int fesom_gpu_set_stream(fesom_gpu_ctx *ctx, void *stream);
 const char *fesom_gpu_last_error(const fesom_gpu_ctx *ctx);
 int fesom_gpu_abi_version(void);
+/* Page-locked host memory (cudaHostAlloc) for the arrays of the host-array steps: copies from and
+ * into it run at the host link's full rate without page-locking a caller's allocation later.
+ * fesom_gpu_host_free releases it (NULL: nothing). */
+int fesom_gpu_host_alloc(size_t bytes, void **ptr);
+int fesom_gpu_host_free(void *ptr);
 /* Copies of the derived init arrays, index_base-based: nboundary_lay (nod2D),
  * edge_up_dn_tri (2, edge2D).  Either pointer may be NULL. */
 int fesom_gpu_get_muscl_init(fesom_gpu_ctx *ctx, int32_t *nboundary_lay, int32_t *edge_up_dn_tri);
