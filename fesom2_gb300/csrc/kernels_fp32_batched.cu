@@ -88,10 +88,12 @@ constexpr int kMaxChunks = 5;         // columns of up to 128 layers, 30 levels 
 // resident blocks per SM each group kernel is built for (registers: 65536 / (256 * blocks))
 template <int G>
 struct MinB {
+    // the LO stage: three blocks per SM (the staged variant's double buffer fits 3 x 74 KB);
+    // two measured 1.3 ms slower per step on the 24-tracer sphere, though its own launch is faster
 #ifdef FESOM_MINB_LO
     static constexpr int lo = FESOM_MINB_LO;
 #else
-    static constexpr int lo = 2;
+    static constexpr int lo = 3;
 #endif
 #ifdef FESOM_MINB_HO
     static constexpr int ho = FESOM_MINB_HO;
