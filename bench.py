@@ -643,7 +643,8 @@ def run_ours(args, rank, world, local_rank):
                       "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                       "ms_per_step": mse / args.e2e_steps, "api": "fesom_gpu_step_host_f32",
                       "tracer_groups": ngr, "group_width": width, "host_link_before": link,
-                      "host_link_after": host_link_gbs(stream)}
+                      "host_link_after": host_link_gbs(stream),
+                      "host_link_after_8gb": host_link_gbs(stream, nbytes=8 << 30, reps=2)}
         # (2) FP64 host arrays, the reference's own layout and precision, through the call a
         # Fortran caller binds for the tracer loop (fesom_gpu_tracer_step, FP32 context):
         # values and valuesold in, both updated in place
