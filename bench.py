@@ -64,7 +64,9 @@ def parse():
     p.add_argument("--width", type=int, default=0, help="FP32 tracer-group width (0: automatic, 2, 4)")
     p.add_argument("--stage-tr", default="", help="tracers per launch of lo_ad,ho,bounds,update (e.g. 8,0,8,8)")
     p.add_argument("--shape", default="", help="blocks per SM of lo_ad,ho,bounds,update (0: one warp per unit)")
-    p.add_argument("--variant", default="", help="kernel variant of lo_ad,ho,bounds,update (0 registers, 1 staged)")
+    p.add_argument("--variant", default="",
+                   help="kernel variant of lo_ad,ho,bounds,update (0 registers, 1 staged; update +2: the "
+                        "vertical diffusion as its own kernel)")
     return p.parse_args()
 
 
@@ -84,10 +86,12 @@ def workload(cfg: int, scale: float, ntr_override):
     return mesh, kind, forcing, tracers, dt, names.get(cfg, f"config {cfg}"), gen_s
 
 
-def algorithmic_bytes(counts, ntr, s):
-    """FCT-minimal dataflow bytes per step: s*[Ntr*(18 N3 + 3 E3) + 3 T3 + 14 N3]."""
+def algorithmic_bytes(counts, ntr, s, vdiff_fused=False):
+    """FCT-minimal dataflow bytes per step: s*[Ntr*(18 N3 + 3 E3) + 3 T3 + 14 N3]; with the
+    implicit vertical diffusion inside the update (the advected column is not stored and read back
+    between two kernels) s*[Ntr*(16 N3 + 3 E3) + 3 T3 + 14 N3]."""
     N3, E3, T3 = counts["N3"], counts["E3"], counts["T3"]
-    return s * (ntr * (18 * N3 + 3 * E3) + 3 * T3 + 14 * N3)
+    return s * (ntr * ((16 if vdiff_fused else 18) * N3 + 3 * E3) + 3 * T3 + 14 * N3)
 
 
 # DRAM bytes (read + write) per tracer-DOF of each FP32 stage, measured with one ncu capture
@@ -95,11 +99,13 @@ def algorithmic_bytes(counts, ntr, s):
 # (sphere of 7 subdivisions, 12 tracers in one launch per stage as in the full workload; inputs
 # far above L2); the traffic of a full-size launch is this figure times the tracer-DOF it
 # processes
-MEASURED_DRAM_B_PER_TRACER_DOF = {"update": 39.88, "bounds": 37.85, "edge_flux": 23.86, "lo_ad": 21.41,
+MEASURED_DRAM_B_PER_TRACER_DOF = {"update": 43.58, "bounds": 37.86, "edge_flux": 23.85, "lo_ad": 21.60,
                                   "vdiff": 9.35}
+# the update without the diffusion epilogue (the vertical diffusion as its own kernel, "vdiff")
+MEASURED_DRAM_B_PER_TRACER_DOF_UPDATE_ALONE = 39.88
 
 
-def stage_bytes(counts, ntr, s, ab=2, form="fp32"):
+def stage_bytes(counts, ntr, s, ab=2, form="fp32", vdiff_fused=False):
     """Compulsory bytes per step of each stage kernel (every input read once, every
     output written once) for ntr tracers, s bytes per value.
 
@@ -115,6 +121,8 @@ def stage_bytes(counts, ntr, s, ab=2, form="fp32"):
                  hnode_new, areasvol (2 N3)
                  (a build with the FCT clamp also writes and reads the bounds: 2 N3 more each)
       vdiff:     per tracer read and write T (2 N3); shared factors (4 N3)
+      vdiff_fused: the update with the diffusion as each node's epilogue: the update's bytes plus
+                 the shared factors (4 N3), no vdiff stage
     FP64 plain form (per tracer, one tracer per launch):
       ab 4 N3; trxy N3 + 2 T3; edge_flux 2 N3 + 2 T3 + 2 E3 (+3 T3 shared); node_lo 3 N3 + E3
       (+8 N3); bounds 4 N3; rpm 5 N3 + E3 (+2 N3); update 6 N3 + E3 (+3 N3); vdiff 2 N3 (+4 N3)
@@ -122,6 +130,10 @@ def stage_bytes(counts, ntr, s, ab=2, form="fp32"):
     """
     N3, E3, T3 = counts["N3"], counts["E3"], counts["T3"]
     if form == "fp32":
+        if vdiff_fused:
+            d = stage_bytes(counts, ntr, s, ab, form)
+            d["update"] += d.pop("vdiff") - s * ntr * 2 * N3
+            return d
         return {
             "vflux": s * (3 * T3 + E3),
             "vfactors": s * 8 * N3,
@@ -548,18 +560,23 @@ def run_ours(args, rank, world, local_rank):
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    sb = stage_bytes(counts, ntr, 4)
     shares = {k: v[0] for k, v in agg.items() if v[1] > 0}
+    # the default update carries the implicit vertical diffusion (no vdiff launch of its own)
+    vdiff_fused = "vdiff" not in shares
+    sb = stage_bytes(counts, ntr, 4, vdiff_fused=vdiff_fused)
     tot = sum(shares.values())
     dom = max(shares, key=shares.get)
     dom_ms = agg[dom][0] / agg[dom][1]
     # bytes per launch: the stage model is per step; a step issues agg[dom][1]/prof_steps launches
     per_launch_bytes = sb[dom] / (agg[dom][1] / prof_steps)
     achieved = per_launch_bytes / (dom_ms / 1e3) / 1e9
-    step_bytes = algorithmic_bytes(counts, ntr, 4)
+    step_bytes = algorithmic_bytes(counts, ntr, 4, vdiff_fused=vdiff_fused)
     traffic = None
     if dom in MEASURED_DRAM_B_PER_TRACER_DOF:
-        traffic = MEASURED_DRAM_B_PER_TRACER_DOF[dom] * ntr * N3 / (agg[dom][1] / prof_steps)
+        b = MEASURED_DRAM_B_PER_TRACER_DOF[dom]
+        if dom == "update" and not vdiff_fused:
+            b = MEASURED_DRAM_B_PER_TRACER_DOF_UPDATE_ALONE
+        traffic = b * ntr * N3 / (agg[dom][1] / prof_steps)
     res["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                        "frac": achieved / hbm_peak, "traffic": traffic, "traffic_unit": "B per launch",
                        "algorithmic_bytes_per_launch": per_launch_bytes, "peak_source": peak_src,
@@ -567,7 +584,7 @@ def run_ours(args, rank, world, local_rank):
                        "stage_ms_per_step": {k: v / prof_steps for k, v in shares.items()},
                        "stage_frac": {k: (sb[k] / (v / prof_steps / 1e3) / 1e9) / hbm_peak
                                       for k, v in shares.items() if k in sb},
-                       "step_algorithmic_bytes": step_bytes,
+                       "vdiff_in_update": vdiff_fused, "step_algorithmic_bytes": step_bytes,
                        "step_achieved_gbs": step_bytes / (ms_max / args.steps / 1e3) / 1e9,
                        "step_frac": step_bytes / (ms_max / args.steps / 1e3) / 1e9 / hbm_peak}
 

@@ -903,18 +903,20 @@ int enqueue_group32(fesom_gpu_ctx *ctx, double dt, int g0, int ng, StageTimer *t
         for (int s0 = 0; s0 < ng; s0 += bg)
             STAGE(4, b32_bounds(ctx->tp, g, sub32(B, s0, std::min(bg, ng - s0)), dt, ctx->shape[2], ctx->stream));
     }
+    // the implicit vertical diffusion: the epilogue of each node of the update (default), or its
+    // own launch after it
+    const bool vd = (B.ivd & ~B.wimpl) != 0, vfuse = vd && !ctx->shape[3].vsep;
+    if (vd && fork && !joined) {
+        CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+        joined = true;
+    }
     {
         const int sg = stage_group(ctx, 3, ng);
         for (int s0 = 0; s0 < ng; s0 += sg)
-            STAGE(6, b32_update(ctx->tp, g, sub32(B, s0, std::min(sg, ng - s0)), dt, ctx->shape[3], ctx->stream));
+            STAGE(6, b32_update(ctx->tp, g, sub32(B, s0, std::min(sg, ng - s0)), dt, ctx->shape[3],
+                                vfuse ? &ctx->vfac : nullptr, ctx->stream));
     }
-    if (B.ivd & ~B.wimpl) {
-        if (fork && !joined) {
-            CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
-            joined = true;
-        }
-        STAGE(7, b32_vdiff(ctx->tp, fg, B, ctx->vfac, ctx->stream));
-    }
+    if (vd && !vfuse) STAGE(7, b32_vdiff(ctx->tp, fg, B, ctx->vfac, ctx->stream));
     if (B.wimpl) STAGE(7, b32_vdiff_w(ctx->tp, g, fk, B, dt, ctx->scratch, ctx->stream));
     return FESOM_OK;
 }
@@ -946,7 +948,8 @@ int launches_per_step(fesom_gpu_ctx *ctx) {
             const int wide = ctx->tp.n_wide ? 2 : 1;
             auto passes = [&](int k) { return (ng + stage_group(ctx, k, ng) - 1) / stage_group(ctx, k, ng); };
             n += wide * (passes(0) + passes(3) + (B.fct ? passes(2) : 0) + (B.diff ? 1 : 0)) +
-                 passes(1) * (ctx->mw.n_items ? 2 : 1) + ((B.ivd & ~B.wimpl) ? 1 : 0) + (ctx->Ki ? 1 : 0) +
+                 passes(1) * (ctx->mw.n_items ? 2 : 1) + (((B.ivd & ~B.wimpl) && ctx->shape[3].vsep) ? 1 : 0) +
+                 (ctx->Ki ? 1 : 0) +
                  (B.ppm ? 1 : 0) + ((ctx->wsplit && B.fct) ? 1 : 0) + (B.wimpl ? 1 : 0);
         }
         return n;
@@ -1709,8 +1712,9 @@ int fesom_gpu_set_launch_shape(fesom_gpu_ctx *ctx, int32_t stage, int32_t blocks
 }
 
 int fesom_gpu_set_stage_variant(fesom_gpu_ctx *ctx, int32_t stage, int32_t variant) {
-    if (!ctx || stage < 0 || stage > 3 || variant < 0 || variant > 1) return FESOM_ERR_ARG;
-    ctx->shape[stage].staged = variant == 1;
+    if (!ctx || stage < 0 || stage > 3 || variant < 0 || variant > (stage == 3 ? 3 : 1)) return FESOM_ERR_ARG;
+    ctx->shape[stage].staged = (variant & 1) != 0;
+    ctx->shape[stage].vsep = (variant & 2) != 0;
     free_graphs32(ctx);
     return FESOM_OK;
 }
@@ -1730,7 +1734,7 @@ struct TuneSetting {
     bool operator==(const TuneSetting &o) const {
         for (int k = 0; k < 4; k++)
             if (stage_tr[k] != o.stage_tr[k] || shape[k].blocks_per_sm != o.shape[k].blocks_per_sm ||
-                shape[k].staged != o.shape[k].staged)
+                shape[k].staged != o.shape[k].staged || shape[k].vsep != o.shape[k].vsep)
                 return false;
         return true;
     }
@@ -1808,13 +1812,15 @@ int fesom_gpu_autotune(fesom_gpu_ctx *ctx, double dt, int32_t steps, fesom_tune_
     const int ntr_slots = ctx->ngr * ctx->gw;
     const int bps[] = {0, 2, 4};
     for (int k = 0; k < 4 && !rc; k++) {
-        const int nvar = 2;
+        // the update: also with the vertical diffusion as its own launch
+        const int nvar = k == 3 ? 4 : 2;
         const int ntrs = (k >= 2 && ntr_slots > 8) ? 2 : 1;
         for (int v = 0; v < nvar && !rc; v++)
             for (int b : bps)
                 for (int q = 0; q < ntrs && !rc; q++) {
                     TuneSetting c = best;
-                    c.shape[k].staged = v == 1;
+                    c.shape[k].staged = (v & 1) != 0;
+                    c.shape[k].vsep = (v & 2) != 0;
                     c.shape[k].blocks_per_sm = b;
                     c.stage_tr[k] = q ? 8 : 0;
                     if (c == best) continue;
@@ -1840,7 +1846,7 @@ int fesom_gpu_autotune(fesom_gpu_ctx *ctx, double dt, int32_t steps, fesom_tune_
     for (int k = 0; k < 4; k++) {
         res->stage_tracers[k] = best.stage_tr[k];
         res->blocks_per_sm[k] = best.shape[k].blocks_per_sm;
-        res->variant[k] = best.shape[k].staged ? 1 : 0;
+        res->variant[k] = (best.shape[k].staged ? 1 : 0) | (best.shape[k].vsep ? 2 : 0);
     }
     return FESOM_OK;
 }

@@ -163,13 +163,17 @@ void b32_vfactors(const DTopo &, const DGeom<float> &, const DForcing<float> &, 
 struct LaunchShape {
     int blocks_per_sm = 0;
     bool staged = false;  // node stages: gathers staged in shared memory (cp.async) instead of registers
+    bool vsep = false;    // the update stage: the implicit vertical diffusion as its own kernel
 };
 void b32_lo_ad(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, const float *VF,
                double dt, const LaunchShape &, cudaStream_t);
 void b32_ho(const DTopo &, const DGeom<float> &, const B32View &, const MusclW &, const float *VF,
             const LaunchShape &, cudaStream_t);
 void b32_bounds(const DTopo &, const DGeom<float> &, const B32View &, double dt, const LaunchShape &, cudaStream_t);
-void b32_update(const DTopo &, const DGeom<float> &, const B32View &, double dt, const LaunchShape &, cudaStream_t);
+// vf: the factors of the implicit vertical diffusion, run as each node's epilogue for the groups in
+// ivd & ~wimpl (null: the diffusion is left to b32_vdiff)
+void b32_update(const DTopo &, const DGeom<float> &, const B32View &, double dt, const LaunchShape &,
+                const VFactors *vf, cudaStream_t);
 void b32_vdiff(const DTopo &, const DForcing<float> &, const B32View &, const VFactors &, cudaStream_t);
 void b32_vppm(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, double dt, cudaStream_t);
 void b32_lo_impl(const DTopo &, const DGeom<float> &, const DForcing<float> &, const B32View &, double dt,

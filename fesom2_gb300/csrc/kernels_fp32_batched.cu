@@ -392,6 +392,28 @@ __device__ __forceinline__ Vec<G> vldc(bool ok, const float *__restrict__ p, int
     if (ok) r = vld<G>(p, i);
     return r;
 }
+// entry i where ok, read at L2 (ld.global.cg): values the same kernel stored before a
+// __syncwarp, which a load through the read-only or L1 path is not bound to see
+template <int G>
+__device__ __forceinline__ Vec<G> vldcg(bool ok, const float *p, int i);
+template <>
+__device__ __forceinline__ Vec<4> vldcg<4>(bool ok, const float *p, int i) {
+    Vec<4> r = vfill<4>(0.f);
+    if (ok) {
+        const float4 q = __ldcg(reinterpret_cast<const float4 *>(p) + i);
+        r = Vec<4>{{q.x, q.y, q.z, q.w}};
+    }
+    return r;
+}
+template <>
+__device__ __forceinline__ Vec<2> vldcg<2>(bool ok, const float *p, int i) {
+    Vec<2> r = vfill<2>(0.f);
+    if (ok) {
+        const float2 q = __ldcg(reinterpret_cast<const float2 *>(p) + i);
+        r = Vec<2>{{q.x, q.y}};
+    }
+    return r;
+}
 template <int G>
 __device__ __forceinline__ void vst(float *p, int i, const Vec<G> &v);
 template <>
@@ -1549,6 +1571,183 @@ k32_bounds(DTopo tp, DGeom<float> g, B32View B, float dt) {
 }
 
 // ---------------------------------------------------------------------------
+// k32_vdiff: implicit vertical diffusion of the advected columns (in Tnew)
+// ---------------------------------------------------------------------------
+// Forward substitution tp_k = inv_k rhs_k - a_k inv_k tp_{k-1} and back substitution
+// x_k = tp_k - cp_k x_{k+1} (oce_ale_tracer.F90:1406-1422) with the column's FP64-derived
+// factors, as scans of affine maps y -> A y + B.  Each lane holds K consecutive levels of the
+// column (K = ceil(layers / 32): one warp covers the whole column): it composes its K maps in
+// registers, the warp scans the lane maps (five shuffles), and each lane then runs its K
+// levels from the carry it receives.  The multipliers A depend on the column only: the lane
+// products and their partial products at each scan step are formed once per node (shared
+// memory), so a slot's scan step is one shuffle and one multiply-add, and a column costs a slot
+// 14 shuffles whatever its depth.  rhs_k = -a_k (T_{k-1} - T_k) - c_k (T_{k+1} - T_k)
+// (+ bc_surface at the top, :1216-1229, 1377-1383); T += x.
+// CG: the column was stored by the same kernel (the update with the diffusion as its epilogue):
+// its values are read at L2.
+constexpr int kWV = 4;                    // warps (nodes) per block of the diffusion kernel
+constexpr int kScan = 5;                  // steps of a 32-lane scan
+constexpr int kVdiffMaxK = 4;             // levels per lane: columns of up to 128 layers
+
+struct VdiffWarp {
+    float4 fac[130];                      // (a, c, 1/m, c/m), 1-based levels
+    float af[kScan][32];                  // forward: lane-map product of the window at each step (0 below the offset)
+    float ab[kScan][32];                  // backward (0 past the offset)
+};
+
+// per-lane column data of a node: the factors of the lane's K levels
+template <int K>
+struct VdiffLane {
+    float a[K], c[K], inv[K], A[K], Ad[K];
+    bool ok[K];
+};
+
+// a group's column values of the lane's K levels and its surface flux
+template <int K, int G>
+struct VdiffCol {
+    Vec<G> a[K];
+    Vec<G> bc;
+};
+
+template <int K, int G, bool CG>
+__device__ __forceinline__ void vdiff_load(const DTopo &tp, const B32View &B, int n, int lane, int nzmin, int gq,
+                                           const VdiffLane<K> &V, VdiffCol<K, G> &x) {
+    const int L1 = tp.L1;
+    const int nz0 = nzmin + lane * K;  // the lane's first level
+    const float *Tg = grp<G>(B.Tnew, gq, B.sN);
+    x.bc = B.fsurf ? vld<G>(B.fsurf, gq * tp.N2 + n) : vfill<G>(0.f);
+#pragma unroll
+    for (int t = 0; t < K; t++)
+        x.a[t] = CG ? vldcg<G>(V.ok[t], Tg, n * L1 + nz0 + t - 1) : vldc<G>(V.ok[t], Tg, n * L1 + nz0 + t - 1);
+}
+
+template <int K, int G>
+__device__ __forceinline__ void vdiff_group(const DTopo &tp, const B32View &B, int n, int lane, int nzmin, int nzmax,
+                                            int gq, const VdiffLane<K> &V, const VdiffWarp &W,
+                                            const VdiffCol<K, G> &x) {
+    const int L1 = tp.L1;
+    const int nz0 = nzmin + lane * K;  // the lane's first level
+    float *__restrict__ Tg = grp<G>(B.Tnew, gq, B.sN);
+    const Vec<G>(&a)[K] = x.a;
+    const Vec<G> &bc = x.bc;
+    Vec<G> y[K];
+#pragma unroll
+    for (int c = 0; c < G; c++) {
+        // the levels next to the lane's ends come from the neighbouring lanes
+        const float up = sh_up(a[K - 1].c[c], 1), dn = sh_dn(a[0].c[c], 1);
+        float bl = 0.f;  // the lane's composed forward map applied to 0
+#pragma unroll
+        for (int t = 0; t < K; t++) {
+            const int nz = nz0 + t;
+            const float tu = t > 0 ? a[t - 1].c[c] : up, td = t < K - 1 ? a[t + 1].c[c] : dn;
+            const float tc = a[t].c[c];
+            float r = 0.f;
+            if (nz > nzmin) r -= V.a[t] * (tu - tc);
+            if (nz < nzmax - 1) r -= V.c[t] * (td - tc);
+            if (nz == nzmin) r += bc.c[c];
+            y[t].c[c] = V.ok[t] ? r * V.inv[t] : 0.f;
+            bl = fmaf(V.A[t], bl, y[t].c[c]);
+        }
+        // inclusive scan of the lane maps: bl = tp at the lane's last level
+#pragma unroll
+        for (int s = 0, off = 1; s < kScan; s++, off <<= 1) bl = fmaf(W.af[s][lane], __shfl_up_sync(kFull, bl, off), bl);
+        float yv = __shfl_up_sync(kFull, bl, 1);
+        if (lane == 0) yv = 0.f;
+#pragma unroll
+        for (int t = 0; t < K; t++) {
+            yv = fmaf(V.A[t], yv, y[t].c[c]);
+            y[t].c[c] = yv;
+        }
+        // back substitution: the lane's composed backward map, the suffix scan, the lane's levels
+        float xl = 0.f;
+#pragma unroll
+        for (int t = K - 1; t >= 0; t--) xl = fmaf(V.Ad[t], xl, y[t].c[c]);
+#pragma unroll
+        for (int s = 0, off = 1; s < kScan; s++, off <<= 1)
+            xl = fmaf(W.ab[s][lane], __shfl_down_sync(kFull, xl, off), xl);
+        float xv = __shfl_down_sync(kFull, xl, 1);
+        if (lane == 31) xv = 0.f;
+#pragma unroll
+        for (int t = K - 1; t >= 0; t--) {
+            xv = fmaf(V.Ad[t], xv, y[t].c[c]);
+            y[t].c[c] = a[t].c[c] + xv;
+        }
+    }
+#pragma unroll
+    for (int t = 0; t < K; t++) {
+        if (!V.ok[t]) continue;
+        bool fin = true;
+#pragma unroll
+        for (int c = 0; c < G; c++) fin = fin && isfinite(y[t].c[c]);
+        vst<G>(Tg, n * L1 + nz0 + t - 1, y[t]);
+        if (!fin) atomicOr(B.status, 1u);
+    }
+}
+
+template <int K, int G, bool CG>
+__device__ __forceinline__ void vdiff_node(const DTopo &tp, const B32View &B, int n, int lane, int nzmin, int nzmax,
+                                           VdiffWarp &W) {
+    VdiffLane<K> V;
+    float A = 1.f, Ad = 1.f;
+#pragma unroll
+    for (int t = 0; t < K; t++) {
+        const int nz = nzmin + lane * K + t;
+        V.ok[t] = nz <= nzmax - 1;
+        const float4 fz = V.ok[t] ? W.fac[nz] : make_float4(0.f, 0.f, 0.f, 0.f);
+        V.a[t] = fz.x;
+        V.c[t] = fz.y;
+        V.inv[t] = fz.z;
+        // levels past the column's end are identity maps
+        V.A[t] = V.ok[t] ? -(fz.x * fz.z) : 1.f;
+        V.Ad[t] = V.ok[t] ? -fz.w : 1.f;
+        A *= V.A[t];
+        Ad *= V.Ad[t];
+    }
+    // partial products of the lane maps at each scan step
+#pragma unroll
+    for (int s = 0, off = 1; s < kScan; s++, off <<= 1) {
+        W.af[s][lane] = lane >= off ? A : 0.f;
+        W.ab[s][lane] = lane + off < 32 ? Ad : 0.f;
+        const float Ap = __shfl_up_sync(kFull, A, off), An = __shfl_down_sync(kFull, Ad, off);
+        if (lane >= off) A *= Ap;
+        if (lane + off < 32) Ad *= An;
+    }
+    __syncwarp();
+    unsigned long long todo = (B.ivd & ~B.wimpl) & (B.ng >= 64 ? ~0ull : ((1ull << B.ng) - 1));
+    // (loading the next group's column during the current solve measured slower after the
+    // update: the extra registers spill)
+    while (todo) {
+        const int gq = __ffsll((long long)todo) - 1;
+        todo &= todo - 1;
+        VdiffCol<K, G> x;
+        vdiff_load<K, G, CG>(tp, B, n, lane, nzmin, gq, V, x);
+        vdiff_group<K, G>(tp, B, n, lane, nzmin, nzmax, gq, V, W, x);
+    }
+}
+
+template <int G, bool CG = false>
+__device__ __forceinline__ void vdiff_unit(const DTopo &tp, const B32View &B, const VFactors &vf, int n,
+                                           VdiffWarp &W) {
+    const int lane = threadIdx.x & 31;
+    if (n >= tp.N2) return;
+    const int L1 = tp.L1;
+    const int nzmin = tp.n_ulev[n], nzmax = tp.n_nlev[n];
+    const int K = (nzmax - nzmin + 31) / 32;
+    __syncwarp();  // the previous node's reads of W are done
+    for (int nz = nzmin + lane; nz <= nzmax - 1; nz += 32) {
+        const int i = n * L1 + nz - 1;
+        W.fac[nz] = make_float4(vf.a[i], vf.c[i], vf.inv[i], vf.cp[i]);
+    }
+    __syncwarp();
+    switch (K) {
+        case 1: vdiff_node<1, G, CG>(tp, B, n, lane, nzmin, nzmax, W); break;
+        case 2: vdiff_node<2, G, CG>(tp, B, n, lane, nzmin, nzmax, W); break;
+        case 3: vdiff_node<3, G, CG>(tp, B, n, lane, nzmin, nzmax, W); break;
+        default: vdiff_node<4, G, CG>(tp, B, n, lane, nzmin, nzmax, W); break;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // k32_update: limited update, T*
 // ---------------------------------------------------------------------------
 template <int G, int KD, bool PACK>
@@ -1796,9 +1995,14 @@ __device__ __forceinline__ void update_node(const DTopo &tp, const DGeom<float> 
     else update_chunk<G, KD, false>(tp, g, B, dt, n, lane, S, nch - 1, 32, 1);
 }
 
-template <int G, bool WIDE, bool PK>
+// VD: the implicit vertical diffusion of the node's column follows its update in the same warp
+// (the diffusion is column-local: it reads only the column's own T*, which the warp has just
+// stored and reads back at L2), so T* is not written to and read back from HBM between two
+// launches.  Vw: the warp's diffusion workspace.
+template <int G, bool WIDE, bool PK, bool VD = false>
 __device__ __forceinline__ void update_unit(const DTopo &tp, const DGeom<float> &g, const B32View &B, float dt, int j,
-                                            WEdges *Se, float *sb) {
+                                            WEdges *Se, float *sb, const VFactors *vf = nullptr,
+                                            VdiffWarp *Vw = nullptr) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int n = unit_node<WIDE>(tp, j);
     if (n < 0) return;
@@ -1808,18 +2012,34 @@ __device__ __forceinline__ void update_unit(const DTopo &tp, const DGeom<float> 
     if (WIDE) update_node<G, kMaxDeg, PK>(tp, g, B, dt, n, lane, S, nullptr);
     else if (S.deg <= 6) update_node<G, 6, PK>(tp, g, B, dt, n, lane, S, sb);
     else update_node<G, 8, PK>(tp, g, B, dt, n, lane, S, nullptr);
+    // (vdiff_unit opens with a __syncwarp: every lane's T* stores are ordered before the reads)
+    if constexpr (VD) vdiff_unit<G, true>(tp, B, *vf, n, *Vw);
 }
 
 template <int G>
 __host__ __device__ constexpr int stage_bytes_update() { return 2 * kNsUpdate * 32 * G * 4; }
 
-template <int G, bool WIDE, bool STG>
+// VD: with the implicit vertical diffusion of the groups in ivd & ~wimpl as the epilogue of each
+// node (factors vf); its workspace is the warp's staging buffer in the staged variant (idle once
+// the node's last pass has landed), static shared memory otherwise
+template <int G, bool WIDE, bool STG, bool VD>
 __global__ void __launch_bounds__(kTB, WIDE ? 1 : (STG ? MinB<G>::node_stg : MinB<G>::update_reg))
-k32_update(DTopo tp, DGeom<float> g, B32View B, float dt) {
+k32_update(DTopo tp, DGeom<float> g, B32View B, float dt, VFactors vf) {
     __shared__ WEdges Se[kWB];
     extern __shared__ __align__(16) float dsm[];
-    float *sb = (WIDE || !STG) ? nullptr : dsm + (size_t)(threadIdx.x >> 5) * (stage_bytes_update<G>() / 4);
-    FOR_WARP_UNITS(j, node_units<WIDE>(tp)) update_unit<G, WIDE, true>(tp, g, B, dt, j, Se, sb);
+    constexpr bool kStaged = STG && !WIDE;
+    static_assert(sizeof(VdiffWarp) <= stage_bytes_update<G>(), "diffusion workspace inside the staging");
+    float *sb = kStaged ? dsm + (size_t)(threadIdx.x >> 5) * (stage_bytes_update<G>() / 4) : nullptr;
+    VdiffWarp *Vw = nullptr;
+    if constexpr (VD) {
+        if constexpr (kStaged) {
+            Vw = reinterpret_cast<VdiffWarp *>(sb);
+        } else {
+            __shared__ VdiffWarp Wsm[kWB];
+            Vw = &Wsm[threadIdx.x >> 5];
+        }
+    }
+    FOR_WARP_UNITS(j, node_units<WIDE>(tp)) update_unit<G, WIDE, true, VD>(tp, g, B, dt, j, Se, sb, &vf, Vw);
 }
 
 // ---------------------------------------------------------------------------
@@ -2360,163 +2580,11 @@ __global__ void __launch_bounds__(kTB) k32_diff(DTopo tp, DGeom<float> g, B32Vie
     FOR_WARP_UNITS(j, node_units<WIDE>(tp)) diff_unit<G, WIDE>(tp, g, B, dt, j, Se);
 }
 
-// ---------------------------------------------------------------------------
-// k32_vdiff: implicit vertical diffusion of the advected columns (in Tnew)
-// ---------------------------------------------------------------------------
-// Forward substitution tp_k = inv_k rhs_k - a_k inv_k tp_{k-1} and back substitution
-// x_k = tp_k - cp_k x_{k+1} (oce_ale_tracer.F90:1406-1422) with the column's FP64-derived
-// factors, as scans of affine maps y -> A y + B.  Each lane holds K consecutive levels of the
-// column (K = ceil(layers / 32): one warp covers the whole column): it composes its K maps in
-// registers, the warp scans the lane maps (five shuffles), and each lane then runs its K
-// levels from the carry it receives.  The multipliers A depend on the column only: the lane
-// products and their partial products at each scan step are formed once per node (shared
-// memory), so a slot's scan step is one shuffle and one multiply-add, and a column costs a slot
-// 14 shuffles whatever its depth.  rhs_k = -a_k (T_{k-1} - T_k) - c_k (T_{k+1} - T_k)
-// (+ bc_surface at the top, :1216-1229, 1377-1383); T += x.
-constexpr int kWV = 4;                    // warps (nodes) per block of the diffusion kernel
-constexpr int kScan = 5;                  // steps of a 32-lane scan
-constexpr int kVdiffMaxK = 4;             // levels per lane: columns of up to 128 layers
-
-struct VdiffWarp {
-    float4 fac[130];                      // (a, c, 1/m, c/m), 1-based levels
-    float af[kScan][32];                  // forward: lane-map product of the window at each step (0 below the offset)
-    float ab[kScan][32];                  // backward (0 past the offset)
-};
-
-// per-lane column data of a node: the factors of the lane's K levels
-template <int K>
-struct VdiffLane {
-    float a[K], c[K], inv[K], A[K], Ad[K];
-    bool ok[K];
-};
-
-template <int K, int G>
-__device__ __forceinline__ void vdiff_group(const DTopo &tp, const B32View &B, int n, int lane, int nzmin, int nzmax,
-                                            int gq, const VdiffLane<K> &V, const VdiffWarp &W) {
-    const int L1 = tp.L1;
-    const int nz0 = nzmin + lane * K;  // the lane's first level
-    float *__restrict__ Tg = grp<G>(B.Tnew, gq, B.sN);
-    const Vec<G> bc = B.fsurf ? vld<G>(B.fsurf, gq * tp.N2 + n) : vfill<G>(0.f);
-    Vec<G> a[K], y[K];
-#pragma unroll
-    for (int t = 0; t < K; t++) a[t] = vldc<G>(V.ok[t], Tg, n * L1 + nz0 + t - 1);
-#pragma unroll
-    for (int c = 0; c < G; c++) {
-        // the levels next to the lane's ends come from the neighbouring lanes
-        const float up = sh_up(a[K - 1].c[c], 1), dn = sh_dn(a[0].c[c], 1);
-        float bl = 0.f;  // the lane's composed forward map applied to 0
-#pragma unroll
-        for (int t = 0; t < K; t++) {
-            const int nz = nz0 + t;
-            const float tu = t > 0 ? a[t - 1].c[c] : up, td = t < K - 1 ? a[t + 1].c[c] : dn;
-            const float tc = a[t].c[c];
-            float r = 0.f;
-            if (nz > nzmin) r -= V.a[t] * (tu - tc);
-            if (nz < nzmax - 1) r -= V.c[t] * (td - tc);
-            if (nz == nzmin) r += bc.c[c];
-            y[t].c[c] = V.ok[t] ? r * V.inv[t] : 0.f;
-            bl = fmaf(V.A[t], bl, y[t].c[c]);
-        }
-        // inclusive scan of the lane maps: bl = tp at the lane's last level
-#pragma unroll
-        for (int s = 0, off = 1; s < kScan; s++, off <<= 1) bl = fmaf(W.af[s][lane], __shfl_up_sync(kFull, bl, off), bl);
-        float yv = __shfl_up_sync(kFull, bl, 1);
-        if (lane == 0) yv = 0.f;
-#pragma unroll
-        for (int t = 0; t < K; t++) {
-            yv = fmaf(V.A[t], yv, y[t].c[c]);
-            y[t].c[c] = yv;
-        }
-        // back substitution: the lane's composed backward map, the suffix scan, the lane's levels
-        float xl = 0.f;
-#pragma unroll
-        for (int t = K - 1; t >= 0; t--) xl = fmaf(V.Ad[t], xl, y[t].c[c]);
-#pragma unroll
-        for (int s = 0, off = 1; s < kScan; s++, off <<= 1)
-            xl = fmaf(W.ab[s][lane], __shfl_down_sync(kFull, xl, off), xl);
-        float xv = __shfl_down_sync(kFull, xl, 1);
-        if (lane == 31) xv = 0.f;
-#pragma unroll
-        for (int t = K - 1; t >= 0; t--) {
-            xv = fmaf(V.Ad[t], xv, y[t].c[c]);
-            y[t].c[c] = a[t].c[c] + xv;
-        }
-    }
-#pragma unroll
-    for (int t = 0; t < K; t++) {
-        if (!V.ok[t]) continue;
-        bool fin = true;
-#pragma unroll
-        for (int c = 0; c < G; c++) fin = fin && isfinite(y[t].c[c]);
-        vst<G>(Tg, n * L1 + nz0 + t - 1, y[t]);
-        if (!fin) atomicOr(B.status, 1u);
-    }
-}
-
-template <int K, int G>
-__device__ __forceinline__ void vdiff_node(const DTopo &tp, const B32View &B, int n, int lane, int nzmin, int nzmax,
-                                           VdiffWarp &W) {
-    VdiffLane<K> V;
-    float A = 1.f, Ad = 1.f;
-#pragma unroll
-    for (int t = 0; t < K; t++) {
-        const int nz = nzmin + lane * K + t;
-        V.ok[t] = nz <= nzmax - 1;
-        const float4 fz = V.ok[t] ? W.fac[nz] : make_float4(0.f, 0.f, 0.f, 0.f);
-        V.a[t] = fz.x;
-        V.c[t] = fz.y;
-        V.inv[t] = fz.z;
-        // levels past the column's end are identity maps
-        V.A[t] = V.ok[t] ? -(fz.x * fz.z) : 1.f;
-        V.Ad[t] = V.ok[t] ? -fz.w : 1.f;
-        A *= V.A[t];
-        Ad *= V.Ad[t];
-    }
-    // partial products of the lane maps at each scan step
-#pragma unroll
-    for (int s = 0, off = 1; s < kScan; s++, off <<= 1) {
-        W.af[s][lane] = lane >= off ? A : 0.f;
-        W.ab[s][lane] = lane + off < 32 ? Ad : 0.f;
-        const float Ap = __shfl_up_sync(kFull, A, off), An = __shfl_down_sync(kFull, Ad, off);
-        if (lane >= off) A *= Ap;
-        if (lane + off < 32) Ad *= An;
-    }
-    __syncwarp();
-    unsigned long long todo = (B.ivd & ~B.wimpl) & (B.ng >= 64 ? ~0ull : ((1ull << B.ng) - 1));
-    while (todo) {
-        const int gq = __ffsll((long long)todo) - 1;
-        todo &= todo - 1;
-        vdiff_group<K, G>(tp, B, n, lane, nzmin, nzmax, gq, V, W);
-    }
-}
-
-template <int G>
-__device__ __forceinline__ void vdiff_unit(const DTopo &tp, const B32View &B, const VFactors &vf, int n,
-                                           VdiffWarp &W) {
-    const int lane = threadIdx.x & 31;
-    if (n >= tp.N2) return;
-    const int L1 = tp.L1;
-    const int nzmin = tp.n_ulev[n], nzmax = tp.n_nlev[n];
-    const int K = (nzmax - nzmin + 31) / 32;
-    __syncwarp();  // the previous node's reads of W are done
-    for (int nz = nzmin + lane; nz <= nzmax - 1; nz += 32) {
-        const int i = n * L1 + nz - 1;
-        W.fac[nz] = make_float4(vf.a[i], vf.c[i], vf.inv[i], vf.cp[i]);
-    }
-    __syncwarp();
-    switch (K) {
-        case 1: vdiff_node<1, G>(tp, B, n, lane, nzmin, nzmax, W); break;
-        case 2: vdiff_node<2, G>(tp, B, n, lane, nzmin, nzmax, W); break;
-        case 3: vdiff_node<3, G>(tp, B, n, lane, nzmin, nzmax, W); break;
-        default: vdiff_node<4, G>(tp, B, n, lane, nzmin, nzmax, W); break;
-    }
-}
-
 template <int G>
 __global__ void __launch_bounds__(32 * kWV) k32_vdiff(DTopo tp, B32View B, VFactors vf) {
     __shared__ VdiffWarp Wsm[kWV];
     const int warp = threadIdx.x >> 5;
-    for (int n = blockIdx.x * kWV + warp; n < tp.N2; n += gridDim.x * kWV) vdiff_unit<G>(tp, B, vf, n, Wsm[warp]);
+    for (int n = blockIdx.x * kWV + warp; n < tp.N2; n += gridDim.x * kWV) vdiff_unit<G, false>(tp, B, vf, n, Wsm[warp]);
 }
 
 // ---------------------------------------------------------------------------
@@ -2777,7 +2845,8 @@ static cudaError_t prepare_g() {
     set((const void *)k32_lo_ad<G, false, false, true>, smem_lo_ad<G>());
     set((const void *)k32_lo_ad<G, false, true, true>, smem_lo_ad<G>());
     set((const void *)k32_bounds<G, false, true>, smem_bounds<G>());
-    set((const void *)k32_update<G, false, true>, smem_update<G>());
+    set((const void *)k32_update<G, false, true, false>, smem_update<G>());
+    set((const void *)k32_update<G, false, true, true>, smem_update<G>());
     set((const void *)k32_ho<G, true>, smem_ho<G>());
     return e;
 }
@@ -2814,12 +2883,19 @@ static void bounds_g(const DTopo &tp, const DGeom<float> &g, const B32View &B, d
     else k32_bounds<G, false, false><<<grid_units(tp.N2, sh), kTB, 0, s>>>(tp, g, B, (float)dt);
     if (tp.n_wide) k32_bounds<G, true, false><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
 }
+template <int G, bool VD>
+static void update_gv(const DTopo &tp, const DGeom<float> &g, const B32View &B, double dt, const LaunchShape &sh,
+                      const VFactors &vf, cudaStream_t s) {
+    const float d = (float)dt;
+    if (sh.staged) k32_update<G, false, true, VD><<<grid_units(tp.N2, sh), kTB, smem_update<G>(), s>>>(tp, g, B, d, vf);
+    else k32_update<G, false, false, VD><<<grid_units(tp.N2, sh), kTB, 0, s>>>(tp, g, B, d, vf);
+    if (tp.n_wide) k32_update<G, true, false, VD><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, d, vf);
+}
 template <int G>
 static void update_g(const DTopo &tp, const DGeom<float> &g, const B32View &B, double dt, const LaunchShape &sh,
-                     cudaStream_t s) {
-    if (sh.staged) k32_update<G, false, true><<<grid_units(tp.N2, sh), kTB, smem_update<G>(), s>>>(tp, g, B, (float)dt);
-    else k32_update<G, false, false><<<grid_units(tp.N2, sh), kTB, 0, s>>>(tp, g, B, (float)dt);
-    if (tp.n_wide) k32_update<G, true, false><<<grid_nodes(tp.n_wide), kTB, 0, s>>>(tp, g, B, (float)dt);
+                     const VFactors *vf, cudaStream_t s) {
+    if (vf) update_gv<G, true>(tp, g, B, dt, sh, *vf, s);
+    else update_gv<G, false>(tp, g, B, dt, sh, VFactors{}, s);
 }
 void b32_lo_ad(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, const B32View &B, const float *VF,
                double dt, const LaunchShape &sh, cudaStream_t s) {
@@ -2848,9 +2924,9 @@ void b32_bounds(const DTopo &tp, const DGeom<float> &g, const B32View &B, double
     else bounds_g<2>(tp, g, B, dt, sh, s);
 }
 void b32_update(const DTopo &tp, const DGeom<float> &g, const B32View &B, double dt, const LaunchShape &sh,
-                cudaStream_t s) {
-    if (B.G == 4) update_g<4>(tp, g, B, dt, sh, s);
-    else update_g<2>(tp, g, B, dt, sh, s);
+                const VFactors *vf, cudaStream_t s) {
+    if (B.G == 4) update_g<4>(tp, g, B, dt, sh, vf, s);
+    else update_g<2>(tp, g, B, dt, sh, vf, s);
 }
 void b32_vdiff(const DTopo &tp, const DForcing<float> &, const B32View &B, const VFactors &v, cudaStream_t s) {
     if (B.G == 4) k32_vdiff<4><<<(tp.N2 + kWV - 1) / kWV, 32 * kWV, 0, s>>>(tp, B, v);

@@ -331,8 +331,9 @@ class Context:
         self._chk(self.L.fesom_gpu_set_launch_shape(self.h, int(stage), int(blocks_per_sm)))
 
     def set_stage_variant(self, stage: int, variant: int):
-        """FP32 form: kernel variant of stage 0 lo_ad, 1 ho, 2 bounds, 3 update (0: gathers in registers,
-        1: staged in shared memory)."""
+        """FP32 form: kernel variant of stage 0 lo_ad, 1 ho, 2 bounds, 3 update (bit 0 clear: gathers
+        in registers, set: staged in shared memory; stage 3, bit 1: the implicit vertical diffusion
+        as its own kernel instead of the update's per-node epilogue)."""
         self._chk(self.L.fesom_gpu_set_stage_variant(self.h, int(stage), int(variant)))
 
     def autotune(self, dt: float, steps: int = 2) -> dict:

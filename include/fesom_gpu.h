@@ -310,14 +310,16 @@ int fesom_gpu_set_stage_tracers(fesom_gpu_ctx *ctx, int32_t stage, int32_t trace
  * launches one warp per unit. */
 int fesom_gpu_set_launch_shape(fesom_gpu_ctx *ctx, int32_t stage, int32_t blocks_per_sm);
 /* Performance setting of the FP32 form: kernel variant of stage 0 (lo_ad), 1 (the edge fluxes),
- * 2 (bounds) or 3 (update): 0 gathers each pass's entries into registers, 1 stages them in shared
- * memory with asynchronous copies while the previous pass computes (fewer resident warps, no
- * register limit on the gathers in flight).  Defaults: lo_ad 1, the others 0.  The two variants
- * are separate compilations and agree to FP32 round-off. */
+ * 2 (bounds) or 3 (update): bit 0 clear gathers each pass's entries into registers, set stages
+ * them in shared memory with asynchronous copies while the previous pass computes (fewer resident
+ * warps, no register limit on the gathers in flight).  Stage 3 only, bit 1 (values 2, 3): the
+ * implicit vertical diffusion runs as its own kernel after the update; clear (the default), each
+ * node's column is diffused by the warp that has just updated it, in the same launch.  Defaults:
+ * lo_ad 1, the others 0.  The variants are separate compilations and agree to FP32 round-off. */
 int fesom_gpu_set_stage_variant(fesom_gpu_ctx *ctx, int32_t stage, int32_t variant);
 /* Autotuner of the FP32 form's launch settings (results do not change): times the step of the
  * context's own state under the library defaults, then by coordinate descent over the four node/edge
- * stages under both kernel variants, blocks per SM (0, 2, 4) and, for bounds and update with more
+ * stages under each kernel variant, blocks per SM (0, 2, 4) and, for bounds and update with more
  * than 8 tracer slots, 8 tracers per launch; a candidate is kept when it is more than 1 % faster.
  * Each candidate runs one untimed and `steps` timed steps (CUDA events on the context's stream).
  * The fastest settings stay on the context; the tracer state and its time levels are restored

@@ -37,3 +37,8 @@ def test_roofline_byte_formulas():
     # the bounds and update passes: 7 N3 + E3 per tracer, hnode_new and areasvol shared
     assert sb["bounds"] == sb["update"] == 4 * (6 * (5 * N3 + E3) + 2 * N3)
     assert set(bench.MEASURED_DRAM_B_PER_TRACER_DOF) <= set(sb)
+    # the update with the vertical diffusion as its epilogue: no T* round trip, the factors read
+    assert bench.algorithmic_bytes(c, 24, 4, vdiff_fused=True) == 4 * (24 * (16 * N3 + 3 * E3) + 3 * T3 + 14 * N3)
+    sf = bench.stage_bytes(c, 6, 4, vdiff_fused=True)
+    assert "vdiff" not in sf and sf["update"] == 4 * (6 * (5 * N3 + E3) + 6 * N3)
+    assert sum(sf.values()) == sum(sb.values()) - 4 * 6 * 2 * N3

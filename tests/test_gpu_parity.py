@@ -345,16 +345,19 @@ def test_fp32_mixed_schemes_in_one_batch(basin_irregular):
 def test_fp32_stage_passes_do_not_change_results(meshname, kind, request):
     """Tracers per launch of each node stage (fesom_gpu_set_stage_tracers), the grid of the
     stage kernels (fesom_gpu_set_launch_shape) and their variant (fesom_gpu_set_stage_variant:
-    gathers in registers or staged in shared memory) are performance settings.  Splits and
-    grids run the same code and give the same bits; the two variants of a stage are separate
-    compilations whose products may contract differently, so they agree to FP32 round-off."""
+    gathers in registers or staged in shared memory; the implicit vertical diffusion as the
+    update's per-node epilogue or as its own kernel) are performance settings.  Splits, grids and
+    the place of the diffusion run the same code and give the same bits; the register and staged
+    variants of a stage are separate compilations whose products may contract differently, so
+    they agree to FP32 round-off."""
     mesh = request.getfixturevalue(meshname)
     f, tr = _setup(mesh, kind, ntr=7)
     cfgs = [G.tra_cfg(["MUSCL", "MFCT", "UPW1"][k % 3], ["QR4C", "UPW1", "PPM", "CDIFF"][k % 4],
                       "FCT" if k % 3 else "NON", id=k + 1) for k in range(7)]
     combos = (([0, 0, 0, 0], [0, 0, 0, 0], [1, 0, 0, 0]), ([3, 2, 5, 1], [2, 3, 1, 2], [1, 0, 0, 0]),
               ([1, 7, 2, 4], [0, 0, 0, 0], [1, 0, 0, 0]), ([3, 2, 5, 1], [0, 0, 0, 0], [0, 1, 1, 1]),
-              ([1, 7, 2, 4], [1, 2, 2, 1], [0, 1, 1, 1]))
+              ([1, 7, 2, 4], [1, 2, 2, 1], [0, 1, 1, 1]), ([0, 0, 0, 0], [0, 0, 0, 0], [1, 0, 0, 2]),
+              ([3, 2, 5, 1], [0, 0, 0, 0], [0, 1, 1, 3]), ([3, 2, 5, 1], [2, 3, 1, 2], [1, 0, 0, 2]))
     outs = []
     for split, shape, variant in combos:
         ctx = G.Context(mesh, G.PREC_FP32, max_tracers=7)
@@ -374,7 +377,7 @@ def test_fp32_stage_passes_do_not_change_results(meshname, kind, request):
         assert ctx.status() == 0
         ctx.close()
     # same variant: bit for bit
-    for i, ref in ((1, 0), (2, 0), (4, 3)):
+    for i, ref in ((1, 0), (2, 0), (4, 3), (5, 0), (6, 3), (7, 0)):
         for k in range(7):
             assert np.array_equal(outs[i][k], outs[ref][k]), (i, k)
     # other variant: FP32 round-off
@@ -428,7 +431,8 @@ def test_autotune_keeps_the_state_and_the_results(sphere_small):
             res = ctx.autotune(f.dt, steps=1)
             assert res["candidates"] >= 2 and res["tuned_ms"] <= res["default_ms"]
             assert all(b in (0, 2, 4) for b in res["blocks_per_sm"])
-            assert all(t in (0, 8) for t in res["stage_tracers"]) and all(v in (0, 1) for v in res["variant"])
+            assert all(t in (0, 8) for t in res["stage_tracers"])
+            assert all(v in (0, 1) for v in res["variant"][:3]) and res["variant"][3] in (0, 1, 2, 3)
             for k in range(12):
                 v, o = ctx.tracer_download(k, dtype=np.float32)
                 assert np.array_equal(v, before[k][0]) and np.array_equal(o, before[k][1])
