@@ -2431,9 +2431,9 @@ void enqueue_batch_step(fesom_gpu_batch *b, cudaStream_t s) {
         bm32_bounds(I, b->ix_n, false, s);
         if (wide) bm32_bounds(I, b->ix_w, true, s);
     }
+    // (the implicit vertical diffusion runs inside the update, per node)
     bm32_update(I, b->ix_n, false, s);
     if (wide) bm32_update(I, b->ix_w, true, s);
-    if (b->any_vd) bm32_vdiff(I, b->ix_n, s);
     if (b->any_wimpl) bm32_vdiff_w(I, b->ix_n, s);
 }
 
@@ -2555,7 +2555,9 @@ int fesom_gpu_batch_launches_per_step(fesom_gpu_batch *b, int32_t *launches) {
     if (!b || !launches) return FESOM_ERR_ARG;
     const bool wide = b->ix_w.start[b->ix_w.n] > 0;
     const int k = wide ? 2 : 1;
-    int n = 1 + (b->any_vd ? 2 : 0) + k * (2 + (b->any_fct ? 1 : 0) + (b->any_diff ? 1 : 0)) + 1 +
+    // vflux, vfactors (the diffusion itself runs inside the update), lo_ad and update (+ bounds,
+    // diff) per node range, ho (+ its node-mean items), the optional stages
+    int n = 1 + (b->any_vd ? 1 : 0) + k * (2 + (b->any_fct ? 1 : 0) + (b->any_diff ? 1 : 0)) + 1 +
             (b->ix_it.start[b->ix_it.n] ? 1 : 0) + (b->any_hd ? 1 : 0) + (b->any_ppm ? 1 : 0) +
             (b->any_lo_impl ? 1 : 0) + (b->any_wimpl ? 1 : 0);
     *launches = n;

@@ -245,7 +245,6 @@ void bm32_vdiff_w(const Inst32 *, const MultiIdx &nodes, cudaStream_t);
 void bm32_ho(const Inst32 *, const MultiIdx &edges, const MultiIdx &items, cudaStream_t);
 void bm32_bounds(const Inst32 *, const MultiIdx &, bool wide, cudaStream_t);
 void bm32_update(const Inst32 *, const MultiIdx &, bool wide, cudaStream_t);
-void bm32_vdiff(const Inst32 *, const MultiIdx &, cudaStream_t);
 void bm32_hdiff(const Inst32 *, const MultiIdx &edges, cudaStream_t);
 void bm32_diff(const Inst32 *, const MultiIdx &nodes, bool wide, cudaStream_t);
 

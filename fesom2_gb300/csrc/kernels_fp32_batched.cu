@@ -17,10 +17,11 @@
 //   k32_bounds       per node: FCT bounds (max/min of LO and T over the node's
 //                    neighbours and the adjacent layers) and R+/R- (oce_adv_tra_fct.F90)
 //   k32_update       per node: limited fluxes, flux divergence, T* update, written to
-//                    the buffer of the oldest time level
+//                    the buffer of the oldest time level; then, by default, the same warp
+//                    runs the node's implicit vertical diffusion (k32_vdiff's column solve)
 //   k32_vdiff        per node: the implicit vertical diffusion as two warp scans of
 //                    affine maps over the column (forward and back substitution with
-//                    the FP64-formed factors)
+//                    the FP64-formed factors); its own launch only when asked for
 //   k32_vppm, k32_lo_impl, k32_vdiff_w, k32_hdiff, k32_diff
 //                    the optional parts: PPM vertical fluxes, the split vertical
 //                    velocity, horizontal and explicit vertical diffusion
@@ -1587,7 +1588,6 @@ k32_bounds(DTopo tp, DGeom<float> g, B32View B, float dt) {
 // its values are read at L2.
 constexpr int kWV = 4;                    // warps (nodes) per block of the diffusion kernel
 constexpr int kScan = 5;                  // steps of a 32-lane scan
-constexpr int kVdiffMaxK = 4;             // levels per lane: columns of up to 128 layers
 
 struct VdiffWarp {
     float4 fac[130];                      // (a, c, 1/m, c/m), 1-based levels
@@ -2742,24 +2742,27 @@ __global__ void __launch_bounds__(kTB, WIDE ? 1 : MinB<4>::node_reg) k32m_bounds
         else bounds_unit<2, WIDE, true>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se, nullptr);
     }
 }
+// each node's column is then diffused by the same warp where its instance has groups in
+// ivd & ~wimpl (as k32_update with the diffusion epilogue)
 template <bool WIDE>
 __global__ void __launch_bounds__(kTB, WIDE ? 1 : MinB<4>::node_reg) k32m_update(const Inst32 *__restrict__ I, MultiIdx ix) {
     __shared__ WEdges Se[kWB];
+    __shared__ VdiffWarp Wsm[kWB];
+    VdiffWarp *Vw = &Wsm[threadIdx.x >> 5];
     FOR_WARP_UNITS(u, ix.start[ix.n]) {
         const int i = find_inst(ix, u);
-        if (I[i].B.G == 4) update_unit<4, WIDE, true>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se, nullptr);
-        else update_unit<2, WIDE, true>(I[i].tp, I[i].g, I[i].B, I[i].dt, u - ix.start[i], Se, nullptr);
+        const Inst32 &d = I[i];
+        const bool vd = (d.B.ivd & ~d.B.wimpl) != 0;
+        const int j = u - ix.start[i];
+        if (d.B.G == 4) {
+            if (vd) update_unit<4, WIDE, true, true>(d.tp, d.g, d.B, d.dt, j, Se, nullptr, &d.vf, Vw);
+            else update_unit<4, WIDE, true>(d.tp, d.g, d.B, d.dt, j, Se, nullptr);
+        } else {
+            if (vd) update_unit<2, WIDE, true, true>(d.tp, d.g, d.B, d.dt, j, Se, nullptr, &d.vf, Vw);
+            else update_unit<2, WIDE, true>(d.tp, d.g, d.B, d.dt, j, Se, nullptr);
+        }
     }
 }
-__global__ void __launch_bounds__(32 * kWV) k32m_vdiff(const Inst32 *__restrict__ I, MultiIdx ix) {
-    __shared__ VdiffWarp Wsm[kWV];
-    for (int u = blockIdx.x * kWV + (threadIdx.x >> 5); u < ix.start[ix.n]; u += gridDim.x * kWV) {
-        const int i = find_inst(ix, u);
-        if (I[i].B.G == 4) vdiff_unit<4>(I[i].tp, I[i].B, I[i].vf, u - ix.start[i], Wsm[threadIdx.x >> 5]);
-        else vdiff_unit<2>(I[i].tp, I[i].B, I[i].vf, u - ix.start[i], Wsm[threadIdx.x >> 5]);
-    }
-}
-
 __global__ void __launch_bounds__(kTB) k32m_vppm(const Inst32 *__restrict__ I, MultiIdx ix) {
     FOR_WARP_UNITS(u, ix.start[ix.n]) {
         const int i = find_inst(ix, u);
@@ -3097,10 +3100,6 @@ void bm32_diff(const Inst32 *I, const MultiIdx &ix, bool wide, cudaStream_t s) {
     if (!u) return;
     if (wide) k32m_diff<true><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
     else k32m_diff<false><<<grid_nodes(u), kTB, 0, s>>>(I, ix);
-}
-void bm32_vdiff(const Inst32 *I, const MultiIdx &ix, cudaStream_t s) {
-    const int u = ix.start[ix.n];
-    if (u) k32m_vdiff<<<(u + kWV - 1) / kWV, 32 * kWV, 0, s>>>(I, ix);
 }
 
 }  // namespace fesom
