@@ -58,8 +58,8 @@ def parse():
     p.add_argument("--profile-only", action="store_true", help="one warm step + one profiled step (for ncu)")
     p.add_argument("--no-tune", action="store_true",
                    help="no autotuning: the library's launch settings and the generators' node order")
-    p.add_argument("--order", default="auto", choices=["auto", "morton", "rcm"],
-                   help="node order of the single-mesh workload (auto: the faster step of the two, timed)")
+    p.add_argument("--order", default="auto", choices=["auto", "morton", "rcm", "hilbert"],
+                   help="node order of the single-mesh workload (auto: the fastest step of the three, timed)")
     p.add_argument("--no-config5", action="store_true", help="skip the configuration-5 sub-run of the default line")
     p.add_argument("--width", type=int, default=0, help="FP32 tracer-group width (0: automatic, 2, 4)")
     p.add_argument("--stage-tr", default="", help="tracers per launch of lo_ad,ho,bounds,update (e.g. 8,0,8,8)")
@@ -372,20 +372,25 @@ def order_trial(mesh, forcing, tracers, dt, args, steps=2):
 
 
 def choose_order(args, mesh, forcing, tracers, dt, rank):
-    """Node order of the workload: the generators' Morton order or reverse Cuthill-McKee of the
-    node graph, the faster FP32 step when timed (--order auto, the benchmark mesh at full size)."""
+    """Node order of the workload: the generators' Morton order, reverse Cuthill-McKee of the
+    node graph or a Hilbert curve through the node positions, the fastest FP32 step when timed
+    (--order auto, the benchmark mesh at full size)."""
     if args.order == "morton" or (args.order == "auto" and (args.no_tune or args.scale != 1.0 or args.profile_only)):
         return {"chosen": "morton", "timed": False}
     from fesom2_gb300 import batch as Bt
-    order = Bt.rcm_order(mesh)
-    if args.order == "rcm":
-        return {"chosen": "rcm", "timed": False, "_order": order}
+    make = {"rcm": Bt.rcm_order, "hilbert": Bt.hilbert_order}
+    if args.order in make:
+        return {"chosen": args.order, "timed": False, "_order": make[args.order](mesh)}
     ms = {"morton": order_trial(mesh, forcing, tracers, dt, args)}
-    pm = Bt.permute_nodes(mesh, order)
-    ms["rcm"] = order_trial(pm, Bt.permute_forcing(forcing, order), np.ascontiguousarray(tracers[:, order]), dt, args)
-    del pm
+    orders = {}
+    for name, fn in make.items():
+        orders[name] = fn(mesh)
+        pm = Bt.permute_nodes(mesh, orders[name])
+        ms[name] = order_trial(pm, Bt.permute_forcing(forcing, orders[name]),
+                               np.ascontiguousarray(tracers[:, orders[name]]), dt, args)
+        del pm
     best = min(ms, key=ms.get)
-    return {"chosen": best, "timed": True, "ms_per_step": ms, "_order": order}
+    return {"chosen": best, "timed": True, "ms_per_step": ms, "_order": orders.get(best)}
 
 
 def run_ours(args, rank, world, local_rank):
@@ -410,7 +415,7 @@ def run_ours(args, rank, world, local_rank):
     mesh, kind, forcing, tracers, dt, wname, gen_s = workload(args.config, args.scale, args.tracers)
     ntr = tracers.shape[0]
     node_order = choose_order(args, mesh, forcing, tracers, dt, rank)
-    if node_order["chosen"] == "rcm":
+    if node_order["chosen"] != "morton":
         from fesom2_gb300 import batch as Bt
         order = node_order.pop("_order")
         mesh = Bt.permute_nodes(mesh, order)

@@ -55,6 +55,32 @@ def test_permuted_mesh_gives_the_permuted_step(basin_irregular):
     assert np.abs(a[order][wet[order]] - b[wet[order]]).max() <= 1e-12 * np.abs(a[wet]).max()
 
 
+def test_hilbert_key_walks_the_grid_in_unit_steps():
+    """The Hilbert index of every point of a full 2^b grid (2-D and 3-D) is a bijection onto
+    0..N-1, and points with consecutive indices are one grid step apart."""
+    for n, bits in ((2, 5), (3, 3), (3, 4)):
+        g = np.stack(np.meshgrid(*[np.arange(1 << bits)] * n, indexing="ij"), -1).reshape(-1, n)
+        k = Bt.hilbert_key(g, bits)
+        assert np.array_equal(np.sort(k), np.arange(len(g)))
+        walk = g[np.argsort(k)]
+        assert np.all(np.abs(np.diff(walk, axis=0)).sum(1) == 1)
+
+
+@pytest.mark.parametrize("meshname", ["basin_irregular", "sphere_small"])
+def test_hilbert_order_is_a_local_permutation(meshname, request):
+    """hilbert_order is a permutation of the nodes, and along it consecutive nodes lie closer
+    together than along a random order (a locality check, on a cartesian and a spherical mesh)."""
+    mesh = request.getfixturevalue(meshname)
+    order = Bt.hilbert_order(mesh)
+    assert np.array_equal(np.sort(order), np.arange(mesh.nod2D))
+    lon, lat = mesh.coord_nod2D[:, 0], mesh.coord_nod2D[:, 1]
+    p = np.stack([lon, lat], 1) if mesh.cartesian else \
+        np.stack([np.cos(lat) * np.cos(lon), np.cos(lat) * np.sin(lon), np.sin(lat)], 1)
+    step = lambda o: np.median(np.linalg.norm(np.diff(p[o], axis=0), axis=1))
+    rnd = np.random.default_rng(0).permutation(mesh.nod2D)
+    assert step(order) < 0.2 * step(rnd)
+
+
 def _rank_main(rank, world, port, out_dir):
     import torch.distributed as dist
     os.environ["MASTER_ADDR"] = "127.0.0.1"

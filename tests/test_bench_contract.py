@@ -42,3 +42,31 @@ def test_roofline_byte_formulas():
     sf = bench.stage_bytes(c, 6, 4, vdiff_fused=True)
     assert "vdiff" not in sf and sf["update"] == 4 * (6 * (5 * N3 + E3) + 6 * N3)
     assert sum(sf.values()) == sum(sb.values()) - 4 * 6 * 2 * N3
+
+
+def test_node_order_choice_times_every_candidate(sphere_small, monkeypatch):
+    """--order auto times the generators' order, reverse Cuthill-McKee and the Hilbert curve and
+    keeps the fastest with its permutation; an explicit order is taken untimed (the trial stubbed:
+    no GPU here)."""
+    import numpy as np
+
+    mesh = sphere_small
+    f = M.make_forcing(mesh, "sphere", seed=3, dt=600.0)
+    T = M.make_tracers(mesh, "sphere", ntr=2, seed=4, dtype=np.float32)
+    seen = []
+
+    def trial(m, forcing, tracers, dt, args, steps=2):
+        seen.append((m.nod2D, tracers.shape))
+        return {0: 10.0, 1: 12.0, 2: 9.0}[len(seen) - 1]
+
+    monkeypatch.setattr(bench, "order_trial", trial)
+    args = bench.argparse.Namespace(order="auto", no_tune=False, scale=1.0, profile_only=False, width=0)
+    r = bench.choose_order(args, mesh, f, T, 600.0, 0)
+    assert r["timed"] and set(r["ms_per_step"]) == {"morton", "rcm", "hilbert"} and r["chosen"] == "hilbert"
+    assert len(seen) == 3 and all(s == (mesh.nod2D, T.shape) for s in seen)
+    assert np.array_equal(np.sort(r["_order"]), np.arange(mesh.nod2D))
+    args.order = "rcm"
+    r = bench.choose_order(args, mesh, f, T, 600.0, 0)
+    assert r["chosen"] == "rcm" and not r["timed"] and len(r["_order"]) == mesh.nod2D
+    args.order, args.no_tune = "auto", True
+    assert bench.choose_order(args, mesh, f, T, 600.0, 0) == {"chosen": "morton", "timed": False}
