@@ -2359,7 +2359,7 @@ struct fesom_gpu_batch {
     cudaStream_t stream = nullptr;
     Inst32 *d_inst = nullptr;  // ab descriptor sets (one per rotation phase), inst.size() each
     double d_dt = -1.0;
-    MultiIdx ix_e{}, ix_vfb{}, ix_n{}, ix_w{}, ix_it{};
+    MultiIdx ix_e{}, ix_n{}, ix_w{}, ix_it{};
     int maxL1 = 0;
     bool any_vd = false, any_fct = false, any_hd = false, any_diff = false;
     bool any_ws = false, any_ppm = false, any_lo_impl = false, any_wimpl = false;
@@ -2416,7 +2416,7 @@ void enqueue_batch_step(fesom_gpu_batch *b, cudaStream_t s) {
     const Inst32 *I = b->d_inst + (size_t)b->phase * b->inst.size();
     const bool wide = b->ix_w.start[b->ix_w.n] > 0;
     bm32_vflux(I, b->ix_e, s);
-    if (b->any_vd) bm32_vfactors(I, b->ix_vfb, s);
+    if (b->any_vd) bm32_vfactors(I, b->ix_n, s);
     bm32_lo_ad(I, b->ix_n, false, b->any_ws, s);
     if (wide) bm32_lo_ad(I, b->ix_w, true, b->any_ws, s);
     if (b->any_ppm) bm32_vppm(I, b->ix_n, s);
@@ -2450,7 +2450,7 @@ int fesom_gpu_batch_create(fesom_gpu_ctx *const *ctxs, int32_t n, fesom_gpu_batc
         b->err = "a batch holds 1 to 64 FP32 contexts";
         return FESOM_ERR_ARG;
     }
-    std::vector<int> ce, cvb, cn, cw, cit;
+    std::vector<int> ce, cn, cw, cit;
     for (int i = 0; i < n; i++) {
         fesom_gpu_ctx *c = ctxs[i];
         if (!c || c->prec != FESOM_PREC_FP32) { b->err = "batch instances must be FP32 contexts"; return FESOM_ERR_ARG; }
@@ -2483,13 +2483,11 @@ int fesom_gpu_batch_create(fesom_gpu_ctx *const *ctxs, int32_t n, fesom_gpu_batc
         b->maxL1 = std::max(b->maxL1, c->L1);
         b->inst.push_back(c);
         ce.push_back(c->E2);
-        cvb.push_back((c->N2 + kVfCols - 1) / kVfCols);
         cn.push_back(c->N2);
         cw.push_back(c->tp.n_wide);
         cit.push_back(c->mw.n_items);
     }
     set_prefix(b->ix_e, ce);
-    set_prefix(b->ix_vfb, cvb);
     set_prefix(b->ix_n, cn);
     set_prefix(b->ix_w, cw);
     set_prefix(b->ix_it, cit);

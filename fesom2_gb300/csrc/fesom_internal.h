@@ -231,7 +231,6 @@ struct Inst32 {
     double *scratch;  // the instance's column scratch (split vertical velocity)
 };
 constexpr int kMaxInst = 64;
-constexpr int kVfCols = 128;  // columns per block of the diffusion-factor kernel
 struct MultiIdx {
     int n;
     int start[kMaxInst + 1];

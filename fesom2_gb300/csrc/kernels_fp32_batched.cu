@@ -4,10 +4,11 @@
 //
 //   k32_vflux        edge volume fluxes per edge-layer (oce_adv_tra_hor.F90:159-250
 //                    segment rule); shared by every tracer
-//   k32_vfactors     FP64 factorisation of the implicit vertical-diffusion matrix of
-//                    every column (oce_ale_tracer.F90:1088-1204, 1406-1414): the
-//                    pivots m = b - cp*a carry the cancellation that thin bottom cells
-//                    cause, so they are formed in FP64; stored as FP32 a, c, 1/m, c/m
+//   k32_vfactors     factorisation of the implicit vertical-diffusion matrix of every
+//                    column (oce_ale_tracer.F90:1088-1204, 1406-1414): the pivots
+//                    m = b - cp*a, where thin bottom cells cancel most bits, are formed
+//                    in FP32 from their excess over |c|, a recurrence of non-negative
+//                    terms; stored as FP32 a, c, 1/m, c/m
 //   k32_lo_ad        per node: the LO solution (edge gather of upwind fluxes + upwind
 //                    vertical flux with w_e) and the vertical antidiffusive flux
 //                    (QR4C / UPW1 / CDIFF on the AB values; PPM in k32_vppm)
@@ -130,6 +131,10 @@ __device__ __forceinline__ float qdiv(float a, float b) { return __fdividef(a, b
 
 }  // namespace
 
+// the value of the lane d below / above in the warp
+__device__ __forceinline__ float sh_up(float v, int d) { return __shfl_up_sync(kFull, v, d); }
+__device__ __forceinline__ float sh_dn(float v, int d) { return __shfl_down_sync(kFull, v, d); }
+
 // ---------------------------------------------------------------------------
 // k32_vflux: volume flux of every edge-layer (shared by all tracers)
 // ---------------------------------------------------------------------------
@@ -176,122 +181,105 @@ __global__ void __launch_bounds__(kTB) k32_vflux(DTopo tp, DGeom<float> g, DForc
 }
 
 // ---------------------------------------------------------------------------
-// k32_vfactors: FP64 factorisation of each column's tridiagonal system
+// k32_vfactors: factorisation of each column's tridiagonal system
 // ---------------------------------------------------------------------------
 // a(k) = -Kv(k) dt/(Z_n(k-1)-Z_n(k)) area(k)/areasvol(k), c(k) = -Kv(k+1) dt/(Z_n(k)-Z_n(k+1))
 // area(k+1)/areasvol(k), b = -a - c + hnode_new (oce_ale_tracer.F90:1099-1204), with
 // Z_n(k)-Z_n(k+1) = (hnode_new(k) + hnode_new(k+1))/2 (the mid-depths of :1088-1096);
 // Thomas pivots m(k) = b(k) - cp(k-1) a(k), cp(k) = c(k)/m(k) (:1406-1414).
-// a, b, c are formed in FP32 and used with those rounded values throughout, so all
-// factors belong to one consistent system; the pivot recurrence, where thin bottom
-// cells cancel most bits, runs in FP64.  One thread per column runs the recurrence; the block's columns move through shared
-// memory in tiles of kVfK levels, loaded and stored with the lanes over the levels of a
-// column (each column's tile is one contiguous run), so no thread walks its own column
-// through the cache.
-constexpr int kVfK = 8;       // levels per tile
-__device__ __forceinline__ void vfactors_block(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
-                                               double dt, const VFactors &vf, int blk) {
-    // inputs for levels lev0 .. lev0 + kVfK (one extra: the next level's h, Kv, area);
-    // outputs for levels lev0 .. lev0 + kVfK - 1
-    __shared__ float s_hn[kVfCols][kVfK + 1], s_ar[kVfCols][kVfK + 1], s_av[kVfCols][kVfK + 1],
-        s_kv[kVfCols][kVfK + 1];
-    __shared__ float s_a[kVfCols][kVfK], s_c[kVfCols][kVfK], s_i[kVfCols][kVfK], s_p[kVfCols][kVfK];
-    __shared__ int s_lmax;
+// With a, c <= 0 and b = |a| + |c| + h, the pivot is m(k) = |c(k)| + d(k) with the excess
+// d(k) = h(k) + |a(k)| d(k-1) / (d(k-1) + |c(k-1)|) (d = h at the top layer): the textbook form
+// subtracts |a| |c(k-1)| / m(k-1) from |a| + |c| + h, which cancels most bits where a thin cell
+// (small h) sits under strong diffusion; every term of the excess form is non-negative, so FP32
+// keeps the pivots within a few ulps of the exact ones for any cell thickness.
+//
+// d(k) is a linear-fractional map of d(k-1): (d, 1) -> M_k (d, 1) projectively, with the
+// non-negative M_k = [[h + |a|, h |c(k-1)|], [1, |c(k-1)|]] (the top layer: [[0, h], [0, 1]]).
+// A warp takes a column, its lanes over 32-level chunks (coalesced loads and stores, each value
+// read once): the lanes' maps are combined by an inclusive warp scan of 2x2 products (the later
+// level's map on the left; each product rescaled by a power of two, exactly), applied to the
+// vector carried from the chunk above.  Products and sums of non-negative numbers do not cancel,
+// so the scan keeps the same few-ulp accuracy as the sequential recurrence.
+struct M22 {
+    float a, b, c, d;  // [[a, b], [c, d]]
+};
+__device__ __forceinline__ M22 m22_mul(const M22 &x, const M22 &y) {
+    return {x.a * y.a + x.b * y.c, x.a * y.b + x.b * y.d, x.c * y.a + x.d * y.c, x.c * y.b + x.d * y.d};
+}
+// 2^-e with 2^e <= x < 2^(e+1) for a normal positive x
+__device__ __forceinline__ float pow2_inv(float x) {
+    const int e = ((__float_as_int(x) >> 23) & 0xff) - 127;
+    return __int_as_float((127 - e) << 23);
+}
+__device__ __forceinline__ M22 m22_norm(const M22 &m) {
+    const float s = pow2_inv(fmaxf(fmaxf(m.a, m.b), fmaxf(m.c, m.d)));
+    return {m.a * s, m.b * s, m.c * s, m.d * s};
+}
+
+__device__ __forceinline__ void vfactors_col(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
+                                             float dtf, const VFactors &vf, int n, int lane) {
     const int L1 = tp.L1, nl = tp.nl;
-    const int c0 = blk * kVfCols, tid = threadIdx.x;
-    const int ncol = min(kVfCols, tp.N2 - c0);
-    const int n = c0 + tid;
-    const bool mine = tid < ncol;
-    const int nzmin = mine ? tp.n_ulev[n] : 1, nzmax = mine ? tp.n_nlev[n] : 1;
-    if (tid == 0) s_lmax = 0;
-    __syncthreads();
-    if (mine) atomicMax(&s_lmax, nzmax - 1);
-    __syncthreads();
-    const int lmax = s_lmax;
-    int lmin = 1 << 30;
-    // the first tile starts at the block's shallowest top layer
-    {
-        __shared__ int s_lmin;
-        if (tid == 0) s_lmin = 1 << 30;
-        __syncthreads();
-        if (mine) atomicMin(&s_lmin, nzmin);
-        __syncthreads();
-        lmin = s_lmin;
-    }
-    const float dtf = (float)dt;
-    double cp = 0.0;
-    float zinv1 = 0.f, hcur = 0.f;
-    for (int lev0 = lmin; lev0 <= lmax; lev0 += kVfK) {
-        // load: item q = column * (kVfK + 1) + k, consecutive threads on consecutive levels
-        for (int q = tid; q < ncol * (kVfK + 1); q += kVfCols) {
-            const int col = q / (kVfK + 1), k = q - col * (kVfK + 1);
-            const int lev = lev0 + k, cn = c0 + col;
-            float hv = 0.f, arv = 0.f, avv = 0.f, kvv = 0.f;
-            if (lev <= L1) hv = g.hnode_new[(size_t)cn * L1 + lev - 1];
-            if (lev <= nl) {
-                const size_t iv = (size_t)cn * nl + lev - 1;
-                arv = g.area[iv];
-                avv = g.areasvol[iv];
-                kvv = f.Kv[iv];
-            }
-            s_hn[col][k] = hv;
-            s_ar[col][k] = arv;
-            s_av[col][k] = avv;
-            s_kv[col][k] = kvv;
+    const int nzmin = tp.n_ulev[n], nzmax = tp.n_nlev[n];
+    float cx = 1.f, cy = 1.f;       // the excess vector at the last level of the chunk above
+    float h_up = 0.f, c_up = 0.f;   // h and c of that level
+    for (int nz0 = nzmin; nz0 <= nzmax - 1; nz0 += 32) {
+        const int nz = nz0 + lane;
+        const bool ok = nz <= nzmax - 1;
+        const size_t i = (size_t)n * L1 + nz - 1, iv = (size_t)n * nl + nz - 1;
+        float h = 0.f, ar = 0.f, av = 1.f, kv = 0.f;
+        if (ok) {
+            h = g.hnode_new[i];
+            ar = g.area[iv];
+            av = g.areasvol[iv];
+            kv = f.Kv[iv];
         }
-        __syncthreads();
-        if (mine) {
-            for (int k = 0; k < kVfK; k++) {
-                const int nz = lev0 + k;
-                float oa = 0.f, oc = 0.f, oi = 0.f, ocp = 0.f;
-                if (nz >= nzmin && nz <= nzmax - 1) {
-                    if (nz == nzmin) hcur = s_hn[tid][k];
-                    const float hnext = nz < nzmax - 1 ? s_hn[tid][k + 1] : 0.f;
-                    const float ravz = 1.f / s_av[tid][k];
-                    const float a = nz > nzmin ? -(s_kv[tid][k] * zinv1 * dtf * (s_ar[tid][k] * ravz)) : 0.f;
-                    float c = 0.f, zinv2 = 0.f;
-                    if (nz < nzmax - 1) {
-                        zinv2 = 2.f / (hcur + hnext);
-                        c = -(s_kv[tid][k + 1] * zinv2 * dtf * s_ar[tid][k + 1] * ravz);
-                    }
-                    // pivot recurrence in FP64 on the FP32-rounded coefficients; 1/m from an FP32
-                    // reciprocal and one Newton-Raphson step r = r0 (2 - m r0)
-                    const double ad = (double)a;
-                    const double m = ((double)(-a - c) + (double)hcur) - cp * ad;
-                    const double r0 = (double)__frcp_rn((float)m);
-                    const double r = r0 * (2.0 - m * r0);
-                    cp = (double)c * r;
-                    oa = a;
-                    oc = c;
-                    oi = (float)r;
-                    ocp = (float)cp;
-                    zinv1 = zinv2;
-                    hcur = hnext;
-                }
-                s_a[tid][k] = oa;
-                s_c[tid][k] = oc;
-                s_i[tid][k] = oi;
-                s_p[tid][k] = ocp;
-            }
+        // the level below (c) from the next lane, the chunk's last lane loads it
+        float hn = sh_dn(h, 1), arn = sh_dn(ar, 1), kvn = sh_dn(kv, 1);
+        if (lane == 31 && nz + 1 <= nzmax - 1) {
+            hn = g.hnode_new[i + 1];
+            arn = g.area[iv + 1];
+            kvn = f.Kv[iv + 1];
         }
-        __syncthreads();
-        for (int q = tid; q < ncol * kVfK; q += kVfCols) {
-            const int col = q / kVfK, k = q - col * kVfK;
-            const int lev = lev0 + k, cn = c0 + col;
-            if (lev > L1) continue;
-            const size_t i = (size_t)cn * L1 + lev - 1;
-            vf.a[i] = s_a[col][k];
-            vf.c[i] = s_c[col][k];
-            vf.inv[i] = s_i[col][k];
-            vf.cp[i] = s_p[col][k];
+        // the level above (a) from the previous lane, the chunk's first lane from the chunk above
+        float hu = sh_up(h, 1);
+        if (lane == 0) hu = h_up;
+        const float ravz = 1.f / av;
+        float a = 0.f, c = 0.f;
+        if (ok && nz > nzmin) a = -(kv * (2.f / (hu + h)) * dtf * (ar * ravz));
+        if (ok && nz < nzmax - 1) c = -(kvn * (2.f / (h + hn)) * dtf * arn * ravz);
+        float cu = sh_up(c, 1);
+        if (lane == 0) cu = c_up;
+        M22 S;
+        if (!ok) S = {1.f, 0.f, 0.f, 1.f};
+        else if (nz == nzmin) S = {0.f, h, 0.f, 1.f};
+        else S = {h - a, h * -cu, 1.f, -cu};
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const M22 P = {sh_up(S.a, off), sh_up(S.b, off), sh_up(S.c, off), sh_up(S.d, off)};
+            if (lane >= off) S = m22_norm(m22_mul(S, P));
         }
-        __syncthreads();
+        const float v0 = S.a * cx + S.b * cy, v1 = S.c * cx + S.d * cy;
+        if (ok) {
+            const float m = v0 / v1 - c;
+            vf.a[i] = a;
+            vf.c[i] = c;
+            vf.inv[i] = 1.f / m;
+            vf.cp[i] = c / m;
+        }
+        // past the column's end the maps are identities: lane 31 holds the chunk's last level
+        const float w0 = __shfl_sync(kFull, v0, 31), w1 = __shfl_sync(kFull, v1, 31);
+        const float sc = pow2_inv(fmaxf(w0, w1));
+        cx = w0 * sc;
+        cy = w1 * sc;
+        h_up = __shfl_sync(kFull, h, 31);
+        c_up = __shfl_sync(kFull, c, 31);
     }
 }
 
-__global__ void __launch_bounds__(kVfCols) k32_vfactors(DTopo tp, DGeom<float> g, DForcing<float> f, double dt,
-                                                        VFactors vf) {
-    vfactors_block(tp, g, f, dt, vf, blockIdx.x);
+__global__ void __launch_bounds__(kTB) k32_vfactors(DTopo tp, DGeom<float> g, DForcing<float> f, float dt,
+                                                    VFactors vf) {
+    for (int n = blockIdx.x * kWB + (threadIdx.x >> 5); n < tp.N2; n += gridDim.x * kWB)
+        vfactors_col(tp, g, f, dt, vf, n, threadIdx.x & 31);
 }
 
 // ---------------------------------------------------------------------------
@@ -356,8 +344,6 @@ struct Chunk {
     }
 };
 
-__device__ __forceinline__ float sh_up(float v, int d) { return __shfl_up_sync(kFull, v, d); }
-__device__ __forceinline__ float sh_dn(float v, int d) { return __shfl_down_sync(kFull, v, d); }
 
 
 // ---------------------------------------------------------------------------
@@ -2702,10 +2688,11 @@ __global__ void __launch_bounds__(kTB) k32m_vflux(const Inst32 *__restrict__ I, 
         vflux_edge(I[i].tp, I[i].g, I[i].f, I[i].VF, u - ix.start[i], threadIdx.x & 31);
     }
 }
-__global__ void __launch_bounds__(kVfCols) k32m_vfactors(const Inst32 *__restrict__ I, MultiIdx ix) {
-    const int u = blockIdx.x;
-    const int i = find_inst(ix, u);
-    vfactors_block(I[i].tp, I[i].g, I[i].f, I[i].dtd, I[i].vf, u - ix.start[i]);
+__global__ void __launch_bounds__(kTB) k32m_vfactors(const Inst32 *__restrict__ I, MultiIdx ix) {
+    FOR_WARP_UNITS(u, ix.start[ix.n]) {
+        const int i = find_inst(ix, u);
+        vfactors_col(I[i].tp, I[i].g, I[i].f, I[i].dt, I[i].vf, u - ix.start[i], threadIdx.x & 31);
+    }
 }
 // WS: some instance has the split vertical velocity (each instance checks its own switch)
 template <bool WIDE, bool WS>
@@ -2826,7 +2813,7 @@ void b32_vflux(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f,
 }
 void b32_vfactors(const DTopo &tp, const DGeom<float> &g, const DForcing<float> &f, double dt, const VFactors &v,
                   cudaStream_t s) {
-    k32_vfactors<<<(tp.N2 + kVfCols - 1) / kVfCols, kVfCols, 0, s>>>(tp, g, f, dt, v);
+    k32_vfactors<<<grid_nodes(tp.N2), kTB, 0, s>>>(tp, g, f, (float)dt, v);
 }
 
 // dynamic shared memory of the staged node kernels: kWB warps' staging
@@ -3049,7 +3036,7 @@ void bm32_vflux(const Inst32 *I, const MultiIdx &ix, cudaStream_t s) {
 }
 void bm32_vfactors(const Inst32 *I, const MultiIdx &ix, cudaStream_t s) {
     const int u = ix.start[ix.n];
-    if (u) k32m_vfactors<<<u, kVfCols, 0, s>>>(I, ix);
+    if (u) k32m_vfactors<<<grid_nodes(u), kTB, 0, s>>>(I, ix);
 }
 void bm32_lo_ad(const Inst32 *I, const MultiIdx &ix, bool wide, bool ws, cudaStream_t s) {
     const int u = ix.start[ix.n];
