@@ -22,7 +22,7 @@
 //                    runs the node's implicit vertical diffusion (k32_vdiff's column solve)
 //   k32_vdiff        per node: the implicit vertical diffusion as two warp scans of
 //                    affine maps over the column (forward and back substitution with
-//                    the FP64-formed factors); its own launch only when asked for
+//                    the factors of k32_vfactors); its own launch only when asked for
 //   k32_vppm, k32_lo_impl, k32_vdiff_w, k32_hdiff, k32_diff
 //                    the optional parts: PPM vertical fluxes, the split vertical
 //                    velocity, horizontal and explicit vertical diffusion
@@ -1561,7 +1561,7 @@ k32_bounds(DTopo tp, DGeom<float> g, B32View B, float dt) {
 // k32_vdiff: implicit vertical diffusion of the advected columns (in Tnew)
 // ---------------------------------------------------------------------------
 // Forward substitution tp_k = inv_k rhs_k - a_k inv_k tp_{k-1} and back substitution
-// x_k = tp_k - cp_k x_{k+1} (oce_ale_tracer.F90:1406-1422) with the column's FP64-derived
+// x_k = tp_k - cp_k x_{k+1} (oce_ale_tracer.F90:1406-1422) with the column's k32_vfactors
 // factors, as scans of affine maps y -> A y + B.  Each lane holds K consecutive levels of the
 // column (K = ceil(layers / 32): one warp covers the whole column): it composes its K maps in
 // registers, the warp scans the lane maps (five shuffles), and each lane then runs its K
