@@ -85,7 +85,6 @@ constexpr bool kFctClamp = FESOM_FCT_CLAMP != 0;
 constexpr int kWB = 8;                // warps (= nodes) per block
 constexpr int kTB = 32 * kWB;
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kMaxChunks = 5;         // columns of up to 128 layers, 30 levels per chunk
 
 // resident blocks per SM each group kernel is built for (registers: 65536 / (256 * blocks))
 template <int G>
